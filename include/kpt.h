@@ -1,0 +1,225 @@
+/*
+ * kpt.h — C ABI of the GB300-native Parker / focused-transport particle push.
+ *
+ * Every entry point is extern "C", takes plain pointers and sizes, returns an
+ * int status (KPT_OK = 0, negative = error; kpt_last_error() describes the
+ * last failure on the calling thread) and never falls back to the CPU: with
+ * no usable CUDA device, kpt_context_create fails.
+ *
+ * Handles are opaque and owned by their creator.  Calls on one context are
+ * ordered on the context's CUDA stream; calls that return host results
+ * (counts, histograms, summaries, downloads) synchronise that stream.
+ *
+ * The entry points replace the reference's driver functions and library
+ * types (paths relative to the reference project):
+ *   kpt_field_create            src/main.cpp:932-962 load_*_coefficient_frame,
+ *                               include/AthenaFieldReader.hpp:290-360 (reader),
+ *                               include/Field.hpp:274-316 (ghost fill),
+ *                               src/main.cpp:840-957 (coefficient tables)
+ *   kpt_particles_*             src/main.cpp:292-333 ReconnectionParticleStorage
+ *   kpt_inject_uniform          src/main.cpp:996-1048 inject_uniform_particles
+ *   kpt_push_interval           src/main.cpp:1084-1327 move_parker_particles_one_interval,
+ *                               src/main.cpp:1334-1755 move_particles_one_interval
+ *   kpt_split                   src/main.cpp:1761-1839 split_particles
+ *   kpt_histogram               src/main.cpp:1907-1964 write_momentum_histogram (binning)
+ *   kpt_summarize               src/main.cpp:1845-1901 summarize_particles
+ *   kpt_sample_table            include/FieldInterpolator.hpp:346-380 LinearPositionInterpolator
+ *                               ::sample with src/main.cpp:1055-1077 time interpolation
+ */
+#ifndef KPT_H
+#define KPT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define KPT_ABI_VERSION 1
+
+enum kpt_status {
+    KPT_OK = 0,
+    KPT_ERROR_INVALID_ARGUMENT = -1,
+    KPT_ERROR_CUDA = -2,
+    KPT_ERROR_OUT_OF_MEMORY = -3,
+    KPT_ERROR_IO = -4,
+    KPT_ERROR_FORMAT = -5,
+    KPT_ERROR_CAPACITY = -6,
+    KPT_ERROR_NO_DEVICE = -7
+};
+
+/* Coefficient table layouts (component order of src/main.cpp:38-79). */
+enum kpt_table_kind {
+    KPT_TABLE_PARKER16 = 0,  /* Vx Vy Bx By Bz |B| dVx/dx dVy/dy dBx/dx dBx/dy dBy/dx
+                                dBy/dy dBz/dx dBz/dy d|B|/dx d|B|/dy */
+    KPT_TABLE_FOCUSED21 = 1  /* Vx Vy Vz Bx By Bz |B|, d(Vx,Vy,Vz)/d(x,y) (6),
+                                d(Bx,By,Bz)/d(x,y) (6), d|B|/dx d|B|/dy */
+};
+
+/* Arithmetic of a table and of the push that reads it. */
+enum kpt_precision {
+    KPT_PRECISION_F64 = 0,   /* plain FP64 throughout */
+    KPT_PRECISION_MIXED = 1  /* FP32 table, interpolation, coefficients and noise; FP64
+                                position, time and momentum accumulation and cell search */
+};
+
+enum kpt_schedule {
+    KPT_SCHEDULE_REFILL = 0,
+    KPT_SCHEDULE_SIMPLE = 1
+};
+
+/* Run parameters: the reference's Reconnection2DSettings physics block
+ * (src/main.cpp:114-241).  Doubles first, then 32-bit ints. */
+typedef struct kpt_settings {
+    double mhd_dt;
+    double p0;
+    double pmin;
+    double pmax;
+    double gamma_turb;
+    double kpara0;
+    double kperp_over_kpara;
+    double dt_min_rel;
+    double dt_max_rel;
+    double drift_param1;
+    double drift_param2;
+    double charge;
+    double particle_v0;
+    double duu0;
+    double split_ratio;
+    double pmin_split_over_p0;
+    double mu_max;
+    int32_t max_steps;
+    int32_t momentum_dependency;
+    int32_t magnetic_dependency;
+    int32_t time_interpolation;
+    int32_t split_particles;
+    int32_t focused;
+} kpt_settings;
+
+/* Per-push counters, summed over the particles pushed. */
+typedef struct kpt_push_stats {
+    uint64_t particle_steps;   /* executed substep-loop iterations */
+    uint64_t pushed;           /* particles active at the start of the push */
+    uint64_t failed;           /* of those, particles that ended with status 2 */
+    uint32_t max_steps;        /* largest per-particle substep count */
+    uint32_t pad;
+} kpt_push_stats;
+
+/* summarize_particles output (src/main.cpp:255-270). */
+typedef struct kpt_summary {
+    uint64_t stored;
+    uint64_t active;
+    uint64_t inactive;
+    double weight_sum;
+    double p_min;
+    double p_max;
+    double p_avg;
+    double dt_min;
+    double dt_max;
+    double dt_avg;
+    int32_t max_split_level;
+    int32_t pad;
+} kpt_summary;
+
+/* Device pointers of a particle store (SoA, length = capacity). */
+typedef struct kpt_particle_arrays {
+    double* x;
+    double* y;
+    double* p;
+    double* t;
+    double* step_dt;
+    double* weight;
+    double* mu;
+    int32_t* status;
+    int32_t* split_level;
+} kpt_particle_arrays;
+
+typedef struct kpt_context kpt_context;
+typedef struct kpt_field kpt_field;
+typedef struct kpt_particles kpt_particles;
+
+/* ---- library ---------------------------------------------------------- */
+int kpt_abi_version(void);
+const char* kpt_last_error(void);
+/* Reference defaults (src/main.cpp:136-154, Reconnection2DSettings). */
+void kpt_default_settings(kpt_settings* out);
+
+/* ---- context: one CUDA device and one stream --------------------------- */
+int kpt_context_create(int device, kpt_context** out);
+int kpt_context_destroy(kpt_context* ctx);
+/* Order later calls on an external stream (cudaStream_t); NULL = own stream. */
+int kpt_context_set_stream(kpt_context* ctx, void* cuda_stream);
+int kpt_context_synchronize(kpt_context* ctx);
+/* Push scheduling: KPT_SCHEDULE_REFILL (persistent warps that refill lanes
+ * from a work cursor; blocks_per_sm x SM count blocks of 128 threads) or
+ * KPT_SCHEDULE_SIMPLE (one particle per thread).  Results do not depend on
+ * the choice; the autotuner picks the faster one. */
+int kpt_context_set_push_schedule(kpt_context* ctx, int schedule, int blocks_per_sm);
+
+/* ---- fields: one MHD frame as a device coefficient table ---------------- */
+/* Cells are 3 x ny x nx arrays (x fastest) of B and V, host memory.  Edges
+ * (nx+1, ny+1) must be finite and ascending; uniform axes use the analytic
+ * map, non-uniform axes the stored-edge map (extension). */
+int kpt_field_create(kpt_context* ctx, int nx, int ny, const double* x_edges,
+                     const double* y_edges, const double* b_cells, const double* v_cells,
+                     int table_kind, int precision, kpt_field** out);
+/* Read a compact field file (AthenaFieldReader.hpp:277-285 layout) and build
+ * its table. */
+int kpt_field_load(kpt_context* ctx, const char* path, int table_kind, int precision,
+                   kpt_field** out);
+int kpt_field_destroy(kpt_field* field);
+/* nx, ny, number of ghosted points and components. */
+int kpt_field_shape(const kpt_field* field, int* nx, int* ny, uint64_t* points,
+                    int* components);
+/* Copy the table to host as float64 (points x components). */
+int kpt_field_download_table(const kpt_field* field, double* out, uint64_t out_len);
+
+/* ---- particles --------------------------------------------------------- */
+int kpt_particles_create(kpt_context* ctx, uint64_t capacity, kpt_particles** out);
+int kpt_particles_destroy(kpt_particles* particles);
+int kpt_particles_count(const kpt_particles* particles, uint64_t* count,
+                        uint64_t* capacity);
+int kpt_particles_set_count(kpt_particles* particles, uint64_t count);
+/* Host SoA in / out for the first `count` particles; NULL skips an array. */
+int kpt_particles_upload(kpt_particles* particles, uint64_t count, const double* x,
+                         const double* y, const double* p, const double* t,
+                         const double* step_dt, const double* weight, const double* mu,
+                         const int32_t* status, const int32_t* split_level);
+int kpt_particles_download(const kpt_particles* particles, uint64_t count, double* x,
+                           double* y, double* p, double* t, double* step_dt, double* weight,
+                           double* mu, int32_t* status, int32_t* split_level);
+int kpt_particles_device_arrays(const kpt_particles* particles, kpt_particle_arrays* out);
+
+/* ---- hot path ---------------------------------------------------------- */
+/* Append min(requested, capacity - count) particles for the interval that
+ * starts at frame * mhd_dt.  band_lo < band_hi draws y in that band instead
+ * of the whole domain.  Noise: Philox4x32-10 keyed (seed, k, frame, 1). */
+int kpt_inject_uniform(kpt_context* ctx, kpt_particles* particles, const kpt_field* grid,
+                       const kpt_settings* settings, uint64_t requested, uint32_t frame,
+                       uint64_t seed, double band_lo, double band_hi, uint64_t* injected);
+/* Push every active particle across the interval [frame*mhd_dt,
+ * frame*mhd_dt + mhd_dt) between tables `lower` and `upper` (same kind,
+ * precision and grid).  Noise: Philox keyed (seed, index, frame, 2). */
+int kpt_push_interval(kpt_context* ctx, kpt_particles* particles, const kpt_field* lower,
+                      const kpt_field* upper, const kpt_settings* settings, uint32_t frame,
+                      uint64_t seed, kpt_push_stats* stats);
+/* Momentum-threshold split, children appended in parent-index order. */
+int kpt_split(kpt_context* ctx, kpt_particles* particles, const kpt_settings* settings,
+              uint64_t* split, uint64_t* skipped);
+/* Weight histogram of active particles over nbins log bins of [pmin, pmax]. */
+int kpt_histogram(kpt_context* ctx, const kpt_particles* particles, double pmin, double pmax,
+                  int nbins, double* bins);
+int kpt_summarize(kpt_context* ctx, const kpt_particles* particles, kpt_summary* out);
+
+/* Interpolated table values at n host positions (x, y) and interval
+ * fraction rt (parity and diagnostics); out is n x components float64. */
+int kpt_sample_table(kpt_context* ctx, const kpt_field* lower, const kpt_field* upper,
+                     uint64_t n, const double* x, const double* y, const double* rt,
+                     int time_interpolation, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

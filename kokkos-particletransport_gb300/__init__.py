@@ -1,0 +1,401 @@
+"""GB300-native Parker / focused-transport particle push — Python binding.
+
+A thin ctypes layer over ``lib/libkpt.so`` (the C ABI declared in
+``include/kpt.h``).  It mirrors the reference driver's objects: a coefficient
+``Field`` per MHD frame (reference ``Field<Grid,16|21>`` built by
+``load_*_coefficient_frame``), a ``ParticleStorage`` (reference
+``ReconnectionParticleStorage``) and the per-frame operations ``inject``,
+``push_interval``, ``split``, ``histogram`` and ``summarize``.
+
+There is no CPU path: importing works without a GPU, but creating a
+``Context`` raises ``KptError`` when no CUDA device or no built library is
+available.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import os
+from typing import Dict, Optional, Sequence
+
+import numpy as np
+
+from . import fields  # noqa: F401  (re-exported module)
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libkpt.so")
+HEADER_PATH = os.path.join(os.path.dirname(HERE), "include", "kpt.h")
+
+TABLE_PARKER16 = 0
+TABLE_FOCUSED21 = 1
+PRECISION_F64 = 0
+PRECISION_MIXED = 1
+SCHEDULE_REFILL = 0
+SCHEDULE_SIMPLE = 1
+
+PARTICLE_FIELDS = ("x", "y", "p", "t", "dt", "w", "mu", "status", "level")
+DOUBLE_SETTINGS = ("mhd_dt", "p0", "pmin", "pmax", "gamma_turb", "kpara0", "kperp_over_kpara",
+                   "dt_min_rel", "dt_max_rel", "drift_param1", "drift_param2", "charge",
+                   "particle_v0", "duu0", "split_ratio", "pmin_split_over_p0", "mu_max")
+INT_SETTINGS = ("max_steps", "momentum_dependency", "magnetic_dependency", "time_interpolation",
+                "split_particles", "focused")
+
+
+class KptError(RuntimeError):
+    """A libkpt call failed (message from kpt_last_error)."""
+
+
+class Settings(ctypes.Structure):
+    """kpt_settings: the reference Reconnection2DSettings physics block."""
+    _fields_ = [(n, ctypes.c_double) for n in DOUBLE_SETTINGS] + \
+               [(n, ctypes.c_int32) for n in INT_SETTINGS]
+
+    def as_dict(self) -> Dict[str, float]:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class PushStats(ctypes.Structure):
+    _fields_ = [("particle_steps", ctypes.c_uint64), ("pushed", ctypes.c_uint64),
+                ("failed", ctypes.c_uint64), ("max_steps", ctypes.c_uint32),
+                ("pad", ctypes.c_uint32)]
+
+
+class Summary(ctypes.Structure):
+    _fields_ = [("stored", ctypes.c_uint64), ("active", ctypes.c_uint64),
+                ("inactive", ctypes.c_uint64), ("weight_sum", ctypes.c_double),
+                ("p_min", ctypes.c_double), ("p_max", ctypes.c_double),
+                ("p_avg", ctypes.c_double), ("dt_min", ctypes.c_double),
+                ("dt_max", ctypes.c_double), ("dt_avg", ctypes.c_double),
+                ("max_split_level", ctypes.c_int32), ("pad", ctypes.c_int32)]
+
+    def as_dict(self) -> Dict[str, float]:
+        return {name: getattr(self, name) for name, _ in self._fields_ if name != "pad"}
+
+
+class ParticleArrays(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in
+                ("x", "y", "p", "t", "step_dt", "weight", "mu", "status", "split_level")]
+
+
+_LIB: Optional[ctypes.CDLL] = None
+
+
+def library_path() -> str:
+    return LIB_PATH
+
+
+def load_library() -> ctypes.CDLL:
+    """Load libkpt.so (raises KptError if it has not been built)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(LIB_PATH):
+        raise KptError(f"libkpt.so not built at {LIB_PATH}; run __graft_entry__.build()")
+    lib = ctypes.CDLL(LIB_PATH)
+    vp, i32, u32, u64, dbl = (ctypes.c_void_p, ctypes.c_int, ctypes.c_uint32, ctypes.c_uint64,
+                              ctypes.c_double)
+    pvp = ctypes.POINTER(ctypes.c_void_p)
+    sig = {
+        "kpt_abi_version": (i32, []),
+        "kpt_last_error": (ctypes.c_char_p, []),
+        "kpt_default_settings": (None, [vp]),
+        "kpt_context_create": (i32, [i32, pvp]),
+        "kpt_context_destroy": (i32, [vp]),
+        "kpt_context_set_stream": (i32, [vp, vp]),
+        "kpt_context_synchronize": (i32, [vp]),
+        "kpt_context_set_push_schedule": (i32, [vp, i32, i32]),
+        "kpt_field_create": (i32, [vp, i32, i32, vp, vp, vp, vp, i32, i32, pvp]),
+        "kpt_field_load": (i32, [vp, ctypes.c_char_p, i32, i32, pvp]),
+        "kpt_field_destroy": (i32, [vp]),
+        "kpt_field_shape": (i32, [vp, vp, vp, vp, vp]),
+        "kpt_field_download_table": (i32, [vp, vp, u64]),
+        "kpt_particles_create": (i32, [vp, u64, pvp]),
+        "kpt_particles_destroy": (i32, [vp]),
+        "kpt_particles_count": (i32, [vp, vp, vp]),
+        "kpt_particles_set_count": (i32, [vp, u64]),
+        "kpt_particles_upload": (i32, [vp, u64] + [vp] * 9),
+        "kpt_particles_download": (i32, [vp, u64] + [vp] * 9),
+        "kpt_particles_device_arrays": (i32, [vp, vp]),
+        "kpt_inject_uniform": (i32, [vp, vp, vp, vp, u64, u32, u64, dbl, dbl, vp]),
+        "kpt_push_interval": (i32, [vp, vp, vp, vp, vp, u32, u64, vp]),
+        "kpt_split": (i32, [vp, vp, vp, vp, vp]),
+        "kpt_histogram": (i32, [vp, vp, dbl, dbl, i32, vp]),
+        "kpt_summarize": (i32, [vp, vp, vp]),
+        "kpt_sample_table": (i32, [vp, vp, vp, u64, vp, vp, vp, i32, vp]),
+    }
+    for name, (restype, argtypes) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = restype
+        fn.argtypes = argtypes
+    _LIB = lib
+    return lib
+
+
+def _check(rc: int) -> None:
+    if rc != 0:
+        raise KptError(f"libkpt error {rc}: {load_library().kpt_last_error().decode()}")
+
+
+def _ptr(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def default_settings(**overrides) -> Settings:
+    """Reference defaults (src/main.cpp:136-154) with keyword overrides."""
+    s = Settings()
+    load_library().kpt_default_settings(ctypes.byref(s))
+    for key, value in overrides.items():
+        if key not in DOUBLE_SETTINGS + INT_SETTINGS:
+            raise KeyError(key)
+        setattr(s, key, value)
+    return s
+
+
+def settings_from_dict(values: Dict[str, float]) -> Settings:
+    s = Settings()
+    for name in DOUBLE_SETTINGS:
+        setattr(s, name, float(values[name]))
+    for name in INT_SETTINGS:
+        setattr(s, name, int(values[name]))
+    return s
+
+
+class Context:
+    """One CUDA device and stream (kpt_context)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        handle = ctypes.c_void_p()
+        _check(self.lib.kpt_context_create(device, ctypes.byref(handle)))
+        self.handle = handle
+
+    def close(self) -> None:
+        if self.handle:
+            self.lib.kpt_context_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def synchronize(self) -> None:
+        _check(self.lib.kpt_context_synchronize(self.handle))
+
+    def set_stream(self, stream_handle: int) -> None:
+        _check(self.lib.kpt_context_set_stream(self.handle, ctypes.c_void_p(stream_handle)))
+
+    def set_push_schedule(self, schedule: int, blocks_per_sm: int) -> None:
+        _check(self.lib.kpt_context_set_push_schedule(self.handle, schedule, blocks_per_sm))
+
+    # -- fields ---------------------------------------------------------
+    def field(self, field, kind: int = TABLE_PARKER16,
+              precision: int = PRECISION_F64) -> "Field":
+        """Device coefficient table for a fields.CompactField."""
+        xe = np.ascontiguousarray(field.x_edges, dtype=np.float64)
+        ye = np.ascontiguousarray(field.y_edges, dtype=np.float64)
+        b = np.ascontiguousarray(field.b, dtype=np.float64)
+        v = np.ascontiguousarray(field.v, dtype=np.float64)
+        handle = ctypes.c_void_p()
+        _check(self.lib.kpt_field_create(self.handle, field.nx, field.ny, _ptr(xe), _ptr(ye),
+                                         _ptr(b), _ptr(v), kind, precision,
+                                         ctypes.byref(handle)))
+        return Field(self, handle)
+
+    def load_field(self, path: str, kind: int = TABLE_PARKER16,
+                   precision: int = PRECISION_F64) -> "Field":
+        handle = ctypes.c_void_p()
+        _check(self.lib.kpt_field_load(self.handle, path.encode(), kind, precision,
+                                       ctypes.byref(handle)))
+        return Field(self, handle)
+
+    # -- particles ------------------------------------------------------
+    def particles(self, capacity: int) -> "ParticleStorage":
+        handle = ctypes.c_void_p()
+        _check(self.lib.kpt_particles_create(self.handle, int(capacity), ctypes.byref(handle)))
+        return ParticleStorage(self, handle)
+
+    # -- hot path -------------------------------------------------------
+    def inject(self, parts: "ParticleStorage", grid: "Field", settings: Settings,
+               requested: int, frame: int, seed: int, band=(0.0, 0.0)) -> int:
+        n = ctypes.c_uint64()
+        _check(self.lib.kpt_inject_uniform(self.handle, parts.handle, grid.handle,
+                                           ctypes.byref(settings), int(requested), int(frame),
+                                           int(seed), float(band[0]), float(band[1]),
+                                           ctypes.byref(n)))
+        return int(n.value)
+
+    def push_interval(self, parts: "ParticleStorage", lower: "Field", upper: "Field",
+                      settings: Settings, frame: int, seed: int,
+                      stats: bool = True) -> Optional[PushStats]:
+        out = PushStats() if stats else None
+        _check(self.lib.kpt_push_interval(self.handle, parts.handle, lower.handle, upper.handle,
+                                          ctypes.byref(settings), int(frame), int(seed),
+                                          ctypes.byref(out) if out is not None else None))
+        return out
+
+    def split(self, parts: "ParticleStorage", settings: Settings):
+        split = ctypes.c_uint64()
+        skipped = ctypes.c_uint64()
+        _check(self.lib.kpt_split(self.handle, parts.handle, ctypes.byref(settings),
+                                  ctypes.byref(split), ctypes.byref(skipped)))
+        return int(split.value), int(skipped.value)
+
+    def histogram(self, parts: "ParticleStorage", pmin: float, pmax: float,
+                  nbins: int = 128) -> np.ndarray:
+        bins = np.zeros(nbins, dtype=np.float64)
+        _check(self.lib.kpt_histogram(self.handle, parts.handle, float(pmin), float(pmax),
+                                      int(nbins), _ptr(bins)))
+        return bins
+
+    def summarize(self, parts: "ParticleStorage") -> Dict[str, float]:
+        out = Summary()
+        _check(self.lib.kpt_summarize(self.handle, parts.handle, ctypes.byref(out)))
+        return out.as_dict()
+
+    def sample(self, lower: "Field", upper: "Field", x, y, rt,
+               time_interpolation: int = 1) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.ascontiguousarray(y, dtype=np.float64)
+        rt = np.ascontiguousarray(rt, dtype=np.float64)
+        ncomp = lower.shape()[3]
+        out = np.zeros((x.size, ncomp), dtype=np.float64)
+        _check(self.lib.kpt_sample_table(self.handle, lower.handle, upper.handle, x.size,
+                                         _ptr(x), _ptr(y), _ptr(rt), int(time_interpolation),
+                                         _ptr(out)))
+        return out
+
+
+class Field:
+    """One frame's coefficient table on the device (kpt_field)."""
+
+    def __init__(self, ctx: Context, handle: ctypes.c_void_p):
+        self.ctx = ctx
+        self.handle = handle
+
+    def close(self) -> None:
+        if self.handle:
+            self.ctx.lib.kpt_field_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def shape(self):
+        nx, ny, comps = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        points = ctypes.c_uint64()
+        _check(self.ctx.lib.kpt_field_shape(self.handle, ctypes.byref(nx), ctypes.byref(ny),
+                                            ctypes.byref(points), ctypes.byref(comps)))
+        return nx.value, ny.value, int(points.value), comps.value
+
+    def table(self) -> np.ndarray:
+        _, _, points, comps = self.shape()
+        out = np.zeros((points, comps), dtype=np.float64)
+        _check(self.ctx.lib.kpt_field_download_table(self.handle, _ptr(out), out.size))
+        return out
+
+
+class ParticleStorage:
+    """Device SoA particle store (kpt_particles)."""
+
+    def __init__(self, ctx: Context, handle: ctypes.c_void_p):
+        self.ctx = ctx
+        self.handle = handle
+
+    def close(self) -> None:
+        if self.handle:
+            self.ctx.lib.kpt_particles_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def count(self) -> int:
+        c = ctypes.c_uint64()
+        _check(self.ctx.lib.kpt_particles_count(self.handle, ctypes.byref(c), None))
+        return int(c.value)
+
+    @property
+    def capacity(self) -> int:
+        c = ctypes.c_uint64()
+        _check(self.ctx.lib.kpt_particles_count(self.handle, None, ctypes.byref(c)))
+        return int(c.value)
+
+    def set_count(self, count: int) -> None:
+        _check(self.ctx.lib.kpt_particles_set_count(self.handle, int(count)))
+
+    def upload(self, arrays: Dict[str, np.ndarray], count: int) -> None:
+        conv = {}
+        for name in PARTICLE_FIELDS:
+            dtype = np.int32 if name in ("status", "level") else np.float64
+            conv[name] = np.ascontiguousarray(arrays[name][:count], dtype=dtype)
+        _check(self.ctx.lib.kpt_particles_upload(self.handle, int(count),
+                                                 *[_ptr(conv[n]) for n in PARTICLE_FIELDS]))
+
+    def download(self, count: Optional[int] = None) -> Dict[str, np.ndarray]:
+        n = self.count if count is None else int(count)
+        out = {name: np.zeros(n, dtype=np.float64) for name in PARTICLE_FIELDS[:7]}
+        out["status"] = np.zeros(n, dtype=np.int32)
+        out["level"] = np.zeros(n, dtype=np.int32)
+        _check(self.ctx.lib.kpt_particles_download(self.handle, n,
+                                                   *[_ptr(out[k]) for k in PARTICLE_FIELDS]))
+        return out
+
+    def device_arrays(self) -> Dict[str, int]:
+        arr = ParticleArrays()
+        _check(self.ctx.lib.kpt_particles_device_arrays(self.handle, ctypes.byref(arr)))
+        return {name: getattr(arr, name) for name, _ in ParticleArrays._fields_}
+
+
+def header_functions(path: str = HEADER_PATH) -> Sequence[str]:
+    """Names of the functions declared in include/kpt.h."""
+    import re
+    text = open(path).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(kpt_[a-z0-9_]+)\s*\(", text)))
+
+
+def smoke_check(device: int = 0) -> None:
+    """One small Parker push on the GPU, checked against the CPU oracle."""
+    import importlib
+    binding = importlib.import_module("binding")  # oracle/binding.py (checker only)
+    field0 = fields.harris_field(32, 64, noise=0.01, seed=1)
+    field1 = fields.harris_field(32, 64, noise=0.01, seed=2)
+    params = binding.default_params(kperp_over_kpara=0.05)
+    oracle = binding.Oracle()
+    grid = oracle.grid(field0.x_edges, field0.y_edges)
+    cap, seed, frame = 512, 114514, 3
+    ref = binding.empty_particles(cap)
+    count = oracle.inject(grid, params, frame * 0.1, frame, seed, cap, 0, 256, ref,
+                          band=(-0.2, 0.2))
+    start = {k: v.copy() for k, v in ref.items()}
+    oracle.push(grid, oracle.table(field0), oracle.table(field1), params, frame * 0.1, frame,
+                seed, count, ref)
+    with Context(device) as ctx:
+        settings = settings_from_dict(params)
+        lower = ctx.field(field0)
+        upper = ctx.field(field1)
+        parts = ctx.particles(cap)
+        parts.upload(start, count)
+        stats = ctx.push_interval(parts, lower, upper, settings, frame, seed)
+        got = parts.download()
+        for name in ("x", "y", "p", "t", "dt"):
+            err = np.max(np.abs(got[name] - ref[name][:count]) /
+                         np.maximum(np.abs(ref[name][:count]), 1e-300))
+            if not err <= 1e-10:
+                raise AssertionError(f"smoke: {name} differs from the oracle (rel {err:.3e})")
+        if not np.array_equal(got["status"], ref["status"][:count]):
+            raise AssertionError("smoke: status differs from the oracle")
+        if stats.particle_steps <= 0:
+            raise AssertionError("smoke: no particle steps executed")
+        for f in (lower, upper):
+            f.close()
+        parts.close()

@@ -1,0 +1,970 @@
+// C-ABI layer of libkpt: handles, validation, host-side file reading and the
+// launches of the device kernels.  Every entry point returns a kpt_status and
+// records a message for kpt_last_error() on failure; there is no CPU path.
+#include "kpt.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <limits>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "kpt_internal.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int set_error(int code, const std::string& message) {
+    g_last_error = message;
+    return code;
+}
+
+#define KPT_CUDA(expr)                                                                  \
+    do {                                                                                \
+        const cudaError_t kpt_err_ = (expr);                                            \
+        if (kpt_err_ != cudaSuccess) {                                                  \
+            return set_error(kpt_err_ == cudaErrorMemoryAllocation ? KPT_ERROR_OUT_OF_MEMORY \
+                                                                   : KPT_ERROR_CUDA,    \
+                             std::string(#expr) + ": " + cudaGetErrorString(kpt_err_)); \
+        }                                                                               \
+    } while (0)
+
+#define KPT_REQUIRE(cond, message)                                   \
+    do {                                                             \
+        if (!(cond)) {                                               \
+            return set_error(KPT_ERROR_INVALID_ARGUMENT, (message)); \
+        }                                                            \
+    } while (0)
+
+// Growable device buffer owned by a context.
+struct DeviceBuffer {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    cudaError_t reserve(size_t want) {
+        if (want <= bytes) {
+            return cudaSuccess;
+        }
+        if (ptr != nullptr) {
+            cudaFree(ptr);
+            ptr = nullptr;
+            bytes = 0;
+        }
+        const cudaError_t err = cudaMalloc(&ptr, want);
+        if (err == cudaSuccess) {
+            bytes = want;
+        }
+        return err;
+    }
+    void release() {
+        if (ptr != nullptr) {
+            cudaFree(ptr);
+        }
+        ptr = nullptr;
+        bytes = 0;
+    }
+    template <typename T>
+    T* as() const {
+        return static_cast<T*>(ptr);
+    }
+};
+
+}  // namespace
+
+struct kpt_context {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    DeviceBuffer counters;
+    DeviceBuffer split_counts, split_offsets, split_totals, split_levels;
+    double split_key[3] = {0.0, 0.0, 0.0};
+    int split_level_count = 0;
+    DeviceBuffer hist_bins, hist_edge_count, hist_edge_index;
+    DeviceBuffer summary_partials, summary_result;
+    DeviceBuffer sample_io;
+    int push_schedule = kpt::kScheduleRefill;
+    int push_blocks_per_sm = 8;
+};
+
+struct kpt_field {
+    kpt_context* ctx = nullptr;
+    int nx = 0, ny = 0;
+    int kind = 0, precision = 0, stride = 0;
+    uint64_t points = 0;
+    void* table = nullptr;
+    double* centers[2] = {nullptr, nullptr};
+    int* buckets[2] = {nullptr, nullptr};
+    kpt::Grid grid{};
+};
+
+struct kpt_particles {
+    kpt_context* ctx = nullptr;
+    uint64_t capacity = 0;
+    uint64_t count = 0;
+    void* block = nullptr;
+    kpt::ParticleArrays arrays{};
+};
+
+namespace {
+
+bool edges_uniform(const double* e, int n, double* step_out) {
+    const double span = e[n] - e[0];
+    const double step = span / static_cast<double>(n);
+    if (!std::isfinite(step) || step <= 0.0) {
+        return false;
+    }
+    for (int i = 1; i <= n; ++i) {
+        const double current = e[i] - e[i - 1];
+        const double magnitude =
+            std::max({std::fabs(span), std::fabs(step), std::fabs(current), 1.0});
+        const double tolerance = 1024.0 * std::numeric_limits<double>::epsilon() * magnitude;
+        if (std::fabs(current - step) > tolerance) {
+            return false;
+        }
+    }
+    *step_out = step;
+    return true;
+}
+
+// Axis map for one dimension (analytic if the edges are uniform by the
+// reference reader's test, AthenaFieldReader.hpp:167-193; stored otherwise).
+int build_axis(int n, const double* e, kpt::Axis& axis, std::vector<double>& centers,
+               std::vector<int>& buckets) {
+    for (int i = 0; i <= n; ++i) {
+        if (!std::isfinite(e[i])) {
+            return set_error(KPT_ERROR_FORMAT, "field: non-finite face coordinate");
+        }
+        if (i > 0 && !(e[i] > e[i - 1])) {
+            return set_error(KPT_ERROR_FORMAT,
+                             "field: face coordinates must be strictly ascending");
+        }
+    }
+    axis = kpt::Axis{};
+    axis.n = n;
+    double step = 0.0;
+    if (edges_uniform(e, n, &step)) {
+        const double x0 = e[0];
+        axis.stored = 0;
+        axis.start = x0;
+        axis.step = step;
+        axis.lower = x0 + 0.0 * step;
+        axis.upper = x0 + static_cast<double>(n) * step;
+    } else {
+        const double w = e[n] - e[0];
+        std::vector<double> faces(static_cast<size_t>(n) + 5);
+        for (int k = -2; k <= n + 2; ++k) {
+            faces[k + 2] = k < 0 ? e[n + k] - w : (k > n ? e[k - n] + w : e[k]);
+        }
+        centers.resize(static_cast<size_t>(n) + 4);
+        for (int s = 0; s < n + 4; ++s) {
+            centers[s] = 0.5 * (faces[s] + faces[s + 1]);
+        }
+        axis.stored = 1;
+        axis.lower = faces[2];
+        axis.upper = faces[n + 2];
+        // Bucket index: for each of 4(n+4) equal buckets over the centre
+        // range, the interval whose left centre is the last <= bucket start.
+        const int m = 4 * (n + 4);
+        const double origin = centers.front();
+        const double span = centers.back() - origin;
+        buckets.resize(static_cast<size_t>(m));
+        int k = -2;
+        for (int b = 0; b < m; ++b) {
+            const double x = origin + span * (static_cast<double>(b) / m);
+            while (k < n && centers[k + 3] <= x) {
+                ++k;
+            }
+            buckets[b] = k;
+        }
+        axis.bucket_count = m;
+        axis.bucket_origin = origin;
+        axis.bucket_scale = static_cast<double>(m) / span;
+    }
+    axis.width = axis.upper - axis.lower;
+    axis.inv_width = axis.width != 0.0 ? 1.0 / axis.width : 0.0;
+    return KPT_OK;
+}
+
+// Reconnection2DSettings::validate, physics block (src/main.cpp:222-239).
+int validate_settings(const kpt_settings* s) {
+    if (s == nullptr) {
+        return set_error(KPT_ERROR_INVALID_ARGUMENT, "settings is NULL");
+    }
+    const bool ok = std::isfinite(s->mhd_dt) && s->mhd_dt > 0.0 && std::isfinite(s->p0) &&
+                    s->p0 > 0.0 && std::isfinite(s->pmin) && s->pmin > 0.0 &&
+                    std::isfinite(s->pmax) && s->pmax > s->pmin &&
+                    std::isfinite(s->gamma_turb) && std::isfinite(s->kpara0) &&
+                    s->kpara0 > 0.0 && std::isfinite(s->kperp_over_kpara) &&
+                    s->kperp_over_kpara >= 0.0 && std::isfinite(s->dt_min_rel) &&
+                    s->dt_min_rel > 0.0 && std::isfinite(s->dt_max_rel) &&
+                    s->dt_max_rel >= s->dt_min_rel && std::isfinite(s->drift_param1) &&
+                    std::isfinite(s->drift_param2) && std::isfinite(s->charge) &&
+                    s->charge != 0.0 && std::isfinite(s->particle_v0) &&
+                    s->particle_v0 > 0.0 && std::isfinite(s->duu0) && s->duu0 >= 0.0 &&
+                    std::isfinite(s->split_ratio) && s->split_ratio > 1.0 &&
+                    std::isfinite(s->pmin_split_over_p0) && s->pmin_split_over_p0 > 0.0 &&
+                    std::isfinite(s->mu_max) && s->mu_max > 0.0;
+    if (!ok) {
+        return set_error(KPT_ERROR_INVALID_ARGUMENT,
+                         "Reconnection2DSettings: invalid physical parameters.");
+    }
+    if (s->max_steps <= 0) {
+        return set_error(KPT_ERROR_INVALID_ARGUMENT,
+                         "Reconnection2DSettings: step guard must be positive.");
+    }
+    return KPT_OK;
+}
+
+// make_device_settings (src/main.cpp:596-636).
+kpt::DeviceSettings device_settings(const kpt_settings* s, const kpt::Grid& g) {
+    kpt::DeviceSettings d{};
+    d.x_lower = g.axis[0].lower;
+    d.x_upper = g.axis[0].upper;
+    d.y_lower = g.axis[1].lower;
+    d.y_upper = g.axis[1].upper;
+    d.x_width = d.x_upper - d.x_lower;
+    d.y_width = d.y_upper - d.y_lower;
+    d.dx = d.x_width / static_cast<double>(g.axis[0].n);
+    d.dy = d.y_width / static_cast<double>(g.axis[1].n);
+    d.shift_x = 0.5 * d.dx;
+    d.shift_y = 0.5 * d.dy;
+    d.mhd_dt = s->mhd_dt;
+    d.p0 = s->p0;
+    d.pmax = s->pmax;
+    d.gamma_turb = s->gamma_turb;
+    d.pindex = 3.0 - s->gamma_turb;
+    d.kpara0 = s->kpara0;
+    d.kperp_over_kpara = s->kperp_over_kpara;
+    d.dt_min = s->dt_min_rel * s->mhd_dt;
+    d.dt_max = s->dt_max_rel * s->mhd_dt;
+    d.drift_param1 = s->drift_param1;
+    d.drift_param2 = s->drift_param2;
+    d.charge = s->charge;
+    d.particle_v0 = s->particle_v0;
+    d.duu0 = s->duu0;
+    d.h0 = 0.2;  // Reconnection2DDeviceSettings::pitch_angle_scattering_h0
+    d.split_ratio = s->split_ratio;
+    d.pmin_split = s->pmin_split_over_p0 * s->p0;
+    d.mu_max = s->mu_max;
+    d.max_steps = s->max_steps;
+    d.momentum_dependency = s->momentum_dependency;
+    d.magnetic_dependency = s->magnetic_dependency;
+    d.time_interpolation = s->time_interpolation;
+    d.split_particles = s->split_particles;
+    d.focused = s->focused;
+    return d;
+}
+
+int activate(kpt_context* ctx) {
+    KPT_CUDA(cudaSetDevice(ctx->device));
+    return KPT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int kpt_abi_version(void) { return KPT_ABI_VERSION; }
+
+const char* kpt_last_error(void) { return g_last_error.c_str(); }
+
+void kpt_default_settings(kpt_settings* s) {
+    if (s == nullptr) {
+        return;
+    }
+    std::memset(s, 0, sizeof(*s));
+    s->mhd_dt = 0.1;
+    s->p0 = 0.1;
+    s->pmin = 1.0e-2;
+    s->pmax = 1.0e1;
+    s->gamma_turb = 1.6666667;
+    s->kpara0 = 0.00743592;
+    s->kperp_over_kpara = 0.01;
+    s->dt_min_rel = 1.0e-7;
+    s->dt_max_rel = 1.0e-2;
+    s->drift_param1 = 850964.408;
+    s->drift_param2 = 13575468.975;
+    s->charge = -1.0;
+    s->particle_v0 = 17.20195;
+    s->duu0 = 5578.445;
+    s->split_ratio = 2.0;
+    s->pmin_split_over_p0 = 2.0;
+    s->mu_max = 0.99;
+    s->max_steps = 200000;
+    s->momentum_dependency = 1;
+    s->magnetic_dependency = 1;
+    s->time_interpolation = 1;
+    s->split_particles = 1;
+    s->focused = 0;
+}
+
+int kpt_context_create(int device, kpt_context** out) {
+    KPT_REQUIRE(out != nullptr, "kpt_context_create: out is NULL");
+    *out = nullptr;
+    int count = 0;
+    const cudaError_t err = cudaGetDeviceCount(&count);
+    if (err != cudaSuccess || count == 0) {
+        return set_error(KPT_ERROR_NO_DEVICE,
+                         std::string("kpt_context_create: no CUDA device (") +
+                             cudaGetErrorString(err) + ")");
+    }
+    KPT_REQUIRE(device >= 0 && device < count, "kpt_context_create: device out of range");
+    std::unique_ptr<kpt_context> ctx(new (std::nothrow) kpt_context());
+    if (!ctx) {
+        return set_error(KPT_ERROR_OUT_OF_MEMORY, "kpt_context_create: host allocation");
+    }
+    ctx->device = device;
+    KPT_CUDA(cudaSetDevice(device));
+    int major = 0;
+    KPT_CUDA(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, device));
+    KPT_CUDA(cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device));
+    KPT_CUDA(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking));
+    ctx->stream = ctx->own_stream;
+    KPT_CUDA(ctx->counters.reserve(sizeof(kpt::PushCounters)));
+    *out = ctx.release();
+    return KPT_OK;
+}
+
+int kpt_context_destroy(kpt_context* ctx) {
+    if (ctx == nullptr) {
+        return KPT_OK;
+    }
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (DeviceBuffer* b : {&ctx->counters, &ctx->split_counts, &ctx->split_offsets,
+                            &ctx->split_totals, &ctx->split_levels, &ctx->hist_bins,
+                            &ctx->hist_edge_count, &ctx->hist_edge_index,
+                            &ctx->summary_partials, &ctx->summary_result, &ctx->sample_io}) {
+        b->release();
+    }
+    if (ctx->own_stream != nullptr) {
+        cudaStreamDestroy(ctx->own_stream);
+    }
+    delete ctx;
+    return KPT_OK;
+}
+
+int kpt_context_set_stream(kpt_context* ctx, void* cuda_stream) {
+    KPT_REQUIRE(ctx != nullptr, "kpt_context_set_stream: ctx is NULL");
+    ctx->stream = cuda_stream != nullptr ? static_cast<cudaStream_t>(cuda_stream)
+                                         : ctx->own_stream;
+    return KPT_OK;
+}
+
+int kpt_context_set_push_schedule(kpt_context* ctx, int schedule, int blocks_per_sm) {
+    KPT_REQUIRE(ctx != nullptr, "kpt_context_set_push_schedule: ctx is NULL");
+    KPT_REQUIRE(schedule == KPT_SCHEDULE_REFILL || schedule == KPT_SCHEDULE_SIMPLE,
+                "kpt_context_set_push_schedule: unknown schedule");
+    KPT_REQUIRE(blocks_per_sm >= 1 && blocks_per_sm <= 32,
+                "kpt_context_set_push_schedule: blocks_per_sm must be in [1, 32]");
+    ctx->push_schedule = schedule == KPT_SCHEDULE_SIMPLE ? kpt::kScheduleSimple
+                                                         : kpt::kScheduleRefill;
+    ctx->push_blocks_per_sm = blocks_per_sm;
+    return KPT_OK;
+}
+
+int kpt_context_synchronize(kpt_context* ctx) {
+    KPT_REQUIRE(ctx != nullptr, "kpt_context_synchronize: ctx is NULL");
+    if (int rc = activate(ctx)) return rc;
+    KPT_CUDA(cudaStreamSynchronize(ctx->stream));
+    return KPT_OK;
+}
+
+int kpt_field_create(kpt_context* ctx, int nx, int ny, const double* x_edges,
+                     const double* y_edges, const double* b_cells, const double* v_cells,
+                     int table_kind, int precision, kpt_field** out) {
+    KPT_REQUIRE(ctx != nullptr && out != nullptr, "kpt_field_create: NULL handle");
+    *out = nullptr;
+    KPT_REQUIRE(nx > 0 && ny > 0, "AthenaFieldReader: Athena binary dimensions must be positive.");
+    KPT_REQUIRE(x_edges && y_edges && b_cells && v_cells, "kpt_field_create: NULL array");
+    KPT_REQUIRE(table_kind == KPT_TABLE_PARKER16 || table_kind == KPT_TABLE_FOCUSED21,
+                "kpt_field_create: unknown table kind");
+    KPT_REQUIRE(precision == KPT_PRECISION_F64 || precision == KPT_PRECISION_MIXED,
+                "kpt_field_create: unknown precision");
+    const size_t cells = static_cast<size_t>(nx) * static_cast<size_t>(ny);
+    for (size_t k = 0; k < 3 * cells; ++k) {
+        if (!std::isfinite(b_cells[k]) || !std::isfinite(v_cells[k])) {
+            return set_error(KPT_ERROR_FORMAT, "AthenaFieldReader: non-finite field value.");
+        }
+    }
+    if (int rc = activate(ctx)) return rc;
+    struct FieldDeleter {
+        void operator()(kpt_field* doomed) const { kpt_field_destroy(doomed); }
+    };
+    std::unique_ptr<kpt_field, FieldDeleter> f(new kpt_field());
+    f->ctx = ctx;
+    f->nx = nx;
+    f->ny = ny;
+    f->kind = table_kind;
+    f->precision = precision;
+    f->stride = kpt::table_stride(table_kind == KPT_TABLE_FOCUSED21, precision);
+    f->points = static_cast<uint64_t>(nx + 4) * static_cast<uint64_t>(ny + 4);
+    f->grid.ex = nx + 4;
+    const double* edges[2] = {x_edges, y_edges};
+    const int counts[2] = {nx, ny};
+    for (int d = 0; d < 2; ++d) {
+        std::vector<double> centers;
+        std::vector<int> buckets;
+        if (int rc = build_axis(counts[d], edges[d], f->grid.axis[d], centers, buckets)) {
+            return rc;
+        }
+        if (!centers.empty()) {
+            KPT_CUDA(cudaMalloc(&f->centers[d], centers.size() * sizeof(double)));
+            KPT_CUDA(cudaMemcpy(f->centers[d], centers.data(), centers.size() * sizeof(double),
+                                cudaMemcpyHostToDevice));
+            KPT_CUDA(cudaMalloc(&f->buckets[d], buckets.size() * sizeof(int)));
+            KPT_CUDA(cudaMemcpy(f->buckets[d], buckets.data(), buckets.size() * sizeof(int),
+                                cudaMemcpyHostToDevice));
+            f->grid.axis[d].centers = f->centers[d];
+            f->grid.axis[d].buckets = f->buckets[d];
+        }
+    }
+    const size_t elem = precision == KPT_PRECISION_F64 ? sizeof(double) : sizeof(float);
+    KPT_CUDA(cudaMalloc(&f->table, f->points * f->stride * elem));
+    double* staging = nullptr;
+    KPT_CUDA(cudaMalloc(&staging, 6 * cells * sizeof(double)));
+    cudaError_t err = cudaMemcpyAsync(staging, b_cells, 3 * cells * sizeof(double),
+                                      cudaMemcpyHostToDevice, ctx->stream);
+    if (err == cudaSuccess) {
+        err = cudaMemcpyAsync(staging + 3 * cells, v_cells, 3 * cells * sizeof(double),
+                              cudaMemcpyHostToDevice, ctx->stream);
+    }
+    if (err == cudaSuccess) {
+        kpt::TableLaunch launch{};
+        launch.grid = f->grid;
+        launch.b_cells = staging;
+        launch.v_cells = staging + 3 * cells;
+        launch.table = f->table;
+        launch.focused = table_kind == KPT_TABLE_FOCUSED21;
+        launch.precision = precision;
+        err = kpt::launch_build_table(launch, ctx->stream);
+    }
+    if (err == cudaSuccess) {
+        err = cudaStreamSynchronize(ctx->stream);
+    }
+    cudaFree(staging);
+    if (err != cudaSuccess) {
+        return set_error(KPT_ERROR_CUDA,
+                         std::string("kpt_field_create: ") + cudaGetErrorString(err));
+    }
+    *out = f.release();
+    return KPT_OK;
+}
+
+// Compact field reader: layout and checks of AthenaFieldReader.hpp:290-360
+// (non-uniform edges accepted as an extension).
+int kpt_field_load(kpt_context* ctx, const char* path, int table_kind, int precision,
+                   kpt_field** out) {
+    KPT_REQUIRE(path != nullptr, "kpt_field_load: path is NULL");
+    std::ifstream stream(path, std::ios::binary);
+    if (!stream) {
+        return set_error(KPT_ERROR_IO, "AthenaFieldReader: failed to open Athena binary file.");
+    }
+    int32_t dims[2] = {0, 0};
+    stream.read(reinterpret_cast<char*>(dims), sizeof(dims));
+    if (!stream) {
+        return set_error(KPT_ERROR_FORMAT, "AthenaFieldReader: failed to read nx.");
+    }
+    const int nx = dims[0], ny = dims[1];
+    if (nx <= 0 || ny <= 0) {
+        return set_error(KPT_ERROR_FORMAT,
+                         "AthenaFieldReader: Athena binary dimensions must be positive.");
+    }
+    const size_t cells = static_cast<size_t>(nx) * static_cast<size_t>(ny);
+    std::vector<double> xe(static_cast<size_t>(nx) + 1), ye(static_cast<size_t>(ny) + 1);
+    std::vector<double> b(3 * cells), v(3 * cells);
+    auto read = [&](std::vector<double>& dst, size_t offset, size_t n, const char* name) -> int {
+        stream.read(reinterpret_cast<char*>(dst.data() + offset),
+                    static_cast<std::streamsize>(n * sizeof(double)));
+        if (!stream) {
+            return set_error(KPT_ERROR_FORMAT,
+                             std::string("AthenaFieldReader: failed to read ") + name + ".");
+        }
+        return KPT_OK;
+    };
+    if (int rc = read(xe, 0, xe.size(), "x_edges")) return rc;
+    if (int rc = read(ye, 0, ye.size(), "y_edges")) return rc;
+    const char* names[6] = {"Bx", "By", "Bz", "Vx", "Vy", "Vz"};
+    for (int c = 0; c < 3; ++c) {
+        if (int rc = read(b, c * cells, cells, names[c])) return rc;
+    }
+    for (int c = 0; c < 3; ++c) {
+        if (int rc = read(v, c * cells, cells, names[3 + c])) return rc;
+    }
+    if (stream.peek() != std::char_traits<char>::eof()) {
+        return set_error(KPT_ERROR_FORMAT,
+                         "AthenaFieldReader: Athena binary file has trailing payload.");
+    }
+    return kpt_field_create(ctx, nx, ny, xe.data(), ye.data(), b.data(), v.data(), table_kind,
+                            precision, out);
+}
+
+int kpt_field_destroy(kpt_field* field) {
+    if (field == nullptr) {
+        return KPT_OK;
+    }
+    cudaSetDevice(field->ctx->device);
+    cudaStreamSynchronize(field->ctx->stream);
+    cudaFree(field->table);
+    for (int d = 0; d < 2; ++d) {
+        cudaFree(field->centers[d]);
+        cudaFree(field->buckets[d]);
+    }
+    delete field;
+    return KPT_OK;
+}
+
+int kpt_field_shape(const kpt_field* field, int* nx, int* ny, uint64_t* points,
+                    int* components) {
+    KPT_REQUIRE(field != nullptr, "kpt_field_shape: field is NULL");
+    if (nx) *nx = field->nx;
+    if (ny) *ny = field->ny;
+    if (points) *points = field->points;
+    if (components) *components = field->kind == KPT_TABLE_FOCUSED21 ? 21 : 16;
+    return KPT_OK;
+}
+
+int kpt_field_download_table(const kpt_field* field, double* out, uint64_t out_len) {
+    KPT_REQUIRE(field != nullptr && out != nullptr, "kpt_field_download_table: NULL");
+    const int ncomp = field->kind == KPT_TABLE_FOCUSED21 ? 21 : 16;
+    KPT_REQUIRE(out_len >= field->points * ncomp, "kpt_field_download_table: out too small");
+    if (int rc = activate(field->ctx)) return rc;
+    const size_t n = field->points * field->stride;
+    if (field->precision == KPT_PRECISION_F64) {
+        std::vector<double> host(n);
+        KPT_CUDA(cudaMemcpyAsync(host.data(), field->table, n * sizeof(double),
+                                 cudaMemcpyDeviceToHost, field->ctx->stream));
+        KPT_CUDA(cudaStreamSynchronize(field->ctx->stream));
+        for (uint64_t p = 0; p < field->points; ++p) {
+            for (int c = 0; c < ncomp; ++c) {
+                out[p * ncomp + c] = host[p * field->stride + c];
+            }
+        }
+    } else {
+        std::vector<float> host(n);
+        KPT_CUDA(cudaMemcpyAsync(host.data(), field->table, n * sizeof(float),
+                                 cudaMemcpyDeviceToHost, field->ctx->stream));
+        KPT_CUDA(cudaStreamSynchronize(field->ctx->stream));
+        for (uint64_t p = 0; p < field->points; ++p) {
+            for (int c = 0; c < ncomp; ++c) {
+                out[p * ncomp + c] = static_cast<double>(host[p * field->stride + c]);
+            }
+        }
+    }
+    return KPT_OK;
+}
+
+int kpt_particles_create(kpt_context* ctx, uint64_t capacity, kpt_particles** out) {
+    KPT_REQUIRE(ctx != nullptr && out != nullptr, "kpt_particles_create: NULL handle");
+    *out = nullptr;
+    KPT_REQUIRE(capacity > 0,
+                "Reconnection2DSettings: particle counts and capacity must be positive.");
+    KPT_REQUIRE(capacity < (1ull << 32), "kpt_particles_create: capacity must be < 2^32");
+    if (int rc = activate(ctx)) return rc;
+    std::unique_ptr<kpt_particles> parts(new kpt_particles());
+    parts->ctx = ctx;
+    parts->capacity = capacity;
+    // One allocation: 7 double arrays then 2 int32 arrays, each 256-byte aligned.
+    auto round_up = [](size_t v) { return (v + 255) & ~static_cast<size_t>(255); };
+    const size_t dbytes = round_up(capacity * sizeof(double));
+    const size_t ibytes = round_up(capacity * sizeof(int32_t));
+    KPT_CUDA(cudaMalloc(&parts->block, 7 * dbytes + 2 * ibytes));
+    char* base = static_cast<char*>(parts->block);
+    double** dptrs[7] = {&parts->arrays.x, &parts->arrays.y, &parts->arrays.p,
+                         &parts->arrays.t, &parts->arrays.step_dt, &parts->arrays.weight,
+                         &parts->arrays.mu};
+    for (int k = 0; k < 7; ++k) {
+        *dptrs[k] = reinterpret_cast<double*>(base + k * dbytes);
+    }
+    parts->arrays.status = reinterpret_cast<int32_t*>(base + 7 * dbytes);
+    parts->arrays.split_level = reinterpret_cast<int32_t*>(base + 7 * dbytes + ibytes);
+    // Storage starts zeroed with status 2 (src/main.cpp:326-331).
+    KPT_CUDA(cudaMemsetAsync(parts->block, 0, 7 * dbytes + 2 * ibytes, ctx->stream));
+    std::vector<int32_t> twos(capacity, 2);
+    KPT_CUDA(cudaMemcpyAsync(parts->arrays.status, twos.data(), capacity * sizeof(int32_t),
+                             cudaMemcpyHostToDevice, ctx->stream));
+    KPT_CUDA(cudaStreamSynchronize(ctx->stream));
+    *out = parts.release();
+    return KPT_OK;
+}
+
+int kpt_particles_destroy(kpt_particles* parts) {
+    if (parts == nullptr) {
+        return KPT_OK;
+    }
+    cudaSetDevice(parts->ctx->device);
+    cudaStreamSynchronize(parts->ctx->stream);
+    cudaFree(parts->block);
+    delete parts;
+    return KPT_OK;
+}
+
+int kpt_particles_count(const kpt_particles* parts, uint64_t* count, uint64_t* capacity) {
+    KPT_REQUIRE(parts != nullptr, "kpt_particles_count: NULL handle");
+    if (count) *count = parts->count;
+    if (capacity) *capacity = parts->capacity;
+    return KPT_OK;
+}
+
+int kpt_particles_set_count(kpt_particles* parts, uint64_t count) {
+    KPT_REQUIRE(parts != nullptr, "kpt_particles_set_count: NULL handle");
+    KPT_REQUIRE(count <= parts->capacity, "kpt_particles_set_count: count exceeds capacity");
+    parts->count = count;
+    return KPT_OK;
+}
+
+int kpt_particles_upload(kpt_particles* parts, uint64_t count, const double* x,
+                         const double* y, const double* p, const double* t,
+                         const double* step_dt, const double* weight, const double* mu,
+                         const int32_t* status, const int32_t* split_level) {
+    KPT_REQUIRE(parts != nullptr, "kpt_particles_upload: NULL handle");
+    KPT_REQUIRE(count <= parts->capacity, "kpt_particles_upload: count exceeds capacity");
+    if (int rc = activate(parts->ctx)) return rc;
+    cudaStream_t s = parts->ctx->stream;
+    const kpt::ParticleArrays& a = parts->arrays;
+    const void* src[9] = {x, y, p, t, step_dt, weight, mu, status, split_level};
+    void* dst[9] = {a.x, a.y, a.p, a.t, a.step_dt, a.weight, a.mu, a.status, a.split_level};
+    for (int k = 0; k < 9; ++k) {
+        if (src[k] != nullptr && count > 0) {
+            const size_t elem = k < 7 ? sizeof(double) : sizeof(int32_t);
+            KPT_CUDA(cudaMemcpyAsync(dst[k], src[k], count * elem, cudaMemcpyHostToDevice, s));
+        }
+    }
+    KPT_CUDA(cudaStreamSynchronize(s));
+    parts->count = count;
+    return KPT_OK;
+}
+
+int kpt_particles_download(const kpt_particles* parts, uint64_t count, double* x, double* y,
+                           double* p, double* t, double* step_dt, double* weight, double* mu,
+                           int32_t* status, int32_t* split_level) {
+    KPT_REQUIRE(parts != nullptr, "kpt_particles_download: NULL handle");
+    KPT_REQUIRE(count <= parts->capacity, "kpt_particles_download: count exceeds capacity");
+    if (int rc = activate(parts->ctx)) return rc;
+    cudaStream_t s = parts->ctx->stream;
+    const kpt::ParticleArrays& a = parts->arrays;
+    void* dst[9] = {x, y, p, t, step_dt, weight, mu, status, split_level};
+    const void* src[9] = {a.x, a.y, a.p, a.t, a.step_dt, a.weight, a.mu, a.status,
+                          a.split_level};
+    for (int k = 0; k < 9; ++k) {
+        if (dst[k] != nullptr && count > 0) {
+            const size_t elem = k < 7 ? sizeof(double) : sizeof(int32_t);
+            KPT_CUDA(cudaMemcpyAsync(dst[k], src[k], count * elem, cudaMemcpyDeviceToHost, s));
+        }
+    }
+    KPT_CUDA(cudaStreamSynchronize(s));
+    return KPT_OK;
+}
+
+int kpt_particles_device_arrays(const kpt_particles* parts, kpt_particle_arrays* out) {
+    KPT_REQUIRE(parts != nullptr && out != nullptr, "kpt_particles_device_arrays: NULL");
+    const kpt::ParticleArrays& a = parts->arrays;
+    out->x = a.x;
+    out->y = a.y;
+    out->p = a.p;
+    out->t = a.t;
+    out->step_dt = a.step_dt;
+    out->weight = a.weight;
+    out->mu = a.mu;
+    out->status = a.status;
+    out->split_level = a.split_level;
+    return KPT_OK;
+}
+
+int kpt_inject_uniform(kpt_context* ctx, kpt_particles* parts, const kpt_field* grid,
+                       const kpt_settings* settings, uint64_t requested, uint32_t frame,
+                       uint64_t seed, double band_lo, double band_hi, uint64_t* injected) {
+    KPT_REQUIRE(ctx && parts && grid, "kpt_inject_uniform: NULL handle");
+    if (int rc = validate_settings(settings)) return rc;
+    if (injected) *injected = 0;
+    if (parts->count >= parts->capacity) {
+        return KPT_OK;
+    }
+    if (int rc = activate(ctx)) return rc;
+    const uint64_t n = std::min(requested, parts->capacity - parts->count);
+    const kpt::DeviceSettings d = device_settings(settings, grid->grid);
+    kpt::InjectLaunch launch{};
+    launch.parts = parts->arrays;
+    launch.first = parts->count;
+    launch.n = n;
+    launch.x_lower = d.x_lower;
+    launch.x_upper = d.x_upper;
+    launch.y_lower = band_lo < band_hi ? band_lo : d.y_lower;
+    launch.y_upper = band_lo < band_hi ? band_hi : d.y_upper;
+    launch.p0 = settings->p0;
+    launch.interval_start = static_cast<double>(frame) * settings->mhd_dt;
+    launch.mhd_dt = settings->mhd_dt;
+    launch.dt_min = d.dt_min;
+    launch.mu_max = settings->mu_max;
+    launch.frame = frame;
+    launch.seed = seed;
+    KPT_CUDA(kpt::launch_inject(launch, ctx->stream));
+    parts->count += n;
+    if (injected) *injected = n;
+    return KPT_OK;
+}
+
+int kpt_push_interval(kpt_context* ctx, kpt_particles* parts, const kpt_field* lower,
+                      const kpt_field* upper, const kpt_settings* settings, uint32_t frame,
+                      uint64_t seed, kpt_push_stats* stats) {
+    KPT_REQUIRE(ctx && parts && lower && upper, "kpt_push_interval: NULL handle");
+    if (int rc = validate_settings(settings)) return rc;
+    KPT_REQUIRE(lower->kind == upper->kind && lower->precision == upper->precision &&
+                    lower->nx == upper->nx && lower->ny == upper->ny,
+                "kpt_push_interval: lower and upper tables differ in kind, precision or shape");
+    KPT_REQUIRE((lower->kind == KPT_TABLE_FOCUSED21) == (settings->focused != 0),
+                "kpt_push_interval: table kind does not match settings.focused");
+    if (int rc = activate(ctx)) return rc;
+    kpt::PushLaunch launch{};
+    launch.grid = lower->grid;
+    launch.lower = lower->table;
+    launch.upper = upper->table;
+    launch.parts = parts->arrays;
+    launch.count = parts->count;
+    launch.settings = device_settings(settings, lower->grid);
+    launch.interval_start = static_cast<double>(frame) * settings->mhd_dt;
+    launch.interval_end = launch.interval_start + settings->mhd_dt;
+    launch.frame = frame;
+    launch.seed = seed;
+    launch.counters = ctx->counters.as<kpt::PushCounters>();
+    launch.precision = lower->precision;
+    launch.focused = settings->focused != 0;
+    launch.schedule = ctx->push_schedule;
+    launch.sm_count = ctx->sm_count;
+    launch.blocks_per_sm = ctx->push_blocks_per_sm;
+    KPT_CUDA(cudaMemsetAsync(launch.counters, 0, sizeof(kpt::PushCounters), ctx->stream));
+    if (parts->count > 0) {
+        KPT_CUDA(kpt::launch_push_interval(launch, ctx->stream));
+    }
+    if (stats != nullptr) {
+        kpt::PushCounters host{};
+        KPT_CUDA(cudaMemcpyAsync(&host, launch.counters, sizeof(host), cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+        KPT_CUDA(cudaStreamSynchronize(ctx->stream));
+        stats->particle_steps = host.particle_steps;
+        stats->pushed = host.pushed;
+        stats->failed = host.failed;
+        stats->max_steps = host.max_steps;
+        stats->pad = 0;
+    }
+    return KPT_OK;
+}
+
+int kpt_split(kpt_context* ctx, kpt_particles* parts, const kpt_settings* settings,
+              uint64_t* split, uint64_t* skipped) {
+    KPT_REQUIRE(ctx && parts, "kpt_split: NULL handle");
+    if (int rc = validate_settings(settings)) return rc;
+    if (split) *split = 0;
+    if (skipped) *skipped = 0;
+    if (parts->count >= parts->capacity || settings->split_particles == 0) {
+        return KPT_OK;
+    }
+    if (int rc = activate(ctx)) return rc;
+    // Per-level thresholds pmin_split * ratio^level (host pow) up to the first
+    // level whose threshold exceeds pmax; later levels can never split.
+    const double pmin_split = settings->pmin_split_over_p0 * settings->p0;
+    if (ctx->split_level_count == 0 || ctx->split_key[0] != pmin_split ||
+        ctx->split_key[1] != settings->split_ratio || ctx->split_key[2] != settings->pmax) {
+        std::vector<double> thresholds;
+        for (int level = 0; level < 65536; ++level) {
+            const double thr = pmin_split * std::pow(settings->split_ratio,
+                                                     static_cast<double>(level));
+            thresholds.push_back(thr);
+            if (!(thr < settings->pmax)) {
+                break;
+            }
+        }
+        if (thresholds.back() < settings->pmax) {
+            return set_error(KPT_ERROR_INVALID_ARGUMENT,
+                             "kpt_split: split ratio too close to 1 for the level table");
+        }
+        const int levels = static_cast<int>(thresholds.size());
+        std::vector<double> table(2 * static_cast<size_t>(levels));
+        for (int level = 0; level < levels; ++level) {
+            table[level] = thresholds[level];
+            table[levels + level] = std::pow(0.5, static_cast<double>(level + 1));
+        }
+        KPT_CUDA(ctx->split_levels.reserve(table.size() * sizeof(double)));
+        KPT_CUDA(cudaMemcpyAsync(ctx->split_levels.ptr, table.data(),
+                                 table.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                 ctx->stream));
+        ctx->split_level_count = levels;
+        ctx->split_key[0] = pmin_split;
+        ctx->split_key[1] = settings->split_ratio;
+        ctx->split_key[2] = settings->pmax;
+    }
+    const size_t nblocks = kpt::split_scratch_blocks(parts->count);
+    KPT_CUDA(ctx->split_counts.reserve(std::max<size_t>(nblocks, 1) * sizeof(unsigned int)));
+    KPT_CUDA(ctx->split_offsets.reserve(std::max<size_t>(nblocks, 1) *
+                                        sizeof(unsigned long long)));
+    KPT_CUDA(ctx->split_totals.reserve(2 * sizeof(unsigned long long)));
+    kpt::SplitLaunch launch{};
+    launch.parts = parts->arrays;
+    launch.count = parts->count;
+    launch.capacity = parts->capacity;
+    launch.thresholds = ctx->split_levels.as<double>();
+    launch.weights = ctx->split_levels.as<double>() + ctx->split_level_count;
+    launch.level_count = ctx->split_level_count;
+    launch.pmax = settings->pmax;
+    launch.block_counts = ctx->split_counts.as<unsigned int>();
+    launch.block_offsets = ctx->split_offsets.as<unsigned long long>();
+    launch.totals = ctx->split_totals.as<unsigned long long>();
+    KPT_CUDA(kpt::launch_split(launch, ctx->stream));
+    unsigned long long wanted = 0;
+    KPT_CUDA(cudaMemcpyAsync(&wanted, launch.totals, sizeof(wanted), cudaMemcpyDeviceToHost,
+                             ctx->stream));
+    KPT_CUDA(cudaStreamSynchronize(ctx->stream));
+    const uint64_t room = parts->capacity - parts->count;
+    const uint64_t written = std::min<uint64_t>(wanted, room);
+    parts->count += written;
+    if (split) *split = written;
+    if (skipped) *skipped = wanted - written;
+    return KPT_OK;
+}
+
+int kpt_histogram(kpt_context* ctx, const kpt_particles* parts, double pmin, double pmax,
+                  int nbins, double* bins) {
+    KPT_REQUIRE(ctx && parts && bins, "kpt_histogram: NULL argument");
+    KPT_REQUIRE(nbins > 0 && nbins <= 4096, "kpt_histogram: nbins must be in [1, 4096]");
+    KPT_REQUIRE(std::isfinite(pmin) && std::isfinite(pmax) && pmin > 0.0 && pmax > pmin,
+                "kpt_histogram: need 0 < pmin < pmax");
+    if (int rc = activate(ctx)) return rc;
+    const uint64_t count = parts->count;
+    KPT_CUDA(ctx->hist_bins.reserve(sizeof(double) * nbins));
+    KPT_CUDA(ctx->hist_edge_count.reserve(sizeof(unsigned long long)));
+    KPT_CUDA(ctx->hist_edge_index.reserve(sizeof(unsigned int) * std::max<uint64_t>(count, 1)));
+    const double log_pmin = std::log(pmin);
+    const double inv_dlogp = static_cast<double>(nbins) / (std::log(pmax) - log_pmin);
+    kpt::HistogramLaunch launch{};
+    launch.p = parts->arrays.p;
+    launch.weight = parts->arrays.weight;
+    launch.status = parts->arrays.status;
+    launch.count = count;
+    launch.pmin = pmin;
+    launch.pmax = pmax;
+    launch.log_pmin = log_pmin;
+    launch.inv_dlogp = inv_dlogp;
+    launch.nbins = nbins;
+    launch.bins = ctx->hist_bins.as<double>();
+    launch.edge_count = ctx->hist_edge_count.as<unsigned long long>();
+    launch.edge_index = ctx->hist_edge_index.as<unsigned int>();
+    KPT_CUDA(kpt::launch_histogram(launch, ctx->stream));
+    unsigned long long edges = 0;
+    KPT_CUDA(cudaMemcpyAsync(bins, launch.bins, sizeof(double) * nbins, cudaMemcpyDeviceToHost,
+                             ctx->stream));
+    KPT_CUDA(cudaMemcpyAsync(&edges, launch.edge_count, sizeof(edges), cudaMemcpyDeviceToHost,
+                             ctx->stream));
+    KPT_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (edges > 0) {
+        // Host re-binning of particles whose bin coordinate sits within 1e-7
+        // of an edge, with the host log the reference uses.
+        std::vector<unsigned int> index(edges);
+        KPT_CUDA(cudaMemcpy(index.data(), launch.edge_index, edges * sizeof(unsigned int),
+                            cudaMemcpyDeviceToHost));
+        for (unsigned long long k = 0; k < edges; ++k) {
+            double p = 0.0, w = 0.0;
+            KPT_CUDA(cudaMemcpy(&p, parts->arrays.p + index[k], sizeof(double),
+                                cudaMemcpyDeviceToHost));
+            KPT_CUDA(cudaMemcpy(&w, parts->arrays.weight + index[k], sizeof(double),
+                                cudaMemcpyDeviceToHost));
+            int bin = static_cast<int>((std::log(p) - log_pmin) * inv_dlogp);
+            bin = bin < 0 ? 0 : (bin >= nbins ? nbins - 1 : bin);
+            bins[bin] += w;
+        }
+    }
+    return KPT_OK;
+}
+
+int kpt_summarize(kpt_context* ctx, const kpt_particles* parts, kpt_summary* out) {
+    KPT_REQUIRE(ctx && parts && out, "kpt_summarize: NULL argument");
+    std::memset(out, 0, sizeof(*out));
+    out->stored = parts->count;
+    if (parts->count == 0) {
+        return KPT_OK;
+    }
+    if (int rc = activate(ctx)) return rc;
+    const int nblocks = kpt::summary_blocks(parts->count);
+    KPT_CUDA(ctx->summary_partials.reserve(sizeof(kpt::SummaryPartial) * nblocks));
+    KPT_CUDA(ctx->summary_result.reserve(sizeof(kpt::SummaryPartial)));
+    kpt::SummaryLaunch launch{};
+    launch.p = parts->arrays.p;
+    launch.dt = parts->arrays.step_dt;
+    launch.weight = parts->arrays.weight;
+    launch.status = parts->arrays.status;
+    launch.level = parts->arrays.split_level;
+    launch.count = parts->count;
+    launch.partials = ctx->summary_partials.as<kpt::SummaryPartial>();
+    launch.result = ctx->summary_result.as<kpt::SummaryPartial>();
+    KPT_CUDA(kpt::launch_summary(launch, ctx->stream));
+    kpt::SummaryPartial r{};
+    KPT_CUDA(cudaMemcpyAsync(&r, launch.result, sizeof(r), cudaMemcpyDeviceToHost, ctx->stream));
+    KPT_CUDA(cudaStreamSynchronize(ctx->stream));
+    out->active = r.active;
+    out->inactive = r.inactive;
+    out->weight_sum = r.weight_sum;
+    out->max_split_level = r.max_level;
+    if (r.active > 0) {
+        out->p_min = r.p_min;
+        out->p_max = r.p_max;
+        out->dt_min = r.dt_min;
+        out->dt_max = r.dt_max;
+        out->p_avg = r.p_sum / static_cast<double>(r.active);
+        out->dt_avg = r.dt_sum / static_cast<double>(r.active);
+    }
+    return KPT_OK;
+}
+
+int kpt_sample_table(kpt_context* ctx, const kpt_field* lower, const kpt_field* upper,
+                     uint64_t n, const double* x, const double* y, const double* rt,
+                     int time_interpolation, double* out) {
+    KPT_REQUIRE(ctx && lower && upper && out && x && y && rt, "kpt_sample_table: NULL argument");
+    KPT_REQUIRE(lower->kind == upper->kind && lower->precision == upper->precision &&
+                    lower->nx == upper->nx && lower->ny == upper->ny,
+                "kpt_sample_table: tables differ");
+    if (n == 0) {
+        return KPT_OK;
+    }
+    if (int rc = activate(ctx)) return rc;
+    const int ncomp = lower->kind == KPT_TABLE_FOCUSED21 ? 21 : 16;
+    const size_t bytes = n * sizeof(double) * (3 + ncomp);
+    KPT_CUDA(ctx->sample_io.reserve(bytes));
+    double* dx = ctx->sample_io.as<double>();
+    double* dy = dx + n;
+    double* drt = dy + n;
+    double* dout = drt + n;
+    KPT_CUDA(cudaMemcpyAsync(dx, x, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    KPT_CUDA(cudaMemcpyAsync(dy, y, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    KPT_CUDA(cudaMemcpyAsync(drt, rt, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    kpt::SampleLaunch launch{};
+    launch.grid = lower->grid;
+    launch.lower = lower->table;
+    launch.upper = upper->table;
+    launch.x = dx;
+    launch.y = dy;
+    launch.rt = drt;
+    launch.n = n;
+    const kpt::Axis& ax = lower->grid.axis[0];
+    const kpt::Axis& ay = lower->grid.axis[1];
+    launch.shift_x = 0.5 * ((ax.upper - ax.lower) / static_cast<double>(ax.n));
+    launch.shift_y = 0.5 * ((ay.upper - ay.lower) / static_cast<double>(ay.n));
+    launch.time_interpolation = time_interpolation;
+    launch.focused = lower->kind == KPT_TABLE_FOCUSED21;
+    launch.precision = lower->precision;
+    launch.out = dout;
+    KPT_CUDA(kpt::launch_sample(launch, ctx->stream));
+    KPT_CUDA(cudaMemcpyAsync(out, dout, n * ncomp * sizeof(double), cudaMemcpyDeviceToHost,
+                             ctx->stream));
+    KPT_CUDA(cudaStreamSynchronize(ctx->stream));
+    return KPT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,135 @@
+// Internal interfaces between the C-ABI layer (kpt_api.cpp) and the kernel
+// translation units.  Host-only code may include this header.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "kpt_types.h"
+
+namespace kpt {
+
+enum Precision : int { kPrecisionF64 = 0, kPrecisionMixed = 1 };
+enum Schedule : int { kScheduleRefill = 0, kScheduleSimple = 1 };
+
+// Table row stride (elements) for a kind/precision: rows start on 16-byte
+// boundaries so a point is streamed with 128-bit loads.
+inline int table_stride(int focused, int precision) {
+    if (!focused) {
+        return 16;
+    }
+    return precision == kPrecisionF64 ? 22 : 24;
+}
+
+struct PushLaunch {
+    Grid grid;
+    const void* lower;
+    const void* upper;
+    ParticleArrays parts;
+    uint64_t count;
+    DeviceSettings settings;
+    double interval_start;
+    double interval_end;
+    uint32_t frame;
+    uint64_t seed;
+    PushCounters* counters;
+    int precision;
+    int focused;
+    int schedule;
+    int sm_count;
+    int blocks_per_sm;
+};
+
+cudaError_t launch_push_interval(const PushLaunch& launch, cudaStream_t stream);
+
+// Coefficient table from cell-centred B and V (3 x ny x nx each, device).
+struct TableLaunch {
+    Grid grid;
+    const double* b_cells;
+    const double* v_cells;
+    void* table;
+    int focused;
+    int precision;
+};
+cudaError_t launch_build_table(const TableLaunch& launch, cudaStream_t stream);
+
+struct InjectLaunch {
+    ParticleArrays parts;
+    uint64_t first;
+    uint64_t n;
+    double x_lower, x_upper, y_lower, y_upper;
+    double p0, interval_start, mhd_dt, dt_min, mu_max;
+    uint32_t frame;
+    uint64_t seed;
+};
+cudaError_t launch_inject(const InjectLaunch& launch, cudaStream_t stream);
+
+// Split scratch: per-block counts (one per 1024 particles) and a 2-word
+// result {children wanted, children written}.
+struct SplitLaunch {
+    ParticleArrays parts;
+    uint64_t count;
+    uint64_t capacity;
+    const double* thresholds;  // per split level, host-computed
+    const double* weights;     // 0.5^(level+1) per level
+    int level_count;
+    double pmax;
+    unsigned int* block_counts;
+    unsigned long long* block_offsets;
+    unsigned long long* totals;
+};
+size_t split_scratch_blocks(uint64_t count);
+cudaError_t launch_split(const SplitLaunch& launch, cudaStream_t stream);
+
+struct HistogramLaunch {
+    const double* p;
+    const double* weight;
+    const int32_t* status;
+    uint64_t count;
+    double pmin, pmax, log_pmin, inv_dlogp;
+    int nbins;
+    double* bins;                       // nbins, zeroed by the kernel launcher
+    unsigned long long* edge_count;     // near-edge particles set aside
+    unsigned int* edge_index;           // capacity >= count
+};
+cudaError_t launch_histogram(const HistogramLaunch& launch, cudaStream_t stream);
+
+struct SummaryPartial {
+    unsigned long long active;
+    unsigned long long inactive;
+    double weight_sum, p_sum, dt_sum;
+    double p_min, p_max, dt_min, dt_max;
+    int max_level;
+    int pad;
+};
+struct SummaryLaunch {
+    const double* p;
+    const double* dt;
+    const double* weight;
+    const int32_t* status;
+    const int32_t* level;
+    uint64_t count;
+    SummaryPartial* partials;  // summary_blocks(count) entries
+    SummaryPartial* result;    // one entry
+};
+int summary_blocks(uint64_t count);
+cudaError_t launch_summary(const SummaryLaunch& launch, cudaStream_t stream);
+
+struct SampleLaunch {
+    Grid grid;
+    const void* lower;
+    const void* upper;
+    const double* x;
+    const double* y;
+    const double* rt;
+    uint64_t n;
+    double shift_x, shift_y;
+    int time_interpolation;
+    int focused;
+    int precision;
+    double* out;
+};
+cudaError_t launch_sample(const SampleLaunch& launch, cudaStream_t stream);
+
+}  // namespace kpt

@@ -1,0 +1,340 @@
+// Particle lifecycle kernels: uniform injection, deterministic momentum
+// split, weighted log-momentum histogram and the run summary reductions.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "kpt_device.cuh"
+#include "kpt_internal.h"
+
+namespace kpt {
+namespace {
+
+// ------------------------------------------------------------- inject
+// inject_uniform_particles (reference src/main.cpp:996-1048): four draws per
+// new particle in the order x, y, t, mu from the stream (seed, k, frame, 1).
+__global__ void inject_kernel(const InjectLaunch L) {
+    const uint2 key = seed_key(L.seed);
+    for (uint64_t k = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; k < L.n;
+         k += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        const uint32_t stream = static_cast<uint32_t>(k);
+        const uint4 r0 = philox4x32_10(make_uint4(0u, stream, L.frame, kTagInject), key);
+        const uint4 r1 = philox4x32_10(make_uint4(1u, stream, L.frame, kTagInject), key);
+        const uint64_t n = L.first + k;
+        const ParticleArrays& a = L.parts;
+        a.x[n] = __dadd_rn(L.x_lower,
+                           __dmul_rn(__dsub_rn(L.x_upper, L.x_lower), u01_f64(r0.x, r0.y)));
+        a.y[n] = __dadd_rn(L.y_lower,
+                           __dmul_rn(__dsub_rn(L.y_upper, L.y_lower), u01_f64(r0.z, r0.w)));
+        a.p[n] = L.p0;
+        a.t[n] = __dadd_rn(L.interval_start,
+                           __dadd_rn(0.0, __dmul_rn(__dsub_rn(L.mhd_dt, 0.0),
+                                                    u01_f64(r1.x, r1.y))));
+        a.step_dt[n] = L.dt_min;
+        a.weight[n] = 1.0;
+        a.mu[n] = __dmul_rn(L.mu_max, __dsub_rn(__dmul_rn(2.0, u01_f64(r1.z, r1.w)), 1.0));
+        a.status[n] = 0;
+        a.split_level[n] = 0;
+    }
+}
+
+// -------------------------------------------------------------- split
+// split_particles (src/main.cpp:1761-1839) with children appended in parent
+// order: per-block eligible counts, one exclusive scan over the blocks, then
+// a ballot/popc rank inside each block.  Thresholds and child weights per
+// split level come from the host (glibc pow), so eligibility is decided on
+// the same doubles as the reference.
+constexpr int kSplitBlock = 1024;
+
+__device__ __forceinline__ bool split_eligible(const SplitLaunch& L, uint64_t i) {
+    if (i >= L.count || L.parts.status[i] != 0) {
+        return false;
+    }
+    const int level = L.parts.split_level[i];
+    if (level < 0 || level >= L.level_count) {
+        return false;
+    }
+    const double p = L.parts.p[i];
+    return p > __ldg(L.thresholds + level) && p <= L.pmax;
+}
+
+__global__ void __launch_bounds__(kSplitBlock) split_count_kernel(const SplitLaunch L) {
+    const uint64_t i = blockIdx.x * static_cast<uint64_t>(kSplitBlock) + threadIdx.x;
+    const int n = __syncthreads_count(split_eligible(L, i) ? 1 : 0);
+    if (threadIdx.x == 0) {
+        L.block_counts[blockIdx.x] = static_cast<unsigned int>(n);
+    }
+}
+
+// Exclusive scan of the block counts by one block (fixed order).
+__global__ void __launch_bounds__(1024) split_scan_kernel(const SplitLaunch L, int nblocks) {
+    __shared__ unsigned long long warp_sums[32];
+    __shared__ unsigned long long carry;
+    if (threadIdx.x == 0) {
+        carry = 0;
+    }
+    __syncthreads();
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned warp = threadIdx.x >> 5;
+    for (int base = 0; base < nblocks; base += 1024) {
+        const int idx = base + static_cast<int>(threadIdx.x);
+        const unsigned long long v = idx < nblocks ? L.block_counts[idx] : 0ull;
+        unsigned long long inclusive = v;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const unsigned long long y = __shfl_up_sync(0xffffffffu, inclusive, off);
+            if (lane >= static_cast<unsigned>(off)) inclusive += y;
+        }
+        if (lane == 31u) warp_sums[warp] = inclusive;
+        __syncthreads();
+        if (warp == 0) {
+            unsigned long long w = warp_sums[lane];
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const unsigned long long y = __shfl_up_sync(0xffffffffu, w, off);
+                if (lane >= static_cast<unsigned>(off)) w += y;
+            }
+            warp_sums[lane] = w;
+        }
+        __syncthreads();
+        const unsigned long long warp_prefix = warp == 0 ? 0ull : warp_sums[warp - 1];
+        if (idx < nblocks) {
+            L.block_offsets[idx] = carry + warp_prefix + inclusive - v;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            carry += warp_sums[31];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        L.totals[0] = carry;
+    }
+}
+
+__global__ void __launch_bounds__(kSplitBlock) split_scatter_kernel(const SplitLaunch L) {
+    __shared__ unsigned int warp_counts[kSplitBlock / 32];
+    const uint64_t i = blockIdx.x * static_cast<uint64_t>(kSplitBlock) + threadIdx.x;
+    const bool eligible = split_eligible(L, i);
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned warp = threadIdx.x >> 5;
+    const unsigned ballot = __ballot_sync(0xffffffffu, eligible);
+    if (lane == 0) {
+        warp_counts[warp] = __popc(ballot);
+    }
+    __syncthreads();
+    if (!eligible) {
+        return;
+    }
+    unsigned int rank = __popc(ballot & ((1u << lane) - 1u));
+    for (unsigned w = 0; w < warp; ++w) {
+        rank += warp_counts[w];
+    }
+    const uint64_t child = L.count + L.block_offsets[blockIdx.x] + rank;
+    if (child >= L.capacity) {
+        return;  // counted as skipped by the host: wanted - written
+    }
+    const ParticleArrays& a = L.parts;
+    const int new_level = a.split_level[i] + 1;
+    const double new_weight = __ldg(L.weights + new_level - 1);
+    a.x[child] = a.x[i];
+    a.y[child] = a.y[i];
+    a.p[child] = a.p[i];
+    a.t[child] = a.t[i];
+    a.step_dt[child] = a.step_dt[i];
+    a.weight[i] = new_weight;
+    a.weight[child] = new_weight;
+    a.mu[child] = a.mu[i];
+    a.status[child] = 0;
+    a.split_level[i] = new_level;
+    a.split_level[child] = new_level;
+}
+
+// ---------------------------------------------------------- histogram
+// write_momentum_histogram binning (src/main.cpp:1915-1940).  Block-private
+// shared bins, FP64 atomics (driver weights are dyadic, so any summation
+// order gives the serial sum).  A particle whose bin coordinate lies within
+// 1e-7 of a bin edge is set aside for the host, which re-bins it with the
+// host log so bins match the reference's host computation exactly.
+__global__ void histogram_kernel(const HistogramLaunch L) {
+    extern __shared__ double shared_bins[];
+    for (int b = threadIdx.x; b < L.nbins; b += blockDim.x) {
+        shared_bins[b] = 0.0;
+    }
+    __syncthreads();
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < L.count;
+         i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        if (L.status[i] != 0) {
+            continue;
+        }
+        const double p = L.p[i];
+        if (p < L.pmin || p > L.pmax) {
+            continue;
+        }
+        const double f = (log(p) - L.log_pmin) * L.inv_dlogp;
+        if (fabs(f - rint(f)) < 1.0e-7) {
+            const unsigned long long slot = atomicAdd(L.edge_count, 1ull);
+            L.edge_index[slot] = static_cast<unsigned int>(i);
+            continue;
+        }
+        int bin = static_cast<int>(f);
+        bin = bin < 0 ? 0 : (bin >= L.nbins ? L.nbins - 1 : bin);
+        atomicAdd(shared_bins + bin, L.weight[i]);
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < L.nbins; b += blockDim.x) {
+        const double v = shared_bins[b];
+        if (v != 0.0) {
+            atomicAdd(L.bins + b, v);
+        }
+    }
+}
+
+// ------------------------------------------------------------ summary
+// summarize_particles (src/main.cpp:1845-1901).  Counts, min/max and the
+// dyadic weight sum are exact in any order; the p and dt sums use a fixed
+// two-level tree (per-block partials, then one block), so they are
+// deterministic and differ from the reference's serial sums only by
+// rounding.
+constexpr int kSummaryThreads = 256;
+constexpr int kSummaryPerThread = 8;
+
+__device__ __forceinline__ SummaryPartial empty_partial() {
+    SummaryPartial s;
+    s.active = 0;
+    s.inactive = 0;
+    s.weight_sum = 0.0;
+    s.p_sum = 0.0;
+    s.dt_sum = 0.0;
+    s.p_min = __longlong_as_double(0x7ff0000000000000ll);
+    s.dt_min = s.p_min;
+    s.p_max = 0.0;
+    s.dt_max = 0.0;
+    s.max_level = 0;
+    s.pad = 0;
+    return s;
+}
+
+__device__ __forceinline__ void combine(SummaryPartial& a, const SummaryPartial& b) {
+    a.active += b.active;
+    a.inactive += b.inactive;
+    a.weight_sum += b.weight_sum;
+    a.p_sum += b.p_sum;
+    a.dt_sum += b.dt_sum;
+    a.p_min = b.p_min < a.p_min ? b.p_min : a.p_min;
+    a.dt_min = b.dt_min < a.dt_min ? b.dt_min : a.dt_min;
+    a.p_max = a.p_max < b.p_max ? b.p_max : a.p_max;
+    a.dt_max = a.dt_max < b.dt_max ? b.dt_max : a.dt_max;
+    a.max_level = a.max_level < b.max_level ? b.max_level : a.max_level;
+}
+
+__device__ void block_reduce(SummaryPartial& mine, SummaryPartial* out) {
+    __shared__ SummaryPartial shared[kSummaryThreads];
+    shared[threadIdx.x] = mine;
+    __syncthreads();
+    for (int stride = kSummaryThreads / 2; stride > 0; stride >>= 1) {
+        if (static_cast<int>(threadIdx.x) < stride) {
+            combine(shared[threadIdx.x], shared[threadIdx.x + stride]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        *out = shared[0];
+    }
+}
+
+__global__ void __launch_bounds__(kSummaryThreads) summary_partial_kernel(const SummaryLaunch L) {
+    SummaryPartial mine = empty_partial();
+    const uint64_t base =
+        (blockIdx.x * static_cast<uint64_t>(kSummaryThreads) + threadIdx.x) * kSummaryPerThread;
+    for (int k = 0; k < kSummaryPerThread; ++k) {
+        const uint64_t i = base + k;
+        if (i >= L.count) {
+            break;
+        }
+        if (L.status[i] == 0) {
+            const double p = L.p[i];
+            const double dt = L.dt[i];
+            mine.active += 1;
+            mine.weight_sum += L.weight[i];
+            mine.p_sum += p;
+            mine.dt_sum += dt;
+            mine.p_min = p < mine.p_min ? p : mine.p_min;
+            mine.p_max = mine.p_max < p ? p : mine.p_max;
+            mine.dt_min = dt < mine.dt_min ? dt : mine.dt_min;
+            mine.dt_max = mine.dt_max < dt ? dt : mine.dt_max;
+            const int level = L.level[i];
+            mine.max_level = mine.max_level < level ? level : mine.max_level;
+        } else {
+            mine.inactive += 1;
+        }
+    }
+    block_reduce(mine, L.partials + blockIdx.x);
+}
+
+__global__ void __launch_bounds__(kSummaryThreads) summary_final_kernel(const SummaryLaunch L,
+                                                                        int nblocks) {
+    SummaryPartial mine = empty_partial();
+    for (int b = threadIdx.x; b < nblocks; b += kSummaryThreads) {
+        combine(mine, L.partials[b]);
+    }
+    block_reduce(mine, L.result);
+}
+
+}  // namespace
+
+cudaError_t launch_inject(const InjectLaunch& L, cudaStream_t stream) {
+    if (L.n == 0) {
+        return cudaSuccess;
+    }
+    const int threads = 256;
+    const uint64_t want = (L.n + threads - 1) / threads;
+    const int blocks = static_cast<int>(want > 152u * 32u ? 152u * 32u : want);
+    inject_kernel<<<blocks, threads, 0, stream>>>(L);
+    return cudaGetLastError();
+}
+
+size_t split_scratch_blocks(uint64_t count) {
+    return static_cast<size_t>((count + kSplitBlock - 1) / kSplitBlock);
+}
+
+cudaError_t launch_split(const SplitLaunch& L, cudaStream_t stream) {
+    const int nblocks = static_cast<int>(split_scratch_blocks(L.count));
+    if (nblocks == 0) {
+        return cudaMemsetAsync(L.totals, 0, sizeof(unsigned long long), stream);
+    }
+    split_count_kernel<<<nblocks, kSplitBlock, 0, stream>>>(L);
+    split_scan_kernel<<<1, 1024, 0, stream>>>(L, nblocks);
+    split_scatter_kernel<<<nblocks, kSplitBlock, 0, stream>>>(L);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_histogram(const HistogramLaunch& L, cudaStream_t stream) {
+    cudaError_t err = cudaMemsetAsync(L.bins, 0, sizeof(double) * L.nbins, stream);
+    if (err != cudaSuccess) return err;
+    err = cudaMemsetAsync(L.edge_count, 0, sizeof(unsigned long long), stream);
+    if (err != cudaSuccess) return err;
+    if (L.count == 0) {
+        return cudaSuccess;
+    }
+    const int threads = 256;
+    const uint64_t want = (L.count + threads - 1) / threads;
+    const int blocks = static_cast<int>(want > 152u * 8u ? 152u * 8u : want);
+    histogram_kernel<<<blocks, threads, sizeof(double) * L.nbins, stream>>>(L);
+    return cudaGetLastError();
+}
+
+int summary_blocks(uint64_t count) {
+    const uint64_t per_block = static_cast<uint64_t>(kSummaryThreads) * kSummaryPerThread;
+    const uint64_t n = (count + per_block - 1) / per_block;
+    return static_cast<int>(n < 1 ? 1 : n);
+}
+
+cudaError_t launch_summary(const SummaryLaunch& L, cudaStream_t stream) {
+    const int nblocks = summary_blocks(L.count);
+    summary_partial_kernel<<<nblocks, kSummaryThreads, 0, stream>>>(L);
+    summary_final_kernel<<<1, kSummaryThreads, 0, stream>>>(L, nblocks);
+    return cudaGetLastError();
+}
+
+}  // namespace kpt

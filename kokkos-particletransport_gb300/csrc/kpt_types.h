@@ -1,0 +1,65 @@
+// Plain structs shared by the host library and the kernels.
+#pragma once
+
+#include <cstdint>
+
+namespace kpt {
+
+// One periodic axis with two ghost layers.  Uniform axes use the analytic map
+// (start + i*step); non-uniform axes keep their ghosted cell centres in
+// device memory plus a bucket index that seeds the interval search.
+struct Axis {
+    int n;
+    int stored;
+    double start;
+    double step;
+    double lower;      // physical face bounds
+    double upper;
+    double width;
+    double inv_width;
+    const double* centers;   // stored: n+4 centres, logical -2..n+1
+    const int* buckets;      // stored: first interval index per bucket
+    int bucket_count;
+    double bucket_origin;
+    double bucket_scale;
+};
+
+struct Grid {
+    Axis axis[2];
+    int ex;  // nx + 4: point stride of one ghosted row
+};
+
+// Device copy of the driver's settings after make_device_settings
+// (reference src/main.cpp:596-636).
+struct DeviceSettings {
+    double x_lower, x_upper, y_lower, y_upper, x_width, y_width, dx, dy;
+    double shift_x, shift_y;
+    double mhd_dt, p0, pmax, gamma_turb, pindex, kpara0, kperp_over_kpara;
+    double dt_min, dt_max, drift_param1, drift_param2, charge, particle_v0, duu0;
+    double h0, split_ratio, pmin_split, mu_max;
+    int max_steps, momentum_dependency, magnetic_dependency, time_interpolation;
+    int split_particles, focused;
+};
+
+struct ParticleArrays {
+    double* x;
+    double* y;
+    double* p;
+    double* t;
+    double* step_dt;
+    double* weight;
+    double* mu;
+    int32_t* status;
+    int32_t* split_level;
+};
+
+// Device-side counters written by the push.
+struct PushCounters {
+    unsigned long long particle_steps;
+    unsigned long long pushed;
+    unsigned long long failed;
+    unsigned int max_steps;
+    unsigned int next_particle;  // work-queue cursor
+};
+
+}  // namespace kpt

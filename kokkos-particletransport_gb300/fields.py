@@ -1,0 +1,154 @@
+"""Synthetic 2D MHD background fields and the compact field file format.
+
+The compact field file is the one the reference reads in
+``include/AthenaFieldReader.hpp:277-285`` (written by ``apps/athena2bin.py``):
+
+    int32 nx, int32 ny
+    float64 x_edges[nx + 1], y_edges[ny + 1]
+    float64 Bx[nx*ny], By[nx*ny], Bz[nx*ny], Vx[nx*ny], Vy[nx*ny], Vz[nx*ny]
+
+little-endian, component arrays row-major with x fastest
+(``source_index = j * nx + i``).  The reference reader rejects non-uniform
+edges (``AthenaFieldReader.hpp:167-193``); this package accepts them as a
+stated extension (stretched y edges of the scale configuration).
+
+The generators below build the seeded synthetic backgrounds that stand in for
+the reference's (absent) Athena++ reconnection data: a Harris current sheet
+with a guide field and inflow, optional magnetic islands from a flux function,
+optional non-uniform y edges and seeded multiplicative noise per frame.
+"""
+from __future__ import annotations
+
+import dataclasses
+import os
+from typing import Optional
+
+import numpy as np
+
+COMPONENTS = ("Bx", "By", "Bz", "Vx", "Vy", "Vz")
+
+
+@dataclasses.dataclass
+class CompactField:
+    """One frame of a 2D background field: face edges plus six cell arrays.
+
+    ``b`` and ``v`` have shape (3, ny, nx) (x fastest in memory), matching the
+    file's component order.
+    """
+
+    x_edges: np.ndarray
+    y_edges: np.ndarray
+    b: np.ndarray
+    v: np.ndarray
+
+    @property
+    def nx(self) -> int:
+        return int(self.x_edges.size - 1)
+
+    @property
+    def ny(self) -> int:
+        return int(self.y_edges.size - 1)
+
+    def file_bytes(self) -> int:
+        return 8 + 8 * (self.nx + 1 + self.ny + 1) + 48 * self.nx * self.ny
+
+
+def write_compact_field(path: str, field: CompactField) -> None:
+    """Write ``field`` in the compact binary layout (little-endian)."""
+    nx, ny = field.nx, field.ny
+    with open(path, "wb") as stream:
+        stream.write(np.asarray([nx, ny], dtype="<i4").tobytes())
+        stream.write(np.ascontiguousarray(field.x_edges, dtype="<f8").tobytes())
+        stream.write(np.ascontiguousarray(field.y_edges, dtype="<f8").tobytes())
+        for comp in range(3):
+            stream.write(np.ascontiguousarray(field.b[comp], dtype="<f8").tobytes())
+        for comp in range(3):
+            stream.write(np.ascontiguousarray(field.v[comp], dtype="<f8").tobytes())
+
+
+def read_compact_field(path: str) -> CompactField:
+    """Read a compact field file; raises ValueError on a malformed file."""
+    raw = np.fromfile(path, dtype=np.uint8)
+    if raw.size < 8:
+        raise ValueError("compact field: file too short for the header")
+    nx, ny = (int(v) for v in raw[:8].view("<i4"))
+    if nx <= 0 or ny <= 0:
+        raise ValueError("compact field: dimensions must be positive")
+    expected = 8 + 8 * (nx + 1 + ny + 1) + 48 * nx * ny
+    if raw.size != expected:
+        raise ValueError(
+            f"compact field: expected {expected} bytes for {nx}x{ny}, found {raw.size}")
+    body = raw[8:].view("<f8")
+    x_edges = body[: nx + 1].copy()
+    y_edges = body[nx + 1: nx + 1 + ny + 1].copy()
+    arrays = body[nx + ny + 2:].reshape(6, ny, nx)
+    return CompactField(x_edges, y_edges, arrays[:3].copy(), arrays[3:].copy())
+
+
+def stretched_edges(n: int, lower: float, upper: float, strength: float = 4.0) -> np.ndarray:
+    """Face edges whose spacing grows as 1 + strength*(y/half)^2, spanning [lower, upper].
+
+    The local spacing d(edge)/ds is proportional to 1 + strength*(y/h)^2 with
+    h = (upper-lower)/2 about the centre; the map is integrated numerically
+    and normalised so the edges land exactly on [lower, upper].
+    """
+    centre = 0.5 * (lower + upper)
+    half = 0.5 * (upper - lower)
+    fine = np.linspace(lower, upper, 64 * n + 1)
+    density = 1.0 / (1.0 + strength * ((fine - centre) / half) ** 2)
+    cumulative = np.concatenate([[0.0], np.cumsum(0.5 * (density[1:] + density[:-1]))])
+    cumulative /= cumulative[-1]
+    edges = np.interp(np.linspace(0.0, 1.0, n + 1), cumulative, fine)
+    edges[0], edges[-1] = lower, upper
+    return edges
+
+
+def harris_field(nx: int, ny: int, *, x_range=(-1.0, 1.0), y_range=(-2.0, 2.0),
+                 sheet_width: float = 0.1, guide: float = 0.1, perturbation: float = 0.05,
+                 inflow: float = 0.05, outflow: float = 0.1, island_amplitude: float = 0.0,
+                 island_count: int = 8, island_width2: float = 0.04,
+                 y_edges: Optional[np.ndarray] = None, noise: float = 0.0,
+                 seed: int = 0) -> CompactField:
+    """Harris sheet with guide field, inflow and optional islands (cell centres).
+
+    Bx = tanh(y/w), By = eps*sin(pi x)*cos(pi y/4), Bz = guide,
+    Vx = outflow*x*sech^2(y/w), Vy = -inflow*tanh(y/w), Vz = 0.
+    Islands add B += z_hat x grad(psi) with
+    psi = A*cos(island_count/2 * 2 pi x / Lx)*exp(-y^2/island_width2), i.e.
+    Bx += dpsi/dy, By -= dpsi/dx.  ``noise`` > 0 multiplies every component by
+    (1 + noise*N(0,1)) drawn from ``seed``.
+    """
+    x_edges = np.linspace(x_range[0], x_range[1], nx + 1)
+    if y_edges is None:
+        y_edges = np.linspace(y_range[0], y_range[1], ny + 1)
+    y_edges = np.asarray(y_edges, dtype=np.float64)
+    xc = 0.5 * (x_edges[1:] + x_edges[:-1])
+    yc = 0.5 * (y_edges[1:] + y_edges[:-1])
+    X, Y = np.meshgrid(xc, yc)  # shape (ny, nx), x fastest
+    t = np.tanh(Y / sheet_width)
+    sech2 = 1.0 / np.cosh(Y / sheet_width) ** 2
+    bx = t.copy()
+    by = perturbation * np.sin(np.pi * X) * np.cos(np.pi * Y / 4.0)
+    bz = np.full_like(X, guide)
+    if island_amplitude != 0.0:
+        lx = x_range[1] - x_range[0]
+        k = np.pi * island_count / lx
+        g = np.exp(-Y * Y / island_width2)
+        # psi = A cos(k x) g(y): dpsi/dy = A cos(kx) g * (-2y/w2); dpsi/dx = -A k sin(kx) g
+        bx = bx + island_amplitude * np.cos(k * X) * g * (-2.0 * Y / island_width2)
+        by = by + island_amplitude * k * np.sin(k * X) * g
+    vx = outflow * X * sech2
+    vy = -inflow * t
+    vz = np.zeros_like(X)
+    b = np.stack([bx, by, bz])
+    v = np.stack([vx, vy, vz])
+    if noise > 0.0:
+        rng = np.random.default_rng(seed)
+        b = b * (1.0 + noise * rng.standard_normal(b.shape))
+        v = v * (1.0 + noise * rng.standard_normal(v.shape))
+    return CompactField(x_edges, y_edges, np.ascontiguousarray(b), np.ascontiguousarray(v))
+
+
+def field_file_path(field_dir: str, frame: int) -> str:
+    """``FIELD_DIR/fieldNNNNN.bin`` as in the reference (src/main.cpp:413-418)."""
+    return os.path.join(field_dir, f"field{frame:05d}.bin")

@@ -1,0 +1,301 @@
+"""ctypes binding to the oracle libraries (test infrastructure only).
+
+``Oracle`` wraps oracle/_build/libkpt_oracle.so (the C restatement);
+``ReferenceHarness`` wraps oracle/_ref/libkpt_ref.so (the reference's own
+sources compiled on the Kokkos-API shim) when it has been built.  Only tests,
+``__graft_entry__.smoke()`` and bench.py's CPU-baseline legs use this module.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from typing import Dict, Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "_build", "libkpt_oracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libkpt_ref.so")
+
+PARTICLE_FIELDS = ("x", "y", "p", "t", "dt", "w", "mu", "status", "level")
+DOUBLE_PARAMS = ("mhd_dt", "p0", "pmin", "pmax", "gamma_turb", "kpara0", "kperp_over_kpara",
+                 "dt_min_rel", "dt_max_rel", "drift_param1", "drift_param2", "charge",
+                 "particle_v0", "duu0", "split_ratio", "pmin_split_over_p0", "mu_max")
+INT_PARAMS = ("max_steps", "momentum_dependency", "magnetic_dependency", "time_interpolation",
+              "split_particles", "focused")
+
+
+class OracleParams(ctypes.Structure):
+    _fields_ = [(name, ctypes.c_double) for name in DOUBLE_PARAMS] + \
+               [(name, ctypes.c_int32) for name in INT_PARAMS]
+
+
+class OracleSummary(ctypes.Structure):
+    _fields_ = [("stored", ctypes.c_uint64), ("active", ctypes.c_uint64),
+                ("inactive", ctypes.c_uint64), ("weight_sum", ctypes.c_double),
+                ("p_min", ctypes.c_double), ("p_max", ctypes.c_double),
+                ("p_avg", ctypes.c_double), ("dt_min", ctypes.c_double),
+                ("dt_max", ctypes.c_double), ("dt_avg", ctypes.c_double),
+                ("max_split_level", ctypes.c_int32), ("pad", ctypes.c_int32)]
+
+
+class OracleGrid(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int * 2), ("stored", ctypes.c_int * 2),
+                ("start", ctypes.c_double * 2), ("step", ctypes.c_double * 2),
+                ("faces", ctypes.c_void_p * 2), ("centers", ctypes.c_void_p * 2),
+                ("lower", ctypes.c_double * 2), ("upper", ctypes.c_double * 2),
+                ("width", ctypes.c_double * 2), ("inv_width", ctypes.c_double * 2),
+                ("ghost_lower", ctypes.c_double * 2), ("ghost_upper", ctypes.c_double * 2)]
+
+
+def default_params(**overrides) -> Dict[str, float]:
+    """Reference defaults (src/main.cpp:136-154) with overrides."""
+    values = dict(mhd_dt=0.1, p0=0.1, pmin=1.0e-2, pmax=1.0e1, gamma_turb=1.6666667,
+                  kpara0=0.00743592, kperp_over_kpara=0.01, dt_min_rel=1.0e-7,
+                  dt_max_rel=1.0e-2, drift_param1=850964.408, drift_param2=13575468.975,
+                  charge=-1.0, particle_v0=17.20195, duu0=5578.445, split_ratio=2.0,
+                  pmin_split_over_p0=2.0, mu_max=0.99, max_steps=200000, momentum_dependency=1,
+                  magnetic_dependency=1, time_interpolation=1, split_particles=1, focused=0)
+    for key, value in overrides.items():
+        if key not in values:
+            raise KeyError(key)
+        values[key] = value
+    return values
+
+
+def make_params(values: Dict[str, float]) -> OracleParams:
+    params = OracleParams()
+    for name in DOUBLE_PARAMS:
+        setattr(params, name, float(values[name]))
+    for name in INT_PARAMS:
+        setattr(params, name, int(values[name]))
+    return params
+
+
+def _ptr(array: Optional[np.ndarray]):
+    return None if array is None else array.ctypes.data_as(ctypes.c_void_p)
+
+
+def empty_particles(capacity: int) -> Dict[str, np.ndarray]:
+    """Particle SoA as the reference allocates it (status 2, src/main.cpp:326-331)."""
+    arrays = {name: np.zeros(capacity, dtype=np.float64) for name in PARTICLE_FIELDS[:7]}
+    arrays["status"] = np.full(capacity, 2, dtype=np.int32)
+    arrays["level"] = np.zeros(capacity, dtype=np.int32)
+    return arrays
+
+
+def build_oracle() -> str:
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return ORACLE_SO
+
+
+class Oracle:
+    """The C restatement (oracle/kpt_oracle.c)."""
+
+    def __init__(self, path: str = ORACLE_SO):
+        if not os.path.exists(path):
+            build_oracle()
+        lib = ctypes.CDLL(path)
+        self.lib = lib
+        vp, dbl, u64, u32, i32 = (ctypes.c_void_p, ctypes.c_double, ctypes.c_uint64,
+                                  ctypes.c_uint32, ctypes.c_int)
+        lib.kpt_oracle_last_error.restype = ctypes.c_char_p
+        lib.kpt_oracle_grid_init.argtypes = [vp, i32, i32, vp, vp, i32]
+        lib.kpt_oracle_grid_free.argtypes = [vp]
+        lib.kpt_oracle_table_from_cells.argtypes = [i32, i32, vp, vp, vp, vp, i32, i32, vp]
+        lib.kpt_oracle_push.argtypes = [vp, vp, vp, vp, dbl, u32, u64, ctypes.c_size_t] + \
+            [vp] * 8 + [i32]
+        lib.kpt_oracle_inject.restype = u64
+        lib.kpt_oracle_inject.argtypes = [vp, vp, dbl, u32, u64, u64, u64, u64, dbl, dbl] + \
+            [vp] * 9
+        lib.kpt_oracle_split.restype = u64
+        lib.kpt_oracle_split.argtypes = [vp, u64, u64] + [vp] * 9 + [vp, vp]
+        lib.kpt_oracle_histogram.argtypes = [dbl, dbl, i32, u64, vp, vp, vp, vp]
+        lib.kpt_oracle_summarize.argtypes = [u64, vp, vp, vp, vp, vp, vp]
+        lib.kpt_oracle_wrap.restype = dbl
+        lib.kpt_oracle_wrap.argtypes = [dbl, dbl, dbl, dbl]
+        lib.kpt_oracle_sample.argtypes = [vp, vp, vp, i32, dbl, dbl, dbl, i32, vp]
+
+    def _error(self) -> str:
+        return self.lib.kpt_oracle_last_error().decode()
+
+    def grid(self, x_edges, y_edges, force_stored: bool = False) -> OracleGrid:
+        grid = OracleGrid()
+        xe = np.ascontiguousarray(x_edges, dtype=np.float64)
+        ye = np.ascontiguousarray(y_edges, dtype=np.float64)
+        if self.lib.kpt_oracle_grid_init(ctypes.byref(grid), xe.size - 1, ye.size - 1, _ptr(xe),
+                                         _ptr(ye), int(force_stored)) != 0:
+            raise ValueError(self._error())
+        return grid
+
+    def free_grid(self, grid: OracleGrid) -> None:
+        self.lib.kpt_oracle_grid_free(ctypes.byref(grid))
+
+    def table(self, field, focused: bool = False, force_stored: bool = False) -> np.ndarray:
+        """Coefficient table (points, 16|21) for a fields.CompactField."""
+        ncomp = 21 if focused else 16
+        nx, ny = field.nx, field.ny
+        out = np.zeros(((nx + 4) * (ny + 4), ncomp), dtype=np.float64)
+        b = np.ascontiguousarray(field.b, dtype=np.float64)
+        v = np.ascontiguousarray(field.v, dtype=np.float64)
+        xe = np.ascontiguousarray(field.x_edges, dtype=np.float64)
+        ye = np.ascontiguousarray(field.y_edges, dtype=np.float64)
+        if self.lib.kpt_oracle_table_from_cells(nx, ny, _ptr(xe), _ptr(ye), _ptr(b), _ptr(v),
+                                                int(focused), int(force_stored),
+                                                _ptr(out)) != 0:
+            raise ValueError(self._error())
+        return out
+
+    def push(self, grid: OracleGrid, lower: np.ndarray, upper: np.ndarray, params: dict,
+             interval_start: float, frame: int, seed: int, count: int,
+             particles: Dict[str, np.ndarray], threads: int = 0) -> np.ndarray:
+        """In-place interval push; returns per-particle substep counts (uint32)."""
+        steps = np.zeros(max(count, 1), dtype=np.uint32)
+        prm = make_params(params)
+        lo = np.ascontiguousarray(lower, dtype=np.float64)
+        up = np.ascontiguousarray(upper, dtype=np.float64)
+        self.lib.kpt_oracle_push(ctypes.byref(grid), _ptr(lo), _ptr(up), ctypes.byref(prm),
+                                 float(interval_start), int(frame), int(seed), int(count),
+                                 _ptr(particles["x"]), _ptr(particles["y"]),
+                                 _ptr(particles["p"]), _ptr(particles["t"]),
+                                 _ptr(particles["dt"]), _ptr(particles["mu"]),
+                                 _ptr(particles["status"]), _ptr(steps), int(threads))
+        return steps[:count]
+
+    def inject(self, grid: OracleGrid, params: dict, interval_start: float, frame: int,
+               seed: int, capacity: int, count: int, requested: int,
+               particles: Dict[str, np.ndarray], band=(0.0, 0.0)) -> int:
+        prm = make_params(params)
+        return int(self.lib.kpt_oracle_inject(ctypes.byref(grid), ctypes.byref(prm),
+                                              float(interval_start), int(frame), int(seed),
+                                              int(capacity), int(count), int(requested),
+                                              float(band[0]), float(band[1]),
+                                              *[_ptr(particles[k]) for k in PARTICLE_FIELDS]))
+
+    def split(self, params: dict, capacity: int, count: int, particles: Dict[str, np.ndarray]):
+        prm = make_params(params)
+        split = ctypes.c_uint64()
+        skipped = ctypes.c_uint64()
+        new_count = self.lib.kpt_oracle_split(ctypes.byref(prm), int(capacity), int(count),
+                                              *[_ptr(particles[k]) for k in PARTICLE_FIELDS],
+                                              ctypes.byref(split), ctypes.byref(skipped))
+        return int(new_count), int(split.value), int(skipped.value)
+
+    def histogram(self, pmin: float, pmax: float, nbins: int, count: int,
+                  particles: Dict[str, np.ndarray]) -> np.ndarray:
+        bins = np.zeros(nbins, dtype=np.float64)
+        self.lib.kpt_oracle_histogram(float(pmin), float(pmax), int(nbins), int(count),
+                                      _ptr(particles["p"]), _ptr(particles["w"]),
+                                      _ptr(particles["status"]), _ptr(bins))
+        return bins
+
+    def summarize(self, count: int, particles: Dict[str, np.ndarray]) -> dict:
+        out = OracleSummary()
+        self.lib.kpt_oracle_summarize(int(count), _ptr(particles["p"]), _ptr(particles["dt"]),
+                                      _ptr(particles["w"]), _ptr(particles["status"]),
+                                      _ptr(particles["level"]), ctypes.byref(out))
+        return {name: getattr(out, name) for name, _ in OracleSummary._fields_ if name != "pad"}
+
+    def wrap(self, value: float, lower: float, upper: float, width: float) -> float:
+        return float(self.lib.kpt_oracle_wrap(value, lower, upper, width))
+
+
+class ReferenceHarness:
+    """The reference's own driver functions on the Kokkos-API shim (oracle/_ref)."""
+
+    def __init__(self, path: str = REF_SO):
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        lib = ctypes.CDLL(path)
+        self.lib = lib
+        vp, cp, i32, ull, dbl, ll = (ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int,
+                                     ctypes.c_ulonglong, ctypes.c_double, ctypes.c_longlong)
+        lib.ref_last_error.restype = ctypes.c_char_p
+        lib.ref_table.restype = ll
+        lib.ref_table.argtypes = [cp, i32, vp, ll]
+        lib.ref_inject.restype = ll
+        lib.ref_inject.argtypes = [cp, vp, vp, ull, i32, ull, ull, ull, dbl, dbl] + [vp] * 9
+        lib.ref_push.restype = ll
+        lib.ref_push.argtypes = [cp, vp, vp, ull, i32, ull, ull] + [vp] * 9
+        lib.ref_split.restype = ll
+        lib.ref_split.argtypes = [cp, vp, vp, i32, ull, ull] + [vp] * 9 + [vp, vp]
+        lib.ref_table_stored.restype = ll
+        lib.ref_table_stored.argtypes = [i32, i32, vp, vp, vp, vp, i32, vp, ll]
+        lib.ref_push_stored.restype = ll
+        lib.ref_push_stored.argtypes = [i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, ull, i32, ull,
+                                        ull] + [vp] * 9
+        lib.ref_main.restype = i32
+        lib.ref_main.argtypes = [i32, ctypes.POINTER(ctypes.c_char_p), i32]
+
+    @staticmethod
+    def _param_arrays(params: dict):
+        d = np.array([float(params[k]) for k in DOUBLE_PARAMS], dtype=np.float64)
+        i = np.array([int(params[k]) for k in INT_PARAMS], dtype=np.int32)
+        return d, i
+
+    def _check(self, value):
+        if value < 0:
+            raise RuntimeError(self.lib.ref_last_error().decode())
+        return value
+
+    def table(self, path: str, focused: bool = False) -> np.ndarray:
+        n = self._check(self.lib.ref_table(path.encode(), int(focused), None, 0))
+        out = np.zeros(n, dtype=np.float64)
+        self._check(self.lib.ref_table(path.encode(), int(focused), _ptr(out), n))
+        return out.reshape(-1, 21 if focused else 16)
+
+    def inject(self, field_dir: str, params: dict, seed: int, frame: int, capacity: int,
+               count: int, requested: int, particles, band=(0.0, 0.0)) -> int:
+        d, i = self._param_arrays(params)
+        return int(self._check(self.lib.ref_inject(
+            field_dir.encode(), _ptr(d), _ptr(i), seed, frame, capacity, count, requested,
+            float(band[0]), float(band[1]), *[_ptr(particles[k]) for k in PARTICLE_FIELDS])))
+
+    def push(self, field_dir: str, params: dict, seed: int, frame: int, capacity: int,
+             count: int, particles) -> int:
+        d, i = self._param_arrays(params)
+        return int(self._check(self.lib.ref_push(
+            field_dir.encode(), _ptr(d), _ptr(i), seed, frame, capacity, count,
+            *[_ptr(particles[k]) for k in PARTICLE_FIELDS])))
+
+    def split(self, field_dir: str, params: dict, frame: int, capacity: int, count: int,
+              particles):
+        d, i = self._param_arrays(params)
+        split = ctypes.c_ulonglong()
+        skipped = ctypes.c_ulonglong()
+        new_count = self._check(self.lib.ref_split(
+            field_dir.encode(), _ptr(d), _ptr(i), frame, capacity, count,
+            *[_ptr(particles[k]) for k in PARTICLE_FIELDS], ctypes.byref(split),
+            ctypes.byref(skipped)))
+        return int(new_count), int(split.value), int(skipped.value)
+
+    def table_stored(self, field, focused: bool = False) -> np.ndarray:
+        """Coefficient table of a fields.CompactField on the stored-edge grid path."""
+        xe = np.ascontiguousarray(field.x_edges, dtype=np.float64)
+        ye = np.ascontiguousarray(field.y_edges, dtype=np.float64)
+        b = np.ascontiguousarray(field.b, dtype=np.float64)
+        v = np.ascontiguousarray(field.v, dtype=np.float64)
+        args = (field.nx, field.ny, _ptr(xe), _ptr(ye), _ptr(b), _ptr(v), int(focused))
+        n = self._check(self.lib.ref_table_stored(*args, None, 0))
+        out = np.zeros(n, dtype=np.float64)
+        self._check(self.lib.ref_table_stored(*args, _ptr(out), n))
+        return out.reshape(-1, 21 if focused else 16)
+
+    def push_stored(self, lower_field, upper_field, params: dict, seed: int, frame: int,
+                    capacity: int, count: int, particles) -> int:
+        d, i = self._param_arrays(params)
+        xe = np.ascontiguousarray(lower_field.x_edges, dtype=np.float64)
+        ye = np.ascontiguousarray(lower_field.y_edges, dtype=np.float64)
+        arrays = [np.ascontiguousarray(a, dtype=np.float64) for a in
+                  (lower_field.b, lower_field.v, upper_field.b, upper_field.v)]
+        return int(self._check(self.lib.ref_push_stored(
+            lower_field.nx, lower_field.ny, _ptr(xe), _ptr(ye), *[_ptr(a) for a in arrays],
+            _ptr(d), _ptr(i), seed, frame, capacity, count,
+            *[_ptr(particles[k]) for k in PARTICLE_FIELDS])))
+
+    def main(self, argv, frame_base: int = 0) -> int:
+        """Run the reference CLI (in-process); noise frames start at frame_base."""
+        args = [b"kokkos_particle_transport_app"] + [a.encode() for a in argv]
+        arr = (ctypes.c_char_p * len(args))(*args)
+        return int(self.lib.ref_main(len(args), arr, int(frame_base)))

@@ -1,0 +1,20 @@
+#!/usr/bin/env bash
+# Compile the reference's own driver sources (src/main.cpp and include/, read
+# in place, unmodified) against the project's Kokkos-API shim into
+# oracle/_ref/libkpt_ref.so.  Test infrastructure: used to make golden vectors
+# and to pin the oracle restatement.  Needs the reference checkout; a machine
+# without it skips this step.
+set -euo pipefail
+here="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
+ref="${KPT_REFERENCE_DIR:-/root/reference}"
+if [ ! -f "$ref/src/main.cpp" ]; then
+    echo "build_ref: reference sources not found at $ref; skipping" >&2
+    exit 0
+fi
+mkdir -p "$here/_ref"
+g++ -O2 -std=c++20 -fopenmp -ffp-contract=off -fPIC -shared \
+    -Dmain=kpt_ref_main \
+    -I "$here/kokkos_shim" -I "$ref" -I "$ref/include" \
+    "$here/ref_harness.cpp" -o "$here/_ref/libkpt_ref.so.tmp"
+mv "$here/_ref/libkpt_ref.so.tmp" "$here/_ref/libkpt_ref.so"
+echo "build_ref: wrote $here/_ref/libkpt_ref.so"

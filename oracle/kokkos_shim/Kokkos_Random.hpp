@@ -1,0 +1,97 @@
+// Random pool with the Kokkos Random_XorShift64_Pool interface whose states
+// draw from the keyed Philox stream of oracle/kpt_philox.h instead of a
+// per-thread XorShift64 state.  get_state() keys the stream by the running
+// kernel (label -> tag), the loop index published by parallel_for, and the
+// frame number the harness sets before each launch; this is the
+// injected-noise hook that makes the reference's unmodified kernels consume
+// the same increments as the GPU kernels.  Oracle-only shim.
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+
+#include "Kokkos_Core.hpp"
+#include "../kpt_philox.h"
+
+namespace Kokkos {
+
+namespace ShimImpl {
+inline std::uint32_t& current_frame() {
+    static std::uint32_t frame = 0;
+    return frame;
+}
+// When set, the frame key is auto_frame_base() + (launch ordinal - 1) of the
+// running kernel: the driver launches inject and push once per frame.
+inline int& auto_frame_enabled() {
+    static int enabled = 0;
+    return enabled;
+}
+inline std::uint32_t& auto_frame_base() {
+    static std::uint32_t base = 0;
+    return base;
+}
+inline std::uint32_t label_tag(const char* label) {
+    if (label == nullptr) {
+        return KPT_ORACLE_TAG_OTHER;
+    }
+    if (std::strstr(label, "inject_uniform_particles") != nullptr) {
+        return KPT_ORACLE_TAG_INJECT;
+    }
+    if (std::strstr(label, "move_parker_particles_one_interval") != nullptr ||
+        std::strstr(label, "move_particles_one_interval") != nullptr) {
+        return KPT_ORACLE_TAG_PUSH;
+    }
+    return KPT_ORACLE_TAG_OTHER;
+}
+}  // namespace ShimImpl
+
+template <class DeviceType>
+class Random_XorShift64 {
+public:
+    kpt_oracle_stream stream{};
+
+    double drand() { return kpt_oracle_stream_u01(&stream); }
+    double drand(const double range) { return range * drand(); }
+    double drand(const double start, const double end) {
+        return start + (end - start) * drand();
+    }
+    // Box-Muller transform on two stream draws (unused by the driver path).
+    double normal() {
+        const double u1 = 1.0 - drand();
+        const double u2 = drand();
+        return std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2);
+    }
+    double normal(const double mean, const double standard_deviation) {
+        return mean + standard_deviation * normal();
+    }
+};
+
+template <class DeviceType>
+class Random_XorShift64_Pool {
+public:
+    using generator_type = Random_XorShift64<DeviceType>;
+    using device_type = DeviceType;
+
+    Random_XorShift64_Pool() = default;
+    explicit Random_XorShift64_Pool(const std::uint64_t seed) : seed_(seed) {}
+
+    generator_type get_state() const {
+        const auto& context = ShimImpl::current_kernel();
+        generator_type generator;
+        const std::uint32_t frame =
+            ShimImpl::auto_frame_enabled() != 0
+                ? ShimImpl::auto_frame_base() + (context.ordinal - 1u)
+                : ShimImpl::current_frame();
+        kpt_oracle_stream_init(&generator.stream, seed_,
+                               static_cast<std::uint32_t>(context.index), frame,
+                               ShimImpl::label_tag(context.label));
+        return generator;
+    }
+    void free_state(const generator_type&) const {}
+
+private:
+    std::uint64_t seed_ = 0;
+};
+
+}  // namespace Kokkos

@@ -1,0 +1,417 @@
+// Harness around the reference driver: it #includes the reference's own
+// src/main.cpp (compiled unmodified against oracle/kokkos_shim, with main
+// renamed to kpt_ref_main) and exposes its namespace functions through a flat
+// C interface that Python (ctypes) calls to make golden vectors and to time
+// the reference's CPU push.  Test infrastructure only; built into oracle/_ref
+// by oracle/build_ref.sh.
+//
+// Functions driven (reference src/main.cpp):
+//   load_parker_coefficient_frame / load_coefficient_frame   :932-962
+//   inject_uniform_particles                                  :996-1048
+//   move_parker_particles_one_interval                        :1084-1327
+//   move_particles_one_interval                               :1334-1755
+//   split_particles                                           :1761-1839
+//   main (as kpt_ref_main)                                    :2692-2705
+#include "src/main.cpp"
+
+#include <string>
+
+namespace {
+
+thread_local std::string g_last_error;
+
+// Parameter blocks passed from the host side.  Order is fixed and mirrored by
+// tests/golden/make_golden.py and bench.py.
+enum DoubleParam {
+    DP_MHD_DT = 0,
+    DP_P0,
+    DP_PMIN,
+    DP_PMAX,
+    DP_GAMMA_TURB,
+    DP_KPARA0,
+    DP_KPERP_OVER_KPARA,
+    DP_DT_MIN_REL,
+    DP_DT_MAX_REL,
+    DP_DRIFT1,
+    DP_DRIFT2,
+    DP_CHARGE,
+    DP_PARTICLE_V0,
+    DP_DUU0,
+    DP_SPLIT_RATIO,
+    DP_PMIN_SPLIT_OVER_P0,
+    DP_MU_MAX,
+    DP_COUNT
+};
+enum IntParam {
+    IP_MAX_STEPS = 0,
+    IP_MOMENTUM_DEPENDENCY,
+    IP_MAGNETIC_DEPENDENCY,
+    IP_TIME_INTERPOLATION,
+    IP_SPLIT,
+    IP_FOCUSED,
+    IP_COUNT
+};
+
+using namespace Reconnection2DCalibration;
+
+Reconnection2DSettings settings_from(const double* d, const int* i) {
+    Reconnection2DSettings s;
+    s.mhd_dt = d[DP_MHD_DT];
+    s.p0 = d[DP_P0];
+    s.pmin = d[DP_PMIN];
+    s.pmax = d[DP_PMAX];
+    s.gamma_turb = d[DP_GAMMA_TURB];
+    s.kpara0 = d[DP_KPARA0];
+    s.kperp_over_kpara = d[DP_KPERP_OVER_KPARA];
+    s.dt_min_rel = d[DP_DT_MIN_REL];
+    s.dt_max_rel = d[DP_DT_MAX_REL];
+    s.drift_param1 = d[DP_DRIFT1];
+    s.drift_param2 = d[DP_DRIFT2];
+    s.charge = d[DP_CHARGE];
+    s.particle_v0 = d[DP_PARTICLE_V0];
+    s.duu0 = d[DP_DUU0];
+    s.split_ratio = d[DP_SPLIT_RATIO];
+    s.pmin_split_over_p0 = d[DP_PMIN_SPLIT_OVER_P0];
+    s.mu_max = d[DP_MU_MAX];
+    s.max_particle_steps_per_interval = i[IP_MAX_STEPS];
+    s.momentum_dependency = i[IP_MOMENTUM_DEPENDENCY];
+    s.magnetic_dependency = i[IP_MAGNETIC_DEPENDENCY];
+    s.time_interpolation = i[IP_TIME_INTERPOLATION] != 0;
+    s.split_particles = i[IP_SPLIT] != 0;
+    s.transport_model = i[IP_FOCUSED] != 0 ? TransportModel::Focused : TransportModel::Parker;
+    return s;
+}
+
+struct HostParticles {
+    double* x;
+    double* y;
+    double* p;
+    double* t;
+    double* dt;
+    double* w;
+    double* mu;
+    int* status;
+    int* level;
+};
+
+template <typename Storage>
+void load_storage(Storage& storage, const HostParticles& h, const std::uint64_t count) {
+    for (std::uint64_t n = 0; n < count; ++n) {
+        storage.position(n, 0) = h.x[n];
+        storage.position(n, 1) = h.y[n];
+        storage.momentum(n) = h.p[n];
+        storage.time(n) = h.t[n];
+        storage.step_dt(n) = h.dt[n];
+        storage.weight(n) = h.w[n];
+        storage.mu(n) = h.mu[n];
+        storage.status(n) = h.status[n];
+        storage.split_level(n) = h.level[n];
+    }
+    storage.count = count;
+}
+
+template <typename Storage>
+void store_storage(const Storage& storage, const HostParticles& h, const std::uint64_t count) {
+    for (std::uint64_t n = 0; n < count; ++n) {
+        h.x[n] = storage.position(n, 0);
+        h.y[n] = storage.position(n, 1);
+        h.p[n] = storage.momentum(n);
+        h.t[n] = storage.time(n);
+        h.dt[n] = storage.step_dt(n);
+        h.w[n] = storage.weight(n);
+        h.mu[n] = storage.mu(n);
+        h.status[n] = storage.status(n);
+        h.level[n] = storage.split_level(n);
+    }
+}
+
+template <typename Table>
+auto device_settings_for(const Reconnection2DSettings& s, const Table& table) {
+    return make_device_settings(s, table.grid);
+}
+
+// Background on explicit (possibly non-uniform) face edges: the reference's
+// StoredCoordinateGrid (include/StoredCoordinateGrid.hpp) with the two ghost
+// faces on each side continued periodically, B and V copied and ghost-filled
+// exactly as the compact reader does (AthenaFieldReader.hpp:330-357).  The
+// driver's coefficient builders and pushers are templates over the
+// background/field type, so they run unchanged on it.
+using StoredGrid = StoredCoordinateGrid<2, Device, typename DeviceTraits<Device>::array_layout, 3>;
+
+struct StoredBackground {
+    using grid_type = StoredGrid;
+    using layout_type = typename DeviceTraits<Device>::array_layout;
+    using vector_field_type = VectorField<grid_type, 3, layout_type>;
+    grid_type grid;
+    vector_field_type magnetic_field;
+    vector_field_type velocity_field;
+};
+
+StoredBackground make_stored_background(int nx, int ny, const double* x_edges,
+                                        const double* y_edges, const double* b,
+                                        const double* v) {
+    using metadata_type = Grid<2, Device, typename DeviceTraits<Device>::array_layout, 3>;
+    typename metadata_type::index_array_type extents{};
+    extents[0] = nx;
+    extents[1] = ny;
+    typename metadata_type::ghost_array_type ghosts{};
+    typename metadata_type::periodic_array_type periodic{};
+    for (int dim = 0; dim < 2; ++dim) {
+        ghosts[dim][LowerBoundary] = 2;
+        ghosts[dim][UpperBoundary] = 2;
+        periodic[dim] = 1;
+    }
+    metadata_type metadata(extents, ghosts, periodic);
+    const int max_faces = std::max(nx, ny) + 5;
+    typename StoredGrid::coordinate_view_type faces("stored_faces", 2, max_faces);
+    const double* edges[2] = {x_edges, y_edges};
+    const int counts[2] = {nx, ny};
+    for (int dim = 0; dim < 2; ++dim) {
+        const int n = counts[dim];
+        const double* e = edges[dim];
+        const double w = e[n] - e[0];
+        for (int storage = 0; storage < max_faces; ++storage) {
+            const int k = storage - 2;
+            double f = 0.0;
+            if (k < 0) {
+                f = e[n + k] - w;
+            } else if (k > n) {
+                f = (k - n <= n) ? e[k - n] + w : e[n] + w;
+            } else {
+                f = e[k];
+            }
+            faces(dim, storage) = f;
+        }
+    }
+    StoredBackground result;
+    result.grid = GridValidation::make_validated_stored_coordinate_grid<2, Device,
+        typename DeviceTraits<Device>::array_layout, 3>(metadata, faces);
+    result.magnetic_field = StoredBackground::vector_field_type(result.grid, "stored_b",
+                                                                GridCentering::CellCentered);
+    result.velocity_field = StoredBackground::vector_field_type(result.grid, "stored_v",
+                                                                GridCentering::CellCentered);
+    const std::size_t cells = static_cast<std::size_t>(nx) * static_cast<std::size_t>(ny);
+    for (int comp = 0; comp < 3; ++comp) {
+        for (int j = 0; j < ny; ++j) {
+            for (int i = 0; i < nx; ++i) {
+                typename StoredGrid::index_array_type idx{};
+                idx[0] = i;
+                idx[1] = j;
+                const std::size_t src = static_cast<std::size_t>(comp) * cells +
+                                        static_cast<std::size_t>(j) * nx + i;
+                result.magnetic_field.data(result.magnetic_field.flatten(idx), comp) = b[src];
+                result.velocity_field.data(result.velocity_field.flatten(idx), comp) = v[src];
+            }
+        }
+    }
+    result.magnetic_field.fill_ghost_cells(FieldGhostFillMode::PeriodicOrClamped, true);
+    result.velocity_field.fill_ghost_cells(FieldGhostFillMode::PeriodicOrClamped, true);
+    return result;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* ref_last_error() { return g_last_error.c_str(); }
+
+// Build the driver's per-cell coefficient table (16 Parker or 21 focused
+// components) for one compact field file.  out holds point_count * C doubles
+// in the Field's flattened order (x fastest over nx+4, then ny+4).
+long long ref_table(const char* path, int focused, double* out, long long out_len) {
+    try {
+        const std::string file(path);
+        const auto slash = file.find_last_of('/');
+        const std::string dir = file.substr(0, slash);
+        const int frame = std::stoi(file.substr(slash + 6, 5));
+        if (focused) {
+            const auto table = load_coefficient_frame<>(dir, frame);
+            const long long n = static_cast<long long>(table.point_count()) *
+                                coefficient_component_count;
+            if (out != nullptr && out_len >= n) {
+                std::copy(table.data.data(), table.data.data() + n, out);
+            }
+            return n;
+        }
+        const auto table = load_parker_coefficient_frame<>(dir, frame);
+        const long long n = static_cast<long long>(table.point_count()) *
+                            parker_coefficient_component_count;
+        if (out != nullptr && out_len >= n) {
+            std::copy(table.data.data(), table.data.data() + n, out);
+        }
+        return n;
+    } catch (const std::exception& error) {
+        g_last_error = error.what();
+        return -1;
+    }
+}
+
+// inject_uniform_particles for one frame.  When band_lo < band_hi the y draw
+// uses [band_lo, band_hi) instead of the whole domain (the injection band of
+// the benchmark configuration; the rest of the kernel is unchanged).
+long long ref_inject(const char* field_dir, const double* d, const int* ip,
+                     unsigned long long seed, int frame, unsigned long long capacity,
+                     unsigned long long count, unsigned long long requested,
+                     double band_lo, double band_hi, double* x, double* y, double* p,
+                     double* t, double* dt, double* w, double* mu, int* status,
+                     int* level) {
+    try {
+        const auto s = settings_from(d, ip);
+        const auto table = load_parker_coefficient_frame<>(field_dir, frame);
+        auto ds = device_settings_for(s, table);
+        if (band_lo < band_hi) {
+            ds.y_lower = band_lo;
+            ds.y_upper = band_hi;
+        }
+        ReconnectionParticleStorage<> storage(capacity);
+        const HostParticles h{x, y, p, t, dt, w, mu, status, level};
+        load_storage(storage, h, count);
+        RandomManager<> rng(seed);
+        Kokkos::ShimImpl::current_frame() = static_cast<std::uint32_t>(frame);
+        const double interval_start = static_cast<double>(frame) * s.mhd_dt;
+        inject_uniform_particles(storage, rng, ds, requested, interval_start);
+        store_storage(storage, h, storage.count);
+        return static_cast<long long>(storage.count);
+    } catch (const std::exception& error) {
+        g_last_error = error.what();
+        return -1;
+    }
+}
+
+// One interval push (Parker or focused per ip[IP_FOCUSED]) between
+// fieldNNNNN.bin frames `frame` and `frame + 1` of field_dir.
+long long ref_push(const char* field_dir, const double* d, const int* ip,
+                   unsigned long long seed, int frame, unsigned long long capacity,
+                   unsigned long long count, double* x, double* y, double* p, double* t,
+                   double* dt, double* w, double* mu, int* status, int* level) {
+    try {
+        const auto s = settings_from(d, ip);
+        ReconnectionParticleStorage<> storage(capacity);
+        const HostParticles h{x, y, p, t, dt, w, mu, status, level};
+        load_storage(storage, h, count);
+        RandomManager<> rng(seed);
+        Kokkos::ShimImpl::current_frame() = static_cast<std::uint32_t>(frame);
+        const double interval_start = static_cast<double>(frame) * s.mhd_dt;
+        if (ip[IP_FOCUSED]) {
+            const auto lower = load_coefficient_frame<>(field_dir, frame);
+            const auto upper = load_coefficient_frame<>(field_dir, frame + 1);
+            const auto ds = device_settings_for(s, lower);
+            move_particles_one_interval(storage, lower, upper, rng, ds, interval_start);
+        } else {
+            const auto lower = load_parker_coefficient_frame<>(field_dir, frame);
+            const auto upper = load_parker_coefficient_frame<>(field_dir, frame + 1);
+            const auto ds = device_settings_for(s, lower);
+            move_parker_particles_one_interval(storage, lower, upper, rng, ds,
+                                               interval_start);
+        }
+        store_storage(storage, h, count);
+        return static_cast<long long>(count);
+    } catch (const std::exception& error) {
+        g_last_error = error.what();
+        return -1;
+    }
+}
+
+// split_particles; writes the split and skipped counters and returns the new
+// stored count.  Run with one OpenMP thread for the serial child order.
+long long ref_split(const char* field_dir, const double* d, const int* ip, int frame,
+                    unsigned long long capacity, unsigned long long count, double* x,
+                    double* y, double* p, double* t, double* dt, double* w, double* mu,
+                    int* status, int* level, unsigned long long* split_out,
+                    unsigned long long* skipped_out) {
+    try {
+        const auto s = settings_from(d, ip);
+        const auto table = load_parker_coefficient_frame<>(field_dir, frame);
+        const auto ds = device_settings_for(s, table);
+        ReconnectionParticleStorage<> storage(capacity);
+        const HostParticles h{x, y, p, t, dt, w, mu, status, level};
+        load_storage(storage, h, count);
+        const auto counts = split_particles(storage, ds);
+        *split_out = counts.first;
+        *skipped_out = counts.second;
+        store_storage(storage, h, storage.count);
+        return static_cast<long long>(storage.count);
+    } catch (const std::exception& error) {
+        g_last_error = error.what();
+        return -1;
+    }
+}
+
+// Coefficient table on explicit face edges (StoredCoordinateGrid path).
+long long ref_table_stored(int nx, int ny, const double* x_edges, const double* y_edges,
+                           const double* b, const double* v, int focused, double* out,
+                           long long out_len) {
+    try {
+        const auto background = make_stored_background(nx, ny, x_edges, y_edges, b, v);
+        if (focused) {
+            const auto table = make_reconnection_coefficients(background, "stored_table");
+            const long long n = static_cast<long long>(table.point_count()) *
+                                coefficient_component_count;
+            if (out != nullptr && out_len >= n) {
+                std::copy(table.data.data(), table.data.data() + n, out);
+            }
+            return n;
+        }
+        const auto table = make_parker_reconnection_coefficients(background, "stored_table");
+        const long long n = static_cast<long long>(table.point_count()) *
+                            parker_coefficient_component_count;
+        if (out != nullptr && out_len >= n) {
+            std::copy(table.data.data(), table.data.data() + n, out);
+        }
+        return n;
+    } catch (const std::exception& error) {
+        g_last_error = error.what();
+        return -1;
+    }
+}
+
+// One interval push on explicit face edges: lower frame (b0, v0) and upper
+// frame (b1, v1) share the edges.
+long long ref_push_stored(int nx, int ny, const double* x_edges, const double* y_edges,
+                          const double* b0, const double* v0, const double* b1,
+                          const double* v1, const double* d, const int* ip,
+                          unsigned long long seed, int frame, unsigned long long capacity,
+                          unsigned long long count, double* x, double* y, double* p, double* t,
+                          double* dt, double* w, double* mu, int* status, int* level) {
+    try {
+        const auto s = settings_from(d, ip);
+        ReconnectionParticleStorage<> storage(capacity);
+        const HostParticles h{x, y, p, t, dt, w, mu, status, level};
+        load_storage(storage, h, count);
+        RandomManager<> rng(seed);
+        Kokkos::ShimImpl::current_frame() = static_cast<std::uint32_t>(frame);
+        const double interval_start = static_cast<double>(frame) * s.mhd_dt;
+        const auto lower_bg = make_stored_background(nx, ny, x_edges, y_edges, b0, v0);
+        const auto upper_bg = make_stored_background(nx, ny, x_edges, y_edges, b1, v1);
+        if (ip[IP_FOCUSED]) {
+            const auto lower = make_reconnection_coefficients(lower_bg, "stored_lower");
+            const auto upper = make_reconnection_coefficients(upper_bg, "stored_upper");
+            const auto ds = device_settings_for(s, lower);
+            move_particles_one_interval(storage, lower, upper, rng, ds, interval_start);
+        } else {
+            const auto lower = make_parker_reconnection_coefficients(lower_bg, "stored_lower");
+            const auto upper = make_parker_reconnection_coefficients(upper_bg, "stored_upper");
+            const auto ds = device_settings_for(s, lower);
+            move_parker_particles_one_interval(storage, lower, upper, rng, ds,
+                                               interval_start);
+        }
+        store_storage(storage, h, count);
+        return static_cast<long long>(count);
+    } catch (const std::exception& error) {
+        g_last_error = error.what();
+        return -1;
+    }
+}
+
+// The reference CLI entry point itself.  Noise frames are keyed as
+// frame_base + launch ordinal, frame_base being the run's start frame.
+int ref_main(int argc, char** argv, int frame_base) {
+    Kokkos::ShimImpl::launch_ordinals() = Kokkos::ShimImpl::LaunchOrdinals{};
+    Kokkos::ShimImpl::auto_frame_enabled() = 1;
+    Kokkos::ShimImpl::auto_frame_base() = static_cast<std::uint32_t>(frame_base);
+    const int rc = kpt_ref_main(argc, argv);
+    Kokkos::ShimImpl::auto_frame_enabled() = 0;
+    return rc;
+}
+
+}  // extern "C"
