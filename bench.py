@@ -137,6 +137,8 @@ def run_gpu(args):
         start = parts.download()
         frame = START_FRAME
         for _ in range(args.warmup):
+            if args.sort_tile > 0:
+                ctx.sort(parts, lower, args.sort_tile, args.sort_tile)
             ctx.push_interval(parts, lower, upper, settings, frame, SEED)
             frame += 1
         torch.cuda.synchronize()
@@ -149,6 +151,8 @@ def run_gpu(args):
             for _ in range(args.steps):
                 e0 = torch.cuda.Event(enable_timing=True)
                 e1 = torch.cuda.Event(enable_timing=True)
+                if args.sort_tile > 0:
+                    ctx.sort(parts, lower, args.sort_tile, args.sort_tile)
                 e0.record(stream)
                 stats = ctx.push_interval(parts, lower, upper, settings, frame, SEED)
                 e1.record(stream)
@@ -165,6 +169,8 @@ def run_gpu(args):
         t0 = time.perf_counter()
         for k in range(args.steps):
             parts.upload(host, n)
+            if args.sort_tile > 0:
+                ctx.sort(parts, lower, args.sort_tile, args.sort_tile)
             stats = ctx.push_interval(parts, lower, upper, settings, START_FRAME + k, SEED)
             host = parts.download(n)
             e2e_steps += stats.particle_steps
@@ -213,12 +219,14 @@ def main():
     parser.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     parser.add_argument("--particles", type=int, default=1 << 20)
     parser.add_argument("--cpu-particles", type=int, default=1 << 15)
+    parser.add_argument("--sort-tile", type=int, default=16,
+                        help="cell-sort tile (cells) before each push; 0 disables")
     args = parser.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     config = {"workload": f"parker push, {NX}x{NY} stretched-y Harris+islands field, "
                           f"{args.particles} particles, consecutive intervals",
               "nx": NX, "ny": NY, "particles": args.particles, "transport": "parker",
-              "l2": "tables larger than L2 (no flush)"}
+              "l2": "tables larger than L2 (no flush)", "sort_tile": args.sort_tile}
     if args.impl == "reference":
         if rank != 0:
             return
@@ -264,7 +272,8 @@ def main():
         "e2e": {"value": mixed["e2e_steps"] / mixed["e2e_s"], "unit": "particle-steps/s",
                 "h2d_bytes_per_step": mixed["state_bytes"],
                 "d2h_bytes_per_step": mixed["state_bytes"]},
-        "gpu_launches": 2 * args.steps,
+        # per timed step: the push, plus 3 cell-sort kernels when sorting
+        "gpu_launches": args.steps * (1 + (3 if args.sort_tile > 0 else 0)),
         "clocks": mixed["clocks"],
     }
     print(json.dumps(line))

@@ -6,7 +6,8 @@
  * last failure on the calling thread) and never falls back to the CPU: with
  * no usable CUDA device, kpt_context_create fails.
  *
- * Handles are opaque and owned by their creator.  Calls on one context are
+ * Handles are opaque and owned by their creator; fields and particle stores
+ * may be destroyed before or after their context.  Calls on one context are
  * ordered on the context's CUDA stream; calls that return host results
  * (counts, histograms, summaries, downloads) synchronise that stream.
  *
@@ -152,9 +153,9 @@ int kpt_context_destroy(kpt_context* ctx);
 int kpt_context_set_stream(kpt_context* ctx, void* cuda_stream);
 int kpt_context_synchronize(kpt_context* ctx);
 /* Push scheduling: KPT_SCHEDULE_REFILL (persistent warps that refill lanes
- * from a work cursor; blocks_per_sm x SM count blocks of 128 threads) or
- * KPT_SCHEDULE_SIMPLE (one particle per thread).  Results do not depend on
- * the choice; the autotuner picks the faster one. */
+ * from a work cursor; blocks_per_sm x SM count blocks of 128 threads, 0 =
+ * as many as are resident) or KPT_SCHEDULE_SIMPLE (one particle per
+ * thread).  Results do not depend on the choice. */
 int kpt_context_set_push_schedule(kpt_context* ctx, int schedule, int blocks_per_sm);
 
 /* ---- fields: one MHD frame as a device coefficient table ---------------- */
@@ -177,6 +178,12 @@ int kpt_field_download_table(const kpt_field* field, double* out, uint64_t out_l
 
 /* ---- particles --------------------------------------------------------- */
 int kpt_particles_create(kpt_context* ctx, uint64_t capacity, kpt_particles** out);
+/* Non-owning store over existing device arrays (for example the CUDA-backend
+ * Views of the reference's ReconnectionParticleStorage, src/main.cpp:292-333:
+ * x = position.data(), y = position.data() + capacity under LayoutLeft).
+ * The caller keeps the memory alive; destroy releases only the handle. */
+int kpt_particles_wrap(kpt_context* ctx, uint64_t capacity, uint64_t count,
+                       const kpt_particle_arrays* arrays, kpt_particles** out);
 int kpt_particles_destroy(kpt_particles* particles);
 int kpt_particles_count(const kpt_particles* particles, uint64_t* count,
                         uint64_t* capacity);
@@ -190,6 +197,15 @@ int kpt_particles_download(const kpt_particles* particles, uint64_t count, doubl
                            double* y, double* p, double* t, double* step_dt, double* weight,
                            double* mu, int32_t* status, int32_t* split_level);
 int kpt_particles_device_arrays(const kpt_particles* particles, kpt_particle_arrays* out);
+
+/* Cell sort of the work order: particle indices are ordered by spatial tile
+ * (tile_x x tile_y cells, inactive particles last) and later pushes visit
+ * particles in that order for cache locality.  Particle storage does not
+ * move, so ids, noise streams and results are unchanged; the order is
+ * dropped whenever the particle count changes (inject, split, upload). */
+int kpt_particles_sort(kpt_context* ctx, kpt_particles* particles, const kpt_field* grid,
+                       int tile_x, int tile_y);
+int kpt_particles_clear_order(kpt_particles* particles);
 
 /* ---- hot path ---------------------------------------------------------- */
 /* Append min(requested, capacity - count) particles for the interval that

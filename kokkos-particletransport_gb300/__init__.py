@@ -14,8 +14,8 @@ available.
 from __future__ import annotations
 
 import ctypes
-import dataclasses
 import os
+import weakref
 from typing import Dict, Optional, Sequence
 
 import numpy as np
@@ -122,6 +122,9 @@ def load_library() -> ctypes.CDLL:
         "kpt_histogram": (i32, [vp, vp, dbl, dbl, i32, vp]),
         "kpt_summarize": (i32, [vp, vp, vp]),
         "kpt_sample_table": (i32, [vp, vp, vp, u64, vp, vp, vp, i32, vp]),
+        "kpt_particles_sort": (i32, [vp, vp, vp, i32, i32]),
+        "kpt_particles_clear_order": (i32, [vp]),
+        "kpt_particles_wrap": (i32, [vp, u64, u64, vp, pvp]),
     }
     for name, (restype, argtypes) in sig.items():
         fn = getattr(lib, name)
@@ -165,11 +168,20 @@ class Context:
 
     def __init__(self, device: int = 0):
         self.lib = load_library()
+        self.handle = ctypes.c_void_p()
+        self._children = weakref.WeakSet()
         handle = ctypes.c_void_p()
         _check(self.lib.kpt_context_create(device, ctypes.byref(handle)))
         self.handle = handle
 
+    def _adopt(self, child):
+        self._children.add(child)
+        return child
+
     def close(self) -> None:
+        """Destroy the context after every field and store created from it."""
+        for child in list(self._children):
+            child.close()
         if self.handle:
             self.lib.kpt_context_destroy(self.handle)
             self.handle = ctypes.c_void_p()
@@ -201,20 +213,29 @@ class Context:
         _check(self.lib.kpt_field_create(self.handle, field.nx, field.ny, _ptr(xe), _ptr(ye),
                                          _ptr(b), _ptr(v), kind, precision,
                                          ctypes.byref(handle)))
-        return Field(self, handle)
+        return self._adopt(Field(self, handle))
 
     def load_field(self, path: str, kind: int = TABLE_PARKER16,
                    precision: int = PRECISION_F64) -> "Field":
         handle = ctypes.c_void_p()
         _check(self.lib.kpt_field_load(self.handle, path.encode(), kind, precision,
                                        ctypes.byref(handle)))
-        return Field(self, handle)
+        return self._adopt(Field(self, handle))
 
     # -- particles ------------------------------------------------------
+    def wrap_particles(self, capacity: int, count: int,
+                       device_arrays: Dict[str, int]) -> "ParticleStorage":
+        """Non-owning store over existing device arrays (pointers as ints)."""
+        arr = ParticleArrays(**{k: device_arrays[k] for k, _ in ParticleArrays._fields_})
+        handle = ctypes.c_void_p()
+        _check(self.lib.kpt_particles_wrap(self.handle, int(capacity), int(count),
+                                           ctypes.byref(arr), ctypes.byref(handle)))
+        return self._adopt(ParticleStorage(self, handle))
+
     def particles(self, capacity: int) -> "ParticleStorage":
         handle = ctypes.c_void_p()
         _check(self.lib.kpt_particles_create(self.handle, int(capacity), ctypes.byref(handle)))
-        return ParticleStorage(self, handle)
+        return self._adopt(ParticleStorage(self, handle))
 
     # -- hot path -------------------------------------------------------
     def inject(self, parts: "ParticleStorage", grid: "Field", settings: Settings,
@@ -241,6 +262,15 @@ class Context:
         _check(self.lib.kpt_split(self.handle, parts.handle, ctypes.byref(settings),
                                   ctypes.byref(split), ctypes.byref(skipped)))
         return int(split.value), int(skipped.value)
+
+    def sort(self, parts: "ParticleStorage", grid: "Field", tile_x: int = 16,
+             tile_y: int = 16) -> None:
+        """Order the work of later pushes by spatial tile (storage unchanged)."""
+        _check(self.lib.kpt_particles_sort(self.handle, parts.handle, grid.handle, int(tile_x),
+                                           int(tile_y)))
+
+    def clear_order(self, parts: "ParticleStorage") -> None:
+        _check(self.lib.kpt_particles_clear_order(parts.handle))
 
     def histogram(self, parts: "ParticleStorage", pmin: float, pmax: float,
                   nbins: int = 128) -> np.ndarray:

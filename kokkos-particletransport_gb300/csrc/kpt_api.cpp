@@ -92,26 +92,35 @@ struct kpt_context {
     DeviceBuffer summary_partials, summary_result;
     DeviceBuffer sample_io;
     int push_schedule = kpt::kScheduleRefill;
-    int push_blocks_per_sm = 8;
+    int push_blocks_per_sm = 0;  // 0: as many as fit (occupancy)
 };
 
 struct kpt_field {
     kpt_context* ctx = nullptr;
+    int device = 0;
     int nx = 0, ny = 0;
     int kind = 0, precision = 0, stride = 0;
     uint64_t points = 0;
     void* table = nullptr;
     double* centers[2] = {nullptr, nullptr};
     int* buckets[2] = {nullptr, nullptr};
+    long long* fixed_centers[2] = {nullptr, nullptr};
+    float* fixed_spacing[2] = {nullptr, nullptr};
+    int* fixed_buckets[2] = {nullptr, nullptr};
     kpt::Grid grid{};
+    kpt::FixedAxis fixed[2]{};
 };
 
 struct kpt_particles {
     kpt_context* ctx = nullptr;
+    int device = 0;
     uint64_t capacity = 0;
     uint64_t count = 0;
-    void* block = nullptr;
+    void* block = nullptr;  // owned storage; NULL for wrapped external arrays
     kpt::ParticleArrays arrays{};
+    // Work order from the last cell sort; valid while count is unchanged.
+    DeviceBuffer order, keys, tile_counts;
+    bool order_valid = false;
 };
 
 namespace {
@@ -192,6 +201,65 @@ int build_axis(int n, const double* e, kpt::Axis& axis, std::vector<double>& cen
     axis.width = axis.upper - axis.lower;
     axis.inv_width = axis.width != 0.0 ? 1.0 / axis.width : 0.0;
     return KPT_OK;
+}
+
+// Fixed-point description of an axis for the mixed-precision push (phase =
+// (x - lower) / width * 2^64).  Stretched axes get their ghosted cell
+// centres at a 2^62 scale, the per-interval inverse spacing and a bucket
+// table that seeds the interval search.
+struct FixedAxisHost {
+    kpt::FixedAxis axis{};
+    std::vector<long long> centers;
+    std::vector<float> inv_spacing;
+    std::vector<int> buckets;
+};
+
+FixedAxisHost build_fixed_axis(const kpt::Axis& a, const std::vector<double>& centers) {
+    FixedAxisHost h;
+    h.axis.n = a.n;
+    h.axis.stored = a.stored;
+    h.axis.half_cell = 9223372036854775808ull / static_cast<unsigned long long>(a.n);
+    h.axis.to_fixed = static_cast<float>(18446744073709551616.0 / a.width);
+    if (!a.stored) {
+        return h;
+    }
+    const long double scale = 4611686018427387904.0L / static_cast<long double>(a.width);
+    h.centers.resize(centers.size());
+    for (size_t k = 0; k < centers.size(); ++k) {
+        h.centers[k] = static_cast<long long>(
+            std::llround(static_cast<long double>(centers[k] - a.lower) * scale));
+    }
+    long long max_spacing = 1;
+    for (size_t k = 0; k + 1 < h.centers.size(); ++k) {
+        max_spacing = std::max(max_spacing, h.centers[k + 1] - h.centers[k]);
+    }
+    int bits = 0;
+    while (bits < 63 && (max_spacing >> bits) != 0) {
+        ++bits;
+    }
+    const int shift = std::max(0, bits - 31);
+    h.axis.spacing_shift = shift;
+    h.inv_spacing.resize(h.centers.size() - 1);
+    for (size_t k = 0; k + 1 < h.centers.size(); ++k) {
+        h.inv_spacing[k] = static_cast<float>(std::ldexp(1.0, shift) /
+                                              static_cast<double>(h.centers[k + 1] - h.centers[k]));
+    }
+    int log2b = 0;
+    while ((1 << log2b) < 4 * (a.n + 4) && log2b < 20) {
+        ++log2b;
+    }
+    h.axis.bucket_shift = 64 - log2b;
+    h.buckets.resize(static_cast<size_t>(1) << log2b);
+    int k = -2;
+    for (size_t b = 0; b < h.buckets.size(); ++b) {
+        const long long start = static_cast<long long>(
+            (static_cast<unsigned long long>(b) << h.axis.bucket_shift) >> 2);
+        while (k < a.n && h.centers[k + 3] <= start) {
+            ++k;
+        }
+        h.buckets[b] = k;
+    }
+    return h;
 }
 
 // Reconnection2DSettings::validate, physics block (src/main.cpp:222-239).
@@ -364,8 +432,8 @@ int kpt_context_set_push_schedule(kpt_context* ctx, int schedule, int blocks_per
     KPT_REQUIRE(ctx != nullptr, "kpt_context_set_push_schedule: ctx is NULL");
     KPT_REQUIRE(schedule == KPT_SCHEDULE_REFILL || schedule == KPT_SCHEDULE_SIMPLE,
                 "kpt_context_set_push_schedule: unknown schedule");
-    KPT_REQUIRE(blocks_per_sm >= 1 && blocks_per_sm <= 32,
-                "kpt_context_set_push_schedule: blocks_per_sm must be in [1, 32]");
+    KPT_REQUIRE(blocks_per_sm >= 0 && blocks_per_sm <= 32,
+                "kpt_context_set_push_schedule: blocks_per_sm must be in [0, 32]");
     ctx->push_schedule = schedule == KPT_SCHEDULE_SIMPLE ? kpt::kScheduleSimple
                                                          : kpt::kScheduleRefill;
     ctx->push_blocks_per_sm = blocks_per_sm;
@@ -402,6 +470,7 @@ int kpt_field_create(kpt_context* ctx, int nx, int ny, const double* x_edges,
     };
     std::unique_ptr<kpt_field, FieldDeleter> f(new kpt_field());
     f->ctx = ctx;
+    f->device = ctx->device;
     f->nx = nx;
     f->ny = ny;
     f->kind = table_kind;
@@ -417,7 +486,21 @@ int kpt_field_create(kpt_context* ctx, int nx, int ny, const double* x_edges,
         if (int rc = build_axis(counts[d], edges[d], f->grid.axis[d], centers, buckets)) {
             return rc;
         }
+        FixedAxisHost fixed = build_fixed_axis(f->grid.axis[d], centers);
+        f->fixed[d] = fixed.axis;
         if (!centers.empty()) {
+            KPT_CUDA(cudaMalloc(&f->fixed_centers[d], fixed.centers.size() * sizeof(long long)));
+            KPT_CUDA(cudaMemcpy(f->fixed_centers[d], fixed.centers.data(),
+                                fixed.centers.size() * sizeof(long long), cudaMemcpyHostToDevice));
+            KPT_CUDA(cudaMalloc(&f->fixed_spacing[d], fixed.inv_spacing.size() * sizeof(float)));
+            KPT_CUDA(cudaMemcpy(f->fixed_spacing[d], fixed.inv_spacing.data(),
+                                fixed.inv_spacing.size() * sizeof(float), cudaMemcpyHostToDevice));
+            KPT_CUDA(cudaMalloc(&f->fixed_buckets[d], fixed.buckets.size() * sizeof(int)));
+            KPT_CUDA(cudaMemcpy(f->fixed_buckets[d], fixed.buckets.data(),
+                                fixed.buckets.size() * sizeof(int), cudaMemcpyHostToDevice));
+            f->fixed[d].centers = f->fixed_centers[d];
+            f->fixed[d].inv_spacing = f->fixed_spacing[d];
+            f->fixed[d].buckets = f->fixed_buckets[d];
             KPT_CUDA(cudaMalloc(&f->centers[d], centers.size() * sizeof(double)));
             KPT_CUDA(cudaMemcpy(f->centers[d], centers.data(), centers.size() * sizeof(double),
                                 cudaMemcpyHostToDevice));
@@ -512,12 +595,16 @@ int kpt_field_destroy(kpt_field* field) {
     if (field == nullptr) {
         return KPT_OK;
     }
-    cudaSetDevice(field->ctx->device);
-    cudaStreamSynchronize(field->ctx->stream);
+    // cudaFree waits for outstanding work on the memory; the context (which
+    // may already be gone) is not touched.
+    cudaSetDevice(field->device);
     cudaFree(field->table);
     for (int d = 0; d < 2; ++d) {
         cudaFree(field->centers[d]);
         cudaFree(field->buckets[d]);
+        cudaFree(field->fixed_centers[d]);
+        cudaFree(field->fixed_spacing[d]);
+        cudaFree(field->fixed_buckets[d]);
     }
     delete field;
     return KPT_OK;
@@ -572,6 +659,7 @@ int kpt_particles_create(kpt_context* ctx, uint64_t capacity, kpt_particles** ou
     if (int rc = activate(ctx)) return rc;
     std::unique_ptr<kpt_particles> parts(new kpt_particles());
     parts->ctx = ctx;
+    parts->device = ctx->device;
     parts->capacity = capacity;
     // One allocation: 7 double arrays then 2 int32 arrays, each 256-byte aligned.
     auto round_up = [](size_t v) { return (v + 255) & ~static_cast<size_t>(255); };
@@ -597,13 +685,49 @@ int kpt_particles_create(kpt_context* ctx, uint64_t capacity, kpt_particles** ou
     return KPT_OK;
 }
 
+int kpt_particles_wrap(kpt_context* ctx, uint64_t capacity, uint64_t count,
+                       const kpt_particle_arrays* arrays, kpt_particles** out) {
+    KPT_REQUIRE(ctx != nullptr && arrays != nullptr && out != nullptr,
+                "kpt_particles_wrap: NULL argument");
+    *out = nullptr;
+    KPT_REQUIRE(capacity > 0 && capacity < (1ull << 32) && count <= capacity,
+                "kpt_particles_wrap: need 0 < capacity < 2^32 and count <= capacity");
+    const void* ptrs[9] = {arrays->x, arrays->y, arrays->p, arrays->t, arrays->step_dt,
+                           arrays->weight, arrays->mu, arrays->status, arrays->split_level};
+    for (const void* ptr : ptrs) {
+        KPT_REQUIRE(ptr != nullptr, "kpt_particles_wrap: NULL array");
+        cudaPointerAttributes attr{};
+        KPT_CUDA(cudaPointerGetAttributes(&attr, ptr));
+        KPT_REQUIRE(attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged,
+                    "kpt_particles_wrap: arrays must be device (or managed) memory");
+    }
+    std::unique_ptr<kpt_particles> parts(new kpt_particles());
+    parts->ctx = ctx;
+    parts->device = ctx->device;
+    parts->capacity = capacity;
+    parts->count = count;
+    parts->arrays.x = arrays->x;
+    parts->arrays.y = arrays->y;
+    parts->arrays.p = arrays->p;
+    parts->arrays.t = arrays->t;
+    parts->arrays.step_dt = arrays->step_dt;
+    parts->arrays.weight = arrays->weight;
+    parts->arrays.mu = arrays->mu;
+    parts->arrays.status = arrays->status;
+    parts->arrays.split_level = arrays->split_level;
+    *out = parts.release();
+    return KPT_OK;
+}
+
 int kpt_particles_destroy(kpt_particles* parts) {
     if (parts == nullptr) {
         return KPT_OK;
     }
-    cudaSetDevice(parts->ctx->device);
-    cudaStreamSynchronize(parts->ctx->stream);
+    cudaSetDevice(parts->device);
     cudaFree(parts->block);
+    parts->order.release();
+    parts->keys.release();
+    parts->tile_counts.release();
     delete parts;
     return KPT_OK;
 }
@@ -619,6 +743,7 @@ int kpt_particles_set_count(kpt_particles* parts, uint64_t count) {
     KPT_REQUIRE(parts != nullptr, "kpt_particles_set_count: NULL handle");
     KPT_REQUIRE(count <= parts->capacity, "kpt_particles_set_count: count exceeds capacity");
     parts->count = count;
+    parts->order_valid = false;
     return KPT_OK;
 }
 
@@ -641,6 +766,7 @@ int kpt_particles_upload(kpt_particles* parts, uint64_t count, const double* x,
     }
     KPT_CUDA(cudaStreamSynchronize(s));
     parts->count = count;
+    parts->order_valid = false;
     return KPT_OK;
 }
 
@@ -709,6 +835,7 @@ int kpt_inject_uniform(kpt_context* ctx, kpt_particles* parts, const kpt_field* 
     launch.seed = seed;
     KPT_CUDA(kpt::launch_inject(launch, ctx->stream));
     parts->count += n;
+    if (n > 0) parts->order_valid = false;
     if (injected) *injected = n;
     return KPT_OK;
 }
@@ -736,6 +863,12 @@ int kpt_push_interval(kpt_context* ctx, kpt_particles* parts, const kpt_field* l
     launch.frame = frame;
     launch.seed = seed;
     launch.counters = ctx->counters.as<kpt::PushCounters>();
+    launch.fixed.axis[0] = lower->fixed[0];
+    launch.fixed.axis[1] = lower->fixed[1];
+    launch.fixed.dt_min = static_cast<float>(launch.settings.dt_min);
+    launch.fixed.dt_max = static_cast<float>(launch.settings.dt_max);
+    launch.fixed.pfloor = 0.25 * settings->p0;
+    launch.order = parts->order_valid ? parts->order.as<uint32_t>() : nullptr;
     launch.precision = lower->precision;
     launch.focused = settings->focused != 0;
     launch.schedule = ctx->push_schedule;
@@ -826,6 +959,7 @@ int kpt_split(kpt_context* ctx, kpt_particles* parts, const kpt_settings* settin
     const uint64_t room = parts->capacity - parts->count;
     const uint64_t written = std::min<uint64_t>(wanted, room);
     parts->count += written;
+    if (written > 0) parts->order_valid = false;
     if (split) *split = written;
     if (skipped) *skipped = wanted - written;
     return KPT_OK;
@@ -920,6 +1054,42 @@ int kpt_summarize(kpt_context* ctx, const kpt_particles* parts, kpt_summary* out
         out->p_avg = r.p_sum / static_cast<double>(r.active);
         out->dt_avg = r.dt_sum / static_cast<double>(r.active);
     }
+    return KPT_OK;
+}
+
+int kpt_particles_sort(kpt_context* ctx, kpt_particles* parts, const kpt_field* grid,
+                       int tile_x, int tile_y) {
+    KPT_REQUIRE(ctx && parts && grid, "kpt_particles_sort: NULL handle");
+    KPT_REQUIRE(tile_x > 0 && tile_y > 0, "kpt_particles_sort: tile sizes must be positive");
+    if (int rc = activate(ctx)) return rc;
+    const int tiles_x = (grid->nx + tile_x - 1) / tile_x;
+    const int tiles_y = (grid->ny + tile_y - 1) / tile_y;
+    KPT_REQUIRE(static_cast<long long>(tiles_x) * tiles_y < (1ll << 30),
+                "kpt_particles_sort: too many tiles");
+    const uint64_t n = std::max<uint64_t>(parts->count, 1);
+    KPT_CUDA(parts->order.reserve(n * sizeof(uint32_t)));
+    KPT_CUDA(parts->keys.reserve(n * sizeof(uint32_t)));
+    KPT_CUDA(parts->tile_counts.reserve((static_cast<size_t>(tiles_x) * tiles_y + 1) *
+                                        sizeof(uint32_t)));
+    kpt::SortLaunch launch{};
+    launch.grid = grid->grid;
+    launch.parts = parts->arrays;
+    launch.count = parts->count;
+    launch.tile_x = tile_x;
+    launch.tile_y = tile_y;
+    launch.tiles_x = tiles_x;
+    launch.tiles_y = tiles_y;
+    launch.keys = parts->keys.as<unsigned int>();
+    launch.counts = parts->tile_counts.as<unsigned int>();
+    launch.order = parts->order.as<unsigned int>();
+    KPT_CUDA(kpt::launch_sort(launch, ctx->stream));
+    parts->order_valid = true;
+    return KPT_OK;
+}
+
+int kpt_particles_clear_order(kpt_particles* parts) {
+    KPT_REQUIRE(parts != nullptr, "kpt_particles_clear_order: NULL handle");
+    parts->order_valid = false;
     return KPT_OK;
 }
 

@@ -24,6 +24,8 @@ inline int table_stride(int focused, int precision) {
 
 struct PushLaunch {
     Grid grid;
+    FixedGrid fixed;
+    const uint32_t* order;  // optional permutation of [0, count) (cell sort)
     const void* lower;
     const void* upper;
     ParticleArrays parts;
@@ -115,6 +117,19 @@ struct SummaryLaunch {
 };
 int summary_blocks(uint64_t count);
 cudaError_t launch_summary(const SummaryLaunch& launch, cudaStream_t stream);
+
+// Counting sort of particle indices by spatial tile (inactive particles
+// last).  counts/offsets hold tiles + 1 entries.
+struct SortLaunch {
+    Grid grid;
+    ParticleArrays parts;
+    uint64_t count;
+    int tile_x, tile_y, tiles_x, tiles_y;
+    unsigned int* keys;     // count
+    unsigned int* counts;   // tiles + 1
+    unsigned int* order;    // count
+};
+cudaError_t launch_sort(const SortLaunch& launch, cudaStream_t stream);
 
 struct SampleLaunch {
     Grid grid;

@@ -281,7 +281,92 @@ __global__ void __launch_bounds__(kSummaryThreads) summary_final_kernel(const Su
     block_reduce(mine, L.result);
 }
 
+// --------------------------------------------------------------- sort
+// Tile key of each particle from its position (cell index by the grid map,
+// mean-spacing estimate refined by the stored centres); inactive particles
+// take the extra key so they sort last.
+__device__ __forceinline__ int cell_of(const Axis& a, double x) {
+    const double f = (x - a.lower) * a.inv_width;
+    int k = static_cast<int>(floor(f * a.n));
+    k = k < 0 ? 0 : (k >= a.n ? a.n - 1 : k);
+    return k;
+}
+
+__global__ void sort_key_kernel(const SortLaunch L) {
+    const unsigned tiles = static_cast<unsigned>(L.tiles_x) * static_cast<unsigned>(L.tiles_y);
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < L.count;
+         i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        unsigned key = tiles;
+        if (L.parts.status[i] == 0) {
+            const int cx = cell_of(L.grid.axis[0], L.parts.x[i]);
+            const int cy = cell_of(L.grid.axis[1], L.parts.y[i]);
+            key = static_cast<unsigned>(cy / L.tile_y) * static_cast<unsigned>(L.tiles_x) +
+                  static_cast<unsigned>(cx / L.tile_x);
+        }
+        L.keys[i] = key;
+        atomicAdd(L.counts + key, 1u);
+    }
+}
+
+// Exclusive scan of the tile counts in place (one block, fixed order).
+__global__ void __launch_bounds__(1024) sort_scan_kernel(unsigned int* counts, int n) {
+    __shared__ unsigned int warp_sums[32];
+    __shared__ unsigned int carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned warp = threadIdx.x >> 5;
+    for (int base = 0; base < n; base += 1024) {
+        const int idx = base + static_cast<int>(threadIdx.x);
+        const unsigned v = idx < n ? counts[idx] : 0u;
+        unsigned inclusive = v;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const unsigned y = __shfl_up_sync(0xffffffffu, inclusive, off);
+            if (lane >= static_cast<unsigned>(off)) inclusive += y;
+        }
+        if (lane == 31u) warp_sums[warp] = inclusive;
+        __syncthreads();
+        if (warp == 0) {
+            unsigned w = warp_sums[lane];
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const unsigned y = __shfl_up_sync(0xffffffffu, w, off);
+                if (lane >= static_cast<unsigned>(off)) w += y;
+            }
+            warp_sums[lane] = w;
+        }
+        __syncthreads();
+        const unsigned prefix = warp == 0 ? 0u : warp_sums[warp - 1];
+        if (idx < n) counts[idx] = carry + prefix + inclusive - v;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += warp_sums[31];
+        __syncthreads();
+    }
+}
+
+__global__ void sort_scatter_kernel(const SortLaunch L) {
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < L.count;
+         i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        const unsigned slot = atomicAdd(L.counts + L.keys[i], 1u);
+        L.order[slot] = static_cast<unsigned int>(i);
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_sort(const SortLaunch& L, cudaStream_t stream) {
+    const int tiles = L.tiles_x * L.tiles_y + 1;
+    cudaError_t err = cudaMemsetAsync(L.counts, 0, sizeof(unsigned int) * tiles, stream);
+    if (err != cudaSuccess || L.count == 0) return err;
+    const int threads = 256;
+    const uint64_t want = (L.count + threads - 1) / threads;
+    const int blocks = static_cast<int>(want > 152u * 16u ? 152u * 16u : want);
+    sort_key_kernel<<<blocks, threads, 0, stream>>>(L);
+    sort_scan_kernel<<<1, 1024, 0, stream>>>(L.counts, tiles);
+    sort_scatter_kernel<<<blocks, threads, 0, stream>>>(L);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_inject(const InjectLaunch& L, cudaStream_t stream) {
     if (L.n == 0) {

@@ -1,14 +1,28 @@
 // Interval push kernels: Parker (16-component table) and focused transport
-// (21 components), plain FP64 or mixed precision (FP32 table, interpolation,
-// coefficients and noise; FP64 position, time, momentum and cell search).
+// (21 components), plain FP64 or mixed precision.
 //
 // The per-substep physics restates reference src/main.cpp:1131-1306 (Parker)
-// and :1384-1733 (focused).  Scheduling is GB300-first: a persistent grid of
-// warps pulls particles from a device cursor, and a lane whose particle has
-// reached the interval end refills from the cursor, so warps stay full while
-// particles need very different substep counts (random injection times).
-// Noise is the keyed Philox stream, so results do not depend on which lane
-// or launch shape pushed a particle.
+// and :1384-1733 (focused) once, templated on the arithmetic type.
+//
+// GB300 notes.  FP64 issues at a small fraction of the FP32 rate on this
+// part, so the two paths differ in how they carry particle state:
+//  * plain FP64: every operation in double, position wrap and cell search as
+//    the reference computes them (parity within 1e-10 of the oracle);
+//  * mixed: table, interpolation, coefficients and noise in FP32; the
+//    position lives in a 64-bit fixed-point phase over the periodic width
+//    (2^-64 of the domain, finer than FP64 near the domain edge), so the
+//    periodic wrap is modular integer addition and the cell search (uniform
+//    axis: a 64x64->128-bit multiply; stretched axis: exact integer compares
+//    against fixed-point cell centres) runs on the integer pipes; time and
+//    momentum accumulate in FP64.
+//
+// Scheduling: a persistent grid of warps pulls particles from a device
+// cursor; a lane whose particle reached the interval end refills from the
+// cursor, so warps stay full although particles need very different substep
+// counts.  An optional permutation (a cell sort of particle indices) orders
+// the work for cache locality without moving particle storage.  Noise is the
+// keyed Philox stream (seed, particle index, frame), so results do not depend
+// on the lane, launch shape or work order.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -48,8 +62,7 @@ struct Num<float> {
     static __device__ __forceinline__ bool finite(float a) { return isfinite(a); }
     static __device__ __forceinline__ float abs(float a) { return fabsf(a); }
     static __device__ __forceinline__ float noise(uint32_t, uint32_t hi) {
-        return -static_cast<float>(kSqrt3) +
-               static_cast<float>(2.0 * kSqrt3) * u01_f32(hi);
+        return -static_cast<float>(kSqrt3) + static_cast<float>(2.0 * kSqrt3) * u01_f32(hi);
     }
 };
 
@@ -70,7 +83,7 @@ __device__ __forceinline__ T clamp_mu(T v, T m) {
     return v;
 }
 
-// Vector width used to stream one table point.
+// ------------------------------------------------------------ sampling
 template <typename T>
 struct Vec;
 template <>
@@ -95,34 +108,105 @@ __device__ __forceinline__ float vec_get<float>(const float4& v, int k) {
     return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w));
 }
 
-// Bilinear sample of one frame at precomputed corner points and weights
-// (LinearPositionInterpolator::sample, FieldInterpolator.hpp:346-380):
-// out = sum over corners in order (00, 10, 01, 11) of weight * value.
+// 256-bit read-only loads (sm_100+): 8 floats or 4 doubles per lane and
+// instruction, half the L1 wavefronts of 128-bit loads for the scattered
+// table gathers.  Table rows are 32-byte aligned (64 B / 96 B FP32 rows,
+// 128 B FP64 Parker rows; the focused FP64 row of 176 B keeps 128-bit loads).
+__device__ __forceinline__ void load8(const float* p, float v[8]) {
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]),
+          "=f"(v[7])
+        : "l"(p));
+}
+
+__device__ __forceinline__ void load8(const double* p, double v[4]) {
+    asm("ld.global.nc.v4.f64 {%0,%1,%2,%3}, [%4];"
+        : "=d"(v[0]), "=d"(v[1]), "=d"(v[2]), "=d"(v[3])
+        : "l"(p));
+}
+
+template <typename T, int STRIDE>
+struct Wide {
+    // elements per 256-bit load, and whether rows allow it
+    static constexpr int width = sizeof(T) == 4 ? 8 : 4;
+    static constexpr bool ok = (STRIDE * sizeof(T)) % 32 == 0;
+};
+
+// Bilinear sample of one frame (LinearPositionInterpolator::sample,
+// FieldInterpolator.hpp:346-380): sum over corners (00, 10, 01, 11) of
+// weight * value.
 template <typename T, int C, int STRIDE>
 __device__ __forceinline__ void sample_frame(const T* __restrict__ table, const size_t pt[4],
                                              const T wc[4], T out[C]) {
-    using V = typename Vec<T>::type;
-    constexpr int W = Vec<T>::width;
+    if constexpr (Wide<T, STRIDE>::ok) {
+        constexpr int W = Wide<T, STRIDE>::width;
 #pragma unroll
-    for (int corner = 0; corner < 4; ++corner) {
-        const V* src = reinterpret_cast<const V*>(table + pt[corner] * STRIDE);
+        for (int corner = 0; corner < 4; ++corner) {
+            const T* src = table + pt[corner] * STRIDE;
 #pragma unroll
-        for (int chunk = 0; chunk < (C + W - 1) / W; ++chunk) {
-            const V v = __ldg(src + chunk);
+            for (int chunk = 0; chunk < (C + W - 1) / W; ++chunk) {
+                T v[W];
+                load8(src + chunk * W, v);
 #pragma unroll
-            for (int k = 0; k < W; ++k) {
-                const int comp = chunk * W + k;
-                if (comp < C) {
-                    const T val = vec_get<T>(v, k);
-                    out[comp] = corner == 0 ? wc[0] * val : out[comp] + wc[corner] * val;
+                for (int k = 0; k < W; ++k) {
+                    const int comp = chunk * W + k;
+                    if (comp < C) {
+                        out[comp] = corner == 0 ? wc[0] * v[k] : out[comp] + wc[corner] * v[k];
+                    }
+                }
+            }
+        }
+    } else {
+        using V = typename Vec<T>::type;
+        constexpr int W = Vec<T>::width;
+#pragma unroll
+        for (int corner = 0; corner < 4; ++corner) {
+            const V* src = reinterpret_cast<const V*>(table + pt[corner] * STRIDE);
+#pragma unroll
+            for (int chunk = 0; chunk < (C + W - 1) / W; ++chunk) {
+                const V v = __ldg(src + chunk);
+#pragma unroll
+                for (int k = 0; k < W; ++k) {
+                    const int comp = chunk * W + k;
+                    if (comp < C) {
+                        const T val = vec_get<T>(v, k);
+                        out[comp] = corner == 0 ? wc[0] * val : out[comp] + wc[corner] * val;
+                    }
                 }
             }
         }
     }
 }
 
-// sample_time_interpolated_coefficients (src/main.cpp:1055-1077) at the
-// driver's shifted position (src/main.cpp:1142-1148).
+// Time interpolation (src/main.cpp:1055-1077) of the two frames sampled at
+// the same stencil.
+template <typename T, int C, int STRIDE>
+__device__ __forceinline__ void sample_stencil(const T* __restrict__ lower,
+                                               const T* __restrict__ upper, const size_t pt[4],
+                                               const T wc[4], T uw, int use_time, T c[C]) {
+    sample_frame<T, C, STRIDE>(lower, pt, wc, c);
+    if (use_time == 0) {
+        return;
+    }
+    T u[C];
+    sample_frame<T, C, STRIDE>(upper, pt, wc, u);
+    const T lw = T(1) - uw;
+#pragma unroll
+    for (int k = 0; k < C; ++k) {
+        c[k] = lw * c[k] + uw * u[k];
+    }
+}
+
+__device__ __forceinline__ void corner_points(int lo0, int hi0, int lo1, int hi1, int ex,
+                                              size_t pt[4]) {
+    const size_t e = static_cast<size_t>(ex);
+    pt[0] = static_cast<size_t>(lo0 + 2) + static_cast<size_t>(lo1 + 2) * e;
+    pt[1] = static_cast<size_t>(hi0 + 2) + static_cast<size_t>(lo1 + 2) * e;
+    pt[2] = static_cast<size_t>(lo0 + 2) + static_cast<size_t>(hi1 + 2) * e;
+    pt[3] = static_cast<size_t>(hi0 + 2) + static_cast<size_t>(hi1 + 2) * e;
+}
+
+// FP64 path: the driver's own sampling arithmetic (src/main.cpp:1142-1148).
 template <typename T, int C, int STRIDE>
 __device__ __forceinline__ void sample_coefficients(const Grid& g, const T* __restrict__ lower,
                                                     const T* __restrict__ upper, double q0,
@@ -138,74 +222,34 @@ __device__ __forceinline__ void sample_coefficients(const Grid& g, const T* __re
     const double a1 = 1.0 - w1;
     const T wc[4] = {static_cast<T>(a0 * a1), static_cast<T>(w0 * a1), static_cast<T>(a0 * w1),
                      static_cast<T>(w0 * w1)};
-    const size_t ex = static_cast<size_t>(g.ex);
-    const size_t pt[4] = {static_cast<size_t>(lo0 + 2) + static_cast<size_t>(lo1 + 2) * ex,
-                          static_cast<size_t>(hi0 + 2) + static_cast<size_t>(lo1 + 2) * ex,
-                          static_cast<size_t>(lo0 + 2) + static_cast<size_t>(hi1 + 2) * ex,
-                          static_cast<size_t>(hi0 + 2) + static_cast<size_t>(hi1 + 2) * ex};
-    sample_frame<T, C, STRIDE>(lower, pt, wc, c);
-    if (use_time == 0) {
-        return;
-    }
-    T u[C];
-    sample_frame<T, C, STRIDE>(upper, pt, wc, u);
+    size_t pt[4];
+    corner_points(lo0, hi0, lo1, hi1, g.ex, pt);
     const double uwd = rt < 0.0 ? 0.0 : (rt > 1.0 ? 1.0 : rt);
-    const T uw = static_cast<T>(uwd);
-    const T lw = static_cast<T>(1.0 - uwd);
-#pragma unroll
-    for (int k = 0; k < C; ++k) {
-        c[k] = lw * c[k] + uw * u[k];
-    }
+    sample_stencil<T, C, STRIDE>(lower, upper, pt, wc, static_cast<T>(uwd), use_time, c);
 }
 
+// ------------------------------------------------------------- physics
 template <typename T>
-struct State {
-    double x, y, p, t, dt, diag_dt;
-    T mu;
-    int steps;
-    int status;
-    uint32_t index;
+struct Rates {
+    T dx_dt, dy_dt, dp_dt, dmu_dt, duu;
+    T skperp, skpara_perp, ib, bx, by, bz;
+    T pitch_mu;
+    T dt;        // limiter result (valid when !fixed_dt)
+    bool fixed_dt;
 };
 
-struct PushParams {
-    Grid grid;
-    const void* lower;
-    const void* upper;
-    ParticleArrays parts;
-    uint64_t count;
-    DeviceSettings s;
-    double interval_start;
-    double interval_end;
-    uint32_t frame;
-    uint2 key;
-    PushCounters* counters;
-};
-
-// One substep of the driver loop body.  Returns false once the particle
-// leaves the loop (interval end, step guard or failure).
+// Coefficients, drift, dp/dt, dmu/dt and the step-size limiters of one
+// substep (src/main.cpp:1167-1257 Parker, :1421-1630 focused).  Returns
+// false where the reference sets status 2.
 template <typename T, bool FOCUSED>
-__device__ __forceinline__ bool substep(State<T>& st, const PushParams& P) {
+__device__ __forceinline__ bool physics(const T* c, T p, T pitch_mu, const DeviceSettings& s,
+                                        Rates<T>& r) {
     using N = Num<T>;
-    constexpr int C = FOCUSED ? 21 : 16;
-    constexpr int STRIDE = FOCUSED ? (sizeof(T) == 8 ? 22 : 24) : 16;
-    const DeviceSettings& s = P.s;
-
-    ++st.steps;
-    st.x = wrap_driver(st.x, s.x_lower, s.x_upper, s.x_width);
-    st.y = wrap_driver(st.y, s.y_lower, s.y_upper, s.y_width);
-    const double q0 = __dadd_rn(st.x, s.shift_x);
-    const double q1 = __dadd_rn(st.y, s.shift_y);
-    const double rt = __ddiv_rn(__dsub_rn(st.t, P.interval_start), s.mhd_dt);
-    T c[C];
-    sample_coefficients<T, C, STRIDE>(P.grid, static_cast<const T*>(P.lower),
-                                      static_cast<const T*>(P.upper), q0, q1, rt,
-                                      s.time_interpolation, c);
-
     T vx, vy, bx, by, bz, b, dvx_dx, dvy_dy, dbx_dx, dbx_dy, dby_dx, dby_dy, dbz_dx, dbz_dy,
         db_dx, db_dy;
-    T vz = 0, dvx_dy = 0, dvy_dx = 0, dvz_dx = 0, dvz_dy = 0;
+    T dvx_dy = 0, dvy_dx = 0, dvz_dx = 0, dvz_dy = 0;
     if (FOCUSED) {
-        vx = c[0]; vy = c[1]; vz = c[2]; bx = c[3]; by = c[4]; bz = c[5]; b = c[6];
+        vx = c[0]; vy = c[1]; bx = c[3]; by = c[4]; bz = c[5]; b = c[6];
         dvx_dx = c[7]; dvx_dy = c[8]; dvy_dx = c[9]; dvy_dy = c[10]; dvz_dx = c[11];
         dvz_dy = c[12]; dbx_dx = c[13]; dbx_dy = c[14]; dby_dx = c[15]; dby_dy = c[16];
         dbz_dx = c[17]; dbz_dy = c[18]; db_dx = c[19]; db_dy = c[20];
@@ -214,11 +258,7 @@ __device__ __forceinline__ bool substep(State<T>& st, const PushParams& P) {
         dvy_dy = c[7]; dbx_dx = c[8]; dbx_dy = c[9]; dby_dx = c[10]; dby_dy = c[11];
         dbz_dx = c[12]; dbz_dy = c[13]; db_dx = c[14]; db_dy = c[15];
     }
-    (void)vz;
-
-    const T p = static_cast<T>(st.p);
-    if (!isfinite(st.p) || st.p <= 0.0 || !N::finite(b) || b <= T(0)) {
-        st.status = 2;
+    if (!N::finite(p) || p <= T(0) || !N::finite(b) || b <= T(0)) {
         return false;
     }
     const T p0 = static_cast<T>(s.p0);
@@ -238,7 +278,6 @@ __device__ __forceinline__ bool substep(State<T>& st, const PushParams& P) {
     const T kpara = static_cast<T>(s.kpara0) * knorm;
     const T kperp = kpara * static_cast<T>(s.kperp_over_kpara);
     if (!N::finite(kpara) || kpara <= T(0) || !N::finite(kperp) || kperp < T(0)) {
-        st.status = 2;
         return false;
     }
     const T skpara = N::sqrt(T(2) * kpara);
@@ -249,7 +288,6 @@ __device__ __forceinline__ bool substep(State<T>& st, const PushParams& P) {
     } else {
         skpara_perp = N::sqrt(T(2) * (kpara - kperp));
     }
-    (void)skpara_perp;
     const T kpp = FOCUSED ? -kperp : kpara - kperp;
 
     T dkdx = T(0);
@@ -275,10 +313,8 @@ __device__ __forceinline__ bool substep(State<T>& st, const PushParams& P) {
 
     T dx_dt, dy_dt, dp_dt;
     T dmu_dt = T(0), duu = T(0);
-    T pitch_mu = st.mu;
     if (FOCUSED) {
-        const T mu_max = static_cast<T>(s.mu_max);
-        pitch_mu = clamp_mu(pitch_mu, mu_max);
+        pitch_mu = clamp_mu(pitch_mu, static_cast<T>(s.mu_max));
         const T mu2 = pitch_mu * pitch_mu;
         const T muf1 = T(0.5) * (T(1) - mu2);
         const T muf2 = T(0.5) * (T(3) * mu2 - T(1));
@@ -293,14 +329,11 @@ __device__ __forceinline__ bool substep(State<T>& st, const PushParams& P) {
                              muf1 * by * bdot_curvb * ib3);
         const T speed = N::div(static_cast<T>(s.particle_v0) * p, p0);
         if (!N::finite(speed) || speed <= T(0)) {
-            st.status = 2;
             return false;
         }
         const T v_parallel_over_b = speed * pitch_mu * ib;
-        const T vbx = v_parallel_over_b * bx;
-        const T vby = v_parallel_over_b * by;
-        dx_dt = vx + vdx + vbx + dkxx_dx + dkxy_dy;
-        dy_dt = vy + vdy + vby + dkxy_dx + dkyy_dy;
+        dx_dt = vx + vdx + v_parallel_over_b * bx + dkxx_dx + dkxy_dy;
+        dy_dt = vy + vdy + v_parallel_over_b * by + dkxy_dx + dkyy_dy;
 
         const T divv = dvx_dx + dvy_dy;
         const T bb_gradv = (bx * (bx * dvx_dx + by * dvx_dy) + by * (bx * dvy_dx + by * dvy_dy) +
@@ -337,7 +370,6 @@ __device__ __forceinline__ bool substep(State<T>& st, const PushParams& P) {
         duu_du *= duu_norm;
         dmu_dt += duu_du;
         if (!N::finite(dmu_dt) || !N::finite(duu) || duu < T(0)) {
-            st.status = 2;
             return false;
         }
     } else {
@@ -350,108 +382,156 @@ __device__ __forceinline__ bool substep(State<T>& st, const PushParams& P) {
         dp_dt = N::div(-p * divv, T(3));
     }
 
-    // Step-size control (src/main.cpp:1243-1277, :1596-1657).
+    // Step-size limiters (src/main.cpp:1243-1257, :1596-1650).
     const T dxs = static_cast<T>(s.dx);
     const T dys = static_cast<T>(s.dy);
-    T dtt;
-    bool fixed = false;
+    r.fixed_dt = false;
+    r.dt = T(0);
     if (FOCUSED) {
         const T diffusion_scale = skperp > T(0) ? skperp : skpara;
         if (dx_dt != T(0) && dy_dt != T(0) && dp_dt != T(0) && dmu_dt != T(0) &&
             diffusion_scale > T(0)) {
-            const T diffusion_dt_x = square(N::div(T(0.5) * dxs, diffusion_scale));
-            const T diffusion_dt_y = square(N::div(T(0.5) * dys, diffusion_scale));
-            const T advection_dt_x = square(N::div(diffusion_scale, dx_dt));
-            const T advection_dt_y = square(N::div(diffusion_scale, dy_dt));
-            const T momentum_dt = N::div(T(0.1) * p, N::abs(dp_dt));
-            const T pitch_advection_dt = N::div(T(0.1), N::abs(dmu_dt));
-            const T pitch_balance_dt = N::div(T(2) * duu, square(dmu_dt));
-            dtt = min_positive(diffusion_dt_x, diffusion_dt_y);
-            dtt = min_positive(dtt, advection_dt_x);
-            dtt = min_positive(dtt, advection_dt_y);
-            dtt = min_positive(dtt, momentum_dt);
-            dtt = min_positive(dtt, pitch_advection_dt);
-            dtt = min_positive(dtt, pitch_balance_dt);
+            T dt = min_positive(square(N::div(T(0.5) * dxs, diffusion_scale)),
+                                square(N::div(T(0.5) * dys, diffusion_scale)));
+            dt = min_positive(dt, square(N::div(diffusion_scale, dx_dt)));
+            dt = min_positive(dt, square(N::div(diffusion_scale, dy_dt)));
+            dt = min_positive(dt, N::div(T(0.1) * p, N::abs(dp_dt)));
+            dt = min_positive(dt, N::div(T(0.1), N::abs(dmu_dt)));
+            dt = min_positive(dt, N::div(T(2) * duu, square(dmu_dt)));
+            r.dt = dt;
         } else {
-            fixed = true;
+            r.fixed_dt = true;
         }
     } else if (dx_dt != T(0) && dy_dt != T(0) && dp_dt != T(0)) {
-        const T diffusion_dt_x = square(N::div(T(0.5) * dxs, skpara));
-        const T diffusion_dt_y = square(N::div(T(0.5) * dys, skpara));
         const T advection_scale = skperp > T(0) ? skperp : skpara;
-        const T advection_dt_x = square(N::div(advection_scale, dx_dt));
-        const T advection_dt_y = square(N::div(advection_scale, dy_dt));
-        const T momentum_dt = N::div(T(0.1) * p, N::abs(dp_dt));
-        dtt = min_positive(diffusion_dt_x, diffusion_dt_y);
-        dtt = min_positive(dtt, advection_dt_x);
-        dtt = min_positive(dtt, advection_dt_y);
-        dtt = min_positive(dtt, momentum_dt);
+        T dt = min_positive(square(N::div(T(0.5) * dxs, skpara)),
+                            square(N::div(T(0.5) * dys, skpara)));
+        dt = min_positive(dt, square(N::div(advection_scale, dx_dt)));
+        dt = min_positive(dt, square(N::div(advection_scale, dy_dt)));
+        dt = min_positive(dt, N::div(T(0.1) * p, N::abs(dp_dt)));
+        r.dt = dt;
     } else {
-        fixed = true;
+        r.fixed_dt = true;
     }
-    double dt = fixed ? s.dt_min : static_cast<double>(dtt);
-    if (dt < s.dt_min) {
-        dt = s.dt_min;
-    }
-    if (dt > s.dt_max) {
-        dt = s.dt_max;
-    }
-    st.diag_dt = dt;
-    const double remaining = __dsub_rn(P.interval_end, st.t);
-    if (dt > remaining) {
-        dt = remaining;
-    }
-    if (!isfinite(dt) || dt <= 0.0) {
-        st.status = 2;
-        return false;
-    }
+    r.dx_dt = dx_dt;
+    r.dy_dt = dy_dt;
+    r.dp_dt = dp_dt;
+    r.dmu_dt = dmu_dt;
+    r.duu = duu;
+    r.skperp = skperp;
+    r.skpara_perp = skpara_perp;
+    r.ib = ib;
+    r.bx = bx;
+    r.by = by;
+    r.bz = bz;
+    r.pitch_mu = pitch_mu;
+    return true;
+}
 
-    // Noise: four uniform_sqrt3 draws per substep, blocks 2(s-1), 2(s-1)+1.
-    const uint32_t block = 2u * static_cast<uint32_t>(st.steps - 1);
-    const uint4 r0 = philox4x32_10(make_uint4(block, st.index, P.frame, kTagPush), P.key);
-    const uint4 r1 = philox4x32_10(make_uint4(block + 1u, st.index, P.frame, kTagPush), P.key);
-    const T dtT = static_cast<T>(dt);
-    const T sdt = N::sqrt(dtT);
-    double delta_x, delta_y;
+// Displacements and the new pitch cosine from the four draws of a substep
+// (src/main.cpp:1280-1291 Parker, :1660-1702 focused).
+template <typename T, bool FOCUSED>
+__device__ __forceinline__ void increments(const Rates<T>& r, T dt, const uint4& r0,
+                                           const uint4& r1, const DeviceSettings& s, T& delta_x,
+                                           T& delta_y, T& new_mu) {
+    using N = Num<T>;
+    const T sdt = N::sqrt(dt);
     if (FOCUSED) {
         const T ran1 = N::noise(r0.x, r0.y);
         const T ran2 = N::noise(r0.z, r0.w);
         const T pitch_random = N::noise(r1.z, r1.w);
-        const T bxn = bx * ib;
-        const T byn = by * ib;
-        const T bzn = bz * ib;
+        const T bxn = r.bx * r.ib;
+        const T byn = r.by * r.ib;
+        const T bzn = r.bz * r.ib;
         const T bxy_norm = N::sqrt(bxn * bxn + byn * byn);
         T stochastic_x = T(0);
         T stochastic_y = T(0);
         if (bxy_norm > T(0)) {
             const T ibxy_norm = N::div(T(1), bxy_norm);
             // (-by, +bx) on ran2 as written in src/main.cpp:1682-1687.
-            stochastic_x = skperp * ibxy_norm * sdt * (-bxn * bzn * ran1 - by * ran2);
-            stochastic_y = skperp * ibxy_norm * sdt * (-byn * bzn * ran1 + bx * ran2);
+            stochastic_x = r.skperp * ibxy_norm * sdt * (-bxn * bzn * ran1 - r.by * ran2);
+            stochastic_y = r.skperp * ibxy_norm * sdt * (-byn * bzn * ran1 + r.bx * ran2);
         }
-        delta_x = static_cast<double>(dx_dt * dtT + stochastic_x);
-        delta_y = static_cast<double>(dy_dt * dtT + stochastic_y);
-        st.mu = clamp_mu(pitch_mu + dmu_dt * dtT + pitch_random * N::sqrt(T(2) * duu) * sdt,
-                         static_cast<T>(s.mu_max));
+        delta_x = r.dx_dt * dt + stochastic_x;
+        delta_y = r.dy_dt * dt + stochastic_y;
+        new_mu = clamp_mu(r.pitch_mu + r.dmu_dt * dt + pitch_random * N::sqrt(T(2) * r.duu) * sdt,
+                          static_cast<T>(s.mu_max));
     } else {
         const T ran1 = N::noise(r0.x, r0.y);
         const T ran2 = N::noise(r0.z, r0.w);
         const T ran3 = N::noise(r1.x, r1.y);
-        delta_x = static_cast<double>(dx_dt * dtT + ran1 * skperp * sdt +
-                                      ran3 * skpara_perp * sdt * bx * ib);
-        delta_y = static_cast<double>(dy_dt * dtT + ran2 * skperp * sdt +
-                                      ran3 * skpara_perp * sdt * by * ib);
+        delta_x = r.dx_dt * dt + ran1 * r.skperp * sdt + ran3 * r.skpara_perp * sdt * r.bx * r.ib;
+        delta_y = r.dy_dt * dt + ran2 * r.skperp * sdt + ran3 * r.skpara_perp * sdt * r.by * r.ib;
+        new_mu = r.pitch_mu;
     }
-    const double delta_p = static_cast<double>(dp_dt * dtT);
+}
 
-    st.x = __dadd_rn(st.x, delta_x);
-    st.y = __dadd_rn(st.y, delta_y);
-    st.p = __dadd_rn(st.p, delta_p);
+struct PushParams {
+    Grid grid;
+    FixedGrid fixed;
+    const void* lower;
+    const void* upper;
+    ParticleArrays parts;
+    const uint32_t* order;  // optional work order (permutation of [0, count))
+    uint64_t count;
+    DeviceSettings s;
+    double interval_start;
+    double interval_end;
+    float inv_mhd_dt;
+    uint32_t frame;
+    uint2 key;
+    PushCounters* counters;
+};
+
+// ------------------------------------------------------------- FP64 path
+struct StateF64 {
+    double x, y, p, t, diag_dt, mu;
+    int steps;
+    int status;
+    uint32_t index;
+};
+
+template <bool FOCUSED>
+__device__ __forceinline__ bool substep(StateF64& st, const PushParams& P) {
+    constexpr int C = FOCUSED ? 21 : 16;
+    constexpr int STRIDE = FOCUSED ? 22 : 16;
+    const DeviceSettings& s = P.s;
+    ++st.steps;
+    st.x = wrap_driver(st.x, s.x_lower, s.x_upper, s.x_width);
+    st.y = wrap_driver(st.y, s.y_lower, s.y_upper, s.y_width);
+    const double rt = __ddiv_rn(__dsub_rn(st.t, P.interval_start), s.mhd_dt);
+    double c[C];
+    sample_coefficients<double, C, STRIDE>(P.grid, static_cast<const double*>(P.lower),
+                                           static_cast<const double*>(P.upper),
+                                           __dadd_rn(st.x, s.shift_x), __dadd_rn(st.y, s.shift_y),
+                                           rt, s.time_interpolation, c);
+    Rates<double> r;
+    if (!physics<double, FOCUSED>(c, st.p, st.mu, s, r)) {
+        st.status = 2;
+        return false;
+    }
+    double dt = r.fixed_dt ? s.dt_min : r.dt;
+    if (dt < s.dt_min) dt = s.dt_min;
+    if (dt > s.dt_max) dt = s.dt_max;
+    st.diag_dt = dt;
+    const double remaining = __dsub_rn(P.interval_end, st.t);
+    if (dt > remaining) dt = remaining;
+    if (!isfinite(dt) || dt <= 0.0) {
+        st.status = 2;
+        return false;
+    }
+    const uint32_t block = 2u * static_cast<uint32_t>(st.steps - 1);
+    const uint4 r0 = philox4x32_10(make_uint4(block, st.index, P.frame, kTagPush), P.key);
+    const uint4 r1 = philox4x32_10(make_uint4(block + 1u, st.index, P.frame, kTagPush), P.key);
+    double dx, dy, mu;
+    increments<double, FOCUSED>(r, dt, r0, r1, s, dx, dy, mu);
+    st.mu = mu;
+    st.x = __dadd_rn(st.x, dx);
+    st.y = __dadd_rn(st.y, dy);
+    st.p = __dadd_rn(st.p, r.dp_dt * dt);
     st.t = __dadd_rn(st.t, dt);
     const double pfloor = 0.25 * s.p0;
-    if (st.p < pfloor) {
-        st.p = pfloor;
-    }
+    if (st.p < pfloor) st.p = pfloor;
     if (!isfinite(st.x) || !isfinite(st.y) || !isfinite(st.p) || !isfinite(st.t)) {
         st.status = 2;
         return false;
@@ -459,40 +539,224 @@ __device__ __forceinline__ bool substep(State<T>& st, const PushParams& P) {
     return st.t < P.interval_end && st.steps < s.max_steps;
 }
 
-template <typename T, bool FOCUSED>
-__device__ __forceinline__ void load_state(State<T>& st, const PushParams& P, uint32_t index) {
+template <bool FOCUSED>
+__device__ __forceinline__ void load(StateF64& st, const PushParams& P, uint32_t index) {
     const ParticleArrays& a = P.parts;
     st.index = index;
     st.x = a.x[index];
     st.y = a.y[index];
     st.p = a.p[index];
     st.t = a.t[index];
-    st.dt = a.step_dt[index];
-    st.diag_dt = st.dt;
-    st.mu = FOCUSED ? clamp_mu(static_cast<T>(a.mu[index]), static_cast<T>(P.s.mu_max)) : T(0);
+    st.diag_dt = a.step_dt[index];
+    st.mu = FOCUSED ? clamp_mu(a.mu[index], P.s.mu_max) : 0.0;
     st.steps = 0;
     st.status = 0;
 }
 
-template <typename T, bool FOCUSED>
-__device__ __forceinline__ void store_state(State<T>& st, const PushParams& P) {
+template <bool FOCUSED>
+__device__ __forceinline__ void store(StateF64& st, const PushParams& P) {
     const ParticleArrays& a = P.parts;
     const DeviceSettings& s = P.s;
-    if (st.steps >= s.max_steps && st.t < P.interval_end) {
-        st.status = 2;
-    }
+    if (st.steps >= s.max_steps && st.t < P.interval_end) st.status = 2;
     const uint32_t i = st.index;
     a.x[i] = wrap_driver(st.x, s.x_lower, s.x_upper, s.x_width);
     a.y[i] = wrap_driver(st.y, s.y_lower, s.y_upper, s.y_width);
     a.p[i] = st.p;
     a.t[i] = st.t;
     a.step_dt[i] = st.diag_dt;
-    if (FOCUSED) {
-        a.mu[i] = static_cast<double>(st.mu);
-    }
+    if (FOCUSED) a.mu[i] = st.mu;
     a.status[i] = st.status;
 }
 
+__device__ __forceinline__ bool live(const StateF64& st, const PushParams& P) {
+    return st.t < P.interval_end && st.steps < P.s.max_steps;
+}
+
+// ------------------------------------------------------------ mixed path
+struct StateMixed {
+    uint64_t px, py;  // fixed-point phase over each periodic width
+    double p, t;
+    float mu, diag_dt;
+    int steps;
+    int status;
+    uint32_t index;
+};
+
+// Exact float -> int64 (truncation) with integer operations only.
+__device__ __forceinline__ long long float_to_s64(float f) {
+    const int bits = __float_as_int(f);
+    const int e = ((bits >> 23) & 0xff) - 150;
+    const long long m = static_cast<long long>((bits & 0x7fffff) | 0x800000);
+    long long v;
+    if (e >= 0) {
+        v = e < 40 ? (m << e) : 0x7fffffffffffffffll;
+    } else {
+        v = e > -24 ? (m >> (-e)) : 0;
+    }
+    return bits < 0 ? -v : v;
+}
+
+// Cell index and upper weight of the driver's stencil for a fixed-point
+// position q (already shifted by half a mean cell), uniform axis:
+// logical = q*n/2^64 - 1/2 from one 64x64->128-bit product.
+__device__ __forceinline__ void fixed_stencil_uniform(uint64_t q, int n, int& lo, float& w) {
+    const uint64_t hi = __umul64hi(q, static_cast<uint64_t>(n));
+    const uint64_t frac = q * static_cast<uint64_t>(n);
+    const uint64_t shifted = frac - (1ull << 63);
+    const int borrow = frac < (1ull << 63) ? 1 : 0;
+    lo = static_cast<int>(hi) - borrow;
+    w = static_cast<float>(static_cast<uint32_t>(shifted >> 40)) * (1.0f / 16777216.0f);
+}
+
+// Stretched axis: find k with C[k] <= q < C[k+1] among the fixed-point
+// ghosted cell centres (exact integer compares), seeded by a bucket table.
+__device__ __forceinline__ void fixed_stencil_stored(const FixedAxis& a, uint64_t q, int& lo,
+                                                     float& w) {
+    const long long qy = static_cast<long long>(q >> 2);  // 2^62 scale
+    int k = __ldg(a.buckets + static_cast<int>(q >> a.bucket_shift));
+    while (k < a.n && __ldg(a.centers + k + 3) <= qy) {
+        ++k;
+    }
+    while (k > -2 && __ldg(a.centers + k + 2) > qy) {
+        --k;
+    }
+    lo = k;
+    const unsigned long long d = static_cast<unsigned long long>(qy - __ldg(a.centers + k + 2));
+    w = static_cast<float>(static_cast<uint32_t>(d >> a.spacing_shift)) *
+        __ldg(a.inv_spacing + k + 2);
+}
+
+template <bool FOCUSED>
+__device__ __forceinline__ bool substep(StateMixed& st, const PushParams& P) {
+    constexpr int C = FOCUSED ? 21 : 16;
+    constexpr int STRIDE = FOCUSED ? 24 : 16;
+    const DeviceSettings& s = P.s;
+    const FixedGrid& F = P.fixed;
+    ++st.steps;
+    const uint64_t qx = st.px + F.axis[0].half_cell;
+    const uint64_t qy = st.py + F.axis[1].half_cell;
+    int lo0, lo1;
+    float w0, w1;
+    if (F.axis[0].stored) {
+        fixed_stencil_stored(F.axis[0], qx, lo0, w0);
+    } else {
+        fixed_stencil_uniform(qx, F.axis[0].n, lo0, w0);
+    }
+    if (F.axis[1].stored) {
+        fixed_stencil_stored(F.axis[1], qy, lo1, w1);
+    } else {
+        fixed_stencil_uniform(qy, F.axis[1].n, lo1, w1);
+    }
+    const float a0 = 1.0f - w0;
+    const float a1 = 1.0f - w1;
+    const float wc[4] = {a0 * a1, w0 * a1, a0 * w1, w0 * w1};
+    size_t pt[4];
+    corner_points(lo0, lo0 + 1, lo1, lo1 + 1, P.grid.ex, pt);
+    float rt = static_cast<float>(st.t - P.interval_start) * P.inv_mhd_dt;
+    rt = rt < 0.0f ? 0.0f : (rt > 1.0f ? 1.0f : rt);
+    float c[C];
+    sample_stencil<float, C, STRIDE>(static_cast<const float*>(P.lower),
+                                     static_cast<const float*>(P.upper), pt, wc, rt,
+                                     s.time_interpolation, c);
+    const float pf = static_cast<float>(st.p);
+    Rates<float> r;
+    if (!physics<float, FOCUSED>(c, pf, st.mu, s, r)) {
+        st.status = 2;
+        return false;
+    }
+    float dtf = r.fixed_dt ? F.dt_min : r.dt;
+    if (dtf < F.dt_min) dtf = F.dt_min;
+    if (dtf > F.dt_max) dtf = F.dt_max;
+    st.diag_dt = dtf;
+    double dt = static_cast<double>(dtf);
+    const double remaining = P.interval_end - st.t;
+    if (dt > remaining) {
+        dt = remaining;
+        dtf = static_cast<float>(remaining);
+    }
+    if (!(dtf > 0.0f) || !isfinite(dtf)) {
+        st.status = 2;
+        return false;
+    }
+    const uint32_t block = 2u * static_cast<uint32_t>(st.steps - 1);
+    const uint4 r0 = philox4x32_10(make_uint4(block, st.index, P.frame, kTagPush), P.key);
+    const uint4 r1 = philox4x32_10(make_uint4(block + 1u, st.index, P.frame, kTagPush), P.key);
+    float dx, dy, mu;
+    increments<float, FOCUSED>(r, dtf, r0, r1, s, dx, dy, mu);
+    const float dp = r.dp_dt * dtf;
+    if (!isfinite(dx) || !isfinite(dy) || !isfinite(dp)) {
+        st.status = 2;
+        return false;
+    }
+    st.mu = mu;
+    st.px += static_cast<uint64_t>(float_to_s64(dx * F.axis[0].to_fixed));
+    st.py += static_cast<uint64_t>(float_to_s64(dy * F.axis[1].to_fixed));
+    st.p += static_cast<double>(dp);
+    st.t += dt;
+    if (st.p < F.pfloor) st.p = F.pfloor;
+    return st.t < P.interval_end && st.steps < s.max_steps;
+}
+
+// Position <-> fixed-point phase (once per particle and push).
+__device__ __forceinline__ uint64_t to_phase(double x, double lower, double inv_width) {
+    double f = (x - lower) * inv_width;
+    f = f - floor(f);
+    const double scaled = f * 18446744073709551616.0;
+    return scaled >= 18446744073709551615.0 ? 0ull : __double2ull_rn(scaled);
+}
+
+__device__ __forceinline__ double from_phase(uint64_t phase, double lower, double width) {
+    return lower + static_cast<double>(phase) * (width * (1.0 / 18446744073709551616.0));
+}
+
+template <bool FOCUSED>
+__device__ __forceinline__ void load(StateMixed& st, const PushParams& P, uint32_t index) {
+    const ParticleArrays& a = P.parts;
+    const DeviceSettings& s = P.s;
+    st.index = index;
+    const double x = wrap_driver(a.x[index], s.x_lower, s.x_upper, s.x_width);
+    const double y = wrap_driver(a.y[index], s.y_lower, s.y_upper, s.y_width);
+    st.px = to_phase(x, s.x_lower, P.grid.axis[0].inv_width);
+    st.py = to_phase(y, s.y_lower, P.grid.axis[1].inv_width);
+    st.p = a.p[index];
+    st.t = a.t[index];
+    st.diag_dt = static_cast<float>(a.step_dt[index]);
+    st.mu = FOCUSED ? clamp_mu(static_cast<float>(a.mu[index]), static_cast<float>(s.mu_max))
+                    : 0.0f;
+    st.steps = 0;
+    st.status = 0;
+    if (!isfinite(a.x[index]) || !isfinite(a.y[index])) {
+        st.status = 2;
+    }
+}
+
+template <bool FOCUSED>
+__device__ __forceinline__ void store(StateMixed& st, const PushParams& P) {
+    const ParticleArrays& a = P.parts;
+    const DeviceSettings& s = P.s;
+    if (st.steps >= s.max_steps && st.t < P.interval_end) st.status = 2;
+    const uint32_t i = st.index;
+    if (st.steps > 0) {
+        a.x[i] = wrap_driver(from_phase(st.px, s.x_lower, s.x_width), s.x_lower, s.x_upper,
+                             s.x_width);
+        a.y[i] = wrap_driver(from_phase(st.py, s.y_lower, s.y_width), s.y_lower, s.y_upper,
+                             s.y_width);
+        a.step_dt[i] = static_cast<double>(st.diag_dt);
+    } else {
+        a.x[i] = wrap_driver(a.x[i], s.x_lower, s.x_upper, s.x_width);
+        a.y[i] = wrap_driver(a.y[i], s.y_lower, s.y_upper, s.y_width);
+    }
+    a.p[i] = st.p;
+    a.t[i] = st.t;
+    if (FOCUSED) a.mu[i] = static_cast<double>(st.mu);
+    a.status[i] = st.status;
+}
+
+__device__ __forceinline__ bool live(const StateMixed& st, const PushParams& P) {
+    return st.status == 0 && st.t < P.interval_end && st.steps < P.s.max_steps;
+}
+
+// ---------------------------------------------------------------- drivers
 __device__ __forceinline__ void flush_counters(PushCounters* counters, unsigned long long steps,
                                                unsigned long long pushed,
                                                unsigned long long failed, unsigned int max_steps) {
@@ -512,18 +776,35 @@ __device__ __forceinline__ void flush_counters(PushCounters* counters, unsigned 
     }
 }
 
-// Persistent warps with lane refill.  Each warp claims particles from the
-// cursor in batches of (number of idle lanes); a lane advances its particle
-// by one substep per loop trip and refills when the particle is done.  The
-// loop ends when the cursor is past `count` and no lane holds a particle;
-// every trip either advances a particle or moves the cursor, so it always
-// terminates.
-template <typename T, bool FOCUSED>
-__global__ void __launch_bounds__(128) push_refill_kernel(const PushParams P) {
+// Persistent warps with lane refill.  A warp claims particles from the
+// cursor in batches of (idle lanes); each trip advances every busy lane by
+// one substep.  Every trip either advances a particle (bounded by the step
+// guard) or moves the cursor, so the loop always terminates.
+// Resident blocks of 128 threads per SM the register budget targets: the
+// mixed kernels are latency-bound gathers and want more warps in flight.
+#ifndef KPT_MIXED_MIN_BLOCKS
+#define KPT_MIXED_MIN_BLOCKS 5
+#endif
+template <typename State, bool FOCUSED>
+struct MinBlocks {
+    static constexpr int value = FOCUSED ? 2 : 4;
+};
+template <>
+struct MinBlocks<StateMixed, false> {
+    static constexpr int value = KPT_MIXED_MIN_BLOCKS;
+};
+template <>
+struct MinBlocks<StateMixed, true> {
+    static constexpr int value = 4;
+};
+
+template <typename State, bool FOCUSED>
+__global__ void __launch_bounds__(128, MinBlocks<State, FOCUSED>::value)
+    push_refill_kernel(const PushParams P) {
     const unsigned full = 0xffffffffu;
     const unsigned lane = threadIdx.x & 31u;
     const unsigned lanes_below = (1u << lane) - 1u;
-    State<T> st;
+    State st;
     bool have = false;
     bool exhausted = false;
     unsigned long long my_steps = 0, my_pushed = 0, my_failed = 0;
@@ -532,8 +813,8 @@ __global__ void __launch_bounds__(128) push_refill_kernel(const PushParams P) {
         const unsigned idle = __ballot_sync(full, !have);
         if (idle != 0u && !exhausted) {
             const unsigned n_idle = __popc(idle);
-            unsigned base = 0;
             const int leader = __ffs(idle) - 1;
+            unsigned base = 0;
             if (static_cast<int>(lane) == leader) {
                 base = atomicAdd(&P.counters->next_particle, n_idle);
             }
@@ -542,14 +823,19 @@ __global__ void __launch_bounds__(128) push_refill_kernel(const PushParams P) {
                 exhausted = true;
             }
             if (!have) {
-                const uint64_t idx = static_cast<uint64_t>(base) + __popc(idle & lanes_below);
-                if (idx < P.count && P.parts.status[idx] == 0) {
-                    load_state<T, FOCUSED>(st, P, static_cast<uint32_t>(idx));
-                    ++my_pushed;
-                    have = true;
-                    if (!(st.t < P.interval_end && st.steps < P.s.max_steps)) {
-                        store_state<T, FOCUSED>(st, P);
-                        have = false;
+                const uint64_t slot = static_cast<uint64_t>(base) + __popc(idle & lanes_below);
+                if (slot < P.count) {
+                    const uint32_t idx = P.order != nullptr ? __ldg(P.order + slot)
+                                                            : static_cast<uint32_t>(slot);
+                    if (P.parts.status[idx] == 0) {
+                        load<FOCUSED>(st, P, idx);
+                        ++my_pushed;
+                        have = true;
+                        if (!live(st, P)) {
+                            store<FOCUSED>(st, P);
+                            my_failed += st.status != 0 ? 1 : 0;
+                            have = false;
+                        }
                     }
                 }
             }
@@ -560,76 +846,84 @@ __global__ void __launch_bounds__(128) push_refill_kernel(const PushParams P) {
             }
             continue;
         }
-        if (have) {
-            if (!substep<T, FOCUSED>(st, P)) {
-                store_state<T, FOCUSED>(st, P);
-                my_steps += static_cast<unsigned long long>(st.steps);
-                my_max = max(my_max, static_cast<unsigned int>(st.steps));
-                if (st.status != 0) {
-                    ++my_failed;
-                }
-                have = false;
-            }
+        if (have && !substep<FOCUSED>(st, P)) {
+            store<FOCUSED>(st, P);
+            my_steps += static_cast<unsigned long long>(st.steps);
+            my_max = max(my_max, static_cast<unsigned int>(st.steps));
+            my_failed += st.status != 0 ? 1 : 0;
+            have = false;
         }
     }
     flush_counters(P.counters, my_steps, my_pushed, my_failed, my_max);
 }
 
-// One particle per thread, no refill (kept for the schedule tuner).
-template <typename T, bool FOCUSED>
+// One particle per thread, no refill (schedule alternative for the tuner).
+template <typename State, bool FOCUSED>
 __global__ void __launch_bounds__(128) push_simple_kernel(const PushParams P) {
     unsigned long long my_steps = 0, my_pushed = 0, my_failed = 0;
     unsigned int my_max = 0;
-    for (uint64_t idx = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
-         idx < P.count; idx += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+    for (uint64_t slot = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
+         slot < P.count; slot += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        const uint32_t idx =
+            P.order != nullptr ? __ldg(P.order + slot) : static_cast<uint32_t>(slot);
         if (P.parts.status[idx] != 0) {
             continue;
         }
-        State<T> st;
-        load_state<T, FOCUSED>(st, P, static_cast<uint32_t>(idx));
+        State st;
+        load<FOCUSED>(st, P, idx);
         ++my_pushed;
-        if (st.t < P.interval_end && st.steps < P.s.max_steps) {
-            while (substep<T, FOCUSED>(st, P)) {
+        if (live(st, P)) {
+            while (substep<FOCUSED>(st, P)) {
             }
         }
-        store_state<T, FOCUSED>(st, P);
+        store<FOCUSED>(st, P);
         my_steps += static_cast<unsigned long long>(st.steps);
         my_max = max(my_max, static_cast<unsigned int>(st.steps));
-        if (st.status != 0) {
-            ++my_failed;
-        }
+        my_failed += st.status != 0 ? 1 : 0;
     }
     flush_counters(P.counters, my_steps, my_pushed, my_failed, my_max);
 }
 
-template <typename T, bool FOCUSED>
+template <typename State, bool FOCUSED>
 cudaError_t launch_push(const PushLaunch& L, cudaStream_t stream) {
     PushParams P;
     P.grid = L.grid;
+    P.fixed = L.fixed;
     P.lower = L.lower;
     P.upper = L.upper;
     P.parts = L.parts;
+    P.order = L.order;
     P.count = L.count;
     P.s = L.settings;
     P.interval_start = L.interval_start;
     P.interval_end = L.interval_end;
+    P.inv_mhd_dt = static_cast<float>(1.0 / L.settings.mhd_dt);
     P.frame = L.frame;
     P.key = make_uint2(static_cast<uint32_t>(L.seed), static_cast<uint32_t>(L.seed >> 32));
     P.counters = L.counters;
     const int threads = 128;
     if (L.schedule == kScheduleSimple) {
         const uint64_t want = (L.count + threads - 1) / threads;
-        const int blocks = static_cast<int>(want < 1 ? 1 : (want > 65535u * 8u ? 65535u * 8u : want));
-        push_simple_kernel<T, FOCUSED><<<blocks, threads, 0, stream>>>(P);
+        const int blocks =
+            static_cast<int>(want < 1 ? 1 : (want > 65535u * 8u ? 65535u * 8u : want));
+        push_simple_kernel<State, FOCUSED><<<blocks, threads, 0, stream>>>(P);
     } else {
-        const int blocks = L.sm_count * L.blocks_per_sm;
-        push_refill_kernel<T, FOCUSED><<<blocks, threads, 0, stream>>>(P);
+        // Persistent grid: as many resident blocks per SM as the kernel's
+        // registers allow (or fewer on request).
+        int resident = 0;
+        cudaError_t err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &resident, push_refill_kernel<State, FOCUSED>, threads, 0);
+        if (err != cudaSuccess) return err;
+        resident = resident < 1 ? 1 : resident;
+        const int per_sm = L.blocks_per_sm > 0 && L.blocks_per_sm < resident ? L.blocks_per_sm
+                                                                            : resident;
+        push_refill_kernel<State, FOCUSED><<<L.sm_count * per_sm, threads, 0, stream>>>(P);
     }
     return cudaGetLastError();
 }
 
-// Table values at given positions, through the push's own sampling path
-// (driver wrap, half-cell shift, grid wrap, stencil, time interpolation).
+// Table values at given positions through the FP64 sampling path (driver
+// wrap, half-cell shift, grid wrap, stencil, time interpolation).
 template <typename T, bool FOCUSED>
 __global__ void sample_kernel(const SampleLaunch L) {
     constexpr int C = FOCUSED ? 21 : 16;
@@ -679,11 +973,11 @@ cudaError_t launch_sample(const SampleLaunch& L, cudaStream_t stream) {
 
 cudaError_t launch_push_interval(const PushLaunch& launch, cudaStream_t stream) {
     if (launch.precision == kPrecisionF64) {
-        return launch.focused ? launch_push<double, true>(launch, stream)
-                              : launch_push<double, false>(launch, stream);
+        return launch.focused ? launch_push<StateF64, true>(launch, stream)
+                              : launch_push<StateF64, false>(launch, stream);
     }
-    return launch.focused ? launch_push<float, true>(launch, stream)
-                          : launch_push<float, false>(launch, stream);
+    return launch.focused ? launch_push<StateMixed, true>(launch, stream)
+                          : launch_push<StateMixed, false>(launch, stream);
 }
 
 }  // namespace kpt

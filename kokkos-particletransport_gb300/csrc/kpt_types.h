@@ -29,6 +29,28 @@ struct Grid {
     int ex;  // nx + 4: point stride of one ghosted row
 };
 
+// The same axis as seen by the mixed-precision push, whose positions are
+// 64-bit fixed-point phases over the periodic width: x = lower + width *
+// phase / 2^64.
+struct FixedAxis {
+    int n;
+    int stored;
+    uint64_t half_cell;            // phase of half a mean cell, 2^63 / n
+    float to_fixed;                // 2^64 / width
+    const long long* centers;      // stored: n+4 ghosted centres, (c - lower) / width * 2^62
+    const float* inv_spacing;      // stored: n+3 entries, 2^spacing_shift / (C[k+1] - C[k])
+    const int* buckets;            // stored: first interval index per phase bucket
+    int bucket_shift;              // phase >> bucket_shift = bucket
+    int spacing_shift;
+};
+
+struct FixedGrid {
+    FixedAxis axis[2];
+    float dt_min;
+    float dt_max;
+    double pfloor;
+};
+
 // Device copy of the driver's settings after make_device_settings
 // (reference src/main.cpp:596-636).
 struct DeviceSettings {

@@ -1,0 +1,158 @@
+"""Statistical and known-answer checks of the GPU push.
+
+* Mixed precision against the FP64 oracle on populations large enough for
+  momentum spectra: 64-bin L1 difference <= 1 % and a chi-square test of the
+  two weighted histograms with p > 0.01.
+* Zero-diffusion advection in a uniform flow, the adiabatic-compression limit
+  and deterministic replay (same seed -> bitwise identical state, whatever
+  the launch schedule or work order).
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+from scipy import stats as sps
+
+pytestmark = pytest.mark.gpu
+
+
+def _spectrum(p, w, status, nbins=64, pmin=1e-2, pmax=1e1):
+    active = (status == 0) & (p >= pmin) & (p <= pmax)
+    bins = np.floor((np.log(p[active]) - np.log(pmin)) * nbins / np.log(pmax / pmin))
+    bins = np.clip(bins.astype(int), 0, nbins - 1)
+    return np.bincount(bins, weights=w[active], minlength=nbins)
+
+
+def _chi2_same(h1, h2):
+    mask = (h1 + h2) > 0
+    a, b = h1[mask], h2[mask]
+    if mask.sum() < 2:
+        return 1.0
+    chi2 = np.sum((a - b) ** 2 / (a + b))
+    return float(sps.chi2.sf(chi2, mask.sum() - 1))
+
+
+def _population(ctx, kpt, oracle, binding, fields_mod, focused, n, frame, seed, intervals):
+    ye = fields_mod.stretched_edges(128, -2.0, 2.0)
+    f0 = fields_mod.harris_field(64, 128, y_edges=ye, island_amplitude=0.1, noise=0.01, seed=5)
+    f1 = fields_mod.harris_field(64, 128, y_edges=ye, island_amplitude=0.1, noise=0.01, seed=6)
+    params = binding.default_params(kperp_over_kpara=0.05, focused=int(focused))
+    grid = oracle.grid(f0.x_edges, f0.y_edges)
+    start = binding.empty_particles(n)
+    count = oracle.inject(grid, params, frame * 0.1, frame, seed, n, 0, n, start)
+    ref = {k: v.copy() for k, v in start.items()}
+    lo, up = oracle.table(f0, focused), oracle.table(f1, focused)
+    for k in range(intervals):
+        oracle.push(grid, lo, up, params, (frame + k) * 0.1, frame + k, seed, count, ref)
+    oracle.free_grid(grid)
+    settings = kpt.settings_from_dict(params)
+    kind = kpt.TABLE_FOCUSED21 if focused else kpt.TABLE_PARKER16
+    out = {}
+    for name, precision in (("f64", kpt.PRECISION_F64), ("mixed", kpt.PRECISION_MIXED)):
+        lower = ctx.field(f0, kind, precision)
+        upper = ctx.field(f1, kind, precision)
+        parts = ctx.particles(n)
+        parts.upload(start, count)
+        for k in range(intervals):
+            ctx.push_interval(parts, lower, upper, settings, frame + k, seed)
+        out[name] = parts.download()
+    return ref, out
+
+
+@pytest.mark.parametrize("focused,n,intervals", [(False, 40000, 3), (True, 6000, 1)])
+def test_mixed_spectrum_matches_oracle(ctx, kpt, oracle, binding, fields_mod, focused, n,
+                                       intervals):
+    ref, out = _population(ctx, kpt, oracle, binding, fields_mod, focused, n, 7, 99, intervals)
+    h_ref = _spectrum(ref["p"], ref["w"], ref["status"])
+    for name in ("f64", "mixed"):
+        got = out[name]
+        h = _spectrum(got["p"], got["w"], got["status"])
+        l1 = np.abs(h - h_ref).sum() / h_ref.sum()
+        assert l1 <= 0.01, (name, l1)
+        assert _chi2_same(h, h_ref) > 0.01, name
+        if focused:
+            # pitch-cosine distribution (16 bins over [-1, 1])
+            mu_ref = np.histogram(ref["mu"][ref["status"] == 0], bins=16, range=(-1, 1))[0]
+            mu_got = np.histogram(got["mu"][got["status"] == 0], bins=16, range=(-1, 1))[0]
+            assert _chi2_same(mu_got.astype(float), mu_ref.astype(float)) > 0.01, name
+
+
+def test_zero_diffusion_uniform_advection(ctx, kpt, fields_mod, binding):
+    """kappa -> 0 in a uniform flow and field: x(t) = x0 + V (t_end - t0)."""
+    f = fields_mod.harris_field(32, 32, x_range=(0.0, 1.0), y_range=(0.0, 1.0))
+    f.b[0], f.b[1], f.b[2] = 1.0, 0.0, 0.5
+    f.v[0], f.v[1], f.v[2] = 0.3, -0.2, 0.0
+    # kperp = 0 leaves only the (kpara - kperp) noise term: ~1e-17 per step
+    params = binding.default_params(kpara0=1e-30, kperp_over_kpara=0.0, dt_min_rel=1e-2,
+                                    dt_max_rel=1e-2)
+    settings = kpt.settings_from_dict(params)
+    for precision in (kpt.PRECISION_F64, kpt.PRECISION_MIXED):
+        lower = ctx.field(f, kpt.TABLE_PARKER16, precision)
+        parts = ctx.particles(1000)
+        ctx.inject(parts, lower, settings, 1000, 2, 11)
+        start = parts.download()
+        ctx.push_interval(parts, lower, lower, settings, 2, 11)
+        got = parts.download()
+        elapsed = 0.30000000000000004 - start["t"]
+        want_x = np.mod(start["x"] + 0.3 * elapsed, 1.0)
+        want_y = np.mod(start["y"] - 0.2 * elapsed, 1.0)
+        dx = np.abs((got["x"] - want_x + 0.5) % 1.0 - 0.5)
+        dy = np.abs((got["y"] - want_y + 0.5) % 1.0 - 0.5)
+        tol = 1e-12 if precision == kpt.PRECISION_F64 else 1e-6
+        assert dx.max() < tol and dy.max() < tol, (precision, dx.max(), dy.max())
+        assert np.all(got["p"] == start["p"])  # div V = 0: no momentum change
+        assert np.allclose(got["t"], 0.30000000000000004, rtol=0, atol=1e-15)
+
+
+def test_adiabatic_compression_limit(ctx, kpt, fields_mod, binding):
+    """Uniform div V with kappa -> 0: p follows p_{n+1} = p_n (1 - divV dt/3)
+    with the step size fixed at dt_max, i.e. p -> p0 exp(-divV t / 3)."""
+    f = fields_mod.harris_field(32, 32, x_range=(0.0, 1.0), y_range=(0.0, 1.0))
+    f.b[0], f.b[1], f.b[2] = 1.0, 0.0, 0.5
+    # V_x vanishes on cell 0 (sampled at x = 0 by the driver's half-cell shift)
+    xc = 0.5 * (f.x_edges[1:] + f.x_edges[:-1])
+    dx = f.x_edges[1] - f.x_edges[0]
+    f.v[0] = np.broadcast_to(0.05 * np.sin(2 * np.pi * (xc - 0.5 * dx))[None, :], f.v[0].shape)
+    f.v[1], f.v[2] = 0.0, 0.0
+    params = binding.default_params(kpara0=1e-20, kperp_over_kpara=0.0, dt_min_rel=1e-2,
+                                    dt_max_rel=1e-2)
+    settings = kpt.settings_from_dict(params)
+    lower = ctx.field(f, kpt.TABLE_PARKER16, kpt.PRECISION_F64)
+    table = lower.table()
+    parts = ctx.particles(1)
+    arrays = binding.empty_particles(1)
+    # sit on the node of cell 8 where dVx/dx is largest and V ~ 0 nearby
+    arrays.update(x=np.array([0.0]), y=np.array([0.5]), p=np.array([0.1]),
+                  t=np.array([0.0]), dt=np.array([1e-3]), status=np.zeros(1, np.int32))
+    parts.upload(arrays, 1)
+    ctx.push_interval(parts, lower, lower, settings, 0, 3)
+    got = parts.download()
+    divv = table[(0 + 2) + (16 + 2) * 36, 6] + table[(0 + 2) + (16 + 2) * 36, 7]
+    # x stays at the node (V(0) = 0 there and kappa = 0), 100 steps of 1e-3
+    p_euler = 0.1 * (1.0 - divv * 1e-3 / 3.0) ** 100
+    assert got["p"][0] == pytest.approx(p_euler, rel=1e-9)
+    assert got["p"][0] == pytest.approx(0.1 * np.exp(-divv * 0.1 / 3.0), rel=1e-5)
+
+
+def test_replay_is_deterministic_across_schedules(ctx, kpt, fields_mod, binding):
+    ye = fields_mod.stretched_edges(256, -2.0, 2.0)
+    f0 = fields_mod.harris_field(128, 256, y_edges=ye, island_amplitude=0.1, noise=0.01, seed=8)
+    settings = kpt.settings_from_dict(binding.default_params(kperp_over_kpara=0.05))
+    for precision in (kpt.PRECISION_F64, kpt.PRECISION_MIXED):
+        lower = ctx.field(f0, kpt.TABLE_PARKER16, precision)
+        results = []
+        for schedule, sort in ((kpt.SCHEDULE_REFILL, False), (kpt.SCHEDULE_SIMPLE, False),
+                               (kpt.SCHEDULE_REFILL, True)):
+            ctx.set_push_schedule(schedule, 0)
+            parts = ctx.particles(20000)
+            ctx.inject(parts, lower, settings, 20000, 4, 21)
+            if sort:
+                ctx.sort(parts, lower, 16, 16)
+            stats = ctx.push_interval(parts, lower, lower, settings, 4, 21)
+            results.append((parts.download(), stats.particle_steps))
+        ctx.set_push_schedule(kpt.SCHEDULE_REFILL, 0)
+        base, steps = results[0]
+        for other, other_steps in results[1:]:
+            assert other_steps == steps
+            for name in base:
+                assert np.array_equal(base[name], other[name]), (precision, name)
