@@ -423,3 +423,4 @@ cudaError_t launch_summary(const SummaryLaunch& L, cudaStream_t stream) {
 }
 
 }  // namespace kpt
+
