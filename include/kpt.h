@@ -228,6 +228,21 @@ int kpt_histogram(kpt_context* ctx, const kpt_particles* particles, double pmin,
                   int nbins, double* bins);
 int kpt_summarize(kpt_context* ctx, const kpt_particles* particles, kpt_summary* out);
 
+/* Summary of particles in caller-owned device arrays, allocating nothing.
+ * No counterpart in the reference: it serves callers that cannot allocate
+ * device memory (a host application that owns all device memory through its
+ * own pool or arena, or code that must not call cudaMalloc while other work
+ * is being captured or timed).  Same result as kpt_summarize.  Its scratch is
+ * one fixed device array of the library (about 0.7 MB per GPU, held until
+ * the process exits), so count is limited to 16,777,216 particles
+ * (KPT_ERROR_CAPACITY above that).  The first call on a device looks up the
+ * array's device address, so make it before any stream capture.  All calls
+ * share the array: calls that overlap on the GPU (other streams, other host
+ * threads) race and must be serialised by the caller.  Runs on cuda_stream
+ * (NULL = legacy default stream) and synchronises it. */
+int kpt_summarize_noalloc(const kpt_particle_arrays* arrays, uint64_t count, void* cuda_stream,
+                          kpt_summary* out);
+
 /* Interpolated table values at n host positions (x, y) and interval
  * fraction rt (parity and diagnostics); out is n x components float64. */
 int kpt_sample_table(kpt_context* ctx, const kpt_field* lower, const kpt_field* upper,

@@ -1093,6 +1093,48 @@ int kpt_particles_clear_order(kpt_particles* parts) {
     return KPT_OK;
 }
 
+int kpt_summarize_noalloc(const kpt_particle_arrays* arrays, uint64_t count, void* cuda_stream,
+                          kpt_summary* out) {
+    KPT_REQUIRE(arrays != nullptr && out != nullptr, "kpt_summarize_noalloc: NULL argument");
+    std::memset(out, 0, sizeof(*out));
+    out->stored = count;
+    if (count == 0) {
+        return KPT_OK;
+    }
+    if (count > kpt::noalloc_summary_max_particles()) {
+        return set_error(KPT_ERROR_CAPACITY,
+                         "kpt_summarize_noalloc: count " + std::to_string(count) +
+                             " exceeds the fixed scratch limit of " +
+                             std::to_string(kpt::noalloc_summary_max_particles()) +
+                             " particles; use kpt_summarize");
+    }
+    KPT_REQUIRE(arrays->p && arrays->step_dt && arrays->weight && arrays->status &&
+                    arrays->split_level,
+                "kpt_summarize_noalloc: NULL device array");
+    kpt::SummaryLaunch launch{};
+    launch.p = arrays->p;
+    launch.dt = arrays->step_dt;
+    launch.weight = arrays->weight;
+    launch.status = arrays->status;
+    launch.level = arrays->split_level;
+    launch.count = count;
+    kpt::SummaryPartial r{};
+    KPT_CUDA(kpt::noalloc_summary(launch, static_cast<cudaStream_t>(cuda_stream), &r));
+    out->active = r.active;
+    out->inactive = r.inactive;
+    out->weight_sum = r.weight_sum;
+    out->max_split_level = r.max_level;
+    if (r.active > 0) {
+        out->p_min = r.p_min;
+        out->p_max = r.p_max;
+        out->dt_min = r.dt_min;
+        out->dt_max = r.dt_max;
+        out->p_avg = r.p_sum / static_cast<double>(r.active);
+        out->dt_avg = r.dt_sum / static_cast<double>(r.active);
+    }
+    return KPT_OK;
+}
+
 int kpt_sample_table(kpt_context* ctx, const kpt_field* lower, const kpt_field* upper,
                      uint64_t n, const double* x, const double* y, const double* rt,
                      int time_interpolation, double* out) {

@@ -117,6 +117,11 @@ struct SummaryLaunch {
 };
 int summary_blocks(uint64_t count);
 cudaError_t launch_summary(const SummaryLaunch& launch, cudaStream_t stream);
+// Summary with its scratch in a fixed device array (no allocation); fills
+// *host (pageable host memory) and synchronises the stream.
+unsigned long long noalloc_summary_max_particles();
+cudaError_t noalloc_summary(const SummaryLaunch& launch, cudaStream_t stream,
+                            SummaryPartial* host);
 
 // Counting sort of particle indices by spatial tile (inactive particles
 // last).  counts/offsets hold tiles + 1 entries.

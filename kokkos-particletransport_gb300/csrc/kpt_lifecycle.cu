@@ -424,3 +424,54 @@ cudaError_t launch_summary(const SummaryLaunch& L, cudaStream_t stream) {
 
 }  // namespace kpt
 
+// ------------------------------------------------- allocation-free summary
+// For callers that must not allocate device memory (code running inside a
+// host application's memory pool or arena, under a CUDA graph being built
+// elsewhere, or in a host thread that is forbidden to call cudaMalloc), the
+// summary reduction has a variant whose per-block partials live in this
+// fixed device array instead of a context buffer.  Every GPU that loads the
+// library holds the array (about 0.7 MB) until the process exits.
+namespace {
+
+constexpr int kNoAllocMaxBlocks = 8192;  // 8192 blocks x 2048 particles
+constexpr unsigned long long kNoAllocMaxParticles =
+    static_cast<unsigned long long>(kNoAllocMaxBlocks) * kpt::kSummaryThreads * kpt::kSummaryPerThread;
+
+// [0, kNoAllocMaxBlocks): per-block partials; [kNoAllocMaxBlocks]: result.
+static __device__ __align__(256) kpt::SummaryPartial g_noalloc_summary[kNoAllocMaxBlocks + 1];
+
+// Device address of g_noalloc_summary per device, looked up once per device
+// (cudaGetSymbolAddress with that device current).
+constexpr int kNoAllocMaxDevices = 64;
+kpt::SummaryPartial* g_noalloc_address[kNoAllocMaxDevices] = {};
+
+}  // namespace
+
+namespace kpt {
+
+unsigned long long noalloc_summary_max_particles() { return kNoAllocMaxParticles; }
+
+cudaError_t noalloc_summary(const SummaryLaunch& in, cudaStream_t stream, SummaryPartial* host) {
+    int device = 0;
+    cudaError_t err = cudaGetDevice(&device);
+    if (err != cudaSuccess) return err;
+    if (device < 0 || device >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
+    if (g_noalloc_address[device] == nullptr) {
+        void* ptr = nullptr;
+        err = cudaGetSymbolAddress(&ptr, g_noalloc_summary);
+        if (err != cudaSuccess) return err;
+        g_noalloc_address[device] = static_cast<SummaryPartial*>(ptr);
+    }
+    SummaryLaunch L = in;
+    L.partials = g_noalloc_address[device];
+    L.result = g_noalloc_address[device] + kNoAllocMaxBlocks;
+    // Every partial that the final pass reads is written by this call, so no
+    // clearing is needed between calls.
+    err = launch_summary(L, stream);
+    if (err != cudaSuccess) return err;
+    err = cudaMemcpyAsync(host, L.result, sizeof(SummaryPartial), cudaMemcpyDeviceToHost, stream);
+    if (err != cudaSuccess) return err;
+    return cudaStreamSynchronize(stream);
+}
+
+}  // namespace kpt
