@@ -184,6 +184,46 @@ def run_gpu(args):
     return results
 
 
+def run_focused(args):
+    """Focused transport with the slab-QLT closure on the same field: one
+    interval push of the population per step, FP64 and mixed."""
+    import torch
+    kpt = importlib.import_module("kokkos-particletransport_gb300")
+    f0, f1 = make_workload()
+    settings = kpt.default_settings(kperp_over_kpara=0.05, focused=1, closure=kpt.CLOSURE_QLT)
+    ctx = kpt.Context(0)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    out = {}
+    for label, precision in (("mixed", kpt.PRECISION_MIXED), ("f64", kpt.PRECISION_F64)):
+        n = args.focused_particles
+        lower = ctx.field(f0, kpt.TABLE_FOCUSED21, precision)
+        upper = ctx.field(f1, kpt.TABLE_FOCUSED21, precision)
+        parts = ctx.particles(n)
+        ctx.inject(parts, lower, settings, n, START_FRAME, SEED)
+        start = parts.download()
+        # warm-up: one interval on a copy of the population
+        ctx.sort(parts, lower, 16, 16)
+        ctx.push_interval(parts, lower, upper, settings, START_FRAME, SEED)
+        parts.upload(start, n)
+        ctx.sort(parts, lower, 16, 16)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        stats = ctx.push_interval(parts, lower, upper, settings, START_FRAME, SEED)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        out[label] = {"value": stats.particle_steps / (ms / 1e3), "ms": ms,
+                      "particle_steps": int(stats.particle_steps), "particles": n}
+        for obj in (lower, upper, parts):
+            obj.close()
+    ctx.close()
+    out["speedup_mixed_over_f64"] = out["mixed"]["value"] / out["f64"]["value"]
+    return out
+
+
 def cpu_baseline(particles: int, steps: int = 1):
     """Oracle restatement (OpenMP, all host threads) on a bounded sample."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -219,6 +259,8 @@ def main():
     parser.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     parser.add_argument("--particles", type=int, default=1 << 20)
     parser.add_argument("--cpu-particles", type=int, default=1 << 15)
+    parser.add_argument("--focused-particles", type=int, default=1 << 16,
+                        help="population of the focused/QLT leg (0 skips it)")
     parser.add_argument("--sort-tile", type=int, default=16,
                         help="cell-sort tile (cells) before each push; 0 disables")
     args = parser.parse_args()
@@ -245,6 +287,7 @@ def main():
         print(json.dumps(line))
         return
     results = run_gpu(args)
+    focused = run_focused(args) if args.focused_particles > 0 else None
     peak, peak_kind = read_peaks()
     mixed, f64 = results["mixed"], results["f64"]
     value = mixed["steps"] / (mixed["total_ms"] / 1e3)
@@ -273,6 +316,7 @@ def main():
                 "h2d_bytes_per_step": mixed["state_bytes"],
                 "d2h_bytes_per_step": mixed["state_bytes"]},
         # per timed step: the push, plus 3 cell-sort kernels when sorting
+        "focused_qlt": focused,
         "gpu_launches": args.steps * (1 + (3 if args.sort_tile > 0 else 0)),
         "clocks": mixed["clocks"],
     }

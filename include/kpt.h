@@ -65,6 +65,14 @@ enum kpt_precision {
                                 position, time and momentum accumulation and cell search */
 };
 
+/* Pitch-angle scattering closure of the focused push. */
+enum kpt_closure {
+    KPT_CLOSURE_DRIVER = 0,    /* the driver's reduced D_mumu (src/main.cpp:1551-1589) */
+    KPT_CLOSURE_QLT = 1,       /* slab-spectrum quasi-linear D_mumu, dD_mumu/dmu
+                                  (include/LegencyModel.hpp:539-645) */
+    KPT_CLOSURE_SURROGATE = 2  /* the QLT closure served by the trained MLP surrogate */
+};
+
 enum kpt_schedule {
     KPT_SCHEDULE_REFILL = 0,
     KPT_SCHEDULE_SIMPLE = 1
@@ -96,6 +104,17 @@ typedef struct kpt_settings {
     int32_t time_interpolation;
     int32_t split_particles;
     int32_t focused;
+    /* Focused transport scattering closure (extension; KPT_CLOSURE_DRIVER
+     * reproduces the reference driver).  The QLT closure evaluates, per
+     * substep, Omega = qlt_omega0 |B| / gamma (gamma = sqrt(1 + p^2)),
+     * v = particle_v0 p / p0, xi = Omega qlt_lc / v and the slab-spectrum
+     * D_mumu of index qlt_spectral_index with regularisation qlt_h0. */
+    int32_t closure;
+    double qlt_sigma2;          /* dB^2 / B^2 */
+    double qlt_spectral_index;  /* gamma_k */
+    double qlt_h0;              /* |mu| regularisation */
+    double qlt_omega0;          /* gyrofrequency at |B| = 1, gamma = 1 */
+    double qlt_lc;              /* correlation length */
 } kpt_settings;
 
 /* Per-push counters, summed over the particles pushed. */

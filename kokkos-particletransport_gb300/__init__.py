@@ -39,6 +39,11 @@ DOUBLE_SETTINGS = ("mhd_dt", "p0", "pmin", "pmax", "gamma_turb", "kpara0", "kper
                    "particle_v0", "duu0", "split_ratio", "pmin_split_over_p0", "mu_max")
 INT_SETTINGS = ("max_steps", "momentum_dependency", "magnetic_dependency", "time_interpolation",
                 "split_particles", "focused")
+CLOSURE_INT = ("closure",)
+CLOSURE_DOUBLE = ("qlt_sigma2", "qlt_spectral_index", "qlt_h0", "qlt_omega0", "qlt_lc")
+CLOSURE_DRIVER = 0
+CLOSURE_QLT = 1
+CLOSURE_SURROGATE = 2
 
 
 class KptError(RuntimeError):
@@ -48,7 +53,8 @@ class KptError(RuntimeError):
 class Settings(ctypes.Structure):
     """kpt_settings: the reference Reconnection2DSettings physics block."""
     _fields_ = [(n, ctypes.c_double) for n in DOUBLE_SETTINGS] + \
-               [(n, ctypes.c_int32) for n in INT_SETTINGS]
+               [(n, ctypes.c_int32) for n in INT_SETTINGS + CLOSURE_INT] + \
+               [(n, ctypes.c_double) for n in CLOSURE_DOUBLE]
 
     def as_dict(self) -> Dict[str, float]:
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -148,18 +154,21 @@ def default_settings(**overrides) -> Settings:
     s = Settings()
     load_library().kpt_default_settings(ctypes.byref(s))
     for key, value in overrides.items():
-        if key not in DOUBLE_SETTINGS + INT_SETTINGS:
+        if key not in DOUBLE_SETTINGS + INT_SETTINGS + CLOSURE_INT + CLOSURE_DOUBLE:
             raise KeyError(key)
         setattr(s, key, value)
     return s
 
 
 def settings_from_dict(values: Dict[str, float]) -> Settings:
-    s = Settings()
-    for name in DOUBLE_SETTINGS:
-        setattr(s, name, float(values[name]))
-    for name in INT_SETTINGS:
-        setattr(s, name, int(values[name]))
+    """Settings from a dict; closure fields missing from it keep their defaults."""
+    s = default_settings()
+    for name in DOUBLE_SETTINGS + CLOSURE_DOUBLE:
+        if name in values:
+            setattr(s, name, float(values[name]))
+    for name in INT_SETTINGS + CLOSURE_INT:
+        if name in values:
+            setattr(s, name, int(values[name]))
     return s
 
 

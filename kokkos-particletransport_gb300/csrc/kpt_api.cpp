@@ -289,6 +289,20 @@ int validate_settings(const kpt_settings* s) {
         return set_error(KPT_ERROR_INVALID_ARGUMENT,
                          "Reconnection2DSettings: step guard must be positive.");
     }
+    if (s->closure != KPT_CLOSURE_DRIVER) {
+        // PitchAngleScatteringParameters::validate (LegencyModel.hpp:205-221)
+        // plus positive Omega_0, L_c and sigma^2 (LegencyModel.hpp:566-570)
+        const bool qlt_ok = (s->closure == KPT_CLOSURE_QLT || s->closure == KPT_CLOSURE_SURROGATE) &&
+                            std::isfinite(s->qlt_spectral_index) && s->qlt_spectral_index > 1.0 &&
+                            std::isfinite(s->qlt_h0) && s->qlt_h0 > 0.0 &&
+                            std::isfinite(s->qlt_sigma2) && s->qlt_sigma2 > 0.0 &&
+                            std::isfinite(s->qlt_omega0) && s->qlt_omega0 > 0.0 &&
+                            std::isfinite(s->qlt_lc) && s->qlt_lc > 0.0;
+        if (!qlt_ok) {
+            return set_error(KPT_ERROR_INVALID_ARGUMENT,
+                             "kpt_settings: invalid scattering closure parameters.");
+        }
+    }
     return KPT_OK;
 }
 
@@ -329,6 +343,15 @@ kpt::DeviceSettings device_settings(const kpt_settings* s, const kpt::Grid& g) {
     d.time_interpolation = s->time_interpolation;
     d.split_particles = s->split_particles;
     d.focused = s->focused;
+    d.closure = s->closure;
+    d.qlt_sigma2 = s->qlt_sigma2;
+    d.qlt_gk = s->qlt_spectral_index;
+    d.qlt_h0 = s->qlt_h0;
+    d.qlt_omega0 = s->qlt_omega0;
+    d.qlt_lc = s->qlt_lc;
+    // pitch_angle_spectrum_normalization (LegencyModel.hpp:539-552)
+    const double pi = 3.141592653589793238462643383279502884;
+    d.qlt_norm = s->qlt_spectral_index * std::sin(pi / s->qlt_spectral_index) / pi;
     return d;
 }
 
@@ -373,6 +396,12 @@ void kpt_default_settings(kpt_settings* s) {
     s->time_interpolation = 1;
     s->split_particles = 1;
     s->focused = 0;
+    s->closure = KPT_CLOSURE_DRIVER;
+    s->qlt_sigma2 = 0.1;
+    s->qlt_spectral_index = 5.0 / 3.0;
+    s->qlt_h0 = 1.0e-6;
+    s->qlt_omega0 = 1000.0;
+    s->qlt_lc = 0.05;
 }
 
 int kpt_context_create(int device, kpt_context** out) {
@@ -867,7 +896,11 @@ int kpt_push_interval(kpt_context* ctx, kpt_particles* parts, const kpt_field* l
     launch.fixed.axis[1] = lower->fixed[1];
     launch.fixed.dt_min = static_cast<float>(launch.settings.dt_min);
     launch.fixed.dt_max = static_cast<float>(launch.settings.dt_max);
-    launch.fixed.pfloor = 0.25 * settings->p0;
+    launch.fixed.tau_per_time = static_cast<float>(4611686018427387904.0 / settings->mhd_dt);
+    launch.fixed.time_per_tau_2_32 = static_cast<float>(settings->mhd_dt / 1073741824.0);
+    const double pfloor = 0.25 * settings->p0;
+    launch.fixed.pfloor_hi = static_cast<float>(pfloor);
+    launch.fixed.pfloor_lo = static_cast<float>(pfloor - static_cast<double>(launch.fixed.pfloor_hi));
     launch.order = parts->order_valid ? parts->order.as<uint32_t>() : nullptr;
     launch.precision = lower->precision;
     launch.focused = settings->focused != 0;

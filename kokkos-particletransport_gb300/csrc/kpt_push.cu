@@ -83,6 +83,46 @@ __device__ __forceinline__ T clamp_mu(T v, T m) {
     return v;
 }
 
+// The settings the substep physics reads, in the arithmetic type of the
+// path (built once per launch on the host, so the FP32 path never converts
+// a double inside the loop).
+template <typename T>
+struct Consts {
+    T p0, gamma_turb, pindex, kpara0, kperp_over_kpara, drift_param1, drift_param2, charge;
+    T particle_v0, duu0, h0, mu_max, dx, dy;
+    T qlt_gk, qlt_h0, qlt_lc, qlt_sigma2, qlt_norm, qlt_omega0;
+    int magnetic_dependency, momentum_dependency, closure;
+};
+
+template <typename T>
+Consts<T> make_consts(const DeviceSettings& s) {
+    Consts<T> k;
+    k.p0 = s.p0;
+    k.gamma_turb = s.gamma_turb;
+    k.pindex = s.pindex;
+    k.kpara0 = s.kpara0;
+    k.kperp_over_kpara = s.kperp_over_kpara;
+    k.drift_param1 = s.drift_param1;
+    k.drift_param2 = s.drift_param2;
+    k.charge = s.charge;
+    k.particle_v0 = s.particle_v0;
+    k.duu0 = s.duu0;
+    k.h0 = s.h0;
+    k.mu_max = s.mu_max;
+    k.dx = s.dx;
+    k.dy = s.dy;
+    k.qlt_gk = s.qlt_gk;
+    k.qlt_h0 = s.qlt_h0;
+    k.qlt_lc = s.qlt_lc;
+    k.qlt_sigma2 = s.qlt_sigma2;
+    k.qlt_norm = s.qlt_norm;
+    k.qlt_omega0 = s.qlt_omega0;
+    k.magnetic_dependency = s.magnetic_dependency;
+    k.momentum_dependency = s.momentum_dependency;
+    k.closure = s.closure;
+    return k;
+}
+
 // ------------------------------------------------------------ sampling
 template <typename T>
 struct Vec;
@@ -229,6 +269,35 @@ __device__ __forceinline__ void sample_coefficients(const Grid& g, const T* __re
 }
 
 // ------------------------------------------------------------- physics
+// Slab quasi-linear pitch-angle scattering (LegencyModel.hpp:557-645):
+// D_mumu and dD_mumu/dmu at one (mu, Omega, v).
+template <typename T>
+__device__ __forceinline__ void qlt_scattering(T mu, T omega, T speed, const Consts<T>& s,
+                                               T& dmumu, T& dmumu_dmu) {
+    using N = Num<T>;
+    dmumu = T(0);
+    dmumu_dmu = T(0);
+    const T one_minus_mu2 = T(1) - mu * mu;
+    if (one_minus_mu2 <= T(0)) {
+        return;
+    }
+    const T gk = s.qlt_gk;
+    const T reg = N::abs(mu) + s.qlt_h0;
+    const T xi = N::div(omega * s.qlt_lc, speed);
+    const T reg_gk1 = N::pow(reg, gk - T(1));
+    const T denominator = N::pow(reg, gk) + N::pow(xi, gk);
+    const T prefactor = static_cast<T>(0.25 * 3.141592653589793238462643383279502884) * omega *
+                        s.qlt_sigma2 * s.qlt_norm;
+    dmumu = N::div(prefactor * one_minus_mu2 * xi * reg_gk1, denominator);
+    if (dmumu == T(0) || mu == T(0)) {
+        return;
+    }
+    const T sign_mu = mu > T(0) ? T(1) : T(-1);
+    const T shape = sign_mu * (N::div(gk - T(1), reg) - N::div(gk * reg_gk1, denominator));
+    const T endpoint = N::div(T(-2) * mu, one_minus_mu2);
+    dmumu_dmu = dmumu * (endpoint + shape);
+}
+
 template <typename T>
 struct Rates {
     T dx_dt, dy_dt, dp_dt, dmu_dt, duu;
@@ -242,7 +311,7 @@ struct Rates {
 // substep (src/main.cpp:1167-1257 Parker, :1421-1630 focused).  Returns
 // false where the reference sets status 2.
 template <typename T, bool FOCUSED>
-__device__ __forceinline__ bool physics(const T* c, T p, T pitch_mu, const DeviceSettings& s,
+__device__ __forceinline__ bool physics(const T* c, T p, T pitch_mu, const Consts<T>& s,
                                         Rates<T>& r) {
     using N = Num<T>;
     T vx, vy, bx, by, bz, b, dvx_dx, dvy_dy, dbx_dx, dbx_dy, dby_dx, dby_dy, dbz_dx, dbz_dy,
@@ -261,8 +330,8 @@ __device__ __forceinline__ bool physics(const T* c, T p, T pitch_mu, const Devic
     if (!N::finite(p) || p <= T(0) || !N::finite(b) || b <= T(0)) {
         return false;
     }
-    const T p0 = static_cast<T>(s.p0);
-    const T gamma = static_cast<T>(s.gamma_turb);
+    const T p0 = s.p0;
+    const T gamma = s.gamma_turb;
     const T ib = N::div(T(1), b);
     const T ib2 = ib * ib;
     const T ib3 = ib2 * ib;
@@ -273,10 +342,10 @@ __device__ __forceinline__ bool physics(const T* c, T p, T pitch_mu, const Devic
     }
     T knorm = knorm_para;
     if (s.momentum_dependency == 1) {
-        knorm *= N::pow(N::div(p, p0), static_cast<T>(s.pindex));
+        knorm *= N::pow(N::div(p, p0), s.pindex);
     }
-    const T kpara = static_cast<T>(s.kpara0) * knorm;
-    const T kperp = kpara * static_cast<T>(s.kperp_over_kpara);
+    const T kpara = s.kpara0 * knorm;
+    const T kperp = kpara * s.kperp_over_kpara;
     if (!N::finite(kpara) || kpara <= T(0) || !N::finite(kperp) || kperp < T(0)) {
         return false;
     }
@@ -306,15 +375,15 @@ __device__ __forceinline__ bool physics(const T* c, T p, T pitch_mu, const Devic
     const T dkxy_dy = kpp * dkdy * bx * by * ib2 +
                       kpp * ((dbx_dy * by + bx * dby_dy) * ib2 - T(2) * bx * by * db_dy * ib3);
 
-    const T d1 = static_cast<T>(s.drift_param1);
-    const T d2 = static_cast<T>(s.drift_param2);
+    const T d1 = s.drift_param1;
+    const T d2 = s.drift_param2;
     const T drift_denominator =
         N::sqrt(square(N::div(d1 * p0, p)) + square(N::div(d2 * p0 * p0, p * p)));
 
     T dx_dt, dy_dt, dp_dt;
     T dmu_dt = T(0), duu = T(0);
     if (FOCUSED) {
-        pitch_mu = clamp_mu(pitch_mu, static_cast<T>(s.mu_max));
+        pitch_mu = clamp_mu(pitch_mu, s.mu_max);
         const T mu2 = pitch_mu * pitch_mu;
         const T muf1 = T(0.5) * (T(1) - mu2);
         const T muf2 = T(0.5) * (T(3) * mu2 - T(1));
@@ -322,12 +391,12 @@ __device__ __forceinline__ bool physics(const T* c, T p, T pitch_mu, const Devic
         const T ky = bx * dby_dx + by * dby_dy;
         const T kz = bx * dbz_dx + by * dbz_dy;
         const T bdot_curvb = bx * dbz_dy - by * dbz_dx + bz * (dby_dx - dbx_dy);
-        const T vdp = N::div(N::div(T(1), static_cast<T>(s.charge)), drift_denominator);
+        const T vdp = N::div(N::div(T(1), s.charge), drift_denominator);
         const T vdx = vdp * (muf1 * (-bz * db_dy) * ib2 + mu2 * (by * kz - bz * ky) * ib3 +
                              muf1 * bx * bdot_curvb * ib3);
         const T vdy = vdp * (muf1 * (bz * db_dx) * ib2 + mu2 * (bz * kx - bx * kz) * ib3 +
                              muf1 * by * bdot_curvb * ib3);
-        const T speed = N::div(static_cast<T>(s.particle_v0) * p, p0);
+        const T speed = N::div(s.particle_v0 * p, p0);
         if (!N::finite(speed) || speed <= T(0)) {
             return false;
         }
@@ -349,31 +418,40 @@ __device__ __forceinline__ bool physics(const T* c, T p, T pitch_mu, const Devic
         dmu_dt = speed * div_bnorm + pitch_mu * divv - T(3) * pitch_mu * bb_gradv -
                  N::div(T(2) * bv_gradv, speed);
         dmu_dt *= T(0.5) * (T(1) - mu2);
-        const T abs_mu = N::abs(pitch_mu);
-        const T dtmp = N::pow(abs_mu, gamma - T(1)) + static_cast<T>(s.h0);
-        const T duu0 = static_cast<T>(s.duu0);
-        duu = duu0 * (T(1) - mu2) * dtmp;
         T duu_du = T(0);
-        if (pitch_mu > T(0)) {
-            duu_du = duu0 * (T(-2) * pitch_mu * dtmp + (T(1) - mu2) * N::pow(abs_mu, gamma - T(2)));
-        } else if (pitch_mu < T(0)) {
-            duu_du = duu0 * (T(-2) * pitch_mu * dtmp - (T(1) - mu2) * N::pow(abs_mu, gamma - T(2)));
+        if (s.closure != 0) {
+            // slab QLT closure (extension): Omega = Omega_0 |B| / gamma
+            const T omega = N::div(s.qlt_omega0 * b, N::sqrt(T(1) + p * p));
+            qlt_scattering<T>(pitch_mu, omega, speed, s, duu, duu_du);
+        } else {
+            // the driver's reduced closure (src/main.cpp:1551-1589)
+            const T abs_mu = N::abs(pitch_mu);
+            const T dtmp = N::pow(abs_mu, gamma - T(1)) + s.h0;
+            const T duu0 = s.duu0;
+            duu = duu0 * (T(1) - mu2) * dtmp;
+            if (pitch_mu > T(0)) {
+                duu_du = duu0 * (T(-2) * pitch_mu * dtmp +
+                                 (T(1) - mu2) * N::pow(abs_mu, gamma - T(2)));
+            } else if (pitch_mu < T(0)) {
+                duu_du = duu0 * (T(-2) * pitch_mu * dtmp -
+                                 (T(1) - mu2) * N::pow(abs_mu, gamma - T(2)));
+            }
+            T duu_norm = T(1);
+            if (s.magnetic_dependency == 1) {
+                duu_norm *= N::pow(b, T(2) - gamma);
+            }
+            if (s.momentum_dependency == 1) {
+                duu_norm *= N::pow(N::div(p, p0), gamma - T(1));
+            }
+            duu *= duu_norm;
+            duu_du *= duu_norm;
         }
-        T duu_norm = T(1);
-        if (s.magnetic_dependency == 1) {
-            duu_norm *= N::pow(b, T(2) - gamma);
-        }
-        if (s.momentum_dependency == 1) {
-            duu_norm *= N::pow(N::div(p, p0), gamma - T(1));
-        }
-        duu *= duu_norm;
-        duu_du *= duu_norm;
         dmu_dt += duu_du;
         if (!N::finite(dmu_dt) || !N::finite(duu) || duu < T(0)) {
             return false;
         }
     } else {
-        const T vdp = N::div(N::div(T(1), T(3) * static_cast<T>(s.charge)), drift_denominator);
+        const T vdp = N::div(N::div(T(1), T(3) * s.charge), drift_denominator);
         const T vdx = vdp * (dbz_dy * ib2 - T(2) * bz * db_dy * ib3);
         const T vdy = vdp * (-dbz_dx * ib2 + T(2) * bz * db_dx * ib3);
         dx_dt = vx + vdx + dkxx_dx + dkxy_dy;
@@ -383,8 +461,8 @@ __device__ __forceinline__ bool physics(const T* c, T p, T pitch_mu, const Devic
     }
 
     // Step-size limiters (src/main.cpp:1243-1257, :1596-1650).
-    const T dxs = static_cast<T>(s.dx);
-    const T dys = static_cast<T>(s.dy);
+    const T dxs = s.dx;
+    const T dys = s.dy;
     r.fixed_dt = false;
     r.dt = T(0);
     if (FOCUSED) {
@@ -432,7 +510,7 @@ __device__ __forceinline__ bool physics(const T* c, T p, T pitch_mu, const Devic
 // (src/main.cpp:1280-1291 Parker, :1660-1702 focused).
 template <typename T, bool FOCUSED>
 __device__ __forceinline__ void increments(const Rates<T>& r, T dt, const uint4& r0,
-                                           const uint4& r1, const DeviceSettings& s, T& delta_x,
+                                           const uint4& r1, const Consts<T>& s, T& delta_x,
                                            T& delta_y, T& new_mu) {
     using N = Num<T>;
     const T sdt = N::sqrt(dt);
@@ -455,7 +533,7 @@ __device__ __forceinline__ void increments(const Rates<T>& r, T dt, const uint4&
         delta_x = r.dx_dt * dt + stochastic_x;
         delta_y = r.dy_dt * dt + stochastic_y;
         new_mu = clamp_mu(r.pitch_mu + r.dmu_dt * dt + pitch_random * N::sqrt(T(2) * r.duu) * sdt,
-                          static_cast<T>(s.mu_max));
+                          s.mu_max);
     } else {
         const T ran1 = N::noise(r0.x, r0.y);
         const T ran2 = N::noise(r0.z, r0.w);
@@ -469,6 +547,8 @@ __device__ __forceinline__ void increments(const Rates<T>& r, T dt, const uint4&
 struct PushParams {
     Grid grid;
     FixedGrid fixed;
+    Consts<double> kd;
+    Consts<float> kf;
     const void* lower;
     const void* upper;
     ParticleArrays parts;
@@ -506,7 +586,7 @@ __device__ __forceinline__ bool substep(StateF64& st, const PushParams& P) {
                                            __dadd_rn(st.x, s.shift_x), __dadd_rn(st.y, s.shift_y),
                                            rt, s.time_interpolation, c);
     Rates<double> r;
-    if (!physics<double, FOCUSED>(c, st.p, st.mu, s, r)) {
+    if (!physics<double, FOCUSED>(c, st.p, st.mu, P.kd, r)) {
         st.status = 2;
         return false;
     }
@@ -524,7 +604,7 @@ __device__ __forceinline__ bool substep(StateF64& st, const PushParams& P) {
     const uint4 r0 = philox4x32_10(make_uint4(block, st.index, P.frame, kTagPush), P.key);
     const uint4 r1 = philox4x32_10(make_uint4(block + 1u, st.index, P.frame, kTagPush), P.key);
     double dx, dy, mu;
-    increments<double, FOCUSED>(r, dt, r0, r1, s, dx, dy, mu);
+    increments<double, FOCUSED>(r, dt, r0, r1, P.kd, dx, dy, mu);
     st.mu = mu;
     st.x = __dadd_rn(st.x, dx);
     st.y = __dadd_rn(st.y, dy);
@@ -573,14 +653,24 @@ __device__ __forceinline__ bool live(const StateF64& st, const PushParams& P) {
 }
 
 // ------------------------------------------------------------ mixed path
+// No FP64 instruction runs inside the mixed substep loop:
+//  * position: 64-bit fixed-point phase over each periodic width;
+//  * time: 64-bit fixed-point fraction of the interval (2^62 = interval
+//    end), so the last step lands exactly on the interval end;
+//  * momentum: an unevaluated pair of floats (hi + lo, ~48-bit significand)
+//    updated with an error-free sum.
+// FP64 is used once per particle and push, to convert state in and out.
 struct StateMixed {
-    uint64_t px, py;  // fixed-point phase over each periodic width
-    double p, t;
+    uint64_t px, py;   // phase over the periodic widths
+    long long tau;     // (t - interval_start) / mhd_dt * 2^62
+    float p_hi, p_lo;  // momentum = p_hi + p_lo
     float mu, diag_dt;
     int steps;
     int status;
     uint32_t index;
 };
+
+constexpr long long kTauEnd = 1ll << 62;
 
 // Exact float -> int64 (truncation) with integer operations only.
 __device__ __forceinline__ long long float_to_s64(float f) {
@@ -594,6 +684,14 @@ __device__ __forceinline__ long long float_to_s64(float f) {
         v = e > -24 ? (m >> (-e)) : 0;
     }
     return bits < 0 ? -v : v;
+}
+
+// Non-negative int64 below 2^63 -> float from its top bits (integer pipe
+// plus one 32-bit conversion).
+__device__ __forceinline__ float s64_to_float_scaled(long long v, float scale_2_32) {
+    return static_cast<float>(static_cast<uint32_t>(static_cast<unsigned long long>(v) >> 32)) *
+               scale_2_32 +
+           static_cast<float>(static_cast<uint32_t>(v)) * (scale_2_32 * (1.0f / 4294967296.0f));
 }
 
 // Cell index and upper weight of the driver's stencil for a fixed-point
@@ -626,6 +724,16 @@ __device__ __forceinline__ void fixed_stencil_stored(const FixedAxis& a, uint64_
         __ldg(a.inv_spacing + k + 2);
 }
 
+// hi + lo += d (error-free sum, then renormalise).
+__device__ __forceinline__ void add_pair(float& hi, float& lo, float d) {
+    const float s = hi + d;
+    const float bb = s - hi;
+    const float err = (hi - (s - bb)) + (d - bb);
+    const float l = lo + err;
+    hi = s + l;
+    lo = l - (hi - s);
+}
+
 template <bool FOCUSED>
 __device__ __forceinline__ bool substep(StateMixed& st, const PushParams& P) {
     constexpr int C = FOCUSED ? 21 : 16;
@@ -652,15 +760,14 @@ __device__ __forceinline__ bool substep(StateMixed& st, const PushParams& P) {
     const float wc[4] = {a0 * a1, w0 * a1, a0 * w1, w0 * w1};
     size_t pt[4];
     corner_points(lo0, lo0 + 1, lo1, lo1 + 1, P.grid.ex, pt);
-    float rt = static_cast<float>(st.t - P.interval_start) * P.inv_mhd_dt;
-    rt = rt < 0.0f ? 0.0f : (rt > 1.0f ? 1.0f : rt);
+    float rt = st.tau <= 0 ? 0.0f : s64_to_float_scaled(st.tau, 1.0f / 1073741824.0f);
+    rt = rt > 1.0f ? 1.0f : rt;
     float c[C];
     sample_stencil<float, C, STRIDE>(static_cast<const float*>(P.lower),
                                      static_cast<const float*>(P.upper), pt, wc, rt,
                                      s.time_interpolation, c);
-    const float pf = static_cast<float>(st.p);
     Rates<float> r;
-    if (!physics<float, FOCUSED>(c, pf, st.mu, s, r)) {
+    if (!physics<float, FOCUSED>(c, st.p_hi, st.mu, P.kf, r)) {
         st.status = 2;
         return false;
     }
@@ -668,13 +775,13 @@ __device__ __forceinline__ bool substep(StateMixed& st, const PushParams& P) {
     if (dtf < F.dt_min) dtf = F.dt_min;
     if (dtf > F.dt_max) dtf = F.dt_max;
     st.diag_dt = dtf;
-    double dt = static_cast<double>(dtf);
-    const double remaining = P.interval_end - st.t;
-    if (dt > remaining) {
-        dt = remaining;
-        dtf = static_cast<float>(remaining);
+    long long dtau = float_to_s64(dtf * F.tau_per_time);
+    const long long remaining = kTauEnd - st.tau;
+    if (dtau >= remaining) {
+        dtau = remaining;
+        dtf = s64_to_float_scaled(remaining, F.time_per_tau_2_32);
     }
-    if (!(dtf > 0.0f) || !isfinite(dtf)) {
+    if (!(dtf > 0.0f) || !isfinite(dtf) || dtau <= 0) {
         st.status = 2;
         return false;
     }
@@ -682,7 +789,7 @@ __device__ __forceinline__ bool substep(StateMixed& st, const PushParams& P) {
     const uint4 r0 = philox4x32_10(make_uint4(block, st.index, P.frame, kTagPush), P.key);
     const uint4 r1 = philox4x32_10(make_uint4(block + 1u, st.index, P.frame, kTagPush), P.key);
     float dx, dy, mu;
-    increments<float, FOCUSED>(r, dtf, r0, r1, s, dx, dy, mu);
+    increments<float, FOCUSED>(r, dtf, r0, r1, P.kf, dx, dy, mu);
     const float dp = r.dp_dt * dtf;
     if (!isfinite(dx) || !isfinite(dy) || !isfinite(dp)) {
         st.status = 2;
@@ -691,10 +798,13 @@ __device__ __forceinline__ bool substep(StateMixed& st, const PushParams& P) {
     st.mu = mu;
     st.px += static_cast<uint64_t>(float_to_s64(dx * F.axis[0].to_fixed));
     st.py += static_cast<uint64_t>(float_to_s64(dy * F.axis[1].to_fixed));
-    st.p += static_cast<double>(dp);
-    st.t += dt;
-    if (st.p < F.pfloor) st.p = F.pfloor;
-    return st.t < P.interval_end && st.steps < s.max_steps;
+    add_pair(st.p_hi, st.p_lo, dp);
+    st.tau += dtau;
+    if (st.p_hi < F.pfloor_hi) {
+        st.p_hi = F.pfloor_hi;
+        st.p_lo = F.pfloor_lo;
+    }
+    return st.tau < kTauEnd && st.steps < s.max_steps;
 }
 
 // Position <-> fixed-point phase (once per particle and push).
@@ -718,14 +828,19 @@ __device__ __forceinline__ void load(StateMixed& st, const PushParams& P, uint32
     const double y = wrap_driver(a.y[index], s.y_lower, s.y_upper, s.y_width);
     st.px = to_phase(x, s.x_lower, P.grid.axis[0].inv_width);
     st.py = to_phase(y, s.y_lower, P.grid.axis[1].inv_width);
-    st.p = a.p[index];
-    st.t = a.t[index];
+    const double p = a.p[index];
+    st.p_hi = static_cast<float>(p);
+    st.p_lo = static_cast<float>(p - static_cast<double>(st.p_hi));
+    const double t = a.t[index];
+    const double f = (t - P.interval_start) / s.mhd_dt;
+    st.tau = t >= P.interval_end ? kTauEnd
+                                 : (f <= -1.0 ? -kTauEnd : __double2ll_rn(f * 4611686018427387904.0));
     st.diag_dt = static_cast<float>(a.step_dt[index]);
     st.mu = FOCUSED ? clamp_mu(static_cast<float>(a.mu[index]), static_cast<float>(s.mu_max))
                     : 0.0f;
     st.steps = 0;
     st.status = 0;
-    if (!isfinite(a.x[index]) || !isfinite(a.y[index])) {
+    if (!isfinite(a.x[index]) || !isfinite(a.y[index]) || !isfinite(p) || !isfinite(t)) {
         st.status = 2;
     }
 }
@@ -734,26 +849,29 @@ template <bool FOCUSED>
 __device__ __forceinline__ void store(StateMixed& st, const PushParams& P) {
     const ParticleArrays& a = P.parts;
     const DeviceSettings& s = P.s;
-    if (st.steps >= s.max_steps && st.t < P.interval_end) st.status = 2;
+    if (st.steps >= s.max_steps && st.tau < kTauEnd) st.status = 2;
     const uint32_t i = st.index;
     if (st.steps > 0) {
         a.x[i] = wrap_driver(from_phase(st.px, s.x_lower, s.x_width), s.x_lower, s.x_upper,
                              s.x_width);
         a.y[i] = wrap_driver(from_phase(st.py, s.y_lower, s.y_width), s.y_lower, s.y_upper,
                              s.y_width);
+        a.p[i] = static_cast<double>(st.p_hi) + static_cast<double>(st.p_lo);
+        a.t[i] = st.tau >= kTauEnd
+                     ? P.interval_end
+                     : P.interval_start + static_cast<double>(st.tau) *
+                                              (s.mhd_dt * (1.0 / 4611686018427387904.0));
         a.step_dt[i] = static_cast<double>(st.diag_dt);
+        if (FOCUSED) a.mu[i] = static_cast<double>(st.mu);
     } else {
         a.x[i] = wrap_driver(a.x[i], s.x_lower, s.x_upper, s.x_width);
         a.y[i] = wrap_driver(a.y[i], s.y_lower, s.y_upper, s.y_width);
     }
-    a.p[i] = st.p;
-    a.t[i] = st.t;
-    if (FOCUSED) a.mu[i] = static_cast<double>(st.mu);
     a.status[i] = st.status;
 }
 
 __device__ __forceinline__ bool live(const StateMixed& st, const PushParams& P) {
-    return st.status == 0 && st.t < P.interval_end && st.steps < P.s.max_steps;
+    return st.status == 0 && st.tau < kTauEnd && st.steps < P.s.max_steps;
 }
 
 // ---------------------------------------------------------------- drivers
@@ -895,6 +1013,8 @@ cudaError_t launch_push(const PushLaunch& L, cudaStream_t stream) {
     P.order = L.order;
     P.count = L.count;
     P.s = L.settings;
+    P.kd = make_consts<double>(L.settings);
+    P.kf = make_consts<float>(L.settings);
     P.interval_start = L.interval_start;
     P.interval_end = L.interval_end;
     P.inv_mhd_dt = static_cast<float>(1.0 / L.settings.mhd_dt);

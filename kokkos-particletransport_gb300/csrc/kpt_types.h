@@ -48,7 +48,10 @@ struct FixedGrid {
     FixedAxis axis[2];
     float dt_min;
     float dt_max;
-    double pfloor;
+    float tau_per_time;        // 2^62 / mhd_dt (fixed-point time units per time unit)
+    float time_per_tau_2_32;   // mhd_dt / 2^30 (time per 2^32 fixed-point units)
+    float pfloor_hi;           // 0.25 p0 as a float pair
+    float pfloor_lo;
 };
 
 // Device copy of the driver's settings after make_device_settings
@@ -61,6 +64,10 @@ struct DeviceSettings {
     double h0, split_ratio, pmin_split, mu_max;
     int max_steps, momentum_dependency, magnetic_dependency, time_interpolation;
     int split_particles, focused;
+    // focused scattering closure (kpt_closure) and its slab-QLT parameters;
+    // qlt_norm = gamma_k sin(pi / gamma_k) / pi, computed on the host
+    int closure;
+    double qlt_sigma2, qlt_gk, qlt_h0, qlt_omega0, qlt_lc, qlt_norm;
 };
 
 struct ParticleArrays {

@@ -24,11 +24,14 @@ DOUBLE_PARAMS = ("mhd_dt", "p0", "pmin", "pmax", "gamma_turb", "kpara0", "kperp_
                  "particle_v0", "duu0", "split_ratio", "pmin_split_over_p0", "mu_max")
 INT_PARAMS = ("max_steps", "momentum_dependency", "magnetic_dependency", "time_interpolation",
               "split_particles", "focused")
+CLOSURE_INT = ("closure",)
+CLOSURE_DOUBLE = ("qlt_sigma2", "qlt_spectral_index", "qlt_h0", "qlt_omega0", "qlt_lc")
 
 
 class OracleParams(ctypes.Structure):
     _fields_ = [(name, ctypes.c_double) for name in DOUBLE_PARAMS] + \
-               [(name, ctypes.c_int32) for name in INT_PARAMS]
+               [(name, ctypes.c_int32) for name in INT_PARAMS + CLOSURE_INT] + \
+               [(name, ctypes.c_double) for name in CLOSURE_DOUBLE]
 
 
 class OracleSummary(ctypes.Structure):
@@ -56,7 +59,9 @@ def default_params(**overrides) -> Dict[str, float]:
                   dt_max_rel=1.0e-2, drift_param1=850964.408, drift_param2=13575468.975,
                   charge=-1.0, particle_v0=17.20195, duu0=5578.445, split_ratio=2.0,
                   pmin_split_over_p0=2.0, mu_max=0.99, max_steps=200000, momentum_dependency=1,
-                  magnetic_dependency=1, time_interpolation=1, split_particles=1, focused=0)
+                  magnetic_dependency=1, time_interpolation=1, split_particles=1, focused=0,
+                  closure=0, qlt_sigma2=0.1, qlt_spectral_index=5.0 / 3.0, qlt_h0=1.0e-6,
+                  qlt_omega0=1000.0, qlt_lc=0.05)
     for key, value in overrides.items():
         if key not in values:
             raise KeyError(key)
@@ -68,8 +73,10 @@ def make_params(values: Dict[str, float]) -> OracleParams:
     params = OracleParams()
     for name in DOUBLE_PARAMS:
         setattr(params, name, float(values[name]))
-    for name in INT_PARAMS:
+    for name in INT_PARAMS + CLOSURE_INT:
         setattr(params, name, int(values[name]))
+    for name in CLOSURE_DOUBLE:
+        setattr(params, name, float(values[name]))
     return params
 
 
@@ -116,6 +123,10 @@ class Oracle:
         lib.kpt_oracle_wrap.restype = dbl
         lib.kpt_oracle_wrap.argtypes = [dbl, dbl, dbl, dbl]
         lib.kpt_oracle_sample.argtypes = [vp, vp, vp, i32, dbl, dbl, dbl, i32, vp]
+        lib.kpt_oracle_qlt_dmumu.restype = dbl
+        lib.kpt_oracle_qlt_dmumu.argtypes = [dbl] * 7
+        lib.kpt_oracle_qlt_dmumu_dmu.restype = dbl
+        lib.kpt_oracle_qlt_dmumu_dmu.argtypes = [dbl] * 7
 
     def _error(self) -> str:
         return self.lib.kpt_oracle_last_error().decode()
@@ -197,6 +208,18 @@ class Oracle:
                                       _ptr(particles["level"]), ctypes.byref(out))
         return {name: getattr(out, name) for name, _ in OracleSummary._fields_ if name != "pad"}
 
+    def qlt(self, mu, omega, speed, sigma2, lc, gk, h0):
+        """D_mumu and dD_mumu/dmu (LegencyModel.hpp:557-645) for arrays of inputs."""
+        args = np.broadcast_arrays(*[np.asarray(a, dtype=np.float64)
+                                     for a in (mu, omega, speed, sigma2, lc, gk, h0)])
+        d = np.empty(args[0].shape)
+        dd = np.empty(args[0].shape)
+        for k in np.ndindex(args[0].shape):
+            m, om, sp, s2, l, g, h = (float(a[k]) for a in args)
+            d[k] = self.lib.kpt_oracle_qlt_dmumu(m, om, sp, s2, l, g, h)
+            dd[k] = self.lib.kpt_oracle_qlt_dmumu_dmu(m, d[k], om, sp, l, g, h)
+        return d, dd
+
     def wrap(self, value: float, lower: float, upper: float, width: float) -> float:
         return float(self.lib.kpt_oracle_wrap(value, lower, upper, width))
 
@@ -225,6 +248,8 @@ class ReferenceHarness:
         lib.ref_push_stored.restype = ll
         lib.ref_push_stored.argtypes = [i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, ull, i32, ull,
                                         ull] + [vp] * 9
+        lib.ref_qlt.restype = ll
+        lib.ref_qlt.argtypes = [ll] + [vp] * 9
         lib.ref_main.restype = i32
         lib.ref_main.argtypes = [i32, ctypes.POINTER(ctypes.c_char_p), i32]
 
@@ -293,6 +318,16 @@ class ReferenceHarness:
             lower_field.nx, lower_field.ny, _ptr(xe), _ptr(ye), *[_ptr(a) for a in arrays],
             _ptr(d), _ptr(i), seed, frame, capacity, count,
             *[_ptr(particles[k]) for k in PARTICLE_FIELDS])))
+
+    def qlt(self, mu, omega, speed, sigma2, lc, gk, h0):
+        """The reference's own LegencyModel D_mumu and dD_mumu/dmu."""
+        args = [np.ascontiguousarray(a, dtype=np.float64).ravel() for a in
+                np.broadcast_arrays(mu, omega, speed, sigma2, lc, gk, h0)]
+        n = args[0].size
+        d = np.empty(n)
+        dd = np.empty(n)
+        self._check(self.lib.ref_qlt(n, *[_ptr(a) for a in args], _ptr(d), _ptr(dd)))
+        return d, dd
 
     def main(self, argv, frame_base: int = 0) -> int:
         """Run the reference CLI (in-process); noise frames start at frame_base."""

@@ -19,6 +19,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <limits>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -257,6 +258,46 @@ void parallel_for(const std::string& label, const RangePolicy<ExecSpace>& policy
         context.ordinal = ordinal;
         functor(static_cast<std::size_t>(i));
     }
+}
+
+// Min reducer: identity is the largest value, join takes the minimum.
+template <class T>
+struct Min {
+    T& result;
+    explicit Min(T& target) : result(target) {}
+};
+
+// parallel_reduce with a Min reducer (functor(i, T& update)).
+template <class ExecSpace, class Functor, class T>
+void parallel_reduce(const std::string& label, const RangePolicy<ExecSpace>& policy,
+                     const Functor& functor, const Min<T>& reducer) {
+    (void)ShimImpl::count_launch(label);
+    T value = std::numeric_limits<T>::max();
+    for (std::int64_t i = policy.begin; i < policy.end; ++i) {
+        auto& context = ShimImpl::current_kernel();
+        context.label = label.c_str();
+        context.index = static_cast<std::uint64_t>(i);
+        T local = std::numeric_limits<T>::max();
+        functor(static_cast<std::size_t>(i), local);
+        value = local < value ? local : value;
+    }
+    reducer.result = value;
+}
+
+// parallel_reduce summing into a scalar (functor(i, T& update)), serial order.
+template <class ExecSpace, class Functor, class T,
+          class = std::enable_if_t<std::is_arithmetic_v<T>>>
+void parallel_reduce(const std::string& label, const RangePolicy<ExecSpace>& policy,
+                     const Functor& functor, T& result) {
+    (void)ShimImpl::count_launch(label);
+    T value = T(0);
+    for (std::int64_t i = policy.begin; i < policy.end; ++i) {
+        auto& context = ShimImpl::current_kernel();
+        context.label = label.c_str();
+        context.index = static_cast<std::uint64_t>(i);
+        functor(static_cast<std::size_t>(i), value);
+    }
+    result = value;
 }
 
 inline void fence() {}

@@ -7,6 +7,7 @@
 
 namespace Kokkos {
 using std::abs;
+using std::cos;
 using std::exp;
 using std::floor;
 using std::isfinite;

@@ -533,6 +533,55 @@ static double clamp_mu(double v, double m) {
 }
 
 static const double kSqrt3 = 1.7320508075688772935;
+static const double kPi = 3.141592653589793238462643383279502884;
+
+/* pitch_angle_spectrum_normalization (LegencyModel.hpp:539-552). */
+static double qlt_normalization(double spectral_index) {
+    const double sine_value = sin(kPi / spectral_index);
+    return spectral_index * sine_value / kPi;
+}
+
+double kpt_oracle_qlt_dmumu(double mu, double omega, double speed, double sigma2, double lc,
+                            double spectral_index, double h0) {
+    const double one_minus_mu2 = 1.0 - mu * mu;
+    if (one_minus_mu2 <= 0.0) {
+        return 0.0;
+    }
+    const double regularized_abs_mu = (mu >= 0.0 ? mu : -mu) + h0;
+    const double gamma_k = spectral_index;
+    const double xi = omega * lc / speed;
+    const double abs_mu_gamma = pow(regularized_abs_mu, gamma_k);
+    const double xi_gamma = pow(xi, gamma_k);
+    const double denominator = abs_mu_gamma + xi_gamma;
+    const double prefactor = 0.25 * kPi * omega * sigma2 * qlt_normalization(gamma_k);
+    return prefactor * one_minus_mu2 * xi * pow(regularized_abs_mu, gamma_k - 1.0) / denominator;
+}
+
+double kpt_oracle_qlt_dmumu_dmu(double mu, double dmumu, double omega, double speed, double lc,
+                                double spectral_index, double h0) {
+    if (dmumu == 0.0) {
+        return 0.0;
+    }
+    const double sign_mu = mu > 0.0 ? 1.0 : (mu < 0.0 ? -1.0 : 0.0);
+    if (sign_mu == 0.0) {
+        return 0.0;
+    }
+    const double one_minus_mu2 = 1.0 - mu * mu;
+    if (one_minus_mu2 <= 0.0) {
+        return 0.0;
+    }
+    const double regularized_abs_mu = (mu >= 0.0 ? mu : -mu) + h0;
+    const double gamma_k = spectral_index;
+    const double xi = omega * lc / speed;
+    const double abs_mu_gamma = pow(regularized_abs_mu, gamma_k);
+    const double xi_gamma = pow(xi, gamma_k);
+    const double denominator = abs_mu_gamma + xi_gamma;
+    const double shape_derivative =
+        sign_mu * ((gamma_k - 1.0) / regularized_abs_mu -
+                   gamma_k * pow(regularized_abs_mu, gamma_k - 1.0) / denominator);
+    const double endpoint_derivative = -2.0 * mu / one_minus_mu2;
+    return dmumu * (endpoint_derivative + shape_derivative);
+}
 
 /* StochasticSampler::uniform_sqrt3 (RandomManager.hpp:111-114). */
 static double uniform_sqrt3(kpt_oracle_stream* s) {
@@ -829,26 +878,37 @@ static void push_focused_one(const kpt_oracle_grid* g, const double* lower_table
         double dmu_dt = speed * div_bnorm + pitch_mu * divv - 3.0 * pitch_mu * bb_gradv -
                         2.0 * bv_gradv / speed;
         dmu_dt *= 0.5 * (1.0 - mu2);
-        const double abs_mu = fabs(pitch_mu);
-        const double dtmp = pow(abs_mu, s->gamma_turb - 1.0) + d->h0;
-        double duu = s->duu0 * (1.0 - mu2) * dtmp;
+        double duu = 0.0;
         double duu_du = 0.0;
-        if (pitch_mu > 0.0) {
-            duu_du = s->duu0 * (-2.0 * pitch_mu * dtmp +
-                                (1.0 - mu2) * pow(abs_mu, s->gamma_turb - 2.0));
-        } else if (pitch_mu < 0.0) {
-            duu_du = s->duu0 * (-2.0 * pitch_mu * dtmp -
-                                (1.0 - mu2) * pow(abs_mu, s->gamma_turb - 2.0));
+        if (s->closure == 1) {
+            /* slab QLT closure (extension): LegencyModel's D_mumu, dD_mumu/dmu */
+            const double lorentz = sqrt(1.0 + p * p);
+            const double omega = s->qlt_omega0 * b / lorentz;
+            duu = kpt_oracle_qlt_dmumu(pitch_mu, omega, speed, s->qlt_sigma2, s->qlt_lc,
+                                       s->qlt_spectral_index, s->qlt_h0);
+            duu_du = kpt_oracle_qlt_dmumu_dmu(pitch_mu, duu, omega, speed, s->qlt_lc,
+                                              s->qlt_spectral_index, s->qlt_h0);
+        } else {
+            const double abs_mu = fabs(pitch_mu);
+            const double dtmp = pow(abs_mu, s->gamma_turb - 1.0) + d->h0;
+            duu = s->duu0 * (1.0 - mu2) * dtmp;
+            if (pitch_mu > 0.0) {
+                duu_du = s->duu0 * (-2.0 * pitch_mu * dtmp +
+                                    (1.0 - mu2) * pow(abs_mu, s->gamma_turb - 2.0));
+            } else if (pitch_mu < 0.0) {
+                duu_du = s->duu0 * (-2.0 * pitch_mu * dtmp -
+                                    (1.0 - mu2) * pow(abs_mu, s->gamma_turb - 2.0));
+            }
+            double duu_norm = 1.0;
+            if (s->magnetic_dependency == 1) {
+                duu_norm *= pow(b, 2.0 - s->gamma_turb);
+            }
+            if (s->momentum_dependency == 1) {
+                duu_norm *= pow(p / s->p0, s->gamma_turb - 1.0);
+            }
+            duu *= duu_norm;
+            duu_du *= duu_norm;
         }
-        double duu_norm = 1.0;
-        if (s->magnetic_dependency == 1) {
-            duu_norm *= pow(b, 2.0 - s->gamma_turb);
-        }
-        if (s->momentum_dependency == 1) {
-            duu_norm *= pow(p / s->p0, s->gamma_turb - 1.0);
-        }
-        duu *= duu_norm;
-        duu_du *= duu_norm;
         dmu_dt += duu_du;
         if (!isfinite(dmu_dt) || !isfinite(duu) || duu < 0.0) {
             st = 2;

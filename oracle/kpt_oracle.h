@@ -46,6 +46,15 @@ typedef struct {
     int32_t time_interpolation;
     int32_t split_particles;
     int32_t focused;
+    /* focused scattering closure: 0 driver (reference), 1 slab QLT
+     * (LegencyModel.hpp:539-645) with Omega = qlt_omega0 |B| / sqrt(1+p^2),
+     * v = particle_v0 p / p0 */
+    int32_t closure;
+    double qlt_sigma2;
+    double qlt_spectral_index;
+    double qlt_h0;
+    double qlt_omega0;
+    double qlt_lc;
 } kpt_oracle_params;
 
 /* 2D periodic grid with two ghost layers.  An axis whose edges are uniform
@@ -139,6 +148,13 @@ void kpt_oracle_histogram(double pmin, double pmax, int nbins, uint64_t count, c
 void kpt_oracle_summarize(uint64_t count, const double* p, const double* step_dt,
                           const double* weight, const int32_t* status,
                           const int32_t* split_level, kpt_oracle_summary* out);
+
+/* pitch_angle_diffusion_coefficient (LegencyModel.hpp:557-594). */
+double kpt_oracle_qlt_dmumu(double mu, double omega, double speed, double sigma2, double lc,
+                            double spectral_index, double h0);
+/* pitch_angle_diffusion_derivative (LegencyModel.hpp:599-645). */
+double kpt_oracle_qlt_dmumu_dmu(double mu, double dmumu, double omega, double speed, double lc,
+                                double spectral_index, double h0);
 
 /* wrap_periodic_coordinate (src/main.cpp:642-665). */
 double kpt_oracle_wrap(double value, double lower, double upper, double width);

@@ -16,6 +16,8 @@
 
 #include <string>
 
+#include "LegencyModel.hpp"
+
 namespace {
 
 thread_local std::string g_last_error;
@@ -401,6 +403,23 @@ long long ref_push_stored(int nx, int ny, const double* x_edges, const double* y
         g_last_error = error.what();
         return -1;
     }
+}
+
+// The reference's slab quasi-linear pitch-angle scattering closure
+// (include/LegencyModel.hpp:557-645) on arrays of inputs.
+long long ref_qlt(long long n, const double* mu, const double* omega, const double* speed,
+                  const double* sigma2, const double* lc, const double* gk, const double* h0,
+                  double* d_out, double* dd_out) {
+    for (long long k = 0; k < n; ++k) {
+        LegencyModel::PitchAngleScatteringParameters parameters;
+        parameters.spectral_index = gk[k];
+        parameters.resonance_regularization_h0 = h0[k];
+        d_out[k] = LegencyModel::pitch_angle_diffusion_coefficient(mu[k], omega[k], speed[k],
+                                                                   sigma2[k], lc[k], parameters);
+        dd_out[k] = LegencyModel::pitch_angle_diffusion_derivative(mu[k], d_out[k], omega[k],
+                                                                   speed[k], lc[k], parameters);
+    }
+    return n;
 }
 
 // The reference CLI entry point itself.  Noise frames are keyed as

@@ -51,12 +51,11 @@ def load_golden(name: str) -> dict:
 
 
 def golden_params(data: dict) -> dict:
-    names = [str(n) for n in data["param_names"]]
-    values = data["param_values"]
-    out = {}
-    for n, v in zip(names, values):
-        out[n] = int(v) if n in ("max_steps", "momentum_dependency", "magnetic_dependency",
-                                 "time_interpolation", "split_particles", "focused") else float(v)
+    """A fixture's parameters over the oracle defaults (closure fields included)."""
+    binding = importlib.import_module("binding")
+    out = binding.default_params()
+    for n, v in zip([str(n) for n in data["param_names"]], data["param_values"]):
+        out[n] = int(v) if isinstance(out.get(n), int) else float(v)
     return out
 
 

@@ -170,6 +170,25 @@ def make_split(ref, out_dir):
                         **particles_arrays("small_end", small, count + 40))
 
 
+def make_qlt(ref, out_dir):
+    """The reference's LegencyModel slab-QLT D_mumu and dD_mumu/dmu on a
+    spread of inputs (including mu = 0, +-1 and the regularised edge)."""
+    rng = np.random.default_rng(11)
+    n = 4000
+    mu = np.concatenate([rng.uniform(-1, 1, n), [0.0, -0.0, 1.0, -1.0, 0.999999, -0.999999,
+                                                 1e-9, -1e-9, 1e-6, -1e-6]])
+    m = mu.size
+    omega = 10 ** rng.uniform(0, 4, m)
+    speed = 10 ** rng.uniform(-1, 3, m)
+    sigma2 = 10 ** rng.uniform(-2, 0, m)
+    lc = rng.uniform(0.01, 0.2, m)
+    gk = rng.uniform(1.5, 2.0, m)
+    h0 = np.where(rng.uniform(size=m) < 0.5, 1e-6, 1e-3)
+    d, dd = ref.qlt(mu, omega, speed, sigma2, lc, gk, h0)
+    np.savez_compressed(os.path.join(out_dir, "qlt_closure.npz"), mu=mu, omega=omega,
+                        speed=speed, sigma2=sigma2, lc=lc, gk=gk, h0=h0, dmumu=d, dmumu_dmu=dd)
+
+
 def make_cli(ref, out_dir):
     cli_dir = os.path.join(out_dir, "cli")
     if os.path.isdir(cli_dir):
@@ -222,6 +241,7 @@ def main() -> None:
     make_push(ref, out_dir, "focused_uniform", True, False, 160, 3, {})
     make_push(ref, out_dir, "focused_stretched", True, True, 96, 1, {})
     make_split(ref, out_dir)
+    make_qlt(ref, out_dir)
     make_cli(ref, out_dir)
 
 

@@ -346,3 +346,35 @@ def test_bad_arguments_raise(ctx, kpt, fields_mod):
         ctx.push_interval(parts, lower, focused, kpt.default_settings(), 0, 1)
     with pytest.raises(kpt.KptError):
         ctx.push_interval(parts, lower, lower, kpt.default_settings(charge=0.0), 0, 1)
+
+
+@pytest.mark.parametrize("case", ["focused_uniform", "focused_stretched"])
+def test_push_f64_qlt_closure_matches_oracle(ctx, kpt, oracle, case):
+    """Focused push with the slab-QLT closure (LegencyModel D_mumu, dD_mumu/dmu;
+    the oracle's closure is bit-identical to the reference's functions)."""
+    data = load_golden(f"push_{case}.npz")
+    params = golden_params(data)
+    params.update(closure=1, max_steps=FOCUSED_PARITY_STEPS)
+    lower_f = golden_field(data, "lower")
+    upper_f = golden_field(data, "upper")
+    count = int(data["count"])
+    frame, seed = int(data["frame"]), int(data["seed"])
+    start = golden_particles(data, "start")
+    grid = oracle.grid(lower_f.x_edges, lower_f.y_edges)
+    want = {k: v.copy() for k, v in start.items()}
+    steps = oracle.push(grid, oracle.table(lower_f, True), oracle.table(upper_f, True), params,
+                        frame * params["mhd_dt"], frame, seed, count, want)
+    widths = (grid.upper[0] - grid.lower[0], grid.upper[1] - grid.lower[1])
+    oracle.free_grid(grid)
+    settings = kpt.settings_from_dict(params)
+    lower = ctx.field(lower_f, kpt.TABLE_FOCUSED21, kpt.PRECISION_F64)
+    upper = ctx.field(upper_f, kpt.TABLE_FOCUSED21, kpt.PRECISION_F64)
+    parts = ctx.particles(count)
+    parts.upload(start, count)
+    stats = ctx.push_interval(parts, lower, upper, settings, frame, seed)
+    got = parts.download()
+    errs = trajectory_errors(got, want, widths[0], widths[1], True)
+    for name, err in errs.items():
+        assert err <= F64_REL, (name, err)
+    assert np.array_equal(got["status"], want["status"])
+    assert stats.particle_steps == int(steps.sum())

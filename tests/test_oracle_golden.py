@@ -89,3 +89,14 @@ def test_wrap_matches_reference_branches(oracle):
     for value, expect in ((0.5, 0.5), (1.0, -1.0), (-1.0, -1.0), (1.5, -0.5), (-1.5, 0.5),
                           (7.25, -0.75), (-9.0, -1.0)):
         assert oracle.wrap(value, lower, upper, width) == pytest.approx(expect, abs=1e-15)
+
+
+def test_qlt_closure_bit_exact(oracle):
+    """Slab-QLT D_mumu and dD_mumu/dmu: the reference's LegencyModel functions."""
+    data = load_golden("qlt_closure.npz")
+    d, dd = oracle.qlt(data["mu"], data["omega"], data["speed"], data["sigma2"], data["lc"],
+                       data["gk"], data["h0"])
+    assert np.array_equal(d, data["dmumu"])
+    assert np.array_equal(dd, data["dmumu_dmu"])
+    assert np.all(data["dmumu"] >= 0.0)
+    assert data["dmumu"][np.abs(data["mu"]) == 1.0].max() == 0.0
