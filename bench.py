@@ -1,23 +1,29 @@
 """Benchmark: particle-steps/s of the interval push on one GB300.
 
-Workload (the scale configuration): a 1024 x 2048 compact field on stretched
-y edges (dy proportional to 1 + 4 (y/2)^2 over [-2, 2], x uniform on [-1, 1]),
-Harris sheet plus 8 magnetic islands (psi = 0.1 cos(4 pi x) exp(-y^2/0.04)),
-two frames with seeded 1 % multiplicative noise; a particle population
-injected uniformly over the domain (p = p0, times spread over the first
-interval) and pushed across consecutive MHD intervals.  One step = one
-``kpt_push_interval`` over the whole population (Parker transport; the mixed
-precision path is the headline, the plain FP64 push is measured beside it).
+Workload: a 1024 x 2048 compact field on stretched y edges (dy proportional
+to 1 + 4 (y/2)^2 over [-2, 2], x uniform on [-1, 1]), Harris sheet plus 8
+magnetic islands (psi = 0.1 cos(4 pi x) exp(-y^2/0.04)), two frames with
+seeded 1 % multiplicative noise; a particle population injected uniformly
+over the domain (p = p0, pitch cosine uniform on [-1, 1], times spread over
+the first interval) and pushed across consecutive MHD intervals.  One step =
+one cell sort + one ``kpt_push_interval`` over the whole population.
+
+Headline: focused transport with the learned slab-QLT closure (sigma^2 =
+0.1, gamma_k = 5/3), mixed precision, network trained on the GPU before the
+timed region; beside it the plain FP64 push with the plain closure (the
+baseline the metric names), the mixed push with the plain closure (what the
+network gains or costs), the spectrum L1 of the headline against FP64 after
+one interval from the same start, and the Parker legs (mixed and FP64).
 
 Timing: CUDA events on the library's stream around exactly K steps after W
-warm-up steps; the tables (2 x 135 MB mixed, 2 x 270 MB FP64) exceed the
-129 MB L2, so no flush is needed between steps.  ``e2e`` is the same metric
-through the C ABI with host buffers: every step uploads the particle state
-from pinned host memory, pushes and downloads it.
+warm-up steps; the tables (2 x 200 MB mixed focused) exceed the 129 MB L2,
+so no flush is needed between steps.  ``e2e`` is the headline metric through
+the C ABI with host buffers: every step uploads the particle state from
+host memory, sorts, pushes and downloads it.
 
 ``--impl reference`` times the CPU baseline: the oracle restatement of the
-reference push (bit-identical to the reference's own code on the same
-inputs), OpenMP on all host cores, on a bounded sample of the same workload.
+focused push with the plain closure, OpenMP on all host cores, on a bounded
+sample of the same workload.
 """
 from __future__ import annotations
 
@@ -41,7 +47,13 @@ NX, NY = 1024, 2048
 SEED = 114514
 START_FRAME = 100
 METRIC = "particle-steps/s, 1 GB300: mixed+surrogate vs plain FP64 at <=1% spectrum error"
-BYTES_PER_STEP = {"f64": 1024, "mixed": 512}  # 2 frames x 4 corners x 16 comps x 8|4 B
+# algorithmic table bytes per particle-step: 2 frames x 4 corners x comps x 8|4 B
+BYTES_PER_STEP = {"focused_mixed": 2 * 4 * 21 * 4, "focused_f64": 2 * 4 * 21 * 8,
+                  "parker_mixed": 2 * 4 * 16 * 4, "parker_f64": 2 * 4 * 16 * 8}
+# tensor-core work of the fused network per particle-step (padded mma tiles:
+# K 5 -> 16 and N 3 -> 8): 2 x (16 x 64 + 64 x 64 + 64 x 8) flop
+TENSOR_FLOP_PER_STEP = 2 * (16 * 64 + 64 * 64 + 64 * 8)
+PROFILE = os.path.join(ROOT, "profiles", "push_refill_surrogate_focused_1024x2048.md")
 
 
 def make_workload():
@@ -49,11 +61,6 @@ def make_workload():
     f0 = fields.harris_field(NX, NY, y_edges=ye, island_amplitude=0.1, noise=0.01, seed=1)
     f1 = fields.harris_field(NX, NY, y_edges=ye, island_amplitude=0.1, noise=0.01, seed=2)
     return f0, f1
-
-
-def settings_dict(kpt):
-    s = kpt.default_settings(kperp_over_kpara=0.05, split_ratio=1.2)
-    return s
 
 
 def read_peaks():
@@ -119,121 +126,173 @@ class ClockSampler:
                 "sm_max_mhz": smax or None, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def run_gpu(args):
+def _timed_intervals(ctx, stream, parts, lower, upper, settings, steps, warmup, sort_tile,
+                     first_frame):
+    """W untimed + K timed interval pushes; returns (total_ms, kernel_ms, steps, clocks)."""
+    import torch
+    frame = first_frame
+    for _ in range(warmup):
+        if sort_tile > 0:
+            ctx.sort(parts, lower, sort_tile, sort_tile)
+        ctx.push_interval(parts, lower, upper, settings, frame, SEED)
+        frame += 1
+    torch.cuda.synchronize()
+    begin = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    kernel_ms, particle_steps = [], 0
+    with ClockSampler() as clocks:
+        begin.record(stream)
+        for _ in range(steps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            if sort_tile > 0:
+                ctx.sort(parts, lower, sort_tile, sort_tile)
+            e0.record(stream)
+            stats = ctx.push_interval(parts, lower, upper, settings, frame, SEED)
+            e1.record(stream)
+            particle_steps += stats.particle_steps
+            frame += 1
+            e1.synchronize()
+            kernel_ms.append(e0.elapsed_time(e1))
+        end.record(stream)
+        end.synchronize()
+    return begin.elapsed_time(end), kernel_ms, particle_steps, clocks.summary()
+
+
+def _spectrum(p, w, status, nbins=64, pmin=1e-2, pmax=1e1):
+    active = (status == 0) & (p >= pmin) & (p <= pmax)
+    bins = np.floor((np.log(p[active]) - np.log(pmin)) * nbins / np.log(pmax / pmin))
+    bins = np.clip(bins.astype(int), 0, nbins - 1)
+    return np.bincount(bins, weights=w[active], minlength=nbins)
+
+
+def focused_settings(kpt, closure):
+    return kpt.default_settings(kperp_over_kpara=0.05, split_ratio=1.2, focused=1,
+                                closure=closure, qlt_sigma2=0.1, qlt_spectral_index=5.0 / 3.0)
+
+
+def run_focused(args, f0, f1):
+    """Headline: mixed + surrogate; beside it FP64 plain and mixed plain."""
     import torch
     kpt = importlib.import_module("kokkos-particletransport_gb300")
-    f0, f1 = make_workload()
-    settings = settings_dict(kpt)
     ctx = kpt.Context(0)
     stream = torch.cuda.current_stream()
     ctx.set_stream(stream.cuda_stream)
     n = args.particles
-    results = {}
-    for label, precision in (("mixed", kpt.PRECISION_MIXED), ("f64", kpt.PRECISION_F64)):
+    plain = focused_settings(kpt, kpt.CLOSURE_QLT)
+    learned = focused_settings(kpt, kpt.CLOSURE_SURROGATE)
+    nets, out = {}, {"train": {}}
+    for label, element in (("surrogate", kpt.SURROGATE_BF16), ("surrogate_fp16",
+                                                               kpt.SURROGATE_FP16)):
+        t0 = time.perf_counter()
+        nets[label] = ctx.train_surrogate(learned, samples=args.train_samples,
+                                          steps=args.train_steps, element_type=element)
+        out["train"][label] = {"seconds": time.perf_counter() - t0,
+                               "final_loss": nets[label].final_loss,
+                               "samples": args.train_samples, "adam_steps": args.train_steps}
+    spectra = {}
+    legs = (("surrogate", kpt.PRECISION_MIXED, learned, args.steps, args.warmup),
+            ("surrogate_fp16", kpt.PRECISION_MIXED, learned, args.steps, args.warmup),
+            ("mixed_qlt", kpt.PRECISION_MIXED, plain, args.steps, args.warmup),
+            ("f64", kpt.PRECISION_F64, plain, args.f64_steps, 1))
+    start = None
+    for label, precision, settings, steps, warmup in legs:
+        if label in nets:
+            ctx.set_surrogate(nets[label])
+        lower = ctx.field(f0, kpt.TABLE_FOCUSED21, precision)
+        upper = ctx.field(f1, kpt.TABLE_FOCUSED21, precision)
+        parts = ctx.particles(n)
+        if start is None:
+            ctx.inject(parts, lower, settings, n, START_FRAME, SEED)
+            start = parts.download()
+        else:
+            parts.upload(start, n)
+        # spectrum after one interval from the common start
+        if args.sort_tile > 0:
+            ctx.sort(parts, lower, args.sort_tile, args.sort_tile)
+        ctx.push_interval(parts, lower, upper, settings, START_FRAME, SEED)
+        one = parts.download(n)
+        spectra[label] = _spectrum(one["p"], one["w"], one["status"])
+        ctx.surrogate_judge()
+        total_ms, kernel_ms, psteps, clocks = _timed_intervals(
+            ctx, stream, parts, lower, upper, settings, steps, max(0, warmup - 1),
+            args.sort_tile, START_FRAME + 1)
+        leg = {"value": psteps / (total_ms / 1e3), "ms_per_step": total_ms / steps,
+               "kernel_ms": float(np.mean(kernel_ms)), "particle_steps": int(psteps),
+               "steps": steps, "clocks": clocks}
+        if label in nets:
+            leg["judge"] = ctx.surrogate_judge()
+        if label == "surrogate":
+            # e2e through the C ABI with host buffers
+            host = {k: v.copy() for k, v in start.items()}
+            e2e_steps = 0
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for k in range(steps):
+                parts.upload(host, n)
+                if args.sort_tile > 0:
+                    ctx.sort(parts, lower, args.sort_tile, args.sort_tile)
+                stats = ctx.push_interval(parts, lower, upper, settings, START_FRAME + k, SEED)
+                host = parts.download(n)
+                e2e_steps += stats.particle_steps
+            leg["e2e"] = e2e_steps / (time.perf_counter() - t0)
+            leg["state_bytes"] = n * (7 * 8 + 2 * 4)
+        out[label] = leg
+        for obj in (lower, upper, parts):
+            obj.close()
+    ref = spectra["f64"]
+    for label in ("surrogate", "surrogate_fp16", "mixed_qlt"):
+        out[label]["spectrum_l1_vs_f64"] = float(np.abs(spectra[label] - ref).sum() / ref.sum())
+    ctx.set_surrogate(None)
+    for net in nets.values():
+        net.close()
+    ctx.close()
+    return out
+
+
+def run_parker(args, f0, f1):
+    """Parker transport on the same field: mixed and FP64."""
+    import torch
+    kpt = importlib.import_module("kokkos-particletransport_gb300")
+    settings = kpt.default_settings(kperp_over_kpara=0.05, split_ratio=1.2)
+    ctx = kpt.Context(0)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    n = args.parker_particles
+    out = {}
+    for label, precision, steps in (("mixed", kpt.PRECISION_MIXED, args.steps),
+                                    ("f64", kpt.PRECISION_F64, args.f64_steps)):
         lower = ctx.field(f0, kpt.TABLE_PARKER16, precision)
         upper = ctx.field(f1, kpt.TABLE_PARKER16, precision)
         parts = ctx.particles(n)
         ctx.inject(parts, lower, settings, n, START_FRAME, SEED)
-        start = parts.download()
-        frame = START_FRAME
-        for _ in range(args.warmup):
-            if args.sort_tile > 0:
-                ctx.sort(parts, lower, args.sort_tile, args.sort_tile)
-            ctx.push_interval(parts, lower, upper, settings, frame, SEED)
-            frame += 1
-        torch.cuda.synchronize()
-        begin = torch.cuda.Event(enable_timing=True)
-        end = torch.cuda.Event(enable_timing=True)
-        kernel_ms = []
-        steps = 0
-        with ClockSampler() as clocks:
-            begin.record(stream)
-            for _ in range(args.steps):
-                e0 = torch.cuda.Event(enable_timing=True)
-                e1 = torch.cuda.Event(enable_timing=True)
-                if args.sort_tile > 0:
-                    ctx.sort(parts, lower, args.sort_tile, args.sort_tile)
-                e0.record(stream)
-                stats = ctx.push_interval(parts, lower, upper, settings, frame, SEED)
-                e1.record(stream)
-                steps += stats.particle_steps
-                frame += 1
-                e1.synchronize()
-                kernel_ms.append(e0.elapsed_time(e1))
-            end.record(stream)
-            end.synchronize()
-        total_ms = begin.elapsed_time(end)
-        # e2e: through the C ABI with host buffers (H2D upload, push, D2H download)
-        host = {k: v.copy() for k, v in start.items()}
-        e2e_steps = 0
-        t0 = time.perf_counter()
-        for k in range(args.steps):
-            parts.upload(host, n)
-            if args.sort_tile > 0:
-                ctx.sort(parts, lower, args.sort_tile, args.sort_tile)
-            stats = ctx.push_interval(parts, lower, upper, settings, START_FRAME + k, SEED)
-            host = parts.download(n)
-            e2e_steps += stats.particle_steps
-        e2e_s = time.perf_counter() - t0
-        results[label] = dict(total_ms=total_ms, kernel_ms=kernel_ms, steps=steps,
-                              clocks=clocks.summary(), e2e_steps=e2e_steps, e2e_s=e2e_s,
-                              state_bytes=n * (7 * 8 + 2 * 4))
-        for obj in (lower, upper, parts):
-            obj.close()
-    ctx.close()
-    return results
-
-
-def run_focused(args):
-    """Focused transport with the slab-QLT closure on the same field: one
-    interval push of the population per step, FP64 and mixed."""
-    import torch
-    kpt = importlib.import_module("kokkos-particletransport_gb300")
-    f0, f1 = make_workload()
-    settings = kpt.default_settings(kperp_over_kpara=0.05, focused=1, closure=kpt.CLOSURE_QLT)
-    ctx = kpt.Context(0)
-    stream = torch.cuda.current_stream()
-    ctx.set_stream(stream.cuda_stream)
-    out = {}
-    for label, precision in (("mixed", kpt.PRECISION_MIXED), ("f64", kpt.PRECISION_F64)):
-        n = args.focused_particles
-        lower = ctx.field(f0, kpt.TABLE_FOCUSED21, precision)
-        upper = ctx.field(f1, kpt.TABLE_FOCUSED21, precision)
-        parts = ctx.particles(n)
-        ctx.inject(parts, lower, settings, n, START_FRAME, SEED)
-        start = parts.download()
-        # warm-up: one interval on a copy of the population
-        ctx.sort(parts, lower, 16, 16)
-        ctx.push_interval(parts, lower, upper, settings, START_FRAME, SEED)
-        parts.upload(start, n)
-        ctx.sort(parts, lower, 16, 16)
-        torch.cuda.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        stats = ctx.push_interval(parts, lower, upper, settings, START_FRAME, SEED)
-        e1.record(stream)
-        e1.synchronize()
-        ms = e0.elapsed_time(e1)
-        out[label] = {"value": stats.particle_steps / (ms / 1e3), "ms": ms,
-                      "particle_steps": int(stats.particle_steps), "particles": n}
+        total_ms, kernel_ms, psteps, _ = _timed_intervals(
+            ctx, stream, parts, lower, upper, settings, steps, 1, args.sort_tile, START_FRAME)
+        out[label] = {"value": psteps / (total_ms / 1e3), "ms_per_step": total_ms / steps,
+                      "kernel_ms": float(np.mean(kernel_ms)), "particle_steps": int(psteps),
+                      "particles": n}
         for obj in (lower, upper, parts):
             obj.close()
     ctx.close()
     out["speedup_mixed_over_f64"] = out["mixed"]["value"] / out["f64"]["value"]
+    achieved = (out["mixed"]["particle_steps"] / args.steps) * BYTES_PER_STEP["parker_mixed"] / \
+        (out["mixed"]["kernel_ms"] / 1e3) / 1e9
+    out["mixed"]["algorithmic_gbs"] = achieved
     return out
 
 
 def cpu_baseline(particles: int, steps: int = 1):
-    """Oracle restatement (OpenMP, all host threads) on a bounded sample."""
+    """Oracle restatement of the focused push with the plain slab-QLT closure
+    (OpenMP, all host threads) on a bounded sample of the headline workload."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     binding = importlib.import_module("binding")
-    kpt = importlib.import_module("kokkos-particletransport_gb300")
     f0, f1 = make_workload()
     oracle = binding.Oracle()
-    params = binding.default_params(kperp_over_kpara=0.05, split_ratio=1.2)
+    params = binding.default_params(kperp_over_kpara=0.05, split_ratio=1.2, focused=1,
+                                    closure=1, qlt_sigma2=0.1,
+                                    qlt_spectral_index=5.0 / 3.0)
     grid = oracle.grid(f0.x_edges, f0.y_edges)
-    lo, up = oracle.table(f0), oracle.table(f1)
+    lo, up = oracle.table(f0, True), oracle.table(f1, True)
     parts = binding.empty_particles(particles)
     oracle.inject(grid, params, START_FRAME * 0.1, START_FRAME, SEED, particles, 0, particles,
                   parts)
@@ -247,8 +306,19 @@ def cpu_baseline(particles: int, steps: int = 1):
         total_steps += int(s.sum())
     elapsed = time.perf_counter() - t0
     oracle.free_grid(grid)
-    del kpt
     return total_steps / elapsed, threads, elapsed, total_steps
+
+
+def profiled_traffic():
+    """DRAM bytes per particle-step of the headline kernel from its committed
+    ncu summary (a line 'dram_bytes_per_particle_step: X'), or None."""
+    if not os.path.exists(PROFILE):
+        return None
+    with open(PROFILE) as stream:
+        for line in stream:
+            if line.strip().startswith("dram_bytes_per_particle_step:"):
+                return float(line.split(":", 1)[1])
+    return None
 
 
 def main():
@@ -257,17 +327,24 @@ def main():
     parser.add_argument("--steps", type=int, default=5)
     parser.add_argument("--warmup", type=int, default=3)
     parser.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    parser.add_argument("--particles", type=int, default=1 << 20)
-    parser.add_argument("--cpu-particles", type=int, default=1 << 15)
-    parser.add_argument("--focused-particles", type=int, default=1 << 16,
-                        help="population of the focused/QLT leg (0 skips it)")
+    parser.add_argument("--particles", type=int, default=1 << 18,
+                        help="focused population (headline)")
+    parser.add_argument("--f64-steps", type=int, default=2,
+                        help="timed intervals of the FP64 legs")
+    parser.add_argument("--parker-particles", type=int, default=1 << 20,
+                        help="Parker population (0 skips the Parker legs)")
+    parser.add_argument("--train-samples", type=int, default=2000000)
+    parser.add_argument("--train-steps", type=int, default=16000)
+    parser.add_argument("--cpu-particles", type=int, default=1 << 16)
     parser.add_argument("--sort-tile", type=int, default=16,
                         help="cell-sort tile (cells) before each push; 0 disables")
     args = parser.parse_args()
     rank = int(os.environ.get("RANK", "0"))
-    config = {"workload": f"parker push, {NX}x{NY} stretched-y Harris+islands field, "
-                          f"{args.particles} particles, consecutive intervals",
-              "nx": NX, "ny": NY, "particles": args.particles, "transport": "parker",
+    config = {"workload": f"focused push, learned slab-QLT closure (sigma2 0.1, gamma_k 5/3), "
+                          f"{NX}x{NY} stretched-y Harris+islands field, {args.particles} "
+                          f"particles, consecutive intervals",
+              "nx": NX, "ny": NY, "particles": args.particles, "transport": "focused",
+              "closure": "surrogate (5-64-64-3 MLP, BF16 tensor cores, FP32 accumulation)",
               "l2": "tables larger than L2 (no flush)", "sort_tile": args.sort_tile}
     if args.impl == "reference":
         if rank != 0:
@@ -275,50 +352,65 @@ def main():
         value, threads, elapsed, total = cpu_baseline(args.cpu_particles, max(1, args.steps))
         line = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "impl": "reference",
+                "ms_per_step": elapsed * 1e3 / max(1, args.steps),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "dtype": "f64", "data": "synthetic", "config": dict(config,
-                                                                    particles=args.cpu_particles),
+                "dtype": "f64", "data": "synthetic",
+                "config": dict(config, particles=args.cpu_particles,
+                               closure="plain slab QLT (FP64 oracle restatement)"),
                 "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": threads,
                                  "kind": "port",
-                                 "sample": f"{args.cpu_particles} particles x {args.steps} "
-                                           f"intervals ({total} particle-steps, {elapsed:.1f} s)"},
+                                 "sample": f"{args.cpu_particles} particles x {max(1, args.steps)}"
+                                           f" intervals ({total} particle-steps, "
+                                           f"{elapsed:.1f} s)"},
                 "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
-    results = run_gpu(args)
-    focused = run_focused(args) if args.focused_particles > 0 else None
+    f0, f1 = make_workload()
+    focused = run_focused(args, f0, f1)
+    parker = run_parker(args, f0, f1) if args.parker_particles > 0 else None
     peak, peak_kind = read_peaks()
-    mixed, f64 = results["mixed"], results["f64"]
-    value = mixed["steps"] / (mixed["total_ms"] / 1e3)
-    f64_value = f64["steps"] / (f64["total_ms"] / 1e3)
-    kernel_s = np.mean(mixed["kernel_ms"]) / 1e3
-    steps_per_launch = mixed["steps"] / args.steps
-    achieved = steps_per_launch * BYTES_PER_STEP["mixed"] / kernel_s / 1e9
+    head, f64, mixed_qlt = focused["surrogate"], focused["f64"], focused["mixed_qlt"]
+    kernel_s = head["kernel_ms"] / 1e3
+    steps_per_launch = head["particle_steps"] / head["steps"]
+    achieved = steps_per_launch * BYTES_PER_STEP["focused_mixed"] / kernel_s / 1e9
+    per_step_traffic = profiled_traffic()
     cpu_value, cpu_threads, cpu_elapsed, cpu_total = cpu_baseline(args.cpu_particles, 1)
     line = {
-        "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": mixed["total_ms"] / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64 (mixed)",
+        "metric": METRIC, "value": head["value"], "unit": "particle-steps/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": head["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+bf16 network, f64 accumulation",
         "data": "synthetic", "config": config,
-        "plain_f64": {"value": f64_value, "ms_per_step": f64["total_ms"] / args.steps,
-                      "speedup_mixed_over_f64": value / f64_value},
+        "plain_f64": {"value": f64["value"], "ms_per_step": f64["ms_per_step"],
+                      "steps": f64["steps"],
+                      "speedup_surrogate_over_f64": head["value"] / f64["value"]},
+        "mixed_plain_qlt": {"value": mixed_qlt["value"], "ms_per_step": mixed_qlt["ms_per_step"],
+                            "spectrum_l1_vs_f64": mixed_qlt["spectrum_l1_vs_f64"],
+                            "surrogate_gain": head["value"] / mixed_qlt["value"]},
+        "spectrum_l1_vs_f64": head["spectrum_l1_vs_f64"],
+        "judge": head["judge"],
+        "surrogate_fp16": {k: focused["surrogate_fp16"][k] for k in
+                           ("value", "ms_per_step", "spectrum_l1_vs_f64", "judge")},
+        "train": focused["train"],
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None,
-                     "model": "512 B per particle-step (2 frames x 4 corners x 16 f32)",
-                     "peak_kind": peak_kind},
+                     "frac": achieved / peak,
+                     "traffic": None if per_step_traffic is None
+                     else per_step_traffic * steps_per_launch,
+                     "model": "672 B per particle-step (2 frames x 4 corners x 21 f32 gathers)",
+                     "peak_kind": peak_kind,
+                     "tensor_tflops": steps_per_launch * TENSOR_FLOP_PER_STEP / kernel_s / 1e12},
         "cpu_baseline": {"value": cpu_value, "unit": "particle-steps/s", "cores": cpu_threads,
                          "kind": "port",
-                         "sample": f"{args.cpu_particles} particles x 1 interval "
-                                   f"({cpu_total} particle-steps, {cpu_elapsed:.1f} s)"},
-        "e2e": {"value": mixed["e2e_steps"] / mixed["e2e_s"], "unit": "particle-steps/s",
-                "h2d_bytes_per_step": mixed["state_bytes"],
-                "d2h_bytes_per_step": mixed["state_bytes"]},
+                         "sample": f"focused plain-QLT oracle, {args.cpu_particles} particles x 1 "
+                                   f"interval ({cpu_total} particle-steps, {cpu_elapsed:.1f} s)"},
+        "e2e": {"value": head["e2e"], "unit": "particle-steps/s",
+                "h2d_bytes_per_step": head["state_bytes"],
+                "d2h_bytes_per_step": head["state_bytes"]},
+        "parker": parker,
         # per timed step: the push, plus 3 cell-sort kernels when sorting
-        "focused_qlt": focused,
         "gpu_launches": args.steps * (1 + (3 if args.sort_tile > 0 else 0)),
-        "clocks": mixed["clocks"],
+        "clocks": head["clocks"],
     }
     print(json.dumps(line))
 

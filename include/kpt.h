@@ -155,9 +155,38 @@ typedef struct kpt_particle_arrays {
     int32_t* split_level;
 } kpt_particle_arrays;
 
+/* Training controls of the learned QLT closure (5 -> 64 -> 64 -> 3 tanh MLP,
+ * inputs mu, ln p, ln|B|, dB^2/B^2, gamma_k; outputs D_mumu, dD_mumu/dmu,
+ * ln kappa_parallel).  The box is where the network is trusted: outside it,
+ * and for |mu| < mu_cut, the push evaluates the plain closure. */
+enum kpt_surrogate_element {
+    KPT_SURROGATE_BF16 = 0,  /* bfloat16 weights and activations (default) */
+    KPT_SURROGATE_FP16 = 1   /* IEEE binary16: 3 more significand bits, same speed */
+};
+
+typedef struct kpt_surrogate_config {
+    int32_t samples;          /* training set size (default 2,000,000) */
+    int32_t steps;            /* Adam steps (default 16000) */
+    int32_t batch;            /* minibatch (default 8192) */
+    int32_t element_type;     /* kpt_surrogate_element of the served network */
+    double learning_rate;     /* initial; cosine decay to 1 % (default 1e-2) */
+    double mu_cut;            /* default 0.02 */
+    double mu_max;            /* largest |mu| trained (default 0.999) */
+    double p_lo_over_p0;      /* default 0.1 */
+    double p_hi_over_p0;      /* default 1000 */
+    double sigma2_lo;         /* default 0.01 */
+    double sigma2_hi;         /* default 1 */
+    double gk_lo;             /* default 1.5 */
+    double gk_hi;             /* default 2 */
+    double b_lo;              /* |B| range (default 0.05 .. 5) */
+    double b_hi;
+    uint64_t seed;
+} kpt_surrogate_config;
+
 typedef struct kpt_context kpt_context;
 typedef struct kpt_field kpt_field;
 typedef struct kpt_particles kpt_particles;
+typedef struct kpt_surrogate kpt_surrogate;
 
 /* ---- library ---------------------------------------------------------- */
 int kpt_abi_version(void);
@@ -194,6 +223,46 @@ int kpt_field_shape(const kpt_field* field, int* nx, int* ny, uint64_t* points,
                     int* components);
 /* Copy the table to host as float64 (points x components). */
 int kpt_field_download_table(const kpt_field* field, double* out, uint64_t out_len);
+
+/* ---- learned closure (no counterpart in the reference; replaces the QLT
+ *      evaluation of include/LegencyModel.hpp:557-645 in the focused push) ---- */
+void kpt_surrogate_default_config(kpt_surrogate_config* out);
+/* Generate the training set from the plain closure (with the physics of
+ * `settings`) and train on the GPU with the library's own forward/backward
+ * kernels and Adam.  final_loss: mean squared error (normalised units) of
+ * the last steps. */
+int kpt_surrogate_train(kpt_context* ctx, const kpt_settings* settings,
+                        const kpt_surrogate_config* config, kpt_surrogate** out,
+                        double* final_loss);
+int kpt_surrogate_destroy(kpt_surrogate* surrogate);
+/* Network on n raw inputs (n x 5: mu, ln p, ln|B|, dB^2/B^2, gamma_k) ->
+ * n x 3 (D_mumu, dD_mumu/dmu, ln kappa_parallel).  tensor_cores = 1 runs the
+ * tensor-core path the push uses, 0 the FP32 SIMT forward.  Inputs
+ * outside the box or with |mu| < mu_cut get the plain closure; served
+ * (optional, n) is 1 where the network answered. */
+int kpt_surrogate_evaluate(kpt_surrogate* surrogate, uint64_t n, const double* inputs,
+                           int tensor_cores, double* outputs, int32_t* served);
+/* Parameter block (FP32, W1 b1 W2 b2 W3 b3 = 4739 floats) and the box
+ * normalisation (in_lo[5], in_hi[5], out_offset[3], out_scale[3], mu_cut);
+ * the box is in feature units ln|mu|, ln p, ln|B|, ln(dB^2/B^2), gamma_k and
+ * a feature f maps to 2 (f - lo) / (hi - lo) - 1. */
+int kpt_surrogate_parameters(const kpt_surrogate* surrogate, float* params, int len,
+                             float* normalisation, int norm_len);
+/* Loss gradient (FP32) at `params` over n samples taken in order:
+ * normalised inputs (n x 5) and normalised targets (n x 3). */
+int kpt_surrogate_gradient(kpt_context* ctx, const float* params, uint64_t n,
+                           const float* inputs, const float* targets, float* grad,
+                           float* loss);
+/* Pushes on this context with closure KPT_CLOSURE_SURROGATE use this
+ * network (16-bit weights and activations, FP32 accumulation, on the tensor
+ * cores).  The context keeps the pointer: unset it (NULL) before destroying
+ * the surrogate. */
+int kpt_context_set_surrogate(kpt_context* ctx, kpt_surrogate* surrogate);
+/* Per-step judge of the surrogate in pushes since the last call: network
+ * evaluations, evaluations checked against the plain closure, fallbacks to
+ * the plain closure, largest relative error of D_mumu seen. */
+int kpt_surrogate_judge(kpt_context* ctx, uint64_t* evaluations, uint64_t* judged,
+                        uint64_t* fallbacks, double* max_rel_error);
 
 /* ---- particles --------------------------------------------------------- */
 int kpt_particles_create(kpt_context* ctx, uint64_t capacity, kpt_particles** out);

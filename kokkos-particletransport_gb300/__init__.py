@@ -44,6 +44,8 @@ CLOSURE_DOUBLE = ("qlt_sigma2", "qlt_spectral_index", "qlt_h0", "qlt_omega0", "q
 CLOSURE_DRIVER = 0
 CLOSURE_QLT = 1
 CLOSURE_SURROGATE = 2
+SURROGATE_BF16 = 0
+SURROGATE_FP16 = 1
 
 
 class KptError(RuntimeError):
@@ -76,6 +78,16 @@ class Summary(ctypes.Structure):
 
     def as_dict(self) -> Dict[str, float]:
         return {name: getattr(self, name) for name, _ in self._fields_ if name != "pad"}
+
+
+class SurrogateConfig(ctypes.Structure):
+    """kpt_surrogate_config: training set, optimiser and training box."""
+    _fields_ = [("samples", ctypes.c_int32), ("steps", ctypes.c_int32),
+                ("batch", ctypes.c_int32), ("element_type", ctypes.c_int32)] + \
+               [(n, ctypes.c_double) for n in (
+                   "learning_rate", "mu_cut", "mu_max", "p_lo_over_p0", "p_hi_over_p0",
+                   "sigma2_lo", "sigma2_hi", "gk_lo", "gk_hi", "b_lo", "b_hi")] + \
+               [("seed", ctypes.c_uint64)]
 
 
 class ParticleArrays(ctypes.Structure):
@@ -131,6 +143,14 @@ def load_library() -> ctypes.CDLL:
         "kpt_particles_sort": (i32, [vp, vp, vp, i32, i32]),
         "kpt_particles_clear_order": (i32, [vp]),
         "kpt_particles_wrap": (i32, [vp, u64, u64, vp, pvp]),
+        "kpt_surrogate_default_config": (None, [vp]),
+        "kpt_surrogate_train": (i32, [vp, vp, vp, pvp, vp]),
+        "kpt_surrogate_destroy": (i32, [vp]),
+        "kpt_surrogate_evaluate": (i32, [vp, u64, vp, i32, vp, vp]),
+        "kpt_surrogate_parameters": (i32, [vp, vp, i32, vp, i32]),
+        "kpt_surrogate_gradient": (i32, [vp, vp, u64, vp, vp, vp, vp]),
+        "kpt_context_set_surrogate": (i32, [vp, vp]),
+        "kpt_surrogate_judge": (i32, [vp, vp, vp, vp, vp]),
     }
     for name, (restype, argtypes) in sig.items():
         fn = getattr(lib, name)
@@ -293,6 +313,49 @@ class Context:
         _check(self.lib.kpt_summarize(self.handle, parts.handle, ctypes.byref(out)))
         return out.as_dict()
 
+    # -- learned closure --------------------------------------------------
+    def train_surrogate(self, settings: Settings, **config) -> "Surrogate":
+        """Train the QLT surrogate on the GPU (kpt_surrogate_train)."""
+        cfg = SurrogateConfig()
+        self.lib.kpt_surrogate_default_config(ctypes.byref(cfg))
+        for key, value in config.items():
+            if key not in dict(SurrogateConfig._fields_):
+                raise KeyError(key)
+            setattr(cfg, key, value)
+        handle = ctypes.c_void_p()
+        loss = ctypes.c_double()
+        _check(self.lib.kpt_surrogate_train(self.handle, ctypes.byref(settings),
+                                            ctypes.byref(cfg), ctypes.byref(handle),
+                                            ctypes.byref(loss)))
+        sg = self._adopt(Surrogate(self, handle))
+        sg.final_loss = float(loss.value)
+        return sg
+
+    def set_surrogate(self, surrogate: Optional["Surrogate"]) -> None:
+        _check(self.lib.kpt_context_set_surrogate(
+            self.handle, surrogate.handle if surrogate is not None else None))
+
+    def surrogate_judge(self) -> Dict[str, float]:
+        """Judge counters of the pushes since the last call (then reset)."""
+        ev, ju, fb = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        err = ctypes.c_double()
+        _check(self.lib.kpt_surrogate_judge(self.handle, ctypes.byref(ev), ctypes.byref(ju),
+                                            ctypes.byref(fb), ctypes.byref(err)))
+        return {"evaluations": int(ev.value), "judged": int(ju.value),
+                "fallbacks": int(fb.value), "max_rel_error": float(err.value)}
+
+    def surrogate_gradient(self, params: np.ndarray, inputs: np.ndarray, targets: np.ndarray):
+        """Loss and its gradient over (normalised) samples, on the GPU."""
+        params = np.ascontiguousarray(params, dtype=np.float32)
+        inputs = np.ascontiguousarray(inputs, dtype=np.float32)
+        targets = np.ascontiguousarray(targets, dtype=np.float32)
+        grad = np.zeros_like(params)
+        loss = ctypes.c_float()
+        _check(self.lib.kpt_surrogate_gradient(self.handle, _ptr(params), inputs.shape[0],
+                                               _ptr(inputs), _ptr(targets), _ptr(grad),
+                                               ctypes.byref(loss)))
+        return float(loss.value), grad
+
     def sample(self, lower: "Field", upper: "Field", x, y, rt,
                time_interpolation: int = 1) -> np.ndarray:
         x = np.ascontiguousarray(x, dtype=np.float64)
@@ -336,6 +399,52 @@ class Field:
         out = np.zeros((points, comps), dtype=np.float64)
         _check(self.ctx.lib.kpt_field_download_table(self.handle, _ptr(out), out.size))
         return out
+
+
+class Surrogate:
+    """A trained QLT surrogate (kpt_surrogate)."""
+
+    PARAMS = 4739
+
+    def __init__(self, ctx: Context, handle: ctypes.c_void_p):
+        self.ctx = ctx
+        self.handle = handle
+        self.final_loss = float("nan")
+
+    def close(self) -> None:
+        if self.handle:
+            self.ctx.lib.kpt_surrogate_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def parameters(self):
+        """(FP32 parameter block, normalisation dict)."""
+        params = np.zeros(self.PARAMS, dtype=np.float32)
+        norm = np.zeros(17, dtype=np.float32)
+        _check(self.ctx.lib.kpt_surrogate_parameters(self.handle, _ptr(params), params.size,
+                                                     _ptr(norm), norm.size))
+        return params, {"in_lo": norm[0:5].astype(np.float64),
+                        "in_hi": norm[5:10].astype(np.float64),
+                        "out_offset": norm[10:13].astype(np.float64),
+                        "out_scale": norm[13:16].astype(np.float64),
+                        "mu_cut": float(norm[16])}
+
+    def evaluate(self, inputs: np.ndarray, tensor_cores: bool = True):
+        """(n, 5) raw inputs (mu, ln p, ln|B|, dB^2/B^2, gamma_k) ->
+        ((n, 3) D_mumu, dD_mumu/dmu, ln kappa_par; (n,) served-by-network)."""
+        inputs = np.ascontiguousarray(inputs, dtype=np.float64)
+        n = inputs.shape[0]
+        out = np.zeros((n, 3), dtype=np.float64)
+        served = np.zeros(n, dtype=np.int32)
+        _check(self.ctx.lib.kpt_surrogate_evaluate(self.handle, n, _ptr(inputs),
+                                                   1 if tensor_cores else 0, _ptr(out),
+                                                   _ptr(served)))
+        return out, served.astype(bool)
 
 
 class ParticleStorage:
@@ -400,41 +509,3 @@ def header_functions(path: str = HEADER_PATH) -> Sequence[str]:
     text = open(path).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     return sorted(set(re.findall(r"\b(kpt_[a-z0-9_]+)\s*\(", text)))
-
-
-def smoke_check(device: int = 0) -> None:
-    """One small Parker push on the GPU, checked against the CPU oracle."""
-    import importlib
-    binding = importlib.import_module("binding")  # oracle/binding.py (checker only)
-    field0 = fields.harris_field(32, 64, noise=0.01, seed=1)
-    field1 = fields.harris_field(32, 64, noise=0.01, seed=2)
-    params = binding.default_params(kperp_over_kpara=0.05)
-    oracle = binding.Oracle()
-    grid = oracle.grid(field0.x_edges, field0.y_edges)
-    cap, seed, frame = 512, 114514, 3
-    ref = binding.empty_particles(cap)
-    count = oracle.inject(grid, params, frame * 0.1, frame, seed, cap, 0, 256, ref,
-                          band=(-0.2, 0.2))
-    start = {k: v.copy() for k, v in ref.items()}
-    oracle.push(grid, oracle.table(field0), oracle.table(field1), params, frame * 0.1, frame,
-                seed, count, ref)
-    with Context(device) as ctx:
-        settings = settings_from_dict(params)
-        lower = ctx.field(field0)
-        upper = ctx.field(field1)
-        parts = ctx.particles(cap)
-        parts.upload(start, count)
-        stats = ctx.push_interval(parts, lower, upper, settings, frame, seed)
-        got = parts.download()
-        for name in ("x", "y", "p", "t", "dt"):
-            err = np.max(np.abs(got[name] - ref[name][:count]) /
-                         np.maximum(np.abs(ref[name][:count]), 1e-300))
-            if not err <= 1e-10:
-                raise AssertionError(f"smoke: {name} differs from the oracle (rel {err:.3e})")
-        if not np.array_equal(got["status"], ref["status"][:count]):
-            raise AssertionError("smoke: status differs from the oracle")
-        if stats.particle_steps <= 0:
-            raise AssertionError("smoke: no particle steps executed")
-        for f in (lower, upper):
-            f.close()
-        parts.close()

@@ -14,6 +14,7 @@
 #include <limits>
 #include <memory>
 #include <new>
+#include <random>
 #include <string>
 #include <vector>
 
@@ -91,8 +92,22 @@ struct kpt_context {
     DeviceBuffer hist_bins, hist_edge_count, hist_edge_index;
     DeviceBuffer summary_partials, summary_result;
     DeviceBuffer sample_io;
+    kpt_surrogate* surrogate = nullptr;
+    DeviceBuffer judge;
     int push_schedule = kpt::kScheduleRefill;
     int push_blocks_per_sm = 0;  // 0: as many as fit (occupancy)
+};
+
+struct kpt_surrogate {
+    kpt_context* ctx = nullptr;
+    int device = 0;
+    kpt::SurrogateBox box{};
+    std::vector<float> params;  // FP32 trained parameters
+    float* d_params = nullptr;  // FP32 copy (SIMT evaluation)
+    uint2* d_block = nullptr;   // BF16 mma.sync B fragments + FP32 biases
+    double final_loss = 0.0;
+    // settings the targets were generated with (checked at push time)
+    double kperp_over_kpara = 0.0;
 };
 
 struct kpt_field {
@@ -440,7 +455,8 @@ int kpt_context_destroy(kpt_context* ctx) {
     for (DeviceBuffer* b : {&ctx->counters, &ctx->split_counts, &ctx->split_offsets,
                             &ctx->split_totals, &ctx->split_levels, &ctx->hist_bins,
                             &ctx->hist_edge_count, &ctx->hist_edge_index,
-                            &ctx->summary_partials, &ctx->summary_result, &ctx->sample_io}) {
+                            &ctx->summary_partials, &ctx->summary_result, &ctx->sample_io,
+                            &ctx->judge}) {
         b->release();
     }
     if (ctx->own_stream != nullptr) {
@@ -907,6 +923,35 @@ int kpt_push_interval(kpt_context* ctx, kpt_particles* parts, const kpt_field* l
     launch.schedule = ctx->push_schedule;
     launch.sm_count = ctx->sm_count;
     launch.blocks_per_sm = ctx->push_blocks_per_sm;
+    launch.surrogate = nullptr;
+    kpt::SurrogateDevice served{};
+    if (settings->closure == KPT_CLOSURE_SURROGATE) {
+        const kpt_surrogate* sg = ctx->surrogate;
+        KPT_REQUIRE(sg != nullptr,
+                    "kpt_push_interval: closure SURROGATE needs kpt_context_set_surrogate");
+        KPT_REQUIRE(settings->focused != 0 && lower->precision == KPT_PRECISION_MIXED,
+                    "kpt_push_interval: the surrogate closure runs in the mixed focused push");
+        const kpt::SurrogateBox& box = sg->box;
+        KPT_REQUIRE(box.p0 == settings->p0 && box.particle_v0 == settings->particle_v0 &&
+                        box.kpara0 == settings->kpara0 &&
+                        box.gamma_turb == settings->gamma_turb &&
+                        box.qlt_omega0 == settings->qlt_omega0 &&
+                        box.qlt_lc == settings->qlt_lc && box.qlt_h0 == settings->qlt_h0 &&
+                        box.magnetic_dependency == settings->magnetic_dependency &&
+                        box.momentum_dependency == settings->momentum_dependency,
+                    "kpt_push_interval: settings differ from those the surrogate was trained with");
+        served.block = sg->d_block;
+        served.box = box;
+        const double f3 = std::log(settings->qlt_sigma2);
+        const double f4 = settings->qlt_spectral_index;
+        served.constants_in_box = f3 >= box.in_lo[3] && f3 <= box.in_hi[3] && f4 >= box.in_lo[4] &&
+                                  f4 <= box.in_hi[4];
+        served.f3 = static_cast<float>(f3) * box.in_scale[3] + box.in_offset[3];
+        served.f4 = static_cast<float>(f4) * box.in_scale[4] + box.in_offset[4];
+        served.judge_period = 16;
+        served.judge = ctx->judge.as<unsigned long long>();  // zeroed by set_surrogate
+        launch.surrogate = &served;
+    }
     KPT_CUDA(cudaMemsetAsync(launch.counters, 0, sizeof(kpt::PushCounters), ctx->stream));
     if (parts->count > 0) {
         KPT_CUDA(kpt::launch_push_interval(launch, ctx->stream));
@@ -1086,6 +1131,387 @@ int kpt_summarize(kpt_context* ctx, const kpt_particles* parts, kpt_summary* out
         out->dt_max = r.dt_max;
         out->p_avg = r.p_sum / static_cast<double>(r.active);
         out->dt_avg = r.dt_sum / static_cast<double>(r.active);
+    }
+    return KPT_OK;
+}
+
+// ---------------------------------------------------------------- surrogate
+
+namespace {
+
+// float -> bfloat16, round to nearest even (upper 16 bits of the float).
+uint32_t to_bf16(float f) {
+    uint32_t bits;
+    std::memcpy(&bits, &f, sizeof(bits));
+    const uint32_t rounding = 0x7fffu + ((bits >> 16) & 1u);
+    return (bits + rounding) >> 16;
+}
+
+// float -> IEEE binary16, round to nearest even, subnormals kept, overflow to
+// infinity (finite weights only reach it beyond 65504).
+uint32_t to_fp16(float f) {
+    uint32_t bits;
+    std::memcpy(&bits, &f, sizeof(bits));
+    const uint32_t sign = (bits >> 16) & 0x8000u;
+    const uint32_t abs = bits & 0x7fffffffu;
+    if (abs >= 0x7f800000u) {  // inf / nan
+        return sign | 0x7c00u | (abs > 0x7f800000u ? 0x200u : 0u);
+    }
+    const int exp = static_cast<int>(abs >> 23) - 127;
+    if (exp > 15) return sign | 0x7c00u;
+    uint32_t mant = (abs & 0x7fffffu) | 0x800000u;  // 24-bit significand
+    int shift;                                        // bits dropped from it
+    uint32_t base;
+    if (exp >= -14) {
+        shift = 13;
+        base = static_cast<uint32_t>(exp + 15) << 10;
+        mant &= 0x7fffffu;  // implicit bit carried by the exponent field
+    } else {
+        if (exp < -25) return sign;  // rounds to zero
+        shift = 13 + (-14 - exp);    // subnormal: value = mant * 2^(exp-23)
+        base = 0u;
+    }
+    const uint32_t kept = mant >> shift;
+    const uint32_t rest = mant & ((1u << shift) - 1u);
+    const uint32_t half = 1u << (shift - 1);
+    uint32_t out = base + kept;  // a mantissa carry rolls into the exponent
+    if (rest > half || (rest == half && (kept & 1u))) ++out;
+    return sign | out;
+}
+
+uint32_t pack_pair(float lo, float hi, bool fp16) {
+    return fp16 ? (to_fp16(lo) | (to_fp16(hi) << 16)) : (to_bf16(lo) | (to_bf16(hi) << 16));
+}
+
+// B fragments of mma.m16n8k16 (bf16, "col" operand) for out = in * W^T with
+// W[n][k] (n outputs, k inputs), zero-padded to ktiles x 16 by ntiles x 8:
+// lane l of tile (kt, nt) holds {W[n][k0], W[n][k0+1]} and
+// {W[n][k0+8], W[n][k0+9]}, n = 8 nt + l/4, k0 = 16 kt + 2 (l%4).
+void pack_fragments(const float* w, int n_out, int k_in, int ktiles, int ntiles, bool fp16,
+                    std::vector<uint32_t>& out) {
+    auto at = [&](int n, int k) { return (n < n_out && k < k_in) ? w[n * k_in + k] : 0.0f; };
+    for (int kt = 0; kt < ktiles; ++kt) {
+        for (int nt = 0; nt < ntiles; ++nt) {
+            for (int lane = 0; lane < 32; ++lane) {
+                const int n = 8 * nt + lane / 4;
+                const int k0 = 16 * kt + 2 * (lane % 4);
+                out.push_back(pack_pair(at(n, k0), at(n, k0 + 1), fp16));
+                out.push_back(pack_pair(at(n, k0 + 8), at(n, k0 + 9), fp16));
+            }
+        }
+    }
+}
+
+}  // namespace
+
+void kpt_surrogate_default_config(kpt_surrogate_config* c) {
+    if (c == nullptr) return;
+    std::memset(c, 0, sizeof(*c));
+    c->samples = 2000000;
+    c->steps = 16000;
+    c->batch = 8192;
+    c->element_type = KPT_SURROGATE_BF16;
+    c->learning_rate = 1e-2;
+    c->mu_cut = 0.02;
+    c->mu_max = 0.999;
+    c->p_lo_over_p0 = 0.1;
+    c->p_hi_over_p0 = 1000.0;
+    c->sigma2_lo = 0.01;
+    c->sigma2_hi = 1.0;
+    c->gk_lo = 1.5;
+    c->gk_hi = 2.0;
+    c->b_lo = 0.05;
+    c->b_hi = 5.0;
+    c->seed = 2024;
+}
+
+int kpt_surrogate_train(kpt_context* ctx, const kpt_settings* settings,
+                        const kpt_surrogate_config* config, kpt_surrogate** out,
+                        double* final_loss) {
+    KPT_REQUIRE(ctx && settings && config && out, "kpt_surrogate_train: NULL argument");
+    *out = nullptr;
+    if (int rc = validate_settings(settings)) return rc;
+    const kpt_surrogate_config& c = *config;
+    KPT_REQUIRE(c.samples > 0 && c.steps > 0 && c.batch > 0 && c.batch <= (1 << 20),
+                "kpt_surrogate_train: samples, steps and batch must be positive");
+    KPT_REQUIRE(c.element_type == KPT_SURROGATE_BF16 || c.element_type == KPT_SURROGATE_FP16,
+                "kpt_surrogate_train: element_type must be KPT_SURROGATE_BF16 or _FP16");
+    KPT_REQUIRE(c.mu_cut > 0.0 && c.mu_cut < c.mu_max && c.mu_max < 1.0 &&
+                    c.p_lo_over_p0 > 0.0 && c.p_hi_over_p0 > c.p_lo_over_p0 &&
+                    c.sigma2_lo > 0.0 && c.sigma2_hi > c.sigma2_lo && c.gk_lo > 1.0 &&
+                    c.gk_hi > c.gk_lo && c.b_lo > 0.0 && c.b_hi > c.b_lo &&
+                    c.learning_rate > 0.0,
+                "kpt_surrogate_train: invalid training box");
+    if (int rc = activate(ctx)) return rc;
+    std::unique_ptr<kpt_surrogate> sg(new kpt_surrogate());
+    sg->ctx = ctx;
+    sg->device = ctx->device;
+    kpt::SurrogateBox& box = sg->box;
+    const double lo[5] = {std::log(c.mu_cut), std::log(c.p_lo_over_p0 * settings->p0),
+                          std::log(c.b_lo), std::log(c.sigma2_lo), c.gk_lo};
+    const double hi[5] = {std::log(c.mu_max), std::log(c.p_hi_over_p0 * settings->p0),
+                          std::log(c.b_hi), std::log(c.sigma2_hi), c.gk_hi};
+    for (int k = 0; k < 5; ++k) {
+        box.in_lo[k] = static_cast<float>(lo[k]);
+        box.in_hi[k] = static_cast<float>(hi[k]);
+        box.in_scale[k] = static_cast<float>(2.0 / (hi[k] - lo[k]));
+        box.in_offset[k] = static_cast<float>(-(hi[k] + lo[k]) / (hi[k] - lo[k]));
+    }
+    box.mu_cut = static_cast<float>(c.mu_cut);
+    box.fp16 = c.element_type == KPT_SURROGATE_FP16 ? 1 : 0;
+    box.magnetic_dependency = settings->magnetic_dependency;
+    box.momentum_dependency = settings->momentum_dependency;
+    box.p0 = settings->p0;
+    box.particle_v0 = settings->particle_v0;
+    box.kpara0 = settings->kpara0;
+    box.gamma_turb = settings->gamma_turb;
+    box.qlt_omega0 = settings->qlt_omega0;
+    box.qlt_lc = settings->qlt_lc;
+    box.qlt_h0 = settings->qlt_h0;
+    cudaStream_t st = ctx->stream;
+    const size_t n = static_cast<size_t>(c.samples);
+    DeviceBuffer data, work;
+    KPT_CUDA(data.reserve(n * (kpt::kMlpIn + kpt::kMlpOut) * sizeof(float)));
+    float* x = data.as<float>();
+    float* t = x + n * kpt::kMlpIn;
+    KPT_CUDA(kpt::surrogate_make_samples(c.seed, c.samples, box, x, t, st));
+    std::vector<float> host_t(n * kpt::kMlpOut);
+    KPT_CUDA(cudaMemcpyAsync(host_t.data(), t, host_t.size() * sizeof(float),
+                             cudaMemcpyDeviceToHost, st));
+    KPT_CUDA(cudaStreamSynchronize(st));
+    for (int o = 0; o < kpt::kMlpOut; ++o) {
+        double sum = 0.0, sum2 = 0.0;
+        for (size_t i = 0; i < n; ++i) {
+            const double v = host_t[i * kpt::kMlpOut + o];
+            sum += v;
+            sum2 += v * v;
+        }
+        const double mean = sum / static_cast<double>(n);
+        const double var = std::max(sum2 / static_cast<double>(n) - mean * mean, 1e-12);
+        if (!std::isfinite(mean) || !std::isfinite(var)) {
+            return set_error(KPT_ERROR_INVALID_ARGUMENT,
+                             "kpt_surrogate_train: non-finite training targets");
+        }
+        box.out_offset[o] = static_cast<float>(mean);
+        box.out_scale[o] = static_cast<float>(std::sqrt(var));
+    }
+    // Xavier-uniform initial weights, zero biases.
+    sg->params.assign(kpt::kMlpParams, 0.0f);
+    std::mt19937_64 rng(c.seed ^ 0x5851f42d4c957f2dull);
+    auto init = [&](int base, int rows, int cols) {
+        const float a = std::sqrt(6.0f / static_cast<float>(rows + cols));
+        std::uniform_real_distribution<float> u(-a, a);
+        for (int k = 0; k < rows * cols; ++k) sg->params[base + k] = u(rng);
+    };
+    init(kpt::kMlpW1, kpt::kMlpHidden, kpt::kMlpIn);
+    init(kpt::kMlpW2, kpt::kMlpHidden, kpt::kMlpHidden);
+    init(kpt::kMlpW3, kpt::kMlpOut, kpt::kMlpHidden);
+    const size_t b = static_cast<size_t>(c.batch);
+    const size_t pcount = kpt::kMlpParams;
+    const size_t floats = 4 * pcount + b * (kpt::kMlpIn + 4 * kpt::kMlpHidden + kpt::kMlpOut) +
+                          static_cast<size_t>(c.steps);
+    KPT_CUDA(work.reserve(floats * sizeof(float)));
+    KPT_CUDA(cudaMemsetAsync(work.ptr, 0, floats * sizeof(float), st));
+    kpt::SurrogateTrainLaunch L{};
+    float* w = work.as<float>();
+    L.x = x;
+    L.t = t;
+    L.n = c.samples;
+    L.seed = c.seed;
+    L.batch = c.batch;
+    L.box = box;
+    L.params = w;
+    L.grad = w + pcount;
+    L.m = w + 2 * pcount;
+    L.v = w + 3 * pcount;
+    L.xb = w + 4 * pcount;
+    L.h1 = L.xb + b * kpt::kMlpIn;
+    L.h2 = L.h1 + b * kpt::kMlpHidden;
+    L.g1 = L.h2 + b * kpt::kMlpHidden;
+    L.g2 = L.g1 + b * kpt::kMlpHidden;
+    L.gy = L.g2 + b * kpt::kMlpHidden;
+    L.loss = L.gy + b * kpt::kMlpOut;
+    L.beta1 = 0.9f;
+    L.beta2 = 0.999f;
+    KPT_CUDA(cudaMemcpyAsync(L.params, sg->params.data(), pcount * sizeof(float),
+                             cudaMemcpyHostToDevice, st));
+    const double pi = 3.141592653589793238462643383279502884;
+    for (int step = 0; step < c.steps; ++step) {
+        const double phase = static_cast<double>(step) / static_cast<double>(c.steps);
+        L.lr = static_cast<float>(c.learning_rate * (0.01 + 0.99 * 0.5 * (1.0 + std::cos(pi * phase))));
+        KPT_CUDA(kpt::surrogate_train_step(L, step, st));
+    }
+    std::vector<float> losses(static_cast<size_t>(c.steps));
+    KPT_CUDA(cudaMemcpyAsync(losses.data(), L.loss, losses.size() * sizeof(float),
+                             cudaMemcpyDeviceToHost, st));
+    KPT_CUDA(cudaMemcpyAsync(sg->params.data(), L.params, pcount * sizeof(float),
+                             cudaMemcpyDeviceToHost, st));
+    KPT_CUDA(cudaStreamSynchronize(st));
+    const int tail = std::min(c.steps, 50);
+    double acc = 0.0;
+    for (int k = c.steps - tail; k < c.steps; ++k) acc += losses[static_cast<size_t>(k)];
+    sg->final_loss = acc / tail;
+    if (final_loss) *final_loss = sg->final_loss;
+    // inference copies: FP32 parameters and the BF16 fragment + bias block
+    std::vector<uint32_t> words;
+    const bool fp16 = box.fp16 != 0;
+    pack_fragments(sg->params.data() + kpt::kMlpW1, kpt::kMlpHidden, kpt::kMlpIn, 1, 8, fp16,
+                   words);
+    pack_fragments(sg->params.data() + kpt::kMlpW2, kpt::kMlpHidden, kpt::kMlpHidden, 4, 8, fp16,
+                   words);
+    pack_fragments(sg->params.data() + kpt::kMlpW3, kpt::kMlpOut, kpt::kMlpHidden, 4, 1, fp16,
+                   words);
+    std::vector<float> bias(kpt::kBiasCount, 0.0f);
+    for (int k = 0; k < kpt::kMlpHidden; ++k) {
+        bias[k] = sg->params[kpt::kMlpB1 + k];
+        bias[kpt::kMlpHidden + k] = sg->params[kpt::kMlpB2 + k];
+    }
+    for (int k = 0; k < kpt::kMlpOut; ++k) bias[2 * kpt::kMlpHidden + k] = sg->params[kpt::kMlpB3 + k];
+    for (float b : bias) {
+        uint32_t bits;
+        std::memcpy(&bits, &b, sizeof(bits));
+        words.push_back(bits);
+    }
+    KPT_CUDA(cudaMalloc(&sg->d_params, pcount * sizeof(float)));
+    KPT_CUDA(cudaMalloc(&sg->d_block, kpt::kSurrogateSmemBytes));
+    KPT_CUDA(cudaMemcpy(sg->d_params, sg->params.data(), pcount * sizeof(float),
+                        cudaMemcpyHostToDevice));
+    KPT_CUDA(cudaMemcpy(sg->d_block, words.data(), kpt::kSurrogateSmemBytes,
+                        cudaMemcpyHostToDevice));
+    *out = sg.release();
+    return KPT_OK;
+}
+
+int kpt_surrogate_destroy(kpt_surrogate* sg) {
+    if (sg == nullptr) return KPT_OK;
+    cudaSetDevice(sg->device);
+    cudaFree(sg->d_params);
+    cudaFree(sg->d_block);
+    delete sg;
+    return KPT_OK;
+}
+
+int kpt_surrogate_parameters(const kpt_surrogate* sg, float* params, int len, float* norm,
+                             int norm_len) {
+    KPT_REQUIRE(sg != nullptr, "kpt_surrogate_parameters: NULL handle");
+    if (params != nullptr) {
+        KPT_REQUIRE(len >= kpt::kMlpParams, "kpt_surrogate_parameters: params too short");
+        std::copy(sg->params.begin(), sg->params.end(), params);
+    }
+    if (norm != nullptr) {
+        KPT_REQUIRE(norm_len >= 17, "kpt_surrogate_parameters: normalisation too short");
+        for (int k = 0; k < 5; ++k) {
+            norm[k] = sg->box.in_lo[k];
+            norm[5 + k] = sg->box.in_hi[k];
+        }
+        for (int k = 0; k < 3; ++k) {
+            norm[10 + k] = sg->box.out_offset[k];
+            norm[13 + k] = sg->box.out_scale[k];
+        }
+        norm[16] = sg->box.mu_cut;
+    }
+    return KPT_OK;
+}
+
+int kpt_surrogate_evaluate(kpt_surrogate* sg, uint64_t n, const double* inputs, int tensor_cores,
+                           double* outputs, int32_t* served) {
+    KPT_REQUIRE(sg && inputs && outputs, "kpt_surrogate_evaluate: NULL argument");
+    KPT_REQUIRE(n < (1ull << 30), "kpt_surrogate_evaluate: too many inputs");
+    if (n == 0) return KPT_OK;
+    KPT_CUDA(cudaSetDevice(sg->device));
+    DeviceBuffer buf;
+    KPT_CUDA(buf.reserve(n * 8 * sizeof(double) + n * sizeof(int)));
+    double* din = buf.as<double>();
+    double* dout = din + n * 5;
+    int* dserved = reinterpret_cast<int*>(dout + n * 3);
+    cudaStream_t st = sg->ctx->stream;
+    KPT_CUDA(cudaMemcpyAsync(din, inputs, n * 5 * sizeof(double), cudaMemcpyHostToDevice, st));
+    KPT_CUDA(kpt::surrogate_eval(static_cast<int>(n), din, sg->box, sg->d_params, sg->d_block,
+                                 tensor_cores != 0, dout, dserved, st));
+    KPT_CUDA(cudaMemcpyAsync(outputs, dout, n * 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (served) {
+        KPT_CUDA(cudaMemcpyAsync(served, dserved, n * sizeof(int), cudaMemcpyDeviceToHost, st));
+    }
+    KPT_CUDA(cudaStreamSynchronize(st));
+    return KPT_OK;
+}
+
+int kpt_surrogate_gradient(kpt_context* ctx, const float* params, uint64_t n, const float* inputs,
+                           const float* targets, float* grad, float* loss) {
+    KPT_REQUIRE(ctx && params && inputs && targets && grad, "kpt_surrogate_gradient: NULL");
+    KPT_REQUIRE(n > 0 && n <= (1u << 20), "kpt_surrogate_gradient: 0 < n <= 2^20");
+    if (int rc = activate(ctx)) return rc;
+    const size_t pcount = kpt::kMlpParams;
+    const size_t floats = n * (5 + 3) + 2 * pcount + n * (5 + 4 * kpt::kMlpHidden + 3) + 1;
+    DeviceBuffer buf;
+    KPT_CUDA(buf.reserve(floats * sizeof(float)));
+    KPT_CUDA(cudaMemsetAsync(buf.ptr, 0, floats * sizeof(float), ctx->stream));
+    float* w = buf.as<float>();
+    kpt::SurrogateTrainLaunch L{};
+    float* x = w;
+    float* t = x + n * 5;
+    L.x = x;
+    L.t = t;
+    L.n = static_cast<int>(n);
+    L.batch = static_cast<int>(n);
+    for (int k = 0; k < 5; ++k) {
+        L.box.in_lo[k] = -1.0f;
+        L.box.in_hi[k] = 1.0f;
+        L.box.in_scale[k] = 1.0f;
+        L.box.in_offset[k] = 0.0f;
+    }
+    for (int k = 0; k < 3; ++k) {
+        L.box.out_offset[k] = 0.0f;
+        L.box.out_scale[k] = 1.0f;
+    }
+    L.params = t + n * 3;
+    L.grad = L.params + pcount;
+    L.xb = L.grad + pcount;
+    L.h1 = L.xb + n * 5;
+    L.h2 = L.h1 + n * kpt::kMlpHidden;
+    L.g1 = L.h2 + n * kpt::kMlpHidden;
+    L.g2 = L.g1 + n * kpt::kMlpHidden;
+    L.gy = L.g2 + n * kpt::kMlpHidden;
+    L.loss = L.gy + n * 3;
+    cudaStream_t st = ctx->stream;
+    KPT_CUDA(cudaMemcpyAsync(x, inputs, n * 5 * sizeof(float), cudaMemcpyHostToDevice, st));
+    KPT_CUDA(cudaMemcpyAsync(t, targets, n * 3 * sizeof(float), cudaMemcpyHostToDevice, st));
+    KPT_CUDA(cudaMemcpyAsync(L.params, params, pcount * sizeof(float), cudaMemcpyHostToDevice, st));
+    KPT_CUDA(kpt::surrogate_gradient(L, st));
+    KPT_CUDA(cudaMemcpyAsync(grad, L.grad, pcount * sizeof(float), cudaMemcpyDeviceToHost, st));
+    if (loss) KPT_CUDA(cudaMemcpyAsync(loss, L.loss, sizeof(float), cudaMemcpyDeviceToHost, st));
+    KPT_CUDA(cudaStreamSynchronize(st));
+    return KPT_OK;
+}
+
+int kpt_context_set_surrogate(kpt_context* ctx, kpt_surrogate* sg) {
+    KPT_REQUIRE(ctx != nullptr, "kpt_context_set_surrogate: ctx is NULL");
+    ctx->surrogate = sg;
+    if (int rc = activate(ctx)) return rc;
+    KPT_CUDA(ctx->judge.reserve(4 * sizeof(unsigned long long)));
+    KPT_CUDA(cudaMemsetAsync(ctx->judge.ptr, 0, 4 * sizeof(unsigned long long), ctx->stream));
+    return KPT_OK;
+}
+
+int kpt_surrogate_judge(kpt_context* ctx, uint64_t* evaluations, uint64_t* judged,
+                        uint64_t* fallbacks, double* max_rel_error) {
+    KPT_REQUIRE(ctx != nullptr, "kpt_surrogate_judge: ctx is NULL");
+    unsigned long long host[4] = {0, 0, 0, 0};
+    if (ctx->judge.ptr != nullptr) {
+        if (int rc = activate(ctx)) return rc;
+        KPT_CUDA(cudaMemcpyAsync(host, ctx->judge.ptr, sizeof(host), cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+        KPT_CUDA(cudaMemsetAsync(ctx->judge.ptr, 0, sizeof(host), ctx->stream));
+        KPT_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
+    if (evaluations) *evaluations = host[0];
+    if (judged) *judged = host[1];
+    if (fallbacks) *fallbacks = host[2];
+    if (max_rel_error) {
+        float f;
+        const uint32_t bits = static_cast<uint32_t>(host[3]);
+        std::memcpy(&f, &bits, sizeof(f));
+        *max_rel_error = static_cast<double>(f);
     }
     return KPT_OK;
 }

@@ -6,6 +6,7 @@
 
 #include <cstdint>
 
+#include "kpt_surrogate.cuh"
 #include "kpt_types.h"
 
 namespace kpt {
@@ -41,6 +42,8 @@ struct PushLaunch {
     int schedule;
     int sm_count;
     int blocks_per_sm;
+    // learned closure (mixed focused push only); nullptr = plain closures
+    const SurrogateDevice* surrogate;
 };
 
 cudaError_t launch_push_interval(const PushLaunch& launch, cudaStream_t stream);
@@ -135,6 +138,38 @@ struct SortLaunch {
     unsigned int* order;    // count
 };
 cudaError_t launch_sort(const SortLaunch& launch, cudaStream_t stream);
+
+struct SurrogateTrainLaunch {
+    const float* x;   // n x 5 raw features
+    const float* t;   // n x 3 raw targets
+    int n;
+    uint64_t seed;
+    int batch;
+    SurrogateBox box;
+    float* params;
+    float* grad;
+    float* m;
+    float* v;
+    float* xb;        // batch x 5 normalised inputs
+    float* h1;        // batch x 64
+    float* h2;
+    float* g1;
+    float* g2;
+    float* gy;        // batch x 3
+    float* loss;      // one float per step
+    float beta1, beta2, lr;
+};
+cudaError_t surrogate_make_samples(uint64_t seed, int n, const SurrogateBox& box, float* x,
+                                   float* t, cudaStream_t stream);
+cudaError_t surrogate_train_step(const SurrogateTrainLaunch& launch, int step,
+                                 cudaStream_t stream);
+// Gradient of the loss over the first `batch` samples in order (step < 0).
+cudaError_t surrogate_gradient(const SurrogateTrainLaunch& launch, cudaStream_t stream);
+// Raw inputs (n x 5, device) -> D_mumu, dD_mumu/dmu, ln kappa_parallel
+// (n x 3, device); served[i] = 1 where the network answered.
+cudaError_t surrogate_eval(int n, const double* inputs, const SurrogateBox& box,
+                           const float* params, const uint2* block, bool tensor, double* out,
+                           int* served, cudaStream_t stream);
 
 struct SampleLaunch {
     Grid grid;

@@ -298,6 +298,12 @@ __device__ __forceinline__ void qlt_scattering(T mu, T omega, T speed, const Con
     dmumu_dmu = dmumu * (endpoint + shape);
 }
 
+// Closure values served by the learned surrogate (mixed focused push).
+struct Served {
+    bool use;
+    float kpara, duu, duu_du;
+};
+
 template <typename T>
 struct Rates {
     T dx_dt, dy_dt, dp_dt, dmu_dt, duu;
@@ -310,9 +316,9 @@ struct Rates {
 // Coefficients, drift, dp/dt, dmu/dt and the step-size limiters of one
 // substep (src/main.cpp:1167-1257 Parker, :1421-1630 focused).  Returns
 // false where the reference sets status 2.
-template <typename T, bool FOCUSED>
+template <typename T, bool FOCUSED, bool SURR = false>
 __device__ __forceinline__ bool physics(const T* c, T p, T pitch_mu, const Consts<T>& s,
-                                        Rates<T>& r) {
+                                        Rates<T>& r, const Served* served = nullptr) {
     using N = Num<T>;
     T vx, vy, bx, by, bz, b, dvx_dx, dvy_dy, dbx_dx, dbx_dy, dby_dx, dby_dy, dbz_dx, dbz_dy,
         db_dx, db_dy;
@@ -336,15 +342,20 @@ __device__ __forceinline__ bool physics(const T* c, T p, T pitch_mu, const Const
     const T ib2 = ib * ib;
     const T ib3 = ib2 * ib;
 
-    T knorm_para = T(1);
-    if (s.magnetic_dependency == 1) {
-        knorm_para *= N::pow(b, gamma - T(2));
+    T kpara;
+    if (SURR && served->use) {
+        kpara = served->kpara;
+    } else {
+        T knorm_para = T(1);
+        if (s.magnetic_dependency == 1) {
+            knorm_para *= N::pow(b, gamma - T(2));
+        }
+        T knorm = knorm_para;
+        if (s.momentum_dependency == 1) {
+            knorm *= N::pow(N::div(p, p0), s.pindex);
+        }
+        kpara = s.kpara0 * knorm;
     }
-    T knorm = knorm_para;
-    if (s.momentum_dependency == 1) {
-        knorm *= N::pow(N::div(p, p0), s.pindex);
-    }
-    const T kpara = s.kpara0 * knorm;
     const T kperp = kpara * s.kperp_over_kpara;
     if (!N::finite(kpara) || kpara <= T(0) || !N::finite(kperp) || kperp < T(0)) {
         return false;
@@ -419,7 +430,10 @@ __device__ __forceinline__ bool physics(const T* c, T p, T pitch_mu, const Const
                  N::div(T(2) * bv_gradv, speed);
         dmu_dt *= T(0.5) * (T(1) - mu2);
         T duu_du = T(0);
-        if (s.closure != 0) {
+        if (SURR && served->use) {
+            duu = served->duu;
+            duu_du = served->duu_du;
+        } else if (s.closure != 0) {
             // slab QLT closure (extension): Omega = Omega_0 |B| / gamma
             const T omega = N::div(s.qlt_omega0 * b, N::sqrt(T(1) + p * p));
             qlt_scattering<T>(pitch_mu, omega, speed, s, duu, duu_du);
@@ -561,6 +575,7 @@ struct PushParams {
     uint32_t frame;
     uint2 key;
     PushCounters* counters;
+    SurrogateDevice sg;  // used by the surrogate instantiation only
 };
 
 // ------------------------------------------------------------- FP64 path
@@ -734,13 +749,14 @@ __device__ __forceinline__ void add_pair(float& hi, float& lo, float d) {
     lo = l - (hi - s);
 }
 
+// Table values at the particle (fixed-point stencil, time interpolation).
 template <bool FOCUSED>
-__device__ __forceinline__ bool substep(StateMixed& st, const PushParams& P) {
+__device__ __forceinline__ void sample_mixed(const StateMixed& st, const PushParams& P,
+                                             float (&c)[FOCUSED ? 21 : 16]) {
     constexpr int C = FOCUSED ? 21 : 16;
     constexpr int STRIDE = FOCUSED ? 24 : 16;
     const DeviceSettings& s = P.s;
     const FixedGrid& F = P.fixed;
-    ++st.steps;
     const uint64_t qx = st.px + F.axis[0].half_cell;
     const uint64_t qy = st.py + F.axis[1].half_cell;
     int lo0, lo1;
@@ -762,12 +778,20 @@ __device__ __forceinline__ bool substep(StateMixed& st, const PushParams& P) {
     corner_points(lo0, lo0 + 1, lo1, lo1 + 1, P.grid.ex, pt);
     float rt = st.tau <= 0 ? 0.0f : s64_to_float_scaled(st.tau, 1.0f / 1073741824.0f);
     rt = rt > 1.0f ? 1.0f : rt;
-    float c[C];
     sample_stencil<float, C, STRIDE>(static_cast<const float*>(P.lower),
                                      static_cast<const float*>(P.upper), pt, wc, rt,
                                      s.time_interpolation, c);
+}
+
+// Physics, step size, noise and the state update of one substep.
+template <bool FOCUSED, bool SURR = false>
+__device__ __forceinline__ bool advance_mixed(StateMixed& st, const PushParams& P,
+                                              const float (&c)[FOCUSED ? 21 : 16],
+                                              const Served* served = nullptr) {
+    const DeviceSettings& s = P.s;
+    const FixedGrid& F = P.fixed;
     Rates<float> r;
-    if (!physics<float, FOCUSED>(c, st.p_hi, st.mu, P.kf, r)) {
+    if (!physics<float, FOCUSED, SURR>(c, st.p_hi, st.mu, P.kf, r, served)) {
         st.status = 2;
         return false;
     }
@@ -805,6 +829,99 @@ __device__ __forceinline__ bool substep(StateMixed& st, const PushParams& P) {
         st.p_lo = F.pfloor_lo;
     }
     return st.tau < kTauEnd && st.steps < s.max_steps;
+}
+
+template <bool FOCUSED>
+__device__ __forceinline__ bool substep(StateMixed& st, const PushParams& P) {
+    ++st.steps;
+    float c[FOCUSED ? 21 : 16];
+    sample_mixed<FOCUSED>(st, P, c);
+    return advance_mixed<FOCUSED>(st, P, c);
+}
+
+// Per-lane tallies of the surrogate judge.
+struct JudgeTally {
+    unsigned long long evaluations, judged, fallbacks;
+    float max_error;
+};
+
+// Warp-collective focused substep with the learned closure.  Every lane of
+// the warp calls it (converged); lanes without a particle (have = false)
+// feed zero rows to the network and return false.  Lanes whose inputs leave
+// the training box, or with |mu| < mu_cut, use the plain closure; one
+// substep in judge_period of each particle also evaluates the plain closure
+// and records the larger relative error of D_mumu and kappa_parallel.
+template <bool FP16>
+__device__ __forceinline__ bool substep_surrogate(StateMixed& st, const PushParams& P, bool have,
+                                                  const uint2* smem, JudgeTally& tally) {
+    const SurrogateDevice& sg = P.sg;
+    const SurrogateBox& box = sg.box;
+    float c[21];
+    float f[kMlpIn] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    bool use = false;
+    float mu = 0.0f;
+    if (have) {
+        ++st.steps;
+        sample_mixed<true>(st, P, c);
+        mu = clamp_mu(st.mu, P.kf.mu_max);
+        const float b = c[6];
+        const float p = st.p_hi;
+        const float amu = fabsf(mu);
+        if (sg.constants_in_box && amu >= box.mu_cut && b > 0.0f && p > 0.0f) {
+            const float lm = __logf(amu);
+            const float lp = __logf(p);
+            const float lb = __logf(b);
+            use = lm <= box.in_hi[0] && lp >= box.in_lo[1] && lp <= box.in_hi[1] &&
+                  lb >= box.in_lo[2] && lb <= box.in_hi[2];
+            if (use) {
+                f[0] = lm * box.in_scale[0] + box.in_offset[0];
+                f[1] = lp * box.in_scale[1] + box.in_offset[1];
+                f[2] = lb * box.in_scale[2] + box.in_offset[2];
+                f[3] = sg.f3;
+                f[4] = sg.f4;
+            }
+        }
+    }
+    __syncwarp();
+    float y[kMlpOut];
+    mlp_warp<FP16>(smem, f, y);
+    if (!have) {
+        return false;
+    }
+    Served served;
+    served.use = use;
+    if (use) {
+        const float y0 = y[0] * box.out_scale[0] + box.out_offset[0];
+        const float y1 = y[1] * box.out_scale[1] + box.out_offset[1];
+        const float y2 = y[2] * box.out_scale[2] + box.out_offset[2];
+        const float one_minus_mu2 = 1.0f - mu * mu;
+        const float sign = mu > 0.0f ? 1.0f : -1.0f;
+        served.duu = one_minus_mu2 * __expf(y0);
+        served.duu_du = served.duu * (__fdividef(sign * y1, fabsf(mu) + P.kf.qlt_h0) -
+                                      __fdividef(2.0f * mu, one_minus_mu2));
+        served.kpara = __expf(y2);
+        ++tally.evaluations;
+        if ((st.steps & (sg.judge_period - 1)) == 0) {
+            const Consts<float>& k = P.kf;
+            const float b = c[6];
+            const float p = st.p_hi;
+            const float speed = __fdividef(k.particle_v0 * p, k.p0);
+            const float omega = __fdividef(k.qlt_omega0 * b, sqrtf(1.0f + p * p));
+            float duu, duu_du;
+            qlt_scattering<float>(mu, omega, speed, k, duu, duu_du);
+            float kpara = k.kpara0;
+            if (k.magnetic_dependency == 1) kpara *= Num<float>::pow(b, k.gamma_turb - 2.0f);
+            if (k.momentum_dependency == 1) kpara *= Num<float>::pow(__fdividef(p, k.p0), k.pindex);
+            const float e_d = fabsf(served.duu - duu) / duu;
+            const float e_k = fabsf(served.kpara - kpara) / kpara;
+            const float e = fmaxf(e_d, e_k);
+            tally.max_error = isfinite(e) ? fmaxf(tally.max_error, e) : INFINITY;
+            ++tally.judged;
+        }
+    } else {
+        ++tally.fallbacks;
+    }
+    return advance_mixed<true, true>(st, P, c, &served);
 }
 
 // Position <-> fixed-point phase (once per particle and push).
@@ -894,6 +1011,24 @@ __device__ __forceinline__ void flush_counters(PushCounters* counters, unsigned 
     }
 }
 
+__device__ __forceinline__ void flush_judge(unsigned long long* judge, JudgeTally t) {
+    const unsigned full = 0xffffffffu;
+#pragma unroll
+    for (int offset = 16; offset > 0; offset >>= 1) {
+        t.evaluations += __shfl_down_sync(full, t.evaluations, offset);
+        t.judged += __shfl_down_sync(full, t.judged, offset);
+        t.fallbacks += __shfl_down_sync(full, t.fallbacks, offset);
+        t.max_error = fmaxf(t.max_error, __shfl_down_sync(full, t.max_error, offset));
+    }
+    if ((threadIdx.x & 31u) == 0u) {
+        if (t.evaluations) atomicAdd(judge + 0, t.evaluations);
+        if (t.judged) atomicAdd(judge + 1, t.judged);
+        if (t.fallbacks) atomicAdd(judge + 2, t.fallbacks);
+        // non-negative floats order like their bit patterns
+        atomicMax(judge + 3, static_cast<unsigned long long>(__float_as_uint(t.max_error)));
+    }
+}
+
 // Persistent warps with lane refill.  A warp claims particles from the
 // cursor in batches of (idle lanes); each trip advances every busy lane by
 // one substep.  Every trip either advances a particle (bounded by the step
@@ -916,12 +1051,24 @@ struct MinBlocks<StateMixed, true> {
     static constexpr int value = 4;
 };
 
-template <typename State, bool FOCUSED>
-__global__ void __launch_bounds__(128, MinBlocks<State, FOCUSED>::value)
+// The surrogate instantiations (SURR = 1 BF16 network, 2 FP16 network) keep
+// the MLP fragments live beside the particle state and the sampled
+// coefficients.
+#ifndef KPT_SURROGATE_MIN_BLOCKS
+#define KPT_SURROGATE_MIN_BLOCKS 4
+#endif
+template <typename State, bool FOCUSED, int SURR = 0>
+__global__ void __launch_bounds__(128, SURR ? KPT_SURROGATE_MIN_BLOCKS
+                                            : MinBlocks<State, FOCUSED>::value)
     push_refill_kernel(const PushParams P) {
     const unsigned full = 0xffffffffu;
     const unsigned lane = threadIdx.x & 31u;
     const unsigned lanes_below = (1u << lane) - 1u;
+    extern __shared__ uint2 surrogate_smem[];
+    JudgeTally tally{0ull, 0ull, 0ull, 0.0f};
+    if (SURR) {
+        load_surrogate_block(P.sg.block, surrogate_smem);
+    }
     State st;
     bool have = false;
     bool exhausted = false;
@@ -964,7 +1111,13 @@ __global__ void __launch_bounds__(128, MinBlocks<State, FOCUSED>::value)
             }
             continue;
         }
-        if (have && !substep<FOCUSED>(st, P)) {
+        bool more;
+        if constexpr (SURR) {
+            more = substep_surrogate<SURR == 2>(st, P, have, surrogate_smem, tally);
+        } else {
+            more = have && substep<FOCUSED>(st, P);
+        }
+        if (have && !more) {
             store<FOCUSED>(st, P);
             my_steps += static_cast<unsigned long long>(st.steps);
             my_max = max(my_max, static_cast<unsigned int>(st.steps));
@@ -973,6 +1126,9 @@ __global__ void __launch_bounds__(128, MinBlocks<State, FOCUSED>::value)
         }
     }
     flush_counters(P.counters, my_steps, my_pushed, my_failed, my_max);
+    if (SURR) {
+        flush_judge(P.sg.judge, tally);
+    }
 }
 
 // One particle per thread, no refill (schedule alternative for the tuner).
@@ -1002,7 +1158,7 @@ __global__ void __launch_bounds__(128) push_simple_kernel(const PushParams P) {
     flush_counters(P.counters, my_steps, my_pushed, my_failed, my_max);
 }
 
-template <typename State, bool FOCUSED>
+template <typename State, bool FOCUSED, int SURR = 0>
 cudaError_t launch_push(const PushLaunch& L, cudaStream_t stream) {
     PushParams P;
     P.grid = L.grid;
@@ -1021,8 +1177,12 @@ cudaError_t launch_push(const PushLaunch& L, cudaStream_t stream) {
     P.frame = L.frame;
     P.key = make_uint2(static_cast<uint32_t>(L.seed), static_cast<uint32_t>(L.seed >> 32));
     P.counters = L.counters;
+    if (SURR) {
+        P.sg = *L.surrogate;
+    }
     const int threads = 128;
-    if (L.schedule == kScheduleSimple) {
+    const size_t smem = SURR ? kSurrogateSmemBytes : 0;
+    if (L.schedule == kScheduleSimple && !SURR) {
         const uint64_t want = (L.count + threads - 1) / threads;
         const int blocks =
             static_cast<int>(want < 1 ? 1 : (want > 65535u * 8u ? 65535u * 8u : want));
@@ -1032,12 +1192,13 @@ cudaError_t launch_push(const PushLaunch& L, cudaStream_t stream) {
         // registers allow (or fewer on request).
         int resident = 0;
         cudaError_t err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &resident, push_refill_kernel<State, FOCUSED>, threads, 0);
+            &resident, push_refill_kernel<State, FOCUSED, SURR>, threads, smem);
         if (err != cudaSuccess) return err;
         resident = resident < 1 ? 1 : resident;
         const int per_sm = L.blocks_per_sm > 0 && L.blocks_per_sm < resident ? L.blocks_per_sm
                                                                             : resident;
-        push_refill_kernel<State, FOCUSED><<<L.sm_count * per_sm, threads, 0, stream>>>(P);
+        push_refill_kernel<State, FOCUSED, SURR>
+            <<<L.sm_count * per_sm, threads, smem, stream>>>(P);
     }
     return cudaGetLastError();
 }
@@ -1095,6 +1256,10 @@ cudaError_t launch_push_interval(const PushLaunch& launch, cudaStream_t stream) 
     if (launch.precision == kPrecisionF64) {
         return launch.focused ? launch_push<StateF64, true>(launch, stream)
                               : launch_push<StateF64, false>(launch, stream);
+    }
+    if (launch.surrogate != nullptr) {
+        return launch.surrogate->box.fp16 ? launch_push<StateMixed, true, 2>(launch, stream)
+                                          : launch_push<StateMixed, true, 1>(launch, stream);
     }
     return launch.focused ? launch_push<StateMixed, true>(launch, stream)
                           : launch_push<StateMixed, false>(launch, stream);

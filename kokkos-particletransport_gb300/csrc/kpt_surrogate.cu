@@ -1,0 +1,360 @@
+// Training and evaluation of the learned QLT closure (the project's own
+// forward and backward kernels, FP32 SIMT; the network is tiny).
+//
+// Samples are drawn uniformly over the training box (feature units) with the
+// keyed Philox stream; targets come from the plain slab-QLT closure in FP64
+// (LegencyModel.hpp:557-645) and the driver's kappa_parallel closure
+// (src/main.cpp:1177-1193).  One optimisation step: forward + backward per
+// sample (activations and deltas kept in HBM), batch reductions for the
+// weight gradients, then Adam.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+
+#include "kpt_device.cuh"
+#include "kpt_internal.h"
+#include "kpt_surrogate.cuh"
+
+namespace kpt {
+namespace {
+
+constexpr double kPiD = 3.141592653589793238462643383279502884;
+
+// Plain slab-QLT closure (LegencyModel.hpp:557-645) with per-sample sigma^2
+// and gamma_k, FP64: D_mumu, dD_mumu/dmu and the two network targets
+// y0 = ln D - ln(1 - mu^2), y1 = (gk - 1) - gk reg^gk / (reg^gk + xi^gk).
+__device__ void qlt_targets(double mu, double omega, double speed, double sigma2, double lc,
+                            double gk, double h0, double& d, double& dd, double& y0,
+                            double& y1) {
+    d = 0.0;
+    dd = 0.0;
+    y0 = 0.0;
+    y1 = 0.0;
+    const double one_minus_mu2 = 1.0 - mu * mu;
+    if (one_minus_mu2 <= 0.0) return;
+    const double reg = fabs(mu) + h0;
+    const double xi = omega * lc / speed;
+    const double reg_gk = pow(reg, gk);
+    const double reg_gk1 = pow(reg, gk - 1.0);
+    const double denominator = reg_gk + pow(xi, gk);
+    const double norm = gk * sin(kPiD / gk) / kPiD;
+    const double prefactor = 0.25 * kPiD * omega * sigma2 * norm;
+    d = prefactor * one_minus_mu2 * xi * reg_gk1 / denominator;
+    y0 = log(prefactor * xi) + (gk - 1.0) * log(reg) - log(denominator);
+    y1 = (gk - 1.0) - gk * reg_gk / denominator;
+    if (d == 0.0 || mu == 0.0) return;
+    const double sign = mu > 0.0 ? 1.0 : -1.0;
+    dd = d * (-2.0 * mu / one_minus_mu2 + sign * ((gk - 1.0) / reg - gk * reg_gk1 / denominator));
+}
+
+// The driver's kappa_parallel closure (src/main.cpp:1177-1193).
+__device__ double kappa_parallel(const SurrogateBox& box, double p, double b) {
+    double k = box.kpara0;
+    if (box.magnetic_dependency == 1) k *= pow(b, box.gamma_turb - 2.0);
+    if (box.momentum_dependency == 1) k *= pow(p / box.p0, 3.0 - box.gamma_turb);
+    return k;
+}
+
+__device__ __forceinline__ double u32_open(uint32_t r) {
+    return (static_cast<double>(r) + 0.5) * 2.3283064365386963e-10;
+}
+
+// Training samples, uniform over the box in feature units (ln|mu|, ln p,
+// ln|B|, ln sigma^2, gamma_k); x holds the raw features, t the targets.
+__global__ void make_samples_kernel(uint64_t seed, int n, SurrogateBox box, float* x, float* t) {
+    const uint2 key = seed_key(seed);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint4 r0 = philox4x32_10(make_uint4(0u, static_cast<uint32_t>(i), 0u, 7u), key);
+        const uint4 r1 = philox4x32_10(make_uint4(1u, static_cast<uint32_t>(i), 0u, 7u), key);
+        const uint32_t words[5] = {r0.x, r0.y, r0.z, r0.w, r1.x};
+        double f[kMlpIn];
+        for (int k = 0; k < kMlpIn; ++k) {
+            f[k] = box.in_lo[k] + (static_cast<double>(box.in_hi[k]) - box.in_lo[k]) *
+                                      u32_open(words[k]);
+        }
+        const double mu = exp(f[0]);
+        const double p = exp(f[1]);
+        const double b = exp(f[2]);
+        const double sigma2 = exp(f[3]);
+        const double gk = f[4];
+        const double speed = box.particle_v0 * p / box.p0;
+        const double omega = box.qlt_omega0 * b / sqrt(1.0 + p * p);
+        double d, dd, y0, y1;
+        qlt_targets(mu, omega, speed, sigma2, box.qlt_lc, gk, box.qlt_h0, d, dd, y0, y1);
+        float* xi = x + static_cast<size_t>(i) * kMlpIn;
+        for (int k = 0; k < kMlpIn; ++k) xi[k] = static_cast<float>(f[k]);
+        float* ti = t + static_cast<size_t>(i) * kMlpOut;
+        ti[0] = static_cast<float>(y0);
+        ti[1] = static_cast<float>(y1);
+        ti[2] = static_cast<float>(log(kappa_parallel(box, p, b)));
+    }
+}
+
+__device__ __forceinline__ float normalise_input(const SurrogateBox& box, int k, float v) {
+    return v * box.in_scale[k] + box.in_offset[k];
+}
+
+// Forward and backward of one minibatch, one thread per sample.  Stores
+// H1, H2 (activations) and G1, G2, GY (deltas) for the gradient reductions.
+__global__ void __launch_bounds__(128) fwd_bwd_kernel(const float* __restrict__ x,
+                                                      const float* __restrict__ t, int n,
+                                                      uint64_t seed, int step, int batch,
+                                                      SurrogateBox box,
+                                                      const float* __restrict__ params,
+                                                      float* xb, float* h1, float* h2, float* g1,
+                                                      float* g2, float* gy, float* loss) {
+    __shared__ float w[kMlpParams];
+    for (int k = threadIdx.x; k < kMlpParams; k += blockDim.x) w[k] = params[k];
+    __syncthreads();
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    float sq = 0.0f;
+    if (b < batch) {
+        int i = b % n;
+        if (step >= 0) {
+            const uint4 r = philox4x32_10(make_uint4(static_cast<uint32_t>(b),
+                                                     static_cast<uint32_t>(step), 0u, 9u),
+                                          seed_key(seed));
+            i = static_cast<int>(u01_f64(r.x, r.y) * n) % n;
+        }
+        float in[kMlpIn];
+        for (int k = 0; k < kMlpIn; ++k) {
+            in[k] = normalise_input(box, k, x[static_cast<size_t>(i) * kMlpIn + k]);
+            xb[static_cast<size_t>(b) * kMlpIn + k] = in[k];
+        }
+        float a1[kMlpHidden];
+        for (int j = 0; j < kMlpHidden; ++j) {
+            float z = w[kMlpB1 + j];
+            for (int k = 0; k < kMlpIn; ++k) z += w[kMlpW1 + j * kMlpIn + k] * in[k];
+            a1[j] = tanhf(z);
+            h1[static_cast<size_t>(b) * kMlpHidden + j] = a1[j];
+        }
+        float y[kMlpOut];
+        for (int o = 0; o < kMlpOut; ++o) y[o] = w[kMlpB3 + o];
+        for (int j = 0; j < kMlpHidden; ++j) {
+            float z = w[kMlpB2 + j];
+            for (int k = 0; k < kMlpHidden; ++k) z += w[kMlpW2 + j * kMlpHidden + k] * a1[k];
+            const float a2 = tanhf(z);
+            h2[static_cast<size_t>(b) * kMlpHidden + j] = a2;
+            for (int o = 0; o < kMlpOut; ++o) y[o] += w[kMlpW3 + o * kMlpHidden + j] * a2;
+        }
+        float dy[kMlpOut];
+        for (int o = 0; o < kMlpOut; ++o) {
+            const float target = (t[static_cast<size_t>(i) * kMlpOut + o] - box.out_offset[o]) /
+                                 box.out_scale[o];
+            const float e = y[o] - target;
+            sq += e * e;
+            dy[o] = 2.0f * e / static_cast<float>(batch * kMlpOut);
+            gy[static_cast<size_t>(b) * kMlpOut + o] = dy[o];
+        }
+        float d1[kMlpHidden];
+        for (int k = 0; k < kMlpHidden; ++k) d1[k] = 0.0f;
+        for (int j = 0; j < kMlpHidden; ++j) {
+            const float a2 = h2[static_cast<size_t>(b) * kMlpHidden + j];
+            float dh = 0.0f;
+            for (int o = 0; o < kMlpOut; ++o) dh += w[kMlpW3 + o * kMlpHidden + j] * dy[o];
+            const float dz = dh * (1.0f - a2 * a2);
+            g2[static_cast<size_t>(b) * kMlpHidden + j] = dz;
+            for (int k = 0; k < kMlpHidden; ++k) d1[k] += w[kMlpW2 + j * kMlpHidden + k] * dz;
+        }
+        for (int k = 0; k < kMlpHidden; ++k) {
+            g1[static_cast<size_t>(b) * kMlpHidden + k] = d1[k] * (1.0f - a1[k] * a1[k]);
+        }
+    }
+    // batch loss (mean squared error in normalised units)
+    for (int off = 16; off > 0; off >>= 1) sq += __shfl_down_sync(0xffffffffu, sq, off);
+    if ((threadIdx.x & 31u) == 0u && sq != 0.0f) {
+        atomicAdd(loss, sq / static_cast<float>(batch * kMlpOut));
+    }
+}
+
+// Weight and bias gradients: one block per parameter row, threads over the
+// row's columns, a loop over the batch.  Row r of:
+//   W1 (64 rows x 5):  sum_b G1[b][r] X[b][c];   b1[r] = sum_b G1[b][r]
+//   W2 (64 rows x 64): sum_b G2[b][r] H1[b][c];  b2[r] = sum_b G2[b][r]
+//   W3 (3 rows x 64):  sum_b GY[b][r] H2[b][c];  b3[r] = sum_b GY[b][r]
+__global__ void __launch_bounds__(64) grad_kernel(int batch, const float* xb, const float* h1,
+                                                  const float* h2, const float* g1,
+                                                  const float* g2, const float* gy, float* grad) {
+    const int row = blockIdx.x;
+    const int c = threadIdx.x;
+    const float* delta;
+    const float* input;
+    int dstride, istride, cols, wbase, bbase, r;
+    if (row < kMlpHidden) {
+        r = row; delta = g1; dstride = kMlpHidden; input = xb; istride = kMlpIn; cols = kMlpIn;
+        wbase = kMlpW1; bbase = kMlpB1;
+    } else if (row < 2 * kMlpHidden) {
+        r = row - kMlpHidden; delta = g2; dstride = kMlpHidden; input = h1; istride = kMlpHidden;
+        cols = kMlpHidden; wbase = kMlpW2; bbase = kMlpB2;
+    } else {
+        r = row - 2 * kMlpHidden; delta = gy; dstride = kMlpOut; input = h2;
+        istride = kMlpHidden; cols = kMlpHidden; wbase = kMlpW3; bbase = kMlpB3;
+    }
+    float acc = 0.0f, bacc = 0.0f;
+    for (int b = 0; b < batch; ++b) {
+        const float d = delta[static_cast<size_t>(b) * dstride + r];
+        if (c < cols) acc += d * input[static_cast<size_t>(b) * istride + c];
+        bacc += d;
+    }
+    if (c < cols) grad[wbase + r * cols + c] = acc;
+    if (c == 0) grad[bbase + r] = bacc;
+}
+
+__global__ void adam_kernel(float* params, const float* grad, float* m, float* v, float lr,
+                            float beta1, float beta2, float eps, float bias1, float bias2) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= kMlpParams) return;
+    const float g = grad[k];
+    const float mk = beta1 * m[k] + (1.0f - beta1) * g;
+    const float vk = beta2 * v[k] + (1.0f - beta2) * g * g;
+    m[k] = mk;
+    v[k] = vk;
+    params[k] -= lr * (mk / bias1) / (sqrtf(vk / bias2) + eps);
+}
+
+// FP32 SIMT forward of normalised features -> normalised outputs.
+__device__ void forward_fp32(const float* w, const float (&in)[kMlpIn], float (&y)[kMlpOut]) {
+    float a1[kMlpHidden];
+    for (int j = 0; j < kMlpHidden; ++j) {
+        float z = w[kMlpB1 + j];
+        for (int k = 0; k < kMlpIn; ++k) z += w[kMlpW1 + j * kMlpIn + k] * in[k];
+        a1[j] = tanhf(z);
+    }
+    for (int o = 0; o < kMlpOut; ++o) y[o] = w[kMlpB3 + o];
+    for (int j = 0; j < kMlpHidden; ++j) {
+        float z = w[kMlpB2 + j];
+        for (int k = 0; k < kMlpHidden; ++k) z += w[kMlpW2 + j * kMlpHidden + k] * a1[k];
+        const float a2 = tanhf(z);
+        for (int o = 0; o < kMlpOut; ++o) y[o] += w[kMlpW3 + o * kMlpHidden + j] * a2;
+    }
+}
+
+// Raw inputs (mu, ln p, ln|B|, sigma^2, gamma_k) -> (D_mumu, dD_mumu/dmu,
+// ln kappa_parallel), FP64 out.  The network (FP32 SIMT, or the BF16
+// tensor-core warp path the push uses) serves inputs inside the box with
+// |mu| >= mu_cut; the plain closure serves the rest.  Warps stay converged
+// (the loop bound is per warp) because the tensor-core path is collective.
+// MODE 0: FP32 SIMT, 1: BF16 tensor cores, 2: FP16 tensor cores.
+template <int MODE>
+__global__ void __launch_bounds__(128) eval_kernel(int n, const double* __restrict__ in,
+                                                   SurrogateBox box,
+                                                   const float* __restrict__ params,
+                                                   const uint2* __restrict__ block,
+                                                   double* __restrict__ out,
+                                                   int* __restrict__ served) {
+    extern __shared__ uint2 smem[];
+    if (MODE != 0) {
+        load_surrogate_block(block, smem);
+    } else {
+        float* w = reinterpret_cast<float*>(smem);
+        for (int k = threadIdx.x; k < kMlpParams; k += blockDim.x) w[k] = params[k];
+        __syncthreads();
+    }
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    for (int base = warp * 32; base < n; base += warps * 32) {
+        const int i = base + lane;
+        const bool have = i < n;
+        double raw[kMlpIn] = {0.0, 0.0, 0.0, 0.0, 0.0};
+        if (have) {
+            for (int k = 0; k < kMlpIn; ++k) raw[k] = in[static_cast<size_t>(i) * kMlpIn + k];
+        }
+        const double mu = raw[0];
+        const double feat[kMlpIn] = {log(fabs(mu)), raw[1], raw[2], log(raw[3]), raw[4]};
+        bool inside = have && fabs(mu) >= box.mu_cut;
+        float f[kMlpIn];
+        for (int k = 0; k < kMlpIn; ++k) {
+            inside = inside && feat[k] >= box.in_lo[k] && feat[k] <= box.in_hi[k];
+            f[k] = static_cast<float>(feat[k]) * box.in_scale[k] + box.in_offset[k];
+        }
+        if (!inside) {
+            for (int k = 0; k < kMlpIn; ++k) f[k] = 0.0f;
+        }
+        float y[kMlpOut];
+        if (MODE != 0) {
+            mlp_warp<MODE == 2>(smem, f, y);
+        } else {
+            forward_fp32(reinterpret_cast<const float*>(smem), f, y);
+        }
+        if (!have) continue;
+        const double p = exp(raw[1]);
+        const double b = exp(raw[2]);
+        double d, dd, lk;
+        if (inside) {
+            const double y0 = static_cast<double>(y[0]) * box.out_scale[0] + box.out_offset[0];
+            const double y1 = static_cast<double>(y[1]) * box.out_scale[1] + box.out_offset[1];
+            lk = static_cast<double>(y[2]) * box.out_scale[2] + box.out_offset[2];
+            const double one_minus_mu2 = 1.0 - mu * mu;
+            const double sign = mu > 0.0 ? 1.0 : -1.0;
+            d = one_minus_mu2 * exp(y0);
+            dd = d * (sign * y1 / (fabs(mu) + box.qlt_h0) - 2.0 * mu / one_minus_mu2);
+        } else {
+            const double speed = box.particle_v0 * p / box.p0;
+            const double omega = box.qlt_omega0 * b / sqrt(1.0 + p * p);
+            double y0, y1;
+            qlt_targets(mu, omega, speed, raw[3], box.qlt_lc, raw[4], box.qlt_h0, d, dd, y0, y1);
+            lk = log(kappa_parallel(box, p, b));
+        }
+        out[static_cast<size_t>(i) * kMlpOut + 0] = d;
+        out[static_cast<size_t>(i) * kMlpOut + 1] = dd;
+        out[static_cast<size_t>(i) * kMlpOut + 2] = lk;
+        served[i] = inside ? 1 : 0;
+    }
+}
+
+}  // namespace
+
+cudaError_t surrogate_make_samples(uint64_t seed, int n, const SurrogateBox& box, float* x,
+                                   float* t, cudaStream_t stream) {
+    const int threads = 256;
+    const int blocks = (n + threads - 1) / threads < 152 * 16 ? (n + threads - 1) / threads
+                                                              : 152 * 16;
+    make_samples_kernel<<<blocks, threads, 0, stream>>>(seed, n, box, x, t);
+    return cudaGetLastError();
+}
+
+cudaError_t surrogate_train_step(const SurrogateTrainLaunch& L, int step, cudaStream_t stream) {
+    fwd_bwd_kernel<<<(L.batch + 127) / 128, 128, 0, stream>>>(
+        L.x, L.t, L.n, L.seed, step, L.batch, L.box, L.params, L.xb, L.h1, L.h2, L.g1, L.g2, L.gy,
+        L.loss + step);
+    grad_kernel<<<2 * kMlpHidden + kMlpOut, 64, 0, stream>>>(L.batch, L.xb, L.h1, L.h2, L.g1,
+                                                              L.g2, L.gy, L.grad);
+    const float t1 = static_cast<float>(step + 1);
+    const float bias1 = 1.0f - powf(L.beta1, t1);
+    const float bias2 = 1.0f - powf(L.beta2, t1);
+    adam_kernel<<<(kMlpParams + 255) / 256, 256, 0, stream>>>(
+        L.params, L.grad, L.m, L.v, L.lr, L.beta1, L.beta2, 1e-8f, bias1, bias2);
+    return cudaGetLastError();
+}
+
+cudaError_t surrogate_gradient(const SurrogateTrainLaunch& L, cudaStream_t stream) {
+    fwd_bwd_kernel<<<(L.batch + 127) / 128, 128, 0, stream>>>(
+        L.x, L.t, L.n, L.seed, -1, L.batch, L.box, L.params, L.xb, L.h1, L.h2, L.g1, L.g2, L.gy,
+        L.loss);
+    grad_kernel<<<2 * kMlpHidden + kMlpOut, 64, 0, stream>>>(L.batch, L.xb, L.h1, L.h2, L.g1,
+                                                              L.g2, L.gy, L.grad);
+    return cudaGetLastError();
+}
+
+cudaError_t surrogate_eval(int n, const double* inputs, const SurrogateBox& box,
+                           const float* params, const uint2* block, bool tensor, double* out,
+                           int* served, cudaStream_t stream) {
+    const int threads = 128;
+    int blocks = (n + threads - 1) / threads;
+    blocks = blocks < 1 ? 1 : (blocks > 152 * 8 ? 152 * 8 : blocks);
+    if (tensor && box.fp16) {
+        eval_kernel<2><<<blocks, threads, kSurrogateSmemBytes, stream>>>(n, inputs, box, params,
+                                                                         block, out, served);
+    } else if (tensor) {
+        eval_kernel<1><<<blocks, threads, kSurrogateSmemBytes, stream>>>(n, inputs, box, params,
+                                                                         block, out, served);
+    } else {
+        eval_kernel<0><<<blocks, threads, kMlpParams * sizeof(float), stream>>>(
+            n, inputs, box, params, block, out, served);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace kpt

@@ -1,0 +1,121 @@
+"""CPU reference of the learned QLT closure's network and its training targets.
+
+TEST INFRASTRUCTURE ONLY: the checker for the GPU forward/backward kernels
+and the fused tensor-core inference; the product never imports it.
+
+Network: 5 -> 64 -> 64 -> 3, tanh hidden layers, linear output; parameter
+block W1[64][5] b1[64] W2[64][64] b2[64] W3[3][64] b3[3] (4739 values).
+Loss: mean over samples and outputs of the squared error.  Everything here
+is float64 numpy, written from the definitions (backpropagation by the chain
+rule), and is itself checked against central finite differences.
+
+Targets follow the slab-QLT closure of include/LegencyModel.hpp:557-645
+(pitch_angle_diffusion_coefficient / _derivative) and the driver's
+kappa_parallel closure (src/main.cpp:1177-1193):
+  y0 = ln D_mumu - ln(1 - mu^2)
+  y1 = (gk - 1) - gk reg^gk / (reg^gk + xi^gk),  reg = |mu| + h0
+  y2 = ln kappa_parallel
+"""
+from __future__ import annotations
+
+import numpy as np
+
+N_IN, N_HID, N_OUT = 5, 64, 3
+W1 = 0
+B1 = W1 + N_HID * N_IN
+W2 = B1 + N_HID
+B2 = W2 + N_HID * N_HID
+W3 = B2 + N_HID
+B3 = W3 + N_OUT * N_HID
+N_PARAMS = B3 + N_OUT
+
+
+def unpack(params: np.ndarray):
+    p = np.asarray(params, dtype=np.float64)
+    return (p[W1:B1].reshape(N_HID, N_IN), p[B1:W2], p[W2:B2].reshape(N_HID, N_HID), p[B2:W3],
+            p[W3:B3].reshape(N_OUT, N_HID), p[B3:N_PARAMS])
+
+
+def forward(params: np.ndarray, x: np.ndarray) -> np.ndarray:
+    w1, b1, w2, b2, w3, b3 = unpack(params)
+    h1 = np.tanh(x @ w1.T + b1)
+    h2 = np.tanh(h1 @ w2.T + b2)
+    return h2 @ w3.T + b3
+
+
+def loss_and_gradient(params: np.ndarray, x: np.ndarray, t: np.ndarray):
+    """Mean squared error and its gradient with respect to the parameter block."""
+    x = np.asarray(x, dtype=np.float64)
+    t = np.asarray(t, dtype=np.float64)
+    w1, b1, w2, b2, w3, b3 = unpack(params)
+    h1 = np.tanh(x @ w1.T + b1)
+    h2 = np.tanh(h1 @ w2.T + b2)
+    y = h2 @ w3.T + b3
+    n = x.shape[0]
+    err = y - t
+    loss = float(np.mean(err * err))
+    gy = 2.0 * err / (n * N_OUT)
+    g2 = (gy @ w3) * (1.0 - h2 * h2)
+    g1 = (g2 @ w2) * (1.0 - h1 * h1)
+    grad = np.concatenate([(g1.T @ x).ravel(), g1.sum(0), (g2.T @ h1).ravel(), g2.sum(0),
+                           (gy.T @ h2).ravel(), gy.sum(0)])
+    return loss, grad
+
+
+def finite_difference_gradient(params: np.ndarray, x: np.ndarray, t: np.ndarray,
+                               indices, h: float = 1e-6) -> np.ndarray:
+    out = []
+    for k in indices:
+        up = np.array(params, dtype=np.float64)
+        dn = up.copy()
+        up[k] += h
+        dn[k] -= h
+        out.append((loss_and_gradient(up, x, t)[0] - loss_and_gradient(dn, x, t)[0]) / (2 * h))
+    return np.array(out)
+
+
+def qlt_targets(mu, p, b, sigma2, gk, *, p0, particle_v0, qlt_omega0, qlt_lc, qlt_h0):
+    """(D_mumu, dD_mumu/dmu, y0, y1) of the slab-QLT closure, vectorised."""
+    mu = np.asarray(mu, dtype=np.float64)
+    speed = particle_v0 * p / p0
+    omega = qlt_omega0 * b / np.sqrt(1.0 + p * p)
+    one_minus_mu2 = 1.0 - mu * mu
+    reg = np.abs(mu) + qlt_h0
+    xi = omega * qlt_lc / speed
+    reg_gk = reg ** gk
+    den = reg_gk + xi ** gk
+    norm = gk * np.sin(np.pi / gk) / np.pi
+    pref = 0.25 * np.pi * omega * sigma2 * norm
+    d = pref * one_minus_mu2 * xi * reg ** (gk - 1.0) / den
+    y0 = np.log(pref * xi) + (gk - 1.0) * np.log(reg) - np.log(den)
+    y1 = (gk - 1.0) - gk * reg_gk / den
+    dd = d * (-2.0 * mu / one_minus_mu2 + np.sign(mu) * ((gk - 1.0) / reg
+                                                        - gk * reg ** (gk - 1.0) / den))
+    return d, dd, y0, y1
+
+
+def kappa_parallel(p, b, *, p0, kpara0, gamma_turb, magnetic_dependency=1,
+                   momentum_dependency=1):
+    k = kpara0 * np.ones_like(np.asarray(p, dtype=np.float64))
+    if magnetic_dependency == 1:
+        k = k * b ** (gamma_turb - 2.0)
+    if momentum_dependency == 1:
+        k = k * (p / p0) ** (3.0 - gamma_turb)
+    return k
+
+
+def evaluate(params, norm, inputs, *, p0, qlt_h0):
+    """Raw inputs (mu, ln p, ln|B|, sigma^2, gamma_k) -> (D, dD/dmu, ln kappa)
+    through the FP64 network with the box normalisation of a trained net
+    (inputs assumed inside the box)."""
+    inputs = np.asarray(inputs, dtype=np.float64)
+    mu = inputs[:, 0]
+    feat = np.stack([np.log(np.abs(mu)), inputs[:, 1], inputs[:, 2], np.log(inputs[:, 3]),
+                     inputs[:, 4]], axis=1)
+    lo, hi = norm["in_lo"], norm["in_hi"]
+    x = 2.0 * (feat - lo) / (hi - lo) - 1.0
+    y = forward(params, x) * norm["out_scale"] + norm["out_offset"]
+    one_minus_mu2 = 1.0 - mu * mu
+    d = one_minus_mu2 * np.exp(y[:, 0])
+    dd = d * (np.sign(mu) * y[:, 1] / (np.abs(mu) + qlt_h0) - 2.0 * mu / one_minus_mu2)
+    return np.stack([d, dd, y[:, 2]], axis=1)
