@@ -337,6 +337,131 @@ int kpt_sample_table(kpt_context* ctx, const kpt_field* lower, const kpt_field* 
                      uint64_t n, const double* x, const double* y, const double* rt,
                      int time_interpolation, double* out);
 
+/* ======================================================================
+ * Header-library step API (ParkerSolver / ParticleSystem), 2D Cartesian
+ * grids with uniform (analytic) axes, FP64.  Same semantics as the
+ * reference's templates; where the reference calls Kokkos::abort or throws,
+ * these return KPT_ERROR_INVALID_ARGUMENT with the reference's message.
+ * ====================================================================== */
+
+/* ParticleProperties (ParticleSystem.hpp:145-160), dimensionless. */
+typedef struct kpt_particle_properties {
+    double rest_mass;
+    double charge;
+    double speed_of_light;
+    double energy_scale_erg;
+} kpt_particle_properties;
+
+/* ParticleSplittingPolicy (ParticleSystem.hpp:280-295). */
+typedef struct kpt_split_policy {
+    double energy_split_ratio;   /* > 1 (reference default 2) */
+    double minimum_child_weight; /* >= 0 */
+} kpt_split_policy;
+
+/* ParticleSplitStatistics (ParticleSystem.hpp:269-275). */
+typedef struct kpt_split_statistics {
+    uint64_t active_count;
+    uint64_t split_count;
+    uint64_t skipped_capacity_count;
+    uint64_t skipped_invalid_baseline_count;
+    uint64_t skipped_minimum_weight_count;
+} kpt_split_statistics;
+
+/* ParticleSystem<2> storage (ParticleSystem.hpp:340-350): host arrays for
+ * upload/download, n entries each. */
+typedef struct kpt_system_arrays {
+    uint64_t* id;
+    double* x;
+    double* y;
+    double* prev_x;
+    double* prev_y;
+    double* prevstep_x;
+    double* prevstep_y;
+    double* p;
+    double* mu;
+    double* weight;
+    double* e0; /* initial_kinetic_energy */
+    int32_t* status;
+    int32_t* split_level;
+    int32_t* sort_key;
+} kpt_system_arrays;
+
+typedef struct kpt_grid kpt_grid;
+typedef struct kpt_system kpt_system;
+typedef struct kpt_parker_solver kpt_parker_solver;
+
+/* Uniform 2D Cartesian grid with two ghost layers (Grid.hpp:65,
+ * AnalyticCoordinateGrid.hpp); edges nx+1 / ny+1 must be uniform (the field
+ * reader's test, AthenaFieldReader.hpp:167-193); periodic[2] per axis. */
+int kpt_grid_create(kpt_context* ctx, int nx, int ny, const double* x_edges,
+                    const double* y_edges, const int32_t* periodic, kpt_grid** out);
+int kpt_grid_destroy(kpt_grid* grid);
+
+/* ParticleSystem(count, capacity, properties, policy) with
+ * initialize_default_state (ParticleSystem.hpp:370-395, :1163-1198). */
+int kpt_system_create(kpt_context* ctx, uint64_t count, uint64_t capacity,
+                      const kpt_particle_properties* properties, const kpt_split_policy* policy,
+                      kpt_system** out);
+int kpt_system_destroy(kpt_system* system);
+int kpt_system_count(const kpt_system* system, uint64_t* count, uint64_t* capacity);
+int kpt_system_set_count(kpt_system* system, uint64_t count);
+int kpt_system_upload(kpt_system* system, uint64_t n, const kpt_system_arrays* host);
+int kpt_system_download(const kpt_system* system, uint64_t n, const kpt_system_arrays* host);
+/* capture_previous_positions (ParticleSystem.hpp:623-629). */
+int kpt_system_capture_previous_positions(kpt_context* ctx, kpt_system* system);
+/* apply_grid_boundary_conditions, physical domain (ParticleSystem.hpp:653-699). */
+int kpt_system_apply_boundary(kpt_context* ctx, kpt_system* system, const kpt_grid* grid);
+/* sort_by_key(minimum_key, maximum_key) (ParticleSystem.hpp:723-759): a
+ * stable sort, so equal keys keep index order (the reference's BinSort
+ * leaves that order to its threads). */
+int kpt_system_sort_by_key(kpt_context* ctx, kpt_system* system, int32_t minimum_key,
+                           int32_t maximum_key);
+/* compact_active_particles (ParticleSystem.hpp:768-789). */
+int kpt_system_compact(kpt_context* ctx, kpt_system* system, uint64_t* active_count);
+/* split_particles_on_energy_growth (ParticleSystem.hpp:791-905); children
+ * in parent-index order (the serial order; the reference's atomics leave it
+ * to its threads). */
+int kpt_system_split_energy(kpt_context* ctx, kpt_system* system, kpt_split_statistics* out);
+/* reset_split_baselines (ParticleSystem.hpp:634-650). */
+int kpt_system_reset_split_baselines(kpt_context* ctx, kpt_system* system);
+
+/* ParkerSolver(particles, grid, B, V, coefficients) with the packed
+ * coefficient basis (ParkerSolver.hpp:122-198): basis holds, for every
+ * ghosted point of the grid (x fastest), 18 values B(3) V(3) drift curl(3)
+ * diffusion primary(3) secondary(3) kappa_par_1 kappa_perp_1 div V
+ * (ParkerSolver.hpp:96-116); constant_ratio selects the constant
+ * kappa_perp/kappa_par branch (secondary ignored).  courant: SolverBase's
+ * courant_scale (default 0.3). */
+int kpt_parker_solver_create(kpt_context* ctx, const kpt_grid* grid, const double* basis,
+                             int constant_ratio, double courant, kpt_parker_solver** out);
+int kpt_parker_solver_destroy(kpt_parker_solver* solver);
+/* set_coefficient_fields (ParkerSolver.hpp:157-163). */
+int kpt_parker_solver_set_basis(kpt_parker_solver* solver, const double* basis,
+                                int constant_ratio);
+int kpt_parker_solver_set_courant(kpt_parker_solver* solver, double courant);
+/* compute_adaptive_time_step (ParkerSolver.hpp:209-222): courant x the
+ * minimum local bound over active particles. */
+int kpt_parker_compute_time_step(kpt_context* ctx, kpt_parker_solver* solver,
+                                 kpt_system* system, double* dt);
+/* advance_stochastic / advance_sde (ParkerSolver.hpp:261-294): boundary
+ * conditions, adaptive dt, capture_previous_positions, Euler-Maruyama
+ * update, boundary conditions.  The noise is the keyed Philox stream of
+ * (seed, particle index, step); dt_used may be NULL. */
+int kpt_parker_advance_stochastic(kpt_context* ctx, kpt_parker_solver* solver,
+                                  kpt_system* system, uint64_t seed, uint32_t step,
+                                  double* dt_used);
+/* advance_deterministic (ParkerSolver.hpp:229-259). */
+int kpt_parker_advance_deterministic(kpt_context* ctx, kpt_parker_solver* solver,
+                                     kpt_system* system, double* dt_used);
+/* steps consecutive advance_stochastic calls (steps first_step ..
+ * first_step+steps-1) recorded once into a CUDA graph and replayed, the dt
+ * staying on the device between steps; dts (optional, steps entries)
+ * receives each step's dt.  Same results as the single-step calls.  No
+ * counterpart in the reference (a host loop of advance_stochastic). */
+int kpt_parker_advance_stochastic_steps(kpt_context* ctx, kpt_parker_solver* solver,
+                                        kpt_system* system, uint64_t seed, uint32_t first_step,
+                                        uint32_t steps, double* dts);
+
 #ifdef __cplusplus
 }
 #endif

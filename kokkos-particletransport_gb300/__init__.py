@@ -90,6 +90,39 @@ class SurrogateConfig(ctypes.Structure):
                [("seed", ctypes.c_uint64)]
 
 
+class ParticleProperties(ctypes.Structure):
+    """kpt_particle_properties (reference ParticleProperties)."""
+    _fields_ = [(n, ctypes.c_double) for n in ("rest_mass", "charge", "speed_of_light",
+                                               "energy_scale_erg")]
+
+
+class SplitPolicy(ctypes.Structure):
+    """kpt_split_policy (reference ParticleSplittingPolicy)."""
+    _fields_ = [("energy_split_ratio", ctypes.c_double),
+                ("minimum_child_weight", ctypes.c_double)]
+
+
+class SplitStatistics(ctypes.Structure):
+    """kpt_split_statistics (reference ParticleSplitStatistics)."""
+    _fields_ = [(n, ctypes.c_uint64) for n in ("active_count", "split_count",
+                                               "skipped_capacity_count",
+                                               "skipped_invalid_baseline_count",
+                                               "skipped_minimum_weight_count")]
+
+
+SYSTEM_DOUBLE_FIELDS = ("x", "y", "prev_x", "prev_y", "prevstep_x", "prevstep_y", "p", "mu",
+                        "w", "e0")
+SYSTEM_INT_FIELDS = ("status", "level", "key")
+
+
+class SystemArrays(ctypes.Structure):
+    """kpt_system_arrays: host pointers of the ParticleSystem storage."""
+    _fields_ = [("id", ctypes.c_void_p)] + \
+               [(n, ctypes.c_void_p) for n in ("x", "y", "prev_x", "prev_y", "prevstep_x",
+                                               "prevstep_y", "p", "mu", "weight", "e0",
+                                               "status", "split_level", "sort_key")]
+
+
 class ParticleArrays(ctypes.Structure):
     _fields_ = [(n, ctypes.c_void_p) for n in
                 ("x", "y", "p", "t", "step_dt", "weight", "mu", "status", "split_level")]
@@ -151,6 +184,28 @@ def load_library() -> ctypes.CDLL:
         "kpt_surrogate_gradient": (i32, [vp, vp, u64, vp, vp, vp, vp]),
         "kpt_context_set_surrogate": (i32, [vp, vp]),
         "kpt_surrogate_judge": (i32, [vp, vp, vp, vp, vp]),
+        "kpt_grid_create": (i32, [vp, i32, i32, vp, vp, vp, pvp]),
+        "kpt_grid_destroy": (i32, [vp]),
+        "kpt_system_create": (i32, [vp, u64, u64, vp, vp, pvp]),
+        "kpt_system_destroy": (i32, [vp]),
+        "kpt_system_count": (i32, [vp, vp, vp]),
+        "kpt_system_set_count": (i32, [vp, u64]),
+        "kpt_system_upload": (i32, [vp, u64, vp]),
+        "kpt_system_download": (i32, [vp, u64, vp]),
+        "kpt_system_capture_previous_positions": (i32, [vp, vp]),
+        "kpt_system_apply_boundary": (i32, [vp, vp, vp]),
+        "kpt_system_sort_by_key": (i32, [vp, vp, ctypes.c_int32, ctypes.c_int32]),
+        "kpt_system_compact": (i32, [vp, vp, vp]),
+        "kpt_system_split_energy": (i32, [vp, vp, vp]),
+        "kpt_system_reset_split_baselines": (i32, [vp, vp]),
+        "kpt_parker_solver_create": (i32, [vp, vp, vp, i32, dbl, pvp]),
+        "kpt_parker_solver_destroy": (i32, [vp]),
+        "kpt_parker_solver_set_basis": (i32, [vp, vp, i32]),
+        "kpt_parker_solver_set_courant": (i32, [vp, dbl]),
+        "kpt_parker_compute_time_step": (i32, [vp, vp, vp, vp]),
+        "kpt_parker_advance_stochastic": (i32, [vp, vp, vp, u64, u32, vp]),
+        "kpt_parker_advance_deterministic": (i32, [vp, vp, vp, vp]),
+        "kpt_parker_advance_stochastic_steps": (i32, [vp, vp, vp, u64, u32, u32, vp]),
     }
     for name, (restype, argtypes) in sig.items():
         fn = getattr(lib, name)
@@ -356,6 +411,37 @@ class Context:
                                                ctypes.byref(loss)))
         return float(loss.value), grad
 
+    # -- header library (ParkerSolver / ParticleSystem) --------------------
+    def grid(self, x_edges, y_edges, periodic=(1, 1)) -> "LibGrid":
+        xe = np.ascontiguousarray(x_edges, dtype=np.float64)
+        ye = np.ascontiguousarray(y_edges, dtype=np.float64)
+        per = np.ascontiguousarray(periodic, dtype=np.int32)
+        handle = ctypes.c_void_p()
+        _check(self.lib.kpt_grid_create(self.handle, xe.size - 1, ye.size - 1, _ptr(xe),
+                                        _ptr(ye), _ptr(per), ctypes.byref(handle)))
+        return self._adopt(LibGrid(self, handle, xe.size - 1, ye.size - 1))
+
+    def system(self, count: int, capacity: int, rest_mass=1.0, charge=1.0, speed_of_light=1.0,
+               energy_scale_erg=1.0, split_ratio=2.0, min_child_weight=0.0) -> "ParticleSystem":
+        props = ParticleProperties(rest_mass, charge, speed_of_light, energy_scale_erg)
+        policy = SplitPolicy(split_ratio, min_child_weight)
+        handle = ctypes.c_void_p()
+        _check(self.lib.kpt_system_create(self.handle, int(count), int(capacity),
+                                          ctypes.byref(props), ctypes.byref(policy),
+                                          ctypes.byref(handle)))
+        return self._adopt(ParticleSystem(self, handle))
+
+    def parker_solver(self, grid: "LibGrid", basis: np.ndarray, constant_ratio: bool = False,
+                      courant: float = 0.3) -> "ParkerSolver":
+        basis = np.ascontiguousarray(basis, dtype=np.float64)
+        if basis.shape != (grid.points, 18):
+            raise ValueError(f"basis must be ({grid.points}, 18)")
+        handle = ctypes.c_void_p()
+        _check(self.lib.kpt_parker_solver_create(self.handle, grid.handle, _ptr(basis),
+                                                 int(constant_ratio), float(courant),
+                                                 ctypes.byref(handle)))
+        return self._adopt(ParkerSolver(self, handle))
+
     def sample(self, lower: "Field", upper: "Field", x, y, rt,
                time_interpolation: int = 1) -> np.ndarray:
         x = np.ascontiguousarray(x, dtype=np.float64)
@@ -445,6 +531,149 @@ class Surrogate:
                                                    1 if tensor_cores else 0, _ptr(out),
                                                    _ptr(served)))
         return out, served.astype(bool)
+
+
+class _Handle:
+    _destroy = ""
+
+    def __init__(self, ctx: Context, handle: ctypes.c_void_p):
+        self.ctx = ctx
+        self.handle = handle
+
+    def close(self) -> None:
+        if self.handle:
+            getattr(self.ctx.lib, self._destroy)(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class LibGrid(_Handle):
+    """Uniform 2D Cartesian grid of the header library (kpt_grid)."""
+    _destroy = "kpt_grid_destroy"
+
+    def __init__(self, ctx, handle, nx, ny):
+        super().__init__(ctx, handle)
+        self.nx, self.ny = nx, ny
+        self.points = (nx + 4) * (ny + 4)
+
+
+class ParticleSystem(_Handle):
+    """Header-library particle container (kpt_system, reference ParticleSystem<2>)."""
+    _destroy = "kpt_system_destroy"
+
+    @property
+    def count(self) -> int:
+        c = ctypes.c_uint64()
+        _check(self.ctx.lib.kpt_system_count(self.handle, ctypes.byref(c), None))
+        return int(c.value)
+
+    @property
+    def capacity(self) -> int:
+        c = ctypes.c_uint64()
+        _check(self.ctx.lib.kpt_system_count(self.handle, None, ctypes.byref(c)))
+        return int(c.value)
+
+    def set_count(self, count: int) -> None:
+        _check(self.ctx.lib.kpt_system_set_count(self.handle, int(count)))
+
+    @staticmethod
+    def _arrays(data: Dict[str, np.ndarray]) -> SystemArrays:
+        a = SystemArrays()
+        a.id = data["id"].ctypes.data
+        names = dict(zip(("x", "y", "prev_x", "prev_y", "prevstep_x", "prevstep_y", "p", "mu",
+                          "weight", "e0", "status", "split_level", "sort_key"),
+                         SYSTEM_DOUBLE_FIELDS + SYSTEM_INT_FIELDS))
+        for field, key in names.items():
+            setattr(a, field, data[key].ctypes.data)
+        return a
+
+    def upload(self, data: Dict[str, np.ndarray], n: Optional[int] = None) -> None:
+        n = self.capacity if n is None else int(n)
+        conv = {"id": np.ascontiguousarray(data["id"][:n], dtype=np.uint64)}
+        for k in SYSTEM_DOUBLE_FIELDS:
+            conv[k] = np.ascontiguousarray(data[k][:n], dtype=np.float64)
+        for k in SYSTEM_INT_FIELDS:
+            conv[k] = np.ascontiguousarray(data[k][:n], dtype=np.int32)
+        _check(self.ctx.lib.kpt_system_upload(self.handle, n, ctypes.byref(self._arrays(conv))))
+
+    def download(self, n: Optional[int] = None) -> Dict[str, np.ndarray]:
+        n = self.capacity if n is None else int(n)
+        out = {"id": np.zeros(n, dtype=np.uint64)}
+        for k in SYSTEM_DOUBLE_FIELDS:
+            out[k] = np.zeros(n, dtype=np.float64)
+        for k in SYSTEM_INT_FIELDS:
+            out[k] = np.zeros(n, dtype=np.int32)
+        _check(self.ctx.lib.kpt_system_download(self.handle, n, ctypes.byref(self._arrays(out))))
+        return out
+
+    def capture_previous_positions(self) -> None:
+        _check(self.ctx.lib.kpt_system_capture_previous_positions(self.ctx.handle, self.handle))
+
+    def apply_boundary(self, grid: LibGrid) -> None:
+        _check(self.ctx.lib.kpt_system_apply_boundary(self.ctx.handle, self.handle, grid.handle))
+
+    def sort_by_key(self, lo: int, hi: int) -> None:
+        _check(self.ctx.lib.kpt_system_sort_by_key(self.ctx.handle, self.handle, int(lo),
+                                                   int(hi)))
+
+    def compact(self) -> int:
+        c = ctypes.c_uint64()
+        _check(self.ctx.lib.kpt_system_compact(self.ctx.handle, self.handle, ctypes.byref(c)))
+        return int(c.value)
+
+    def split_energy(self) -> Dict[str, int]:
+        st = SplitStatistics()
+        _check(self.ctx.lib.kpt_system_split_energy(self.ctx.handle, self.handle,
+                                                    ctypes.byref(st)))
+        return {name: int(getattr(st, name)) for name, _ in SplitStatistics._fields_}
+
+    def reset_split_baselines(self) -> None:
+        _check(self.ctx.lib.kpt_system_reset_split_baselines(self.ctx.handle, self.handle))
+
+
+class ParkerSolver(_Handle):
+    """Header-library Parker solver (kpt_parker_solver, reference ParkerSolver)."""
+    _destroy = "kpt_parker_solver_destroy"
+
+    def set_courant(self, courant: float) -> None:
+        _check(self.ctx.lib.kpt_parker_solver_set_courant(self.handle, float(courant)))
+
+    def set_basis(self, basis: np.ndarray, constant_ratio: bool = False) -> None:
+        basis = np.ascontiguousarray(basis, dtype=np.float64)
+        _check(self.ctx.lib.kpt_parker_solver_set_basis(self.handle, _ptr(basis),
+                                                        int(constant_ratio)))
+
+    def compute_time_step(self, system: ParticleSystem) -> float:
+        dt = ctypes.c_double()
+        _check(self.ctx.lib.kpt_parker_compute_time_step(self.ctx.handle, self.handle,
+                                                         system.handle, ctypes.byref(dt)))
+        return float(dt.value)
+
+    def advance_stochastic(self, system: ParticleSystem, seed: int, step: int) -> float:
+        dt = ctypes.c_double()
+        _check(self.ctx.lib.kpt_parker_advance_stochastic(self.ctx.handle, self.handle,
+                                                          system.handle, int(seed), int(step),
+                                                          ctypes.byref(dt)))
+        return float(dt.value)
+
+    def advance_deterministic(self, system: ParticleSystem) -> float:
+        dt = ctypes.c_double()
+        _check(self.ctx.lib.kpt_parker_advance_deterministic(self.ctx.handle, self.handle,
+                                                             system.handle, ctypes.byref(dt)))
+        return float(dt.value)
+
+    def advance_stochastic_steps(self, system: ParticleSystem, seed: int, first_step: int,
+                                 steps: int) -> np.ndarray:
+        dts = np.zeros(max(1, steps), dtype=np.float64)
+        _check(self.ctx.lib.kpt_parker_advance_stochastic_steps(
+            self.ctx.handle, self.handle, system.handle, int(seed), int(first_step), int(steps),
+            _ptr(dts)))
+        return dts[:steps]
 
 
 class ParticleStorage:

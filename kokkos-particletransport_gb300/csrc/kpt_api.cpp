@@ -1639,3 +1639,558 @@ int kpt_sample_table(kpt_context* ctx, const kpt_field* lower, const kpt_field* 
 }
 
 }  // extern "C"
+
+// ====================================================================
+// Header-library step API: ParkerSolver / ParticleSystem (2D Cartesian)
+// ====================================================================
+
+struct kpt_grid {
+    kpt_context* ctx = nullptr;
+    int device = 0;
+    int nx = 0, ny = 0;
+    kpt::LibGrid g{};
+};
+
+struct kpt_system {
+    kpt_context* ctx = nullptr;
+    int device = 0;
+    uint64_t count = 0;
+    uint64_t capacity = 0;
+    kpt_particle_properties props{};
+    kpt_split_policy policy{};
+    void* block = nullptr;
+    kpt::SystemArrays a{};
+    DeviceBuffer flags, block_counts, tallies;
+    DeviceBuffer keys_a, keys_b, idx_a, idx_b, hist, staging, scalars;
+};
+
+struct kpt_parker_solver {
+    kpt_context* ctx = nullptr;
+    int device = 0;
+    kpt::LibGrid grid{};
+    uint64_t points = 0;
+    double* basis = nullptr;
+    int constant_ratio = 0;
+    double courant = 0.3;
+    DeviceBuffer terms;
+    // min bits (u64), dt (f64), error (i32 + pad), error index (u64)
+    DeviceBuffer scalars;
+    DeviceBuffer dt_history;
+};
+
+namespace {
+
+const char* lib_error_message(int code) {
+    switch (code) {
+        case 1: return "FieldInterpolator: position lies outside the interpolation domain.";
+        case 2: return "ParkerSolver: stochastic diffusion requires |B| > 0.";
+        case 3: return "ParkerSolver: diffusion coefficients must be finite and non-negative.";
+        case 4: return "ParkerSolver: projected diffusion coefficient is invalid.";
+        case 5: return "ParkerSolver: local physical cell width must be positive.";
+        case 7: return "ParkerSolver: adaptive deterministic time step is not positive and finite.";
+        default: return "ParkerSolver: adaptive stochastic time step is not positive and finite.";
+    }
+}
+
+int validate_properties(const kpt_particle_properties* p) {
+    // ParticleProperties::validate (ParticleSystem.hpp:152-164)
+    KPT_REQUIRE(p != nullptr, "ParticleProperties: NULL");
+    if (!std::isfinite(p->rest_mass) || p->rest_mass <= 0.0 || !std::isfinite(p->charge) ||
+        !std::isfinite(p->speed_of_light) || p->speed_of_light <= 0.0 ||
+        !std::isfinite(p->energy_scale_erg) || p->energy_scale_erg <= 0.0) {
+        return set_error(KPT_ERROR_INVALID_ARGUMENT,
+                         "ParticleProperties: rest mass and speed of light must be positive "
+                         "finite dimensionless values, charge must be finite, and the energy "
+                         "scale must be positive and finite.");
+    }
+    return KPT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int kpt_grid_create(kpt_context* ctx, int nx, int ny, const double* x_edges,
+                    const double* y_edges, const int32_t* periodic, kpt_grid** out) {
+    KPT_REQUIRE(ctx && x_edges && y_edges && periodic && out, "kpt_grid_create: NULL argument");
+    *out = nullptr;
+    KPT_REQUIRE(nx > 0 && ny > 0, "kpt_grid_create: nx and ny must be positive");
+    std::unique_ptr<kpt_grid> g(new kpt_grid());
+    g->ctx = ctx;
+    g->device = ctx->device;
+    g->nx = nx;
+    g->ny = ny;
+    const double* edges[2] = {x_edges, y_edges};
+    const int counts[2] = {nx, ny};
+    for (int dim = 0; dim < 2; ++dim) {
+        const double* e = edges[dim];
+        const int n = counts[dim];
+        for (int i = 0; i <= n; ++i) {
+            KPT_REQUIRE(std::isfinite(e[i]) && (i == 0 || e[i] > e[i - 1]),
+                        "kpt_grid_create: face coordinates must be finite and strictly ascending");
+        }
+        double step = 0.0;
+        KPT_REQUIRE(edges_uniform(e, n, &step),
+                    "kpt_grid_create: the library grid needs uniform edges");
+        kpt::LibAxis& a = g->g.axis[dim];
+        a.n = n;
+        a.periodic = periodic[dim] != 0 ? 1 : 0;
+        a.x0 = e[0];
+        a.dx = step;
+        // AnalyticCoordinateMapping face coordinates x0 + i dx
+        // (MappedCoordinateGrid.hpp:118-147)
+        a.lower = a.x0 + 0.0 * a.dx;
+        a.upper = a.x0 + static_cast<double>(n) * a.dx;
+        a.ghost_lower = a.x0 + (-2.0) * a.dx;
+        a.ghost_upper = a.x0 + static_cast<double>(n + 2) * a.dx;
+        a.width = a.upper - a.lower;
+        a.inv_width = a.width != 0.0 ? 1.0 / a.width : 0.0;
+    }
+    g->g.ex = nx + 4;
+    *out = g.release();
+    return KPT_OK;
+}
+
+int kpt_grid_destroy(kpt_grid* grid) {
+    delete grid;
+    return KPT_OK;
+}
+
+int kpt_system_create(kpt_context* ctx, uint64_t count, uint64_t capacity,
+                      const kpt_particle_properties* properties, const kpt_split_policy* policy,
+                      kpt_system** out) {
+    KPT_REQUIRE(ctx && out, "kpt_system_create: NULL argument");
+    *out = nullptr;
+    if (int rc = validate_properties(properties)) return rc;
+    kpt_split_policy pol{2.0, 0.0};
+    if (policy != nullptr) pol = *policy;
+    // ParticleSplittingPolicy::validate (ParticleSystem.hpp:287-294)
+    KPT_REQUIRE(std::isfinite(pol.energy_split_ratio) && pol.energy_split_ratio > 1.0 &&
+                    std::isfinite(pol.minimum_child_weight) && pol.minimum_child_weight >= 0.0,
+                "ParticleSplittingPolicy: energy split ratio must be greater than one and "
+                "minimum child weight must be finite and non-negative.");
+    KPT_REQUIRE(capacity >= count,
+                "ParticleSystem: capacity must be greater than or equal to count.");
+    KPT_REQUIRE(capacity < (1ull << 31), "kpt_system_create: capacity must be below 2^31");
+    if (int rc = activate(ctx)) return rc;
+    std::unique_ptr<kpt_system> sys(new kpt_system());
+    sys->ctx = ctx;
+    sys->device = ctx->device;
+    sys->count = count;
+    sys->capacity = capacity;
+    sys->props = *properties;
+    sys->policy = pol;
+    const size_t cap = capacity > 0 ? capacity : 1;
+    const size_t dbytes = (cap * sizeof(double) + 255) & ~size_t(255);
+    const size_t ibytes = (cap * sizeof(int32_t) + 255) & ~size_t(255);
+    const size_t total = 12 * dbytes + 3 * ibytes;  // id (8 B) + 11 doubles
+    KPT_CUDA(cudaMalloc(&sys->block, total));
+    char* base = static_cast<char*>(sys->block);
+    kpt::SystemArrays& a = sys->a;
+    a.id = reinterpret_cast<uint64_t*>(base);
+    double** dptrs[11] = {&a.x, &a.y, &a.prev_x, &a.prev_y, &a.prevstep_x, &a.prevstep_y,
+                          &a.p, &a.mu, &a.weight, &a.e0, nullptr};
+    for (int k = 0; k < 10; ++k) *dptrs[k] = reinterpret_cast<double*>(base + (k + 1) * dbytes);
+    a.status = reinterpret_cast<int*>(base + 12 * dbytes);
+    a.split_level = reinterpret_cast<int*>(base + 12 * dbytes + ibytes);
+    a.sort_key = reinterpret_cast<int*>(base + 12 * dbytes + 2 * ibytes);
+    KPT_CUDA(kpt::system_default_state(a, count, capacity, ctx->stream));
+    KPT_CUDA(cudaStreamSynchronize(ctx->stream));
+    *out = sys.release();
+    return KPT_OK;
+}
+
+int kpt_system_destroy(kpt_system* sys) {
+    if (sys == nullptr) return KPT_OK;
+    cudaSetDevice(sys->device);
+    cudaFree(sys->block);
+    for (DeviceBuffer* b : {&sys->flags, &sys->block_counts, &sys->tallies, &sys->keys_a,
+                            &sys->keys_b, &sys->idx_a, &sys->idx_b, &sys->hist, &sys->staging,
+                            &sys->scalars}) {
+        b->release();
+    }
+    delete sys;
+    return KPT_OK;
+}
+
+int kpt_system_count(const kpt_system* sys, uint64_t* count, uint64_t* capacity) {
+    KPT_REQUIRE(sys != nullptr, "kpt_system_count: NULL handle");
+    if (count) *count = sys->count;
+    if (capacity) *capacity = sys->capacity;
+    return KPT_OK;
+}
+
+int kpt_system_set_count(kpt_system* sys, uint64_t count) {
+    KPT_REQUIRE(sys != nullptr, "kpt_system_set_count: NULL handle");
+    KPT_REQUIRE(count <= sys->capacity, "kpt_system_set_count: count exceeds capacity");
+    sys->count = count;
+    return KPT_OK;
+}
+
+namespace {
+
+int system_copy(const kpt_system* sys, uint64_t n, const kpt_system_arrays* h, bool upload) {
+    KPT_REQUIRE(sys && h, "kpt_system copy: NULL argument");
+    KPT_REQUIRE(n <= sys->capacity, "kpt_system copy: n exceeds capacity");
+    KPT_CUDA(cudaSetDevice(sys->device));
+    const kpt::SystemArrays& a = sys->a;
+    cudaStream_t st = sys->ctx->stream;
+    struct Pair {
+        void* dev;
+        void* host;
+        size_t size;
+    } pairs[14] = {{a.id, h->id, 8},         {a.x, h->x, 8},
+                   {a.y, h->y, 8},           {a.prev_x, h->prev_x, 8},
+                   {a.prev_y, h->prev_y, 8}, {a.prevstep_x, h->prevstep_x, 8},
+                   {a.prevstep_y, h->prevstep_y, 8}, {a.p, h->p, 8},
+                   {a.mu, h->mu, 8},         {a.weight, h->weight, 8},
+                   {a.e0, h->e0, 8},         {a.status, h->status, 4},
+                   {a.split_level, h->split_level, 4}, {a.sort_key, h->sort_key, 4}};
+    for (const Pair& pr : pairs) {
+        if (pr.host == nullptr || n == 0) continue;
+        if (upload) {
+            KPT_CUDA(cudaMemcpyAsync(pr.dev, pr.host, n * pr.size, cudaMemcpyHostToDevice, st));
+        } else {
+            KPT_CUDA(cudaMemcpyAsync(pr.host, pr.dev, n * pr.size, cudaMemcpyDeviceToHost, st));
+        }
+    }
+    KPT_CUDA(cudaStreamSynchronize(st));
+    return KPT_OK;
+}
+
+}  // namespace
+
+int kpt_system_upload(kpt_system* sys, uint64_t n, const kpt_system_arrays* host) {
+    return system_copy(sys, n, host, true);
+}
+
+int kpt_system_download(const kpt_system* sys, uint64_t n, const kpt_system_arrays* host) {
+    return system_copy(sys, n, host, false);
+}
+
+int kpt_system_capture_previous_positions(kpt_context* ctx, kpt_system* sys) {
+    KPT_REQUIRE(ctx && sys, "kpt_system_capture_previous_positions: NULL handle");
+    if (int rc = activate(ctx)) return rc;
+    KPT_CUDA(kpt::system_capture(sys->a, sys->capacity, ctx->stream));
+    KPT_CUDA(cudaStreamSynchronize(ctx->stream));
+    return KPT_OK;
+}
+
+int kpt_system_apply_boundary(kpt_context* ctx, kpt_system* sys, const kpt_grid* grid) {
+    KPT_REQUIRE(ctx && sys && grid, "kpt_system_apply_boundary: NULL handle");
+    if (int rc = activate(ctx)) return rc;
+    KPT_CUDA(kpt::system_boundary(grid->g, sys->a, sys->count, ctx->stream));
+    KPT_CUDA(cudaStreamSynchronize(ctx->stream));
+    return KPT_OK;
+}
+
+int kpt_system_sort_by_key(kpt_context* ctx, kpt_system* sys, int32_t minimum_key,
+                           int32_t maximum_key) {
+    KPT_REQUIRE(ctx && sys, "kpt_system_sort_by_key: NULL handle");
+    if (sys->count <= 1 || minimum_key == maximum_key) return KPT_OK;
+    KPT_REQUIRE(maximum_key >= minimum_key, "ParticleSystem: invalid sort key range.");
+    if (int rc = activate(ctx)) return rc;
+    const uint64_t n = sys->count;
+    const uint64_t blocks = (n + 255) / 256;
+    KPT_CUDA(sys->keys_a.reserve(n * 4));
+    KPT_CUDA(sys->keys_b.reserve(n * 4));
+    KPT_CUDA(sys->idx_a.reserve(n * 4));
+    KPT_CUDA(sys->idx_b.reserve(n * 4));
+    KPT_CUDA(sys->hist.reserve(256 * blocks * 4));
+    KPT_CUDA(sys->staging.reserve(n * 8));
+    KPT_CUDA(sys->scalars.reserve(64));
+    kpt::LibSortLaunch L{};
+    L.sys = sys->a;
+    L.count = n;
+    L.lo = minimum_key;
+    L.hi = maximum_key;
+    L.keys_a = sys->keys_a.as<unsigned int>();
+    L.keys_b = sys->keys_b.as<unsigned int>();
+    L.idx_a = sys->idx_a.as<unsigned int>();
+    L.idx_b = sys->idx_b.as<unsigned int>();
+    L.hist = sys->hist.as<unsigned int>();
+    L.scratch_total = sys->scalars.as<unsigned long long>();
+    L.staging = sys->staging.ptr;
+    KPT_CUDA(kpt::system_sort(L, ctx->stream));
+    KPT_CUDA(cudaStreamSynchronize(ctx->stream));
+    return KPT_OK;
+}
+
+int kpt_system_compact(kpt_context* ctx, kpt_system* sys, uint64_t* active_count) {
+    KPT_REQUIRE(ctx && sys, "kpt_system_compact: NULL handle");
+    if (active_count) *active_count = 0;
+    if (sys->count == 0) return KPT_OK;
+    if (int rc = activate(ctx)) return rc;
+    KPT_CUDA(sys->scalars.reserve(64));
+    unsigned long long* active = sys->scalars.as<unsigned long long>() + 1;
+    KPT_CUDA(kpt::system_compact_keys(sys->a, sys->count, active, ctx->stream));
+    unsigned long long host = 0;
+    KPT_CUDA(cudaMemcpyAsync(&host, active, sizeof(host), cudaMemcpyDeviceToHost, ctx->stream));
+    KPT_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (int rc = kpt_system_sort_by_key(ctx, sys, 0, 1)) return rc;
+    sys->count = host;
+    if (active_count) *active_count = host;
+    return KPT_OK;
+}
+
+int kpt_system_split_energy(kpt_context* ctx, kpt_system* sys, kpt_split_statistics* out) {
+    KPT_REQUIRE(ctx && sys, "kpt_system_split_energy: NULL handle");
+    kpt_split_statistics stats{};
+    if (out) *out = stats;
+    if (sys->count == 0 || sys->count >= sys->capacity) return KPT_OK;
+    if (int rc = activate(ctx)) return rc;
+    const uint64_t n = sys->count;
+    const uint64_t blocks = (n + 255) / 256;
+    KPT_REQUIRE(blocks <= 1024ull * 1024ull, "kpt_system_split_energy: too many particles");
+    KPT_CUDA(sys->flags.reserve(n * sizeof(int)));
+    KPT_CUDA(sys->block_counts.reserve(blocks * sizeof(unsigned int)));
+    KPT_CUDA(sys->tallies.reserve(8 * sizeof(unsigned long long)));
+    KPT_CUDA(cudaMemsetAsync(sys->tallies.ptr, 0, 8 * sizeof(unsigned long long), ctx->stream));
+    kpt::LibSplitLaunch L{};
+    L.sys = sys->a;
+    L.count = n;
+    L.capacity = sys->capacity;
+    L.rest_mass = sys->props.rest_mass;
+    L.speed_of_light = sys->props.speed_of_light;
+    L.mc = sys->props.rest_mass * sys->props.speed_of_light;
+    L.split_ratio = sys->policy.energy_split_ratio;
+    L.log_split_ratio = std::log(sys->policy.energy_split_ratio);
+    L.min_child_weight = sys->policy.minimum_child_weight;
+    L.flags = sys->flags.as<int>();
+    L.block_counts = sys->block_counts.as<unsigned int>();
+    L.tallies = sys->tallies.as<unsigned long long>();
+    KPT_CUDA(kpt::system_split(L, ctx->stream));
+    unsigned long long host[8] = {};
+    KPT_CUDA(cudaMemcpyAsync(host, L.tallies, sizeof(host), cudaMemcpyDeviceToHost, ctx->stream));
+    KPT_CUDA(cudaStreamSynchronize(ctx->stream));
+    // tallies: 0 active, 1 skipped capacity, 2 invalid baseline, 3 min weight, 4 wanted
+    const uint64_t available = sys->capacity - n;
+    const uint64_t appended = std::min<uint64_t>(host[4], available);
+    sys->count = n + appended;
+    stats.active_count = host[0];
+    stats.split_count = appended;
+    stats.skipped_capacity_count = host[1];
+    stats.skipped_invalid_baseline_count = host[2];
+    stats.skipped_minimum_weight_count = host[3];
+    if (out) *out = stats;
+    return KPT_OK;
+}
+
+int kpt_system_reset_split_baselines(kpt_context* ctx, kpt_system* sys) {
+    KPT_REQUIRE(ctx && sys, "kpt_system_reset_split_baselines: NULL handle");
+    if (int rc = activate(ctx)) return rc;
+    kpt::LibSplitLaunch L{};
+    L.sys = sys->a;
+    L.count = sys->count;
+    L.capacity = sys->capacity;
+    L.rest_mass = sys->props.rest_mass;
+    L.speed_of_light = sys->props.speed_of_light;
+    L.mc = sys->props.rest_mass * sys->props.speed_of_light;
+    KPT_CUDA(kpt::system_reset_baselines(L, ctx->stream));
+    KPT_CUDA(cudaStreamSynchronize(ctx->stream));
+    return KPT_OK;
+}
+
+int kpt_parker_solver_create(kpt_context* ctx, const kpt_grid* grid, const double* basis,
+                             int constant_ratio, double courant, kpt_parker_solver** out) {
+    KPT_REQUIRE(ctx && grid && basis && out, "kpt_parker_solver_create: NULL argument");
+    *out = nullptr;
+    if (int rc = activate(ctx)) return rc;
+    std::unique_ptr<kpt_parker_solver> s(new kpt_parker_solver());
+    s->ctx = ctx;
+    s->device = ctx->device;
+    s->grid = grid->g;
+    s->points = static_cast<uint64_t>(grid->nx + 4) * static_cast<uint64_t>(grid->ny + 4);
+    s->courant = courant;
+    KPT_CUDA(cudaMalloc(&s->basis, s->points * kpt::kLibBasisStride * sizeof(double)));
+    KPT_CUDA(s->scalars.reserve(64));
+    kpt_parker_solver* raw = s.release();
+    if (int rc = kpt_parker_solver_set_basis(raw, basis, constant_ratio)) {
+        kpt_parker_solver_destroy(raw);
+        return rc;
+    }
+    *out = raw;
+    return KPT_OK;
+}
+
+int kpt_parker_solver_destroy(kpt_parker_solver* s) {
+    if (s == nullptr) return KPT_OK;
+    cudaSetDevice(s->device);
+    cudaFree(s->basis);
+    s->terms.release();
+    s->scalars.release();
+    s->dt_history.release();
+    delete s;
+    return KPT_OK;
+}
+
+int kpt_parker_solver_set_basis(kpt_parker_solver* s, const double* basis, int constant_ratio) {
+    KPT_REQUIRE(s && basis, "kpt_parker_solver_set_basis: NULL argument");
+    KPT_CUDA(cudaSetDevice(s->device));
+    KPT_CUDA(cudaMemcpy(s->basis, basis, s->points * kpt::kLibBasis * sizeof(double),
+                        cudaMemcpyHostToDevice));
+    s->constant_ratio = constant_ratio != 0 ? 1 : 0;
+    return KPT_OK;
+}
+
+int kpt_parker_solver_set_courant(kpt_parker_solver* s, double courant) {
+    KPT_REQUIRE(s != nullptr, "kpt_parker_solver_set_courant: NULL handle");
+    s->courant = courant;
+    return KPT_OK;
+}
+
+namespace {
+
+// validate_for_deterministic_step (ParkerSolver.hpp:311-340).
+int parker_validate(const kpt_parker_solver* s, const kpt_system* sys) {
+    if (!std::isfinite(s->courant) || s->courant <= 0.0) {
+        return set_error(KPT_ERROR_INVALID_ARGUMENT,
+                         "ParkerSolver: Courant scale must be positive and finite.");
+    }
+    if (!std::isfinite(sys->props.charge) || sys->props.charge == 0.0) {
+        return set_error(KPT_ERROR_INVALID_ARGUMENT,
+                         "ParkerSolver: Parker drift requires a finite nonzero particle charge.");
+    }
+    return KPT_OK;
+}
+
+int parker_launch(kpt_context* ctx, kpt_parker_solver* s, kpt_system* sys, int advance,
+                  int stochastic, uint64_t seed, uint32_t step, double* dt_history,
+                  kpt::LibParkerLaunch* out) {
+    KPT_CUDA(s->terms.reserve(std::max<uint64_t>(sys->count, 1) * kpt::kLibTermCount *
+                              sizeof(double)));
+    kpt::LibParkerLaunch& L = *out;
+    L = kpt::LibParkerLaunch{};
+    L.grid = s->grid;
+    L.basis = s->basis;
+    L.constant_ratio = s->constant_ratio;
+    L.sys = sys->a;
+    L.count = sys->count;
+    L.capacity = sys->capacity;
+    L.rest_mass = sys->props.rest_mass;
+    L.charge = sys->props.charge;
+    L.speed_of_light = sys->props.speed_of_light;
+    L.mc = sys->props.rest_mass * sys->props.speed_of_light;
+    L.courant = s->courant;
+    L.terms = s->terms.as<double>();
+    char* sc = static_cast<char*>(s->scalars.ptr);
+    L.min_bits = reinterpret_cast<unsigned long long*>(sc);
+    L.dt_device_out = reinterpret_cast<double*>(sc + 8);
+    L.error = reinterpret_cast<int*>(sc + 16);
+    L.error_index = reinterpret_cast<unsigned long long*>(sc + 24);
+    L.dt_history = dt_history;
+    L.apply_boundary = advance;
+    L.advance = advance;
+    L.stochastic = stochastic;
+    L.capture = 1;
+    L.key = make_uint2(static_cast<uint32_t>(seed), static_cast<uint32_t>(seed >> 32));
+    L.frame = step;
+    return KPT_OK;
+}
+
+int parker_finish(kpt_context* ctx, kpt_parker_solver* s, double* dt_out, bool stochastic) {
+    char host[32];
+    KPT_CUDA(cudaMemcpyAsync(host, s->scalars.ptr, sizeof(host), cudaMemcpyDeviceToHost,
+                             ctx->stream));
+    KPT_CUDA(cudaStreamSynchronize(ctx->stream));
+    double dt;
+    int error;
+    unsigned long long index;
+    std::memcpy(&dt, host + 8, sizeof(dt));
+    std::memcpy(&error, host + 16, sizeof(error));
+    std::memcpy(&index, host + 24, sizeof(index));
+    if (dt_out) *dt_out = dt;
+    if (error != 0) {
+        std::string msg = lib_error_message(error == 6 && !stochastic ? 7 : error);
+        if (error != 6) msg += " (particle " + std::to_string(index) + ")";
+        return set_error(KPT_ERROR_INVALID_ARGUMENT, msg);
+    }
+    return KPT_OK;
+}
+
+int parker_step(kpt_context* ctx, kpt_parker_solver* s, kpt_system* sys, int advance,
+                int stochastic, uint64_t seed, uint32_t step, double* dt_out) {
+    KPT_REQUIRE(ctx && s && sys, "ParkerSolver: NULL handle");
+    if (int rc = parker_validate(s, sys)) return rc;
+    if (int rc = activate(ctx)) return rc;
+    kpt::LibParkerLaunch L;
+    if (int rc = parker_launch(ctx, s, sys, advance, stochastic, seed, step, nullptr, &L)) {
+        return rc;
+    }
+    KPT_CUDA(cudaMemsetAsync(s->scalars.ptr, 0, 32, ctx->stream));
+    KPT_CUDA(kpt::lib_parker_step(L, ctx->stream));
+    return parker_finish(ctx, s, dt_out, stochastic != 0);
+}
+
+}  // namespace
+
+int kpt_parker_compute_time_step(kpt_context* ctx, kpt_parker_solver* s, kpt_system* sys,
+                                 double* dt) {
+    return parker_step(ctx, s, sys, 0, 0, 0, 0, dt);
+}
+
+int kpt_parker_advance_stochastic(kpt_context* ctx, kpt_parker_solver* s, kpt_system* sys,
+                                  uint64_t seed, uint32_t step, double* dt_used) {
+    return parker_step(ctx, s, sys, 1, 1, seed, step, dt_used);
+}
+
+int kpt_parker_advance_deterministic(kpt_context* ctx, kpt_parker_solver* s, kpt_system* sys,
+                                     double* dt_used) {
+    return parker_step(ctx, s, sys, 1, 0, 0, 0, dt_used);
+}
+
+int kpt_parker_advance_stochastic_steps(kpt_context* ctx, kpt_parker_solver* s,
+                                        kpt_system* sys, uint64_t seed, uint32_t first_step,
+                                        uint32_t steps, double* dts) {
+    KPT_REQUIRE(ctx && s && sys, "ParkerSolver: NULL handle");
+    if (steps == 0) return KPT_OK;
+    if (int rc = parker_validate(s, sys)) return rc;
+    if (int rc = activate(ctx)) return rc;
+    KPT_CUDA(s->dt_history.reserve(static_cast<size_t>(steps) * sizeof(double)));
+    KPT_CUDA(cudaMemsetAsync(s->scalars.ptr, 0, 32, ctx->stream));
+    std::vector<kpt::LibParkerLaunch> launches(steps);
+    for (uint32_t k = 0; k < steps; ++k) {
+        if (int rc = parker_launch(ctx, s, sys, 1, 1, seed, first_step + k,
+                                   s->dt_history.as<double>() + k, &launches[k])) {
+            return rc;
+        }
+    }
+    // Record the step sequence once and replay it; a stream that cannot be
+    // captured (the legacy default stream) runs the same launches directly.
+    cudaGraph_t graph = nullptr;
+    bool captured = false;
+    if (ctx->stream != nullptr &&
+        cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        cudaError_t err = cudaSuccess;
+        for (uint32_t k = 0; k < steps && err == cudaSuccess; ++k) {
+            err = kpt::lib_parker_step(launches[k], ctx->stream);
+        }
+        const cudaError_t end = cudaStreamEndCapture(ctx->stream, &graph);
+        KPT_CUDA(err);
+        KPT_CUDA(end);
+        captured = true;
+    }
+    if (captured) {
+        cudaGraphExec_t exec = nullptr;
+        const cudaError_t inst = cudaGraphInstantiate(&exec, graph, 0);
+        if (inst != cudaSuccess) {
+            cudaGraphDestroy(graph);
+            KPT_CUDA(inst);
+        }
+        const cudaError_t run = cudaGraphLaunch(exec, ctx->stream);
+        cudaGraphExecDestroy(exec);
+        cudaGraphDestroy(graph);
+        KPT_CUDA(run);
+    } else {
+        for (uint32_t k = 0; k < steps; ++k) {
+            KPT_CUDA(kpt::lib_parker_step(launches[k], ctx->stream));
+        }
+    }
+    if (dts) {
+        KPT_CUDA(cudaMemcpyAsync(dts, s->dt_history.ptr, steps * sizeof(double),
+                                 cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    return parker_finish(ctx, s, nullptr, true);
+}
+
+}  // extern "C"

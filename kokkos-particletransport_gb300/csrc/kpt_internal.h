@@ -171,6 +171,90 @@ cudaError_t surrogate_eval(int n, const double* inputs, const SurrogateBox& box,
                            const float* params, const uint2* block, bool tensor, double* out,
                            int* served, cudaStream_t stream);
 
+// ---- header library (ParkerSolver / ParticleSystem), 2D Cartesian ---------
+// One axis of an analytic uniform grid (AnalyticCoordinateGrid.hpp) with the
+// MappedCoordinateGrid bound caches (MappedCoordinateGrid.hpp:118-147).
+struct LibAxis {
+    int n;
+    int periodic;
+    double x0, dx;
+    double lower, upper;              // faces 0 and n
+    double ghost_lower, ghost_upper;  // faces -2 and n+2
+    double width, inv_width;          // periodic width (upper - lower) and 1/width
+};
+struct LibGrid {
+    LibAxis axis[2];
+    int ex;  // nx + 4 (ghosted points per row)
+};
+
+// ParticleSystem storage (ParticleSystem.hpp:340-350), SpaceDim 2.
+struct SystemArrays {
+    uint64_t* id;
+    double *x, *y, *prev_x, *prev_y, *prevstep_x, *prevstep_y, *p, *mu, *weight, *e0;
+    int *status, *split_level, *sort_key;
+};
+
+// Packed Parker coefficient basis (ParkerSolver.hpp:96-116) for VecDim 3:
+// B(3) V(3) drift curl(3) primary(3) secondary(3) kappa_par kappa_perp divV.
+constexpr int kLibBasis = 18;
+constexpr int kLibBasisStride = 18;
+constexpr int kLibTermCount = 9;
+
+struct LibParkerLaunch {
+    LibGrid grid;
+    const double* basis;  // ghosted points x kLibBasisStride
+    int constant_ratio;
+    SystemArrays sys;
+    uint64_t count, capacity;
+    double rest_mass, charge, speed_of_light, mc;
+    double courant;
+    double* terms;                  // count x kLibTermCount
+    unsigned long long* min_bits;   // global minimum of the local dt bounds
+    double* dt_device_out;          // courant * min (device)
+    double* dt_history;             // optional per-step record (device)
+    const double* dt_device;        // advance: dt read from the device
+    double dt;
+    int apply_boundary;             // boundary conditions before the terms
+    int advance;                    // run the update pass
+    int stochastic;
+    int capture;                    // rotate previous positions
+    uint2 key;
+    uint32_t frame;
+    int* error;                     // first abort condition met (code)
+    unsigned long long* error_index;
+};
+cudaError_t lib_parker_step(const LibParkerLaunch& launch, cudaStream_t stream);
+
+struct LibSplitLaunch {
+    SystemArrays sys;
+    uint64_t count, capacity;
+    double rest_mass, speed_of_light, mc;
+    double split_ratio, log_split_ratio, min_child_weight;
+    int* flags;                    // count
+    unsigned int* block_counts;    // one per 256 particles
+    unsigned long long* tallies;   // active, skipped capacity, invalid baseline, min weight, wanted
+};
+cudaError_t system_split(const LibSplitLaunch& launch, cudaStream_t stream);
+cudaError_t system_reset_baselines(const LibSplitLaunch& launch, cudaStream_t stream);
+
+struct LibSortLaunch {
+    SystemArrays sys;
+    uint64_t count;
+    int lo, hi;
+    unsigned int *keys_a, *keys_b, *idx_a, *idx_b;
+    unsigned int* hist;            // 256 x blocks
+    unsigned long long* scratch_total;
+    void* staging;                 // count x 8 bytes
+};
+cudaError_t system_sort(const LibSortLaunch& launch, cudaStream_t stream);
+cudaError_t system_default_state(const SystemArrays& s, uint64_t count, uint64_t capacity,
+                                 cudaStream_t stream);
+cudaError_t system_boundary(const LibGrid& g, const SystemArrays& s, uint64_t count,
+                            cudaStream_t stream);
+cudaError_t system_capture(const SystemArrays& s, uint64_t capacity, cudaStream_t stream);
+cudaError_t system_compact_keys(const SystemArrays& s, uint64_t count,
+                                unsigned long long* active, cudaStream_t stream);
+
 struct SampleLaunch {
     Grid grid;
     const void* lower;

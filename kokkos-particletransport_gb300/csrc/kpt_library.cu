@@ -1,0 +1,787 @@
+// The header library's step API on the GPU: ParkerSolver's lockstep
+// global-dt step (include/ParkerSolver.hpp:209-294, kernels :443-477,
+// :771-875, :956-1007, :1147-1174, :1477-1520) and the ParticleSystem
+// lifecycle (include/ParticleSystem.hpp:623-917), on a 2D Cartesian grid with
+// analytic uniform axes.  FP64 throughout, evaluation order as written in the
+// reference; index arithmetic with explicit rounding so the branch decisions
+// (wrap, cell index, stencil) match the reference bit for bit.
+//
+// One step is two kernels.  The first applies the boundary conditions,
+// samples the packed coefficient basis once per particle, keeps the terms the
+// update needs (coordinate rates, momentum rate, kappa_par, kappa_perp, the
+// field direction, |p|) and folds the local stable time step into a global
+// minimum (an atomic min on the bit pattern of a positive double, exact and
+// order independent).  The second rotates the previous positions, draws the
+// noise, updates every active particle from the kept terms and applies the
+// boundary conditions again.  The reference evaluates the same terms twice
+// (once for dt, once for the update) from the same positions; keeping them
+// gives the same numbers with one gather pass instead of two.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "kpt_device.cuh"
+#include "kpt_internal.h"
+
+namespace kpt {
+namespace {
+
+constexpr double kLargeTimeStep = 1.0e300;
+
+// MappedCoordinateGrid::wrap_coordinate (MappedCoordinateGrid.hpp:294-315).
+__device__ __forceinline__ double lib_wrap(const LibAxis& a, double x) {
+    if (!a.periodic) {
+        return x;
+    }
+    double wrapped = __dsub_rn(
+        x, __dmul_rn(floor(__dmul_rn(__dsub_rn(x, a.lower), a.inv_width)), a.width));
+    if (wrapped >= a.upper) {
+        wrapped = __dsub_rn(wrapped, a.width);
+    }
+    if (wrapped < a.lower) {
+        wrapped = __dadd_rn(wrapped, a.width);
+    }
+    return wrapped;
+}
+
+__device__ __forceinline__ bool lib_contains(double lower, double upper, double x) {
+    return x >= lower && x <= upper;
+}
+
+// Analytic uniform face coordinate x0 + i dx (AnalyticCoordinateGrid.hpp:167-171).
+__device__ __forceinline__ double lib_face(const LibAxis& a, double i) {
+    return __dadd_rn(a.x0, __dmul_rn(i, a.dx));
+}
+
+// MappedCoordinateGrid::cell_index over the physical domain (:255-276).
+__device__ __forceinline__ int lib_cell_index(const LibAxis& a, double x) {
+    if (x < a.lower) return -1;
+    if (x > a.upper) return a.n;
+    if (x == a.upper) return a.n - 1;
+    return static_cast<int>(floor(__ddiv_rn(__dsub_rn(x, a.x0), a.dx)));
+}
+
+// Cell-centred stencil over the ghosted domain [-2, n+1]
+// (FieldInterpolator.hpp:509-559; AnalyticCoordinateGrid.hpp:216-230).
+__device__ __forceinline__ void lib_stencil(const LibAxis& a, double x, int& lo, int& hi,
+                                            double& w) {
+    const int lower_bound = -2;
+    const int upper_bound = a.n + 1;
+    const double logical = __dsub_rn(__ddiv_rn(__dsub_rn(x, a.x0), a.dx), 0.5);
+    if (logical <= static_cast<double>(lower_bound)) {
+        lo = hi = lower_bound;
+        w = 0.0;
+        return;
+    }
+    if (logical >= static_cast<double>(upper_bound)) {
+        lo = hi = upper_bound;
+        w = 0.0;
+        return;
+    }
+    const int candidate = static_cast<int>(floor(logical));
+    lo = candidate;
+    hi = candidate + 1;
+    w = __dsub_rn(logical, static_cast<double>(candidate));
+    if (hi > upper_bound) {
+        lo = hi = upper_bound;
+        w = 0.0;
+    }
+}
+
+// LinearPositionInterpolator::sample of the 18-component packed basis
+// (FieldInterpolator.hpp:346-380): corners in order, weight = product of the
+// per-axis factors, values accumulated in component order.
+__device__ __forceinline__ void lib_sample(const LibGrid& g, const double* __restrict__ basis,
+                                           double x, double y, double (&out)[kLibBasis]) {
+    int lo[2], hi[2];
+    double w[2];
+    lib_stencil(g.axis[0], x, lo[0], hi[0], w[0]);
+    lib_stencil(g.axis[1], y, lo[1], hi[1], w[1]);
+#pragma unroll
+    for (int c = 0; c < kLibBasis; ++c) out[c] = 0.0;
+#pragma unroll
+    for (int corner = 0; corner < 4; ++corner) {
+        const bool ux = (corner & 1) != 0;
+        const bool uy = (corner & 2) != 0;
+        double weight = 1.0;
+        weight = __dmul_rn(weight, ux ? w[0] : __dsub_rn(1.0, w[0]));
+        weight = __dmul_rn(weight, uy ? w[1] : __dsub_rn(1.0, w[1]));
+        const int i = (ux ? hi[0] : lo[0]) + 2;
+        const int j = (uy ? hi[1] : lo[1]) + 2;
+        const double* row = basis + (static_cast<size_t>(j) * g.ex + i) * kLibBasisStride;
+#pragma unroll
+        for (int c = 0; c < kLibBasis; c += 2) {
+            const double2 v = __ldg(reinterpret_cast<const double2*>(row + c));
+            out[c] = __dadd_rn(out[c], __dmul_rn(weight, v.x));
+            out[c + 1] = __dadd_rn(out[c + 1], __dmul_rn(weight, v.y));
+        }
+    }
+}
+
+__device__ __forceinline__ bool finite_positive(double v) { return isfinite(v) && v > 0.0; }
+__device__ __forceinline__ bool finite_nonnegative(double v) { return isfinite(v) && v >= 0.0; }
+
+// apply_grid_boundary_conditions for one active particle (ParticleSystem.hpp:
+// 653-699).  Returns false when the particle escaped.
+__device__ __forceinline__ bool lib_boundary(const LibGrid& g, const SystemArrays& s, size_t i) {
+    bool escaped = false;
+#pragma unroll
+    for (int dim = 0; dim < 2; ++dim) {
+        const LibAxis& a = g.axis[dim];
+        double* pos = dim == 0 ? s.x : s.y;
+        const double x = pos[i];
+        if (a.periodic) {
+            const double wrapped = lib_wrap(a, x);
+            const double shift = __dsub_rn(wrapped, x);
+            pos[i] = wrapped;
+            double* prev = dim == 0 ? s.prev_x : s.prev_y;
+            double* prevstep = dim == 0 ? s.prevstep_x : s.prevstep_y;
+            prev[i] = __dadd_rn(prev[i], shift);
+            prevstep[i] = __dadd_rn(prevstep[i], shift);
+        } else if (!lib_contains(a.lower, a.upper, x)) {
+            escaped = true;
+        }
+    }
+    if (escaped) {
+        s.status[i] = 1;
+    }
+    return !escaped;
+}
+
+// Kept per-particle terms (one row per particle, kLibTermCount doubles).
+enum TermSlot {
+    kRateX = 0, kRateY, kMomentumRate, kKappaPar, kKappaPerp, kDirX, kDirY, kDirZ, kMomentum
+};
+static_assert(kMomentum + 1 == kLibTermCount, "term row layout");
+
+// evaluate_terms_from_packed + local_stable_time_step
+// (ParkerSolver.hpp:766-868, :689-760, :880-942).  Returns the local dt bound
+// or a negative error code.
+__device__ double lib_parker_terms(const LibParkerLaunch& L, size_t i, double* terms) {
+    const LibGrid& g = L.grid;
+    const SystemArrays& s = L.sys;
+    double pos[2] = {s.x[i], s.y[i]};
+    // prepare_physical_position (:620-633)
+#pragma unroll
+    for (int dim = 0; dim < 2; ++dim) {
+        pos[dim] = lib_wrap(g.axis[dim], pos[dim]);
+        if (!lib_contains(g.axis[dim].lower, g.axis[dim].upper, pos[dim])) {
+            // the reference's empty terms: zero rates, zero time step
+            for (int k = 0; k < kLibTermCount; ++k) terms[k] = 0.0;
+            return 0.0;
+        }
+    }
+    // interpolator prepare_coordinate: wrap, then the ghosted-domain check
+    double q[2];
+#pragma unroll
+    for (int dim = 0; dim < 2; ++dim) {
+        q[dim] = lib_wrap(g.axis[dim], pos[dim]);
+        if (!lib_contains(g.axis[dim].ghost_lower, g.axis[dim].ghost_upper, q[dim])) {
+            return -1.0;  // "position lies outside the interpolation domain"
+        }
+    }
+    double v[kLibBasis];
+    lib_sample(g, L.basis, q[0], q[1], v);
+
+    const double p_in = s.p[i];
+    const double p = p_in >= 0.0 ? p_in : -p_in;
+    const double normalized = p / L.mc;
+    const double gamma = sqrt(1.0 + normalized * normalized);
+    const double speed = p / (gamma * L.rest_mass);
+    double b2 = 0.0;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) b2 += v[c] * v[c];
+    const double bmag = sqrt(b2);
+    if (!finite_positive(bmag)) {
+        return -2.0;  // "stochastic diffusion requires |B| > 0"
+    }
+    const double ib = 1.0 / bmag;
+    double dir[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) dir[c] = v[c] * ib;
+    const double g13 = pow(gamma, 1.0 / 3.0);
+    double diff[3];
+    if (L.constant_ratio) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) diff[c] = g13 * v[9 + c];
+    } else {
+        const double g19 = pow(gamma, 1.0 / 9.0);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) diff[c] = g13 * v[9 + c] + g19 * v[12 + c];
+    }
+    const double kpar = v[15] * pow(gamma, 1.0 / 3.0);
+    const double kperp = v[16] * (L.constant_ratio ? pow(gamma, 1.0 / 3.0) : pow(gamma, 1.0 / 9.0));
+    if (!finite_nonnegative(kpar) || !finite_nonnegative(kperp)) {
+        return -3.0;  // "diffusion coefficients must be finite and non-negative"
+    }
+    double keff[2];
+#pragma unroll
+    for (int d = 0; d < 2; ++d) {
+        keff[d] = kperp + (kpar - kperp) * dir[d] * dir[d];
+        if (!finite_nonnegative(keff[d])) {
+            return -4.0;  // "projected diffusion coefficient is invalid"
+        }
+    }
+    const double divv = v[17];
+    const double prefactor = p * speed * L.speed_of_light / (3.0 * L.charge);
+    double total[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) total[c] = v[3 + c] + prefactor * v[6 + c] + diff[c];
+    // Cartesian: h_inv = 1
+    terms[kRateX] = total[0] * 1.0;
+    terms[kRateY] = total[1] * 1.0;
+    terms[kMomentumRate] = -(p / 3.0) * divv;
+    terms[kKappaPar] = kpar;
+    terms[kKappaPerp] = kperp;
+    terms[kDirX] = dir[0];
+    terms[kDirY] = dir[1];
+    terms[kDirZ] = dir[2];
+    terms[kMomentum] = p;
+
+    // local_stable_time_step: prepare_physical_position again, then per-axis
+    // cell widths at the physical cell index
+    double dmin = kLargeTimeStep;
+    double amin = kLargeTimeStep;
+#pragma unroll
+    for (int dim = 0; dim < 2; ++dim) {
+        const LibAxis& a = g.axis[dim];
+        const double x = lib_wrap(a, pos[dim]);
+        if (!lib_contains(a.lower, a.upper, x)) {
+            return kLargeTimeStep;
+        }
+        const double cell = static_cast<double>(lib_cell_index(a, x));
+        const double width = __dsub_rn(lib_face(a, __dadd_rn(cell, 1.0)), lib_face(a, cell));
+        const double dx = fabs(__dmul_rn(1.0, width));
+        if (!finite_positive(dx)) {
+            return -5.0;  // "local physical cell width must be positive"
+        }
+        double diffusion_dt = kLargeTimeStep;
+        if (keff[dim] > 0.0) {
+            const double limited = 0.5 * dx;
+            diffusion_dt = limited * limited / (2.0 * keff[dim]);
+        }
+        const double adv = fabs(total[dim]);
+        double advection_dt = kLargeTimeStep;
+        if (adv > 0.0) {
+            advection_dt = 1.0 * dx / adv;
+        }
+        dmin = diffusion_dt < dmin ? diffusion_dt : dmin;
+        amin = advection_dt < amin ? advection_dt : amin;
+    }
+    double mdt = kLargeTimeStep;
+    const double dm = fabs(divv);
+    if (dm > 0.0) {
+        mdt = 3.0 * 1.0 / dm;
+    }
+    const double da = dmin < amin ? dmin : amin;
+    return da < mdt ? da : mdt;
+}
+
+__device__ __forceinline__ void record_error(int* error, int code, uint32_t index,
+                                             unsigned long long* error_index) {
+    if (atomicCAS(error, 0, code) == 0) {
+        *error_index = index;
+    }
+}
+
+// Pass 1: boundary conditions, terms, local dt -> global min (bit pattern).
+__global__ void __launch_bounds__(256) lib_parker_terms_kernel(const LibParkerLaunch L) {
+    double local = kLargeTimeStep;
+    const bool stopped = *L.error != 0;  // an earlier step of a replayed sequence failed
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
+         !stopped && i < L.count; i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        if (L.sys.status[i] != 0) {
+            continue;
+        }
+        if (L.apply_boundary && !lib_boundary(L.grid, L.sys, i)) {
+            continue;
+        }
+        const double dt = lib_parker_terms(L, i, L.terms + i * kLibTermCount);
+        if (dt < 0.0) {
+            record_error(L.error, static_cast<int>(-dt), static_cast<uint32_t>(i),
+                         L.error_index);
+            continue;
+        }
+        local = dt < local ? dt : local;
+    }
+    // warp then block minimum, one atomic per block
+    for (int off = 16; off > 0; off >>= 1) {
+        const double o = __shfl_down_sync(0xffffffffu, local, off);
+        local = o < local ? o : local;
+    }
+    __shared__ double warp_min[8];
+    if ((threadIdx.x & 31u) == 0u) warp_min[threadIdx.x >> 5] = local;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = warp_min[0];
+        for (int k = 1; k < static_cast<int>(blockDim.x >> 5); ++k) m = warp_min[k] < m ? warp_min[k] : m;
+        // positive doubles order like their bit patterns
+        atomicMin(L.min_bits, static_cast<unsigned long long>(__double_as_longlong(m)));
+    }
+}
+
+// Box-Muller normal from two stream draws (u1 = 1 - draw, u2 = draw), the
+// shim pool's normal(): stream draws 2k and 2k+1 are block k.
+__device__ __forceinline__ double lib_normal(uint2 key, uint32_t block, uint32_t index,
+                                             uint32_t frame) {
+    const uint4 r = philox4x32_10(make_uint4(block, index, frame, kTagLibrary), key);
+    const double u1 = 1.0 - u01_f64(r.x, r.y);
+    const double u2 = u01_f64(r.z, r.w);
+    return sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2);
+}
+
+// Pass 2: capture previous positions (whole capacity), update, boundary.
+__global__ void __launch_bounds__(256) lib_parker_advance_kernel(const LibParkerLaunch L) {
+    const double dt = L.dt_device != nullptr ? *L.dt_device : L.dt;
+    // a failed step (no positive dt, or an abort condition) changes nothing
+    // beyond the boundary pass, as the reference throws before its update
+    if (!(isfinite(dt) && dt > 0.0) || *L.error != 0) {
+        return;
+    }
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
+         i < L.capacity; i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        const SystemArrays& s = L.sys;
+        if (L.capture) {
+            s.prevstep_x[i] = s.prev_x[i];
+            s.prevstep_y[i] = s.prev_y[i];
+            s.prev_x[i] = s.x[i];
+            s.prev_y[i] = s.y[i];
+        }
+        if (i >= L.count || s.status[i] != 0) {
+            continue;
+        }
+        const double* t = L.terms + i * kLibTermCount;
+        double inc[2] = {0.0, 0.0};
+        if (L.stochastic) {
+            const uint32_t index = static_cast<uint32_t>(i);
+            double gv[3];
+            double iso = 0.0;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                gv[c] = lib_normal(L.key, static_cast<uint32_t>(c), index, L.frame);
+                iso += gv[c] * t[kDirX + c];
+            }
+            const double pg = lib_normal(L.key, 3u, index, L.frame);
+            const double kperp = t[kKappaPerp];
+            const double kpar = t[kKappaPar];
+            const double perp_scale = kperp > 0.0 ? sqrt(2.0 * kperp * dt) : 0.0;
+            const double par_scale = kpar > 0.0 ? sqrt(2.0 * kpar * dt) : 0.0;
+            const double replacement = par_scale * pg - perp_scale * iso;
+#pragma unroll
+            for (int c = 0; c < 2; ++c) inc[c] = perp_scale * gv[c] + replacement * t[kDirX + c];
+        }
+        if (L.stochastic) {
+            s.x[i] += dt * t[kRateX] + inc[0] * 1.0;
+            s.y[i] += dt * t[kRateY] + inc[1] * 1.0;
+        } else {
+            s.x[i] += dt * t[kRateX];
+            s.y[i] += dt * t[kRateY];
+        }
+        const double updated = t[kMomentum] + dt * t[kMomentumRate];
+        s.p[i] = updated > 0.0 ? updated : 0.0;
+        lib_boundary(L.grid, s, i);
+    }
+}
+
+// dt = courant * min over the active particles, on the device (0 when no
+// particle bounded it; the host reports that as an error).
+__global__ void lib_finish_dt_kernel(const unsigned long long* min_bits, double courant,
+                                     double* dt_out, double* dt_history, int* error,
+                                     int require_positive) {
+    const double m = __longlong_as_double(static_cast<long long>(*min_bits));
+    const double dt = (!isfinite(m) || m >= 0.5 * kLargeTimeStep) ? 0.0 : courant * m;
+    *dt_out = dt;
+    if (dt_history != nullptr) *dt_history = *error != 0 ? 0.0 : dt;
+    if (require_positive && !(isfinite(dt) && dt > 0.0) && *error == 0) {
+        *error = 6;  // "adaptive time step is not positive and finite"
+    }
+}
+
+__global__ void lib_reset_min_kernel(unsigned long long* min_bits) {
+    *min_bits = static_cast<unsigned long long>(__double_as_longlong(kLargeTimeStep));
+}
+
+// ---- ParticleSystem lifecycle ------------------------------------------------
+
+__global__ void system_default_kernel(SystemArrays s, uint64_t count, uint64_t capacity) {
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < capacity;
+         i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        s.id[i] = i;
+        s.mu[i] = 0.0;
+        s.weight[i] = 1.0;
+        s.e0[i] = 0.0;
+        s.status[i] = i < count ? 0 : 2;
+        s.split_level[i] = 0;
+        s.sort_key[i] = 0;
+        s.x[i] = s.y[i] = s.prev_x[i] = s.prev_y[i] = s.prevstep_x[i] = s.prevstep_y[i] = 0.0;
+        s.p[i] = 0.0;
+    }
+}
+
+__global__ void system_boundary_kernel(LibGrid g, SystemArrays s, uint64_t count) {
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < count;
+         i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        if (s.status[i] == 0) lib_boundary(g, s, i);
+    }
+}
+
+__global__ void system_capture_kernel(SystemArrays s, uint64_t capacity) {
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < capacity;
+         i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        s.prevstep_x[i] = s.prev_x[i];
+        s.prevstep_y[i] = s.prev_y[i];
+        s.prev_x[i] = s.x[i];
+        s.prev_y[i] = s.y[i];
+    }
+}
+
+// kinetic energy (gamma - 1) m c^2 (ParticleSystem.hpp:190-193)
+__device__ __forceinline__ double kinetic_energy(const LibSplitLaunch& L, double p) {
+    const double normalized = p / L.mc;
+    const double gamma = sqrt(1.0 + normalized * normalized);
+    return (gamma - 1.0) * L.rest_mass * L.speed_of_light * L.speed_of_light;
+}
+
+__global__ void system_reset_baselines_kernel(LibSplitLaunch L) {
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < L.count;
+         i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        const double p = L.sys.p[i] >= 0.0 ? L.sys.p[i] : -L.sys.p[i];
+        L.sys.e0[i] = kinetic_energy(L, p);
+        L.sys.split_level[i] = 0;
+    }
+}
+
+// Energy-growth split decision per active parent
+// (ParticleSystem.hpp:791-905): 1 = wants a child.  Also counts the active
+// parents, the invalid baselines (and repairs them) and the minimum-weight
+// refusals.
+__device__ __forceinline__ int split_decision(const LibSplitLaunch& L, uint64_t i,
+                                              unsigned long long* tallies) {
+    const SystemArrays& s = L.sys;
+    if (s.status[i] != 0) return 0;
+    atomicAdd(tallies + 0, 1ull);
+    const double p = s.p[i] >= 0.0 ? s.p[i] : -s.p[i];
+    const double current = kinetic_energy(L, p);
+    const double baseline = s.e0[i];
+    if (!isfinite(baseline) || baseline <= 0.0) {
+        if (isfinite(current) && current > 0.0) s.e0[i] = current;
+        atomicAdd(tallies + 2, 1ull);
+        return 0;
+    }
+    const double ratio = current / baseline;
+    if (!isfinite(ratio) || ratio < L.split_ratio) return 0;
+    const int target = static_cast<int>(floor(log(ratio) / L.log_split_ratio));
+    if (target <= s.split_level[i]) return 0;
+    const double child_weight = 0.5 * s.weight[i];
+    if (!isfinite(child_weight) || child_weight <= 0.0 || child_weight < L.min_child_weight) {
+        atomicAdd(tallies + 3, 1ull);
+        return 0;
+    }
+    return 1;
+}
+
+// Per-block counts of children wanted (parents in index order).
+__global__ void __launch_bounds__(256) system_split_count_kernel(LibSplitLaunch L) {
+    __shared__ unsigned int block_total;
+    if (threadIdx.x == 0) block_total = 0;
+    __syncthreads();
+    const uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
+    int want = 0;
+    if (i < L.count) {
+        want = split_decision(L, i, L.tallies);
+        L.flags[i] = want;
+    }
+    const unsigned ballot = __ballot_sync(0xffffffffu, want != 0);
+    if ((threadIdx.x & 31u) == 0u && ballot) atomicAdd(&block_total, __popc(ballot));
+    __syncthreads();
+    if (threadIdx.x == 0) L.block_counts[blockIdx.x] = block_total;
+}
+
+// Exclusive scan of the block counts (one block; serial over blocks per
+// thread chunk, then a block scan).
+__global__ void __launch_bounds__(1024) system_split_scan_kernel(unsigned int* counts, int n,
+                                                                 unsigned long long* total) {
+    __shared__ unsigned long long partial[1024];
+    const int t = threadIdx.x;
+    const int per = (n + blockDim.x - 1) / blockDim.x;
+    const int begin = t * per;
+    const int end = begin + per < n ? begin + per : n;
+    unsigned long long sum = 0;
+    for (int k = begin; k < end; ++k) sum += counts[k];
+    partial[t] = sum;
+    __syncthreads();
+    for (int off = 1; off < static_cast<int>(blockDim.x); off <<= 1) {
+        const unsigned long long v = t >= off ? partial[t - off] : 0ull;
+        __syncthreads();
+        partial[t] += v;
+        __syncthreads();
+    }
+    unsigned long long run = t > 0 ? partial[t - 1] : 0ull;
+    for (int k = begin; k < end; ++k) {
+        const unsigned int c = counts[k];
+        counts[k] = static_cast<unsigned int>(run);
+        run += c;
+    }
+    if (t == static_cast<int>(blockDim.x) - 1) *total = partial[t];
+}
+
+// Children in parent-index order (the serial order of the reference loop).
+__global__ void __launch_bounds__(256) system_split_scatter_kernel(LibSplitLaunch L) {
+    __shared__ unsigned int warp_base[8];
+    const uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
+    const int want = i < L.count ? L.flags[i] : 0;
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned ballot = __ballot_sync(0xffffffffu, want != 0);
+    if (lane == 0) warp_base[threadIdx.x >> 5] = __popc(ballot);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned int run = 0;
+        for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) {
+            const unsigned int c = warp_base[w];
+            warp_base[w] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+    if (!want) return;
+    const uint64_t offset = static_cast<uint64_t>(L.block_counts[blockIdx.x]) +
+                            warp_base[threadIdx.x >> 5] + __popc(ballot & ((1u << lane) - 1u));
+    const uint64_t child = L.count + offset;
+    const SystemArrays& s = L.sys;
+    if (child >= L.capacity) {
+        atomicAdd(L.tallies + 1, 1ull);
+        return;
+    }
+    const double child_weight = 0.5 * s.weight[i];
+    s.id[child] = child;
+    s.x[child] = s.x[i];
+    s.y[child] = s.y[i];
+    s.prev_x[child] = s.prev_x[i];
+    s.prev_y[child] = s.prev_y[i];
+    s.prevstep_x[child] = s.prevstep_x[i];
+    s.prevstep_y[child] = s.prevstep_y[i];
+    s.p[child] = s.p[i];
+    s.mu[child] = s.mu[i];
+    s.weight[i] = child_weight;
+    s.weight[child] = child_weight;
+    s.e0[child] = s.e0[i];
+    s.status[child] = 0;
+    s.sort_key[child] = s.sort_key[i];
+    const int next = s.split_level[i] + 1;
+    s.split_level[i] = next;
+    s.split_level[child] = next;
+}
+
+// sort_by_key (ParticleSystem.hpp:723-759, Kokkos::BinSort with BinOp1D):
+// a stable LSD radix sort of (key - lo) with 8-bit digits, so particles with
+// equal keys keep their index order (the serial BinSort order).  Per pass:
+// block digit histograms, a digit-major scan, then a stable scatter whose
+// in-block ranks come from warp match masks and per-warp digit counts.
+constexpr int kRadixThreads = 256;
+constexpr int kRadixWarps = kRadixThreads / 32;
+
+__global__ void radix_init_kernel(const int* keys, uint64_t count, int lo, int bins,
+                                  unsigned int* k_out, unsigned int* idx_out) {
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < count;
+         i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        long long b = static_cast<long long>(keys[i]) - lo;
+        b = b < 0 ? 0 : (b >= bins ? bins - 1 : b);
+        k_out[i] = static_cast<unsigned int>(b);
+        idx_out[i] = static_cast<unsigned int>(i);
+    }
+}
+
+__global__ void __launch_bounds__(kRadixThreads) radix_hist_kernel(const unsigned int* keys,
+                                                                   uint64_t count, int shift,
+                                                                   unsigned int* hist,
+                                                                   int blocks) {
+    __shared__ unsigned int local[256];
+    local[threadIdx.x] = 0;
+    __syncthreads();
+    const uint64_t i = blockIdx.x * static_cast<uint64_t>(kRadixThreads) + threadIdx.x;
+    if (i < count) atomicAdd(&local[(keys[i] >> shift) & 255u], 1u);
+    __syncthreads();
+    hist[static_cast<size_t>(threadIdx.x) * blocks + blockIdx.x] = local[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(kRadixThreads) radix_scatter_kernel(
+    const unsigned int* keys_in, const unsigned int* idx_in, uint64_t count, int shift,
+    const unsigned int* offsets, int blocks, unsigned int* keys_out, unsigned int* idx_out) {
+    __shared__ unsigned int warp_counts[kRadixWarps][257];
+    for (int k = threadIdx.x; k < kRadixWarps * 257; k += kRadixThreads) {
+        (&warp_counts[0][0])[k] = 0;
+    }
+    __syncthreads();
+    const uint64_t i = blockIdx.x * static_cast<uint64_t>(kRadixThreads) + threadIdx.x;
+    const bool have = i < count;
+    const unsigned int key = have ? keys_in[i] : 0u;
+    const unsigned int digit = have ? ((key >> shift) & 255u) : 256u;
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned warp = threadIdx.x >> 5;
+    const unsigned peers = __match_any_sync(0xffffffffu, digit);
+    const unsigned rank = __popc(peers & ((1u << lane) - 1u));
+    if (rank == 0) warp_counts[warp][digit] = __popc(peers);
+    __syncthreads();
+    // exclusive prefix over the warps, per digit (thread t owns digit t)
+    {
+        unsigned int run = 0;
+        for (int w = 0; w < kRadixWarps; ++w) {
+            const unsigned int c = warp_counts[w][threadIdx.x];
+            warp_counts[w][threadIdx.x] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+    if (!have) return;
+    const unsigned int dest = offsets[static_cast<size_t>(digit) * blocks + blockIdx.x] +
+                              warp_counts[warp][digit] + rank;
+    keys_out[dest] = key;
+    idx_out[dest] = idx_in[i];
+}
+
+template <typename T>
+__global__ void gather_kernel(const T* __restrict__ src, T* __restrict__ dst,
+                              const unsigned int* __restrict__ perm, uint64_t count) {
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < count;
+         i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        dst[i] = src[perm[i]];
+    }
+}
+
+__global__ void compact_keys_kernel(const int* status, int* keys, uint64_t count,
+                                    unsigned long long* active) {
+    unsigned long long mine = 0;
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < count;
+         i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        const bool alive = status[i] == 0;
+        keys[i] = alive ? 0 : 1;
+        mine += alive ? 1 : 0;
+    }
+    for (int off = 16; off > 0; off >>= 1) mine += __shfl_down_sync(0xffffffffu, mine, off);
+    if ((threadIdx.x & 31u) == 0u && mine) atomicAdd(active, mine);
+}
+
+int grid_for(uint64_t n, int threads) {
+    const uint64_t want = (n + threads - 1) / threads;
+    return static_cast<int>(want < 1 ? 1 : (want > 152u * 32u ? 152u * 32u : want));
+}
+
+}  // namespace
+
+cudaError_t lib_parker_step(const LibParkerLaunch& L, cudaStream_t stream) {
+    lib_reset_min_kernel<<<1, 1, 0, stream>>>(L.min_bits);
+    if (L.count > 0) {
+        lib_parker_terms_kernel<<<grid_for(L.count, 256), 256, 0, stream>>>(L);
+    }
+    lib_finish_dt_kernel<<<1, 1, 0, stream>>>(L.min_bits, L.courant, L.dt_device_out,
+                                              L.dt_history, L.error, L.advance);
+    if (L.advance) {
+        LibParkerLaunch A = L;
+        A.dt_device = L.dt_device_out;
+        lib_parker_advance_kernel<<<grid_for(L.capacity, 256), 256, 0, stream>>>(A);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t system_default_state(const SystemArrays& s, uint64_t count, uint64_t capacity,
+                                 cudaStream_t stream) {
+    if (capacity == 0) return cudaSuccess;
+    system_default_kernel<<<grid_for(capacity, 256), 256, 0, stream>>>(s, count, capacity);
+    return cudaGetLastError();
+}
+
+cudaError_t system_boundary(const LibGrid& g, const SystemArrays& s, uint64_t count,
+                            cudaStream_t stream) {
+    if (count == 0) return cudaSuccess;
+    system_boundary_kernel<<<grid_for(count, 256), 256, 0, stream>>>(g, s, count);
+    return cudaGetLastError();
+}
+
+cudaError_t system_capture(const SystemArrays& s, uint64_t capacity, cudaStream_t stream) {
+    if (capacity == 0) return cudaSuccess;
+    system_capture_kernel<<<grid_for(capacity, 256), 256, 0, stream>>>(s, capacity);
+    return cudaGetLastError();
+}
+
+cudaError_t system_reset_baselines(const LibSplitLaunch& L, cudaStream_t stream) {
+    if (L.count == 0) return cudaSuccess;
+    system_reset_baselines_kernel<<<grid_for(L.count, 256), 256, 0, stream>>>(L);
+    return cudaGetLastError();
+}
+
+cudaError_t system_split(const LibSplitLaunch& L, cudaStream_t stream) {
+    const int blocks = static_cast<int>((L.count + 255) / 256);
+    system_split_count_kernel<<<blocks, 256, 0, stream>>>(L);
+    system_split_scan_kernel<<<1, 1024, 0, stream>>>(L.block_counts, blocks, L.tallies + 4);
+    system_split_scatter_kernel<<<blocks, 256, 0, stream>>>(L);
+    return cudaGetLastError();
+}
+
+cudaError_t system_sort(const LibSortLaunch& L, cudaStream_t stream) {
+    const long long range = static_cast<long long>(L.hi) - L.lo + 1;
+    const int bins = static_cast<int>(range);
+    int bits = 0;
+    while (bits < 32 && (1ll << bits) < range) ++bits;
+    const int passes = (bits + 7) / 8;
+    const int blocks = static_cast<int>((L.count + kRadixThreads - 1) / kRadixThreads);
+    unsigned int* k_cur = L.keys_a;
+    unsigned int* i_cur = L.idx_a;
+    unsigned int* k_alt = L.keys_b;
+    unsigned int* i_alt = L.idx_b;
+    radix_init_kernel<<<grid_for(L.count, 256), 256, 0, stream>>>(L.sys.sort_key, L.count, L.lo,
+                                                                  bins, k_cur, i_cur);
+    for (int pass = 0; pass < passes; ++pass) {
+        const int shift = 8 * pass;
+        radix_hist_kernel<<<blocks, kRadixThreads, 0, stream>>>(k_cur, L.count, shift, L.hist,
+                                                                blocks);
+        system_split_scan_kernel<<<1, 1024, 0, stream>>>(L.hist, 256 * blocks, L.scratch_total);
+        radix_scatter_kernel<<<blocks, kRadixThreads, 0, stream>>>(
+            k_cur, i_cur, L.count, shift, L.hist, blocks, k_alt, i_alt);
+        unsigned int* t = k_cur;
+        k_cur = k_alt;
+        k_alt = t;
+        t = i_cur;
+        i_cur = i_alt;
+        i_alt = t;
+    }
+    const unsigned int* perm = i_cur;
+    const int g = grid_for(L.count, 256);
+    const SystemArrays& s = L.sys;
+    cudaError_t err;
+    // gather every array through the permutation via the staging buffer
+    double* sd[10] = {s.x, s.y, s.prev_x, s.prev_y, s.prevstep_x, s.prevstep_y, s.p, s.mu,
+                      s.weight, s.e0};
+    for (double* a : sd) {
+        gather_kernel<double><<<g, 256, 0, stream>>>(a, static_cast<double*>(L.staging), perm,
+                                                     L.count);
+        err = cudaMemcpyAsync(a, L.staging, sizeof(double) * L.count, cudaMemcpyDeviceToDevice,
+                              stream);
+        if (err != cudaSuccess) return err;
+    }
+    int* si[3] = {s.status, s.split_level, s.sort_key};
+    for (int* a : si) {
+        gather_kernel<int><<<g, 256, 0, stream>>>(a, static_cast<int*>(L.staging), perm, L.count);
+        err = cudaMemcpyAsync(a, L.staging, sizeof(int) * L.count, cudaMemcpyDeviceToDevice,
+                              stream);
+        if (err != cudaSuccess) return err;
+    }
+    gather_kernel<unsigned long long><<<g, 256, 0, stream>>>(
+        reinterpret_cast<const unsigned long long*>(s.id),
+        static_cast<unsigned long long*>(L.staging), perm, L.count);
+    err = cudaMemcpyAsync(s.id, L.staging, sizeof(uint64_t) * L.count, cudaMemcpyDeviceToDevice,
+                          stream);
+    if (err != cudaSuccess) return err;
+    return cudaGetLastError();
+}
+
+cudaError_t system_compact_keys(const SystemArrays& s, uint64_t count, unsigned long long* active,
+                                cudaStream_t stream) {
+    cudaError_t err = cudaMemsetAsync(active, 0, sizeof(unsigned long long), stream);
+    if (err != cudaSuccess) return err;
+    if (count == 0) return cudaSuccess;
+    compact_keys_kernel<<<grid_for(count, 256), 256, 0, stream>>>(s.status, s.sort_key, count,
+                                                                  active);
+    return cudaGetLastError();
+}
+
+}  // namespace kpt

@@ -84,6 +84,22 @@ def _ptr(array: Optional[np.ndarray]):
     return None if array is None else array.ctypes.data_as(ctypes.c_void_p)
 
 
+LIB_DOUBLE_FIELDS = ("x", "y", "prev_x", "prev_y", "prevstep_x", "prevstep_y", "p", "mu", "w",
+                     "e0")
+LIB_INT_FIELDS = ("status", "level", "key")
+
+
+def lib_default_system(count: int, capacity: int) -> Dict[str, np.ndarray]:
+    """ParticleSystem::initialize_default_state (ParticleSystem.hpp:1163-1198)."""
+    out = {name: np.zeros(capacity, dtype=np.float64) for name in LIB_DOUBLE_FIELDS}
+    out["w"][:] = 1.0
+    out["id"] = np.arange(capacity, dtype=np.uint64)
+    out["status"] = np.where(np.arange(capacity) < count, 0, 2).astype(np.int32)
+    out["level"] = np.zeros(capacity, dtype=np.int32)
+    out["key"] = np.zeros(capacity, dtype=np.int32)
+    return out
+
+
 def empty_particles(capacity: int) -> Dict[str, np.ndarray]:
     """Particle SoA as the reference allocates it (status 2, src/main.cpp:326-331)."""
     arrays = {name: np.zeros(capacity, dtype=np.float64) for name in PARTICLE_FIELDS[:7]}
@@ -252,6 +268,12 @@ class ReferenceHarness:
         lib.ref_qlt.argtypes = [ll] + [vp] * 9
         lib.ref_main.restype = i32
         lib.ref_main.argtypes = [i32, ctypes.POINTER(ctypes.c_char_p), i32]
+        lib.ref_lib_parker.restype = ll
+        lib.ref_lib_parker.argtypes = [i32, i32, vp, vp, vp, vp, i32, vp, ull, i32, i32, i32, ll,
+                                       ll, vp, vp, vp, vp]
+        lib.ref_lib_system.restype = ll
+        lib.ref_lib_system.argtypes = [i32, i32, vp, vp, vp, vp, i32, i32, i32, ll, ll, vp, vp,
+                                       vp, vp]
 
     @staticmethod
     def _param_arrays(params: dict):
@@ -328,6 +350,62 @@ class ReferenceHarness:
         dd = np.empty(n)
         self._check(self.lib.ref_qlt(n, *[_ptr(a) for a in args], _ptr(d), _ptr(dd)))
         return d, dd
+
+    @staticmethod
+    def _lib_blocks(system: Dict[str, np.ndarray]):
+        ids = np.ascontiguousarray(system["id"], dtype=np.uint64)
+        d = np.ascontiguousarray(np.stack([system[k] for k in LIB_DOUBLE_FIELDS]),
+                                 dtype=np.float64)
+        i = np.ascontiguousarray(np.stack([system[k] for k in LIB_INT_FIELDS]), dtype=np.int32)
+        return ids, d, i
+
+    @staticmethod
+    def _lib_unblock(system, ids, d, i):
+        system["id"][:] = ids
+        for k, name in enumerate(LIB_DOUBLE_FIELDS):
+            system[name][:] = d[k]
+        for k, name in enumerate(LIB_INT_FIELDS):
+            system[name][:] = i[k]
+
+    def lib_parker(self, grid: dict, basis: np.ndarray, constant_ratio: bool, props: dict,
+                   seed: int, first_step: int, steps: int, stochastic: bool, count: int,
+                   system: Dict[str, np.ndarray]) -> np.ndarray:
+        """ParkerSolver steps (include/ParkerSolver.hpp) on a uniform Cartesian grid;
+        updates `system` in place and returns the dt of each step."""
+        xe = np.ascontiguousarray(grid["x_edges"], dtype=np.float64)
+        ye = np.ascontiguousarray(grid["y_edges"], dtype=np.float64)
+        periodic = np.ascontiguousarray(grid["periodic"], dtype=np.int32)
+        basis = np.ascontiguousarray(basis, dtype=np.float64)
+        pr = np.array([props["rest_mass"], props["charge"], props["speed_of_light"],
+                       props.get("energy_scale", 1.0), props["courant"]], dtype=np.float64)
+        ids, d, i = self._lib_blocks(system)
+        dts = np.zeros(max(1, steps), dtype=np.float64)
+        self._check(self.lib.ref_lib_parker(
+            len(xe) - 1, len(ye) - 1, _ptr(xe), _ptr(ye), _ptr(periodic), _ptr(basis),
+            int(constant_ratio), _ptr(pr), seed, first_step, steps, 0 if stochastic else 1,
+            count, ids.size, _ptr(ids), _ptr(d), _ptr(i), _ptr(dts)))
+        self._lib_unblock(system, ids, d, i)
+        return dts[:steps]
+
+    def lib_system(self, grid: dict, props: dict, op: str, count: int,
+                   system: Dict[str, np.ndarray], key_range=(0, 0)):
+        """One ParticleSystem lifecycle call; returns (count after, split statistics)."""
+        ops = {"boundary": 0, "sort": 1, "compact": 2, "split": 3, "capture": 4}
+        xe = np.ascontiguousarray(grid["x_edges"], dtype=np.float64)
+        ye = np.ascontiguousarray(grid["y_edges"], dtype=np.float64)
+        periodic = np.ascontiguousarray(grid["periodic"], dtype=np.int32)
+        pr = np.array([props["rest_mass"], props["charge"], props["speed_of_light"],
+                       props.get("energy_scale", 1.0), props.get("courant", 0.3),
+                       props.get("split_ratio", 2.0), props.get("min_child_weight", 0.0)],
+                      dtype=np.float64)
+        ids, d, i = self._lib_blocks(system)
+        stats = np.zeros(6, dtype=np.uint64)
+        self._check(self.lib.ref_lib_system(
+            len(xe) - 1, len(ye) - 1, _ptr(xe), _ptr(ye), _ptr(periodic), _ptr(pr), ops[op],
+            int(key_range[0]), int(key_range[1]), count, ids.size, _ptr(ids), _ptr(d), _ptr(i),
+            _ptr(stats)))
+        self._lib_unblock(system, ids, d, i)
+        return int(stats[0]), [int(v) for v in stats[1:]]
 
     def main(self, argv, frame_base: int = 0) -> int:
         """Run the reference CLI (in-process); noise frames start at frame_base."""

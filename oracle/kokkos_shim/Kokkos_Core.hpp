@@ -42,6 +42,7 @@ struct LayoutRight {};
 struct LayoutLeft {};
 struct HostSpace {
     using memory_space = HostSpace;
+    using size_type = std::size_t;
 };
 
 template <class ExecSpace, class MemSpace>
@@ -57,6 +58,8 @@ struct OpenMP {
     using array_layout = LayoutRight;
     using device_type = Device<OpenMP, HostSpace>;
     using size_type = std::size_t;
+    // an execution-space instance: work is synchronous, so fencing is a no-op
+    void fence(const char* = nullptr) const {}
 };
 
 using DefaultExecutionSpace = OpenMP;

@@ -42,6 +42,11 @@ inline std::uint32_t label_tag(const char* label) {
         std::strstr(label, "move_particles_one_interval") != nullptr) {
         return KPT_ORACLE_TAG_PUSH;
     }
+    if (std::strstr(label, "ParkerSolver::") != nullptr ||
+        std::strstr(label, "FocusTransportSolver::") != nullptr ||
+        std::strstr(label, "FocusSolver::") != nullptr) {
+        return KPT_ORACLE_TAG_LIBRARY;
+    }
     return KPT_ORACLE_TAG_OTHER;
 }
 }  // namespace ShimImpl

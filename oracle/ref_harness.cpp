@@ -12,11 +12,18 @@
 //   move_particles_one_interval                               :1334-1755
 //   split_particles                                           :1761-1839
 //   main (as kpt_ref_main)                                    :2692-2705
+// and the header library's step API on a 2D Cartesian grid:
+//   ParkerSolver::{advance_stochastic, advance_deterministic,
+//                  compute_adaptive_time_step}           ParkerSolver.hpp:209-294
+//   ParticleSystem::{apply_grid_boundary_conditions, sort_by_key,
+//                    compact_active_particles,
+//                    split_particles_on_energy_growth}    ParticleSystem.hpp:623-917
 #include "src/main.cpp"
 
 #include <string>
 
 #include "LegencyModel.hpp"
+#include "ParkerSolver.hpp"
 
 namespace {
 
@@ -209,6 +216,101 @@ StoredBackground make_stored_background(int nx, int ny, const double* x_edges,
     result.magnetic_field.fill_ghost_cells(FieldGhostFillMode::PeriodicOrClamped, true);
     result.velocity_field.fill_ghost_cells(FieldGhostFillMode::PeriodicOrClamped, true);
     return result;
+}
+
+// ---- header library on a 2D Cartesian grid -------------------------------
+using LibLayout = typename DeviceTraits<Device>::array_layout;
+using LibMeta = Grid<2, Device, LibLayout, 3>;
+using LibAnalyticGrid = AnalyticCoordinateGrid<2, Device, LibLayout, 3>;
+using LibSystem = ParticleSystem<2, Device, LibLayout>;
+
+// Uniform edges -> the analytic grid the field reader builds
+// (AthenaFieldReader.hpp:195-227); periodic flags per axis.
+LibAnalyticGrid make_lib_analytic_grid(int nx, int ny, const double* x_edges,
+                                       const double* y_edges, const int* periodic) {
+    typename LibMeta::index_array_type extents{};
+    extents[0] = nx;
+    extents[1] = ny;
+    typename LibMeta::ghost_array_type ghosts{};
+    typename LibMeta::periodic_array_type flags{};
+    for (int dim = 0; dim < 2; ++dim) {
+        ghosts[dim][LowerBoundary] = 2;
+        ghosts[dim][UpperBoundary] = 2;
+        flags[dim] = periodic[dim];
+    }
+    LibMeta metadata(extents, ghosts, flags);
+    typename LibAnalyticGrid::discretization_array_type discretization{};
+    typename LibAnalyticGrid::scalar_array_type start{};
+    typename LibAnalyticGrid::scalar_array_type step{};
+    const double* edges[2] = {x_edges, y_edges};
+    const int counts[2] = {nx, ny};
+    for (int dim = 0; dim < 2; ++dim) {
+        discretization[dim] = AnalyticGridDiscretization::UniformSpacing;
+        start[dim] = edges[dim][0];
+        step[dim] = (edges[dim][counts[dim]] - edges[dim][0]) / counts[dim];
+    }
+    return GridValidation::make_validated_analytic_coordinate_grid<2, Device, LibLayout, 3>(
+        metadata, discretization, start, step);
+}
+
+// Particle arrays of the host side: doubles [10][capacity] = x, y, prev x,
+// prev y, prev-step x, prev-step y, momentum, mu, weight, E0; ints
+// [3][capacity] = status, split level, sort key; ids [capacity].
+struct LibHost {
+    unsigned long long* id;
+    double* d;
+    int* i;
+    long long capacity;
+};
+
+void lib_load(LibSystem& sys, const LibHost& h) {
+    const long long c = h.capacity;
+    for (long long n = 0; n < c; ++n) {
+        sys.particle_id(n) = h.id[n];
+        sys.position(n, 0) = h.d[0 * c + n];
+        sys.position(n, 1) = h.d[1 * c + n];
+        sys.previous_position(n, 0) = h.d[2 * c + n];
+        sys.previous_position(n, 1) = h.d[3 * c + n];
+        sys.previous_step_position(n, 0) = h.d[4 * c + n];
+        sys.previous_step_position(n, 1) = h.d[5 * c + n];
+        sys.momentum(n) = h.d[6 * c + n];
+        sys.mu(n) = h.d[7 * c + n];
+        sys.weight(n) = h.d[8 * c + n];
+        sys.initial_kinetic_energy(n) = h.d[9 * c + n];
+        sys.status(n) = h.i[0 * c + n];
+        sys.split_level(n) = h.i[1 * c + n];
+        sys.sort_key(n) = h.i[2 * c + n];
+    }
+}
+
+void lib_store(const LibSystem& sys, const LibHost& h) {
+    const long long c = h.capacity;
+    for (long long n = 0; n < c; ++n) {
+        h.id[n] = sys.particle_id(n);
+        h.d[0 * c + n] = sys.position(n, 0);
+        h.d[1 * c + n] = sys.position(n, 1);
+        h.d[2 * c + n] = sys.previous_position(n, 0);
+        h.d[3 * c + n] = sys.previous_position(n, 1);
+        h.d[4 * c + n] = sys.previous_step_position(n, 0);
+        h.d[5 * c + n] = sys.previous_step_position(n, 1);
+        h.d[6 * c + n] = sys.momentum(n);
+        h.d[7 * c + n] = sys.mu(n);
+        h.d[8 * c + n] = sys.weight(n);
+        h.d[9 * c + n] = sys.initial_kinetic_energy(n);
+        h.i[0 * c + n] = sys.status(n);
+        h.i[1 * c + n] = sys.split_level(n);
+        h.i[2 * c + n] = sys.sort_key(n);
+    }
+}
+
+ParticleProperties lib_properties(const double* props) {
+    ParticleProperties p;
+    p.species = ParticleSpecies::Custom;
+    p.rest_mass = props[0];
+    p.charge = props[1];
+    p.speed_of_light = props[2];
+    p.energy_scale_erg = props[3];
+    return p;
 }
 
 }  // namespace
@@ -420,6 +522,128 @@ long long ref_qlt(long long n, const double* mu, const double* omega, const doub
                                                                    speed[k], lc[k], parameters);
     }
     return n;
+}
+
+// ParkerSolver steps on a uniform 2D Cartesian grid.  basis holds the
+// packed coefficient basis on every ghosted point (x fastest), 18 values per
+// point in the solver's packed order: B(3) V(3) drift curl(3) primary(3)
+// secondary(3) kappa_par kappa_perp divV (ParkerSolver.hpp:96-116); the
+// fields handed to the solver are cut from it, so the solver rebuilds the
+// same packed basis.  props = rest mass, charge, c, energy scale, courant.
+// mode: 0 stochastic, 1 deterministic.  dts[steps] receives each step's dt;
+// the noise frame of step s is first_step + s.
+long long ref_lib_parker(int nx, int ny, const double* x_edges, const double* y_edges,
+                         const int* periodic, const double* basis, int constant_ratio,
+                         const double* props, unsigned long long seed, int first_step,
+                         int steps, int mode, long long count, long long capacity,
+                         unsigned long long* ids, double* d, int* ints, double* dts) {
+    try {
+        using solver_type = ParkerSolver<LibAnalyticGrid>;
+        using vector_field = typename solver_type::vector_field_type;
+        using scalar_field = typename solver_type::scalar_field_type;
+        const LibAnalyticGrid grid = make_lib_analytic_grid(nx, ny, x_edges, y_edges, periodic);
+        vector_field b(grid, "lib_b", GridCentering::CellCentered);
+        vector_field v(grid, "lib_v", GridCentering::CellCentered);
+        vector_field curl(grid, "lib_curl", GridCentering::CellCentered);
+        vector_field primary(grid, "lib_primary", GridCentering::CellCentered);
+        vector_field secondary(grid, "lib_secondary", GridCentering::CellCentered);
+        scalar_field kpar(grid, "lib_kpar", GridCentering::CellCentered);
+        scalar_field kperp(grid, "lib_kperp", GridCentering::CellCentered);
+        scalar_field divv(grid, "lib_divv", GridCentering::CellCentered);
+        const std::size_t points = b.point_count();
+        for (std::size_t k = 0; k < points; ++k) {
+            const double* row = basis + 18 * k;
+            for (int c = 0; c < 3; ++c) {
+                b.data(k, c) = row[c];
+                v.data(k, c) = row[3 + c];
+                curl.data(k, c) = row[6 + c];
+                primary.data(k, c) = row[9 + c];
+                secondary.data(k, c) = row[12 + c];
+            }
+            kpar.data(k, 0) = row[15];
+            kperp.data(k, 0) = row[16];
+            divv.data(k, 0) = row[17];
+        }
+        LegencyModel::DiffusionModelParameters parameters;
+        ParkerCoefficient::DiffusionTensorDivergenceFieldSet<LibAnalyticGrid> divergence;
+        if (constant_ratio) {
+            parameters.set_constant_perpendicular_parallel_ratio(1.0);
+            divergence.perpendicular_model =
+                LegencyModel::PerpendicularDiffusionModelKind::ConstantParallelRatio;
+            divergence.constant_ratio_basis = primary;
+        } else {
+            divergence.parallel_basis = primary;
+            divergence.perpendicular_basis = secondary;
+        }
+        typename solver_type::coefficient_field_set_type coefficients(
+            curl, divergence, kpar, kperp, divv, parameters);
+        LibSystem sys(static_cast<typename LibSystem::size_type>(count),
+                      static_cast<typename LibSystem::size_type>(capacity),
+                      lib_properties(props));
+        const LibHost h{ids, d, ints, capacity};
+        lib_load(sys, h);
+        solver_type solver(sys, grid, b, v, coefficients);
+        solver.set_dimensionless_courant_scale(Units::DimensionlessValue(props[4]));
+        RandomManager<> random_manager(seed);
+        Kokkos::ShimImpl::auto_frame_enabled() = 0;
+        for (int s = 0; s < steps; ++s) {
+            Kokkos::ShimImpl::current_frame() = static_cast<std::uint32_t>(first_step + s);
+            dts[s] = mode == 0 ? solver.advance_stochastic(random_manager)
+                               : solver.advance_deterministic();
+        }
+        lib_store(solver.particles, h);
+        return 0;
+    } catch (const std::exception& error) {
+        g_last_error = error.what();
+        return -1;
+    }
+}
+
+// ParticleSystem lifecycle on the same grid: op 0 boundary conditions,
+// 1 sort_by_key(key_lo, key_hi), 2 compact_active_particles, 3
+// split_particles_on_energy_growth (policy = split_ratio, min child weight),
+// 4 capture_previous_positions.  stats[6]: count after, then the split
+// statistics (active, split, skipped capacity, skipped invalid baseline,
+// skipped minimum weight) for op 3.
+long long ref_lib_system(int nx, int ny, const double* x_edges, const double* y_edges,
+                         const int* periodic, const double* props, int op, int key_lo,
+                         int key_hi, long long count, long long capacity,
+                         unsigned long long* ids, double* d, int* ints,
+                         unsigned long long* stats) {
+    try {
+        const LibAnalyticGrid grid = make_lib_analytic_grid(nx, ny, x_edges, y_edges, periodic);
+        ParticleSplittingPolicy policy;
+        policy.energy_split_ratio = props[5];
+        policy.minimum_child_weight = props[6];
+        LibSystem sys(static_cast<typename LibSystem::size_type>(count),
+                      static_cast<typename LibSystem::size_type>(capacity),
+                      lib_properties(props), policy);
+        const LibHost h{ids, d, ints, capacity};
+        lib_load(sys, h);
+        for (int k = 0; k < 6; ++k) stats[k] = 0;
+        if (op == 0) {
+            sys.apply_grid_boundary_conditions(grid, GridDomain::PhysicalDomain);
+        } else if (op == 1) {
+            sys.sort_by_key(key_lo, key_hi);
+        } else if (op == 2) {
+            sys.compact_active_particles();
+        } else if (op == 3) {
+            const auto st = sys.split_particles_on_energy_growth();
+            stats[1] = st.active_count;
+            stats[2] = st.split_count;
+            stats[3] = st.skipped_capacity_count;
+            stats[4] = st.skipped_invalid_baseline_count;
+            stats[5] = st.skipped_minimum_weight_count;
+        } else if (op == 4) {
+            sys.capture_previous_positions();
+        }
+        stats[0] = sys.particle_count();
+        lib_store(sys, h);
+        return 0;
+    } catch (const std::exception& error) {
+        g_last_error = error.what();
+        return -1;
+    }
 }
 
 // The reference CLI entry point itself.  Noise frames are keyed as

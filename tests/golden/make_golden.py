@@ -23,6 +23,14 @@ Cases
   cli/                the reference CLI run end to end: summary.csv,
                       momentum_histogram_*.csv, particles_*.bin (v4), and a
                       restart from the frame-2 snapshot
+  lib_parker_*.npz    the header library's ParkerSolver (stochastic and
+                      deterministic steps, both diffusion branches, periodic
+                      and open boundaries) on a uniform Cartesian grid
+  lib_system.npz      ParticleSystem lifecycle: boundary conditions,
+                      sort_by_key, compact_active_particles,
+                      split_particles_on_energy_growth, capture_previous_positions
+
+``python tests/golden/make_golden.py lib`` regenerates only the lib_* files.
 """
 from __future__ import annotations
 
@@ -229,9 +237,116 @@ def make_cli(ref, out_dir):
         stream.write(" ".join(argv_common) + "\n")
 
 
+def lib_basis(nx: int, ny: int, x_edges, y_edges, readme: bool) -> np.ndarray:
+    """Smooth periodic coefficient fields on every ghosted cell centre, in the
+    packed order B(3) V(3) drift curl(3) primary(3) secondary(3) kpar kperp divV."""
+    dx = (x_edges[-1] - x_edges[0]) / nx
+    dy = (y_edges[-1] - y_edges[0]) / ny
+    xc = x_edges[0] + (np.arange(-2, nx + 2) + 0.5) * dx
+    yc = y_edges[0] + (np.arange(-2, ny + 2) + 0.5) * dy
+    y, x = np.meshgrid(yc, xc, indexing="ij")
+    kx, ky = np.pi, np.pi / 2.0
+    out = np.zeros((ny + 4, nx + 4, 18))
+    out[..., 0] = np.tanh(np.sin(ky * y) / 0.3) + 0.05
+    out[..., 1] = 0.1 * np.sin(kx * x) * np.cos(ky * y)
+    out[..., 2] = 0.2
+    out[..., 3] = 0.1 * np.cos(kx * x)
+    out[..., 4] = -0.05 * np.sin(ky * y)
+    out[..., 6] = 0.02 * np.sin(kx * x + ky * y)
+    out[..., 7] = 0.02 * np.cos(kx * x - ky * y)
+    out[..., 8] = 0.01 * np.sin(ky * y)
+    out[..., 9] = 1e-3 * np.cos(kx * x)
+    out[..., 10] = 1e-3 * np.sin(ky * y)
+    if readme:
+        out[..., 12] = 5e-4 * np.sin(kx * x)
+        out[..., 13] = 5e-4 * np.cos(ky * y)
+    out[..., 15] = 0.01 * (1.2 + np.sin(kx * x) * np.cos(ky * y))
+    out[..., 16] = 0.05 * out[..., 15] if not readme else 1e-3 * (1.1 + np.cos(kx * x))
+    out[..., 17] = 0.1 * np.cos(kx * x) * np.sin(ky * y)
+    return out.reshape(-1, 18)
+
+
+def lib_population(rng, count: int, capacity: int, x_edges, y_edges, open_y: bool) -> dict:
+    system = binding.lib_default_system(count, capacity)
+    system["x"][:count] = rng.uniform(x_edges[0], x_edges[-1], count)
+    lo, hi = y_edges[0], y_edges[-1]
+    if open_y:
+        hi_band = hi - 0.02 * (hi - lo)
+        system["y"][:count] = rng.uniform(lo, hi, count)
+        system["y"][:count:7] = rng.uniform(hi_band, hi, len(system["y"][:count:7]))
+    else:
+        system["y"][:count] = rng.uniform(lo, hi, count)
+    system["prev_x"][:count] = system["x"][:count] - 0.01
+    system["prev_y"][:count] = system["y"][:count] + 0.01
+    system["p"][:count] = np.exp(rng.uniform(np.log(0.05), np.log(3.0), count))
+    system["mu"][:count] = rng.uniform(-1, 1, count)
+    system["status"][:count:13] = 2  # a few inactive particles inside the count
+    return system
+
+
+def lib_save(out_dir, name, **arrays):
+    np.savez_compressed(os.path.join(out_dir, name), **arrays)
+
+
+def make_lib(ref, out_dir):
+    rng = np.random.default_rng(2718)
+    nx, ny = 24, 40
+    xe = np.linspace(-1.0, 1.0, nx + 1)
+    ye = np.linspace(-2.0, 2.0, ny + 1)
+    props = dict(rest_mass=1.0, charge=1.0, speed_of_light=1.0, energy_scale=1.0, courant=0.3)
+    cases = (("readme_periodic", True, (1, 1), True, 4),
+             ("ratio_open", False, (1, 0), True, 4),
+             ("readme_deterministic", True, (1, 0), False, 3))
+    for name, readme, periodic, stochastic, steps in cases:
+        grid = dict(x_edges=xe, y_edges=ye, periodic=np.array(periodic, dtype=np.int32))
+        basis = lib_basis(nx, ny, xe, ye, readme)
+        count, capacity = 700, 768
+        start = lib_population(rng, count, capacity, xe, ye, periodic[1] == 0)
+        system = {k: v.copy() for k, v in start.items()}
+        dts = ref.lib_parker(grid, basis, not readme, props, SEED, 10, steps, stochastic, count,
+                             system)
+        lib_save(out_dir, f"lib_parker_{name}.npz", x_edges=xe, y_edges=ye,
+                 periodic=grid["periodic"], basis=basis, constant_ratio=int(not readme),
+                 stochastic=int(stochastic), steps=steps, first_step=10, seed=SEED,
+                 count=count, courant=props["courant"], dts=dts,
+                 **{f"start_{k}": v for k, v in start.items()},
+                 **{f"end_{k}": v for k, v in system.items()})
+    # ParticleSystem lifecycle
+    grid = dict(x_edges=xe, y_edges=ye, periodic=np.array((1, 0), dtype=np.int32))
+    props_sys = dict(props, split_ratio=2.0, min_child_weight=0.2)
+    arrays = {}
+    count, capacity = 500, 560
+    base = lib_population(rng, count, capacity, xe, ye, True)
+    base["x"][:count:5] += 2.5  # outside the periodic x range
+    base["y"][:count:9] = 2.1   # outside the open y range
+    base["key"][:count] = rng.integers(-3, 41, count)
+    base["w"][:count] = 2.0 ** -rng.integers(0, 4, count)
+    # baselines: valid for most, zero for a few; momenta spread energy ratios
+    ke = np.sqrt(1.0 + base["p"] ** 2) - 1.0
+    base["e0"][:count] = ke[:count] / np.exp(rng.uniform(0.0, np.log(20.0), count))
+    base["e0"][:count:11] = 0.0
+    base["level"][:count] = rng.integers(0, 3, count)
+    for op, key_range in (("boundary", (0, 0)), ("sort", (-3, 40)), ("compact", (0, 0)),
+                          ("split", (0, 0)), ("capture", (0, 0))):
+        system = {k: v.copy() for k, v in base.items()}
+        new_count, stats = ref.lib_system(grid, props_sys, op, count, system, key_range)
+        arrays[f"{op}_count"] = new_count
+        arrays[f"{op}_stats"] = np.array(stats, dtype=np.uint64)
+        for k, v in system.items():
+            arrays[f"{op}_{k}"] = v
+    for k, v in base.items():
+        arrays[f"start_{k}"] = v
+    lib_save(out_dir, "lib_system.npz", x_edges=xe, y_edges=ye, periodic=grid["periodic"],
+             count=count, split_ratio=props_sys["split_ratio"],
+             min_child_weight=props_sys["min_child_weight"], **arrays)
+
+
 def main() -> None:
     ref = binding.ReferenceHarness()
     out_dir = HERE
+    make_lib(ref, out_dir)
+    if sys.argv[1:] == ["lib"]:
+        return
     make_tables(ref, out_dir)
     make_inject(ref, out_dir)
     make_push(ref, out_dir, "parker_uniform", False, False, 1500, 3, {})
