@@ -386,9 +386,20 @@ typedef struct kpt_system_arrays {
     int32_t* sort_key;
 } kpt_system_arrays;
 
+/* PitchAngleScatteringParameters (LegencyModel.hpp:196-221). */
+typedef struct kpt_scattering_parameters {
+    double spectral_index;      /* > 1 (default 5/3) */
+    double h0;                  /* resonance regularisation (default 1e-6) */
+    double minimum_magnetic_field_magnitude;
+    double minimum_sigma2;
+    double minimum_correlation_length;
+    double minimum_speed;
+} kpt_scattering_parameters;
+
 typedef struct kpt_grid kpt_grid;
 typedef struct kpt_system kpt_system;
 typedef struct kpt_parker_solver kpt_parker_solver;
+typedef struct kpt_focus_solver kpt_focus_solver;
 
 /* Uniform 2D Cartesian grid with two ghost layers (Grid.hpp:65,
  * AnalyticCoordinateGrid.hpp); edges nx+1 / ny+1 must be uniform (the field
@@ -461,6 +472,41 @@ int kpt_parker_advance_deterministic(kpt_context* ctx, kpt_parker_solver* solver
 int kpt_parker_advance_stochastic_steps(kpt_context* ctx, kpt_parker_solver* solver,
                                         kpt_system* system, uint64_t seed, uint32_t first_step,
                                         uint32_t steps, double* dts);
+
+/* FocusTransportSolver / FocusSolver(particles, grid, B, V, coefficients)
+ * with the packed basis (FocusSolver.hpp:106-198): basis holds, for every
+ * ghosted point (x fastest), 27 values B(3) b(3) V(3) gradient drift basis(3)
+ * curvature drift basis(3) perpendicular diffusion advection(3) |B|
+ * kappa_par_1 kappa_perp_1 div V magnetic focusing bb:grad V b.dV/dt sigma^2
+ * L_c.  scattering NULL = reference defaults.  Pitch-angle scattering is the
+ * slab-QLT closure evaluated four times per step (once for the limiters,
+ * three Picard iterations, FocusSolver.hpp:697-740). */
+int kpt_focus_solver_create(kpt_context* ctx, const kpt_grid* grid, const double* basis,
+                            int constant_ratio, double courant,
+                            const kpt_scattering_parameters* scattering,
+                            kpt_focus_solver** out);
+int kpt_focus_solver_destroy(kpt_focus_solver* solver);
+int kpt_focus_solver_set_basis(kpt_focus_solver* solver, const double* basis,
+                               int constant_ratio);
+int kpt_focus_solver_set_courant(kpt_focus_solver* solver, double courant);
+/* set_maximum_pitch_angle_cosine (FocusSolver.hpp:219-226): 0 < value <= 1. */
+int kpt_focus_solver_set_maximum_mu(kpt_focus_solver* solver, double maximum_mu);
+/* compute_adaptive_time_step (FocusSolver.hpp:240-246). */
+int kpt_focus_compute_time_step(kpt_context* ctx, kpt_focus_solver* solver,
+                                kpt_system* system, double* dt);
+/* advance_stochastic / advance_sde (FocusSolver.hpp:276-301); keyed noise of
+ * (seed, particle index, step). */
+int kpt_focus_advance_stochastic(kpt_context* ctx, kpt_focus_solver* solver,
+                                 kpt_system* system, uint64_t seed, uint32_t step,
+                                 double* dt_used);
+/* advance_deterministic (FocusSolver.hpp:251-271). */
+int kpt_focus_advance_deterministic(kpt_context* ctx, kpt_focus_solver* solver,
+                                    kpt_system* system, double* dt_used);
+/* steps consecutive advance_stochastic calls replayed from one CUDA graph
+ * (as kpt_parker_advance_stochastic_steps). */
+int kpt_focus_advance_stochastic_steps(kpt_context* ctx, kpt_focus_solver* solver,
+                                       kpt_system* system, uint64_t seed, uint32_t first_step,
+                                       uint32_t steps, double* dts);
 
 #ifdef __cplusplus
 }

@@ -96,6 +96,13 @@ class ParticleProperties(ctypes.Structure):
                                                "energy_scale_erg")]
 
 
+class ScatteringParameters(ctypes.Structure):
+    """kpt_scattering_parameters (reference PitchAngleScatteringParameters)."""
+    _fields_ = [(n, ctypes.c_double) for n in (
+        "spectral_index", "h0", "minimum_magnetic_field_magnitude", "minimum_sigma2",
+        "minimum_correlation_length", "minimum_speed")]
+
+
 class SplitPolicy(ctypes.Structure):
     """kpt_split_policy (reference ParticleSplittingPolicy)."""
     _fields_ = [("energy_split_ratio", ctypes.c_double),
@@ -206,6 +213,15 @@ def load_library() -> ctypes.CDLL:
         "kpt_parker_advance_stochastic": (i32, [vp, vp, vp, u64, u32, vp]),
         "kpt_parker_advance_deterministic": (i32, [vp, vp, vp, vp]),
         "kpt_parker_advance_stochastic_steps": (i32, [vp, vp, vp, u64, u32, u32, vp]),
+        "kpt_focus_solver_create": (i32, [vp, vp, vp, i32, dbl, vp, pvp]),
+        "kpt_focus_solver_destroy": (i32, [vp]),
+        "kpt_focus_solver_set_basis": (i32, [vp, vp, i32]),
+        "kpt_focus_solver_set_courant": (i32, [vp, dbl]),
+        "kpt_focus_solver_set_maximum_mu": (i32, [vp, dbl]),
+        "kpt_focus_compute_time_step": (i32, [vp, vp, vp, vp]),
+        "kpt_focus_advance_stochastic": (i32, [vp, vp, vp, u64, u32, vp]),
+        "kpt_focus_advance_deterministic": (i32, [vp, vp, vp, vp]),
+        "kpt_focus_advance_stochastic_steps": (i32, [vp, vp, vp, u64, u32, u32, vp]),
     }
     for name, (restype, argtypes) in sig.items():
         fn = getattr(lib, name)
@@ -442,6 +458,22 @@ class Context:
                                                  ctypes.byref(handle)))
         return self._adopt(ParkerSolver(self, handle))
 
+    def focus_solver(self, grid: "LibGrid", basis: np.ndarray, constant_ratio: bool = False,
+                     courant: float = 0.3, spectral_index: float = 5.0 / 3.0, h0: float = 1e-6,
+                     floors=(0.0, 0.0, 0.0, 0.0), maximum_mu: float = 1.0) -> "FocusSolver":
+        basis = np.ascontiguousarray(basis, dtype=np.float64)
+        if basis.shape != (grid.points, 27):
+            raise ValueError(f"basis must be ({grid.points}, 27)")
+        sc = ScatteringParameters(spectral_index, h0, *floors)
+        handle = ctypes.c_void_p()
+        _check(self.lib.kpt_focus_solver_create(self.handle, grid.handle, _ptr(basis),
+                                                int(constant_ratio), float(courant),
+                                                ctypes.byref(sc), ctypes.byref(handle)))
+        solver = self._adopt(FocusSolver(self, handle))
+        if maximum_mu != 1.0:
+            solver.set_maximum_mu(maximum_mu)
+        return solver
+
     def sample(self, lower: "Field", upper: "Field", x, y, rt,
                time_interpolation: int = 1) -> np.ndarray:
         x = np.ascontiguousarray(x, dtype=np.float64)
@@ -671,6 +703,44 @@ class ParkerSolver(_Handle):
                                  steps: int) -> np.ndarray:
         dts = np.zeros(max(1, steps), dtype=np.float64)
         _check(self.ctx.lib.kpt_parker_advance_stochastic_steps(
+            self.ctx.handle, self.handle, system.handle, int(seed), int(first_step), int(steps),
+            _ptr(dts)))
+        return dts[:steps]
+
+
+class FocusSolver(_Handle):
+    """Header-library focused-transport solver (kpt_focus_solver, reference FocusSolver)."""
+    _destroy = "kpt_focus_solver_destroy"
+
+    def set_courant(self, courant: float) -> None:
+        _check(self.ctx.lib.kpt_focus_solver_set_courant(self.handle, float(courant)))
+
+    def set_maximum_mu(self, maximum_mu: float) -> None:
+        _check(self.ctx.lib.kpt_focus_solver_set_maximum_mu(self.handle, float(maximum_mu)))
+
+    def compute_time_step(self, system: ParticleSystem) -> float:
+        dt = ctypes.c_double()
+        _check(self.ctx.lib.kpt_focus_compute_time_step(self.ctx.handle, self.handle,
+                                                        system.handle, ctypes.byref(dt)))
+        return float(dt.value)
+
+    def advance_stochastic(self, system: ParticleSystem, seed: int, step: int) -> float:
+        dt = ctypes.c_double()
+        _check(self.ctx.lib.kpt_focus_advance_stochastic(self.ctx.handle, self.handle,
+                                                         system.handle, int(seed), int(step),
+                                                         ctypes.byref(dt)))
+        return float(dt.value)
+
+    def advance_deterministic(self, system: ParticleSystem) -> float:
+        dt = ctypes.c_double()
+        _check(self.ctx.lib.kpt_focus_advance_deterministic(self.ctx.handle, self.handle,
+                                                            system.handle, ctypes.byref(dt)))
+        return float(dt.value)
+
+    def advance_stochastic_steps(self, system: ParticleSystem, seed: int, first_step: int,
+                                 steps: int) -> np.ndarray:
+        dts = np.zeros(max(1, steps), dtype=np.float64)
+        _check(self.ctx.lib.kpt_focus_advance_stochastic_steps(
             self.ctx.handle, self.handle, system.handle, int(seed), int(first_step), int(steps),
             _ptr(dts)))
         return dts[:steps]

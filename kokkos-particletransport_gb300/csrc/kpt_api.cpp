@@ -1308,8 +1308,9 @@ int kpt_surrogate_train(kpt_context* ctx, const kpt_settings* settings,
     init(kpt::kMlpW3, kpt::kMlpOut, kpt::kMlpHidden);
     const size_t b = static_cast<size_t>(c.batch);
     const size_t pcount = kpt::kMlpParams;
+    const size_t chunks = (b + kpt::kGradChunk - 1) / kpt::kGradChunk;
     const size_t floats = 4 * pcount + b * (kpt::kMlpIn + 4 * kpt::kMlpHidden + kpt::kMlpOut) +
-                          static_cast<size_t>(c.steps);
+                          static_cast<size_t>(c.steps) + chunks * pcount;
     KPT_CUDA(work.reserve(floats * sizeof(float)));
     KPT_CUDA(cudaMemsetAsync(work.ptr, 0, floats * sizeof(float), st));
     kpt::SurrogateTrainLaunch L{};
@@ -1331,6 +1332,7 @@ int kpt_surrogate_train(kpt_context* ctx, const kpt_settings* settings,
     L.g2 = L.g1 + b * kpt::kMlpHidden;
     L.gy = L.g2 + b * kpt::kMlpHidden;
     L.loss = L.gy + b * kpt::kMlpOut;
+    L.partial = L.loss + c.steps;
     L.beta1 = 0.9f;
     L.beta2 = 0.999f;
     KPT_CUDA(cudaMemcpyAsync(L.params, sg->params.data(), pcount * sizeof(float),
@@ -1442,7 +1444,9 @@ int kpt_surrogate_gradient(kpt_context* ctx, const float* params, uint64_t n, co
     KPT_REQUIRE(n > 0 && n <= (1u << 20), "kpt_surrogate_gradient: 0 < n <= 2^20");
     if (int rc = activate(ctx)) return rc;
     const size_t pcount = kpt::kMlpParams;
-    const size_t floats = n * (5 + 3) + 2 * pcount + n * (5 + 4 * kpt::kMlpHidden + 3) + 1;
+    const size_t chunks = (n + kpt::kGradChunk - 1) / kpt::kGradChunk;
+    const size_t floats =
+        n * (5 + 3) + 2 * pcount + n * (5 + 4 * kpt::kMlpHidden + 3) + 1 + chunks * pcount;
     DeviceBuffer buf;
     KPT_CUDA(buf.reserve(floats * sizeof(float)));
     KPT_CUDA(cudaMemsetAsync(buf.ptr, 0, floats * sizeof(float), ctx->stream));
@@ -1473,6 +1477,7 @@ int kpt_surrogate_gradient(kpt_context* ctx, const float* params, uint64_t n, co
     L.g2 = L.g1 + n * kpt::kMlpHidden;
     L.gy = L.g2 + n * kpt::kMlpHidden;
     L.loss = L.gy + n * 3;
+    L.partial = L.loss + 1;
     cudaStream_t st = ctx->stream;
     KPT_CUDA(cudaMemcpyAsync(x, inputs, n * 5 * sizeof(float), cudaMemcpyHostToDevice, st));
     KPT_CUDA(cudaMemcpyAsync(t, targets, n * 3 * sizeof(float), cudaMemcpyHostToDevice, st));
@@ -1664,6 +1669,19 @@ struct kpt_system {
     DeviceBuffer keys_a, keys_b, idx_a, idx_b, hist, staging, scalars;
 };
 
+struct kpt_focus_solver {
+    kpt_context* ctx = nullptr;
+    int device = 0;
+    kpt::LibGrid grid{};
+    uint64_t points = 0;
+    double* basis = nullptr;
+    int constant_ratio = 0;
+    double courant = 0.3;
+    double max_mu = 1.0;
+    kpt_scattering_parameters scattering{};
+    DeviceBuffer terms, scalars, dt_history;
+};
+
 struct kpt_parker_solver {
     kpt_context* ctx = nullptr;
     int device = 0;
@@ -1688,6 +1706,16 @@ const char* lib_error_message(int code) {
         case 4: return "ParkerSolver: projected diffusion coefficient is invalid.";
         case 5: return "ParkerSolver: local physical cell width must be positive.";
         case 7: return "ParkerSolver: adaptive deterministic time step is not positive and finite.";
+        case 8: return "FocusTransportSolver: pitch-angle cosine is not finite.";
+        case 9: return "FocusTransportSolver: focused transport requires |B| > 0.";
+        case 10: return "FocusTransportSolver: interpolated magnetic direction is invalid.";
+        case 11: return "FocusTransportSolver: diffusion coefficients must be finite and non-negative.";
+        case 12: return "FocusTransportSolver: pitch-angle stepping requires positive particle speed.";
+        case 13: return "LegencyModel: pitch-angle scattering requires positive local inputs.";
+        case 14: return "LegencyModel: D_mumu requires positive omega, speed, sigma2, and Lc.";
+        case 15: return "LegencyModel: D_mumu denominator must be positive.";
+        case 16: return "FocusTransportSolver: adaptive stochastic time step is not positive and finite.";
+        case 17: return "FocusTransportSolver: adaptive deterministic time step is not positive and finite.";
         default: return "ParkerSolver: adaptive stochastic time step is not positive and finite.";
     }
 }
@@ -2088,10 +2116,9 @@ int parker_launch(kpt_context* ctx, kpt_parker_solver* s, kpt_system* sys, int a
     return KPT_OK;
 }
 
-int parker_finish(kpt_context* ctx, kpt_parker_solver* s, double* dt_out, bool stochastic) {
+int step_finish(kpt_context* ctx, void* scalars, double* dt_out, bool stochastic, bool focus) {
     char host[32];
-    KPT_CUDA(cudaMemcpyAsync(host, s->scalars.ptr, sizeof(host), cudaMemcpyDeviceToHost,
-                             ctx->stream));
+    KPT_CUDA(cudaMemcpyAsync(host, scalars, sizeof(host), cudaMemcpyDeviceToHost, ctx->stream));
     KPT_CUDA(cudaStreamSynchronize(ctx->stream));
     double dt;
     int error;
@@ -2101,7 +2128,9 @@ int parker_finish(kpt_context* ctx, kpt_parker_solver* s, double* dt_out, bool s
     std::memcpy(&index, host + 24, sizeof(index));
     if (dt_out) *dt_out = dt;
     if (error != 0) {
-        std::string msg = lib_error_message(error == 6 && !stochastic ? 7 : error);
+        int code = error;
+        if (error == 6) code = focus ? (stochastic ? 16 : 17) : (stochastic ? 6 : 7);
+        std::string msg = lib_error_message(code);
         if (error != 6) msg += " (particle " + std::to_string(index) + ")";
         return set_error(KPT_ERROR_INVALID_ARGUMENT, msg);
     }
@@ -2119,7 +2148,7 @@ int parker_step(kpt_context* ctx, kpt_parker_solver* s, kpt_system* sys, int adv
     }
     KPT_CUDA(cudaMemsetAsync(s->scalars.ptr, 0, 32, ctx->stream));
     KPT_CUDA(kpt::lib_parker_step(L, ctx->stream));
-    return parker_finish(ctx, s, dt_out, stochastic != 0);
+    return step_finish(ctx, s->scalars.ptr, dt_out, stochastic != 0, false);
 }
 
 }  // namespace
@@ -2190,7 +2219,228 @@ int kpt_parker_advance_stochastic_steps(kpt_context* ctx, kpt_parker_solver* s,
         KPT_CUDA(cudaMemcpyAsync(dts, s->dt_history.ptr, steps * sizeof(double),
                                  cudaMemcpyDeviceToHost, ctx->stream));
     }
-    return parker_finish(ctx, s, nullptr, true);
+    return step_finish(ctx, s->scalars.ptr, nullptr, true, false);
+}
+
+}  // extern "C"
+
+// ---- FocusTransportSolver ----------------------------------------------------
+
+namespace {
+
+int focus_validate(const kpt_focus_solver* s, const kpt_system* sys) {
+    if (!std::isfinite(s->courant) || s->courant <= 0.0) {
+        return set_error(KPT_ERROR_INVALID_ARGUMENT,
+                         "FocusTransportSolver: Courant scale must be positive and finite.");
+    }
+    if (!std::isfinite(sys->props.charge) || sys->props.charge == 0.0) {
+        return set_error(KPT_ERROR_INVALID_ARGUMENT,
+                         "FocusTransportSolver: focused drift requires nonzero charge.");
+    }
+    return KPT_OK;
+}
+
+int focus_launch(kpt_focus_solver* s, kpt_system* sys, int advance, int stochastic,
+                 uint64_t seed, uint32_t step, double* dt_history, kpt::LibFocusLaunch* out) {
+    KPT_CUDA(s->terms.reserve(std::max<uint64_t>(sys->count, 1) * kpt::kFocusTermCount *
+                              sizeof(double)));
+    kpt::LibFocusLaunch& L = *out;
+    L = kpt::LibFocusLaunch{};
+    L.grid = s->grid;
+    L.basis = s->basis;
+    L.constant_ratio = s->constant_ratio;
+    L.sys = sys->a;
+    L.count = sys->count;
+    L.capacity = sys->capacity;
+    L.rest_mass = sys->props.rest_mass;
+    L.charge = sys->props.charge;
+    L.abs_charge = std::fabs(sys->props.charge);
+    L.speed_of_light = sys->props.speed_of_light;
+    L.mc = sys->props.rest_mass * sys->props.speed_of_light;
+    const kpt_scattering_parameters& sc = s->scattering;
+    L.gk = sc.spectral_index;
+    L.h0 = sc.h0;
+    // pitch_angle_spectrum_normalization (LegencyModel.hpp:539-552)
+    L.qlt_norm = sc.spectral_index * std::sin(3.141592653589793238462643383279502884 /
+                                              sc.spectral_index) /
+                 3.141592653589793238462643383279502884;
+    L.min_b = sc.minimum_magnetic_field_magnitude;
+    L.min_sigma2 = sc.minimum_sigma2;
+    L.min_lc = sc.minimum_correlation_length;
+    L.min_speed = sc.minimum_speed;
+    L.max_mu = s->max_mu;
+    L.courant = s->courant;
+    L.terms = s->terms.as<double>();
+    char* scp = static_cast<char*>(s->scalars.ptr);
+    L.min_bits = reinterpret_cast<unsigned long long*>(scp);
+    L.dt_device_out = reinterpret_cast<double*>(scp + 8);
+    L.error = reinterpret_cast<int*>(scp + 16);
+    L.error_index = reinterpret_cast<unsigned long long*>(scp + 24);
+    L.dt_history = dt_history;
+    L.apply_boundary = advance;
+    L.advance = advance;
+    L.stochastic = stochastic;
+    L.capture = 1;
+    L.key = make_uint2(static_cast<uint32_t>(seed), static_cast<uint32_t>(seed >> 32));
+    L.frame = step;
+    return KPT_OK;
+}
+
+int focus_step(kpt_context* ctx, kpt_focus_solver* s, kpt_system* sys, int advance,
+               int stochastic, uint64_t seed, uint32_t step, double* dt_out) {
+    KPT_REQUIRE(ctx && s && sys, "FocusTransportSolver: NULL handle");
+    if (int rc = focus_validate(s, sys)) return rc;
+    if (int rc = activate(ctx)) return rc;
+    kpt::LibFocusLaunch L;
+    if (int rc = focus_launch(s, sys, advance, stochastic, seed, step, nullptr, &L)) return rc;
+    KPT_CUDA(cudaMemsetAsync(s->scalars.ptr, 0, 32, ctx->stream));
+    KPT_CUDA(kpt::lib_focus_step(L, ctx->stream));
+    return step_finish(ctx, s->scalars.ptr, dt_out, stochastic != 0, true);
+}
+
+}  // namespace
+
+extern "C" {
+
+int kpt_focus_solver_create(kpt_context* ctx, const kpt_grid* grid, const double* basis,
+                            int constant_ratio, double courant,
+                            const kpt_scattering_parameters* scattering,
+                            kpt_focus_solver** out) {
+    KPT_REQUIRE(ctx && grid && basis && out, "kpt_focus_solver_create: NULL argument");
+    *out = nullptr;
+    kpt_scattering_parameters sc{5.0 / 3.0, 1.0e-6, 0.0, 0.0, 0.0, 0.0};
+    if (scattering != nullptr) sc = *scattering;
+    // PitchAngleScatteringParameters::validate (LegencyModel.hpp:205-221)
+    KPT_REQUIRE(std::isfinite(sc.spectral_index) && sc.spectral_index > 1.0 &&
+                    std::isfinite(sc.h0) && sc.h0 > 0.0 &&
+                    std::isfinite(sc.minimum_magnetic_field_magnitude) &&
+                    sc.minimum_magnetic_field_magnitude >= 0.0 &&
+                    std::isfinite(sc.minimum_sigma2) && sc.minimum_sigma2 >= 0.0 &&
+                    std::isfinite(sc.minimum_correlation_length) &&
+                    sc.minimum_correlation_length >= 0.0 && std::isfinite(sc.minimum_speed) &&
+                    sc.minimum_speed >= 0.0,
+                "LegencyModel::PitchAngleScatteringParameters: coefficients and floors must be "
+                "finite, with spectral_index > 1 and resonance_regularization_h0 > 0.");
+    if (int rc = activate(ctx)) return rc;
+    std::unique_ptr<kpt_focus_solver> s(new kpt_focus_solver());
+    s->ctx = ctx;
+    s->device = ctx->device;
+    s->grid = grid->g;
+    s->points = static_cast<uint64_t>(grid->nx + 4) * static_cast<uint64_t>(grid->ny + 4);
+    s->courant = courant;
+    s->scattering = sc;
+    KPT_CUDA(cudaMalloc(&s->basis, s->points * kpt::kFocusBasisStride * sizeof(double)));
+    KPT_CUDA(s->scalars.reserve(64));
+    kpt_focus_solver* raw = s.release();
+    if (int rc = kpt_focus_solver_set_basis(raw, basis, constant_ratio)) {
+        kpt_focus_solver_destroy(raw);
+        return rc;
+    }
+    *out = raw;
+    return KPT_OK;
+}
+
+int kpt_focus_solver_destroy(kpt_focus_solver* s) {
+    if (s == nullptr) return KPT_OK;
+    cudaSetDevice(s->device);
+    cudaFree(s->basis);
+    s->terms.release();
+    s->scalars.release();
+    s->dt_history.release();
+    delete s;
+    return KPT_OK;
+}
+
+int kpt_focus_solver_set_basis(kpt_focus_solver* s, const double* basis, int constant_ratio) {
+    KPT_REQUIRE(s && basis, "kpt_focus_solver_set_basis: NULL argument");
+    KPT_CUDA(cudaSetDevice(s->device));
+    // rows of 27 values to the 28-value stride
+    KPT_CUDA(cudaMemcpy2D(s->basis, kpt::kFocusBasisStride * sizeof(double), basis,
+                          kpt::kFocusBasis * sizeof(double), kpt::kFocusBasis * sizeof(double),
+                          s->points, cudaMemcpyHostToDevice));
+    s->constant_ratio = constant_ratio != 0 ? 1 : 0;
+    return KPT_OK;
+}
+
+int kpt_focus_solver_set_courant(kpt_focus_solver* s, double courant) {
+    KPT_REQUIRE(s != nullptr, "kpt_focus_solver_set_courant: NULL handle");
+    s->courant = courant;
+    return KPT_OK;
+}
+
+int kpt_focus_solver_set_maximum_mu(kpt_focus_solver* s, double maximum_mu) {
+    KPT_REQUIRE(s != nullptr, "kpt_focus_solver_set_maximum_mu: NULL handle");
+    KPT_REQUIRE(std::isfinite(maximum_mu) && maximum_mu > 0.0 && maximum_mu <= 1.0,
+                "FocusTransportSolver: maximum |mu| must satisfy 0 < value <= 1.");
+    s->max_mu = maximum_mu;
+    return KPT_OK;
+}
+
+int kpt_focus_compute_time_step(kpt_context* ctx, kpt_focus_solver* s, kpt_system* sys,
+                                double* dt) {
+    return focus_step(ctx, s, sys, 0, 0, 0, 0, dt);
+}
+
+int kpt_focus_advance_stochastic(kpt_context* ctx, kpt_focus_solver* s, kpt_system* sys,
+                                 uint64_t seed, uint32_t step, double* dt_used) {
+    return focus_step(ctx, s, sys, 1, 1, seed, step, dt_used);
+}
+
+int kpt_focus_advance_deterministic(kpt_context* ctx, kpt_focus_solver* s, kpt_system* sys,
+                                    double* dt_used) {
+    return focus_step(ctx, s, sys, 1, 0, 0, 0, dt_used);
+}
+
+int kpt_focus_advance_stochastic_steps(kpt_context* ctx, kpt_focus_solver* s, kpt_system* sys,
+                                       uint64_t seed, uint32_t first_step, uint32_t steps,
+                                       double* dts) {
+    KPT_REQUIRE(ctx && s && sys, "FocusTransportSolver: NULL handle");
+    if (steps == 0) return KPT_OK;
+    if (int rc = focus_validate(s, sys)) return rc;
+    if (int rc = activate(ctx)) return rc;
+    KPT_CUDA(s->dt_history.reserve(static_cast<size_t>(steps) * sizeof(double)));
+    KPT_CUDA(cudaMemsetAsync(s->scalars.ptr, 0, 32, ctx->stream));
+    std::vector<kpt::LibFocusLaunch> launches(steps);
+    for (uint32_t k = 0; k < steps; ++k) {
+        if (int rc = focus_launch(s, sys, 1, 1, seed, first_step + k,
+                                  s->dt_history.as<double>() + k, &launches[k])) {
+            return rc;
+        }
+    }
+    cudaGraph_t graph = nullptr;
+    bool captured = false;
+    if (ctx->stream != nullptr &&
+        cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        cudaError_t err = cudaSuccess;
+        for (uint32_t k = 0; k < steps && err == cudaSuccess; ++k) {
+            err = kpt::lib_focus_step(launches[k], ctx->stream);
+        }
+        const cudaError_t end = cudaStreamEndCapture(ctx->stream, &graph);
+        KPT_CUDA(err);
+        KPT_CUDA(end);
+        captured = true;
+    }
+    if (captured) {
+        cudaGraphExec_t exec = nullptr;
+        const cudaError_t inst = cudaGraphInstantiate(&exec, graph, 0);
+        if (inst != cudaSuccess) {
+            cudaGraphDestroy(graph);
+            KPT_CUDA(inst);
+        }
+        const cudaError_t run = cudaGraphLaunch(exec, ctx->stream);
+        cudaGraphExecDestroy(exec);
+        cudaGraphDestroy(graph);
+        KPT_CUDA(run);
+    } else {
+        for (uint32_t k = 0; k < steps; ++k) {
+            KPT_CUDA(kpt::lib_focus_step(launches[k], ctx->stream));
+        }
+    }
+    if (dts) {
+        KPT_CUDA(cudaMemcpyAsync(dts, s->dt_history.ptr, steps * sizeof(double),
+                                 cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    return step_finish(ctx, s->scalars.ptr, nullptr, true, true);
 }
 
 }  // extern "C"

@@ -157,8 +157,10 @@ struct SurrogateTrainLaunch {
     float* g2;
     float* gy;        // batch x 3
     float* loss;      // one float per step
+    float* partial;   // ceil(batch / kGradChunk) x kMlpParams gradient partials
     float beta1, beta2, lr;
 };
+constexpr int kGradChunk = 256;
 cudaError_t surrogate_make_samples(uint64_t seed, int n, const SurrogateBox& box, float* x,
                                    float* t, cudaStream_t stream);
 cudaError_t surrogate_train_step(const SurrogateTrainLaunch& launch, int step,
@@ -224,6 +226,37 @@ struct LibParkerLaunch {
     unsigned long long* error_index;
 };
 cudaError_t lib_parker_step(const LibParkerLaunch& launch, cudaStream_t stream);
+
+// Packed focused basis (FocusSolver.hpp:106-136) for VecDim 3: B(3) b(3)
+// V(3) gradient drift(3) curvature drift(3) perpendicular diffusion
+// advection(3) |B| kappa_par kappa_perp divV focusing bb:gradV b.dV/dt
+// sigma^2 Lc; rows padded to 28 doubles (16-byte aligned).
+constexpr int kFocusBasis = 27;
+constexpr int kFocusBasisStride = 28;
+constexpr int kFocusTermCount = 18;
+
+struct LibFocusLaunch {
+    LibGrid grid;
+    const double* basis;  // ghosted points x kFocusBasisStride
+    int constant_ratio;
+    SystemArrays sys;
+    uint64_t count, capacity;
+    double rest_mass, charge, abs_charge, speed_of_light, mc;
+    double gk, h0, qlt_norm, min_b, min_sigma2, min_lc, min_speed, max_mu;
+    double courant;
+    double* terms;  // count x kFocusTermCount
+    unsigned long long* min_bits;
+    double* dt_device_out;
+    double* dt_history;
+    const double* dt_device;
+    double dt;
+    int apply_boundary, advance, stochastic, capture;
+    uint2 key;
+    uint32_t frame;
+    int* error;
+    unsigned long long* error_index;
+};
+cudaError_t lib_focus_step(const LibFocusLaunch& launch, cudaStream_t stream);
 
 struct LibSplitLaunch {
     SystemArrays sys;

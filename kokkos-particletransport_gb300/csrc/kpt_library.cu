@@ -91,14 +91,15 @@ __device__ __forceinline__ void lib_stencil(const LibAxis& a, double x, int& lo,
 // LinearPositionInterpolator::sample of the 18-component packed basis
 // (FieldInterpolator.hpp:346-380): corners in order, weight = product of the
 // per-axis factors, values accumulated in component order.
+template <int C, int STRIDE>
 __device__ __forceinline__ void lib_sample(const LibGrid& g, const double* __restrict__ basis,
-                                           double x, double y, double (&out)[kLibBasis]) {
+                                           double x, double y, double (&out)[C]) {
     int lo[2], hi[2];
     double w[2];
     lib_stencil(g.axis[0], x, lo[0], hi[0], w[0]);
     lib_stencil(g.axis[1], y, lo[1], hi[1], w[1]);
 #pragma unroll
-    for (int c = 0; c < kLibBasis; ++c) out[c] = 0.0;
+    for (int c = 0; c < C; ++c) out[c] = 0.0;
 #pragma unroll
     for (int corner = 0; corner < 4; ++corner) {
         const bool ux = (corner & 1) != 0;
@@ -108,12 +109,15 @@ __device__ __forceinline__ void lib_sample(const LibGrid& g, const double* __res
         weight = __dmul_rn(weight, uy ? w[1] : __dsub_rn(1.0, w[1]));
         const int i = (ux ? hi[0] : lo[0]) + 2;
         const int j = (uy ? hi[1] : lo[1]) + 2;
-        const double* row = basis + (static_cast<size_t>(j) * g.ex + i) * kLibBasisStride;
+        const double* row = basis + (static_cast<size_t>(j) * g.ex + i) * STRIDE;
 #pragma unroll
-        for (int c = 0; c < kLibBasis; c += 2) {
+        for (int c = 0; c + 1 < C; c += 2) {
             const double2 v = __ldg(reinterpret_cast<const double2*>(row + c));
             out[c] = __dadd_rn(out[c], __dmul_rn(weight, v.x));
             out[c + 1] = __dadd_rn(out[c + 1], __dmul_rn(weight, v.y));
+        }
+        if (C % 2 == 1) {
+            out[C - 1] = __dadd_rn(out[C - 1], __dmul_rn(weight, __ldg(row + C - 1)));
         }
     }
 }
@@ -181,7 +185,7 @@ __device__ double lib_parker_terms(const LibParkerLaunch& L, size_t i, double* t
         }
     }
     double v[kLibBasis];
-    lib_sample(g, L.basis, q[0], q[1], v);
+    lib_sample<kLibBasis, kLibBasisStride>(g, L.basis, q[0], q[1], v);
 
     const double p_in = s.p[i];
     const double p = p_in >= 0.0 ? p_in : -p_in;
@@ -401,6 +405,325 @@ __global__ void lib_reset_min_kernel(unsigned long long* min_bits) {
     *min_bits = static_cast<unsigned long long>(__double_as_longlong(kLargeTimeStep));
 }
 
+// ---- FocusTransportSolver ----------------------------------------------------
+
+enum FocusSlot {
+    fRateX = 0, fRateY, fMomentumRate, fKappaPerp, fDirX, fDirY, fDirZ, fMomentum, fMu, fSpeed,
+    fGamma, fBmag, fDivV, fBBGradV, fConvective, fFocusing, fSigma2, fLc
+};
+static_assert(fLc + 1 <= kFocusTermCount, "focus term row layout");
+
+// reflected_pitch_angle_cosine (FocusSolver.hpp:453-470).
+__device__ __forceinline__ double focus_reflect(double mu, double max_mu, int* error) {
+    if (!isfinite(mu)) {
+        *error = 8;  // "pitch-angle cosine is not finite"
+        return 0.0;
+    }
+    const double upper = max_mu;
+    const double lower = -max_mu;
+    for (int guard = 0; guard < 64 && (mu > upper || mu < lower); ++guard) {
+        if (mu > upper) mu = 2.0 * upper - mu;
+        if (mu < lower) mu = 2.0 * lower - mu;
+    }
+    return mu;
+}
+
+__device__ __forceinline__ double positive_floor(double v, double floor_value) {
+    if (floor_value <= 0.0) return v;
+    return v < floor_value ? floor_value : v;
+}
+
+struct PitchRates {
+    double focusing, D, dD, rate;
+};
+
+// evaluate_pitch_angle_at_mu (FocusSolver.hpp:664-695) with the slab-QLT
+// evaluate_pitch_angle_scattering (LegencyModel.hpp:539-693).
+__device__ PitchRates focus_pitch(const LibFocusLaunch& L, const double* t, double trial,
+                                  int* error) {
+    PitchRates r{0.0, 0.0, 0.0, 0.0};
+    const double mu = focus_reflect(trial, L.max_mu, error);
+    const double mu2 = mu * mu;
+    const double one_minus_mu2 = 1.0 - mu2;
+    const double speed = t[fSpeed];
+    if (speed <= 0.0) {
+        *error = 12;  // "pitch-angle stepping requires positive particle speed"
+        return r;
+    }
+    r.focusing = 0.5 * one_minus_mu2 *
+                 (-speed * t[fFocusing] + mu * t[fDivV] - 3.0 * mu * t[fBBGradV] -
+                  2.0 * t[fConvective] / speed);
+    const double safe_b = positive_floor(t[fBmag], L.min_b);
+    const double safe_sigma2 = positive_floor(t[fSigma2], L.min_sigma2);
+    const double safe_lc = positive_floor(t[fLc], L.min_lc);
+    const double safe_speed = positive_floor(speed, L.min_speed);
+    if (safe_b <= 0.0 || safe_sigma2 <= 0.0 || safe_lc <= 0.0 || safe_speed <= 0.0) {
+        *error = 13;  // "pitch-angle scattering requires positive local inputs"
+        return r;
+    }
+    const double omega = L.abs_charge * safe_b / (L.rest_mass * L.speed_of_light) / t[fGamma];
+    // pitch_angle_diffusion_coefficient (LegencyModel.hpp:557-594)
+    if (omega <= 0.0) {
+        *error = 14;  // "D_mumu requires positive omega, speed, sigma2, and Lc"
+        return r;
+    }
+    double d = 0.0;
+    double dd = 0.0;
+    if (one_minus_mu2 > 0.0) {
+        const double reg = (mu >= 0.0 ? mu : -mu) + L.h0;
+        const double gk = L.gk;
+        const double xi = omega * safe_lc / safe_speed;
+        const double den = pow(reg, gk) + pow(xi, gk);
+        if (den <= 0.0) {
+            *error = 15;  // "D_mumu denominator must be positive"
+            return r;
+        }
+        const double pref = 0.25 * 3.141592653589793238462643383279502884 * omega * safe_sigma2 *
+                            L.qlt_norm;
+        const double reg_gk1 = pow(reg, gk - 1.0);
+        d = pref * one_minus_mu2 * xi * reg_gk1 / den;
+        // pitch_angle_diffusion_derivative (LegencyModel.hpp:599-645)
+        const double sign = mu > 0.0 ? 1.0 : (mu < 0.0 ? -1.0 : 0.0);
+        if (d != 0.0 && sign != 0.0) {
+            const double shape = sign * ((gk - 1.0) / reg - gk * reg_gk1 / den);
+            dd = d * (-2.0 * mu / one_minus_mu2 + shape);
+        }
+    }
+    r.D = d;
+    r.dD = dd;
+    r.rate = r.focusing + dd;
+    return r;
+}
+
+// evaluate_terms_from_packed + local_stable_time_step
+// (FocusSolver.hpp:904-1008, :1148-1233).
+__device__ double focus_terms(const LibFocusLaunch& L, size_t i, double* t, int* error) {
+    const LibGrid& g = L.grid;
+    const SystemArrays& s = L.sys;
+    double pos[2] = {s.x[i], s.y[i]};
+#pragma unroll
+    for (int dim = 0; dim < 2; ++dim) {
+        pos[dim] = lib_wrap(g.axis[dim], pos[dim]);
+        if (!lib_contains(g.axis[dim].lower, g.axis[dim].upper, pos[dim])) {
+            for (int k = 0; k < kFocusTermCount; ++k) t[k] = 0.0;
+            return 0.0;
+        }
+    }
+    double q[2];
+#pragma unroll
+    for (int dim = 0; dim < 2; ++dim) {
+        q[dim] = lib_wrap(g.axis[dim], pos[dim]);
+        if (!lib_contains(g.axis[dim].ghost_lower, g.axis[dim].ghost_upper, q[dim])) {
+            *error = 1;
+            return -1.0;
+        }
+    }
+    double v[kFocusBasis];
+    lib_sample<kFocusBasis, kFocusBasisStride>(g, L.basis, q[0], q[1], v);
+    const double p_in = s.p[i];
+    const double p = p_in >= 0.0 ? p_in : -p_in;
+    const double mu = focus_reflect(s.mu[i], L.max_mu, error);
+    const double normalized = p / L.mc;
+    const double gamma = sqrt(1.0 + normalized * normalized);
+    const double speed = p / (gamma * L.rest_mass);
+    const double bmag = v[18];
+    if (!finite_positive(bmag)) {
+        *error = 9;  // "focused transport requires |B| > 0"
+        return -1.0;
+    }
+    double s2 = 0.0;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) s2 += v[3 + c] * v[3 + c];
+    const double smag = sqrt(s2);
+    if (!finite_positive(smag)) {
+        *error = 10;  // "interpolated magnetic direction is invalid"
+        return -1.0;
+    }
+    const double inv = 1.0 / smag;
+    double dir[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) dir[c] = v[3 + c] * inv;
+    const double perp_factor = L.constant_ratio ? pow(gamma, 1.0 / 3.0) : pow(gamma, 1.0 / 9.0);
+    const double kpar = v[19] * pow(gamma, 1.0 / 3.0);
+    const double kperp = v[20] * perp_factor;
+    if (!finite_nonnegative(kpar) || !finite_nonnegative(kperp)) {
+        *error = 11;  // "diffusion coefficients must be finite and non-negative"
+        return -1.0;
+    }
+    const double mu2 = mu * mu;
+    const double gdf = 0.5 * (1.0 - mu2);
+    const double cdf = mu2;
+    const double prefactor = p * speed * L.speed_of_light / L.charge;
+    double total[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const double streaming = speed * mu * dir[c];
+        const double drift = prefactor * (gdf * v[9 + c] + cdf * v[12 + c]);
+        const double diffadv = perp_factor * v[15 + c];
+        total[c] = streaming + v[6 + c] + drift + diffadv;
+    }
+    double keff[2];
+#pragma unroll
+    for (int d = 0; d < 2; ++d) {
+        const double projection = 1.0 - dir[d] * dir[d];
+        keff[d] = projection > 0.0 ? kperp * projection : 0.0;
+    }
+    t[fRateX] = total[0] * 1.0;
+    t[fRateY] = total[1] * 1.0;
+    t[fKappaPerp] = kperp;
+    t[fDirX] = dir[0];
+    t[fDirY] = dir[1];
+    t[fDirZ] = dir[2];
+    t[fMomentum] = p;
+    t[fMu] = mu;
+    t[fSpeed] = speed;
+    t[fGamma] = gamma;
+    t[fBmag] = bmag;
+    t[fDivV] = v[21];
+    t[fFocusing] = v[22];
+    t[fBBGradV] = v[23];
+    t[fConvective] = v[24];
+    t[fSigma2] = v[25];
+    t[fLc] = v[26];
+    const double one_minus_mu2 = 1.0 - mu2;
+    double acceleration = 0.0;
+    if (speed > 0.0) acceleration = mu * v[24] / speed;
+    const double momentum_factor = 0.5 * one_minus_mu2 * (v[21] - v[23]) + mu2 * v[23] +
+                                   acceleration;
+    const double momentum_rate = -p * momentum_factor;
+    t[fMomentumRate] = momentum_rate;
+    const PitchRates pitch = focus_pitch(L, t, mu, error);
+
+    double dmin = kLargeTimeStep;
+    double amin = kLargeTimeStep;
+#pragma unroll
+    for (int dim = 0; dim < 2; ++dim) {
+        const LibAxis& a = g.axis[dim];
+        const double x = lib_wrap(a, pos[dim]);
+        if (!lib_contains(a.lower, a.upper, x)) {
+            return kLargeTimeStep;
+        }
+        const double cell = static_cast<double>(lib_cell_index(a, x));
+        const double width = __dsub_rn(lib_face(a, __dadd_rn(cell, 1.0)), lib_face(a, cell));
+        const double dx = fabs(__dmul_rn(1.0, width));
+        if (!finite_positive(dx)) {
+            *error = 5;
+            return -1.0;
+        }
+        double diffusion_dt = kLargeTimeStep;
+        if (keff[dim] > 0.0) {
+            const double limited = 0.5 * dx;
+            diffusion_dt = limited * limited / (2.0 * keff[dim]);
+        }
+        const double adv = fabs(total[dim]);
+        double advection_dt = kLargeTimeStep;
+        if (adv > 0.0) advection_dt = 1.0 * dx / adv;
+        dmin = diffusion_dt < dmin ? diffusion_dt : dmin;
+        amin = advection_dt < amin ? advection_dt : amin;
+    }
+    double mdt = kLargeTimeStep;
+    const double mrate = fabs(momentum_rate);
+    if (p > 0.0 && mrate > 0.0) mdt = 1.0 * p / mrate;
+    double padv = kLargeTimeStep;
+    const double murate = fabs(pitch.rate);
+    if (murate > 0.0) padv = 10.0 * 0.1 / murate;
+    double pdiff = kLargeTimeStep;
+    if (pitch.D > 0.0) pdiff = 10.0 * 0.1 * 0.1 / (2.0 * pitch.D);
+    double pbal = kLargeTimeStep;
+    if (pitch.D > 0.0 && murate > 0.0) pbal = 10.0 * 2.0 * pitch.D / (murate * murate);
+    const double a1 = dmin < amin ? dmin : amin;
+    const double a2 = a1 < mdt ? a1 : mdt;
+    const double b1 = pdiff < pbal ? pdiff : pbal;
+    const double b2 = padv < b1 ? padv : b1;
+    return a2 < b2 ? a2 : b2;
+}
+
+__global__ void __launch_bounds__(256) focus_terms_kernel(const LibFocusLaunch L) {
+    double local = kLargeTimeStep;
+    const bool stopped = *L.error != 0;
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
+         !stopped && i < L.count; i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        if (L.sys.status[i] != 0) continue;
+        if (L.apply_boundary && !lib_boundary(L.grid, L.sys, i)) continue;
+        int err = 0;
+        const double dt = focus_terms(L, i, L.terms + i * kFocusTermCount, &err);
+        if (err != 0) {
+            record_error(L.error, err, static_cast<uint32_t>(i), L.error_index);
+            continue;
+        }
+        local = dt < local ? dt : local;
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        const double o = __shfl_down_sync(0xffffffffu, local, off);
+        local = o < local ? o : local;
+    }
+    __shared__ double warp_min[8];
+    if ((threadIdx.x & 31u) == 0u) warp_min[threadIdx.x >> 5] = local;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = warp_min[0];
+        for (int k = 1; k < static_cast<int>(blockDim.x >> 5); ++k) m = warp_min[k] < m ? warp_min[k] : m;
+        atomicMin(L.min_bits, static_cast<unsigned long long>(__double_as_longlong(m)));
+    }
+}
+
+// advance_*_with_packed_interpolator (FocusSolver.hpp:1580-1637) with the
+// Picard pitch-angle update (:697-740).
+__global__ void __launch_bounds__(256) focus_advance_kernel(const LibFocusLaunch L) {
+    const double dt = L.dt_device != nullptr ? *L.dt_device : L.dt;
+    if (!(isfinite(dt) && dt > 0.0) || *L.error != 0) {
+        return;
+    }
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
+         i < L.capacity; i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        const SystemArrays& s = L.sys;
+        if (L.capture) {
+            s.prevstep_x[i] = s.prev_x[i];
+            s.prevstep_y[i] = s.prev_y[i];
+            s.prev_x[i] = s.x[i];
+            s.prev_y[i] = s.y[i];
+        }
+        if (i >= L.count || s.status[i] != 0) continue;
+        const double* t = L.terms + i * kFocusTermCount;
+        double inc[2] = {0.0, 0.0};
+        double pitch_normal = 0.0;
+        if (L.stochastic) {
+            const uint32_t index = static_cast<uint32_t>(i);
+            double gv[3];
+            double parallel = 0.0;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                gv[c] = lib_normal(L.key, static_cast<uint32_t>(c), index, L.frame);
+                parallel += gv[c] * t[fDirX + c];
+            }
+            const double kperp = t[fKappaPerp];
+            const double scale = kperp > 0.0 ? sqrt(2.0 * kperp * dt) : 0.0;
+#pragma unroll
+            for (int c = 0; c < 2; ++c) inc[c] = scale * (gv[c] - parallel * t[fDirX + c]);
+            pitch_normal = lib_normal(L.key, 3u, index, L.frame);
+        }
+        s.x[i] += dt * t[fRateX] + inc[0] * 1.0;
+        s.y[i] += dt * t[fRateY] + inc[1] * 1.0;
+        const double updated = t[fMomentum] + dt * t[fMomentumRate];
+        s.p[i] = updated > 0.0 ? updated : 0.0;
+        int err = 0;
+        const double initial = focus_reflect(t[fMu], L.max_mu, &err);
+        double trial = initial;
+        for (int it = 0; it < 3; ++it) {
+            const PitchRates pitch = focus_pitch(L, t, trial, &err);
+            const double scale = pitch.D > 0.0 ? sqrt(2.0 * pitch.D * dt) : 0.0;
+            trial = initial + dt * pitch.rate + scale * pitch_normal;
+            trial = focus_reflect(trial, L.max_mu, &err);
+        }
+        if (err != 0) {
+            record_error(L.error, err, static_cast<uint32_t>(i), L.error_index);
+            continue;
+        }
+        s.mu[i] = trial;
+        lib_boundary(L.grid, s, i);
+    }
+}
+
 // ---- ParticleSystem lifecycle ------------------------------------------------
 
 __global__ void system_default_kernel(SystemArrays s, uint64_t count, uint64_t capacity) {
@@ -435,11 +758,14 @@ __global__ void system_capture_kernel(SystemArrays s, uint64_t capacity) {
     }
 }
 
-// kinetic energy (gamma - 1) m c^2 (ParticleSystem.hpp:190-193)
+// kinetic energy (gamma - 1) m c^2 (ParticleSystem.hpp:171-193), every
+// operation rounded on its own as the reference build evaluates it (the
+// baselines it writes are compared bit for bit)
 __device__ __forceinline__ double kinetic_energy(const LibSplitLaunch& L, double p) {
-    const double normalized = p / L.mc;
-    const double gamma = sqrt(1.0 + normalized * normalized);
-    return (gamma - 1.0) * L.rest_mass * L.speed_of_light * L.speed_of_light;
+    const double normalized = __ddiv_rn(p, L.mc);
+    const double gamma = __dsqrt_rn(__dadd_rn(1.0, __dmul_rn(normalized, normalized)));
+    return __dmul_rn(__dmul_rn(__dmul_rn(__dsub_rn(gamma, 1.0), L.rest_mass), L.speed_of_light),
+                     L.speed_of_light);
 }
 
 __global__ void system_reset_baselines_kernel(LibSplitLaunch L) {
@@ -468,11 +794,11 @@ __device__ __forceinline__ int split_decision(const LibSplitLaunch& L, uint64_t 
         atomicAdd(tallies + 2, 1ull);
         return 0;
     }
-    const double ratio = current / baseline;
+    const double ratio = __ddiv_rn(current, baseline);
     if (!isfinite(ratio) || ratio < L.split_ratio) return 0;
-    const int target = static_cast<int>(floor(log(ratio) / L.log_split_ratio));
+    const int target = static_cast<int>(floor(__ddiv_rn(log(ratio), L.log_split_ratio)));
     if (target <= s.split_level[i]) return 0;
-    const double child_weight = 0.5 * s.weight[i];
+    const double child_weight = __dmul_rn(0.5, s.weight[i]);
     if (!isfinite(child_weight) || child_weight <= 0.0 || child_weight < L.min_child_weight) {
         atomicAdd(tallies + 3, 1ull);
         return 0;
@@ -679,6 +1005,21 @@ cudaError_t lib_parker_step(const LibParkerLaunch& L, cudaStream_t stream) {
         LibParkerLaunch A = L;
         A.dt_device = L.dt_device_out;
         lib_parker_advance_kernel<<<grid_for(L.capacity, 256), 256, 0, stream>>>(A);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t lib_focus_step(const LibFocusLaunch& L, cudaStream_t stream) {
+    lib_reset_min_kernel<<<1, 1, 0, stream>>>(L.min_bits);
+    if (L.count > 0) {
+        focus_terms_kernel<<<grid_for(L.count, 256), 256, 0, stream>>>(L);
+    }
+    lib_finish_dt_kernel<<<1, 1, 0, stream>>>(L.min_bits, L.courant, L.dt_device_out,
+                                              L.dt_history, L.error, L.advance);
+    if (L.advance) {
+        LibFocusLaunch A = L;
+        A.dt_device = L.dt_device_out;
+        focus_advance_kernel<<<grid_for(L.capacity, 256), 256, 0, stream>>>(A);
     }
     return cudaGetLastError();
 }

@@ -168,15 +168,19 @@ __global__ void __launch_bounds__(128) fwd_bwd_kernel(const float* __restrict__ 
     }
 }
 
-// Weight and bias gradients: one block per parameter row, threads over the
-// row's columns, a loop over the batch.  Row r of:
+// Weight and bias gradients, deterministic two-level reduction: block
+// (row, chunk) sums its chunk of kGradChunk samples for one parameter row,
+// threads over the row's columns; grad_sum_kernel then adds the chunk
+// partials in chunk order.  Row r of:
 //   W1 (64 rows x 5):  sum_b G1[b][r] X[b][c];   b1[r] = sum_b G1[b][r]
 //   W2 (64 rows x 64): sum_b G2[b][r] H1[b][c];  b2[r] = sum_b G2[b][r]
 //   W3 (3 rows x 64):  sum_b GY[b][r] H2[b][c];  b3[r] = sum_b GY[b][r]
-__global__ void __launch_bounds__(64) grad_kernel(int batch, const float* xb, const float* h1,
-                                                  const float* h2, const float* g1,
-                                                  const float* g2, const float* gy, float* grad) {
+__global__ void __launch_bounds__(64) grad_partial_kernel(int batch, const float* xb,
+                                                          const float* h1, const float* h2,
+                                                          const float* g1, const float* g2,
+                                                          const float* gy, float* partial) {
     const int row = blockIdx.x;
+    const int chunk = blockIdx.y;
     const int c = threadIdx.x;
     const float* delta;
     const float* input;
@@ -191,14 +195,33 @@ __global__ void __launch_bounds__(64) grad_kernel(int batch, const float* xb, co
         r = row - 2 * kMlpHidden; delta = gy; dstride = kMlpOut; input = h2;
         istride = kMlpHidden; cols = kMlpHidden; wbase = kMlpW3; bbase = kMlpB3;
     }
+    const int b0 = chunk * kGradChunk;
+    const int b1 = b0 + kGradChunk < batch ? b0 + kGradChunk : batch;
     float acc = 0.0f, bacc = 0.0f;
-    for (int b = 0; b < batch; ++b) {
+    for (int b = b0; b < b1; ++b) {
         const float d = delta[static_cast<size_t>(b) * dstride + r];
         if (c < cols) acc += d * input[static_cast<size_t>(b) * istride + c];
         bacc += d;
     }
-    if (c < cols) grad[wbase + r * cols + c] = acc;
-    if (c == 0) grad[bbase + r] = bacc;
+    float* out = partial + static_cast<size_t>(chunk) * kMlpParams;
+    if (c < cols) out[wbase + r * cols + c] = acc;
+    if (c == 0) out[bbase + r] = bacc;
+}
+
+__global__ void grad_sum_kernel(const float* partial, int chunks, float* grad) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= kMlpParams) return;
+    float sum = 0.0f;
+    for (int ch = 0; ch < chunks; ++ch) sum += partial[static_cast<size_t>(ch) * kMlpParams + k];
+    grad[k] = sum;
+}
+
+cudaError_t launch_gradients(const SurrogateTrainLaunch& L, cudaStream_t stream) {
+    const int chunks = (L.batch + kGradChunk - 1) / kGradChunk;
+    grad_partial_kernel<<<dim3(2 * kMlpHidden + kMlpOut, chunks), 64, 0, stream>>>(
+        L.batch, L.xb, L.h1, L.h2, L.g1, L.g2, L.gy, L.partial);
+    grad_sum_kernel<<<(kMlpParams + 255) / 256, 256, 0, stream>>>(L.partial, chunks, L.grad);
+    return cudaGetLastError();
 }
 
 __global__ void adam_kernel(float* params, const float* grad, float* m, float* v, float lr,
@@ -319,8 +342,7 @@ cudaError_t surrogate_train_step(const SurrogateTrainLaunch& L, int step, cudaSt
     fwd_bwd_kernel<<<(L.batch + 127) / 128, 128, 0, stream>>>(
         L.x, L.t, L.n, L.seed, step, L.batch, L.box, L.params, L.xb, L.h1, L.h2, L.g1, L.g2, L.gy,
         L.loss + step);
-    grad_kernel<<<2 * kMlpHidden + kMlpOut, 64, 0, stream>>>(L.batch, L.xb, L.h1, L.h2, L.g1,
-                                                              L.g2, L.gy, L.grad);
+    launch_gradients(L, stream);
     const float t1 = static_cast<float>(step + 1);
     const float bias1 = 1.0f - powf(L.beta1, t1);
     const float bias2 = 1.0f - powf(L.beta2, t1);
@@ -333,9 +355,7 @@ cudaError_t surrogate_gradient(const SurrogateTrainLaunch& L, cudaStream_t strea
     fwd_bwd_kernel<<<(L.batch + 127) / 128, 128, 0, stream>>>(
         L.x, L.t, L.n, L.seed, -1, L.batch, L.box, L.params, L.xb, L.h1, L.h2, L.g1, L.g2, L.gy,
         L.loss);
-    grad_kernel<<<2 * kMlpHidden + kMlpOut, 64, 0, stream>>>(L.batch, L.xb, L.h1, L.h2, L.g1,
-                                                              L.g2, L.gy, L.grad);
-    return cudaGetLastError();
+    return launch_gradients(L, stream);
 }
 
 cudaError_t surrogate_eval(int n, const double* inputs, const SurrogateBox& box,

@@ -271,6 +271,9 @@ class ReferenceHarness:
         lib.ref_lib_parker.restype = ll
         lib.ref_lib_parker.argtypes = [i32, i32, vp, vp, vp, vp, i32, vp, ull, i32, i32, i32, ll,
                                        ll, vp, vp, vp, vp]
+        lib.ref_lib_focus.restype = ll
+        lib.ref_lib_focus.argtypes = [i32, i32, vp, vp, vp, vp, i32, vp, vp, ull, i32, i32, i32,
+                                      ll, ll, vp, vp, vp, vp]
         lib.ref_lib_system.restype = ll
         lib.ref_lib_system.argtypes = [i32, i32, vp, vp, vp, vp, i32, i32, i32, ll, ll, vp, vp,
                                        vp, vp]
@@ -384,6 +387,30 @@ class ReferenceHarness:
             len(xe) - 1, len(ye) - 1, _ptr(xe), _ptr(ye), _ptr(periodic), _ptr(basis),
             int(constant_ratio), _ptr(pr), seed, first_step, steps, 0 if stochastic else 1,
             count, ids.size, _ptr(ids), _ptr(d), _ptr(i), _ptr(dts)))
+        self._lib_unblock(system, ids, d, i)
+        return dts[:steps]
+
+    def lib_focus(self, grid: dict, basis: np.ndarray, constant_ratio: bool, props: dict,
+                  scattering: dict, seed: int, first_step: int, steps: int, stochastic: bool,
+                  count: int, system: Dict[str, np.ndarray]) -> np.ndarray:
+        """FocusTransportSolver steps (include/FocusSolver.hpp) on a uniform Cartesian
+        grid; updates `system` in place and returns the dt of each step."""
+        xe = np.ascontiguousarray(grid["x_edges"], dtype=np.float64)
+        ye = np.ascontiguousarray(grid["y_edges"], dtype=np.float64)
+        periodic = np.ascontiguousarray(grid["periodic"], dtype=np.int32)
+        basis = np.ascontiguousarray(basis, dtype=np.float64)
+        pr = np.array([props["rest_mass"], props["charge"], props["speed_of_light"],
+                       props.get("energy_scale", 1.0), props["courant"]], dtype=np.float64)
+        sc = np.array([scattering["spectral_index"], scattering["h0"],
+                       scattering.get("min_b", 0.0), scattering.get("min_sigma2", 0.0),
+                       scattering.get("min_lc", 0.0), scattering.get("min_speed", 0.0),
+                       scattering.get("max_mu", 1.0)], dtype=np.float64)
+        ids, d, i = self._lib_blocks(system)
+        dts = np.zeros(max(1, steps), dtype=np.float64)
+        self._check(self.lib.ref_lib_focus(
+            len(xe) - 1, len(ye) - 1, _ptr(xe), _ptr(ye), _ptr(periodic), _ptr(basis),
+            int(constant_ratio), _ptr(pr), _ptr(sc), seed, first_step, steps,
+            0 if stochastic else 1, count, ids.size, _ptr(ids), _ptr(d), _ptr(i), _ptr(dts)))
         self._lib_unblock(system, ids, d, i)
         return dts[:steps]
 

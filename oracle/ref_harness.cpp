@@ -22,6 +22,7 @@
 
 #include <string>
 
+#include "FocusSolver.hpp"
 #include "LegencyModel.hpp"
 #include "ParkerSolver.hpp"
 
@@ -584,6 +585,93 @@ long long ref_lib_parker(int nx, int ny, const double* x_edges, const double* y_
         lib_load(sys, h);
         solver_type solver(sys, grid, b, v, coefficients);
         solver.set_dimensionless_courant_scale(Units::DimensionlessValue(props[4]));
+        RandomManager<> random_manager(seed);
+        Kokkos::ShimImpl::auto_frame_enabled() = 0;
+        for (int s = 0; s < steps; ++s) {
+            Kokkos::ShimImpl::current_frame() = static_cast<std::uint32_t>(first_step + s);
+            dts[s] = mode == 0 ? solver.advance_stochastic(random_manager)
+                               : solver.advance_deterministic();
+        }
+        lib_store(solver.particles, h);
+        return 0;
+    } catch (const std::exception& error) {
+        g_last_error = error.what();
+        return -1;
+    }
+}
+
+// FocusTransportSolver steps on a uniform 2D Cartesian grid.  basis holds
+// the 27-value packed basis per ghosted point (FocusSolver.hpp:106-136):
+// B(3) b(3) V(3) gradient drift basis(3) curvature drift basis(3)
+// perpendicular diffusion advection(3) |B| kappa_par kappa_perp divV
+// focusing bb:gradV b.dV/dt sigma^2 Lc.  Fields the step does not read
+// (ln B, grad ln B, curvature, dV/dt) are zero.  props = rest mass, charge,
+// c, energy scale, courant; scat = spectral index, h0, floors (|B|, sigma^2,
+// Lc, speed), maximum |mu|.
+long long ref_lib_focus(int nx, int ny, const double* x_edges, const double* y_edges,
+                        const int* periodic, const double* basis, int constant_ratio,
+                        const double* props, const double* scat, unsigned long long seed,
+                        int first_step, int steps, int mode, long long count, long long capacity,
+                        unsigned long long* ids, double* d, int* ints, double* dts) {
+    try {
+        using solver_type = FocusSolver<LibAnalyticGrid>;
+        using vector_field = typename solver_type::vector_field_type;
+        using scalar_field = typename solver_type::scalar_field_type;
+        const LibAnalyticGrid grid = make_lib_analytic_grid(nx, ny, x_edges, y_edges, periodic);
+        auto vec = [&](const char* name) { return vector_field(grid, name, GridCentering::CellCentered); };
+        auto sca = [&](const char* name) { return scalar_field(grid, name, GridCentering::CellCentered); };
+        vector_field b = vec("f_b"), dir = vec("f_dir"), v = vec("f_v"), grad = vec("f_grad"),
+                     curv = vec("f_curv"), perp = vec("f_perp"), glb = vec("f_glb"),
+                     kcurv = vec("f_kcurv"), dvdt = vec("f_dvdt");
+        scalar_field bmag = sca("f_bmag"), kpar = sca("f_kpar"), kperp = sca("f_kperp"),
+                     divv = sca("f_divv"), focus = sca("f_focus"), bbgv = sca("f_bbgv"),
+                     conv = sca("f_conv"), sig = sca("f_sig"), lc = sca("f_lc"),
+                     logb = sca("f_logb");
+        const std::size_t points = b.point_count();
+        for (std::size_t k = 0; k < points; ++k) {
+            const double* row = basis + 27 * k;
+            for (int c = 0; c < 3; ++c) {
+                b.data(k, c) = row[c];
+                dir.data(k, c) = row[3 + c];
+                v.data(k, c) = row[6 + c];
+                grad.data(k, c) = row[9 + c];
+                curv.data(k, c) = row[12 + c];
+                perp.data(k, c) = row[15 + c];
+                glb.data(k, c) = 0.0;
+                kcurv.data(k, c) = 0.0;
+                dvdt.data(k, c) = 0.0;
+            }
+            bmag.data(k, 0) = row[18];
+            kpar.data(k, 0) = row[19];
+            kperp.data(k, 0) = row[20];
+            divv.data(k, 0) = row[21];
+            focus.data(k, 0) = row[22];
+            bbgv.data(k, 0) = row[23];
+            conv.data(k, 0) = row[24];
+            sig.data(k, 0) = row[25];
+            lc.data(k, 0) = row[26];
+            logb.data(k, 0) = 0.0;
+        }
+        LegencyModel::DiffusionModelParameters diffusion;
+        if (constant_ratio) diffusion.set_constant_perpendicular_parallel_ratio(1.0);
+        LegencyModel::PitchAngleScatteringParameters scattering;
+        scattering.spectral_index = scat[0];
+        scattering.resonance_regularization_h0 = scat[1];
+        scattering.minimum_magnetic_field_magnitude = scat[2];
+        scattering.minimum_sigma2 = scat[3];
+        scattering.minimum_correlation_length = scat[4];
+        scattering.minimum_speed = scat[5];
+        typename solver_type::coefficient_field_set_type coefficients(
+            dir, bmag, logb, glb, kcurv, grad, curv, perp, kpar, kperp, divv, focus, bbgv, dvdt,
+            conv, sig, lc, diffusion, scattering);
+        LibSystem sys(static_cast<typename LibSystem::size_type>(count),
+                      static_cast<typename LibSystem::size_type>(capacity),
+                      lib_properties(props));
+        const LibHost h{ids, d, ints, capacity};
+        lib_load(sys, h);
+        solver_type solver(sys, grid, b, v, coefficients);
+        solver.set_dimensionless_courant_scale(Units::DimensionlessValue(props[4]));
+        solver.set_maximum_pitch_angle_cosine(scat[6]);
         RandomManager<> random_manager(seed);
         Kokkos::ShimImpl::auto_frame_enabled() = 0;
         for (int s = 0; s < steps; ++s) {

@@ -266,6 +266,42 @@ def lib_basis(nx: int, ny: int, x_edges, y_edges, readme: bool) -> np.ndarray:
     return out.reshape(-1, 18)
 
 
+def lib_focus_basis(nx: int, ny: int, x_edges, y_edges) -> np.ndarray:
+    """Smooth periodic focused-transport fields on every ghosted cell centre in
+    the packed order B(3) b(3) V(3) grad-drift(3) curvature-drift(3) perp-adv(3)
+    |B| kpar kperp divV focusing bb:gradV b.dV/dt sigma^2 Lc."""
+    parker = lib_basis(nx, ny, x_edges, y_edges, True).reshape(ny + 4, nx + 4, 18)
+    dx = (x_edges[-1] - x_edges[0]) / nx
+    dy = (y_edges[-1] - y_edges[0]) / ny
+    xc = x_edges[0] + (np.arange(-2, nx + 2) + 0.5) * dx
+    yc = y_edges[0] + (np.arange(-2, ny + 2) + 0.5) * dy
+    y, x = np.meshgrid(yc, xc, indexing="ij")
+    kx, ky = np.pi, np.pi / 2.0
+    out = np.zeros((ny + 4, nx + 4, 27))
+    b = parker[..., 0:3]
+    bmag = np.sqrt((b * b).sum(-1))
+    out[..., 0:3] = b
+    out[..., 3:6] = b / bmag[..., None]
+    out[..., 6:9] = parker[..., 3:6]
+    out[..., 9] = 0.01 * np.sin(kx * x)
+    out[..., 10] = 0.01 * np.cos(ky * y)
+    out[..., 12] = 0.005 * np.cos(kx * x + ky * y)
+    out[..., 13] = 0.005 * np.sin(kx * x)
+    out[..., 14] = 0.002
+    out[..., 15] = 1e-4 * np.sin(ky * y)
+    out[..., 16] = 1e-4 * np.cos(kx * x)
+    out[..., 18] = bmag
+    out[..., 19] = 0.01 * (1.2 + np.sin(kx * x) * np.cos(ky * y))
+    out[..., 20] = 5e-4 * (1.1 + np.cos(kx * x))
+    out[..., 21] = 0.1 * np.cos(kx * x) * np.sin(ky * y)
+    out[..., 22] = 0.2 * np.sin(kx * x - ky * y)
+    out[..., 23] = 0.05 * np.cos(ky * y)
+    out[..., 24] = 0.02 * np.sin(kx * x)
+    out[..., 25] = 0.1 * (1.0 + 0.5 * np.sin(kx * x) * np.sin(ky * y))
+    out[..., 26] = 0.05 * (1.0 + 0.2 * np.cos(kx * x))
+    return out.reshape(-1, 27)
+
+
 def lib_population(rng, count: int, capacity: int, x_edges, y_edges, open_y: bool) -> dict:
     system = binding.lib_default_system(count, capacity)
     system["x"][:count] = rng.uniform(x_edges[0], x_edges[-1], count)
@@ -309,6 +345,28 @@ def make_lib(ref, out_dir):
                  periodic=grid["periodic"], basis=basis, constant_ratio=int(not readme),
                  stochastic=int(stochastic), steps=steps, first_step=10, seed=SEED,
                  count=count, courant=props["courant"], dts=dts,
+                 **{f"start_{k}": v for k, v in start.items()},
+                 **{f"end_{k}": v for k, v in system.items()})
+    # FocusTransportSolver
+    focus_cases = (("readme_periodic", False, (1, 1), True, 4, 1.0),
+                   ("ratio_open_mumax", True, (1, 0), True, 3, 0.95),
+                   ("deterministic", False, (1, 1), False, 3, 1.0))
+    scattering = dict(spectral_index=5.0 / 3.0, h0=1e-6)
+    for name, ratio, periodic, stochastic, steps, max_mu in focus_cases:
+        grid = dict(x_edges=xe, y_edges=ye, periodic=np.array(periodic, dtype=np.int32))
+        basis = lib_focus_basis(nx, ny, xe, ye)
+        count, capacity = 600, 640
+        start = lib_population(rng, count, capacity, xe, ye, periodic[1] == 0)
+        system = {k: v.copy() for k, v in start.items()}
+        scat = dict(scattering, max_mu=max_mu)
+        dts = ref.lib_focus(grid, basis, ratio, props, scat, SEED, 20, steps, stochastic, count,
+                            system)
+        lib_save(out_dir, f"lib_focus_{name}.npz", x_edges=xe, y_edges=ye,
+                 periodic=grid["periodic"], basis=basis, constant_ratio=int(ratio),
+                 stochastic=int(stochastic), steps=steps, first_step=20, seed=SEED,
+                 count=count, courant=props["courant"], dts=dts,
+                 spectral_index=scattering["spectral_index"], h0=scattering["h0"],
+                 max_mu=max_mu,
                  **{f"start_{k}": v for k, v in start.items()},
                  **{f"end_{k}": v for k, v in system.items()})
     # ParticleSystem lifecycle

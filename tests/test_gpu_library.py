@@ -10,17 +10,18 @@ pool (tests/golden/make_golden.py).
   distance for wrapped coordinates); statuses and ids exact.  Both diffusion
   branches, periodic and open boundaries, stochastic and deterministic steps,
   and the graph-replayed multi-step call.
+* FocusTransportSolver: the same bars, pitch cosines included (reflection at
+  a maximum |mu| below 1, the three Picard iterations with the slab-QLT
+  closure).
 * ParticleSystem: boundary conditions, sort_by_key, compact, energy split and
   capture_previous_positions bit for bit.
 """
 from __future__ import annotations
 
-import os
-
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, load_golden
+from conftest import load_golden
 
 pytestmark = pytest.mark.gpu
 
@@ -123,6 +124,65 @@ def test_no_active_particle_is_an_error(ctx, kpt):
     assert solver.compute_time_step(system) == 0.0
     with pytest.raises(kpt.KptError, match="not positive and finite"):
         solver.advance_stochastic(system, 1, 0)
+    for h in (solver, system, grid):
+        h.close()
+
+
+FOCUS_CASES = ("readme_periodic", "ratio_open_mumax", "deterministic")
+
+
+def _focus_setup(ctx, data):
+    grid = ctx.grid(data["x_edges"], data["y_edges"], data["periodic"])
+    start = _state(data, "start")
+    system = ctx.system(int(data["count"]), start["x"].size)
+    system.upload(start)
+    solver = ctx.focus_solver(grid, data["basis"], bool(data["constant_ratio"]),
+                              float(data["courant"]), float(data["spectral_index"]),
+                              float(data["h0"]), maximum_mu=float(data["max_mu"]))
+    return grid, system, solver
+
+
+@pytest.mark.parametrize("case", FOCUS_CASES)
+def test_focus_solver_steps_match_reference(ctx, case):
+    data = load_golden(f"lib_focus_{case}.npz")
+    grid, system, solver = _focus_setup(ctx, data)
+    steps, first, seed = int(data["steps"]), int(data["first_step"]), int(data["seed"])
+    dts = []
+    for k in range(steps):
+        if int(data["stochastic"]):
+            dts.append(solver.advance_stochastic(system, seed, first + k))
+        else:
+            dts.append(solver.advance_deterministic(system))
+    # the pitch-angle limiters and reflections amplify last-bit pow/log
+    # differences between the two builds to ~3e-12 in dt after one step
+    np.testing.assert_allclose(dts, data["dts"], rtol=1e-10, atol=0)
+    got = system.download()
+    want = _state(data, "end")
+    for key in ("status", "level", "key", "id", "w", "e0"):
+        assert np.array_equal(got[key], want[key]), key
+    width_x = data["x_edges"][-1] - data["x_edges"][0]
+    width_y = data["y_edges"][-1] - data["y_edges"][0]
+    for key, width in (("x", width_x), ("prev_x", width_x), ("prevstep_x", width_x),
+                       ("y", width_y), ("prev_y", width_y), ("prevstep_y", width_y)):
+        diff = np.abs(got[key] - want[key])
+        diff = np.minimum(diff, np.abs(width - diff)) / width
+        assert diff.max() <= 1e-10, (key, diff.max())
+    for key in ("p", "mu"):
+        scale = np.maximum(np.abs(want[key]), 1e-12)
+        assert (np.abs(got[key] - want[key]) / scale).max() <= 1e-10, key
+    for h in (solver, system, grid):
+        h.close()
+
+
+def test_focus_graph_steps_and_limits(ctx, kpt):
+    data = load_golden("lib_focus_readme_periodic.npz")
+    grid, system, solver = _focus_setup(ctx, data)
+    assert solver.compute_time_step(system) == pytest.approx(float(data["dts"][0]), rel=1e-12)
+    steps, first, seed = int(data["steps"]), int(data["first_step"]), int(data["seed"])
+    dts = solver.advance_stochastic_steps(system, seed, first, steps)
+    np.testing.assert_allclose(dts, data["dts"], rtol=1e-12, atol=0)
+    with pytest.raises(kpt.KptError, match="maximum"):
+        solver.set_maximum_mu(1.5)
     for h in (solver, system, grid):
         h.close()
 
