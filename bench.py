@@ -281,6 +281,93 @@ def run_parker(args, f0, f1):
     return out
 
 
+def run_batched(args):
+    """64 independent mixed-precision Parker runs: fields drawn from
+    {128x128, 256x512, 512x1024, 1024x2048} with seeded sheet width U[0.05, 0.2]
+    and island amplitude U[0, 0.2]; N log-uniform in [1e4, 1e6]; fixed dt of
+    1/200 interval, so every particle takes 200 substeps per interval.  One
+    interval pushed as 64 sequential per-run launches (cell sort + push each)
+    against the same interval pushed by the batched graph with the autotuned
+    schedule, from the same state."""
+    import torch
+    kpt = importlib.import_module("kokkos-particletransport_gb300")
+    rng = np.random.default_rng(SEED)
+    sizes = [(128, 128), (256, 512), (512, 1024), (1024, 2048)]
+    ctx = kpt.Context(0)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    runs = []
+    t0 = time.perf_counter()
+    for r in range(args.batch_runs):
+        nx, ny = sizes[int(rng.integers(0, len(sizes)))]
+        width = float(rng.uniform(0.05, 0.2))
+        amp = float(rng.uniform(0.0, 0.2))
+        n = int(np.exp(rng.uniform(np.log(1e4), np.log(1e6))))
+        field = fields.harris_field(nx, ny, sheet_width=width, island_amplitude=amp,
+                                    noise=0.01, seed=SEED + r)
+        table = ctx.field(field, kpt.TABLE_PARKER16, kpt.PRECISION_MIXED)
+        settings = kpt.default_settings(kperp_over_kpara=0.05, dt_min_rel=0.005,
+                                        dt_max_rel=0.005)
+        parts = ctx.particles(n)
+        ctx.inject(parts, table, settings, n, START_FRAME, SEED + r)
+        ctx.push_interval(parts, table, table, settings, START_FRAME, SEED + r)  # spread-in
+        runs.append(dict(table=table, settings=settings, parts=parts, n=n, seed=SEED + r,
+                         state=parts.download(), size=(nx, ny)))
+    setup_s = time.perf_counter() - t0
+    frame = START_FRAME + 1
+    total = sum(r["n"] for r in runs)
+    # sequential: one launch sequence per run
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    seq_steps = 0
+    for run in runs:
+        ctx.sort(run["parts"], run["table"], 16, 16)
+        seq_steps += ctx.push_interval(run["parts"], run["table"], run["table"], run["settings"],
+                                       frame, run["seed"]).particle_steps
+    e1.record(stream)
+    e1.synchronize()
+    seq_ms = e0.elapsed_time(e1)
+    sequential = [run["parts"].download() for run in runs]
+    for run in runs:
+        run["parts"].upload(run["state"], run["n"])
+    batch = ctx.batch()
+    for run in runs:
+        batch.add_run(run["parts"], run["table"], run["table"], run["settings"], run["seed"],
+                      frame)
+    tuning = batch.autotune(1)  # times the candidate schedules on a saved copy
+    batch.run(1)  # records the graph of the chosen schedule
+    for k, run in enumerate(runs):
+        run["parts"].upload(run["state"], run["n"])
+        batch.set_frame(k, frame)
+    torch.cuda.synchronize()
+    b0 = torch.cuda.Event(enable_timing=True)
+    b1 = torch.cuda.Event(enable_timing=True)
+    b0.record(stream)
+    batch.run(1)  # graph replay: per-run cell sorts, one batched push, next frame
+    b1.record(stream)
+    b1.synchronize()
+    batch_s = b0.elapsed_time(b1) / 1e3
+    bat_steps = sum(batch.stats(k).particle_steps for k in range(len(runs)))
+    identical = all(np.array_equal(run["parts"].download()["x"], seq["x"])
+                    for run, seq in zip(runs, sequential))
+    batch.close()
+    for run in runs:
+        run["parts"].close()
+        run["table"].close()
+    ctx.close()
+    return {"runs": len(runs), "particles": int(total), "substeps_per_interval": 200,
+            "sizes": {f"{a}x{b}": sum(1 for r in runs if r["size"] == (a, b))
+                      for a, b in sizes},
+            "sequential": {"value": seq_steps / (seq_ms / 1e3), "ms": seq_ms,
+                           "launches": 4 * len(runs)},
+            "batched": {"value": bat_steps / batch_s, "ms": batch_s * 1e3,
+                        "graph": True, "schedule": tuning},
+            "speedup_batched_over_sequential": (bat_steps / batch_s) / (seq_steps / (seq_ms / 1e3)),
+            "bitwise_identical": bool(identical), "setup_s": setup_s}
+
+
 def cpu_baseline(particles: int, steps: int = 1):
     """Oracle restatement of the focused push with the plain slab-QLT closure
     (OpenMP, all host threads) on a bounded sample of the headline workload."""
@@ -336,6 +423,8 @@ def main():
     parser.add_argument("--train-samples", type=int, default=2000000)
     parser.add_argument("--train-steps", type=int, default=16000)
     parser.add_argument("--cpu-particles", type=int, default=1 << 16)
+    parser.add_argument("--batch-runs", type=int, default=64,
+                        help="independent runs of the batched leg (0 skips it)")
     parser.add_argument("--sort-tile", type=int, default=16,
                         help="cell-sort tile (cells) before each push; 0 disables")
     args = parser.parse_args()
@@ -369,6 +458,7 @@ def main():
     f0, f1 = make_workload()
     focused = run_focused(args, f0, f1)
     parker = run_parker(args, f0, f1) if args.parker_particles > 0 else None
+    batched = run_batched(args) if args.batch_runs > 0 else None
     peak, peak_kind = read_peaks()
     head, f64, mixed_qlt = focused["surrogate"], focused["f64"], focused["mixed_qlt"]
     kernel_s = head["kernel_ms"] / 1e3
@@ -409,6 +499,7 @@ def main():
                 "h2d_bytes_per_step": head["state_bytes"],
                 "d2h_bytes_per_step": head["state_bytes"]},
         "parker": parker,
+        "batched_runs": batched,
         # per timed step: the push, plus 3 cell-sort kernels when sorting
         "gpu_launches": args.steps * (1 + (3 if args.sort_tile > 0 else 0)),
         "clocks": head["clocks"],

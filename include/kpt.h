@@ -508,6 +508,50 @@ int kpt_focus_advance_stochastic_steps(kpt_context* ctx, kpt_focus_solver* solve
                                        kpt_system* system, uint64_t seed, uint32_t first_step,
                                        uint32_t steps, double* dts);
 
+/* ======================================================================
+ * Batched runs (no counterpart in the reference, which runs one simulation
+ * per process): many independent driver runs -- each with its own particle
+ * store, coefficient tables, settings, seed and frame -- pushed by one
+ * persistent launch per interval, the interval loop recorded once into a
+ * CUDA graph and replayed.  Results per run are bitwise those of
+ * kpt_push_interval on that run (same seed and frame), whatever the batch
+ * composition or schedule.  Mixed-precision tables, one transport model per
+ * batch, plain closures.
+ * ====================================================================== */
+typedef struct kpt_batch kpt_batch;
+
+typedef struct kpt_batch_tuning {
+    int32_t sort_tile;      /* cell-sort tile (cells), 0 = no sort */
+    int32_t blocks_per_sm;  /* resident 128-thread blocks per SM, 0 = as many as fit */
+    int32_t sort_every;     /* sort every k intervals */
+    int32_t candidates;     /* schedules timed */
+    float best_ms;          /* time of the chosen schedule over the tuning intervals */
+    float pad;
+} kpt_batch_tuning;
+
+int kpt_batch_create(kpt_context* ctx, kpt_batch** out);
+int kpt_batch_destroy(kpt_batch* batch);
+/* Add a run; its next interval is first_frame.  The store, tables and
+ * settings stay owned by the caller and must outlive the batch. */
+int kpt_batch_add_run(kpt_batch* batch, kpt_particles* particles, const kpt_field* lower,
+                      const kpt_field* upper, const kpt_settings* settings, uint64_t seed,
+                      uint32_t first_frame, int* run_index);
+int kpt_batch_set_schedule(kpt_batch* batch, int sort_tile, int blocks_per_sm, int sort_every);
+int kpt_batch_get_schedule(const kpt_batch* batch, int* sort_tile, int* blocks_per_sm,
+                           int* sort_every);
+/* Push every run through `intervals` consecutive intervals (graph replay when
+ * use_graph != 0 and the context's stream can be captured). */
+int kpt_batch_run(kpt_batch* batch, uint32_t intervals, int use_graph);
+/* Counters of a run's last interval. */
+int kpt_batch_stats(const kpt_batch* batch, int run, kpt_push_stats* out);
+/* A run's next interval (get / set). */
+int kpt_batch_frame(const kpt_batch* batch, int run, uint32_t* frame);
+int kpt_batch_set_frame(kpt_batch* batch, int run, uint32_t frame);
+/* Time the candidate schedules (cell-sort tile 0/8/16/32, sort every 1 or 2
+ * intervals, 2 / 3 / all-resident blocks per SM) over `intervals` intervals
+ * on the current state, restore the state, keep the fastest schedule. */
+int kpt_batch_autotune(kpt_batch* batch, uint32_t intervals, kpt_batch_tuning* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -103,6 +103,13 @@ class ScatteringParameters(ctypes.Structure):
         "minimum_correlation_length", "minimum_speed")]
 
 
+class BatchTuning(ctypes.Structure):
+    """kpt_batch_tuning: the schedule the autotuner chose."""
+    _fields_ = [("sort_tile", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
+                ("sort_every", ctypes.c_int32), ("candidates", ctypes.c_int32),
+                ("best_ms", ctypes.c_float), ("pad", ctypes.c_float)]
+
+
 class SplitPolicy(ctypes.Structure):
     """kpt_split_policy (reference ParticleSplittingPolicy)."""
     _fields_ = [("energy_split_ratio", ctypes.c_double),
@@ -213,6 +220,16 @@ def load_library() -> ctypes.CDLL:
         "kpt_parker_advance_stochastic": (i32, [vp, vp, vp, u64, u32, vp]),
         "kpt_parker_advance_deterministic": (i32, [vp, vp, vp, vp]),
         "kpt_parker_advance_stochastic_steps": (i32, [vp, vp, vp, u64, u32, u32, vp]),
+        "kpt_batch_create": (i32, [vp, pvp]),
+        "kpt_batch_destroy": (i32, [vp]),
+        "kpt_batch_add_run": (i32, [vp, vp, vp, vp, vp, u64, u32, vp]),
+        "kpt_batch_set_schedule": (i32, [vp, i32, i32, i32]),
+        "kpt_batch_get_schedule": (i32, [vp, vp, vp, vp]),
+        "kpt_batch_run": (i32, [vp, u32, i32]),
+        "kpt_batch_stats": (i32, [vp, i32, vp]),
+        "kpt_batch_frame": (i32, [vp, i32, vp]),
+        "kpt_batch_set_frame": (i32, [vp, i32, u32]),
+        "kpt_batch_autotune": (i32, [vp, u32, vp]),
         "kpt_focus_solver_create": (i32, [vp, vp, vp, i32, dbl, vp, pvp]),
         "kpt_focus_solver_destroy": (i32, [vp]),
         "kpt_focus_solver_set_basis": (i32, [vp, vp, i32]),
@@ -457,6 +474,11 @@ class Context:
                                                  int(constant_ratio), float(courant),
                                                  ctypes.byref(handle)))
         return self._adopt(ParkerSolver(self, handle))
+
+    def batch(self) -> "Batch":
+        handle = ctypes.c_void_p()
+        _check(self.lib.kpt_batch_create(self.handle, ctypes.byref(handle)))
+        return self._adopt(Batch(self, handle))
 
     def focus_solver(self, grid: "LibGrid", basis: np.ndarray, constant_ratio: bool = False,
                      courant: float = 0.3, spectral_index: float = 5.0 / 3.0, h0: float = 1e-6,
@@ -706,6 +728,56 @@ class ParkerSolver(_Handle):
             self.ctx.handle, self.handle, system.handle, int(seed), int(first_step), int(steps),
             _ptr(dts)))
         return dts[:steps]
+
+
+class Batch(_Handle):
+    """Many independent runs pushed by one launch per interval (kpt_batch)."""
+    _destroy = "kpt_batch_destroy"
+
+    def __init__(self, ctx, handle):
+        super().__init__(ctx, handle)
+        self._keep = []
+
+    def add_run(self, parts: "ParticleStorage", lower: "Field", upper: "Field",
+                settings: Settings, seed: int, first_frame: int) -> int:
+        idx = ctypes.c_int()
+        _check(self.ctx.lib.kpt_batch_add_run(self.handle, parts.handle, lower.handle,
+                                              upper.handle, ctypes.byref(settings), int(seed),
+                                              int(first_frame), ctypes.byref(idx)))
+        self._keep.append((parts, lower, upper, settings))
+        return int(idx.value)
+
+    def set_schedule(self, sort_tile: int = 16, blocks_per_sm: int = 0,
+                     sort_every: int = 1) -> None:
+        _check(self.ctx.lib.kpt_batch_set_schedule(self.handle, int(sort_tile),
+                                                   int(blocks_per_sm), int(sort_every)))
+
+    def schedule(self):
+        t, b, e = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _check(self.ctx.lib.kpt_batch_get_schedule(self.handle, ctypes.byref(t), ctypes.byref(b),
+                                                   ctypes.byref(e)))
+        return {"sort_tile": t.value, "blocks_per_sm": b.value, "sort_every": e.value}
+
+    def run(self, intervals: int, use_graph: bool = True) -> None:
+        _check(self.ctx.lib.kpt_batch_run(self.handle, int(intervals), int(use_graph)))
+
+    def stats(self, run: int) -> PushStats:
+        st = PushStats()
+        _check(self.ctx.lib.kpt_batch_stats(self.handle, int(run), ctypes.byref(st)))
+        return st
+
+    def frame(self, run: int) -> int:
+        f = ctypes.c_uint32()
+        _check(self.ctx.lib.kpt_batch_frame(self.handle, int(run), ctypes.byref(f)))
+        return int(f.value)
+
+    def set_frame(self, run: int, frame: int) -> None:
+        _check(self.ctx.lib.kpt_batch_set_frame(self.handle, int(run), int(frame)))
+
+    def autotune(self, intervals: int = 1) -> Dict[str, float]:
+        t = BatchTuning()
+        _check(self.ctx.lib.kpt_batch_autotune(self.handle, int(intervals), ctypes.byref(t)))
+        return {name: getattr(t, name) for name, _ in BatchTuning._fields_ if name != "pad"}
 
 
 class FocusSolver(_Handle):

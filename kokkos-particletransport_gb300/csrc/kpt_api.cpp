@@ -885,6 +885,50 @@ int kpt_inject_uniform(kpt_context* ctx, kpt_particles* parts, const kpt_field* 
     return KPT_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// The push launch of one interval of one particle store (shared by
+// kpt_push_interval and the batched runs).
+void fill_push_launch(const kpt_context* ctx, const kpt_particles* parts, const kpt_field* lower,
+                      const kpt_field* upper, const kpt_settings* settings, uint32_t frame,
+                      uint64_t seed, kpt::PushCounters* counters, kpt::PushLaunch& launch) {
+    launch = kpt::PushLaunch{};
+    launch.grid = lower->grid;
+    launch.lower = lower->table;
+    launch.upper = upper->table;
+    launch.parts = parts->arrays;
+    launch.count = parts->count;
+    launch.settings = device_settings(settings, lower->grid);
+    launch.interval_start = static_cast<double>(frame) * settings->mhd_dt;
+    launch.interval_end = launch.interval_start + settings->mhd_dt;
+    launch.frame = frame;
+    launch.seed = seed;
+    launch.counters = counters;
+    launch.fixed.axis[0] = lower->fixed[0];
+    launch.fixed.axis[1] = lower->fixed[1];
+    launch.fixed.dt_min = static_cast<float>(launch.settings.dt_min);
+    launch.fixed.dt_max = static_cast<float>(launch.settings.dt_max);
+    launch.fixed.tau_per_time = static_cast<float>(4611686018427387904.0 / settings->mhd_dt);
+    launch.fixed.time_per_tau_2_32 = static_cast<float>(settings->mhd_dt / 1073741824.0);
+    const double pfloor = 0.25 * settings->p0;
+    launch.fixed.pfloor_hi = static_cast<float>(pfloor);
+    launch.fixed.pfloor_lo =
+        static_cast<float>(pfloor - static_cast<double>(launch.fixed.pfloor_hi));
+    launch.order = parts->order_valid ? parts->order.as<uint32_t>() : nullptr;
+    launch.precision = lower->precision;
+    launch.focused = settings->focused != 0;
+    launch.schedule = ctx->push_schedule;
+    launch.sm_count = ctx->sm_count;
+    launch.blocks_per_sm = ctx->push_blocks_per_sm;
+    launch.surrogate = nullptr;
+}
+
+}  // namespace
+
+extern "C" {
+
 int kpt_push_interval(kpt_context* ctx, kpt_particles* parts, const kpt_field* lower,
                       const kpt_field* upper, const kpt_settings* settings, uint32_t frame,
                       uint64_t seed, kpt_push_stats* stats) {
@@ -897,32 +941,8 @@ int kpt_push_interval(kpt_context* ctx, kpt_particles* parts, const kpt_field* l
                 "kpt_push_interval: table kind does not match settings.focused");
     if (int rc = activate(ctx)) return rc;
     kpt::PushLaunch launch{};
-    launch.grid = lower->grid;
-    launch.lower = lower->table;
-    launch.upper = upper->table;
-    launch.parts = parts->arrays;
-    launch.count = parts->count;
-    launch.settings = device_settings(settings, lower->grid);
-    launch.interval_start = static_cast<double>(frame) * settings->mhd_dt;
-    launch.interval_end = launch.interval_start + settings->mhd_dt;
-    launch.frame = frame;
-    launch.seed = seed;
-    launch.counters = ctx->counters.as<kpt::PushCounters>();
-    launch.fixed.axis[0] = lower->fixed[0];
-    launch.fixed.axis[1] = lower->fixed[1];
-    launch.fixed.dt_min = static_cast<float>(launch.settings.dt_min);
-    launch.fixed.dt_max = static_cast<float>(launch.settings.dt_max);
-    launch.fixed.tau_per_time = static_cast<float>(4611686018427387904.0 / settings->mhd_dt);
-    launch.fixed.time_per_tau_2_32 = static_cast<float>(settings->mhd_dt / 1073741824.0);
-    const double pfloor = 0.25 * settings->p0;
-    launch.fixed.pfloor_hi = static_cast<float>(pfloor);
-    launch.fixed.pfloor_lo = static_cast<float>(pfloor - static_cast<double>(launch.fixed.pfloor_hi));
-    launch.order = parts->order_valid ? parts->order.as<uint32_t>() : nullptr;
-    launch.precision = lower->precision;
-    launch.focused = settings->focused != 0;
-    launch.schedule = ctx->push_schedule;
-    launch.sm_count = ctx->sm_count;
-    launch.blocks_per_sm = ctx->push_blocks_per_sm;
+    fill_push_launch(ctx, parts, lower, upper, settings, frame, seed,
+                     ctx->counters.as<kpt::PushCounters>(), launch);
     launch.surrogate = nullptr;
     kpt::SurrogateDevice served{};
     if (settings->closure == KPT_CLOSURE_SURROGATE) {
@@ -2441,6 +2461,361 @@ int kpt_focus_advance_stochastic_steps(kpt_context* ctx, kpt_focus_solver* s, kp
                                  cudaMemcpyDeviceToHost, ctx->stream));
     }
     return step_finish(ctx, s->scalars.ptr, nullptr, true, true);
+}
+
+}  // extern "C"
+
+// ====================================================================
+// Batched runs: many independent driver runs pushed by one launch
+// ====================================================================
+
+struct kpt_batch {
+    kpt_context* ctx = nullptr;
+    int device = 0;
+    struct Run {
+        kpt_particles* parts;
+        const kpt_field* lower;
+        const kpt_field* upper;
+        kpt_settings settings;
+        uint64_t seed;
+        uint32_t frame;
+    };
+    std::vector<Run> runs;
+    int focused = -1;
+    int sort_tile = 16;
+    int blocks_per_sm = 0;
+    int sort_every = 1;
+    DeviceBuffer params, offsets, cursor, counters, saved;
+    // cached graph of the last interval loop
+    cudaGraphExec_t graph = nullptr;
+    uint32_t graph_key[5] = {0, 0, 0, 0, 0};
+};
+
+namespace {
+
+int batch_prepare(kpt_batch* b) {
+    kpt_context* ctx = b->ctx;
+    const size_t runs = b->runs.size();
+    const size_t psize = kpt::push_params_size();
+    KPT_CUDA(b->params.reserve(runs * psize));
+    KPT_CUDA(b->offsets.reserve((runs + 1) * sizeof(uint64_t)));
+    KPT_CUDA(b->cursor.reserve(sizeof(unsigned long long)));
+    KPT_CUDA(b->counters.reserve(runs * sizeof(kpt::PushCounters)));
+    std::vector<char> host(runs * psize);
+    std::vector<uint64_t> offsets(runs + 1, 0);
+    for (size_t r = 0; r < runs; ++r) {
+        kpt_batch::Run& run = b->runs[r];
+        kpt_particles* parts = run.parts;
+        if (b->sort_tile > 0) {
+            // reserve the sort buffers outside any capture
+            const int tx = (run.lower->nx + b->sort_tile - 1) / b->sort_tile;
+            const int ty = (run.lower->ny + b->sort_tile - 1) / b->sort_tile;
+            const uint64_t n = std::max<uint64_t>(parts->count, 1);
+            KPT_CUDA(parts->order.reserve(n * sizeof(uint32_t)));
+            KPT_CUDA(parts->keys.reserve(n * sizeof(uint32_t)));
+            KPT_CUDA(parts->tile_counts.reserve((static_cast<size_t>(tx) * ty + 1) *
+                                                sizeof(uint32_t)));
+            parts->order_valid = true;
+        } else {
+            parts->order_valid = false;
+        }
+        kpt::PushLaunch launch;
+        fill_push_launch(ctx, parts, run.lower, run.upper, &run.settings, run.frame, run.seed,
+                         b->counters.as<kpt::PushCounters>() + r, launch);
+        kpt::build_push_params(launch, host.data() + r * psize);
+        offsets[r + 1] = offsets[r] + parts->count;
+    }
+    KPT_CUDA(cudaMemcpyAsync(b->params.ptr, host.data(), host.size(), cudaMemcpyHostToDevice,
+                             ctx->stream));
+    KPT_CUDA(cudaMemcpyAsync(b->offsets.ptr, offsets.data(), offsets.size() * sizeof(uint64_t),
+                             cudaMemcpyHostToDevice, ctx->stream));
+    KPT_CUDA(cudaStreamSynchronize(ctx->stream));
+    return KPT_OK;
+}
+
+kpt::BatchLaunch batch_launch(const kpt_batch* b) {
+    kpt::BatchLaunch B{};
+    B.params = b->params.ptr;
+    B.offsets = b->offsets.as<uint64_t>();
+    B.runs = static_cast<int>(b->runs.size());
+    B.focused = b->focused;
+    B.cursor = b->cursor.as<unsigned long long>();
+    B.sm_count = b->ctx->sm_count;
+    B.blocks_per_sm = b->blocks_per_sm;
+    return B;
+}
+
+cudaError_t batch_sort_all(const kpt_batch* b, cudaStream_t stream) {
+    for (const kpt_batch::Run& run : b->runs) {
+        kpt_particles* parts = run.parts;
+        if (parts->count == 0) continue;
+        kpt::SortLaunch s{};
+        s.grid = run.lower->grid;
+        s.parts = parts->arrays;
+        s.count = parts->count;
+        s.tile_x = b->sort_tile;
+        s.tile_y = b->sort_tile;
+        s.tiles_x = (run.lower->nx + b->sort_tile - 1) / b->sort_tile;
+        s.tiles_y = (run.lower->ny + b->sort_tile - 1) / b->sort_tile;
+        s.keys = parts->keys.as<unsigned int>();
+        s.counts = parts->tile_counts.as<unsigned int>();
+        s.order = parts->order.as<unsigned int>();
+        const cudaError_t err = kpt::launch_sort(s, stream);
+        if (err != cudaSuccess) return err;
+    }
+    return cudaSuccess;
+}
+
+// intervals x (cell sort every sort_every intervals, batched push, next frame)
+cudaError_t batch_enqueue(const kpt_batch* b, uint32_t intervals, cudaStream_t stream) {
+    const kpt::BatchLaunch B = batch_launch(b);
+    for (uint32_t k = 0; k < intervals; ++k) {
+        if (b->sort_tile > 0 && (k % static_cast<uint32_t>(b->sort_every)) == 0) {
+            cudaError_t err = batch_sort_all(b, stream);
+            if (err != cudaSuccess) return err;
+        }
+        cudaError_t err = kpt::launch_push_batch(B, stream);
+        if (err != cudaSuccess) return err;
+        err = kpt::launch_batch_next_frame(B, stream);
+        if (err != cudaSuccess) return err;
+    }
+    return cudaSuccess;
+}
+
+void batch_drop_graph(kpt_batch* b) {
+    if (b->graph != nullptr) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int kpt_batch_create(kpt_context* ctx, kpt_batch** out) {
+    KPT_REQUIRE(ctx && out, "kpt_batch_create: NULL argument");
+    *out = nullptr;
+    std::unique_ptr<kpt_batch> b(new kpt_batch());
+    b->ctx = ctx;
+    b->device = ctx->device;
+    *out = b.release();
+    return KPT_OK;
+}
+
+int kpt_batch_destroy(kpt_batch* b) {
+    if (b == nullptr) return KPT_OK;
+    cudaSetDevice(b->device);
+    batch_drop_graph(b);
+    for (DeviceBuffer* d : {&b->params, &b->offsets, &b->cursor, &b->counters, &b->saved}) {
+        d->release();
+    }
+    delete b;
+    return KPT_OK;
+}
+
+int kpt_batch_add_run(kpt_batch* b, kpt_particles* parts, const kpt_field* lower,
+                      const kpt_field* upper, const kpt_settings* settings, uint64_t seed,
+                      uint32_t first_frame, int* run_index) {
+    KPT_REQUIRE(b && parts && lower && upper, "kpt_batch_add_run: NULL handle");
+    if (int rc = validate_settings(settings)) return rc;
+    KPT_REQUIRE(static_cast<int>(b->runs.size()) < kpt::batch_max_runs(),
+                "kpt_batch_add_run: too many runs in one batch");
+    KPT_REQUIRE(lower->precision == KPT_PRECISION_MIXED && upper->precision == KPT_PRECISION_MIXED,
+                "kpt_batch_add_run: batched runs use mixed-precision tables");
+    KPT_REQUIRE(lower->kind == upper->kind && lower->nx == upper->nx && lower->ny == upper->ny,
+                "kpt_batch_add_run: lower and upper tables differ in kind or shape");
+    KPT_REQUIRE((lower->kind == KPT_TABLE_FOCUSED21) == (settings->focused != 0),
+                "kpt_batch_add_run: table kind does not match settings.focused");
+    KPT_REQUIRE(settings->closure != KPT_CLOSURE_SURROGATE,
+                "kpt_batch_add_run: the learned closure is not batched");
+    KPT_REQUIRE(b->focused < 0 || b->focused == (settings->focused != 0 ? 1 : 0),
+                "kpt_batch_add_run: all runs of a batch share the transport model");
+    for (const kpt_batch::Run& run : b->runs) {
+        KPT_REQUIRE(run.parts != parts, "kpt_batch_add_run: a particle store is in the batch twice");
+    }
+    b->focused = settings->focused != 0 ? 1 : 0;
+    b->runs.push_back(kpt_batch::Run{parts, lower, upper, *settings, seed, first_frame});
+    batch_drop_graph(b);
+    if (run_index) *run_index = static_cast<int>(b->runs.size()) - 1;
+    return KPT_OK;
+}
+
+int kpt_batch_set_schedule(kpt_batch* b, int sort_tile, int blocks_per_sm, int sort_every) {
+    KPT_REQUIRE(b != nullptr, "kpt_batch_set_schedule: NULL handle");
+    KPT_REQUIRE(sort_tile >= 0 && blocks_per_sm >= 0 && sort_every >= 1,
+                "kpt_batch_set_schedule: sort_tile >= 0, blocks_per_sm >= 0, sort_every >= 1");
+    b->sort_tile = sort_tile;
+    b->blocks_per_sm = blocks_per_sm;
+    b->sort_every = sort_every;
+    batch_drop_graph(b);
+    return KPT_OK;
+}
+
+int kpt_batch_get_schedule(const kpt_batch* b, int* sort_tile, int* blocks_per_sm,
+                           int* sort_every) {
+    KPT_REQUIRE(b != nullptr, "kpt_batch_get_schedule: NULL handle");
+    if (sort_tile) *sort_tile = b->sort_tile;
+    if (blocks_per_sm) *blocks_per_sm = b->blocks_per_sm;
+    if (sort_every) *sort_every = b->sort_every;
+    return KPT_OK;
+}
+
+int kpt_batch_run(kpt_batch* b, uint32_t intervals, int use_graph) {
+    KPT_REQUIRE(b != nullptr, "kpt_batch_run: NULL handle");
+    KPT_REQUIRE(!b->runs.empty(), "kpt_batch_run: no runs");
+    if (intervals == 0) return KPT_OK;
+    kpt_context* ctx = b->ctx;
+    if (int rc = activate(ctx)) return rc;
+    if (int rc = batch_prepare(b)) return rc;
+    cudaStream_t st = ctx->stream;
+    const uint32_t key[5] = {intervals, static_cast<uint32_t>(b->sort_tile),
+                             static_cast<uint32_t>(b->blocks_per_sm),
+                             static_cast<uint32_t>(b->sort_every),
+                             static_cast<uint32_t>(b->runs.size())};
+    if (use_graph && st != nullptr) {
+        if (b->graph == nullptr || std::memcmp(key, b->graph_key, sizeof(key)) != 0) {
+            batch_drop_graph(b);
+            cudaGraph_t graph = nullptr;
+            KPT_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            const cudaError_t err = batch_enqueue(b, intervals, st);
+            const cudaError_t end = cudaStreamEndCapture(st, &graph);
+            KPT_CUDA(err);
+            KPT_CUDA(end);
+            const cudaError_t inst = cudaGraphInstantiate(&b->graph, graph, 0);
+            cudaGraphDestroy(graph);
+            KPT_CUDA(inst);
+            std::memcpy(b->graph_key, key, sizeof(key));
+        }
+        KPT_CUDA(cudaGraphLaunch(b->graph, st));
+    } else {
+        KPT_CUDA(batch_enqueue(b, intervals, st));
+    }
+    KPT_CUDA(cudaStreamSynchronize(st));
+    for (kpt_batch::Run& run : b->runs) run.frame += intervals;
+    return KPT_OK;
+}
+
+int kpt_batch_stats(const kpt_batch* b, int run, kpt_push_stats* out) {
+    KPT_REQUIRE(b && out, "kpt_batch_stats: NULL argument");
+    KPT_REQUIRE(run >= 0 && run < static_cast<int>(b->runs.size()),
+                "kpt_batch_stats: run index out of range");
+    KPT_REQUIRE(b->counters.ptr != nullptr, "kpt_batch_stats: the batch has not run");
+    KPT_CUDA(cudaSetDevice(b->device));
+    kpt::PushCounters host{};
+    KPT_CUDA(cudaMemcpy(&host, b->counters.as<kpt::PushCounters>() + run, sizeof(host),
+                        cudaMemcpyDeviceToHost));
+    out->particle_steps = host.particle_steps;
+    out->pushed = host.pushed;
+    out->failed = host.failed;
+    out->max_steps = host.max_steps;
+    out->pad = 0;
+    return KPT_OK;
+}
+
+int kpt_batch_frame(const kpt_batch* b, int run, uint32_t* frame) {
+    KPT_REQUIRE(b && frame, "kpt_batch_frame: NULL argument");
+    KPT_REQUIRE(run >= 0 && run < static_cast<int>(b->runs.size()),
+                "kpt_batch_frame: run index out of range");
+    *frame = b->runs[static_cast<size_t>(run)].frame;
+    return KPT_OK;
+}
+
+int kpt_batch_set_frame(kpt_batch* b, int run, uint32_t frame) {
+    KPT_REQUIRE(b != nullptr, "kpt_batch_set_frame: NULL handle");
+    KPT_REQUIRE(run >= 0 && run < static_cast<int>(b->runs.size()),
+                "kpt_batch_set_frame: run index out of range");
+    b->runs[static_cast<size_t>(run)].frame = frame;
+    return KPT_OK;
+}
+
+int kpt_batch_autotune(kpt_batch* b, uint32_t intervals, kpt_batch_tuning* out) {
+    KPT_REQUIRE(b != nullptr, "kpt_batch_autotune: NULL handle");
+    KPT_REQUIRE(!b->runs.empty(), "kpt_batch_autotune: no runs");
+    kpt_context* ctx = b->ctx;
+    if (int rc = activate(ctx)) return rc;
+    cudaStream_t st = ctx->stream;
+    intervals = intervals == 0 ? 1 : intervals;
+    // save the pushed state of every run (x, y, p, t, step_dt, mu, status)
+    size_t bytes = 0;
+    for (const kpt_batch::Run& run : b->runs) bytes += run.parts->count * (6 * 8 + 4);
+    KPT_CUDA(b->saved.reserve(std::max<size_t>(bytes, 8)));
+    auto copy_state = [&](bool save) -> int {
+        char* cur = static_cast<char*>(b->saved.ptr);
+        for (const kpt_batch::Run& run : b->runs) {
+            const kpt::ParticleArrays& a = run.parts->arrays;
+            const size_t n = run.parts->count;
+            void* arrays[7] = {a.x, a.y, a.p, a.t, a.step_dt, a.mu, a.status};
+            for (int k = 0; k < 7; ++k) {
+                const size_t sz = n * (k < 6 ? 8 : 4);
+                if (sz == 0) continue;
+                if (save) {
+                    KPT_CUDA(cudaMemcpyAsync(cur, arrays[k], sz, cudaMemcpyDeviceToDevice, st));
+                } else {
+                    KPT_CUDA(cudaMemcpyAsync(arrays[k], cur, sz, cudaMemcpyDeviceToDevice, st));
+                }
+                cur += sz;
+            }
+        }
+        return KPT_OK;
+    };
+    if (int rc = copy_state(true)) return rc;
+    const int tiles[4] = {0, 8, 16, 32};
+    const int every[2] = {1, 2};
+    const int bps[3] = {0, 3, 2};  // 0 = as many as fit
+    const std::vector<uint32_t> frames = [&] {
+        std::vector<uint32_t> f;
+        for (const kpt_batch::Run& run : b->runs) f.push_back(run.frame);
+        return f;
+    }();
+    cudaEvent_t e0, e1;
+    KPT_CUDA(cudaEventCreate(&e0));
+    KPT_CUDA(cudaEventCreate(&e1));
+    float best_ms = 0.0f;
+    int best_tile = b->sort_tile, best_bps = b->blocks_per_sm, best_every = b->sort_every;
+    int tried = 0;
+    for (int tile : tiles) {
+        for (int ev : every) {
+            if (tile == 0 && ev != 1) continue;
+            for (int bp : bps) {
+                b->sort_tile = tile;
+                b->sort_every = ev;
+                b->blocks_per_sm = bp;
+                batch_drop_graph(b);
+                if (int rc = batch_prepare(b)) return rc;
+                KPT_CUDA(cudaEventRecord(e0, st));
+                KPT_CUDA(batch_enqueue(b, intervals, st));
+                KPT_CUDA(cudaEventRecord(e1, st));
+                KPT_CUDA(cudaEventSynchronize(e1));
+                float ms = 0.0f;
+                KPT_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                if (int rc = copy_state(false)) return rc;
+                if (tried == 0 || ms < best_ms) {
+                    best_ms = ms;
+                    best_tile = tile;
+                    best_bps = bp;
+                    best_every = ev;
+                }
+                ++tried;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    KPT_CUDA(cudaStreamSynchronize(st));
+    for (size_t r = 0; r < b->runs.size(); ++r) b->runs[r].frame = frames[r];
+    b->sort_tile = best_tile;
+    b->blocks_per_sm = best_bps;
+    b->sort_every = best_every;
+    batch_drop_graph(b);
+    if (out) {
+        out->sort_tile = best_tile;
+        out->blocks_per_sm = best_bps;
+        out->sort_every = best_every;
+        out->candidates = tried;
+        out->best_ms = best_ms;
+    }
+    return KPT_OK;
 }
 
 }  // extern "C"

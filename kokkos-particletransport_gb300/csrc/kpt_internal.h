@@ -48,6 +48,25 @@ struct PushLaunch {
 
 cudaError_t launch_push_interval(const PushLaunch& launch, cudaStream_t stream);
 
+// Batched mixed-precision push over many independent runs (one launch).
+// params: device array of per-run parameter blocks (push_params_size()
+// bytes each, built by build_push_params); offsets: runs + 1 prefix sums of
+// the runs' particle counts; cursor: one device word.
+struct BatchLaunch {
+    void* params;
+    const uint64_t* offsets;
+    int runs;
+    int focused;
+    unsigned long long* cursor;
+    int sm_count;
+    int blocks_per_sm;
+};
+size_t push_params_size();
+void build_push_params(const PushLaunch& launch, void* out);
+cudaError_t launch_push_batch(const BatchLaunch& launch, cudaStream_t stream);
+cudaError_t launch_batch_next_frame(const BatchLaunch& launch, cudaStream_t stream);
+int batch_max_runs();
+
 // Coefficient table from cell-centred B and V (3 x ny x nx each, device).
 struct TableLaunch {
     Grid grid;

@@ -26,6 +26,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstring>
 
 #include "kpt_device.cuh"
 #include "kpt_internal.h"
@@ -1158,8 +1159,7 @@ __global__ void __launch_bounds__(128) push_simple_kernel(const PushParams P) {
     flush_counters(P.counters, my_steps, my_pushed, my_failed, my_max);
 }
 
-template <typename State, bool FOCUSED, int SURR = 0>
-cudaError_t launch_push(const PushLaunch& L, cudaStream_t stream) {
+PushParams make_push_params(const PushLaunch& L) {
     PushParams P;
     P.grid = L.grid;
     P.fixed = L.fixed;
@@ -1177,9 +1177,15 @@ cudaError_t launch_push(const PushLaunch& L, cudaStream_t stream) {
     P.frame = L.frame;
     P.key = make_uint2(static_cast<uint32_t>(L.seed), static_cast<uint32_t>(L.seed >> 32));
     P.counters = L.counters;
-    if (SURR) {
+    if (L.surrogate != nullptr) {
         P.sg = *L.surrogate;
     }
+    return P;
+}
+
+template <typename State, bool FOCUSED, int SURR = 0>
+cudaError_t launch_push(const PushLaunch& L, cudaStream_t stream) {
+    const PushParams P = make_push_params(L);
     const int threads = 128;
     const size_t smem = SURR ? kSurrogateSmemBytes : 0;
     if (L.schedule == kScheduleSimple && !SURR) {
@@ -1201,6 +1207,121 @@ cudaError_t launch_push(const PushLaunch& L, cudaStream_t stream) {
             <<<L.sm_count * per_sm, threads, smem, stream>>>(P);
     }
     return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- batches
+// Many independent runs (own fields, settings, particles, seeds and frames)
+// in one persistent launch.  The work cursor walks the concatenation of the
+// runs' particle ranges; a lane finds its run by binary search over the run
+// offsets (kept in shared memory) and reads that run's parameter block from
+// global memory.  Lanes of one warp may belong to different runs.  Each
+// finished particle adds its counters to its run's counters.
+constexpr int kBatchMaxRuns = 1024;
+
+__device__ __forceinline__ int batch_run_of(const uint64_t* offsets, int runs, uint64_t slot) {
+    int lo = 0;
+    int hi = runs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (offsets[mid] <= slot) {
+            lo = mid;
+        } else {
+            hi = mid - 1;
+        }
+    }
+    return lo;
+}
+
+__device__ __forceinline__ void batch_finish(const PushParams& P, const StateMixed& st) {
+    atomicAdd(&P.counters->particle_steps, static_cast<unsigned long long>(st.steps));
+    atomicAdd(&P.counters->pushed, 1ull);
+    if (st.status != 0) atomicAdd(&P.counters->failed, 1ull);
+    atomicMax(&P.counters->max_steps, static_cast<unsigned int>(st.steps));
+}
+
+template <bool FOCUSED>
+__global__ void __launch_bounds__(128, MinBlocks<StateMixed, FOCUSED>::value)
+    push_batch_kernel(const BatchLaunch B) {
+    __shared__ uint64_t offsets[kBatchMaxRuns + 1];
+    for (int k = threadIdx.x; k <= B.runs; k += blockDim.x) offsets[k] = B.offsets[k];
+    __syncthreads();
+    const PushParams* runs = static_cast<const PushParams*>(B.params);
+    const unsigned full = 0xffffffffu;
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned lanes_below = (1u << lane) - 1u;
+    const uint64_t total = offsets[B.runs];
+    StateMixed st;
+    int run = 0;
+    bool have = false;
+    bool exhausted = false;
+    for (;;) {
+        const unsigned idle = __ballot_sync(full, !have);
+        if (idle != 0u && !exhausted) {
+            const unsigned n_idle = __popc(idle);
+            const int leader = __ffs(idle) - 1;
+            unsigned long long base = 0;
+            if (static_cast<int>(lane) == leader) {
+                base = atomicAdd(B.cursor, static_cast<unsigned long long>(n_idle));
+            }
+            base = __shfl_sync(full, base, leader);
+            if (base + n_idle >= total) {
+                exhausted = true;
+            }
+            if (!have) {
+                const uint64_t slot = base + __popc(idle & lanes_below);
+                if (slot < total) {
+                    run = batch_run_of(offsets, B.runs, slot);
+                    const PushParams& P = runs[run];
+                    const uint64_t local = slot - offsets[run];
+                    const uint32_t idx = P.order != nullptr ? __ldg(P.order + local)
+                                                            : static_cast<uint32_t>(local);
+                    if (P.parts.status[idx] == 0) {
+                        load<FOCUSED>(st, P, idx);
+                        have = true;
+                        if (!live(st, P)) {
+                            store<FOCUSED>(st, P);
+                            batch_finish(P, st);
+                            have = false;
+                        }
+                    }
+                }
+            }
+        }
+        if (!__any_sync(full, have)) {
+            if (exhausted) {
+                break;
+            }
+            continue;
+        }
+        if (have && !substep<FOCUSED>(st, runs[run])) {
+            const PushParams& P = runs[run];
+            store<FOCUSED>(st, P);
+            batch_finish(P, st);
+            have = false;
+        }
+    }
+}
+
+// Next interval of every run: frame + 1, interval bounds recomputed as the
+// host computes them (frame x mhd_dt), counters cleared.
+__global__ void batch_next_frame_kernel(void* params, int runs) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= runs) return;
+    PushParams& P = static_cast<PushParams*>(params)[r];
+    P.frame += 1u;
+    P.interval_start = static_cast<double>(P.frame) * P.s.mhd_dt;
+    P.interval_end = P.interval_start + P.s.mhd_dt;
+}
+
+__global__ void batch_clear_counters_kernel(void* params, int runs, unsigned long long* cursor) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r == 0) *cursor = 0ull;
+    if (r >= runs) return;
+    PushCounters* c = static_cast<PushParams*>(params)[r].counters;
+    c->particle_steps = 0;
+    c->pushed = 0;
+    c->failed = 0;
+    c->max_steps = 0;
 }
 
 // Table values at given positions through the FP64 sampling path (driver
@@ -1251,6 +1372,45 @@ cudaError_t launch_sample(const SampleLaunch& L, cudaStream_t stream) {
     }
     return cudaGetLastError();
 }
+
+size_t push_params_size() { return sizeof(PushParams); }
+
+void build_push_params(const PushLaunch& launch, void* out) {
+    const PushParams P = make_push_params(launch);
+    std::memcpy(out, &P, sizeof(P));
+}
+
+cudaError_t launch_push_batch(const BatchLaunch& B, cudaStream_t stream) {
+    if (B.runs <= 0 || B.runs > kBatchMaxRuns) return cudaErrorInvalidValue;
+    cudaError_t err = cudaSuccess;
+    batch_clear_counters_kernel<<<(B.runs + 127) / 128, 128, 0, stream>>>(B.params, B.runs,
+                                                                          B.cursor);
+    int resident = 0;
+    if (B.focused) {
+        err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, push_batch_kernel<true>,
+                                                            128, 0);
+    } else {
+        err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, push_batch_kernel<false>,
+                                                            128, 0);
+    }
+    if (err != cudaSuccess) return err;
+    resident = resident < 1 ? 1 : resident;
+    const int per_sm = B.blocks_per_sm > 0 && B.blocks_per_sm < resident ? B.blocks_per_sm
+                                                                        : resident;
+    if (B.focused) {
+        push_batch_kernel<true><<<B.sm_count * per_sm, 128, 0, stream>>>(B);
+    } else {
+        push_batch_kernel<false><<<B.sm_count * per_sm, 128, 0, stream>>>(B);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_next_frame(const BatchLaunch& B, cudaStream_t stream) {
+    batch_next_frame_kernel<<<(B.runs + 127) / 128, 128, 0, stream>>>(B.params, B.runs);
+    return cudaGetLastError();
+}
+
+int batch_max_runs() { return kBatchMaxRuns; }
 
 cudaError_t launch_push_interval(const PushLaunch& launch, cudaStream_t stream) {
     if (launch.precision == kPrecisionF64) {
