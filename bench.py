@@ -44,6 +44,9 @@ sys.path.insert(0, ROOT)
 fields = importlib.import_module("kokkos-particletransport_gb300.fields")
 
 NX, NY = 1024, 2048
+# one process per GPU under torchrun: replicas of the same workload (weak scaling)
+DEVICE = int(os.environ.get("LOCAL_RANK", "0"))
+WORLD = int(os.environ.get("WORLD_SIZE", "1"))
 SEED = 114514
 START_FRAME = 100
 METRIC = "particle-steps/s, 1 GB300: mixed+surrogate vs plain FP64 at <=1% spectrum error"
@@ -140,6 +143,7 @@ def _timed_intervals(ctx, stream, parts, lower, upper, settings, steps, warmup, 
     begin = torch.cuda.Event(enable_timing=True)
     end = torch.cuda.Event(enable_timing=True)
     kernel_ms, particle_steps = [], 0
+    _barrier()
     with ClockSampler() as clocks:
         begin.record(stream)
         for _ in range(steps):
@@ -156,7 +160,27 @@ def _timed_intervals(ctx, stream, parts, lower, upper, settings, steps, warmup, 
             kernel_ms.append(e0.elapsed_time(e1))
         end.record(stream)
         end.synchronize()
+    _barrier()
     return begin.elapsed_time(end), kernel_ms, particle_steps, clocks.summary()
+
+
+def _barrier():
+    if WORLD > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.synchronize()
+        dist.barrier()
+
+
+def _reduce(value: float, op: str) -> float:
+    """Whole-job aggregate over the ranks (max of times, sum of work)."""
+    if WORLD == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device=f"cuda:{DEVICE}")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
+    return float(t.item())
 
 
 def _spectrum(p, w, status, nbins=64, pmin=1e-2, pmax=1e1):
@@ -175,7 +199,7 @@ def run_focused(args, f0, f1):
     """Headline: mixed + surrogate; beside it FP64 plain and mixed plain."""
     import torch
     kpt = importlib.import_module("kokkos-particletransport_gb300")
-    ctx = kpt.Context(0)
+    ctx = kpt.Context(DEVICE)
     stream = torch.cuda.current_stream()
     ctx.set_stream(stream.cuda_stream)
     n = args.particles
@@ -195,6 +219,9 @@ def run_focused(args, f0, f1):
             ("surrogate_fp16", kpt.PRECISION_MIXED, learned, args.steps, args.warmup),
             ("mixed_qlt", kpt.PRECISION_MIXED, plain, args.steps, args.warmup),
             ("f64", kpt.PRECISION_F64, plain, args.f64_steps, 1))
+    if WORLD > 1:
+        # replicas: every rank runs the headline leg and the FP64 baseline leg
+        legs = (legs[0], legs[3])
     start = None
     for label, precision, settings, steps, warmup in legs:
         if label in nets:
@@ -242,7 +269,9 @@ def run_focused(args, f0, f1):
             obj.close()
     ref = spectra["f64"]
     for label in ("surrogate", "surrogate_fp16", "mixed_qlt"):
-        out[label]["spectrum_l1_vs_f64"] = float(np.abs(spectra[label] - ref).sum() / ref.sum())
+        if label in out:
+            out[label]["spectrum_l1_vs_f64"] = float(np.abs(spectra[label] - ref).sum() /
+                                                     ref.sum())
     ctx.set_surrogate(None)
     for net in nets.values():
         net.close()
@@ -255,7 +284,7 @@ def run_parker(args, f0, f1):
     import torch
     kpt = importlib.import_module("kokkos-particletransport_gb300")
     settings = kpt.default_settings(kperp_over_kpara=0.05, split_ratio=1.2)
-    ctx = kpt.Context(0)
+    ctx = kpt.Context(DEVICE)
     stream = torch.cuda.current_stream()
     ctx.set_stream(stream.cuda_stream)
     n = args.parker_particles
@@ -293,7 +322,7 @@ def run_batched(args):
     kpt = importlib.import_module("kokkos-particletransport_gb300")
     rng = np.random.default_rng(SEED)
     sizes = [(128, 128), (256, 512), (512, 1024), (1024, 2048)]
-    ctx = kpt.Context(0)
+    ctx = kpt.Context(DEVICE)
     stream = torch.cuda.current_stream()
     ctx.set_stream(stream.cuda_stream)
     runs = []
@@ -455,17 +484,38 @@ def main():
                         "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
+    if WORLD > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(DEVICE)
+        dist.init_process_group("nccl")
     f0, f1 = make_workload()
     focused = run_focused(args, f0, f1)
-    parker = run_parker(args, f0, f1) if args.parker_particles > 0 else None
-    batched = run_batched(args) if args.batch_runs > 0 else None
+    parker = run_parker(args, f0, f1) if args.parker_particles > 0 and WORLD == 1 else None
+    batched = run_batched(args) if args.batch_runs > 0 and WORLD == 1 else None
     peak, peak_kind = read_peaks()
-    head, f64, mixed_qlt = focused["surrogate"], focused["f64"], focused["mixed_qlt"]
+    head, f64 = focused["surrogate"], focused["f64"]
+    mixed_qlt = focused.get("mixed_qlt")
     kernel_s = head["kernel_ms"] / 1e3
     steps_per_launch = head["particle_steps"] / head["steps"]
     achieved = steps_per_launch * BYTES_PER_STEP["focused_mixed"] / kernel_s / 1e9
     per_step_traffic = profiled_traffic()
-    cpu_value, cpu_threads, cpu_elapsed, cpu_total = cpu_baseline(args.cpu_particles, 1)
+    # whole-job value: all ranks' particle-steps over the slowest rank's time
+    total_ms = _reduce(head["ms_per_step"] * head["steps"], "max")
+    total_steps = _reduce(float(head["particle_steps"]), "sum")
+    head["value"] = total_steps / (total_ms / 1e3)
+    head["ms_per_step"] = total_ms / head["steps"]
+    head["e2e"] = _reduce(head["e2e"], "sum")
+    if WORLD > 1 and rank != 0:
+        return
+    if WORLD == 1:
+        cpu_value, cpu_threads, cpu_elapsed, cpu_total = cpu_baseline(args.cpu_particles, 1)
+        cpu = {"value": cpu_value, "unit": "particle-steps/s", "cores": cpu_threads,
+               "kind": "port",
+               "sample": f"focused plain-QLT oracle, {args.cpu_particles} particles x 1 "
+                         f"interval ({cpu_total} particle-steps, {cpu_elapsed:.1f} s)"}
+    else:
+        cpu = None  # the CPU baseline runs at N = 1 only
     line = {
         "metric": METRIC, "value": head["value"], "unit": "particle-steps/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -474,15 +524,17 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+bf16 network, f64 accumulation",
         "data": "synthetic", "config": config,
         "plain_f64": {"value": f64["value"], "ms_per_step": f64["ms_per_step"],
-                      "steps": f64["steps"],
-                      "speedup_surrogate_over_f64": head["value"] / f64["value"]},
-        "mixed_plain_qlt": {"value": mixed_qlt["value"], "ms_per_step": mixed_qlt["ms_per_step"],
-                            "spectrum_l1_vs_f64": mixed_qlt["spectrum_l1_vs_f64"],
-                            "surrogate_gain": head["value"] / mixed_qlt["value"]},
+                      "steps": f64["steps"], "per_gpu": WORLD > 1,
+                      "speedup_surrogate_over_f64": head["value"] / (f64["value"] * WORLD)},
+        "mixed_plain_qlt": None if mixed_qlt is None else {
+            "value": mixed_qlt["value"], "ms_per_step": mixed_qlt["ms_per_step"],
+            "spectrum_l1_vs_f64": mixed_qlt["spectrum_l1_vs_f64"],
+            "surrogate_gain": head["value"] / mixed_qlt["value"]},
         "spectrum_l1_vs_f64": head["spectrum_l1_vs_f64"],
         "judge": head["judge"],
-        "surrogate_fp16": {k: focused["surrogate_fp16"][k] for k in
-                           ("value", "ms_per_step", "spectrum_l1_vs_f64", "judge")},
+        "surrogate_fp16": None if "surrogate_fp16" not in focused else {
+            k: focused["surrogate_fp16"][k] for k in
+            ("value", "ms_per_step", "spectrum_l1_vs_f64", "judge")},
         "train": focused["train"],
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak,
@@ -491,10 +543,7 @@ def main():
                      "model": "672 B per particle-step (2 frames x 4 corners x 21 f32 gathers)",
                      "peak_kind": peak_kind,
                      "tensor_tflops": steps_per_launch * TENSOR_FLOP_PER_STEP / kernel_s / 1e12},
-        "cpu_baseline": {"value": cpu_value, "unit": "particle-steps/s", "cores": cpu_threads,
-                         "kind": "port",
-                         "sample": f"focused plain-QLT oracle, {args.cpu_particles} particles x 1 "
-                                   f"interval ({cpu_total} particle-steps, {cpu_elapsed:.1f} s)"},
+        "cpu_baseline": cpu,
         "e2e": {"value": head["e2e"], "unit": "particle-steps/s",
                 "h2d_bytes_per_step": head["state_bytes"],
                 "d2h_bytes_per_step": head["state_bytes"]},

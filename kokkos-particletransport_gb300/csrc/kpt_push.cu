@@ -897,12 +897,15 @@ __device__ __forceinline__ bool substep_surrogate(StateMixed& st, const PushPara
         const float y2 = y[2] * box.out_scale[2] + box.out_offset[2];
         const float one_minus_mu2 = 1.0f - mu * mu;
         const float sign = mu > 0.0f ? 1.0f : -1.0f;
+        const float amu = fabsf(mu);
         served.duu = one_minus_mu2 * __expf(y0);
-        served.duu_du = served.duu * (__fdividef(sign * y1, fabsf(mu) + P.kf.qlt_h0) -
+        served.duu_du = served.duu * (__fdividef(sign * y1, amu + P.kf.qlt_h0) -
                                       __fdividef(2.0f * mu, one_minus_mu2));
         served.kpara = __expf(y2);
         ++tally.evaluations;
-        if ((st.steps & (sg.judge_period - 1)) == 0) {
+        const bool blend = amu < 2.0f * box.mu_cut;
+        const bool judge = (st.steps & (sg.judge_period - 1)) == 0;
+        if (blend || judge) {
             const Consts<float>& k = P.kf;
             const float b = c[6];
             const float p = st.p_hi;
@@ -913,11 +916,24 @@ __device__ __forceinline__ bool substep_surrogate(StateMixed& st, const PushPara
             float kpara = k.kpara0;
             if (k.magnetic_dependency == 1) kpara *= Num<float>::pow(b, k.gamma_turb - 2.0f);
             if (k.momentum_dependency == 1) kpara *= Num<float>::pow(__fdividef(p, k.p0), k.pindex);
-            const float e_d = fabsf(served.duu - duu) / duu;
-            const float e_k = fabsf(served.kpara - kpara) / kpara;
-            const float e = fmaxf(e_d, e_k);
-            tally.max_error = isfinite(e) ? fmaxf(tally.max_error, e) : INFINITY;
-            ++tally.judged;
+            if (judge) {
+                const float e_d = fabsf(served.duu - duu) / duu;
+                const float e_k = fabsf(served.kpara - kpara) / kpara;
+                const float e = fmaxf(e_d, e_k);
+                tally.max_error = isfinite(e) ? fmaxf(tally.max_error, e) : INFINITY;
+                ++tally.judged;
+            }
+            if (blend) {
+                // continuous hand-over to the plain closure below mu_cut: a
+                // linear blend over [mu_cut, 2 mu_cut], with the weight's
+                // derivative in dD/dmu so the Ito drift stays consistent
+                const float w = __fdividef(amu - box.mu_cut, box.mu_cut);
+                const float dw = __fdividef(sign, box.mu_cut);
+                const float dd = served.duu - duu;
+                served.duu_du = duu_du + w * (served.duu_du - duu_du) + dw * dd;
+                served.duu = duu + w * dd;
+                served.kpara = kpara + w * (served.kpara - kpara);
+            }
         }
     } else {
         ++tally.fallbacks;

@@ -305,6 +305,11 @@ __global__ void __launch_bounds__(128) eval_kernel(int n, const double* __restri
         const double p = exp(raw[1]);
         const double b = exp(raw[2]);
         double d, dd, lk;
+        const double speed = box.particle_v0 * p / box.p0;
+        const double omega = box.qlt_omega0 * b / sqrt(1.0 + p * p);
+        double pd, pdd, py0, py1;
+        qlt_targets(mu, omega, speed, raw[3], box.qlt_lc, raw[4], box.qlt_h0, pd, pdd, py0, py1);
+        const double plk = log(kappa_parallel(box, p, b));
         if (inside) {
             const double y0 = static_cast<double>(y[0]) * box.out_scale[0] + box.out_offset[0];
             const double y1 = static_cast<double>(y[1]) * box.out_scale[1] + box.out_offset[1];
@@ -313,12 +318,19 @@ __global__ void __launch_bounds__(128) eval_kernel(int n, const double* __restri
             const double sign = mu > 0.0 ? 1.0 : -1.0;
             d = one_minus_mu2 * exp(y0);
             dd = d * (sign * y1 / (fabs(mu) + box.qlt_h0) - 2.0 * mu / one_minus_mu2);
+            const double amu = fabs(mu);
+            if (amu < 2.0 * box.mu_cut) {
+                // the push's hand-over to the plain closure over [mu_cut, 2 mu_cut]
+                const double w = (amu - box.mu_cut) / box.mu_cut;
+                const double dw = sign / box.mu_cut;
+                dd = pdd + w * (dd - pdd) + dw * (d - pd);
+                d = pd + w * (d - pd);
+                lk = log(exp(plk) + w * (exp(lk) - exp(plk)));
+            }
         } else {
-            const double speed = box.particle_v0 * p / box.p0;
-            const double omega = box.qlt_omega0 * b / sqrt(1.0 + p * p);
-            double y0, y1;
-            qlt_targets(mu, omega, speed, raw[3], box.qlt_lc, raw[4], box.qlt_h0, d, dd, y0, y1);
-            lk = log(kappa_parallel(box, p, b));
+            d = pd;
+            dd = pdd;
+            lk = plk;
         }
         out[static_cast<size_t>(i) * kMlpOut + 0] = d;
         out[static_cast<size_t>(i) * kMlpOut + 1] = dd;

@@ -104,10 +104,13 @@ def kappa_parallel(p, b, *, p0, kpara0, gamma_turb, magnetic_dependency=1,
     return k
 
 
-def evaluate(params, norm, inputs, *, p0, qlt_h0):
+def evaluate(params, norm, inputs, *, p0, qlt_h0, particle_v0=None, qlt_omega0=None,
+             qlt_lc=None, kpara0=None, gamma_turb=None):
     """Raw inputs (mu, ln p, ln|B|, sigma^2, gamma_k) -> (D, dD/dmu, ln kappa)
     through the FP64 network with the box normalisation of a trained net
-    (inputs assumed inside the box)."""
+    (inputs assumed inside the box).  With the physics constants given, the
+    served values blend linearly into the plain closure over
+    mu_cut <= |mu| < 2 mu_cut, as the push does."""
     inputs = np.asarray(inputs, dtype=np.float64)
     mu = inputs[:, 0]
     feat = np.stack([np.log(np.abs(mu)), inputs[:, 1], inputs[:, 2], np.log(inputs[:, 3]),
@@ -118,4 +121,19 @@ def evaluate(params, norm, inputs, *, p0, qlt_h0):
     one_minus_mu2 = 1.0 - mu * mu
     d = one_minus_mu2 * np.exp(y[:, 0])
     dd = d * (np.sign(mu) * y[:, 1] / (np.abs(mu) + qlt_h0) - 2.0 * mu / one_minus_mu2)
-    return np.stack([d, dd, y[:, 2]], axis=1)
+    lk = y[:, 2]
+    if particle_v0 is not None:
+        cut = norm["mu_cut"]
+        amu = np.abs(mu)
+        blend = amu < 2.0 * cut
+        p, b = np.exp(inputs[:, 1]), np.exp(inputs[:, 2])
+        pd, pdd, _, _ = qlt_targets(mu, p, b, inputs[:, 3], inputs[:, 4], p0=p0,
+                                    particle_v0=particle_v0, qlt_omega0=qlt_omega0,
+                                    qlt_lc=qlt_lc, qlt_h0=qlt_h0)
+        pk = kappa_parallel(p, b, p0=p0, kpara0=kpara0, gamma_turb=gamma_turb)
+        w = (amu - cut) / cut
+        dw = np.sign(mu) / cut
+        dd = np.where(blend, pdd + w * (dd - pdd) + dw * (d - pd), dd)
+        d = np.where(blend, pd + w * (d - pd), d)
+        lk = np.where(blend, np.log(pk + w * (np.exp(lk) - pk)), lk)
+    return np.stack([d, dd, lk], axis=1)
