@@ -169,6 +169,10 @@ typedef struct kpt_surrogate_config {
     int32_t steps;            /* Adam steps (default 16000) */
     int32_t batch;            /* minibatch (default 8192) */
     int32_t element_type;     /* kpt_surrogate_element of the served network */
+    int32_t quantization_aware; /* 1: the last quarter of the steps trains through the
+                                   served element type's rounding (default 0; measured
+                                   no gain for BF16, whose error is activation rounding) */
+    int32_t pad;
     double learning_rate;     /* initial; cosine decay to 1 % (default 1e-2) */
     double mu_cut;            /* default 0.02 */
     double mu_max;            /* largest |mu| trained (default 0.999) */

@@ -83,7 +83,8 @@ class Summary(ctypes.Structure):
 class SurrogateConfig(ctypes.Structure):
     """kpt_surrogate_config: training set, optimiser and training box."""
     _fields_ = [("samples", ctypes.c_int32), ("steps", ctypes.c_int32),
-                ("batch", ctypes.c_int32), ("element_type", ctypes.c_int32)] + \
+                ("batch", ctypes.c_int32), ("element_type", ctypes.c_int32),
+                ("quantization_aware", ctypes.c_int32), ("pad", ctypes.c_int32)] + \
                [(n, ctypes.c_double) for n in (
                    "learning_rate", "mu_cut", "mu_max", "p_lo_over_p0", "p_hi_over_p0",
                    "sigma2_lo", "sigma2_hi", "gk_lo", "gk_hi", "b_lo", "b_hi")] + \

@@ -1231,6 +1231,7 @@ void kpt_surrogate_default_config(kpt_surrogate_config* c) {
     c->steps = 16000;
     c->batch = 8192;
     c->element_type = KPT_SURROGATE_BF16;
+    c->quantization_aware = 0;
     c->learning_rate = 1e-2;
     c->mu_cut = 0.02;
     c->mu_max = 0.999;
@@ -1355,6 +1356,10 @@ int kpt_surrogate_train(kpt_context* ctx, const kpt_settings* settings,
     L.partial = L.loss + c.steps;
     L.beta1 = 0.9f;
     L.beta2 = 0.999f;
+    // quantization-aware fine-tuning: the last quarter of the steps sees the
+    // served element type's rounding
+    L.quant = c.quantization_aware ? (box.fp16 ? 2 : 1) : 0;
+    L.quant_from = c.steps - c.steps / 4;
     KPT_CUDA(cudaMemcpyAsync(L.params, sg->params.data(), pcount * sizeof(float),
                              cudaMemcpyHostToDevice, st));
     const double pi = 3.141592653589793238462643383279502884;

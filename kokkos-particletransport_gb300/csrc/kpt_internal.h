@@ -178,6 +178,8 @@ struct SurrogateTrainLaunch {
     float* loss;      // one float per step
     float* partial;   // ceil(batch / kGradChunk) x kMlpParams gradient partials
     float beta1, beta2, lr;
+    int quant;        // rounding emulated from step quant_from on: 0 none, 1 BF16, 2 FP16
+    int quant_from;
 };
 constexpr int kGradChunk = 256;
 cudaError_t surrogate_make_samples(uint64_t seed, int n, const SurrogateBox& box, float* x,

@@ -7,6 +7,7 @@
 // (src/main.cpp:1177-1193).  One optimisation step: forward + backward per
 // sample (activations and deltas kept in HBM), batch reductions for the
 // weight gradients, then Adam.
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -91,6 +92,20 @@ __global__ void make_samples_kernel(uint64_t seed, int n, SurrogateBox box, floa
     }
 }
 
+// Rounding of the served network's 16-bit element type (quantization-aware
+// fine-tuning): 0 none, 1 BF16 (round to nearest even), 2 FP16.
+__device__ __forceinline__ float quantize(float v, int q) {
+    if (q == 1) {
+        uint32_t bits = __float_as_uint(v);
+        bits = (bits + 0x7fffu + ((bits >> 16) & 1u)) & 0xffff0000u;
+        return __uint_as_float(bits);
+    }
+    if (q == 2) {
+        return __half2float(__float2half_rn(v));
+    }
+    return v;
+}
+
 __device__ __forceinline__ float normalise_input(const SurrogateBox& box, int k, float v) {
     return v * box.in_scale[k] + box.in_offset[k];
 }
@@ -103,9 +118,17 @@ __global__ void __launch_bounds__(128) fwd_bwd_kernel(const float* __restrict__ 
                                                       SurrogateBox box,
                                                       const float* __restrict__ params,
                                                       float* xb, float* h1, float* h2, float* g1,
-                                                      float* g2, float* gy, float* loss) {
+                                                      float* g2, float* gy, float* loss,
+                                                      int quant) {
+    // quant != 0: the forward sees the served network's rounding (weights,
+    // inputs, pre-activations and activations in the 16-bit type; biases and
+    // accumulation FP32) and the backward passes straight through it
     __shared__ float w[kMlpParams];
-    for (int k = threadIdx.x; k < kMlpParams; k += blockDim.x) w[k] = params[k];
+    for (int k = threadIdx.x; k < kMlpParams; k += blockDim.x) {
+        const bool bias = (k >= kMlpB1 && k < kMlpW2) || (k >= kMlpB2 && k < kMlpW3) ||
+                          k >= kMlpB3;
+        w[k] = bias ? params[k] : quantize(params[k], quant);
+    }
     __syncthreads();
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     float sq = 0.0f;
@@ -119,14 +142,15 @@ __global__ void __launch_bounds__(128) fwd_bwd_kernel(const float* __restrict__ 
         }
         float in[kMlpIn];
         for (int k = 0; k < kMlpIn; ++k) {
-            in[k] = normalise_input(box, k, x[static_cast<size_t>(i) * kMlpIn + k]);
+            in[k] = quantize(normalise_input(box, k, x[static_cast<size_t>(i) * kMlpIn + k]),
+                             quant);
             xb[static_cast<size_t>(b) * kMlpIn + k] = in[k];
         }
         float a1[kMlpHidden];
         for (int j = 0; j < kMlpHidden; ++j) {
             float z = w[kMlpB1 + j];
             for (int k = 0; k < kMlpIn; ++k) z += w[kMlpW1 + j * kMlpIn + k] * in[k];
-            a1[j] = tanhf(z);
+            a1[j] = quantize(tanhf(quantize(z, quant)), quant);
             h1[static_cast<size_t>(b) * kMlpHidden + j] = a1[j];
         }
         float y[kMlpOut];
@@ -134,7 +158,7 @@ __global__ void __launch_bounds__(128) fwd_bwd_kernel(const float* __restrict__ 
         for (int j = 0; j < kMlpHidden; ++j) {
             float z = w[kMlpB2 + j];
             for (int k = 0; k < kMlpHidden; ++k) z += w[kMlpW2 + j * kMlpHidden + k] * a1[k];
-            const float a2 = tanhf(z);
+            const float a2 = quantize(tanhf(quantize(z, quant)), quant);
             h2[static_cast<size_t>(b) * kMlpHidden + j] = a2;
             for (int o = 0; o < kMlpOut; ++o) y[o] += w[kMlpW3 + o * kMlpHidden + j] * a2;
         }
@@ -353,7 +377,7 @@ cudaError_t surrogate_make_samples(uint64_t seed, int n, const SurrogateBox& box
 cudaError_t surrogate_train_step(const SurrogateTrainLaunch& L, int step, cudaStream_t stream) {
     fwd_bwd_kernel<<<(L.batch + 127) / 128, 128, 0, stream>>>(
         L.x, L.t, L.n, L.seed, step, L.batch, L.box, L.params, L.xb, L.h1, L.h2, L.g1, L.g2, L.gy,
-        L.loss + step);
+        L.loss + step, step >= L.quant_from ? L.quant : 0);
     launch_gradients(L, stream);
     const float t1 = static_cast<float>(step + 1);
     const float bias1 = 1.0f - powf(L.beta1, t1);
@@ -366,7 +390,7 @@ cudaError_t surrogate_train_step(const SurrogateTrainLaunch& L, int step, cudaSt
 cudaError_t surrogate_gradient(const SurrogateTrainLaunch& L, cudaStream_t stream) {
     fwd_bwd_kernel<<<(L.batch + 127) / 128, 128, 0, stream>>>(
         L.x, L.t, L.n, L.seed, -1, L.batch, L.box, L.params, L.xb, L.h1, L.h2, L.g1, L.g2, L.gy,
-        L.loss);
+        L.loss, 0);
     return launch_gradients(L, stream);
 }
 
