@@ -222,6 +222,18 @@ int kpt_field_create(kpt_context* ctx, int nx, int ny, const double* x_edges,
 int kpt_field_load(kpt_context* ctx, const char* path, int table_kind, int precision,
                    kpt_field** out);
 int kpt_field_destroy(kpt_field* field);
+/* The reader and the table build of kpt_field_load as two calls, so a host
+ * thread can read frame f+2 from disk while the GPU pushes frame f (the
+ * reference reads each frame between pushes, src/main.cpp:2300-2312).
+ * kpt_field_data_read launches nothing on the device and may run on any host
+ * thread; the cell data lands in page-locked memory (cudaHostAlloc) for a
+ * full-bandwidth upload. */
+typedef struct kpt_field_data kpt_field_data;
+int kpt_field_data_read(const kpt_context* ctx, const char* path, kpt_field_data** out);
+int kpt_field_data_free(kpt_field_data* data);
+int kpt_field_data_shape(const kpt_field_data* data, int* nx, int* ny);
+int kpt_field_create_from_data(kpt_context* ctx, const kpt_field_data* data, int table_kind,
+                               int precision, kpt_field** out);
 /* nx, ny, number of ghosted points and components. */
 int kpt_field_shape(const kpt_field* field, int* nx, int* ny, uint64_t* points,
                     int* components);

@@ -20,6 +20,12 @@
 
 #include "kpt_internal.h"
 
+// One substep in KPT_JUDGE_PERIOD (a power of two) of every particle also
+// evaluates the plain closure to judge the learned one.
+#ifndef KPT_JUDGE_PERIOD
+#define KPT_JUDGE_PERIOD 64
+#endif
+
 namespace {
 
 thread_local std::string g_last_error;
@@ -124,6 +130,12 @@ struct kpt_field {
     int* fixed_buckets[2] = {nullptr, nullptr};
     kpt::Grid grid{};
     kpt::FixedAxis fixed[2]{};
+};
+
+struct kpt_field_data {
+    int nx = 0, ny = 0;
+    std::vector<double> x_edges, y_edges;
+    double* cells = nullptr;  // Bx By Bz Vx Vy Vz (ny x nx each), page-locked
 };
 
 struct kpt_particles {
@@ -492,9 +504,30 @@ int kpt_context_synchronize(kpt_context* ctx) {
     return KPT_OK;
 }
 
+namespace {
+int field_create(kpt_context* ctx, int nx, int ny, const double* x_edges, const double* y_edges,
+                 const double* b_cells, const double* v_cells, int table_kind, int precision,
+                 const double* b_device, const double* v_device, kpt_field** out);
+}  // namespace
+
 int kpt_field_create(kpt_context* ctx, int nx, int ny, const double* x_edges,
                      const double* y_edges, const double* b_cells, const double* v_cells,
                      int table_kind, int precision, kpt_field** out) {
+    return field_create(ctx, nx, ny, x_edges, y_edges, b_cells, v_cells, table_kind, precision,
+                        nullptr, nullptr, out);
+}
+
+}  // extern "C"
+
+namespace {
+
+// b_device / v_device (optional): device addresses of mapped page-locked
+// cells the kernels read in place (NVLink-C2C / PCIe reads), so no staging
+// copy is made; b_cells / v_cells stay the host view used for validation.
+int field_create(kpt_context* ctx, int nx, int ny, const double* x_edges, const double* y_edges,
+                 const double* b_cells, const double* v_cells, int table_kind, int precision,
+                 const double* b_device, const double* v_device, kpt_field** out) {
+    const bool device_readable = b_device != nullptr && v_device != nullptr;
     KPT_REQUIRE(ctx != nullptr && out != nullptr, "kpt_field_create: NULL handle");
     *out = nullptr;
     KPT_REQUIRE(nx > 0 && ny > 0, "AthenaFieldReader: Athena binary dimensions must be positive.");
@@ -504,7 +537,8 @@ int kpt_field_create(kpt_context* ctx, int nx, int ny, const double* x_edges,
     KPT_REQUIRE(precision == KPT_PRECISION_F64 || precision == KPT_PRECISION_MIXED,
                 "kpt_field_create: unknown precision");
     const size_t cells = static_cast<size_t>(nx) * static_cast<size_t>(ny);
-    for (size_t k = 0; k < 3 * cells; ++k) {
+    // data read by kpt_field_data_read was checked on the reading thread
+    for (size_t k = 0; !device_readable && k < 3 * cells; ++k) {
         if (!std::isfinite(b_cells[k]) || !std::isfinite(v_cells[k])) {
             return set_error(KPT_ERROR_FORMAT, "AthenaFieldReader: non-finite field value.");
         }
@@ -559,18 +593,21 @@ int kpt_field_create(kpt_context* ctx, int nx, int ny, const double* x_edges,
     const size_t elem = precision == KPT_PRECISION_F64 ? sizeof(double) : sizeof(float);
     KPT_CUDA(cudaMalloc(&f->table, f->points * f->stride * elem));
     double* staging = nullptr;
-    KPT_CUDA(cudaMalloc(&staging, 6 * cells * sizeof(double)));
-    cudaError_t err = cudaMemcpyAsync(staging, b_cells, 3 * cells * sizeof(double),
-                                      cudaMemcpyHostToDevice, ctx->stream);
-    if (err == cudaSuccess) {
-        err = cudaMemcpyAsync(staging + 3 * cells, v_cells, 3 * cells * sizeof(double),
+    cudaError_t err = cudaSuccess;
+    if (!device_readable) {
+        KPT_CUDA(cudaMalloc(&staging, 6 * cells * sizeof(double)));
+        err = cudaMemcpyAsync(staging, b_cells, 3 * cells * sizeof(double),
                               cudaMemcpyHostToDevice, ctx->stream);
+        if (err == cudaSuccess) {
+            err = cudaMemcpyAsync(staging + 3 * cells, v_cells, 3 * cells * sizeof(double),
+                                  cudaMemcpyHostToDevice, ctx->stream);
+        }
     }
     if (err == cudaSuccess) {
         kpt::TableLaunch launch{};
         launch.grid = f->grid;
-        launch.b_cells = staging;
-        launch.v_cells = staging + 3 * cells;
+        launch.b_cells = device_readable ? b_device : staging;
+        launch.v_cells = device_readable ? v_device : staging + 3 * cells;
         launch.table = f->table;
         launch.focused = table_kind == KPT_TABLE_FOCUSED21;
         launch.precision = precision;
@@ -588,11 +625,18 @@ int kpt_field_create(kpt_context* ctx, int nx, int ny, const double* x_edges,
     return KPT_OK;
 }
 
+}  // namespace
+
+extern "C" {
+
 // Compact field reader: layout and checks of AthenaFieldReader.hpp:290-360
 // (non-uniform edges accepted as an extension).
-int kpt_field_load(kpt_context* ctx, const char* path, int table_kind, int precision,
-                   kpt_field** out) {
-    KPT_REQUIRE(path != nullptr, "kpt_field_load: path is NULL");
+int kpt_field_data_read(const kpt_context* ctx, const char* path, kpt_field_data** out) {
+    KPT_REQUIRE(ctx != nullptr && path != nullptr && out != nullptr,
+                "kpt_field_data_read: NULL argument");
+    *out = nullptr;
+    // the calling thread may be a helper thread: bind it to the context's device
+    KPT_CUDA(cudaSetDevice(ctx->device));
     std::ifstream stream(path, std::ios::binary);
     if (!stream) {
         return set_error(KPT_ERROR_IO, "AthenaFieldReader: failed to open Athena binary file.");
@@ -607,33 +651,80 @@ int kpt_field_load(kpt_context* ctx, const char* path, int table_kind, int preci
         return set_error(KPT_ERROR_FORMAT,
                          "AthenaFieldReader: Athena binary dimensions must be positive.");
     }
+    std::unique_ptr<kpt_field_data, int (*)(kpt_field_data*)> d(new kpt_field_data(),
+                                                                kpt_field_data_free);
+    d->nx = nx;
+    d->ny = ny;
     const size_t cells = static_cast<size_t>(nx) * static_cast<size_t>(ny);
-    std::vector<double> xe(static_cast<size_t>(nx) + 1), ye(static_cast<size_t>(ny) + 1);
-    std::vector<double> b(3 * cells), v(3 * cells);
-    auto read = [&](std::vector<double>& dst, size_t offset, size_t n, const char* name) -> int {
-        stream.read(reinterpret_cast<char*>(dst.data() + offset),
-                    static_cast<std::streamsize>(n * sizeof(double)));
+    d->x_edges.resize(static_cast<size_t>(nx) + 1);
+    d->y_edges.resize(static_cast<size_t>(ny) + 1);
+    // cell data in page-locked memory (portable across devices) so the
+    // upload runs at full host-device bandwidth
+    KPT_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&d->cells), 6 * cells * sizeof(double),
+                           cudaHostAllocPortable | cudaHostAllocMapped));
+    auto read = [&](double* dst, size_t n, const char* name) -> int {
+        stream.read(reinterpret_cast<char*>(dst), static_cast<std::streamsize>(n * sizeof(double)));
         if (!stream) {
             return set_error(KPT_ERROR_FORMAT,
                              std::string("AthenaFieldReader: failed to read ") + name + ".");
         }
         return KPT_OK;
     };
-    if (int rc = read(xe, 0, xe.size(), "x_edges")) return rc;
-    if (int rc = read(ye, 0, ye.size(), "y_edges")) return rc;
+    if (int rc = read(d->x_edges.data(), d->x_edges.size(), "x_edges")) return rc;
+    if (int rc = read(d->y_edges.data(), d->y_edges.size(), "y_edges")) return rc;
     const char* names[6] = {"Bx", "By", "Bz", "Vx", "Vy", "Vz"};
-    for (int c = 0; c < 3; ++c) {
-        if (int rc = read(b, c * cells, cells, names[c])) return rc;
-    }
-    for (int c = 0; c < 3; ++c) {
-        if (int rc = read(v, c * cells, cells, names[3 + c])) return rc;
+    for (int c = 0; c < 6; ++c) {
+        if (int rc = read(d->cells + c * cells, cells, names[c])) return rc;
     }
     if (stream.peek() != std::char_traits<char>::eof()) {
         return set_error(KPT_ERROR_FORMAT,
                          "AthenaFieldReader: Athena binary file has trailing payload.");
     }
-    return kpt_field_create(ctx, nx, ny, xe.data(), ye.data(), b.data(), v.data(), table_kind,
-                            precision, out);
+    for (size_t k = 0; k < 6 * cells; ++k) {
+        if (!std::isfinite(d->cells[k])) {
+            return set_error(KPT_ERROR_FORMAT, "AthenaFieldReader: non-finite field value.");
+        }
+    }
+    *out = d.release();
+    return KPT_OK;
+}
+
+int kpt_field_data_free(kpt_field_data* data) {
+    if (data == nullptr) return KPT_OK;
+    if (data->cells != nullptr) cudaFreeHost(data->cells);
+    delete data;
+    return KPT_OK;
+}
+
+int kpt_field_data_shape(const kpt_field_data* data, int* nx, int* ny) {
+    KPT_REQUIRE(data != nullptr, "kpt_field_data_shape: NULL handle");
+    if (nx) *nx = data->nx;
+    if (ny) *ny = data->ny;
+    return KPT_OK;
+}
+
+int kpt_field_create_from_data(kpt_context* ctx, const kpt_field_data* data, int table_kind,
+                               int precision, kpt_field** out) {
+    KPT_REQUIRE(ctx && data && out, "kpt_field_create_from_data: NULL argument");
+    const size_t cells = static_cast<size_t>(data->nx) * static_cast<size_t>(data->ny);
+    if (int rc = activate(ctx)) return rc;
+    // the device's address of the mapped page-locked cells
+    void* mapped = nullptr;
+    KPT_CUDA(cudaHostGetDevicePointer(&mapped, data->cells, 0));
+    const double* cells_dev = static_cast<const double*>(mapped);
+    return field_create(ctx, data->nx, data->ny, data->x_edges.data(), data->y_edges.data(),
+                        data->cells, data->cells + 3 * cells, table_kind, precision, cells_dev,
+                        cells_dev + 3 * cells, out);
+}
+
+int kpt_field_load(kpt_context* ctx, const char* path, int table_kind, int precision,
+                   kpt_field** out) {
+    KPT_REQUIRE(ctx != nullptr, "kpt_field_load: ctx is NULL");
+    kpt_field_data* data = nullptr;
+    if (int rc = kpt_field_data_read(ctx, path, &data)) return rc;
+    const int rc = kpt_field_create_from_data(ctx, data, table_kind, precision, out);
+    kpt_field_data_free(data);
+    return rc;
 }
 
 int kpt_field_destroy(kpt_field* field) {
@@ -968,7 +1059,7 @@ int kpt_push_interval(kpt_context* ctx, kpt_particles* parts, const kpt_field* l
                                   f4 <= box.in_hi[4];
         served.f3 = static_cast<float>(f3) * box.in_scale[3] + box.in_offset[3];
         served.f4 = static_cast<float>(f4) * box.in_scale[4] + box.in_offset[4];
-        served.judge_period = 16;
+        served.judge_period = KPT_JUDGE_PERIOD;
         served.judge = ctx->judge.as<unsigned long long>();  // zeroed by set_surrogate
         launch.surrogate = &served;
     }

@@ -9,7 +9,7 @@
 // momentum_histogram_NNNNN.csv, v4 particles_NNNNN.bin), same overwrite guard,
 // restart and walltime behaviour, exit code 0, or 1 with "Error: <msg>".
 // Extensions (stated in --help): --precision, --kperp-over-kpara,
-// --inject-y-band, --histogram-bins, --device.
+// --inject-y-band, --histogram-bins, --device, --frame-prefetch.
 #include <algorithm>
 #include <array>
 #include <chrono>
@@ -19,6 +19,7 @@
 #include <cstring>
 #include <filesystem>
 #include <fstream>
+#include <future>
 #include <iomanip>
 #include <iostream>
 #include <limits>
@@ -79,6 +80,7 @@ struct RunSettings {
     double band_lo{0.0};
     double band_hi{0.0};
     int histogram_bins{128};
+    bool prefetch{true};  // read the next frame file while the GPU pushes
     int device{0};
 
     int intervals() const { return end_frame - start_frame; }
@@ -352,6 +354,7 @@ void print_usage() {
         << "  --precision f64|mixed         push arithmetic (default f64)\n"
         << "  --kperp-over-kpara X          perpendicular/parallel diffusion ratio (default 0.01)\n"
         << "  --inject-y-band LO HI         inject y uniformly in [LO, HI) instead of the domain\n"
+        << "  --frame-prefetch on|off       read the next field file during the push (default on)\n"
         << "  --histogram-bins N            momentum histogram bins (default 128)\n"
         << "  --device N                    CUDA device (default 0)\n";
 }
@@ -469,6 +472,12 @@ RunSettings parse(int argc, char** argv) {
             s.histogram_bins = std::stoi(next_value(argc, argv, i, arg));
         } else if (arg == "--device") {
             s.device = std::stoi(next_value(argc, argv, i, arg));
+        } else if (arg == "--frame-prefetch") {
+            const std::string v = next_value(argc, argv, i, arg);
+            if (v != "on" && v != "off") {
+                throw std::runtime_error("--frame-prefetch needs on or off.");
+            }
+            s.prefetch = v == "on";
         } else {
             throw std::runtime_error("Unknown option: " + arg);
         }
@@ -728,6 +737,32 @@ FieldPtr load_frame(kpt_context* ctx, const RunSettings& s, int frame) {
     return FieldPtr(f);
 }
 
+struct FieldDataDeleter {
+    void operator()(kpt_field_data* d) const { kpt_field_data_free(d); }
+};
+using FieldDataPtr = std::unique_ptr<kpt_field_data, FieldDataDeleter>;
+
+// Frame prefetch: the compact file of a later frame is read into page-locked
+// host memory on a second host thread while the GPU pushes the current
+// frame; the table is built from it when the frame is needed.  A read error
+// is reported when that frame is needed, as the serial reader would.
+std::future<FieldDataPtr> prefetch_frame(const kpt_context* ctx, const RunSettings& s,
+                                         int frame) {
+    const std::string path = field_path(s.field_dir, frame);
+    return std::async(std::launch::async, [ctx, path]() {
+        kpt_field_data* d = nullptr;
+        check(kpt_field_data_read(ctx, path.c_str(), &d));
+        return FieldDataPtr(d);
+    });
+}
+
+FieldPtr build_frame(kpt_context* ctx, const RunSettings& s, const FieldDataPtr& data) {
+    kpt_field* f = nullptr;
+    const int kind = s.transport == Transport::Focused ? KPT_TABLE_FOCUSED21 : KPT_TABLE_PARKER16;
+    check(kpt_field_create_from_data(ctx, data.get(), kind, s.precision, &f));
+    return FieldPtr(f);
+}
+
 // run + run_transport_loop (src/main.cpp:2255-2429, 2616-2688).
 int run(const RunSettings& s) {
     require_fresh_output(s);
@@ -806,6 +841,7 @@ int run(const RunSettings& s) {
     const auto run_start = Clock::now();
     bool stopped = false;
     int last_frame = s.start_frame;
+    std::future<FieldDataPtr> next_upper;
     for (int frame = s.start_frame; frame < s.end_frame; ++frame) {
         const auto frame_start = Clock::now();
         FrameTiming timing;
@@ -813,8 +849,12 @@ int run(const RunSettings& s) {
         if (frame > s.start_frame) {
             lower = std::move(upper);
             const auto t0 = Clock::now();
-            upper = load_frame(ctx.get(), s, frame + 1);
-            timing.read_s = seconds_since(t0);
+            upper = s.prefetch ? build_frame(ctx.get(), s, next_upper.get())
+                               : load_frame(ctx.get(), s, frame + 1);
+            timing.read_s = seconds_since(t0);  // the part of the read not hidden by the push
+        }
+        if (s.prefetch && frame + 1 < s.end_frame) {
+            next_upper = prefetch_frame(ctx.get(), s, frame + 2);
         }
         auto t0 = Clock::now();
         check(kpt_inject_uniform(ctx.get(), parts.get(), lower.get(), &physics,

@@ -96,11 +96,13 @@ def _compare_histogram(got_path, want_path, formats):
         assert np.all(np.abs(got[key] - want[key]) <= 1e-14 * want[key]), key
 
 
-def test_cli_run_and_restart_match_reference(tmp_path, field_dir, fields_mod):
+@pytest.mark.parametrize("prefetch", ["on", "off"])
+def test_cli_run_and_restart_match_reference(tmp_path, field_dir, fields_mod, prefetch):
     import importlib
     formats = importlib.import_module("kokkos-particletransport_gb300.formats")
     run_dir = tmp_path / "run"
-    _run(_argv() + ["--field-dir", field_dir, "--output-dir", str(run_dir), "--frames", "2"])
+    _run(_argv() + ["--field-dir", field_dir, "--output-dir", str(run_dir), "--frames", "2",
+                    "--frame-prefetch", prefetch])
     want_dir = os.path.join(CLI, "run")
     names = sorted(os.listdir(want_dir))
     assert sorted(os.listdir(run_dir)) == names
