@@ -301,6 +301,17 @@ int kpt_particles_download(const kpt_particles* particles, uint64_t count, doubl
                            double* y, double* p, double* t, double* step_dt, double* weight,
                            double* mu, int32_t* status, int32_t* split_level);
 int kpt_particles_device_arrays(const kpt_particles* particles, kpt_particle_arrays* out);
+/* The driver's v4 snapshot records of the stored particles, packed on the
+ * GPU (write_reconnection_particle_snapshot's record loop,
+ * src/main.cpp:2155-2201): count x 100 bytes (id = storage index, status,
+ * split level, sort key 0, position written as position, previous and
+ * previous-step position, p, mu, weight, initial_kinetic_energy) copied to
+ * `out` (page-locked memory from kpt_host_alloc copies fastest). */
+int kpt_particles_pack_records(kpt_context* ctx, const kpt_particles* particles,
+                               double initial_kinetic_energy, void* out, uint64_t out_len);
+/* Page-locked host memory (for snapshot buffers and prefetched frames). */
+int kpt_host_alloc(uint64_t bytes, void** out);
+int kpt_host_free(void* ptr);
 
 /* Cell sort of the work order: particle indices are ordered by spatial tile
  * (tile_x x tile_y cells, inactive particles last) and later pushes visit

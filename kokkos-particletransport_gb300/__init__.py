@@ -191,6 +191,7 @@ def load_library() -> ctypes.CDLL:
         "kpt_particles_sort": (i32, [vp, vp, vp, i32, i32]),
         "kpt_particles_clear_order": (i32, [vp]),
         "kpt_particles_wrap": (i32, [vp, u64, u64, vp, pvp]),
+        "kpt_particles_pack_records": (i32, [vp, vp, dbl, vp, u64]),
         "kpt_surrogate_default_config": (None, [vp]),
         "kpt_surrogate_train": (i32, [vp, vp, vp, pvp, vp]),
         "kpt_surrogate_destroy": (i32, [vp]),
@@ -867,6 +868,15 @@ class ParticleStorage:
         out["level"] = np.zeros(n, dtype=np.int32)
         _check(self.ctx.lib.kpt_particles_download(self.handle, n,
                                                    *[_ptr(out[k]) for k in PARTICLE_FIELDS]))
+        return out
+
+    def pack_records(self, initial_kinetic_energy: float) -> np.ndarray:
+        """The driver's v4 snapshot records of the stored particles (packed on the GPU)."""
+        n = self.count
+        out = np.zeros(n * 100, dtype=np.uint8)
+        _check(self.ctx.lib.kpt_particles_pack_records(self.ctx.handle, self.handle,
+                                                       float(initial_kinetic_energy), _ptr(out),
+                                                       out.size))
         return out
 
     def device_arrays(self) -> Dict[str, int]:

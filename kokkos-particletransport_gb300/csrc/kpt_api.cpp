@@ -1667,6 +1667,34 @@ int kpt_particles_sort(kpt_context* ctx, kpt_particles* parts, const kpt_field* 
     return KPT_OK;
 }
 
+int kpt_particles_pack_records(kpt_context* ctx, const kpt_particles* parts,
+                               double initial_kinetic_energy, void* out, uint64_t out_len) {
+    KPT_REQUIRE(ctx && parts && out, "kpt_particles_pack_records: NULL argument");
+    const uint64_t bytes = parts->count * 100;
+    KPT_REQUIRE(out_len >= bytes, "kpt_particles_pack_records: output shorter than count x 100");
+    if (parts->count == 0) return KPT_OK;
+    if (int rc = activate(ctx)) return rc;
+    KPT_CUDA(ctx->sample_io.reserve(bytes));
+    KPT_CUDA(kpt::launch_pack_records(parts->arrays, parts->count, initial_kinetic_energy,
+                                      ctx->sample_io.as<uint32_t>(), ctx->stream));
+    KPT_CUDA(cudaMemcpyAsync(out, ctx->sample_io.ptr, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    KPT_CUDA(cudaStreamSynchronize(ctx->stream));
+    return KPT_OK;
+}
+
+int kpt_host_alloc(uint64_t bytes, void** out) {
+    KPT_REQUIRE(out != nullptr, "kpt_host_alloc: NULL argument");
+    *out = nullptr;
+    if (bytes == 0) return KPT_OK;
+    KPT_CUDA(cudaHostAlloc(out, bytes, cudaHostAllocPortable));
+    return KPT_OK;
+}
+
+int kpt_host_free(void* ptr) {
+    if (ptr != nullptr) cudaFreeHost(ptr);
+    return KPT_OK;
+}
+
 int kpt_particles_clear_order(kpt_particles* parts) {
     KPT_REQUIRE(parts != nullptr, "kpt_particles_clear_order: NULL handle");
     parts->order_valid = false;

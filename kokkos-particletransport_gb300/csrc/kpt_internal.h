@@ -157,6 +157,9 @@ struct SortLaunch {
     unsigned int* order;    // count
 };
 cudaError_t launch_sort(const SortLaunch& launch, cudaStream_t stream);
+// v4 snapshot records (25 words each) of particles [0, count).
+cudaError_t launch_pack_records(const ParticleArrays& a, uint64_t count, double e0,
+                                uint32_t* out, cudaStream_t stream);
 
 struct SurrogateTrainLaunch {
     const float* x;   // n x 5 raw features

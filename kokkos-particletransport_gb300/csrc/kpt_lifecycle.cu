@@ -474,4 +474,50 @@ cudaError_t noalloc_summary(const SummaryLaunch& in, cudaStream_t stream, Summar
     return cudaStreamSynchronize(stream);
 }
 
+// v4 snapshot records of the driver (src/main.cpp:2155-2201), 100 bytes
+// each as 25 little-endian 32-bit words: id u64, status, split level,
+// sort key 0, position / previous position / previous-step position (the
+// driver writes the position three times), momentum, mu, weight, the initial
+// kinetic energy.  8-byte fields sit on 4-byte boundaries, so they are
+// written as word pairs.
+namespace {
+__device__ __forceinline__ void put64(uint32_t* w, double v) {
+    const unsigned long long bits = static_cast<unsigned long long>(__double_as_longlong(v));
+    w[0] = static_cast<uint32_t>(bits);
+    w[1] = static_cast<uint32_t>(bits >> 32);
+}
+
+__global__ void pack_records_kernel(ParticleArrays a, uint64_t count, double e0,
+                                    uint32_t* out) {
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < count;
+         i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        uint32_t* r = out + i * 25;
+        r[0] = static_cast<uint32_t>(i);
+        r[1] = static_cast<uint32_t>(i >> 32);
+        r[2] = static_cast<uint32_t>(a.status[i]);
+        r[3] = static_cast<uint32_t>(a.split_level[i]);
+        r[4] = 0u;
+        const double x = a.x[i];
+        const double y = a.y[i];
+        for (int k = 0; k < 3; ++k) {
+            put64(r + 5 + 4 * k, x);
+            put64(r + 7 + 4 * k, y);
+        }
+        put64(r + 17, a.p[i]);
+        put64(r + 19, a.mu[i]);
+        put64(r + 21, a.weight[i]);
+        put64(r + 23, e0);
+    }
+}
+}  // namespace
+
+cudaError_t launch_pack_records(const ParticleArrays& a, uint64_t count, double e0,
+                                uint32_t* out, cudaStream_t stream) {
+    if (count == 0) return cudaSuccess;
+    const uint64_t want = (count + 255) / 256;
+    const int blocks = static_cast<int>(want > 152u * 32u ? 152u * 32u : want);
+    pack_records_kernel<<<blocks, 256, 0, stream>>>(a, count, e0, out);
+    return cudaGetLastError();
+}
+
 }  // namespace kpt

@@ -633,60 +633,80 @@ std::uint64_t load_snapshot(const RunSettings& s, int restart_frame, kpt_particl
 }
 
 // v4 snapshot writer (src/main.cpp:2132-2202).
-void write_snapshot(const RunSettings& s, kpt_particles* parts, int frame) {
-    std::uint64_t count = 0, capacity = 0;
-    check(kpt_particles_count(parts, &count, &capacity));
-    const std::string path = snapshot_path(s.output_dir, frame);
-    std::ofstream stream(path, std::ios::binary);
-    if (!stream) {
-        throw std::runtime_error("Failed to open particle snapshot output.");
+// Snapshot writer: the records are packed on the GPU into a page-locked
+// buffer (one copy), and the file is written on a second host thread while
+// the next frame is pushed.  The file is opened on the calling thread, so an
+// unwritable path fails at once; a later write error is reported when the
+// next snapshot starts or the run ends.
+class SnapshotWriter {
+public:
+    ~SnapshotWriter() {
+        if (pending_.valid()) pending_.wait();
+        kpt_host_free(buffer_);
     }
-    HostParticles h;
-    h.resize(count);
-    check(kpt_particles_download(parts, count, h.x.data(), h.y.data(), h.p.data(), nullptr,
-                                 nullptr, h.w.data(), h.mu.data(), h.status.data(),
-                                 h.level.data()));
-    const char magic[8] = {'K', 'P', 'T', 'P', 'R', 'T', '\0', '\0'};
-    stream.write(magic, 8);
-    put(stream, std::uint32_t{4});
-    put(stream, std::uint32_t{0x01020304u});
-    put(stream, std::int32_t{2});
-    put(stream, std::int32_t{3});
-    put(stream, count);
-    put(stream, capacity);
-    put(stream, 1.0);
-    put(stream, s.charge);
-    put(stream, 1.0);
-    put(stream, 1.0);
-    put(stream, s.split_ratio);
-    put(stream, 0.0);
-    const double e0 = std::sqrt(1.0 + s.p0 * s.p0) - 1.0;
-    // Records are assembled in memory and written in one call.
-    std::vector<char> records(static_cast<std::size_t>(count) * 100);
-    char* out = records.data();
-    auto emit = [&out](const auto& value) {
-        std::memcpy(out, &value, sizeof(value));
-        out += sizeof(value);
-    };
-    for (std::uint64_t i = 0; i < count; ++i) {
-        emit(i);
-        emit(h.status[i]);
-        emit(h.level[i]);
-        emit(std::int32_t{0});
-        for (int k = 0; k < 3; ++k) {
-            emit(h.x[i]);
-            emit(h.y[i]);
+
+    void finish() {
+        if (pending_.valid()) pending_.get();
+    }
+
+    void write(const RunSettings& s, kpt_context* ctx, kpt_particles* parts, int frame) {
+        finish();
+        std::uint64_t count = 0, capacity = 0;
+        check(kpt_particles_count(parts, &count, &capacity));
+        const std::string path = snapshot_path(s.output_dir, frame);
+        auto stream = std::make_shared<std::ofstream>(path, std::ios::binary);
+        if (!*stream) {
+            throw std::runtime_error("Failed to open particle snapshot output.");
         }
-        emit(h.p[i]);
-        emit(h.mu[i]);
-        emit(h.w[i]);
-        emit(e0);
+        std::vector<char> header;
+        auto put_bytes = [&header](const auto& value) {
+            const char* b = reinterpret_cast<const char*>(&value);
+            header.insert(header.end(), b, b + sizeof(value));
+        };
+        const char magic[8] = {'K', 'P', 'T', 'P', 'R', 'T', '\0', '\0'};
+        header.insert(header.end(), magic, magic + 8);
+        put_bytes(std::uint32_t{4});
+        put_bytes(std::uint32_t{0x01020304u});
+        put_bytes(std::int32_t{2});
+        put_bytes(std::int32_t{3});
+        put_bytes(count);
+        put_bytes(capacity);
+        put_bytes(1.0);
+        put_bytes(s.charge);
+        put_bytes(1.0);
+        put_bytes(1.0);
+        put_bytes(s.split_ratio);
+        put_bytes(0.0);
+        const double e0 = std::sqrt(1.0 + s.p0 * s.p0) - 1.0;
+        const std::uint64_t bytes = count * 100;
+        if (bytes > size_) {
+            kpt_host_free(buffer_);
+            buffer_ = nullptr;
+            size_ = 0;
+            check(kpt_host_alloc(bytes, &buffer_));
+            size_ = bytes;
+        }
+        if (bytes > 0) {
+            check(kpt_particles_pack_records(ctx, parts, e0, buffer_, size_));
+        }
+        const char* records = static_cast<const char*>(buffer_);
+        pending_ = std::async(std::launch::async, [stream, header, records, bytes]() {
+            stream->write(header.data(), static_cast<std::streamsize>(header.size()));
+            if (bytes > 0) {
+                stream->write(records, static_cast<std::streamsize>(bytes));
+            }
+            stream->flush();
+            if (!*stream) {
+                throw std::runtime_error("Failed to write particle binary scalar.");
+            }
+        });
     }
-    stream.write(records.data(), static_cast<std::streamsize>(records.size()));
-    if (!stream) {
-        throw std::runtime_error("Failed to write particle binary scalar.");
-    }
-}
+
+private:
+    void* buffer_ = nullptr;
+    std::uint64_t size_ = 0;
+    std::future<void> pending_;
+};
 
 // Histogram CSV (src/main.cpp:1942-1963).  Bin edges are formed as
 // fma(bin, dlogp, log(pmin)), the contracted form the reference's optimised
@@ -842,6 +862,7 @@ int run(const RunSettings& s) {
     bool stopped = false;
     int last_frame = s.start_frame;
     std::future<FieldDataPtr> next_upper;
+    SnapshotWriter snapshots;
     for (int frame = s.start_frame; frame < s.end_frame; ++frame) {
         const auto frame_start = Clock::now();
         FrameTiming timing;
@@ -897,7 +918,7 @@ int run(const RunSettings& s) {
         }
         if (s.snapshot_interval > 0 && (done % s.snapshot_interval == 0 || finishing)) {
             const auto snap_start = Clock::now();
-            write_snapshot(s, parts.get(), frame + 1);
+            snapshots.write(s, ctx.get(), parts.get(), frame + 1);
             std::ostringstream line;
             line << "wrote particle snapshot " << snapshot_path(s.output_dir, frame + 1) << " in "
                  << seconds_since(snap_start) << " s";
@@ -914,6 +935,7 @@ int run(const RunSettings& s) {
             break;
         }
     }
+    snapshots.finish();
     std::ostringstream footer;
     if (stopped) {
         footer << "Stopped by walltime after frame " << last_frame << " in "

@@ -30,7 +30,11 @@ Cases
                       sort_by_key, compact_active_particles,
                       split_particles_on_energy_growth, capture_previous_positions
 
-``python tests/golden/make_golden.py lib`` regenerates only the lib_* files.
+  c1/                 the strict CLI run of the 256x512 configuration
+                      (summary, 128-bin histogram, first snapshot records)
+
+``python tests/golden/make_golden.py lib`` (or ``c1``) regenerates only those
+files.
 """
 from __future__ import annotations
 
@@ -237,6 +241,41 @@ def make_cli(ref, out_dir):
         stream.write(" ".join(argv_common) + "\n")
 
 
+C1_ARGV = ["--profile", "smoke", "--frames", "1", "--particles-per-frame", "1600",
+           "--rank-scale", "16", "--capacity", "65536", "--overwrite-output"]
+
+
+def make_c1(ref, out_dir):
+    """The strict CLI run of the 256x512 configuration: Harris sheet with the
+    default parameters, no islands, no noise, identical frames 0 and 1;
+    25,600 particles.  Kept: summary.csv, the 128-bin histogram and the first
+    2048 snapshot records (the snapshot itself is 2.5 MB)."""
+    formats = importlib.import_module("kokkos-particletransport_gb300.formats")
+    c1_dir = os.path.join(out_dir, "c1")
+    if os.path.isdir(c1_dir):
+        shutil.rmtree(c1_dir)
+    os.makedirs(c1_dir)
+    field = fields.harris_field(256, 512)
+    with tempfile.TemporaryDirectory() as tmp:
+        field_dir = os.path.join(tmp, "fields")
+        os.makedirs(field_dir)
+        for k in range(2):
+            fields.write_compact_field(fields.field_file_path(field_dir, k), field)
+        run_dir = os.path.join(tmp, "run")
+        rc = ref.main(C1_ARGV + ["--field-dir", field_dir, "--output-dir", run_dir],
+                      frame_base=0)
+        assert rc == 0
+        for name in ("summary.csv", "momentum_histogram_00001.csv"):
+            shutil.copy(os.path.join(run_dir, name), c1_dir)
+        snap = formats.read_snapshot(os.path.join(run_dir, "particles_00001.bin"))
+        head = snap.records[:2048]
+        np.savez_compressed(os.path.join(c1_dir, "snapshot_head.npz"), count=snap.count,
+                            capacity=snap.capacity,
+                            **{name: head[name] for name in head.dtype.names})
+    with open(os.path.join(c1_dir, "argv.txt"), "w") as stream:
+        stream.write(" ".join(C1_ARGV) + "\n")
+
+
 def lib_basis(nx: int, ny: int, x_edges, y_edges, readme: bool) -> np.ndarray:
     """Smooth periodic coefficient fields on every ghosted cell centre, in the
     packed order B(3) V(3) drift curl(3) primary(3) secondary(3) kpar kperp divV."""
@@ -402,9 +441,13 @@ def make_lib(ref, out_dir):
 def main() -> None:
     ref = binding.ReferenceHarness()
     out_dir = HERE
+    if sys.argv[1:] == ["c1"]:
+        make_c1(ref, out_dir)
+        return
     make_lib(ref, out_dir)
     if sys.argv[1:] == ["lib"]:
         return
+    make_c1(ref, out_dir)
     make_tables(ref, out_dir)
     make_inject(ref, out_dir)
     make_push(ref, out_dir, "parker_uniform", False, False, 1500, 3, {})

@@ -378,3 +378,29 @@ def test_push_f64_qlt_closure_matches_oracle(ctx, kpt, oracle, case):
         assert err <= F64_REL, (name, err)
     assert np.array_equal(got["status"], want["status"])
     assert stats.particle_steps == int(steps.sum())
+
+
+def test_snapshot_records_packed_on_gpu(ctx, kpt):
+    """v4 records of write_reconnection_particle_snapshot (src/main.cpp:2155-2201)
+    packed by the GPU: byte-identical to records built on the host from the
+    downloaded arrays."""
+    import importlib
+    formats = importlib.import_module("kokkos-particletransport_gb300.formats")
+    data = load_golden("push_parker_uniform.npz")
+    n = int(data["count"])
+    parts = ctx.particles(n + 5)
+    parts.upload(golden_particles(data, "end"), n)
+    e0 = float(np.sqrt(1.0 + 0.1 ** 2) - 1.0)
+    got = parts.pack_records(e0)
+    host = parts.download()
+    want = np.zeros(n, dtype=formats.RECORD_DTYPE)
+    want["id"] = np.arange(n)
+    want["status"] = host["status"]
+    want["split_level"] = host["level"]
+    xy = np.stack([host["x"], host["y"]], axis=1)
+    for key in ("position", "previous_position", "previous_step_position"):
+        want[key] = xy
+    want["p"], want["mu"], want["weight"] = host["p"], host["mu"], host["w"]
+    want["initial_kinetic_energy"] = e0
+    assert got.tobytes() == want.tobytes()
+    parts.close()
