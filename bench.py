@@ -397,6 +397,62 @@ def run_batched(args):
             "bitwise_identical": bool(identical), "setup_s": setup_s}
 
 
+def run_library(args):
+    """The header library's lockstep solvers (ParkerSolver, FocusSolver; FP64)
+    on a uniform 1024x2048 periodic grid with smooth synthetic coefficient
+    fields: N particles, K steps replayed from one CUDA graph; particle-steps
+    = N x K (every particle advances once per step)."""
+    import torch
+    kpt = importlib.import_module("kokkos-particletransport_gb300")
+    ctx = kpt.Context(DEVICE)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    xe = np.linspace(-1.0, 1.0, NX + 1)
+    ye = np.linspace(-2.0, 2.0, NY + 1)
+    grid = ctx.grid(xe, ye, (1, 1))
+    n = args.library_particles
+    rng = np.random.default_rng(SEED)
+    state = {"id": np.arange(n, dtype=np.uint64)}
+    for key in kpt.SYSTEM_DOUBLE_FIELDS:
+        state[key] = np.zeros(n)
+    for key in kpt.SYSTEM_INT_FIELDS:
+        state[key] = np.zeros(n, dtype=np.int32)
+    state["x"] = rng.uniform(-1.0, 1.0, n)
+    state["y"] = rng.uniform(-2.0, 2.0, n)
+    state["p"] = np.exp(rng.uniform(np.log(0.05), np.log(3.0), n))
+    state["mu"] = rng.uniform(-1.0, 1.0, n)
+    state["w"] = np.ones(n)
+    out = {"particles": n, "grid": f"{NX}x{NY}", "steps": args.library_steps}
+    for label in ("parker", "focus"):
+        if label == "parker":
+            basis = fields.library_parker_basis(NX, NY, xe, ye, True)
+            solver = ctx.parker_solver(grid, basis)
+        else:
+            basis = fields.library_focus_basis(NX, NY, xe, ye)
+            solver = ctx.focus_solver(grid, basis)
+        del basis
+        system = ctx.system(n, n)
+        system.upload(state)
+        solver.advance_stochastic_steps(system, SEED, 0, 2)  # warm-up, records nothing
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        dts = solver.advance_stochastic_steps(system, SEED, 2, args.library_steps)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        active = int((system.download()["status"] == 0).sum())
+        out[label] = {"value": n * args.library_steps / (ms / 1e3),
+                      "ms_per_step": ms / args.library_steps, "dt_first": float(dts[0]),
+                      "active_after": active}
+        solver.close()
+        system.close()
+    grid.close()
+    ctx.close()
+    return out
+
+
 def cpu_baseline(particles: int, steps: int = 1):
     """Oracle restatement of the focused push with the plain slab-QLT closure
     (OpenMP, all host threads) on a bounded sample of the headline workload."""
@@ -454,6 +510,9 @@ def main():
     parser.add_argument("--cpu-particles", type=int, default=1 << 16)
     parser.add_argument("--batch-runs", type=int, default=64,
                         help="independent runs of the batched leg (0 skips it)")
+    parser.add_argument("--library-particles", type=int, default=1 << 20,
+                        help="particles of the library-solver leg (0 skips it)")
+    parser.add_argument("--library-steps", type=int, default=10)
     parser.add_argument("--sort-tile", type=int, default=16,
                         help="cell-sort tile (cells) before each push; 0 disables")
     args = parser.parse_args()
@@ -493,6 +552,7 @@ def main():
     focused = run_focused(args, f0, f1)
     parker = run_parker(args, f0, f1) if args.parker_particles > 0 and WORLD == 1 else None
     batched = run_batched(args) if args.batch_runs > 0 and WORLD == 1 else None
+    library = run_library(args) if args.library_particles > 0 and WORLD == 1 else None
     peak, peak_kind = read_peaks()
     head, f64 = focused["surrogate"], focused["f64"]
     mixed_qlt = focused.get("mixed_qlt")
@@ -549,6 +609,7 @@ def main():
                 "d2h_bytes_per_step": head["state_bytes"]},
         "parker": parker,
         "batched_runs": batched,
+        "library_solvers": library,
         # per timed step: the push, plus 3 cell-sort kernels when sorting
         "gpu_launches": args.steps * (1 + (3 if args.sort_tile > 0 else 0)),
         "clocks": head["clocks"],

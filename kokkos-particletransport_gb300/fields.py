@@ -152,3 +152,71 @@ def harris_field(nx: int, ny: int, *, x_range=(-1.0, 1.0), y_range=(-2.0, 2.0),
 def field_file_path(field_dir: str, frame: int) -> str:
     """``FIELD_DIR/fieldNNNNN.bin`` as in the reference (src/main.cpp:413-418)."""
     return os.path.join(field_dir, f"field{frame:05d}.bin")
+
+
+def library_parker_basis(nx: int, ny: int, x_edges, y_edges, readme: bool = True) -> np.ndarray:
+    """Synthetic smooth periodic coefficient fields for the library Parker solver
+    on every ghosted cell centre of a uniform grid, in the packed order of
+    ParkerSolver.hpp:96-116: B(3) V(3) drift curl(3) diffusion primary(3)
+    secondary(3) kappa_par kappa_perp div V (points x 18, x fastest).
+    readme = False gives the constant-ratio branch (secondary zero)."""
+    dx = (x_edges[-1] - x_edges[0]) / nx
+    dy = (y_edges[-1] - y_edges[0]) / ny
+    xc = x_edges[0] + (np.arange(-2, nx + 2) + 0.5) * dx
+    yc = y_edges[0] + (np.arange(-2, ny + 2) + 0.5) * dy
+    y, x = np.meshgrid(yc, xc, indexing="ij")
+    kx, ky = np.pi, np.pi / 2.0
+    out = np.zeros((ny + 4, nx + 4, 18))
+    out[..., 0] = np.tanh(np.sin(ky * y) / 0.3) + 0.05
+    out[..., 1] = 0.1 * np.sin(kx * x) * np.cos(ky * y)
+    out[..., 2] = 0.2
+    out[..., 3] = 0.1 * np.cos(kx * x)
+    out[..., 4] = -0.05 * np.sin(ky * y)
+    out[..., 6] = 0.02 * np.sin(kx * x + ky * y)
+    out[..., 7] = 0.02 * np.cos(kx * x - ky * y)
+    out[..., 8] = 0.01 * np.sin(ky * y)
+    out[..., 9] = 1e-3 * np.cos(kx * x)
+    out[..., 10] = 1e-3 * np.sin(ky * y)
+    if readme:
+        out[..., 12] = 5e-4 * np.sin(kx * x)
+        out[..., 13] = 5e-4 * np.cos(ky * y)
+    out[..., 15] = 0.01 * (1.2 + np.sin(kx * x) * np.cos(ky * y))
+    out[..., 16] = 0.05 * out[..., 15] if not readme else 1e-3 * (1.1 + np.cos(kx * x))
+    out[..., 17] = 0.1 * np.cos(kx * x) * np.sin(ky * y)
+    return out.reshape(-1, 18)
+
+
+def library_focus_basis(nx: int, ny: int, x_edges, y_edges) -> np.ndarray:
+    """Smooth periodic focused-transport fields on every ghosted cell centre in
+    the packed order B(3) b(3) V(3) grad-drift(3) curvature-drift(3) perp-adv(3)
+    |B| kpar kperp divV focusing bb:gradV b.dV/dt sigma^2 Lc."""
+    parker = library_parker_basis(nx, ny, x_edges, y_edges, True).reshape(ny + 4, nx + 4, 18)
+    dx = (x_edges[-1] - x_edges[0]) / nx
+    dy = (y_edges[-1] - y_edges[0]) / ny
+    xc = x_edges[0] + (np.arange(-2, nx + 2) + 0.5) * dx
+    yc = y_edges[0] + (np.arange(-2, ny + 2) + 0.5) * dy
+    y, x = np.meshgrid(yc, xc, indexing="ij")
+    kx, ky = np.pi, np.pi / 2.0
+    out = np.zeros((ny + 4, nx + 4, 27))
+    b = parker[..., 0:3]
+    bmag = np.sqrt((b * b).sum(-1))
+    out[..., 0:3] = b
+    out[..., 3:6] = b / bmag[..., None]
+    out[..., 6:9] = parker[..., 3:6]
+    out[..., 9] = 0.01 * np.sin(kx * x)
+    out[..., 10] = 0.01 * np.cos(ky * y)
+    out[..., 12] = 0.005 * np.cos(kx * x + ky * y)
+    out[..., 13] = 0.005 * np.sin(kx * x)
+    out[..., 14] = 0.002
+    out[..., 15] = 1e-4 * np.sin(ky * y)
+    out[..., 16] = 1e-4 * np.cos(kx * x)
+    out[..., 18] = bmag
+    out[..., 19] = 0.01 * (1.2 + np.sin(kx * x) * np.cos(ky * y))
+    out[..., 20] = 5e-4 * (1.1 + np.cos(kx * x))
+    out[..., 21] = 0.1 * np.cos(kx * x) * np.sin(ky * y)
+    out[..., 22] = 0.2 * np.sin(kx * x - ky * y)
+    out[..., 23] = 0.05 * np.cos(ky * y)
+    out[..., 24] = 0.02 * np.sin(kx * x)
+    out[..., 25] = 0.1 * (1.0 + 0.5 * np.sin(kx * x) * np.sin(ky * y))
+    out[..., 26] = 0.05 * (1.0 + 0.2 * np.cos(kx * x))
+    return out.reshape(-1, 27)
