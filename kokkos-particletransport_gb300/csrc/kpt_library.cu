@@ -122,6 +122,21 @@ __device__ __forceinline__ void lib_sample(const LibGrid& g, const double* __res
     }
 }
 
+// The momentum scalings gamma^(1/3) and gamma^(1/9) of the diffusion
+// coefficients (LegencyModel.hpp:483-502, FocusSolver.hpp:820, :968 call
+// pow(gamma, 1/3) and pow(gamma, 1/9)) as one and two cube roots: the same
+// values to within two ulp, at a fraction of pow's FP64 work.  The kernels
+// here are FP64-pipe bound, so every transcendental counts.
+struct GammaRoots {
+    double third, ninth;
+};
+__device__ __forceinline__ GammaRoots gamma_roots(double gamma, bool ninth) {
+    GammaRoots r;
+    r.third = cbrt(gamma);
+    r.ninth = ninth ? cbrt(r.third) : r.third;
+    return r;
+}
+
 __device__ __forceinline__ bool finite_positive(double v) { return isfinite(v) && v > 0.0; }
 __device__ __forceinline__ bool finite_nonnegative(double v) { return isfinite(v) && v >= 0.0; }
 
@@ -203,18 +218,19 @@ __device__ double lib_parker_terms(const LibParkerLaunch& L, size_t i, double* t
     double dir[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) dir[c] = v[c] * ib;
-    const double g13 = pow(gamma, 1.0 / 3.0);
+    const GammaRoots roots = gamma_roots(gamma, !L.constant_ratio);
+    const double g13 = roots.third;
     double diff[3];
     if (L.constant_ratio) {
 #pragma unroll
         for (int c = 0; c < 3; ++c) diff[c] = g13 * v[9 + c];
     } else {
-        const double g19 = pow(gamma, 1.0 / 9.0);
+        const double g19 = roots.ninth;
 #pragma unroll
         for (int c = 0; c < 3; ++c) diff[c] = g13 * v[9 + c] + g19 * v[12 + c];
     }
-    const double kpar = v[15] * pow(gamma, 1.0 / 3.0);
-    const double kperp = v[16] * (L.constant_ratio ? pow(gamma, 1.0 / 3.0) : pow(gamma, 1.0 / 9.0));
+    const double kpar = v[15] * g13;
+    const double kperp = v[16] * (L.constant_ratio ? g13 : roots.ninth);
     if (!finite_nonnegative(kpar) || !finite_nonnegative(kperp)) {
         return -3.0;  // "diffusion coefficients must be finite and non-negative"
     }
@@ -324,14 +340,18 @@ __global__ void __launch_bounds__(256) lib_parker_terms_kernel(const LibParkerLa
     }
 }
 
-// Box-Muller normal from two stream draws (u1 = 1 - draw, u2 = draw), the
-// shim pool's normal(): stream draws 2k and 2k+1 are block k.
-__device__ __forceinline__ double lib_normal(uint2 key, uint32_t block, uint32_t index,
-                                             uint32_t frame) {
+// Box-Muller pair from two stream draws (u1 = 1 - draw, u2 = draw): normals
+// 2m and 2m+1 of a particle's step are r cos(theta) and r sin(theta) of
+// block m, as the shim pool's normal() hands them out.
+__device__ __forceinline__ double2 lib_normal_pair(uint2 key, uint32_t block, uint32_t index,
+                                                   uint32_t frame) {
     const uint4 r = philox4x32_10(make_uint4(block, index, frame, kTagLibrary), key);
     const double u1 = 1.0 - u01_f64(r.x, r.y);
     const double u2 = u01_f64(r.z, r.w);
-    return sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2);
+    const double radius = sqrt(-2.0 * log(u1));
+    double s, c;
+    sincos(6.283185307179586 * u2, &s, &c);
+    return make_double2(radius * c, radius * s);
 }
 
 // Pass 2: capture previous positions (whole capacity), update, boundary.
@@ -358,14 +378,13 @@ __global__ void __launch_bounds__(256) lib_parker_advance_kernel(const LibParker
         double inc[2] = {0.0, 0.0};
         if (L.stochastic) {
             const uint32_t index = static_cast<uint32_t>(i);
-            double gv[3];
+            const double2 n01 = lib_normal_pair(L.key, 0u, index, L.frame);
+            const double2 n23 = lib_normal_pair(L.key, 1u, index, L.frame);
+            const double gv[3] = {n01.x, n01.y, n23.x};
             double iso = 0.0;
 #pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                gv[c] = lib_normal(L.key, static_cast<uint32_t>(c), index, L.frame);
-                iso += gv[c] * t[kDirX + c];
-            }
-            const double pg = lib_normal(L.key, 3u, index, L.frame);
+            for (int c = 0; c < 3; ++c) iso += gv[c] * t[kDirX + c];
+            const double pg = n23.y;
             const double kperp = t[kKappaPerp];
             const double kpar = t[kKappaPar];
             const double perp_scale = kperp > 0.0 ? sqrt(2.0 * kperp * dt) : 0.0;
@@ -413,10 +432,16 @@ enum FocusSlot {
 };
 static_assert(fLc + 1 <= kFocusTermCount, "focus term row layout");
 
+// The first failure of a particle's step is the one reported, as the
+// reference throws at its first failed check.
+__device__ __forceinline__ void set_error(int* error, int code) {
+    if (*error == 0) *error = code;
+}
+
 // reflected_pitch_angle_cosine (FocusSolver.hpp:453-470).
 __device__ __forceinline__ double focus_reflect(double mu, double max_mu, int* error) {
     if (!isfinite(mu)) {
-        *error = 8;  // "pitch-angle cosine is not finite"
+        set_error(error, 8);  // "pitch-angle cosine is not finite"
         return 0.0;
     }
     const double upper = max_mu;
@@ -437,51 +462,74 @@ struct PitchRates {
     double focusing, D, dD, rate;
 };
 
-// evaluate_pitch_angle_at_mu (FocusSolver.hpp:664-695) with the slab-QLT
-// evaluate_pitch_angle_scattering (LegencyModel.hpp:539-693).
-__device__ PitchRates focus_pitch(const LibFocusLaunch& L, const double* t, double trial,
-                                  int* error) {
-    PitchRates r{0.0, 0.0, 0.0, 0.0};
-    const double mu = focus_reflect(trial, L.max_mu, error);
-    const double mu2 = mu * mu;
-    const double one_minus_mu2 = 1.0 - mu2;
-    const double speed = t[fSpeed];
-    if (speed <= 0.0) {
-        *error = 12;  // "pitch-angle stepping requires positive particle speed"
-        return r;
+// The parts of evaluate_pitch_angle_at_mu (FocusSolver.hpp:664-695) and of
+// the slab-QLT D_mumu (LegencyModel.hpp:557-645) that do not depend on mu:
+// one step evaluates the rates at four trial cosines (the time-step bound and
+// three Picard iterations) of the same particle, so omega, xi, xi^gamma_k
+// and the prefactor are formed once.  The reference forms pow(|mu|+h0, gk),
+// pow(xi, gk) and pow(|mu|+h0, gk-1) in both D and D'; here one pow per trial
+// cosine remains (|mu|+h0)^(gk-1), with (|mu|+h0)^gk as its product with
+// |mu|+h0 (equal to within two ulp).
+struct PitchSetup {
+    double speed, focusing0, convective, omega, xi, xi_gk, pref;
+    int error;  // 12, 13 or 14: the input check that fails, in the reference's order
+};
+
+__device__ PitchSetup focus_pitch_setup(const LibFocusLaunch& L, const double* t) {
+    PitchSetup q{};
+    q.speed = t[fSpeed];
+    if (q.speed <= 0.0) {
+        q.error = 12;  // "pitch-angle stepping requires positive particle speed"
+        return q;
     }
-    r.focusing = 0.5 * one_minus_mu2 *
-                 (-speed * t[fFocusing] + mu * t[fDivV] - 3.0 * mu * t[fBBGradV] -
-                  2.0 * t[fConvective] / speed);
+    q.focusing0 = -q.speed * t[fFocusing];
+    q.convective = 2.0 * t[fConvective] / q.speed;
     const double safe_b = positive_floor(t[fBmag], L.min_b);
     const double safe_sigma2 = positive_floor(t[fSigma2], L.min_sigma2);
     const double safe_lc = positive_floor(t[fLc], L.min_lc);
-    const double safe_speed = positive_floor(speed, L.min_speed);
+    const double safe_speed = positive_floor(q.speed, L.min_speed);
     if (safe_b <= 0.0 || safe_sigma2 <= 0.0 || safe_lc <= 0.0 || safe_speed <= 0.0) {
-        *error = 13;  // "pitch-angle scattering requires positive local inputs"
+        q.error = 13;  // "pitch-angle scattering requires positive local inputs"
+        return q;
+    }
+    q.omega = L.abs_charge * safe_b / (L.rest_mass * L.speed_of_light) / t[fGamma];
+    if (q.omega <= 0.0) {
+        q.error = 14;  // "D_mumu requires positive omega, speed, sigma2, and Lc"
+        return q;
+    }
+    q.xi = q.omega * safe_lc / safe_speed;
+    q.xi_gk = pow(q.xi, L.gk);
+    q.pref = 0.25 * 3.141592653589793238462643383279502884 * q.omega * safe_sigma2 * L.qlt_norm;
+    return q;
+}
+
+// evaluate_pitch_angle_at_mu with the slab-QLT evaluate_pitch_angle_scattering
+// (LegencyModel.hpp:539-693) at one trial cosine.
+__device__ PitchRates focus_pitch(const LibFocusLaunch& L, const double* t, const PitchSetup& q,
+                                  double trial, int* error) {
+    PitchRates r{0.0, 0.0, 0.0, 0.0};
+    const double mu = focus_reflect(trial, L.max_mu, error);
+    if (q.error != 0) {
+        set_error(error, q.error);
         return r;
     }
-    const double omega = L.abs_charge * safe_b / (L.rest_mass * L.speed_of_light) / t[fGamma];
-    // pitch_angle_diffusion_coefficient (LegencyModel.hpp:557-594)
-    if (omega <= 0.0) {
-        *error = 14;  // "D_mumu requires positive omega, speed, sigma2, and Lc"
-        return r;
-    }
+    const double mu2 = mu * mu;
+    const double one_minus_mu2 = 1.0 - mu2;
+    r.focusing = 0.5 * one_minus_mu2 *
+                 (q.focusing0 + mu * t[fDivV] - 3.0 * mu * t[fBBGradV] - q.convective);
     double d = 0.0;
     double dd = 0.0;
     if (one_minus_mu2 > 0.0) {
         const double reg = (mu >= 0.0 ? mu : -mu) + L.h0;
         const double gk = L.gk;
-        const double xi = omega * safe_lc / safe_speed;
-        const double den = pow(reg, gk) + pow(xi, gk);
+        const double reg_gk1 = pow(reg, gk - 1.0);
+        const double reg_gk = reg > 0.0 ? reg_gk1 * reg : pow(reg, gk);
+        const double den = reg_gk + q.xi_gk;
         if (den <= 0.0) {
-            *error = 15;  // "D_mumu denominator must be positive"
+            set_error(error, 15);  // "D_mumu denominator must be positive"
             return r;
         }
-        const double pref = 0.25 * 3.141592653589793238462643383279502884 * omega * safe_sigma2 *
-                            L.qlt_norm;
-        const double reg_gk1 = pow(reg, gk - 1.0);
-        d = pref * one_minus_mu2 * xi * reg_gk1 / den;
+        d = q.pref * one_minus_mu2 * q.xi * reg_gk1 / den;
         // pitch_angle_diffusion_derivative (LegencyModel.hpp:599-645)
         const double sign = mu > 0.0 ? 1.0 : (mu < 0.0 ? -1.0 : 0.0);
         if (d != 0.0 && sign != 0.0) {
@@ -514,7 +562,7 @@ __device__ double focus_terms(const LibFocusLaunch& L, size_t i, double* t, int*
     for (int dim = 0; dim < 2; ++dim) {
         q[dim] = lib_wrap(g.axis[dim], pos[dim]);
         if (!lib_contains(g.axis[dim].ghost_lower, g.axis[dim].ghost_upper, q[dim])) {
-            *error = 1;
+            set_error(error, 1);
             return -1.0;
         }
     }
@@ -528,7 +576,7 @@ __device__ double focus_terms(const LibFocusLaunch& L, size_t i, double* t, int*
     const double speed = p / (gamma * L.rest_mass);
     const double bmag = v[18];
     if (!finite_positive(bmag)) {
-        *error = 9;  // "focused transport requires |B| > 0"
+        set_error(error, 9);  // "focused transport requires |B| > 0"
         return -1.0;
     }
     double s2 = 0.0;
@@ -536,18 +584,19 @@ __device__ double focus_terms(const LibFocusLaunch& L, size_t i, double* t, int*
     for (int c = 0; c < 3; ++c) s2 += v[3 + c] * v[3 + c];
     const double smag = sqrt(s2);
     if (!finite_positive(smag)) {
-        *error = 10;  // "interpolated magnetic direction is invalid"
+        set_error(error, 10);  // "interpolated magnetic direction is invalid"
         return -1.0;
     }
     const double inv = 1.0 / smag;
     double dir[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) dir[c] = v[3 + c] * inv;
-    const double perp_factor = L.constant_ratio ? pow(gamma, 1.0 / 3.0) : pow(gamma, 1.0 / 9.0);
-    const double kpar = v[19] * pow(gamma, 1.0 / 3.0);
+    const GammaRoots roots = gamma_roots(gamma, !L.constant_ratio);
+    const double perp_factor = L.constant_ratio ? roots.third : roots.ninth;
+    const double kpar = v[19] * roots.third;
     const double kperp = v[20] * perp_factor;
     if (!finite_nonnegative(kpar) || !finite_nonnegative(kperp)) {
-        *error = 11;  // "diffusion coefficients must be finite and non-negative"
+        set_error(error, 11);  // "diffusion coefficients must be finite and non-negative"
         return -1.0;
     }
     const double mu2 = mu * mu;
@@ -592,7 +641,7 @@ __device__ double focus_terms(const LibFocusLaunch& L, size_t i, double* t, int*
                                    acceleration;
     const double momentum_rate = -p * momentum_factor;
     t[fMomentumRate] = momentum_rate;
-    const PitchRates pitch = focus_pitch(L, t, mu, error);
+    const PitchRates pitch = focus_pitch(L, t, focus_pitch_setup(L, t), mu, error);
 
     double dmin = kLargeTimeStep;
     double amin = kLargeTimeStep;
@@ -607,7 +656,7 @@ __device__ double focus_terms(const LibFocusLaunch& L, size_t i, double* t, int*
         const double width = __dsub_rn(lib_face(a, __dadd_rn(cell, 1.0)), lib_face(a, cell));
         const double dx = fabs(__dmul_rn(1.0, width));
         if (!finite_positive(dx)) {
-            *error = 5;
+            set_error(error, 5);
             return -1.0;
         }
         double diffusion_dt = kLargeTimeStep;
@@ -689,18 +738,17 @@ __global__ void __launch_bounds__(256) focus_advance_kernel(const LibFocusLaunch
         double pitch_normal = 0.0;
         if (L.stochastic) {
             const uint32_t index = static_cast<uint32_t>(i);
-            double gv[3];
+            const double2 n01 = lib_normal_pair(L.key, 0u, index, L.frame);
+            const double2 n23 = lib_normal_pair(L.key, 1u, index, L.frame);
+            const double gv[3] = {n01.x, n01.y, n23.x};
             double parallel = 0.0;
 #pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                gv[c] = lib_normal(L.key, static_cast<uint32_t>(c), index, L.frame);
-                parallel += gv[c] * t[fDirX + c];
-            }
+            for (int c = 0; c < 3; ++c) parallel += gv[c] * t[fDirX + c];
             const double kperp = t[fKappaPerp];
             const double scale = kperp > 0.0 ? sqrt(2.0 * kperp * dt) : 0.0;
 #pragma unroll
             for (int c = 0; c < 2; ++c) inc[c] = scale * (gv[c] - parallel * t[fDirX + c]);
-            pitch_normal = lib_normal(L.key, 3u, index, L.frame);
+            pitch_normal = n23.y;
         }
         s.x[i] += dt * t[fRateX] + inc[0] * 1.0;
         s.y[i] += dt * t[fRateY] + inc[1] * 1.0;
@@ -708,9 +756,10 @@ __global__ void __launch_bounds__(256) focus_advance_kernel(const LibFocusLaunch
         s.p[i] = updated > 0.0 ? updated : 0.0;
         int err = 0;
         const double initial = focus_reflect(t[fMu], L.max_mu, &err);
+        const PitchSetup setup = focus_pitch_setup(L, t);
         double trial = initial;
         for (int it = 0; it < 3; ++it) {
-            const PitchRates pitch = focus_pitch(L, t, trial, &err);
+            const PitchRates pitch = focus_pitch(L, t, setup, trial, &err);
             const double scale = pitch.D > 0.0 ? sqrt(2.0 * pitch.D * dt) : 0.0;
             trial = initial + dt * pitch.rate + scale * pitch_normal;
             trial = focus_reflect(trial, L.max_mu, &err);

@@ -55,17 +55,31 @@ template <class DeviceType>
 class Random_XorShift64 {
 public:
     kpt_oracle_stream stream{};
+    bool has_spare = false;
+    double spare = 0.0;
 
     double drand() { return kpt_oracle_stream_u01(&stream); }
     double drand(const double range) { return range * drand(); }
     double drand(const double start, const double end) {
         return start + (end - start) * drand();
     }
-    // Box-Muller transform on two stream draws (unused by the driver path).
+    // Box-Muller transform on two stream draws, both of its normals used:
+    // normal 2m is r cos(theta) and normal 2m+1 is r sin(theta) of draws 2m
+    // and 2m+1 (u1 = 1 - draw 2m, u2 = draw 2m+1, theta = 2 pi u2).  Only
+    // the header library's solvers draw normals; the driver path draws
+    // uniforms alone.
     double normal() {
+        if (has_spare) {
+            has_spare = false;
+            return spare;
+        }
         const double u1 = 1.0 - drand();
         const double u2 = drand();
-        return std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2);
+        const double r = std::sqrt(-2.0 * std::log(u1));
+        const double theta = 6.283185307179586 * u2;
+        spare = r * std::sin(theta);
+        has_spare = true;
+        return r * std::cos(theta);
     }
     double normal(const double mean, const double standard_deviation) {
         return mean + standard_deviation * normal();
