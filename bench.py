@@ -448,8 +448,64 @@ def run_library(args):
                       "active_after": active}
         solver.close()
         system.close()
+    out["generator"] = run_generator(kpt, ctx, grid, xe, ye, n, stream)
     grid.close()
     ctx.close()
+    return out
+
+
+def run_generator(kpt, ctx, grid, xe, ye, n, stream):
+    """ParticleGenerator on the same grid: a field-threshold candidate set
+    over the 1024x2048 cells (compaction + cumulative volumes), N particles
+    injected from it, N injected by cell volume over the grid, and N
+    recycled by region rejection sampling against the field predicate."""
+    import torch
+    dx, dy = (xe[-1] - xe[0]) / NX, 4.0 / NY
+    xc = xe[0] + (np.arange(NX + 4) - 1.5) * dx
+    yc = -2.0 + (np.arange(NY + 4) - 1.5) * dy
+    values = (np.cos(2.0 * np.pi * xc)[None, :] * np.exp(-yc[:, None] ** 2)).ravel()
+    field = ctx.lib_field(grid, values)
+    system = ctx.system(0, n)
+    rng = kpt.RandomManager(SEED, 0)
+    kin = kpt.ParticleInjectionKinematics(1.0, 0.0, 1.0, 0)
+    out = {"particles": n}
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        result = fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1), result
+
+    for _ in range(2):  # warm-up, then the timed pass
+        ms_cand, cands = timed(lambda: ctx.make_field_particle_candidate_set(field, 0.2,
+                                                                             "greater"))
+        ms_field, _ = timed(lambda: kpt.inject_particles_from_field_candidates(
+            system, rng, cands, kpt.make_particle_injection_plan(0, n), kin))
+        ms_grid, _ = timed(lambda: kpt.inject_particles_uniform_in_grid(
+            system, rng, grid, kpt.make_particle_injection_plan(0, n), kin))
+        state = system.download()
+        state["status"][::2] = 1  # half the particles escaped
+        system.upload(state)
+        region = kpt.make_particle_region((xe[0], -2.0), (xe[-1], 2.0))
+        pred = kpt.make_field_threshold_particle_predicate(field, 0.2, "greater")
+        ms_recycle, recycled = timed(lambda: kpt.recycle_particles_uniform_if(
+            system, rng, region, kin, pred, "escaped_only"))
+        count = cands.candidate_count()
+        cands.close()
+    out.update({"field_candidates": {"points": int(values.size), "candidates": count,
+                                     "ms": ms_cand},
+                "inject_field_candidates": {"value": n / (ms_field / 1e3), "ms": ms_field},
+                "inject_in_grid": {"value": n / (ms_grid / 1e3), "ms": ms_grid,
+                                   "note": "includes the grid candidate set build"},
+                "recycle_uniform_if": {"value": recycled / (ms_recycle / 1e3),
+                                       "ms": ms_recycle, "recycled": recycled},
+                "unit": "particles/s"})
+    system.close()
+    field.close()
     return out
 
 

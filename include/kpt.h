@@ -536,6 +536,121 @@ int kpt_focus_advance_stochastic_steps(kpt_context* ctx, kpt_focus_solver* solve
                                        uint32_t steps, double* dts);
 
 /* ======================================================================
+ * ParticleGenerator (include/ParticleGenerator.hpp:659-1493): injection and
+ * recycling on the library grid.  The reference draws from
+ * RandomManager's XorShift pool; here each particle slot draws from its
+ * own keyed stream (seed, slot, frame, tag 4), so the results do not depend
+ * on thread scheduling.  Particle slot = local index for injection, particle
+ * index for recycling (the reference's loop indices).
+ * ====================================================================== */
+
+typedef struct kpt_lib_field kpt_lib_field;
+typedef struct kpt_candidates kpt_candidates;
+
+enum kpt_centering { KPT_CELL_CENTERED = 0, KPT_FACE_CENTERED = 1 };
+enum kpt_grid_domain { KPT_PHYSICAL_DOMAIN = 0, KPT_GHOSTED_DOMAIN = 1 };
+/* FieldPredicateComparison (ParticleGenerator.hpp:117-124). */
+enum kpt_field_comparison {
+    KPT_GREATER = 0, KPT_GREATER_EQUAL = 1, KPT_LESS = 2, KPT_LESS_EQUAL = 3,
+    KPT_ABS_GREATER = 4, KPT_ABS_LESS = 5
+};
+/* ParticleRecycleSelection (ParticleGenerator.hpp:129-133). */
+enum kpt_recycle_selection {
+    KPT_RECYCLE_ESCAPED_ONLY = 0, KPT_RECYCLE_INACTIVE_ONLY = 1, KPT_RECYCLE_RECYCLABLE = 2
+};
+
+/* AxisAlignedParticleRegion<2> (ParticleGenerator.hpp:18-62). */
+typedef struct kpt_region {
+    double lower[2];
+    double upper[2];
+} kpt_region;
+
+/* ParticleInjectionKinematics<2> (ParticleGenerator.hpp:68-74); status as
+ * ParticleStatus (0 active, 1 escaped, 2 inactive). */
+typedef struct kpt_injection_kinematics {
+    double momentum_magnitude;
+    double mu;
+    double weight;
+    int32_t status;
+    int32_t pad;
+} kpt_injection_kinematics;
+
+/* ParticleInjectionPlan (ParticleGenerator.hpp:107-112). */
+typedef struct kpt_injection_plan {
+    uint64_t first_particle_index;
+    uint64_t particle_count;
+    uint64_t first_particle_id;
+    int32_t max_attempts;
+    int32_t pad;
+} kpt_injection_plan;
+
+/* FieldThresholdParticlePredicate settings (ParticleGenerator.hpp:255-296). */
+typedef struct kpt_field_predicate {
+    const kpt_lib_field* field;
+    double threshold;
+    int32_t comparison;
+    int32_t component;
+    int32_t domain;
+    int32_t pad;
+} kpt_field_predicate;
+
+/* Field<Grid, components> (Field.hpp:33-215) on a library grid: values
+ * holds `components` doubles per stored point, dim 0 fastest over the
+ * ghosted extent of the centering (cells n+4, faces n+5 per axis). */
+int kpt_lib_field_create(kpt_context* ctx, const kpt_grid* grid, int32_t components,
+                         const int32_t centering[2], const double* values, kpt_lib_field** out);
+int kpt_lib_field_destroy(kpt_lib_field* field);
+/* Stored points of the field (Field::point_count). */
+int kpt_lib_field_points(const kpt_lib_field* field, uint64_t* points);
+
+/* make_particle_region_from_grid (ParticleGenerator.hpp:208-226). */
+int kpt_region_from_grid(const kpt_grid* grid, int32_t domain, kpt_region* out);
+
+/* make_field_particle_candidate_set[_in_region] (ParticleGenerator.hpp:
+ * 659-784); region NULL = the grid's domain. */
+int kpt_candidates_from_field(kpt_context* ctx, const kpt_lib_field* field,
+                              const kpt_region* region, double threshold, int32_t comparison,
+                              int32_t component, int32_t domain, kpt_candidates** out);
+/* make_grid_particle_candidate_set (ParticleGenerator.hpp:786-856). */
+int kpt_candidates_from_grid(kpt_context* ctx, const kpt_grid* grid, int32_t domain,
+                             kpt_candidates** out);
+int kpt_candidates_info(const kpt_candidates* candidates, uint64_t* count, double* total_weight);
+/* Candidate point indices (field sets; grid sets give cell ordinals) and
+ * cumulative weights, either pointer may be NULL. */
+int kpt_candidates_download(kpt_context* ctx, const kpt_candidates* candidates,
+                            uint64_t* indices, double* cumulative_weights);
+int kpt_candidates_destroy(kpt_candidates* candidates);
+
+/* inject_particles_uniform / inject_particles_uniform_if with the field
+ * threshold predicate (predicate NULL: accept all) (ParticleGenerator.hpp:
+ * 885-960, :1106-1119). */
+int kpt_generator_inject_uniform(kpt_context* ctx, kpt_system* system, uint64_t seed,
+                                 uint32_t frame, const kpt_region* region,
+                                 const kpt_injection_plan* plan,
+                                 const kpt_injection_kinematics* kinematics,
+                                 const kpt_field_predicate* predicate);
+/* inject_particles_from_field_candidates / _from_grid_candidates
+ * (ParticleGenerator.hpp:962-1104); with the candidate builders above this
+ * covers inject_particles_uniform_where_field and _uniform_in_grid. */
+int kpt_generator_inject_candidates(kpt_context* ctx, kpt_system* system, uint64_t seed,
+                                    uint32_t frame, const kpt_candidates* candidates,
+                                    const kpt_injection_plan* plan,
+                                    const kpt_injection_kinematics* kinematics);
+/* recycle_particles_uniform / _uniform_if (ParticleGenerator.hpp:1180-1272);
+ * recycled (may be NULL) receives the number of particles rewritten. */
+int kpt_generator_recycle_uniform(kpt_context* ctx, kpt_system* system, uint64_t seed,
+                                  uint32_t frame, const kpt_region* region,
+                                  const kpt_injection_kinematics* kinematics,
+                                  const kpt_field_predicate* predicate, int32_t selection,
+                                  int32_t max_attempts, uint64_t* recycled);
+/* recycle_particles_from_grid_candidates / _from_field_candidates
+ * (ParticleGenerator.hpp:1305-1447). */
+int kpt_generator_recycle_candidates(kpt_context* ctx, kpt_system* system, uint64_t seed,
+                                     uint32_t frame, const kpt_candidates* candidates,
+                                     const kpt_injection_kinematics* kinematics,
+                                     int32_t selection, uint64_t* recycled);
+
+/* ======================================================================
  * Batched runs (no counterpart in the reference, which runs one simulation
  * per process): many independent driver runs -- each with its own particle
  * store, coefficient tables, settings, seed and frame -- pushed by one

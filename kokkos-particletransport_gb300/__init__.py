@@ -146,6 +146,35 @@ class ParticleArrays(ctypes.Structure):
 _LIB: Optional[ctypes.CDLL] = None
 
 
+class Region(ctypes.Structure):
+    """AxisAlignedParticleRegion<2> (ParticleGenerator.hpp:18-62)."""
+    _fields_ = [("lower", ctypes.c_double * 2), ("upper", ctypes.c_double * 2)]
+
+
+class ParticleInjectionKinematics(ctypes.Structure):
+    """Constant state of injected particles (ParticleGenerator.hpp:68-74);
+    status 0 active, 1 escaped, 2 inactive."""
+    _fields_ = [("momentum_magnitude", ctypes.c_double), ("mu", ctypes.c_double),
+                ("weight", ctypes.c_double), ("status", ctypes.c_int32),
+                ("pad", ctypes.c_int32)]
+
+    def __init__(self, momentum_magnitude=0.0, mu=0.0, weight=1.0, status=0):
+        super().__init__(float(momentum_magnitude), float(mu), float(weight), int(status), 0)
+
+
+class ParticleInjectionPlan(ctypes.Structure):
+    """Injection range and rejection-sampling attempts (ParticleGenerator.hpp:107-112)."""
+    _fields_ = [("first_particle_index", ctypes.c_uint64), ("particle_count", ctypes.c_uint64),
+                ("first_particle_id", ctypes.c_uint64), ("max_attempts", ctypes.c_int32),
+                ("pad", ctypes.c_int32)]
+
+
+class _FieldPredicate(ctypes.Structure):
+    _fields_ = [("field", ctypes.c_void_p), ("threshold", ctypes.c_double),
+                ("comparison", ctypes.c_int32), ("component", ctypes.c_int32),
+                ("domain", ctypes.c_int32), ("pad", ctypes.c_int32)]
+
+
 def library_path() -> str:
     return LIB_PATH
 
@@ -241,6 +270,19 @@ def load_library() -> ctypes.CDLL:
         "kpt_focus_advance_stochastic": (i32, [vp, vp, vp, u64, u32, vp]),
         "kpt_focus_advance_deterministic": (i32, [vp, vp, vp, vp]),
         "kpt_focus_advance_stochastic_steps": (i32, [vp, vp, vp, u64, u32, u32, vp]),
+        "kpt_lib_field_create": (i32, [vp, vp, i32, vp, vp, pvp]),
+        "kpt_lib_field_destroy": (i32, [vp]),
+        "kpt_lib_field_points": (i32, [vp, vp]),
+        "kpt_region_from_grid": (i32, [vp, i32, vp]),
+        "kpt_candidates_from_field": (i32, [vp, vp, vp, dbl, i32, i32, i32, pvp]),
+        "kpt_candidates_from_grid": (i32, [vp, vp, i32, pvp]),
+        "kpt_candidates_info": (i32, [vp, vp, vp]),
+        "kpt_candidates_download": (i32, [vp, vp, vp, vp]),
+        "kpt_candidates_destroy": (i32, [vp]),
+        "kpt_generator_inject_uniform": (i32, [vp, vp, u64, u32, vp, vp, vp, vp]),
+        "kpt_generator_inject_candidates": (i32, [vp, vp, u64, u32, vp, vp, vp]),
+        "kpt_generator_recycle_uniform": (i32, [vp, vp, u64, u32, vp, vp, vp, i32, i32, vp]),
+        "kpt_generator_recycle_candidates": (i32, [vp, vp, u64, u32, vp, vp, i32, vp]),
     }
     for name, (restype, argtypes) in sig.items():
         fn = getattr(lib, name)
@@ -498,6 +540,44 @@ class Context:
             solver.set_maximum_mu(maximum_mu)
         return solver
 
+    # -- ParticleGenerator ---------------------------------------------------
+    def lib_field(self, grid: "LibGrid", values, centering=(0, 0)) -> "LibField":
+        """Field<Grid, C> on a library grid: values (points,) or (points, C),
+        points in the field's flattened order (dim 0 fastest over the ghosted
+        extent: cells n+4, faces n+5 per axis); centering 0 cell, 1 face."""
+        values = np.asarray(values, dtype=np.float64)
+        comps = 1 if values.ndim == 1 else values.shape[1]
+        values = np.ascontiguousarray(values.reshape(-1, comps))
+        cent = np.ascontiguousarray([_centering(c) for c in centering], dtype=np.int32)
+        want = 1
+        for n, c in zip((grid.nx, grid.ny), cent):
+            want *= n + 4 + int(c)
+        if values.shape[0] != want:
+            raise ValueError(f"field needs {want} points for this grid and centering")
+        handle = ctypes.c_void_p()
+        _check(self.lib.kpt_lib_field_create(self.handle, grid.handle, comps, _ptr(cent),
+                                             _ptr(values), ctypes.byref(handle)))
+        return self._adopt(LibField(self, handle, grid, comps, tuple(int(c) for c in cent)))
+
+    def make_field_particle_candidate_set(self, field: "LibField", threshold: float,
+                                          comparison="greater_equal", component: int = 0,
+                                          domain=0, region: Optional[Region] = None
+                                          ) -> "CandidateSet":
+        """make_field_particle_candidate_set[_in_region] (ParticleGenerator.hpp:659-784)."""
+        handle = ctypes.c_void_p()
+        _check(self.lib.kpt_candidates_from_field(
+            self.handle, field.handle, None if region is None else ctypes.byref(region),
+            float(threshold), _comparison(comparison), int(component), _domain(domain),
+            ctypes.byref(handle)))
+        return self._adopt(CandidateSet(self, handle, "field"))
+
+    def make_grid_particle_candidate_set(self, grid: "LibGrid", domain=0) -> "CandidateSet":
+        """make_grid_particle_candidate_set (ParticleGenerator.hpp:786-856)."""
+        handle = ctypes.c_void_p()
+        _check(self.lib.kpt_candidates_from_grid(self.handle, grid.handle, _domain(domain),
+                                                 ctypes.byref(handle)))
+        return self._adopt(CandidateSet(self, handle, "grid"))
+
     def sample(self, lower: "Field", upper: "Field", x, y, rt,
                time_interpolation: int = 1) -> np.ndarray:
         x = np.ascontiguousarray(x, dtype=np.float64)
@@ -692,6 +772,50 @@ class ParticleSystem(_Handle):
         _check(self.ctx.lib.kpt_system_reset_split_baselines(self.ctx.handle, self.handle))
 
 
+class LibField(_Handle):
+    """Lattice field on a library grid (kpt_lib_field, reference Field<Grid, C>)."""
+    _destroy = "kpt_lib_field_destroy"
+
+    def __init__(self, ctx, handle, grid, components, centering):
+        super().__init__(ctx, handle)
+        self.grid = grid
+        self.components = components
+        self.centering = centering
+
+
+class CandidateSet(_Handle):
+    """Field-point or grid-cell candidate set with cumulative physical-volume
+    weights (kpt_candidates, ParticleGenerator.hpp:464-646)."""
+    _destroy = "kpt_candidates_destroy"
+
+    def __init__(self, ctx, handle, kind):
+        super().__init__(ctx, handle)
+        self.kind = kind
+
+    def candidate_count(self) -> int:
+        n = ctypes.c_uint64()
+        _check(self.ctx.lib.kpt_candidates_info(self.handle, ctypes.byref(n), None))
+        return int(n.value)
+
+    def total_weight(self) -> float:
+        t = ctypes.c_double()
+        _check(self.ctx.lib.kpt_candidates_info(self.handle, None, ctypes.byref(t)))
+        return float(t.value)
+
+    def empty(self) -> bool:
+        return self.candidate_count() == 0
+
+    def download(self):
+        """(point indices or cell ordinals, cumulative weights)."""
+        n = self.candidate_count()
+        idx = np.zeros(n, dtype=np.uint64)
+        cum = np.zeros(n, dtype=np.float64)
+        if n:
+            _check(self.ctx.lib.kpt_candidates_download(self.ctx.handle, self.handle, _ptr(idx),
+                                                        _ptr(cum)))
+        return idx, cum
+
+
 class ParkerSolver(_Handle):
     """Header-library Parker solver (kpt_parker_solver, reference ParkerSolver)."""
     _destroy = "kpt_parker_solver_destroy"
@@ -883,6 +1007,207 @@ class ParticleStorage:
         arr = ParticleArrays()
         _check(self.ctx.lib.kpt_particles_device_arrays(self.handle, ctypes.byref(arr)))
         return {name: getattr(arr, name) for name, _ in ParticleArrays._fields_}
+
+
+# ---- ParticleGenerator (ParticleGenerator.hpp) ---------------------------------
+
+COMPARISONS = {"greater": 0, "greater_equal": 1, "less": 2, "less_equal": 3,
+               "abs_greater": 4, "abs_less": 5}
+RECYCLE_SELECTIONS = {"escaped_only": 0, "inactive_only": 1, "recyclable": 2}
+DOMAINS = {"physical": 0, "ghosted": 1}
+
+
+def _comparison(value) -> int:
+    return COMPARISONS[value] if isinstance(value, str) else int(value)
+
+
+def _selection(value) -> int:
+    return RECYCLE_SELECTIONS[value] if isinstance(value, str) else int(value)
+
+
+def _domain(value) -> int:
+    return DOMAINS[value] if isinstance(value, str) else int(value)
+
+
+def _centering(value) -> int:
+    if isinstance(value, str):
+        return {"cell": 0, "face": 1}[value]
+    return int(value)
+
+
+class RandomManager:
+    """Noise source of the generator calls (RandomManager.hpp): the seed and
+    the frame that key every particle slot's stream, so results are the same
+    for any thread schedule."""
+
+    def __init__(self, seed: int = 114514, frame: int = 0):
+        self.seed = int(seed)
+        self.frame = int(frame)
+
+
+class FieldThresholdParticlePredicate:
+    """make_field_threshold_particle_predicate (ParticleGenerator.hpp:360-369)."""
+
+    def __init__(self, field: LibField, threshold: float, comparison="greater_equal",
+                 component: int = 0, domain=0):
+        self.field = field
+        self.struct = _FieldPredicate(field.handle.value, float(threshold),
+                                      _comparison(comparison), int(component), _domain(domain), 0)
+
+
+def make_field_threshold_particle_predicate(field, threshold, comparison="greater_equal",
+                                            component=0, domain=0):
+    return FieldThresholdParticlePredicate(field, threshold, comparison, component, domain)
+
+
+def make_particle_region(lower, upper) -> Region:
+    """make_particle_region (ParticleGenerator.hpp:196-203)."""
+    r = Region((ctypes.c_double * 2)(*map(float, lower)), (ctypes.c_double * 2)(*map(float, upper)))
+    for dim in range(2):
+        if not (np.isfinite(r.lower[dim]) and np.isfinite(r.upper[dim])
+                and r.upper[dim] > r.lower[dim]):
+            raise KptError("AxisAlignedParticleRegion: bounds must be finite and ascending.")
+    return r
+
+
+def make_particle_region_from_grid(grid: LibGrid, domain=0) -> Region:
+    """make_particle_region_from_grid (ParticleGenerator.hpp:208-226)."""
+    r = Region()
+    _check(grid.ctx.lib.kpt_region_from_grid(grid.handle, _domain(domain), ctypes.byref(r)))
+    return r
+
+
+def make_particle_injection_plan(first_particle_index: int, particle_count: int,
+                                 max_attempts: int = 64) -> ParticleInjectionPlan:
+    """make_particle_injection_plan (ParticleGenerator.hpp:169-179)."""
+    return ParticleInjectionPlan(int(first_particle_index), int(particle_count),
+                                 int(first_particle_index), int(max_attempts), 0)
+
+
+def make_particle_append_plan(system: ParticleSystem, particle_count: int,
+                              max_attempts: int = 64) -> ParticleInjectionPlan:
+    """make_particle_append_plan (ParticleGenerator.hpp:183-191)."""
+    return make_particle_injection_plan(system.count, particle_count, max_attempts)
+
+
+def _kin(kinematics) -> ParticleInjectionKinematics:
+    return ParticleInjectionKinematics() if kinematics is None else kinematics
+
+
+def inject_particles_uniform_if(system: ParticleSystem, random: RandomManager, region: Region,
+                                plan: ParticleInjectionPlan, kinematics=None,
+                                predicate: Optional[FieldThresholdParticlePredicate] = None
+                                ) -> None:
+    """inject_particles_uniform_if (ParticleGenerator.hpp:885-960); no
+    predicate = AlwaysAcceptParticlePredicate."""
+    lib = system.ctx.lib
+    _check(lib.kpt_generator_inject_uniform(
+        system.ctx.handle, system.handle, random.seed, random.frame, ctypes.byref(region),
+        ctypes.byref(plan), ctypes.byref(_kin(kinematics)),
+        None if predicate is None else ctypes.byref(predicate.struct)))
+
+
+def inject_particles_uniform(system, random, region, plan, kinematics=None) -> None:
+    """inject_particles_uniform (ParticleGenerator.hpp:1106-1119)."""
+    inject_particles_uniform_if(system, random, region, plan, kinematics, None)
+
+
+def inject_particles_from_field_candidates(system: ParticleSystem, random: RandomManager,
+                                           candidates: CandidateSet,
+                                           plan: ParticleInjectionPlan, kinematics=None) -> None:
+    """inject_particles_from_field_candidates (ParticleGenerator.hpp:962-1032)."""
+    _check(system.ctx.lib.kpt_generator_inject_candidates(
+        system.ctx.handle, system.handle, random.seed, random.frame, candidates.handle,
+        ctypes.byref(plan), ctypes.byref(_kin(kinematics))))
+
+
+inject_particles_from_grid_candidates = inject_particles_from_field_candidates
+
+
+def inject_particles_uniform_in_grid(system, random, grid: LibGrid, plan, kinematics=None,
+                                     domain=0) -> None:
+    """inject_particles_uniform_in_grid (ParticleGenerator.hpp:1121-1137)."""
+    candidates = system.ctx.make_grid_particle_candidate_set(grid, domain)
+    try:
+        inject_particles_from_field_candidates(system, random, candidates, plan, kinematics)
+    finally:
+        candidates.close()
+
+
+def inject_particles_uniform_where_field(system, random, plan, kinematics, field: LibField,
+                                         threshold: float, comparison="greater_equal",
+                                         component: int = 0, domain=0,
+                                         region: Optional[Region] = None) -> None:
+    """inject_particles_uniform_where_field, both overloads
+    (ParticleGenerator.hpp:1139-1184): region None = the grid's domain."""
+    candidates = system.ctx.make_field_particle_candidate_set(field, threshold, comparison,
+                                                              component, domain, region)
+    try:
+        inject_particles_from_field_candidates(system, random, candidates, plan, kinematics)
+    finally:
+        candidates.close()
+
+
+def recycle_particles_uniform_if(system: ParticleSystem, random: RandomManager, region: Region,
+                                 kinematics=None, predicate=None, selection="escaped_only",
+                                 max_attempts: int = 64) -> int:
+    """recycle_particles_uniform_if (ParticleGenerator.hpp:1186-1258); returns
+    how many particles were rewritten."""
+    n = ctypes.c_uint64()
+    _check(system.ctx.lib.kpt_generator_recycle_uniform(
+        system.ctx.handle, system.handle, random.seed, random.frame, ctypes.byref(region),
+        ctypes.byref(_kin(kinematics)),
+        None if predicate is None else ctypes.byref(predicate.struct), _selection(selection),
+        int(max_attempts), ctypes.byref(n)))
+    return int(n.value)
+
+
+def recycle_particles_uniform(system, random, region, kinematics=None,
+                              selection="escaped_only") -> int:
+    """recycle_particles_uniform (ParticleGenerator.hpp:1260-1272)."""
+    return recycle_particles_uniform_if(system, random, region, kinematics, None, selection)
+
+
+def recycle_particles_from_field_candidates(system: ParticleSystem, random: RandomManager,
+                                            candidates: CandidateSet, kinematics=None,
+                                            selection="escaped_only") -> int:
+    """recycle_particles_from_field_candidates / _from_grid_candidates
+    (ParticleGenerator.hpp:1305-1447)."""
+    n = ctypes.c_uint64()
+    _check(system.ctx.lib.kpt_generator_recycle_candidates(
+        system.ctx.handle, system.handle, random.seed, random.frame, candidates.handle,
+        ctypes.byref(_kin(kinematics)), _selection(selection), ctypes.byref(n)))
+    return int(n.value)
+
+
+recycle_particles_from_grid_candidates = recycle_particles_from_field_candidates
+
+
+def recycle_particles_uniform_in_grid(system, random, grid: LibGrid, kinematics=None,
+                                      selection="escaped_only", domain=0) -> int:
+    """recycle_particles_uniform_in_grid (ParticleGenerator.hpp:1283-1299)."""
+    candidates = system.ctx.make_grid_particle_candidate_set(grid, domain)
+    try:
+        return recycle_particles_from_field_candidates(system, random, candidates, kinematics,
+                                                       selection)
+    finally:
+        candidates.close()
+
+
+def recycle_particles_uniform_where_field(system, random, kinematics, field: LibField,
+                                          threshold: float, comparison="greater_equal",
+                                          component: int = 0, domain=0,
+                                          selection="escaped_only",
+                                          region: Optional[Region] = None) -> int:
+    """recycle_particles_uniform_where_field, both overloads
+    (ParticleGenerator.hpp:1449-1493)."""
+    candidates = system.ctx.make_field_particle_candidate_set(field, threshold, comparison,
+                                                              component, domain, region)
+    try:
+        return recycle_particles_from_field_candidates(system, random, candidates, kinematics,
+                                                       selection)
+    finally:
+        candidates.close()
 
 
 def header_functions(path: str = HEADER_PATH) -> Sequence[str]:

@@ -2590,6 +2590,457 @@ int kpt_focus_advance_stochastic_steps(kpt_context* ctx, kpt_focus_solver* s, kp
 }  // extern "C"
 
 // ====================================================================
+// ParticleGenerator: injection and recycling on the library grid
+// ====================================================================
+
+struct kpt_lib_field {
+    kpt_context* ctx = nullptr;
+    int device = 0;
+    kpt::LibGrid grid{};
+    int components = 0;
+    int centering[2] = {0, 0};
+    int ext[2] = {0, 0};
+    uint64_t points = 0;
+    double* values = nullptr;
+    ~kpt_lib_field() {
+        if (values) cudaFree(values);
+    }
+};
+
+struct kpt_candidates {
+    kpt_context* ctx = nullptr;
+    int device = 0;
+    kpt::LibGrid grid{};
+    kpt::GenCandidates view{};
+    DeviceBuffer indices, cumulative;
+};
+
+namespace {
+
+kpt::GenField gen_field_view(const kpt_lib_field* f) {
+    kpt::GenField v{};
+    v.values = f->values;
+    v.components = f->components;
+    for (int dim = 0; dim < 2; ++dim) {
+        v.centering[dim] = f->centering[dim];
+        v.ext[dim] = f->ext[dim];
+    }
+    return v;
+}
+
+// AxisAlignedParticleRegion::validate (ParticleGenerator.hpp:27-36).
+int validate_region(const kpt_region* r) {
+    for (int dim = 0; dim < 2; ++dim) {
+        KPT_REQUIRE(std::isfinite(r->lower[dim]) && std::isfinite(r->upper[dim]) &&
+                        r->upper[dim] > r->lower[dim],
+                    "AxisAlignedParticleRegion: bounds must be finite and ascending.");
+    }
+    return KPT_OK;
+}
+
+// validate_particle_injection_kinematics (ParticleGenerator.hpp:89-103).
+int validate_kinematics(const kpt_injection_kinematics* k) {
+    KPT_REQUIRE(std::isfinite(k->mu) && std::isfinite(k->weight) && k->weight > 0.0,
+                "ParticleInjectionKinematics: mu must be finite and weight must be positive.");
+    KPT_REQUIRE(std::isfinite(k->momentum_magnitude) && k->momentum_magnitude >= 0.0,
+                "ParticleInjectionKinematics: momentum magnitude must be finite and "
+                "non-negative.");
+    KPT_REQUIRE(k->status >= 0 && k->status <= 2,
+                "ParticleInjectionKinematics: status must be a ParticleStatus value");
+    return KPT_OK;
+}
+
+// validate_particle_injection_plan (ParticleGenerator.hpp:860-881).
+int validate_plan(const kpt_system* sys, const kpt_injection_plan* plan) {
+    KPT_REQUIRE(plan->max_attempts > 0, "ParticleInjectionPlan: max_attempts must be positive.");
+    KPT_REQUIRE(plan->first_particle_index <= sys->count,
+                "ParticleInjectionPlan: first index is out of range.");
+    KPT_REQUIRE(plan->first_particle_index <= sys->capacity,
+                "ParticleInjectionPlan: first index exceeds capacity.");
+    KPT_REQUIRE(plan->particle_count <= sys->capacity - plan->first_particle_index,
+                "ParticleInjectionPlan: requested range exceeds capacity.");
+    return KPT_OK;
+}
+
+int gen_common(kpt_context* ctx, kpt_system* sys, kpt::GenLaunch& L, uint64_t seed,
+               uint32_t frame, const kpt_injection_kinematics* k) {
+    L.sys = sys->a;
+    L.momentum = k->momentum_magnitude;
+    L.mu = k->mu;
+    L.weight = k->weight;
+    L.status = k->status;
+    L.rest_mass = sys->props.rest_mass;
+    L.speed_of_light = sys->props.speed_of_light;
+    L.mc = sys->props.rest_mass * sys->props.speed_of_light;
+    L.key = make_uint2(static_cast<uint32_t>(seed), static_cast<uint32_t>(seed >> 32));
+    L.frame = frame;
+    (void)ctx;
+    return KPT_OK;
+}
+
+int gen_predicate(const kpt_field_predicate* p, const kpt_grid* grid_or_null,
+                  kpt::GenPredicate* out) {
+    *out = kpt::GenPredicate{};
+    if (p == nullptr) return KPT_OK;
+    KPT_REQUIRE(p->field != nullptr, "kpt_field_predicate: field is NULL");
+    KPT_REQUIRE(p->component >= 0 && p->component < p->field->components,
+                "FieldThresholdParticlePredicate: component index is out of range.");
+    KPT_REQUIRE(p->comparison >= 0 && p->comparison <= 5,
+                "kpt_field_predicate: unknown comparison");
+    KPT_REQUIRE(p->domain == 0 || p->domain == 1, "kpt_field_predicate: unknown domain");
+    (void)grid_or_null;
+    out->enabled = 1;
+    out->field = gen_field_view(p->field);
+    out->threshold = p->threshold;
+    out->comparison = p->comparison;
+    out->component = p->component;
+    out->domain = p->domain;
+    return KPT_OK;
+}
+
+int gen_finish(kpt_context* ctx, kpt_system* sys, kpt::GenLaunch& L, uint64_t* recycled) {
+    DeviceBuffer& counter = sys->scalars;
+    if (L.recycle) {
+        KPT_CUDA(counter.reserve(64));
+        L.recycled = counter.as<unsigned long long>();
+    }
+    KPT_CUDA(kpt::generator_run(L, ctx->stream));
+    if (L.recycle) {
+        unsigned long long n = 0;
+        KPT_CUDA(cudaMemcpyAsync(&n, L.recycled, sizeof(n), cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+        KPT_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (recycled) *recycled = n;
+    } else {
+        // commit_particle_range (ParticleSystem.hpp:474-491)
+        const uint64_t end = L.first_index + L.count;
+        if (L.count > 0 && end > sys->count) sys->count = end;
+    }
+    return KPT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int kpt_lib_field_create(kpt_context* ctx, const kpt_grid* grid, int32_t components,
+                         const int32_t centering[2], const double* values,
+                         kpt_lib_field** out) {
+    KPT_REQUIRE(ctx && grid && centering && values && out, "kpt_lib_field_create: NULL argument");
+    *out = nullptr;
+    KPT_REQUIRE(components > 0 && components <= 64,
+                "kpt_lib_field_create: components must be in [1, 64]");
+    KPT_REQUIRE((centering[0] == 0 || centering[0] == 1) &&
+                    (centering[1] == 0 || centering[1] == 1),
+                "kpt_lib_field_create: centering must be 0 (cell) or 1 (face)");
+    if (int rc = activate(ctx)) return rc;
+    std::unique_ptr<kpt_lib_field> f(new kpt_lib_field());
+    f->ctx = ctx;
+    f->device = ctx->device;
+    f->grid = grid->g;
+    f->components = components;
+    const int n[2] = {grid->nx, grid->ny};
+    f->points = 1;
+    for (int dim = 0; dim < 2; ++dim) {
+        f->centering[dim] = centering[dim];
+        // Field::compute_extents: ghosted cells n+4, faces n+5
+        f->ext[dim] = n[dim] + 4 + (centering[dim] != 0 ? 1 : 0);
+        f->points *= static_cast<uint64_t>(f->ext[dim]);
+    }
+    const size_t bytes = f->points * static_cast<size_t>(components) * sizeof(double);
+    KPT_CUDA(cudaMalloc(&f->values, bytes));
+    KPT_CUDA(cudaMemcpyAsync(f->values, values, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    KPT_CUDA(cudaStreamSynchronize(ctx->stream));
+    *out = f.release();
+    return KPT_OK;
+}
+
+int kpt_lib_field_destroy(kpt_lib_field* field) {
+    delete field;
+    return KPT_OK;
+}
+
+int kpt_lib_field_points(const kpt_lib_field* field, uint64_t* points) {
+    KPT_REQUIRE(field && points, "kpt_lib_field_points: NULL argument");
+    *points = field->points;
+    return KPT_OK;
+}
+
+int kpt_region_from_grid(const kpt_grid* grid, int32_t domain, kpt_region* out) {
+    KPT_REQUIRE(grid && out, "kpt_region_from_grid: NULL argument");
+    KPT_REQUIRE(domain == 0 || domain == 1, "kpt_region_from_grid: unknown domain");
+    for (int dim = 0; dim < 2; ++dim) {
+        const kpt::LibAxis& a = grid->g.axis[dim];
+        out->lower[dim] = domain != 0 ? a.ghost_lower : a.lower;
+        out->upper[dim] = domain != 0 ? a.ghost_upper : a.upper;
+    }
+    return validate_region(out);
+}
+
+int kpt_candidates_from_field(kpt_context* ctx, const kpt_lib_field* field,
+                              const kpt_region* region, double threshold, int32_t comparison,
+                              int32_t component, int32_t domain, kpt_candidates** out) {
+    KPT_REQUIRE(ctx && field && out, "kpt_candidates_from_field: NULL argument");
+    *out = nullptr;
+    KPT_REQUIRE(component >= 0 && component < field->components,
+                "Field particle injection: component index is out of range.");
+    KPT_REQUIRE(comparison >= 0 && comparison <= 5,
+                "kpt_candidates_from_field: unknown comparison");
+    KPT_REQUIRE(domain == 0 || domain == 1, "kpt_candidates_from_field: unknown domain");
+    kpt_region whole{};
+    if (region == nullptr) {
+        for (int dim = 0; dim < 2; ++dim) {
+            const kpt::LibAxis& a = field->grid.axis[dim];
+            whole.lower[dim] = domain != 0 ? a.ghost_lower : a.lower;
+            whole.upper[dim] = domain != 0 ? a.ghost_upper : a.upper;
+        }
+        region = &whole;
+    }
+    if (int rc = validate_region(region)) return rc;
+    if (int rc = activate(ctx)) return rc;
+    std::unique_ptr<kpt_candidates> c(new kpt_candidates());
+    c->ctx = ctx;
+    c->device = ctx->device;
+    c->grid = field->grid;
+    const uint64_t points = field->points;
+    KPT_CUDA(c->indices.reserve(points * sizeof(uint64_t)));
+    DeviceBuffer block_counts, scratch;
+    const uint64_t blocks = (points + 255) / 256;
+    KPT_CUDA(block_counts.reserve(blocks * sizeof(unsigned int) + sizeof(unsigned long long) * 2));
+    kpt::GenCandidateBuild B{};
+    B.grid = field->grid;
+    B.field = gen_field_view(field);
+    for (int dim = 0; dim < 2; ++dim) {
+        B.region_lo[dim] = region->lower[dim];
+        B.region_hi[dim] = region->upper[dim];
+    }
+    B.threshold = threshold;
+    B.comparison = comparison;
+    B.component = component;
+    B.domain = domain;
+    B.points = points;
+    B.indices = c->indices.as<uint64_t>();
+    B.block_counts = block_counts.as<unsigned int>();
+    B.count_out = reinterpret_cast<unsigned long long*>(
+        static_cast<char*>(block_counts.ptr) +
+        ((blocks * sizeof(unsigned int) + 7) / 8) * 8);
+    KPT_CUDA(kpt::generator_field_candidates(B, ctx->stream));
+    unsigned long long count = 0;
+    KPT_CUDA(cudaMemcpyAsync(&count, B.count_out, sizeof(count), cudaMemcpyDeviceToHost,
+                             ctx->stream));
+    KPT_CUDA(cudaStreamSynchronize(ctx->stream));
+    double total = 0.0;
+    if (count > 0) {
+        KPT_CUDA(c->cumulative.reserve(count * sizeof(double)));
+        KPT_CUDA(scratch.reserve(kpt::generator_scan_scratch(count) * sizeof(double)));
+        B.cumulative = c->cumulative.as<double>();
+        B.block_sums = scratch.as<double>();
+        KPT_CUDA(kpt::generator_field_weights(B, count, ctx->stream));
+        KPT_CUDA(cudaMemcpyAsync(&total, B.cumulative + (count - 1), sizeof(double),
+                                 cudaMemcpyDeviceToHost, ctx->stream));
+        KPT_CUDA(cudaStreamSynchronize(ctx->stream));
+        KPT_REQUIRE(std::isfinite(total) && total > 0.0,
+                    "Field particle candidate set: total physical volume must be positive.");
+    }
+    kpt::GenCandidates& v = c->view;
+    v.kind = 0;
+    v.indices = c->indices.as<uint64_t>();
+    v.cumulative = count > 0 ? c->cumulative.as<double>() : nullptr;
+    v.count = count;
+    v.total = total;
+    v.field = B.field;
+    v.field.values = nullptr;  // the candidate set needs the layout, not the values
+    *out = c.release();
+    return KPT_OK;
+}
+
+int kpt_candidates_from_grid(kpt_context* ctx, const kpt_grid* grid, int32_t domain,
+                             kpt_candidates** out) {
+    KPT_REQUIRE(ctx && grid && out, "kpt_candidates_from_grid: NULL argument");
+    *out = nullptr;
+    KPT_REQUIRE(domain == 0 || domain == 1, "kpt_candidates_from_grid: unknown domain");
+    if (int rc = activate(ctx)) return rc;
+    std::unique_ptr<kpt_candidates> c(new kpt_candidates());
+    c->ctx = ctx;
+    c->device = ctx->device;
+    c->grid = grid->g;
+    kpt::GenCandidates& v = c->view;
+    v.kind = 1;
+    uint64_t count = 1;
+    const int n[2] = {grid->nx, grid->ny};
+    for (int dim = 0; dim < 2; ++dim) {
+        v.lower[dim] = domain != 0 ? -2 : 0;
+        const int upper = domain != 0 ? n[dim] + 1 : n[dim] - 1;
+        v.extents[dim] = upper - v.lower[dim] + 1;
+        KPT_REQUIRE(v.extents[dim] > 0, "Grid particle candidate set: grid domain has no cells.");
+        count *= static_cast<uint64_t>(v.extents[dim]);
+    }
+    KPT_CUDA(c->cumulative.reserve(count * sizeof(double)));
+    DeviceBuffer scratch;
+    KPT_CUDA(scratch.reserve(kpt::generator_scan_scratch(count) * sizeof(double)));
+    KPT_CUDA(kpt::generator_grid_weights(grid->g, v.lower, v.extents, count,
+                                         c->cumulative.as<double>(), scratch.as<double>(),
+                                         ctx->stream));
+    double total = 0.0;
+    KPT_CUDA(cudaMemcpyAsync(&total, c->cumulative.as<double>() + (count - 1), sizeof(double),
+                             cudaMemcpyDeviceToHost, ctx->stream));
+    KPT_CUDA(cudaStreamSynchronize(ctx->stream));
+    KPT_REQUIRE(std::isfinite(total) && total > 0.0,
+                "Grid particle candidate set: total physical volume must be positive.");
+    v.cumulative = c->cumulative.as<double>();
+    v.count = count;
+    v.total = total;
+    *out = c.release();
+    return KPT_OK;
+}
+
+int kpt_candidates_info(const kpt_candidates* c, uint64_t* count, double* total_weight) {
+    KPT_REQUIRE(c, "kpt_candidates_info: NULL handle");
+    if (count) *count = c->view.count;
+    if (total_weight) *total_weight = c->view.total;
+    return KPT_OK;
+}
+
+int kpt_candidates_download(kpt_context* ctx, const kpt_candidates* c, uint64_t* indices,
+                            double* cumulative_weights) {
+    KPT_REQUIRE(ctx && c, "kpt_candidates_download: NULL handle");
+    if (int rc = activate(ctx)) return rc;
+    const uint64_t n = c->view.count;
+    if (n == 0) return KPT_OK;
+    if (indices) {
+        if (c->view.kind == 0) {
+            KPT_CUDA(cudaMemcpyAsync(indices, c->view.indices, n * sizeof(uint64_t),
+                                     cudaMemcpyDeviceToHost, ctx->stream));
+        } else {
+            for (uint64_t k = 0; k < n; ++k) indices[k] = k;
+        }
+    }
+    if (cumulative_weights) {
+        KPT_CUDA(cudaMemcpyAsync(cumulative_weights, c->view.cumulative, n * sizeof(double),
+                                 cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    KPT_CUDA(cudaStreamSynchronize(ctx->stream));
+    return KPT_OK;
+}
+
+int kpt_candidates_destroy(kpt_candidates* candidates) {
+    delete candidates;
+    return KPT_OK;
+}
+
+int kpt_generator_inject_uniform(kpt_context* ctx, kpt_system* sys, uint64_t seed,
+                                 uint32_t frame, const kpt_region* region,
+                                 const kpt_injection_plan* plan,
+                                 const kpt_injection_kinematics* kinematics,
+                                 const kpt_field_predicate* predicate) {
+    KPT_REQUIRE(ctx && sys && region && plan && kinematics,
+                "kpt_generator_inject_uniform: NULL argument");
+    if (int rc = validate_region(region)) return rc;
+    if (int rc = validate_kinematics(kinematics)) return rc;
+    if (int rc = validate_plan(sys, plan)) return rc;
+    kpt::GenLaunch L{};
+    if (int rc = gen_predicate(predicate, nullptr, &L.predicate)) return rc;
+    if (int rc = activate(ctx)) return rc;
+    gen_common(ctx, sys, L, seed, frame, kinematics);
+    if (predicate) L.grid = predicate->field->grid;
+    L.recycle = 0;
+    L.source = 0;
+    for (int dim = 0; dim < 2; ++dim) {
+        L.region_lo[dim] = region->lower[dim];
+        L.region_hi[dim] = region->upper[dim];
+    }
+    L.first_index = plan->first_particle_index;
+    L.count = plan->particle_count;
+    L.first_id = plan->first_particle_id;
+    L.max_attempts = plan->max_attempts;
+    return gen_finish(ctx, sys, L, nullptr);
+}
+
+int kpt_generator_inject_candidates(kpt_context* ctx, kpt_system* sys, uint64_t seed,
+                                    uint32_t frame, const kpt_candidates* candidates,
+                                    const kpt_injection_plan* plan,
+                                    const kpt_injection_kinematics* kinematics) {
+    KPT_REQUIRE(ctx && sys && candidates && plan && kinematics,
+                "kpt_generator_inject_candidates: NULL argument");
+    if (int rc = validate_kinematics(kinematics)) return rc;
+    if (int rc = validate_plan(sys, plan)) return rc;
+    KPT_REQUIRE(candidates->view.count > 0,
+                candidates->view.kind == 0
+                    ? "ParticleGenerator: field-conditioned injection has no candidate grid "
+                      "points."
+                    : "ParticleGenerator: grid injection has no candidate cells.");
+    if (int rc = activate(ctx)) return rc;
+    kpt::GenLaunch L{};
+    gen_common(ctx, sys, L, seed, frame, kinematics);
+    L.grid = candidates->grid;
+    L.recycle = 0;
+    L.source = 1;
+    L.candidates = candidates->view;
+    L.first_index = plan->first_particle_index;
+    L.count = plan->particle_count;
+    L.first_id = plan->first_particle_id;
+    L.max_attempts = plan->max_attempts;
+    return gen_finish(ctx, sys, L, nullptr);
+}
+
+int kpt_generator_recycle_uniform(kpt_context* ctx, kpt_system* sys, uint64_t seed,
+                                  uint32_t frame, const kpt_region* region,
+                                  const kpt_injection_kinematics* kinematics,
+                                  const kpt_field_predicate* predicate, int32_t selection,
+                                  int32_t max_attempts, uint64_t* recycled) {
+    KPT_REQUIRE(ctx && sys && region && kinematics,
+                "kpt_generator_recycle_uniform: NULL argument");
+    if (recycled) *recycled = 0;
+    if (int rc = validate_region(region)) return rc;
+    if (int rc = validate_kinematics(kinematics)) return rc;
+    KPT_REQUIRE(max_attempts > 0, "ParticleGenerator: recycle max_attempts must be positive.");
+    KPT_REQUIRE(selection >= 0 && selection <= 2, "kpt_generator_recycle_uniform: unknown selection");
+    kpt::GenLaunch L{};
+    if (int rc = gen_predicate(predicate, nullptr, &L.predicate)) return rc;
+    if (int rc = activate(ctx)) return rc;
+    gen_common(ctx, sys, L, seed, frame, kinematics);
+    if (predicate) L.grid = predicate->field->grid;
+    L.recycle = 1;
+    L.source = 0;
+    for (int dim = 0; dim < 2; ++dim) {
+        L.region_lo[dim] = region->lower[dim];
+        L.region_hi[dim] = region->upper[dim];
+    }
+    L.count = sys->count;
+    L.selection = selection;
+    L.max_attempts = max_attempts;
+    return gen_finish(ctx, sys, L, recycled);
+}
+
+int kpt_generator_recycle_candidates(kpt_context* ctx, kpt_system* sys, uint64_t seed,
+                                     uint32_t frame, const kpt_candidates* candidates,
+                                     const kpt_injection_kinematics* kinematics,
+                                     int32_t selection, uint64_t* recycled) {
+    KPT_REQUIRE(ctx && sys && candidates && kinematics,
+                "kpt_generator_recycle_candidates: NULL argument");
+    if (recycled) *recycled = 0;
+    if (int rc = validate_kinematics(kinematics)) return rc;
+    KPT_REQUIRE(candidates->view.count > 0,
+                candidates->view.kind == 0
+                    ? "ParticleGenerator: field-conditioned recycling has no candidate grid "
+                      "points."
+                    : "ParticleGenerator: grid recycling has no candidate cells.");
+    KPT_REQUIRE(selection >= 0 && selection <= 2, "kpt_generator_recycle_candidates: unknown selection");
+    if (int rc = activate(ctx)) return rc;
+    kpt::GenLaunch L{};
+    gen_common(ctx, sys, L, seed, frame, kinematics);
+    L.grid = candidates->grid;
+    L.recycle = 1;
+    L.source = 1;
+    L.candidates = candidates->view;
+    L.count = sys->count;
+    L.selection = selection;
+    return gen_finish(ctx, sys, L, recycled);
+}
+
+}  // extern "C"
+
+// ====================================================================
 // Batched runs: many independent driver runs pushed by one launch
 // ====================================================================
 

@@ -14,7 +14,7 @@ namespace kpt {
 // Philox4x32-10 (Salmon et al., SC'11).  Stream layout: key = seed halves,
 // counter = (block, index, frame, tag); draw n uses block n/2, words
 // 2(n%2) (low) and 2(n%2)+1 (high).
-enum : uint32_t { kTagInject = 1u, kTagPush = 2u, kTagLibrary = 3u };
+enum : uint32_t { kTagInject = 1u, kTagPush = 2u, kTagLibrary = 3u, kTagGenerator = 4u };
 
 __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
 #pragma unroll

@@ -312,6 +312,82 @@ cudaError_t system_capture(const SystemArrays& s, uint64_t capacity, cudaStream_
 cudaError_t system_compact_keys(const SystemArrays& s, uint64_t count,
                                 unsigned long long* active, cudaStream_t stream);
 
+// ParticleGenerator (ParticleGenerator.hpp): a lattice field on the library
+// grid (Field.hpp:33-215): `components` doubles per stored point, dim 0
+// fastest over the ghosted extent of the field's centering (cells n+4,
+// faces n+5; logical index -2 first).
+struct GenField {
+    const double* values;
+    int components;
+    int centering[2];  // 0 cell centred, 1 face centred
+    int ext[2];
+};
+
+// FieldThresholdParticlePredicate (ParticleGenerator.hpp:255-358).
+struct GenPredicate {
+    int enabled;  // 0: AlwaysAcceptParticlePredicate
+    GenField field;
+    double threshold;
+    int comparison, component, domain;
+};
+
+// Field or grid candidate set (ParticleGenerator.hpp:464-646).
+struct GenCandidates {
+    int kind;                    // 0 field points, 1 grid cells
+    const uint64_t* indices;     // field point indices (kind 0)
+    const double* cumulative;    // cumulative physical-volume weights
+    uint64_t count;
+    double total;
+    int lower[2], extents[2];    // grid cells (kind 1)
+    GenField field;              // centering and extents (kind 0)
+};
+
+struct GenLaunch {
+    LibGrid grid;
+    SystemArrays sys;
+    int recycle;                 // 0 inject over a plan, 1 recycle selected particles
+    int source;                  // 0 region sampling with predicate, 1 candidates
+    double region_lo[2], region_hi[2];
+    GenPredicate predicate;
+    GenCandidates candidates;
+    uint64_t first_index, count, first_id;  // inject: plan; recycle: count = particle count
+    int max_attempts;
+    int selection;               // ParticleRecycleSelection
+    double momentum, mu, weight;
+    int status;
+    double rest_mass, speed_of_light, mc;
+    uint2 key;
+    uint32_t frame;
+    unsigned long long* recycled;  // particles written by a recycle call
+};
+cudaError_t generator_run(const GenLaunch& launch, cudaStream_t stream);
+
+// Field candidates: stable compaction of the points passing the predicate
+// inside the region, then their cumulative cell volumes.  count_out is a
+// device word; block_counts holds one entry per 256 points.
+struct GenCandidateBuild {
+    LibGrid grid;
+    GenField field;
+    double region_lo[2], region_hi[2];
+    double threshold;
+    int comparison, component, domain;
+    uint64_t points;
+    uint64_t* indices;           // points (upper bound)
+    double* cumulative;          // points (upper bound)
+    unsigned int* block_counts;  // (points + 255) / 256
+    unsigned long long* count_out;
+    double* block_sums;          // scan scratch
+};
+cudaError_t generator_field_candidates(const GenCandidateBuild& build, cudaStream_t stream);
+cudaError_t generator_field_weights(const GenCandidateBuild& build, uint64_t count,
+                                    cudaStream_t stream);
+// Grid candidates: cumulative cell volumes of the domain's cells in order.
+cudaError_t generator_grid_weights(const LibGrid& grid, const int lower[2], const int extents[2],
+                                   uint64_t count, double* cumulative, double* block_sums,
+                                   cudaStream_t stream);
+// Scratch doubles generator_*_weights need for count candidates.
+uint64_t generator_scan_scratch(uint64_t count);
+
 struct SampleLaunch {
     Grid grid;
     const void* lower;

@@ -810,11 +810,15 @@ __global__ void system_capture_kernel(SystemArrays s, uint64_t capacity) {
 // kinetic energy (gamma - 1) m c^2 (ParticleSystem.hpp:171-193), every
 // operation rounded on its own as the reference build evaluates it (the
 // baselines it writes are compared bit for bit)
-__device__ __forceinline__ double kinetic_energy(const LibSplitLaunch& L, double p) {
-    const double normalized = __ddiv_rn(p, L.mc);
+__device__ __forceinline__ double kinetic_energy_of(double p, double mc, double rest_mass,
+                                                    double speed_of_light) {
+    const double normalized = __ddiv_rn(p, mc);
     const double gamma = __dsqrt_rn(__dadd_rn(1.0, __dmul_rn(normalized, normalized)));
-    return __dmul_rn(__dmul_rn(__dmul_rn(__dsub_rn(gamma, 1.0), L.rest_mass), L.speed_of_light),
-                     L.speed_of_light);
+    return __dmul_rn(__dmul_rn(__dmul_rn(__dsub_rn(gamma, 1.0), rest_mass), speed_of_light),
+                     speed_of_light);
+}
+__device__ __forceinline__ double kinetic_energy(const LibSplitLaunch& L, double p) {
+    return kinetic_energy_of(p, L.mc, L.rest_mass, L.speed_of_light);
 }
 
 __global__ void system_reset_baselines_kernel(LibSplitLaunch L) {
@@ -1036,6 +1040,415 @@ __global__ void compact_keys_kernel(const int* status, int* keys, uint64_t count
     if ((threadIdx.x & 31u) == 0u && mine) atomicAdd(active, mine);
 }
 
+// ---- ParticleGenerator -------------------------------------------------------
+//
+// Injection and recycling (ParticleGenerator.hpp:659-1493).  Every particle's
+// draws come from its own keyed stream (seed, particle slot, frame, tag 4), so
+// the results do not depend on the launch shape; the shim's pool hands the
+// reference templates the same stream.  Candidate sets are a stable
+// compaction (field points in index order, the order of the reference's
+// parallel_scan) plus an FP64 inclusive scan of the cell volumes.
+
+// Uniform draws of one particle's stream: draw n is half n%2 of block n/2.
+struct DrawStream {
+    uint2 key;
+    uint32_t index, frame, draw;
+    uint4 block;
+    __device__ double next() {
+        if ((draw & 1u) == 0u) {
+            block = philox4x32_10(make_uint4(draw >> 1, index, frame, kTagGenerator), key);
+        }
+        const double u = (draw & 1u) == 0u ? u01_f64(block.x, block.y) : u01_f64(block.z, block.w);
+        ++draw;
+        return u;
+    }
+    // drand(start, end) = start + (end - start) drand()
+    __device__ double range(double start, double end) {
+        return __dadd_rn(start, __dmul_rn(__dsub_rn(end, start), next()));
+    }
+};
+
+// Logical index range of a domain for cells (Grid.hpp:253-287); faces end
+// one further.
+__device__ __forceinline__ int gen_lower_cell(const LibAxis& a, int domain) {
+    return domain != 0 ? -2 : 0;
+}
+__device__ __forceinline__ int gen_upper_cell(const LibAxis& a, int domain) {
+    return domain != 0 ? a.n + 1 : a.n - 1;
+}
+__device__ __forceinline__ int gen_lower_index(const LibAxis& a, int centering, int domain) {
+    return gen_lower_cell(a, domain);
+}
+__device__ __forceinline__ int gen_upper_index(const LibAxis& a, int centering, int domain) {
+    return gen_upper_cell(a, domain) + (centering != 0 ? 1 : 0);
+}
+
+// Field point coordinate: face x0 + i dx, cell centre the midpoint of its
+// faces (AnalyticCoordinateGrid.hpp:109-187).
+__device__ __forceinline__ double gen_coordinate(const LibAxis& a, int index, int centering) {
+    const double i = static_cast<double>(index);
+    if (centering != 0) return lib_face(a, i);
+    return __dmul_rn(0.5, __dadd_rn(lib_face(a, i), lib_face(a, __dadd_rn(i, 1.0))));
+}
+
+// compare_field_predicate_value (ParticleGenerator.hpp:230-251).
+__device__ __forceinline__ bool gen_compare(double value, double threshold, int comparison) {
+    switch (comparison) {
+        case 0: return value > threshold;
+        case 1: return value >= threshold;
+        case 2: return value < threshold;
+        case 3: return value <= threshold;
+        case 4: return fabs(value) > threshold;
+        case 5: return fabs(value) < threshold;
+    }
+    return false;
+}
+
+// FieldThresholdParticlePredicate::operator() (ParticleGenerator.hpp:297-353)
+// with MappedCoordinateGrid::cell_index and contains_coordinate for a domain
+// (MappedCoordinateGrid.hpp:255-292).
+__device__ bool gen_predicate(const LibGrid& g, const GenPredicate& P, const double (&pt)[2]) {
+    if (!P.enabled) return true;
+    int idx[2];
+#pragma unroll
+    for (int dim = 0; dim < 2; ++dim) {
+        const LibAxis& a = g.axis[dim];
+        const double lower_x = P.domain != 0 ? a.ghost_lower : a.lower;
+        const double upper_x = P.domain != 0 ? a.ghost_upper : a.upper;
+        const double x = pt[dim];
+        if (!(x >= lower_x && x <= upper_x)) return false;
+        const int centering = P.field.centering[dim];
+        int index;
+        if (centering == 0) {
+            if (x == upper_x) {
+                index = gen_upper_cell(a, P.domain);
+            } else {
+                index = static_cast<int>(floor(__ddiv_rn(__dsub_rn(x, a.x0), a.dx)));
+            }
+        } else {
+            index = static_cast<int>(
+                floor(__dadd_rn(__ddiv_rn(__dsub_rn(x, a.x0), a.dx), 0.5)));
+        }
+        if (index < gen_lower_index(a, centering, P.domain) ||
+            index > gen_upper_index(a, centering, P.domain)) {
+            return false;
+        }
+        idx[dim] = index;
+    }
+    const size_t point = static_cast<size_t>(idx[0] + 2) +
+                         static_cast<size_t>(idx[1] + 2) * static_cast<size_t>(P.field.ext[0]);
+    const double value = P.field.values[point * P.field.components + P.component];
+    return gen_compare(value, P.threshold, P.comparison);
+}
+
+// sample_cumulative_weight_index (ParticleGenerator.hpp:437-461).
+__device__ uint64_t gen_sample_index(const GenCandidates& C, DrawStream& st) {
+    if (C.count == 0 || C.total <= 0.0) return 0;
+    const double target = st.range(0.0, C.total);
+    uint64_t left = 0;
+    uint64_t right = C.count - 1;
+    while (left < right) {
+        const uint64_t middle = left + (right - left) / 2;
+        if (target < C.cumulative[middle]) {
+            right = middle;
+        } else {
+            left = middle + 1;
+        }
+    }
+    return left;
+}
+
+// ParticleRecycleSelection (ParticleGenerator.hpp:129-151): 1 escaped, 2 inactive.
+__device__ __forceinline__ bool gen_selected(int status, int selection) {
+    switch (selection) {
+        case 0: return status == 1;
+        case 1: return status == 2;
+        case 2: return status == 1 || status == 2;
+    }
+    return false;
+}
+
+// One particle of an inject_* or recycle_* call.
+__global__ void __launch_bounds__(256) generator_kernel(const GenLaunch L) {
+    unsigned long long written = 0;
+    for (uint64_t k = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; k < L.count;
+         k += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        const SystemArrays& s = L.sys;
+        const uint64_t slot = L.recycle ? k : L.first_index + k;
+        if (L.recycle && !gen_selected(s.status[slot], L.selection)) continue;
+        DrawStream st{L.key, static_cast<uint32_t>(k), L.frame, 0u, make_uint4(0, 0, 0, 0)};
+        double pt[2] = {0.0, 0.0};
+        bool accepted = true;
+        if (L.source == 0) {
+            accepted = false;
+            for (int attempt = 0; attempt < L.max_attempts; ++attempt) {
+                pt[0] = st.range(L.region_lo[0], L.region_hi[0]);
+                pt[1] = st.range(L.region_lo[1], L.region_hi[1]);
+                if (gen_predicate(L.grid, L.predicate, pt)) {
+                    accepted = true;
+                    break;
+                }
+            }
+        } else {
+            const GenCandidates& C = L.candidates;
+            const uint64_t c = gen_sample_index(C, st);
+            if (C.kind == 0) {
+                // FieldParticleCandidateSet::coordinate (:530-541)
+                uint64_t linear = C.indices[c];
+#pragma unroll
+                for (int dim = 0; dim < 2; ++dim) {
+                    const uint64_t e = static_cast<uint64_t>(C.field.ext[dim]);
+                    const int index = static_cast<int>(linear % e) - 2;
+                    linear /= e;
+                    pt[dim] = gen_coordinate(L.grid.axis[dim], index, C.field.centering[dim]);
+                }
+            } else {
+                // GridParticleCandidateSet::sample_coordinate (:627-645)
+                uint64_t linear = c;
+#pragma unroll
+                for (int dim = 0; dim < 2; ++dim) {
+                    const uint64_t e = static_cast<uint64_t>(C.extents[dim]);
+                    const int index = C.lower[dim] + static_cast<int>(linear % e);
+                    linear /= e;
+                    const LibAxis& a = L.grid.axis[dim];
+                    const double lo = lib_face(a, static_cast<double>(index));
+                    const double hi = lib_face(a, static_cast<double>(index + 1));
+                    pt[dim] = lo <= hi ? st.range(lo, hi) : st.range(hi, lo);
+                }
+            }
+        }
+        if (!L.recycle) s.id[slot] = L.first_id + k;
+        s.x[slot] = s.prev_x[slot] = s.prevstep_x[slot] = pt[0];
+        s.y[slot] = s.prev_y[slot] = s.prevstep_y[slot] = pt[1];
+        s.p[slot] = L.momentum;
+        s.mu[slot] = L.mu;
+        s.weight[slot] = L.weight;
+        s.e0[slot] = kinetic_energy_of(L.momentum, L.mc, L.rest_mass, L.speed_of_light);
+        s.status[slot] = accepted ? L.status : 2;
+        s.split_level[slot] = 0;
+        s.sort_key[slot] = 0;
+        ++written;
+    }
+    if (L.recycled != nullptr) {
+        for (int off = 16; off > 0; off >>= 1) written += __shfl_down_sync(0xffffffffu, written, off);
+        if ((threadIdx.x & 31u) == 0u && written) atomicAdd(L.recycled, written);
+    }
+}
+
+// make_field_particle_candidate_set_in_region's predicate over one stored
+// point (ParticleGenerator.hpp:689-725).
+__device__ bool gen_point_accepted(const GenCandidateBuild& B, uint64_t point) {
+    uint64_t linear = point;
+    double coord[2];
+#pragma unroll
+    for (int dim = 0; dim < 2; ++dim) {
+        const uint64_t e = static_cast<uint64_t>(B.field.ext[dim]);
+        const int index = static_cast<int>(linear % e) - 2;
+        linear /= e;
+        const LibAxis& a = B.grid.axis[dim];
+        const int centering = B.field.centering[dim];
+        if (index < gen_lower_index(a, centering, B.domain) ||
+            index > gen_upper_index(a, centering, B.domain)) {
+            return false;
+        }
+        coord[dim] = gen_coordinate(a, index, centering);
+    }
+#pragma unroll
+    for (int dim = 0; dim < 2; ++dim) {
+        if (coord[dim] < B.region_lo[dim] || coord[dim] > B.region_hi[dim]) return false;
+    }
+    return gen_compare(B.field.values[point * B.field.components + B.component], B.threshold,
+                       B.comparison);
+}
+
+__global__ void __launch_bounds__(256) gen_candidate_count_kernel(const GenCandidateBuild B) {
+    __shared__ unsigned int block_total;
+    if (threadIdx.x == 0) block_total = 0;
+    __syncthreads();
+    const uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
+    const bool take = i < B.points && gen_point_accepted(B, i);
+    const unsigned ballot = __ballot_sync(0xffffffffu, take);
+    if ((threadIdx.x & 31u) == 0u && ballot) atomicAdd(&block_total, __popc(ballot));
+    __syncthreads();
+    if (threadIdx.x == 0) B.block_counts[blockIdx.x] = block_total;
+}
+
+// Accepted points in index order (the serial scan's order).
+__global__ void __launch_bounds__(256) gen_candidate_scatter_kernel(const GenCandidateBuild B) {
+    __shared__ unsigned int warp_base[8];
+    const uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
+    const bool take = i < B.points && gen_point_accepted(B, i);
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned ballot = __ballot_sync(0xffffffffu, take);
+    if (lane == 0) warp_base[threadIdx.x >> 5] = __popc(ballot);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned int run = 0;
+        for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) {
+            const unsigned int c = warp_base[w];
+            warp_base[w] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+    if (!take) return;
+    const uint64_t dest = static_cast<uint64_t>(B.block_counts[blockIdx.x]) +
+                          warp_base[threadIdx.x >> 5] + __popc(ballot & ((1u << lane) - 1u));
+    B.indices[dest] = i;
+}
+
+// approximate_grid_cell_physical_volume on the Cartesian grid
+// (ParticleGenerator.hpp:379-394): |jacobian| = 1 times the face-to-face
+// widths, each width face(i+1) - face(i) as the analytic mapping rounds it.
+__device__ __forceinline__ double gen_cell_volume(const LibGrid& g, const int (&cell)[2]) {
+    double volume = 1.0;
+#pragma unroll
+    for (int dim = 0; dim < 2; ++dim) {
+        const LibAxis& a = g.axis[dim];
+        const double i = static_cast<double>(cell[dim]);
+        const double width = __dsub_rn(lib_face(a, __dadd_rn(i, 1.0)), lib_face(a, i));
+        volume = __dmul_rn(volume, fabs(width));
+    }
+    return isfinite(volume) && volume > 0.0 ? volume : 0.0;
+}
+
+// Candidate weights: field points clamp to the domain's cells
+// (field_indices_to_volume_cell_indices, :419-433); grid candidates are the
+// domain's cells in order (:823-845).
+__global__ void gen_field_weight_kernel(const GenCandidateBuild B, uint64_t count) {
+    for (uint64_t c = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; c < count;
+         c += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        uint64_t linear = B.indices[c];
+        int cell[2];
+#pragma unroll
+        for (int dim = 0; dim < 2; ++dim) {
+            const uint64_t e = static_cast<uint64_t>(B.field.ext[dim]);
+            int index = static_cast<int>(linear % e) - 2;
+            linear /= e;
+            const int lo = gen_lower_cell(B.grid.axis[dim], B.domain);
+            const int hi = gen_upper_cell(B.grid.axis[dim], B.domain);
+            cell[dim] = index < lo ? lo : (index > hi ? hi : index);
+        }
+        B.cumulative[c] = gen_cell_volume(B.grid, cell);
+    }
+}
+
+__global__ void gen_grid_weight_kernel(LibGrid g, int lower0, int lower1, int extent0,
+                                       int extent1, uint64_t count, double* weights) {
+    for (uint64_t c = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; c < count;
+         c += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        const int cell[2] = {lower0 + static_cast<int>(c % static_cast<uint64_t>(extent0)),
+                             lower1 + static_cast<int>((c / static_cast<uint64_t>(extent0)) %
+                                                       static_cast<uint64_t>(extent1))};
+        weights[c] = gen_cell_volume(g, cell);
+    }
+}
+
+// FP64 inclusive scan in place: tiles of kScanTile values per block, each
+// thread adding kScanItems consecutive values serially from its running
+// offset.  Pass 1 writes the tile sums, pass 2 scans them (one block),
+// pass 3 rewrites the tile.  The association is fixed, so the result is
+// deterministic; it differs from a one-thread serial sum only by rounding.
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 8;
+constexpr uint64_t kScanTile = static_cast<uint64_t>(kScanThreads) * kScanItems;
+
+__device__ double block_exclusive_sum(double v, double* shared_warp, double* block_total) {
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned warp = threadIdx.x >> 5;
+    double inclusive = v;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const double o = __shfl_up_sync(0xffffffffu, inclusive, off);
+        if (lane >= static_cast<unsigned>(off)) inclusive += o;
+    }
+    if (lane == 31u) shared_warp[warp] = inclusive;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double run = 0.0;
+        for (int w = 0; w < kScanThreads / 32; ++w) {
+            const double t = shared_warp[w];
+            shared_warp[w] = run;
+            run += t;
+        }
+        *block_total = run;
+    }
+    __syncthreads();
+    double exclusive = __shfl_up_sync(0xffffffffu, inclusive, 1);
+    if (lane == 0u) exclusive = 0.0;
+    return shared_warp[warp] + exclusive;
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_tile_sums_kernel(const double* values,
+                                                                      uint64_t n,
+                                                                      double* tile_sums) {
+    __shared__ double warp_sums[kScanThreads / 32];
+    __shared__ double total;
+    const uint64_t base = blockIdx.x * kScanTile + static_cast<uint64_t>(threadIdx.x) * kScanItems;
+    double sum = 0.0;
+    for (int k = 0; k < kScanItems; ++k) {
+        if (base + k < n) sum += values[base + k];
+    }
+    (void)block_exclusive_sum(sum, warp_sums, &total);
+    if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(1024) scan_offsets_kernel(double* tile_sums, int tiles) {
+    __shared__ double partial[1024];
+    const int t = threadIdx.x;
+    const int per = (tiles + blockDim.x - 1) / blockDim.x;
+    const int begin = t * per;
+    const int end = begin + per < tiles ? begin + per : tiles;
+    double sum = 0.0;
+    for (int k = begin; k < end; ++k) sum += tile_sums[k];
+    partial[t] = sum;
+    __syncthreads();
+    if (t == 0) {
+        double run = 0.0;
+        for (int k = 0; k < static_cast<int>(blockDim.x); ++k) {
+            const double v = partial[k];
+            partial[k] = run;
+            run += v;
+        }
+    }
+    __syncthreads();
+    double run = partial[t];
+    for (int k = begin; k < end; ++k) {
+        const double v = tile_sums[k];
+        tile_sums[k] = run;
+        run += v;
+    }
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_apply_kernel(double* values, uint64_t n,
+                                                                  const double* tile_offsets) {
+    __shared__ double warp_sums[kScanThreads / 32];
+    __shared__ double total;
+    const uint64_t base = blockIdx.x * kScanTile + static_cast<uint64_t>(threadIdx.x) * kScanItems;
+    double local[kScanItems];
+    double sum = 0.0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        local[k] = base + k < n ? values[base + k] : 0.0;
+        sum += local[k];
+    }
+    double run = tile_offsets[blockIdx.x] + block_exclusive_sum(sum, warp_sums, &total);
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        run += local[k];
+        if (base + k < n) values[base + k] = run;
+    }
+}
+
+cudaError_t scan_inclusive_f64(double* values, uint64_t n, double* scratch, cudaStream_t stream) {
+    if (n == 0) return cudaSuccess;
+    const int tiles = static_cast<int>((n + kScanTile - 1) / kScanTile);
+    scan_tile_sums_kernel<<<tiles, kScanThreads, 0, stream>>>(values, n, scratch);
+    scan_offsets_kernel<<<1, 1024, 0, stream>>>(scratch, tiles);
+    scan_apply_kernel<<<tiles, kScanThreads, 0, stream>>>(values, n, scratch);
+    return cudaGetLastError();
+}
+
 int grid_for(uint64_t n, int threads) {
     const uint64_t want = (n + threads - 1) / threads;
     return static_cast<int>(want < 1 ? 1 : (want > 152u * 32u ? 152u * 32u : want));
@@ -1172,6 +1585,51 @@ cudaError_t system_compact_keys(const SystemArrays& s, uint64_t count, unsigned 
     compact_keys_kernel<<<grid_for(count, 256), 256, 0, stream>>>(s.status, s.sort_key, count,
                                                                   active);
     return cudaGetLastError();
+}
+
+cudaError_t generator_run(const GenLaunch& L, cudaStream_t stream) {
+    if (L.recycled != nullptr) {
+        const cudaError_t err = cudaMemsetAsync(L.recycled, 0, sizeof(unsigned long long), stream);
+        if (err != cudaSuccess) return err;
+    }
+    if (L.count == 0) return cudaSuccess;
+    generator_kernel<<<grid_for(L.count, 256), 256, 0, stream>>>(L);
+    return cudaGetLastError();
+}
+
+cudaError_t generator_field_candidates(const GenCandidateBuild& B, cudaStream_t stream) {
+    if (B.points == 0) {
+        return cudaMemsetAsync(B.count_out, 0, sizeof(unsigned long long), stream);
+    }
+    const int blocks = static_cast<int>((B.points + 255) / 256);
+    gen_candidate_count_kernel<<<blocks, 256, 0, stream>>>(B);
+    system_split_scan_kernel<<<1, 1024, 0, stream>>>(B.block_counts, blocks, B.count_out);
+    gen_candidate_scatter_kernel<<<blocks, 256, 0, stream>>>(B);
+    return cudaGetLastError();
+}
+
+cudaError_t generator_field_weights(const GenCandidateBuild& B, uint64_t count,
+                                    cudaStream_t stream) {
+    if (count == 0) return cudaSuccess;
+    gen_field_weight_kernel<<<grid_for(count, 256), 256, 0, stream>>>(B, count);
+    const cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+    return scan_inclusive_f64(B.cumulative, count, B.block_sums, stream);
+}
+
+cudaError_t generator_grid_weights(const LibGrid& g, const int lower[2], const int extents[2],
+                                   uint64_t count, double* cumulative, double* block_sums,
+                                   cudaStream_t stream) {
+    if (count == 0) return cudaSuccess;
+    gen_grid_weight_kernel<<<grid_for(count, 256), 256, 0, stream>>>(
+        g, lower[0], lower[1], extents[0], extents[1], count, cumulative);
+    const cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+    return scan_inclusive_f64(cumulative, count, block_sums, stream);
+}
+
+uint64_t generator_scan_scratch(uint64_t count) {
+    return (count + kScanTile - 1) / kScanTile + 1;
 }
 
 }  // namespace kpt

@@ -277,6 +277,12 @@ class ReferenceHarness:
         lib.ref_lib_system.restype = ll
         lib.ref_lib_system.argtypes = [i32, i32, vp, vp, vp, vp, i32, i32, i32, ll, ll, vp, vp,
                                        vp, vp]
+        lib.ref_lib_generator.restype = ll
+        lib.ref_lib_generator.argtypes = [i32, i32, vp, vp, vp, vp, i32, i32, vp, vp, vp, vp, vp,
+                                          vp, i32, ull, ctypes.c_uint, ll, ll, vp, vp, vp, vp]
+        lib.ref_lib_candidates.restype = ll
+        lib.ref_lib_candidates.argtypes = [i32, i32, vp, vp, vp, i32, i32, vp, vp, vp, vp, vp,
+                                           vp, ll, vp]
 
     @staticmethod
     def _param_arrays(params: dict):
@@ -433,6 +439,68 @@ class ReferenceHarness:
             _ptr(stats)))
         self._lib_unblock(system, ids, d, i)
         return int(stats[0]), [int(v) for v in stats[1:]]
+
+    # ParticleGenerator (include/ParticleGenerator.hpp): the reference's own
+    # templates on the library grid, noise frame `frame`.
+    GENERATOR_OPS = {"inject_uniform": 0, "inject_uniform_if": 1, "inject_where_field": 2,
+                     "inject_in_grid": 3, "recycle_uniform": 4, "recycle_uniform_if": 5,
+                     "recycle_where_field": 6, "recycle_in_grid": 7}
+
+    @staticmethod
+    def _generator_inputs(grid, field, centering, region, predicate):
+        xe = np.ascontiguousarray(grid["x_edges"], dtype=np.float64)
+        ye = np.ascontiguousarray(grid["y_edges"], dtype=np.float64)
+        periodic = np.ascontiguousarray(grid["periodic"], dtype=np.int32)
+        values = np.ascontiguousarray(field, dtype=np.float64)
+        components = 1 if values.ndim == 1 else values.shape[1]
+        cent = np.ascontiguousarray(centering, dtype=np.int32)
+        reg = None if region is None else np.ascontiguousarray(region, dtype=np.float64)
+        pred = np.array([predicate.get("threshold", 0.0), predicate.get("comparison", 1),
+                         predicate.get("component", 0), predicate.get("domain", 0)],
+                        dtype=np.float64)
+        return xe, ye, periodic, values, components, cent, reg, pred
+
+    def lib_generator(self, grid: dict, props: dict, op: str, count: int,
+                      system: Dict[str, np.ndarray], *, field, centering=(0, 0), region=None,
+                      predicate=None, kinematics=(1.0, 0.0, 1.0, 0), plan=(0, 0, 0, 64),
+                      selection: int = 0, seed: int = 114514, frame: int = 0) -> int:
+        """One injection or recycling call; returns the particle count after it."""
+        xe, ye, periodic, values, components, cent, reg, pred = self._generator_inputs(
+            grid, field, centering, region, predicate or {})
+        pr = np.array([props["rest_mass"], props["charge"], props["speed_of_light"],
+                       props.get("energy_scale", 1.0)], dtype=np.float64)
+        kin = np.ascontiguousarray(kinematics, dtype=np.float64)
+        pl = np.ascontiguousarray(plan, dtype=np.uint64)
+        ids, d, i = self._lib_blocks(system)
+        out_count = np.zeros(1, dtype=np.uint64)
+        self._check(self.lib.ref_lib_generator(
+            len(xe) - 1, len(ye) - 1, _ptr(xe), _ptr(ye), _ptr(periodic), _ptr(pr),
+            self.GENERATOR_OPS[op], components, _ptr(cent), _ptr(values),
+            None if reg is None else _ptr(reg), _ptr(pred), _ptr(kin), _ptr(pl), int(selection),
+            ctypes.c_ulonglong(seed), ctypes.c_uint(frame), count, ids.size, _ptr(ids), _ptr(d),
+            _ptr(i), _ptr(out_count)))
+        self._lib_unblock(system, ids, d, i)
+        return int(out_count[0])
+
+    def lib_candidates(self, grid: dict, kind: str, *, field=None, centering=(0, 0),
+                       region=None, predicate=None):
+        """Candidate set: kind "field" or "grid"; returns (indices, cumulative weights, total)."""
+        if field is None:
+            field = np.zeros(1)
+        xe, ye, periodic, values, components, cent, reg, pred = self._generator_inputs(
+            grid, field, centering, region, predicate or {})
+        cells = (len(xe) + 3) * (len(ye) + 3)
+        max_out = max(cells, values.shape[0])
+        idx = np.zeros(max_out, dtype=np.uint64)
+        cum = np.zeros(max_out, dtype=np.float64)
+        total = np.zeros(1, dtype=np.float64)
+        n = self.lib.ref_lib_candidates(
+            len(xe) - 1, len(ye) - 1, _ptr(xe), _ptr(ye), _ptr(periodic),
+            0 if kind == "field" else 1, components, _ptr(cent), _ptr(values),
+            None if reg is None else _ptr(reg), _ptr(pred), _ptr(idx), _ptr(cum), max_out,
+            _ptr(total))
+        self._check(0 if n >= 0 else -1)
+        return idx[:n].copy(), cum[:n].copy(), float(total[0])
 
     def main(self, argv, frame_base: int = 0) -> int:
         """Run the reference CLI (in-process); noise frames start at frame_base."""

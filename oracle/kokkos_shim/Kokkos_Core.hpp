@@ -303,6 +303,23 @@ void parallel_reduce(const std::string& label, const RangePolicy<ExecSpace>& pol
     result = value;
 }
 
+// parallel_scan (functor(i, T& update, bool final_pass)) in serial order: a
+// single final pass in which update holds the exclusive prefix on entry;
+// result receives the total.
+template <class ExecSpace, class Functor, class T>
+void parallel_scan(const std::string& label, const RangePolicy<ExecSpace>& policy,
+                   const Functor& functor, T& result) {
+    (void)ShimImpl::count_launch(label);
+    T value = T(0);
+    for (std::int64_t i = policy.begin; i < policy.end; ++i) {
+        auto& context = ShimImpl::current_kernel();
+        context.label = label.c_str();
+        context.index = static_cast<std::uint64_t>(i);
+        functor(static_cast<std::size_t>(i), value, true);
+    }
+    result = value;
+}
+
 inline void fence() {}
 inline void fence(const std::string&) {}
 

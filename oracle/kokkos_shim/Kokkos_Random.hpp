@@ -47,6 +47,9 @@ inline std::uint32_t label_tag(const char* label) {
         std::strstr(label, "FocusSolver::") != nullptr) {
         return KPT_ORACLE_TAG_LIBRARY;
     }
+    if (std::strstr(label, "ParticleGenerator::") != nullptr) {
+        return KPT_ORACLE_TAG_GENERATOR;
+    }
     return KPT_ORACLE_TAG_OTHER;
 }
 }  // namespace ShimImpl

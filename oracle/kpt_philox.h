@@ -28,6 +28,7 @@ enum {
     KPT_ORACLE_TAG_INJECT = 1u,
     KPT_ORACLE_TAG_PUSH = 2u,
     KPT_ORACLE_TAG_LIBRARY = 3u,
+    KPT_ORACLE_TAG_GENERATOR = 4u,
     KPT_ORACLE_TAG_OTHER = 255u
 };
 

@@ -23,6 +23,7 @@
 #include <string>
 
 #include "FocusSolver.hpp"
+#include "ParticleGenerator.hpp"
 #include "LegencyModel.hpp"
 #include "ParkerSolver.hpp"
 
@@ -743,6 +744,222 @@ int ref_main(int argc, char** argv, int frame_base) {
     const int rc = kpt_ref_main(argc, argv);
     Kokkos::ShimImpl::auto_frame_enabled() = 0;
     return rc;
+}
+
+}  // extern "C"
+
+// ---- ParticleGenerator on the library grid ----------------------------------
+namespace {
+
+template <int C>
+using LibGenField = Field<LibAnalyticGrid, C>;
+
+// field values: C doubles per stored point in the Field's flattened order
+// (dim 0 fastest over the ghosted extent of its centering);
+// centering[dim]: 0 cell, 1 face.
+template <int C>
+LibGenField<C> lib_gen_field(const LibAnalyticGrid& grid, const int* centering,
+                             const double* values) {
+    typename LibGenField<C>::centering_array_type c{};
+    for (int dim = 0; dim < 2; ++dim) {
+        c[dim] = centering[dim] == 0 ? GridCentering::CellCentered : GridCentering::FaceCentered;
+    }
+    LibGenField<C> field(grid, "lib_generator_field", c);
+    const std::size_t points = field.point_count();
+    for (std::size_t k = 0; k < points; ++k) {
+        for (int comp = 0; comp < C; ++comp) field.data(k, comp) = values[k * C + comp];
+    }
+    return field;
+}
+
+AxisAlignedParticleRegion<2> lib_gen_region(const double* r) {
+    Kokkos::Array<double, 2> lower{};
+    Kokkos::Array<double, 2> upper{};
+    lower[0] = r[0];
+    lower[1] = r[1];
+    upper[0] = r[2];
+    upper[1] = r[3];
+    return make_particle_region<2>(lower, upper);
+}
+
+template <int C>
+void lib_generator_run(const LibAnalyticGrid& grid, LibSystem& sys, int op, const int* centering,
+                       const double* values, const double* region, const double* pred,
+                       const double* kin, const unsigned long long* plan_in, int selection,
+                       unsigned long long seed) {
+    const auto field = lib_gen_field<C>(grid, centering, values);
+    const double threshold = pred[0];
+    const auto comparison = static_cast<FieldPredicateComparison>(static_cast<int>(pred[1]));
+    const int component = static_cast<int>(pred[2]);
+    const auto domain = static_cast<GridDomain>(static_cast<int>(pred[3]));
+    ParticleInjectionKinematics<2> kinematics;
+    kinematics.momentum_magnitude = kin[0];
+    kinematics.mu = kin[1];
+    kinematics.weight = kin[2];
+    kinematics.status = static_cast<ParticleStatus>(static_cast<int>(kin[3]));
+    ParticleInjectionPlan plan{plan_in[0], plan_in[1], plan_in[2], static_cast<int>(plan_in[3])};
+    const auto select = static_cast<ParticleRecycleSelection>(selection);
+    RandomManager<> random_manager(seed);
+    switch (op) {
+        case 0:
+            inject_particles_uniform(sys, random_manager, lib_gen_region(region), plan, kinematics);
+            break;
+        case 1:
+            inject_particles_uniform_if(
+                sys, random_manager, lib_gen_region(region), plan, kinematics,
+                make_field_threshold_particle_predicate(field, threshold, comparison, component,
+                                                        domain));
+            break;
+        case 2:
+            if (region != nullptr) {
+                inject_particles_uniform_where_field(sys, random_manager, lib_gen_region(region),
+                                                     plan, kinematics, field, threshold,
+                                                     comparison, component, domain);
+            } else {
+                inject_particles_uniform_where_field(sys, random_manager, plan, kinematics, field,
+                                                     threshold, comparison, component, domain);
+            }
+            break;
+        case 3:
+            inject_particles_uniform_in_grid(sys, random_manager, grid, plan, kinematics, domain);
+            break;
+        case 4:
+            recycle_particles_uniform(sys, random_manager, lib_gen_region(region), kinematics,
+                                      select);
+            break;
+        case 5:
+            recycle_particles_uniform_if(
+                sys, random_manager, lib_gen_region(region), kinematics,
+                make_field_threshold_particle_predicate(field, threshold, comparison, component,
+                                                        domain),
+                select, static_cast<int>(plan_in[3]));
+            break;
+        case 6:
+            if (region != nullptr) {
+                recycle_particles_uniform_where_field(sys, random_manager, lib_gen_region(region),
+                                                      kinematics, field, threshold, comparison,
+                                                      component, domain, select);
+            } else {
+                recycle_particles_uniform_where_field(sys, random_manager, kinematics, field,
+                                                      threshold, comparison, component, domain,
+                                                      select);
+            }
+            break;
+        case 7:
+            recycle_particles_uniform_in_grid(sys, random_manager, grid, kinematics, select,
+                                              domain);
+            break;
+        default:
+            throw std::runtime_error("ref_lib_generator: unknown op");
+    }
+}
+
+template <int C>
+long long lib_candidates_run(const LibAnalyticGrid& grid, int kind, const int* centering,
+                             const double* values, const double* region, const double* pred,
+                             unsigned long long* indices, double* cumulative, long long max_out,
+                             double* total) {
+    const auto domain = static_cast<GridDomain>(static_cast<int>(pred[3]));
+    if (kind == 1) {
+        const auto set = make_grid_particle_candidate_set(grid, domain);
+        const long long n = static_cast<long long>(set.candidate_count());
+        for (long long k = 0; k < n && k < max_out; ++k) {
+            indices[k] = static_cast<unsigned long long>(k);
+            cumulative[k] = set.cumulative_weights(k);
+        }
+        *total = set.total_weight_cache;
+        return n;
+    }
+    const auto field = lib_gen_field<C>(grid, centering, values);
+    const auto comparison = static_cast<FieldPredicateComparison>(static_cast<int>(pred[1]));
+    const int component = static_cast<int>(pred[2]);
+    const auto set = region != nullptr
+                         ? make_field_particle_candidate_set_in_region(
+                               field, lib_gen_region(region), pred[0], comparison, component,
+                               domain)
+                         : make_field_particle_candidate_set(field, pred[0], comparison,
+                                                            component, domain);
+    const long long n = static_cast<long long>(set.candidate_count());
+    for (long long k = 0; k < n && k < max_out; ++k) {
+        indices[k] = static_cast<unsigned long long>(set.point_indices(k));
+        cumulative[k] = set.cumulative_weights(k);
+    }
+    *total = set.total_weight_cache;
+    return n;
+}
+
+}  // namespace
+
+extern "C" {
+
+// ParticleGenerator (include/ParticleGenerator.hpp) on the library grid.
+// components 1 or 3 of the field (centering[2]: 0 cell, 1 face); region[4]
+// = lower x, lower y, upper x, upper y, or NULL for the grid-domain
+// overloads of op 2 and 6; pred[4] = threshold, comparison, component,
+// domain; kin[4] = momentum, mu, weight, status; plan[4] = first index,
+// count, first id, max attempts (op 5 takes its max attempts from plan[3]).
+// op: 0 inject_particles_uniform, 1 inject_particles_uniform_if with the
+// field threshold predicate, 2 inject_particles_uniform_where_field, 3
+// inject_particles_uniform_in_grid, 4 recycle_particles_uniform, 5
+// recycle_particles_uniform_if, 6 recycle_particles_uniform_where_field, 7
+// recycle_particles_uniform_in_grid.  The noise frame is `frame`.
+// out_count receives the particle count afterwards.
+long long ref_lib_generator(int nx, int ny, const double* x_edges, const double* y_edges,
+                            const int* periodic, const double* props, int op, int components,
+                            const int* centering, const double* values, const double* region,
+                            const double* pred, const double* kin,
+                            const unsigned long long* plan, int selection,
+                            unsigned long long seed, unsigned frame, long long count,
+                            long long capacity, unsigned long long* ids, double* d, int* ints,
+                            unsigned long long* out_count) {
+    try {
+        const LibAnalyticGrid grid = make_lib_analytic_grid(nx, ny, x_edges, y_edges, periodic);
+        LibSystem sys(static_cast<typename LibSystem::size_type>(count),
+                      static_cast<typename LibSystem::size_type>(capacity),
+                      lib_properties(props));
+        const LibHost h{ids, d, ints, capacity};
+        lib_load(sys, h);
+        Kokkos::ShimImpl::auto_frame_enabled() = 0;
+        Kokkos::ShimImpl::current_frame() = frame;
+        if (components == 1) {
+            lib_generator_run<1>(grid, sys, op, centering, values, region, pred, kin, plan,
+                                 selection, seed);
+        } else if (components == 3) {
+            lib_generator_run<3>(grid, sys, op, centering, values, region, pred, kin, plan,
+                                 selection, seed);
+        } else {
+            throw std::runtime_error("ref_lib_generator: components must be 1 or 3");
+        }
+        *out_count = sys.particle_count();
+        lib_store(sys, h);
+        return 0;
+    } catch (const std::exception& error) {
+        g_last_error = error.what();
+        return -1;
+    }
+}
+
+// Candidate sets: kind 0 field points passing the predicate (region or NULL
+// for the whole domain), kind 1 grid cells of the domain (pred[3]).  Writes
+// up to max_out point indices (cell ordinals for kind 1) and cumulative
+// weights; returns the candidate count (-1 on error) and the total weight.
+long long ref_lib_candidates(int nx, int ny, const double* x_edges, const double* y_edges,
+                             const int* periodic, int kind, int components,
+                             const int* centering, const double* values, const double* region,
+                             const double* pred, unsigned long long* indices, double* cumulative,
+                             long long max_out, double* total) {
+    try {
+        const LibAnalyticGrid grid = make_lib_analytic_grid(nx, ny, x_edges, y_edges, periodic);
+        if (components == 3) {
+            return lib_candidates_run<3>(grid, kind, centering, values, region, pred, indices,
+                                         cumulative, max_out, total);
+        }
+        return lib_candidates_run<1>(grid, kind, centering, values, region, pred, indices,
+                                     cumulative, max_out, total);
+    } catch (const std::exception& error) {
+        g_last_error = error.what();
+        return -1;
+    }
 }
 
 }  // extern "C"

@@ -26,6 +26,11 @@ Cases
   lib_parker_*.npz    the header library's ParkerSolver (stochastic and
                       deterministic steps, both diffusion branches, periodic
                       and open boundaries) on a uniform Cartesian grid
+  lib_generator.npz   ParticleGenerator: region sampling with and without the
+                      field threshold predicate, field and grid candidate
+                      sets (indices and cumulative volumes), injection and
+                      recycling from them, cell/face/mixed centred fields,
+                      physical and ghosted domains
   lib_system.npz      ParticleSystem lifecycle: boundary conditions,
                       sort_by_key, compact_active_particles,
                       split_particles_on_energy_growth, capture_previous_positions
@@ -377,13 +382,142 @@ def make_lib(ref, out_dir):
              min_child_weight=props_sys["min_child_weight"], **arrays)
 
 
+def generator_fields(nx: int, ny: int, x_edges, y_edges) -> dict:
+    """Fields of the ParticleGenerator cases, in the Field's stored order
+    (dim 0 fastest over the ghosted extent of the centering)."""
+    dx = (x_edges[-1] - x_edges[0]) / nx
+    dy = (y_edges[-1] - y_edges[0]) / ny
+
+    def coords(n, x0, d, face):
+        k = np.arange(n + 4 + int(face)) - 2.0
+        return x0 + (k if face else k + 0.5) * d
+
+    xc, yc = coords(nx, x_edges[0], dx, False), coords(ny, y_edges[0], dy, False)
+    xf, yf = coords(nx, x_edges[0], dx, True), coords(ny, y_edges[0], dy, True)
+    scalar_cell = (np.cos(2.0 * xc)[None, :] * np.exp(-yc[:, None] ** 2)).ravel()
+    vec_face = np.stack([np.sin(3.0 * xf)[None, :] + 0.0 * yf[:, None],
+                         np.tanh(yf[:, None] / 0.4) * np.cos(xf)[None, :],
+                         xf[None, :] * yf[:, None]], axis=-1).reshape(-1, 3)
+    mixed = (np.sin(xc)[None, :] * yf[:, None]).ravel()
+    return {"scalar_cell": (scalar_cell, (0, 0)), "vec_face": (vec_face, (1, 1)),
+            "mixed": (mixed, (0, 1))}
+
+
+# op, field, region (None = grid domain), predicate (threshold, comparison,
+# component, domain), kinematics (p, mu, weight, status), plan (first index,
+# count, first id, attempts), selection, population
+GENERATOR_CASES = (
+    ("inject_uniform", "inject_uniform", "scalar_cell", (-1.0, -1.5, 1.5, 1.0),
+     (0.0, 1, 0, 0), (0.7, -0.3, 2.0, 0), (0, 500, 0, 64), 0, "empty"),
+    ("inject_uniform_if", "inject_uniform_if", "scalar_cell", (-1.3, -2.0, 2.1, 2.0),
+     (0.2, 0, 0, 0), (1.1, 0.5, 1.0, 0), (120, 400, 9000, 4), 0, "partial"),
+    ("inject_if_face_ghosted", "inject_uniform_if", "vec_face", (-1.5, -2.2, 2.3, 2.2),
+     (0.5, 4, 1, 1), (0.3, 0.0, 0.5, 0), (0, 300, 5, 16), 0, "empty"),
+    ("inject_where_field_region", "inject_where_field", "scalar_cell", (-0.8, -1.0, 1.2, 1.5),
+     (0.1, 1, 0, 0), (0.9, 0.1, 1.0, 0), (120, 600, 120, 64), 0, "partial"),
+    ("inject_where_field_whole", "inject_where_field", "vec_face", None,
+     (0.4, 5, 2, 0), (2.0, -0.9, 1.0, 1), (0, 500, 0, 64), 0, "empty"),
+    ("inject_where_field_mixed", "inject_where_field", "mixed", None,
+     (0.3, 0, 0, 1), (0.2, 0.2, 3.0, 0), (0, 400, 77, 64), 0, "empty"),
+    ("inject_in_grid", "inject_in_grid", "scalar_cell", None,
+     (0.0, 1, 0, 0), (0.5, 0.0, 1.0, 0), (0, 700, 0, 64), 0, "empty"),
+    ("inject_in_grid_ghosted", "inject_in_grid", "scalar_cell", None,
+     (0.0, 1, 0, 1), (0.5, 0.4, 1.0, 0), (120, 300, 1000, 64), 0, "partial"),
+    ("recycle_uniform_escaped", "recycle_uniform", "scalar_cell", (-1.0, -1.0, 1.0, 1.0),
+     (0.0, 1, 0, 0), (0.8, 0.0, 1.0, 0), (0, 0, 0, 64), 0, "mixed"),
+    ("recycle_uniform_if_recyclable", "recycle_uniform_if", "scalar_cell",
+     (-1.3, -2.0, 2.1, 2.0), (0.3, 0, 0, 0), (0.6, 0.2, 1.5, 0), (0, 0, 0, 3), 2, "mixed"),
+    ("recycle_where_field_inactive", "recycle_where_field", "vec_face", (-1.0, -1.5, 1.0, 1.5),
+     (0.2, 2, 0, 0), (1.2, -0.5, 1.0, 0), (0, 0, 0, 64), 1, "mixed"),
+    ("recycle_where_field_whole", "recycle_where_field", "mixed", None,
+     (-0.1, 3, 0, 0), (0.4, 0.0, 1.0, 0), (0, 0, 0, 64), 2, "mixed"),
+    ("recycle_in_grid", "recycle_in_grid", "scalar_cell", None,
+     (0.0, 1, 0, 0), (0.7, 0.3, 1.0, 0), (0, 0, 0, 64), 2, "mixed"),
+)
+
+# field, region, predicate (threshold, comparison, component, domain); field
+# None = the grid's cells
+CANDIDATE_CASES = (
+    ("field_cell_region", "scalar_cell", (-0.8, -1.0, 1.2, 1.5), (0.1, 1, 0, 0)),
+    ("field_face_ghosted", "vec_face", None, (0.4, 5, 2, 1)),
+    ("field_mixed", "mixed", None, (0.3, 0, 0, 0)),
+    ("grid_physical", None, None, (0.0, 0, 0, 0)),
+    ("grid_ghosted", None, None, (0.0, 0, 0, 1)),
+)
+
+
+def make_generator(ref, out_dir):
+    """ParticleGenerator cases from the reference's own templates."""
+    rng = np.random.default_rng(1618)
+    nx, ny = 24, 40
+    xe = np.linspace(-1.3, 2.1, nx + 1)
+    ye = np.linspace(-2.0, 2.0, ny + 1)
+    grid = dict(x_edges=xe, y_edges=ye, periodic=np.array((1, 0), dtype=np.int32))
+    props = dict(rest_mass=1.0, charge=1.0, speed_of_light=1.0, energy_scale=1.0)
+    fields = generator_fields(nx, ny, xe, ye)
+    arrays = {f"field_{name}": values for name, (values, _) in fields.items()}
+    for name, (_, cent) in fields.items():
+        arrays[f"centering_{name}"] = np.array(cent, dtype=np.int32)
+    capacity = 1024
+    for k, (name, op, field, region, pred, kin, plan, selection, population) in enumerate(
+            GENERATOR_CASES):
+        count = {"empty": 0, "partial": 120, "mixed": 900}[population]
+        start = lib_population(rng, count, capacity, xe, ye, True) if count else \
+            binding.lib_default_system(0, capacity)
+        if population == "mixed":
+            start["status"][:count] = rng.choice([0, 1, 2], count, p=[0.4, 0.35, 0.25])
+        system = {key: v.copy() for key, v in start.items()}
+        values, cent = fields[field]
+        predicate = dict(threshold=pred[0], comparison=pred[1], component=pred[2],
+                         domain=pred[3])
+        seed, frame = SEED + k, 3 + k
+        end_count = ref.lib_generator(grid, props, op, count, system, field=values,
+                                      centering=cent, region=region, predicate=predicate,
+                                      kinematics=kin, plan=plan, selection=selection, seed=seed,
+                                      frame=frame)
+        arrays[f"{name}_case"] = np.array(
+            [k, count, end_count, selection, seed, frame], dtype=np.int64)
+        arrays[f"{name}_op"] = np.array(op)
+        arrays[f"{name}_field"] = np.array(field)
+        arrays[f"{name}_region"] = np.array(region if region is not None else [np.nan] * 4)
+        arrays[f"{name}_predicate"] = np.array(pred, dtype=np.float64)
+        arrays[f"{name}_kinematics"] = np.array(kin, dtype=np.float64)
+        arrays[f"{name}_plan"] = np.array(plan, dtype=np.uint64)
+        for key, v in start.items():
+            arrays[f"{name}_start_{key}"] = v
+        for key, v in system.items():
+            arrays[f"{name}_end_{key}"] = v
+    for name, field, region, pred in CANDIDATE_CASES:
+        predicate = dict(threshold=pred[0], comparison=pred[1], component=pred[2],
+                         domain=pred[3])
+        if field is None:
+            idx, cum, total = ref.lib_candidates(grid, "grid", predicate=predicate)
+        else:
+            values, cent = fields[field]
+            idx, cum, total = ref.lib_candidates(grid, "field", field=values, centering=cent,
+                                                 region=region, predicate=predicate)
+        arrays[f"cand_{name}_indices"] = idx
+        arrays[f"cand_{name}_cumulative"] = cum
+        arrays[f"cand_{name}_total"] = np.array(total)
+        arrays[f"cand_{name}_field"] = np.array(field if field is not None else "")
+        arrays[f"cand_{name}_region"] = np.array(region if region is not None else [np.nan] * 4)
+        arrays[f"cand_{name}_predicate"] = np.array(pred, dtype=np.float64)
+    lib_save(out_dir, "lib_generator.npz", x_edges=xe, y_edges=ye, periodic=grid["periodic"],
+             cases=np.array([c[0] for c in GENERATOR_CASES]),
+             candidate_cases=np.array([c[0] for c in CANDIDATE_CASES]), **arrays)
+
+
 def main() -> None:
     ref = binding.ReferenceHarness()
     out_dir = HERE
     if sys.argv[1:] == ["c1"]:
         make_c1(ref, out_dir)
         return
+    if sys.argv[1:] == ["generator"]:
+        make_generator(ref, out_dir)
+        return
     make_lib(ref, out_dir)
+    make_generator(ref, out_dir)
     if sys.argv[1:] == ["lib"]:
         return
     make_c1(ref, out_dir)
