@@ -449,9 +449,37 @@ def run_library(args):
         solver.close()
         system.close()
     out["generator"] = run_generator(kpt, ctx, grid, xe, ye, n, stream)
+    out["coefficients"] = run_coefficients(ctx, grid, xe, ye)
     grid.close()
     ctx.close()
     return out
+
+
+def run_coefficients(ctx, grid, xe, ye):
+    """make_legacy_transport_coefficient_fields + the packed basis for the
+    1024x2048 grid from host B and V (2 x 50 MB uploaded inside the timed
+    call): the per-frame precompute a library user runs before stepping."""
+    import torch
+    dx, dy = (xe[-1] - xe[0]) / NX, 4.0 / NY
+    xc = xe[0] + (np.arange(NX + 4) - 1.5) * dx
+    yc = -2.0 + (np.arange(NY + 4) - 1.5) * dy
+    X, Y = np.meshgrid(xc, yc)
+    b = np.stack([np.tanh(Y / 0.2), 0.1 * np.sin(np.pi * X), 0.3 + 0.0 * X],
+                 axis=-1).reshape(-1, 3)
+    v = np.stack([1.0 + 0.1 * np.cos(np.pi * X), 0.1 * np.sin(Y), 0.0 * X],
+                 axis=-1).reshape(-1, 3)
+    turbulence = {"sigma2": 0.35, "l2d": 0.9, "lslab": 1.4}
+    times = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        solver = ctx.parker_solver_from_fields(grid, b, v, turbulence)
+        times.append((time.perf_counter() - t0) * 1e3)
+        solver.close()
+    points = b.shape[0]
+    return {"points": points, "ms": min(times),
+            "value": points / (min(times) / 1e3), "unit": "grid points/s",
+            "note": "host B, V upload included; basis stays on the device"}
 
 
 def run_generator(kpt, ctx, grid, xe, ye, n, stream):

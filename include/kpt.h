@@ -535,6 +535,63 @@ int kpt_focus_advance_stochastic_steps(kpt_context* ctx, kpt_focus_solver* solve
                                        kpt_system* system, uint64_t seed, uint32_t first_step,
                                        uint32_t steps, double* dts);
 
+/* ----------------------------------------------------------------------
+ * Parker coefficient precompute on the library grid
+ * (ParkerCoefficient::make_legacy_transport_coefficient_fields,
+ * include/ParkerCoefficient.hpp:1102-1155, with LegencyModel's gamma-one
+ * diffusion fields, LegencyModel.hpp:795-898, and FieldOperator's
+ * divergence, FieldOperator.hpp:262-277, 487-530) straight into the packed
+ * basis the solver samples (ParkerSolver.hpp:514-598).
+ * ---------------------------------------------------------------------- */
+
+/* TurbulenceProperties (TurbulenceProperties.hpp:294-484): storage 0 =
+ * the constant state of TurbulencePropertyModel::constant_code_units(sigma2,
+ * l2d, lslab, lc) (lc <= 0: the slab length); storage 1 = per-point fields
+ * (host arrays over the ghosted cells, x fastest) as Field storage holds
+ * them (lslab_field unused by the coefficients, may be NULL). */
+typedef struct kpt_turbulence {
+    int32_t storage;
+    int32_t pad;
+    double sigma2, l2d, lslab, lc;
+    const double* sigma2_field;
+    const double* l2d_field;
+    const double* lslab_field;
+    const double* lc_field;
+} kpt_turbulence;
+
+/* LegencyModel::DiffusionModelParameters (LegencyModel.hpp:33-117) plus
+ * the drift floor and ghost-fill mode of make_legacy_transport_coefficient_
+ * fields. perpendicular_model 0 README formula, 1 constant parallel ratio;
+ * ghost_fill_mode 0 PeriodicOrClamped, 1 PeriodicOnly (Field.hpp:20-23). */
+typedef struct kpt_diffusion_parameters {
+    int32_t perpendicular_model;
+    int32_t ghost_fill_mode;
+    double parallel_prefactor;
+    double perpendicular_prefactor;
+    double perpendicular_parallel_ratio;
+    double minimum_magnetic_field_magnitude;
+    double minimum_solar_wind_speed;
+    double minimum_sigma2;
+    double minimum_magnetic_field_squared_for_drift;
+} kpt_diffusion_parameters;
+
+/* The reference defaults: README formula, 1.622, 0.198, zero floors. */
+void kpt_default_diffusion_parameters(kpt_diffusion_parameters* out);
+
+/* Packed Parker basis (grid points x 18, host) from cell-centred B and V
+ * (grid points x 3, host, ghost cells as the caller filled them). */
+int kpt_parker_coefficients(kpt_context* ctx, const kpt_grid* grid, const double* b,
+                            const double* v, const kpt_turbulence* turbulence,
+                            const kpt_particle_properties* properties,
+                            const kpt_diffusion_parameters* parameters, double* packed);
+/* ParkerSolver(particles, grid, B, V, make_legacy_transport_coefficient_
+ * fields(...)): the basis is built on the device and stays there. */
+int kpt_parker_solver_create_from_fields(kpt_context* ctx, const kpt_grid* grid, const double* b,
+                                         const double* v, const kpt_turbulence* turbulence,
+                                         const kpt_particle_properties* properties,
+                                         const kpt_diffusion_parameters* parameters,
+                                         double courant, kpt_parker_solver** out);
+
 /* ======================================================================
  * ParticleGenerator (include/ParticleGenerator.hpp:659-1493): injection and
  * recycling on the library grid.  The reference draws from

@@ -146,6 +146,30 @@ class ParticleArrays(ctypes.Structure):
 _LIB: Optional[ctypes.CDLL] = None
 
 
+class Turbulence(ctypes.Structure):
+    """TurbulenceProperties for the coefficient precompute: storage 0 = the
+    constant state (sigma2, l2d, lslab, lc; lc <= 0 = the slab length),
+    storage 1 = per-point fields over the ghosted cells."""
+    _fields_ = [("storage", ctypes.c_int32), ("pad", ctypes.c_int32),
+                ("sigma2", ctypes.c_double), ("l2d", ctypes.c_double),
+                ("lslab", ctypes.c_double), ("lc", ctypes.c_double),
+                ("sigma2_field", ctypes.c_void_p), ("l2d_field", ctypes.c_void_p),
+                ("lslab_field", ctypes.c_void_p), ("lc_field", ctypes.c_void_p)]
+
+
+class DiffusionParameters(ctypes.Structure):
+    """LegencyModel::DiffusionModelParameters plus the drift floor and the
+    ghost-fill mode of make_legacy_transport_coefficient_fields."""
+    _fields_ = [("perpendicular_model", ctypes.c_int32), ("ghost_fill_mode", ctypes.c_int32),
+                ("parallel_prefactor", ctypes.c_double),
+                ("perpendicular_prefactor", ctypes.c_double),
+                ("perpendicular_parallel_ratio", ctypes.c_double),
+                ("minimum_magnetic_field_magnitude", ctypes.c_double),
+                ("minimum_solar_wind_speed", ctypes.c_double),
+                ("minimum_sigma2", ctypes.c_double),
+                ("minimum_magnetic_field_squared_for_drift", ctypes.c_double)]
+
+
 class Region(ctypes.Structure):
     """AxisAlignedParticleRegion<2> (ParticleGenerator.hpp:18-62)."""
     _fields_ = [("lower", ctypes.c_double * 2), ("upper", ctypes.c_double * 2)]
@@ -270,6 +294,9 @@ def load_library() -> ctypes.CDLL:
         "kpt_focus_advance_stochastic": (i32, [vp, vp, vp, u64, u32, vp]),
         "kpt_focus_advance_deterministic": (i32, [vp, vp, vp, vp]),
         "kpt_focus_advance_stochastic_steps": (i32, [vp, vp, vp, u64, u32, u32, vp]),
+        "kpt_default_diffusion_parameters": (None, [vp]),
+        "kpt_parker_coefficients": (i32, [vp, vp, vp, vp, vp, vp, vp, vp]),
+        "kpt_parker_solver_create_from_fields": (i32, [vp, vp, vp, vp, vp, vp, vp, dbl, pvp]),
         "kpt_lib_field_create": (i32, [vp, vp, i32, vp, vp, pvp]),
         "kpt_lib_field_destroy": (i32, [vp]),
         "kpt_lib_field_points": (i32, [vp, vp]),
@@ -539,6 +566,74 @@ class Context:
         if maximum_mu != 1.0:
             solver.set_maximum_mu(maximum_mu)
         return solver
+
+    # -- Parker coefficient precompute --------------------------------------
+    def diffusion_parameters(self, **overrides) -> DiffusionParameters:
+        p = DiffusionParameters()
+        self.lib.kpt_default_diffusion_parameters(ctypes.byref(p))
+        for k, v in overrides.items():
+            setattr(p, k, v)
+        return p
+
+    @staticmethod
+    def _turbulence(turbulence, keep: list) -> Turbulence:
+        t = Turbulence()
+        if turbulence is None:
+            turbulence = {"sigma2": 0.5, "l2d": 1.0, "lslab": 1.0, "lc": -1.0}
+        if isinstance(turbulence, Turbulence):
+            return turbulence
+        if "sigma2_field" in turbulence:
+            t.storage = 1
+            for name in ("sigma2", "l2d", "lslab", "lc"):
+                arr = turbulence.get(f"{name}_field")
+                if arr is not None:
+                    arr = np.ascontiguousarray(arr, dtype=np.float64)
+                    keep.append(arr)
+                    setattr(t, f"{name}_field", arr.ctypes.data)
+        else:
+            t.storage = 0
+            t.sigma2, t.l2d = float(turbulence["sigma2"]), float(turbulence["l2d"])
+            t.lslab, t.lc = float(turbulence["lslab"]), float(turbulence.get("lc", -1.0))
+        return t
+
+    def parker_coefficients(self, grid: "LibGrid", b, v, turbulence=None, parameters=None,
+                            rest_mass=1.0, charge=1.0, speed_of_light=1.0,
+                            energy_scale_erg=1.0) -> np.ndarray:
+        """make_legacy_transport_coefficient_fields + the solver's packed basis:
+        (points, 18) from cell-centred B and V (points, 3), ghosts as given."""
+        keep = []
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        if b.shape != (grid.points, 3) or v.shape != (grid.points, 3):
+            raise ValueError(f"B and V must be ({grid.points}, 3)")
+        t = self._turbulence(turbulence, keep)
+        props = ParticleProperties(rest_mass, charge, speed_of_light, energy_scale_erg)
+        params = parameters if parameters is not None else self.diffusion_parameters()
+        out = np.zeros((grid.points, 18), dtype=np.float64)
+        _check(self.lib.kpt_parker_coefficients(self.handle, grid.handle, _ptr(b), _ptr(v),
+                                                ctypes.byref(t), ctypes.byref(props),
+                                                ctypes.byref(params), _ptr(out)))
+        return out
+
+    def parker_solver_from_fields(self, grid: "LibGrid", b, v, turbulence=None,
+                                  parameters=None, courant: float = 0.3, rest_mass=1.0,
+                                  charge=1.0, speed_of_light=1.0,
+                                  energy_scale_erg=1.0) -> "ParkerSolver":
+        """ParkerSolver(particles, grid, B, V, make_legacy_transport_coefficient_
+        fields(...)) with the basis built and kept on the device."""
+        keep = []
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        if b.shape != (grid.points, 3) or v.shape != (grid.points, 3):
+            raise ValueError(f"B and V must be ({grid.points}, 3)")
+        t = self._turbulence(turbulence, keep)
+        props = ParticleProperties(rest_mass, charge, speed_of_light, energy_scale_erg)
+        params = parameters if parameters is not None else self.diffusion_parameters()
+        handle = ctypes.c_void_p()
+        _check(self.lib.kpt_parker_solver_create_from_fields(
+            self.handle, grid.handle, _ptr(b), _ptr(v), ctypes.byref(t), ctypes.byref(props),
+            ctypes.byref(params), float(courant), ctypes.byref(handle)))
+        return self._adopt(ParkerSolver(self, handle))
 
     # -- ParticleGenerator ---------------------------------------------------
     def lib_field(self, grid: "LibGrid", values, centering=(0, 0)) -> "LibField":

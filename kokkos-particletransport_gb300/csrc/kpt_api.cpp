@@ -84,6 +84,15 @@ struct DeviceBuffer {
     }
 };
 
+// A DeviceBuffer freed when it goes out of scope (scratch of one call; the
+// call synchronises its stream before returning).
+struct ScopedBuffer : DeviceBuffer {
+    ScopedBuffer() = default;
+    ScopedBuffer(const ScopedBuffer&) = delete;
+    ScopedBuffer& operator=(const ScopedBuffer&) = delete;
+    ~ScopedBuffer() { release(); }
+};
+
 }  // namespace
 
 struct kpt_context {
@@ -1382,7 +1391,7 @@ int kpt_surrogate_train(kpt_context* ctx, const kpt_settings* settings,
     box.qlt_h0 = settings->qlt_h0;
     cudaStream_t st = ctx->stream;
     const size_t n = static_cast<size_t>(c.samples);
-    DeviceBuffer data, work;
+    ScopedBuffer data, work;
     KPT_CUDA(data.reserve(n * (kpt::kMlpIn + kpt::kMlpOut) * sizeof(float)));
     float* x = data.as<float>();
     float* t = x + n * kpt::kMlpIn;
@@ -1537,7 +1546,7 @@ int kpt_surrogate_evaluate(kpt_surrogate* sg, uint64_t n, const double* inputs, 
     KPT_REQUIRE(n < (1ull << 30), "kpt_surrogate_evaluate: too many inputs");
     if (n == 0) return KPT_OK;
     KPT_CUDA(cudaSetDevice(sg->device));
-    DeviceBuffer buf;
+    ScopedBuffer buf;
     KPT_CUDA(buf.reserve(n * 8 * sizeof(double) + n * sizeof(int)));
     double* din = buf.as<double>();
     double* dout = din + n * 5;
@@ -1563,7 +1572,7 @@ int kpt_surrogate_gradient(kpt_context* ctx, const float* params, uint64_t n, co
     const size_t chunks = (n + kpt::kGradChunk - 1) / kpt::kGradChunk;
     const size_t floats =
         n * (5 + 3) + 2 * pcount + n * (5 + 4 * kpt::kMlpHidden + 3) + 1 + chunks * pcount;
-    DeviceBuffer buf;
+    ScopedBuffer buf;
     KPT_CUDA(buf.reserve(floats * sizeof(float)));
     KPT_CUDA(cudaMemsetAsync(buf.ptr, 0, floats * sizeof(float), ctx->stream));
     float* w = buf.as<float>();
@@ -2590,6 +2599,199 @@ int kpt_focus_advance_stochastic_steps(kpt_context* ctx, kpt_focus_solver* s, kp
 }  // extern "C"
 
 // ====================================================================
+// Parker coefficient precompute on the library grid
+// ====================================================================
+
+namespace {
+
+// DiffusionModelParameters::validate (LegencyModel.hpp:95-116),
+// ParticleProperties::validate (ParticleSystem.hpp:155-165) and the
+// floors' checks of the curl and divergence builders.
+int validate_coefficient_inputs(const kpt_turbulence* t, const kpt_particle_properties* pr,
+                                const kpt_diffusion_parameters* p) {
+    KPT_REQUIRE(std::isfinite(p->parallel_prefactor) && p->parallel_prefactor > 0.0 &&
+                    std::isfinite(p->perpendicular_prefactor) &&
+                    p->perpendicular_prefactor > 0.0 &&
+                    std::isfinite(p->perpendicular_parallel_ratio) &&
+                    p->perpendicular_parallel_ratio >= 0.0 &&
+                    std::isfinite(p->minimum_magnetic_field_magnitude) &&
+                    p->minimum_magnetic_field_magnitude >= 0.0 &&
+                    std::isfinite(p->minimum_solar_wind_speed) &&
+                    p->minimum_solar_wind_speed >= 0.0 && std::isfinite(p->minimum_sigma2) &&
+                    p->minimum_sigma2 >= 0.0,
+                "LegencyModel::DiffusionModelParameters: coefficients and floors must be "
+                "finite positive or non-negative values.");
+    KPT_REQUIRE(p->perpendicular_model == 0 || p->perpendicular_model == 1,
+                "kpt_diffusion_parameters: unknown perpendicular model");
+    KPT_REQUIRE(p->perpendicular_model == 0 || p->perpendicular_parallel_ratio > 0.0,
+                "LegencyModel::DiffusionModelParameters: constant perpendicular ratio must be "
+                "positive when selected.");
+    KPT_REQUIRE(p->ghost_fill_mode == 0 || p->ghost_fill_mode == 1,
+                "kpt_diffusion_parameters: unknown ghost fill mode");
+    KPT_REQUIRE(std::isfinite(pr->rest_mass) && pr->rest_mass > 0.0 &&
+                    std::isfinite(pr->charge) && std::isfinite(pr->speed_of_light) &&
+                    pr->speed_of_light > 0.0 && std::isfinite(pr->energy_scale_erg) &&
+                    pr->energy_scale_erg > 0.0,
+                "ParticleProperties: rest mass and speed of light must be positive finite "
+                "dimensionless values, charge must be finite, and the energy scale must be "
+                "positive and finite.");
+    KPT_REQUIRE(std::isfinite(p->minimum_magnetic_field_squared_for_drift) &&
+                    p->minimum_magnetic_field_squared_for_drift >= 0.0,
+                "ParkerCoefficient: magnetic field floor must be finite and non-negative.");
+    KPT_REQUIRE(t->storage == 0 || t->storage == 1, "kpt_turbulence: unknown storage");
+    if (t->storage == 0) {
+        const double lc = t->lc > 0.0 ? t->lc : t->lslab;
+        KPT_REQUIRE(std::isfinite(t->sigma2) && t->sigma2 > 0.0 && std::isfinite(t->l2d) &&
+                        t->l2d > 0.0 && std::isfinite(t->lslab) && t->lslab > 0.0 &&
+                        std::isfinite(lc) && lc > 0.0,
+                    "TurbulencePropertyModel: coefficients must be positive finite values.");
+    } else {
+        KPT_REQUIRE(t->sigma2_field && t->l2d_field && t->lc_field,
+                    "kpt_turbulence: field storage needs sigma2, l2d and lc fields");
+    }
+    return KPT_OK;
+}
+
+const char* coefficient_error_message(int code) {
+    switch (code) {
+        case 20: return "ParkerCoefficient: curl(B/B^2) is undefined where B^2 <= 0.";
+        case 21: return "LegencyModel: gyrofrequency requires |B| > 0.";
+        case 22: return "LegencyModel: kappa_parallel requires positive Vsw, Lc, omega, and sigma2.";
+        case 23:
+            return "LegencyModel: kappa_perpendicular requires positive Vsw, L2D, sigma2_2D, "
+                   "and kappa_parallel.";
+        case 24:
+            return "LegencyModel: constant-ratio kappa_perpendicular requires positive "
+                   "kappa_parallel and ratio.";
+        case 26:
+            return "ParkerCoefficient: diffusion tensor direction is undefined where |B| <= 0.";
+    }
+    return "ParkerCoefficient: coefficient precompute failed";
+}
+
+// Builds the packed basis into `packed` (device, points x kLibBasisStride).
+int build_parker_coefficients(kpt_context* ctx, const kpt_grid* grid, const double* b,
+                              const double* v, const kpt_turbulence* t,
+                              const kpt_particle_properties* pr,
+                              const kpt_diffusion_parameters* p, double* packed) {
+    if (int rc = validate_coefficient_inputs(t, pr, p)) return rc;
+    const uint64_t points = static_cast<uint64_t>(grid->nx + 4) * (grid->ny + 4);
+    const int fields = t->storage == 1 ? 3 : 0;
+    ScopedBuffer inputs;
+    const size_t vec_bytes = points * 3 * sizeof(double);
+    KPT_CUDA(inputs.reserve(2 * vec_bytes + fields * points * sizeof(double) + 64));
+    char* base = static_cast<char*>(inputs.ptr);
+    double* db = reinterpret_cast<double*>(base);
+    double* dv = reinterpret_cast<double*>(base + vec_bytes);
+    double* dt = reinterpret_cast<double*>(base + 2 * vec_bytes);
+    int* err = reinterpret_cast<int*>(base + 2 * vec_bytes + fields * points * sizeof(double));
+    KPT_CUDA(cudaMemcpyAsync(db, b, vec_bytes, cudaMemcpyHostToDevice, ctx->stream));
+    KPT_CUDA(cudaMemcpyAsync(dv, v, vec_bytes, cudaMemcpyHostToDevice, ctx->stream));
+    if (fields) {
+        const double* src[3] = {t->sigma2_field, t->l2d_field, t->lc_field};
+        for (int k = 0; k < 3; ++k) {
+            KPT_CUDA(cudaMemcpyAsync(dt + k * points, src[k], points * sizeof(double),
+                                     cudaMemcpyHostToDevice, ctx->stream));
+        }
+    }
+    const int no_error = kpt::parker_coefficients_no_error();
+    KPT_CUDA(cudaMemcpyAsync(err, &no_error, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    kpt::CoefLaunch L{};
+    L.grid = grid->g;
+    L.b = db;
+    L.v = dv;
+    L.turbulence_fields = fields ? 1 : 0;
+    L.sigma2 = t->sigma2;
+    L.l2d = t->l2d;
+    L.lc = t->lc > 0.0 ? t->lc : t->lslab;
+    L.sigma2_field = fields ? dt : nullptr;
+    L.l2d_field = fields ? dt + points : nullptr;
+    L.lc_field = fields ? dt + 2 * points : nullptr;
+    L.abs_charge = std::fabs(pr->charge);
+    L.rest_mass = pr->rest_mass;
+    L.speed_of_light = pr->speed_of_light;
+    L.constant_ratio = p->perpendicular_model == 1 ? 1 : 0;
+    L.parallel_prefactor = p->parallel_prefactor;
+    L.perpendicular_prefactor = p->perpendicular_prefactor;
+    L.ratio = p->perpendicular_parallel_ratio;
+    L.min_b = p->minimum_magnetic_field_magnitude;
+    L.min_vsw = p->minimum_solar_wind_speed;
+    L.min_sigma2 = p->minimum_sigma2;
+    L.drift_floor = p->minimum_magnetic_field_squared_for_drift;
+    L.ghost_mode = p->ghost_fill_mode;
+    L.packed = packed;
+    L.error = err;
+    KPT_CUDA(kpt::parker_coefficients(L, ctx->stream));
+    int code = no_error;
+    KPT_CUDA(cudaMemcpyAsync(&code, err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    KPT_CUDA(cudaStreamSynchronize(ctx->stream));
+    KPT_REQUIRE(code == no_error, coefficient_error_message(code));
+    return KPT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void kpt_default_diffusion_parameters(kpt_diffusion_parameters* out) {
+    if (out == nullptr) return;
+    *out = kpt_diffusion_parameters{};
+    out->perpendicular_model = 0;
+    out->ghost_fill_mode = 0;
+    out->parallel_prefactor = 1.622;
+    out->perpendicular_prefactor = 0.198;
+}
+
+int kpt_parker_coefficients(kpt_context* ctx, const kpt_grid* grid, const double* b,
+                            const double* v, const kpt_turbulence* turbulence,
+                            const kpt_particle_properties* properties,
+                            const kpt_diffusion_parameters* parameters, double* packed) {
+    KPT_REQUIRE(ctx && grid && b && v && turbulence && properties && parameters && packed,
+                "kpt_parker_coefficients: NULL argument");
+    if (int rc = activate(ctx)) return rc;
+    const uint64_t points = static_cast<uint64_t>(grid->nx + 4) * (grid->ny + 4);
+    ScopedBuffer out;
+    KPT_CUDA(out.reserve(points * kpt::kLibBasisStride * sizeof(double)));
+    if (int rc = build_parker_coefficients(ctx, grid, b, v, turbulence, properties, parameters,
+                                           out.as<double>())) {
+        return rc;
+    }
+    KPT_CUDA(cudaMemcpy(packed, out.ptr, points * kpt::kLibBasisStride * sizeof(double),
+                        cudaMemcpyDeviceToHost));
+    return KPT_OK;
+}
+
+int kpt_parker_solver_create_from_fields(kpt_context* ctx, const kpt_grid* grid, const double* b,
+                                         const double* v, const kpt_turbulence* turbulence,
+                                         const kpt_particle_properties* properties,
+                                         const kpt_diffusion_parameters* parameters,
+                                         double courant, kpt_parker_solver** out) {
+    KPT_REQUIRE(ctx && grid && b && v && turbulence && properties && parameters && out,
+                "kpt_parker_solver_create_from_fields: NULL argument");
+    *out = nullptr;
+    if (int rc = activate(ctx)) return rc;
+    std::unique_ptr<kpt_parker_solver> s(new kpt_parker_solver());
+    s->ctx = ctx;
+    s->device = ctx->device;
+    s->grid = grid->g;
+    s->points = static_cast<uint64_t>(grid->nx + 4) * static_cast<uint64_t>(grid->ny + 4);
+    s->courant = courant;
+    s->constant_ratio = parameters->perpendicular_model == 1 ? 1 : 0;
+    KPT_CUDA(cudaMalloc(&s->basis, s->points * kpt::kLibBasisStride * sizeof(double)));
+    KPT_CUDA(s->scalars.reserve(64));
+    kpt_parker_solver* raw = s.release();
+    if (int rc = build_parker_coefficients(ctx, grid, b, v, turbulence, properties, parameters,
+                                           raw->basis)) {
+        kpt_parker_solver_destroy(raw);
+        return rc;
+    }
+    *out = raw;
+    return KPT_OK;
+}
+
+}  // extern "C"
+
+// ====================================================================
 // ParticleGenerator: injection and recycling on the library grid
 // ====================================================================
 
@@ -2612,7 +2814,7 @@ struct kpt_candidates {
     int device = 0;
     kpt::LibGrid grid{};
     kpt::GenCandidates view{};
-    DeviceBuffer indices, cumulative;
+    ScopedBuffer indices, cumulative;
 };
 
 namespace {
@@ -2804,7 +3006,7 @@ int kpt_candidates_from_field(kpt_context* ctx, const kpt_lib_field* field,
     c->grid = field->grid;
     const uint64_t points = field->points;
     KPT_CUDA(c->indices.reserve(points * sizeof(uint64_t)));
-    DeviceBuffer block_counts, scratch;
+    ScopedBuffer block_counts, scratch;
     const uint64_t blocks = (points + 255) / 256;
     KPT_CUDA(block_counts.reserve(blocks * sizeof(unsigned int) + sizeof(unsigned long long) * 2));
     kpt::GenCandidateBuild B{};
@@ -2876,7 +3078,7 @@ int kpt_candidates_from_grid(kpt_context* ctx, const kpt_grid* grid, int32_t dom
         count *= static_cast<uint64_t>(v.extents[dim]);
     }
     KPT_CUDA(c->cumulative.reserve(count * sizeof(double)));
-    DeviceBuffer scratch;
+    ScopedBuffer scratch;
     KPT_CUDA(scratch.reserve(kpt::generator_scan_scratch(count) * sizeof(double)));
     KPT_CUDA(kpt::generator_grid_weights(grid->g, v.lower, v.extents, count,
                                          c->cumulative.as<double>(), scratch.as<double>(),

@@ -388,6 +388,31 @@ cudaError_t generator_grid_weights(const LibGrid& grid, const int lower[2], cons
 // Scratch doubles generator_*_weights need for count candidates.
 uint64_t generator_scan_scratch(uint64_t count);
 
+// Parker coefficient precompute (ParkerCoefficient.hpp:1102-1155) into the
+// packed basis (ParkerSolver.hpp:514-598) on the library grid: cell-centred
+// B and V (3 doubles per ghosted point) in, kLibBasisStride doubles per
+// point out.
+struct CoefLaunch {
+    LibGrid grid;
+    const double* b;
+    const double* v;
+    int turbulence_fields;          // 0 constant state, 1 per-point fields
+    double sigma2, l2d, lc;         // constant state (lc already resolved)
+    const double* sigma2_field;     // per point (turbulence_fields = 1)
+    const double* l2d_field;
+    const double* lc_field;
+    double abs_charge, rest_mass, speed_of_light;
+    int constant_ratio;
+    double parallel_prefactor, perpendicular_prefactor, ratio;
+    double min_b, min_vsw, min_sigma2;
+    double drift_floor;
+    int ghost_mode;                 // 0 PeriodicOrClamped, 1 PeriodicOnly
+    double* packed;
+    int* error;                     // failed check (device), parker_coefficients_no_error() if none
+};
+cudaError_t parker_coefficients(const CoefLaunch& launch, cudaStream_t stream);
+int parker_coefficients_no_error();
+
 struct SampleLaunch {
     Grid grid;
     const void* lower;

@@ -1449,6 +1449,301 @@ cudaError_t scan_inclusive_f64(double* values, uint64_t n, double* scratch, cuda
     return cudaGetLastError();
 }
 
+// ---- Parker coefficient precompute ------------------------------------------
+//
+// make_legacy_transport_coefficient_fields (ParkerCoefficient.hpp:1102-1155)
+// on the Cartesian library grid, written straight into the packed basis the
+// solver samples: curl(B/B^2), the gamma-one kappas, the diffusion-tensor
+// divergence bases, div V, each with its ghost cells filled.  Metric factors
+// are 1 and enter as exact multiplications by 1; every other operation is
+// rounded on its own in the reference's order, so only pow's last bits
+// differ from the reference build.
+
+__device__ __forceinline__ size_t coef_point(const LibGrid& g, int i, int j) {
+    return static_cast<size_t>(i + 2) + static_cast<size_t>(j + 2) * static_cast<size_t>(g.ex);
+}
+
+// centered_three_point_derivative (ParkerCoefficient.hpp:215-234).
+__device__ double coef_d3(double lc, double cc, double uc, double lv, double cv, double uv) {
+    const double lw = __dsub_rn(cc, lc);
+    const double uw = __dsub_rn(uc, cc);
+    const double tw = __dsub_rn(uc, lc);
+    const double a = __ddiv_rn(-uw, __dmul_rn(lw, tw));
+    const double b = __ddiv_rn(__dsub_rn(uw, lw), __dmul_rn(lw, uw));
+    const double c = __ddiv_rn(lw, __dmul_rn(uw, tw));
+    return __dadd_rn(__dadd_rn(__dmul_rn(a, lv), __dmul_rn(b, cv)), __dmul_rn(c, uv));
+}
+
+__device__ __forceinline__ double coef_norm2(const double* row) {
+    double s = 0.0;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) s = __dadd_rn(s, __dmul_rn(row[c], row[c]));
+    return s;
+}
+
+// Errors: the word starts at kCoefNoError and keeps the smallest code, the
+// codes numbered in the reference's stage order (curl before the kappas
+// before the divergence bases), so the message is the one the reference
+// aborts with first.
+constexpr int kCoefNoError = 0x7fffffff;
+__device__ __forceinline__ void coef_set_error(int* error, int code) { atomicMin(error, code); }
+
+// B_c / max(B^2, floor) (ParkerCoefficient.hpp:278-305), times h_c = 1.
+__device__ __forceinline__ double coef_b_over_b2(const CoefLaunch& L, int i, int j, int c) {
+    const double* row = L.b + 3 * coef_point(L.grid, i, j);
+    const double b2 = coef_norm2(row);
+    if (b2 <= 0.0 && L.drift_floor <= 0.0) {
+        coef_set_error(L.error, 20);  // curl(B/B^2) is undefined where B^2 <= 0
+    }
+    const double den = b2 > L.drift_floor ? b2 : L.drift_floor;
+    return __ddiv_rn(row[c], den);
+}
+
+// centered_metric_weighted_derivative (ParkerCoefficient.hpp:332-387):
+// (upper - lower) / (x_upper - x_lower) along dim of h_c B_c / B^2.
+__device__ double coef_curl_derivative(const CoefLaunch& L, int i, int j, int dim, int c) {
+    if (dim >= 2 || L.grid.axis[dim].n <= 1) return 0.0;
+    const int li = dim == 0 ? i - 1 : i, lj = dim == 1 ? j - 1 : j;
+    const int ui = dim == 0 ? i + 1 : i, uj = dim == 1 ? j + 1 : j;
+    const LibAxis& a = L.grid.axis[dim];
+    const double width = __dsub_rn(gen_coordinate(a, dim == 0 ? ui : uj, 0),
+                                   gen_coordinate(a, dim == 0 ? li : lj, 0));
+    return __ddiv_rn(__dsub_rn(coef_b_over_b2(L, ui, uj, c), coef_b_over_b2(L, li, lj, c)),
+                     width);
+}
+
+// One gamma-independent diffusion tensor basis component
+// (ParkerCoefficient.hpp:606-641); basis 0 parallel projection, 1
+// perpendicular projection, 2 constant parallel ratio.
+__device__ double coef_tensor(const CoefLaunch& L, int i, int j, int oc, int dc, int basis) {
+    const size_t p = coef_point(L.grid, i, j);
+    const double* row = L.b + 3 * p;
+    const double magnitude = __dsqrt_rn(coef_norm2(row));
+    if (magnitude <= 0.0 && L.min_b <= 0.0) {
+        coef_set_error(L.error, 26);  // diffusion tensor direction is undefined where |B| <= 0
+    }
+    const double den = magnitude > L.min_b ? magnitude : L.min_b;
+    const double bi = __ddiv_rn(row[oc], den);
+    const double bj = __ddiv_rn(row[dc], den);
+    const double projection = __dmul_rn(bi, bj);
+    const double identity = oc == dc ? 1.0 : 0.0;
+    const double kpar = L.packed[p * kLibBasisStride + 15];
+    if (basis == 0) return __dmul_rn(kpar, projection);
+    if (basis == 1) {
+        return __dmul_rn(L.packed[p * kLibBasisStride + 16], __dsub_rn(identity, projection));
+    }
+    return __dmul_rn(kpar, __dadd_rn(__dmul_rn(L.ratio, identity),
+                                     __dmul_rn(__dsub_rn(1.0, L.ratio), projection)));
+}
+
+// centered_lame_derivative of h = 1 along dim (ParkerCoefficient.hpp:746-790).
+__device__ double coef_lame(const CoefLaunch& L, int i, int j, int dim) {
+    if (dim >= 2 || L.grid.axis[dim].n <= 1) return 0.0;
+    const LibAxis& a = L.grid.axis[dim];
+    const int k = dim == 0 ? i : j;
+    return coef_d3(gen_coordinate(a, k - 1, 0), gen_coordinate(a, k, 0),
+                   gen_coordinate(a, k + 1, 0), 1.0, 1.0, 1.0);
+}
+
+// diffusion_tensor_divergence_basis_component (ParkerCoefficient.hpp:794-877).
+__device__ double coef_divergence_basis(const CoefLaunch& L, int i, int j, int oc, int basis) {
+    double result = 0.0;
+    for (int dim = 0; dim < 2; ++dim) {
+        if (L.grid.axis[dim].n <= 1) {
+            result = __dadd_rn(result, 0.0);
+            continue;
+        }
+        const LibAxis& a = L.grid.axis[dim];
+        const int k = dim == 0 ? i : j;
+        const double lv = coef_tensor(L, dim == 0 ? i - 1 : i, dim == 1 ? j - 1 : j, oc, dim, basis);
+        const double cv = coef_tensor(L, i, j, oc, dim, basis);
+        const double uv = coef_tensor(L, dim == 0 ? i + 1 : i, dim == 1 ? j + 1 : j, oc, dim, basis);
+        result = __dadd_rn(result, coef_d3(gen_coordinate(a, k - 1, 0), gen_coordinate(a, k, 0),
+                                           gen_coordinate(a, k + 1, 0), lv, cv, uv));
+    }
+    for (int c = 0; c < 3; ++c) {
+        if (c == oc) continue;
+        if (c < 2) {
+            const double t = coef_tensor(L, i, j, oc, c, basis);
+            result = __dadd_rn(result, __dmul_rn(t, coef_lame(L, i, j, c)));
+        }
+        if (oc < 2) {
+            const double t = coef_tensor(L, i, j, c, c, basis);
+            result = __dsub_rn(result, __dmul_rn(t, coef_lame(L, i, j, oc)));
+        }
+    }
+    return result;
+}
+
+__device__ __forceinline__ double coef_floor(double v, double f) {
+    if (f <= 0.0) return v;
+    return v < f ? f : v;
+}
+
+// Stage 1: B and V into the packed rows (every point, ghosts as given), the
+// derived slots zeroed (the reference's freshly allocated fields), and the
+// gamma-one kappas at the physical points
+// (LegencyModel.hpp:434-470, :801-862).
+__global__ void coef_kappa_kernel(const CoefLaunch L) {
+    const uint64_t points = static_cast<uint64_t>(L.grid.ex) * (L.grid.axis[1].n + 4);
+    for (uint64_t p = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; p < points;
+         p += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        double* out = L.packed + p * kLibBasisStride;
+        const double* b = L.b + 3 * p;
+        const double* v = L.v + 3 * p;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            out[c] = b[c];
+            out[3 + c] = v[c];
+        }
+#pragma unroll
+        for (int c = 6; c < kLibBasis; ++c) out[c] = 0.0;
+        const int i = static_cast<int>(p % static_cast<uint64_t>(L.grid.ex)) - 2;
+        const int j = static_cast<int>(p / static_cast<uint64_t>(L.grid.ex)) - 2;
+        if (i < 0 || i >= L.grid.axis[0].n || j < 0 || j >= L.grid.axis[1].n) continue;
+        const double safe_b = coef_floor(__dsqrt_rn(coef_norm2(b)), L.min_b);
+        const double safe_vsw = coef_floor(__dsqrt_rn(coef_norm2(v)), L.min_vsw);
+        const double sigma2 = L.turbulence_fields ? L.sigma2_field[p] : L.sigma2;
+        const double l2d = L.turbulence_fields ? L.l2d_field[p] : L.l2d;
+        const double lc = L.turbulence_fields ? L.lc_field[p] : L.lc;
+        const double safe_sigma2 = coef_floor(sigma2, L.min_sigma2);
+        // curl(B/B^2) reads B^2 at the x and y neighbours first
+        if (L.drift_floor <= 0.0) {
+#pragma unroll
+            for (int dim = 0; dim < 2; ++dim) {
+                if (L.grid.axis[dim].n <= 1) continue;
+#pragma unroll
+                for (int side = -1; side <= 1; side += 2) {
+                    const size_t q = coef_point(L.grid, dim == 0 ? i + side : i,
+                                                dim == 1 ? j + side : j);
+                    if (coef_norm2(L.b + 3 * q) <= 0.0) coef_set_error(L.error, 20);
+                }
+            }
+        }
+        if (safe_b <= 0.0) {
+            coef_set_error(L.error, 21);  // gyrofrequency requires |B| > 0
+            continue;
+        }
+        const double omega = __ddiv_rn(__dmul_rn(L.abs_charge, safe_b),
+                                       __dmul_rn(L.rest_mass, L.speed_of_light));
+        if (safe_vsw <= 0.0 || lc <= 0.0 || omega <= 0.0 || safe_sigma2 <= 0.0) {
+            coef_set_error(L.error, 22);  // kappa_parallel requires positive inputs
+            continue;
+        }
+        const double kpar = __ddiv_rn(
+            __dmul_rn(__dmul_rn(L.parallel_prefactor, pow(safe_vsw, 4.0 / 3.0)),
+                      pow(lc, 2.0 / 3.0)),
+            __dmul_rn(pow(omega, 1.0 / 3.0), safe_sigma2));
+        double kperp;
+        if (L.constant_ratio) {
+            if (kpar <= 0.0 || L.ratio <= 0.0) {
+                coef_set_error(L.error, 24);
+                continue;
+            }
+            kperp = __dmul_rn(L.ratio, kpar);
+        } else {
+            if (safe_vsw <= 0.0 || l2d <= 0.0 || safe_sigma2 <= 0.0 || kpar <= 0.0) {
+                coef_set_error(L.error, 23);
+                continue;
+            }
+            kperp = __dmul_rn(
+                __dmul_rn(__ddiv_rn(safe_vsw, 3.0),
+                          pow(__ddiv_rn(__dmul_rn(3.0, kpar), safe_vsw), 1.0 / 3.0)),
+                pow(__dmul_rn(__dmul_rn(L.perpendicular_prefactor, safe_sigma2), l2d),
+                    2.0 / 3.0));
+        }
+        out[15] = kpar;
+        out[16] = kperp;
+    }
+}
+
+// Field::fill_ghost_cells for cell-centred packed slots [first, last] and
+// slot `extra` (Field.hpp:274-316): a ghost point copies its periodic image
+// or, on an open axis, the nearest physical point (PeriodicOnly leaves it).
+__global__ void coef_ghost_kernel(const CoefLaunch L, int first, int last, int extra) {
+    const uint64_t points = static_cast<uint64_t>(L.grid.ex) * (L.grid.axis[1].n + 4);
+    for (uint64_t p = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; p < points;
+         p += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        int idx[2] = {static_cast<int>(p % static_cast<uint64_t>(L.grid.ex)) - 2,
+                      static_cast<int>(p / static_cast<uint64_t>(L.grid.ex)) - 2};
+        bool ghost = false;
+        bool skip = false;
+#pragma unroll
+        for (int dim = 0; dim < 2; ++dim) {
+            const int n = L.grid.axis[dim].n;
+            if (idx[dim] < 0 || idx[dim] > n - 1) {
+                ghost = true;
+                if (L.grid.axis[dim].periodic) {
+                    int w = idx[dim] % n;
+                    if (w < 0) w += n;
+                    idx[dim] = w;
+                } else if (L.ghost_mode == 1) {
+                    skip = true;
+                } else {
+                    idx[dim] = idx[dim] < 0 ? 0 : n - 1;
+                }
+            }
+        }
+        if (!ghost || skip) continue;
+        const double* src = L.packed + coef_point(L.grid, idx[0], idx[1]) * kLibBasisStride;
+        double* dst = L.packed + p * kLibBasisStride;
+        for (int c = first; c <= last; ++c) dst[c] = src[c];
+        if (extra >= 0) dst[extra] = src[extra];
+    }
+}
+
+// Stage 2 (after the kappas' ghosts): curl(B/B^2), the divergence bases
+// and div V at the physical points.
+__global__ void coef_derivative_kernel(const CoefLaunch L) {
+    const int nx = L.grid.axis[0].n, ny = L.grid.axis[1].n;
+    const uint64_t cells = static_cast<uint64_t>(nx) * ny;
+    if (*L.error != kCoefNoError) return;
+    for (uint64_t q = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; q < cells;
+         q += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        const int i = static_cast<int>(q % static_cast<uint64_t>(nx));
+        const int j = static_cast<int>(q / static_cast<uint64_t>(nx));
+        double* out = L.packed + coef_point(L.grid, i, j) * kLibBasisStride;
+        // magnetic_field_over_magnitude_squared_curl_component (:389-422)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const int da = (c + 1) % 3, db = (c + 2) % 3;
+            const double a = coef_curl_derivative(L, i, j, da, db);
+            const double b = coef_curl_derivative(L, i, j, db, da);
+            out[6 + c] = __dsub_rn(a, b);
+        }
+        // diffusion tensor divergence bases (:960-1095)
+#pragma unroll 1
+        for (int c = 0; c < 3; ++c) {
+            if (L.constant_ratio) {
+                const double value = coef_divergence_basis(L, i, j, c, 2);
+                out[9 + c] = value;
+                out[12 + c] = value;
+            } else {
+                out[9 + c] = coef_divergence_basis(L, i, j, c, 0);
+                out[12 + c] = coef_divergence_basis(L, i, j, c, 1);
+            }
+        }
+        // FieldOperator::divergence_value of V (FieldOperator.hpp:262-277)
+        double div = 0.0;
+        for (int dim = 0; dim < 2; ++dim) {
+            if (L.grid.axis[dim].n <= 1) {
+                div = __dadd_rn(div, 0.0);
+                continue;
+            }
+            const LibAxis& a = L.grid.axis[dim];
+            const int k = dim == 0 ? i : j;
+            const double lv = L.v[3 * coef_point(L.grid, dim == 0 ? i - 1 : i,
+                                                 dim == 1 ? j - 1 : j) + dim];
+            const double cv = L.v[3 * coef_point(L.grid, i, j) + dim];
+            const double uv = L.v[3 * coef_point(L.grid, dim == 0 ? i + 1 : i,
+                                                 dim == 1 ? j + 1 : j) + dim];
+            div = __dadd_rn(div, coef_d3(gen_coordinate(a, k - 1, 0), gen_coordinate(a, k, 0),
+                                         gen_coordinate(a, k + 1, 0), lv, cv, uv));
+        }
+        out[17] = div;
+    }
+}
+
 int grid_for(uint64_t n, int threads) {
     const uint64_t want = (n + threads - 1) / threads;
     return static_cast<int>(want < 1 ? 1 : (want > 152u * 32u ? 152u * 32u : want));
@@ -1630,6 +1925,18 @@ cudaError_t generator_grid_weights(const LibGrid& g, const int lower[2], const i
 
 uint64_t generator_scan_scratch(uint64_t count) {
     return (count + kScanTile - 1) / kScanTile + 1;
+}
+
+int parker_coefficients_no_error() { return kCoefNoError; }
+
+cudaError_t parker_coefficients(const CoefLaunch& L, cudaStream_t stream) {
+    const uint64_t points = static_cast<uint64_t>(L.grid.ex) * (L.grid.axis[1].n + 4);
+    const uint64_t cells = static_cast<uint64_t>(L.grid.axis[0].n) * L.grid.axis[1].n;
+    coef_kappa_kernel<<<grid_for(points, 256), 256, 0, stream>>>(L);
+    coef_ghost_kernel<<<grid_for(points, 256), 256, 0, stream>>>(L, 15, 16, -1);
+    coef_derivative_kernel<<<grid_for(cells, 128), 128, 0, stream>>>(L);
+    coef_ghost_kernel<<<grid_for(points, 256), 256, 0, stream>>>(L, 6, 14, 17);
+    return cudaGetLastError();
 }
 
 }  // namespace kpt

@@ -963,3 +963,82 @@ long long ref_lib_candidates(int nx, int ny, const double* x_edges, const double
 }
 
 }  // extern "C"
+
+// ---- Parker coefficient precompute on the library grid ---------------------
+extern "C" {
+
+// ParkerCoefficient::make_legacy_transport_coefficient_fields
+// (include/ParkerCoefficient.hpp:1102-1155) from cell-centred B and V (3
+// doubles per ghosted point, ghosts as given), then the solver's packed
+// basis (ParkerSolver.hpp:514-598) copied to packed (18 doubles per point).
+// turb_mode 0: constant state turb[4] = sigma2, l2d, lslab, lc (lc <= 0 =
+// the slab length); 1: per-point fields turb_fields[4][points] = sigma2,
+// l2d, lslab, lc.  props = rest mass, charge, c, energy scale; params =
+// model (0 README, 1 constant ratio), parallel prefactor, perpendicular
+// prefactor, ratio, minimum |B|, minimum Vsw, minimum sigma2; drift_floor =
+// minimum B^2 of curl(B/B^2); ghost_mode 0 PeriodicOrClamped, 1 PeriodicOnly.
+long long ref_lib_parker_coefficients(int nx, int ny, const double* x_edges,
+                                      const double* y_edges, const int* periodic,
+                                      const double* b_values, const double* v_values,
+                                      int turb_mode, const double* turb,
+                                      const double* turb_fields, const double* props,
+                                      const double* params, double drift_floor, int ghost_mode,
+                                      double* packed_out) {
+    try {
+        using solver_type = ParkerSolver<LibAnalyticGrid>;
+        using vector_field = typename solver_type::vector_field_type;
+        const LibAnalyticGrid grid = make_lib_analytic_grid(nx, ny, x_edges, y_edges, periodic);
+        vector_field b(grid, "coef_b", GridCentering::CellCentered);
+        vector_field v(grid, "coef_v", GridCentering::CellCentered);
+        const std::size_t points = b.point_count();
+        for (std::size_t k = 0; k < points; ++k) {
+            for (int c = 0; c < 3; ++c) {
+                b.data(k, c) = b_values[3 * k + c];
+                v.data(k, c) = v_values[3 * k + c];
+            }
+        }
+        const auto model = TurbulencePropertyModel::constant_code_units(turb[0], turb[1],
+                                                                        turb[2], turb[3]);
+        TurbulenceProperties<LibAnalyticGrid> turbulence(
+            grid, model,
+            turb_mode == 0 ? TurbulencePropertyStorageMode::ConstantOnly
+                           : TurbulencePropertyStorageMode::Field);
+        if (turb_mode != 0) {
+            for (std::size_t k = 0; k < points; ++k) {
+                turbulence.sigma2.data(k, 0) = turb_fields[0 * points + k];
+                turbulence.l2d.data(k, 0) = turb_fields[1 * points + k];
+                turbulence.lslab.data(k, 0) = turb_fields[2 * points + k];
+                turbulence.lc.data(k, 0) = turb_fields[3 * points + k];
+            }
+        }
+        LegencyModel::DiffusionModelParameters parameters;
+        parameters.parallel_prefactor = params[1];
+        parameters.perpendicular_prefactor = params[2];
+        parameters.minimum_magnetic_field_magnitude = params[4];
+        parameters.minimum_solar_wind_speed = params[5];
+        parameters.minimum_sigma2 = params[6];
+        if (static_cast<int>(params[0]) == 1) {
+            parameters.set_constant_perpendicular_parallel_ratio(params[3]);
+        } else {
+            parameters.perpendicular_parallel_ratio = params[3];
+            parameters.use_readme_perpendicular_formula();
+        }
+        const auto coefficients = ParkerCoefficient::make_legacy_transport_coefficient_fields(
+            b, v, turbulence, lib_properties(props), "coef", parameters, drift_floor,
+            ghost_mode == 0 ? FieldGhostFillMode::PeriodicOrClamped
+                            : FieldGhostFillMode::PeriodicOnly);
+        LibSystem sys(0, 1, lib_properties(props));
+        solver_type solver(sys, grid, b, v, coefficients);
+        for (std::size_t k = 0; k < points; ++k) {
+            for (int c = 0; c < 18; ++c) {
+                packed_out[18 * k + c] = solver.packed_coefficient_basis.data(k, c);
+            }
+        }
+        return static_cast<long long>(points);
+    } catch (const std::exception& error) {
+        g_last_error = error.what();
+        return -1;
+    }
+}
+
+}  // extern "C"

@@ -31,6 +31,12 @@ Cases
                       sets (indices and cumulative volumes), injection and
                       recycling from them, cell/face/mixed centred fields,
                       physical and ghosted domains
+  lib_parker_coefficients.npz
+                      ParkerCoefficient::make_legacy_transport_coefficient_
+                      fields and the solver's packed basis: README and
+                      constant-ratio branches, constant and field
+                      turbulence, floors, both ghost-fill modes, open and
+                      periodic axes, and two failures' messages
   lib_system.npz      ParticleSystem lifecycle: boundary conditions,
                       sort_by_key, compact_active_particles,
                       split_particles_on_energy_growth, capture_previous_positions
@@ -46,6 +52,7 @@ from __future__ import annotations
 import importlib
 import os
 import shutil
+import subprocess
 import sys
 import tempfile
 
@@ -54,7 +61,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
-sys.path.insert(0, os.path.join(ROOT, "oracle"))
+ORACLE = os.path.join(ROOT, "oracle")
+sys.path.insert(0, ORACLE)
 
 fields = importlib.import_module("kokkos-particletransport_gb300.fields")
 binding = importlib.import_module("binding")
@@ -507,6 +515,103 @@ def make_generator(ref, out_dir):
              candidate_cases=np.array([c[0] for c in CANDIDATE_CASES]), **arrays)
 
 
+def coefficient_inputs(nx: int, ny: int, x_edges, y_edges, variant: int):
+    """Cell-centred B and V over the ghosted cells (x fastest), analytic
+    everywhere (the caller's ghost values), plus turbulence fields."""
+    dx = (x_edges[-1] - x_edges[0]) / nx
+    dy = (y_edges[-1] - y_edges[0]) / ny
+    xc = x_edges[0] + (np.arange(nx + 4) - 1.5) * dx
+    yc = y_edges[0] + (np.arange(ny + 4) - 1.5) * dy
+    X, Y = np.meshgrid(xc, yc)
+    bz = 0.3 + 0.1 * variant * np.cos(X + Y)
+    b = np.stack([np.tanh(Y / 0.5) + 0.05 * np.sin(3 * X), 0.2 * np.sin(X) + 0.1 * variant,
+                  bz], axis=-1).reshape(-1, 3)
+    v = np.stack([1.0 + 0.1 * np.cos(X), 0.2 * np.sin(Y), 0.05 * variant * X],
+                 axis=-1).reshape(-1, 3)
+    fields = (0.3 + 0.1 * np.cos(2 * X) * np.exp(-Y ** 2),   # sigma2
+              0.8 + 0.3 * np.abs(np.sin(Y)),                # l2d
+              1.2 + 0.2 * X ** 2,                           # lslab
+              0.9 + 0.1 * np.cos(X * Y))                    # lc
+    return b, v, [f.ravel() for f in fields]
+
+
+# name, periodic, variant, turbulence ("constant" or "fields"), params,
+# charge, drift floor, ghost mode
+COEFFICIENT_CASES = (
+    ("readme_constant", (1, 0), 0, "constant", dict(), 1.0, 0.0, 0),
+    ("ratio_floors", (1, 0), 1, "constant",
+     dict(model=1, ratio=0.05, minimum_b=0.25, minimum_vsw=0.9, minimum_sigma2=0.4), -2.0,
+     1e-3, 0),
+    ("readme_fields_periodic_only", (0, 1), 2, "fields",
+     dict(parallel_prefactor=1.5, perpendicular_prefactor=0.25), 1.0, 0.0, 1),
+    ("ratio_fields_open", (0, 0), 1, "fields", dict(model=1, ratio=0.3), 0.5, 0.0, 0),
+)
+
+
+def make_parker_coefficients(ref, out_dir):
+    """The reference's Parker coefficient precompute and packed basis."""
+    nx, ny = 20, 28
+    xe = np.linspace(-1.3, 2.1, nx + 1)
+    ye = np.linspace(-2.0, 2.0, ny + 1)
+    arrays = {}
+    for name, periodic, variant, turb, params, charge, floor, ghost in COEFFICIENT_CASES:
+        grid = dict(x_edges=xe, y_edges=ye, periodic=np.array(periodic, dtype=np.int32))
+        b, v, fields = coefficient_inputs(nx, ny, xe, ye, variant)
+        constant = (0.35, 0.9, 1.4, -1.0 if variant == 0 else 1.1)
+        props = dict(rest_mass=1.0, charge=charge, speed_of_light=1.0)
+        packed = ref.lib_parker_coefficients(
+            grid, b, v, turbulence=constant,
+            turbulence_fields=fields if turb == "fields" else None, props=props,
+            params=params, drift_floor=floor, ghost_mode=ghost)
+        arrays[f"{name}_periodic"] = grid["periodic"]
+        arrays[f"{name}_b"] = b
+        arrays[f"{name}_v"] = v
+        arrays[f"{name}_turbulence"] = np.array(constant)
+        arrays[f"{name}_fields"] = np.stack(fields) if turb == "fields" else np.zeros((0,))
+        arrays[f"{name}_params"] = np.array(
+            [params.get("model", 0), params.get("parallel_prefactor", 1.622),
+             params.get("perpendicular_prefactor", 0.198), params.get("ratio", 0.0),
+             params.get("minimum_b", 0.0), params.get("minimum_vsw", 0.0),
+             params.get("minimum_sigma2", 0.0), floor, ghost, charge])
+        arrays[f"{name}_packed"] = packed
+    # failures: the reference's messages
+    grid = dict(x_edges=xe, y_edges=ye, periodic=np.array((1, 0), dtype=np.int32))
+    errors = []
+    b, v, fields = coefficient_inputs(nx, ny, xe, ye, 0)
+    zero_b = b.copy()
+    zero_b[(nx + 4) * 10 + 7] = 0.0
+    bad_lc = [f.copy() for f in fields]
+    bad_lc[3][(nx + 4) * 12 + 9] = -1.0
+    # Kokkos::abort ends the process, so each failure runs in a child
+    # that reports the shim's abort message
+    with tempfile.TemporaryDirectory() as tmp:
+        for label, b_in, turb_fields in (("zero_b", zero_b, None),
+                                         ("negative_lc", b, bad_lc)):
+            path = os.path.join(tmp, f"{label}.npz")
+            np.savez(path, b=b_in, v=v, xe=xe, ye=ye,
+                     fields=np.stack(turb_fields) if turb_fields is not None else np.zeros(0))
+            code = (
+                "import sys, numpy as np; sys.path.insert(0, %r); import binding\n"
+                "d = np.load(%r); f = d['fields']\n"
+                "grid = dict(x_edges=d['xe'], y_edges=d['ye'], periodic=np.array((1, 0)))\n"
+                "binding.ReferenceHarness().lib_parker_coefficients(grid, d['b'], d['v'], "
+                "turbulence_fields=list(f) if f.size else None)\n" % (ORACLE, path))
+            proc = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True)
+            message = ""
+            for line in proc.stderr.splitlines():
+                if line.startswith("Kokkos shim abort: "):
+                    message = line[len("Kokkos shim abort: "):].strip()
+            errors.append((label, message))
+    arrays["error_names"] = np.array([e[0] for e in errors])
+    arrays["error_messages"] = np.array([e[1] for e in errors])
+    arrays["error_zero_b"] = zero_b
+    arrays["error_negative_lc"] = np.stack(bad_lc)
+    arrays["error_b"] = b
+    arrays["error_v"] = v
+    lib_save(out_dir, "lib_parker_coefficients.npz", x_edges=xe, y_edges=ye,
+             cases=np.array([c[0] for c in COEFFICIENT_CASES]), **arrays)
+
+
 def main() -> None:
     ref = binding.ReferenceHarness()
     out_dir = HERE
@@ -516,8 +621,12 @@ def main() -> None:
     if sys.argv[1:] == ["generator"]:
         make_generator(ref, out_dir)
         return
+    if sys.argv[1:] == ["coefficients"]:
+        make_parker_coefficients(ref, out_dir)
+        return
     make_lib(ref, out_dir)
     make_generator(ref, out_dir)
+    make_parker_coefficients(ref, out_dir)
     if sys.argv[1:] == ["lib"]:
         return
     make_c1(ref, out_dir)
