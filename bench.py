@@ -469,17 +469,21 @@ def run_coefficients(ctx, grid, xe, ye):
     v = np.stack([1.0 + 0.1 * np.cos(np.pi * X), 0.1 * np.sin(Y), 0.0 * X],
                  axis=-1).reshape(-1, 3)
     turbulence = {"sigma2": 0.35, "l2d": 0.9, "lslab": 1.4}
-    times = []
-    for _ in range(3):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        solver = ctx.parker_solver_from_fields(grid, b, v, turbulence)
-        times.append((time.perf_counter() - t0) * 1e3)
-        solver.close()
     points = b.shape[0]
-    return {"points": points, "ms": min(times),
-            "value": points / (min(times) / 1e3), "unit": "grid points/s",
-            "note": "host B, V upload included; basis stays on the device"}
+    out = {"points": points, "unit": "grid points/s",
+           "note": "host B, V upload included; basis stays on the device"}
+    for label, make in (("parker", lambda: ctx.parker_solver_from_fields(grid, b, v, turbulence)),
+                        ("focus", lambda: ctx.focus_solver_from_fields(grid, b, v, None,
+                                                                       turbulence))):
+        times = []
+        for _ in range(3):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            solver = make()
+            times.append((time.perf_counter() - t0) * 1e3)
+            solver.close()
+        out[label] = {"ms": min(times), "value": points / (min(times) / 1e3)}
+    return out
 
 
 def run_generator(kpt, ctx, grid, xe, ye, n, stream):

@@ -584,6 +584,28 @@ int kpt_parker_coefficients(kpt_context* ctx, const kpt_grid* grid, const double
                             const double* v, const kpt_turbulence* turbulence,
                             const kpt_particle_properties* properties,
                             const kpt_diffusion_parameters* parameters, double* packed);
+/* Focused packed basis (grid points x 27, host) from cell-centred B, V and
+ * partial_t V (grid points x 3, host; dvdt NULL = zero, the
+ * make_legacy_transport_coefficient_fields overload): FocusCoefficient::
+ * make_legacy_transport_coefficient_fields_with_time_derivative
+ * (FocusCoefficient.hpp:852-993) and FocusSolver's packed layout
+ * (FocusSolver.hpp:106-136).  minimum_magnetic_field_magnitude is the
+ * builder's floor for b, ln |B| and the drift bases. */
+int kpt_focus_coefficients(kpt_context* ctx, const kpt_grid* grid, const double* b,
+                           const double* v, const double* dvdt, const kpt_turbulence* turbulence,
+                           const kpt_particle_properties* properties,
+                           const kpt_diffusion_parameters* parameters,
+                           double minimum_magnetic_field_magnitude, double* packed);
+/* FocusTransportSolver(particles, grid, B, V, coefficients) with the
+ * coefficients built on the device and kept there. */
+int kpt_focus_solver_create_from_fields(kpt_context* ctx, const kpt_grid* grid, const double* b,
+                                        const double* v, const double* dvdt,
+                                        const kpt_turbulence* turbulence,
+                                        const kpt_particle_properties* properties,
+                                        const kpt_diffusion_parameters* parameters,
+                                        double minimum_magnetic_field_magnitude, double courant,
+                                        const kpt_scattering_parameters* scattering,
+                                        kpt_focus_solver** out);
 /* ParkerSolver(particles, grid, B, V, make_legacy_transport_coefficient_
  * fields(...)): the basis is built on the device and stays there. */
 int kpt_parker_solver_create_from_fields(kpt_context* ctx, const kpt_grid* grid, const double* b,

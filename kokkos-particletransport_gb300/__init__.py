@@ -297,6 +297,9 @@ def load_library() -> ctypes.CDLL:
         "kpt_default_diffusion_parameters": (None, [vp]),
         "kpt_parker_coefficients": (i32, [vp, vp, vp, vp, vp, vp, vp, vp]),
         "kpt_parker_solver_create_from_fields": (i32, [vp, vp, vp, vp, vp, vp, vp, dbl, pvp]),
+        "kpt_focus_coefficients": (i32, [vp, vp, vp, vp, vp, vp, vp, vp, dbl, vp]),
+        "kpt_focus_solver_create_from_fields": (i32, [vp, vp, vp, vp, vp, vp, vp, vp, dbl, dbl,
+                                                      vp, pvp]),
         "kpt_lib_field_create": (i32, [vp, vp, i32, vp, vp, pvp]),
         "kpt_lib_field_destroy": (i32, [vp]),
         "kpt_lib_field_points": (i32, [vp, vp]),
@@ -634,6 +637,60 @@ class Context:
             self.handle, grid.handle, _ptr(b), _ptr(v), ctypes.byref(t), ctypes.byref(props),
             ctypes.byref(params), float(courant), ctypes.byref(handle)))
         return self._adopt(ParkerSolver(self, handle))
+
+    def focus_coefficients(self, grid: "LibGrid", b, v, dvdt=None, turbulence=None,
+                           parameters=None, minimum_magnetic_field_magnitude: float = 0.0,
+                           rest_mass=1.0, charge=1.0, speed_of_light=1.0,
+                           energy_scale_erg=1.0) -> np.ndarray:
+        """FocusCoefficient::make_legacy_transport_coefficient_fields[_with_time_
+        derivative] + the focused packed basis: (points, 27)."""
+        keep = []
+        b, v, dvdt = self._vectors(grid, b, v, dvdt)
+        t = self._turbulence(turbulence, keep)
+        props = ParticleProperties(rest_mass, charge, speed_of_light, energy_scale_erg)
+        params = parameters if parameters is not None else self.diffusion_parameters()
+        out = np.zeros((grid.points, 27), dtype=np.float64)
+        _check(self.lib.kpt_focus_coefficients(
+            self.handle, grid.handle, _ptr(b), _ptr(v), _ptr(dvdt), ctypes.byref(t),
+            ctypes.byref(props), ctypes.byref(params),
+            float(minimum_magnetic_field_magnitude), _ptr(out)))
+        return out
+
+    def focus_solver_from_fields(self, grid: "LibGrid", b, v, dvdt=None, turbulence=None,
+                                 parameters=None, minimum_magnetic_field_magnitude: float = 0.0,
+                                 courant: float = 0.3, spectral_index: float = 5.0 / 3.0,
+                                 h0: float = 1e-6, floors=(0.0, 0.0, 0.0, 0.0),
+                                 maximum_mu: float = 1.0, rest_mass=1.0, charge=1.0,
+                                 speed_of_light=1.0, energy_scale_erg=1.0) -> "FocusSolver":
+        """FocusTransportSolver(particles, grid, B, V, coefficients) with the
+        coefficient precompute and packed basis built on the device."""
+        keep = []
+        b, v, dvdt = self._vectors(grid, b, v, dvdt)
+        t = self._turbulence(turbulence, keep)
+        props = ParticleProperties(rest_mass, charge, speed_of_light, energy_scale_erg)
+        params = parameters if parameters is not None else self.diffusion_parameters()
+        sc = ScatteringParameters(spectral_index, h0, *floors)
+        handle = ctypes.c_void_p()
+        _check(self.lib.kpt_focus_solver_create_from_fields(
+            self.handle, grid.handle, _ptr(b), _ptr(v), _ptr(dvdt), ctypes.byref(t),
+            ctypes.byref(props), ctypes.byref(params), float(minimum_magnetic_field_magnitude),
+            float(courant), ctypes.byref(sc), ctypes.byref(handle)))
+        solver = self._adopt(FocusSolver(self, handle))
+        if maximum_mu != 1.0:
+            solver.set_maximum_mu(maximum_mu)
+        return solver
+
+    @staticmethod
+    def _vectors(grid, b, v, dvdt):
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        if b.shape != (grid.points, 3) or v.shape != (grid.points, 3):
+            raise ValueError(f"B and V must be ({grid.points}, 3)")
+        if dvdt is not None:
+            dvdt = np.ascontiguousarray(dvdt, dtype=np.float64)
+            if dvdt.shape != (grid.points, 3):
+                raise ValueError(f"dV/dt must be ({grid.points}, 3)")
+        return b, v, dvdt
 
     # -- ParticleGenerator ---------------------------------------------------
     def lib_field(self, grid: "LibGrid", values, centering=(0, 0)) -> "LibField":

@@ -2455,12 +2455,13 @@ int focus_step(kpt_context* ctx, kpt_focus_solver* s, kpt_system* sys, int advan
 
 extern "C" {
 
-int kpt_focus_solver_create(kpt_context* ctx, const kpt_grid* grid, const double* basis,
-                            int constant_ratio, double courant,
-                            const kpt_scattering_parameters* scattering,
-                            kpt_focus_solver** out) {
-    KPT_REQUIRE(ctx && grid && basis && out, "kpt_focus_solver_create: NULL argument");
-    *out = nullptr;
+}  // extern "C"
+
+// The solver without its basis: validated scattering parameters, the
+// device basis allocated.
+static int focus_solver_allocate(kpt_context* ctx, const kpt_grid* grid, double courant,
+                                 const kpt_scattering_parameters* scattering,
+                                 kpt_focus_solver** out) {
     kpt_scattering_parameters sc{5.0 / 3.0, 1.0e-6, 0.0, 0.0, 0.0, 0.0};
     if (scattering != nullptr) sc = *scattering;
     // PitchAngleScatteringParameters::validate (LegencyModel.hpp:205-221)
@@ -2483,8 +2484,22 @@ int kpt_focus_solver_create(kpt_context* ctx, const kpt_grid* grid, const double
     s->courant = courant;
     s->scattering = sc;
     KPT_CUDA(cudaMalloc(&s->basis, s->points * kpt::kFocusBasisStride * sizeof(double)));
+    KPT_CUDA(cudaMemset(s->basis, 0, s->points * kpt::kFocusBasisStride * sizeof(double)));
     KPT_CUDA(s->scalars.reserve(64));
-    kpt_focus_solver* raw = s.release();
+    *out = s.release();
+    return KPT_OK;
+}
+
+extern "C" {
+
+int kpt_focus_solver_create(kpt_context* ctx, const kpt_grid* grid, const double* basis,
+                            int constant_ratio, double courant,
+                            const kpt_scattering_parameters* scattering,
+                            kpt_focus_solver** out) {
+    KPT_REQUIRE(ctx && grid && basis && out, "kpt_focus_solver_create: NULL argument");
+    *out = nullptr;
+    kpt_focus_solver* raw = nullptr;
+    if (int rc = focus_solver_allocate(ctx, grid, courant, scattering, &raw)) return rc;
     if (int rc = kpt_focus_solver_set_basis(raw, basis, constant_ratio)) {
         kpt_focus_solver_destroy(raw);
         return rc;
@@ -2654,6 +2669,9 @@ int validate_coefficient_inputs(const kpt_turbulence* t, const kpt_particle_prop
 
 const char* coefficient_error_message(int code) {
     switch (code) {
+        case 10: return "FieldOperator: direction is undefined at zero magnitude.";
+        case 11: return "FocusCoefficient: ln |B| requires a positive magnetic field.";
+        case 12: return "FocusCoefficient: focused drift requires |B| > 0.";
         case 20: return "ParkerCoefficient: curl(B/B^2) is undefined where B^2 <= 0.";
         case 21: return "LegencyModel: gyrofrequency requires |B| > 0.";
         case 22: return "LegencyModel: kappa_parallel requires positive Vsw, Lc, omega, and sigma2.";
@@ -2669,24 +2687,41 @@ const char* coefficient_error_message(int code) {
     return "ParkerCoefficient: coefficient precompute failed";
 }
 
-// Builds the packed basis into `packed` (device, points x kLibBasisStride).
-int build_parker_coefficients(kpt_context* ctx, const kpt_grid* grid, const double* b,
-                              const double* v, const kpt_turbulence* t,
-                              const kpt_particle_properties* pr,
-                              const kpt_diffusion_parameters* p, double* packed) {
+// Builds the packed basis into `packed` (device): the Parker basis
+// (kLibBasisStride per point) or, with focused set, the focused basis
+// (kFocusBasisStride per point) from B, V and dV/dt (NULL = zero).
+int build_coefficients(kpt_context* ctx, const kpt_grid* grid, const double* b, const double* v,
+                       const double* dvdt, const kpt_turbulence* t,
+                       const kpt_particle_properties* pr, const kpt_diffusion_parameters* p,
+                       bool focused, double builder_floor, double* packed) {
     if (int rc = validate_coefficient_inputs(t, pr, p)) return rc;
+    if (focused) {
+        KPT_REQUIRE(std::isfinite(builder_floor) && builder_floor >= 0.0,
+                    "FocusCoefficient: magnetic-field magnitude floor must be finite and "
+                    "non-negative.");
+    }
     const uint64_t points = static_cast<uint64_t>(grid->nx + 4) * (grid->ny + 4);
     const int fields = t->storage == 1 ? 3 : 0;
+    const int vectors = focused && dvdt != nullptr ? 3 : 2;
     ScopedBuffer inputs;
     const size_t vec_bytes = points * 3 * sizeof(double);
-    KPT_CUDA(inputs.reserve(2 * vec_bytes + fields * points * sizeof(double) + 64));
+    const size_t scratch_bytes = focused ? points * 8 * sizeof(double) : 0;
+    KPT_CUDA(inputs.reserve(vectors * vec_bytes + fields * points * sizeof(double) +
+                            scratch_bytes + 64));
     char* base = static_cast<char*>(inputs.ptr);
     double* db = reinterpret_cast<double*>(base);
     double* dv = reinterpret_cast<double*>(base + vec_bytes);
-    double* dt = reinterpret_cast<double*>(base + 2 * vec_bytes);
-    int* err = reinterpret_cast<int*>(base + 2 * vec_bytes + fields * points * sizeof(double));
+    double* ddvdt = vectors == 3 ? reinterpret_cast<double*>(base + 2 * vec_bytes) : nullptr;
+    double* dt = reinterpret_cast<double*>(base + vectors * vec_bytes);
+    double* dscratch = reinterpret_cast<double*>(base + vectors * vec_bytes +
+                                                 fields * points * sizeof(double));
+    int* err = reinterpret_cast<int*>(base + vectors * vec_bytes +
+                                      fields * points * sizeof(double) + scratch_bytes);
     KPT_CUDA(cudaMemcpyAsync(db, b, vec_bytes, cudaMemcpyHostToDevice, ctx->stream));
     KPT_CUDA(cudaMemcpyAsync(dv, v, vec_bytes, cudaMemcpyHostToDevice, ctx->stream));
+    if (ddvdt != nullptr) {
+        KPT_CUDA(cudaMemcpyAsync(ddvdt, dvdt, vec_bytes, cudaMemcpyHostToDevice, ctx->stream));
+    }
     if (fields) {
         const double* src[3] = {t->sigma2_field, t->l2d_field, t->lc_field};
         for (int k = 0; k < 3; ++k) {
@@ -2721,7 +2756,20 @@ int build_parker_coefficients(kpt_context* ctx, const kpt_grid* grid, const doub
     L.ghost_mode = p->ghost_fill_mode;
     L.packed = packed;
     L.error = err;
-    KPT_CUDA(kpt::parker_coefficients(L, ctx->stream));
+    if (focused) {
+        L.stride = kpt::kFocusBasisStride;
+        L.kpar_slot = 19;
+        L.kperp_slot = 20;
+        L.dvdt = ddvdt;
+        L.direction_floor = builder_floor;
+        L.scratch = dscratch;
+        KPT_CUDA(kpt::focus_coefficients(L, ctx->stream));
+    } else {
+        L.stride = kpt::kLibBasisStride;
+        L.kpar_slot = 15;
+        L.kperp_slot = 16;
+        KPT_CUDA(kpt::parker_coefficients(L, ctx->stream));
+    }
     int code = no_error;
     KPT_CUDA(cudaMemcpyAsync(&code, err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     KPT_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -2752,12 +2800,57 @@ int kpt_parker_coefficients(kpt_context* ctx, const kpt_grid* grid, const double
     const uint64_t points = static_cast<uint64_t>(grid->nx + 4) * (grid->ny + 4);
     ScopedBuffer out;
     KPT_CUDA(out.reserve(points * kpt::kLibBasisStride * sizeof(double)));
-    if (int rc = build_parker_coefficients(ctx, grid, b, v, turbulence, properties, parameters,
-                                           out.as<double>())) {
+    if (int rc = build_coefficients(ctx, grid, b, v, nullptr, turbulence, properties, parameters,
+                                    false, 0.0, out.as<double>())) {
         return rc;
     }
     KPT_CUDA(cudaMemcpy(packed, out.ptr, points * kpt::kLibBasisStride * sizeof(double),
                         cudaMemcpyDeviceToHost));
+    return KPT_OK;
+}
+
+int kpt_focus_coefficients(kpt_context* ctx, const kpt_grid* grid, const double* b,
+                           const double* v, const double* dvdt, const kpt_turbulence* turbulence,
+                           const kpt_particle_properties* properties,
+                           const kpt_diffusion_parameters* parameters,
+                           double minimum_magnetic_field_magnitude, double* packed) {
+    KPT_REQUIRE(ctx && grid && b && v && turbulence && properties && parameters && packed,
+                "kpt_focus_coefficients: NULL argument");
+    if (int rc = activate(ctx)) return rc;
+    const uint64_t points = static_cast<uint64_t>(grid->nx + 4) * (grid->ny + 4);
+    ScopedBuffer out;
+    KPT_CUDA(out.reserve(points * kpt::kFocusBasisStride * sizeof(double)));
+    if (int rc = build_coefficients(ctx, grid, b, v, dvdt, turbulence, properties, parameters,
+                                    true, minimum_magnetic_field_magnitude, out.as<double>())) {
+        return rc;
+    }
+    // device rows of kFocusBasisStride -> host rows of kFocusBasis
+    KPT_CUDA(cudaMemcpy2D(packed, kpt::kFocusBasis * sizeof(double), out.ptr,
+                          kpt::kFocusBasisStride * sizeof(double),
+                          kpt::kFocusBasis * sizeof(double), points, cudaMemcpyDeviceToHost));
+    return KPT_OK;
+}
+
+int kpt_focus_solver_create_from_fields(kpt_context* ctx, const kpt_grid* grid, const double* b,
+                                        const double* v, const double* dvdt,
+                                        const kpt_turbulence* turbulence,
+                                        const kpt_particle_properties* properties,
+                                        const kpt_diffusion_parameters* parameters,
+                                        double minimum_magnetic_field_magnitude, double courant,
+                                        const kpt_scattering_parameters* scattering,
+                                        kpt_focus_solver** out) {
+    KPT_REQUIRE(ctx && grid && b && v && turbulence && properties && parameters && out,
+                "kpt_focus_solver_create_from_fields: NULL argument");
+    *out = nullptr;
+    kpt_focus_solver* raw = nullptr;
+    if (int rc = focus_solver_allocate(ctx, grid, courant, scattering, &raw)) return rc;
+    raw->constant_ratio = parameters->perpendicular_model == 1 ? 1 : 0;
+    if (int rc = build_coefficients(ctx, grid, b, v, dvdt, turbulence, properties, parameters,
+                                    true, minimum_magnetic_field_magnitude, raw->basis)) {
+        kpt_focus_solver_destroy(raw);
+        return rc;
+    }
+    *out = raw;
     return KPT_OK;
 }
 
@@ -2780,8 +2873,8 @@ int kpt_parker_solver_create_from_fields(kpt_context* ctx, const kpt_grid* grid,
     KPT_CUDA(cudaMalloc(&s->basis, s->points * kpt::kLibBasisStride * sizeof(double)));
     KPT_CUDA(s->scalars.reserve(64));
     kpt_parker_solver* raw = s.release();
-    if (int rc = build_parker_coefficients(ctx, grid, b, v, turbulence, properties, parameters,
-                                           raw->basis)) {
+    if (int rc = build_coefficients(ctx, grid, b, v, nullptr, turbulence, properties, parameters,
+                                    false, 0.0, raw->basis)) {
         kpt_parker_solver_destroy(raw);
         return rc;
     }

@@ -408,9 +408,19 @@ struct CoefLaunch {
     double drift_floor;
     int ghost_mode;                 // 0 PeriodicOrClamped, 1 PeriodicOnly
     double* packed;
+    int stride;                     // packed row length
+    int kpar_slot, kperp_slot;      // gamma-one kappas in the packed row
     int* error;                     // failed check (device), parker_coefficients_no_error() if none
+    // focused transport only
+    const double* dvdt;             // partial_t V (3 per point) or nullptr (zero)
+    double direction_floor;         // the builder's minimum |B| (direction, ln |B|, drifts)
+    double* scratch;                // 8 doubles per point: ln|B|, grad ln|B| (3), curvature (3)
 };
 cudaError_t parker_coefficients(const CoefLaunch& launch, cudaStream_t stream);
+// FocusCoefficient::make_legacy_transport_coefficient_fields_with_time_
+// derivative (FocusCoefficient.hpp:852-993) into the focused packed basis
+// (FocusSolver.hpp:106-136, :504-585), kFocusBasisStride doubles per point.
+cudaError_t focus_coefficients(const CoefLaunch& launch, cudaStream_t stream);
 int parker_coefficients_no_error();
 
 struct SampleLaunch {

@@ -1527,10 +1527,10 @@ __device__ double coef_tensor(const CoefLaunch& L, int i, int j, int oc, int dc,
     const double bj = __ddiv_rn(row[dc], den);
     const double projection = __dmul_rn(bi, bj);
     const double identity = oc == dc ? 1.0 : 0.0;
-    const double kpar = L.packed[p * kLibBasisStride + 15];
+    const double kpar = L.packed[p * L.stride + L.kpar_slot];
     if (basis == 0) return __dmul_rn(kpar, projection);
     if (basis == 1) {
-        return __dmul_rn(L.packed[p * kLibBasisStride + 16], __dsub_rn(identity, projection));
+        return __dmul_rn(L.packed[p * L.stride + L.kperp_slot], __dsub_rn(identity, projection));
     }
     return __dmul_rn(kpar, __dadd_rn(__dmul_rn(L.ratio, identity),
                                      __dmul_rn(__dsub_rn(1.0, L.ratio), projection)));
@@ -1580,6 +1580,51 @@ __device__ __forceinline__ double coef_floor(double v, double f) {
     return v < f ? f : v;
 }
 
+// The gamma-one kappas at one physical point (LegencyModel.hpp:434-470,
+// :801-862); false after recording the failed check.
+__device__ bool coef_kappas(const CoefLaunch& L, uint64_t p, const double* b, const double* v,
+                            double& kpar_out, double& kperp_out) {
+    const double safe_b = coef_floor(__dsqrt_rn(coef_norm2(b)), L.min_b);
+    const double safe_vsw = coef_floor(__dsqrt_rn(coef_norm2(v)), L.min_vsw);
+    const double sigma2 = L.turbulence_fields ? L.sigma2_field[p] : L.sigma2;
+    const double l2d = L.turbulence_fields ? L.l2d_field[p] : L.l2d;
+    const double lc = L.turbulence_fields ? L.lc_field[p] : L.lc;
+    const double safe_sigma2 = coef_floor(sigma2, L.min_sigma2);
+    if (safe_b <= 0.0) {
+        coef_set_error(L.error, 21);  // gyrofrequency requires |B| > 0
+        return false;
+    }
+    const double omega = __ddiv_rn(__dmul_rn(L.abs_charge, safe_b),
+                                   __dmul_rn(L.rest_mass, L.speed_of_light));
+    if (safe_vsw <= 0.0 || lc <= 0.0 || omega <= 0.0 || safe_sigma2 <= 0.0) {
+        coef_set_error(L.error, 22);  // kappa_parallel requires positive inputs
+        return false;
+    }
+    const double kpar = __ddiv_rn(
+        __dmul_rn(__dmul_rn(L.parallel_prefactor, pow(safe_vsw, 4.0 / 3.0)), pow(lc, 2.0 / 3.0)),
+        __dmul_rn(pow(omega, 1.0 / 3.0), safe_sigma2));
+    double kperp;
+    if (L.constant_ratio) {
+        if (kpar <= 0.0 || L.ratio <= 0.0) {
+            coef_set_error(L.error, 24);
+            return false;
+        }
+        kperp = __dmul_rn(L.ratio, kpar);
+    } else {
+        if (safe_vsw <= 0.0 || l2d <= 0.0 || safe_sigma2 <= 0.0 || kpar <= 0.0) {
+            coef_set_error(L.error, 23);
+            return false;
+        }
+        kperp = __dmul_rn(
+            __dmul_rn(__ddiv_rn(safe_vsw, 3.0),
+                      pow(__ddiv_rn(__dmul_rn(3.0, kpar), safe_vsw), 1.0 / 3.0)),
+            pow(__dmul_rn(__dmul_rn(L.perpendicular_prefactor, safe_sigma2), l2d), 2.0 / 3.0));
+    }
+    kpar_out = kpar;
+    kperp_out = kperp;
+    return true;
+}
+
 // Stage 1: B and V into the packed rows (every point, ghosts as given), the
 // derived slots zeroed (the reference's freshly allocated fields), and the
 // gamma-one kappas at the physical points
@@ -1601,12 +1646,6 @@ __global__ void coef_kappa_kernel(const CoefLaunch L) {
         const int i = static_cast<int>(p % static_cast<uint64_t>(L.grid.ex)) - 2;
         const int j = static_cast<int>(p / static_cast<uint64_t>(L.grid.ex)) - 2;
         if (i < 0 || i >= L.grid.axis[0].n || j < 0 || j >= L.grid.axis[1].n) continue;
-        const double safe_b = coef_floor(__dsqrt_rn(coef_norm2(b)), L.min_b);
-        const double safe_vsw = coef_floor(__dsqrt_rn(coef_norm2(v)), L.min_vsw);
-        const double sigma2 = L.turbulence_fields ? L.sigma2_field[p] : L.sigma2;
-        const double l2d = L.turbulence_fields ? L.l2d_field[p] : L.l2d;
-        const double lc = L.turbulence_fields ? L.lc_field[p] : L.lc;
-        const double safe_sigma2 = coef_floor(sigma2, L.min_sigma2);
         // curl(B/B^2) reads B^2 at the x and y neighbours first
         if (L.drift_floor <= 0.0) {
 #pragma unroll
@@ -1620,38 +1659,8 @@ __global__ void coef_kappa_kernel(const CoefLaunch L) {
                 }
             }
         }
-        if (safe_b <= 0.0) {
-            coef_set_error(L.error, 21);  // gyrofrequency requires |B| > 0
-            continue;
-        }
-        const double omega = __ddiv_rn(__dmul_rn(L.abs_charge, safe_b),
-                                       __dmul_rn(L.rest_mass, L.speed_of_light));
-        if (safe_vsw <= 0.0 || lc <= 0.0 || omega <= 0.0 || safe_sigma2 <= 0.0) {
-            coef_set_error(L.error, 22);  // kappa_parallel requires positive inputs
-            continue;
-        }
-        const double kpar = __ddiv_rn(
-            __dmul_rn(__dmul_rn(L.parallel_prefactor, pow(safe_vsw, 4.0 / 3.0)),
-                      pow(lc, 2.0 / 3.0)),
-            __dmul_rn(pow(omega, 1.0 / 3.0), safe_sigma2));
-        double kperp;
-        if (L.constant_ratio) {
-            if (kpar <= 0.0 || L.ratio <= 0.0) {
-                coef_set_error(L.error, 24);
-                continue;
-            }
-            kperp = __dmul_rn(L.ratio, kpar);
-        } else {
-            if (safe_vsw <= 0.0 || l2d <= 0.0 || safe_sigma2 <= 0.0 || kpar <= 0.0) {
-                coef_set_error(L.error, 23);
-                continue;
-            }
-            kperp = __dmul_rn(
-                __dmul_rn(__ddiv_rn(safe_vsw, 3.0),
-                          pow(__ddiv_rn(__dmul_rn(3.0, kpar), safe_vsw), 1.0 / 3.0)),
-                pow(__dmul_rn(__dmul_rn(L.perpendicular_prefactor, safe_sigma2), l2d),
-                    2.0 / 3.0));
-        }
+        double kpar = 0.0, kperp = 0.0;
+        if (!coef_kappas(L, p, b, v, kpar, kperp)) continue;
         out[15] = kpar;
         out[16] = kperp;
     }
@@ -1660,7 +1669,8 @@ __global__ void coef_kappa_kernel(const CoefLaunch L) {
 // Field::fill_ghost_cells for cell-centred packed slots [first, last] and
 // slot `extra` (Field.hpp:274-316): a ghost point copies its periodic image
 // or, on an open axis, the nearest physical point (PeriodicOnly leaves it).
-__global__ void coef_ghost_kernel(const CoefLaunch L, int first, int last, int extra) {
+__global__ void coef_ghost_kernel(const CoefLaunch L, double* base, int stride, int first,
+                                  int last, int extra) {
     const uint64_t points = static_cast<uint64_t>(L.grid.ex) * (L.grid.axis[1].n + 4);
     for (uint64_t p = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; p < points;
          p += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
@@ -1685,8 +1695,8 @@ __global__ void coef_ghost_kernel(const CoefLaunch L, int first, int last, int e
             }
         }
         if (!ghost || skip) continue;
-        const double* src = L.packed + coef_point(L.grid, idx[0], idx[1]) * kLibBasisStride;
-        double* dst = L.packed + p * kLibBasisStride;
+        const double* src = base + coef_point(L.grid, idx[0], idx[1]) * stride;
+        double* dst = base + p * stride;
         for (int c = first; c <= last; ++c) dst[c] = src[c];
         if (extra >= 0) dst[extra] = src[extra];
     }
@@ -1741,6 +1751,192 @@ __global__ void coef_derivative_kernel(const CoefLaunch L) {
                                          gen_coordinate(a, k + 1, 0), lv, cv, uv));
         }
         out[17] = div;
+    }
+}
+
+// ---- focused transport coefficient precompute --------------------------------
+//
+// make_legacy_transport_coefficient_fields_with_time_derivative
+// (FocusCoefficient.hpp:852-993) into the focused packed basis
+// (FocusSolver.hpp:106-136): B b V, drift bases over |B|, the perpendicular
+// diffusion advection, |B|, the kappas, div V, b.grad ln|B|, bb:grad V,
+// b.dV/dt, sigma^2 and Lc.  ln|B|, grad ln|B| and the curvature (b.grad)b
+// live in an 8-double scratch row per point.  Fields the reference fills
+// at every point (|B|, b, ln|B|, the drift bases, the scattering inputs)
+// are computed at every point here too, before the same ghost fills.
+constexpr int kFocusScratch = 8;
+
+// Centred derivative of one component along dim at a physical point
+// (FieldOperator.hpp:106-143), 0 on an ignorable or single-cell axis.
+__device__ __forceinline__ double coef_component_derivative(const CoefLaunch& L,
+                                                           const double* base, int stride,
+                                                           int i, int j, int dim, int c) {
+    if (dim >= 2 || L.grid.axis[dim].n <= 1) return 0.0;
+    const LibAxis& a = L.grid.axis[dim];
+    const int k = dim == 0 ? i : j;
+    const double lv = base[coef_point(L.grid, dim == 0 ? i - 1 : i, dim == 1 ? j - 1 : j) * stride + c];
+    const double cv = base[coef_point(L.grid, i, j) * stride + c];
+    const double uv = base[coef_point(L.grid, dim == 0 ? i + 1 : i, dim == 1 ? j + 1 : j) * stride + c];
+    return coef_d3(gen_coordinate(a, k - 1, 0), gen_coordinate(a, k, 0),
+                   gen_coordinate(a, k + 1, 0), lv, cv, uv);
+}
+
+__device__ __forceinline__ bool coef_physical(const CoefLaunch& L, uint64_t p, int& i, int& j) {
+    i = static_cast<int>(p % static_cast<uint64_t>(L.grid.ex)) - 2;
+    j = static_cast<int>(p / static_cast<uint64_t>(L.grid.ex)) - 2;
+    return i >= 0 && i < L.grid.axis[0].n && j >= 0 && j < L.grid.axis[1].n;
+}
+
+// Stage 1, every point: B, V, |B| (fill_magnitude), b (fill_direction with
+// ZeroMagnitudePolicy::Abort), ln max(|B|, floor), the scattering sigma^2
+// and Lc; the kappas at the physical points.
+__global__ void focus_stage1_kernel(const CoefLaunch L) {
+    const uint64_t points = static_cast<uint64_t>(L.grid.ex) * (L.grid.axis[1].n + 4);
+    for (uint64_t p = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; p < points;
+         p += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        double* out = L.packed + p * L.stride;
+        const double* b = L.b + 3 * p;
+        const double* v = L.v + 3 * p;
+        for (int c = 0; c < L.stride; ++c) out[c] = 0.0;
+        const double magnitude = __dsqrt_rn(coef_norm2(b));
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            out[c] = b[c];
+            out[6 + c] = v[c];
+        }
+        out[18] = magnitude;
+        if (magnitude <= L.direction_floor) {
+            coef_set_error(L.error, 10);  // direction is undefined at zero magnitude
+        } else {
+            const double inverse = __ddiv_rn(1.0, magnitude);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) out[3 + c] = __dmul_rn(b[c], inverse);
+        }
+        const double safe = magnitude > L.direction_floor ? magnitude : L.direction_floor;
+        double* scratch = L.scratch + p * kFocusScratch;
+#pragma unroll
+        for (int c = 0; c < kFocusScratch; ++c) scratch[c] = 0.0;
+        if (safe <= 0.0) {
+            coef_set_error(L.error, 11);  // ln |B| requires a positive magnetic field
+        } else {
+            scratch[0] = log(safe);
+        }
+        out[25] = L.turbulence_fields ? L.sigma2_field[p] : L.sigma2;
+        out[26] = L.turbulence_fields ? L.lc_field[p] : L.lc;
+        int i, j;
+        if (!coef_physical(L, p, i, j)) continue;
+        double kpar = 0.0, kperp = 0.0;
+        if (!coef_kappas(L, p, b, v, kpar, kperp)) continue;
+        out[19] = kpar;
+        out[20] = kperp;
+    }
+}
+
+// Stage 2, physical points: grad ln|B| (fill_gradient) and the curvature
+// (b.grad)b (FocusCoefficient.hpp:428-452, :559-595).
+__global__ void focus_stage2_kernel(const CoefLaunch L) {
+    const uint64_t points = static_cast<uint64_t>(L.grid.ex) * (L.grid.axis[1].n + 4);
+    for (uint64_t p = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; p < points;
+         p += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        int i, j;
+        if (!coef_physical(L, p, i, j)) continue;
+        double* scratch = L.scratch + p * kFocusScratch;
+        const double* dir = L.packed + p * L.stride + 3;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            scratch[1 + c] = c < 2 ? coef_component_derivative(L, L.scratch, kFocusScratch, i, j, c, 0)
+                                   : 0.0;
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            double result = 0.0;
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                const double g = coef_component_derivative(L, L.packed + 3, L.stride, i, j, d, c);
+                result = __dadd_rn(result, __dmul_rn(dir[d], g));
+            }
+            scratch[4 + c] = result;
+        }
+    }
+}
+
+__device__ __forceinline__ double coef_cross(const double* a, const double* b, int c) {
+    if (c == 0) return __dsub_rn(__dmul_rn(a[1], b[2]), __dmul_rn(a[2], b[1]));
+    if (c == 1) return __dsub_rn(__dmul_rn(a[2], b[0]), __dmul_rn(a[0], b[2]));
+    return __dsub_rn(__dmul_rn(a[0], b[1]), __dmul_rn(a[1], b[0]));
+}
+
+// Stage 3, every point: the drift bases b x grad ln|B| / |B| and
+// b x (b.grad)b / |B| (FocusCoefficient.hpp:617-703).
+__global__ void focus_stage3_kernel(const CoefLaunch L) {
+    const uint64_t points = static_cast<uint64_t>(L.grid.ex) * (L.grid.axis[1].n + 4);
+    for (uint64_t p = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; p < points;
+         p += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        double* out = L.packed + p * L.stride;
+        const double* scratch = L.scratch + p * kFocusScratch;
+        const double m = out[18] > L.direction_floor ? out[18] : L.direction_floor;
+        if (m <= 0.0) {
+            coef_set_error(L.error, 12);  // focused drift requires |B| > 0
+            continue;
+        }
+        const double inverse = __ddiv_rn(1.0, m);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            out[9 + c] = __dmul_rn(coef_cross(out + 3, scratch + 1, c), inverse);
+            out[12 + c] = __dmul_rn(coef_cross(out + 3, scratch + 4, c), inverse);
+        }
+    }
+}
+
+// Velocity gradient (grad V)_{oc, dc} in Cartesian components
+// (FocusCoefficient.hpp:240-326).
+__device__ __forceinline__ double coef_velocity_gradient(const CoefLaunch& L, int i, int j,
+                                                         int oc, int dc) {
+    return coef_component_derivative(L, L.v, 3, i, j, dc, oc);
+}
+
+// Stage 4, physical points: the perpendicular diffusion advection
+// (FocusCoefficient.hpp:829-850), div V and the contractions
+// (FocusCoefficient.hpp:705-781).
+__global__ void focus_stage4_kernel(const CoefLaunch L) {
+    const uint64_t points = static_cast<uint64_t>(L.grid.ex) * (L.grid.axis[1].n + 4);
+    if (*L.error != kCoefNoError) return;
+    for (uint64_t p = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; p < points;
+         p += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        int i, j;
+        if (!coef_physical(L, p, i, j)) continue;
+        double* out = L.packed + p * L.stride;
+        const double* scratch = L.scratch + p * kFocusScratch;
+#pragma unroll 1
+        for (int c = 0; c < 3; ++c) out[15 + c] = coef_divergence_basis(L, i, j, c, 1);
+        double div = 0.0;
+        for (int dim = 0; dim < 2; ++dim) {
+            div = __dadd_rn(div, coef_component_derivative(L, L.v, 3, i, j, dim, dim));
+        }
+        out[21] = div;
+        const double* dir = out + 3;
+        const double* v = L.v + 3 * p;
+        double focusing = 0.0;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) focusing = __dadd_rn(focusing, __dmul_rn(dir[c], scratch[1 + c]));
+        out[22] = focusing;
+        double bb = 0.0;
+        double convective = 0.0;
+        for (int oc = 0; oc < 3; ++oc) {
+            for (int dc = 0; dc < 3; ++dc) {
+                const double g = coef_velocity_gradient(L, i, j, oc, dc);
+                bb = __dadd_rn(bb, __dmul_rn(__dmul_rn(dir[oc], dir[dc]), g));
+                convective = __dadd_rn(convective, __dmul_rn(__dmul_rn(dir[oc], v[dc]), g));
+            }
+        }
+        out[23] = bb;
+        double partial = 0.0;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const double dv = L.dvdt != nullptr ? L.dvdt[3 * p + c] : 0.0;
+            partial = __dadd_rn(partial, __dmul_rn(dir[c], dv));
+        }
+        out[24] = __dadd_rn(partial, convective);
     }
 }
 
@@ -1933,9 +2129,28 @@ cudaError_t parker_coefficients(const CoefLaunch& L, cudaStream_t stream) {
     const uint64_t points = static_cast<uint64_t>(L.grid.ex) * (L.grid.axis[1].n + 4);
     const uint64_t cells = static_cast<uint64_t>(L.grid.axis[0].n) * L.grid.axis[1].n;
     coef_kappa_kernel<<<grid_for(points, 256), 256, 0, stream>>>(L);
-    coef_ghost_kernel<<<grid_for(points, 256), 256, 0, stream>>>(L, 15, 16, -1);
+    coef_ghost_kernel<<<grid_for(points, 256), 256, 0, stream>>>(L, L.packed, L.stride, 15, 16,
+                                                                 -1);
     coef_derivative_kernel<<<grid_for(cells, 128), 128, 0, stream>>>(L);
-    coef_ghost_kernel<<<grid_for(points, 256), 256, 0, stream>>>(L, 6, 14, 17);
+    coef_ghost_kernel<<<grid_for(points, 256), 256, 0, stream>>>(L, L.packed, L.stride, 6, 14,
+                                                                 17);
+    return cudaGetLastError();
+}
+
+cudaError_t focus_coefficients(const CoefLaunch& L, cudaStream_t stream) {
+    const uint64_t points = static_cast<uint64_t>(L.grid.ex) * (L.grid.axis[1].n + 4);
+    const int g = grid_for(points, 256);
+    focus_stage1_kernel<<<g, 256, 0, stream>>>(L);
+    coef_ghost_kernel<<<g, 256, 0, stream>>>(L, L.scratch, kFocusScratch, 0, 0, -1);
+    coef_ghost_kernel<<<g, 256, 0, stream>>>(L, L.packed, L.stride, 19, 20, -1);
+    coef_ghost_kernel<<<g, 256, 0, stream>>>(L, L.packed, L.stride, 25, 26, -1);
+    focus_stage2_kernel<<<grid_for(points, 128), 128, 0, stream>>>(L);
+    coef_ghost_kernel<<<g, 256, 0, stream>>>(L, L.scratch, kFocusScratch, 1, 6, -1);
+    focus_stage3_kernel<<<g, 256, 0, stream>>>(L);
+    coef_ghost_kernel<<<g, 256, 0, stream>>>(L, L.packed, L.stride, 9, 14, -1);
+    focus_stage4_kernel<<<grid_for(points, 128), 128, 0, stream>>>(L);
+    coef_ghost_kernel<<<g, 256, 0, stream>>>(L, L.packed, L.stride, 15, 17, -1);
+    coef_ghost_kernel<<<g, 256, 0, stream>>>(L, L.packed, L.stride, 21, 24, -1);
     return cudaGetLastError();
 }
 

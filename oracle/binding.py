@@ -283,6 +283,9 @@ class ReferenceHarness:
         lib.ref_lib_parker_coefficients.restype = ll
         lib.ref_lib_parker_coefficients.argtypes = [i32, i32, vp, vp, vp, vp, vp, i32, vp, vp,
                                                     vp, vp, dbl, i32, vp]
+        lib.ref_lib_focus_coefficients.restype = ll
+        lib.ref_lib_focus_coefficients.argtypes = [i32, i32, vp, vp, vp, vp, vp, vp, i32, vp, vp,
+                                                   vp, vp, dbl, i32, vp]
         lib.ref_lib_candidates.restype = ll
         lib.ref_lib_candidates.argtypes = [i32, i32, vp, vp, vp, i32, i32, vp, vp, vp, vp, vp,
                                            vp, ll, vp]
@@ -533,6 +536,39 @@ class ReferenceHarness:
             len(xe) - 1, len(ye) - 1, _ptr(xe), _ptr(ye), _ptr(periodic), _ptr(b), _ptr(v),
             0 if fields is None else 1, _ptr(turb), None if fields is None else _ptr(fields),
             _ptr(pr), _ptr(pa), float(drift_floor), int(ghost_mode), _ptr(out)))
+        return out
+
+    def lib_focus_coefficients(self, grid: dict, b, v, dvdt=None, *,
+                               turbulence=(0.5, 1.0, 1.0, -1.0), turbulence_fields=None,
+                               props=None, params=None, builder_floor: float = 0.0,
+                               ghost_mode: int = 0) -> np.ndarray:
+        """The reference's focused coefficient precompute and packed basis
+        (points x 27) from cell-centred B, V and dV/dt (points x 3)."""
+        xe = np.ascontiguousarray(grid["x_edges"], dtype=np.float64)
+        ye = np.ascontiguousarray(grid["y_edges"], dtype=np.float64)
+        periodic = np.ascontiguousarray(grid["periodic"], dtype=np.int32)
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        dv = None if dvdt is None else np.ascontiguousarray(dvdt, dtype=np.float64)
+        points = b.shape[0]
+        props = props or dict(rest_mass=1.0, charge=1.0, speed_of_light=1.0)
+        pr = np.array([props["rest_mass"], props["charge"], props["speed_of_light"],
+                       props.get("energy_scale", 1.0)], dtype=np.float64)
+        params = params or {}
+        pa = np.array([params.get("model", 0), params.get("parallel_prefactor", 1.622),
+                       params.get("perpendicular_prefactor", 0.198), params.get("ratio", 0.0),
+                       params.get("minimum_b", 0.0), params.get("minimum_vsw", 0.0),
+                       params.get("minimum_sigma2", 0.0)], dtype=np.float64)
+        turb = np.ascontiguousarray(turbulence, dtype=np.float64)
+        fields = None
+        if turbulence_fields is not None:
+            fields = np.ascontiguousarray(np.stack(turbulence_fields), dtype=np.float64)
+        out = np.zeros((points, 27), dtype=np.float64)
+        self._check(self.lib.ref_lib_focus_coefficients(
+            len(xe) - 1, len(ye) - 1, _ptr(xe), _ptr(ye), _ptr(periodic), _ptr(b), _ptr(v),
+            None if dv is None else _ptr(dv), 0 if fields is None else 1, _ptr(turb),
+            None if fields is None else _ptr(fields), _ptr(pr), _ptr(pa), float(builder_floor),
+            int(ghost_mode), _ptr(out)))
         return out
 
     def main(self, argv, frame_base: int = 0) -> int:

@@ -1042,3 +1042,82 @@ long long ref_lib_parker_coefficients(int nx, int ny, const double* x_edges,
 }
 
 }  // extern "C"
+
+// ---- focused-transport coefficient precompute on the library grid ----------
+extern "C" {
+
+// FocusCoefficient::make_legacy_transport_coefficient_fields_with_time_
+// derivative (include/FocusCoefficient.hpp:852-993) from cell-centred B, V
+// and dV/dt (3 doubles per ghosted point; dvdt NULL = zero), then the
+// solver's packed basis (FocusSolver.hpp:504-585) copied to packed (27
+// doubles per point).  turbulence, props and params as
+// ref_lib_parker_coefficients; builder_floor = the builder's minimum |B|.
+long long ref_lib_focus_coefficients(int nx, int ny, const double* x_edges, const double* y_edges,
+                                     const int* periodic, const double* b_values,
+                                     const double* v_values, const double* dvdt_values,
+                                     int turb_mode, const double* turb,
+                                     const double* turb_fields, const double* props,
+                                     const double* params, double builder_floor, int ghost_mode,
+                                     double* packed_out) {
+    try {
+        using solver_type = FocusSolver<LibAnalyticGrid>;
+        using vector_field = typename solver_type::vector_field_type;
+        const LibAnalyticGrid grid = make_lib_analytic_grid(nx, ny, x_edges, y_edges, periodic);
+        vector_field b(grid, "fc_b", GridCentering::CellCentered);
+        vector_field v(grid, "fc_v", GridCentering::CellCentered);
+        vector_field dvdt(grid, "fc_dvdt", GridCentering::CellCentered);
+        const std::size_t points = b.point_count();
+        for (std::size_t k = 0; k < points; ++k) {
+            for (int c = 0; c < 3; ++c) {
+                b.data(k, c) = b_values[3 * k + c];
+                v.data(k, c) = v_values[3 * k + c];
+                dvdt.data(k, c) = dvdt_values != nullptr ? dvdt_values[3 * k + c] : 0.0;
+            }
+        }
+        const auto model = TurbulencePropertyModel::constant_code_units(turb[0], turb[1],
+                                                                        turb[2], turb[3]);
+        TurbulenceProperties<LibAnalyticGrid> turbulence(
+            grid, model,
+            turb_mode == 0 ? TurbulencePropertyStorageMode::ConstantOnly
+                           : TurbulencePropertyStorageMode::Field);
+        if (turb_mode != 0) {
+            for (std::size_t k = 0; k < points; ++k) {
+                turbulence.sigma2.data(k, 0) = turb_fields[0 * points + k];
+                turbulence.l2d.data(k, 0) = turb_fields[1 * points + k];
+                turbulence.lslab.data(k, 0) = turb_fields[2 * points + k];
+                turbulence.lc.data(k, 0) = turb_fields[3 * points + k];
+            }
+        }
+        LegencyModel::DiffusionModelParameters parameters;
+        parameters.parallel_prefactor = params[1];
+        parameters.perpendicular_prefactor = params[2];
+        parameters.minimum_magnetic_field_magnitude = params[4];
+        parameters.minimum_solar_wind_speed = params[5];
+        parameters.minimum_sigma2 = params[6];
+        if (static_cast<int>(params[0]) == 1) {
+            parameters.set_constant_perpendicular_parallel_ratio(params[3]);
+        } else {
+            parameters.perpendicular_parallel_ratio = params[3];
+            parameters.use_readme_perpendicular_formula();
+        }
+        const auto coefficients =
+            FocusCoefficient::make_legacy_transport_coefficient_fields_with_time_derivative(
+                b, v, dvdt, turbulence, lib_properties(props), "fcoef", parameters,
+                LegencyModel::PitchAngleScatteringParameters{}, builder_floor,
+                ghost_mode == 0 ? FieldGhostFillMode::PeriodicOrClamped
+                                : FieldGhostFillMode::PeriodicOnly);
+        LibSystem sys(0, 1, lib_properties(props));
+        solver_type solver(sys, grid, b, v, coefficients);
+        for (std::size_t k = 0; k < points; ++k) {
+            for (int c = 0; c < 27; ++c) {
+                packed_out[27 * k + c] = solver.packed_coefficient_basis.data(k, c);
+            }
+        }
+        return static_cast<long long>(points);
+    } catch (const std::exception& error) {
+        g_last_error = error.what();
+        return -1;
+    }
+}
+
+}  // extern "C"

@@ -37,6 +37,11 @@ Cases
                       constant-ratio branches, constant and field
                       turbulence, floors, both ghost-fill modes, open and
                       periodic axes, and two failures' messages
+  lib_focus_coefficients.npz
+                      FocusCoefficient::make_legacy_transport_coefficient_
+                      fields[_with_time_derivative] and the focused packed
+                      basis over the same variations, with and without
+                      partial_t V
   lib_system.npz      ParticleSystem lifecycle: boundary conditions,
                       sort_by_key, compact_active_particles,
                       split_particles_on_energy_growth, capture_previous_positions
@@ -612,6 +617,54 @@ def make_parker_coefficients(ref, out_dir):
              cases=np.array([c[0] for c in COEFFICIENT_CASES]), **arrays)
 
 
+# name, periodic, variant, turbulence, params, charge, builder floor, ghost
+# mode, with dV/dt
+FOCUS_COEFFICIENT_CASES = (
+    ("readme_constant", (1, 0), 0, "constant", dict(), 1.0, 0.0, 0, False),
+    ("ratio_floors_dvdt", (1, 0), 1, "constant",
+     dict(model=1, ratio=0.05, minimum_b=0.25, minimum_vsw=0.9, minimum_sigma2=0.4), -2.0,
+     0.05, 0, True),
+    ("readme_fields_periodic_only", (0, 1), 2, "fields",
+     dict(parallel_prefactor=1.5, perpendicular_prefactor=0.25), 1.0, 0.0, 1, True),
+    ("ratio_fields_open", (0, 0), 1, "fields", dict(model=1, ratio=0.3), 0.5, 0.0, 0, False),
+)
+
+
+def make_focus_coefficients(ref, out_dir):
+    """The reference's focused coefficient precompute and packed basis."""
+    nx, ny = 20, 28
+    xe = np.linspace(-1.3, 2.1, nx + 1)
+    ye = np.linspace(-2.0, 2.0, ny + 1)
+    arrays = {}
+    for (name, periodic, variant, turb, params, charge, floor, ghost,
+         with_dvdt) in FOCUS_COEFFICIENT_CASES:
+        grid = dict(x_edges=xe, y_edges=ye, periodic=np.array(periodic, dtype=np.int32))
+        b, v, fields = coefficient_inputs(nx, ny, xe, ye, variant)
+        dvdt = None
+        if with_dvdt:
+            dvdt = np.stack([np.cos(v[:, 0]), 0.3 * v[:, 1], 0.1 + 0.0 * v[:, 2]], axis=-1)
+        constant = (0.35, 0.9, 1.4, -1.0 if variant == 0 else 1.1)
+        props = dict(rest_mass=1.0, charge=charge, speed_of_light=1.0)
+        packed = ref.lib_focus_coefficients(
+            grid, b, v, dvdt, turbulence=constant,
+            turbulence_fields=fields if turb == "fields" else None, props=props,
+            params=params, builder_floor=floor, ghost_mode=ghost)
+        arrays[f"{name}_periodic"] = grid["periodic"]
+        arrays[f"{name}_b"] = b
+        arrays[f"{name}_v"] = v
+        arrays[f"{name}_dvdt"] = dvdt if dvdt is not None else np.zeros((0,))
+        arrays[f"{name}_turbulence"] = np.array(constant)
+        arrays[f"{name}_fields"] = np.stack(fields) if turb == "fields" else np.zeros((0,))
+        arrays[f"{name}_params"] = np.array(
+            [params.get("model", 0), params.get("parallel_prefactor", 1.622),
+             params.get("perpendicular_prefactor", 0.198), params.get("ratio", 0.0),
+             params.get("minimum_b", 0.0), params.get("minimum_vsw", 0.0),
+             params.get("minimum_sigma2", 0.0), floor, ghost, charge])
+        arrays[f"{name}_packed"] = packed
+    lib_save(out_dir, "lib_focus_coefficients.npz", x_edges=xe, y_edges=ye,
+             cases=np.array([c[0] for c in FOCUS_COEFFICIENT_CASES]), **arrays)
+
+
 def main() -> None:
     ref = binding.ReferenceHarness()
     out_dir = HERE
@@ -623,10 +676,12 @@ def main() -> None:
         return
     if sys.argv[1:] == ["coefficients"]:
         make_parker_coefficients(ref, out_dir)
+        make_focus_coefficients(ref, out_dir)
         return
     make_lib(ref, out_dir)
     make_generator(ref, out_dir)
     make_parker_coefficients(ref, out_dir)
+    make_focus_coefficients(ref, out_dir)
     if sys.argv[1:] == ["lib"]:
         return
     make_c1(ref, out_dir)
