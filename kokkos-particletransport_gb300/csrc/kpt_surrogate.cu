@@ -121,8 +121,9 @@ __global__ void __launch_bounds__(128) fwd_bwd_kernel(const float* __restrict__ 
                                                       float* g2, float* gy, float* loss,
                                                       int quant) {
     // quant != 0: the forward sees the served network's rounding (weights,
-    // inputs, pre-activations and activations in the 16-bit type; biases and
-    // accumulation FP32) and the backward passes straight through it
+    // inputs and activations in the 16-bit type, FP16 pre-activations too;
+    // biases and accumulation FP32) and the backward passes straight
+    // through it
     __shared__ float w[kMlpParams];
     for (int k = threadIdx.x; k < kMlpParams; k += blockDim.x) {
         const bool bias = (k >= kMlpB1 && k < kMlpW2) || (k >= kMlpB2 && k < kMlpW3) ||
@@ -150,7 +151,7 @@ __global__ void __launch_bounds__(128) fwd_bwd_kernel(const float* __restrict__ 
         for (int j = 0; j < kMlpHidden; ++j) {
             float z = w[kMlpB1 + j];
             for (int k = 0; k < kMlpIn; ++k) z += w[kMlpW1 + j * kMlpIn + k] * in[k];
-            a1[j] = quantize(tanhf(quantize(z, quant)), quant);
+            a1[j] = quantize(tanhf(quant == 2 ? quantize(z, quant) : z), quant);
             h1[static_cast<size_t>(b) * kMlpHidden + j] = a1[j];
         }
         float y[kMlpOut];
@@ -158,7 +159,7 @@ __global__ void __launch_bounds__(128) fwd_bwd_kernel(const float* __restrict__ 
         for (int j = 0; j < kMlpHidden; ++j) {
             float z = w[kMlpB2 + j];
             for (int k = 0; k < kMlpHidden; ++k) z += w[kMlpW2 + j * kMlpHidden + k] * a1[k];
-            const float a2 = quantize(tanhf(quantize(z, quant)), quant);
+            const float a2 = quantize(tanhf(quant == 2 ? quantize(z, quant) : z), quant);
             h2[static_cast<size_t>(b) * kMlpHidden + j] = a2;
             for (int o = 0; o < kMlpOut; ++o) y[o] += w[kMlpW3 + o * kMlpHidden + j] * a2;
         }

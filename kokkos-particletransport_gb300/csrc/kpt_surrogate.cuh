@@ -82,7 +82,7 @@ struct SurrogateDevice {
 
 #ifdef __CUDACC__
 
-// Packed pair conversion, packed tanh and the m16n8k16 MMA for the two
+// Packed pair conversion, the activation and the m16n8k16 MMA for the two
 // element types (FP16 = true: IEEE binary16, else BF16).
 template <bool FP16>
 __device__ __forceinline__ uint32_t pack_x2(float lo, float hi) {
@@ -96,28 +96,34 @@ __device__ __forceinline__ uint32_t pack_x2(float lo, float hi) {
     return r;
 }
 
+// tanh of two FP32 accumulators packed as the next layer's 16-bit pair.
+// FP16: packed tanh.approx.f16x2 on the rounded pre-activations.  BF16:
+// tanh.approx.f32 on each accumulator, then one rounding to BF16 -- faster on
+// this GPU than the packed bf16x2 form and more accurate (one rounding after
+// the activation instead of one before and one after).
 template <bool FP16>
-__device__ __forceinline__ uint32_t tanh_x2(uint32_t x) {
-    uint32_t r;
+__device__ __forceinline__ uint32_t act_x2(float lo, float hi) {
     if (FP16) {
+        uint32_t r;
+        const uint32_t x = pack_x2<true>(lo, hi);
         asm("tanh.approx.f16x2 %0, %1;" : "=r"(r) : "r"(x));
-    } else {
-        asm("tanh.approx.bf16x2 %0, %1;" : "=r"(r) : "r"(x));
+        return r;
     }
-    return r;
+    float tlo, thi;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(tlo) : "f"(lo));
+    asm("tanh.approx.f32 %0, %1;" : "=f"(thi) : "f"(hi));
+    return pack_x2<false>(tlo, thi);
 }
 
 template <bool FP16>
 __device__ __forceinline__ void mma_16816(float (&d)[4], const uint32_t (&a)[4], uint2 b) {
     if (FP16) {
-        asm volatile(
-            "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 "
+        asm("mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 "
             "{%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, {%0, %1, %2, %3};"
             : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
             : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b.x), "r"(b.y));
     } else {
-        asm volatile(
-            "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
+        asm("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
             "{%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, {%0, %1, %2, %3};"
             : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
             : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b.x), "r"(b.y));
@@ -145,12 +151,14 @@ __device__ __forceinline__ void mlp_warp(const uint2* smem, const float (&f)[kMl
     const uint32_t pk0 = pack_x2<FP16>(f[0], f[1]);
     const uint32_t pk1 = pack_x2<FP16>(f[2], f[3]);
     const uint32_t pk2 = pack_x2<FP16>(f[4], 0.0f);
-    float out[2][4];
-    // one row tile at a time keeps the live fragments to one tile's worth
-#pragma unroll 1
+    // Both row tiles advance together: every weight fragment and bias read
+    // from shared memory feeds two MMAs, and the two tiles' dependency
+    // chains interleave.
+    // A fragments of the input tiles: columns 2tig, 2tig+1 of rows g and
+    // g+8; columns 8..15 (and 5..7) are zero padding.
+    uint32_t ax[2][4];
+#pragma unroll
     for (int mt = 0; mt < 2; ++mt) {
-        // A fragment of the input tile: columns 2tig, 2tig+1 of rows g and
-        // g+8; columns 8..15 (and 5..7) are zero padding.
         const int src_lo = 16 * mt + g;
         const uint32_t l0 = __shfl_sync(full, pk0, src_lo);
         const uint32_t l1 = __shfl_sync(full, pk1, src_lo);
@@ -158,45 +166,53 @@ __device__ __forceinline__ void mlp_warp(const uint2* smem, const float (&f)[kMl
         const uint32_t h0 = __shfl_sync(full, pk0, src_lo + 8);
         const uint32_t h1 = __shfl_sync(full, pk1, src_lo + 8);
         const uint32_t h2 = __shfl_sync(full, pk2, src_lo + 8);
-        const uint32_t ax[4] = {tig == 0 ? l0 : (tig == 1 ? l1 : (tig == 2 ? l2 : 0u)),
-                                tig == 0 ? h0 : (tig == 1 ? h1 : (tig == 2 ? h2 : 0u)), 0u, 0u};
-        // layer 1: 8 column tiles -> A fragments of layer 2 (4 k tiles)
-        uint32_t a2[4][4];
+        ax[mt][0] = tig == 0 ? l0 : (tig == 1 ? l1 : (tig == 2 ? l2 : 0u));
+        ax[mt][1] = tig == 0 ? h0 : (tig == 1 ? h1 : (tig == 2 ? h2 : 0u));
+        ax[mt][2] = 0u;
+        ax[mt][3] = 0u;
+    }
+    // layer 1: 8 column tiles -> A fragments of layer 2 (4 k tiles)
+    uint32_t a2[2][4][4];
 #pragma unroll
-        for (int nt = 0; nt < 8; ++nt) {
-            const float2 b = *reinterpret_cast<const float2*>(bias + 8 * nt + 2 * tig);
-            float acc[4] = {b.x, b.y, b.x, b.y};
-            mma_16816<FP16>(acc, ax, smem[kFragW1 + nt * 32 + lane]);
-            a2[nt >> 1][(nt & 1) * 2 + 0] = tanh_x2<FP16>(pack_x2<FP16>(acc[0], acc[1]));
-            a2[nt >> 1][(nt & 1) * 2 + 1] = tanh_x2<FP16>(pack_x2<FP16>(acc[2], acc[3]));
+    for (int nt = 0; nt < 8; ++nt) {
+        const float2 bv = *reinterpret_cast<const float2*>(bias + 8 * nt + 2 * tig);
+        const uint2 w = smem[kFragW1 + nt * 32 + lane];
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt) {
+            float acc[4] = {bv.x, bv.y, bv.x, bv.y};
+            mma_16816<FP16>(acc, ax[mt], w);
+            a2[mt][nt >> 1][(nt & 1) * 2 + 0] = act_x2<FP16>(acc[0], acc[1]);
+            a2[mt][nt >> 1][(nt & 1) * 2 + 1] = act_x2<FP16>(acc[2], acc[3]);
         }
-        // layer 2, with layer 3 accumulated as each pair of column tiles
-        // completes a k tile of its A fragment
-        const float2 b3 = *reinterpret_cast<const float2*>(bias + 2 * kMlpHidden + 2 * tig);
-        float acc3[4] = {b3.x, b3.y, b3.x, b3.y};
+    }
+    // layer 2, with layer 3 accumulated as each pair of column tiles
+    // completes a k tile of its A fragment
+    const float2 b3 = *reinterpret_cast<const float2*>(bias + 2 * kMlpHidden + 2 * tig);
+    float out[2][4] = {{b3.x, b3.y, b3.x, b3.y}, {b3.x, b3.y, b3.x, b3.y}};
 #pragma unroll
-        for (int kt3 = 0; kt3 < 4; ++kt3) {
-            uint32_t a3[4];
+    for (int kt3 = 0; kt3 < 4; ++kt3) {
+        uint32_t a3[2][4];
 #pragma unroll
-            for (int half = 0; half < 2; ++half) {
-                const int nt = 2 * kt3 + half;
-                const float2 b = *reinterpret_cast<const float2*>(bias + kMlpHidden + 8 * nt +
-                                                                  2 * tig);
-                float acc[4] = {b.x, b.y, b.x, b.y};
+        for (int half = 0; half < 2; ++half) {
+            const int nt = 2 * kt3 + half;
+            const float2 bv = *reinterpret_cast<const float2*>(bias + kMlpHidden + 8 * nt +
+                                                               2 * tig);
+            float acc[2][4] = {{bv.x, bv.y, bv.x, bv.y}, {bv.x, bv.y, bv.x, bv.y}};
 #pragma unroll
-                for (int kt = 0; kt < 4; ++kt) {
-                    mma_16816<FP16>(acc, a2[kt], smem[kFragW2 + (kt * 8 + nt) * 32 + lane]);
-                }
-                a3[half * 2 + 0] = tanh_x2<FP16>(pack_x2<FP16>(acc[0], acc[1]));
-                a3[half * 2 + 1] = tanh_x2<FP16>(pack_x2<FP16>(acc[2], acc[3]));
+            for (int kt = 0; kt < 4; ++kt) {
+                const uint2 w = smem[kFragW2 + (kt * 8 + nt) * 32 + lane];
+                mma_16816<FP16>(acc[0], a2[0][kt], w);
+                mma_16816<FP16>(acc[1], a2[1][kt], w);
             }
-            mma_16816<FP16>(acc3, a3, smem[kFragW3 + kt3 * 32 + lane]);
-        }
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            out[0][k] = mt == 0 ? acc3[k] : out[0][k];
-            out[1][k] = mt == 0 ? out[1][k] : acc3[k];
+            for (int mt = 0; mt < 2; ++mt) {
+                a3[mt][half * 2 + 0] = act_x2<FP16>(acc[mt][0], acc[mt][1]);
+                a3[mt][half * 2 + 1] = act_x2<FP16>(acc[mt][2], acc[mt][3]);
+            }
         }
+        const uint2 w3 = smem[kFragW3 + kt3 * 32 + lane];
+        mma_16816<FP16>(out[0], a3[0], w3);
+        mma_16816<FP16>(out[1], a3[1], w3);
     }
     // Row r = 16 mt + 8 h + g' sits in lane 4 g' (columns 0, 1; registers
     // 2h, 2h+1) and lane 4 g' + 1 (column 2; register 2h) of tile mt.
