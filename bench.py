@@ -55,7 +55,10 @@ BYTES_PER_STEP = {"focused_mixed": 2 * 4 * 21 * 4, "focused_f64": 2 * 4 * 21 * 8
                   "parker_mixed": 2 * 4 * 16 * 4, "parker_f64": 2 * 4 * 16 * 8}
 # tensor-core work of the fused network per particle-step (padded mma tiles:
 # K 5 -> 16 and N 3 -> 8): 2 x (16 x 64 + 64 x 64 + 64 x 8) flop
-TENSOR_FLOP_PER_STEP = 2 * (16 * 64 + 64 * 64 + 64 * 8)
+def tensor_flop_per_step(hidden: int) -> int:
+    """Tensor flops of one network evaluation (one particle-step): K = 16
+    padded input layer, H x H hidden layer, 8-column padded output layer."""
+    return 2 * (16 * hidden + hidden * hidden + hidden * 8)
 PROFILE = os.path.join(ROOT, "profiles", "push_refill_surrogate_focused_1024x2048.md")
 
 
@@ -206,22 +209,30 @@ def run_focused(args, f0, f1):
     plain = focused_settings(kpt, kpt.CLOSURE_QLT)
     learned = focused_settings(kpt, kpt.CLOSURE_SURROGATE)
     nets, out = {}, {"train": {}}
-    for label, element in (("surrogate", kpt.SURROGATE_BF16), ("surrogate_fp16",
-                                                               kpt.SURROGATE_FP16)):
+    nets_to_train = (("surrogate", kpt.SURROGATE_BF16, args.hidden_width),
+                     ("surrogate_fp16", kpt.SURROGATE_FP16, args.hidden_width),
+                     ("surrogate_h64", kpt.SURROGATE_BF16, 64))
+    if args.hidden_width == 64 or WORLD > 1:
+        nets_to_train = nets_to_train[:2]
+    for label, element, width in nets_to_train:
         t0 = time.perf_counter()
         nets[label] = ctx.train_surrogate(learned, samples=args.train_samples,
-                                          steps=args.train_steps, element_type=element)
+                                          steps=args.train_steps, element_type=element,
+                                          hidden_width=width)
         out["train"][label] = {"seconds": time.perf_counter() - t0,
                                "final_loss": nets[label].final_loss,
                                "samples": args.train_samples, "adam_steps": args.train_steps}
     spectra = {}
     legs = (("surrogate", kpt.PRECISION_MIXED, learned, args.steps, args.warmup),
+            ("f64", kpt.PRECISION_F64, plain, args.f64_steps, 1),
             ("surrogate_fp16", kpt.PRECISION_MIXED, learned, args.steps, args.warmup),
-            ("mixed_qlt", kpt.PRECISION_MIXED, plain, args.steps, args.warmup),
-            ("f64", kpt.PRECISION_F64, plain, args.f64_steps, 1))
+            ("mixed_qlt", kpt.PRECISION_MIXED, plain, args.steps, args.warmup))
+    if "surrogate_h64" in nets:
+        legs = legs + (("surrogate_h64", kpt.PRECISION_MIXED, learned, args.steps,
+                        args.warmup),)
     if WORLD > 1:
         # replicas: every rank runs the headline leg and the FP64 baseline leg
-        legs = (legs[0], legs[3])
+        legs = legs[:2]
     start = None
     for label, precision, settings, steps, warmup in legs:
         if label in nets:
@@ -268,7 +279,7 @@ def run_focused(args, f0, f1):
         for obj in (lower, upper, parts):
             obj.close()
     ref = spectra["f64"]
-    for label in ("surrogate", "surrogate_fp16", "mixed_qlt"):
+    for label in ("surrogate", "surrogate_fp16", "surrogate_h64", "mixed_qlt"):
         if label in out:
             out[label]["spectrum_l1_vs_f64"] = float(np.abs(spectra[label] - ref).sum() /
                                                      ref.sum())
@@ -601,6 +612,9 @@ def main():
     parser.add_argument("--library-particles", type=int, default=1 << 20,
                         help="particles of the library-solver leg (0 skips it)")
     parser.add_argument("--library-steps", type=int, default=10)
+    parser.add_argument("--hidden-width", type=int, default=32, choices=(32, 64),
+                        help="hidden width of the headline network (a width-64 BF16 network "
+                             "is measured beside a width-32 headline)")
     parser.add_argument("--sort-tile", type=int, default=16,
                         help="cell-sort tile (cells) before each push; 0 disables")
     args = parser.parse_args()
@@ -609,7 +623,8 @@ def main():
                           f"{NX}x{NY} stretched-y Harris+islands field, {args.particles} "
                           f"particles, consecutive intervals",
               "nx": NX, "ny": NY, "particles": args.particles, "transport": "focused",
-              "closure": "surrogate (5-64-64-3 MLP, BF16 tensor cores, FP32 accumulation)",
+              "closure": f"surrogate (5-{args.hidden_width}-{args.hidden_width}-3 MLP, BF16 "
+                         f"tensor cores, FP32 accumulation)",
               "l2": "tables larger than L2 (no flush)", "sort_tile": args.sort_tile}
     if args.impl == "reference":
         if rank != 0:
@@ -683,6 +698,9 @@ def main():
         "surrogate_fp16": None if "surrogate_fp16" not in focused else {
             k: focused["surrogate_fp16"][k] for k in
             ("value", "ms_per_step", "spectrum_l1_vs_f64", "judge")},
+        "surrogate_h64": None if "surrogate_h64" not in focused else {
+            k: focused["surrogate_h64"][k] for k in
+            ("value", "ms_per_step", "spectrum_l1_vs_f64", "judge")},
         "train": focused["train"],
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak,
@@ -690,7 +708,8 @@ def main():
                      else per_step_traffic * steps_per_launch,
                      "model": "672 B per particle-step (2 frames x 4 corners x 21 f32 gathers)",
                      "peak_kind": peak_kind,
-                     "tensor_tflops": steps_per_launch * TENSOR_FLOP_PER_STEP / kernel_s / 1e12},
+                     "tensor_tflops": steps_per_launch * tensor_flop_per_step(args.hidden_width)
+                     / kernel_s / 1e12},
         "cpu_baseline": cpu,
         "e2e": {"value": head["e2e"], "unit": "particle-steps/s",
                 "h2d_bytes_per_step": head["state_bytes"],

@@ -155,7 +155,7 @@ typedef struct kpt_particle_arrays {
     int32_t* split_level;
 } kpt_particle_arrays;
 
-/* Training controls of the learned QLT closure (5 -> 64 -> 64 -> 3 tanh MLP,
+/* Training controls of the learned QLT closure (5 -> H -> H -> 3 tanh MLP,
  * inputs mu, ln p, ln|B|, dB^2/B^2, gamma_k; outputs D_mumu, dD_mumu/dmu,
  * ln kappa_parallel).  The box is where the network is trusted: outside it,
  * and for |mu| < mu_cut, the push evaluates the plain closure. */
@@ -172,7 +172,7 @@ typedef struct kpt_surrogate_config {
     int32_t quantization_aware; /* 1: the last quarter of the steps trains through the
                                    served element type's rounding (default 0; measured
                                    no gain for BF16, whose error is activation rounding) */
-    int32_t pad;
+    int32_t hidden_width;     /* H: 32 (default) or 64 */
     double learning_rate;     /* initial; cosine decay to 1 % (default 1e-2) */
     double mu_cut;            /* default 0.02 */
     double mu_max;            /* largest |mu| trained (default 0.999) */
@@ -258,16 +258,21 @@ int kpt_surrogate_destroy(kpt_surrogate* surrogate);
  * (optional, n) is 1 where the network answered. */
 int kpt_surrogate_evaluate(kpt_surrogate* surrogate, uint64_t n, const double* inputs,
                            int tensor_cores, double* outputs, int32_t* served);
-/* Parameter block (FP32, W1 b1 W2 b2 W3 b3 = 4739 floats) and the box
+/* Parameter block (FP32, W1[H][5] b1[H] W2[H][H] b2[H] W3[3][H] b3[3]:
+ * 1379 floats for H = 32, 4739 for H = 64) and the box
  * normalisation (in_lo[5], in_hi[5], out_offset[3], out_scale[3], mu_cut);
  * the box is in feature units ln|mu|, ln p, ln|B|, ln(dB^2/B^2), gamma_k and
  * a feature f maps to 2 (f - lo) / (hi - lo) - 1. */
 int kpt_surrogate_parameters(const kpt_surrogate* surrogate, float* params, int len,
                              float* normalisation, int norm_len);
-/* Loss gradient (FP32) at `params` over n samples taken in order:
- * normalised inputs (n x 5) and normalised targets (n x 3). */
-int kpt_surrogate_gradient(kpt_context* ctx, const float* params, uint64_t n,
-                           const float* inputs, const float* targets, float* grad,
+/* Hidden width and parameter count of a trained network. */
+int kpt_surrogate_shape(const kpt_surrogate* surrogate, int32_t* hidden_width,
+                        int32_t* parameters);
+/* Loss gradient (FP32) at `params` (a network of hidden width H, 0 = the
+ * default) over n samples taken in order: normalised inputs (n x 5) and
+ * normalised targets (n x 3). */
+int kpt_surrogate_gradient(kpt_context* ctx, int32_t hidden_width, const float* params,
+                           uint64_t n, const float* inputs, const float* targets, float* grad,
                            float* loss);
 /* Pushes on this context with closure KPT_CLOSURE_SURROGATE use this
  * network (16-bit weights and activations, FP32 accumulation, on the tensor

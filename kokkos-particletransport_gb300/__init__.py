@@ -84,7 +84,7 @@ class SurrogateConfig(ctypes.Structure):
     """kpt_surrogate_config: training set, optimiser and training box."""
     _fields_ = [("samples", ctypes.c_int32), ("steps", ctypes.c_int32),
                 ("batch", ctypes.c_int32), ("element_type", ctypes.c_int32),
-                ("quantization_aware", ctypes.c_int32), ("pad", ctypes.c_int32)] + \
+                ("quantization_aware", ctypes.c_int32), ("hidden_width", ctypes.c_int32)] + \
                [(n, ctypes.c_double) for n in (
                    "learning_rate", "mu_cut", "mu_max", "p_lo_over_p0", "p_hi_over_p0",
                    "sigma2_lo", "sigma2_hi", "gk_lo", "gk_hi", "b_lo", "b_hi")] + \
@@ -250,7 +250,8 @@ def load_library() -> ctypes.CDLL:
         "kpt_surrogate_destroy": (i32, [vp]),
         "kpt_surrogate_evaluate": (i32, [vp, u64, vp, i32, vp, vp]),
         "kpt_surrogate_parameters": (i32, [vp, vp, i32, vp, i32]),
-        "kpt_surrogate_gradient": (i32, [vp, vp, u64, vp, vp, vp, vp]),
+        "kpt_surrogate_gradient": (i32, [vp, i32, vp, u64, vp, vp, vp, vp]),
+        "kpt_surrogate_shape": (i32, [vp, vp, vp]),
         "kpt_context_set_surrogate": (i32, [vp, vp]),
         "kpt_surrogate_judge": (i32, [vp, vp, vp, vp, vp]),
         "kpt_grid_create": (i32, [vp, i32, i32, vp, vp, vp, pvp]),
@@ -506,14 +507,17 @@ class Context:
         return {"evaluations": int(ev.value), "judged": int(ju.value),
                 "fallbacks": int(fb.value), "max_rel_error": float(err.value)}
 
-    def surrogate_gradient(self, params: np.ndarray, inputs: np.ndarray, targets: np.ndarray):
-        """Loss and its gradient over (normalised) samples, on the GPU."""
+    def surrogate_gradient(self, params: np.ndarray, inputs: np.ndarray, targets: np.ndarray,
+                           hidden_width: int = 0):
+        """Loss and its gradient over (normalised) samples, on the GPU, for a
+        network of the given hidden width (0 = the default)."""
         params = np.ascontiguousarray(params, dtype=np.float32)
         inputs = np.ascontiguousarray(inputs, dtype=np.float32)
         targets = np.ascontiguousarray(targets, dtype=np.float32)
         grad = np.zeros_like(params)
         loss = ctypes.c_float()
-        _check(self.lib.kpt_surrogate_gradient(self.handle, _ptr(params), inputs.shape[0],
+        _check(self.lib.kpt_surrogate_gradient(self.handle, int(hidden_width), _ptr(params),
+                                               inputs.shape[0],
                                                _ptr(inputs), _ptr(targets), _ptr(grad),
                                                ctypes.byref(loss)))
         return float(loss.value), grad
@@ -778,12 +782,14 @@ class Field:
 class Surrogate:
     """A trained QLT surrogate (kpt_surrogate)."""
 
-    PARAMS = 4739
-
     def __init__(self, ctx: Context, handle: ctypes.c_void_p):
         self.ctx = ctx
         self.handle = handle
         self.final_loss = float("nan")
+        hidden, count = ctypes.c_int32(), ctypes.c_int32()
+        _check(ctx.lib.kpt_surrogate_shape(handle, ctypes.byref(hidden), ctypes.byref(count)))
+        self.hidden_width = int(hidden.value)
+        self.parameter_count = int(count.value)
 
     def close(self) -> None:
         if self.handle:
@@ -798,7 +804,7 @@ class Surrogate:
 
     def parameters(self):
         """(FP32 parameter block, normalisation dict)."""
-        params = np.zeros(self.PARAMS, dtype=np.float32)
+        params = np.zeros(self.parameter_count, dtype=np.float32)
         norm = np.zeros(17, dtype=np.float32)
         _check(self.ctx.lib.kpt_surrogate_parameters(self.handle, _ptr(params), params.size,
                                                      _ptr(norm), norm.size))

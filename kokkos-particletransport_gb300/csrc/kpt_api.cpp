@@ -1332,6 +1332,7 @@ void kpt_surrogate_default_config(kpt_surrogate_config* c) {
     c->batch = 8192;
     c->element_type = KPT_SURROGATE_BF16;
     c->quantization_aware = 0;
+    c->hidden_width = kpt::kMlpHiddenDefault;
     c->learning_rate = 1e-2;
     c->mu_cut = 0.02;
     c->mu_max = 0.999;
@@ -1357,6 +1358,8 @@ int kpt_surrogate_train(kpt_context* ctx, const kpt_settings* settings,
                 "kpt_surrogate_train: samples, steps and batch must be positive");
     KPT_REQUIRE(c.element_type == KPT_SURROGATE_BF16 || c.element_type == KPT_SURROGATE_FP16,
                 "kpt_surrogate_train: element_type must be KPT_SURROGATE_BF16 or _FP16");
+    const int hidden = c.hidden_width == 0 ? kpt::kMlpHiddenDefault : c.hidden_width;
+    KPT_REQUIRE(hidden == 32 || hidden == 64, "kpt_surrogate_train: hidden_width must be 32 or 64");
     KPT_REQUIRE(c.mu_cut > 0.0 && c.mu_cut < c.mu_max && c.mu_max < 1.0 &&
                     c.p_lo_over_p0 > 0.0 && c.p_hi_over_p0 > c.p_lo_over_p0 &&
                     c.sigma2_lo > 0.0 && c.sigma2_hi > c.sigma2_lo && c.gk_lo > 1.0 &&
@@ -1380,6 +1383,7 @@ int kpt_surrogate_train(kpt_context* ctx, const kpt_settings* settings,
     }
     box.mu_cut = static_cast<float>(c.mu_cut);
     box.fp16 = c.element_type == KPT_SURROGATE_FP16 ? 1 : 0;
+    box.hidden = hidden;
     box.magnetic_dependency = settings->magnetic_dependency;
     box.momentum_dependency = settings->momentum_dependency;
     box.p0 = settings->p0;
@@ -1417,20 +1421,22 @@ int kpt_surrogate_train(kpt_context* ctx, const kpt_settings* settings,
         box.out_scale[o] = static_cast<float>(std::sqrt(var));
     }
     // Xavier-uniform initial weights, zero biases.
-    sg->params.assign(kpt::kMlpParams, 0.0f);
+    const int pw1 = 0, pw2 = pw1 + hidden * kpt::kMlpIn + hidden;
+    const int pw3 = pw2 + hidden * hidden + hidden;
+    sg->params.assign(kpt::mlp_params(hidden), 0.0f);
     std::mt19937_64 rng(c.seed ^ 0x5851f42d4c957f2dull);
     auto init = [&](int base, int rows, int cols) {
         const float a = std::sqrt(6.0f / static_cast<float>(rows + cols));
         std::uniform_real_distribution<float> u(-a, a);
         for (int k = 0; k < rows * cols; ++k) sg->params[base + k] = u(rng);
     };
-    init(kpt::kMlpW1, kpt::kMlpHidden, kpt::kMlpIn);
-    init(kpt::kMlpW2, kpt::kMlpHidden, kpt::kMlpHidden);
-    init(kpt::kMlpW3, kpt::kMlpOut, kpt::kMlpHidden);
+    init(pw1, hidden, kpt::kMlpIn);
+    init(pw2, hidden, hidden);
+    init(pw3, kpt::kMlpOut, hidden);
     const size_t b = static_cast<size_t>(c.batch);
-    const size_t pcount = kpt::kMlpParams;
+    const size_t pcount = static_cast<size_t>(kpt::mlp_params(hidden));
     const size_t chunks = (b + kpt::kGradChunk - 1) / kpt::kGradChunk;
-    const size_t floats = 4 * pcount + b * (kpt::kMlpIn + 4 * kpt::kMlpHidden + kpt::kMlpOut) +
+    const size_t floats = 4 * pcount + b * (kpt::kMlpIn + 4 * hidden + kpt::kMlpOut) +
                           static_cast<size_t>(c.steps) + chunks * pcount;
     KPT_CUDA(work.reserve(floats * sizeof(float)));
     KPT_CUDA(cudaMemsetAsync(work.ptr, 0, floats * sizeof(float), st));
@@ -1448,10 +1454,10 @@ int kpt_surrogate_train(kpt_context* ctx, const kpt_settings* settings,
     L.v = w + 3 * pcount;
     L.xb = w + 4 * pcount;
     L.h1 = L.xb + b * kpt::kMlpIn;
-    L.h2 = L.h1 + b * kpt::kMlpHidden;
-    L.g1 = L.h2 + b * kpt::kMlpHidden;
-    L.g2 = L.g1 + b * kpt::kMlpHidden;
-    L.gy = L.g2 + b * kpt::kMlpHidden;
+    L.h2 = L.h1 + b * hidden;
+    L.g1 = L.h2 + b * hidden;
+    L.g2 = L.g1 + b * hidden;
+    L.gy = L.g2 + b * hidden;
     L.loss = L.gy + b * kpt::kMlpOut;
     L.partial = L.loss + c.steps;
     L.beta1 = 0.9f;
@@ -1482,29 +1488,31 @@ int kpt_surrogate_train(kpt_context* ctx, const kpt_settings* settings,
     // inference copies: FP32 parameters and the BF16 fragment + bias block
     std::vector<uint32_t> words;
     const bool fp16 = box.fp16 != 0;
-    pack_fragments(sg->params.data() + kpt::kMlpW1, kpt::kMlpHidden, kpt::kMlpIn, 1, 8, fp16,
-                   words);
-    pack_fragments(sg->params.data() + kpt::kMlpW2, kpt::kMlpHidden, kpt::kMlpHidden, 4, 8, fp16,
-                   words);
-    pack_fragments(sg->params.data() + kpt::kMlpW3, kpt::kMlpOut, kpt::kMlpHidden, 4, 1, fp16,
-                   words);
-    std::vector<float> bias(kpt::kBiasCount, 0.0f);
-    for (int k = 0; k < kpt::kMlpHidden; ++k) {
-        bias[k] = sg->params[kpt::kMlpB1 + k];
-        bias[kpt::kMlpHidden + k] = sg->params[kpt::kMlpB2 + k];
+    const int nt = hidden / 8, kt = hidden / 16;
+    pack_fragments(sg->params.data() + pw1, hidden, kpt::kMlpIn, 1, nt, fp16, words);
+    pack_fragments(sg->params.data() + pw2, hidden, hidden, kt, nt, fp16, words);
+    pack_fragments(sg->params.data() + pw3, kpt::kMlpOut, hidden, kt, 1, fp16, words);
+    std::vector<float> bias(2 * hidden + 8, 0.0f);
+    for (int k = 0; k < hidden; ++k) {
+        bias[k] = sg->params[pw1 + hidden * kpt::kMlpIn + k];
+        bias[hidden + k] = sg->params[pw2 + hidden * hidden + k];
     }
-    for (int k = 0; k < kpt::kMlpOut; ++k) bias[2 * kpt::kMlpHidden + k] = sg->params[kpt::kMlpB3 + k];
+    for (int k = 0; k < kpt::kMlpOut; ++k) {
+        bias[2 * hidden + k] = sg->params[pw3 + kpt::kMlpOut * hidden + k];
+    }
     for (float b : bias) {
         uint32_t bits;
         std::memcpy(&bits, &b, sizeof(bits));
         words.push_back(bits);
     }
     KPT_CUDA(cudaMalloc(&sg->d_params, pcount * sizeof(float)));
-    KPT_CUDA(cudaMalloc(&sg->d_block, kpt::kSurrogateSmemBytes));
+    const size_t block_bytes = kpt::mlp_smem_bytes(hidden);
+    KPT_REQUIRE(words.size() * sizeof(uint32_t) == block_bytes,
+                "kpt_surrogate_train: fragment block size mismatch");
+    KPT_CUDA(cudaMalloc(&sg->d_block, block_bytes));
     KPT_CUDA(cudaMemcpy(sg->d_params, sg->params.data(), pcount * sizeof(float),
                         cudaMemcpyHostToDevice));
-    KPT_CUDA(cudaMemcpy(sg->d_block, words.data(), kpt::kSurrogateSmemBytes,
-                        cudaMemcpyHostToDevice));
+    KPT_CUDA(cudaMemcpy(sg->d_block, words.data(), block_bytes, cudaMemcpyHostToDevice));
     *out = sg.release();
     return KPT_OK;
 }
@@ -1522,7 +1530,8 @@ int kpt_surrogate_parameters(const kpt_surrogate* sg, float* params, int len, fl
                              int norm_len) {
     KPT_REQUIRE(sg != nullptr, "kpt_surrogate_parameters: NULL handle");
     if (params != nullptr) {
-        KPT_REQUIRE(len >= kpt::kMlpParams, "kpt_surrogate_parameters: params too short");
+        KPT_REQUIRE(len >= static_cast<int>(sg->params.size()),
+                    "kpt_surrogate_parameters: params too short");
         std::copy(sg->params.begin(), sg->params.end(), params);
     }
     if (norm != nullptr) {
@@ -1537,6 +1546,13 @@ int kpt_surrogate_parameters(const kpt_surrogate* sg, float* params, int len, fl
         }
         norm[16] = sg->box.mu_cut;
     }
+    return KPT_OK;
+}
+
+int kpt_surrogate_shape(const kpt_surrogate* sg, int32_t* hidden_width, int32_t* parameters) {
+    KPT_REQUIRE(sg != nullptr, "kpt_surrogate_shape: NULL handle");
+    if (hidden_width) *hidden_width = sg->box.hidden;
+    if (parameters) *parameters = static_cast<int32_t>(sg->params.size());
     return KPT_OK;
 }
 
@@ -1563,15 +1579,19 @@ int kpt_surrogate_evaluate(kpt_surrogate* sg, uint64_t n, const double* inputs, 
     return KPT_OK;
 }
 
-int kpt_surrogate_gradient(kpt_context* ctx, const float* params, uint64_t n, const float* inputs,
-                           const float* targets, float* grad, float* loss) {
+int kpt_surrogate_gradient(kpt_context* ctx, int32_t hidden_width, const float* params,
+                           uint64_t n, const float* inputs, const float* targets, float* grad,
+                           float* loss) {
     KPT_REQUIRE(ctx && params && inputs && targets && grad, "kpt_surrogate_gradient: NULL");
     KPT_REQUIRE(n > 0 && n <= (1u << 20), "kpt_surrogate_gradient: 0 < n <= 2^20");
+    const int hidden = hidden_width == 0 ? kpt::kMlpHiddenDefault : hidden_width;
+    KPT_REQUIRE(hidden == 32 || hidden == 64,
+                "kpt_surrogate_gradient: hidden_width must be 32 or 64");
     if (int rc = activate(ctx)) return rc;
-    const size_t pcount = kpt::kMlpParams;
+    const size_t pcount = static_cast<size_t>(kpt::mlp_params(hidden));
     const size_t chunks = (n + kpt::kGradChunk - 1) / kpt::kGradChunk;
     const size_t floats =
-        n * (5 + 3) + 2 * pcount + n * (5 + 4 * kpt::kMlpHidden + 3) + 1 + chunks * pcount;
+        n * (5 + 3) + 2 * pcount + n * (5 + 4 * hidden + 3) + 1 + chunks * pcount;
     ScopedBuffer buf;
     KPT_CUDA(buf.reserve(floats * sizeof(float)));
     KPT_CUDA(cudaMemsetAsync(buf.ptr, 0, floats * sizeof(float), ctx->stream));
@@ -1596,11 +1616,12 @@ int kpt_surrogate_gradient(kpt_context* ctx, const float* params, uint64_t n, co
     L.params = t + n * 3;
     L.grad = L.params + pcount;
     L.xb = L.grad + pcount;
+    L.box.hidden = hidden;
     L.h1 = L.xb + n * 5;
-    L.h2 = L.h1 + n * kpt::kMlpHidden;
-    L.g1 = L.h2 + n * kpt::kMlpHidden;
-    L.g2 = L.g1 + n * kpt::kMlpHidden;
-    L.gy = L.g2 + n * kpt::kMlpHidden;
+    L.h2 = L.h1 + n * hidden;
+    L.g1 = L.h2 + n * hidden;
+    L.g2 = L.g1 + n * hidden;
+    L.gy = L.g2 + n * hidden;
     L.loss = L.gy + n * 3;
     L.partial = L.loss + 1;
     cudaStream_t st = ctx->stream;

@@ -179,7 +179,7 @@ struct SurrogateTrainLaunch {
     float* g2;
     float* gy;        // batch x 3
     float* loss;      // one float per step
-    float* partial;   // ceil(batch / kGradChunk) x kMlpParams gradient partials
+    float* partial;   // ceil(batch / kGradChunk) x parameter-count gradient partials
     float beta1, beta2, lr;
     int quant;        // rounding emulated from step quant_from on: 0 none, 1 BF16, 2 FP16
     int quant_from;

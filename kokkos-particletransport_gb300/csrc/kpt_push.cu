@@ -852,7 +852,7 @@ struct JudgeTally {
 // the training box, or with |mu| < mu_cut, use the plain closure; one
 // substep in judge_period of each particle also evaluates the plain closure
 // and records the larger relative error of D_mumu and kappa_parallel.
-template <bool FP16>
+template <bool FP16, int H>
 __device__ __forceinline__ bool substep_surrogate(StateMixed& st, const PushParams& P, bool have,
                                                   const uint2* smem, JudgeTally& tally) {
     const SurrogateDevice& sg = P.sg;
@@ -885,7 +885,7 @@ __device__ __forceinline__ bool substep_surrogate(StateMixed& st, const PushPara
     }
     __syncwarp();
     float y[kMlpOut];
-    mlp_warp<FP16>(smem, f, y);
+    mlp_warp<FP16, H>(smem, f, y);
     if (!have) {
         return false;
     }
@@ -1068,12 +1068,14 @@ struct MinBlocks<StateMixed, true> {
     static constexpr int value = 4;
 };
 
-// The surrogate instantiations (SURR = 1 BF16 network, 2 FP16 network) keep
-// the MLP fragments live beside the particle state and the sampled
-// coefficients.
+// The surrogate instantiations keep the MLP fragments live beside the
+// particle state and the sampled coefficients.  SURR: 1 BF16 and 2 FP16
+// networks of hidden width 64, 3 BF16 and 4 FP16 networks of width 32.
 #ifndef KPT_SURROGATE_MIN_BLOCKS
 #define KPT_SURROGATE_MIN_BLOCKS 4
 #endif
+__host__ __device__ constexpr bool surr_fp16(int surr) { return surr == 2 || surr == 4; }
+__host__ __device__ constexpr int surr_hidden(int surr) { return surr <= 2 ? 64 : 32; }
 template <typename State, bool FOCUSED, int SURR = 0>
 __global__ void __launch_bounds__(128, SURR ? KPT_SURROGATE_MIN_BLOCKS
                                             : MinBlocks<State, FOCUSED>::value)
@@ -1084,7 +1086,7 @@ __global__ void __launch_bounds__(128, SURR ? KPT_SURROGATE_MIN_BLOCKS
     extern __shared__ uint2 surrogate_smem[];
     JudgeTally tally{0ull, 0ull, 0ull, 0.0f};
     if (SURR) {
-        load_surrogate_block(P.sg.block, surrogate_smem);
+        load_surrogate_block<surr_hidden(SURR)>(P.sg.block, surrogate_smem);
     }
     State st;
     bool have = false;
@@ -1130,7 +1132,8 @@ __global__ void __launch_bounds__(128, SURR ? KPT_SURROGATE_MIN_BLOCKS
         }
         bool more;
         if constexpr (SURR) {
-            more = substep_surrogate<SURR == 2>(st, P, have, surrogate_smem, tally);
+            more = substep_surrogate<surr_fp16(SURR), surr_hidden(SURR)>(st, P, have,
+                                                                          surrogate_smem, tally);
         } else {
             more = have && substep<FOCUSED>(st, P);
         }
@@ -1203,7 +1206,7 @@ template <typename State, bool FOCUSED, int SURR = 0>
 cudaError_t launch_push(const PushLaunch& L, cudaStream_t stream) {
     const PushParams P = make_push_params(L);
     const int threads = 128;
-    const size_t smem = SURR ? kSurrogateSmemBytes : 0;
+    const size_t smem = SURR ? mlp_smem_bytes(surr_hidden(SURR)) : 0;
     if (L.schedule == kScheduleSimple && !SURR) {
         const uint64_t want = (L.count + threads - 1) / threads;
         const int blocks =
@@ -1434,8 +1437,13 @@ cudaError_t launch_push_interval(const PushLaunch& launch, cudaStream_t stream) 
                               : launch_push<StateF64, false>(launch, stream);
     }
     if (launch.surrogate != nullptr) {
-        return launch.surrogate->box.fp16 ? launch_push<StateMixed, true, 2>(launch, stream)
-                                          : launch_push<StateMixed, true, 1>(launch, stream);
+        const SurrogateBox& box = launch.surrogate->box;
+        if (box.hidden == 64) {
+            return box.fp16 ? launch_push<StateMixed, true, 2>(launch, stream)
+                            : launch_push<StateMixed, true, 1>(launch, stream);
+        }
+        return box.fp16 ? launch_push<StateMixed, true, 4>(launch, stream)
+                        : launch_push<StateMixed, true, 3>(launch, stream);
     }
     return launch.focused ? launch_push<StateMixed, true>(launch, stream)
                           : launch_push<StateMixed, false>(launch, stream);

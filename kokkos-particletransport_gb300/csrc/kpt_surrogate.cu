@@ -112,6 +112,7 @@ __device__ __forceinline__ float normalise_input(const SurrogateBox& box, int k,
 
 // Forward and backward of one minibatch, one thread per sample.  Stores
 // H1, H2 (activations) and G1, G2, GY (deltas) for the gradient reductions.
+template <int H>
 __global__ void __launch_bounds__(128) fwd_bwd_kernel(const float* __restrict__ x,
                                                       const float* __restrict__ t, int n,
                                                       uint64_t seed, int step, int batch,
@@ -124,10 +125,10 @@ __global__ void __launch_bounds__(128) fwd_bwd_kernel(const float* __restrict__ 
     // inputs and activations in the 16-bit type, FP16 pre-activations too;
     // biases and accumulation FP32) and the backward passes straight
     // through it
-    __shared__ float w[kMlpParams];
-    for (int k = threadIdx.x; k < kMlpParams; k += blockDim.x) {
-        const bool bias = (k >= kMlpB1 && k < kMlpW2) || (k >= kMlpB2 && k < kMlpW3) ||
-                          k >= kMlpB3;
+    using M = Mlp<H>;
+    __shared__ float w[M::Params];
+    for (int k = threadIdx.x; k < M::Params; k += blockDim.x) {
+        const bool bias = (k >= M::B1 && k < M::W2) || (k >= M::B2 && k < M::W3) || k >= M::B3;
         w[k] = bias ? params[k] : quantize(params[k], quant);
     }
     __syncthreads();
@@ -147,21 +148,21 @@ __global__ void __launch_bounds__(128) fwd_bwd_kernel(const float* __restrict__ 
                              quant);
             xb[static_cast<size_t>(b) * kMlpIn + k] = in[k];
         }
-        float a1[kMlpHidden];
-        for (int j = 0; j < kMlpHidden; ++j) {
-            float z = w[kMlpB1 + j];
-            for (int k = 0; k < kMlpIn; ++k) z += w[kMlpW1 + j * kMlpIn + k] * in[k];
+        float a1[H];
+        for (int j = 0; j < H; ++j) {
+            float z = w[M::B1 + j];
+            for (int k = 0; k < kMlpIn; ++k) z += w[M::W1 + j * kMlpIn + k] * in[k];
             a1[j] = quantize(tanhf(quant == 2 ? quantize(z, quant) : z), quant);
-            h1[static_cast<size_t>(b) * kMlpHidden + j] = a1[j];
+            h1[static_cast<size_t>(b) * H + j] = a1[j];
         }
         float y[kMlpOut];
-        for (int o = 0; o < kMlpOut; ++o) y[o] = w[kMlpB3 + o];
-        for (int j = 0; j < kMlpHidden; ++j) {
-            float z = w[kMlpB2 + j];
-            for (int k = 0; k < kMlpHidden; ++k) z += w[kMlpW2 + j * kMlpHidden + k] * a1[k];
+        for (int o = 0; o < kMlpOut; ++o) y[o] = w[M::B3 + o];
+        for (int j = 0; j < H; ++j) {
+            float z = w[M::B2 + j];
+            for (int k = 0; k < H; ++k) z += w[M::W2 + j * H + k] * a1[k];
             const float a2 = quantize(tanhf(quant == 2 ? quantize(z, quant) : z), quant);
-            h2[static_cast<size_t>(b) * kMlpHidden + j] = a2;
-            for (int o = 0; o < kMlpOut; ++o) y[o] += w[kMlpW3 + o * kMlpHidden + j] * a2;
+            h2[static_cast<size_t>(b) * H + j] = a2;
+            for (int o = 0; o < kMlpOut; ++o) y[o] += w[M::W3 + o * H + j] * a2;
         }
         float dy[kMlpOut];
         for (int o = 0; o < kMlpOut; ++o) {
@@ -172,18 +173,18 @@ __global__ void __launch_bounds__(128) fwd_bwd_kernel(const float* __restrict__ 
             dy[o] = 2.0f * e / static_cast<float>(batch * kMlpOut);
             gy[static_cast<size_t>(b) * kMlpOut + o] = dy[o];
         }
-        float d1[kMlpHidden];
-        for (int k = 0; k < kMlpHidden; ++k) d1[k] = 0.0f;
-        for (int j = 0; j < kMlpHidden; ++j) {
-            const float a2 = h2[static_cast<size_t>(b) * kMlpHidden + j];
+        float d1[H];
+        for (int k = 0; k < H; ++k) d1[k] = 0.0f;
+        for (int j = 0; j < H; ++j) {
+            const float a2 = h2[static_cast<size_t>(b) * H + j];
             float dh = 0.0f;
-            for (int o = 0; o < kMlpOut; ++o) dh += w[kMlpW3 + o * kMlpHidden + j] * dy[o];
+            for (int o = 0; o < kMlpOut; ++o) dh += w[M::W3 + o * H + j] * dy[o];
             const float dz = dh * (1.0f - a2 * a2);
-            g2[static_cast<size_t>(b) * kMlpHidden + j] = dz;
-            for (int k = 0; k < kMlpHidden; ++k) d1[k] += w[kMlpW2 + j * kMlpHidden + k] * dz;
+            g2[static_cast<size_t>(b) * H + j] = dz;
+            for (int k = 0; k < H; ++k) d1[k] += w[M::W2 + j * H + k] * dz;
         }
-        for (int k = 0; k < kMlpHidden; ++k) {
-            g1[static_cast<size_t>(b) * kMlpHidden + k] = d1[k] * (1.0f - a1[k] * a1[k]);
+        for (int k = 0; k < H; ++k) {
+            g1[static_cast<size_t>(b) * H + k] = d1[k] * (1.0f - a1[k] * a1[k]);
         }
     }
     // batch loss (mean squared error in normalised units)
@@ -197,28 +198,30 @@ __global__ void __launch_bounds__(128) fwd_bwd_kernel(const float* __restrict__ 
 // (row, chunk) sums its chunk of kGradChunk samples for one parameter row,
 // threads over the row's columns; grad_sum_kernel then adds the chunk
 // partials in chunk order.  Row r of:
-//   W1 (64 rows x 5):  sum_b G1[b][r] X[b][c];   b1[r] = sum_b G1[b][r]
-//   W2 (64 rows x 64): sum_b G2[b][r] H1[b][c];  b2[r] = sum_b G2[b][r]
-//   W3 (3 rows x 64):  sum_b GY[b][r] H2[b][c];  b3[r] = sum_b GY[b][r]
+//   W1 (H rows x 5):  sum_b G1[b][r] X[b][c];   b1[r] = sum_b G1[b][r]
+//   W2 (H rows x H):  sum_b G2[b][r] H1[b][c];  b2[r] = sum_b G2[b][r]
+//   W3 (3 rows x H):  sum_b GY[b][r] H2[b][c];  b3[r] = sum_b GY[b][r]
+template <int H>
 __global__ void __launch_bounds__(64) grad_partial_kernel(int batch, const float* xb,
                                                           const float* h1, const float* h2,
                                                           const float* g1, const float* g2,
                                                           const float* gy, float* partial) {
+    using M = Mlp<H>;
     const int row = blockIdx.x;
     const int chunk = blockIdx.y;
     const int c = threadIdx.x;
     const float* delta;
     const float* input;
     int dstride, istride, cols, wbase, bbase, r;
-    if (row < kMlpHidden) {
-        r = row; delta = g1; dstride = kMlpHidden; input = xb; istride = kMlpIn; cols = kMlpIn;
-        wbase = kMlpW1; bbase = kMlpB1;
-    } else if (row < 2 * kMlpHidden) {
-        r = row - kMlpHidden; delta = g2; dstride = kMlpHidden; input = h1; istride = kMlpHidden;
-        cols = kMlpHidden; wbase = kMlpW2; bbase = kMlpB2;
+    if (row < H) {
+        r = row; delta = g1; dstride = H; input = xb; istride = kMlpIn; cols = kMlpIn;
+        wbase = M::W1; bbase = M::B1;
+    } else if (row < 2 * H) {
+        r = row - H; delta = g2; dstride = H; input = h1; istride = H;
+        cols = H; wbase = M::W2; bbase = M::B2;
     } else {
-        r = row - 2 * kMlpHidden; delta = gy; dstride = kMlpOut; input = h2;
-        istride = kMlpHidden; cols = kMlpHidden; wbase = kMlpW3; bbase = kMlpB3;
+        r = row - 2 * H; delta = gy; dstride = kMlpOut; input = h2;
+        istride = H; cols = H; wbase = M::W3; bbase = M::B3;
     }
     const int b0 = chunk * kGradChunk;
     const int b1 = b0 + kGradChunk < batch ? b0 + kGradChunk : batch;
@@ -228,31 +231,35 @@ __global__ void __launch_bounds__(64) grad_partial_kernel(int batch, const float
         if (c < cols) acc += d * input[static_cast<size_t>(b) * istride + c];
         bacc += d;
     }
-    float* out = partial + static_cast<size_t>(chunk) * kMlpParams;
+    float* out = partial + static_cast<size_t>(chunk) * M::Params;
     if (c < cols) out[wbase + r * cols + c] = acc;
     if (c == 0) out[bbase + r] = bacc;
 }
 
-__global__ void grad_sum_kernel(const float* partial, int chunks, float* grad) {
+__global__ void grad_sum_kernel(const float* partial, int chunks, int params, float* grad) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= kMlpParams) return;
+    if (k >= params) return;
     float sum = 0.0f;
-    for (int ch = 0; ch < chunks; ++ch) sum += partial[static_cast<size_t>(ch) * kMlpParams + k];
+    for (int ch = 0; ch < chunks; ++ch) sum += partial[static_cast<size_t>(ch) * params + k];
     grad[k] = sum;
 }
 
+template <int H>
 cudaError_t launch_gradients(const SurrogateTrainLaunch& L, cudaStream_t stream) {
+    using M = Mlp<H>;
     const int chunks = (L.batch + kGradChunk - 1) / kGradChunk;
-    grad_partial_kernel<<<dim3(2 * kMlpHidden + kMlpOut, chunks), 64, 0, stream>>>(
+    grad_partial_kernel<H><<<dim3(2 * H + kMlpOut, chunks), 64, 0, stream>>>(
         L.batch, L.xb, L.h1, L.h2, L.g1, L.g2, L.gy, L.partial);
-    grad_sum_kernel<<<(kMlpParams + 255) / 256, 256, 0, stream>>>(L.partial, chunks, L.grad);
+    grad_sum_kernel<<<(M::Params + 255) / 256, 256, 0, stream>>>(L.partial, chunks, M::Params,
+                                                                 L.grad);
     return cudaGetLastError();
 }
 
-__global__ void adam_kernel(float* params, const float* grad, float* m, float* v, float lr,
-                            float beta1, float beta2, float eps, float bias1, float bias2) {
+__global__ void adam_kernel(float* params, const float* grad, float* m, float* v, int count,
+                            float lr, float beta1, float beta2, float eps, float bias1,
+                            float bias2) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= kMlpParams) return;
+    if (k >= count) return;
     const float g = grad[k];
     const float mk = beta1 * m[k] + (1.0f - beta1) * g;
     const float vk = beta2 * v[k] + (1.0f - beta2) * g * g;
@@ -262,19 +269,21 @@ __global__ void adam_kernel(float* params, const float* grad, float* m, float* v
 }
 
 // FP32 SIMT forward of normalised features -> normalised outputs.
+template <int H>
 __device__ void forward_fp32(const float* w, const float (&in)[kMlpIn], float (&y)[kMlpOut]) {
-    float a1[kMlpHidden];
-    for (int j = 0; j < kMlpHidden; ++j) {
-        float z = w[kMlpB1 + j];
-        for (int k = 0; k < kMlpIn; ++k) z += w[kMlpW1 + j * kMlpIn + k] * in[k];
+    using M = Mlp<H>;
+    float a1[H];
+    for (int j = 0; j < H; ++j) {
+        float z = w[M::B1 + j];
+        for (int k = 0; k < kMlpIn; ++k) z += w[M::W1 + j * kMlpIn + k] * in[k];
         a1[j] = tanhf(z);
     }
-    for (int o = 0; o < kMlpOut; ++o) y[o] = w[kMlpB3 + o];
-    for (int j = 0; j < kMlpHidden; ++j) {
-        float z = w[kMlpB2 + j];
-        for (int k = 0; k < kMlpHidden; ++k) z += w[kMlpW2 + j * kMlpHidden + k] * a1[k];
+    for (int o = 0; o < kMlpOut; ++o) y[o] = w[M::B3 + o];
+    for (int j = 0; j < H; ++j) {
+        float z = w[M::B2 + j];
+        for (int k = 0; k < H; ++k) z += w[M::W2 + j * H + k] * a1[k];
         const float a2 = tanhf(z);
-        for (int o = 0; o < kMlpOut; ++o) y[o] += w[kMlpW3 + o * kMlpHidden + j] * a2;
+        for (int o = 0; o < kMlpOut; ++o) y[o] += w[M::W3 + o * H + j] * a2;
     }
 }
 
@@ -284,7 +293,7 @@ __device__ void forward_fp32(const float* w, const float (&in)[kMlpIn], float (&
 // |mu| >= mu_cut; the plain closure serves the rest.  Warps stay converged
 // (the loop bound is per warp) because the tensor-core path is collective.
 // MODE 0: FP32 SIMT, 1: BF16 tensor cores, 2: FP16 tensor cores.
-template <int MODE>
+template <int MODE, int H>
 __global__ void __launch_bounds__(128) eval_kernel(int n, const double* __restrict__ in,
                                                    SurrogateBox box,
                                                    const float* __restrict__ params,
@@ -293,10 +302,10 @@ __global__ void __launch_bounds__(128) eval_kernel(int n, const double* __restri
                                                    int* __restrict__ served) {
     extern __shared__ uint2 smem[];
     if (MODE != 0) {
-        load_surrogate_block(block, smem);
+        load_surrogate_block<H>(block, smem);
     } else {
         float* w = reinterpret_cast<float*>(smem);
-        for (int k = threadIdx.x; k < kMlpParams; k += blockDim.x) w[k] = params[k];
+        for (int k = threadIdx.x; k < Mlp<H>::Params; k += blockDim.x) w[k] = params[k];
         __syncthreads();
     }
     const int lane = threadIdx.x & 31;
@@ -322,9 +331,9 @@ __global__ void __launch_bounds__(128) eval_kernel(int n, const double* __restri
         }
         float y[kMlpOut];
         if (MODE != 0) {
-            mlp_warp<MODE == 2>(smem, f, y);
+            mlp_warp<MODE == 2, H>(smem, f, y);
         } else {
-            forward_fp32(reinterpret_cast<const float*>(smem), f, y);
+            forward_fp32<H>(reinterpret_cast<const float*>(smem), f, y);
         }
         if (!have) continue;
         const double p = exp(raw[1]);
@@ -375,43 +384,67 @@ cudaError_t surrogate_make_samples(uint64_t seed, int n, const SurrogateBox& box
     return cudaGetLastError();
 }
 
-cudaError_t surrogate_train_step(const SurrogateTrainLaunch& L, int step, cudaStream_t stream) {
-    fwd_bwd_kernel<<<(L.batch + 127) / 128, 128, 0, stream>>>(
+namespace {
+
+template <int H>
+cudaError_t train_step(const SurrogateTrainLaunch& L, int step, cudaStream_t stream) {
+    fwd_bwd_kernel<H><<<(L.batch + 127) / 128, 128, 0, stream>>>(
         L.x, L.t, L.n, L.seed, step, L.batch, L.box, L.params, L.xb, L.h1, L.h2, L.g1, L.g2, L.gy,
         L.loss + step, step >= L.quant_from ? L.quant : 0);
-    launch_gradients(L, stream);
+    launch_gradients<H>(L, stream);
     const float t1 = static_cast<float>(step + 1);
     const float bias1 = 1.0f - powf(L.beta1, t1);
     const float bias2 = 1.0f - powf(L.beta2, t1);
-    adam_kernel<<<(kMlpParams + 255) / 256, 256, 0, stream>>>(
-        L.params, L.grad, L.m, L.v, L.lr, L.beta1, L.beta2, 1e-8f, bias1, bias2);
+    adam_kernel<<<(Mlp<H>::Params + 255) / 256, 256, 0, stream>>>(
+        L.params, L.grad, L.m, L.v, Mlp<H>::Params, L.lr, L.beta1, L.beta2, 1e-8f, bias1, bias2);
     return cudaGetLastError();
 }
 
-cudaError_t surrogate_gradient(const SurrogateTrainLaunch& L, cudaStream_t stream) {
-    fwd_bwd_kernel<<<(L.batch + 127) / 128, 128, 0, stream>>>(
+template <int H>
+cudaError_t gradient(const SurrogateTrainLaunch& L, cudaStream_t stream) {
+    fwd_bwd_kernel<H><<<(L.batch + 127) / 128, 128, 0, stream>>>(
         L.x, L.t, L.n, L.seed, -1, L.batch, L.box, L.params, L.xb, L.h1, L.h2, L.g1, L.g2, L.gy,
         L.loss, 0);
-    return launch_gradients(L, stream);
+    return launch_gradients<H>(L, stream);
+}
+
+template <int H>
+cudaError_t eval(int n, const double* inputs, const SurrogateBox& box, const float* params,
+                 const uint2* block, bool tensor, double* out, int* served,
+                 cudaStream_t stream) {
+    const int threads = 128;
+    int blocks = (n + threads - 1) / threads;
+    blocks = blocks < 1 ? 1 : (blocks > 152 * 8 ? 152 * 8 : blocks);
+    const size_t smem = Mlp<H>::SmemBytes;
+    if (tensor && box.fp16) {
+        eval_kernel<2, H><<<blocks, threads, smem, stream>>>(n, inputs, box, params, block, out,
+                                                             served);
+    } else if (tensor) {
+        eval_kernel<1, H><<<blocks, threads, smem, stream>>>(n, inputs, box, params, block, out,
+                                                             served);
+    } else {
+        eval_kernel<0, H><<<blocks, threads, Mlp<H>::Params * sizeof(float), stream>>>(
+            n, inputs, box, params, block, out, served);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t surrogate_train_step(const SurrogateTrainLaunch& L, int step, cudaStream_t stream) {
+    return L.box.hidden == 64 ? train_step<64>(L, step, stream) : train_step<32>(L, step, stream);
+}
+
+cudaError_t surrogate_gradient(const SurrogateTrainLaunch& L, cudaStream_t stream) {
+    return L.box.hidden == 64 ? gradient<64>(L, stream) : gradient<32>(L, stream);
 }
 
 cudaError_t surrogate_eval(int n, const double* inputs, const SurrogateBox& box,
                            const float* params, const uint2* block, bool tensor, double* out,
                            int* served, cudaStream_t stream) {
-    const int threads = 128;
-    int blocks = (n + threads - 1) / threads;
-    blocks = blocks < 1 ? 1 : (blocks > 152 * 8 ? 152 * 8 : blocks);
-    if (tensor && box.fp16) {
-        eval_kernel<2><<<blocks, threads, kSurrogateSmemBytes, stream>>>(n, inputs, box, params,
-                                                                         block, out, served);
-    } else if (tensor) {
-        eval_kernel<1><<<blocks, threads, kSurrogateSmemBytes, stream>>>(n, inputs, box, params,
-                                                                         block, out, served);
-    } else {
-        eval_kernel<0><<<blocks, threads, kMlpParams * sizeof(float), stream>>>(
-            n, inputs, box, params, block, out, served);
-    }
-    return cudaGetLastError();
+    return box.hidden == 64 ? eval<64>(n, inputs, box, params, block, tensor, out, served, stream)
+                            : eval<32>(n, inputs, box, params, block, tensor, out, served,
+                                       stream);
 }
 
 }  // namespace kpt

@@ -1,7 +1,8 @@
 // The learned closure shared by the trainer (kpt_surrogate.cu) and the push
-// (kpt_push.cu): a 5 -> 64 -> 64 -> 3 tanh MLP standing in for the slab-QLT
-// pitch-angle scattering closure (LegencyModel.hpp:557-645) and the
-// kappa_parallel closure of the driver (src/main.cpp:1177-1193).
+// (kpt_push.cu): a 5 -> H -> H -> 3 tanh MLP (hidden width H = 32 or 64)
+// standing in for the slab-QLT pitch-angle scattering closure
+// (LegencyModel.hpp:557-645) and the kappa_parallel closure of the driver
+// (src/main.cpp:1177-1193).
 //
 // Features (each mapped affinely from the training box onto [-1, 1]):
 //   f0 = ln|mu|, f1 = ln p, f2 = ln|B|, f3 = ln(dB^2/B^2), f4 = gamma_k.
@@ -19,9 +20,9 @@
 //
 // Inference is warp-collective: the 32 particles of a warp are the M = 32
 // rows of three mma.sync.m16n8k16 GEMMs (BF16, or FP16 on request) with FP32
-// accumulation.  The
-// accumulator fragment of one layer is, after tanh and packing to 16-bit pairs,
-// exactly the A fragment of the next, so activations never leave registers.
+// accumulation.  The accumulator fragment of one layer is, after the
+// activation and packing to 16-bit pairs, exactly the A fragment of the
+// next, so activations never leave registers.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -31,26 +32,41 @@
 namespace kpt {
 
 constexpr int kMlpIn = 5;
-constexpr int kMlpHidden = 64;
 constexpr int kMlpOut = 3;
-// parameter block, FP32: W1[64][5] b1[64] W2[64][64] b2[64] W3[3][64] b3[3]
-constexpr int kMlpW1 = 0;
-constexpr int kMlpB1 = kMlpW1 + kMlpHidden * kMlpIn;
-constexpr int kMlpW2 = kMlpB1 + kMlpHidden;
-constexpr int kMlpB2 = kMlpW2 + kMlpHidden * kMlpHidden;
-constexpr int kMlpW3 = kMlpB2 + kMlpHidden;
-constexpr int kMlpB3 = kMlpW3 + kMlpOut * kMlpHidden;
-constexpr int kMlpParams = kMlpB3 + kMlpOut;
+constexpr int kMlpHiddenDefault = 32;
 
-// 16-bit B fragments (one uint2 per lane per 16x8 tile), in this order:
-// layer 1 [nt 8], layer 2 [kt 4][nt 8], layer 3 [kt 4]; then FP32 biases
-// b1[64], b2[64], b3[8] (zero padded).
-constexpr int kFragW1 = 0;
-constexpr int kFragW2 = kFragW1 + 8 * 32;
-constexpr int kFragW3 = kFragW2 + 4 * 8 * 32;
-constexpr int kFragCount = kFragW3 + 4 * 32;  // uint2 entries
-constexpr int kBiasCount = 2 * kMlpHidden + 8;
-constexpr size_t kSurrogateSmemBytes = kFragCount * sizeof(uint2) + kBiasCount * sizeof(float);
+// Parameter block, FP32: W1[H][5] b1[H] W2[H][H] b2[H] W3[3][H] b3[3].
+// Shared-memory block of the served network: 16-bit B fragments (one uint2
+// per lane per 16x8 tile) in the order layer 1 [nt H/8], layer 2
+// [kt H/16][nt H/8], layer 3 [kt H/16]; then FP32 biases b1[H], b2[H],
+// b3[8] (zero padded).
+template <int H>
+struct Mlp {
+    static_assert(H == 32 || H == 64, "hidden width 32 or 64");
+    static constexpr int W1 = 0;
+    static constexpr int B1 = W1 + H * kMlpIn;
+    static constexpr int W2 = B1 + H;
+    static constexpr int B2 = W2 + H * H;
+    static constexpr int W3 = B2 + H;
+    static constexpr int B3 = W3 + kMlpOut * H;
+    static constexpr int Params = B3 + kMlpOut;
+    static constexpr int NT = H / 8;   // 8-column tiles of a hidden layer
+    static constexpr int KT = H / 16;  // 16-deep k tiles of a hidden layer
+    static constexpr int FragW1 = 0;
+    static constexpr int FragW2 = FragW1 + NT * 32;
+    static constexpr int FragW3 = FragW2 + KT * NT * 32;
+    static constexpr int FragCount = FragW3 + KT * 32;  // uint2 entries
+    static constexpr int BiasCount = 2 * H + 8;
+    static constexpr size_t SmemBytes = FragCount * sizeof(uint2) + BiasCount * sizeof(float);
+};
+
+__host__ __device__ constexpr int mlp_params(int hidden) {
+    return hidden == 64 ? Mlp<64>::Params : Mlp<32>::Params;
+}
+__host__ __device__ constexpr size_t mlp_smem_bytes(int hidden) {
+    return hidden == 64 ? Mlp<64>::SmemBytes : Mlp<32>::SmemBytes;
+}
+constexpr size_t kSurrogateSmemMax = Mlp<64>::SmemBytes;
 
 // Training box and normalisation of one trained network.
 struct SurrogateBox {
@@ -61,13 +77,14 @@ struct SurrogateBox {
     float out_offset[kMlpOut];
     float out_scale[kMlpOut];
     float mu_cut;
-    int fp16;  // element type of weights and activations: 0 BF16, 1 FP16
+    int fp16;    // element type of weights and activations: 0 BF16, 1 FP16
+    int hidden;  // hidden width H (32 or 64)
     int magnetic_dependency, momentum_dependency;
     // physics constants the targets were generated with
     double p0, particle_v0, kpara0, gamma_turb, qlt_omega0, qlt_lc, qlt_h0;
 };
 
-// What a push needs: the fragment/bias block (kSurrogateSmemBytes, copied to
+// What a push needs: the fragment/bias block (Mlp<H>::SmemBytes, copied to
 // shared memory by each block), the box, the run's constant features f3, f4
 // (normalised) and the judge counters
 // {evaluations, judged, fallbacks, max relative error (float bits)}.
@@ -131,8 +148,9 @@ __device__ __forceinline__ void mma_16816(float (&d)[4], const uint32_t (&a)[4],
 }
 
 // Copy the fragment/bias block into shared memory (whole block, then sync).
+template <int H>
 __device__ __forceinline__ void load_surrogate_block(const uint2* src, uint2* smem) {
-    constexpr int words = static_cast<int>(kSurrogateSmemBytes / sizeof(uint2));
+    constexpr int words = static_cast<int>(Mlp<H>::SmemBytes / sizeof(uint2));
     for (int k = threadIdx.x; k < words; k += blockDim.x) smem[k] = src[k];
     __syncthreads();
 }
@@ -140,14 +158,15 @@ __device__ __forceinline__ void load_surrogate_block(const uint2* src, uint2* sm
 // Warp-collective forward pass.  Every lane of the warp must call it with the
 // warp converged; lane r supplies row r (its five normalised features; zeros
 // for an idle lane) and receives the three normalised outputs of row r.
-template <bool FP16>
+template <bool FP16, int H>
 __device__ __forceinline__ void mlp_warp(const uint2* smem, const float (&f)[kMlpIn],
                                          float (&y)[kMlpOut]) {
+    using M = Mlp<H>;
     const unsigned full = 0xffffffffu;
     const int lane = static_cast<int>(threadIdx.x & 31u);
     const int g = lane >> 2;
     const int tig = lane & 3;
-    const float* bias = reinterpret_cast<const float*>(smem + kFragCount);
+    const float* bias = reinterpret_cast<const float*>(smem + M::FragCount);
     const uint32_t pk0 = pack_x2<FP16>(f[0], f[1]);
     const uint32_t pk1 = pack_x2<FP16>(f[2], f[3]);
     const uint32_t pk2 = pack_x2<FP16>(f[4], 0.0f);
@@ -171,12 +190,12 @@ __device__ __forceinline__ void mlp_warp(const uint2* smem, const float (&f)[kMl
         ax[mt][2] = 0u;
         ax[mt][3] = 0u;
     }
-    // layer 1: 8 column tiles -> A fragments of layer 2 (4 k tiles)
-    uint32_t a2[2][4][4];
+    // layer 1: NT column tiles -> A fragments of layer 2 (KT k tiles)
+    uint32_t a2[2][M::KT][4];
 #pragma unroll
-    for (int nt = 0; nt < 8; ++nt) {
+    for (int nt = 0; nt < M::NT; ++nt) {
         const float2 bv = *reinterpret_cast<const float2*>(bias + 8 * nt + 2 * tig);
-        const uint2 w = smem[kFragW1 + nt * 32 + lane];
+        const uint2 w = smem[M::FragW1 + nt * 32 + lane];
 #pragma unroll
         for (int mt = 0; mt < 2; ++mt) {
             float acc[4] = {bv.x, bv.y, bv.x, bv.y};
@@ -187,20 +206,19 @@ __device__ __forceinline__ void mlp_warp(const uint2* smem, const float (&f)[kMl
     }
     // layer 2, with layer 3 accumulated as each pair of column tiles
     // completes a k tile of its A fragment
-    const float2 b3 = *reinterpret_cast<const float2*>(bias + 2 * kMlpHidden + 2 * tig);
+    const float2 b3 = *reinterpret_cast<const float2*>(bias + 2 * H + 2 * tig);
     float out[2][4] = {{b3.x, b3.y, b3.x, b3.y}, {b3.x, b3.y, b3.x, b3.y}};
 #pragma unroll
-    for (int kt3 = 0; kt3 < 4; ++kt3) {
+    for (int kt3 = 0; kt3 < M::KT; ++kt3) {
         uint32_t a3[2][4];
 #pragma unroll
         for (int half = 0; half < 2; ++half) {
             const int nt = 2 * kt3 + half;
-            const float2 bv = *reinterpret_cast<const float2*>(bias + kMlpHidden + 8 * nt +
-                                                               2 * tig);
+            const float2 bv = *reinterpret_cast<const float2*>(bias + H + 8 * nt + 2 * tig);
             float acc[2][4] = {{bv.x, bv.y, bv.x, bv.y}, {bv.x, bv.y, bv.x, bv.y}};
 #pragma unroll
-            for (int kt = 0; kt < 4; ++kt) {
-                const uint2 w = smem[kFragW2 + (kt * 8 + nt) * 32 + lane];
+            for (int kt = 0; kt < M::KT; ++kt) {
+                const uint2 w = smem[M::FragW2 + (kt * M::NT + nt) * 32 + lane];
                 mma_16816<FP16>(acc[0], a2[0][kt], w);
                 mma_16816<FP16>(acc[1], a2[1][kt], w);
             }
@@ -210,7 +228,7 @@ __device__ __forceinline__ void mlp_warp(const uint2* smem, const float (&f)[kMl
                 a3[mt][half * 2 + 1] = act_x2<FP16>(acc[mt][2], acc[mt][3]);
             }
         }
-        const uint2 w3 = smem[kFragW3 + kt3 * 32 + lane];
+        const uint2 w3 = smem[M::FragW3 + kt3 * 32 + lane];
         mma_16816<FP16>(out[0], a3[0], w3);
         mma_16816<FP16>(out[1], a3[1], w3);
     }

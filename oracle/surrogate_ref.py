@@ -3,8 +3,9 @@
 TEST INFRASTRUCTURE ONLY: the checker for the GPU forward/backward kernels
 and the fused tensor-core inference; the product never imports it.
 
-Network: 5 -> 64 -> 64 -> 3, tanh hidden layers, linear output; parameter
-block W1[64][5] b1[64] W2[64][64] b2[64] W3[3][64] b3[3] (4739 values).
+Network: 5 -> H -> H -> 3 (H = 32 or 64), tanh hidden layers, linear output;
+parameter block W1[H][5] b1[H] W2[H][H] b2[H] W3[3][H] b3[3] (1379 values for
+H = 32, 4739 for H = 64; the width is read off the block's length).
 Loss: mean over samples and outputs of the squared error.  Everything here
 is float64 numpy, written from the definitions (backpropagation by the chain
 rule), and is itself checked against central finite differences.
@@ -20,20 +21,35 @@ from __future__ import annotations
 
 import numpy as np
 
-N_IN, N_HID, N_OUT = 5, 64, 3
-W1 = 0
-B1 = W1 + N_HID * N_IN
-W2 = B1 + N_HID
-B2 = W2 + N_HID * N_HID
-W3 = B2 + N_HID
-B3 = W3 + N_OUT * N_HID
-N_PARAMS = B3 + N_OUT
+N_IN, N_OUT = 5, 3
+
+
+def layout(hidden: int) -> dict:
+    """Offsets of W1 b1 W2 b2 W3 b3 and the block length for width `hidden`."""
+    w1 = 0
+    b1 = w1 + hidden * N_IN
+    w2 = b1 + hidden
+    b2 = w2 + hidden * hidden
+    w3 = b2 + hidden
+    b3 = w3 + N_OUT * hidden
+    return {"W1": w1, "B1": b1, "W2": w2, "B2": b2, "W3": w3, "B3": b3,
+            "N_PARAMS": b3 + N_OUT, "hidden": hidden}
+
+
+def hidden_of(count: int) -> int:
+    for hidden in (32, 64):
+        if layout(hidden)["N_PARAMS"] == count:
+            return hidden
+    raise ValueError(f"no network width has {count} parameters")
 
 
 def unpack(params: np.ndarray):
     p = np.asarray(params, dtype=np.float64)
-    return (p[W1:B1].reshape(N_HID, N_IN), p[B1:W2], p[W2:B2].reshape(N_HID, N_HID), p[B2:W3],
-            p[W3:B3].reshape(N_OUT, N_HID), p[B3:N_PARAMS])
+    h = hidden_of(p.size)
+    o = layout(h)
+    return (p[o["W1"]:o["B1"]].reshape(h, N_IN), p[o["B1"]:o["W2"]],
+            p[o["W2"]:o["B2"]].reshape(h, h), p[o["B2"]:o["W3"]],
+            p[o["W3"]:o["B3"]].reshape(N_OUT, h), p[o["B3"]:o["N_PARAMS"]])
 
 
 def forward(params: np.ndarray, x: np.ndarray) -> np.ndarray:

@@ -4,7 +4,8 @@
   (oracle/surrogate_ref.py, itself pinned to finite differences).
 * The FP32 forward against the CPU reference on the trained parameters, the
   BF16 and FP16 tensor-core forwards (the ones fused into the push) against
-  the plain closure, and the plain-closure fallback outside the box.
+  the plain closure, for hidden widths 32 (the default) and 64, and the
+  plain-closure fallback outside the box.
 * The mixed focused push served by the network against the FP64 oracle with
   the plain closure: momentum spectrum L1 <= 1 %, chi-square p > 0.01, and
   the in-kernel judge's record of the network's per-step error.
@@ -31,6 +32,17 @@ def _train(ctx, kpt, binding, element_type):
 @pytest.fixture(scope="module")
 def trained(ctx, kpt, binding):
     params, settings, surrogate = _train(ctx, kpt, binding, kpt.SURROGATE_BF16)
+    yield params, settings, surrogate
+    ctx.set_surrogate(None)
+    surrogate.close()
+
+
+@pytest.fixture(scope="module")
+def trained64(ctx, kpt, binding):
+    params = binding.default_params(kperp_over_kpara=0.05, focused=1, closure=2)
+    settings = kpt.settings_from_dict(params)
+    surrogate = ctx.train_surrogate(settings, element_type=kpt.SURROGATE_BF16, hidden_width=64,
+                                    **TRAIN)
     yield params, settings, surrogate
     ctx.set_surrogate(None)
     surrogate.close()
@@ -64,20 +76,22 @@ def _plain(params, inputs):
     return d, dd, np.log(k)
 
 
-def test_gradient_matches_cpu_reference(ctx):
+@pytest.mark.parametrize("hidden", [32, 64])
+def test_gradient_matches_cpu_reference(ctx, hidden):
     rng = np.random.default_rng(21)
-    params = rng.normal(0.0, 0.3, sr.N_PARAMS).astype(np.float32)
+    o = sr.layout(hidden)
+    params = rng.normal(0.0, 0.3, o["N_PARAMS"]).astype(np.float32)
     x = rng.uniform(-1.0, 1.0, (1024, 5)).astype(np.float32)
     t = rng.normal(0.0, 1.0, (1024, 3)).astype(np.float32)
-    loss, grad = ctx.surrogate_gradient(params, x, t)
+    loss, grad = ctx.surrogate_gradient(params, x, t, hidden)
     ref_loss, ref_grad = sr.loss_and_gradient(params.astype(np.float64), x.astype(np.float64),
                                               t.astype(np.float64))
     assert loss == pytest.approx(ref_loss, rel=1e-5)
     scale = np.abs(ref_grad).max()
     assert np.abs(grad - ref_grad).max() <= 1e-5 * scale
     # every block of the parameter vector, relative to its own scale
-    for lo, hi in ((sr.W1, sr.B1), (sr.B1, sr.W2), (sr.W2, sr.B2), (sr.B2, sr.W3),
-                   (sr.W3, sr.B3), (sr.B3, sr.N_PARAMS)):
+    for lo, hi in ((o["W1"], o["B1"]), (o["B1"], o["W2"]), (o["W2"], o["B2"]),
+                   (o["B2"], o["W3"]), (o["W3"], o["B3"]), (o["B3"], o["N_PARAMS"])):
         block = np.abs(ref_grad[lo:hi]).max()
         assert np.abs(grad[lo:hi] - ref_grad[lo:hi]).max() <= 1e-4 * block, (lo, hi)
 
@@ -88,8 +102,10 @@ def _errors(params, inputs, out):
             np.abs(out[:, 1] - dd) / np.maximum(np.abs(dd), d))
 
 
-def test_trained_network_forward_and_accuracy(trained, trained16):
-    params, _, surrogate = trained
+@pytest.mark.parametrize("width", [32, 64])
+def test_trained_network_forward_and_accuracy(trained, trained16, trained64, width):
+    params, _, surrogate = trained if width == 32 else trained64
+    assert surrogate.hidden_width == width
     assert surrogate.final_loss < 1e-3
     weights, norm = surrogate.parameters()
     rng = np.random.default_rng(5)
@@ -143,7 +159,7 @@ def test_fallback_outside_the_box_is_the_plain_closure(trained):
         assert np.allclose(out[:, 2], lk, rtol=0, atol=1e-12)
 
 
-@pytest.mark.parametrize("net", ["trained", "trained16"])
+@pytest.mark.parametrize("net", ["trained", "trained16", "trained64"])
 def test_surrogate_push_matches_fp64_spectrum(ctx, kpt, oracle, binding, fields_mod, net, request):
     params, settings, surrogate = request.getfixturevalue(net)
     ye = fields_mod.stretched_edges(128, -2.0, 2.0)

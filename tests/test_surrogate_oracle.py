@@ -11,28 +11,31 @@ import pytest
 import surrogate_ref as sr
 
 
-def _random_problem(seed=3, n=48):
+def _random_problem(seed=3, n=48, hidden=32):
     rng = np.random.default_rng(seed)
-    params = rng.normal(0.0, 0.3, sr.N_PARAMS)
+    params = rng.normal(0.0, 0.3, sr.layout(hidden)["N_PARAMS"])
     x = rng.uniform(-1.0, 1.0, (n, sr.N_IN))
     t = rng.normal(0.0, 1.0, (n, sr.N_OUT))
     return params, x, t
 
 
-def test_gradient_matches_finite_differences():
-    params, x, t = _random_problem()
+@pytest.mark.parametrize("hidden", [32, 64])
+def test_gradient_matches_finite_differences(hidden):
+    params, x, t = _random_problem(hidden=hidden)
     _, grad = sr.loss_and_gradient(params, x, t)
     rng = np.random.default_rng(7)
+    o = sr.layout(hidden)
     # every block: W1, b1, W2, b2, W3, b3
     idx = np.concatenate([rng.integers(lo, hi, 12) for lo, hi in
-                          ((sr.W1, sr.B1), (sr.B1, sr.W2), (sr.W2, sr.B2), (sr.B2, sr.W3),
-                           (sr.W3, sr.B3), (sr.B3, sr.N_PARAMS))])
+                          ((o["W1"], o["B1"]), (o["B1"], o["W2"]), (o["W2"], o["B2"]),
+                           (o["B2"], o["W3"]), (o["W3"], o["B3"]), (o["B3"], o["N_PARAMS"]))])
     fd = sr.finite_difference_gradient(params, x, t, idx)
     assert np.allclose(grad[idx], fd, rtol=1e-6, atol=1e-9)
 
 
-def test_forward_matches_loss_definition():
-    params, x, t = _random_problem(seed=5)
+@pytest.mark.parametrize("hidden", [32, 64])
+def test_forward_matches_loss_definition(hidden):
+    params, x, t = _random_problem(seed=5, hidden=hidden)
     loss, _ = sr.loss_and_gradient(params, x, t)
     assert loss == pytest.approx(np.mean((sr.forward(params, x) - t) ** 2), rel=1e-14)
 
