@@ -290,6 +290,92 @@ def run_focused(args, f0, f1):
     return out
 
 
+def run_c3(args, f0, f1):
+    """Configuration C3: 4 Mi particles (p = p0, mu uniform on [-1, 1]) on the
+    1024x2048 field, plain slab-QLT closure, the same start and noise in FP64
+    and in mixed precision.  Per-substep error: one substep of dt = 1e-4 in
+    both precisions (mhd_dt = dt, fixed dt), the mixed displacement against
+    the FP64 one.  Final spectra: 1000 substeps of the same dt (one interval
+    of mhd_dt = 0.1 with dt fixed at 1e-3 mhd_dt), momentum (64 log bins) and
+    pitch-cosine (16 bins) spectra of the two runs."""
+    import torch
+    kpt = importlib.import_module("kokkos-particletransport_gb300")
+    ctx = kpt.Context(DEVICE)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    n = args.c3_particles
+    long = focused_settings(kpt, kpt.CLOSURE_QLT)
+    long.dt_min_rel = long.dt_max_rel = 1e-3
+    one = focused_settings(kpt, kpt.CLOSURE_QLT)
+    one.mhd_dt = long.mhd_dt * 1e-3
+    one.dt_min_rel = one.dt_max_rel = 1.0
+    tables = {prec: (ctx.field(f0, kpt.TABLE_FOCUSED21, prec),
+                     ctx.field(f1, kpt.TABLE_FOCUSED21, prec))
+              for prec in (kpt.PRECISION_F64, kpt.PRECISION_MIXED)}
+    parts = ctx.particles(n)
+    ctx.inject(parts, tables[kpt.PRECISION_MIXED][0], long, n, START_FRAME, SEED)
+    start = parts.download(n)
+    start["status"][:] = 0
+    runs = {}
+    for prec, label in ((kpt.PRECISION_F64, "f64"), (kpt.PRECISION_MIXED, "mixed")):
+        lower, upper = tables[prec]
+        state = {k: v.copy() for k, v in start.items()}
+        state["t"][:] = START_FRAME * one.mhd_dt
+        parts.upload(state, n)
+        ctx.push_interval(parts, lower, upper, one, START_FRAME, SEED)
+        after_one = parts.download(n)
+        state = {k: v.copy() for k, v in start.items()}
+        state["t"][:] = START_FRAME * long.mhd_dt
+        parts.upload(state, n)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        stats = ctx.push_interval(parts, lower, upper, long, START_FRAME, SEED)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        runs[label] = {"one": after_one, "final": parts.download(n), "ms": ms,
+                       "particle_steps": int(stats.particle_steps)}
+    parts.close()
+    for lo, up in tables.values():
+        lo.close()
+        up.close()
+    ctx.close()
+    a64, a32 = runs["f64"]["one"], runs["mixed"]["one"]
+    ok = (a64["status"] == 0) & (a32["status"] == 0)
+    widths = {"x": 2.0, "y": 4.0}
+    step_error = {}
+    for key in ("x", "y", "p", "mu"):
+        d64 = a64[key][ok] - start[key][ok]
+        d32 = a32[key][ok] - start[key][ok]
+        if key in widths:  # periodic images
+            w = widths[key]
+            d64 = (d64 + 0.5 * w) % w - 0.5 * w
+            d32 = (d32 + 0.5 * w) % w - 0.5 * w
+        rel = np.abs(d32 - d64) / np.maximum(np.abs(d64), 1e-300)
+        step_error[key] = {"median": float(np.median(rel)), "p99": float(np.quantile(rel, 0.99))}
+    f64, f32 = runs["f64"]["final"], runs["mixed"]["final"]
+    h64 = _spectrum(f64["p"], f64["w"], f64["status"])
+    h32 = _spectrum(f32["p"], f32["w"], f32["status"])
+
+    def mu_spectrum(st):
+        sel = st["status"] == 0
+        return np.histogram(st["mu"][sel], bins=16, range=(-1.0, 1.0), weights=st["w"][sel])[0]
+
+    m64, m32 = mu_spectrum(f64), mu_spectrum(f32)
+    return {"particles": n, "substeps_per_particle": runs["f64"]["particle_steps"] / n,
+            "dt": long.mhd_dt * 1e-3,
+            "per_substep_relative_error": step_error,
+            "p_spectrum_l1": float(np.abs(h32 - h64).sum() / h64.sum()),
+            "mu_spectrum_l1": float(np.abs(m32 - m64).sum() / m64.sum()),
+            "mixed": {"value": runs["mixed"]["particle_steps"] / (runs["mixed"]["ms"] / 1e3),
+                      "ms": runs["mixed"]["ms"],
+                      "particle_steps": runs["mixed"]["particle_steps"]},
+            "f64": {"value": runs["f64"]["particle_steps"] / (runs["f64"]["ms"] / 1e3),
+                    "ms": runs["f64"]["ms"], "particle_steps": runs["f64"]["particle_steps"]}}
+
+
 def run_parker(args, f0, f1):
     """Parker transport on the same field: mixed and FP64."""
     import torch
@@ -612,6 +698,8 @@ def main():
     parser.add_argument("--library-particles", type=int, default=1 << 20,
                         help="particles of the library-solver leg (0 skips it)")
     parser.add_argument("--library-steps", type=int, default=10)
+    parser.add_argument("--c3-particles", type=int, default=1 << 22,
+                        help="particles of the C3 precision leg (0 skips it)")
     parser.add_argument("--hidden-width", type=int, default=32, choices=(32, 64),
                         help="hidden width of the headline network (a width-64 BF16 network "
                              "is measured beside a width-32 headline)")
@@ -654,6 +742,7 @@ def main():
     f0, f1 = make_workload()
     focused = run_focused(args, f0, f1)
     parker = run_parker(args, f0, f1) if args.parker_particles > 0 and WORLD == 1 else None
+    c3 = run_c3(args, f0, f1) if args.c3_particles > 0 and WORLD == 1 else None
     batched = run_batched(args) if args.batch_runs > 0 and WORLD == 1 else None
     library = run_library(args) if args.library_particles > 0 and WORLD == 1 else None
     peak, peak_kind = read_peaks()
@@ -715,6 +804,7 @@ def main():
                 "h2d_bytes_per_step": head["state_bytes"],
                 "d2h_bytes_per_step": head["state_bytes"]},
         "parker": parker,
+        "c3_precision": c3,
         "batched_runs": batched,
         "library_solvers": library,
         # per timed step: the push, plus 3 cell-sort kernels when sorting
