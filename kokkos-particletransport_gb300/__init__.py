@@ -999,6 +999,9 @@ class ParkerSolver(_Handle):
                                                           ctypes.byref(dt)))
         return float(dt.value)
 
+    # advance_sde is the reference's alias of advance_stochastic (ParkerSolver.hpp:296-301)
+    advance_sde = advance_stochastic
+
     def advance_deterministic(self, system: ParticleSystem) -> float:
         dt = ctypes.c_double()
         _check(self.ctx.lib.kpt_parker_advance_deterministic(self.ctx.handle, self.handle,
@@ -1086,6 +1089,9 @@ class FocusSolver(_Handle):
                                                          system.handle, int(seed), int(step),
                                                          ctypes.byref(dt)))
         return float(dt.value)
+
+    # advance_sde is the reference's alias of advance_stochastic (FocusSolver.hpp:298-303)
+    advance_sde = advance_stochastic
 
     def advance_deterministic(self, system: ParticleSystem) -> float:
         dt = ctypes.c_double()
