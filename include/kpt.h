@@ -496,6 +496,13 @@ int kpt_parker_advance_stochastic(kpt_context* ctx, kpt_parker_solver* solver,
 /* advance_deterministic (ParkerSolver.hpp:229-259). */
 int kpt_parker_advance_deterministic(kpt_context* ctx, kpt_parker_solver* solver,
                                      kpt_system* system, double* dt_used);
+/* Injected-noise step: advance_stochastic with the four standard normals of
+ * every particle slot supplied by the caller instead of drawn from the
+ * keyed stream: normals[k * count + i] is normal k of slot i (k = 0, 1, 2:
+ * the spatial Wiener increments, 3: the parallel one; ParkerSolver.hpp:
+ * 436-477), count = the system's particle count. */
+int kpt_parker_advance_with_noise(kpt_context* ctx, kpt_parker_solver* solver,
+                                  kpt_system* system, const double* normals, double* dt_used);
 /* steps consecutive advance_stochastic calls (steps first_step ..
  * first_step+steps-1) recorded once into a CUDA graph and replayed, the dt
  * staying on the device between steps; dts (optional, steps entries)
@@ -534,6 +541,11 @@ int kpt_focus_advance_stochastic(kpt_context* ctx, kpt_focus_solver* solver,
 /* advance_deterministic (FocusSolver.hpp:251-271). */
 int kpt_focus_advance_deterministic(kpt_context* ctx, kpt_focus_solver* solver,
                                     kpt_system* system, double* dt_used);
+/* Injected-noise step of the focused solver: normals[k * count + i], k = 0,
+ * 1, 2 the spatial increments (projected perpendicular to b), 3 the
+ * pitch-angle increment (FocusSolver.hpp:641-645, :1612). */
+int kpt_focus_advance_with_noise(kpt_context* ctx, kpt_focus_solver* solver, kpt_system* system,
+                                 const double* normals, double* dt_used);
 /* steps consecutive advance_stochastic calls replayed from one CUDA graph
  * (as kpt_parker_advance_stochastic_steps). */
 int kpt_focus_advance_stochastic_steps(kpt_context* ctx, kpt_focus_solver* solver,

@@ -276,6 +276,7 @@ def load_library() -> ctypes.CDLL:
         "kpt_parker_advance_stochastic": (i32, [vp, vp, vp, u64, u32, vp]),
         "kpt_parker_advance_deterministic": (i32, [vp, vp, vp, vp]),
         "kpt_parker_advance_stochastic_steps": (i32, [vp, vp, vp, u64, u32, u32, vp]),
+        "kpt_parker_advance_with_noise": (i32, [vp, vp, vp, vp, vp]),
         "kpt_batch_create": (i32, [vp, pvp]),
         "kpt_batch_destroy": (i32, [vp]),
         "kpt_batch_add_run": (i32, [vp, vp, vp, vp, vp, u64, u32, vp]),
@@ -295,6 +296,7 @@ def load_library() -> ctypes.CDLL:
         "kpt_focus_advance_stochastic": (i32, [vp, vp, vp, u64, u32, vp]),
         "kpt_focus_advance_deterministic": (i32, [vp, vp, vp, vp]),
         "kpt_focus_advance_stochastic_steps": (i32, [vp, vp, vp, u64, u32, u32, vp]),
+        "kpt_focus_advance_with_noise": (i32, [vp, vp, vp, vp, vp]),
         "kpt_default_diffusion_parameters": (None, [vp]),
         "kpt_parker_coefficients": (i32, [vp, vp, vp, vp, vp, vp, vp, vp]),
         "kpt_parker_solver_create_from_fields": (i32, [vp, vp, vp, vp, vp, vp, vp, dbl, pvp]),
@@ -1016,6 +1018,18 @@ class ParkerSolver(_Handle):
             _ptr(dts)))
         return dts[:steps]
 
+    def advance_with_noise(self, system: ParticleSystem, normals: np.ndarray) -> float:
+        """One stochastic step driven by caller-supplied standard normals,
+        normals[k][i] (k = 0..3) for particle slot i < system.count."""
+        normals = np.ascontiguousarray(normals, dtype=np.float64)
+        if normals.shape != (4, system.count):
+            raise KptError(f"normals must have shape (4, {system.count})")
+        dt = ctypes.c_double()
+        _check(self.ctx.lib.kpt_parker_advance_with_noise(self.ctx.handle, self.handle,
+                                                          system.handle, _ptr(normals),
+                                                          ctypes.byref(dt)))
+        return float(dt.value)
+
 
 class Batch(_Handle):
     """Many independent runs pushed by one launch per interval (kpt_batch)."""
@@ -1106,6 +1120,18 @@ class FocusSolver(_Handle):
             self.ctx.handle, self.handle, system.handle, int(seed), int(first_step), int(steps),
             _ptr(dts)))
         return dts[:steps]
+
+    def advance_with_noise(self, system: ParticleSystem, normals: np.ndarray) -> float:
+        """One stochastic step driven by caller-supplied standard normals,
+        normals[k][i] (k = 0..3) for particle slot i < system.count."""
+        normals = np.ascontiguousarray(normals, dtype=np.float64)
+        if normals.shape != (4, system.count):
+            raise KptError(f"normals must have shape (4, {system.count})")
+        dt = ctypes.c_double()
+        _check(self.ctx.lib.kpt_focus_advance_with_noise(self.ctx.handle, self.handle,
+                                                         system.handle, _ptr(normals),
+                                                         ctypes.byref(dt)))
+        return float(dt.value)
 
 
 class ParticleStorage:

@@ -2311,8 +2311,21 @@ int step_finish(kpt_context* ctx, void* scalars, double* dt_out, bool stochastic
     return KPT_OK;
 }
 
+// Caller normals [4][count] (host) copied to the device for one step.
+int upload_noise(kpt_context* ctx, const double* normals, uint64_t count, ScopedBuffer& buf,
+                 const double** device) {
+    *device = nullptr;
+    if (normals == nullptr || count == 0) return KPT_OK;
+    KPT_CUDA(buf.reserve(4 * count * sizeof(double)));
+    KPT_CUDA(cudaMemcpyAsync(buf.ptr, normals, 4 * count * sizeof(double),
+                             cudaMemcpyHostToDevice, ctx->stream));
+    *device = buf.as<double>();
+    return KPT_OK;
+}
+
 int parker_step(kpt_context* ctx, kpt_parker_solver* s, kpt_system* sys, int advance,
-                int stochastic, uint64_t seed, uint32_t step, double* dt_out) {
+                int stochastic, uint64_t seed, uint32_t step, double* dt_out,
+                const double* normals = nullptr) {
     KPT_REQUIRE(ctx && s && sys, "ParkerSolver: NULL handle");
     if (int rc = parker_validate(s, sys)) return rc;
     if (int rc = activate(ctx)) return rc;
@@ -2320,6 +2333,8 @@ int parker_step(kpt_context* ctx, kpt_parker_solver* s, kpt_system* sys, int adv
     if (int rc = parker_launch(ctx, s, sys, advance, stochastic, seed, step, nullptr, &L)) {
         return rc;
     }
+    ScopedBuffer noise;
+    if (int rc = upload_noise(ctx, normals, sys->count, noise, &L.noise)) return rc;
     KPT_CUDA(cudaMemsetAsync(s->scalars.ptr, 0, 32, ctx->stream));
     KPT_CUDA(kpt::lib_parker_step(L, ctx->stream));
     return step_finish(ctx, s->scalars.ptr, dt_out, stochastic != 0, false);
@@ -2340,6 +2355,12 @@ int kpt_parker_advance_stochastic(kpt_context* ctx, kpt_parker_solver* s, kpt_sy
 int kpt_parker_advance_deterministic(kpt_context* ctx, kpt_parker_solver* s, kpt_system* sys,
                                      double* dt_used) {
     return parker_step(ctx, s, sys, 1, 0, 0, 0, dt_used);
+}
+
+int kpt_parker_advance_with_noise(kpt_context* ctx, kpt_parker_solver* s, kpt_system* sys,
+                                  const double* normals, double* dt_used) {
+    KPT_REQUIRE(normals != nullptr, "kpt_parker_advance_with_noise: normals is NULL");
+    return parker_step(ctx, s, sys, 1, 1, 0, 0, dt_used, normals);
 }
 
 int kpt_parker_advance_stochastic_steps(kpt_context* ctx, kpt_parker_solver* s,
@@ -2461,22 +2482,21 @@ int focus_launch(kpt_focus_solver* s, kpt_system* sys, int advance, int stochast
 }
 
 int focus_step(kpt_context* ctx, kpt_focus_solver* s, kpt_system* sys, int advance,
-               int stochastic, uint64_t seed, uint32_t step, double* dt_out) {
+               int stochastic, uint64_t seed, uint32_t step, double* dt_out,
+               const double* normals = nullptr) {
     KPT_REQUIRE(ctx && s && sys, "FocusTransportSolver: NULL handle");
     if (int rc = focus_validate(s, sys)) return rc;
     if (int rc = activate(ctx)) return rc;
     kpt::LibFocusLaunch L;
     if (int rc = focus_launch(s, sys, advance, stochastic, seed, step, nullptr, &L)) return rc;
+    ScopedBuffer noise;
+    if (int rc = upload_noise(ctx, normals, sys->count, noise, &L.noise)) return rc;
     KPT_CUDA(cudaMemsetAsync(s->scalars.ptr, 0, 32, ctx->stream));
     KPT_CUDA(kpt::lib_focus_step(L, ctx->stream));
     return step_finish(ctx, s->scalars.ptr, dt_out, stochastic != 0, true);
 }
 
 }  // namespace
-
-extern "C" {
-
-}  // extern "C"
 
 // The solver without its basis: validated scattering parameters, the
 // device basis allocated.
@@ -2578,6 +2598,12 @@ int kpt_focus_advance_stochastic(kpt_context* ctx, kpt_focus_solver* s, kpt_syst
 int kpt_focus_advance_deterministic(kpt_context* ctx, kpt_focus_solver* s, kpt_system* sys,
                                     double* dt_used) {
     return focus_step(ctx, s, sys, 1, 0, 0, 0, dt_used);
+}
+
+int kpt_focus_advance_with_noise(kpt_context* ctx, kpt_focus_solver* s, kpt_system* sys,
+                                 const double* normals, double* dt_used) {
+    KPT_REQUIRE(normals != nullptr, "kpt_focus_advance_with_noise: normals is NULL");
+    return focus_step(ctx, s, sys, 1, 1, 0, 0, dt_used, normals);
 }
 
 int kpt_focus_advance_stochastic_steps(kpt_context* ctx, kpt_focus_solver* s, kpt_system* sys,

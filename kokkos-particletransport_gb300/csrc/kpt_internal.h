@@ -246,6 +246,7 @@ struct LibParkerLaunch {
     int capture;                    // rotate previous positions
     uint2 key;
     uint32_t frame;
+    const double* noise;            // caller normals [4][count] instead of the keyed stream
     int* error;                     // first abort condition met (code)
     unsigned long long* error_index;
 };
@@ -277,6 +278,7 @@ struct LibFocusLaunch {
     int apply_boundary, advance, stochastic, capture;
     uint2 key;
     uint32_t frame;
+    const double* noise;  // caller normals [4][count] instead of the keyed stream
     int* error;
     unsigned long long* error_index;
 };

@@ -378,8 +378,14 @@ __global__ void __launch_bounds__(256) lib_parker_advance_kernel(const LibParker
         double inc[2] = {0.0, 0.0};
         if (L.stochastic) {
             const uint32_t index = static_cast<uint32_t>(i);
-            const double2 n01 = lib_normal_pair(L.key, 0u, index, L.frame);
-            const double2 n23 = lib_normal_pair(L.key, 1u, index, L.frame);
+            double2 n01, n23;
+            if (L.noise != nullptr) {
+                n01 = make_double2(L.noise[i], L.noise[L.count + i]);
+                n23 = make_double2(L.noise[2 * L.count + i], L.noise[3 * L.count + i]);
+            } else {
+                n01 = lib_normal_pair(L.key, 0u, index, L.frame);
+                n23 = lib_normal_pair(L.key, 1u, index, L.frame);
+            }
             const double gv[3] = {n01.x, n01.y, n23.x};
             double iso = 0.0;
 #pragma unroll
@@ -738,8 +744,14 @@ __global__ void __launch_bounds__(256) focus_advance_kernel(const LibFocusLaunch
         double pitch_normal = 0.0;
         if (L.stochastic) {
             const uint32_t index = static_cast<uint32_t>(i);
-            const double2 n01 = lib_normal_pair(L.key, 0u, index, L.frame);
-            const double2 n23 = lib_normal_pair(L.key, 1u, index, L.frame);
+            double2 n01, n23;
+            if (L.noise != nullptr) {
+                n01 = make_double2(L.noise[i], L.noise[L.count + i]);
+                n23 = make_double2(L.noise[2 * L.count + i], L.noise[3 * L.count + i]);
+            } else {
+                n01 = lib_normal_pair(L.key, 0u, index, L.frame);
+                n23 = lib_normal_pair(L.key, 1u, index, L.frame);
+            }
             const double gv[3] = {n01.x, n01.y, n23.x};
             double parallel = 0.0;
 #pragma unroll

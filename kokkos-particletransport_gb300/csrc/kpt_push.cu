@@ -1074,11 +1074,15 @@ struct MinBlocks<StateMixed, true> {
 #ifndef KPT_SURROGATE_MIN_BLOCKS
 #define KPT_SURROGATE_MIN_BLOCKS 4
 #endif
+#ifndef KPT_SURROGATE32_MIN_BLOCKS
+#define KPT_SURROGATE32_MIN_BLOCKS 4
+#endif
 __host__ __device__ constexpr bool surr_fp16(int surr) { return surr == 2 || surr == 4; }
 __host__ __device__ constexpr int surr_hidden(int surr) { return surr <= 2 ? 64 : 32; }
 template <typename State, bool FOCUSED, int SURR = 0>
-__global__ void __launch_bounds__(128, SURR ? KPT_SURROGATE_MIN_BLOCKS
-                                            : MinBlocks<State, FOCUSED>::value)
+__global__ void __launch_bounds__(128, SURR >= 3 ? KPT_SURROGATE32_MIN_BLOCKS
+                                       : SURR ? KPT_SURROGATE_MIN_BLOCKS
+                                              : MinBlocks<State, FOCUSED>::value)
     push_refill_kernel(const PushParams P) {
     const unsigned full = 0xffffffffu;
     const unsigned lane = threadIdx.x & 31u;

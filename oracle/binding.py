@@ -270,10 +270,10 @@ class ReferenceHarness:
         lib.ref_main.argtypes = [i32, ctypes.POINTER(ctypes.c_char_p), i32]
         lib.ref_lib_parker.restype = ll
         lib.ref_lib_parker.argtypes = [i32, i32, vp, vp, vp, vp, i32, vp, ull, i32, i32, i32, ll,
-                                       ll, vp, vp, vp, vp]
+                                       ll, vp, vp, vp, vp, vp]
         lib.ref_lib_focus.restype = ll
         lib.ref_lib_focus.argtypes = [i32, i32, vp, vp, vp, vp, i32, vp, vp, ull, i32, i32, i32,
-                                      ll, ll, vp, vp, vp, vp]
+                                      ll, ll, vp, vp, vp, vp, vp]
         lib.ref_lib_system.restype = ll
         lib.ref_lib_system.argtypes = [i32, i32, vp, vp, vp, vp, i32, i32, i32, ll, ll, vp, vp,
                                        vp, vp]
@@ -384,9 +384,10 @@ class ReferenceHarness:
 
     def lib_parker(self, grid: dict, basis: np.ndarray, constant_ratio: bool, props: dict,
                    seed: int, first_step: int, steps: int, stochastic: bool, count: int,
-                   system: Dict[str, np.ndarray]) -> np.ndarray:
+                   system: Dict[str, np.ndarray], normals=None) -> np.ndarray:
         """ParkerSolver steps (include/ParkerSolver.hpp) on a uniform Cartesian grid;
-        updates `system` in place and returns the dt of each step."""
+        updates `system` in place and returns the dt of each step.  normals
+        ([steps][4][count], optional) replaces the keyed stream's normals."""
         xe = np.ascontiguousarray(grid["x_edges"], dtype=np.float64)
         ye = np.ascontiguousarray(grid["y_edges"], dtype=np.float64)
         periodic = np.ascontiguousarray(grid["periodic"], dtype=np.int32)
@@ -398,15 +399,17 @@ class ReferenceHarness:
         self._check(self.lib.ref_lib_parker(
             len(xe) - 1, len(ye) - 1, _ptr(xe), _ptr(ye), _ptr(periodic), _ptr(basis),
             int(constant_ratio), _ptr(pr), seed, first_step, steps, 0 if stochastic else 1,
-            count, ids.size, _ptr(ids), _ptr(d), _ptr(i), _ptr(dts)))
+            count, ids.size, _ptr(ids), _ptr(d), _ptr(i), _ptr(dts),
+            None if normals is None else _ptr(np.ascontiguousarray(normals, dtype=np.float64))))
         self._lib_unblock(system, ids, d, i)
         return dts[:steps]
 
     def lib_focus(self, grid: dict, basis: np.ndarray, constant_ratio: bool, props: dict,
                   scattering: dict, seed: int, first_step: int, steps: int, stochastic: bool,
-                  count: int, system: Dict[str, np.ndarray]) -> np.ndarray:
+                  count: int, system: Dict[str, np.ndarray], normals=None) -> np.ndarray:
         """FocusTransportSolver steps (include/FocusSolver.hpp) on a uniform Cartesian
-        grid; updates `system` in place and returns the dt of each step."""
+        grid; updates `system` in place and returns the dt of each step.  normals
+        ([steps][4][count], optional) replaces the keyed stream's normals."""
         xe = np.ascontiguousarray(grid["x_edges"], dtype=np.float64)
         ye = np.ascontiguousarray(grid["y_edges"], dtype=np.float64)
         periodic = np.ascontiguousarray(grid["periodic"], dtype=np.int32)
@@ -422,7 +425,8 @@ class ReferenceHarness:
         self._check(self.lib.ref_lib_focus(
             len(xe) - 1, len(ye) - 1, _ptr(xe), _ptr(ye), _ptr(periodic), _ptr(basis),
             int(constant_ratio), _ptr(pr), _ptr(sc), seed, first_step, steps,
-            0 if stochastic else 1, count, ids.size, _ptr(ids), _ptr(d), _ptr(i), _ptr(dts)))
+            0 if stochastic else 1, count, ids.size, _ptr(ids), _ptr(d), _ptr(i), _ptr(dts),
+            None if normals is None else _ptr(np.ascontiguousarray(normals, dtype=np.float64))))
         self._lib_unblock(system, ids, d, i)
         return dts[:steps]
 

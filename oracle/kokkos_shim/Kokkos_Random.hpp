@@ -52,6 +52,17 @@ inline std::uint32_t label_tag(const char* label) {
     }
     return KPT_ORACLE_TAG_OTHER;
 }
+// Injected noise: when set, normal() returns external[k * count + index],
+// k the number of normals the state has drawn (the library solvers'
+// advance-with-noise parity mode).
+inline const double*& external_normals() {
+    static const double* normals = nullptr;
+    return normals;
+}
+inline std::uint64_t& external_count() {
+    static std::uint64_t count = 0;
+    return count;
+}
 }  // namespace ShimImpl
 
 template <class DeviceType>
@@ -60,6 +71,7 @@ public:
     kpt_oracle_stream stream{};
     bool has_spare = false;
     double spare = 0.0;
+    int normals_drawn = 0;
 
     double drand() { return kpt_oracle_stream_u01(&stream); }
     double drand(const double range) { return range * drand(); }
@@ -72,6 +84,10 @@ public:
     // the header library's solvers draw normals; the driver path draws
     // uniforms alone.
     double normal() {
+        if (const double* ext = ShimImpl::external_normals()) {
+            const std::uint64_t k = static_cast<std::uint64_t>(normals_drawn++);
+            return ext[k * ShimImpl::external_count() + stream.index];
+        }
         if (has_spare) {
             has_spare = false;
             return spare;

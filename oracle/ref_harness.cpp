@@ -533,12 +533,14 @@ long long ref_qlt(long long n, const double* mu, const double* omega, const doub
 // fields handed to the solver are cut from it, so the solver rebuilds the
 // same packed basis.  props = rest mass, charge, c, energy scale, courant.
 // mode: 0 stochastic, 1 deterministic.  dts[steps] receives each step's dt;
-// the noise frame of step s is first_step + s.
+// the noise frame of step s is first_step + s.  normals (NULL: the keyed
+// stream) holds [steps][4][count] injected normals.
 long long ref_lib_parker(int nx, int ny, const double* x_edges, const double* y_edges,
                          const int* periodic, const double* basis, int constant_ratio,
                          const double* props, unsigned long long seed, int first_step,
                          int steps, int mode, long long count, long long capacity,
-                         unsigned long long* ids, double* d, int* ints, double* dts) {
+                         unsigned long long* ids, double* d, int* ints, double* dts,
+                         const double* normals) {
     try {
         using solver_type = ParkerSolver<LibAnalyticGrid>;
         using vector_field = typename solver_type::vector_field_type;
@@ -590,9 +592,13 @@ long long ref_lib_parker(int nx, int ny, const double* x_edges, const double* y_
         Kokkos::ShimImpl::auto_frame_enabled() = 0;
         for (int s = 0; s < steps; ++s) {
             Kokkos::ShimImpl::current_frame() = static_cast<std::uint32_t>(first_step + s);
+            Kokkos::ShimImpl::external_normals() =
+                normals != nullptr ? normals + static_cast<std::size_t>(s) * 4 * count : nullptr;
+            Kokkos::ShimImpl::external_count() = static_cast<std::uint64_t>(count);
             dts[s] = mode == 0 ? solver.advance_stochastic(random_manager)
                                : solver.advance_deterministic();
         }
+        Kokkos::ShimImpl::external_normals() = nullptr;
         lib_store(solver.particles, h);
         return 0;
     } catch (const std::exception& error) {
@@ -613,7 +619,8 @@ long long ref_lib_focus(int nx, int ny, const double* x_edges, const double* y_e
                         const int* periodic, const double* basis, int constant_ratio,
                         const double* props, const double* scat, unsigned long long seed,
                         int first_step, int steps, int mode, long long count, long long capacity,
-                        unsigned long long* ids, double* d, int* ints, double* dts) {
+                        unsigned long long* ids, double* d, int* ints, double* dts,
+                        const double* normals) {
     try {
         using solver_type = FocusSolver<LibAnalyticGrid>;
         using vector_field = typename solver_type::vector_field_type;
@@ -677,9 +684,13 @@ long long ref_lib_focus(int nx, int ny, const double* x_edges, const double* y_e
         Kokkos::ShimImpl::auto_frame_enabled() = 0;
         for (int s = 0; s < steps; ++s) {
             Kokkos::ShimImpl::current_frame() = static_cast<std::uint32_t>(first_step + s);
+            Kokkos::ShimImpl::external_normals() =
+                normals != nullptr ? normals + static_cast<std::size_t>(s) * 4 * count : nullptr;
+            Kokkos::ShimImpl::external_count() = static_cast<std::uint64_t>(count);
             dts[s] = mode == 0 ? solver.advance_stochastic(random_manager)
                                : solver.advance_deterministic();
         }
+        Kokkos::ShimImpl::external_normals() = nullptr;
         lib_store(solver.particles, h);
         return 0;
     } catch (const std::exception& error) {

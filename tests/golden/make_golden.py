@@ -365,6 +365,33 @@ def make_lib(ref, out_dir):
                  max_mu=max_mu,
                  **{f"start_{k}": v for k, v in start.items()},
                  **{f"end_{k}": v for k, v in system.items()})
+    # injected noise: caller normals [steps][4][count] replace the random pool's
+    # draws on both sides; a tenth of them widened fourfold to reach the
+    # pitch-angle clamp and the open boundaries
+    nrng = np.random.default_rng(31415)
+    for kind, periodic, steps in (("parker", (1, 0), 3), ("focus", (1, 0), 3)):
+        grid = dict(x_edges=xe, y_edges=ye, periodic=np.array(periodic, dtype=np.int32))
+        count, capacity = 500, 512
+        start = lib_population(nrng, count, capacity, xe, ye, True)
+        system = {k: v.copy() for k, v in start.items()}
+        normals = nrng.standard_normal((steps, 4, count))
+        normals[nrng.random(normals.shape) < 0.1] *= 4.0
+        if kind == "parker":
+            basis = lib_basis(nx, ny, xe, ye, True)
+            dts = ref.lib_parker(grid, basis, False, props, SEED, 0, steps, True, count, system,
+                                 normals)
+            extra = dict(constant_ratio=0)
+        else:
+            basis = lib_focus_basis(nx, ny, xe, ye)
+            dts = ref.lib_focus(grid, basis, False, props, dict(scattering, max_mu=0.97), SEED,
+                                0, steps, True, count, system, normals)
+            extra = dict(constant_ratio=0, spectral_index=scattering["spectral_index"],
+                         h0=scattering["h0"], max_mu=0.97)
+        lib_save(out_dir, f"lib_noise_{kind}.npz", x_edges=xe, y_edges=ye,
+                 periodic=grid["periodic"], basis=basis, steps=steps, count=count,
+                 courant=props["courant"], dts=dts, normals=normals, **extra,
+                 **{f"start_{k}": v for k, v in start.items()},
+                 **{f"end_{k}": v for k, v in system.items()})
     # ParticleSystem lifecycle
     grid = dict(x_edges=xe, y_edges=ye, periodic=np.array((1, 0), dtype=np.int32))
     props_sys = dict(props, split_ratio=2.0, min_child_weight=0.2)

@@ -13,6 +13,9 @@ pool (tests/golden/make_golden.py).
 * FocusTransportSolver: the same bars, pitch cosines included (reflection at
   a maximum |mu| below 1, the three Picard iterations with the slab-QLT
   closure).
+* Injected noise: both solvers stepped with caller normals (a tenth of
+  them widened fourfold) against the reference templates fed the same
+  normals through their random pool: the same bars.
 * ParticleSystem: boundary conditions, sort_by_key, compact, energy split and
   capture_previous_positions bit for bit.
 """
@@ -219,3 +222,33 @@ def test_particle_system_lifecycle_matches_reference(ctx, op):
             [int(v) for v in data["split_stats"]]
     system.close()
     grid.close()
+
+
+@pytest.mark.parametrize("kind", ["parker", "focus"])
+def test_injected_noise_steps_match_reference(ctx, kpt, kind):
+    data = load_golden(f"lib_noise_{kind}.npz")
+    if kind == "parker":
+        grid, system, solver = _setup(ctx, data)
+    else:
+        grid, system, solver = _focus_setup(ctx, data)
+    normals = data["normals"]
+    with pytest.raises(kpt.KptError, match="normals must have shape"):
+        solver.advance_with_noise(system, normals[0][:3])
+    dts = [solver.advance_with_noise(system, normals[k]) for k in range(int(data["steps"]))]
+    np.testing.assert_allclose(dts, data["dts"], rtol=1e-10, atol=0)
+    got = system.download()
+    want = _state(data, "end")
+    for key in ("status", "level", "key", "id", "w", "e0"):
+        assert np.array_equal(got[key], want[key]), key
+    width_x = data["x_edges"][-1] - data["x_edges"][0]
+    width_y = data["y_edges"][-1] - data["y_edges"][0]
+    for key, width in (("x", width_x), ("prev_x", width_x), ("prevstep_x", width_x),
+                       ("y", width_y), ("prev_y", width_y), ("prevstep_y", width_y)):
+        diff = np.abs(got[key] - want[key])
+        diff = np.minimum(diff, np.abs(width - diff)) / width
+        assert diff.max() <= 1e-10, (key, diff.max())
+    for key in ("p", "mu"):
+        scale = np.maximum(np.abs(want[key]), 1e-12)
+        assert (np.abs(got[key] - want[key]) / scale).max() <= 1e-10, key
+    for h in (solver, system, grid):
+        h.close()
