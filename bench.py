@@ -3,17 +3,20 @@
 Workload: a 1024 x 2048 compact field on stretched y edges (dy proportional
 to 1 + 4 (y/2)^2 over [-2, 2], x uniform on [-1, 1]), Harris sheet plus 8
 magnetic islands (psi = 0.1 cos(4 pi x) exp(-y^2/0.04)), two frames with
-seeded 1 % multiplicative noise; a particle population injected uniformly
-over the domain (p = p0, pitch cosine uniform on [-1, 1], times spread over
-the first interval) and pushed across consecutive MHD intervals.  One step =
-one cell sort + one ``kpt_push_interval`` over the whole population.
+seeded 1 % multiplicative noise; 4 Mi particles injected uniformly over the
+domain (p = p0, pitch cosine uniform on [-1, 1]) and pushed across
+consecutive MHD intervals of 1000 fixed steps each.  One step = one cell
+sort + one ``kpt_push_interval`` over the whole population.
 
 Headline: focused transport with the learned slab-QLT closure (sigma^2 =
-0.1, gamma_k = 5/3), mixed precision, network trained on the GPU before the
-timed region; beside it the plain FP64 push with the plain closure (the
-baseline the metric names), the mixed push with the plain closure (what the
-network gains or costs), the spectrum L1 of the headline against FP64 after
-one interval from the same start, and the Parker legs (mixed and FP64).
+0.1, gamma_k = 5/3; a 5-64-64-3 network with BF16 weights and FP32
+accumulation, trained on the GPU on 2 M closure samples before the timed
+region), mixed precision; beside it the plain FP64 push with the plain
+closure (the baseline the metric names), the mixed push with the plain
+closure (what the network gains or costs), momentum and pitch-cosine
+spectrum L1 of every leg against FP64 after one interval from the same
+start, the per-step error of the mixed push, and the Parker legs (mixed and
+FP64).
 
 Timing: CUDA events on the library's stream around exactly K steps after W
 warm-up steps; the tables (2 x 200 MB mixed focused) exceed the 129 MB L2,
@@ -198,22 +201,52 @@ def focused_settings(kpt, closure):
                                 closure=closure, qlt_sigma2=0.1, qlt_spectral_index=5.0 / 3.0)
 
 
+def fixed_step_settings(kpt, closure, substeps):
+    """Focused settings with the step fixed at (1 + 1e-6) mhd_dt / substeps:
+    every particle takes exactly `substeps` steps per interval, the last one
+    cut to land on the interval end (at exactly mhd_dt / substeps the
+    rounding of the accumulated time can leave one more, tiny step)."""
+    s = focused_settings(kpt, closure)
+    s.dt_min_rel = s.dt_max_rel = (1.0 + 1e-6) / substeps
+    return s
+
+
+def _mu_spectrum(st):
+    sel = st["status"] == 0
+    return np.histogram(st["mu"][sel], bins=16, range=(-1.0, 1.0), weights=st["w"][sel])[0]
+
+
 def run_focused(args, f0, f1):
-    """Headline: mixed + surrogate; beside it FP64 plain and mixed plain."""
+    """Headline and its comparison legs, all from one start: 4 Mi particles
+    (p = p0, pitch cosine uniform on [-1, 1]) on the 1024x2048 field, every
+    interval `substeps` fixed steps (dt = mhd_dt / substeps).
+
+    * surrogate: mixed precision, learned closure (5-64-64-3 BF16 network,
+      FP32 accumulation), the headline;
+    * f64: the plain FP64 push with the plain closure (the metric's baseline),
+      one interval from the start;
+    * mixed_qlt: the mixed push with the plain closure (what the network
+      gains or costs; with f64 the precision report: per-step error of one
+      step, momentum and pitch-cosine spectra after one interval);
+    * surrogate_fp16 / surrogate_h32: the same network served in FP16, and
+      a width-32 BF16 network.
+    Each mixed leg pushes one interval from the start (its spectra), then
+    W - 1 more warm-up intervals and K timed consecutive intervals."""
     import torch
     kpt = importlib.import_module("kokkos-particletransport_gb300")
     ctx = kpt.Context(DEVICE)
     stream = torch.cuda.current_stream()
     ctx.set_stream(stream.cuda_stream)
     n = args.particles
-    plain = focused_settings(kpt, kpt.CLOSURE_QLT)
-    learned = focused_settings(kpt, kpt.CLOSURE_SURROGATE)
+    plain = fixed_step_settings(kpt, kpt.CLOSURE_QLT, args.substeps)
+    learned = fixed_step_settings(kpt, kpt.CLOSURE_SURROGATE, args.substeps)
+    other = 96 - args.hidden_width
     nets, out = {}, {"train": {}}
     nets_to_train = (("surrogate", kpt.SURROGATE_BF16, args.hidden_width),
                      ("surrogate_fp16", kpt.SURROGATE_FP16, args.hidden_width),
-                     ("surrogate_h64", kpt.SURROGATE_BF16, 64))
-    if args.hidden_width == 64 or WORLD > 1:
-        nets_to_train = nets_to_train[:2]
+                     (f"surrogate_h{other}", kpt.SURROGATE_BF16, other))
+    if WORLD > 1:
+        nets_to_train = nets_to_train[:1]
     for label, element, width in nets_to_train:
         t0 = time.perf_counter()
         nets[label] = ctx.train_surrogate(learned, samples=args.train_samples,
@@ -222,38 +255,45 @@ def run_focused(args, f0, f1):
         out["train"][label] = {"seconds": time.perf_counter() - t0,
                                "final_loss": nets[label].final_loss,
                                "samples": args.train_samples, "adam_steps": args.train_steps}
-    spectra = {}
-    legs = (("surrogate", kpt.PRECISION_MIXED, learned, args.steps, args.warmup),
-            ("f64", kpt.PRECISION_F64, plain, args.f64_steps, 1),
-            ("surrogate_fp16", kpt.PRECISION_MIXED, learned, args.steps, args.warmup),
-            ("mixed_qlt", kpt.PRECISION_MIXED, plain, args.steps, args.warmup))
-    if "surrogate_h64" in nets:
-        legs = legs + (("surrogate_h64", kpt.PRECISION_MIXED, learned, args.steps,
-                        args.warmup),)
-    if WORLD > 1:
-        # replicas: every rank runs the headline leg and the FP64 baseline leg
-        legs = legs[:2]
-    start = None
-    for label, precision, settings, steps, warmup in legs:
-        if label in nets:
-            ctx.set_surrogate(nets[label])
-        lower = ctx.field(f0, kpt.TABLE_FOCUSED21, precision)
-        upper = ctx.field(f1, kpt.TABLE_FOCUSED21, precision)
-        parts = ctx.particles(n)
-        if start is None:
-            ctx.inject(parts, lower, settings, n, START_FRAME, SEED)
-            start = parts.download()
-        else:
-            parts.upload(start, n)
-        # spectrum after one interval from the common start
+    tables = {prec: (ctx.field(f0, kpt.TABLE_FOCUSED21, prec),
+                     ctx.field(f1, kpt.TABLE_FOCUSED21, prec))
+              for prec in (kpt.PRECISION_MIXED, kpt.PRECISION_F64)}
+    parts = ctx.particles(n)
+    ctx.inject(parts, tables[kpt.PRECISION_MIXED][0], plain, n, START_FRAME, SEED)
+    start = parts.download(n)
+    start["status"][:] = 0
+    start["t"][:] = START_FRAME * plain.mhd_dt
+    legs = [("surrogate", kpt.PRECISION_MIXED, learned, args.steps),
+            ("f64", kpt.PRECISION_F64, plain, 0)]
+    if WORLD == 1:
+        legs += [("mixed_qlt", kpt.PRECISION_MIXED, plain, args.steps),
+                 ("surrogate_fp16", kpt.PRECISION_MIXED, learned, args.steps),
+                 (f"surrogate_h{other}", kpt.PRECISION_MIXED, learned, args.steps)]
+    finals = {}
+    for label, precision, settings, steps in legs:
+        ctx.set_surrogate(nets.get(label))
+        lower, upper = tables[precision]
+        parts.upload(start, n)
+        ctx.surrogate_judge()
+        # one interval from the common start: the spectra (and the FP64 timing)
         if args.sort_tile > 0:
             ctx.sort(parts, lower, args.sort_tile, args.sort_tile)
-        ctx.push_interval(parts, lower, upper, settings, START_FRAME, SEED)
-        one = parts.download(n)
-        spectra[label] = _spectrum(one["p"], one["w"], one["status"])
-        ctx.surrogate_judge()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        stats = ctx.push_interval(parts, lower, upper, settings, START_FRAME, SEED)
+        e1.record(stream)
+        e1.synchronize()
+        finals[label] = parts.download(n)
+        if steps == 0:
+            ms = e0.elapsed_time(e1)
+            out[label] = {"value": stats.particle_steps / (ms / 1e3), "ms_per_step": ms,
+                          "kernel_ms": ms, "particle_steps": int(stats.particle_steps),
+                          "steps": 1}
+            continue
         total_ms, kernel_ms, psteps, clocks = _timed_intervals(
-            ctx, stream, parts, lower, upper, settings, steps, max(0, warmup - 1),
+            ctx, stream, parts, lower, upper, settings, steps, max(0, args.warmup - 1),
             args.sort_tile, START_FRAME + 1)
         leg = {"value": psteps / (total_ms / 1e3), "ms_per_step": total_ms / steps,
                "kernel_ms": float(np.mean(kernel_ms)), "particle_steps": int(psteps),
@@ -276,73 +316,47 @@ def run_focused(args, f0, f1):
             leg["e2e"] = e2e_steps / (time.perf_counter() - t0)
             leg["state_bytes"] = n * (7 * 8 + 2 * 4)
         out[label] = leg
-        for obj in (lower, upper, parts):
-            obj.close()
-    ref = spectra["f64"]
-    for label in ("surrogate", "surrogate_fp16", "surrogate_h64", "mixed_qlt"):
-        if label in out:
-            out[label]["spectrum_l1_vs_f64"] = float(np.abs(spectra[label] - ref).sum() /
-                                                     ref.sum())
+    ref = finals["f64"]
+    hp, hm = _spectrum(ref["p"], ref["w"], ref["status"]), _mu_spectrum(ref)
+    for label in finals:
+        if label != "f64":
+            fin = finals[label]
+            out[label]["spectrum_l1_vs_f64"] = float(
+                np.abs(_spectrum(fin["p"], fin["w"], fin["status"]) - hp).sum() / hp.sum())
+            out[label]["mu_spectrum_l1_vs_f64"] = float(
+                np.abs(_mu_spectrum(fin) - hm).sum() / hm.sum())
+    if WORLD == 1:
+        out["c3"] = precision_report(kpt, ctx, parts, tables, start, n, plain)
+        out["c3"].update(
+            p_spectrum_l1=out["mixed_qlt"]["spectrum_l1_vs_f64"],
+            mu_spectrum_l1=out["mixed_qlt"]["mu_spectrum_l1_vs_f64"],
+            substeps_per_particle=out["f64"]["particle_steps"] / n)
     ctx.set_surrogate(None)
     for net in nets.values():
         net.close()
-    ctx.close()
-    return out
-
-
-def run_c3(args, f0, f1):
-    """Configuration C3: 4 Mi particles (p = p0, mu uniform on [-1, 1]) on the
-    1024x2048 field, plain slab-QLT closure, the same start and noise in FP64
-    and in mixed precision.  Per-substep error: one substep of dt = 1e-4 in
-    both precisions (mhd_dt = dt, fixed dt), the mixed displacement against
-    the FP64 one.  Final spectra: 1000 substeps of the same dt (one interval
-    of mhd_dt = 0.1 with dt fixed at 1e-3 mhd_dt), momentum (64 log bins) and
-    pitch-cosine (16 bins) spectra of the two runs."""
-    import torch
-    kpt = importlib.import_module("kokkos-particletransport_gb300")
-    ctx = kpt.Context(DEVICE)
-    stream = torch.cuda.current_stream()
-    ctx.set_stream(stream.cuda_stream)
-    n = args.c3_particles
-    long = focused_settings(kpt, kpt.CLOSURE_QLT)
-    long.dt_min_rel = long.dt_max_rel = 1e-3
-    one = focused_settings(kpt, kpt.CLOSURE_QLT)
-    one.mhd_dt = long.mhd_dt * 1e-3
-    one.dt_min_rel = one.dt_max_rel = 1.0
-    tables = {prec: (ctx.field(f0, kpt.TABLE_FOCUSED21, prec),
-                     ctx.field(f1, kpt.TABLE_FOCUSED21, prec))
-              for prec in (kpt.PRECISION_F64, kpt.PRECISION_MIXED)}
-    parts = ctx.particles(n)
-    ctx.inject(parts, tables[kpt.PRECISION_MIXED][0], long, n, START_FRAME, SEED)
-    start = parts.download(n)
-    start["status"][:] = 0
-    runs = {}
-    for prec, label in ((kpt.PRECISION_F64, "f64"), (kpt.PRECISION_MIXED, "mixed")):
-        lower, upper = tables[prec]
-        state = {k: v.copy() for k, v in start.items()}
-        state["t"][:] = START_FRAME * one.mhd_dt
-        parts.upload(state, n)
-        ctx.push_interval(parts, lower, upper, one, START_FRAME, SEED)
-        after_one = parts.download(n)
-        state = {k: v.copy() for k, v in start.items()}
-        state["t"][:] = START_FRAME * long.mhd_dt
-        parts.upload(state, n)
-        torch.cuda.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        stats = ctx.push_interval(parts, lower, upper, long, START_FRAME, SEED)
-        e1.record(stream)
-        e1.synchronize()
-        ms = e0.elapsed_time(e1)
-        runs[label] = {"one": after_one, "final": parts.download(n), "ms": ms,
-                       "particle_steps": int(stats.particle_steps)}
     parts.close()
     for lo, up in tables.values():
         lo.close()
         up.close()
     ctx.close()
-    a64, a32 = runs["f64"]["one"], runs["mixed"]["one"]
+    return out
+
+
+def precision_report(kpt, ctx, parts, tables, start, n, plain):
+    """Per-step error of the mixed push: one step of dt = mhd_dt / substeps
+    from the common start in both precisions (plain closure), the relative
+    error of the mixed displacement against the FP64 one (median and p99)."""
+    one = fixed_step_settings(kpt, kpt.CLOSURE_QLT, 1)
+    one.mhd_dt = plain.mhd_dt / round(1.0 / plain.dt_min_rel)
+    after = {}
+    for prec in (kpt.PRECISION_F64, kpt.PRECISION_MIXED):
+        lower, upper = tables[prec]
+        state = {k: v.copy() for k, v in start.items()}
+        state["t"][:] = START_FRAME * one.mhd_dt
+        parts.upload(state, n)
+        ctx.push_interval(parts, lower, upper, one, START_FRAME, SEED)
+        after[prec] = parts.download(n)
+    a64, a32 = after[kpt.PRECISION_F64], after[kpt.PRECISION_MIXED]
     ok = (a64["status"] == 0) & (a32["status"] == 0)
     widths = {"x": 2.0, "y": 4.0}
     step_error = {}
@@ -355,25 +369,7 @@ def run_c3(args, f0, f1):
             d32 = (d32 + 0.5 * w) % w - 0.5 * w
         rel = np.abs(d32 - d64) / np.maximum(np.abs(d64), 1e-300)
         step_error[key] = {"median": float(np.median(rel)), "p99": float(np.quantile(rel, 0.99))}
-    f64, f32 = runs["f64"]["final"], runs["mixed"]["final"]
-    h64 = _spectrum(f64["p"], f64["w"], f64["status"])
-    h32 = _spectrum(f32["p"], f32["w"], f32["status"])
-
-    def mu_spectrum(st):
-        sel = st["status"] == 0
-        return np.histogram(st["mu"][sel], bins=16, range=(-1.0, 1.0), weights=st["w"][sel])[0]
-
-    m64, m32 = mu_spectrum(f64), mu_spectrum(f32)
-    return {"particles": n, "substeps_per_particle": runs["f64"]["particle_steps"] / n,
-            "dt": long.mhd_dt * 1e-3,
-            "per_substep_relative_error": step_error,
-            "p_spectrum_l1": float(np.abs(h32 - h64).sum() / h64.sum()),
-            "mu_spectrum_l1": float(np.abs(m32 - m64).sum() / m64.sum()),
-            "mixed": {"value": runs["mixed"]["particle_steps"] / (runs["mixed"]["ms"] / 1e3),
-                      "ms": runs["mixed"]["ms"],
-                      "particle_steps": runs["mixed"]["particle_steps"]},
-            "f64": {"value": runs["f64"]["particle_steps"] / (runs["f64"]["ms"] / 1e3),
-                    "ms": runs["f64"]["ms"], "particle_steps": runs["f64"]["particle_steps"]}}
+    return {"particles": n, "dt": one.mhd_dt, "per_substep_relative_error": step_error}
 
 
 def run_parker(args, f0, f1):
@@ -638,21 +634,26 @@ def run_generator(kpt, ctx, grid, xe, ye, n, stream):
     return out
 
 
-def cpu_baseline(particles: int, steps: int = 1):
+def cpu_baseline(particles: int, substeps: int, steps: int = 1):
     """Oracle restatement of the focused push with the plain slab-QLT closure
-    (OpenMP, all host threads) on a bounded sample of the headline workload."""
+    (OpenMP, all host threads) on a bounded sample of the headline workload:
+    `particles` of its particles, `substeps` fixed steps per interval."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     binding = importlib.import_module("binding")
     f0, f1 = make_workload()
     oracle = binding.Oracle()
     params = binding.default_params(kperp_over_kpara=0.05, split_ratio=1.2, focused=1,
                                     closure=1, qlt_sigma2=0.1,
-                                    qlt_spectral_index=5.0 / 3.0)
+                                    qlt_spectral_index=5.0 / 3.0,
+                                    dt_min_rel=(1.0 + 1e-6) / substeps,
+                                    dt_max_rel=(1.0 + 1e-6) / substeps)
     grid = oracle.grid(f0.x_edges, f0.y_edges)
     lo, up = oracle.table(f0, True), oracle.table(f1, True)
     parts = binding.empty_particles(particles)
-    oracle.inject(grid, params, START_FRAME * 0.1, START_FRAME, SEED, particles, 0, particles,
-                  parts)
+    oracle.inject(grid, params, START_FRAME * params["mhd_dt"], START_FRAME, SEED, particles, 0,
+                  particles, parts)
+    parts["status"][:] = 0
+    parts["t"][:] = START_FRAME * params["mhd_dt"]
     threads = os.cpu_count() or 1
     total_steps = 0
     t0 = time.perf_counter()
@@ -684,40 +685,44 @@ def main():
     parser.add_argument("--steps", type=int, default=5)
     parser.add_argument("--warmup", type=int, default=3)
     parser.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    parser.add_argument("--particles", type=int, default=1 << 18,
+    parser.add_argument("--particles", type=int, default=1 << 22,
                         help="focused population (headline)")
+    parser.add_argument("--substeps", type=int, default=1000,
+                        help="fixed steps per interval of the focused legs")
     parser.add_argument("--f64-steps", type=int, default=2,
-                        help="timed intervals of the FP64 legs")
+                        help="timed intervals of the Parker FP64 leg")
     parser.add_argument("--parker-particles", type=int, default=1 << 20,
                         help="Parker population (0 skips the Parker legs)")
     parser.add_argument("--train-samples", type=int, default=2000000)
     parser.add_argument("--train-steps", type=int, default=16000)
-    parser.add_argument("--cpu-particles", type=int, default=1 << 16)
+    parser.add_argument("--cpu-particles", type=int, default=1 << 18,
+                        help="particles of the CPU baseline's sample (one interval each step)")
     parser.add_argument("--batch-runs", type=int, default=64,
                         help="independent runs of the batched leg (0 skips it)")
     parser.add_argument("--library-particles", type=int, default=1 << 20,
                         help="particles of the library-solver leg (0 skips it)")
     parser.add_argument("--library-steps", type=int, default=10)
-    parser.add_argument("--c3-particles", type=int, default=1 << 22,
-                        help="particles of the C3 precision leg (0 skips it)")
-    parser.add_argument("--hidden-width", type=int, default=32, choices=(32, 64),
-                        help="hidden width of the headline network (a width-64 BF16 network "
-                             "is measured beside a width-32 headline)")
+    parser.add_argument("--hidden-width", type=int, default=64, choices=(32, 64),
+                        help="hidden width of the headline network (a BF16 network of the "
+                             "other width is measured beside it)")
     parser.add_argument("--sort-tile", type=int, default=16,
                         help="cell-sort tile (cells) before each push; 0 disables")
     args = parser.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     config = {"workload": f"focused push, learned slab-QLT closure (sigma2 0.1, gamma_k 5/3), "
                           f"{NX}x{NY} stretched-y Harris+islands field, {args.particles} "
-                          f"particles, consecutive intervals",
+                          f"particles (p = p0, mu uniform on [-1, 1]), {args.substeps} fixed "
+                          f"steps per interval, consecutive intervals",
               "nx": NX, "ny": NY, "particles": args.particles, "transport": "focused",
+              "steps_per_interval": args.substeps,
               "closure": f"surrogate (5-{args.hidden_width}-{args.hidden_width}-3 MLP, BF16 "
                          f"tensor cores, FP32 accumulation)",
               "l2": "tables larger than L2 (no flush)", "sort_tile": args.sort_tile}
     if args.impl == "reference":
         if rank != 0:
             return
-        value, threads, elapsed, total = cpu_baseline(args.cpu_particles, max(1, args.steps))
+        value, threads, elapsed, total = cpu_baseline(args.cpu_particles, args.substeps,
+                                                      max(1, args.steps))
         line = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "impl": "reference",
                 "ms_per_step": elapsed * 1e3 / max(1, args.steps),
@@ -742,7 +747,6 @@ def main():
     f0, f1 = make_workload()
     focused = run_focused(args, f0, f1)
     parker = run_parker(args, f0, f1) if args.parker_particles > 0 and WORLD == 1 else None
-    c3 = run_c3(args, f0, f1) if args.c3_particles > 0 and WORLD == 1 else None
     batched = run_batched(args) if args.batch_runs > 0 and WORLD == 1 else None
     library = run_library(args) if args.library_particles > 0 and WORLD == 1 else None
     peak, peak_kind = read_peaks()
@@ -761,11 +765,13 @@ def main():
     if WORLD > 1 and rank != 0:
         return
     if WORLD == 1:
-        cpu_value, cpu_threads, cpu_elapsed, cpu_total = cpu_baseline(args.cpu_particles, 1)
+        cpu_value, cpu_threads, cpu_elapsed, cpu_total = cpu_baseline(args.cpu_particles,
+                                                                      args.substeps, 1)
         cpu = {"value": cpu_value, "unit": "particle-steps/s", "cores": cpu_threads,
                "kind": "port",
                "sample": f"focused plain-QLT oracle, {args.cpu_particles} particles x 1 "
-                         f"interval ({cpu_total} particle-steps, {cpu_elapsed:.1f} s)"}
+                         f"interval of {args.substeps} steps ({cpu_total} particle-steps, "
+                         f"{cpu_elapsed:.1f} s)"}
     else:
         cpu = None  # the CPU baseline runs at N = 1 only
     line = {
@@ -781,15 +787,15 @@ def main():
         "mixed_plain_qlt": None if mixed_qlt is None else {
             "value": mixed_qlt["value"], "ms_per_step": mixed_qlt["ms_per_step"],
             "spectrum_l1_vs_f64": mixed_qlt["spectrum_l1_vs_f64"],
+            "mu_spectrum_l1_vs_f64": mixed_qlt["mu_spectrum_l1_vs_f64"],
             "surrogate_gain": head["value"] / mixed_qlt["value"]},
         "spectrum_l1_vs_f64": head["spectrum_l1_vs_f64"],
+        "mu_spectrum_l1_vs_f64": head["mu_spectrum_l1_vs_f64"],
         "judge": head["judge"],
-        "surrogate_fp16": None if "surrogate_fp16" not in focused else {
-            k: focused["surrogate_fp16"][k] for k in
-            ("value", "ms_per_step", "spectrum_l1_vs_f64", "judge")},
-        "surrogate_h64": None if "surrogate_h64" not in focused else {
-            k: focused["surrogate_h64"][k] for k in
-            ("value", "ms_per_step", "spectrum_l1_vs_f64", "judge")},
+        **{label: None if label not in focused else {
+            k: focused[label][k] for k in
+            ("value", "ms_per_step", "spectrum_l1_vs_f64", "mu_spectrum_l1_vs_f64", "judge")}
+           for label in ("surrogate_fp16", f"surrogate_h{96 - args.hidden_width}")},
         "train": focused["train"],
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak,
@@ -804,7 +810,10 @@ def main():
                 "h2d_bytes_per_step": head["state_bytes"],
                 "d2h_bytes_per_step": head["state_bytes"]},
         "parker": parker,
-        "c3_precision": c3,
+        "c3_precision": None if "c3" not in focused else dict(
+            focused["c3"],
+            mixed={"value": mixed_qlt["value"], "ms_per_step": mixed_qlt["ms_per_step"]},
+            f64={"value": f64["value"], "ms": f64["ms_per_step"]}),
         "batched_runs": batched,
         "library_solvers": library,
         # per timed step: the push, plus 3 cell-sort kernels when sorting

@@ -155,24 +155,88 @@ __device__ __forceinline__ void load_surrogate_block(const uint2* src, uint2* sm
     __syncthreads();
 }
 
+// Row tiles [0, MT) of the three layers: ax the input A fragments, out the
+// output accumulators.  With MT = 2 both row tiles advance together: every
+// weight fragment and bias read from shared memory feeds two MMAs, and the
+// two tiles' dependency chains interleave, at the cost of twice the live
+// activation registers.
+template <bool FP16, int H, int MT>
+__device__ __forceinline__ void mlp_rows(const uint2* smem, const uint32_t (*ax)[4],
+                                         float (*out)[4]) {
+    using M = Mlp<H>;
+    const int lane = static_cast<int>(threadIdx.x & 31u);
+    const int tig = lane & 3;
+    const float* bias = reinterpret_cast<const float*>(smem + M::FragCount);
+    // layer 1: NT column tiles -> A fragments of layer 2 (KT k tiles)
+    uint32_t a2[MT][M::KT][4];
+#pragma unroll
+    for (int nt = 0; nt < M::NT; ++nt) {
+        const float2 bv = *reinterpret_cast<const float2*>(bias + 8 * nt + 2 * tig);
+        const uint2 w = smem[M::FragW1 + nt * 32 + lane];
+#pragma unroll
+        for (int mt = 0; mt < MT; ++mt) {
+            float acc[4] = {bv.x, bv.y, bv.x, bv.y};
+            mma_16816<FP16>(acc, ax[mt], w);
+            a2[mt][nt >> 1][(nt & 1) * 2 + 0] = act_x2<FP16>(acc[0], acc[1]);
+            a2[mt][nt >> 1][(nt & 1) * 2 + 1] = act_x2<FP16>(acc[2], acc[3]);
+        }
+    }
+    // layer 2, with layer 3 accumulated as each pair of column tiles
+    // completes a k tile of its A fragment
+    const float2 b3 = *reinterpret_cast<const float2*>(bias + 2 * H + 2 * tig);
+#pragma unroll
+    for (int mt = 0; mt < MT; ++mt) {
+        out[mt][0] = b3.x;
+        out[mt][1] = b3.y;
+        out[mt][2] = b3.x;
+        out[mt][3] = b3.y;
+    }
+#pragma unroll
+    for (int kt3 = 0; kt3 < M::KT; ++kt3) {
+        uint32_t a3[MT][4];
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            const int nt = 2 * kt3 + half;
+            const float2 bv = *reinterpret_cast<const float2*>(bias + H + 8 * nt + 2 * tig);
+            float acc[MT][4];
+#pragma unroll
+            for (int mt = 0; mt < MT; ++mt) {
+                acc[mt][0] = bv.x;
+                acc[mt][1] = bv.y;
+                acc[mt][2] = bv.x;
+                acc[mt][3] = bv.y;
+            }
+#pragma unroll
+            for (int kt = 0; kt < M::KT; ++kt) {
+                const uint2 w = smem[M::FragW2 + (kt * M::NT + nt) * 32 + lane];
+#pragma unroll
+                for (int mt = 0; mt < MT; ++mt) mma_16816<FP16>(acc[mt], a2[mt][kt], w);
+            }
+#pragma unroll
+            for (int mt = 0; mt < MT; ++mt) {
+                a3[mt][half * 2 + 0] = act_x2<FP16>(acc[mt][0], acc[mt][1]);
+                a3[mt][half * 2 + 1] = act_x2<FP16>(acc[mt][2], acc[mt][3]);
+            }
+        }
+        const uint2 w3 = smem[M::FragW3 + kt3 * 32 + lane];
+#pragma unroll
+        for (int mt = 0; mt < MT; ++mt) mma_16816<FP16>(out[mt], a3[mt], w3);
+    }
+}
+
 // Warp-collective forward pass.  Every lane of the warp must call it with the
 // warp converged; lane r supplies row r (its five normalised features; zeros
 // for an idle lane) and receives the three normalised outputs of row r.
 template <bool FP16, int H>
 __device__ __forceinline__ void mlp_warp(const uint2* smem, const float (&f)[kMlpIn],
                                          float (&y)[kMlpOut]) {
-    using M = Mlp<H>;
     const unsigned full = 0xffffffffu;
     const int lane = static_cast<int>(threadIdx.x & 31u);
     const int g = lane >> 2;
     const int tig = lane & 3;
-    const float* bias = reinterpret_cast<const float*>(smem + M::FragCount);
     const uint32_t pk0 = pack_x2<FP16>(f[0], f[1]);
     const uint32_t pk1 = pack_x2<FP16>(f[2], f[3]);
     const uint32_t pk2 = pack_x2<FP16>(f[4], 0.0f);
-    // Both row tiles advance together: every weight fragment and bias read
-    // from shared memory feeds two MMAs, and the two tiles' dependency
-    // chains interleave.
     // A fragments of the input tiles: columns 2tig, 2tig+1 of rows g and
     // g+8; columns 8..15 (and 5..7) are zero padding.
     uint32_t ax[2][4];
@@ -190,48 +254,9 @@ __device__ __forceinline__ void mlp_warp(const uint2* smem, const float (&f)[kMl
         ax[mt][2] = 0u;
         ax[mt][3] = 0u;
     }
-    // layer 1: NT column tiles -> A fragments of layer 2 (KT k tiles)
-    uint32_t a2[2][M::KT][4];
-#pragma unroll
-    for (int nt = 0; nt < M::NT; ++nt) {
-        const float2 bv = *reinterpret_cast<const float2*>(bias + 8 * nt + 2 * tig);
-        const uint2 w = smem[M::FragW1 + nt * 32 + lane];
-#pragma unroll
-        for (int mt = 0; mt < 2; ++mt) {
-            float acc[4] = {bv.x, bv.y, bv.x, bv.y};
-            mma_16816<FP16>(acc, ax[mt], w);
-            a2[mt][nt >> 1][(nt & 1) * 2 + 0] = act_x2<FP16>(acc[0], acc[1]);
-            a2[mt][nt >> 1][(nt & 1) * 2 + 1] = act_x2<FP16>(acc[2], acc[3]);
-        }
-    }
-    // layer 2, with layer 3 accumulated as each pair of column tiles
-    // completes a k tile of its A fragment
-    const float2 b3 = *reinterpret_cast<const float2*>(bias + 2 * H + 2 * tig);
-    float out[2][4] = {{b3.x, b3.y, b3.x, b3.y}, {b3.x, b3.y, b3.x, b3.y}};
-#pragma unroll
-    for (int kt3 = 0; kt3 < M::KT; ++kt3) {
-        uint32_t a3[2][4];
-#pragma unroll
-        for (int half = 0; half < 2; ++half) {
-            const int nt = 2 * kt3 + half;
-            const float2 bv = *reinterpret_cast<const float2*>(bias + H + 8 * nt + 2 * tig);
-            float acc[2][4] = {{bv.x, bv.y, bv.x, bv.y}, {bv.x, bv.y, bv.x, bv.y}};
-#pragma unroll
-            for (int kt = 0; kt < M::KT; ++kt) {
-                const uint2 w = smem[M::FragW2 + (kt * M::NT + nt) * 32 + lane];
-                mma_16816<FP16>(acc[0], a2[0][kt], w);
-                mma_16816<FP16>(acc[1], a2[1][kt], w);
-            }
-#pragma unroll
-            for (int mt = 0; mt < 2; ++mt) {
-                a3[mt][half * 2 + 0] = act_x2<FP16>(acc[mt][0], acc[mt][1]);
-                a3[mt][half * 2 + 1] = act_x2<FP16>(acc[mt][2], acc[mt][3]);
-            }
-        }
-        const uint2 w3 = smem[M::FragW3 + kt3 * 32 + lane];
-        mma_16816<FP16>(out[0], a3[0], w3);
-        mma_16816<FP16>(out[1], a3[1], w3);
-    }
+    // both row tiles together (one tile after the other spills at H = 64)
+    float out[2][4];
+    mlp_rows<FP16, H, 2>(smem, ax, out);
     // Row r = 16 mt + 8 h + g' sits in lane 4 g' (columns 0, 1; registers
     // 2h, 2h+1) and lane 4 g' + 1 (column 2; register 2h) of tile mt.
     const int src0 = 4 * (lane & 7);
