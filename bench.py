@@ -263,15 +263,22 @@ def run_focused(args, f0, f1):
     start = parts.download(n)
     start["status"][:] = 0
     start["t"][:] = START_FRAME * plain.mhd_dt
-    legs = [("surrogate", kpt.PRECISION_MIXED, learned, args.steps),
-            ("f64", kpt.PRECISION_F64, plain, 0)]
+    tc, warp = kpt.ENGINE_TCGEN05, kpt.ENGINE_MMA_SYNC
+    legs = [("surrogate", kpt.PRECISION_MIXED, learned, args.steps, "surrogate", tc),
+            ("f64", kpt.PRECISION_F64, plain, 0, None, tc)]
     if WORLD == 1:
-        legs += [("mixed_qlt", kpt.PRECISION_MIXED, plain, args.steps),
-                 ("surrogate_fp16", kpt.PRECISION_MIXED, learned, args.steps),
-                 (f"surrogate_h{other}", kpt.PRECISION_MIXED, learned, args.steps)]
+        legs += [("mixed_qlt", kpt.PRECISION_MIXED, plain, args.steps, None, tc),
+                 ("surrogate_mma_sync", kpt.PRECISION_MIXED, learned, args.steps, "surrogate",
+                  warp),
+                 ("surrogate_fp16", kpt.PRECISION_MIXED, learned, args.steps, "surrogate_fp16",
+                  tc),
+                 (f"surrogate_h{other}", kpt.PRECISION_MIXED, learned, args.steps,
+                  f"surrogate_h{other}", tc)]
     finals = {}
-    for label, precision, settings, steps in legs:
-        ctx.set_surrogate(nets.get(label))
+    for label, precision, settings, steps, net_label, engine in legs:
+        if net_label is not None:
+            nets[net_label].engine = engine
+        ctx.set_surrogate(nets.get(net_label))
         lower, upper = tables[precision]
         parts.upload(start, n)
         ctx.surrogate_judge()
@@ -298,8 +305,9 @@ def run_focused(args, f0, f1):
         leg = {"value": psteps / (total_ms / 1e3), "ms_per_step": total_ms / steps,
                "kernel_ms": float(np.mean(kernel_ms)), "particle_steps": int(psteps),
                "steps": steps, "clocks": clocks}
-        if label in nets:
+        if net_label is not None:
             leg["judge"] = ctx.surrogate_judge()
+            leg["engine"] = "tcgen05" if engine == tc else "mma.sync"
         if label == "surrogate":
             # e2e through the C ABI with host buffers
             host = {k: v.copy() for k, v in start.items()}
@@ -716,7 +724,8 @@ def main():
               "nx": NX, "ny": NY, "particles": args.particles, "transport": "focused",
               "steps_per_interval": args.substeps,
               "closure": f"surrogate (5-{args.hidden_width}-{args.hidden_width}-3 MLP, BF16 "
-                         f"tensor cores, FP32 accumulation)",
+                         f"weights on the tcgen05 tensor cores, activations in tensor "
+                         f"memory, FP32 accumulation)",
               "l2": "tables larger than L2 (no flush)", "sort_tile": args.sort_tile}
     if args.impl == "reference":
         if rank != 0:
@@ -795,7 +804,8 @@ def main():
         **{label: None if label not in focused else {
             k: focused[label][k] for k in
             ("value", "ms_per_step", "spectrum_l1_vs_f64", "mu_spectrum_l1_vs_f64", "judge")}
-           for label in ("surrogate_fp16", f"surrogate_h{96 - args.hidden_width}")},
+           for label in ("surrogate_mma_sync", "surrogate_fp16",
+                         f"surrogate_h{96 - args.hidden_width}")},
         "train": focused["train"],
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak,

@@ -78,6 +78,12 @@ enum kpt_schedule {
     KPT_SCHEDULE_SIMPLE = 1
 };
 
+/* How the learned closure's network is served (push and evaluate). */
+enum kpt_network_engine {
+    KPT_ENGINE_TCGEN05 = 0,  /* block-collective tcgen05.mma, activations in tensor memory */
+    KPT_ENGINE_MMA_SYNC = 1  /* warp-collective mma.sync, activations in registers */
+};
+
 /* Run parameters: the reference's Reconnection2DSettings physics block
  * (src/main.cpp:114-241).  Doubles first, then 32-bit ints. */
 typedef struct kpt_settings {
@@ -172,7 +178,7 @@ typedef struct kpt_surrogate_config {
     int32_t quantization_aware; /* 1: the last quarter of the steps trains through the
                                    served element type's rounding (default 0; measured
                                    no gain for BF16, whose error is activation rounding) */
-    int32_t hidden_width;     /* H: 32 (default) or 64 */
+    int32_t hidden_width;     /* H: 64 (default) or 32 */
     double learning_rate;     /* initial; cosine decay to 1 % (default 1e-2) */
     double mu_cut;            /* default 0.02 */
     double mu_max;            /* largest |mu| trained (default 0.999) */
@@ -258,6 +264,12 @@ int kpt_surrogate_destroy(kpt_surrogate* surrogate);
  * (optional, n) is 1 where the network answered. */
 int kpt_surrogate_evaluate(kpt_surrogate* surrogate, uint64_t n, const double* inputs,
                            int tensor_cores, double* outputs, int32_t* served);
+/* Engine that serves the network in the push and in evaluate's
+ * tensor-core path (default KPT_ENGINE_TCGEN05).  The engines compute the
+ * same BF16/FP16 network with FP32 accumulation; their sums associate
+ * differently, so results agree to FP32 rounding, not bit for bit. */
+int kpt_surrogate_set_engine(kpt_surrogate* surrogate, int engine);
+int kpt_surrogate_get_engine(const kpt_surrogate* surrogate, int32_t* engine);
 /* Parameter block (FP32, W1[H][5] b1[H] W2[H][H] b2[H] W3[3][H] b3[3]:
  * 1379 floats for H = 32, 4739 for H = 64) and the box
  * normalisation (in_lo[5], in_hi[5], out_offset[3], out_scale[3], mu_cut);

@@ -32,6 +32,8 @@ PRECISION_F64 = 0
 PRECISION_MIXED = 1
 SCHEDULE_REFILL = 0
 SCHEDULE_SIMPLE = 1
+ENGINE_TCGEN05 = 0   # block-collective tcgen05.mma network, activations in tensor memory
+ENGINE_MMA_SYNC = 1  # warp-collective mma.sync network, activations in registers
 
 PARTICLE_FIELDS = ("x", "y", "p", "t", "dt", "w", "mu", "status", "level")
 DOUBLE_SETTINGS = ("mhd_dt", "p0", "pmin", "pmax", "gamma_turb", "kpara0", "kperp_over_kpara",
@@ -252,6 +254,8 @@ def load_library() -> ctypes.CDLL:
         "kpt_surrogate_parameters": (i32, [vp, vp, i32, vp, i32]),
         "kpt_surrogate_gradient": (i32, [vp, i32, vp, u64, vp, vp, vp, vp]),
         "kpt_surrogate_shape": (i32, [vp, vp, vp]),
+        "kpt_surrogate_set_engine": (i32, [vp, i32]),
+        "kpt_surrogate_get_engine": (i32, [vp, vp]),
         "kpt_context_set_surrogate": (i32, [vp, vp]),
         "kpt_surrogate_judge": (i32, [vp, vp, vp, vp, vp]),
         "kpt_grid_create": (i32, [vp, i32, i32, vp, vp, vp, pvp]),
@@ -815,6 +819,18 @@ class Surrogate:
                         "out_offset": norm[10:13].astype(np.float64),
                         "out_scale": norm[13:16].astype(np.float64),
                         "mu_cut": float(norm[16])}
+
+    @property
+    def engine(self) -> int:
+        """ENGINE_TCGEN05 (default) or ENGINE_MMA_SYNC: how the push and
+        evaluate(tensor_cores=True) serve the network."""
+        value = ctypes.c_int32()
+        _check(self.ctx.lib.kpt_surrogate_get_engine(self.handle, ctypes.byref(value)))
+        return int(value.value)
+
+    @engine.setter
+    def engine(self, value: int) -> None:
+        _check(self.ctx.lib.kpt_surrogate_set_engine(self.handle, int(value)))
 
     def evaluate(self, inputs: np.ndarray, tensor_cores: bool = True):
         """(n, 5) raw inputs (mu, ln p, ln|B|, dB^2/B^2, gamma_k) ->

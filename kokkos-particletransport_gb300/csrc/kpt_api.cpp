@@ -120,6 +120,8 @@ struct kpt_surrogate {
     std::vector<float> params;  // FP32 trained parameters
     float* d_params = nullptr;  // FP32 copy (SIMT evaluation)
     uint2* d_block = nullptr;   // BF16 mma.sync B fragments + FP32 biases
+    uint4* d_tc_block = nullptr;  // tcgen05 B operands, biases folded in (canonical layout)
+    int engine = kpt::kEngineTcgen05;
     double final_loss = 0.0;
     // settings the targets were generated with (checked at push time)
     double kperp_over_kpara = 0.0;
@@ -1061,6 +1063,8 @@ int kpt_push_interval(kpt_context* ctx, kpt_particles* parts, const kpt_field* l
                         box.momentum_dependency == settings->momentum_dependency,
                     "kpt_push_interval: settings differ from those the surrogate was trained with");
         served.block = sg->d_block;
+        served.tc_block = sg->d_tc_block;
+        served.engine = sg->engine;
         served.box = box;
         const double f3 = std::log(settings->qlt_sigma2);
         const double f4 = settings->qlt_spectral_index;
@@ -1086,6 +1090,9 @@ int kpt_push_interval(kpt_context* ctx, kpt_particles* parts, const kpt_field* l
         stats->failed = host.failed;
         stats->max_steps = host.max_steps;
         stats->pad = 0;
+        KPT_REQUIRE(host.network_timeouts == 0,
+                    "kpt_push_interval: a tensor-core completion wait timed out (results of "
+                    "this push are invalid)");
     }
     return KPT_OK;
 }
@@ -1299,6 +1306,22 @@ uint32_t to_fp16(float f) {
     return sign | out;
 }
 
+// 16-bit pattern (bfloat16 or IEEE binary16) -> float, exactly.
+float from_16(uint32_t h, bool fp16) {
+    if (!fp16) {
+        const uint32_t bits = h << 16;
+        float f;
+        std::memcpy(&f, &bits, sizeof(f));
+        return f;
+    }
+    const float sign = (h & 0x8000u) ? -1.0f : 1.0f;
+    const int exp = static_cast<int>((h >> 10) & 0x1fu);
+    const int mant = static_cast<int>(h & 0x3ffu);
+    if (exp == 0) return sign * std::ldexp(static_cast<float>(mant), -24);
+    if (exp == 31) return mant ? std::nanf("") : sign * INFINITY;
+    return sign * std::ldexp(static_cast<float>(mant + 1024), exp - 25);
+}
+
 uint32_t pack_pair(float lo, float hi, bool fp16) {
     return fp16 ? (to_fp16(lo) | (to_fp16(hi) << 16)) : (to_bf16(lo) | (to_bf16(hi) << 16));
 }
@@ -1318,6 +1341,23 @@ void pack_fragments(const float* w, int n_out, int k_in, int ktiles, int ntiles,
                 out.push_back(pack_pair(at(n, k0), at(n, k0 + 1), fp16));
                 out.push_back(pack_pair(at(n, k0 + 8), at(n, k0 + 9), fp16));
             }
+        }
+    }
+}
+
+// B operand of a tcgen05 MMA in the canonical K-major, no-swizzle layout:
+// W[n][k] (n outputs, k inputs) zero padded to n_rows x k_cols, element
+// (n, k) at byte (n/8) (k_cols/8) 128 + (k/8) 128 + (n%8) 16 + (k%8) 2.
+void pack_canonical(const float* w, int n_out, int k_in, int n_rows, int k_cols, bool fp16,
+                    std::vector<uint16_t>& out) {
+    const size_t base = out.size();
+    out.resize(base + static_cast<size_t>(n_rows) * k_cols, 0);
+    for (int n = 0; n < n_rows; ++n) {
+        for (int k = 0; k < k_cols; ++k) {
+            const float v = (n < n_out && k < k_in) ? w[n * k_in + k] : 0.0f;
+            const size_t byte = static_cast<size_t>(n / 8) * (k_cols / 8) * 128 +
+                                static_cast<size_t>(k / 8) * 128 + (n % 8) * 16 + (k % 8) * 2;
+            out[base + byte / 2] = static_cast<uint16_t>(fp16 ? to_fp16(v) : to_bf16(v));
         }
     }
 }
@@ -1513,6 +1553,39 @@ int kpt_surrogate_train(kpt_context* ctx, const kpt_settings* settings,
     KPT_CUDA(cudaMemcpy(sg->d_params, sg->params.data(), pcount * sizeof(float),
                         cudaMemcpyHostToDevice));
     KPT_CUDA(cudaMemcpy(sg->d_block, words.data(), block_bytes, cudaMemcpyHostToDevice));
+    // the tcgen05 engine: canonical-layout weights, each layer's bias as two
+    // extra input columns (16-bit head and remainder) fed by constant ones
+    std::vector<uint16_t> tc;
+    {
+        const float* p = sg->params.data();
+        const int k2 = hidden + 16;
+        std::vector<float> w1(static_cast<size_t>(hidden) * 16, 0.0f);
+        std::vector<float> w2(static_cast<size_t>(hidden) * k2, 0.0f);
+        std::vector<float> w3(static_cast<size_t>(16) * k2, 0.0f);
+        auto split = [&](float b, float* row) {
+            const float hi = from_16(fp16 ? to_fp16(b) : to_bf16(b), fp16);
+            row[0] = hi;
+            row[1] = b - hi;
+        };
+        for (int n = 0; n < hidden; ++n) {
+            for (int k = 0; k < kpt::kMlpIn; ++k) w1[n * 16 + k] = p[pw1 + n * kpt::kMlpIn + k];
+            split(p[pw1 + hidden * kpt::kMlpIn + n], &w1[n * 16 + kpt::kMlpIn]);
+            for (int k = 0; k < hidden; ++k) w2[n * k2 + k] = p[pw2 + n * hidden + k];
+            split(p[pw2 + hidden * hidden + n], &w2[n * k2 + hidden]);
+        }
+        for (int n = 0; n < kpt::kMlpOut; ++n) {
+            for (int k = 0; k < hidden; ++k) w3[n * k2 + k] = p[pw3 + n * hidden + k];
+            split(p[pw3 + kpt::kMlpOut * hidden + n], &w3[n * k2 + hidden]);
+        }
+        pack_canonical(w1.data(), hidden, 16, hidden, 16, fp16, tc);
+        pack_canonical(w2.data(), hidden, k2, hidden, k2, fp16, tc);
+        pack_canonical(w3.data(), 16, k2, 16, k2, fp16, tc);
+    }
+    const size_t tc_bytes = kpt::tc_block_bytes(hidden);
+    KPT_REQUIRE(tc.size() * sizeof(uint16_t) == tc_bytes,
+                "kpt_surrogate_train: tensor-core block size mismatch");
+    KPT_CUDA(cudaMalloc(&sg->d_tc_block, tc_bytes));
+    KPT_CUDA(cudaMemcpy(sg->d_tc_block, tc.data(), tc_bytes, cudaMemcpyHostToDevice));
     *out = sg.release();
     return KPT_OK;
 }
@@ -1522,6 +1595,7 @@ int kpt_surrogate_destroy(kpt_surrogate* sg) {
     cudaSetDevice(sg->device);
     cudaFree(sg->d_params);
     cudaFree(sg->d_block);
+    cudaFree(sg->d_tc_block);
     delete sg;
     return KPT_OK;
 }
@@ -1563,19 +1637,39 @@ int kpt_surrogate_evaluate(kpt_surrogate* sg, uint64_t n, const double* inputs, 
     if (n == 0) return KPT_OK;
     KPT_CUDA(cudaSetDevice(sg->device));
     ScopedBuffer buf;
-    KPT_CUDA(buf.reserve(n * 8 * sizeof(double) + n * sizeof(int)));
+    KPT_CUDA(buf.reserve(n * 8 * sizeof(double) + n * sizeof(int) + sizeof(unsigned int)));
     double* din = buf.as<double>();
     double* dout = din + n * 5;
     int* dserved = reinterpret_cast<int*>(dout + n * 3);
     cudaStream_t st = sg->ctx->stream;
     KPT_CUDA(cudaMemcpyAsync(din, inputs, n * 5 * sizeof(double), cudaMemcpyHostToDevice, st));
-    KPT_CUDA(kpt::surrogate_eval(static_cast<int>(n), din, sg->box, sg->d_params, sg->d_block,
-                                 tensor_cores != 0, dout, dserved, st));
+    unsigned int* dtimeouts = reinterpret_cast<unsigned int*>(dserved + n);
+    KPT_CUDA(cudaMemsetAsync(dtimeouts, 0, sizeof(unsigned int), st));
+    kpt::SurrogateServe serve{sg->d_params, sg->d_block, sg->d_tc_block,
+                              tensor_cores == 0 ? -1 : sg->engine, dtimeouts};
+    KPT_CUDA(kpt::surrogate_eval(static_cast<int>(n), din, sg->box, serve, dout, dserved, st));
+    unsigned int timeouts = 0;
+    KPT_CUDA(cudaMemcpyAsync(&timeouts, dtimeouts, sizeof(timeouts), cudaMemcpyDeviceToHost, st));
     KPT_CUDA(cudaMemcpyAsync(outputs, dout, n * 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
     if (served) {
         KPT_CUDA(cudaMemcpyAsync(served, dserved, n * sizeof(int), cudaMemcpyDeviceToHost, st));
     }
     KPT_CUDA(cudaStreamSynchronize(st));
+    KPT_REQUIRE(timeouts == 0, "kpt_surrogate_evaluate: a tensor-core completion wait timed out");
+    return KPT_OK;
+}
+
+int kpt_surrogate_set_engine(kpt_surrogate* sg, int engine) {
+    KPT_REQUIRE(sg != nullptr, "kpt_surrogate_set_engine: NULL handle");
+    KPT_REQUIRE(engine == KPT_ENGINE_TCGEN05 || engine == KPT_ENGINE_MMA_SYNC,
+                "kpt_surrogate_set_engine: unknown engine");
+    sg->engine = engine;
+    return KPT_OK;
+}
+
+int kpt_surrogate_get_engine(const kpt_surrogate* sg, int32_t* engine) {
+    KPT_REQUIRE(sg && engine, "kpt_surrogate_get_engine: NULL argument");
+    *engine = sg->engine;
     return KPT_OK;
 }
 

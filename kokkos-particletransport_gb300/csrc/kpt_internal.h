@@ -193,9 +193,19 @@ cudaError_t surrogate_train_step(const SurrogateTrainLaunch& launch, int step,
 cudaError_t surrogate_gradient(const SurrogateTrainLaunch& launch, cudaStream_t stream);
 // Raw inputs (n x 5, device) -> D_mumu, dD_mumu/dmu, ln kappa_parallel
 // (n x 3, device); served[i] = 1 where the network answered.
+// How the network is served by surrogate_eval: engine -1 = the FP32 SIMT
+// forward, kEngineMmaSync / kEngineTcgen05 = the tensor-core paths of the
+// push; timeouts counts blocks stopped by a tcgen05 completion timeout.
+struct SurrogateServe {
+    const float* params;
+    const uint2* block;
+    const uint4* tc_block;
+    int engine;
+    unsigned int* timeouts;
+};
 cudaError_t surrogate_eval(int n, const double* inputs, const SurrogateBox& box,
-                           const float* params, const uint2* block, bool tensor, double* out,
-                           int* served, cudaStream_t stream);
+                           const SurrogateServe& serve, double* out, int* served,
+                           cudaStream_t stream);
 
 // ---- header library (ParkerSolver / ParticleSystem), 2D Cartesian ---------
 // One axis of an analytic uniform grid (AnalyticCoordinateGrid.hpp) with the

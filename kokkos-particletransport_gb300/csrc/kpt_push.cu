@@ -852,9 +852,14 @@ struct JudgeTally {
 // the training box, or with |mu| < mu_cut, use the plain closure; one
 // substep in judge_period of each particle also evaluates the plain closure
 // and records the larger relative error of D_mumu and kappa_parallel.
-template <bool FP16, int H>
+// TC = true serves the network on the tensor cores, block-collective (every
+// thread of the block calls it); *stop is then set, uniformly over the
+// block, when a completion wait timed out (the substep is abandoned).
+template <bool FP16, int H, bool TC = false>
 __device__ __forceinline__ bool substep_surrogate(StateMixed& st, const PushParams& P, bool have,
-                                                  const uint2* smem, JudgeTally& tally) {
+                                                  const uint2* smem, JudgeTally& tally,
+                                                  TcNet* net = nullptr, bool* fail = nullptr,
+                                                  bool* stop = nullptr) {
     const SurrogateDevice& sg = P.sg;
     const SurrogateBox& box = sg.box;
     float c[21];
@@ -883,9 +888,17 @@ __device__ __forceinline__ bool substep_surrogate(StateMixed& st, const PushPara
             }
         }
     }
-    __syncwarp();
     float y[kMlpOut];
-    mlp_warp<FP16, H>(smem, f, y);
+    if constexpr (TC) {
+        __syncwarp();
+        *stop = mlp_cta<FP16, H>(*net, f, y, *fail);
+        if (*stop) {
+            return false;
+        }
+    } else {
+        __syncwarp();
+        mlp_warp<FP16, H>(smem, f, y);
+    }
     if (!have) {
         return false;
     }
@@ -1155,6 +1168,93 @@ __global__ void __launch_bounds__(128, SURR >= 3 ? KPT_SURROGATE32_MIN_BLOCKS
     }
 }
 
+// The learned-closure push with the network on the tcgen05 tensor cores.
+// Warps refill their lanes from the cursor as in push_refill_kernel, but the
+// network is block-collective (M = 128 rows = the block's lanes), so the
+// block advances in lockstep: a trip runs while any lane of the block holds
+// a particle, idle lanes feed zero rows, and the loop ends once every warp
+// has found the cursor exhausted.  A completion wait that times out stops
+// the block (counted in PushCounters::network_timeouts); the block frees its
+// TMEM before it returns.
+#ifndef KPT_SURROGATE_TC_MIN_BLOCKS
+#define KPT_SURROGATE_TC_MIN_BLOCKS 4
+#endif
+template <bool FP16, int H>
+__global__ void __launch_bounds__(128, KPT_SURROGATE_TC_MIN_BLOCKS)
+    push_tc_kernel(const PushParams P) {
+    const unsigned full = 0xffffffffu;
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned lanes_below = (1u << lane) - 1u;
+    extern __shared__ __align__(128) unsigned char tc_smem[];
+    TcNet net = tc_setup<H>(P.sg.tc_block, tc_smem);
+    tc_constants<FP16, H>(net);
+    JudgeTally tally{0ull, 0ull, 0ull, 0.0f};
+    StateMixed st;
+    bool have = false;
+    bool exhausted = false;
+    bool fail = false;
+    unsigned long long my_steps = 0, my_pushed = 0, my_failed = 0;
+    unsigned int my_max = 0;
+    for (;;) {
+        const unsigned idle = __ballot_sync(full, !have);
+        if (idle != 0u && !exhausted) {
+            const unsigned n_idle = __popc(idle);
+            const int leader = __ffs(idle) - 1;
+            unsigned base = 0;
+            if (static_cast<int>(lane) == leader) {
+                base = atomicAdd(&P.counters->next_particle, n_idle);
+            }
+            base = __shfl_sync(full, base, leader);
+            if (static_cast<uint64_t>(base) + n_idle >= P.count) {
+                exhausted = true;
+            }
+            if (!have) {
+                const uint64_t slot = static_cast<uint64_t>(base) + __popc(idle & lanes_below);
+                if (slot < P.count) {
+                    const uint32_t idx = P.order != nullptr ? __ldg(P.order + slot)
+                                                            : static_cast<uint32_t>(slot);
+                    if (P.parts.status[idx] == 0) {
+                        load<true>(st, P, idx);
+                        ++my_pushed;
+                        have = true;
+                        if (!live(st, P)) {
+                            store<true>(st, P);
+                            my_failed += st.status != 0 ? 1 : 0;
+                            have = false;
+                        }
+                    }
+                }
+            }
+        }
+        if (!__syncthreads_or(have ? 1 : 0)) {
+            if (__syncthreads_and(exhausted ? 1 : 0)) {
+                break;
+            }
+            continue;
+        }
+        bool stop = false;
+        const bool more =
+            substep_surrogate<FP16, H, true>(st, P, have, nullptr, tally, &net, &fail, &stop);
+        if (stop) {
+            break;
+        }
+        if (have && !more) {
+            store<true>(st, P);
+            my_steps += static_cast<unsigned long long>(st.steps);
+            my_max = max(my_max, static_cast<unsigned int>(st.steps));
+            my_failed += st.status != 0 ? 1 : 0;
+            have = false;
+        }
+    }
+    fail = __syncthreads_or(fail ? 1 : 0) != 0;
+    if (fail && threadIdx.x == 0) {
+        atomicAdd(&P.counters->network_timeouts, 1u);
+    }
+    tc_teardown<H>(net, fail);
+    flush_counters(P.counters, my_steps, my_pushed, my_failed, my_max);
+    flush_judge(P.sg.judge, tally);
+}
+
 // One particle per thread, no refill (schedule alternative for the tuner).
 template <typename State, bool FOCUSED>
 __global__ void __launch_bounds__(128) push_simple_kernel(const PushParams P) {
@@ -1206,10 +1306,52 @@ PushParams make_push_params(const PushLaunch& L) {
     return P;
 }
 
+// Persistent grid of the tcgen05 push: at most 4 resident blocks per SM
+// (each holds TcMlp<H>::Cols of the SM's 512 TMEM columns); if the kernel's
+// registers would let more blocks in, the dynamic shared memory is padded
+// until they do not.
+template <bool FP16, int H>
+cudaError_t launch_push_tc(const PushParams& P, const PushLaunch& L, cudaStream_t stream) {
+    const int threads = 128;
+    constexpr int kTmemBlocks = 512 / static_cast<int>(TcMlp<H>::Cols);
+    size_t smem = tc_smem_bytes<H>();
+    int resident = 0;
+    cudaError_t err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &resident, push_tc_kernel<FP16, H>, threads, smem);
+    if (err != cudaSuccess) return err;
+    if (resident > kTmemBlocks) {
+        int device = 0, per_sm_smem = 0;
+        err = cudaGetDevice(&device);
+        if (err != cudaSuccess) return err;
+        err = cudaDeviceGetAttribute(&per_sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor,
+                                     device);
+        if (err != cudaSuccess) return err;
+        smem = static_cast<size_t>(per_sm_smem) / (kTmemBlocks + 1) + 1;
+        err = cudaFuncSetAttribute(push_tc_kernel<FP16, H>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   static_cast<int>(smem));
+        if (err != cudaSuccess) return err;
+        err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, push_tc_kernel<FP16, H>,
+                                                            threads, smem);
+        if (err != cudaSuccess) return err;
+    }
+    // the grid asks for the TMEM budget's blocks per SM whatever the
+    // occupancy query says (blocks that are not resident start when others
+    // finish and find the cursor further on)
+    resident = kTmemBlocks;
+    const int per_sm =
+        L.blocks_per_sm > 0 && L.blocks_per_sm < resident ? L.blocks_per_sm : resident;
+    push_tc_kernel<FP16, H><<<L.sm_count * per_sm, threads, smem, stream>>>(P);
+    return cudaGetLastError();
+}
+
 template <typename State, bool FOCUSED, int SURR = 0>
 cudaError_t launch_push(const PushLaunch& L, cudaStream_t stream) {
     const PushParams P = make_push_params(L);
     const int threads = 128;
+    if (SURR && L.surrogate->engine == kEngineTcgen05) {
+        return launch_push_tc<surr_fp16(SURR), surr_hidden(SURR)>(P, L, stream);
+    }
     const size_t smem = SURR ? mlp_smem_bytes(surr_hidden(SURR)) : 0;
     if (L.schedule == kScheduleSimple && !SURR) {
         const uint64_t want = (L.count + threads - 1) / threads;

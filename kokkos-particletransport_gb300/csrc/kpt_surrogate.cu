@@ -288,11 +288,77 @@ __device__ void forward_fp32(const float* w, const float (&in)[kMlpIn], float (&
 }
 
 // Raw inputs (mu, ln p, ln|B|, sigma^2, gamma_k) -> (D_mumu, dD_mumu/dmu,
-// ln kappa_parallel), FP64 out.  The network (FP32 SIMT, or the BF16
-// tensor-core warp path the push uses) serves inputs inside the box with
-// |mu| >= mu_cut; the plain closure serves the rest.  Warps stay converged
-// (the loop bound is per warp) because the tensor-core path is collective.
-// MODE 0: FP32 SIMT, 1: BF16 tensor cores, 2: FP16 tensor cores.
+// ln kappa_parallel), FP64 out.  The network (FP32 SIMT, or a tensor-core
+// engine of the push) serves inputs inside the box with |mu| >= mu_cut; the
+// plain closure serves the rest.
+//
+// Features of input i (zeros for an idle thread and outside the box);
+// returns whether the network serves it.
+__device__ __forceinline__ bool eval_features(int i, bool have, const double* __restrict__ in,
+                                              const SurrogateBox& box, double (&raw)[kMlpIn],
+                                              float (&f)[kMlpIn]) {
+    for (int k = 0; k < kMlpIn; ++k) raw[k] = 0.0;
+    if (have) {
+        for (int k = 0; k < kMlpIn; ++k) raw[k] = in[static_cast<size_t>(i) * kMlpIn + k];
+    }
+    const double mu = raw[0];
+    const double feat[kMlpIn] = {log(fabs(mu)), raw[1], raw[2], log(raw[3]), raw[4]};
+    bool inside = have && fabs(mu) >= box.mu_cut;
+    for (int k = 0; k < kMlpIn; ++k) {
+        inside = inside && feat[k] >= box.in_lo[k] && feat[k] <= box.in_hi[k];
+        f[k] = static_cast<float>(feat[k]) * box.in_scale[k] + box.in_offset[k];
+    }
+    if (!inside) {
+        for (int k = 0; k < kMlpIn; ++k) f[k] = 0.0f;
+    }
+    return inside;
+}
+
+// Closure values of input i from the network outputs y (or the plain
+// closure outside the box), with the push's hand-over near mu_cut.
+__device__ __forceinline__ void eval_store(int i, const double (&raw)[kMlpIn], bool inside,
+                                           const float (&y)[kMlpOut], const SurrogateBox& box,
+                                           double* __restrict__ out, int* __restrict__ served) {
+    const double mu = raw[0];
+    const double p = exp(raw[1]);
+    const double b = exp(raw[2]);
+    double d, dd, lk;
+    const double speed = box.particle_v0 * p / box.p0;
+    const double omega = box.qlt_omega0 * b / sqrt(1.0 + p * p);
+    double pd, pdd, py0, py1;
+    qlt_targets(mu, omega, speed, raw[3], box.qlt_lc, raw[4], box.qlt_h0, pd, pdd, py0, py1);
+    const double plk = log(kappa_parallel(box, p, b));
+    if (inside) {
+        const double y0 = static_cast<double>(y[0]) * box.out_scale[0] + box.out_offset[0];
+        const double y1 = static_cast<double>(y[1]) * box.out_scale[1] + box.out_offset[1];
+        lk = static_cast<double>(y[2]) * box.out_scale[2] + box.out_offset[2];
+        const double one_minus_mu2 = 1.0 - mu * mu;
+        const double sign = mu > 0.0 ? 1.0 : -1.0;
+        d = one_minus_mu2 * exp(y0);
+        dd = d * (sign * y1 / (fabs(mu) + box.qlt_h0) - 2.0 * mu / one_minus_mu2);
+        const double amu = fabs(mu);
+        if (amu < 2.0 * box.mu_cut) {
+            // the push's hand-over to the plain closure over [mu_cut, 2 mu_cut]
+            const double w = (amu - box.mu_cut) / box.mu_cut;
+            const double dw = sign / box.mu_cut;
+            dd = pdd + w * (dd - pdd) + dw * (d - pd);
+            d = pd + w * (d - pd);
+            lk = log(exp(plk) + w * (exp(lk) - exp(plk)));
+        }
+    } else {
+        d = pd;
+        dd = pdd;
+        lk = plk;
+    }
+    out[static_cast<size_t>(i) * kMlpOut + 0] = d;
+    out[static_cast<size_t>(i) * kMlpOut + 1] = dd;
+    out[static_cast<size_t>(i) * kMlpOut + 2] = lk;
+    served[i] = inside ? 1 : 0;
+}
+
+// FP32 SIMT (MODE 0) or the warp-collective mma.sync engine (MODE 1 BF16,
+// 2 FP16).  Warps stay converged (the loop bound is per warp) because the
+// tensor-core path is collective.
 template <int MODE, int H>
 __global__ void __launch_bounds__(128) eval_kernel(int n, const double* __restrict__ in,
                                                    SurrogateBox box,
@@ -314,63 +380,49 @@ __global__ void __launch_bounds__(128) eval_kernel(int n, const double* __restri
     for (int base = warp * 32; base < n; base += warps * 32) {
         const int i = base + lane;
         const bool have = i < n;
-        double raw[kMlpIn] = {0.0, 0.0, 0.0, 0.0, 0.0};
-        if (have) {
-            for (int k = 0; k < kMlpIn; ++k) raw[k] = in[static_cast<size_t>(i) * kMlpIn + k];
-        }
-        const double mu = raw[0];
-        const double feat[kMlpIn] = {log(fabs(mu)), raw[1], raw[2], log(raw[3]), raw[4]};
-        bool inside = have && fabs(mu) >= box.mu_cut;
+        double raw[kMlpIn];
         float f[kMlpIn];
-        for (int k = 0; k < kMlpIn; ++k) {
-            inside = inside && feat[k] >= box.in_lo[k] && feat[k] <= box.in_hi[k];
-            f[k] = static_cast<float>(feat[k]) * box.in_scale[k] + box.in_offset[k];
-        }
-        if (!inside) {
-            for (int k = 0; k < kMlpIn; ++k) f[k] = 0.0f;
-        }
+        const bool inside = eval_features(i, have, in, box, raw, f);
         float y[kMlpOut];
         if (MODE != 0) {
             mlp_warp<MODE == 2, H>(smem, f, y);
         } else {
             forward_fp32<H>(reinterpret_cast<const float*>(smem), f, y);
         }
-        if (!have) continue;
-        const double p = exp(raw[1]);
-        const double b = exp(raw[2]);
-        double d, dd, lk;
-        const double speed = box.particle_v0 * p / box.p0;
-        const double omega = box.qlt_omega0 * b / sqrt(1.0 + p * p);
-        double pd, pdd, py0, py1;
-        qlt_targets(mu, omega, speed, raw[3], box.qlt_lc, raw[4], box.qlt_h0, pd, pdd, py0, py1);
-        const double plk = log(kappa_parallel(box, p, b));
-        if (inside) {
-            const double y0 = static_cast<double>(y[0]) * box.out_scale[0] + box.out_offset[0];
-            const double y1 = static_cast<double>(y[1]) * box.out_scale[1] + box.out_offset[1];
-            lk = static_cast<double>(y[2]) * box.out_scale[2] + box.out_offset[2];
-            const double one_minus_mu2 = 1.0 - mu * mu;
-            const double sign = mu > 0.0 ? 1.0 : -1.0;
-            d = one_minus_mu2 * exp(y0);
-            dd = d * (sign * y1 / (fabs(mu) + box.qlt_h0) - 2.0 * mu / one_minus_mu2);
-            const double amu = fabs(mu);
-            if (amu < 2.0 * box.mu_cut) {
-                // the push's hand-over to the plain closure over [mu_cut, 2 mu_cut]
-                const double w = (amu - box.mu_cut) / box.mu_cut;
-                const double dw = sign / box.mu_cut;
-                dd = pdd + w * (dd - pdd) + dw * (d - pd);
-                d = pd + w * (d - pd);
-                lk = log(exp(plk) + w * (exp(lk) - exp(plk)));
-            }
-        } else {
-            d = pd;
-            dd = pdd;
-            lk = plk;
-        }
-        out[static_cast<size_t>(i) * kMlpOut + 0] = d;
-        out[static_cast<size_t>(i) * kMlpOut + 1] = dd;
-        out[static_cast<size_t>(i) * kMlpOut + 2] = lk;
-        served[i] = inside ? 1 : 0;
+        if (have) eval_store(i, raw, inside, y, box, out, served);
     }
+}
+
+// The tcgen05 engine: each block takes 128 inputs per trip (its rows), the
+// trip count uniform over the block.
+template <bool FP16, int H>
+__global__ void __launch_bounds__(128) eval_tc_kernel(int n, const double* __restrict__ in,
+                                                      SurrogateBox box,
+                                                      const uint4* __restrict__ block,
+                                                      double* __restrict__ out,
+                                                      int* __restrict__ served,
+                                                      unsigned int* __restrict__ timeouts) {
+    extern __shared__ __align__(128) unsigned char tc_smem[];
+    TcNet net = tc_setup<H>(block, tc_smem);
+    tc_constants<FP16, H>(net);
+    bool fail = false;
+    for (int base = blockIdx.x * 128; base < n; base += gridDim.x * 128) {
+        const int i = base + static_cast<int>(threadIdx.x);
+        const bool have = i < n;
+        double raw[kMlpIn];
+        float f[kMlpIn];
+        const bool inside = eval_features(i, have, in, box, raw, f);
+        float y[kMlpOut];
+        if (mlp_cta<FP16, H>(net, f, y, fail)) {
+            break;
+        }
+        if (have) eval_store(i, raw, inside, y, box, out, served);
+    }
+    fail = __syncthreads_or(fail ? 1 : 0) != 0;
+    if (fail && threadIdx.x == 0) {
+        atomicAdd(timeouts, 1u);
+    }
+    tc_teardown<H>(net, fail);
 }
 
 }  // namespace
@@ -409,22 +461,35 @@ cudaError_t gradient(const SurrogateTrainLaunch& L, cudaStream_t stream) {
 }
 
 template <int H>
-cudaError_t eval(int n, const double* inputs, const SurrogateBox& box, const float* params,
-                 const uint2* block, bool tensor, double* out, int* served,
-                 cudaStream_t stream) {
+cudaError_t eval(int n, const double* inputs, const SurrogateBox& box, const SurrogateServe& sv,
+                 double* out, int* served, cudaStream_t stream) {
     const int threads = 128;
     int blocks = (n + threads - 1) / threads;
+    if (sv.engine == kEngineTcgen05) {
+        // blocks beyond the 4 per SM whose TMEM fits wait in tcgen05.alloc
+        // until a resident block frees its columns
+        blocks = blocks < 1 ? 1 : (blocks > 152 * 4 ? 152 * 4 : blocks);
+        const size_t smem = tc_smem_bytes<H>();
+        if (box.fp16) {
+            eval_tc_kernel<true, H><<<blocks, threads, smem, stream>>>(
+                n, inputs, box, sv.tc_block, out, served, sv.timeouts);
+        } else {
+            eval_tc_kernel<false, H><<<blocks, threads, smem, stream>>>(
+                n, inputs, box, sv.tc_block, out, served, sv.timeouts);
+        }
+        return cudaGetLastError();
+    }
     blocks = blocks < 1 ? 1 : (blocks > 152 * 8 ? 152 * 8 : blocks);
     const size_t smem = Mlp<H>::SmemBytes;
-    if (tensor && box.fp16) {
-        eval_kernel<2, H><<<blocks, threads, smem, stream>>>(n, inputs, box, params, block, out,
-                                                             served);
-    } else if (tensor) {
-        eval_kernel<1, H><<<blocks, threads, smem, stream>>>(n, inputs, box, params, block, out,
-                                                             served);
+    if (sv.engine == kEngineMmaSync && box.fp16) {
+        eval_kernel<2, H><<<blocks, threads, smem, stream>>>(n, inputs, box, sv.params, sv.block,
+                                                             out, served);
+    } else if (sv.engine == kEngineMmaSync) {
+        eval_kernel<1, H><<<blocks, threads, smem, stream>>>(n, inputs, box, sv.params, sv.block,
+                                                             out, served);
     } else {
         eval_kernel<0, H><<<blocks, threads, Mlp<H>::Params * sizeof(float), stream>>>(
-            n, inputs, box, params, block, out, served);
+            n, inputs, box, sv.params, sv.block, out, served);
     }
     return cudaGetLastError();
 }
@@ -440,11 +505,10 @@ cudaError_t surrogate_gradient(const SurrogateTrainLaunch& L, cudaStream_t strea
 }
 
 cudaError_t surrogate_eval(int n, const double* inputs, const SurrogateBox& box,
-                           const float* params, const uint2* block, bool tensor, double* out,
-                           int* served, cudaStream_t stream) {
-    return box.hidden == 64 ? eval<64>(n, inputs, box, params, block, tensor, out, served, stream)
-                            : eval<32>(n, inputs, box, params, block, tensor, out, served,
-                                       stream);
+                           const SurrogateServe& serve, double* out, int* served,
+                           cudaStream_t stream) {
+    return box.hidden == 64 ? eval<64>(n, inputs, box, serve, out, served, stream)
+                            : eval<32>(n, inputs, box, serve, out, served, stream);
 }
 
 }  // namespace kpt

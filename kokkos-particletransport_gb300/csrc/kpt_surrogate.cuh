@@ -33,7 +33,7 @@ namespace kpt {
 
 constexpr int kMlpIn = 5;
 constexpr int kMlpOut = 3;
-constexpr int kMlpHiddenDefault = 32;
+constexpr int kMlpHiddenDefault = 64;
 
 // Parameter block, FP32: W1[H][5] b1[H] W2[H][H] b2[H] W3[3][H] b3[3].
 // Shared-memory block of the served network: 16-bit B fragments (one uint2
@@ -68,6 +68,40 @@ __host__ __device__ constexpr size_t mlp_smem_bytes(int hidden) {
 }
 constexpr size_t kSurrogateSmemMax = Mlp<64>::SmemBytes;
 
+// The same network served by the fifth-generation tensor cores (tcgen05),
+// CTA-collective: the 128 threads of a block are the M = 128 rows.  Weights
+// are the B operands in shared memory, K-major with no swizzle: 8-row x
+// 16-byte core matrices, W[n][k] at byte (n/8) SBO + (k/8) 128 + (n%8) 16 +
+// (k%8) 2 with SBO = K/8 x 128.  The biases ride in the GEMMs as two extra
+// inputs fixed at 1 whose weights are the bias split into a 16-bit head and
+// its 16-bit remainder (b = hi + lo to ~2^-16 relative): layer 1 is N = H x
+// K = 16 (inputs 0..4, bias 5..6), layer 2 N = H x K = H + 16 (bias at
+// H, H+1), layer 3 N = 16 x K = H + 16 (outputs 3..15 zero).  Activations
+// live in tensor memory: the A operand of each layer (H/2 columns of 16-bit
+// pairs, row = TMEM lane) followed by the constant block (one column of
+// (1, 1), seven of zeros), the hidden accumulators (H FP32 columns) and the
+// output accumulators (16 columns).
+template <int H>
+struct TcMlp {
+    static constexpr int K2 = H + 16;  // K of layers 2 and 3 (bias block included)
+    static constexpr int W1 = 0;
+    static constexpr int W2 = W1 + H * 16 * 2;
+    static constexpr int W3 = W2 + H * K2 * 2;
+    static constexpr int Bytes = W3 + 16 * K2 * 2;
+    static constexpr uint32_t ColA = 0;
+    static constexpr uint32_t ColOne = H / 2;  // constant block
+    static constexpr uint32_t ColD = H / 2 + 8;
+    static constexpr uint32_t ColOut = ColD + H;
+    static constexpr uint32_t Cols = 128;  // TMEM allocation (power of two >= ColOut + 16)
+    static_assert(ColOut + 16 <= Cols, "tensor-memory layout exceeds the allocation");
+};
+__host__ __device__ constexpr size_t tc_block_bytes(int hidden) {
+    return hidden == 64 ? TcMlp<64>::Bytes : TcMlp<32>::Bytes;
+}
+// Network engines of the push and of kpt_surrogate_evaluate.
+constexpr int kEngineTcgen05 = 0;  // CTA-collective tcgen05.mma, TMEM activations
+constexpr int kEngineMmaSync = 1;  // warp-collective mma.sync, register activations
+
 // Training box and normalisation of one trained network.
 struct SurrogateBox {
     float in_lo[kMlpIn];   // feature units (see above)
@@ -90,6 +124,8 @@ struct SurrogateBox {
 // {evaluations, judged, fallbacks, max relative error (float bits)}.
 struct SurrogateDevice {
     const uint2* block;
+    const uint4* tc_block;  // canonical-layout weights of the tcgen05 engine
+    int engine;             // kEngineTcgen05 or kEngineMmaSync
     SurrogateBox box;
     float f3, f4;
     int constants_in_box;
@@ -275,6 +311,304 @@ __device__ __forceinline__ void mlp_warp(const uint2* smem, const float (&f)[kMl
     y[0] = second ? (upper ? c0[1][2] : c0[1][0]) : (upper ? c0[0][2] : c0[0][0]);
     y[1] = second ? (upper ? c0[1][3] : c0[1][1]) : (upper ? c0[0][3] : c0[0][1]);
     y[2] = second ? (upper ? c2[1][1] : c2[1][0]) : (upper ? c2[0][1] : c2[0][0]);
+}
+
+// ------------------------------------------------------------ tcgen05
+// Shared-memory address of a generic pointer into shared memory.
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// Shared-memory matrix descriptor: start, leading (K-direction core-matrix)
+// and stride (MN-direction 8-row group) byte offsets, descriptor version 1,
+// no swizzle.
+__device__ __forceinline__ uint64_t tc_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return static_cast<uint64_t>((addr >> 4) & 0x3FFFu) |
+           (static_cast<uint64_t>((lbo >> 4) & 0x3FFFu) << 16) |
+           (static_cast<uint64_t>((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator, A and B both BF16
+// (or both FP16), both K-major, M = 128, N.
+__host__ __device__ constexpr uint32_t tc_idesc(bool fp16, int n) {
+    return (1u << 4) | ((fp16 ? 0u : 1u) << 7) | ((fp16 ? 0u : 1u) << 10) |
+           (static_cast<uint32_t>(n >> 3) << 17) | (static_cast<uint32_t>(128 >> 4) << 24);
+}
+
+// D[tmem] (+)= A[tmem] x B[smem]; accumulate = 0 overwrites D.
+__device__ __forceinline__ void tc_mma(uint32_t d, uint32_t a, uint64_t b, uint32_t idesc,
+                                       uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}"
+        :
+        : "r"(d), "r"(a), "l"(b), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+// Arrive on the mbarrier once every MMA this thread issued has completed.
+__device__ __forceinline__ void tc_commit(uint32_t mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                 :
+                 : "r"(mbar)
+                 : "memory");
+}
+
+// 16 consecutive FP32 columns of this thread's row, waited for.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+        "%11, %12, %13, %14, %15}, [%16];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+          "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+#pragma unroll
+    for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
+}
+
+__device__ __forceinline__ void tmem_ld4(uint32_t taddr, float (&v)[4]) {
+    uint32_t r[4];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+        : "r"(taddr)
+        : "memory");
+#pragma unroll
+    for (int k = 0; k < 4; ++k) v[k] = __uint_as_float(r[k]);
+}
+
+// 8 consecutive 32-bit columns of this thread's row, waited for.
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const uint32_t (&v)[8]) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};\n\t"
+        "tcgen05.wait::st.sync.aligned;"
+        :
+        : "r"(taddr), "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]),
+          "r"(v[6]), "r"(v[7])
+        : "memory");
+}
+
+// Completion waits give up after this many polls (each poll may suspend the
+// thread for a while); the block then reports the timeout and stops.
+#ifndef KPT_TC_WAIT_POLLS
+#define KPT_TC_WAIT_POLLS (1u << 20)
+#endif
+
+#ifndef KPT_TC_WAIT_MODE
+#define KPT_TC_WAIT_MODE 0
+#endif
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+    for (uint32_t i = 0; i < KPT_TC_WAIT_POLLS; ++i) {
+        uint32_t done;
+#if KPT_TC_WAIT_MODE == 1
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(mbar), "r"(parity)
+            : "memory");
+#elif KPT_TC_WAIT_MODE == 2
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(mbar), "r"(parity), "r"(200)
+            : "memory");
+#else
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(mbar), "r"(parity)
+            : "memory");
+#endif
+        if (done) return true;
+    }
+    return false;
+}
+
+// One block's tensor-core network: TMEM base, shared-memory weights and the
+// completion barrier with the parity of its next phase.
+struct TcNet {
+    uint32_t tmem;
+    uint32_t w;
+    uint32_t mbar;
+    uint32_t phase;
+};
+
+// Shared-memory footprint of the tcgen05 engine: weights, then the
+// mbarrier (8 B) and the TMEM address slot (4 B).
+template <int H>
+__host__ __device__ constexpr size_t tc_smem_bytes() {
+    return static_cast<size_t>(TcMlp<H>::Bytes) + 16;
+}
+
+// Block prologue (all threads): weights to shared memory, barrier init,
+// TMEM allocation by warp 0.
+template <int H>
+__device__ __forceinline__ TcNet tc_setup(const uint4* __restrict__ block, unsigned char* smem) {
+    using T = TcMlp<H>;
+    uint4* w = reinterpret_cast<uint4*>(smem);
+    for (int k = threadIdx.x; k < T::Bytes / 16; k += blockDim.x) w[k] = block[k];
+    const uint32_t mbar = smem_u32(smem + T::Bytes);
+    const uint32_t slot = smem_u32(smem + T::Bytes + 8);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" : : "r"(mbar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (threadIdx.x < 32) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     :
+                     : "r"(slot), "r"(T::Cols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    // weights written by generic stores become visible to the tensor cores
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    TcNet net;
+    net.tmem = *reinterpret_cast<volatile uint32_t*>(smem + T::Bytes + 8);
+    net.w = smem_u32(smem);
+    net.mbar = mbar;
+    net.phase = 0;
+    return net;
+}
+
+// Write this thread's row of the constant block (after tc_setup).
+template <bool FP16, int H>
+__device__ __forceinline__ void tc_constants(const TcNet& net) {
+    const uint32_t row = (threadIdx.x & 0x60u) << 16;
+    const uint32_t ones[8] = {pack_x2<FP16>(1.0f, 1.0f), 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+    tmem_st8(net.tmem + row + TcMlp<H>::ColOne, ones);
+}
+
+// Block epilogue (all threads, uniform): after a timeout, wait once more
+// (bounded) for the MMAs in flight; then warp 0 frees the TMEM.
+template <int H>
+__device__ __forceinline__ void tc_teardown(const TcNet& net, bool failed) {
+    if (failed && threadIdx.x == 0) {
+        mbar_wait(net.mbar, net.phase ^ 1u);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (threadIdx.x < 32) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;"
+                     :
+                     : "r"(net.tmem), "r"(TcMlp<H>::Cols)
+                     : "memory");
+    }
+}
+
+// Block-wide hand-over to the MMA issuer: TMEM stores ordered before the
+// barrier, the failure flag made uniform.  Returns false (for every thread)
+// once any thread has failed.
+__device__ __forceinline__ bool tc_sync(bool& fail) {
+    tc_fence_before();
+    fail = __syncthreads_or(fail ? 1 : 0) != 0;
+    tc_fence_after();
+    return !fail;
+}
+
+// Wait for the MMAs of the current phase.
+__device__ __forceinline__ void tc_complete(TcNet& net, bool& fail) {
+    if (!mbar_wait(net.mbar, net.phase)) fail = true;
+    net.phase ^= 1u;
+    tc_fence_after();
+}
+
+// Hidden-layer epilogue of this thread's row: accumulators (bias included)
+// -> activation -> 16-bit pairs, the next layer's A operand.
+template <bool FP16, int H>
+__device__ __forceinline__ void tc_hidden(uint32_t td, uint32_t ta) {
+#pragma unroll
+    for (int c = 0; c < H / 16; ++c) {
+        float acc[16];
+        tmem_ld16(td + 16 * c, acc);
+        uint32_t a[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) a[j] = act_x2<FP16>(acc[2 * j], acc[2 * j + 1]);
+        tmem_st8(ta + 8 * c, a);
+    }
+}
+
+// Block-collective forward pass: every thread of the block calls it (block
+// converged); thread r supplies row r (its five normalised features; zeros
+// for an idle thread) and receives the three normalised outputs of row r.
+// Returns true when the block stops (a completion wait timed out: fail is
+// then set in every thread); the outputs are then undefined.
+template <bool FP16, int H>
+__device__ __forceinline__ bool mlp_cta(TcNet& net, const float (&f)[kMlpIn],
+                                        float (&y)[kMlpOut], bool& fail) {
+    using T = TcMlp<H>;
+    // warp w of the block owns TMEM lanes 32 w .. 32 w + 31
+    const uint32_t row = (threadIdx.x & 0x60u) << 16;
+    const uint32_t ta = net.tmem + row + T::ColA;
+    const uint32_t td = net.tmem + row + T::ColD;
+    const uint32_t a_op = net.tmem + T::ColA;
+    const uint32_t d_op = net.tmem + T::ColD;
+    const bool issuer = threadIdx.x == 0;
+    {
+        // inputs 0..4, then 1, 1 for the layer-1 bias head and remainder
+        const uint32_t in[8] = {pack_x2<FP16>(f[0], f[1]), pack_x2<FP16>(f[2], f[3]),
+                                pack_x2<FP16>(f[4], 1.0f), pack_x2<FP16>(1.0f, 0.0f),
+                                0u, 0u, 0u, 0u};
+        tmem_st8(ta, in);
+    }
+    // layer 1: K = 16
+    if (!tc_sync(fail)) return true;
+    if (issuer) {
+        tc_mma(d_op, a_op, tc_desc(net.w + T::W1, 128, 256), tc_idesc(FP16, H), 0u);
+        tc_commit(net.mbar);
+    }
+    tc_complete(net, fail);
+    tc_hidden<FP16, H>(td, ta);
+    // layer 2: K = H + 16 in steps of 16, the last step the bias block
+    if (!tc_sync(fail)) return true;
+    if (issuer) {
+#pragma unroll
+        for (int s = 0; s < T::K2 / 16; ++s) {
+            tc_mma(d_op, a_op + 8 * s, tc_desc(net.w + T::W2 + 256 * s, 128, 16 * T::K2),
+                   tc_idesc(FP16, H), s > 0 ? 1u : 0u);
+        }
+        tc_commit(net.mbar);
+    }
+    tc_complete(net, fail);
+    tc_hidden<FP16, H>(td, ta);
+    // layer 3: N = 16, K = H + 16
+    if (!tc_sync(fail)) return true;
+    if (issuer) {
+#pragma unroll
+        for (int s = 0; s < T::K2 / 16; ++s) {
+            tc_mma(net.tmem + T::ColOut, a_op + 8 * s,
+                   tc_desc(net.w + T::W3 + 256 * s, 128, 16 * T::K2), tc_idesc(FP16, 16),
+                   s > 0 ? 1u : 0u);
+        }
+        tc_commit(net.mbar);
+    }
+    tc_complete(net, fail);
+    float o[4];
+    tmem_ld4(net.tmem + row + T::ColOut, o);
+#pragma unroll
+    for (int k = 0; k < kMlpOut; ++k) y[k] = o[k];
+    return false;
 }
 
 #endif  // __CUDACC__

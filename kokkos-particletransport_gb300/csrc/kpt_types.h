@@ -89,6 +89,8 @@ struct PushCounters {
     unsigned long long failed;
     unsigned int max_steps;
     unsigned int next_particle;  // work-queue cursor
+    unsigned int network_timeouts;  // blocks stopped by a tensor-core completion timeout
+    unsigned int pad;
 };
 
 }  // namespace kpt

@@ -4,11 +4,20 @@
   (oracle/surrogate_ref.py, itself pinned to finite differences).
 * The FP32 forward against the CPU reference on the trained parameters, the
   BF16 and FP16 tensor-core forwards (the ones fused into the push) against
-  the plain closure, for hidden widths 32 (the default) and 64, and the
+  the plain closure, for hidden widths 64 (the default) and 32, and the
   plain-closure fallback outside the box.
-* The mixed focused push served by the network against the FP64 oracle with
-  the plain closure: momentum spectrum L1 <= 1 %, chi-square p > 0.01, and
-  the in-kernel judge's record of the network's per-step error.
+* The two engines that serve the network (block-collective tcgen05 with
+  activations in tensor memory, the default; warp-collective mma.sync) on
+  the same trained weights: the same inputs served, outputs equal to FP32
+  rounding (the tensor cores associate the sums differently and the
+  tcgen05 engine carries the biases as 16-bit head + remainder inputs of
+  the GEMMs, so a 16-bit activation can round the other way: median
+  relative difference <= 2e-5, every output within 3 %), and the same
+  accuracy against the plain closure.
+* The mixed focused push served by the network, on either engine, against
+  the FP64 oracle with the plain closure: momentum spectrum L1 <= 1 %,
+  chi-square p > 0.01, and the in-kernel judge's record of the network's
+  per-step error.
 """
 from __future__ import annotations
 
@@ -26,7 +35,8 @@ TRAIN = dict(samples=524288, steps=8000, batch=4096, learning_rate=1e-2, seed=20
 def _train(ctx, kpt, binding, element_type):
     params = binding.default_params(kperp_over_kpara=0.05, focused=1, closure=2)
     settings = kpt.settings_from_dict(params)
-    return params, settings, ctx.train_surrogate(settings, element_type=element_type, **TRAIN)
+    return params, settings, ctx.train_surrogate(settings, element_type=element_type,
+                                                 hidden_width=32, **TRAIN)
 
 
 @pytest.fixture(scope="module")
@@ -140,6 +150,33 @@ def test_trained_network_forward_and_accuracy(trained, trained16, trained64, wid
     assert p99["fp16"] < p99["fp16-net fp32"] + 0.01
 
 
+@pytest.mark.parametrize("net", ["trained", "trained16", "trained64"])
+def test_engines_agree(kpt, net, request):
+    params, _, surrogate = request.getfixturevalue(net)
+    _, norm = surrogate.parameters()
+    rng = np.random.default_rng(17)
+    inputs = _box_inputs(rng, 20000, norm)  # 156 blocks of 128 and a ragged one
+    inputs[:50, 0] *= 1e-3  # some below mu_cut: the plain closure
+    outs = {}
+    try:
+        for engine in (kpt.ENGINE_TCGEN05, kpt.ENGINE_MMA_SYNC):
+            surrogate.engine = engine
+            outs[engine] = surrogate.evaluate(inputs)
+    finally:
+        surrogate.engine = kpt.ENGINE_TCGEN05
+    (tc, served_tc), (warp, served_warp) = outs[kpt.ENGINE_TCGEN05], outs[kpt.ENGINE_MMA_SYNC]
+    assert np.array_equal(served_tc, served_warp)
+    assert not served_tc[:50].any() and served_tc[50:].all()
+    np.testing.assert_array_equal(tc[:50], warp[:50])
+    for c in range(3):
+        scale = np.abs(warp[:, c]) if c == 0 else np.abs(warp[:, c]).max()
+        rel = np.abs(tc[:, c] - warp[:, c]) / scale
+        assert np.median(rel) <= 2e-5, (c, np.median(rel))
+        assert rel.max() <= 3e-2, (c, rel.max())
+    p99 = [np.quantile(_errors(params, inputs[50:], out[50:])[0], 0.99) for out in (tc, warp)]
+    assert p99[0] <= p99[1] + 0.005, p99
+
+
 def test_fallback_outside_the_box_is_the_plain_closure(trained):
     params, _, surrogate = trained
     _, norm = surrogate.parameters()
@@ -159,9 +196,12 @@ def test_fallback_outside_the_box_is_the_plain_closure(trained):
         assert np.allclose(out[:, 2], lk, rtol=0, atol=1e-12)
 
 
+@pytest.mark.parametrize("engine", ["tcgen05", "mma_sync"])
 @pytest.mark.parametrize("net", ["trained", "trained16", "trained64"])
-def test_surrogate_push_matches_fp64_spectrum(ctx, kpt, oracle, binding, fields_mod, net, request):
+def test_surrogate_push_matches_fp64_spectrum(ctx, kpt, oracle, binding, fields_mod, net, engine,
+                                              request):
     params, settings, surrogate = request.getfixturevalue(net)
+    surrogate.engine = kpt.ENGINE_TCGEN05 if engine == "tcgen05" else kpt.ENGINE_MMA_SYNC
     ye = fields_mod.stretched_edges(128, -2.0, 2.0)
     f0 = fields_mod.harris_field(64, 128, y_edges=ye, island_amplitude=0.1, noise=0.01, seed=5)
     f1 = fields_mod.harris_field(64, 128, y_edges=ye, island_amplitude=0.1, noise=0.01, seed=6)
@@ -208,6 +248,7 @@ def test_surrogate_push_matches_fp64_spectrum(ctx, kpt, oracle, binding, fields_
     other = kpt.settings_from_dict(dict(params, kpara0=params["kpara0"] * 2))
     with pytest.raises(kpt.KptError, match="trained"):
         ctx.push_interval(parts, lower, upper, other, frame, seed)
+    surrogate.engine = kpt.ENGINE_TCGEN05
     for f in (lower, upper):
         f.close()
     parts.close()
