@@ -62,7 +62,7 @@ def tensor_flop_per_step(hidden: int) -> int:
     """Tensor flops of one network evaluation (one particle-step): K = 16
     padded input layer, H x H hidden layer, 8-column padded output layer."""
     return 2 * (16 * hidden + hidden * hidden + hidden * 8)
-PROFILE = os.path.join(ROOT, "profiles", "push_refill_surrogate_focused_1024x2048.md")
+PROFILE = os.path.join(ROOT, "profiles", "push_tc_surrogate_focused_1024x2048.md")
 
 
 def make_workload():
