@@ -713,7 +713,7 @@ def main():
     parser.add_argument("--hidden-width", type=int, default=64, choices=(32, 64),
                         help="hidden width of the headline network (a BF16 network of the "
                              "other width is measured beside it)")
-    parser.add_argument("--sort-tile", type=int, default=16,
+    parser.add_argument("--sort-tile", type=int, default=8,
                         help="cell-sort tile (cells) before each push; 0 disables")
     args = parser.parse_args()
     rank = int(os.environ.get("RANK", "0"))
