@@ -174,19 +174,31 @@ def _barrier():
     if WORLD > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.synchronize()
+        if torch.cuda.is_available():
+            torch.cuda.synchronize()
         dist.barrier()
 
 
 def _reduce(value: float, op: str) -> float:
-    """Whole-job aggregate over the ranks (max of times, sum of work)."""
+    """Whole-job aggregate over the ranks (max of times, sum of work); the
+    value travels on the GPU under NCCL, on the host under gloo."""
     if WORLD == 1:
         return value
     import torch
     import torch.distributed as dist
-    t = torch.tensor([value], dtype=torch.float64, device=f"cuda:{DEVICE}")
+    device = f"cuda:{DEVICE}" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
     return float(t.item())
+
+
+def whole_job(total_ms: float, particle_steps: float):
+    """Replicas (one process per GPU, no data-path collective): the job's
+    throughput is all ranks' particle-steps over the slowest rank's time.
+    Returns (particle-steps/s, slowest total ms)."""
+    slowest = _reduce(total_ms, "max")
+    steps = _reduce(float(particle_steps), "sum")
+    return steps / (slowest / 1e3), slowest
 
 
 def _spectrum(p, w, status, nbins=64, pmin=1e-2, pmax=1e1):
@@ -766,9 +778,8 @@ def main():
     achieved = steps_per_launch * BYTES_PER_STEP["focused_mixed"] / kernel_s / 1e9
     per_step_traffic = profiled_traffic()
     # whole-job value: all ranks' particle-steps over the slowest rank's time
-    total_ms = _reduce(head["ms_per_step"] * head["steps"], "max")
-    total_steps = _reduce(float(head["particle_steps"]), "sum")
-    head["value"] = total_steps / (total_ms / 1e3)
+    head["value"], total_ms = whole_job(head["ms_per_step"] * head["steps"],
+                                        head["particle_steps"])
     head["ms_per_step"] = total_ms / head["steps"]
     head["e2e"] = _reduce(head["e2e"], "sum")
     if WORLD > 1 and rank != 0:
