@@ -1191,11 +1191,22 @@ class ParticleStorage:
         _check(self.ctx.lib.kpt_particles_upload(self.handle, int(count),
                                                  *[_ptr(conv[n]) for n in PARTICLE_FIELDS]))
 
-    def download(self, count: Optional[int] = None) -> Dict[str, np.ndarray]:
+    def download(self, count: Optional[int] = None,
+                 out: Optional[Dict[str, np.ndarray]] = None) -> Dict[str, np.ndarray]:
+        """The first `count` particles (default: all stored), into new arrays or
+        into `out` (contiguous arrays of the field dtypes, at least count long,
+        e.g. views of pinned host memory)."""
         n = self.count if count is None else int(count)
-        out = {name: np.zeros(n, dtype=np.float64) for name in PARTICLE_FIELDS[:7]}
-        out["status"] = np.zeros(n, dtype=np.int32)
-        out["level"] = np.zeros(n, dtype=np.int32)
+        if out is None:
+            out = {name: np.zeros(n, dtype=np.float64) for name in PARTICLE_FIELDS[:7]}
+            out["status"] = np.zeros(n, dtype=np.int32)
+            out["level"] = np.zeros(n, dtype=np.int32)
+        for name in PARTICLE_FIELDS:
+            dtype = np.int32 if name in ("status", "level") else np.float64
+            a = out[name]
+            if a.dtype != dtype or not a.flags.c_contiguous or a.shape[0] < n:
+                raise KptError(f"download: out[{name!r}] must be contiguous {dtype.__name__} "
+                               f"of length >= {n}")
         _check(self.ctx.lib.kpt_particles_download(self.handle, n,
                                                    *[_ptr(out[k]) for k in PARTICLE_FIELDS]))
         return out
