@@ -252,3 +252,44 @@ def test_surrogate_push_matches_fp64_spectrum(ctx, kpt, oracle, binding, fields_
     for f in (lower, upper):
         f.close()
     parts.close()
+
+
+@pytest.mark.parametrize("net", ["trained64", "trained"])
+def test_tcgen05_push_does_not_depend_on_the_schedule(ctx, kpt, fields_mod, net, request):
+    """Each particle's row of the block-collective GEMMs is computed alone
+    (no row sees another), and the noise is keyed by particle: the same
+    population pushed unsorted, cell-sorted, and with 1 or 2 blocks per SM
+    (other rows beside every particle, other lockstep partners) ends bit for
+    bit the same."""
+    _, settings, surrogate = request.getfixturevalue(net)
+    assert surrogate.engine == kpt.ENGINE_TCGEN05
+    ye = fields_mod.stretched_edges(128, -2.0, 2.0)
+    f0 = fields_mod.harris_field(64, 128, y_edges=ye, island_amplitude=0.1, noise=0.01, seed=5)
+    f1 = fields_mod.harris_field(64, 128, y_edges=ye, island_amplitude=0.1, noise=0.01, seed=6)
+    lower = ctx.field(f0, kpt.TABLE_FOCUSED21, kpt.PRECISION_MIXED)
+    upper = ctx.field(f1, kpt.TABLE_FOCUSED21, kpt.PRECISION_MIXED)
+    ctx.set_surrogate(surrogate)
+    n = 5000
+    parts = ctx.particles(n)
+    ctx.inject(parts, lower, settings, n, 7, 99)
+    start = parts.download(n)
+    results = []
+    try:
+        for sort, blocks in ((False, 0), (True, 0), (True, 1), (False, 2)):
+            ctx.set_push_schedule(kpt.SCHEDULE_REFILL, blocks)
+            parts.upload(start, n)
+            if sort:
+                ctx.sort(parts, lower, 8, 8)
+            stats = ctx.push_interval(parts, lower, upper, settings, 7, 99)
+            results.append((parts.download(n), stats.particle_steps))
+    finally:
+        ctx.set_push_schedule(kpt.SCHEDULE_REFILL, 0)
+    base, steps = results[0]
+    assert steps > 0
+    for other, other_steps in results[1:]:
+        assert other_steps == steps
+        for name in base:
+            assert np.array_equal(base[name], other[name]), name
+    for f in (lower, upper):
+        f.close()
+    parts.close()
