@@ -270,6 +270,14 @@ int kpt_surrogate_evaluate(kpt_surrogate* surrogate, uint64_t n, const double* i
  * differently, so results agree to FP32 rounding, not bit for bit. */
 int kpt_surrogate_set_engine(kpt_surrogate* surrogate, int engine);
 int kpt_surrogate_get_engine(const kpt_surrogate* surrogate, int32_t* engine);
+/* Failure-path check of the tcgen05 engine, no fault involved: `blocks`
+ * blocks set up the width-64 network (weights, completion barrier, tensor
+ * memory), wait `polls` polls for a completion that nothing signals, and
+ * tear down as a timed-out push does (bounded second wait, tensor memory
+ * freed).  timed_out / finished receive the blocks that reported the
+ * timeout / got past the teardown (both = blocks when the bounds work). */
+int kpt_surrogate_check_timeout(kpt_surrogate* surrogate, uint32_t blocks, uint32_t polls,
+                                uint32_t* timed_out, uint32_t* finished);
 /* Parameter block (FP32, W1[H][5] b1[H] W2[H][H] b2[H] W3[3][H] b3[3]:
  * 1379 floats for H = 32, 4739 for H = 64) and the box
  * normalisation (in_lo[5], in_hi[5], out_offset[3], out_scale[3], mu_cut);

@@ -256,6 +256,7 @@ def load_library() -> ctypes.CDLL:
         "kpt_surrogate_shape": (i32, [vp, vp, vp]),
         "kpt_surrogate_set_engine": (i32, [vp, i32]),
         "kpt_surrogate_get_engine": (i32, [vp, vp]),
+        "kpt_surrogate_check_timeout": (i32, [vp, u32, u32, vp, vp]),
         "kpt_context_set_surrogate": (i32, [vp, vp]),
         "kpt_surrogate_judge": (i32, [vp, vp, vp, vp, vp]),
         "kpt_grid_create": (i32, [vp, i32, i32, vp, vp, vp, pvp]),
@@ -831,6 +832,15 @@ class Surrogate:
     @engine.setter
     def engine(self, value: int) -> None:
         _check(self.ctx.lib.kpt_surrogate_set_engine(self.handle, int(value)))
+
+    def check_timeout(self, blocks: int = 8, polls: int = 64):
+        """(blocks that timed out, blocks that finished the teardown) of the
+        tcgen05 engine's failure-path check (kpt_surrogate_check_timeout)."""
+        timed_out, finished = ctypes.c_uint32(), ctypes.c_uint32()
+        _check(self.ctx.lib.kpt_surrogate_check_timeout(self.handle, int(blocks), int(polls),
+                                                        ctypes.byref(timed_out),
+                                                        ctypes.byref(finished)))
+        return int(timed_out.value), int(finished.value)
 
     def evaluate(self, inputs: np.ndarray, tensor_cores: bool = True):
         """(n, 5) raw inputs (mu, ln p, ln|B|, dB^2/B^2, gamma_k) ->

@@ -1667,6 +1667,27 @@ int kpt_surrogate_set_engine(kpt_surrogate* sg, int engine) {
     return KPT_OK;
 }
 
+int kpt_surrogate_check_timeout(kpt_surrogate* sg, uint32_t blocks, uint32_t polls,
+                                uint32_t* timed_out, uint32_t* finished) {
+    KPT_REQUIRE(sg != nullptr, "kpt_surrogate_check_timeout: NULL handle");
+    KPT_REQUIRE(sg->box.hidden == 64, "kpt_surrogate_check_timeout: needs a width-64 network");
+    KPT_REQUIRE(blocks >= 1 && blocks <= 4096, "kpt_surrogate_check_timeout: 1 <= blocks <= 4096");
+    KPT_REQUIRE(polls >= 1 && polls <= (1u << 20), "kpt_surrogate_check_timeout: 1 <= polls <= 2^20");
+    KPT_CUDA(cudaSetDevice(sg->device));
+    cudaStream_t st = sg->ctx->stream;
+    ScopedBuffer buf;
+    KPT_CUDA(buf.reserve(2 * sizeof(unsigned int)));
+    KPT_CUDA(cudaMemsetAsync(buf.ptr, 0, 2 * sizeof(unsigned int), st));
+    KPT_CUDA(kpt::surrogate_tc_timeout_check(sg->d_tc_block, static_cast<int>(blocks), polls,
+                                             buf.as<unsigned int>(), st));
+    unsigned int host[2] = {0, 0};
+    KPT_CUDA(cudaMemcpyAsync(host, buf.ptr, sizeof(host), cudaMemcpyDeviceToHost, st));
+    KPT_CUDA(cudaStreamSynchronize(st));
+    if (timed_out) *timed_out = host[0];
+    if (finished) *finished = host[1];
+    return KPT_OK;
+}
+
 int kpt_surrogate_get_engine(const kpt_surrogate* sg, int32_t* engine) {
     KPT_REQUIRE(sg && engine, "kpt_surrogate_get_engine: NULL argument");
     *engine = sg->engine;

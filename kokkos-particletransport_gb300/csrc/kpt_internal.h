@@ -206,6 +206,10 @@ struct SurrogateServe {
 cudaError_t surrogate_eval(int n, const double* inputs, const SurrogateBox& box,
                            const SurrogateServe& serve, double* out, int* served,
                            cudaStream_t stream);
+// out[0]: blocks whose bounded completion wait timed out; out[1]: blocks that
+// finished their teardown (a width-64 block of weights).
+cudaError_t surrogate_tc_timeout_check(const uint4* block, int blocks, uint32_t polls,
+                                       unsigned int* out, cudaStream_t stream);
 
 // ---- header library (ParkerSolver / ParticleSystem), 2D Cartesian ---------
 // One axis of an analytic uniform grid (AnalyticCoordinateGrid.hpp) with the

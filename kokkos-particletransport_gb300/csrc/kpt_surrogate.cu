@@ -425,7 +425,35 @@ __global__ void __launch_bounds__(128) eval_tc_kernel(int n, const double* __res
     tc_teardown<H>(net, fail);
 }
 
+// The failure path of the tcgen05 engine without a fault: every block sets
+// up its network (weights, barrier, 128 TMEM columns), waits for a
+// completion that nothing will signal (no MMA is issued) with `polls`
+// polls, records the timeout, and tears down as a timed-out push block does
+// (a second bounded wait, then the TMEM is freed).
+__global__ void __launch_bounds__(128) tc_timeout_check_kernel(const uint4* __restrict__ block,
+                                                               uint32_t polls,
+                                                               unsigned int* __restrict__ out) {
+    extern __shared__ __align__(128) unsigned char tc_smem[];
+    TcNet net = tc_setup<64>(block, tc_smem);
+    bool fail = !mbar_wait(net.mbar, net.phase, polls);
+    net.phase ^= 1u;
+    fail = __syncthreads_or(fail ? 1 : 0) != 0;
+    if (fail && threadIdx.x == 0) {
+        atomicAdd(out, 1u);
+    }
+    tc_teardown<64>(net, fail, polls);
+    if (threadIdx.x == 0) {
+        atomicAdd(out + 1, 1u);  // blocks that got past the teardown
+    }
+}
+
 }  // namespace
+
+cudaError_t surrogate_tc_timeout_check(const uint4* block, int blocks, uint32_t polls,
+                                       unsigned int* out, cudaStream_t stream) {
+    tc_timeout_check_kernel<<<blocks, 128, tc_smem_bytes<64>(), stream>>>(block, polls, out);
+    return cudaGetLastError();
+}
 
 cudaError_t surrogate_make_samples(uint64_t seed, int n, const SurrogateBox& box, float* x,
                                    float* t, cudaStream_t stream) {

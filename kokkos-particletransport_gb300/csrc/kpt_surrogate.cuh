@@ -425,29 +425,10 @@ __device__ __forceinline__ void tmem_st8(uint32_t taddr, const uint32_t (&v)[8])
 #define KPT_TC_WAIT_POLLS (1u << 20)
 #endif
 
-#ifndef KPT_TC_WAIT_MODE
-#define KPT_TC_WAIT_MODE 0
-#endif
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
-    for (uint32_t i = 0; i < KPT_TC_WAIT_POLLS; ++i) {
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity,
+                                          uint32_t polls = KPT_TC_WAIT_POLLS) {
+    for (uint32_t i = 0; i < polls; ++i) {
         uint32_t done;
-#if KPT_TC_WAIT_MODE == 1
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(done)
-            : "r"(mbar), "r"(parity)
-            : "memory");
-#elif KPT_TC_WAIT_MODE == 2
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
-            "selp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(done)
-            : "r"(mbar), "r"(parity), "r"(200)
-            : "memory");
-#else
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
             "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
@@ -455,7 +436,6 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
             : "=r"(done)
             : "r"(mbar), "r"(parity)
             : "memory");
-#endif
         if (done) return true;
     }
     return false;
@@ -521,9 +501,10 @@ __device__ __forceinline__ void tc_constants(const TcNet& net) {
 // Block epilogue (all threads, uniform): after a timeout, wait once more
 // (bounded) for the MMAs in flight; then warp 0 frees the TMEM.
 template <int H>
-__device__ __forceinline__ void tc_teardown(const TcNet& net, bool failed) {
+__device__ __forceinline__ void tc_teardown(const TcNet& net, bool failed,
+                                            uint32_t polls = KPT_TC_WAIT_POLLS) {
     if (failed && threadIdx.x == 0) {
-        mbar_wait(net.mbar, net.phase ^ 1u);
+        mbar_wait(net.mbar, net.phase ^ 1u, polls);
     }
     tc_fence_before();
     __syncthreads();

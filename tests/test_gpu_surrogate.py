@@ -293,3 +293,18 @@ def test_tcgen05_push_does_not_depend_on_the_schedule(ctx, kpt, fields_mod, net,
     for f in (lower, upper):
         f.close()
     parts.close()
+
+
+def test_tcgen05_completion_wait_is_bounded(trained64, kpt):
+    """A completion that never comes (no MMA issued): every block gives up
+    after its bounded wait, reports it, frees its tensor memory and returns;
+    the engine then serves the network as before."""
+    params, _, surrogate = trained64
+    timed_out, finished = surrogate.check_timeout(blocks=8, polls=64)
+    assert (timed_out, finished) == (8, 8)
+    _, norm = surrogate.parameters()
+    inputs = _box_inputs(np.random.default_rng(2), 1000, norm)
+    out, served = surrogate.evaluate(inputs)
+    assert served.all() and np.isfinite(out).all()
+    with pytest.raises(kpt.KptError, match="polls"):
+        surrogate.check_timeout(blocks=1, polls=0)
