@@ -56,12 +56,12 @@ METRIC = "particle-steps/s, 1 GB300: mixed+surrogate vs plain FP64 at <=1% spect
 # algorithmic table bytes per particle-step: 2 frames x 4 corners x comps x 8|4 B
 BYTES_PER_STEP = {"focused_mixed": 2 * 4 * 21 * 4, "focused_f64": 2 * 4 * 21 * 8,
                   "parker_mixed": 2 * 4 * 16 * 4, "parker_f64": 2 * 4 * 16 * 8}
-# tensor-core work of the fused network per particle-step (padded mma tiles:
-# K 5 -> 16 and N 3 -> 8): 2 x (16 x 64 + 64 x 64 + 64 x 8) flop
 def tensor_flop_per_step(hidden: int) -> int:
-    """Tensor flops of one network evaluation (one particle-step): K = 16
-    padded input layer, H x H hidden layer, 8-column padded output layer."""
-    return 2 * (16 * hidden + hidden * hidden + hidden * 8)
+    """Tensor flops of one network evaluation (one particle-step) on the
+    tcgen05 engine, as issued: layer 1 K = 16 (5 inputs, 2 bias inputs,
+    padding) x N = H, layer 2 K = H + 16 (the bias block) x N = H, layer 3
+    K = H + 16 x N = 16 (3 outputs, padding): 14 848 flop at H = 64."""
+    return 2 * (16 * hidden + (hidden + 16) * hidden + (hidden + 16) * 16)
 PROFILE = os.path.join(ROOT, "profiles", "push_tc_surrogate_focused_1024x2048.md")
 
 
