@@ -1306,41 +1306,39 @@ PushParams make_push_params(const PushLaunch& L) {
     return P;
 }
 
-// Persistent grid of the tcgen05 push: at most 4 resident blocks per SM
-// (each holds TcMlp<H>::Cols of the SM's 512 TMEM columns); if the kernel's
-// registers would let more blocks in, the dynamic shared memory is padded
-// until they do not.
+// Persistent grid of the tcgen05 push: 4 blocks per SM, the number whose
+// TMEM (TcMlp<H>::Cols each) fills the SM's 512 columns.  The occupancy
+// query reports 1 block per SM for this kernel, so the register bound is
+// computed from the kernel's attributes instead: should the registers ever
+// admit more than 4 blocks, the dynamic shared memory is padded until they
+// do not (a fifth block would only wait in tcgen05.alloc).
 template <bool FP16, int H>
 cudaError_t launch_push_tc(const PushParams& P, const PushLaunch& L, cudaStream_t stream) {
     const int threads = 128;
     constexpr int kTmemBlocks = 512 / static_cast<int>(TcMlp<H>::Cols);
     size_t smem = tc_smem_bytes<H>();
-    int resident = 0;
-    cudaError_t err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &resident, push_tc_kernel<FP16, H>, threads, smem);
+    cudaFuncAttributes attr{};
+    cudaError_t err = cudaFuncGetAttributes(&attr, push_tc_kernel<FP16, H>);
     if (err != cudaSuccess) return err;
-    if (resident > kTmemBlocks) {
+    const int regs = attr.numRegs > 0 ? attr.numRegs : 1;
+    if (65536 / (regs * threads) > kTmemBlocks) {
         int device = 0, per_sm_smem = 0;
         err = cudaGetDevice(&device);
         if (err != cudaSuccess) return err;
         err = cudaDeviceGetAttribute(&per_sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor,
                                      device);
         if (err != cudaSuccess) return err;
-        smem = static_cast<size_t>(per_sm_smem) / (kTmemBlocks + 1) + 1;
-        err = cudaFuncSetAttribute(push_tc_kernel<FP16, H>,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   static_cast<int>(smem));
-        if (err != cudaSuccess) return err;
-        err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, push_tc_kernel<FP16, H>,
-                                                            threads, smem);
-        if (err != cudaSuccess) return err;
+        const size_t padded = static_cast<size_t>(per_sm_smem) / (kTmemBlocks + 1) + 1;
+        if (padded > smem) {
+            smem = padded;
+            err = cudaFuncSetAttribute(push_tc_kernel<FP16, H>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(smem));
+            if (err != cudaSuccess) return err;
+        }
     }
-    // the grid asks for the TMEM budget's blocks per SM whatever the
-    // occupancy query says (blocks that are not resident start when others
-    // finish and find the cursor further on)
-    resident = kTmemBlocks;
     const int per_sm =
-        L.blocks_per_sm > 0 && L.blocks_per_sm < resident ? L.blocks_per_sm : resident;
+        L.blocks_per_sm > 0 && L.blocks_per_sm < kTmemBlocks ? L.blocks_per_sm : kTmemBlocks;
     push_tc_kernel<FP16, H><<<L.sm_count * per_sm, threads, smem, stream>>>(P);
     return cudaGetLastError();
 }
