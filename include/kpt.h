@@ -278,6 +278,18 @@ int kpt_surrogate_get_engine(const kpt_surrogate* surrogate, int32_t* engine);
  * timeout / got past the teardown (both = blocks when the bounds work). */
 int kpt_surrogate_check_timeout(kpt_surrogate* surrogate, uint32_t blocks, uint32_t polls,
                                 uint32_t* timed_out, uint32_t* finished);
+/* Host only: the tcgen05 engine's weight block of a parameter block (the
+ * FP32 layout of kpt_surrogate_parameters) as 16-bit values (BF16, or FP16
+ * when fp16 != 0).  Three K-major, unswizzled tcgen05 B operands follow each
+ * other: layer 1 (N = H rows, K = 16: inputs 0..4, bias head, bias
+ * remainder, zeros), layer 2 (N = H, K = H + 16: weights, bias head,
+ * remainder, zeros), layer 3 (N = 16, K = H + 16; rows 3..15 zero); element
+ * (n, k) of an N x K operand sits at 16-bit index ((n/8) (K/8) 64 + (k/8) 64
+ * + (n%8) 8 + k%8).  The bias head is the bias rounded to 16 bits, the
+ * remainder the rounding of (bias - head).  out_len >= 16 H + H (H + 16) +
+ * 16 (H + 16) values. */
+int kpt_surrogate_pack_tc(const float* params, int32_t hidden_width, int32_t fp16,
+                          uint16_t* out, uint64_t out_len);
 /* Parameter block (FP32, W1[H][5] b1[H] W2[H][H] b2[H] W3[3][H] b3[3]:
  * 1379 floats for H = 32, 4739 for H = 64) and the box
  * normalisation (in_lo[5], in_hi[5], out_offset[3], out_scale[3], mu_cut);

@@ -257,6 +257,7 @@ def load_library() -> ctypes.CDLL:
         "kpt_surrogate_set_engine": (i32, [vp, i32]),
         "kpt_surrogate_get_engine": (i32, [vp, vp]),
         "kpt_surrogate_check_timeout": (i32, [vp, u32, u32, vp, vp]),
+        "kpt_surrogate_pack_tc": (i32, [vp, i32, i32, vp, u64]),
         "kpt_context_set_surrogate": (i32, [vp, vp]),
         "kpt_surrogate_judge": (i32, [vp, vp, vp, vp, vp]),
         "kpt_grid_create": (i32, [vp, i32, i32, vp, vp, vp, pvp]),
@@ -784,6 +785,17 @@ class Field:
         out = np.zeros((points, comps), dtype=np.float64)
         _check(self.ctx.lib.kpt_field_download_table(self.handle, _ptr(out), out.size))
         return out
+
+
+def surrogate_pack_tc(params: np.ndarray, hidden_width: int, fp16: bool = False) -> np.ndarray:
+    """The tcgen05 engine's 16-bit weight block of an FP32 parameter block
+    (kpt_surrogate_pack_tc; host only)."""
+    params = np.ascontiguousarray(params, dtype=np.float32)
+    h = int(hidden_width)
+    out = np.zeros(16 * h + h * (h + 16) + 16 * (h + 16), dtype=np.uint16)
+    _check(load_library().kpt_surrogate_pack_tc(_ptr(params), h, 1 if fp16 else 0, _ptr(out),
+                                                out.size))
+    return out
 
 
 class Surrogate:

@@ -1362,7 +1362,52 @@ void pack_canonical(const float* w, int n_out, int k_in, int n_rows, int k_cols,
     }
 }
 
+// The tcgen05 engine's B operands from the FP32 parameter block (W1[H][5]
+// b1[H] W2[H][H] b2[H] W3[3][H] b3[3]): each layer's bias becomes two extra
+// input columns, its 16-bit head and the 16-bit rounding of the remainder,
+// fed by constant ones; layer 1 is H x 16, layer 2 H x (H + 16), layer 3
+// 16 x (H + 16), each in the canonical layout.
+void pack_tc_block(const float* p, int hidden, bool fp16, std::vector<uint16_t>& tc) {
+    const int pw1 = 0;
+    const int pw2 = pw1 + hidden * kpt::kMlpIn + hidden;
+    const int pw3 = pw2 + hidden * hidden + hidden;
+    const int k2 = hidden + 16;
+    std::vector<float> w1(static_cast<size_t>(hidden) * 16, 0.0f);
+    std::vector<float> w2(static_cast<size_t>(hidden) * k2, 0.0f);
+    std::vector<float> w3(static_cast<size_t>(16) * k2, 0.0f);
+    auto split = [&](float b, float* row) {
+        const float hi = from_16(fp16 ? to_fp16(b) : to_bf16(b), fp16);
+        row[0] = hi;
+        row[1] = b - hi;
+    };
+    for (int n = 0; n < hidden; ++n) {
+        for (int k = 0; k < kpt::kMlpIn; ++k) w1[n * 16 + k] = p[pw1 + n * kpt::kMlpIn + k];
+        split(p[pw1 + hidden * kpt::kMlpIn + n], &w1[n * 16 + kpt::kMlpIn]);
+        for (int k = 0; k < hidden; ++k) w2[n * k2 + k] = p[pw2 + n * hidden + k];
+        split(p[pw2 + hidden * hidden + n], &w2[n * k2 + hidden]);
+    }
+    for (int n = 0; n < kpt::kMlpOut; ++n) {
+        for (int k = 0; k < hidden; ++k) w3[n * k2 + k] = p[pw3 + n * hidden + k];
+        split(p[pw3 + kpt::kMlpOut * hidden + n], &w3[n * k2 + hidden]);
+    }
+    pack_canonical(w1.data(), hidden, 16, hidden, 16, fp16, tc);
+    pack_canonical(w2.data(), hidden, k2, hidden, k2, fp16, tc);
+    pack_canonical(w3.data(), 16, k2, 16, k2, fp16, tc);
+}
+
 }  // namespace
+
+int kpt_surrogate_pack_tc(const float* params, int32_t hidden_width, int32_t fp16,
+                          uint16_t* out, uint64_t out_len) {
+    KPT_REQUIRE(params && out, "kpt_surrogate_pack_tc: NULL argument");
+    KPT_REQUIRE(hidden_width == 32 || hidden_width == 64,
+                "kpt_surrogate_pack_tc: hidden_width must be 32 or 64");
+    std::vector<uint16_t> tc;
+    pack_tc_block(params, hidden_width, fp16 != 0, tc);
+    KPT_REQUIRE(out_len >= tc.size(), "kpt_surrogate_pack_tc: output too short");
+    std::copy(tc.begin(), tc.end(), out);
+    return KPT_OK;
+}
 
 void kpt_surrogate_default_config(kpt_surrogate_config* c) {
     if (c == nullptr) return;
@@ -1553,34 +1598,9 @@ int kpt_surrogate_train(kpt_context* ctx, const kpt_settings* settings,
     KPT_CUDA(cudaMemcpy(sg->d_params, sg->params.data(), pcount * sizeof(float),
                         cudaMemcpyHostToDevice));
     KPT_CUDA(cudaMemcpy(sg->d_block, words.data(), block_bytes, cudaMemcpyHostToDevice));
-    // the tcgen05 engine: canonical-layout weights, each layer's bias as two
-    // extra input columns (16-bit head and remainder) fed by constant ones
+    // the tcgen05 engine's operand block
     std::vector<uint16_t> tc;
-    {
-        const float* p = sg->params.data();
-        const int k2 = hidden + 16;
-        std::vector<float> w1(static_cast<size_t>(hidden) * 16, 0.0f);
-        std::vector<float> w2(static_cast<size_t>(hidden) * k2, 0.0f);
-        std::vector<float> w3(static_cast<size_t>(16) * k2, 0.0f);
-        auto split = [&](float b, float* row) {
-            const float hi = from_16(fp16 ? to_fp16(b) : to_bf16(b), fp16);
-            row[0] = hi;
-            row[1] = b - hi;
-        };
-        for (int n = 0; n < hidden; ++n) {
-            for (int k = 0; k < kpt::kMlpIn; ++k) w1[n * 16 + k] = p[pw1 + n * kpt::kMlpIn + k];
-            split(p[pw1 + hidden * kpt::kMlpIn + n], &w1[n * 16 + kpt::kMlpIn]);
-            for (int k = 0; k < hidden; ++k) w2[n * k2 + k] = p[pw2 + n * hidden + k];
-            split(p[pw2 + hidden * hidden + n], &w2[n * k2 + hidden]);
-        }
-        for (int n = 0; n < kpt::kMlpOut; ++n) {
-            for (int k = 0; k < hidden; ++k) w3[n * k2 + k] = p[pw3 + n * hidden + k];
-            split(p[pw3 + kpt::kMlpOut * hidden + n], &w3[n * k2 + hidden]);
-        }
-        pack_canonical(w1.data(), hidden, 16, hidden, 16, fp16, tc);
-        pack_canonical(w2.data(), hidden, k2, hidden, k2, fp16, tc);
-        pack_canonical(w3.data(), 16, k2, 16, k2, fp16, tc);
-    }
+    pack_tc_block(sg->params.data(), hidden, fp16, tc);
     const size_t tc_bytes = kpt::tc_block_bytes(hidden);
     KPT_REQUIRE(tc.size() * sizeof(uint16_t) == tc_bytes,
                 "kpt_surrogate_train: tensor-core block size mismatch");
