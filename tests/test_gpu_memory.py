@@ -58,3 +58,29 @@ def test_repeated_calls_do_not_leak_device_memory(ctx, kpt, fields_mod, binding)
     surrogate.close()
     field.close()
     grid.close()
+
+
+def test_download_into_caller_arrays(ctx, kpt, fields_mod, binding):
+    """ParticleStorage.download(out=...) fills caller arrays (the bench's
+    pinned buffers) with what a plain download returns, and refuses arrays
+    of the wrong type or length."""
+    f = fields_mod.harris_field(32, 64, noise=0.01, seed=1)
+    settings = kpt.settings_from_dict(binding.default_params(kperp_over_kpara=0.05))
+    lower = ctx.field(f)
+    parts = ctx.particles(1000)
+    ctx.inject(parts, lower, settings, 700, 3, 11)
+    want = parts.download()
+    out = {k: np.full(1000, 7, dtype=v.dtype) for k, v in want.items()}
+    got = parts.download(out=out)
+    assert got is out
+    for k in want:
+        assert np.array_equal(out[k][:want[k].size], want[k]), k
+        assert np.all(out[k][want[k].size:] == 7), k
+    bad = dict(out, p=np.zeros(1000, dtype=np.float32))
+    with pytest.raises(kpt.KptError, match="contiguous"):
+        parts.download(out=bad)
+    short = dict(out, x=np.zeros(10))
+    with pytest.raises(kpt.KptError, match="length"):
+        parts.download(out=short)
+    for h in (parts, lower):
+        h.close()

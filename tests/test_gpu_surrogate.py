@@ -164,6 +164,8 @@ def test_engines_agree(kpt, net, request):
             outs[engine] = surrogate.evaluate(inputs)
     finally:
         surrogate.engine = kpt.ENGINE_TCGEN05
+    with pytest.raises(kpt.KptError, match="unknown engine"):
+        surrogate.engine = 7
     (tc, served_tc), (warp, served_warp) = outs[kpt.ENGINE_TCGEN05], outs[kpt.ENGINE_MMA_SYNC]
     assert np.array_equal(served_tc, served_warp)
     assert not served_tc[:50].any() and served_tc[50:].all()
