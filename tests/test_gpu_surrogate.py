@@ -59,6 +59,17 @@ def trained64(ctx, kpt, binding):
 
 
 @pytest.fixture(scope="module")
+def trained64fp16(ctx, kpt, binding):
+    params = binding.default_params(kperp_over_kpara=0.05, focused=1, closure=2)
+    settings = kpt.settings_from_dict(params)
+    surrogate = ctx.train_surrogate(settings, element_type=kpt.SURROGATE_FP16, hidden_width=64,
+                                    **TRAIN)
+    yield params, settings, surrogate
+    ctx.set_surrogate(None)
+    surrogate.close()
+
+
+@pytest.fixture(scope="module")
 def trained16(ctx, kpt, binding):
     params, settings, surrogate = _train(ctx, kpt, binding, kpt.SURROGATE_FP16)
     yield params, settings, surrogate
@@ -150,7 +161,7 @@ def test_trained_network_forward_and_accuracy(trained, trained16, trained64, wid
     assert p99["fp16"] < p99["fp16-net fp32"] + 0.01
 
 
-@pytest.mark.parametrize("net", ["trained", "trained16", "trained64"])
+@pytest.mark.parametrize("net", ["trained", "trained16", "trained64", "trained64fp16"])
 def test_engines_agree(kpt, net, request):
     params, _, surrogate = request.getfixturevalue(net)
     _, norm = surrogate.parameters()
@@ -199,7 +210,7 @@ def test_fallback_outside_the_box_is_the_plain_closure(trained):
 
 
 @pytest.mark.parametrize("engine", ["tcgen05", "mma_sync"])
-@pytest.mark.parametrize("net", ["trained", "trained16", "trained64"])
+@pytest.mark.parametrize("net", ["trained", "trained16", "trained64", "trained64fp16"])
 def test_surrogate_push_matches_fp64_spectrum(ctx, kpt, oracle, binding, fields_mod, net, engine,
                                               request):
     params, settings, surrogate = request.getfixturevalue(net)
