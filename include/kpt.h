@@ -368,7 +368,12 @@ int kpt_inject_uniform(kpt_context* ctx, kpt_particles* particles, const kpt_fie
                        uint64_t seed, double band_lo, double band_hi, uint64_t* injected);
 /* Push every active particle across the interval [frame*mhd_dt,
  * frame*mhd_dt + mhd_dt) between tables `lower` and `upper` (same kind,
- * precision and grid).  Noise: Philox keyed (seed, index, frame, 2). */
+ * precision and grid).  Noise: Philox keyed (seed, index, frame, 2).
+ * Replaces move_parker_particles_one_interval / move_particles_one_interval
+ * (src/main.cpp:1084-1327, :1334-1755).  stats (optional) synchronises the
+ * stream and receives the counters; with the learned closure on the tcgen05
+ * engine it is also where a timed-out tensor-core completion wait is
+ * reported (KPT_ERROR_INVALID_ARGUMENT with the message). */
 int kpt_push_interval(kpt_context* ctx, kpt_particles* particles, const kpt_field* lower,
                       const kpt_field* upper, const kpt_settings* settings, uint32_t frame,
                       uint64_t seed, kpt_push_stats* stats);
