@@ -373,7 +373,7 @@ int kpt_inject_uniform(kpt_context* ctx, kpt_particles* particles, const kpt_fie
  * (src/main.cpp:1084-1327, :1334-1755).  stats (optional) synchronises the
  * stream and receives the counters; with the learned closure on the tcgen05
  * engine it is also where a timed-out tensor-core completion wait is
- * reported (KPT_ERROR_INVALID_ARGUMENT with the message). */
+ * reported (KPT_ERROR_CUDA with the message). */
 int kpt_push_interval(kpt_context* ctx, kpt_particles* particles, const kpt_field* lower,
                       const kpt_field* upper, const kpt_settings* settings, uint32_t frame,
                       uint64_t seed, kpt_push_stats* stats);

@@ -1090,9 +1090,11 @@ int kpt_push_interval(kpt_context* ctx, kpt_particles* parts, const kpt_field* l
         stats->failed = host.failed;
         stats->max_steps = host.max_steps;
         stats->pad = 0;
-        KPT_REQUIRE(host.network_timeouts == 0,
-                    "kpt_push_interval: a tensor-core completion wait timed out (results of "
-                    "this push are invalid)");
+        if (host.network_timeouts != 0) {
+            return set_error(KPT_ERROR_CUDA,
+                             "kpt_push_interval: a tensor-core completion wait timed out "
+                             "(results of this push are invalid)");
+        }
     }
     return KPT_OK;
 }
@@ -1675,7 +1677,10 @@ int kpt_surrogate_evaluate(kpt_surrogate* sg, uint64_t n, const double* inputs, 
         KPT_CUDA(cudaMemcpyAsync(served, dserved, n * sizeof(int), cudaMemcpyDeviceToHost, st));
     }
     KPT_CUDA(cudaStreamSynchronize(st));
-    KPT_REQUIRE(timeouts == 0, "kpt_surrogate_evaluate: a tensor-core completion wait timed out");
+    if (timeouts != 0) {
+        return set_error(KPT_ERROR_CUDA,
+                         "kpt_surrogate_evaluate: a tensor-core completion wait timed out");
+    }
     return KPT_OK;
 }
 
