@@ -36,6 +36,13 @@ namespace {
 
 constexpr double kSqrt3 = 1.7320508075688772935;
 
+// FP32 square roots of the mixed path through sqrt.approx.f32 (a couple of
+// ulp, like the path's other fast intrinsics): +2.3 % on the learned-closure
+// push, no change on the plain-closure one.
+#ifndef KPT_FAST_SQRT
+#define KPT_FAST_SQRT 1
+#endif
+
 template <typename T>
 struct Num;
 
@@ -58,7 +65,17 @@ struct Num<float> {
     static __device__ __forceinline__ float pow(float a, float b) {
         return exp2f(b * __log2f(a));
     }
+#if KPT_FAST_SQRT
+    // sqrt.approx.f32: one MUFU-based instruction (sqrt(+0) = +0,
+    // negative -> NaN, +inf -> +inf)
+    static __device__ __forceinline__ float sqrt(float a) {
+        float r;
+        asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(a));
+        return r;
+    }
+#else
     static __device__ __forceinline__ float sqrt(float a) { return sqrtf(a); }
+#endif
     static __device__ __forceinline__ float div(float a, float b) { return __fdividef(a, b); }
     static __device__ __forceinline__ bool finite(float a) { return isfinite(a); }
     static __device__ __forceinline__ float abs(float a) { return fabsf(a); }
