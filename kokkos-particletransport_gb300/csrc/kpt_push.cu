@@ -940,7 +940,7 @@ __device__ __forceinline__ bool substep_surrogate(StateMixed& st, const PushPara
             const float b = c[6];
             const float p = st.p_hi;
             const float speed = __fdividef(k.particle_v0 * p, k.p0);
-            const float omega = __fdividef(k.qlt_omega0 * b, sqrtf(1.0f + p * p));
+            const float omega = __fdividef(k.qlt_omega0 * b, Num<float>::sqrt(1.0f + p * p));
             float duu, duu_du;
             qlt_scattering<float>(mu, omega, speed, k, duu, duu_du);
             float kpara = k.kpara0;
