@@ -371,9 +371,10 @@ int kpt_inject_uniform(kpt_context* ctx, kpt_particles* particles, const kpt_fie
  * precision and grid).  Noise: Philox keyed (seed, index, frame, 2).
  * Replaces move_parker_particles_one_interval / move_particles_one_interval
  * (src/main.cpp:1084-1327, :1334-1755).  stats (optional) synchronises the
- * stream and receives the counters; with the learned closure on the tcgen05
- * engine it is also where a timed-out tensor-core completion wait is
- * reported (KPT_ERROR_CUDA with the message). */
+ * stream and receives the counters.  With the learned closure on the tcgen05
+ * engine the call always synchronises (stats or not) and reads the counters
+ * back, so a timed-out tensor-core completion wait is always reported
+ * (KPT_ERROR_CUDA with the message; the push's results are then invalid). */
 int kpt_push_interval(kpt_context* ctx, kpt_particles* particles, const kpt_field* lower,
                       const kpt_field* upper, const kpt_settings* settings, uint32_t frame,
                       uint64_t seed, kpt_push_stats* stats);
@@ -392,8 +393,11 @@ int kpt_summarize(kpt_context* ctx, const kpt_particles* particles, kpt_summary*
  * is being captured or timed).  Same result as kpt_summarize.  Its scratch is
  * one fixed device array of the library (about 0.7 MB per GPU, held until
  * the process exits), so count is limited to 16,777,216 particles
- * (KPT_ERROR_CAPACITY above that).  The first call on a device looks up the
- * array's device address, so make it before any stream capture.  All calls
+ * (KPT_ERROR_CAPACITY above that).  The first call in each CUDA context
+ * looks up the array's device address in that context (kept under the
+ * context's unique id, so a second context on a device, or a context
+ * recreated after cudaDeviceReset, looks it up afresh), so make that first
+ * call before any stream capture.  All calls
  * share the array: calls that overlap on the GPU (other streams, other host
  * threads) race and must be serialised by the caller.  Runs on cuda_stream
  * (NULL = legacy default stream) and synchronises it. */

@@ -1080,16 +1080,29 @@ int kpt_push_interval(kpt_context* ctx, kpt_particles* parts, const kpt_field* l
     if (parts->count > 0) {
         KPT_CUDA(kpt::launch_push_interval(launch, ctx->stream));
     }
-    if (stats != nullptr) {
+    // The tcgen05 engine's completion waits are bounded; a block that gives
+    // up stops early, so its particles are not stored back.  Its counters are
+    // therefore always read back and checked, with or without `stats`.
+    const bool bounded_waits =
+        launch.surrogate != nullptr && served.engine == KPT_ENGINE_TCGEN05 && parts->count > 0;
+    if (stats != nullptr || bounded_waits) {
         kpt::PushCounters host{};
         KPT_CUDA(cudaMemcpyAsync(&host, launch.counters, sizeof(host), cudaMemcpyDeviceToHost,
                                  ctx->stream));
         KPT_CUDA(cudaStreamSynchronize(ctx->stream));
-        stats->particle_steps = host.particle_steps;
-        stats->pushed = host.pushed;
-        stats->failed = host.failed;
-        stats->max_steps = host.max_steps;
-        stats->pad = 0;
+        if (stats != nullptr) {
+            stats->particle_steps = host.particle_steps;
+            stats->pushed = host.pushed;
+            stats->failed = host.failed;
+            stats->max_steps = host.max_steps;
+            stats->pad = 0;
+        }
+        if (host.teardown_incomplete != 0) {
+            return set_error(KPT_ERROR_CUDA,
+                             "kpt_push_interval: a tensor-core completion wait timed out and "
+                             "tensor memory was freed with MMAs in flight (results of this "
+                             "push are invalid for every particle)");
+        }
         if (host.network_timeouts != 0) {
             return set_error(KPT_ERROR_CUDA,
                              "kpt_push_interval: a tensor-core completion wait timed out "
@@ -2530,6 +2543,9 @@ int kpt_parker_advance_stochastic_steps(kpt_context* ctx, kpt_parker_solver* s,
             err = kpt::lib_parker_step(launches[k], ctx->stream);
         }
         const cudaError_t end = cudaStreamEndCapture(ctx->stream, &graph);
+        if ((err != cudaSuccess || end != cudaSuccess) && graph != nullptr) {
+            cudaGraphDestroy(graph);  // a capture that failed part-way still returns a graph
+        }
         KPT_CUDA(err);
         KPT_CUDA(end);
         captured = true;
@@ -2771,6 +2787,9 @@ int kpt_focus_advance_stochastic_steps(kpt_context* ctx, kpt_focus_solver* s, kp
             err = kpt::lib_focus_step(launches[k], ctx->stream);
         }
         const cudaError_t end = cudaStreamEndCapture(ctx->stream, &graph);
+        if ((err != cudaSuccess || end != cudaSuccess) && graph != nullptr) {
+            cudaGraphDestroy(graph);  // a capture that failed part-way still returns a graph
+        }
         KPT_CUDA(err);
         KPT_CUDA(end);
         captured = true;
@@ -3737,6 +3756,9 @@ int kpt_batch_run(kpt_batch* b, uint32_t intervals, int use_graph) {
             KPT_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
             const cudaError_t err = batch_enqueue(b, intervals, st);
             const cudaError_t end = cudaStreamEndCapture(st, &graph);
+            if ((err != cudaSuccess || end != cudaSuccess) && graph != nullptr) {
+                cudaGraphDestroy(graph);
+            }
             KPT_CUDA(err);
             KPT_CUDA(end);
             const cudaError_t inst = cudaGraphInstantiate(&b->graph, graph, 0);

@@ -1,8 +1,10 @@
 // Particle lifecycle kernels: uniform injection, deterministic momentum
 // split, weighted log-momentum histogram and the run summary reductions.
+#include <cuda.h>  // CUcontext / CUresult types only; entry points come from the runtime
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <mutex>
 
 #include "kpt_device.cuh"
 #include "kpt_internal.h"
@@ -440,10 +442,80 @@ constexpr unsigned long long kNoAllocMaxParticles =
 // [0, kNoAllocMaxBlocks): per-block partials; [kNoAllocMaxBlocks]: result.
 static __device__ __align__(256) kpt::SummaryPartial g_noalloc_summary[kNoAllocMaxBlocks + 1];
 
-// Device address of g_noalloc_summary per device, looked up once per device
-// (cudaGetSymbolAddress with that device current).
-constexpr int kNoAllocMaxDevices = 64;
-kpt::SummaryPartial* g_noalloc_address[kNoAllocMaxDevices] = {};
+// Device address of g_noalloc_summary per CUDA context.  The address is
+// looked up (cudaGetSymbolAddress) the first time a context calls, and kept
+// under the context's unique id (cuCtxGetId), so a second context on the
+// same device, or a primary context recreated after cudaDeviceReset, gets its
+// own lookup instead of another context's (possibly stale) address.
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
+
+struct NoAllocSlot {
+    unsigned long long context_id;
+    kpt::SummaryPartial* address;
+};
+constexpr int kNoAllocMaxContexts = 64;
+std::mutex g_noalloc_mutex;
+NoAllocSlot g_noalloc_slots[kNoAllocMaxContexts] = {};
+int g_noalloc_used = 0;
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+
+// Id of the calling thread's current context (0 when none is current).
+// Caller holds g_noalloc_mutex.
+cudaError_t current_context_id(unsigned long long* id) {
+    *id = 0;
+    if (g_ctx_get_current == nullptr || g_ctx_get_id == nullptr) {
+        cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSuccess;
+        cudaDriverEntryPointQueryResult q2 = cudaDriverEntryPointSuccess;
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        cudaError_t err = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000,
+                                                           cudaEnableDefault, &q1);
+        if (err != cudaSuccess) return err;
+        err = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2);
+        if (err != cudaSuccess) return err;
+        if (q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess ||
+            f1 == nullptr || f2 == nullptr) {
+            return cudaErrorNotSupported;
+        }
+        g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+        g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(f2);
+    }
+    CUcontext ctx = nullptr;
+    if (g_ctx_get_current(&ctx) != CUDA_SUCCESS) return cudaErrorDeviceUninitialized;
+    if (ctx == nullptr) return cudaSuccess;
+    if (g_ctx_get_id(ctx, id) != CUDA_SUCCESS) return cudaErrorDeviceUninitialized;
+    return cudaSuccess;
+}
+
+// Device address of g_noalloc_summary in the current context.
+cudaError_t noalloc_address(kpt::SummaryPartial** out) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    unsigned long long id = 0;
+    cudaError_t err = current_context_id(&id);
+    if (err != cudaSuccess) return err;
+    for (int k = 0; k < g_noalloc_used && id != 0; ++k) {
+        if (g_noalloc_slots[k].context_id == id) {
+            *out = g_noalloc_slots[k].address;
+            return cudaSuccess;
+        }
+    }
+    // First call in this context (or no context current yet: the lookup
+    // makes the device's primary context current, as any runtime call does).
+    void* ptr = nullptr;
+    err = cudaGetSymbolAddress(&ptr, g_noalloc_summary);
+    if (err != cudaSuccess) return err;
+    if (id == 0) {
+        err = current_context_id(&id);
+        if (err != cudaSuccess) return err;
+    }
+    if (id != 0 && g_noalloc_used < kNoAllocMaxContexts) {
+        g_noalloc_slots[g_noalloc_used++] = NoAllocSlot{id, static_cast<kpt::SummaryPartial*>(ptr)};
+    }
+    *out = static_cast<kpt::SummaryPartial*>(ptr);
+    return cudaSuccess;
+}
 
 }  // namespace
 
@@ -452,19 +524,12 @@ namespace kpt {
 unsigned long long noalloc_summary_max_particles() { return kNoAllocMaxParticles; }
 
 cudaError_t noalloc_summary(const SummaryLaunch& in, cudaStream_t stream, SummaryPartial* host) {
-    int device = 0;
-    cudaError_t err = cudaGetDevice(&device);
+    SummaryPartial* scratch = nullptr;
+    cudaError_t err = noalloc_address(&scratch);
     if (err != cudaSuccess) return err;
-    if (device < 0 || device >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
-    if (g_noalloc_address[device] == nullptr) {
-        void* ptr = nullptr;
-        err = cudaGetSymbolAddress(&ptr, g_noalloc_summary);
-        if (err != cudaSuccess) return err;
-        g_noalloc_address[device] = static_cast<SummaryPartial*>(ptr);
-    }
     SummaryLaunch L = in;
-    L.partials = g_noalloc_address[device];
-    L.result = g_noalloc_address[device] + kNoAllocMaxBlocks;
+    L.partials = scratch;
+    L.result = scratch + kNoAllocMaxBlocks;
     // Every partial that the final pass reads is written by this call, so no
     // clearing is needed between calls.
     err = launch_summary(L, stream);

@@ -1272,7 +1272,9 @@ __global__ void __launch_bounds__(128, KPT_SURROGATE_TC_MIN_BLOCKS)
     if (fail && threadIdx.x == 0) {
         atomicAdd(&P.counters->network_timeouts, 1u);
     }
-    tc_teardown<H>(net, fail);
+    if (!tc_teardown<H>(net, fail) && threadIdx.x == 0) {
+        atomicAdd(&P.counters->teardown_incomplete, 1u);
+    }
     flush_counters(P.counters, my_steps, my_pushed, my_failed, my_max);
     flush_judge(P.sg.judge, tally);
 }

@@ -499,12 +499,18 @@ __device__ __forceinline__ void tc_constants(const TcNet& net) {
 }
 
 // Block epilogue (all threads, uniform): after a timeout, wait once more
-// (bounded) for the MMAs in flight; then warp 0 frees the TMEM.
+// (bounded) for the MMAs in flight; then warp 0 frees the TMEM.  The TMEM is
+// freed even when that second wait also gives up (keeping it would leave the
+// blocks queued in tcgen05.alloc waiting forever); a late MMA may then write
+// into columns another block of the same launch has allocated, so a false
+// return means every result of the launch is invalid, not only this block's.
+// Returns true when the block did not fail or its MMAs completed in time.
 template <int H>
-__device__ __forceinline__ void tc_teardown(const TcNet& net, bool failed,
+__device__ __forceinline__ bool tc_teardown(const TcNet& net, bool failed,
                                             uint32_t polls = KPT_TC_WAIT_POLLS) {
-    if (failed && threadIdx.x == 0) {
-        mbar_wait(net.mbar, net.phase ^ 1u, polls);
+    __shared__ int drained;
+    if (threadIdx.x == 0) {
+        drained = failed ? (mbar_wait(net.mbar, net.phase ^ 1u, polls) ? 1 : 0) : 1;
     }
     tc_fence_before();
     __syncthreads();
@@ -515,6 +521,7 @@ __device__ __forceinline__ void tc_teardown(const TcNet& net, bool failed,
                      : "r"(net.tmem), "r"(TcMlp<H>::Cols)
                      : "memory");
     }
+    return drained != 0;
 }
 
 // Block-wide hand-over to the MMA issuer: TMEM stores ordered before the

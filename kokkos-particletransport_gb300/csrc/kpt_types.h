@@ -90,7 +90,8 @@ struct PushCounters {
     unsigned int max_steps;
     unsigned int next_particle;  // work-queue cursor
     unsigned int network_timeouts;  // blocks stopped by a tensor-core completion timeout
-    unsigned int pad;
+    unsigned int teardown_incomplete;  // of those, blocks whose MMAs were still in flight
+                                       // when their tensor memory was freed
 };
 
 }  // namespace kpt
