@@ -15,8 +15,10 @@ region), mixed precision; beside it the plain FP64 push with the plain
 closure (the baseline the metric names), the mixed push with the plain
 closure (what the network gains or costs), momentum and pitch-cosine
 spectrum L1 of every leg against FP64 after one interval from the same
-start, the per-step error of the mixed push, and the Parker legs (mixed and
-FP64).
+start, the spectrum bar over ten consecutive intervals (``accuracy``: L1
+and chi-square of 64 momentum bins, a fine ln(p/p0) histogram and 16
+pitch-cosine bins, paired and independent noise), the per-step error of the
+mixed push, and the Parker legs (mixed and FP64).
 
 Timing: CUDA events on the library's stream around exactly K steps after W
 warm-up steps; the tables (2 x 200 MB mixed focused) exceed the 129 MB L2,
@@ -63,6 +65,8 @@ def tensor_flop_per_step(hidden: int) -> int:
     K = H + 16 x N = 16 (3 outputs, padding): 14 848 flop at H = 64."""
     return 2 * (16 * hidden + (hidden + 16) * hidden + (hidden + 16) * 16)
 PROFILE = os.path.join(ROOT, "profiles", "push_tc_surrogate_focused_1024x2048.md")
+PROFILE_F64_FOCUSED = os.path.join(ROOT, "profiles", "push_refill_f64_focused_1024x2048.md")
+PROFILE_F64_PARKER = os.path.join(ROOT, "profiles", "push_refill_f64_parker_1024x2048.md")
 
 
 def make_workload():
@@ -361,6 +365,9 @@ def run_focused(args, f0, f1):
                 np.abs(_spectrum(fin["p"], fin["w"], fin["status"]) - hp).sum() / hp.sum())
             out[label]["mu_spectrum_l1_vs_f64"] = float(
                 np.abs(_mu_spectrum(fin) - hm).sum() / hm.sum())
+    if WORLD == 1 and args.accuracy_intervals > 0:
+        out["accuracy"] = accuracy_report(args, kpt, ctx, nets, tables, start, plain, learned,
+                                          stream)
     if WORLD == 1:
         out["c3"] = precision_report(kpt, ctx, parts, tables, start, n, plain)
         out["c3"].update(
@@ -375,6 +382,65 @@ def run_focused(args, f0, f1):
         lo.close()
         up.close()
     ctx.close()
+    return out
+
+
+def accuracy_report(args, kpt, ctx, nets, tables, start, plain, learned, stream):
+    """The spectrum bar of the metric over many consecutive intervals: the
+    first `accuracy_particles` particles of the headline population pushed
+    `accuracy_intervals` intervals of `substeps` fixed steps from the common
+    start by the plain FP64 push (plain closure; the reference), the mixed
+    push with the plain closure and the mixed push with the learned closure
+    (tcgen05).  Each mixed leg runs twice: with the reference's noise
+    (paired: the histograms differ only by the arithmetic; the L1 bar) and
+    with an independent seed (a Monte Carlo chi-square test of the
+    distributions).  Histograms: 64 driver bins of p, 64 fine bins of
+    ln(p/p0) fitted to the reference, 16 bins of the pitch cosine."""
+    import torch
+    spectra = importlib.import_module("kokkos-particletransport_gb300.spectra")
+    n = min(args.accuracy_particles, len(start["x"]))
+    sub = {k: v[:n].copy() for k, v in start.items()}
+    parts = ctx.particles(n)
+    tc = kpt.ENGINE_TCGEN05
+    legs = [("f64", kpt.PRECISION_F64, plain, None, SEED),
+            ("mixed_qlt", kpt.PRECISION_MIXED, plain, None, SEED),
+            ("surrogate", kpt.PRECISION_MIXED, learned, "surrogate", SEED),
+            ("mixed_qlt_independent", kpt.PRECISION_MIXED, plain, None, SEED + 1),
+            ("surrogate_independent", kpt.PRECISION_MIXED, learned, "surrogate", SEED + 1)]
+    finals, seconds = {}, {}
+    for label, precision, settings, net_label, seed in legs:
+        if net_label is not None:
+            nets[net_label].engine = tc
+        ctx.set_surrogate(nets.get(net_label))
+        lower, upper = tables[precision]
+        parts.upload(sub, n)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in range(args.accuracy_intervals):
+            if args.sort_tile > 0:
+                ctx.sort(parts, lower, args.sort_tile, args.sort_tile)
+            ctx.push_interval(parts, lower, upper, settings, START_FRAME + k, seed)
+        torch.cuda.synchronize()
+        seconds[label] = time.perf_counter() - t0
+        finals[label] = parts.download(n)
+    ctx.set_surrogate(None)
+    parts.close()
+    ref = finals["f64"]
+    out = {"particles": n, "intervals": args.accuracy_intervals,
+           "steps_per_interval": args.substeps,
+           "reference": "plain FP64 push, plain slab-QLT closure, same start and noise",
+           "bar": {"l1_max": 0.01, "chi2_p_min": 0.01},
+           "seconds": seconds}
+    ok = True
+    for label in ("mixed_qlt", "surrogate"):
+        paired = spectra.compare_populations(finals[label], ref, plain.p0)
+        indep = spectra.compare_populations(finals[label + "_independent"], ref, plain.p0)
+        out[label] = {"paired": paired, "independent": indep}
+        ok &= paired["p64"]["l1"] <= 0.01 and paired["mu16"]["l1"] <= 0.01
+        ok &= all(indep[key]["p_value"] > 0.01 for key in ("p64", "lnp_fine", "mu16"))
+    out["reference_populated_bins"] = out["mixed_qlt"]["paired"]["p64"]["populated_bins"]
+    out["reference_bins_with_1pct_weight"] = out["mixed_qlt"]["paired"]["bins_with_1pct_weight"]
+    out["pass"] = bool(ok)
     return out
 
 
@@ -524,6 +590,87 @@ def run_batched(args):
                         "graph": True, "schedule": tuning},
             "speedup_batched_over_sequential": (bat_steps / batch_s) / (seq_steps / (seq_ms / 1e3)),
             "bitwise_identical": bool(identical), "setup_s": setup_s}
+
+
+def run_c2_cli(args):
+    """The at-scale Parker configuration through the command-line driver: a
+    sequence of 1024x2048 stretched-y Harris + islands frames, each freshly
+    noised (1 % multiplicative, its own seed), written as compact field
+    files; ``--profile full`` (1600 x 16 particles injected per frame,
+    capacity 16 M, histogram and snapshot every 10 frames, adaptive dt) with
+    split ratio 1.2 and kperp/kpara 0.05, run for `c2_frames` frames in
+    mixed precision and in FP64 from the same seed.  Reports frames/s,
+    particle-steps/s (push time and whole loop) and the per-phase times of
+    each run, and the final histograms and split counts of the two runs
+    against each other."""
+    import shutil
+    import tempfile
+    formats = importlib.import_module("kokkos-particletransport_gb300.formats")
+    spectra = importlib.import_module("kokkos-particletransport_gb300.spectra")
+    app = os.path.join(ROOT, "kokkos-particletransport_gb300", "bin",
+                       "kokkos_particle_transport_app")
+    frames = args.c2_frames
+    work = tempfile.mkdtemp(prefix="kpt_c2_")
+    try:
+        field_dir = os.path.join(work, "fields")
+        os.makedirs(field_dir)
+        ye = fields.stretched_edges(NY, -2.0, 2.0, strength=4.0)
+        t0 = time.perf_counter()
+        for f in range(frames + 1):
+            field = fields.harris_field(NX, NY, y_edges=ye, island_amplitude=0.1, noise=0.01,
+                                        seed=SEED + f)
+            fields.write_compact_field(fields.field_file_path(field_dir, f), field)
+        out = {"frames": frames, "nx": NX, "ny": NY,
+               "field_files_bytes": os.path.getsize(fields.field_file_path(field_dir, 0)),
+               "field_generation_s": time.perf_counter() - t0}
+        finals = {}
+        for precision in ("mixed", "f64"):
+            outdir = os.path.join(work, precision)
+            stats_path = os.path.join(work, f"push_{precision}.csv")
+            cmd = [app, "--profile", "full", "--field-dir", field_dir, "--output-dir", outdir,
+                   "--start-frame", "0", "--frames", str(frames), "--split-ratio", "1.2",
+                   "--kperp-over-kpara", "0.05", "--precision", precision,
+                   "--push-stats", stats_path, "--device", str(DEVICE)]
+            t0 = time.perf_counter()
+            proc = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT,
+                                  text=True)
+            wall = time.perf_counter() - t0
+            if proc.returncode != 0:
+                raise RuntimeError("C2 run failed: " + " ".join(cmd) + "\n" + proc.stdout[-2000:])
+            rows = formats.read_summary_csv(os.path.join(outdir, "summary.csv"))
+            push = np.genfromtxt(stats_path, delimiter=",", names=True)
+            steps = float(push["particle_steps"].sum())
+            phases = {name: float(push[f"{name}_seconds"].sum())
+                      for name in ("read", "inject", "move", "split", "summary", "histogram")}
+            loop_s = float(rows[-1]["total_elapsed_seconds"])
+            last = rows[-1]
+            hist = formats.read_histogram_csv(
+                os.path.join(outdir, f"momentum_histogram_{frames:05d}.csv"))["weight"]
+            finals[precision] = {"hist": hist,
+                                 "split": np.array([int(r["split"]) for r in rows])}
+            out[precision] = {
+                "frames_per_s": frames / loop_s, "loop_s": loop_s, "process_wall_s": wall,
+                "particle_steps": int(steps),
+                "value": steps / phases["move"], "unit": "particle-steps/s (push time)",
+                "loop_particle_steps_per_s": steps / loop_s,
+                "phase_seconds": phases,
+                "stored": int(last["stored"]), "active": int(last["active"]),
+                "split_total": int(finals[precision]["split"].sum()),
+                "max_split_level": int(last["max_split_level"]),
+                "failed": int(push["failed"].sum()), "max_steps": int(push["max_steps"].max())}
+        mixed, f64 = finals["mixed"], finals["f64"]
+        h128 = spectra.compare(mixed["hist"], f64["hist"])
+        h64 = spectra.compare(mixed["hist"].reshape(-1, 2).sum(1), f64["hist"].reshape(-1, 2).sum(1))
+        out["mixed_vs_f64"] = {
+            "frame": frames, "histogram_128": h128, "histogram_64": h64,
+            "split_total_relative_difference":
+                abs(out["mixed"]["split_total"] - out["f64"]["split_total"]) /
+                max(1, out["f64"]["split_total"]),
+            "split_per_frame_equal": bool(np.array_equal(mixed["split"], f64["split"]))}
+        out["speedup_mixed_over_f64_push"] = out["mixed"]["value"] / out["f64"]["value"]
+        return out
+    finally:
+        shutil.rmtree(work, ignore_errors=True)
 
 
 def run_library(args):
@@ -703,16 +850,53 @@ def cpu_baseline(particles: int, substeps: int, steps: int = 1):
     return total_steps / elapsed, threads, elapsed, total_steps
 
 
-def profiled_traffic():
-    """DRAM bytes per particle-step of the headline kernel from its committed
-    ncu summary (a line 'dram_bytes_per_particle_step: X'), or None."""
-    if not os.path.exists(PROFILE):
+def profile_value(path, key):
+    """A figure of a committed ncu summary (a line 'key: X'), or None.  These
+    are properties of the kernel measured once by ncu (DRAM bytes and FP64
+    operations per particle-step, a pipe's share of its peak), not of the
+    run; the bench line labels them with the summary they come from."""
+    if not os.path.exists(path):
         return None
-    with open(PROFILE) as stream:
+    with open(path) as stream:
         for line in stream:
-            if line.strip().startswith("dram_bytes_per_particle_step:"):
+            if line.strip().startswith(key + ":"):
                 return float(line.split(":", 1)[1])
     return None
+
+
+def read_bf16_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as stream:
+            return float(json.load(stream)["bf16_tflops"]), "measured"
+    return 1900.0, "fallback"
+
+
+def fp64_roofline(focused_f64, parker_f64):
+    """The plain FP64 pushes against the FP64 pipe: the pipe's FMA rate
+    measured now on this GPU by the library's probe kernel, the pushes' FP64
+    operations per particle-step from their ncu summaries (dadd + dmul +
+    2 dfma, flop), and the HBM fraction of the algorithmic gather model
+    beside it."""
+    kpt = importlib.import_module("kokkos-particletransport_gb300")
+    with kpt.Context(DEVICE) as ctx:
+        peak = ctx.fp64_fma_rate()
+    hbm, _ = read_peaks()
+    out = {"peak_tflops": peak, "peak_kind": "measured (project FMA-chain kernel, this run)"}
+    for label, value, model, path in (
+            ("focused_f64", focused_f64, "focused_f64", PROFILE_F64_FOCUSED),
+            ("parker_f64", parker_f64, "parker_f64", PROFILE_F64_PARKER)):
+        if value is None:
+            continue
+        flop = profile_value(path, "fp64_flop_per_particle_step")
+        entry = {"value": value, "hbm_frac": value * BYTES_PER_STEP[model] / 1e9 / hbm,
+                 "fp64_flop_per_particle_step": flop,
+                 "flop_source": os.path.relpath(path, ROOT) if flop is not None else None}
+        if flop is not None:
+            entry["fp64_tflops"] = value * flop / 1e12
+            entry["fp64_frac"] = entry["fp64_tflops"] / peak
+        out[label] = entry
+    return out
 
 
 def main():
@@ -741,6 +925,12 @@ def main():
     parser.add_argument("--hidden-width", type=int, default=64, choices=(32, 64),
                         help="hidden width of the headline network (a BF16 network of the "
                              "other width is measured beside it)")
+    parser.add_argument("--c2-frames", type=int, default=20,
+                        help="frames of the at-scale Parker run through the CLI (0 skips it)")
+    parser.add_argument("--accuracy-particles", type=int, default=1 << 18,
+                        help="particles of the multi-interval spectrum comparison")
+    parser.add_argument("--accuracy-intervals", type=int, default=10,
+                        help="consecutive intervals of the spectrum comparison (0 skips it)")
     parser.add_argument("--sort-tile", type=int, default=8,
                         help="cell-sort tile (cells) before each push; 0 disables")
     args = parser.parse_args()
@@ -786,13 +976,20 @@ def main():
     parker = run_parker(args, f0, f1) if args.parker_particles > 0 and WORLD == 1 else None
     batched = run_batched(args) if args.batch_runs > 0 and WORLD == 1 else None
     library = run_library(args) if args.library_particles > 0 and WORLD == 1 else None
+    c2 = run_c2_cli(args) if args.c2_frames > 0 and WORLD == 1 else None
     peak, peak_kind = read_peaks()
     head, f64 = focused["surrogate"], focused["f64"]
+    acc = focused.get("accuracy")
     mixed_qlt = focused.get("mixed_qlt")
     kernel_s = head["kernel_ms"] / 1e3
     steps_per_launch = head["particle_steps"] / head["steps"]
     achieved = steps_per_launch * BYTES_PER_STEP["focused_mixed"] / kernel_s / 1e9
-    per_step_traffic = profiled_traffic()
+    per_step_traffic = profile_value(PROFILE, "dram_bytes_per_particle_step")
+    l1tex_frac = profile_value(PROFILE, "l1tex_data_pipe_frac")
+    bf16_peak, bf16_kind = read_bf16_peak()
+    tensor_tflops = steps_per_launch * tensor_flop_per_step(args.hidden_width) / kernel_s / 1e12
+    fp64 = fp64_roofline(f64["value"], None if parker is None else parker["f64"]["value"]) \
+        if WORLD == 1 else None
     # whole-job value: all ranks' particle-steps over the slowest rank's time
     head["value"], total_ms = whole_job(head["ms_per_step"] * head["steps"],
                                         head["particle_steps"])
@@ -822,11 +1019,21 @@ def main():
                       "speedup_surrogate_over_f64": head["value"] / (f64["value"] * WORLD)},
         "mixed_plain_qlt": None if mixed_qlt is None else {
             "value": mixed_qlt["value"], "ms_per_step": mixed_qlt["ms_per_step"],
-            "spectrum_l1_vs_f64": mixed_qlt["spectrum_l1_vs_f64"],
-            "mu_spectrum_l1_vs_f64": mixed_qlt["mu_spectrum_l1_vs_f64"],
+            "spectrum_l1_vs_f64": None if acc is None
+            else acc["mixed_qlt"]["paired"]["p64"]["l1"],
+            "mu_spectrum_l1_vs_f64": None if acc is None
+            else acc["mixed_qlt"]["paired"]["mu16"]["l1"],
+            "spectrum_one_interval": {"p64_l1": mixed_qlt["spectrum_l1_vs_f64"],
+                                      "mu16_l1": mixed_qlt["mu_spectrum_l1_vs_f64"]},
             "surrogate_gain": head["value"] / mixed_qlt["value"]},
-        "spectrum_l1_vs_f64": head["spectrum_l1_vs_f64"],
-        "mu_spectrum_l1_vs_f64": head["mu_spectrum_l1_vs_f64"],
+        # the metric's spectrum bar: 64-bin momentum and 16-bin pitch-cosine
+        # L1 against FP64 after `accuracy_intervals` intervals (paired noise)
+        "spectrum_l1_vs_f64": None if acc is None else acc["surrogate"]["paired"]["p64"]["l1"],
+        "mu_spectrum_l1_vs_f64":
+            None if acc is None else acc["surrogate"]["paired"]["mu16"]["l1"],
+        "spectrum_one_interval": {"p64_l1": head["spectrum_l1_vs_f64"],
+                                  "mu16_l1": head["mu_spectrum_l1_vs_f64"]},
+        "accuracy": acc,
         "judge": head["judge"],
         **{label: None if label not in focused else {
             k: focused[label][k] for k in
@@ -834,14 +1041,30 @@ def main():
            for label in ("surrogate_mma_sync", "surrogate_fp16",
                          f"surrogate_h{96 - args.hidden_width}")},
         "train": focused["train"],
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak,
+        # The gather model counts every table gather as HBM traffic; the
+        # kernel's real limiter is the latency and rate of those gathers,
+        # served from L2 (97 % hits) through the L1TEX data pipe, while DRAM
+        # moves ~13 B per particle-step: "bound" names that path.
+        "roofline": {"bound": "l1tex_l2_gather", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                     "model": "672 B per particle-step (2 frames x 4 corners x 21 f32 "
+                              "gathers), every gather counted as HBM traffic",
                      "traffic": None if per_step_traffic is None
                      else per_step_traffic * steps_per_launch,
-                     "model": "672 B per particle-step (2 frames x 4 corners x 21 f32 gathers)",
-                     "peak_kind": peak_kind,
-                     "tensor_tflops": steps_per_launch * tensor_flop_per_step(args.hidden_width)
-                     / kernel_s / 1e12},
+                     "traffic_source": "from_profile: ncu dram__bytes_read.sum + "
+                                       "dram__bytes_write.sum of push_tc_kernel per "
+                                       "particle-step (capture of 100 steps per particle, "
+                                       f"{os.path.relpath(PROFILE, ROOT)}) x this launch's "
+                                       "particle-steps",
+                     "dram_frac": None if per_step_traffic is None
+                     else per_step_traffic * steps_per_launch / kernel_s / 1e9 / peak,
+                     "l1tex_frac": l1tex_frac,
+                     "l1tex_source": "from_profile: L1TEX LSU data-pipe wavefronts, share of "
+                                     "peak (ncu)",
+                     "tensor_tflops": tensor_tflops,
+                     "tensor_frac": tensor_tflops / bf16_peak,
+                     "tensor_peak_kind": bf16_kind},
+        "fp64_roofline": fp64,
         "cpu_baseline": cpu,
         "e2e": {"value": head["e2e"], "unit": "particle-steps/s",
                 "h2d_bytes_per_step": head["state_bytes"],
@@ -853,6 +1076,7 @@ def main():
             f64={"value": f64["value"], "ms": f64["ms_per_step"]}),
         "batched_runs": batched,
         "library_solvers": library,
+        "c2_cli": c2,
         # per timed step: the push, plus 3 cell-sort kernels when sorting
         "gpu_launches": args.steps * (1 + (3 if args.sort_tile > 0 else 0)),
         "clocks": head["clocks"],

@@ -210,6 +210,11 @@ int kpt_context_destroy(kpt_context* ctx);
 /* Order later calls on an external stream (cudaStream_t); NULL = own stream. */
 int kpt_context_set_stream(kpt_context* ctx, void* cuda_stream);
 int kpt_context_synchronize(kpt_context* ctx);
+/* FP64 FMA throughput of the context's GPU in TFLOP/s, measured by a
+ * project-written FMA-chain kernel (best of five launches, clocks as they
+ * are).  No counterpart in the reference: it is the denominator of the plain
+ * FP64 pushes' roofline, since GB300's FP64 pipe, not memory, bounds them. */
+int kpt_context_fp64_fma_rate(kpt_context* ctx, double* tflops);
 /* Push scheduling: KPT_SCHEDULE_REFILL (persistent warps that refill lanes
  * from a work cursor; blocks_per_sm x SM count blocks of 128 threads, 0 =
  * as many as are resident) or KPT_SCHEDULE_SIMPLE (one particle per

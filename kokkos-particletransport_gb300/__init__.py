@@ -224,6 +224,7 @@ def load_library() -> ctypes.CDLL:
         "kpt_context_destroy": (i32, [vp]),
         "kpt_context_set_stream": (i32, [vp, vp]),
         "kpt_context_synchronize": (i32, [vp]),
+        "kpt_context_fp64_fma_rate": (i32, [vp, ctypes.POINTER(ctypes.c_double)]),
         "kpt_context_set_push_schedule": (i32, [vp, i32, i32]),
         "kpt_field_create": (i32, [vp, i32, i32, vp, vp, vp, vp, i32, i32, pvp]),
         "kpt_field_load": (i32, [vp, ctypes.c_char_p, i32, i32, pvp]),
@@ -394,6 +395,13 @@ class Context:
 
     def synchronize(self) -> None:
         _check(self.lib.kpt_context_synchronize(self.handle))
+
+    def fp64_fma_rate(self) -> float:
+        """FP64 FMA throughput of this context's GPU in TFLOP/s, measured now
+        (the denominator of the FP64 pushes' roofline)."""
+        out = ctypes.c_double()
+        _check(self.lib.kpt_context_fp64_fma_rate(self.handle, ctypes.byref(out)))
+        return out.value
 
     def set_stream(self, stream_handle: int) -> None:
         _check(self.lib.kpt_context_set_stream(self.handle, ctypes.c_void_p(stream_handle)))

@@ -515,6 +515,13 @@ int kpt_context_synchronize(kpt_context* ctx) {
     return KPT_OK;
 }
 
+int kpt_context_fp64_fma_rate(kpt_context* ctx, double* tflops) {
+    KPT_REQUIRE(ctx != nullptr && tflops != nullptr, "kpt_context_fp64_fma_rate: NULL argument");
+    if (int rc = activate(ctx)) return rc;
+    KPT_CUDA(kpt::fp64_fma_rate(ctx->sm_count, ctx->stream, tflops));
+    return KPT_OK;
+}
+
 namespace {
 int field_create(kpt_context* ctx, int nx, int ny, const double* x_edges, const double* y_edges,
                  const double* b_cells, const double* v_cells, int table_kind, int precision,

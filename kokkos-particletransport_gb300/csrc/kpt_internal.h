@@ -455,4 +455,8 @@ struct SampleLaunch {
 };
 cudaError_t launch_sample(const SampleLaunch& launch, cudaStream_t stream);
 
+// FP64 FMA throughput of the current device in TFLOP/s (best of five timed
+// launches of a project-written FMA-chain kernel on `stream`).
+cudaError_t fp64_fma_rate(int sm_count, cudaStream_t stream, double* tflops);
+
 }  // namespace kpt

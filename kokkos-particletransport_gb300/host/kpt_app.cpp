@@ -82,6 +82,7 @@ struct RunSettings {
     int histogram_bins{128};
     bool prefetch{true};  // read the next frame file while the GPU pushes
     int device{0};
+    std::string push_stats_path{};  // per-frame push counters and diagnostic times
 
     int intervals() const { return end_frame - start_frame; }
     bool restart() const { return !restart_path.empty(); }
@@ -356,7 +357,9 @@ void print_usage() {
         << "  --inject-y-band LO HI         inject y uniformly in [LO, HI) instead of the domain\n"
         << "  --frame-prefetch on|off       read the next field file during the push (default on)\n"
         << "  --histogram-bins N            momentum histogram bins (default 128)\n"
-        << "  --device N                    CUDA device (default 0)\n";
+        << "  --device N                    CUDA device (default 0)\n"
+        << "  --push-stats PATH             write per-frame substep counts and diagnostic\n"
+        << "                                times to PATH (CSV)\n";
 }
 
 std::string next_value(int argc, char** argv, int& i, const std::string& option) {
@@ -478,6 +481,8 @@ RunSettings parse(int argc, char** argv) {
                 throw std::runtime_error("--frame-prefetch needs on or off.");
             }
             s.prefetch = v == "on";
+        } else if (arg == "--push-stats") {
+            s.push_stats_path = next_value(argc, argv, i, arg);
         } else {
             throw std::runtime_error("Unknown option: " + arg);
         }
@@ -731,6 +736,7 @@ void write_histogram(const RunSettings& s, kpt_context* ctx, kpt_particles* part
 
 struct FrameTiming {
     double read_s{0.0}, inject_s{0.0}, move_s{0.0}, split_s{0.0};
+    double summary_s{0.0}, histogram_s{0.0};
     std::uint64_t injected{0}, split{0}, skipped{0};
 };
 
@@ -804,6 +810,16 @@ int run(const RunSettings& s) {
     std::ofstream log(log_path, s.restart() ? (std::ios::out | std::ios::app) : std::ios::out);
     if (!log) {
         throw std::runtime_error("Failed to open run log output.");
+    }
+    std::ofstream push_stats;
+    if (!s.push_stats_path.empty()) {
+        push_stats.open(s.push_stats_path, std::ios::out);
+        if (!push_stats) {
+            throw std::runtime_error("Failed to open push stats output.");
+        }
+        push_stats << "frame,stored,pushed,particle_steps,failed,max_steps,read_seconds,"
+                      "inject_seconds,move_seconds,split_seconds,summary_seconds,"
+                      "histogram_seconds\n";
     }
     const std::uint64_t seed =
         s.restart() ? s.seed + 0x9e3779b97f4a7c15ull * static_cast<std::uint64_t>(s.start_frame + 1)
@@ -885,8 +901,10 @@ int run(const RunSettings& s) {
         check(kpt_context_synchronize(ctx.get()));
         timing.inject_s = seconds_since(t0);
         t0 = Clock::now();
+        kpt_push_stats push{};
         check(kpt_push_interval(ctx.get(), parts.get(), lower.get(), upper.get(), &physics,
-                                static_cast<std::uint32_t>(frame), seed, nullptr));
+                                static_cast<std::uint32_t>(frame), seed,
+                                push_stats.is_open() ? &push : nullptr));
         check(kpt_context_synchronize(ctx.get()));
         timing.move_s = seconds_since(t0);
         t0 = Clock::now();
@@ -900,8 +918,10 @@ int run(const RunSettings& s) {
         const bool finishing = final_frame || walltime_hit;
         const int done = frame + 1 - s.start_frame;
         if (done % s.diagnostic_interval == 0 || finishing) {
+            const auto summary_start = Clock::now();
             kpt_summary sum{};
             check(kpt_summarize(ctx.get(), parts.get(), &sum));
+            timing.summary_s = seconds_since(summary_start);
             write_summary_row(summary, frame + 1, static_cast<double>(frame + 1) * s.mhd_dt, sum,
                               timing, frame_s, elapsed_s);
             summary.flush();
@@ -914,7 +934,19 @@ int run(const RunSettings& s) {
             log_line(log, line.str());
         }
         if ((s.histogram_interval > 0 && done % s.histogram_interval == 0) || finishing) {
+            const auto histogram_start = Clock::now();
             write_histogram(s, ctx.get(), parts.get(), frame + 1);
+            timing.histogram_s = seconds_since(histogram_start);
+        }
+        if (push_stats.is_open()) {
+            std::uint64_t stored = 0;
+            check(kpt_particles_count(parts.get(), &stored, nullptr));
+            push_stats << frame + 1 << ',' << stored << ',' << push.pushed << ','
+                       << push.particle_steps << ',' << push.failed << ',' << push.max_steps
+                       << ',' << std::setprecision(9) << timing.read_s << ',' << timing.inject_s
+                       << ',' << timing.move_s << ',' << timing.split_s << ','
+                       << timing.summary_s << ',' << timing.histogram_s << '\n';
+            push_stats.flush();
         }
         if (s.snapshot_interval > 0 && (done % s.snapshot_interval == 0 || finishing)) {
             const auto snap_start = Clock::now();

@@ -1,0 +1,115 @@
+"""The metric's spectrum bar over many consecutive intervals.
+
+The focused push (slab-QLT closure, sigma^2 = 0.1, gamma_k = 5/3) on a
+128x256 stretched-y Harris + islands field, 16 384 particles (p = p0, pitch
+cosine uniform on [-1, 1]) pushed 10 consecutive intervals of 500 fixed
+steps: by the FP64 oracle (the reference), and on the GPU by the mixed push
+with the plain closure and by the mixed push with the learned closure on
+either tensor-core engine.  After 10 intervals the oracle's momentum spectrum
+spans at least 10 of the driver's 64 bins.
+
+* paired (same seed, so the same keyed noise): 64-bin momentum and 16-bin
+  pitch-cosine L1 <= 1 % against the oracle;
+* independent (another seed, same start): two-sample chi-square p > 0.01 for
+  the 64 momentum bins, a fine ln(p/p0) histogram fitted to the oracle and
+  the 16 pitch-cosine bins.
+
+The comparison itself is pinned on the CPU (tests/test_spectra.py): the same
+figures reject an oracle run with a planted closure error.
+"""
+from __future__ import annotations
+
+import importlib
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+N, INTERVALS, SUBSTEPS, FRAME, SEED = 16384, 10, 500, 7, 99
+TRAIN = dict(samples=524288, steps=8000, batch=4096, learning_rate=1e-2, seed=2024)
+
+
+def _params(binding, closure):
+    rel = (1.0 + 1e-6) / SUBSTEPS
+    return binding.default_params(kperp_over_kpara=0.05, focused=1, closure=closure,
+                                  qlt_sigma2=0.1, qlt_spectral_index=5.0 / 3.0,
+                                  dt_min_rel=rel, dt_max_rel=rel)
+
+
+@pytest.fixture(scope="module")
+def workload(fields_mod, binding, oracle):
+    ye = fields_mod.stretched_edges(256, -2.0, 2.0, strength=4.0)
+    f0 = fields_mod.harris_field(128, 256, y_edges=ye, island_amplitude=0.1, noise=0.01, seed=5)
+    f1 = fields_mod.harris_field(128, 256, y_edges=ye, island_amplitude=0.1, noise=0.01, seed=6)
+    plain = _params(binding, 1)
+    grid = oracle.grid(f0.x_edges, f0.y_edges)
+    start = binding.empty_particles(N)
+    count = oracle.inject(grid, plain, FRAME * 0.1, FRAME, SEED, N, 0, N, start)
+    assert count == N
+    start["status"][:] = 0
+    start["t"][:] = FRAME * plain["mhd_dt"]
+    ref = {k: v.copy() for k, v in start.items()}
+    lo, up = oracle.table(f0, True), oracle.table(f1, True)
+    for k in range(INTERVALS):
+        oracle.push(grid, lo, up, plain, (FRAME + k) * plain["mhd_dt"], FRAME + k, SEED, N, ref)
+    oracle.free_grid(grid)
+    return f0, f1, start, ref
+
+
+@pytest.fixture(scope="module")
+def network(ctx, kpt, binding):
+    settings = kpt.settings_from_dict(_params(binding, 2))
+    net = ctx.train_surrogate(settings, element_type=kpt.SURROGATE_BF16, hidden_width=64,
+                              **TRAIN)
+    yield net
+    ctx.set_surrogate(None)
+    net.close()
+
+
+def _gpu_run(ctx, kpt, f0, f1, start, settings, seed):
+    lower = ctx.field(f0, kpt.TABLE_FOCUSED21, kpt.PRECISION_MIXED)
+    upper = ctx.field(f1, kpt.TABLE_FOCUSED21, kpt.PRECISION_MIXED)
+    parts = ctx.particles(N)
+    parts.upload(start, N)
+    failed = 0
+    for k in range(INTERVALS):
+        ctx.sort(parts, lower, 8, 8)
+        failed += ctx.push_interval(parts, lower, upper, settings, FRAME + k, seed).failed
+    out = parts.download(N)
+    for obj in (lower, upper, parts):
+        obj.close()
+    return out, failed
+
+
+@pytest.mark.parametrize("closure", ["plain", "learned_tcgen05", "learned_mma_sync"])
+def test_spectra_match_fp64_oracle_over_ten_intervals(ctx, kpt, binding, workload, network,
+                                                       closure):
+    spectra = importlib.import_module("kokkos-particletransport_gb300.spectra")
+    f0, f1, start, ref = workload
+    if closure == "plain":
+        ctx.set_surrogate(None)
+        settings = kpt.settings_from_dict(_params(binding, 1))
+    else:
+        network.engine = (kpt.ENGINE_TCGEN05 if closure == "learned_tcgen05"
+                          else kpt.ENGINE_MMA_SYNC)
+        ctx.set_surrogate(network)
+        settings = kpt.settings_from_dict(_params(binding, 2))
+    try:
+        paired, failed = _gpu_run(ctx, kpt, f0, f1, start, settings, SEED)
+        assert failed == 0
+        indep, failed = _gpu_run(ctx, kpt, f0, f1, start, settings, SEED + 1)
+        assert failed == 0
+    finally:
+        ctx.set_surrogate(None)
+        network.engine = kpt.ENGINE_TCGEN05
+    p0 = settings.p0
+    same = spectra.compare_populations(paired, ref, p0)
+    other = spectra.compare_populations(indep, ref, p0)
+    print(closure, "paired", {k: same[k]["l1"] for k in ("p64", "lnp_fine", "mu16")},
+          "independent p", {k: other[k]["p_value"] for k in ("p64", "lnp_fine", "mu16")})
+    assert same["p64"]["populated_bins"] >= 10
+    assert same["p64"]["l1"] <= 0.01
+    assert same["mu16"]["l1"] <= 0.01
+    for key in ("p64", "lnp_fine", "mu16"):
+        assert other[key]["p_value"] > 0.01, (key, other[key])
