@@ -215,6 +215,12 @@ int kpt_context_synchronize(kpt_context* ctx);
  * are).  No counterpart in the reference: it is the denominator of the plain
  * FP64 pushes' roofline, since GB300's FP64 pipe, not memory, bounds them. */
 int kpt_context_fp64_fma_rate(kpt_context* ctx, double* tflops);
+/* out[i] = x[i]^y[i] by the FP64 push's power function, evaluated on the GPU
+ * (host arrays; parity and diagnostics).  The FP64 push computes every
+ * Kokkos::pow of the reference's kernels (src/main.cpp:1180-1185,
+ * :1439-1444, :1553-1580) with this function; the oracle and the reference
+ * build on the shim use the same one, so powers round alike on both sides. */
+int kpt_math_pow(kpt_context* ctx, uint64_t n, const double* x, const double* y, double* out);
 /* Push scheduling: KPT_SCHEDULE_REFILL (persistent warps that refill lanes
  * from a work cursor; blocks_per_sm x SM count blocks of 128 threads, 0 =
  * as many as are resident) or KPT_SCHEDULE_SIMPLE (one particle per

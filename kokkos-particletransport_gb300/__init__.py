@@ -225,6 +225,7 @@ def load_library() -> ctypes.CDLL:
         "kpt_context_set_stream": (i32, [vp, vp]),
         "kpt_context_synchronize": (i32, [vp]),
         "kpt_context_fp64_fma_rate": (i32, [vp, ctypes.POINTER(ctypes.c_double)]),
+        "kpt_math_pow": (i32, [vp, ctypes.c_uint64, vp, vp, vp]),
         "kpt_context_set_push_schedule": (i32, [vp, i32, i32]),
         "kpt_field_create": (i32, [vp, i32, i32, vp, vp, vp, vp, i32, i32, pvp]),
         "kpt_field_load": (i32, [vp, ctypes.c_char_p, i32, i32, pvp]),
@@ -395,6 +396,17 @@ class Context:
 
     def synchronize(self) -> None:
         _check(self.lib.kpt_context_synchronize(self.handle))
+
+    def pow(self, x, y) -> np.ndarray:
+        """x^y elementwise by the FP64 push's power function, on the GPU."""
+        x, y = np.broadcast_arrays(np.asarray(x, dtype=np.float64),
+                                   np.asarray(y, dtype=np.float64))
+        x = np.ascontiguousarray(x).ravel()
+        y = np.ascontiguousarray(y).ravel()
+        out = np.empty_like(x)
+        _check(self.lib.kpt_math_pow(self.handle, x.size, x.ctypes.data, y.ctypes.data,
+                                     out.ctypes.data))
+        return out
 
     def fp64_fma_rate(self) -> float:
         """FP64 FMA throughput of this context's GPU in TFLOP/s, measured now

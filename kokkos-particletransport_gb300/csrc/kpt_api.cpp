@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "kpt_internal.h"
+#include "kpt_pow.h"
 
 // One substep in KPT_JUDGE_PERIOD (a power of two) of every particle also
 // evaluates the plain closure to judge the learned one.
@@ -519,6 +520,23 @@ int kpt_context_fp64_fma_rate(kpt_context* ctx, double* tflops) {
     KPT_REQUIRE(ctx != nullptr && tflops != nullptr, "kpt_context_fp64_fma_rate: NULL argument");
     if (int rc = activate(ctx)) return rc;
     KPT_CUDA(kpt::fp64_fma_rate(ctx->sm_count, ctx->stream, tflops));
+    return KPT_OK;
+}
+
+int kpt_math_pow(kpt_context* ctx, uint64_t n, const double* x, const double* y, double* out) {
+    KPT_REQUIRE(ctx != nullptr && (n == 0 || (x && y && out)), "kpt_math_pow: NULL argument");
+    if (n == 0) return KPT_OK;
+    if (int rc = activate(ctx)) return rc;
+    ScopedBuffer buf;
+    KPT_CUDA(buf.reserve(3 * n * sizeof(double)));
+    double* dx = buf.as<double>();
+    double* dy = dx + n;
+    double* dout = dy + n;
+    KPT_CUDA(cudaMemcpyAsync(dx, x, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    KPT_CUDA(cudaMemcpyAsync(dy, y, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    KPT_CUDA(kpt::launch_pow(n, dx, dy, dout, ctx->sm_count, ctx->stream));
+    KPT_CUDA(cudaMemcpyAsync(out, dout, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    KPT_CUDA(cudaStreamSynchronize(ctx->stream));
     return KPT_OK;
 }
 
@@ -1129,14 +1147,14 @@ int kpt_split(kpt_context* ctx, kpt_particles* parts, const kpt_settings* settin
         return KPT_OK;
     }
     if (int rc = activate(ctx)) return rc;
-    // Per-level thresholds pmin_split * ratio^level (host pow) up to the first
+    // Per-level thresholds pmin_split * ratio^level (the project pow) up to the first
     // level whose threshold exceeds pmax; later levels can never split.
     const double pmin_split = settings->pmin_split_over_p0 * settings->p0;
     if (ctx->split_level_count == 0 || ctx->split_key[0] != pmin_split ||
         ctx->split_key[1] != settings->split_ratio || ctx->split_key[2] != settings->pmax) {
         std::vector<double> thresholds;
         for (int level = 0; level < 65536; ++level) {
-            const double thr = pmin_split * std::pow(settings->split_ratio,
+            const double thr = pmin_split * kpt_pow(settings->split_ratio,
                                                      static_cast<double>(level));
             thresholds.push_back(thr);
             if (!(thr < settings->pmax)) {
@@ -1151,7 +1169,7 @@ int kpt_split(kpt_context* ctx, kpt_particles* parts, const kpt_settings* settin
         std::vector<double> table(2 * static_cast<size_t>(levels));
         for (int level = 0; level < levels; ++level) {
             table[level] = thresholds[level];
-            table[levels + level] = std::pow(0.5, static_cast<double>(level + 1));
+            table[levels + level] = kpt_pow(0.5, static_cast<double>(level + 1));
         }
         KPT_CUDA(ctx->split_levels.reserve(table.size() * sizeof(double)));
         KPT_CUDA(cudaMemcpyAsync(ctx->split_levels.ptr, table.data(),

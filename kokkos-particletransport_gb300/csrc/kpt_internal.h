@@ -47,6 +47,11 @@ struct PushLaunch {
 };
 
 cudaError_t launch_push_interval(const PushLaunch& launch, cudaStream_t stream);
+// The plain FP64 push and FP64 table sampling, built in their own translation
+// unit without FMA contraction (kpt_push_f64.cu).
+cudaError_t launch_push_interval_f64(const PushLaunch& launch, cudaStream_t stream);
+struct SampleLaunch;
+cudaError_t launch_sample_f64(const SampleLaunch& launch, int blocks, cudaStream_t stream);
 
 // Batched mixed-precision push over many independent runs (one launch).
 // params: device array of per-run parameter blocks (push_params_size()
@@ -458,5 +463,8 @@ cudaError_t launch_sample(const SampleLaunch& launch, cudaStream_t stream);
 // FP64 FMA throughput of the current device in TFLOP/s (best of five timed
 // launches of a project-written FMA-chain kernel on `stream`).
 cudaError_t fp64_fma_rate(int sm_count, cudaStream_t stream, double* tflops);
+// out[i] = kpt_pow(x[i], y[i]) on the device (device arrays).
+cudaError_t launch_pow(uint64_t n, const double* x, const double* y, double* out, int sm_count,
+                       cudaStream_t stream);
 
 }  // namespace kpt

@@ -1,14 +1,18 @@
-// Throughput probe of the FP64 pipe: the denominator of the FP64 pushes'
-// roofline.  GB300 executes FP64 at a small fraction of its FP32 rate, and
-// the plain FP64 push is bound there, not by memory; this kernel measures
-// the rate the pipe actually sustains on the part the library runs on, with
-// the clocks as they are (nothing is locked or changed).
+// Diagnostics of the FP64 arithmetic:
+//  * a throughput probe of the FP64 pipe, the denominator of the FP64
+//    pushes' roofline.  GB300 executes FP64 at a small fraction of its FP32
+//    rate, and the plain FP64 push is bound there, not by memory; the probe
+//    measures the rate the pipe sustains on the part the library runs on,
+//    with the clocks as they are (nothing is locked or changed);
+//  * the FP64 push's power function (kpt_pow.h) evaluated on the device, so
+//    tests can compare it bit for bit with the host's.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cstdint>
 
 #include "kpt_internal.h"
+#include "kpt_pow.h"
 
 namespace kpt {
 namespace {
@@ -40,7 +44,25 @@ __global__ void __launch_bounds__(256) fp64_fma_kernel(int iters, double m, doub
     }
 }
 
+__global__ void __launch_bounds__(256) pow_kernel(uint64_t n, const double* __restrict__ x,
+                                                  const double* __restrict__ y,
+                                                  double* __restrict__ out) {
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        out[i] = kpt_pow(x[i], y[i]);
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_pow(uint64_t n, const double* x, const double* y, double* out, int sm_count,
+                       cudaStream_t stream) {
+    if (n == 0) return cudaSuccess;
+    const uint64_t want = (n + 255) / 256;
+    const uint64_t cap = static_cast<uint64_t>(sm_count) * 16;
+    pow_kernel<<<static_cast<int>(want < cap ? want : cap), 256, 0, stream>>>(n, x, y, out);
+    return cudaGetLastError();
+}
 
 cudaError_t fp64_fma_rate(int sm_count, cudaStream_t stream, double* tflops) {
     const int threads = 256;

@@ -30,6 +30,16 @@
 
 #include "kpt_device.cuh"
 #include "kpt_internal.h"
+#include "kpt_pow.h"
+
+// What this translation unit emits.  0 (the default): everything but the
+// plain FP64 push and the FP64 table sampling; 1: only those two, compiled
+// apart with FMA contraction off (kpt_push_f64.cu, nvcc -fmad=false), so
+// their double arithmetic rounds exactly as written, as the host oracle's
+// does (the oracle and the reference build use -ffp-contract=off).
+#ifndef KPT_PUSH_PART
+#define KPT_PUSH_PART 0
+#endif
 
 namespace kpt {
 namespace {
@@ -48,7 +58,8 @@ struct Num;
 
 template <>
 struct Num<double> {
-    static __device__ __forceinline__ double pow(double a, double b) { return ::pow(a, b); }
+    // the project pow (kpt_pow.h): rounds exactly as the host oracle does
+    static __device__ __forceinline__ double pow(double a, double b) { return kpt_pow(a, b); }
     static __device__ __forceinline__ double sqrt(double a) { return ::sqrt(a); }
     static __device__ __forceinline__ double div(double a, double b) { return a / b; }
     static __device__ __forceinline__ bool finite(double a) { return isfinite(a); }
@@ -1396,6 +1407,7 @@ cudaError_t launch_push(const PushLaunch& L, cudaStream_t stream) {
     return cudaGetLastError();
 }
 
+#if KPT_PUSH_PART == 0
 // ---------------------------------------------------------------- batches
 // Many independent runs (own fields, settings, particles, seeds and frames)
 // in one persistent launch.  The work cursor walks the concatenation of the
@@ -1511,6 +1523,8 @@ __global__ void batch_clear_counters_kernel(void* params, int runs, unsigned lon
     c->max_steps = 0;
 }
 
+#endif  // KPT_PUSH_PART == 0
+
 // Table values at given positions through the FP64 sampling path (driver
 // wrap, half-cell shift, grid wrap, stencil, time interpolation).
 template <typename T, bool FOCUSED>
@@ -1537,6 +1551,24 @@ __global__ void sample_kernel(const SampleLaunch L) {
 
 }  // namespace
 
+#if KPT_PUSH_PART == 1
+
+cudaError_t launch_push_interval_f64(const PushLaunch& launch, cudaStream_t stream) {
+    return launch.focused ? launch_push<StateF64, true>(launch, stream)
+                          : launch_push<StateF64, false>(launch, stream);
+}
+
+cudaError_t launch_sample_f64(const SampleLaunch& L, int blocks, cudaStream_t stream) {
+    if (L.focused) {
+        sample_kernel<double, true><<<blocks, 128, 0, stream>>>(L);
+    } else {
+        sample_kernel<double, false><<<blocks, 128, 0, stream>>>(L);
+    }
+    return cudaGetLastError();
+}
+
+#else  // KPT_PUSH_PART == 0
+
 cudaError_t launch_sample(const SampleLaunch& L, cudaStream_t stream) {
     if (L.n == 0) {
         return cudaSuccess;
@@ -1545,17 +1577,12 @@ cudaError_t launch_sample(const SampleLaunch& L, cudaStream_t stream) {
     const uint64_t want = (L.n + threads - 1) / threads;
     const int blocks = static_cast<int>(want > 152u * 16u ? 152u * 16u : want);
     if (L.precision == kPrecisionF64) {
-        if (L.focused) {
-            sample_kernel<double, true><<<blocks, threads, 0, stream>>>(L);
-        } else {
-            sample_kernel<double, false><<<blocks, threads, 0, stream>>>(L);
-        }
+        return launch_sample_f64(L, blocks, stream);
+    }
+    if (L.focused) {
+        sample_kernel<float, true><<<blocks, threads, 0, stream>>>(L);
     } else {
-        if (L.focused) {
-            sample_kernel<float, true><<<blocks, threads, 0, stream>>>(L);
-        } else {
-            sample_kernel<float, false><<<blocks, threads, 0, stream>>>(L);
-        }
+        sample_kernel<float, false><<<blocks, threads, 0, stream>>>(L);
     }
     return cudaGetLastError();
 }
@@ -1601,8 +1628,7 @@ int batch_max_runs() { return kBatchMaxRuns; }
 
 cudaError_t launch_push_interval(const PushLaunch& launch, cudaStream_t stream) {
     if (launch.precision == kPrecisionF64) {
-        return launch.focused ? launch_push<StateF64, true>(launch, stream)
-                              : launch_push<StateF64, false>(launch, stream);
+        return launch_push_interval_f64(launch, stream);
     }
     if (launch.surrogate != nullptr) {
         const SurrogateBox& box = launch.surrogate->box;
@@ -1616,5 +1642,7 @@ cudaError_t launch_push_interval(const PushLaunch& launch, cudaStream_t stream) 
     return launch.focused ? launch_push<StateMixed, true>(launch, stream)
                           : launch_push<StateMixed, false>(launch, stream);
 }
+
+#endif  // KPT_PUSH_PART
 
 }  // namespace kpt

@@ -138,6 +138,7 @@ class Oracle:
         lib.kpt_oracle_summarize.argtypes = [u64, vp, vp, vp, vp, vp, vp]
         lib.kpt_oracle_wrap.restype = dbl
         lib.kpt_oracle_wrap.argtypes = [dbl, dbl, dbl, dbl]
+        lib.kpt_oracle_pow_array.argtypes = [u64, vp, vp, vp]
         lib.kpt_oracle_sample.argtypes = [vp, vp, vp, i32, dbl, dbl, dbl, i32, vp]
         lib.kpt_oracle_qlt_dmumu.restype = dbl
         lib.kpt_oracle_qlt_dmumu.argtypes = [dbl] * 7
@@ -238,6 +239,15 @@ class Oracle:
 
     def wrap(self, value: float, lower: float, upper: float, width: float) -> float:
         return float(self.lib.kpt_oracle_wrap(value, lower, upper, width))
+
+    def pow(self, x, y) -> np.ndarray:
+        """The project pow (kpt_pow.h) on the host, elementwise."""
+        x, y = np.broadcast_arrays(np.asarray(x, dtype=np.float64),
+                                   np.asarray(y, dtype=np.float64))
+        x, y = np.ascontiguousarray(x).ravel(), np.ascontiguousarray(y).ravel()
+        out = np.empty_like(x)
+        self.lib.kpt_oracle_pow_array(ctypes.c_uint64(x.size), _ptr(x), _ptr(y), _ptr(out))
+        return out
 
 
 class ReferenceHarness:

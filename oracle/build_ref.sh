@@ -14,7 +14,8 @@ fi
 mkdir -p "$here/_ref"
 g++ -O2 -std=c++20 -fopenmp -ffp-contract=off -fPIC -shared \
     -Dmain=kpt_ref_main \
-    -I "$here/kokkos_shim" -I "$ref" -I "$ref/include" \
+    -I "$here/kokkos_shim" -I "$here/../kokkos-particletransport_gb300/csrc" \
+    -I "$ref" -I "$ref/include" \
     "$here/ref_harness.cpp" -o "$here/_ref/libkpt_ref.so.tmp"
 mv "$here/_ref/libkpt_ref.so.tmp" "$here/_ref/libkpt_ref.so"
 echo "build_ref: wrote $here/_ref/libkpt_ref.so"

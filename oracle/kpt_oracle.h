@@ -159,6 +159,9 @@ double kpt_oracle_qlt_dmumu_dmu(double mu, double dmumu, double omega, double sp
 /* wrap_periodic_coordinate (src/main.cpp:642-665). */
 double kpt_oracle_wrap(double value, double lower, double upper, double width);
 
+/* The project pow (kpt_pow.h) on the host, elementwise: out[i] = x[i]^y[i]. */
+void kpt_oracle_pow_array(uint64_t n, const double* x, const double* y, double* out);
+
 /* Sample a table (C components) at one particle position the way the push
  * does (src/main.cpp:1055-1077, 1142-1148). */
 void kpt_oracle_sample(const kpt_oracle_grid* grid, const double* lower_table,
