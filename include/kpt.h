@@ -37,7 +37,7 @@
 extern "C" {
 #endif
 
-#define KPT_ABI_VERSION 1
+#define KPT_ABI_VERSION 2
 
 enum kpt_status {
     KPT_OK = 0,
@@ -812,11 +812,15 @@ typedef struct kpt_batch kpt_batch;
 
 typedef struct kpt_batch_tuning {
     int32_t sort_tile;      /* cell-sort tile (cells), 0 = no sort */
-    int32_t blocks_per_sm;  /* resident 128-thread blocks per SM, 0 = as many as fit */
+    int32_t blocks_per_sm;  /* resident blocks per SM, 0 = as many as fit */
     int32_t sort_every;     /* sort every k intervals */
     int32_t candidates;     /* schedules timed */
-    float best_ms;          /* time of the chosen schedule over the tuning intervals */
-    float pad;
+    float best_ms;          /* median time of the chosen schedule over the tuning intervals */
+    float spread;           /* (max - min) / median of the chosen schedule's timings */
+    int32_t threads_per_block;   /* 64, 128 or 256 */
+    int32_t particles_per_lane;  /* 1 or 2 */
+    int32_t repeats;        /* timings per candidate */
+    int32_t pad;
 } kpt_batch_tuning;
 
 int kpt_batch_create(kpt_context* ctx, kpt_batch** out);
@@ -829,6 +833,13 @@ int kpt_batch_add_run(kpt_batch* batch, kpt_particles* particles, const kpt_fiel
 int kpt_batch_set_schedule(kpt_batch* batch, int sort_tile, int blocks_per_sm, int sort_every);
 int kpt_batch_get_schedule(const kpt_batch* batch, int* sort_tile, int* blocks_per_sm,
                            int* sort_every);
+/* Launch shape of the batched push: threads per block (64, 128 or 256) and
+ * particles per lane (1 or 2: a lane advances that many particles side by
+ * side, each slot refilling from the work cursor on its own).  Results do not
+ * depend on the shape (noise is keyed by particle). */
+int kpt_batch_set_launch_shape(kpt_batch* batch, int threads_per_block, int particles_per_lane);
+int kpt_batch_get_launch_shape(const kpt_batch* batch, int* threads_per_block,
+                               int* particles_per_lane);
 /* Push every run through `intervals` consecutive intervals (graph replay when
  * use_graph != 0 and the context's stream can be captured). */
 int kpt_batch_run(kpt_batch* batch, uint32_t intervals, int use_graph);
@@ -837,9 +848,13 @@ int kpt_batch_stats(const kpt_batch* batch, int run, kpt_push_stats* out);
 /* A run's next interval (get / set). */
 int kpt_batch_frame(const kpt_batch* batch, int run, uint32_t* frame);
 int kpt_batch_set_frame(kpt_batch* batch, int run, uint32_t frame);
-/* Time the candidate schedules (cell-sort tile 0/8/16/32, sort every 1 or 2
- * intervals, 2 / 3 / all-resident blocks per SM) over `intervals` intervals
- * on the current state, restore the state, keep the fastest schedule. */
+/* Time candidate schedules over `intervals` intervals on the current state,
+ * restoring the state after each timing, and keep the fastest (median of
+ * three timings per candidate).  Stage 1: cell-sort tile 0/8/16/32 and sort
+ * every 1 or 2 intervals, at 128 threads, one particle per lane, all resident
+ * blocks.  Stage 2, with the chosen sort: 64/128/256 threads per block x 1 or
+ * 2 particles per lane x residency (all that fit, or the threads of 3 or 2
+ * blocks of 128). */
 int kpt_batch_autotune(kpt_batch* batch, uint32_t intervals, kpt_batch_tuning* out);
 
 #ifdef __cplusplus

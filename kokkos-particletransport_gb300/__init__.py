@@ -110,7 +110,9 @@ class BatchTuning(ctypes.Structure):
     """kpt_batch_tuning: the schedule the autotuner chose."""
     _fields_ = [("sort_tile", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
                 ("sort_every", ctypes.c_int32), ("candidates", ctypes.c_int32),
-                ("best_ms", ctypes.c_float), ("pad", ctypes.c_float)]
+                ("best_ms", ctypes.c_float), ("spread", ctypes.c_float),
+                ("threads_per_block", ctypes.c_int32), ("particles_per_lane", ctypes.c_int32),
+                ("repeats", ctypes.c_int32), ("pad", ctypes.c_int32)]
 
 
 class SplitPolicy(ctypes.Structure):
@@ -290,6 +292,8 @@ def load_library() -> ctypes.CDLL:
         "kpt_batch_add_run": (i32, [vp, vp, vp, vp, vp, u64, u32, vp]),
         "kpt_batch_set_schedule": (i32, [vp, i32, i32, i32]),
         "kpt_batch_get_schedule": (i32, [vp, vp, vp, vp]),
+        "kpt_batch_set_launch_shape": (i32, [vp, i32, i32]),
+        "kpt_batch_get_launch_shape": (i32, [vp, vp, vp]),
         "kpt_batch_run": (i32, [vp, u32, i32]),
         "kpt_batch_stats": (i32, [vp, i32, vp]),
         "kpt_batch_frame": (i32, [vp, i32, vp]),
@@ -1116,6 +1120,16 @@ class Batch(_Handle):
         _check(self.ctx.lib.kpt_batch_get_schedule(self.handle, ctypes.byref(t), ctypes.byref(b),
                                                    ctypes.byref(e)))
         return {"sort_tile": t.value, "blocks_per_sm": b.value, "sort_every": e.value}
+
+    def set_launch_shape(self, threads_per_block: int = 128, particles_per_lane: int = 1) -> None:
+        _check(self.ctx.lib.kpt_batch_set_launch_shape(self.handle, int(threads_per_block),
+                                                       int(particles_per_lane)))
+
+    def launch_shape(self):
+        t, p = ctypes.c_int(), ctypes.c_int()
+        _check(self.ctx.lib.kpt_batch_get_launch_shape(self.handle, ctypes.byref(t),
+                                                       ctypes.byref(p)))
+        return {"threads_per_block": t.value, "particles_per_lane": p.value}
 
     def run(self, intervals: int, use_graph: bool = True) -> None:
         _check(self.ctx.lib.kpt_batch_run(self.handle, int(intervals), int(use_graph)))

@@ -3586,10 +3586,12 @@ struct kpt_batch {
     int sort_tile = 16;
     int blocks_per_sm = 0;
     int sort_every = 1;
+    int threads = 128;            // threads per block of the batched push
+    int particles_per_lane = 1;   // particles a lane advances side by side
     DeviceBuffer params, offsets, cursor, counters, saved;
     // cached graph of the last interval loop
     cudaGraphExec_t graph = nullptr;
-    uint32_t graph_key[5] = {0, 0, 0, 0, 0};
+    uint32_t graph_key[7] = {0, 0, 0, 0, 0, 0, 0};
 };
 
 namespace {
@@ -3643,6 +3645,8 @@ kpt::BatchLaunch batch_launch(const kpt_batch* b) {
     B.cursor = b->cursor.as<unsigned long long>();
     B.sm_count = b->ctx->sm_count;
     B.blocks_per_sm = b->blocks_per_sm;
+    B.threads = b->threads;
+    B.particles_per_lane = b->particles_per_lane;
     return B;
 }
 
@@ -3753,6 +3757,25 @@ int kpt_batch_set_schedule(kpt_batch* b, int sort_tile, int blocks_per_sm, int s
     return KPT_OK;
 }
 
+int kpt_batch_set_launch_shape(kpt_batch* b, int threads_per_block, int particles_per_lane) {
+    KPT_REQUIRE(b != nullptr, "kpt_batch_set_launch_shape: NULL handle");
+    KPT_REQUIRE(kpt::batch_shape_supported(threads_per_block, particles_per_lane),
+                "kpt_batch_set_launch_shape: threads_per_block 64, 128 or 256 and "
+                "particles_per_lane 1 or 2");
+    b->threads = threads_per_block;
+    b->particles_per_lane = particles_per_lane;
+    batch_drop_graph(b);
+    return KPT_OK;
+}
+
+int kpt_batch_get_launch_shape(const kpt_batch* b, int* threads_per_block,
+                               int* particles_per_lane) {
+    KPT_REQUIRE(b != nullptr, "kpt_batch_get_launch_shape: NULL handle");
+    if (threads_per_block) *threads_per_block = b->threads;
+    if (particles_per_lane) *particles_per_lane = b->particles_per_lane;
+    return KPT_OK;
+}
+
 int kpt_batch_get_schedule(const kpt_batch* b, int* sort_tile, int* blocks_per_sm,
                            int* sort_every) {
     KPT_REQUIRE(b != nullptr, "kpt_batch_get_schedule: NULL handle");
@@ -3770,10 +3793,12 @@ int kpt_batch_run(kpt_batch* b, uint32_t intervals, int use_graph) {
     if (int rc = activate(ctx)) return rc;
     if (int rc = batch_prepare(b)) return rc;
     cudaStream_t st = ctx->stream;
-    const uint32_t key[5] = {intervals, static_cast<uint32_t>(b->sort_tile),
+    const uint32_t key[7] = {intervals, static_cast<uint32_t>(b->sort_tile),
                              static_cast<uint32_t>(b->blocks_per_sm),
                              static_cast<uint32_t>(b->sort_every),
-                             static_cast<uint32_t>(b->runs.size())};
+                             static_cast<uint32_t>(b->runs.size()),
+                             static_cast<uint32_t>(b->threads),
+                             static_cast<uint32_t>(b->particles_per_lane)};
     if (use_graph && st != nullptr) {
         if (b->graph == nullptr || std::memcmp(key, b->graph_key, sizeof(key)) != 0) {
             batch_drop_graph(b);
@@ -3864,9 +3889,6 @@ int kpt_batch_autotune(kpt_batch* b, uint32_t intervals, kpt_batch_tuning* out) 
         return KPT_OK;
     };
     if (int rc = copy_state(true)) return rc;
-    const int tiles[4] = {0, 8, 16, 32};
-    const int every[2] = {1, 2};
-    const int bps[3] = {0, 3, 2};  // 0 = as many as fit
     const std::vector<uint32_t> frames = [&] {
         std::vector<uint32_t> f;
         for (const kpt_batch::Run& run : b->runs) f.push_back(run.frame);
@@ -3875,32 +3897,76 @@ int kpt_batch_autotune(kpt_batch* b, uint32_t intervals, kpt_batch_tuning* out) 
     cudaEvent_t e0, e1;
     KPT_CUDA(cudaEventCreate(&e0));
     KPT_CUDA(cudaEventCreate(&e1));
-    float best_ms = 0.0f;
-    int best_tile = b->sort_tile, best_bps = b->blocks_per_sm, best_every = b->sort_every;
+    const int repeats = 3;
+    // One candidate: its median over `repeats` timings of `intervals`
+    // intervals from the saved state, and the spread (max - min) / median.
+    auto time_candidate = [&](float* median, float* spread) -> int {
+        batch_drop_graph(b);
+        if (int rc = batch_prepare(b)) return rc;
+        float ms[repeats];
+        for (int r = 0; r < repeats; ++r) {
+            KPT_CUDA(cudaEventRecord(e0, st));
+            KPT_CUDA(batch_enqueue(b, intervals, st));
+            KPT_CUDA(cudaEventRecord(e1, st));
+            KPT_CUDA(cudaEventSynchronize(e1));
+            KPT_CUDA(cudaEventElapsedTime(&ms[r], e0, e1));
+            if (int rc = copy_state(false)) return rc;
+            for (size_t k = 0; k < b->runs.size(); ++k) b->runs[k].frame = frames[k];
+            if (int rc = batch_prepare(b)) return rc;
+        }
+        std::sort(ms, ms + repeats);
+        *median = ms[repeats / 2];
+        *spread = *median > 0.0f ? (ms[repeats - 1] - ms[0]) / *median : 0.0f;
+        return KPT_OK;
+    };
+    struct Choice {
+        int tile, every, bps, threads, ppl;
+        float ms, spread;
+    };
+    Choice best{b->sort_tile, b->sort_every, b->blocks_per_sm, b->threads,
+                b->particles_per_lane, 0.0f, 0.0f};
     int tried = 0;
+    auto consider = [&](const Choice& c) -> int {
+        b->sort_tile = c.tile;
+        b->sort_every = c.every;
+        b->blocks_per_sm = c.bps;
+        b->threads = c.threads;
+        b->particles_per_lane = c.ppl;
+        float ms = 0.0f, spread = 0.0f;
+        if (int rc = time_candidate(&ms, &spread)) return rc;
+        if (tried == 0 || ms < best.ms) {
+            best = c;
+            best.ms = ms;
+            best.spread = spread;
+        }
+        ++tried;
+        return KPT_OK;
+    };
+    // Stage 1: the cell-sort tile and interval at the default launch shape.
+    const int tiles[4] = {0, 8, 16, 32};
+    const int every[2] = {1, 2};
     for (int tile : tiles) {
         for (int ev : every) {
             if (tile == 0 && ev != 1) continue;
-            for (int bp : bps) {
-                b->sort_tile = tile;
-                b->sort_every = ev;
-                b->blocks_per_sm = bp;
-                batch_drop_graph(b);
-                if (int rc = batch_prepare(b)) return rc;
-                KPT_CUDA(cudaEventRecord(e0, st));
-                KPT_CUDA(batch_enqueue(b, intervals, st));
-                KPT_CUDA(cudaEventRecord(e1, st));
-                KPT_CUDA(cudaEventSynchronize(e1));
-                float ms = 0.0f;
-                KPT_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-                if (int rc = copy_state(false)) return rc;
-                if (tried == 0 || ms < best_ms) {
-                    best_ms = ms;
-                    best_tile = tile;
-                    best_bps = bp;
-                    best_every = ev;
+            if (int rc = consider(Choice{tile, ev, 0, 128, 1, 0.0f, 0.0f})) return rc;
+        }
+    }
+    // Stage 2: block shape, particles per lane and residency with that sort.
+    // Residency candidates are resident threads per SM (all that fit, or the
+    // threads of 3 or 2 blocks of 128), as blocks of the shape.
+    const int sort_tile = best.tile, sort_every = best.every;
+    const int shapes[3] = {64, 128, 256};
+    const int lanes[2] = {1, 2};
+    const int resident_threads[3] = {0, 384, 256};
+    for (int threads : shapes) {
+        for (int ppl : lanes) {
+            for (int rt : resident_threads) {
+                const int bps = rt == 0 ? 0 : std::max(1, rt / threads);
+                if (threads == 128 && ppl == 1 && rt == 0) continue;  // timed in stage 1
+                if (int rc = consider(Choice{sort_tile, sort_every, bps, threads, ppl, 0.0f,
+                                             0.0f})) {
+                    return rc;
                 }
-                ++tried;
             }
         }
     }
@@ -3908,16 +3974,23 @@ int kpt_batch_autotune(kpt_batch* b, uint32_t intervals, kpt_batch_tuning* out) 
     cudaEventDestroy(e1);
     KPT_CUDA(cudaStreamSynchronize(st));
     for (size_t r = 0; r < b->runs.size(); ++r) b->runs[r].frame = frames[r];
-    b->sort_tile = best_tile;
-    b->blocks_per_sm = best_bps;
-    b->sort_every = best_every;
+    b->sort_tile = best.tile;
+    b->blocks_per_sm = best.bps;
+    b->sort_every = best.every;
+    b->threads = best.threads;
+    b->particles_per_lane = best.ppl;
     batch_drop_graph(b);
     if (out) {
-        out->sort_tile = best_tile;
-        out->blocks_per_sm = best_bps;
-        out->sort_every = best_every;
+        out->sort_tile = best.tile;
+        out->blocks_per_sm = best.bps;
+        out->sort_every = best.every;
         out->candidates = tried;
-        out->best_ms = best_ms;
+        out->best_ms = best.ms;
+        out->spread = best.spread;
+        out->threads_per_block = best.threads;
+        out->particles_per_lane = best.ppl;
+        out->repeats = repeats;
+        out->pad = 0;
     }
     return KPT_OK;
 }

@@ -64,8 +64,12 @@ struct BatchLaunch {
     int focused;
     unsigned long long* cursor;
     int sm_count;
-    int blocks_per_sm;
+    int blocks_per_sm;       // resident blocks per SM, 0 = as many as fit
+    int threads;             // threads per block: 64, 128 or 256
+    int particles_per_lane;  // particles a lane advances side by side: 1 or 2
 };
+// The launch shapes the batched push is built for.
+bool batch_shape_supported(int threads, int particles_per_lane);
 size_t push_params_size();
 void build_push_params(const PushLaunch& launch, void* out);
 cudaError_t launch_push_batch(const BatchLaunch& launch, cudaStream_t stream);

@@ -1438,8 +1438,21 @@ __device__ __forceinline__ void batch_finish(const PushParams& P, const StateMix
     atomicMax(&P.counters->max_steps, static_cast<unsigned int>(st.steps));
 }
 
-template <bool FOCUSED>
-__global__ void __launch_bounds__(128, MinBlocks<StateMixed, FOCUSED>::value)
+// Register budget of the batched push per launch shape: the resident
+// threads per SM of the single-run mixed push (MinBlocks x 128), divided by
+// the particles a lane carries (each carries its own state).
+template <bool FOCUSED, int THREADS, int PPL>
+struct BatchMinBlocks {
+    static constexpr int threads_per_sm = MinBlocks<StateMixed, FOCUSED>::value * 128 / PPL;
+    static constexpr int value = threads_per_sm / THREADS > 0 ? threads_per_sm / THREADS : 1;
+};
+
+// PPL particles per lane: each lane keeps PPL particle states and advances
+// every one it holds by one substep per trip, so the table gathers of
+// independent particles are in flight together; each slot refills from the
+// cursor on its own.
+template <bool FOCUSED, int THREADS, int PPL>
+__global__ void __launch_bounds__(THREADS, (BatchMinBlocks<FOCUSED, THREADS, PPL>::value))
     push_batch_kernel(const BatchLaunch B) {
     __shared__ uint64_t offsets[kBatchMaxRuns + 1];
     for (int k = threadIdx.x; k <= B.runs; k += blockDim.x) offsets[k] = B.offsets[k];
@@ -1449,54 +1462,68 @@ __global__ void __launch_bounds__(128, MinBlocks<StateMixed, FOCUSED>::value)
     const unsigned lane = threadIdx.x & 31u;
     const unsigned lanes_below = (1u << lane) - 1u;
     const uint64_t total = offsets[B.runs];
-    StateMixed st;
-    int run = 0;
-    bool have = false;
+    StateMixed st[PPL];
+    int run[PPL];
+    bool have[PPL];
+#pragma unroll
+    for (int s = 0; s < PPL; ++s) {
+        run[s] = 0;
+        have[s] = false;
+    }
     bool exhausted = false;
     for (;;) {
-        const unsigned idle = __ballot_sync(full, !have);
-        if (idle != 0u && !exhausted) {
-            const unsigned n_idle = __popc(idle);
-            const int leader = __ffs(idle) - 1;
-            unsigned long long base = 0;
-            if (static_cast<int>(lane) == leader) {
-                base = atomicAdd(B.cursor, static_cast<unsigned long long>(n_idle));
-            }
-            base = __shfl_sync(full, base, leader);
-            if (base + n_idle >= total) {
-                exhausted = true;
-            }
-            if (!have) {
-                const uint64_t slot = base + __popc(idle & lanes_below);
-                if (slot < total) {
-                    run = batch_run_of(offsets, B.runs, slot);
-                    const PushParams& P = runs[run];
-                    const uint64_t local = slot - offsets[run];
-                    const uint32_t idx = P.order != nullptr ? __ldg(P.order + local)
-                                                            : static_cast<uint32_t>(local);
-                    if (P.parts.status[idx] == 0) {
-                        load<FOCUSED>(st, P, idx);
-                        have = true;
-                        if (!live(st, P)) {
-                            store<FOCUSED>(st, P);
-                            batch_finish(P, st);
-                            have = false;
+#pragma unroll
+        for (int s = 0; s < PPL; ++s) {
+            const unsigned idle = __ballot_sync(full, !have[s]);
+            if (idle != 0u && !exhausted) {
+                const unsigned n_idle = __popc(idle);
+                const int leader = __ffs(idle) - 1;
+                unsigned long long base = 0;
+                if (static_cast<int>(lane) == leader) {
+                    base = atomicAdd(B.cursor, static_cast<unsigned long long>(n_idle));
+                }
+                base = __shfl_sync(full, base, leader);
+                if (base + n_idle >= total) {
+                    exhausted = true;
+                }
+                if (!have[s]) {
+                    const uint64_t slot = base + __popc(idle & lanes_below);
+                    if (slot < total) {
+                        run[s] = batch_run_of(offsets, B.runs, slot);
+                        const PushParams& P = runs[run[s]];
+                        const uint64_t local = slot - offsets[run[s]];
+                        const uint32_t idx = P.order != nullptr ? __ldg(P.order + local)
+                                                                : static_cast<uint32_t>(local);
+                        if (P.parts.status[idx] == 0) {
+                            load<FOCUSED>(st[s], P, idx);
+                            have[s] = true;
+                            if (!live(st[s], P)) {
+                                store<FOCUSED>(st[s], P);
+                                batch_finish(P, st[s]);
+                                have[s] = false;
+                            }
                         }
                     }
                 }
             }
         }
-        if (!__any_sync(full, have)) {
+        bool any = false;
+#pragma unroll
+        for (int s = 0; s < PPL; ++s) any = any || have[s];
+        if (!__any_sync(full, any)) {
             if (exhausted) {
                 break;
             }
             continue;
         }
-        if (have && !substep<FOCUSED>(st, runs[run])) {
-            const PushParams& P = runs[run];
-            store<FOCUSED>(st, P);
-            batch_finish(P, st);
-            have = false;
+#pragma unroll
+        for (int s = 0; s < PPL; ++s) {
+            if (have[s] && !substep<FOCUSED>(st[s], runs[run[s]])) {
+                const PushParams& P = runs[run[s]];
+                store<FOCUSED>(st[s], P);
+                batch_finish(P, st[s]);
+                have[s] = false;
+            }
         }
     }
 }
@@ -1594,29 +1621,48 @@ void build_push_params(const PushLaunch& launch, void* out) {
     std::memcpy(out, &P, sizeof(P));
 }
 
-cudaError_t launch_push_batch(const BatchLaunch& B, cudaStream_t stream) {
-    if (B.runs <= 0 || B.runs > kBatchMaxRuns) return cudaErrorInvalidValue;
-    cudaError_t err = cudaSuccess;
-    batch_clear_counters_kernel<<<(B.runs + 127) / 128, 128, 0, stream>>>(B.params, B.runs,
-                                                                          B.cursor);
+namespace {
+
+template <bool FOCUSED, int THREADS, int PPL>
+cudaError_t launch_batch_shape(const BatchLaunch& B, cudaStream_t stream) {
     int resident = 0;
-    if (B.focused) {
-        err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, push_batch_kernel<true>,
-                                                            128, 0);
-    } else {
-        err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, push_batch_kernel<false>,
-                                                            128, 0);
-    }
+    cudaError_t err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &resident, push_batch_kernel<FOCUSED, THREADS, PPL>, THREADS, 0);
     if (err != cudaSuccess) return err;
     resident = resident < 1 ? 1 : resident;
     const int per_sm = B.blocks_per_sm > 0 && B.blocks_per_sm < resident ? B.blocks_per_sm
                                                                         : resident;
-    if (B.focused) {
-        push_batch_kernel<true><<<B.sm_count * per_sm, 128, 0, stream>>>(B);
-    } else {
-        push_batch_kernel<false><<<B.sm_count * per_sm, 128, 0, stream>>>(B);
-    }
+    push_batch_kernel<FOCUSED, THREADS, PPL><<<B.sm_count * per_sm, THREADS, 0, stream>>>(B);
     return cudaGetLastError();
+}
+
+template <bool FOCUSED>
+cudaError_t launch_batch_focused(const BatchLaunch& B, cudaStream_t stream) {
+    switch (B.threads * 4 + B.particles_per_lane) {
+        case 64 * 4 + 1: return launch_batch_shape<FOCUSED, 64, 1>(B, stream);
+        case 64 * 4 + 2: return launch_batch_shape<FOCUSED, 64, 2>(B, stream);
+        case 128 * 4 + 1: return launch_batch_shape<FOCUSED, 128, 1>(B, stream);
+        case 128 * 4 + 2: return launch_batch_shape<FOCUSED, 128, 2>(B, stream);
+        case 256 * 4 + 1: return launch_batch_shape<FOCUSED, 256, 1>(B, stream);
+        case 256 * 4 + 2: return launch_batch_shape<FOCUSED, 256, 2>(B, stream);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace
+
+bool batch_shape_supported(int threads, int particles_per_lane) {
+    return (threads == 64 || threads == 128 || threads == 256) &&
+           (particles_per_lane == 1 || particles_per_lane == 2);
+}
+
+cudaError_t launch_push_batch(const BatchLaunch& B, cudaStream_t stream) {
+    if (B.runs <= 0 || B.runs > kBatchMaxRuns) return cudaErrorInvalidValue;
+    if (!batch_shape_supported(B.threads, B.particles_per_lane)) return cudaErrorInvalidValue;
+    batch_clear_counters_kernel<<<(B.runs + 127) / 128, 128, 0, stream>>>(B.params, B.runs,
+                                                                          B.cursor);
+    return B.focused ? launch_batch_focused<true>(B, stream)
+                     : launch_batch_focused<false>(B, stream);
 }
 
 cudaError_t launch_batch_next_frame(const BatchLaunch& B, cudaStream_t stream) {

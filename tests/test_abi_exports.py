@@ -35,7 +35,7 @@ def test_no_device_fails_loudly(kpt):
 
 def test_abi_version_and_defaults(kpt):
     lib = kpt.load_library()
-    assert lib.kpt_abi_version() == 1
+    assert lib.kpt_abi_version() == 2
     s = kpt.default_settings()
     assert s.mhd_dt == 0.1 and s.p0 == 0.1 and s.max_steps == 200000
     assert s.kperp_over_kpara == 0.01 and s.split_ratio == 2.0

@@ -90,6 +90,45 @@ def test_batch_equals_runs_pushed_one_by_one(ctx, kpt, fields_mod, binding, orac
             h.close()
 
 
+@pytest.mark.parametrize("focused", [False, True])
+def test_launch_shapes_give_identical_results(ctx, kpt, fields_mod, binding, oracle, focused):
+    """Block size and particles per lane change only the schedule: every
+    shape ends bit for bit where the default one does."""
+    runs = _runs(kpt, fields_mod, binding, oracle, focused)
+    results = {}
+    for shape in ((128, 1), (64, 1), (256, 1), (64, 2), (128, 2), (256, 2)):
+        batch = ctx.batch()
+        handles = []
+        for run in runs:
+            lower, upper = _tables(ctx, kpt, run, focused)
+            parts = ctx.particles(run["count"])
+            parts.upload(run["start"], run["count"])
+            batch.add_run(parts, lower, upper, run["settings"], run["seed"], run["frame"])
+            handles.append((parts, lower, upper))
+        batch.set_schedule(sort_tile=8, blocks_per_sm=0, sort_every=1)
+        batch.set_launch_shape(*shape)
+        batch.run(2)
+        results[shape] = [h[0].download() for h in handles]
+        steps = [batch.stats(r).particle_steps for r in range(len(runs))]
+        if shape == (128, 1):
+            base_steps = steps
+        assert steps == base_steps, shape
+        batch.close()
+        for hs in handles:
+            for h in hs:
+                h.close()
+    for shape, got in results.items():
+        for r in range(len(runs)):
+            for name in NAMES:
+                assert np.array_equal(got[r][name], results[(128, 1)][r][name]), (shape, r, name)
+    with pytest.raises(kpt.KptError, match="threads_per_block"):
+        batch = ctx.batch()
+        try:
+            batch.set_launch_shape(96, 1)
+        finally:
+            batch.close()
+
+
 def test_autotune_keeps_state_and_results(ctx, kpt, fields_mod, binding, oracle):
     runs = _runs(kpt, fields_mod, binding, oracle, False)
     batch = ctx.batch()
@@ -102,9 +141,16 @@ def test_autotune_keeps_state_and_results(ctx, kpt, fields_mod, binding, oracle)
         handles.append((parts, lower, upper))
     before = [h[0].download() for h in handles]
     tuning = batch.autotune(1)
-    assert tuning["candidates"] >= 8 and tuning["best_ms"] > 0
+    # stage 1: 7 sort schedules; stage 2: 3 block shapes x 2 particles per
+    # lane x 3 residencies, less the default already timed
+    assert tuning["candidates"] == 7 + 17 and tuning["best_ms"] > 0
+    assert tuning["repeats"] == 3 and tuning["spread"] >= 0.0
+    assert tuning["threads_per_block"] in (64, 128, 256)
+    assert tuning["particles_per_lane"] in (1, 2)
     sched = batch.schedule()
     assert sched["sort_tile"] == tuning["sort_tile"]
+    assert batch.launch_shape() == {"threads_per_block": tuning["threads_per_block"],
+                                    "particles_per_lane": tuning["particles_per_lane"]}
     for r, (parts, _, _) in enumerate(handles):
         after = parts.download()
         for name in NAMES:
