@@ -294,10 +294,14 @@ def run_focused(args, f0, f1):
     start["status"][:] = 0
     start["t"][:] = START_FRAME * plain.mhd_dt
     tc, warp = kpt.ENGINE_TCGEN05, kpt.ENGINE_MMA_SYNC
+    # the FP64 baseline is the faster of the two FP64 arithmetics (contracted:
+    # FMA fusion and CUDA's pow); the strict one (the oracle's rounding, bit
+    # for bit) is timed beside it
     legs = [("surrogate", kpt.PRECISION_MIXED, learned, args.steps, "surrogate", tc),
             ("f64", kpt.PRECISION_F64, plain, 0, None, tc)]
     if WORLD == 1:
-        legs += [("mixed_qlt", kpt.PRECISION_MIXED, plain, args.steps, None, tc),
+        legs += [("f64_strict", kpt.PRECISION_F64, plain, 0, None, tc),
+                 ("mixed_qlt", kpt.PRECISION_MIXED, plain, args.steps, None, tc),
                  ("surrogate_mma_sync", kpt.PRECISION_MIXED, learned, args.steps, "surrogate",
                   warp),
                  ("surrogate_fp16", kpt.PRECISION_MIXED, learned, args.steps, "surrogate_fp16",
@@ -309,6 +313,8 @@ def run_focused(args, f0, f1):
         if net_label is not None:
             nets[net_label].engine = engine
         ctx.set_surrogate(nets.get(net_label))
+        ctx.set_fp64_arithmetic(kpt.FP64_STRICT if label == "f64_strict"
+                                else kpt.FP64_CONTRACTED)
         lower, upper = tables[precision]
         parts.upload(start, n)
         ctx.surrogate_judge()
@@ -358,8 +364,9 @@ def run_focused(args, f0, f1):
         out[label] = leg
     ref = finals["f64"]
     hp, hm = _spectrum(ref["p"], ref["w"], ref["status"]), _mu_spectrum(ref)
+    ctx.set_fp64_arithmetic(kpt.FP64_STRICT)
     for label in finals:
-        if label != "f64":
+        if label not in ("f64", "f64_strict"):
             fin = finals[label]
             out[label]["spectrum_l1_vs_f64"] = float(
                 np.abs(_spectrum(fin["p"], fin["w"], fin["status"]) - hp).sum() / hp.sum())
@@ -402,6 +409,7 @@ def accuracy_report(args, kpt, ctx, nets, tables, start, plain, learned, stream)
     sub = {k: v[:n].copy() for k, v in start.items()}
     parts = ctx.particles(n)
     tc = kpt.ENGINE_TCGEN05
+    ctx.set_fp64_arithmetic(kpt.FP64_STRICT)  # the reference leg rounds as the oracle does
     legs = [("f64", kpt.PRECISION_F64, plain, None, SEED),
             ("mixed_qlt", kpt.PRECISION_MIXED, plain, None, SEED),
             ("surrogate", kpt.PRECISION_MIXED, learned, "surrogate", SEED),
@@ -428,7 +436,8 @@ def accuracy_report(args, kpt, ctx, nets, tables, start, plain, learned, stream)
     ref = finals["f64"]
     out = {"particles": n, "intervals": args.accuracy_intervals,
            "steps_per_interval": args.substeps,
-           "reference": "plain FP64 push, plain slab-QLT closure, same start and noise",
+           "reference": "plain FP64 push (strict rounding: the oracle's trajectories bit for "
+                        "bit), plain slab-QLT closure, same start and noise",
            "bar": {"l1_max": 0.01, "chi2_p_min": 0.01},
            "seconds": seconds}
     ok = True
@@ -485,7 +494,10 @@ def run_parker(args, f0, f1):
     n = args.parker_particles
     out = {}
     for label, precision, steps in (("mixed", kpt.PRECISION_MIXED, args.steps),
-                                    ("f64", kpt.PRECISION_F64, args.f64_steps)):
+                                    ("f64", kpt.PRECISION_F64, args.f64_steps),
+                                    ("f64_strict", kpt.PRECISION_F64, args.f64_steps)):
+        ctx.set_fp64_arithmetic(kpt.FP64_STRICT if label == "f64_strict"
+                                else kpt.FP64_CONTRACTED)
         lower = ctx.field(f0, kpt.TABLE_PARKER16, precision)
         upper = ctx.field(f1, kpt.TABLE_PARKER16, precision)
         parts = ctx.particles(n)
@@ -503,6 +515,35 @@ def run_parker(args, f0, f1):
         (out["mixed"]["kernel_ms"] / 1e3) / 1e9
     out["mixed"]["algorithmic_gbs"] = achieved
     return out
+
+
+def run_batched_once(args):
+    """`batch_runs` runs as run_batched builds them, one batched interval of
+    20 steps at the default schedule (no autotuning): the batched kernel for
+    a profile capture."""
+    kpt = importlib.import_module("kokkos-particletransport_gb300")
+    rng = np.random.default_rng(SEED)
+    ctx = kpt.Context(DEVICE)
+    runs = []
+    for r in range(args.batch_runs):
+        field = fields.harris_field(512, 1024, sheet_width=float(rng.uniform(0.05, 0.2)),
+                                    island_amplitude=float(rng.uniform(0.0, 0.2)), noise=0.01,
+                                    seed=SEED + r)
+        table = ctx.field(field, kpt.TABLE_PARKER16, kpt.PRECISION_MIXED)
+        settings = kpt.default_settings(kperp_over_kpara=0.05, dt_min_rel=0.05,
+                                        dt_max_rel=0.05)
+        parts = ctx.particles(1 << 16)
+        ctx.inject(parts, table, settings, 1 << 16, START_FRAME, SEED + r)
+        runs.append((table, settings, parts))
+    batch = ctx.batch()
+    for r, (table, settings, parts) in enumerate(runs):
+        batch.add_run(parts, table, table, settings, SEED + r, START_FRAME)
+    batch.run(1, use_graph=False)
+    batch.close()
+    for table, _, parts in runs:
+        table.close()
+        parts.close()
+    ctx.close()
 
 
 def run_batched(args):
@@ -630,6 +671,7 @@ def run_c2_cli(args):
             cmd = [app, "--profile", "full", "--field-dir", field_dir, "--output-dir", outdir,
                    "--start-frame", "0", "--frames", str(frames), "--split-ratio", "1.2",
                    "--kperp-over-kpara", "0.05", "--precision", precision,
+                   "--fp64-arithmetic", "contracted",
                    "--push-stats", stats_path, "--device", str(DEVICE)]
             t0 = time.perf_counter()
             proc = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT,
@@ -671,6 +713,64 @@ def run_c2_cli(args):
         return out
     finally:
         shutil.rmtree(work, ignore_errors=True)
+
+
+def run_kernel_sweep(args):
+    """Every lifecycle and precompute kernel once on full-size inputs, for
+    per-kernel ncu captures (HBM bytes, L2 hit rate): the per-frame tables of
+    the 1024x2048 field (focused mixed, Parker FP64), injection of 4 Mi
+    particles, the cell sort, a split with half the particles above the
+    first threshold, the momentum histogram and the summary; the header
+    library's Parker coefficient precompute on the same grid, a field-threshold
+    candidate set with injection from it; and one batched push of 16 runs
+    (20 steps per interval).  Prints the units each call processed."""
+    import torch
+    kpt = importlib.import_module("kokkos-particletransport_gb300")
+    f0, f1 = make_workload()
+    ctx = kpt.Context(DEVICE)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    n = args.particles
+    settings = focused_settings(kpt, kpt.CLOSURE_QLT)
+    out = {"particles": n, "points": (NX + 4) * (NY + 4)}
+    lower = ctx.field(f0, kpt.TABLE_FOCUSED21, kpt.PRECISION_MIXED)
+    parker64 = ctx.field(f1, kpt.TABLE_PARKER16, kpt.PRECISION_F64)
+    parts = ctx.particles(n)
+    ctx.inject(parts, lower, settings, n, START_FRAME, SEED)
+    ctx.sort(parts, lower, args.sort_tile, args.sort_tile)
+    state = parts.download(n)
+    state["p"][::2] = 3.0 * settings.p0  # above the first split threshold (2 p0)
+    parts.upload(state, n // 2 + n // 4)  # room for the children
+    split, skipped = ctx.split(parts, settings)
+    out["split"] = {"split": int(split), "skipped": int(skipped)}
+    ctx.histogram(parts, 1e-2, 1e1, 128)
+    ctx.summarize(parts)
+    torch.cuda.synchronize()
+    for obj in (lower, parker64, parts):
+        obj.close()
+    # header library: coefficient precompute and injection from candidates
+    xe = np.linspace(-1.0, 1.0, NX + 1)
+    ye = np.linspace(-2.0, 2.0, NY + 1)
+    grid = ctx.grid(xe, ye, (1, 1))
+    solver = None
+    try:
+        b = np.zeros(((NX + 4) * (NY + 4), 3))
+        b[:, 0], b[:, 2] = 1.0, 0.3
+        v = np.zeros_like(b)
+        v[:, 0] = 0.1
+        solver = ctx.parker_solver_from_fields(grid, b, v, {"sigma2": 0.35, "l2d": 0.9,
+                                                            "lslab": 1.4})
+        run_generator(kpt, ctx, grid, xe, ye, 1 << 20, stream)
+    finally:
+        if solver is not None:
+            solver.close()
+        grid.close()
+    ctx.close()
+    # one batched push
+    sub = argparse.Namespace(**vars(args))
+    sub.batch_runs = 16
+    run_batched_once(sub)
+    print(json.dumps({"kernel_sweep": out}))
 
 
 def run_library(args):
@@ -883,19 +983,23 @@ def fp64_roofline(focused_f64, parker_f64):
         peak = ctx.fp64_fma_rate()
     hbm, _ = read_peaks()
     out = {"peak_tflops": peak, "peak_kind": "measured (project FMA-chain kernel, this run)"}
-    for label, value, model, path in (
+    for label, values, model, path in (
             ("focused_f64", focused_f64, "focused_f64", PROFILE_F64_FOCUSED),
             ("parker_f64", parker_f64, "parker_f64", PROFILE_F64_PARKER)):
-        if value is None:
+        if values is None:
             continue
-        flop = profile_value(path, "fp64_flop_per_particle_step")
-        entry = {"value": value, "hbm_frac": value * BYTES_PER_STEP[model] / 1e9 / hbm,
-                 "fp64_flop_per_particle_step": flop,
-                 "flop_source": os.path.relpath(path, ROOT) if flop is not None else None}
-        if flop is not None:
-            entry["fp64_tflops"] = value * flop / 1e12
-            entry["fp64_frac"] = entry["fp64_tflops"] / peak
-        out[label] = entry
+        for mode, value in values.items():
+            if value is None:
+                continue
+            flop = profile_value(path, f"fp64_flop_per_particle_step_{mode}")
+            entry = {"value": value, "hbm_frac": value * BYTES_PER_STEP[model] / 1e9 / hbm,
+                     "fp64_flop_per_particle_step": flop,
+                     "flop_source": "from_profile: ncu dadd + dmul + 2 dfma per particle-step, "
+                                    + os.path.relpath(path, ROOT) if flop is not None else None}
+            if flop is not None:
+                entry["fp64_tflops"] = value * flop / 1e12
+                entry["fp64_frac"] = entry["fp64_tflops"] / peak
+            out[f"{label}_{mode}"] = entry
     return out
 
 
@@ -931,10 +1035,15 @@ def main():
                         help="particles of the multi-interval spectrum comparison")
     parser.add_argument("--accuracy-intervals", type=int, default=10,
                         help="consecutive intervals of the spectrum comparison (0 skips it)")
+    parser.add_argument("--kernel-sweep", action="store_true",
+                        help="run each lifecycle/precompute kernel once (for ncu) and exit")
     parser.add_argument("--sort-tile", type=int, default=8,
                         help="cell-sort tile (cells) before each push; 0 disables")
     args = parser.parse_args()
     rank = int(os.environ.get("RANK", "0"))
+    if args.kernel_sweep:
+        run_kernel_sweep(args)
+        return
     config = {"workload": f"focused push, learned slab-QLT closure (sigma2 0.1, gamma_k 5/3), "
                           f"{NX}x{NY} stretched-y Harris+islands field, {args.particles} "
                           f"particles (p = p0, mu uniform on [-1, 1]), {args.substeps} fixed "
@@ -988,7 +1097,10 @@ def main():
     l1tex_frac = profile_value(PROFILE, "l1tex_data_pipe_frac")
     bf16_peak, bf16_kind = read_bf16_peak()
     tensor_tflops = steps_per_launch * tensor_flop_per_step(args.hidden_width) / kernel_s / 1e12
-    fp64 = fp64_roofline(f64["value"], None if parker is None else parker["f64"]["value"]) \
+    fp64 = fp64_roofline(
+        {"contracted": f64["value"], "strict": focused.get("f64_strict", {}).get("value")},
+        None if parker is None else {"contracted": parker["f64"]["value"],
+                                     "strict": parker["f64_strict"]["value"]}) \
         if WORLD == 1 else None
     # whole-job value: all ranks' particle-steps over the slowest rank's time
     head["value"], total_ms = whole_job(head["ms_per_step"] * head["steps"],
@@ -1016,7 +1128,13 @@ def main():
         "data": "synthetic", "config": config,
         "plain_f64": {"value": f64["value"], "ms_per_step": f64["ms_per_step"],
                       "steps": f64["steps"], "per_gpu": WORLD > 1,
+                      "arithmetic": "contracted (FMA fusion, CUDA pow): the faster FP64 push",
                       "speedup_surrogate_over_f64": head["value"] / (f64["value"] * WORLD)},
+        "plain_f64_strict": None if "f64_strict" not in focused else {
+            "value": focused["f64_strict"]["value"],
+            "ms_per_step": focused["f64_strict"]["ms_per_step"],
+            "arithmetic": "strict (no contraction, the project pow): the oracle's "
+                          "trajectories bit for bit"},
         "mixed_plain_qlt": None if mixed_qlt is None else {
             "value": mixed_qlt["value"], "ms_per_step": mixed_qlt["ms_per_step"],
             "spectrum_l1_vs_f64": None if acc is None

@@ -226,6 +226,16 @@ int kpt_math_pow(kpt_context* ctx, uint64_t n, const double* x, const double* y,
  * as many as are resident) or KPT_SCHEDULE_SIMPLE (one particle per
  * thread).  Results do not depend on the choice. */
 int kpt_context_set_push_schedule(kpt_context* ctx, int schedule, int blocks_per_sm);
+/* Arithmetic of the plain FP64 push (precision KPT_PRECISION_F64):
+ * KPT_FP64_STRICT (default) rounds every operation as the reference's code
+ * is written (no FMA contraction) and computes powers with the library's
+ * kpt_math_pow function, as the oracle does, so FP64 trajectories equal the
+ * reference's on the Kokkos shim bit for bit over whole intervals;
+ * KPT_FP64_CONTRACTED lets the compiler fuse multiply-adds and uses CUDA's
+ * pow: about a quarter faster, trajectories within ~1e-15 per step of the
+ * strict ones (the reference's own optimised builds contract too). */
+enum kpt_fp64_arithmetic { KPT_FP64_STRICT = 0, KPT_FP64_CONTRACTED = 1 };
+int kpt_context_set_fp64_arithmetic(kpt_context* ctx, int mode);
 
 /* ---- fields: one MHD frame as a device coefficient table ---------------- */
 /* Cells are 3 x ny x nx arrays (x fastest) of B and V, host memory.  Edges

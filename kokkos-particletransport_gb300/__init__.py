@@ -32,6 +32,8 @@ PRECISION_F64 = 0
 PRECISION_MIXED = 1
 SCHEDULE_REFILL = 0
 SCHEDULE_SIMPLE = 1
+FP64_STRICT = 0       # FP64 push rounds as the reference's code is written (oracle-exact)
+FP64_CONTRACTED = 1   # FP64 push with FMA contraction and CUDA's pow (faster)
 ENGINE_TCGEN05 = 0   # block-collective tcgen05.mma network, activations in tensor memory
 ENGINE_MMA_SYNC = 1  # warp-collective mma.sync network, activations in registers
 
@@ -228,6 +230,7 @@ def load_library() -> ctypes.CDLL:
         "kpt_context_synchronize": (i32, [vp]),
         "kpt_context_fp64_fma_rate": (i32, [vp, ctypes.POINTER(ctypes.c_double)]),
         "kpt_math_pow": (i32, [vp, ctypes.c_uint64, vp, vp, vp]),
+        "kpt_context_set_fp64_arithmetic": (i32, [vp, i32]),
         "kpt_context_set_push_schedule": (i32, [vp, i32, i32]),
         "kpt_field_create": (i32, [vp, i32, i32, vp, vp, vp, vp, i32, i32, pvp]),
         "kpt_field_load": (i32, [vp, ctypes.c_char_p, i32, i32, pvp]),
@@ -400,6 +403,11 @@ class Context:
 
     def synchronize(self) -> None:
         _check(self.lib.kpt_context_synchronize(self.handle))
+
+    def set_fp64_arithmetic(self, mode: int) -> None:
+        """FP64_STRICT (oracle-exact rounding, the default) or FP64_CONTRACTED
+        (FMA contraction and CUDA's pow, faster) for the FP64 push."""
+        _check(self.lib.kpt_context_set_fp64_arithmetic(self.handle, int(mode)))
 
     def pow(self, x, y) -> np.ndarray:
         """x^y elementwise by the FP64 push's power function, on the GPU."""

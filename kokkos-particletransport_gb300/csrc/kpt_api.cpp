@@ -111,6 +111,7 @@ struct kpt_context {
     kpt_surrogate* surrogate = nullptr;
     DeviceBuffer judge;
     int push_schedule = kpt::kScheduleRefill;
+    int fp64_arithmetic = KPT_FP64_STRICT;
     int push_blocks_per_sm = 0;  // 0: as many as fit (occupancy)
 };
 
@@ -506,6 +507,15 @@ int kpt_context_set_push_schedule(kpt_context* ctx, int schedule, int blocks_per
     ctx->push_schedule = schedule == KPT_SCHEDULE_SIMPLE ? kpt::kScheduleSimple
                                                          : kpt::kScheduleRefill;
     ctx->push_blocks_per_sm = blocks_per_sm;
+    return KPT_OK;
+}
+
+int kpt_context_set_fp64_arithmetic(kpt_context* ctx, int mode) {
+    KPT_REQUIRE(ctx != nullptr, "kpt_context_set_fp64_arithmetic: ctx is NULL");
+    KPT_REQUIRE(mode == KPT_FP64_STRICT || mode == KPT_FP64_CONTRACTED,
+                "kpt_context_set_fp64_arithmetic: mode must be KPT_FP64_STRICT or "
+                "KPT_FP64_CONTRACTED");
+    ctx->fp64_arithmetic = mode;
     return KPT_OK;
 }
 
@@ -1047,6 +1057,7 @@ void fill_push_launch(const kpt_context* ctx, const kpt_particles* parts, const 
     launch.precision = lower->precision;
     launch.focused = settings->focused != 0;
     launch.schedule = ctx->push_schedule;
+    launch.fp64_contracted = ctx->fp64_arithmetic == KPT_FP64_CONTRACTED ? 1 : 0;
     launch.sm_count = ctx->sm_count;
     launch.blocks_per_sm = ctx->push_blocks_per_sm;
     launch.surrogate = nullptr;

@@ -42,6 +42,7 @@ struct PushLaunch {
     int schedule;
     int sm_count;
     int blocks_per_sm;
+    int fp64_contracted;  // FP64 push: 0 strict rounding (oracle-exact), 1 FMA contraction
     // learned closure (mixed focused push only); nullptr = plain closures
     const SurrogateDevice* surrogate;
 };
@@ -50,6 +51,8 @@ cudaError_t launch_push_interval(const PushLaunch& launch, cudaStream_t stream);
 // The plain FP64 push and FP64 table sampling, built in their own translation
 // unit without FMA contraction (kpt_push_f64.cu).
 cudaError_t launch_push_interval_f64(const PushLaunch& launch, cudaStream_t stream);
+// The plain FP64 push with FMA contraction and CUDA's pow (kpt_push.cu).
+cudaError_t launch_push_interval_f64_contracted(const PushLaunch& launch, cudaStream_t stream);
 struct SampleLaunch;
 cudaError_t launch_sample_f64(const SampleLaunch& launch, int blocks, cudaStream_t stream);
 

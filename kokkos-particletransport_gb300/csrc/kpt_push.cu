@@ -33,10 +33,12 @@
 #include "kpt_pow.h"
 
 // What this translation unit emits.  0 (the default): everything but the
-// plain FP64 push and the FP64 table sampling; 1: only those two, compiled
-// apart with FMA contraction off (kpt_push_f64.cu, nvcc -fmad=false), so
-// their double arithmetic rounds exactly as written, as the host oracle's
-// does (the oracle and the reference build use -ffp-contract=off).
+// strict FP64 push and the FP64 table sampling, with FMA contraction and
+// CUDA's pow in the FP64 push it does contain (the contracted mode); 1: only
+// the strict FP64 push and FP64 sampling, compiled apart with FMA contraction
+// off (kpt_push_f64.cu, nvcc -fmad=false) and the project pow, so their
+// double arithmetic rounds exactly as written, as the host oracle's does (the
+// oracle and the reference build use -ffp-contract=off).
 #ifndef KPT_PUSH_PART
 #define KPT_PUSH_PART 0
 #endif
@@ -58,8 +60,13 @@ struct Num;
 
 template <>
 struct Num<double> {
+#if KPT_PUSH_PART == 1
     // the project pow (kpt_pow.h): rounds exactly as the host oracle does
     static __device__ __forceinline__ double pow(double a, double b) { return kpt_pow(a, b); }
+#else
+    // the contracted FP64 push: CUDA's pow
+    static __device__ __forceinline__ double pow(double a, double b) { return ::pow(a, b); }
+#endif
     static __device__ __forceinline__ double sqrt(double a) { return ::sqrt(a); }
     static __device__ __forceinline__ double div(double a, double b) { return a / b; }
     static __device__ __forceinline__ bool finite(double a) { return isfinite(a); }
@@ -1651,6 +1658,11 @@ cudaError_t launch_batch_focused(const BatchLaunch& B, cudaStream_t stream) {
 
 }  // namespace
 
+cudaError_t launch_push_interval_f64_contracted(const PushLaunch& launch, cudaStream_t stream) {
+    return launch.focused ? launch_push<StateF64, true>(launch, stream)
+                          : launch_push<StateF64, false>(launch, stream);
+}
+
 bool batch_shape_supported(int threads, int particles_per_lane) {
     return (threads == 64 || threads == 128 || threads == 256) &&
            (particles_per_lane == 1 || particles_per_lane == 2);
@@ -1674,7 +1686,8 @@ int batch_max_runs() { return kBatchMaxRuns; }
 
 cudaError_t launch_push_interval(const PushLaunch& launch, cudaStream_t stream) {
     if (launch.precision == kPrecisionF64) {
-        return launch_push_interval_f64(launch, stream);
+        return launch.fp64_contracted ? launch_push_interval_f64_contracted(launch, stream)
+                                      : launch_push_interval_f64(launch, stream);
     }
     if (launch.surrogate != nullptr) {
         const SurrogateBox& box = launch.surrogate->box;

@@ -83,6 +83,7 @@ struct RunSettings {
     bool prefetch{true};  // read the next frame file while the GPU pushes
     int device{0};
     std::string push_stats_path{};  // per-frame push counters and diagnostic times
+    int fp64_arithmetic{KPT_FP64_STRICT};
 
     int intervals() const { return end_frame - start_frame; }
     bool restart() const { return !restart_path.empty(); }
@@ -359,7 +360,10 @@ void print_usage() {
         << "  --histogram-bins N            momentum histogram bins (default 128)\n"
         << "  --device N                    CUDA device (default 0)\n"
         << "  --push-stats PATH             write per-frame substep counts and diagnostic\n"
-        << "                                times to PATH (CSV)\n";
+        << "                                times to PATH (CSV)\n"
+        << "  --fp64-arithmetic strict|contracted\n"
+        << "                                FP64 push rounding: as written, bit for bit with\n"
+        << "                                the reference (default), or FMA-fused and faster\n";
 }
 
 std::string next_value(int argc, char** argv, int& i, const std::string& option) {
@@ -483,6 +487,12 @@ RunSettings parse(int argc, char** argv) {
             s.prefetch = v == "on";
         } else if (arg == "--push-stats") {
             s.push_stats_path = next_value(argc, argv, i, arg);
+        } else if (arg == "--fp64-arithmetic") {
+            const std::string v = next_value(argc, argv, i, arg);
+            if (v != "strict" && v != "contracted") {
+                throw std::runtime_error("--fp64-arithmetic needs strict or contracted.");
+            }
+            s.fp64_arithmetic = v == "strict" ? KPT_FP64_STRICT : KPT_FP64_CONTRACTED;
         } else {
             throw std::runtime_error("Unknown option: " + arg);
         }
@@ -827,6 +837,7 @@ int run(const RunSettings& s) {
     kpt_context* raw_ctx = nullptr;
     check(kpt_context_create(s.device, &raw_ctx));
     std::unique_ptr<kpt_context, int (*)(kpt_context*)> ctx(raw_ctx, kpt_context_destroy);
+    check(kpt_context_set_fp64_arithmetic(ctx.get(), s.fp64_arithmetic));
     kpt_particles* raw_parts = nullptr;
     check(kpt_particles_create(ctx.get(), s.capacity, &raw_parts));
     std::unique_ptr<kpt_particles, int (*)(kpt_particles*)> parts(raw_parts,

@@ -424,3 +424,25 @@ def test_snapshot_records_packed_on_gpu(ctx, kpt):
     want["initial_kinetic_energy"] = e0
     assert got.tobytes() == want.tobytes()
     parts.close()
+
+
+@pytest.mark.parametrize("case", ["parker_uniform", "focused_uniform"])
+def test_push_f64_contracted_stays_close_to_strict(ctx, kpt, oracle, case):
+    """The contracted FP64 arithmetic (FMA fusion, CUDA's pow) is the faster
+    FP64 push; it leaves the oracle's trajectories by last-bit differences
+    only: within the 1e-10 bar over a Parker interval and over the first
+    1000 focused substeps (the focused pitch-angle dynamics amplify them
+    later in the interval)."""
+    focused_case = case.startswith("focused")
+    ctx.set_fp64_arithmetic(kpt.FP64_CONTRACTED)
+    try:
+        got, want, steps, stats, widths, focused = _push_case(
+            ctx, kpt, oracle, case, kpt.PRECISION_F64,
+            FOCUSED_PARITY_STEPS if focused_case else None)
+    finally:
+        ctx.set_fp64_arithmetic(kpt.FP64_STRICT)
+    errs = trajectory_errors(got, want, widths[0], widths[1], focused)
+    print(case, "contracted", errs)
+    for name, err in errs.items():
+        assert err <= F64_REL, (name, err)
+    assert np.array_equal(got["status"], want["status"])
