@@ -329,8 +329,11 @@ int kpt_surrogate_gradient(kpt_context* ctx, int32_t hidden_width, const float* 
                            float* loss);
 /* Pushes on this context with closure KPT_CLOSURE_SURROGATE use this
  * network (16-bit weights and activations, FP32 accumulation, on the tensor
- * cores).  The context keeps the pointer: unset it (NULL) before destroying
- * the surrogate. */
+ * cores).  The mixed focused push serves it on the surrogate's engine; the
+ * FP64 focused push (precision KPT_PRECISION_F64, contracted FP64 arithmetic)
+ * serves it on the mma.sync engine, where it replaces the plain closure's
+ * five FP64 powers per substep.  The context keeps the pointer: unset it
+ * (NULL) before destroying the surrogate. */
 int kpt_context_set_surrogate(kpt_context* ctx, kpt_surrogate* surrogate);
 /* Per-step judge of the surrogate in pushes since the last call: network
  * evaluations, evaluations checked against the plain closure, fallbacks to

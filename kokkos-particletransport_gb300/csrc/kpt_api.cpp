@@ -1087,8 +1087,8 @@ int kpt_push_interval(kpt_context* ctx, kpt_particles* parts, const kpt_field* l
         const kpt_surrogate* sg = ctx->surrogate;
         KPT_REQUIRE(sg != nullptr,
                     "kpt_push_interval: closure SURROGATE needs kpt_context_set_surrogate");
-        KPT_REQUIRE(settings->focused != 0 && lower->precision == KPT_PRECISION_MIXED,
-                    "kpt_push_interval: the surrogate closure runs in the mixed focused push");
+        KPT_REQUIRE(settings->focused != 0,
+                    "kpt_push_interval: the surrogate closure runs in the focused push");
         const kpt::SurrogateBox& box = sg->box;
         KPT_REQUIRE(box.p0 == settings->p0 && box.particle_v0 == settings->particle_v0 &&
                         box.kpara0 == settings->kpara0 &&
@@ -1100,7 +1100,8 @@ int kpt_push_interval(kpt_context* ctx, kpt_particles* parts, const kpt_field* l
                     "kpt_push_interval: settings differ from those the surrogate was trained with");
         served.block = sg->d_block;
         served.tc_block = sg->d_tc_block;
-        served.engine = sg->engine;
+        // the FP64 push serves the network on the warp-collective engine
+        served.engine = lower->precision == KPT_PRECISION_F64 ? kpt::kEngineMmaSync : sg->engine;
         served.box = box;
         const double f3 = std::log(settings->qlt_sigma2);
         const double f4 = settings->qlt_spectral_index;

@@ -27,6 +27,7 @@
 
 #include <cstdint>
 #include <cstring>
+#include <type_traits>
 
 #include "kpt_device.cuh"
 #include "kpt_internal.h"
@@ -622,8 +623,11 @@ struct StateF64 {
     uint32_t index;
 };
 
+// The first part of an FP64 substep: count it, wrap the position and sample
+// the time-interpolated table at the shifted position.
 template <bool FOCUSED>
-__device__ __forceinline__ bool substep(StateF64& st, const PushParams& P) {
+__device__ __forceinline__ void sample_f64(StateF64& st, const PushParams& P,
+                                           double c[FOCUSED ? 21 : 16]) {
     constexpr int C = FOCUSED ? 21 : 16;
     constexpr int STRIDE = FOCUSED ? 22 : 16;
     const DeviceSettings& s = P.s;
@@ -631,13 +635,20 @@ __device__ __forceinline__ bool substep(StateF64& st, const PushParams& P) {
     st.x = wrap_driver(st.x, s.x_lower, s.x_upper, s.x_width);
     st.y = wrap_driver(st.y, s.y_lower, s.y_upper, s.y_width);
     const double rt = __ddiv_rn(__dsub_rn(st.t, P.interval_start), s.mhd_dt);
-    double c[C];
     sample_coefficients<double, C, STRIDE>(P.grid, static_cast<const double*>(P.lower),
                                            static_cast<const double*>(P.upper),
                                            __dadd_rn(st.x, s.shift_x), __dadd_rn(st.y, s.shift_y),
                                            rt, s.time_interpolation, c);
+}
+
+// The rest of an FP64 substep from the sampled table values: physics (with
+// the served closure when SURR), step size, noise and the update.
+template <bool FOCUSED, bool SURR = false>
+__device__ __forceinline__ bool advance_f64(StateF64& st, const PushParams& P, const double* c,
+                                            const Served* served = nullptr) {
+    const DeviceSettings& s = P.s;
     Rates<double> r;
-    if (!physics<double, FOCUSED>(c, st.p, st.mu, P.kd, r)) {
+    if (!physics<double, FOCUSED, SURR>(c, st.p, st.mu, P.kd, r, served)) {
         st.status = 2;
         return false;
     }
@@ -668,6 +679,13 @@ __device__ __forceinline__ bool substep(StateF64& st, const PushParams& P) {
         return false;
     }
     return st.t < P.interval_end && st.steps < s.max_steps;
+}
+
+template <bool FOCUSED>
+__device__ __forceinline__ bool substep(StateF64& st, const PushParams& P) {
+    double c[FOCUSED ? 21 : 16];
+    sample_f64<FOCUSED>(st, P, c);
+    return advance_f64<FOCUSED>(st, P, c);
 }
 
 template <bool FOCUSED>
@@ -989,6 +1007,98 @@ __device__ __forceinline__ bool substep_surrogate(StateMixed& st, const PushPara
     return advance_mixed<true, true>(st, P, c, &served);
 }
 
+// The FP64 focused substep with the learned closure, warp-collective on the
+// mma.sync engine (as the mixed one above): the table is sampled and the
+// physics evaluated in FP64, the network serves D_mumu, dD_mumu/dmu and
+// kappa_parallel in place of the plain closure's powers.  The plain closure
+// answers outside the training box and below mu_cut, blends in over
+// [mu_cut, 2 mu_cut] and judges one substep in judge_period, in FP64.
+template <bool FP16, int H>
+__device__ __forceinline__ bool substep_surrogate(StateF64& st, const PushParams& P, bool have,
+                                                  const uint2* smem, JudgeTally& tally) {
+    const SurrogateDevice& sg = P.sg;
+    const SurrogateBox& box = sg.box;
+    double c[21];
+    float f[kMlpIn] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    bool use = false;
+    double mu = 0.0;
+    if (have) {
+        sample_f64<true>(st, P, c);
+        mu = clamp_mu(st.mu, P.kd.mu_max);
+        const float b = static_cast<float>(c[6]);
+        const float p = static_cast<float>(st.p);
+        const float amu = fabsf(static_cast<float>(mu));
+        if (sg.constants_in_box && amu >= box.mu_cut && b > 0.0f && p > 0.0f) {
+            const float lm = __logf(amu);
+            const float lp = __logf(p);
+            const float lb = __logf(b);
+            use = lm <= box.in_hi[0] && lp >= box.in_lo[1] && lp <= box.in_hi[1] &&
+                  lb >= box.in_lo[2] && lb <= box.in_hi[2];
+            if (use) {
+                f[0] = lm * box.in_scale[0] + box.in_offset[0];
+                f[1] = lp * box.in_scale[1] + box.in_offset[1];
+                f[2] = lb * box.in_scale[2] + box.in_offset[2];
+                f[3] = sg.f3;
+                f[4] = sg.f4;
+            }
+        }
+    }
+    float y[kMlpOut];
+    __syncwarp();
+    mlp_warp<FP16, H>(smem, f, y);
+    if (!have) {
+        return false;
+    }
+    Served served;
+    served.use = use;
+    if (use) {
+        const double y0 = static_cast<double>(y[0] * box.out_scale[0] + box.out_offset[0]);
+        const double y1 = static_cast<double>(y[1] * box.out_scale[1] + box.out_offset[1]);
+        const double y2 = static_cast<double>(y[2] * box.out_scale[2] + box.out_offset[2]);
+        const double one_minus_mu2 = 1.0 - mu * mu;
+        const double sign = mu > 0.0 ? 1.0 : -1.0;
+        const double amu = fabs(mu);
+        double duu = one_minus_mu2 * exp(y0);
+        double duu_du = duu * (sign * y1 / (amu + P.kd.qlt_h0) - 2.0 * mu / one_minus_mu2);
+        double kpara = exp(y2);
+        ++tally.evaluations;
+        const bool blend = amu < 2.0 * box.mu_cut;
+        const bool judge = (st.steps & (sg.judge_period - 1)) == 0;
+        if (blend || judge) {
+            const Consts<double>& k = P.kd;
+            const double b = c[6];
+            const double p = st.p;
+            const double speed = k.particle_v0 * p / k.p0;
+            const double omega = k.qlt_omega0 * b / sqrt(1.0 + p * p);
+            double pd, pdd;
+            qlt_scattering<double>(mu, omega, speed, k, pd, pdd);
+            double pk = k.kpara0;
+            if (k.magnetic_dependency == 1) pk *= Num<double>::pow(b, k.gamma_turb - 2.0);
+            if (k.momentum_dependency == 1) pk *= Num<double>::pow(p / k.p0, k.pindex);
+            if (judge) {
+                const double e = fmax(fabs(duu - pd) / pd, fabs(kpara - pk) / pk);
+                tally.max_error = isfinite(e) ? fmaxf(tally.max_error, static_cast<float>(e))
+                                              : INFINITY;
+                ++tally.judged;
+            }
+            if (blend) {
+                const double w = (amu - box.mu_cut) / box.mu_cut;
+                const double dw = sign / box.mu_cut;
+                const double dd = duu - pd;
+                duu_du = pdd + w * (duu_du - pdd) + dw * dd;
+                duu = pd + w * dd;
+                kpara = pk + w * (kpara - pk);
+            }
+        }
+        served.duu = static_cast<float>(duu);
+        served.duu_du = static_cast<float>(duu_du);
+        served.kpara = static_cast<float>(kpara);
+    } else {
+        ++tally.fallbacks;
+    }
+    return advance_f64<true, true>(st, P, c, &served);
+}
+
 // Position <-> fixed-point phase (once per particle and push).
 __device__ __forceinline__ uint64_t to_phase(double x, double lower, double inv_width) {
     double f = (x - lower) * inv_width;
@@ -1133,9 +1243,11 @@ struct MinBlocks<StateMixed, true> {
 __host__ __device__ constexpr bool surr_fp16(int surr) { return surr == 2 || surr == 4; }
 __host__ __device__ constexpr int surr_hidden(int surr) { return surr <= 2 ? 64 : 32; }
 template <typename State, bool FOCUSED, int SURR = 0>
-__global__ void __launch_bounds__(128, SURR >= 3 ? KPT_SURROGATE32_MIN_BLOCKS
-                                       : SURR ? KPT_SURROGATE_MIN_BLOCKS
-                                              : MinBlocks<State, FOCUSED>::value)
+__global__ void __launch_bounds__(128, !std::is_same<State, StateMixed>::value
+                                           ? MinBlocks<State, FOCUSED>::value
+                                       : SURR >= 3 ? KPT_SURROGATE32_MIN_BLOCKS
+                                       : SURR      ? KPT_SURROGATE_MIN_BLOCKS
+                                                   : MinBlocks<State, FOCUSED>::value)
     push_refill_kernel(const PushParams P) {
     const unsigned full = 0xffffffffu;
     const unsigned lane = threadIdx.x & 31u;
@@ -1389,8 +1501,10 @@ template <typename State, bool FOCUSED, int SURR = 0>
 cudaError_t launch_push(const PushLaunch& L, cudaStream_t stream) {
     const PushParams P = make_push_params(L);
     const int threads = 128;
-    if (SURR && L.surrogate->engine == kEngineTcgen05) {
-        return launch_push_tc<surr_fp16(SURR), surr_hidden(SURR)>(P, L, stream);
+    if constexpr (SURR != 0 && std::is_same<State, StateMixed>::value) {
+        if (L.surrogate->engine == kEngineTcgen05) {
+            return launch_push_tc<surr_fp16(SURR), surr_hidden(SURR)>(P, L, stream);
+        }
     }
     const size_t smem = SURR ? mlp_smem_bytes(surr_hidden(SURR)) : 0;
     if (L.schedule == kScheduleSimple && !SURR) {
@@ -1686,6 +1800,17 @@ int batch_max_runs() { return kBatchMaxRuns; }
 
 cudaError_t launch_push_interval(const PushLaunch& launch, cudaStream_t stream) {
     if (launch.precision == kPrecisionF64) {
+        if (launch.surrogate != nullptr) {
+            // the FP64 push with the learned closure (mma.sync engine), built
+            // with the contracted FP64 arithmetic
+            const SurrogateBox& box = launch.surrogate->box;
+            if (box.hidden == 64) {
+                return box.fp16 ? launch_push<StateF64, true, 2>(launch, stream)
+                                : launch_push<StateF64, true, 1>(launch, stream);
+            }
+            return box.fp16 ? launch_push<StateF64, true, 4>(launch, stream)
+                            : launch_push<StateF64, true, 3>(launch, stream);
+        }
         return launch.fp64_contracted ? launch_push_interval_f64_contracted(launch, stream)
                                       : launch_push_interval_f64(launch, stream);
     }

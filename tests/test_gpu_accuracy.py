@@ -4,8 +4,9 @@ The focused push (slab-QLT closure, sigma^2 = 0.1, gamma_k = 5/3) on a
 128x256 stretched-y Harris + islands field, 16 384 particles (p = p0, pitch
 cosine uniform on [-1, 1]) pushed 10 consecutive intervals of 500 fixed
 steps: by the FP64 oracle (the reference), and on the GPU by the mixed push
-with the plain closure and by the mixed push with the learned closure on
-either tensor-core engine.  After 10 intervals the oracle's momentum spectrum
+with the plain closure, by the mixed push with the learned closure on either
+tensor-core engine, and by the FP64 push with the learned closure in place of
+the closure's powers.  After 10 intervals the oracle's momentum spectrum
 spans at least 10 of the driver's 64 bins.
 
 * paired (same seed, so the same keyed noise): the metric's bar, 64-bin
@@ -76,9 +77,10 @@ def network(ctx, kpt, binding):
     net.close()
 
 
-def _gpu_run(ctx, kpt, f0, f1, start, settings, seed):
-    lower = ctx.field(f0, kpt.TABLE_FOCUSED21, kpt.PRECISION_MIXED)
-    upper = ctx.field(f1, kpt.TABLE_FOCUSED21, kpt.PRECISION_MIXED)
+def _gpu_run(ctx, kpt, f0, f1, start, settings, seed, precision=None):
+    precision = kpt.PRECISION_MIXED if precision is None else precision
+    lower = ctx.field(f0, kpt.TABLE_FOCUSED21, precision)
+    upper = ctx.field(f1, kpt.TABLE_FOCUSED21, precision)
     parts = ctx.particles(N)
     parts.upload(start, N)
     failed = 0
@@ -91,7 +93,8 @@ def _gpu_run(ctx, kpt, f0, f1, start, settings, seed):
     return out, failed
 
 
-@pytest.mark.parametrize("closure", ["plain", "learned_tcgen05", "learned_mma_sync"])
+@pytest.mark.parametrize("closure", ["plain", "learned_tcgen05", "learned_mma_sync",
+                                     "learned_f64"])
 def test_spectra_match_fp64_oracle_over_ten_intervals(ctx, kpt, binding, workload, network,
                                                        closure):
     spectra = importlib.import_module("kokkos-particletransport_gb300.spectra")
@@ -104,11 +107,16 @@ def test_spectra_match_fp64_oracle_over_ten_intervals(ctx, kpt, binding, workloa
                           else kpt.ENGINE_MMA_SYNC)
         ctx.set_surrogate(network)
         settings = kpt.settings_from_dict(_params(binding, 2))
+    # learned_f64: the FP64 push with the network in place of the closure's powers
+    precision = kpt.PRECISION_F64 if closure == "learned_f64" else kpt.PRECISION_MIXED
     try:
-        paired, failed = _gpu_run(ctx, kpt, f0, f1, start, settings, SEED)
+        paired, failed = _gpu_run(ctx, kpt, f0, f1, start, settings, SEED, precision)
         assert failed == 0
-        indep, failed = _gpu_run(ctx, kpt, f0, f1, start, settings, SEED + 1)
+        indep, failed = _gpu_run(ctx, kpt, f0, f1, start, settings, SEED + 1, precision)
         assert failed == 0
+        if closure.startswith("learned"):
+            judge = ctx.surrogate_judge()
+            assert judge["evaluations"] > 0 and judge["max_rel_error"] < 0.2, judge
     finally:
         ctx.set_surrogate(None)
         network.engine = kpt.ENGINE_TCGEN05
