@@ -158,30 +158,64 @@ __global__ void __launch_bounds__(kSplitBlock) split_scatter_kernel(const SplitL
 // order gives the serial sum).  A particle whose bin coordinate lies within
 // 1e-7 of a bin edge is set aside for the host, which re-bins it with the
 // host log so bins match the reference's host computation exactly.
+//
+// Two things keep the kernel at memory speed: the bin coordinate is first
+// formed in FP32 (a few 1e-6 from the FP64 one), and only particles whose
+// FP32 coordinate lies within 1e-3 of an edge pay for the FP64 log; and the
+// lanes of a warp that fall in the same bin add their weights together
+// before one shared-memory atomic (the momentum spectra of a push sit in a
+// handful of bins, so most of a warp's lanes share one).
 __global__ void histogram_kernel(const HistogramLaunch L) {
     extern __shared__ double shared_bins[];
     for (int b = threadIdx.x; b < L.nbins; b += blockDim.x) {
         shared_bins[b] = 0.0;
     }
     __syncthreads();
-    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < L.count;
-         i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
-        if (L.status[i] != 0) {
-            continue;
+    const unsigned full = 0xffffffffu;
+    const unsigned lane = threadIdx.x & 31u;
+    const uint64_t warp_first = blockIdx.x * static_cast<uint64_t>(blockDim.x) +
+                                (threadIdx.x & ~31u);
+    const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+    const float log_pmin_f = static_cast<float>(L.log_pmin);
+    const float inv_dlogp_f = static_cast<float>(L.inv_dlogp);
+    // the loop bound is uniform over the warp, so every lane takes part in
+    // the warp-wide bin match
+    for (uint64_t base = warp_first; base < L.count; base += stride) {
+        const uint64_t i = base + lane;
+        int bin = -1;
+        double w = 0.0;
+        if (i < L.count && L.status[i] == 0) {
+            const double p = L.p[i];
+            if (p >= L.pmin && p <= L.pmax) {
+                const float ff = (__logf(static_cast<float>(p)) - log_pmin_f) * inv_dlogp_f;
+                bool edge = false;
+                if (fabsf(ff - rintf(ff)) < 1.0e-3f) {
+                    const double f = (log(p) - L.log_pmin) * L.inv_dlogp;
+                    edge = fabs(f - rint(f)) < 1.0e-7;
+                    bin = static_cast<int>(f);
+                } else {
+                    bin = static_cast<int>(ff);
+                }
+                if (edge) {
+                    const unsigned long long slot = atomicAdd(L.edge_count, 1ull);
+                    L.edge_index[slot] = static_cast<unsigned int>(i);
+                    bin = -1;
+                } else {
+                    bin = bin < 0 ? 0 : (bin >= L.nbins ? L.nbins - 1 : bin);
+                    w = L.weight[i];
+                }
+            }
         }
-        const double p = L.p[i];
-        if (p < L.pmin || p > L.pmax) {
-            continue;
+        const unsigned peers = __match_any_sync(full, bin);
+        if (bin >= 0) {
+            double sum = 0.0;
+            for (unsigned m = peers; m != 0u; m &= m - 1u) {
+                sum += __shfl_sync(peers, w, __ffs(m) - 1);
+            }
+            if (lane == static_cast<unsigned>(__ffs(peers) - 1)) {
+                atomicAdd(shared_bins + bin, sum);
+            }
         }
-        const double f = (log(p) - L.log_pmin) * L.inv_dlogp;
-        if (fabs(f - rint(f)) < 1.0e-7) {
-            const unsigned long long slot = atomicAdd(L.edge_count, 1ull);
-            L.edge_index[slot] = static_cast<unsigned int>(i);
-            continue;
-        }
-        int bin = static_cast<int>(f);
-        bin = bin < 0 ? 0 : (bin >= L.nbins ? L.nbins - 1 : bin);
-        atomicAdd(shared_bins + bin, L.weight[i]);
     }
     __syncthreads();
     for (int b = threadIdx.x; b < L.nbins; b += blockDim.x) {
