@@ -274,6 +274,87 @@ __device__ __forceinline__ void sample_stencil(const T* __restrict__ lower,
     }
 }
 
+// Packed FP32 pairs (sm_100+ f32x2 arithmetic): two table components per
+// instruction, carried in a 64-bit register.
+__device__ __forceinline__ unsigned long long f2_fma(unsigned long long a, unsigned long long b,
+                                                     unsigned long long c) {
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+
+__device__ __forceinline__ unsigned long long f2_mul(unsigned long long a, unsigned long long b) {
+    unsigned long long d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+
+__device__ __forceinline__ unsigned long long f2_splat(float v) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1,%1};" : "=l"(r) : "f"(v));
+    return r;
+}
+
+__device__ __forceinline__ void f2_split(unsigned long long v, float& lo, float& hi) {
+    asm("mov.b64 {%0,%1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+
+// 256-bit read-only load as four component pairs.
+__device__ __forceinline__ void load4_pairs(const float* p, unsigned long long v[4]) {
+    asm("ld.global.nc.v4.u64 {%0,%1,%2,%3}, [%4];"
+        : "=l"(v[0]), "=l"(v[1]), "=l"(v[2]), "=l"(v[3])
+        : "l"(p));
+}
+
+// Mixed path: the bilinear and the time interpolation in one pass over the
+// eight rows, on component pairs: c = sum over corners of
+// (w (1 - uw)) lower + (w uw) upper (lower alone without time
+// interpolation).  Rows hold STRIDE floats (a multiple of 8, the components
+// padded); the pair of the last odd component carries a padding value that
+// is dropped.
+template <int C, int STRIDE>
+__device__ __forceinline__ void sample_stencil_pairs(const float* __restrict__ lower,
+                                                     const float* __restrict__ upper,
+                                                     const size_t pt[4], const float wc[4],
+                                                     float uw, int use_time, float c[C]) {
+    static_assert(STRIDE % 8 == 0, "rows must hold whole 256-bit chunks");
+    constexpr int kPairs = (C + 1) / 2;
+    constexpr int kChunks = (C + 7) / 8;
+    unsigned long long acc[kPairs];
+    const float lw = use_time != 0 ? 1.0f - uw : 1.0f;
+#pragma unroll
+    for (int frame = 0; frame < 2; ++frame) {
+        if (frame == 1 && use_time == 0) break;
+        const float* table = frame == 0 ? lower : upper;
+        const float tw = frame == 0 ? lw : uw;
+#pragma unroll
+        for (int corner = 0; corner < 4; ++corner) {
+            const unsigned long long w2 = f2_splat(wc[corner] * tw);
+            const float* src = table + pt[corner] * STRIDE;
+#pragma unroll
+            for (int chunk = 0; chunk < kChunks; ++chunk) {
+                unsigned long long v[4];
+                load4_pairs(src + chunk * 8, v);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const int pair = chunk * 4 + k;
+                    if (pair < kPairs) {
+                        acc[pair] = frame == 0 && corner == 0 ? f2_mul(w2, v[k])
+                                                              : f2_fma(w2, v[k], acc[pair]);
+                    }
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int pair = 0; pair < kPairs; ++pair) {
+        float lo, hi;
+        f2_split(acc[pair], lo, hi);
+        c[2 * pair] = lo;
+        if (2 * pair + 1 < C) c[2 * pair + 1] = hi;
+    }
+}
+
 __device__ __forceinline__ void corner_points(int lo0, int hi0, int lo1, int hi1, int ex,
                                               size_t pt[4]) {
     const size_t e = static_cast<size_t>(ex);
@@ -832,9 +913,9 @@ __device__ __forceinline__ void sample_mixed(const StateMixed& st, const PushPar
     corner_points(lo0, lo0 + 1, lo1, lo1 + 1, P.grid.ex, pt);
     float rt = st.tau <= 0 ? 0.0f : s64_to_float_scaled(st.tau, 1.0f / 1073741824.0f);
     rt = rt > 1.0f ? 1.0f : rt;
-    sample_stencil<float, C, STRIDE>(static_cast<const float*>(P.lower),
-                                     static_cast<const float*>(P.upper), pt, wc, rt,
-                                     s.time_interpolation, c);
+    sample_stencil_pairs<C, STRIDE>(static_cast<const float*>(P.lower),
+                                    static_cast<const float*>(P.upper), pt, wc, rt,
+                                    s.time_interpolation, c);
 }
 
 // Physics, step size, noise and the state update of one substep.
@@ -899,6 +980,78 @@ struct JudgeTally {
     float max_error;
 };
 
+// The closure values of one lane, in FP32: the network's normalised outputs
+// y mapped back to D_mumu, dD_mumu/dmu and kappa_parallel (use = inside the
+// training box), with the plain slab-QLT closure evaluated beside them in
+// FP32 to judge one substep in judge_period, to blend over [mu_cut,
+// 2 mu_cut] and to serve the lanes outside the box.  All of a warp's lanes
+// that need the plain closure take it in this one branch, so a warp
+// evaluates it at most once per substep.  A lane whose plain values are not
+// finite and positive returns use = false: the physics then evaluates the
+// plain closure in its own precision.
+__device__ __forceinline__ Served serve_closure(const PushParams& P, bool use, float mu,
+                                                float b, float p, int steps,
+                                                const float (&y)[kMlpOut], JudgeTally& tally) {
+    const SurrogateBox& box = P.sg.box;
+    Served served;
+    served.use = use;
+    const float amu = fabsf(mu);
+    const float sign = mu > 0.0f ? 1.0f : -1.0f;
+    if (use) {
+        const float y0 = y[0] * box.out_scale[0] + box.out_offset[0];
+        const float y1 = y[1] * box.out_scale[1] + box.out_offset[1];
+        const float y2 = y[2] * box.out_scale[2] + box.out_offset[2];
+        const float one_minus_mu2 = 1.0f - mu * mu;
+        served.duu = one_minus_mu2 * __expf(y0);
+        served.duu_du = served.duu * (__fdividef(sign * y1, amu + P.kf.qlt_h0) -
+                                      __fdividef(2.0f * mu, one_minus_mu2));
+        served.kpara = __expf(y2);
+        ++tally.evaluations;
+    } else {
+        ++tally.fallbacks;
+    }
+    const bool blend = use && amu < 2.0f * box.mu_cut;
+    const bool judge = use && (steps & (P.sg.judge_period - 1)) == 0;
+    if (blend || judge || !use) {
+        const Consts<float>& k = P.kf;
+        const float speed = __fdividef(k.particle_v0 * p, k.p0);
+        const float omega = __fdividef(k.qlt_omega0 * b, Num<float>::sqrt(1.0f + p * p));
+        float duu, duu_du;
+        qlt_scattering<float>(mu, omega, speed, k, duu, duu_du);
+        // kappa_parallel in the order the physics forms it
+        float knorm = 1.0f;
+        if (k.magnetic_dependency == 1) knorm *= Num<float>::pow(b, k.gamma_turb - 2.0f);
+        if (k.momentum_dependency == 1) knorm *= Num<float>::pow(__fdividef(p, k.p0), k.pindex);
+        const float kpara = k.kpara0 * knorm;
+        if (judge) {
+            const float e_d = fabsf(served.duu - duu) / duu;
+            const float e_k = fabsf(served.kpara - kpara) / kpara;
+            const float e = fmaxf(e_d, e_k);
+            tally.max_error = isfinite(e) ? fmaxf(tally.max_error, e) : INFINITY;
+            ++tally.judged;
+        }
+        if (blend) {
+            // continuous hand-over to the plain closure below mu_cut: a
+            // linear blend over [mu_cut, 2 mu_cut], with the weight's
+            // derivative in dD/dmu so the Ito drift stays consistent
+            const float w = __fdividef(amu - box.mu_cut, box.mu_cut);
+            const float dw = __fdividef(sign, box.mu_cut);
+            const float dd = served.duu - duu;
+            served.duu_du = duu_du + w * (served.duu_du - duu_du) + dw * dd;
+            served.duu = duu + w * dd;
+            served.kpara = kpara + w * (served.kpara - kpara);
+        }
+        if (!use) {
+            served.duu = duu;
+            served.duu_du = duu_du;
+            served.kpara = kpara;
+            served.use = isfinite(duu) && duu >= 0.0f && isfinite(duu_du) && isfinite(kpara) &&
+                         kpara > 0.0f;
+        }
+    }
+    return served;
+}
+
 // Warp-collective focused substep with the learned closure.  Every lane of
 // the warp calls it (converged); lanes without a particle (have = false)
 // feed zero rows to the network and return false.  Lanes whose inputs leave
@@ -955,55 +1108,7 @@ __device__ __forceinline__ bool substep_surrogate(StateMixed& st, const PushPara
     if (!have) {
         return false;
     }
-    Served served;
-    served.use = use;
-    if (use) {
-        const float y0 = y[0] * box.out_scale[0] + box.out_offset[0];
-        const float y1 = y[1] * box.out_scale[1] + box.out_offset[1];
-        const float y2 = y[2] * box.out_scale[2] + box.out_offset[2];
-        const float one_minus_mu2 = 1.0f - mu * mu;
-        const float sign = mu > 0.0f ? 1.0f : -1.0f;
-        const float amu = fabsf(mu);
-        served.duu = one_minus_mu2 * __expf(y0);
-        served.duu_du = served.duu * (__fdividef(sign * y1, amu + P.kf.qlt_h0) -
-                                      __fdividef(2.0f * mu, one_minus_mu2));
-        served.kpara = __expf(y2);
-        ++tally.evaluations;
-        const bool blend = amu < 2.0f * box.mu_cut;
-        const bool judge = (st.steps & (sg.judge_period - 1)) == 0;
-        if (blend || judge) {
-            const Consts<float>& k = P.kf;
-            const float b = c[6];
-            const float p = st.p_hi;
-            const float speed = __fdividef(k.particle_v0 * p, k.p0);
-            const float omega = __fdividef(k.qlt_omega0 * b, Num<float>::sqrt(1.0f + p * p));
-            float duu, duu_du;
-            qlt_scattering<float>(mu, omega, speed, k, duu, duu_du);
-            float kpara = k.kpara0;
-            if (k.magnetic_dependency == 1) kpara *= Num<float>::pow(b, k.gamma_turb - 2.0f);
-            if (k.momentum_dependency == 1) kpara *= Num<float>::pow(__fdividef(p, k.p0), k.pindex);
-            if (judge) {
-                const float e_d = fabsf(served.duu - duu) / duu;
-                const float e_k = fabsf(served.kpara - kpara) / kpara;
-                const float e = fmaxf(e_d, e_k);
-                tally.max_error = isfinite(e) ? fmaxf(tally.max_error, e) : INFINITY;
-                ++tally.judged;
-            }
-            if (blend) {
-                // continuous hand-over to the plain closure below mu_cut: a
-                // linear blend over [mu_cut, 2 mu_cut], with the weight's
-                // derivative in dD/dmu so the Ito drift stays consistent
-                const float w = __fdividef(amu - box.mu_cut, box.mu_cut);
-                const float dw = __fdividef(sign, box.mu_cut);
-                const float dd = served.duu - duu;
-                served.duu_du = duu_du + w * (served.duu_du - duu_du) + dw * dd;
-                served.duu = duu + w * dd;
-                served.kpara = kpara + w * (served.kpara - kpara);
-            }
-        }
-    } else {
-        ++tally.fallbacks;
-    }
+    const Served served = serve_closure(P, use, mu, c[6], st.p_hi, st.steps, y, tally);
     return advance_mixed<true, true>(st, P, c, &served);
 }
 
@@ -1049,53 +1154,12 @@ __device__ __forceinline__ bool substep_surrogate(StateF64& st, const PushParams
     if (!have) {
         return false;
     }
-    Served served;
-    served.use = use;
-    if (use) {
-        const double y0 = static_cast<double>(y[0] * box.out_scale[0] + box.out_offset[0]);
-        const double y1 = static_cast<double>(y[1] * box.out_scale[1] + box.out_offset[1]);
-        const double y2 = static_cast<double>(y[2] * box.out_scale[2] + box.out_offset[2]);
-        const double one_minus_mu2 = 1.0 - mu * mu;
-        const double sign = mu > 0.0 ? 1.0 : -1.0;
-        const double amu = fabs(mu);
-        double duu = one_minus_mu2 * exp(y0);
-        double duu_du = duu * (sign * y1 / (amu + P.kd.qlt_h0) - 2.0 * mu / one_minus_mu2);
-        double kpara = exp(y2);
-        ++tally.evaluations;
-        const bool blend = amu < 2.0 * box.mu_cut;
-        const bool judge = (st.steps & (sg.judge_period - 1)) == 0;
-        if (blend || judge) {
-            const Consts<double>& k = P.kd;
-            const double b = c[6];
-            const double p = st.p;
-            const double speed = k.particle_v0 * p / k.p0;
-            const double omega = k.qlt_omega0 * b / sqrt(1.0 + p * p);
-            double pd, pdd;
-            qlt_scattering<double>(mu, omega, speed, k, pd, pdd);
-            double pk = k.kpara0;
-            if (k.magnetic_dependency == 1) pk *= Num<double>::pow(b, k.gamma_turb - 2.0);
-            if (k.momentum_dependency == 1) pk *= Num<double>::pow(p / k.p0, k.pindex);
-            if (judge) {
-                const double e = fmax(fabs(duu - pd) / pd, fabs(kpara - pk) / pk);
-                tally.max_error = isfinite(e) ? fmaxf(tally.max_error, static_cast<float>(e))
-                                              : INFINITY;
-                ++tally.judged;
-            }
-            if (blend) {
-                const double w = (amu - box.mu_cut) / box.mu_cut;
-                const double dw = sign / box.mu_cut;
-                const double dd = duu - pd;
-                duu_du = pdd + w * (duu_du - pdd) + dw * dd;
-                duu = pd + w * dd;
-                kpara = pk + w * (kpara - pk);
-            }
-        }
-        served.duu = static_cast<float>(duu);
-        served.duu_du = static_cast<float>(duu_du);
-        served.kpara = static_cast<float>(kpara);
-    } else {
-        ++tally.fallbacks;
-    }
+    // The served values are FP32 whichever closure gives them, so the lanes
+    // outside the training box (and the judged and blended ones) take the
+    // plain closure in FP32 too: a warp then never runs the FP64 closure's
+    // five powers for a few of its lanes.
+    const Served served = serve_closure(P, use, static_cast<float>(mu), static_cast<float>(c[6]),
+                                        static_cast<float>(st.p), st.steps, y, tally);
     return advance_f64<true, true>(st, P, c, &served);
 }
 
