@@ -778,6 +778,12 @@ def run_kernel_sweep(args):
     out["split"] = {"split": int(split), "skipped": int(skipped)}
     ctx.histogram(parts, 1e-2, 1e1, 128)
     ctx.summarize(parts)
+    # surrogate training: the 2 M closure samples and a few Adam steps of
+    # the width-64 network (sample generation, forward/backward, gradient
+    # reductions, Adam)
+    net = ctx.train_surrogate(focused_settings(kpt, kpt.CLOSURE_SURROGATE), samples=2000000,
+                              steps=8, batch=8192, hidden_width=64)
+    net.close()
     torch.cuda.synchronize()
     for obj in (lower, parker64, parts):
         obj.close()
