@@ -825,7 +825,9 @@ int kpt_field_download_table(const kpt_field* field, double* out, uint64_t out_l
         KPT_CUDA(cudaStreamSynchronize(field->ctx->stream));
         for (uint64_t p = 0; p < field->points; ++p) {
             for (int c = 0; c < ncomp; ++c) {
-                out[p * ncomp + c] = static_cast<double>(host[p * field->stride + c]);
+                out[p * ncomp + c] =
+                    static_cast<double>(host[kpt::table_f32_offset(
+                        field->kind == KPT_TABLE_FOCUSED21, field->points, p, c)]);
             }
         }
     }

@@ -143,10 +143,30 @@ __global__ void build_table_kernel(const TableLaunch L) {
                 out[k] = 0.0;
             }
         }
-        T* row = table + pnt * STRIDE;
+        if constexpr (sizeof(T) == 8) {
+            T* row = table + pnt * STRIDE;
 #pragma unroll
-        for (int k = 0; k < STRIDE; ++k) {
-            row[k] = static_cast<T>(out[k]);
+            for (int k = 0; k < STRIDE; ++k) {
+                row[k] = static_cast<T>(out[k]);
+            }
+        } else {
+            // FP32 layout (table_f32_offset): 8 floats per 256-bit store
+#pragma unroll
+            for (int chunk = 0; chunk < STRIDE / 8; ++chunk) {
+                float4 lo, hi;
+                lo.x = static_cast<float>(out[8 * chunk + 0]);
+                lo.y = static_cast<float>(out[8 * chunk + 1]);
+                lo.z = static_cast<float>(out[8 * chunk + 2]);
+                lo.w = static_cast<float>(out[8 * chunk + 3]);
+                hi.x = static_cast<float>(out[8 * chunk + 4]);
+                hi.y = static_cast<float>(out[8 * chunk + 5]);
+                hi.z = static_cast<float>(out[8 * chunk + 6]);
+                hi.w = static_cast<float>(out[8 * chunk + 7]);
+                float4* dst = reinterpret_cast<float4*>(
+                    table + table_f32_offset(FOCUSED, points, pnt, 8 * chunk));
+                dst[0] = lo;
+                dst[1] = hi;
+            }
         }
     }
 }

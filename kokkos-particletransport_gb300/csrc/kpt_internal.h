@@ -14,13 +14,28 @@ namespace kpt {
 enum Precision : int { kPrecisionF64 = 0, kPrecisionMixed = 1 };
 enum Schedule : int { kScheduleRefill = 0, kScheduleSimple = 1 };
 
-// Table row stride (elements) for a kind/precision: rows start on 16-byte
-// boundaries so a point is streamed with 128-bit loads.
+// Table elements per point for a kind/precision (FP64 rows are 16-byte
+// aligned and streamed with 128/256-bit loads).
 inline int table_stride(int focused, int precision) {
     if (!focused) {
         return 16;
     }
     return precision == kPrecisionF64 ? 22 : 24;
+}
+
+// Layout of the FP32 tables.  FP64 tables are point-major rows of
+// table_stride doubles.  An FP32 table is cut into planes of
+// table_plane_floats(focused) floats per point, plane after plane: Parker
+// tables are chunk-major (two planes of 8 floats: lanes sampling
+// x-neighbouring points read neighbouring 32-byte sectors of one cache
+// line), focused tables keep one plane of whole 24-float rows (their
+// particles stream along x and rarely share lines, while a row then spans
+// one or two lines instead of three).  Component c of point p sits at
+// table_f32_offset.
+__host__ __device__ constexpr int table_plane_floats(bool focused) { return focused ? 24 : 8; }
+__host__ __device__ inline size_t table_f32_offset(bool focused, size_t points, size_t p, int c) {
+    const int w = table_plane_floats(focused);
+    return (static_cast<size_t>(c / w) * points + p) * w + c % w;
 }
 
 struct PushLaunch {

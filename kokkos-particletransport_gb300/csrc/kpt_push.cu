@@ -211,19 +211,23 @@ struct Wide {
 
 // Bilinear sample of one frame (LinearPositionInterpolator::sample,
 // FieldInterpolator.hpp:346-380): sum over corners (00, 10, 01, 11) of
-// weight * value.
+// weight * value.  FP64 tables are point-major rows of STRIDE doubles; FP32
+// tables are laid out in planes over `points` (table_f32_offset).
 template <typename T, int C, int STRIDE>
-__device__ __forceinline__ void sample_frame(const T* __restrict__ table, const size_t pt[4],
-                                             const T wc[4], T out[C]) {
+__device__ __forceinline__ void sample_frame(const T* __restrict__ table, uint64_t points,
+                                             const size_t pt[4], const T wc[4], T out[C]) {
     if constexpr (Wide<T, STRIDE>::ok) {
         constexpr int W = Wide<T, STRIDE>::width;
 #pragma unroll
         for (int corner = 0; corner < 4; ++corner) {
-            const T* src = table + pt[corner] * STRIDE;
 #pragma unroll
             for (int chunk = 0; chunk < (C + W - 1) / W; ++chunk) {
                 T v[W];
-                load8(src + chunk * W, v);
+                if constexpr (sizeof(T) == 4) {
+                    load8(table + table_f32_offset(C == 21, points, pt[corner], chunk * W), v);
+                } else {
+                    load8(table + pt[corner] * STRIDE + chunk * W, v);
+                }
 #pragma unroll
                 for (int k = 0; k < W; ++k) {
                     const int comp = chunk * W + k;
@@ -234,6 +238,7 @@ __device__ __forceinline__ void sample_frame(const T* __restrict__ table, const 
             }
         }
     } else {
+        static_assert(sizeof(T) == 8, "FP32 tables are read in whole 256-bit chunks");
         using V = typename Vec<T>::type;
         constexpr int W = Vec<T>::width;
 #pragma unroll
@@ -259,14 +264,15 @@ __device__ __forceinline__ void sample_frame(const T* __restrict__ table, const 
 // the same stencil.
 template <typename T, int C, int STRIDE>
 __device__ __forceinline__ void sample_stencil(const T* __restrict__ lower,
-                                               const T* __restrict__ upper, const size_t pt[4],
-                                               const T wc[4], T uw, int use_time, T c[C]) {
-    sample_frame<T, C, STRIDE>(lower, pt, wc, c);
+                                               const T* __restrict__ upper, uint64_t points,
+                                               const size_t pt[4], const T wc[4], T uw,
+                                               int use_time, T c[C]) {
+    sample_frame<T, C, STRIDE>(lower, points, pt, wc, c);
     if (use_time == 0) {
         return;
     }
     T u[C];
-    sample_frame<T, C, STRIDE>(upper, pt, wc, u);
+    sample_frame<T, C, STRIDE>(upper, points, pt, wc, u);
     const T lw = T(1) - uw;
 #pragma unroll
     for (int k = 0; k < C; ++k) {
@@ -307,17 +313,20 @@ __device__ __forceinline__ void load4_pairs(const float* p, unsigned long long v
 }
 
 // Mixed path: the bilinear and the time interpolation in one pass over the
-// eight rows, on component pairs: c = sum over corners of
+// eight corner points, on component pairs: c = sum over corners of
 // (w (1 - uw)) lower + (w uw) upper (lower alone without time
-// interpolation).  Rows hold STRIDE floats (a multiple of 8, the components
+// interpolation).  The 8 floats of chunk k of point p sit at
+// table_f32_offset(p, 8 k) (Parker: chunk-major planes; focused: whole
+// rows).  A point holds STRIDE floats (whole chunks, the components
 // padded); the pair of the last odd component carries a padding value that
 // is dropped.
 template <int C, int STRIDE>
 __device__ __forceinline__ void sample_stencil_pairs(const float* __restrict__ lower,
                                                      const float* __restrict__ upper,
-                                                     const size_t pt[4], const float wc[4],
-                                                     float uw, int use_time, float c[C]) {
-    static_assert(STRIDE % 8 == 0, "rows must hold whole 256-bit chunks");
+                                                     uint64_t points, const size_t pt[4],
+                                                     const float wc[4], float uw, int use_time,
+                                                     float c[C]) {
+    static_assert(STRIDE % 8 == 0, "points must hold whole 256-bit chunks");
     constexpr int kPairs = (C + 1) / 2;
     constexpr int kChunks = (C + 7) / 8;
     unsigned long long acc[kPairs];
@@ -330,11 +339,10 @@ __device__ __forceinline__ void sample_stencil_pairs(const float* __restrict__ l
 #pragma unroll
         for (int corner = 0; corner < 4; ++corner) {
             const unsigned long long w2 = f2_splat(wc[corner] * tw);
-            const float* src = table + pt[corner] * STRIDE;
 #pragma unroll
             for (int chunk = 0; chunk < kChunks; ++chunk) {
                 unsigned long long v[4];
-                load4_pairs(src + chunk * 8, v);
+                load4_pairs(table + table_f32_offset(C == 21, points, pt[corner], 8 * chunk), v);
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
                     const int pair = chunk * 4 + k;
@@ -383,7 +391,8 @@ __device__ __forceinline__ void sample_coefficients(const Grid& g, const T* __re
     size_t pt[4];
     corner_points(lo0, hi0, lo1, hi1, g.ex, pt);
     const double uwd = rt < 0.0 ? 0.0 : (rt > 1.0 ? 1.0 : rt);
-    sample_stencil<T, C, STRIDE>(lower, upper, pt, wc, static_cast<T>(uwd), use_time, c);
+    const uint64_t points = static_cast<uint64_t>(g.ex) * static_cast<uint64_t>(g.axis[1].n + 4);
+    sample_stencil<T, C, STRIDE>(lower, upper, points, pt, wc, static_cast<T>(uwd), use_time, c);
 }
 
 // ------------------------------------------------------------- physics
@@ -683,6 +692,7 @@ struct PushParams {
     Consts<float> kf;
     const void* lower;
     const void* upper;
+    uint64_t table_points;  // ghosted points of a table (chunk plane of FP32 tables)
     ParticleArrays parts;
     const uint32_t* order;  // optional work order (permutation of [0, count))
     uint64_t count;
@@ -914,8 +924,8 @@ __device__ __forceinline__ void sample_mixed(const StateMixed& st, const PushPar
     float rt = st.tau <= 0 ? 0.0f : s64_to_float_scaled(st.tau, 1.0f / 1073741824.0f);
     rt = rt > 1.0f ? 1.0f : rt;
     sample_stencil_pairs<C, STRIDE>(static_cast<const float*>(P.lower),
-                                    static_cast<const float*>(P.upper), pt, wc, rt,
-                                    s.time_interpolation, c);
+                                    static_cast<const float*>(P.upper), P.table_points, pt, wc,
+                                    rt, s.time_interpolation, c);
 }
 
 // Physics, step size, noise and the state update of one substep.
@@ -1506,6 +1516,8 @@ PushParams make_push_params(const PushLaunch& L) {
     P.fixed = L.fixed;
     P.lower = L.lower;
     P.upper = L.upper;
+    P.table_points = static_cast<uint64_t>(L.grid.ex) *
+                     static_cast<uint64_t>(L.grid.axis[1].n + 4);
     P.parts = L.parts;
     P.order = L.order;
     P.count = L.count;
