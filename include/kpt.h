@@ -503,6 +503,17 @@ typedef struct kpt_focus_solver kpt_focus_solver;
  * reader's test, AthenaFieldReader.hpp:167-193); periodic[2] per axis. */
 int kpt_grid_create(kpt_context* ctx, int nx, int ny, const double* x_edges,
                     const double* y_edges, const int32_t* periodic, kpt_grid** out);
+/* StoredCoordinateGrid(metadata, face_coordinates) through
+ * GridValidation::make_validated_stored_coordinate_grid
+ * (StoredCoordinateGrid.hpp:53-66, GridValidation.hpp:773-784): a 2D
+ * Cartesian grid on explicit, possibly non-uniform face coordinates.
+ * x_faces / y_faces hold nx+5 / ny+5 faces in storage order, face -2 first
+ * (the two ghost faces on each side included), strictly ascending; the
+ * reference's validation messages on failure.  Every library call that takes
+ * a kpt_grid accepts it: the solvers' sampling and limiters, boundary
+ * conditions, the generator and the coefficient builders. */
+int kpt_grid_create_stored(kpt_context* ctx, int nx, int ny, const double* x_faces,
+                           const double* y_faces, const int32_t* periodic, kpt_grid** out);
 int kpt_grid_destroy(kpt_grid* grid);
 
 /* ParticleSystem(count, capacity, properties, policy) with

@@ -1,5 +1,7 @@
-// Uniform 2D Cartesian grid with two ghost layers per side (Grid.hpp:65,
-// AnalyticCoordinateGrid.hpp) on the device, for the library solvers.
+// 2D Cartesian grids with two ghost layers per side (Grid.hpp:65) on the
+// device, for the library solvers: uniform analytic axes
+// (AnalyticCoordinateGrid.hpp) or explicit face coordinates
+// (StoredCoordinateGrid.hpp).
 #pragma once
 
 #include <array>
@@ -58,12 +60,47 @@ public:
     kpt_grid* get() const { return handle_.get(); }
     const Context& context() const { return context_; }
 
+protected:
+    struct StoredFaces {};
+    // explicit faces: nx + 5 and ny + 5 values, face -2 first
+    CartesianGrid2D(StoredFaces, int nx, int ny, const std::vector<double>& x_faces,
+                    const std::vector<double>& y_faces, std::array<bool, 2> periodic,
+                    Context context)
+        : context_(context), nx_(nx), ny_(ny), periodic_(periodic) {
+        if (static_cast<int>(x_faces.size()) != nx + 5 ||
+            static_cast<int>(y_faces.size()) != ny + 5) {
+            throw std::runtime_error(
+                "StoredCoordinateGrid: face coordinate view is too short.");
+        }
+        x_edges_.assign(x_faces.begin() + ghost_layers, x_faces.end() - ghost_layers);
+        y_edges_.assign(y_faces.begin() + ghost_layers, y_faces.end() - ghost_layers);
+        const int32_t flags[2] = {periodic[0] ? 1 : 0, periodic[1] ? 1 : 0};
+        kpt_grid* raw = nullptr;
+        check(kpt_grid_create_stored(context_.get(), nx, ny, x_faces.data(), y_faces.data(),
+                                     flags, &raw));
+        handle_ = std::shared_ptr<kpt_grid>(raw, [](kpt_grid* g) { kpt_grid_destroy(g); });
+    }
+
 private:
     Context context_;
     int nx_, ny_;
     std::vector<double> x_edges_, y_edges_;
     std::array<bool, 2> periodic_;
     std::shared_ptr<kpt_grid> handle_;
+};
+
+// StoredCoordinateGrid (StoredCoordinateGrid.hpp:53-66, validated as
+// GridValidation::make_validated_stored_coordinate_grid does): the same 2D
+// Cartesian grid on explicit, possibly non-uniform face coordinates, nx + 5
+// and ny + 5 of them in storage order, face -2 first (the two ghost faces
+// on each side included).  It is a CartesianGrid2D: every field, solver and
+// lifecycle call takes it; edges(dim) are its physical faces 0 .. n.
+class StoredCoordinateGrid2D : public CartesianGrid2D {
+public:
+    StoredCoordinateGrid2D(int nx, int ny, const std::vector<double>& x_faces,
+                           const std::vector<double>& y_faces, std::array<bool, 2> periodic,
+                           Context context = default_context())
+        : CartesianGrid2D(StoredFaces{}, nx, ny, x_faces, y_faces, periodic, context) {}
 };
 
 // Cell-centred field values on the host, C components per ghosted point of

@@ -268,6 +268,7 @@ def load_library() -> ctypes.CDLL:
         "kpt_context_set_surrogate": (i32, [vp, vp]),
         "kpt_surrogate_judge": (i32, [vp, vp, vp, vp, vp]),
         "kpt_grid_create": (i32, [vp, i32, i32, vp, vp, vp, pvp]),
+        "kpt_grid_create_stored": (i32, [vp, i32, i32, vp, vp, vp, pvp]),
         "kpt_grid_destroy": (i32, [vp]),
         "kpt_system_create": (i32, [vp, u64, u64, vp, vp, pvp]),
         "kpt_system_destroy": (i32, [vp]),
@@ -571,6 +572,18 @@ class Context:
         _check(self.lib.kpt_grid_create(self.handle, xe.size - 1, ye.size - 1, _ptr(xe),
                                         _ptr(ye), _ptr(per), ctypes.byref(handle)))
         return self._adopt(LibGrid(self, handle, xe.size - 1, ye.size - 1))
+
+    def stored_grid(self, x_faces, y_faces, periodic=(1, 1)) -> "LibGrid":
+        """StoredCoordinateGrid on explicit face coordinates: nx + 5 / ny + 5
+        faces in storage order, face -2 first (two ghost faces on each side),
+        strictly ascending, possibly non-uniform."""
+        xf = np.ascontiguousarray(x_faces, dtype=np.float64)
+        yf = np.ascontiguousarray(y_faces, dtype=np.float64)
+        per = np.ascontiguousarray(periodic, dtype=np.int32)
+        handle = ctypes.c_void_p()
+        _check(self.lib.kpt_grid_create_stored(self.handle, xf.size - 5, yf.size - 5, _ptr(xf),
+                                               _ptr(yf), _ptr(per), ctypes.byref(handle)))
+        return self._adopt(LibGrid(self, handle, xf.size - 5, yf.size - 5))
 
     def system(self, count: int, capacity: int, rest_mass=1.0, charge=1.0, speed_of_light=1.0,
                energy_scale_erg=1.0, split_ratio=2.0, min_child_weight=0.0) -> "ParticleSystem":
@@ -919,7 +932,8 @@ class _Handle:
 
 
 class LibGrid(_Handle):
-    """Uniform 2D Cartesian grid of the header library (kpt_grid)."""
+    """2D Cartesian grid of the header library (kpt_grid): analytic uniform
+    axes (Context.grid) or explicit faces (Context.stored_grid)."""
     _destroy = "kpt_grid_destroy"
 
     def __init__(self, ctx, handle, nx, ny):

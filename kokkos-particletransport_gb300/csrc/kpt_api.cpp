@@ -2020,6 +2020,13 @@ struct kpt_grid {
     int device = 0;
     int nx = 0, ny = 0;
     kpt::LibGrid g{};
+    DeviceBuffer coordinates;  // stored axes: faces then cell centres of each axis
+    ~kpt_grid() {
+        if (coordinates.ptr != nullptr) {
+            cudaSetDevice(device);
+            coordinates.release();
+        }
+    }
 };
 
 struct kpt_system {
@@ -2137,6 +2144,89 @@ int kpt_grid_create(kpt_context* ctx, int nx, int ny, const double* x_edges,
         a.upper = a.x0 + static_cast<double>(n) * a.dx;
         a.ghost_lower = a.x0 + (-2.0) * a.dx;
         a.ghost_upper = a.x0 + static_cast<double>(n + 2) * a.dx;
+        a.width = a.upper - a.lower;
+        a.inv_width = a.width != 0.0 ? 1.0 / a.width : 0.0;
+    }
+    g->g.ex = nx + 4;
+    *out = g.release();
+    return KPT_OK;
+}
+
+// StoredCoordinateGrid from face coordinates (StoredCoordinateGrid.hpp:53-66,
+// GridValidation.hpp:123-170, :773-784): n + 5 faces per axis including the
+// two ghost faces on each side, checked as the reference's validation does;
+// cell centres are the midpoints of adjacent faces (:423-436) and the cached
+// bounds faces 0, n (physical) and -2, n + 2 (ghosted) (:79-103).
+int kpt_grid_create_stored(kpt_context* ctx, int nx, int ny, const double* x_faces,
+                           const double* y_faces, const int32_t* periodic, kpt_grid** out) {
+    KPT_REQUIRE(ctx && x_faces && y_faces && periodic && out,
+                "kpt_grid_create_stored: NULL argument");
+    *out = nullptr;
+    KPT_REQUIRE(nx > 0 && ny > 0, "kpt_grid_create_stored: nx and ny must be positive");
+    const double* faces[2] = {x_faces, y_faces};
+    const int counts[2] = {nx, ny};
+    for (int dim = 0; dim < 2; ++dim) {
+        const double* f = faces[dim];
+        const int count = counts[dim] + 5;
+        const std::string label = "dim " + std::to_string(dim);
+        for (int i = 0; i < count; ++i) {
+            KPT_REQUIRE(std::isfinite(f[i]),
+                        "GridValidation: non-finite face-centered coordinate in " + label + ".");
+        }
+        const double first_dx = f[1] - f[0];
+        KPT_REQUIRE(first_dx != 0.0,
+                    "GridValidation: duplicate adjacent face-centered coordinates in " + label +
+                        ".");
+        KPT_REQUIRE(first_dx > 0.0,
+                    "GridValidation: descending face-centered coordinates are not supported in " +
+                        label + ".");
+        for (int i = 1; i < count - 1; ++i) {
+            const double dx = f[i + 1] - f[i];
+            KPT_REQUIRE(dx != 0.0,
+                        "GridValidation: duplicate adjacent face-centered coordinates in " +
+                            label + ".");
+            KPT_REQUIRE(dx > 0.0,
+                        "GridValidation: non-monotonic face-centered coordinates in " + label +
+                            ".");
+        }
+    }
+    if (int rc = activate(ctx)) return rc;
+    std::unique_ptr<kpt_grid> g(new kpt_grid());
+    g->ctx = ctx;
+    g->device = ctx->device;
+    g->nx = nx;
+    g->ny = ny;
+    // per axis: n + 5 faces, then n + 4 cell centres
+    std::vector<double> host;
+    size_t offsets[2][2];
+    for (int dim = 0; dim < 2; ++dim) {
+        const int n = counts[dim];
+        const double* f = faces[dim];
+        offsets[dim][0] = host.size();
+        host.insert(host.end(), f, f + n + 5);
+        offsets[dim][1] = host.size();
+        for (int k = 0; k < n + 4; ++k) {
+            host.push_back(0.5 * (f[k] + f[k + 1]));
+        }
+    }
+    KPT_CUDA(g->coordinates.reserve(host.size() * sizeof(double)));
+    KPT_CUDA(cudaMemcpy(g->coordinates.ptr, host.data(), host.size() * sizeof(double),
+                        cudaMemcpyHostToDevice));
+    for (int dim = 0; dim < 2; ++dim) {
+        const int n = counts[dim];
+        const double* f = faces[dim];
+        kpt::LibAxis& a = g->g.axis[dim];
+        a.n = n;
+        a.periodic = periodic[dim] != 0 ? 1 : 0;
+        a.stored = 1;
+        a.faces = g->coordinates.as<double>() + offsets[dim][0];
+        a.cells = g->coordinates.as<double>() + offsets[dim][1];
+        a.x0 = f[2];
+        a.dx = 0.0;
+        a.lower = f[2];
+        a.upper = f[n + 2];
+        a.ghost_lower = f[0];
+        a.ghost_upper = f[n + 4];
         a.width = a.upper - a.lower;
         a.inv_width = a.width != 0.0 ? 1.0 / a.width : 0.0;
     }

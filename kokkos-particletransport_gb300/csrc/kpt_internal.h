@@ -244,10 +244,15 @@ cudaError_t surrogate_tc_timeout_check(const uint4* block, int blocks, uint32_t 
 struct LibAxis {
     int n;
     int periodic;
-    double x0, dx;
+    double x0, dx;                    // analytic uniform axis: face i at x0 + i dx
     double lower, upper;              // faces 0 and n
     double ghost_lower, ghost_upper;  // faces -2 and n+2
     double width, inv_width;          // periodic width (upper - lower) and 1/width
+    // stored axis (StoredCoordinateGrid): explicit coordinates on the device,
+    // storage index = logical index + 2; n + 5 faces, n + 4 cell centres
+    int stored;
+    const double* faces;
+    const double* cells;
 };
 struct LibGrid {
     LibAxis axis[2];

@@ -48,13 +48,80 @@ __device__ __forceinline__ bool lib_contains(double lower, double upper, double 
     return x >= lower && x <= upper;
 }
 
-// Analytic uniform face coordinate x0 + i dx (AnalyticCoordinateGrid.hpp:167-171).
+// Face coordinate of logical index i: analytic uniform x0 + i dx
+// (AnalyticCoordinateGrid.hpp:167-171), or the stored face
+// (StoredCoordinateGrid.hpp:108-113).
 __device__ __forceinline__ double lib_face(const LibAxis& a, double i) {
+    if (a.stored) return a.faces[static_cast<int>(i) + 2];
     return __dadd_rn(a.x0, __dmul_rn(i, a.dx));
 }
 
-// MappedCoordinateGrid::cell_index over the physical domain (:255-276).
+// StoredCoordinateGrid::cell_index (StoredCoordinateGrid.hpp:301-341): the
+// cell [face k, face k + 1) holding x, cells lower_cell .. upper_cell of a
+// domain whose faces span [lower_x, upper_x].  The interval is unique (faces
+// ascend), so the bisection finds the reference's cell.
+__device__ int stored_cell_index(const LibAxis& a, double x, int lower_cell, int upper_cell,
+                                 double lower_x, double upper_x) {
+    if (x < lower_x) return lower_cell - 1;
+    if (x > upper_x) return upper_cell + 1;
+    if (x == upper_x) return upper_cell;
+    int left = lower_cell;
+    int right = upper_cell;
+    while (left <= right) {
+        const int mid = left + (right - left) / 2;
+        const double face_left = a.faces[mid + 2];
+        const double face_right = a.faces[mid + 3];
+        if (x >= face_left && x < face_right) return mid;
+        if (x < face_left) {
+            right = mid - 1;
+        } else {
+            left = mid + 1;
+        }
+    }
+    return x < lower_x ? lower_cell - 1 : upper_cell + 1;
+}
+
+// StoredCoordinateGrid::grid_index over the ghosted domain
+// (StoredCoordinateGrid.hpp:130-174): the logical index of x between the
+// stored coordinates (cell centres -2 .. n+1, or faces -2 .. n+2),
+// extrapolated linearly from the end intervals.
+__device__ double stored_grid_index(const LibAxis& a, double x, bool faces) {
+    const double* c = faces ? a.faces : a.cells;
+    const int lower_index = -2;
+    const int upper_index = faces ? a.n + 2 : a.n + 1;
+    int left = lower_index;
+    if (x <= c[lower_index + 2]) {
+        left = lower_index;
+    } else if (x >= c[upper_index + 2]) {
+        left = upper_index - 1;
+    } else {
+        int lo = lower_index;
+        int hi = upper_index - 1;
+        while (lo <= hi) {
+            const int mid = lo + (hi - lo) / 2;
+            if (x >= c[mid + 2] && x < c[mid + 3]) {
+                lo = mid;
+                break;
+            }
+            if (x < c[mid + 2]) {
+                hi = mid - 1;
+            } else {
+                lo = mid + 1;
+            }
+        }
+        left = lo;
+    }
+    const double x_left = c[left + 2];
+    const double x_right = c[left + 3];
+    return __dadd_rn(static_cast<double>(left),
+                     __ddiv_rn(__dsub_rn(x, x_left), __dsub_rn(x_right, x_left)));
+}
+
+// Cell index over the physical domain: MappedCoordinateGrid::cell_index
+// (:255-276) on an analytic axis, StoredCoordinateGrid::cell_index on a
+// stored one.
 __device__ __forceinline__ int lib_cell_index(const LibAxis& a, double x) {
+    if (a.stored) return stored_cell_index(a, x, 0, a.n - 1, a.lower, a.upper);
     if (x < a.lower) return -1;
     if (x > a.upper) return a.n;
     if (x == a.upper) return a.n - 1;
@@ -62,12 +129,14 @@ __device__ __forceinline__ int lib_cell_index(const LibAxis& a, double x) {
 }
 
 // Cell-centred stencil over the ghosted domain [-2, n+1]
-// (FieldInterpolator.hpp:509-559; AnalyticCoordinateGrid.hpp:216-230).
+// (FieldInterpolator.hpp:509-559) on the logical index of
+// AnalyticCoordinateGrid.hpp:216-230 or StoredCoordinateGrid::grid_index.
 __device__ __forceinline__ void lib_stencil(const LibAxis& a, double x, int& lo, int& hi,
                                             double& w) {
     const int lower_bound = -2;
     const int upper_bound = a.n + 1;
-    const double logical = __dsub_rn(__ddiv_rn(__dsub_rn(x, a.x0), a.dx), 0.5);
+    const double logical = a.stored ? stored_grid_index(a, x, false)
+                                    : __dsub_rn(__ddiv_rn(__dsub_rn(x, a.x0), a.dx), 0.5);
     if (logical <= static_cast<double>(lower_bound)) {
         lo = hi = lower_bound;
         w = 0.0;
@@ -1131,7 +1200,17 @@ __device__ bool gen_predicate(const LibGrid& g, const GenPredicate& P, const dou
         if (!(x >= lower_x && x <= upper_x)) return false;
         const int centering = P.field.centering[dim];
         int index;
-        if (centering == 0) {
+        if (a.stored) {
+            // StoredCoordinateGrid::cell_index for a cell-centred field, the
+            // nearest face of StoredCoordinateGrid::grid_index for a
+            // face-centred one (ParticleGenerator.hpp:317-326)
+            if (centering == 0) {
+                index = stored_cell_index(a, x, gen_lower_cell(a, P.domain),
+                                          gen_upper_cell(a, P.domain), lower_x, upper_x);
+            } else {
+                index = static_cast<int>(floor(__dadd_rn(stored_grid_index(a, x, true), 0.5)));
+            }
+        } else if (centering == 0) {
             if (x == upper_x) {
                 index = gen_upper_cell(a, P.domain);
             } else {

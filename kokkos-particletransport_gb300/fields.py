@@ -154,16 +154,39 @@ def field_file_path(field_dir: str, frame: int) -> str:
     return os.path.join(field_dir, f"field{frame:05d}.bin")
 
 
-def library_parker_basis(nx: int, ny: int, x_edges, y_edges, readme: bool = True) -> np.ndarray:
+def ghosted_faces(edges) -> np.ndarray:
+    """The n + 5 face coordinates of a stored library grid axis from its n + 1
+    physical faces: the two ghost faces on each side continue the axis
+    periodically (face -k = face n-k minus the width), face -2 first."""
+    e = np.asarray(edges, dtype=np.float64)
+    n = e.size - 1
+    w = e[-1] - e[0]
+    return np.concatenate([e[n - 2:n] - w, e, e[1:3] + w])
+
+
+def cell_centres(faces) -> np.ndarray:
+    """Cell centres of a stored axis: the midpoints of adjacent faces."""
+    f = np.asarray(faces, dtype=np.float64)
+    return 0.5 * (f[:-1] + f[1:])
+
+
+def _ghosted_centres(n: int, edges, centres):
+    if centres is not None:
+        return np.asarray(centres, dtype=np.float64)
+    d = (edges[-1] - edges[0]) / n
+    return edges[0] + (np.arange(-2, n + 2) + 0.5) * d
+
+
+def library_parker_basis(nx: int, ny: int, x_edges, y_edges, readme: bool = True,
+                         centres=None) -> np.ndarray:
     """Synthetic smooth periodic coefficient fields for the library Parker solver
-    on every ghosted cell centre of a uniform grid, in the packed order of
-    ParkerSolver.hpp:96-116: B(3) V(3) drift curl(3) diffusion primary(3)
-    secondary(3) kappa_par kappa_perp div V (points x 18, x fastest).
-    readme = False gives the constant-ratio branch (secondary zero)."""
-    dx = (x_edges[-1] - x_edges[0]) / nx
-    dy = (y_edges[-1] - y_edges[0]) / ny
-    xc = x_edges[0] + (np.arange(-2, nx + 2) + 0.5) * dx
-    yc = y_edges[0] + (np.arange(-2, ny + 2) + 0.5) * dy
+    on every ghosted cell centre (of a uniform grid, or the given (xc, yc)
+    centres of a stored one), in the packed order of ParkerSolver.hpp:96-116:
+    B(3) V(3) drift curl(3) diffusion primary(3) secondary(3) kappa_par
+    kappa_perp div V (points x 18, x fastest).  readme = False gives the
+    constant-ratio branch (secondary zero)."""
+    xc = _ghosted_centres(nx, x_edges, None if centres is None else centres[0])
+    yc = _ghosted_centres(ny, y_edges, None if centres is None else centres[1])
     y, x = np.meshgrid(yc, xc, indexing="ij")
     kx, ky = np.pi, np.pi / 2.0
     out = np.zeros((ny + 4, nx + 4, 18))
@@ -186,15 +209,14 @@ def library_parker_basis(nx: int, ny: int, x_edges, y_edges, readme: bool = True
     return out.reshape(-1, 18)
 
 
-def library_focus_basis(nx: int, ny: int, x_edges, y_edges) -> np.ndarray:
+def library_focus_basis(nx: int, ny: int, x_edges, y_edges, centres=None) -> np.ndarray:
     """Smooth periodic focused-transport fields on every ghosted cell centre in
     the packed order B(3) b(3) V(3) grad-drift(3) curvature-drift(3) perp-adv(3)
     |B| kpar kperp divV focusing bb:gradV b.dV/dt sigma^2 Lc."""
-    parker = library_parker_basis(nx, ny, x_edges, y_edges, True).reshape(ny + 4, nx + 4, 18)
-    dx = (x_edges[-1] - x_edges[0]) / nx
-    dy = (y_edges[-1] - y_edges[0]) / ny
-    xc = x_edges[0] + (np.arange(-2, nx + 2) + 0.5) * dx
-    yc = y_edges[0] + (np.arange(-2, ny + 2) + 0.5) * dy
+    parker = library_parker_basis(nx, ny, x_edges, y_edges, True,
+                                  centres).reshape(ny + 4, nx + 4, 18)
+    xc = _ghosted_centres(nx, x_edges, None if centres is None else centres[0])
+    yc = _ghosted_centres(ny, y_edges, None if centres is None else centres[1])
     y, x = np.meshgrid(yc, xc, indexing="ij")
     kx, ky = np.pi, np.pi / 2.0
     out = np.zeros((ny + 4, nx + 4, 27))

@@ -300,6 +300,23 @@ class ReferenceHarness:
         lib.ref_lib_candidates.restype = ll
         lib.ref_lib_candidates.argtypes = [i32, i32, vp, vp, vp, i32, i32, vp, vp, vp, vp, vp,
                                            vp, ll, vp]
+        lib.ref_set_lib_stored_faces.restype = None
+        lib.ref_set_lib_stored_faces.argtypes = [vp, vp]
+        self._faces_alive = None
+
+    def _lib_grid(self, grid: dict) -> None:
+        """Select the grid of the library call that follows: a stored grid
+        (StoredCoordinateGrid) when `grid` carries x_faces / y_faces (n + 5
+        faces each, face -2 first; x_edges / y_edges are then the physical
+        faces), else the analytic grid on the uniform x_edges / y_edges."""
+        if "x_faces" in grid:
+            xf = np.ascontiguousarray(grid["x_faces"], dtype=np.float64)
+            yf = np.ascontiguousarray(grid["y_faces"], dtype=np.float64)
+            self._faces_alive = (xf, yf)
+            self.lib.ref_set_lib_stored_faces(_ptr(xf), _ptr(yf))
+        else:
+            self._faces_alive = None
+            self.lib.ref_set_lib_stored_faces(None, None)
 
     @staticmethod
     def _param_arrays(params: dict):
@@ -404,6 +421,7 @@ class ReferenceHarness:
         """ParkerSolver steps (include/ParkerSolver.hpp) on a uniform Cartesian grid;
         updates `system` in place and returns the dt of each step.  normals
         ([steps][4][count], optional) replaces the keyed stream's normals."""
+        self._lib_grid(grid)
         xe = np.ascontiguousarray(grid["x_edges"], dtype=np.float64)
         ye = np.ascontiguousarray(grid["y_edges"], dtype=np.float64)
         periodic = np.ascontiguousarray(grid["periodic"], dtype=np.int32)
@@ -426,6 +444,7 @@ class ReferenceHarness:
         """FocusTransportSolver steps (include/FocusSolver.hpp) on a uniform Cartesian
         grid; updates `system` in place and returns the dt of each step.  normals
         ([steps][4][count], optional) replaces the keyed stream's normals."""
+        self._lib_grid(grid)
         xe = np.ascontiguousarray(grid["x_edges"], dtype=np.float64)
         ye = np.ascontiguousarray(grid["y_edges"], dtype=np.float64)
         periodic = np.ascontiguousarray(grid["periodic"], dtype=np.int32)
@@ -449,6 +468,7 @@ class ReferenceHarness:
     def lib_system(self, grid: dict, props: dict, op: str, count: int,
                    system: Dict[str, np.ndarray], key_range=(0, 0)):
         """One ParticleSystem lifecycle call; returns (count after, split statistics)."""
+        self._lib_grid(grid)
         ops = {"boundary": 0, "sort": 1, "compact": 2, "split": 3, "capture": 4}
         xe = np.ascontiguousarray(grid["x_edges"], dtype=np.float64)
         ye = np.ascontiguousarray(grid["y_edges"], dtype=np.float64)
@@ -491,6 +511,7 @@ class ReferenceHarness:
                       predicate=None, kinematics=(1.0, 0.0, 1.0, 0), plan=(0, 0, 0, 64),
                       selection: int = 0, seed: int = 114514, frame: int = 0) -> int:
         """One injection or recycling call; returns the particle count after it."""
+        self._lib_grid(grid)
         xe, ye, periodic, values, components, cent, reg, pred = self._generator_inputs(
             grid, field, centering, region, predicate or {})
         pr = np.array([props["rest_mass"], props["charge"], props["speed_of_light"],
@@ -511,6 +532,7 @@ class ReferenceHarness:
     def lib_candidates(self, grid: dict, kind: str, *, field=None, centering=(0, 0),
                        region=None, predicate=None):
         """Candidate set: kind "field" or "grid"; returns (indices, cumulative weights, total)."""
+        self._lib_grid(grid)
         if field is None:
             field = np.zeros(1)
         xe, ye, periodic, values, components, cent, reg, pred = self._generator_inputs(
@@ -533,6 +555,7 @@ class ReferenceHarness:
                                 drift_floor: float = 0.0, ghost_mode: int = 0) -> np.ndarray:
         """The reference's Parker coefficient precompute and packed basis
         (points x 18) from cell-centred B and V (points x 3, ghosts as given)."""
+        self._lib_grid(grid)
         xe = np.ascontiguousarray(grid["x_edges"], dtype=np.float64)
         ye = np.ascontiguousarray(grid["y_edges"], dtype=np.float64)
         periodic = np.ascontiguousarray(grid["periodic"], dtype=np.int32)
@@ -564,6 +587,7 @@ class ReferenceHarness:
                                ghost_mode: int = 0) -> np.ndarray:
         """The reference's focused coefficient precompute and packed basis
         (points x 27) from cell-centred B, V and dV/dt (points x 3)."""
+        self._lib_grid(grid)
         xe = np.ascontiguousarray(grid["x_edges"], dtype=np.float64)
         ye = np.ascontiguousarray(grid["y_edges"], dtype=np.float64)
         periodic = np.ascontiguousarray(grid["periodic"], dtype=np.int32)

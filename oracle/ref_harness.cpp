@@ -20,6 +20,7 @@
 //                    split_particles_on_energy_growth}    ParticleSystem.hpp:623-917
 #include "src/main.cpp"
 
+#include <type_traits>
 #include <string>
 
 #include "FocusSolver.hpp"
@@ -258,6 +259,62 @@ LibAnalyticGrid make_lib_analytic_grid(int nx, int ny, const double* x_edges,
         metadata, discretization, start, step);
 }
 
+// Explicit faces (nx+5 / ny+5, face -2 first) -> the reference's validated
+// StoredCoordinateGrid (StoredCoordinateGrid.hpp:53-66,
+// GridValidation.hpp:773-784) with the same metadata as the analytic grid.
+using LibStoredGrid = StoredCoordinateGrid<2, Device, LibLayout, 3>;
+LibStoredGrid make_lib_stored_grid(int nx, int ny, const double* x_faces, const double* y_faces,
+                                   const int* periodic) {
+    typename LibMeta::index_array_type extents{};
+    extents[0] = nx;
+    extents[1] = ny;
+    typename LibMeta::ghost_array_type ghosts{};
+    typename LibMeta::periodic_array_type flags{};
+    for (int dim = 0; dim < 2; ++dim) {
+        ghosts[dim][LowerBoundary] = 2;
+        ghosts[dim][UpperBoundary] = 2;
+        flags[dim] = periodic[dim];
+    }
+    LibMeta metadata(extents, ghosts, flags);
+    const int max_faces = std::max(nx, ny) + 5;
+    typename LibStoredGrid::coordinate_view_type faces("lib_stored_faces", 2, max_faces);
+    const double* f[2] = {x_faces, y_faces};
+    const int counts[2] = {nx, ny};
+    for (int dim = 0; dim < 2; ++dim) {
+        for (int k = 0; k < max_faces; ++k) {
+            // the shorter axis' unused tail continues its last spacing
+            const int n = counts[dim] + 5;
+            faces(dim, k) = k < n ? f[dim][k]
+                                  : f[dim][n - 1] + (k - n + 1) * (f[dim][n - 1] - f[dim][n - 2]);
+        }
+    }
+    return GridValidation::make_validated_stored_coordinate_grid<2, Device, LibLayout, 3>(
+        metadata, faces);
+}
+
+// Faces of a stored grid for the library calls that follow (NULL: the
+// analytic grid on the calls' uniform edges).
+const double* g_lib_faces[2] = {nullptr, nullptr};
+
+// Run body(grid) on the grid the next library call asks for; exceptions
+// become the -1 return with the message kept.
+template <typename Body>
+long long on_lib_grid(int nx, int ny, const double* x_edges, const double* y_edges,
+                      const int* periodic, Body&& body) {
+    try {
+        if (g_lib_faces[0] != nullptr) {
+            const LibStoredGrid grid =
+                make_lib_stored_grid(nx, ny, g_lib_faces[0], g_lib_faces[1], periodic);
+            return body(grid);
+        }
+        const LibAnalyticGrid grid = make_lib_analytic_grid(nx, ny, x_edges, y_edges, periodic);
+        return body(grid);
+    } catch (const std::exception& error) {
+        g_last_error = error.what();
+        return -1;
+    }
+}
+
 // Particle arrays of the host side: doubles [10][capacity] = x, y, prev x,
 // prev y, prev-step x, prev-step y, momentum, mu, weight, E0; ints
 // [3][capacity] = status, split level, sort key; ids [capacity].
@@ -324,6 +381,13 @@ extern "C" {
 
 const char* ref_last_error() { return g_last_error.c_str(); }
 double ref_last_move_seconds() { return g_last_move_seconds; }
+
+// Library calls after this one run on the stored grid of these faces
+// (nx+5 / ny+5 each, face -2 first); NULL restores the analytic grid.
+void ref_set_lib_stored_faces(const double* x_faces, const double* y_faces) {
+    g_lib_faces[0] = x_faces;
+    g_lib_faces[1] = y_faces;
+}
 
 // Build the driver's per-cell coefficient table (16 Parker or 21 focused
 // components) for one compact field file.  out holds point_count * C doubles
@@ -555,11 +619,12 @@ long long ref_lib_parker(int nx, int ny, const double* x_edges, const double* y_
                          int steps, int mode, long long count, long long capacity,
                          unsigned long long* ids, double* d, int* ints, double* dts,
                          const double* normals) {
-    try {
-        using solver_type = ParkerSolver<LibAnalyticGrid>;
+    return on_lib_grid(nx, ny, x_edges, y_edges, periodic,
+                       [&](const auto& grid) -> long long {
+        using G = std::decay_t<decltype(grid)>;
+        using solver_type = ParkerSolver<G>;
         using vector_field = typename solver_type::vector_field_type;
         using scalar_field = typename solver_type::scalar_field_type;
-        const LibAnalyticGrid grid = make_lib_analytic_grid(nx, ny, x_edges, y_edges, periodic);
         vector_field b(grid, "lib_b", GridCentering::CellCentered);
         vector_field v(grid, "lib_v", GridCentering::CellCentered);
         vector_field curl(grid, "lib_curl", GridCentering::CellCentered);
@@ -583,7 +648,7 @@ long long ref_lib_parker(int nx, int ny, const double* x_edges, const double* y_
             divv.data(k, 0) = row[17];
         }
         LegencyModel::DiffusionModelParameters parameters;
-        ParkerCoefficient::DiffusionTensorDivergenceFieldSet<LibAnalyticGrid> divergence;
+        ParkerCoefficient::DiffusionTensorDivergenceFieldSet<G> divergence;
         if (constant_ratio) {
             parameters.set_constant_perpendicular_parallel_ratio(1.0);
             divergence.perpendicular_model =
@@ -615,10 +680,7 @@ long long ref_lib_parker(int nx, int ny, const double* x_edges, const double* y_
         Kokkos::ShimImpl::external_normals() = nullptr;
         lib_store(solver.particles, h);
         return 0;
-    } catch (const std::exception& error) {
-        g_last_error = error.what();
-        return -1;
-    }
+    });
 }
 
 // FocusTransportSolver steps on a uniform 2D Cartesian grid.  basis holds
@@ -635,11 +697,12 @@ long long ref_lib_focus(int nx, int ny, const double* x_edges, const double* y_e
                         int first_step, int steps, int mode, long long count, long long capacity,
                         unsigned long long* ids, double* d, int* ints, double* dts,
                         const double* normals) {
-    try {
-        using solver_type = FocusSolver<LibAnalyticGrid>;
+    return on_lib_grid(nx, ny, x_edges, y_edges, periodic,
+                       [&](const auto& grid) -> long long {
+        using G = std::decay_t<decltype(grid)>;
+        using solver_type = FocusSolver<G>;
         using vector_field = typename solver_type::vector_field_type;
         using scalar_field = typename solver_type::scalar_field_type;
-        const LibAnalyticGrid grid = make_lib_analytic_grid(nx, ny, x_edges, y_edges, periodic);
         auto vec = [&](const char* name) { return vector_field(grid, name, GridCentering::CellCentered); };
         auto sca = [&](const char* name) { return scalar_field(grid, name, GridCentering::CellCentered); };
         vector_field b = vec("f_b"), dir = vec("f_dir"), v = vec("f_v"), grad = vec("f_grad"),
@@ -707,10 +770,7 @@ long long ref_lib_focus(int nx, int ny, const double* x_edges, const double* y_e
         Kokkos::ShimImpl::external_normals() = nullptr;
         lib_store(solver.particles, h);
         return 0;
-    } catch (const std::exception& error) {
-        g_last_error = error.what();
-        return -1;
-    }
+    });
 }
 
 // ParticleSystem lifecycle on the same grid: op 0 boundary conditions,
@@ -724,8 +784,9 @@ long long ref_lib_system(int nx, int ny, const double* x_edges, const double* y_
                          int key_hi, long long count, long long capacity,
                          unsigned long long* ids, double* d, int* ints,
                          unsigned long long* stats) {
-    try {
-        const LibAnalyticGrid grid = make_lib_analytic_grid(nx, ny, x_edges, y_edges, periodic);
+    return on_lib_grid(nx, ny, x_edges, y_edges, periodic,
+                       [&](const auto& grid) -> long long {
+        using G = std::decay_t<decltype(grid)>;
         ParticleSplittingPolicy policy;
         policy.energy_split_ratio = props[5];
         policy.minimum_child_weight = props[6];
@@ -754,10 +815,7 @@ long long ref_lib_system(int nx, int ny, const double* x_edges, const double* y_
         stats[0] = sys.particle_count();
         lib_store(sys, h);
         return 0;
-    } catch (const std::exception& error) {
-        g_last_error = error.what();
-        return -1;
-    }
+    });
 }
 
 // The reference CLI entry point itself.  Noise frames are keyed as
@@ -776,20 +834,19 @@ int ref_main(int argc, char** argv, int frame_base) {
 // ---- ParticleGenerator on the library grid ----------------------------------
 namespace {
 
-template <int C>
-using LibGenField = Field<LibAnalyticGrid, C>;
+template <typename G, int C>
+using LibGenField = Field<G, C>;
 
 // field values: C doubles per stored point in the Field's flattened order
 // (dim 0 fastest over the ghosted extent of its centering);
 // centering[dim]: 0 cell, 1 face.
-template <int C>
-LibGenField<C> lib_gen_field(const LibAnalyticGrid& grid, const int* centering,
-                             const double* values) {
-    typename LibGenField<C>::centering_array_type c{};
+template <int C, typename G>
+LibGenField<G, C> lib_gen_field(const G& grid, const int* centering, const double* values) {
+    typename LibGenField<G, C>::centering_array_type c{};
     for (int dim = 0; dim < 2; ++dim) {
         c[dim] = centering[dim] == 0 ? GridCentering::CellCentered : GridCentering::FaceCentered;
     }
-    LibGenField<C> field(grid, "lib_generator_field", c);
+    LibGenField<G, C> field(grid, "lib_generator_field", c);
     const std::size_t points = field.point_count();
     for (std::size_t k = 0; k < points; ++k) {
         for (int comp = 0; comp < C; ++comp) field.data(k, comp) = values[k * C + comp];
@@ -807,8 +864,8 @@ AxisAlignedParticleRegion<2> lib_gen_region(const double* r) {
     return make_particle_region<2>(lower, upper);
 }
 
-template <int C>
-void lib_generator_run(const LibAnalyticGrid& grid, LibSystem& sys, int op, const int* centering,
+template <int C, typename G>
+void lib_generator_run(const G& grid, LibSystem& sys, int op, const int* centering,
                        const double* values, const double* region, const double* pred,
                        const double* kin, const unsigned long long* plan_in, int selection,
                        unsigned long long seed) {
@@ -879,8 +936,8 @@ void lib_generator_run(const LibAnalyticGrid& grid, LibSystem& sys, int op, cons
     }
 }
 
-template <int C>
-long long lib_candidates_run(const LibAnalyticGrid& grid, int kind, const int* centering,
+template <int C, typename G>
+long long lib_candidates_run(const G& grid, int kind, const int* centering,
                              const double* values, const double* region, const double* pred,
                              unsigned long long* indices, double* cumulative, long long max_out,
                              double* total) {
@@ -937,8 +994,9 @@ long long ref_lib_generator(int nx, int ny, const double* x_edges, const double*
                             unsigned long long seed, unsigned frame, long long count,
                             long long capacity, unsigned long long* ids, double* d, int* ints,
                             unsigned long long* out_count) {
-    try {
-        const LibAnalyticGrid grid = make_lib_analytic_grid(nx, ny, x_edges, y_edges, periodic);
+    return on_lib_grid(nx, ny, x_edges, y_edges, periodic,
+                       [&](const auto& grid) -> long long {
+        using G = std::decay_t<decltype(grid)>;
         LibSystem sys(static_cast<typename LibSystem::size_type>(count),
                       static_cast<typename LibSystem::size_type>(capacity),
                       lib_properties(props));
@@ -958,10 +1016,7 @@ long long ref_lib_generator(int nx, int ny, const double* x_edges, const double*
         *out_count = sys.particle_count();
         lib_store(sys, h);
         return 0;
-    } catch (const std::exception& error) {
-        g_last_error = error.what();
-        return -1;
-    }
+    });
 }
 
 // Candidate sets: kind 0 field points passing the predicate (region or NULL
@@ -973,18 +1028,16 @@ long long ref_lib_candidates(int nx, int ny, const double* x_edges, const double
                              const int* centering, const double* values, const double* region,
                              const double* pred, unsigned long long* indices, double* cumulative,
                              long long max_out, double* total) {
-    try {
-        const LibAnalyticGrid grid = make_lib_analytic_grid(nx, ny, x_edges, y_edges, periodic);
+    return on_lib_grid(nx, ny, x_edges, y_edges, periodic,
+                       [&](const auto& grid) -> long long {
+        using G = std::decay_t<decltype(grid)>;
         if (components == 3) {
             return lib_candidates_run<3>(grid, kind, centering, values, region, pred, indices,
                                          cumulative, max_out, total);
         }
         return lib_candidates_run<1>(grid, kind, centering, values, region, pred, indices,
                                      cumulative, max_out, total);
-    } catch (const std::exception& error) {
-        g_last_error = error.what();
-        return -1;
-    }
+    });
 }
 
 }  // extern "C"
@@ -1009,10 +1062,11 @@ long long ref_lib_parker_coefficients(int nx, int ny, const double* x_edges,
                                       const double* turb_fields, const double* props,
                                       const double* params, double drift_floor, int ghost_mode,
                                       double* packed_out) {
-    try {
-        using solver_type = ParkerSolver<LibAnalyticGrid>;
+    return on_lib_grid(nx, ny, x_edges, y_edges, periodic,
+                       [&](const auto& grid) -> long long {
+        using G = std::decay_t<decltype(grid)>;
+        using solver_type = ParkerSolver<G>;
         using vector_field = typename solver_type::vector_field_type;
-        const LibAnalyticGrid grid = make_lib_analytic_grid(nx, ny, x_edges, y_edges, periodic);
         vector_field b(grid, "coef_b", GridCentering::CellCentered);
         vector_field v(grid, "coef_v", GridCentering::CellCentered);
         const std::size_t points = b.point_count();
@@ -1024,7 +1078,7 @@ long long ref_lib_parker_coefficients(int nx, int ny, const double* x_edges,
         }
         const auto model = TurbulencePropertyModel::constant_code_units(turb[0], turb[1],
                                                                         turb[2], turb[3]);
-        TurbulenceProperties<LibAnalyticGrid> turbulence(
+        TurbulenceProperties<G> turbulence(
             grid, model,
             turb_mode == 0 ? TurbulencePropertyStorageMode::ConstantOnly
                            : TurbulencePropertyStorageMode::Field);
@@ -1060,10 +1114,7 @@ long long ref_lib_parker_coefficients(int nx, int ny, const double* x_edges,
             }
         }
         return static_cast<long long>(points);
-    } catch (const std::exception& error) {
-        g_last_error = error.what();
-        return -1;
-    }
+    });
 }
 
 }  // extern "C"
@@ -1084,10 +1135,11 @@ long long ref_lib_focus_coefficients(int nx, int ny, const double* x_edges, cons
                                      const double* turb_fields, const double* props,
                                      const double* params, double builder_floor, int ghost_mode,
                                      double* packed_out) {
-    try {
-        using solver_type = FocusSolver<LibAnalyticGrid>;
+    return on_lib_grid(nx, ny, x_edges, y_edges, periodic,
+                       [&](const auto& grid) -> long long {
+        using G = std::decay_t<decltype(grid)>;
+        using solver_type = FocusSolver<G>;
         using vector_field = typename solver_type::vector_field_type;
-        const LibAnalyticGrid grid = make_lib_analytic_grid(nx, ny, x_edges, y_edges, periodic);
         vector_field b(grid, "fc_b", GridCentering::CellCentered);
         vector_field v(grid, "fc_v", GridCentering::CellCentered);
         vector_field dvdt(grid, "fc_dvdt", GridCentering::CellCentered);
@@ -1101,7 +1153,7 @@ long long ref_lib_focus_coefficients(int nx, int ny, const double* x_edges, cons
         }
         const auto model = TurbulencePropertyModel::constant_code_units(turb[0], turb[1],
                                                                         turb[2], turb[3]);
-        TurbulenceProperties<LibAnalyticGrid> turbulence(
+        TurbulenceProperties<G> turbulence(
             grid, model,
             turb_mode == 0 ? TurbulencePropertyStorageMode::ConstantOnly
                            : TurbulencePropertyStorageMode::Field);
@@ -1139,10 +1191,7 @@ long long ref_lib_focus_coefficients(int nx, int ny, const double* x_edges, cons
             }
         }
         return static_cast<long long>(points);
-    } catch (const std::exception& error) {
-        g_last_error = error.what();
-        return -1;
-    }
+    });
 }
 
 }  // extern "C"

@@ -50,6 +50,15 @@ def load_golden(name: str) -> dict:
         return {k: data[k] for k in data.files}
 
 
+def lib_grid(ctx, data: dict, periodic=None):
+    """The library grid of a golden file: a stored grid on its x_faces /
+    y_faces when it has them, else the analytic grid on its uniform edges."""
+    periodic = data["periodic"] if periodic is None else periodic
+    if "x_faces" in data:
+        return ctx.stored_grid(data["x_faces"], data["y_faces"], periodic)
+    return ctx.grid(data["x_edges"], data["y_edges"], periodic)
+
+
 def golden_params(data: dict) -> dict:
     """A fixture's parameters over the oracle defaults (closure fields included)."""
     binding = importlib.import_module("binding")

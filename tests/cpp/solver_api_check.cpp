@@ -115,10 +115,19 @@ kpt::HostParticles start_state(const std::map<std::string, Record>& in) {
     return h;
 }
 
+// The analytic grid on uniform edges, or a StoredCoordinateGrid2D when the
+// input carries explicit faces.
 kpt::CartesianGrid2D make_grid(const std::map<std::string, Record>& in) {
+    const auto per = in.at("periodic").as<int32_t>();
+    if (in.count("x_faces") != 0) {
+        const auto xf = in.at("x_faces").as<double>();
+        const auto yf = in.at("y_faces").as<double>();
+        return kpt::StoredCoordinateGrid2D(static_cast<int>(xf.size()) - 5,
+                                           static_cast<int>(yf.size()) - 5, xf, yf,
+                                           {per.at(0) != 0, per.at(1) != 0});
+    }
     const auto xe = in.at("x_edges").as<double>();
     const auto ye = in.at("y_edges").as<double>();
-    const auto per = in.at("periodic").as<int32_t>();
     return kpt::CartesianGrid2D(static_cast<int>(xe.size()) - 1, static_cast<int>(ye.size()) - 1,
                                 xe, ye, {per.at(0) != 0, per.at(1) != 0});
 }

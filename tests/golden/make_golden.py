@@ -45,12 +45,14 @@ Cases
   lib_system.npz      ParticleSystem lifecycle: boundary conditions,
                       sort_by_key, compact_active_particles,
                       split_particles_on_energy_growth, capture_previous_positions
+  lib_*_stored*.npz   the solver, lifecycle, generator and coefficient cases
+                      on a StoredCoordinateGrid with stretched x and y faces
 
   c1/                 the strict CLI run of the 256x512 configuration
                       (summary, 128-bin histogram, first snapshot records)
 
-``python tests/golden/make_golden.py lib`` (or ``c1``) regenerates only those
-files.
+``python tests/golden/make_golden.py lib`` (or ``c1``, ``stored``) regenerates
+only those files.
 """
 from __future__ import annotations
 
@@ -320,24 +322,62 @@ def lib_save(out_dir, name, **arrays):
     np.savez_compressed(os.path.join(out_dir, name), **arrays)
 
 
-def make_lib(ref, out_dir):
-    rng = np.random.default_rng(2718)
+class LibGeometry:
+    """Axes of a library grid: uniform edges (the analytic grid), or
+    stretched edges whose n + 5 faces (two ghost faces per side, continued
+    periodically) make a StoredCoordinateGrid.  The stored files carry the
+    faces, the tests build the same grid from them."""
+
+    def __init__(self, nx, ny, xlim, ylim, stored):
+        self.nx, self.ny, self.stored = nx, ny, stored
+        if stored:
+            self.xe = fields.stretched_edges(nx, xlim[0], xlim[1], strength=1.5)
+            self.ye = fields.stretched_edges(ny, ylim[0], ylim[1], strength=4.0)
+            self.xf = fields.ghosted_faces(self.xe)
+            self.yf = fields.ghosted_faces(self.ye)
+        else:
+            self.xe = np.linspace(xlim[0], xlim[1], nx + 1)
+            self.ye = np.linspace(ylim[0], ylim[1], ny + 1)
+
+    @property
+    def suffix(self):
+        return "_stored" if self.stored else ""
+
+    def grid(self, periodic):
+        g = dict(x_edges=self.xe, y_edges=self.ye, periodic=np.array(periodic, dtype=np.int32))
+        g.update(self.extra())
+        return g
+
+    def extra(self):
+        return dict(x_faces=self.xf, y_faces=self.yf) if self.stored else {}
+
+    def centres(self):
+        """Ghosted cell centres (n + 4) of each axis; None on the uniform
+        grid, whose helpers form them from the spacing."""
+        if not self.stored:
+            return None
+        return fields.cell_centres(self.xf), fields.cell_centres(self.yf)
+
+
+def make_lib(ref, out_dir, stored=False):
+    rng = np.random.default_rng(2718 + (1 if stored else 0))
     nx, ny = 24, 40
-    xe = np.linspace(-1.0, 1.0, nx + 1)
-    ye = np.linspace(-2.0, 2.0, ny + 1)
+    geo = LibGeometry(nx, ny, (-1.0, 1.0), (-2.0, 2.0), stored)
+    xe, ye = geo.xe, geo.ye
     props = dict(rest_mass=1.0, charge=1.0, speed_of_light=1.0, energy_scale=1.0, courant=0.3)
     cases = (("readme_periodic", True, (1, 1), True, 4),
              ("ratio_open", False, (1, 0), True, 4),
              ("readme_deterministic", True, (1, 0), False, 3))
     for name, readme, periodic, stochastic, steps in cases:
-        grid = dict(x_edges=xe, y_edges=ye, periodic=np.array(periodic, dtype=np.int32))
-        basis = lib_basis(nx, ny, xe, ye, readme)
+        grid = geo.grid(periodic)
+        basis = lib_basis(nx, ny, xe, ye, readme, centres=geo.centres())
         count, capacity = 700, 768
         start = lib_population(rng, count, capacity, xe, ye, periodic[1] == 0)
         system = {k: v.copy() for k, v in start.items()}
         dts = ref.lib_parker(grid, basis, not readme, props, SEED, 10, steps, stochastic, count,
                              system)
-        lib_save(out_dir, f"lib_parker_{name}.npz", x_edges=xe, y_edges=ye,
+        lib_save(out_dir, f"lib_parker{geo.suffix}_{name}.npz", x_edges=xe, y_edges=ye,
+                 **geo.extra(),
                  periodic=grid["periodic"], basis=basis, constant_ratio=int(not readme),
                  stochastic=int(stochastic), steps=steps, first_step=10, seed=SEED,
                  count=count, courant=props["courant"], dts=dts,
@@ -349,15 +389,16 @@ def make_lib(ref, out_dir):
                    ("deterministic", False, (1, 1), False, 3, 1.0))
     scattering = dict(spectral_index=5.0 / 3.0, h0=1e-6)
     for name, ratio, periodic, stochastic, steps, max_mu in focus_cases:
-        grid = dict(x_edges=xe, y_edges=ye, periodic=np.array(periodic, dtype=np.int32))
-        basis = lib_focus_basis(nx, ny, xe, ye)
+        grid = geo.grid(periodic)
+        basis = lib_focus_basis(nx, ny, xe, ye, centres=geo.centres())
         count, capacity = 600, 640
         start = lib_population(rng, count, capacity, xe, ye, periodic[1] == 0)
         system = {k: v.copy() for k, v in start.items()}
         scat = dict(scattering, max_mu=max_mu)
         dts = ref.lib_focus(grid, basis, ratio, props, scat, SEED, 20, steps, stochastic, count,
                             system)
-        lib_save(out_dir, f"lib_focus_{name}.npz", x_edges=xe, y_edges=ye,
+        lib_save(out_dir, f"lib_focus{geo.suffix}_{name}.npz", x_edges=xe, y_edges=ye,
+                 **geo.extra(),
                  periodic=grid["periodic"], basis=basis, constant_ratio=int(ratio),
                  stochastic=int(stochastic), steps=steps, first_step=20, seed=SEED,
                  count=count, courant=props["courant"], dts=dts,
@@ -369,7 +410,7 @@ def make_lib(ref, out_dir):
     # draws on both sides; a tenth of them widened fourfold to reach the
     # pitch-angle clamp and the open boundaries
     nrng = np.random.default_rng(31415)
-    for kind, periodic, steps in (("parker", (1, 0), 3), ("focus", (1, 0), 3)):
+    for kind, periodic, steps in () if stored else (("parker", (1, 0), 3), ("focus", (1, 0), 3)):
         grid = dict(x_edges=xe, y_edges=ye, periodic=np.array(periodic, dtype=np.int32))
         count, capacity = 500, 512
         start = lib_population(nrng, count, capacity, xe, ye, True)
@@ -393,7 +434,7 @@ def make_lib(ref, out_dir):
                  **{f"start_{k}": v for k, v in start.items()},
                  **{f"end_{k}": v for k, v in system.items()})
     # ParticleSystem lifecycle
-    grid = dict(x_edges=xe, y_edges=ye, periodic=np.array((1, 0), dtype=np.int32))
+    grid = geo.grid((1, 0))
     props_sys = dict(props, split_ratio=2.0, min_child_weight=0.2)
     arrays = {}
     count, capacity = 500, 560
@@ -417,14 +458,16 @@ def make_lib(ref, out_dir):
             arrays[f"{op}_{k}"] = v
     for k, v in base.items():
         arrays[f"start_{k}"] = v
-    lib_save(out_dir, "lib_system.npz", x_edges=xe, y_edges=ye, periodic=grid["periodic"],
+    lib_save(out_dir, f"lib_system{geo.suffix}.npz", x_edges=xe, y_edges=ye,
+             periodic=grid["periodic"], **geo.extra(),
              count=count, split_ratio=props_sys["split_ratio"],
              min_child_weight=props_sys["min_child_weight"], **arrays)
 
 
-def generator_fields(nx: int, ny: int, x_edges, y_edges) -> dict:
+def generator_fields(nx: int, ny: int, x_edges, y_edges, geo=None) -> dict:
     """Fields of the ParticleGenerator cases, in the Field's stored order
-    (dim 0 fastest over the ghosted extent of the centering)."""
+    (dim 0 fastest over the ghosted extent of the centering), at the cell
+    centres and faces of the uniform grid or of `geo`'s stored one."""
     dx = (x_edges[-1] - x_edges[0]) / nx
     dy = (y_edges[-1] - y_edges[0]) / ny
 
@@ -432,8 +475,11 @@ def generator_fields(nx: int, ny: int, x_edges, y_edges) -> dict:
         k = np.arange(n + 4 + int(face)) - 2.0
         return x0 + (k if face else k + 0.5) * d
 
-    xc, yc = coords(nx, x_edges[0], dx, False), coords(ny, y_edges[0], dy, False)
-    xf, yf = coords(nx, x_edges[0], dx, True), coords(ny, y_edges[0], dy, True)
+    if geo is not None and geo.stored:
+        (xc, yc), xf, yf = geo.centres(), geo.xf, geo.yf
+    else:
+        xc, yc = coords(nx, x_edges[0], dx, False), coords(ny, y_edges[0], dy, False)
+        xf, yf = coords(nx, x_edges[0], dx, True), coords(ny, y_edges[0], dy, True)
     scalar_cell = (np.cos(2.0 * xc)[None, :] * np.exp(-yc[:, None] ** 2)).ravel()
     vec_face = np.stack([np.sin(3.0 * xf)[None, :] + 0.0 * yf[:, None],
                          np.tanh(yf[:, None] / 0.4) * np.cos(xf)[None, :],
@@ -486,15 +532,15 @@ CANDIDATE_CASES = (
 )
 
 
-def make_generator(ref, out_dir):
+def make_generator(ref, out_dir, stored=False):
     """ParticleGenerator cases from the reference's own templates."""
-    rng = np.random.default_rng(1618)
+    rng = np.random.default_rng(1618 + (1 if stored else 0))
     nx, ny = 24, 40
-    xe = np.linspace(-1.3, 2.1, nx + 1)
-    ye = np.linspace(-2.0, 2.0, ny + 1)
-    grid = dict(x_edges=xe, y_edges=ye, periodic=np.array((1, 0), dtype=np.int32))
+    geo = LibGeometry(nx, ny, (-1.3, 2.1), (-2.0, 2.0), stored)
+    xe, ye = geo.xe, geo.ye
+    grid = geo.grid((1, 0))
     props = dict(rest_mass=1.0, charge=1.0, speed_of_light=1.0, energy_scale=1.0)
-    fields = generator_fields(nx, ny, xe, ye)
+    fields = generator_fields(nx, ny, xe, ye, geo)
     arrays = {f"field_{name}": values for name, (values, _) in fields.items()}
     for name, (_, cent) in fields.items():
         arrays[f"centering_{name}"] = np.array(cent, dtype=np.int32)
@@ -542,18 +588,22 @@ def make_generator(ref, out_dir):
         arrays[f"cand_{name}_field"] = np.array(field if field is not None else "")
         arrays[f"cand_{name}_region"] = np.array(region if region is not None else [np.nan] * 4)
         arrays[f"cand_{name}_predicate"] = np.array(pred, dtype=np.float64)
-    lib_save(out_dir, "lib_generator.npz", x_edges=xe, y_edges=ye, periodic=grid["periodic"],
+    lib_save(out_dir, f"lib_generator{geo.suffix}.npz", x_edges=xe, y_edges=ye,
+             periodic=grid["periodic"], **geo.extra(),
              cases=np.array([c[0] for c in GENERATOR_CASES]),
              candidate_cases=np.array([c[0] for c in CANDIDATE_CASES]), **arrays)
 
 
-def coefficient_inputs(nx: int, ny: int, x_edges, y_edges, variant: int):
+def coefficient_inputs(nx: int, ny: int, x_edges, y_edges, variant: int, centres=None):
     """Cell-centred B and V over the ghosted cells (x fastest), analytic
-    everywhere (the caller's ghost values), plus turbulence fields."""
+    everywhere (the caller's ghost values), plus turbulence fields; at the
+    uniform grid's centres or the given (xc, yc) of a stored one."""
     dx = (x_edges[-1] - x_edges[0]) / nx
     dy = (y_edges[-1] - y_edges[0]) / ny
     xc = x_edges[0] + (np.arange(nx + 4) - 1.5) * dx
     yc = y_edges[0] + (np.arange(ny + 4) - 1.5) * dy
+    if centres is not None:
+        xc, yc = centres
     X, Y = np.meshgrid(xc, yc)
     bz = 0.3 + 0.1 * variant * np.cos(X + Y)
     b = np.stack([np.tanh(Y / 0.5) + 0.05 * np.sin(3 * X), 0.2 * np.sin(X) + 0.1 * variant,
@@ -580,15 +630,15 @@ COEFFICIENT_CASES = (
 )
 
 
-def make_parker_coefficients(ref, out_dir):
+def make_parker_coefficients(ref, out_dir, stored=False):
     """The reference's Parker coefficient precompute and packed basis."""
     nx, ny = 20, 28
-    xe = np.linspace(-1.3, 2.1, nx + 1)
-    ye = np.linspace(-2.0, 2.0, ny + 1)
+    geo = LibGeometry(nx, ny, (-1.3, 2.1), (-2.0, 2.0), stored)
+    xe, ye = geo.xe, geo.ye
     arrays = {}
     for name, periodic, variant, turb, params, charge, floor, ghost in COEFFICIENT_CASES:
-        grid = dict(x_edges=xe, y_edges=ye, periodic=np.array(periodic, dtype=np.int32))
-        b, v, fields = coefficient_inputs(nx, ny, xe, ye, variant)
+        grid = geo.grid(periodic)
+        b, v, fields = coefficient_inputs(nx, ny, xe, ye, variant, geo.centres())
         constant = (0.35, 0.9, 1.4, -1.0 if variant == 0 else 1.1)
         props = dict(rest_mass=1.0, charge=charge, speed_of_light=1.0)
         packed = ref.lib_parker_coefficients(
@@ -606,6 +656,10 @@ def make_parker_coefficients(ref, out_dir):
              params.get("minimum_b", 0.0), params.get("minimum_vsw", 0.0),
              params.get("minimum_sigma2", 0.0), floor, ghost, charge])
         arrays[f"{name}_packed"] = packed
+    if stored:
+        lib_save(out_dir, "lib_parker_coefficients_stored.npz", x_edges=xe, y_edges=ye,
+                 **geo.extra(), cases=np.array([c[0] for c in COEFFICIENT_CASES]), **arrays)
+        return
     # failures: the reference's messages
     grid = dict(x_edges=xe, y_edges=ye, periodic=np.array((1, 0), dtype=np.int32))
     errors = []
@@ -657,16 +711,16 @@ FOCUS_COEFFICIENT_CASES = (
 )
 
 
-def make_focus_coefficients(ref, out_dir):
+def make_focus_coefficients(ref, out_dir, stored=False):
     """The reference's focused coefficient precompute and packed basis."""
     nx, ny = 20, 28
-    xe = np.linspace(-1.3, 2.1, nx + 1)
-    ye = np.linspace(-2.0, 2.0, ny + 1)
+    geo = LibGeometry(nx, ny, (-1.3, 2.1), (-2.0, 2.0), stored)
+    xe, ye = geo.xe, geo.ye
     arrays = {}
     for (name, periodic, variant, turb, params, charge, floor, ghost,
          with_dvdt) in FOCUS_COEFFICIENT_CASES:
-        grid = dict(x_edges=xe, y_edges=ye, periodic=np.array(periodic, dtype=np.int32))
-        b, v, fields = coefficient_inputs(nx, ny, xe, ye, variant)
+        grid = geo.grid(periodic)
+        b, v, fields = coefficient_inputs(nx, ny, xe, ye, variant, geo.centres())
         dvdt = None
         if with_dvdt:
             dvdt = np.stack([np.cos(v[:, 0]), 0.3 * v[:, 1], 0.1 + 0.0 * v[:, 2]], axis=-1)
@@ -688,8 +742,18 @@ def make_focus_coefficients(ref, out_dir):
              params.get("minimum_b", 0.0), params.get("minimum_vsw", 0.0),
              params.get("minimum_sigma2", 0.0), floor, ghost, charge])
         arrays[f"{name}_packed"] = packed
-    lib_save(out_dir, "lib_focus_coefficients.npz", x_edges=xe, y_edges=ye,
-             cases=np.array([c[0] for c in FOCUS_COEFFICIENT_CASES]), **arrays)
+    lib_save(out_dir, f"lib_focus_coefficients{geo.suffix}.npz", x_edges=xe, y_edges=ye,
+             **geo.extra(), cases=np.array([c[0] for c in FOCUS_COEFFICIENT_CASES]), **arrays)
+
+
+def make_stored(ref, out_dir):
+    """The library cases again on stored (explicit, stretched) grids:
+    lib_parker_stored_*, lib_focus_stored_*, lib_system_stored,
+    lib_generator_stored, lib_*_coefficients_stored."""
+    make_lib(ref, out_dir, stored=True)
+    make_generator(ref, out_dir, stored=True)
+    make_parker_coefficients(ref, out_dir, stored=True)
+    make_focus_coefficients(ref, out_dir, stored=True)
 
 
 def main() -> None:
@@ -705,10 +769,14 @@ def main() -> None:
         make_parker_coefficients(ref, out_dir)
         make_focus_coefficients(ref, out_dir)
         return
+    if sys.argv[1:] == ["stored"]:
+        make_stored(ref, out_dir)
+        return
     make_lib(ref, out_dir)
     make_generator(ref, out_dir)
     make_parker_coefficients(ref, out_dir)
     make_focus_coefficients(ref, out_dir)
+    make_stored(ref, out_dir)
     if sys.argv[1:] == ["lib"]:
         return
     make_c1(ref, out_dir)

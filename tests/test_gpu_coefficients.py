@@ -14,6 +14,9 @@ ghost-fill modes, open and periodic axes), compiled on the Kokkos-API shim
 * The diffusion-tensor divergence bases are three-point differences of those
   kappas: 1e-12 of each component's largest magnitude.
 * The reference's abort messages for a magnetic null and a negative Lc.
+* lib_*_coefficients_stored.npz: the same configurations on a
+  StoredCoordinateGrid with stretched faces (three-point differences on the
+  stored coordinates): the same bars.
 
 tests/golden/lib_focus_coefficients.npz does the same for the focused
 builder (include/FocusCoefficient.hpp:852-993) and the focused packed basis:
@@ -27,21 +30,34 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-from conftest import load_golden
+from conftest import lib_grid, load_golden
 
 pytestmark = pytest.mark.gpu
 
-CASES = [str(c) for c in load_golden("lib_parker_coefficients.npz")["cases"]]
-FOCUS_CASES = [str(c) for c in load_golden("lib_focus_coefficients.npz")["cases"]]
+# the uniform (analytic) grid's files and the stored (explicit, stretched
+# faces) grid's files hold the same configurations
+PARKER_FILES = ("lib_parker_coefficients.npz", "lib_parker_coefficients_stored.npz")
+FOCUS_FILES = ("lib_focus_coefficients.npz", "lib_focus_coefficients_stored.npz")
+_LOADED = {}
+
+
+def _golden(name):
+    if name not in _LOADED:
+        _LOADED[name] = load_golden(name)
+    return _LOADED[name]
+
+
+CASES = [(f, str(c)) for f in PARKER_FILES for c in _golden(f)["cases"]]
+FOCUS_CASES = [(f, str(c)) for f in FOCUS_FILES for c in _golden(f)["cases"]]
 
 
 @pytest.fixture(scope="module")
 def coef():
-    return load_golden("lib_parker_coefficients.npz")
+    return _golden("lib_parker_coefficients.npz")
 
 
 def _inputs(ctx, data, name):
-    grid = ctx.grid(data["x_edges"], data["y_edges"], data[f"{name}_periodic"])
+    grid = lib_grid(ctx, data, data[f"{name}_periodic"])
     s2, l2d, lslab, lc = data[f"{name}_turbulence"]
     fields = data[f"{name}_fields"]
     if fields.size:
@@ -59,8 +75,9 @@ def _inputs(ctx, data, name):
     return grid, turbulence, params, float(charge)
 
 
-@pytest.mark.parametrize("name", CASES)
-def test_packed_basis_matches_reference(ctx, coef, name):
+@pytest.mark.parametrize("file,name", CASES)
+def test_packed_basis_matches_reference(ctx, file, name):
+    coef = _golden(file)
     grid, turbulence, params, charge = _inputs(ctx, coef, name)
     got = ctx.parker_coefficients(grid, coef[f"{name}_b"], coef[f"{name}_v"], turbulence,
                                   params, charge=charge)
@@ -129,7 +146,7 @@ def test_failures_report_the_reference_messages(ctx, kpt, coef):
 
 @pytest.fixture(scope="module")
 def fcoef():
-    return load_golden("lib_focus_coefficients.npz")
+    return _golden("lib_focus_coefficients.npz")
 
 
 def _focus_inputs(ctx, data, name):
@@ -139,8 +156,9 @@ def _focus_inputs(ctx, data, name):
     return grid, turbulence, params, charge, (dvdt if dvdt.size else None), floor
 
 
-@pytest.mark.parametrize("name", FOCUS_CASES)
-def test_focus_packed_basis_matches_reference(ctx, fcoef, name):
+@pytest.mark.parametrize("file,name", FOCUS_CASES)
+def test_focus_packed_basis_matches_reference(ctx, file, name):
+    fcoef = _golden(file)
     grid, turbulence, params, charge, dvdt, floor = _focus_inputs(ctx, fcoef, name)
     # the Parker floor slot carries the builder's floor for the focused cases
     params.minimum_magnetic_field_squared_for_drift = 0.0

@@ -106,11 +106,15 @@ def _compare_state(got, want, prefix, data, rtol=1e-10):
 @pytest.mark.parametrize("kind,case", [("parker", "readme_periodic"), ("parker", "ratio_open"),
                                        ("parker", "readme_deterministic"),
                                        ("focus", "readme_periodic"),
-                                       ("focus", "ratio_open_mumax"), ("focus", "deterministic")])
+                                       ("focus", "ratio_open_mumax"), ("focus", "deterministic"),
+                                       ("parker", "stored_ratio_open"),
+                                       ("focus", "stored_ratio_open_mumax")])
 def test_cxx_solver_steps_match_reference(tmp_path, kind, case):
     data = load_golden(f"lib_{kind}_{case}.npz")
     keys = ["x_edges", "y_edges", "count", "basis", "constant_ratio", "courant", "seed",
             "first_step", "steps", "stochastic"]
+    if "x_faces" in data:  # a StoredCoordinateGrid2D
+        keys += ["x_faces", "y_faces"]
     if kind == "focus":
         keys += ["max_mu", "spectral_index", "h0"]
     got = _run(tmp_path, kind, _inputs(data, keys))
@@ -129,9 +133,13 @@ def test_cxx_solver_steps_match_reference(tmp_path, kind, case):
         assert "Courant" in _text(got["error_courant"])
 
 
-def test_cxx_particle_system_lifecycle_matches_reference(tmp_path):
-    data = load_golden("lib_system.npz")
-    rec = _inputs(data, ["x_edges", "y_edges", "count", "split_ratio", "min_child_weight"])
+@pytest.mark.parametrize("name", ["lib_system.npz", "lib_system_stored.npz"])
+def test_cxx_particle_system_lifecycle_matches_reference(tmp_path, name):
+    data = load_golden(name)
+    keys = ["x_edges", "y_edges", "count", "split_ratio", "min_child_weight"]
+    if "x_faces" in data:
+        keys += ["x_faces", "y_faces"]
+    rec = _inputs(data, keys)
     got = _run(tmp_path, "system", rec)
     for op in ("boundary", "sort", "compact", "split", "capture"):
         assert int(got[f"{op}_count"][0]) == int(data[f"{op}_count"]), op

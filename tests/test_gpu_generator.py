@@ -21,7 +21,7 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-from conftest import load_golden
+from conftest import lib_grid, load_golden
 
 pytestmark = pytest.mark.gpu
 
@@ -29,13 +29,16 @@ FIELDS = ("x", "y", "prev_x", "prev_y", "prevstep_x", "prevstep_y", "p", "mu", "
           "status", "level", "key", "id")
 
 
-@pytest.fixture(scope="module")
-def gen():
-    return load_golden("lib_generator.npz")
+FILES = ("lib_generator.npz", "lib_generator_stored.npz")
+
+
+@pytest.fixture(scope="module", params=FILES)
+def gen(request):
+    return load_golden(request.param)
 
 
 def _setup(ctx, data):
-    grid = ctx.grid(data["x_edges"], data["y_edges"], data["periodic"])
+    grid = lib_grid(ctx, data)
     fields = {}
     for name in ("scalar_cell", "vec_face", "mixed"):
         fields[name] = ctx.lib_field(grid, data[f"field_{name}"],

@@ -18,19 +18,23 @@ pool (tests/golden/make_golden.py).
   normals through their random pool: the same bars.
 * ParticleSystem: boundary conditions, sort_by_key, compact, energy split and
   capture_previous_positions bit for bit.
+* Stored grids (lib_*_stored*.npz): the solver and lifecycle cases again on
+  a StoredCoordinateGrid with stretched x and y faces (cell search by
+  bisection, per-cell widths in the limiters): the same bars.
 """
 from __future__ import annotations
 
 import numpy as np
 import pytest
 
-from conftest import load_golden
+from conftest import lib_grid, load_golden
 
 pytestmark = pytest.mark.gpu
 
 FIELDS = ("x", "y", "prev_x", "prev_y", "prevstep_x", "prevstep_y", "p", "mu", "w", "e0",
           "status", "level", "key", "id")
-PARKER_CASES = ("readme_periodic", "ratio_open", "readme_deterministic")
+PARKER_CASES = ("readme_periodic", "ratio_open", "readme_deterministic",
+                "stored_readme_periodic", "stored_ratio_open", "stored_readme_deterministic")
 
 
 def _state(data, prefix):
@@ -50,7 +54,7 @@ def _compare(got, want, x_width, y_width, rtol=1e-10):
 
 
 def _setup(ctx, data):
-    grid = ctx.grid(data["x_edges"], data["y_edges"], data["periodic"])
+    grid = lib_grid(ctx, data)
     start = _state(data, "start")
     count = int(data["count"])
     system = ctx.system(count, start["x"].size)
@@ -131,11 +135,12 @@ def test_no_active_particle_is_an_error(ctx, kpt):
         h.close()
 
 
-FOCUS_CASES = ("readme_periodic", "ratio_open_mumax", "deterministic")
+FOCUS_CASES = ("readme_periodic", "ratio_open_mumax", "deterministic",
+               "stored_readme_periodic", "stored_ratio_open_mumax", "stored_deterministic")
 
 
 def _focus_setup(ctx, data):
-    grid = ctx.grid(data["x_edges"], data["y_edges"], data["periodic"])
+    grid = lib_grid(ctx, data)
     start = _state(data, "start")
     system = ctx.system(int(data["count"]), start["x"].size)
     system.upload(start)
@@ -190,10 +195,11 @@ def test_focus_graph_steps_and_limits(ctx, kpt):
         h.close()
 
 
+@pytest.mark.parametrize("name", ["lib_system.npz", "lib_system_stored.npz"])
 @pytest.mark.parametrize("op", ["boundary", "sort", "compact", "split", "capture"])
-def test_particle_system_lifecycle_matches_reference(ctx, op):
-    data = load_golden("lib_system.npz")
-    grid = ctx.grid(data["x_edges"], data["y_edges"], data["periodic"])
+def test_particle_system_lifecycle_matches_reference(ctx, op, name):
+    data = load_golden(name)
+    grid = lib_grid(ctx, data)
     start = _state(data, "start")
     system = ctx.system(int(data["count"]), start["x"].size,
                         split_ratio=float(data["split_ratio"]),
