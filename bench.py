@@ -809,10 +809,11 @@ def run_kernel_sweep(args):
 
 
 def run_library(args):
-    """The header library's lockstep solvers (ParkerSolver, FocusSolver; FP64)
-    on a uniform 1024x2048 periodic grid with smooth synthetic coefficient
-    fields: N particles, K steps replayed from one CUDA graph; particle-steps
-    = N x K (every particle advances once per step)."""
+    """The header library's lockstep solvers (ParkerSolver, FocusSolver; FP64,
+    and the mixed step: FP32 basis, terms and noise with FP64 state) on a
+    uniform 1024x2048 periodic grid with smooth synthetic coefficient fields:
+    N particles, K steps replayed from one CUDA graph; particle-steps = N x K
+    (every particle advances once per step)."""
     import torch
     kpt = importlib.import_module("kokkos-particletransport_gb300")
     ctx = kpt.Context(DEVICE)
@@ -834,14 +835,17 @@ def run_library(args):
     state["mu"] = rng.uniform(-1.0, 1.0, n)
     state["w"] = np.ones(n)
     out = {"particles": n, "grid": f"{NX}x{NY}", "steps": args.library_steps}
-    for label in ("parker", "focus"):
-        if label == "parker":
+    for label in ("parker", "focus", "parker_mixed", "focus_mixed"):
+        if label.startswith("parker"):
             basis = fields.library_parker_basis(NX, NY, xe, ye, True)
             solver = ctx.parker_solver(grid, basis)
         else:
             basis = fields.library_focus_basis(NX, NY, xe, ye)
             solver = ctx.focus_solver(grid, basis)
         del basis
+        # the mixed step: FP32 basis, terms and noise, FP64 positions/momenta/dt
+        solver.set_precision(kpt.PRECISION_MIXED if label.endswith("mixed")
+                             else kpt.PRECISION_F64)
         system = ctx.system(n, n)
         system.upload(state)
         solver.advance_stochastic_steps(system, SEED, 0, 2)  # warm-up, records nothing
@@ -859,6 +863,9 @@ def run_library(args):
                       "active_after": active}
         solver.close()
         system.close()
+    for label in ("parker", "focus"):
+        out[f"{label}_mixed"]["speedup_over_f64"] = (out[f"{label}_mixed"]["value"] /
+                                                     out[label]["value"])
     out["generator"] = run_generator(kpt, ctx, grid, xe, ye, n, stream)
     out["coefficients"] = run_coefficients(ctx, grid, xe, ye)
     grid.close()

@@ -558,6 +558,13 @@ int kpt_parker_solver_destroy(kpt_parker_solver* solver);
 int kpt_parker_solver_set_basis(kpt_parker_solver* solver, const double* basis,
                                 int constant_ratio);
 int kpt_parker_solver_set_courant(kpt_parker_solver* solver, double courant);
+/* Arithmetic of the steps (no counterpart in the reference, whose solvers
+ * are FP64): KPT_PRECISION_F64 (default) follows the reference's FP64
+ * arithmetic; KPT_PRECISION_MIXED samples an FP32 copy of the packed basis
+ * and forms the terms, the local dt bounds and the Box-Muller noise in FP32,
+ * keeping positions, momenta, the global dt and the boundary decisions in
+ * FP64 (trajectories within a stated tolerance of the FP64 steps). */
+int kpt_parker_solver_set_precision(kpt_parker_solver* solver, int precision);
 /* compute_adaptive_time_step (ParkerSolver.hpp:209-222): courant x the
  * minimum local bound over active particles. */
 int kpt_parker_compute_time_step(kpt_context* ctx, kpt_parker_solver* solver,
@@ -604,6 +611,9 @@ int kpt_focus_solver_destroy(kpt_focus_solver* solver);
 int kpt_focus_solver_set_basis(kpt_focus_solver* solver, const double* basis,
                                int constant_ratio);
 int kpt_focus_solver_set_courant(kpt_focus_solver* solver, double courant);
+/* As kpt_parker_solver_set_precision; the mixed step also evaluates the
+ * slab-QLT closure of the Picard pitch-angle update in FP32. */
+int kpt_focus_solver_set_precision(kpt_focus_solver* solver, int precision);
 /* set_maximum_pitch_angle_cosine (FocusSolver.hpp:219-226): 0 < value <= 1. */
 int kpt_focus_solver_set_maximum_mu(kpt_focus_solver* solver, double maximum_mu);
 /* compute_adaptive_time_step (FocusSolver.hpp:240-246). */

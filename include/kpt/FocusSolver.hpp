@@ -144,7 +144,15 @@ public:
         return dt;
     }
 
+    // Extension: the arithmetic of the steps, KPT_PRECISION_F64 (the
+    // reference's, the default) or KPT_PRECISION_MIXED (FP32 basis, terms and
+    // noise with FP64 positions, momenta and dt; within a stated tolerance of
+    // the FP64 steps).
+    void set_precision(int precision) { precision_ = precision; }
+    int precision() const { return precision_; }
+
 private:
+    int precision_{KPT_PRECISION_F64};
     bool use_packed_{true};
     std::shared_ptr<kpt_focus_solver> solver_;
 
@@ -157,6 +165,7 @@ private:
             throw std::runtime_error("FocusTransportSolver: the solver has no particle system.");
         }
         check(kpt_focus_solver_set_courant(solver_.get(), courant_scale));
+        check(kpt_focus_solver_set_precision(solver_.get(), precision_));
         check(kpt_focus_solver_set_maximum_mu(solver_.get(), maximum_pitch_angle_cosine));
     }
 };

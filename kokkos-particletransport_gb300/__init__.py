@@ -286,6 +286,7 @@ def load_library() -> ctypes.CDLL:
         "kpt_parker_solver_destroy": (i32, [vp]),
         "kpt_parker_solver_set_basis": (i32, [vp, vp, i32]),
         "kpt_parker_solver_set_courant": (i32, [vp, dbl]),
+        "kpt_parker_solver_set_precision": (i32, [vp, i32]),
         "kpt_parker_compute_time_step": (i32, [vp, vp, vp, vp]),
         "kpt_parker_advance_stochastic": (i32, [vp, vp, vp, u64, u32, vp]),
         "kpt_parker_advance_deterministic": (i32, [vp, vp, vp, vp]),
@@ -307,6 +308,7 @@ def load_library() -> ctypes.CDLL:
         "kpt_focus_solver_destroy": (i32, [vp]),
         "kpt_focus_solver_set_basis": (i32, [vp, vp, i32]),
         "kpt_focus_solver_set_courant": (i32, [vp, dbl]),
+        "kpt_focus_solver_set_precision": (i32, [vp, i32]),
         "kpt_focus_solver_set_maximum_mu": (i32, [vp, dbl]),
         "kpt_focus_compute_time_step": (i32, [vp, vp, vp, vp]),
         "kpt_focus_advance_stochastic": (i32, [vp, vp, vp, u64, u32, vp]),
@@ -1067,6 +1069,11 @@ class ParkerSolver(_Handle):
     def set_courant(self, courant: float) -> None:
         _check(self.ctx.lib.kpt_parker_solver_set_courant(self.handle, float(courant)))
 
+    def set_precision(self, precision: int) -> None:
+        """PRECISION_F64 (the reference's arithmetic) or PRECISION_MIXED (FP32
+        basis, terms and noise; FP64 positions, momenta and dt)."""
+        _check(self.ctx.lib.kpt_parker_solver_set_precision(self.handle, int(precision)))
+
     def set_basis(self, basis: np.ndarray, constant_ratio: bool = False) -> None:
         basis = np.ascontiguousarray(basis, dtype=np.float64)
         _check(self.ctx.lib.kpt_parker_solver_set_basis(self.handle, _ptr(basis),
@@ -1181,6 +1188,11 @@ class FocusSolver(_Handle):
 
     def set_courant(self, courant: float) -> None:
         _check(self.ctx.lib.kpt_focus_solver_set_courant(self.handle, float(courant)))
+
+    def set_precision(self, precision: int) -> None:
+        """PRECISION_F64 (the reference's arithmetic) or PRECISION_MIXED (FP32
+        basis, terms, closure and noise; FP64 positions, momenta and dt)."""
+        _check(self.ctx.lib.kpt_focus_solver_set_precision(self.handle, int(precision)))
 
     def set_maximum_mu(self, maximum_mu: float) -> None:
         _check(self.ctx.lib.kpt_focus_solver_set_maximum_mu(self.handle, float(maximum_mu)))

@@ -2053,6 +2053,9 @@ struct kpt_focus_solver {
     double max_mu = 1.0;
     kpt_scattering_parameters scattering{};
     DeviceBuffer terms, scalars, dt_history;
+    int precision = KPT_PRECISION_F64;
+    DeviceBuffer basis_f32;        // the mixed step's FP32 copy of the basis
+    bool basis_f32_valid = false;  // cleared whenever the FP64 basis changes
 };
 
 struct kpt_parker_solver {
@@ -2063,6 +2066,9 @@ struct kpt_parker_solver {
     double* basis = nullptr;
     int constant_ratio = 0;
     double courant = 0.3;
+    int precision = KPT_PRECISION_F64;
+    DeviceBuffer basis_f32;        // the mixed step's FP32 copy of the basis
+    bool basis_f32_valid = false;  // cleared whenever the FP64 basis changes
     DeviceBuffer terms;
     // min bits (u64), dt (f64), error (i32 + pad), error index (u64)
     DeviceBuffer scalars;
@@ -2501,6 +2507,7 @@ int kpt_parker_solver_destroy(kpt_parker_solver* s) {
     if (s == nullptr) return KPT_OK;
     cudaSetDevice(s->device);
     cudaFree(s->basis);
+    s->basis_f32.release();
     s->terms.release();
     s->scalars.release();
     s->dt_history.release();
@@ -2514,6 +2521,16 @@ int kpt_parker_solver_set_basis(kpt_parker_solver* s, const double* basis, int c
     KPT_CUDA(cudaMemcpy(s->basis, basis, s->points * kpt::kLibBasis * sizeof(double),
                         cudaMemcpyHostToDevice));
     s->constant_ratio = constant_ratio != 0 ? 1 : 0;
+    s->basis_f32_valid = false;
+    return KPT_OK;
+}
+
+int kpt_parker_solver_set_precision(kpt_parker_solver* s, int precision) {
+    KPT_REQUIRE(s != nullptr, "kpt_parker_solver_set_precision: NULL handle");
+    KPT_REQUIRE(precision == KPT_PRECISION_F64 || precision == KPT_PRECISION_MIXED,
+                "kpt_parker_solver_set_precision: precision must be KPT_PRECISION_F64 or "
+                "KPT_PRECISION_MIXED");
+    s->precision = precision;
     return KPT_OK;
 }
 
@@ -2547,6 +2564,17 @@ int parker_launch(kpt_context* ctx, kpt_parker_solver* s, kpt_system* sys, int a
     L = kpt::LibParkerLaunch{};
     L.grid = s->grid;
     L.basis = s->basis;
+    if (s->precision == KPT_PRECISION_MIXED) {
+        if (!s->basis_f32_valid) {
+            KPT_CUDA(s->basis_f32.reserve(s->points * kpt::kLibBasisStrideF32 * sizeof(float)));
+            KPT_CUDA(kpt::lib_basis_to_f32(s->basis, kpt::kLibBasisStride,
+                                           s->basis_f32.as<float>(), kpt::kLibBasisStrideF32,
+                                           kpt::kLibBasis, s->points, ctx->stream));
+            s->basis_f32_valid = true;
+        }
+        L.basis_f32 = s->basis_f32.as<float>();
+        L.mixed = 1;
+    }
     L.constant_ratio = s->constant_ratio;
     L.sys = sys->a;
     L.count = sys->count;
@@ -2728,6 +2756,18 @@ int focus_launch(kpt_focus_solver* s, kpt_system* sys, int advance, int stochast
     L = kpt::LibFocusLaunch{};
     L.grid = s->grid;
     L.basis = s->basis;
+    if (s->precision == KPT_PRECISION_MIXED) {
+        if (!s->basis_f32_valid) {
+            KPT_CUDA(s->basis_f32.reserve(s->points * kpt::kFocusBasisStrideF32 *
+                                          sizeof(float)));
+            KPT_CUDA(kpt::lib_basis_to_f32(s->basis, kpt::kFocusBasisStride,
+                                           s->basis_f32.as<float>(), kpt::kFocusBasisStrideF32,
+                                           kpt::kFocusBasis, s->points, s->ctx->stream));
+            s->basis_f32_valid = true;
+        }
+        L.basis_f32 = s->basis_f32.as<float>();
+        L.mixed = 1;
+    }
     L.constant_ratio = s->constant_ratio;
     L.sys = sys->a;
     L.count = sys->count;
@@ -2838,6 +2878,7 @@ int kpt_focus_solver_destroy(kpt_focus_solver* s) {
     if (s == nullptr) return KPT_OK;
     cudaSetDevice(s->device);
     cudaFree(s->basis);
+    s->basis_f32.release();
     s->terms.release();
     s->scalars.release();
     s->dt_history.release();
@@ -2853,6 +2894,16 @@ int kpt_focus_solver_set_basis(kpt_focus_solver* s, const double* basis, int con
                           kpt::kFocusBasis * sizeof(double), kpt::kFocusBasis * sizeof(double),
                           s->points, cudaMemcpyHostToDevice));
     s->constant_ratio = constant_ratio != 0 ? 1 : 0;
+    s->basis_f32_valid = false;
+    return KPT_OK;
+}
+
+int kpt_focus_solver_set_precision(kpt_focus_solver* s, int precision) {
+    KPT_REQUIRE(s != nullptr, "kpt_focus_solver_set_precision: NULL handle");
+    KPT_REQUIRE(precision == KPT_PRECISION_F64 || precision == KPT_PRECISION_MIXED,
+                "kpt_focus_solver_set_precision: precision must be KPT_PRECISION_F64 or "
+                "KPT_PRECISION_MIXED");
+    s->precision = precision;
     return KPT_OK;
 }
 

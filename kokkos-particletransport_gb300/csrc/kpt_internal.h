@@ -270,11 +270,14 @@ struct SystemArrays {
 // B(3) V(3) drift curl(3) primary(3) secondary(3) kappa_par kappa_perp divV.
 constexpr int kLibBasis = 18;
 constexpr int kLibBasisStride = 18;
+constexpr int kLibBasisStrideF32 = 20;  // FP32 copy: rows of five 16-byte chunks
 constexpr int kLibTermCount = 9;
 
 struct LibParkerLaunch {
     LibGrid grid;
-    const double* basis;  // ghosted points x kLibBasisStride
+    const double* basis;      // ghosted points x kLibBasisStride
+    const float* basis_f32;   // mixed step: ghosted points x kLibBasisStrideF32
+    int mixed;                // 1: FP32 basis, terms and noise; FP64 positions and momenta
     int constant_ratio;
     SystemArrays sys;
     uint64_t count, capacity;
@@ -297,6 +300,9 @@ struct LibParkerLaunch {
     unsigned long long* error_index;
 };
 cudaError_t lib_parker_step(const LibParkerLaunch& launch, cudaStream_t stream);
+// FP32 copy of a packed basis (rows rounded, padded with zeros to dst_stride).
+cudaError_t lib_basis_to_f32(const double* src, int src_stride, float* dst, int dst_stride,
+                             int comps, uint64_t points, cudaStream_t stream);
 
 // Packed focused basis (FocusSolver.hpp:106-136) for VecDim 3: B(3) b(3)
 // V(3) gradient drift(3) curvature drift(3) perpendicular diffusion
@@ -304,11 +310,14 @@ cudaError_t lib_parker_step(const LibParkerLaunch& launch, cudaStream_t stream);
 // sigma^2 Lc; rows padded to 28 doubles (16-byte aligned).
 constexpr int kFocusBasis = 27;
 constexpr int kFocusBasisStride = 28;
+constexpr int kFocusBasisStrideF32 = 28;  // FP32 copy: rows of seven 16-byte chunks
 constexpr int kFocusTermCount = 18;
 
 struct LibFocusLaunch {
     LibGrid grid;
-    const double* basis;  // ghosted points x kFocusBasisStride
+    const double* basis;      // ghosted points x kFocusBasisStride
+    const float* basis_f32;   // mixed step: ghosted points x kFocusBasisStrideF32
+    int mixed;                // 1: FP32 basis, terms, closure and noise; FP64 state
     int constant_ratio;
     SystemArrays sys;
     uint64_t count, capacity;

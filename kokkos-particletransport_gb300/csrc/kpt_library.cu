@@ -191,23 +191,80 @@ __device__ __forceinline__ void lib_sample(const LibGrid& g, const double* __res
     }
 }
 
+// The mixed-precision library step samples an FP32 copy of the packed basis
+// (rows padded to whole 16-byte chunks) with the same stencil and weights
+// (formed in FP64 from the FP64 positions), accumulated in FP32.
+template <int C, int STRIDE>
+__device__ __forceinline__ void lib_sample(const LibGrid& g, const float* __restrict__ basis,
+                                           double x, double y, float (&out)[C]) {
+    static_assert(STRIDE % 4 == 0 && STRIDE >= C, "FP32 rows hold whole 16-byte chunks");
+    int lo[2], hi[2];
+    double w[2];
+    lib_stencil(g.axis[0], x, lo[0], hi[0], w[0]);
+    lib_stencil(g.axis[1], y, lo[1], hi[1], w[1]);
+#pragma unroll
+    for (int c = 0; c < C; ++c) out[c] = 0.0f;
+#pragma unroll
+    for (int corner = 0; corner < 4; ++corner) {
+        const bool ux = (corner & 1) != 0;
+        const bool uy = (corner & 2) != 0;
+        const float weight = static_cast<float>((ux ? w[0] : 1.0 - w[0]) *
+                                                (uy ? w[1] : 1.0 - w[1]));
+        const int i = (ux ? hi[0] : lo[0]) + 2;
+        const int j = (uy ? hi[1] : lo[1]) + 2;
+        const float4* row =
+            reinterpret_cast<const float4*>(basis + (static_cast<size_t>(j) * g.ex + i) * STRIDE);
+#pragma unroll
+        for (int k = 0; k < (C + 3) / 4; ++k) {
+            const float4 v = __ldg(row + k);
+            const float e[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                if (4 * k + m < C) out[4 * k + m] = fmaf(weight, e[m], out[4 * k + m]);
+            }
+        }
+    }
+}
+
+// Math of the two library precisions.
+template <typename T>
+struct LibMath;
+template <>
+struct LibMath<double> {
+    static __device__ __forceinline__ double sqrt(double v) { return ::sqrt(v); }
+    static __device__ __forceinline__ double cbrt(double v) { return ::cbrt(v); }
+    static __device__ __forceinline__ double pow(double a, double b) { return ::pow(a, b); }
+    static __device__ __forceinline__ double abs(double v) { return fabs(v); }
+};
+template <>
+struct LibMath<float> {
+    static __device__ __forceinline__ float sqrt(float v) { return sqrtf(v); }
+    static __device__ __forceinline__ float cbrt(float v) { return cbrtf(v); }
+    static __device__ __forceinline__ float pow(float a, float b) { return powf(a, b); }
+    static __device__ __forceinline__ float abs(float v) { return fabsf(v); }
+};
+
 // The momentum scalings gamma^(1/3) and gamma^(1/9) of the diffusion
 // coefficients (LegencyModel.hpp:483-502, FocusSolver.hpp:820, :968 call
 // pow(gamma, 1/3) and pow(gamma, 1/9)) as one and two cube roots: the same
 // values to within two ulp, at a fraction of pow's FP64 work.  The kernels
 // here are FP64-pipe bound, so every transcendental counts.
+template <typename T>
 struct GammaRoots {
-    double third, ninth;
+    T third, ninth;
 };
-__device__ __forceinline__ GammaRoots gamma_roots(double gamma, bool ninth) {
-    GammaRoots r;
-    r.third = cbrt(gamma);
-    r.ninth = ninth ? cbrt(r.third) : r.third;
+template <typename T>
+__device__ __forceinline__ GammaRoots<T> gamma_roots(T gamma, bool ninth) {
+    GammaRoots<T> r;
+    r.third = LibMath<T>::cbrt(gamma);
+    r.ninth = ninth ? LibMath<T>::cbrt(r.third) : r.third;
     return r;
 }
 
-__device__ __forceinline__ bool finite_positive(double v) { return isfinite(v) && v > 0.0; }
-__device__ __forceinline__ bool finite_nonnegative(double v) { return isfinite(v) && v >= 0.0; }
+template <typename T>
+__device__ __forceinline__ bool finite_positive(T v) { return isfinite(v) && v > T(0); }
+template <typename T>
+__device__ __forceinline__ bool finite_nonnegative(T v) { return isfinite(v) && v >= T(0); }
 
 // apply_grid_boundary_conditions for one active particle (ParticleSystem.hpp:
 // 653-699).  Returns false when the particle escaped.
@@ -244,8 +301,12 @@ static_assert(kMomentum + 1 == kLibTermCount, "term row layout");
 
 // evaluate_terms_from_packed + local_stable_time_step
 // (ParkerSolver.hpp:766-868, :689-760, :880-942).  Returns the local dt bound
-// or a negative error code.
+// or a negative error code.  T = double: the reference's FP64 arithmetic;
+// T = float: the mixed step (FP32 basis and terms; the positions, the
+// boundary and cell-width decisions stay FP64).
+template <typename T>
 __device__ double lib_parker_terms(const LibParkerLaunch& L, size_t i, double* terms) {
+    using M = LibMath<T>;
     const LibGrid& g = L.grid;
     const SystemArrays& s = L.sys;
     double pos[2] = {s.x[i], s.y[i]};
@@ -268,42 +329,46 @@ __device__ double lib_parker_terms(const LibParkerLaunch& L, size_t i, double* t
             return -1.0;  // "position lies outside the interpolation domain"
         }
     }
-    double v[kLibBasis];
-    lib_sample<kLibBasis, kLibBasisStride>(g, L.basis, q[0], q[1], v);
+    T v[kLibBasis];
+    if constexpr (sizeof(T) == 8) {
+        lib_sample<kLibBasis, kLibBasisStride>(g, L.basis, q[0], q[1], v);
+    } else {
+        lib_sample<kLibBasis, kLibBasisStrideF32>(g, L.basis_f32, q[0], q[1], v);
+    }
 
-    const double p_in = s.p[i];
-    const double p = p_in >= 0.0 ? p_in : -p_in;
-    const double normalized = p / L.mc;
-    const double gamma = sqrt(1.0 + normalized * normalized);
-    const double speed = p / (gamma * L.rest_mass);
-    double b2 = 0.0;
+    const T p_in = static_cast<T>(s.p[i]);
+    const T p = p_in >= T(0) ? p_in : -p_in;
+    const T normalized = p / static_cast<T>(L.mc);
+    const T gamma = M::sqrt(T(1) + normalized * normalized);
+    const T speed = p / (gamma * static_cast<T>(L.rest_mass));
+    T b2 = T(0);
 #pragma unroll
     for (int c = 0; c < 3; ++c) b2 += v[c] * v[c];
-    const double bmag = sqrt(b2);
+    const T bmag = M::sqrt(b2);
     if (!finite_positive(bmag)) {
         return -2.0;  // "stochastic diffusion requires |B| > 0"
     }
-    const double ib = 1.0 / bmag;
-    double dir[3];
+    const T ib = T(1) / bmag;
+    T dir[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) dir[c] = v[c] * ib;
-    const GammaRoots roots = gamma_roots(gamma, !L.constant_ratio);
-    const double g13 = roots.third;
-    double diff[3];
+    const GammaRoots<T> roots = gamma_roots<T>(gamma, !L.constant_ratio);
+    const T g13 = roots.third;
+    T diff[3];
     if (L.constant_ratio) {
 #pragma unroll
         for (int c = 0; c < 3; ++c) diff[c] = g13 * v[9 + c];
     } else {
-        const double g19 = roots.ninth;
+        const T g19 = roots.ninth;
 #pragma unroll
         for (int c = 0; c < 3; ++c) diff[c] = g13 * v[9 + c] + g19 * v[12 + c];
     }
-    const double kpar = v[15] * g13;
-    const double kperp = v[16] * (L.constant_ratio ? g13 : roots.ninth);
+    const T kpar = v[15] * g13;
+    const T kperp = v[16] * (L.constant_ratio ? g13 : roots.ninth);
     if (!finite_nonnegative(kpar) || !finite_nonnegative(kperp)) {
         return -3.0;  // "diffusion coefficients must be finite and non-negative"
     }
-    double keff[2];
+    T keff[2];
 #pragma unroll
     for (int d = 0; d < 2; ++d) {
         keff[d] = kperp + (kpar - kperp) * dir[d] * dir[d];
@@ -311,26 +376,28 @@ __device__ double lib_parker_terms(const LibParkerLaunch& L, size_t i, double* t
             return -4.0;  // "projected diffusion coefficient is invalid"
         }
     }
-    const double divv = v[17];
-    const double prefactor = p * speed * L.speed_of_light / (3.0 * L.charge);
-    double total[3];
+    const T divv = v[17];
+    const T prefactor = p * speed * static_cast<T>(L.speed_of_light) /
+                        (T(3) * static_cast<T>(L.charge));
+    T total[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) total[c] = v[3 + c] + prefactor * v[6 + c] + diff[c];
     // Cartesian: h_inv = 1
-    terms[kRateX] = total[0] * 1.0;
-    terms[kRateY] = total[1] * 1.0;
-    terms[kMomentumRate] = -(p / 3.0) * divv;
+    terms[kRateX] = total[0] * T(1);
+    terms[kRateY] = total[1] * T(1);
+    terms[kMomentumRate] = -(p / T(3)) * divv;
     terms[kKappaPar] = kpar;
     terms[kKappaPerp] = kperp;
     terms[kDirX] = dir[0];
     terms[kDirY] = dir[1];
     terms[kDirZ] = dir[2];
-    terms[kMomentum] = p;
+    terms[kMomentum] = sizeof(T) == 8 ? static_cast<double>(p)
+                                      : (s.p[i] >= 0.0 ? s.p[i] : -s.p[i]);
 
     // local_stable_time_step: prepare_physical_position again, then per-axis
     // cell widths at the physical cell index
-    double dmin = kLargeTimeStep;
-    double amin = kLargeTimeStep;
+    T dmin = static_cast<T>(kLargeTimeStep);
+    T amin = static_cast<T>(kLargeTimeStep);
 #pragma unroll
     for (int dim = 0; dim < 2; ++dim) {
         const LibAxis& a = g.axis[dim];
@@ -340,30 +407,30 @@ __device__ double lib_parker_terms(const LibParkerLaunch& L, size_t i, double* t
         }
         const double cell = static_cast<double>(lib_cell_index(a, x));
         const double width = __dsub_rn(lib_face(a, __dadd_rn(cell, 1.0)), lib_face(a, cell));
-        const double dx = fabs(__dmul_rn(1.0, width));
+        const T dx = static_cast<T>(fabs(__dmul_rn(1.0, width)));
         if (!finite_positive(dx)) {
             return -5.0;  // "local physical cell width must be positive"
         }
-        double diffusion_dt = kLargeTimeStep;
-        if (keff[dim] > 0.0) {
-            const double limited = 0.5 * dx;
-            diffusion_dt = limited * limited / (2.0 * keff[dim]);
+        T diffusion_dt = static_cast<T>(kLargeTimeStep);
+        if (keff[dim] > T(0)) {
+            const T limited = T(0.5) * dx;
+            diffusion_dt = limited * limited / (T(2) * keff[dim]);
         }
-        const double adv = fabs(total[dim]);
-        double advection_dt = kLargeTimeStep;
-        if (adv > 0.0) {
-            advection_dt = 1.0 * dx / adv;
+        const T adv = M::abs(total[dim]);
+        T advection_dt = static_cast<T>(kLargeTimeStep);
+        if (adv > T(0)) {
+            advection_dt = T(1) * dx / adv;
         }
         dmin = diffusion_dt < dmin ? diffusion_dt : dmin;
         amin = advection_dt < amin ? advection_dt : amin;
     }
-    double mdt = kLargeTimeStep;
-    const double dm = fabs(divv);
-    if (dm > 0.0) {
-        mdt = 3.0 * 1.0 / dm;
+    T mdt = static_cast<T>(kLargeTimeStep);
+    const T dm = M::abs(divv);
+    if (dm > T(0)) {
+        mdt = T(3) * T(1) / dm;
     }
-    const double da = dmin < amin ? dmin : amin;
-    return da < mdt ? da : mdt;
+    const T da = dmin < amin ? dmin : amin;
+    return static_cast<double>(da < mdt ? da : mdt);
 }
 
 __device__ __forceinline__ void record_error(int* error, int code, uint32_t index,
@@ -374,6 +441,7 @@ __device__ __forceinline__ void record_error(int* error, int code, uint32_t inde
 }
 
 // Pass 1: boundary conditions, terms, local dt -> global min (bit pattern).
+template <typename T>
 __global__ void __launch_bounds__(256) lib_parker_terms_kernel(const LibParkerLaunch L) {
     double local = kLargeTimeStep;
     const bool stopped = *L.error != 0;  // an earlier step of a replayed sequence failed
@@ -385,7 +453,7 @@ __global__ void __launch_bounds__(256) lib_parker_terms_kernel(const LibParkerLa
         if (L.apply_boundary && !lib_boundary(L.grid, L.sys, i)) {
             continue;
         }
-        const double dt = lib_parker_terms(L, i, L.terms + i * kLibTermCount);
+        const double dt = lib_parker_terms<T>(L, i, L.terms + i * kLibTermCount);
         if (dt < 0.0) {
             record_error(L.error, static_cast<int>(-dt), static_cast<uint32_t>(i),
                          L.error_index);
@@ -411,19 +479,33 @@ __global__ void __launch_bounds__(256) lib_parker_terms_kernel(const LibParkerLa
 
 // Box-Muller pair from two stream draws (u1 = 1 - draw, u2 = draw): normals
 // 2m and 2m+1 of a particle's step are r cos(theta) and r sin(theta) of
-// block m, as the shim pool's normal() hands them out.
+// block m, as the shim pool's normal() hands them out.  The FP32 pair takes
+// the high word of each draw (24 bits), so it tracks the FP64 pair.
+template <typename T>
 __device__ __forceinline__ double2 lib_normal_pair(uint2 key, uint32_t block, uint32_t index,
                                                    uint32_t frame) {
     const uint4 r = philox4x32_10(make_uint4(block, index, frame, kTagLibrary), key);
-    const double u1 = 1.0 - u01_f64(r.x, r.y);
-    const double u2 = u01_f64(r.z, r.w);
-    const double radius = sqrt(-2.0 * log(u1));
-    double s, c;
-    sincos(6.283185307179586 * u2, &s, &c);
-    return make_double2(radius * c, radius * s);
+    if constexpr (sizeof(T) == 8) {
+        const double u1 = 1.0 - u01_f64(r.x, r.y);
+        const double u2 = u01_f64(r.z, r.w);
+        const double radius = sqrt(-2.0 * log(u1));
+        double s, c;
+        sincos(6.283185307179586 * u2, &s, &c);
+        return make_double2(radius * c, radius * s);
+    } else {
+        const float u1 = 1.0f - u01_f32(r.y);
+        const float u2 = u01_f32(r.w);
+        const float radius = sqrtf(-2.0f * logf(u1));
+        float s, c;
+        sincosf(6.2831853071795865f * u2, &s, &c);
+        return make_double2(radius * c, radius * s);
+    }
 }
 
 // Pass 2: capture previous positions (whole capacity), update, boundary.
+// The mixed step (T = float) forms the noise increments in FP32 and adds
+// them, with the FP64 drift dt * rate, to the FP64 positions and momenta.
+template <typename T>
 __global__ void __launch_bounds__(256) lib_parker_advance_kernel(const LibParkerLaunch L) {
     const double dt = L.dt_device != nullptr ? *L.dt_device : L.dt;
     // a failed step (no positive dt, or an abort condition) changes nothing
@@ -452,21 +534,24 @@ __global__ void __launch_bounds__(256) lib_parker_advance_kernel(const LibParker
                 n01 = make_double2(L.noise[i], L.noise[L.count + i]);
                 n23 = make_double2(L.noise[2 * L.count + i], L.noise[3 * L.count + i]);
             } else {
-                n01 = lib_normal_pair(L.key, 0u, index, L.frame);
-                n23 = lib_normal_pair(L.key, 1u, index, L.frame);
+                n01 = lib_normal_pair<T>(L.key, 0u, index, L.frame);
+                n23 = lib_normal_pair<T>(L.key, 1u, index, L.frame);
             }
-            const double gv[3] = {n01.x, n01.y, n23.x};
-            double iso = 0.0;
+            const T tdt = static_cast<T>(dt);
+            const T gv[3] = {static_cast<T>(n01.x), static_cast<T>(n01.y), static_cast<T>(n23.x)};
+            const T d[3] = {static_cast<T>(t[kDirX]), static_cast<T>(t[kDirY]),
+                            static_cast<T>(t[kDirZ])};
+            T iso = T(0);
 #pragma unroll
-            for (int c = 0; c < 3; ++c) iso += gv[c] * t[kDirX + c];
-            const double pg = n23.y;
-            const double kperp = t[kKappaPerp];
-            const double kpar = t[kKappaPar];
-            const double perp_scale = kperp > 0.0 ? sqrt(2.0 * kperp * dt) : 0.0;
-            const double par_scale = kpar > 0.0 ? sqrt(2.0 * kpar * dt) : 0.0;
-            const double replacement = par_scale * pg - perp_scale * iso;
+            for (int c = 0; c < 3; ++c) iso += gv[c] * d[c];
+            const T pg = static_cast<T>(n23.y);
+            const T kperp = static_cast<T>(t[kKappaPerp]);
+            const T kpar = static_cast<T>(t[kKappaPar]);
+            const T perp_scale = kperp > T(0) ? LibMath<T>::sqrt(T(2) * kperp * tdt) : T(0);
+            const T par_scale = kpar > T(0) ? LibMath<T>::sqrt(T(2) * kpar * tdt) : T(0);
+            const T replacement = par_scale * pg - perp_scale * iso;
 #pragma unroll
-            for (int c = 0; c < 2; ++c) inc[c] = perp_scale * gv[c] + replacement * t[kDirX + c];
+            for (int c = 0; c < 2; ++c) inc[c] = perp_scale * gv[c] + replacement * d[c];
         }
         if (L.stochastic) {
             s.x[i] += dt * t[kRateX] + inc[0] * 1.0;
@@ -514,27 +599,30 @@ __device__ __forceinline__ void set_error(int* error, int code) {
 }
 
 // reflected_pitch_angle_cosine (FocusSolver.hpp:453-470).
-__device__ __forceinline__ double focus_reflect(double mu, double max_mu, int* error) {
+template <typename T>
+__device__ __forceinline__ T focus_reflect(T mu, T max_mu, int* error) {
     if (!isfinite(mu)) {
         set_error(error, 8);  // "pitch-angle cosine is not finite"
-        return 0.0;
+        return T(0);
     }
-    const double upper = max_mu;
-    const double lower = -max_mu;
+    const T upper = max_mu;
+    const T lower = -max_mu;
     for (int guard = 0; guard < 64 && (mu > upper || mu < lower); ++guard) {
-        if (mu > upper) mu = 2.0 * upper - mu;
-        if (mu < lower) mu = 2.0 * lower - mu;
+        if (mu > upper) mu = T(2) * upper - mu;
+        if (mu < lower) mu = T(2) * lower - mu;
     }
     return mu;
 }
 
-__device__ __forceinline__ double positive_floor(double v, double floor_value) {
-    if (floor_value <= 0.0) return v;
+template <typename T>
+__device__ __forceinline__ T positive_floor(T v, T floor_value) {
+    if (floor_value <= T(0)) return v;
     return v < floor_value ? floor_value : v;
 }
 
+template <typename T>
 struct PitchRates {
-    double focusing, D, dD, rate;
+    T focusing, D, dD, rate;
 };
 
 // The parts of evaluate_pitch_angle_at_mu (FocusSolver.hpp:664-695) and of
@@ -545,71 +633,78 @@ struct PitchRates {
 // pow(xi, gk) and pow(|mu|+h0, gk-1) in both D and D'; here one pow per trial
 // cosine remains (|mu|+h0)^(gk-1), with (|mu|+h0)^gk as its product with
 // |mu|+h0 (equal to within two ulp).
+template <typename T>
 struct PitchSetup {
-    double speed, focusing0, convective, omega, xi, xi_gk, pref;
+    T speed, focusing0, convective, omega, xi, xi_gk, pref;
     int error;  // 12, 13 or 14: the input check that fails, in the reference's order
 };
 
-__device__ PitchSetup focus_pitch_setup(const LibFocusLaunch& L, const double* t) {
-    PitchSetup q{};
-    q.speed = t[fSpeed];
-    if (q.speed <= 0.0) {
+template <typename T>
+__device__ PitchSetup<T> focus_pitch_setup(const LibFocusLaunch& L, const double* t) {
+    PitchSetup<T> q{};
+    q.speed = static_cast<T>(t[fSpeed]);
+    if (q.speed <= T(0)) {
         q.error = 12;  // "pitch-angle stepping requires positive particle speed"
         return q;
     }
-    q.focusing0 = -q.speed * t[fFocusing];
-    q.convective = 2.0 * t[fConvective] / q.speed;
-    const double safe_b = positive_floor(t[fBmag], L.min_b);
-    const double safe_sigma2 = positive_floor(t[fSigma2], L.min_sigma2);
-    const double safe_lc = positive_floor(t[fLc], L.min_lc);
-    const double safe_speed = positive_floor(q.speed, L.min_speed);
-    if (safe_b <= 0.0 || safe_sigma2 <= 0.0 || safe_lc <= 0.0 || safe_speed <= 0.0) {
+    q.focusing0 = -q.speed * static_cast<T>(t[fFocusing]);
+    q.convective = T(2) * static_cast<T>(t[fConvective]) / q.speed;
+    const T safe_b = positive_floor(static_cast<T>(t[fBmag]), static_cast<T>(L.min_b));
+    const T safe_sigma2 = positive_floor(static_cast<T>(t[fSigma2]), static_cast<T>(L.min_sigma2));
+    const T safe_lc = positive_floor(static_cast<T>(t[fLc]), static_cast<T>(L.min_lc));
+    const T safe_speed = positive_floor(q.speed, static_cast<T>(L.min_speed));
+    if (safe_b <= T(0) || safe_sigma2 <= T(0) || safe_lc <= T(0) || safe_speed <= T(0)) {
         q.error = 13;  // "pitch-angle scattering requires positive local inputs"
         return q;
     }
-    q.omega = L.abs_charge * safe_b / (L.rest_mass * L.speed_of_light) / t[fGamma];
-    if (q.omega <= 0.0) {
+    q.omega = static_cast<T>(L.abs_charge) * safe_b /
+              (static_cast<T>(L.rest_mass) * static_cast<T>(L.speed_of_light)) /
+              static_cast<T>(t[fGamma]);
+    if (q.omega <= T(0)) {
         q.error = 14;  // "D_mumu requires positive omega, speed, sigma2, and Lc"
         return q;
     }
     q.xi = q.omega * safe_lc / safe_speed;
-    q.xi_gk = pow(q.xi, L.gk);
-    q.pref = 0.25 * 3.141592653589793238462643383279502884 * q.omega * safe_sigma2 * L.qlt_norm;
+    q.xi_gk = LibMath<T>::pow(q.xi, static_cast<T>(L.gk));
+    q.pref = static_cast<T>(0.25 * 3.141592653589793238462643383279502884) * q.omega *
+             safe_sigma2 * static_cast<T>(L.qlt_norm);
     return q;
 }
 
 // evaluate_pitch_angle_at_mu with the slab-QLT evaluate_pitch_angle_scattering
 // (LegencyModel.hpp:539-693) at one trial cosine.
-__device__ PitchRates focus_pitch(const LibFocusLaunch& L, const double* t, const PitchSetup& q,
-                                  double trial, int* error) {
-    PitchRates r{0.0, 0.0, 0.0, 0.0};
-    const double mu = focus_reflect(trial, L.max_mu, error);
+template <typename T>
+__device__ PitchRates<T> focus_pitch(const LibFocusLaunch& L, const double* t,
+                                     const PitchSetup<T>& q, T trial, int* error) {
+    PitchRates<T> r{T(0), T(0), T(0), T(0)};
+    const T mu = focus_reflect(trial, static_cast<T>(L.max_mu), error);
     if (q.error != 0) {
         set_error(error, q.error);
         return r;
     }
-    const double mu2 = mu * mu;
-    const double one_minus_mu2 = 1.0 - mu2;
-    r.focusing = 0.5 * one_minus_mu2 *
-                 (q.focusing0 + mu * t[fDivV] - 3.0 * mu * t[fBBGradV] - q.convective);
-    double d = 0.0;
-    double dd = 0.0;
-    if (one_minus_mu2 > 0.0) {
-        const double reg = (mu >= 0.0 ? mu : -mu) + L.h0;
-        const double gk = L.gk;
-        const double reg_gk1 = pow(reg, gk - 1.0);
-        const double reg_gk = reg > 0.0 ? reg_gk1 * reg : pow(reg, gk);
-        const double den = reg_gk + q.xi_gk;
-        if (den <= 0.0) {
+    const T mu2 = mu * mu;
+    const T one_minus_mu2 = T(1) - mu2;
+    r.focusing = T(0.5) * one_minus_mu2 *
+                 (q.focusing0 + mu * static_cast<T>(t[fDivV]) -
+                  T(3) * mu * static_cast<T>(t[fBBGradV]) - q.convective);
+    T d = T(0);
+    T dd = T(0);
+    if (one_minus_mu2 > T(0)) {
+        const T reg = (mu >= T(0) ? mu : -mu) + static_cast<T>(L.h0);
+        const T gk = static_cast<T>(L.gk);
+        const T reg_gk1 = LibMath<T>::pow(reg, gk - T(1));
+        const T reg_gk = reg > T(0) ? reg_gk1 * reg : LibMath<T>::pow(reg, gk);
+        const T den = reg_gk + q.xi_gk;
+        if (den <= T(0)) {
             set_error(error, 15);  // "D_mumu denominator must be positive"
             return r;
         }
         d = q.pref * one_minus_mu2 * q.xi * reg_gk1 / den;
         // pitch_angle_diffusion_derivative (LegencyModel.hpp:599-645)
-        const double sign = mu > 0.0 ? 1.0 : (mu < 0.0 ? -1.0 : 0.0);
-        if (d != 0.0 && sign != 0.0) {
-            const double shape = sign * ((gk - 1.0) / reg - gk * reg_gk1 / den);
-            dd = d * (-2.0 * mu / one_minus_mu2 + shape);
+        const T sign = mu > T(0) ? T(1) : (mu < T(0) ? T(-1) : T(0));
+        if (d != T(0) && sign != T(0)) {
+            const T shape = sign * ((gk - T(1)) / reg - gk * reg_gk1 / den);
+            dd = d * (T(-2) * mu / one_minus_mu2 + shape);
         }
     }
     r.D = d;
@@ -619,8 +714,12 @@ __device__ PitchRates focus_pitch(const LibFocusLaunch& L, const double* t, cons
 }
 
 // evaluate_terms_from_packed + local_stable_time_step
-// (FocusSolver.hpp:904-1008, :1148-1233).
+// (FocusSolver.hpp:904-1008, :1148-1233).  T = double: the reference's FP64
+// arithmetic; T = float: the mixed step (FP32 basis, terms and closure; the
+// positions, boundary and cell-width decisions and the momentum stay FP64).
+template <typename T>
 __device__ double focus_terms(const LibFocusLaunch& L, size_t i, double* t, int* error) {
+    using M = LibMath<T>;
     const LibGrid& g = L.grid;
     const SystemArrays& s = L.sys;
     double pos[2] = {s.x[i], s.y[i]};
@@ -641,64 +740,69 @@ __device__ double focus_terms(const LibFocusLaunch& L, size_t i, double* t, int*
             return -1.0;
         }
     }
-    double v[kFocusBasis];
-    lib_sample<kFocusBasis, kFocusBasisStride>(g, L.basis, q[0], q[1], v);
-    const double p_in = s.p[i];
-    const double p = p_in >= 0.0 ? p_in : -p_in;
-    const double mu = focus_reflect(s.mu[i], L.max_mu, error);
-    const double normalized = p / L.mc;
-    const double gamma = sqrt(1.0 + normalized * normalized);
-    const double speed = p / (gamma * L.rest_mass);
-    const double bmag = v[18];
+    T v[kFocusBasis];
+    if constexpr (sizeof(T) == 8) {
+        lib_sample<kFocusBasis, kFocusBasisStride>(g, L.basis, q[0], q[1], v);
+    } else {
+        lib_sample<kFocusBasis, kFocusBasisStrideF32>(g, L.basis_f32, q[0], q[1], v);
+    }
+    const double p_state = s.p[i] >= 0.0 ? s.p[i] : -s.p[i];
+    const T p_in = static_cast<T>(s.p[i]);
+    const T p = p_in >= T(0) ? p_in : -p_in;
+    const T mu = focus_reflect(static_cast<T>(s.mu[i]), static_cast<T>(L.max_mu), error);
+    const T normalized = p / static_cast<T>(L.mc);
+    const T gamma = M::sqrt(T(1) + normalized * normalized);
+    const T speed = p / (gamma * static_cast<T>(L.rest_mass));
+    const T bmag = v[18];
     if (!finite_positive(bmag)) {
         set_error(error, 9);  // "focused transport requires |B| > 0"
         return -1.0;
     }
-    double s2 = 0.0;
+    T s2 = T(0);
 #pragma unroll
     for (int c = 0; c < 3; ++c) s2 += v[3 + c] * v[3 + c];
-    const double smag = sqrt(s2);
+    const T smag = M::sqrt(s2);
     if (!finite_positive(smag)) {
         set_error(error, 10);  // "interpolated magnetic direction is invalid"
         return -1.0;
     }
-    const double inv = 1.0 / smag;
-    double dir[3];
+    const T inv = T(1) / smag;
+    T dir[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) dir[c] = v[3 + c] * inv;
-    const GammaRoots roots = gamma_roots(gamma, !L.constant_ratio);
-    const double perp_factor = L.constant_ratio ? roots.third : roots.ninth;
-    const double kpar = v[19] * roots.third;
-    const double kperp = v[20] * perp_factor;
+    const GammaRoots<T> roots = gamma_roots<T>(gamma, !L.constant_ratio);
+    const T perp_factor = L.constant_ratio ? roots.third : roots.ninth;
+    const T kpar = v[19] * roots.third;
+    const T kperp = v[20] * perp_factor;
     if (!finite_nonnegative(kpar) || !finite_nonnegative(kperp)) {
         set_error(error, 11);  // "diffusion coefficients must be finite and non-negative"
         return -1.0;
     }
-    const double mu2 = mu * mu;
-    const double gdf = 0.5 * (1.0 - mu2);
-    const double cdf = mu2;
-    const double prefactor = p * speed * L.speed_of_light / L.charge;
-    double total[3];
+    const T mu2 = mu * mu;
+    const T gdf = T(0.5) * (T(1) - mu2);
+    const T cdf = mu2;
+    const T prefactor = p * speed * static_cast<T>(L.speed_of_light) / static_cast<T>(L.charge);
+    T total[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        const double streaming = speed * mu * dir[c];
-        const double drift = prefactor * (gdf * v[9 + c] + cdf * v[12 + c]);
-        const double diffadv = perp_factor * v[15 + c];
+        const T streaming = speed * mu * dir[c];
+        const T drift = prefactor * (gdf * v[9 + c] + cdf * v[12 + c]);
+        const T diffadv = perp_factor * v[15 + c];
         total[c] = streaming + v[6 + c] + drift + diffadv;
     }
-    double keff[2];
+    T keff[2];
 #pragma unroll
     for (int d = 0; d < 2; ++d) {
-        const double projection = 1.0 - dir[d] * dir[d];
-        keff[d] = projection > 0.0 ? kperp * projection : 0.0;
+        const T projection = T(1) - dir[d] * dir[d];
+        keff[d] = projection > T(0) ? kperp * projection : T(0);
     }
-    t[fRateX] = total[0] * 1.0;
-    t[fRateY] = total[1] * 1.0;
+    t[fRateX] = total[0] * T(1);
+    t[fRateY] = total[1] * T(1);
     t[fKappaPerp] = kperp;
     t[fDirX] = dir[0];
     t[fDirY] = dir[1];
     t[fDirZ] = dir[2];
-    t[fMomentum] = p;
+    t[fMomentum] = sizeof(T) == 8 ? static_cast<double>(p) : p_state;
     t[fMu] = mu;
     t[fSpeed] = speed;
     t[fGamma] = gamma;
@@ -709,17 +813,17 @@ __device__ double focus_terms(const LibFocusLaunch& L, size_t i, double* t, int*
     t[fConvective] = v[24];
     t[fSigma2] = v[25];
     t[fLc] = v[26];
-    const double one_minus_mu2 = 1.0 - mu2;
-    double acceleration = 0.0;
-    if (speed > 0.0) acceleration = mu * v[24] / speed;
-    const double momentum_factor = 0.5 * one_minus_mu2 * (v[21] - v[23]) + mu2 * v[23] +
-                                   acceleration;
-    const double momentum_rate = -p * momentum_factor;
+    const T one_minus_mu2 = T(1) - mu2;
+    T acceleration = T(0);
+    if (speed > T(0)) acceleration = mu * v[24] / speed;
+    const T momentum_factor = T(0.5) * one_minus_mu2 * (v[21] - v[23]) + mu2 * v[23] +
+                              acceleration;
+    const T momentum_rate = -p * momentum_factor;
     t[fMomentumRate] = momentum_rate;
-    const PitchRates pitch = focus_pitch(L, t, focus_pitch_setup(L, t), mu, error);
+    const PitchRates<T> pitch = focus_pitch<T>(L, t, focus_pitch_setup<T>(L, t), mu, error);
 
-    double dmin = kLargeTimeStep;
-    double amin = kLargeTimeStep;
+    T dmin = static_cast<T>(kLargeTimeStep);
+    T amin = static_cast<T>(kLargeTimeStep);
 #pragma unroll
     for (int dim = 0; dim < 2; ++dim) {
         const LibAxis& a = g.axis[dim];
@@ -729,39 +833,40 @@ __device__ double focus_terms(const LibFocusLaunch& L, size_t i, double* t, int*
         }
         const double cell = static_cast<double>(lib_cell_index(a, x));
         const double width = __dsub_rn(lib_face(a, __dadd_rn(cell, 1.0)), lib_face(a, cell));
-        const double dx = fabs(__dmul_rn(1.0, width));
+        const T dx = static_cast<T>(fabs(__dmul_rn(1.0, width)));
         if (!finite_positive(dx)) {
             set_error(error, 5);
             return -1.0;
         }
-        double diffusion_dt = kLargeTimeStep;
-        if (keff[dim] > 0.0) {
-            const double limited = 0.5 * dx;
-            diffusion_dt = limited * limited / (2.0 * keff[dim]);
+        T diffusion_dt = static_cast<T>(kLargeTimeStep);
+        if (keff[dim] > T(0)) {
+            const T limited = T(0.5) * dx;
+            diffusion_dt = limited * limited / (T(2) * keff[dim]);
         }
-        const double adv = fabs(total[dim]);
-        double advection_dt = kLargeTimeStep;
-        if (adv > 0.0) advection_dt = 1.0 * dx / adv;
+        const T adv = M::abs(total[dim]);
+        T advection_dt = static_cast<T>(kLargeTimeStep);
+        if (adv > T(0)) advection_dt = T(1) * dx / adv;
         dmin = diffusion_dt < dmin ? diffusion_dt : dmin;
         amin = advection_dt < amin ? advection_dt : amin;
     }
-    double mdt = kLargeTimeStep;
-    const double mrate = fabs(momentum_rate);
-    if (p > 0.0 && mrate > 0.0) mdt = 1.0 * p / mrate;
-    double padv = kLargeTimeStep;
-    const double murate = fabs(pitch.rate);
-    if (murate > 0.0) padv = 10.0 * 0.1 / murate;
-    double pdiff = kLargeTimeStep;
-    if (pitch.D > 0.0) pdiff = 10.0 * 0.1 * 0.1 / (2.0 * pitch.D);
-    double pbal = kLargeTimeStep;
-    if (pitch.D > 0.0 && murate > 0.0) pbal = 10.0 * 2.0 * pitch.D / (murate * murate);
-    const double a1 = dmin < amin ? dmin : amin;
-    const double a2 = a1 < mdt ? a1 : mdt;
-    const double b1 = pdiff < pbal ? pdiff : pbal;
-    const double b2 = padv < b1 ? padv : b1;
-    return a2 < b2 ? a2 : b2;
+    T mdt = static_cast<T>(kLargeTimeStep);
+    const T mrate = M::abs(momentum_rate);
+    if (p > T(0) && mrate > T(0)) mdt = T(1) * p / mrate;
+    T padv = static_cast<T>(kLargeTimeStep);
+    const T murate = M::abs(pitch.rate);
+    if (murate > T(0)) padv = T(10) * T(0.1) / murate;
+    T pdiff = static_cast<T>(kLargeTimeStep);
+    if (pitch.D > T(0)) pdiff = T(10) * T(0.1) * T(0.1) / (T(2) * pitch.D);
+    T pbal = static_cast<T>(kLargeTimeStep);
+    if (pitch.D > T(0) && murate > T(0)) pbal = T(10) * T(2) * pitch.D / (murate * murate);
+    const T a1 = dmin < amin ? dmin : amin;
+    const T a2 = a1 < mdt ? a1 : mdt;
+    const T b1 = pdiff < pbal ? pdiff : pbal;
+    const T b2 = padv < b1 ? padv : b1;
+    return static_cast<double>(a2 < b2 ? a2 : b2);
 }
 
+template <typename T>
 __global__ void __launch_bounds__(256) focus_terms_kernel(const LibFocusLaunch L) {
     double local = kLargeTimeStep;
     const bool stopped = *L.error != 0;
@@ -770,7 +875,7 @@ __global__ void __launch_bounds__(256) focus_terms_kernel(const LibFocusLaunch L
         if (L.sys.status[i] != 0) continue;
         if (L.apply_boundary && !lib_boundary(L.grid, L.sys, i)) continue;
         int err = 0;
-        const double dt = focus_terms(L, i, L.terms + i * kFocusTermCount, &err);
+        const double dt = focus_terms<T>(L, i, L.terms + i * kFocusTermCount, &err);
         if (err != 0) {
             record_error(L.error, err, static_cast<uint32_t>(i), L.error_index);
             continue;
@@ -792,7 +897,10 @@ __global__ void __launch_bounds__(256) focus_terms_kernel(const LibFocusLaunch L
 }
 
 // advance_*_with_packed_interpolator (FocusSolver.hpp:1580-1637) with the
-// Picard pitch-angle update (:697-740).
+// Picard pitch-angle update (:697-740).  The mixed step (T = float) forms the
+// noise increments and the pitch-angle update in FP32 and adds the
+// increments, with the FP64 drift dt * rate, to the FP64 positions.
+template <typename T>
 __global__ void __launch_bounds__(256) focus_advance_kernel(const LibFocusLaunch L) {
     const double dt = L.dt_device != nullptr ? *L.dt_device : L.dt;
     if (!(isfinite(dt) && dt > 0.0) || *L.error != 0) {
@@ -810,7 +918,8 @@ __global__ void __launch_bounds__(256) focus_advance_kernel(const LibFocusLaunch
         if (i >= L.count || s.status[i] != 0) continue;
         const double* t = L.terms + i * kFocusTermCount;
         double inc[2] = {0.0, 0.0};
-        double pitch_normal = 0.0;
+        T pitch_normal = T(0);
+        const T tdt = static_cast<T>(dt);
         if (L.stochastic) {
             const uint32_t index = static_cast<uint32_t>(i);
             double2 n01, n23;
@@ -818,32 +927,35 @@ __global__ void __launch_bounds__(256) focus_advance_kernel(const LibFocusLaunch
                 n01 = make_double2(L.noise[i], L.noise[L.count + i]);
                 n23 = make_double2(L.noise[2 * L.count + i], L.noise[3 * L.count + i]);
             } else {
-                n01 = lib_normal_pair(L.key, 0u, index, L.frame);
-                n23 = lib_normal_pair(L.key, 1u, index, L.frame);
+                n01 = lib_normal_pair<T>(L.key, 0u, index, L.frame);
+                n23 = lib_normal_pair<T>(L.key, 1u, index, L.frame);
             }
-            const double gv[3] = {n01.x, n01.y, n23.x};
-            double parallel = 0.0;
+            const T gv[3] = {static_cast<T>(n01.x), static_cast<T>(n01.y), static_cast<T>(n23.x)};
+            const T d[3] = {static_cast<T>(t[fDirX]), static_cast<T>(t[fDirY]),
+                            static_cast<T>(t[fDirZ])};
+            T parallel = T(0);
 #pragma unroll
-            for (int c = 0; c < 3; ++c) parallel += gv[c] * t[fDirX + c];
-            const double kperp = t[fKappaPerp];
-            const double scale = kperp > 0.0 ? sqrt(2.0 * kperp * dt) : 0.0;
+            for (int c = 0; c < 3; ++c) parallel += gv[c] * d[c];
+            const T kperp = static_cast<T>(t[fKappaPerp]);
+            const T scale = kperp > T(0) ? LibMath<T>::sqrt(T(2) * kperp * tdt) : T(0);
 #pragma unroll
-            for (int c = 0; c < 2; ++c) inc[c] = scale * (gv[c] - parallel * t[fDirX + c]);
-            pitch_normal = n23.y;
+            for (int c = 0; c < 2; ++c) inc[c] = scale * (gv[c] - parallel * d[c]);
+            pitch_normal = static_cast<T>(n23.y);
         }
         s.x[i] += dt * t[fRateX] + inc[0] * 1.0;
         s.y[i] += dt * t[fRateY] + inc[1] * 1.0;
         const double updated = t[fMomentum] + dt * t[fMomentumRate];
         s.p[i] = updated > 0.0 ? updated : 0.0;
         int err = 0;
-        const double initial = focus_reflect(t[fMu], L.max_mu, &err);
-        const PitchSetup setup = focus_pitch_setup(L, t);
-        double trial = initial;
+        const T max_mu = static_cast<T>(L.max_mu);
+        const T initial = focus_reflect(static_cast<T>(t[fMu]), max_mu, &err);
+        const PitchSetup<T> setup = focus_pitch_setup<T>(L, t);
+        T trial = initial;
         for (int it = 0; it < 3; ++it) {
-            const PitchRates pitch = focus_pitch(L, t, setup, trial, &err);
-            const double scale = pitch.D > 0.0 ? sqrt(2.0 * pitch.D * dt) : 0.0;
-            trial = initial + dt * pitch.rate + scale * pitch_normal;
-            trial = focus_reflect(trial, L.max_mu, &err);
+            const PitchRates<T> pitch = focus_pitch<T>(L, t, setup, trial, &err);
+            const T scale = pitch.D > T(0) ? LibMath<T>::sqrt(T(2) * pitch.D * tdt) : T(0);
+            trial = initial + tdt * pitch.rate + scale * pitch_normal;
+            trial = focus_reflect(trial, max_mu, &err);
         }
         if (err != 0) {
             record_error(L.error, err, static_cast<uint32_t>(i), L.error_index);
@@ -2038,17 +2150,47 @@ int grid_for(uint64_t n, int threads) {
 
 }  // namespace
 
+// The FP32 copy of a packed basis for the mixed step: each row rounded to
+// FP32 and padded with zeros to dst_stride floats.
+__global__ void basis_to_f32_kernel(const double* __restrict__ src, int src_stride,
+                                    float* __restrict__ dst, int dst_stride, int comps,
+                                    uint64_t points) {
+    const uint64_t n = points * static_cast<uint64_t>(dst_stride);
+    for (uint64_t k = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; k < n;
+         k += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        const uint64_t point = k / dst_stride;
+        const int c = static_cast<int>(k % dst_stride);
+        dst[k] = c < comps ? static_cast<float>(src[point * src_stride + c]) : 0.0f;
+    }
+}
+
+cudaError_t lib_basis_to_f32(const double* src, int src_stride, float* dst, int dst_stride,
+                             int comps, uint64_t points, cudaStream_t stream) {
+    if (points == 0) return cudaSuccess;
+    basis_to_f32_kernel<<<grid_for(points * dst_stride, 256), 256, 0, stream>>>(
+        src, src_stride, dst, dst_stride, comps, points);
+    return cudaGetLastError();
+}
+
 cudaError_t lib_parker_step(const LibParkerLaunch& L, cudaStream_t stream) {
     lib_reset_min_kernel<<<1, 1, 0, stream>>>(L.min_bits);
     if (L.count > 0) {
-        lib_parker_terms_kernel<<<grid_for(L.count, 256), 256, 0, stream>>>(L);
+        if (L.mixed) {
+            lib_parker_terms_kernel<float><<<grid_for(L.count, 256), 256, 0, stream>>>(L);
+        } else {
+            lib_parker_terms_kernel<double><<<grid_for(L.count, 256), 256, 0, stream>>>(L);
+        }
     }
     lib_finish_dt_kernel<<<1, 1, 0, stream>>>(L.min_bits, L.courant, L.dt_device_out,
                                               L.dt_history, L.error, L.advance);
     if (L.advance) {
         LibParkerLaunch A = L;
         A.dt_device = L.dt_device_out;
-        lib_parker_advance_kernel<<<grid_for(L.capacity, 256), 256, 0, stream>>>(A);
+        if (L.mixed) {
+            lib_parker_advance_kernel<float><<<grid_for(L.capacity, 256), 256, 0, stream>>>(A);
+        } else {
+            lib_parker_advance_kernel<double><<<grid_for(L.capacity, 256), 256, 0, stream>>>(A);
+        }
     }
     return cudaGetLastError();
 }
@@ -2056,14 +2198,22 @@ cudaError_t lib_parker_step(const LibParkerLaunch& L, cudaStream_t stream) {
 cudaError_t lib_focus_step(const LibFocusLaunch& L, cudaStream_t stream) {
     lib_reset_min_kernel<<<1, 1, 0, stream>>>(L.min_bits);
     if (L.count > 0) {
-        focus_terms_kernel<<<grid_for(L.count, 256), 256, 0, stream>>>(L);
+        if (L.mixed) {
+            focus_terms_kernel<float><<<grid_for(L.count, 256), 256, 0, stream>>>(L);
+        } else {
+            focus_terms_kernel<double><<<grid_for(L.count, 256), 256, 0, stream>>>(L);
+        }
     }
     lib_finish_dt_kernel<<<1, 1, 0, stream>>>(L.min_bits, L.courant, L.dt_device_out,
                                               L.dt_history, L.error, L.advance);
     if (L.advance) {
         LibFocusLaunch A = L;
         A.dt_device = L.dt_device_out;
-        focus_advance_kernel<<<grid_for(L.capacity, 256), 256, 0, stream>>>(A);
+        if (L.mixed) {
+            focus_advance_kernel<float><<<grid_for(L.capacity, 256), 256, 0, stream>>>(A);
+        } else {
+            focus_advance_kernel<double><<<grid_for(L.capacity, 256), 256, 0, stream>>>(A);
+        }
     }
     return cudaGetLastError();
 }
