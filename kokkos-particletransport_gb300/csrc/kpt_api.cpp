@@ -2144,6 +2144,7 @@ int kpt_grid_create(kpt_context* ctx, int nx, int ny, const double* x_edges,
         a.periodic = periodic[dim] != 0 ? 1 : 0;
         a.x0 = e[0];
         a.dx = step;
+        a.inv_dx = 1.0 / step;
         // AnalyticCoordinateMapping face coordinates x0 + i dx
         // (MappedCoordinateGrid.hpp:118-147)
         a.lower = a.x0 + 0.0 * a.dx;
@@ -2229,6 +2230,7 @@ int kpt_grid_create_stored(kpt_context* ctx, int nx, int ny, const double* x_fac
         a.cells = g->coordinates.as<double>() + offsets[dim][1];
         a.x0 = f[2];
         a.dx = 0.0;
+        a.inv_dx = 0.0;
         a.lower = f[2];
         a.upper = f[n + 2];
         a.ghost_lower = f[0];

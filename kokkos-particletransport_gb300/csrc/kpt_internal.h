@@ -245,6 +245,7 @@ struct LibAxis {
     int n;
     int periodic;
     double x0, dx;                    // analytic uniform axis: face i at x0 + i dx
+    double inv_dx;                    // 1 / dx (the mixed library step's stencil)
     double lower, upper;              // faces 0 and n
     double ghost_lower, ghost_upper;  // faces -2 and n+2
     double width, inv_width;          // periodic width (upper - lower) and 1/width

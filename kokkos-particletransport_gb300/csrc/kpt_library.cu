@@ -131,12 +131,31 @@ __device__ __forceinline__ int lib_cell_index(const LibAxis& a, double x) {
 // Cell-centred stencil over the ghosted domain [-2, n+1]
 // (FieldInterpolator.hpp:509-559) on the logical index of
 // AnalyticCoordinateGrid.hpp:216-230 or StoredCoordinateGrid::grid_index.
+__device__ __forceinline__ void stencil_from_logical(const LibAxis& a, double logical, int& lo,
+                                                     int& hi, double& w);
+
 __device__ __forceinline__ void lib_stencil(const LibAxis& a, double x, int& lo, int& hi,
                                             double& w) {
-    const int lower_bound = -2;
-    const int upper_bound = a.n + 1;
     const double logical = a.stored ? stored_grid_index(a, x, false)
                                     : __dsub_rn(__ddiv_rn(__dsub_rn(x, a.x0), a.dx), 0.5);
+    stencil_from_logical(a, logical, lo, hi, w);
+}
+
+// The mixed step's stencil: on a uniform axis the logical index comes from
+// one FP64 multiply-add by 1/dx instead of the reference's division (the
+// FP64 pipe is the scarce one here); stored axes keep their bisection.
+__device__ __forceinline__ void lib_stencil_mixed(const LibAxis& a, double x, int& lo, int& hi,
+                                                  double& w) {
+    const double logical = a.stored ? stored_grid_index(a, x, false)
+                                    : fma(x - a.x0, a.inv_dx, -0.5);
+    stencil_from_logical(a, logical, lo, hi, w);
+}
+
+// FieldInterpolator's compute_axis_stencil on a logical index.
+__device__ __forceinline__ void stencil_from_logical(const LibAxis& a, double logical, int& lo,
+                                                     int& hi, double& w) {
+    const int lower_bound = -2;
+    const int upper_bound = a.n + 1;
     if (logical <= static_cast<double>(lower_bound)) {
         lo = hi = lower_bound;
         w = 0.0;
@@ -200,16 +219,17 @@ __device__ __forceinline__ void lib_sample(const LibGrid& g, const float* __rest
     static_assert(STRIDE % 4 == 0 && STRIDE >= C, "FP32 rows hold whole 16-byte chunks");
     int lo[2], hi[2];
     double w[2];
-    lib_stencil(g.axis[0], x, lo[0], hi[0], w[0]);
-    lib_stencil(g.axis[1], y, lo[1], hi[1], w[1]);
+    lib_stencil_mixed(g.axis[0], x, lo[0], hi[0], w[0]);
+    lib_stencil_mixed(g.axis[1], y, lo[1], hi[1], w[1]);
 #pragma unroll
     for (int c = 0; c < C; ++c) out[c] = 0.0f;
 #pragma unroll
     for (int corner = 0; corner < 4; ++corner) {
         const bool ux = (corner & 1) != 0;
         const bool uy = (corner & 2) != 0;
-        const float weight = static_cast<float>((ux ? w[0] : 1.0 - w[0]) *
-                                                (uy ? w[1] : 1.0 - w[1]));
+        const float wx = static_cast<float>(w[0]);
+        const float wy = static_cast<float>(w[1]);
+        const float weight = (ux ? wx : 1.0f - wx) * (uy ? wy : 1.0f - wy);
         const int i = (ux ? hi[0] : lo[0]) + 2;
         const int j = (uy ? hi[1] : lo[1]) + 2;
         const float4* row =
@@ -302,11 +322,13 @@ static_assert(kMomentum + 1 == kLibTermCount, "term row layout");
 // evaluate_terms_from_packed + local_stable_time_step
 // (ParkerSolver.hpp:766-868, :689-760, :880-942).  Returns the local dt bound
 // or a negative error code.  T = double: the reference's FP64 arithmetic;
-// T = float: the mixed step (FP32 basis and terms; the positions, the
-// boundary and cell-width decisions stay FP64).
+// T = float: the mixed step (FP32 basis, terms and bounds in an FP32 term
+// row; the positions and the boundary decisions stay FP64, wrapped once, and
+// the momentum base is read from the FP64 state by the update).
 template <typename T>
-__device__ double lib_parker_terms(const LibParkerLaunch& L, size_t i, double* terms) {
+__device__ T lib_parker_terms(const LibParkerLaunch& L, size_t i, T* terms) {
     using M = LibMath<T>;
+    constexpr bool kMixed = sizeof(T) == 4;
     const LibGrid& g = L.grid;
     const SystemArrays& s = L.sys;
     double pos[2] = {s.x[i], s.y[i]};
@@ -316,24 +338,25 @@ __device__ double lib_parker_terms(const LibParkerLaunch& L, size_t i, double* t
         pos[dim] = lib_wrap(g.axis[dim], pos[dim]);
         if (!lib_contains(g.axis[dim].lower, g.axis[dim].upper, pos[dim])) {
             // the reference's empty terms: zero rates, zero time step
-            for (int k = 0; k < kLibTermCount; ++k) terms[k] = 0.0;
-            return 0.0;
-        }
-    }
-    // interpolator prepare_coordinate: wrap, then the ghosted-domain check
-    double q[2];
-#pragma unroll
-    for (int dim = 0; dim < 2; ++dim) {
-        q[dim] = lib_wrap(g.axis[dim], pos[dim]);
-        if (!lib_contains(g.axis[dim].ghost_lower, g.axis[dim].ghost_upper, q[dim])) {
-            return -1.0;  // "position lies outside the interpolation domain"
+            for (int k = 0; k < kLibTermCount; ++k) terms[k] = T(0);
+            return T(0);
         }
     }
     T v[kLibBasis];
-    if constexpr (sizeof(T) == 8) {
-        lib_sample<kLibBasis, kLibBasisStride>(g, L.basis, q[0], q[1], v);
+    if constexpr (kMixed) {
+        // a wrapped physical position is its own wrap and inside the ghosts
+        lib_sample<kLibBasis, kLibBasisStrideF32>(g, L.basis_f32, pos[0], pos[1], v);
     } else {
-        lib_sample<kLibBasis, kLibBasisStrideF32>(g, L.basis_f32, q[0], q[1], v);
+        // interpolator prepare_coordinate: wrap, then the ghosted-domain check
+        double q[2];
+#pragma unroll
+        for (int dim = 0; dim < 2; ++dim) {
+            q[dim] = lib_wrap(g.axis[dim], pos[dim]);
+            if (!lib_contains(g.axis[dim].ghost_lower, g.axis[dim].ghost_upper, q[dim])) {
+                return T(-1);  // "position lies outside the interpolation domain"
+            }
+        }
+        lib_sample<kLibBasis, kLibBasisStride>(g, L.basis, q[0], q[1], v);
     }
 
     const T p_in = static_cast<T>(s.p[i]);
@@ -346,7 +369,7 @@ __device__ double lib_parker_terms(const LibParkerLaunch& L, size_t i, double* t
     for (int c = 0; c < 3; ++c) b2 += v[c] * v[c];
     const T bmag = M::sqrt(b2);
     if (!finite_positive(bmag)) {
-        return -2.0;  // "stochastic diffusion requires |B| > 0"
+        return T(-2);  // "stochastic diffusion requires |B| > 0"
     }
     const T ib = T(1) / bmag;
     T dir[3];
@@ -366,14 +389,14 @@ __device__ double lib_parker_terms(const LibParkerLaunch& L, size_t i, double* t
     const T kpar = v[15] * g13;
     const T kperp = v[16] * (L.constant_ratio ? g13 : roots.ninth);
     if (!finite_nonnegative(kpar) || !finite_nonnegative(kperp)) {
-        return -3.0;  // "diffusion coefficients must be finite and non-negative"
+        return T(-3);  // "diffusion coefficients must be finite and non-negative"
     }
     T keff[2];
 #pragma unroll
     for (int d = 0; d < 2; ++d) {
         keff[d] = kperp + (kpar - kperp) * dir[d] * dir[d];
         if (!finite_nonnegative(keff[d])) {
-            return -4.0;  // "projected diffusion coefficient is invalid"
+            return T(-4);  // "projected diffusion coefficient is invalid"
         }
     }
     const T divv = v[17];
@@ -391,46 +414,74 @@ __device__ double lib_parker_terms(const LibParkerLaunch& L, size_t i, double* t
     terms[kDirX] = dir[0];
     terms[kDirY] = dir[1];
     terms[kDirZ] = dir[2];
-    terms[kMomentum] = sizeof(T) == 8 ? static_cast<double>(p)
-                                      : (s.p[i] >= 0.0 ? s.p[i] : -s.p[i]);
+    if constexpr (!kMixed) terms[kMomentum] = p;
 
     // local_stable_time_step: prepare_physical_position again, then per-axis
     // cell widths at the physical cell index
-    T dmin = static_cast<T>(kLargeTimeStep);
-    T amin = static_cast<T>(kLargeTimeStep);
+    const T large = static_cast<T>(kLargeTimeStep);  // +inf in FP32
+    T dmin = large;
+    T amin = large;
 #pragma unroll
     for (int dim = 0; dim < 2; ++dim) {
         const LibAxis& a = g.axis[dim];
-        const double x = lib_wrap(a, pos[dim]);
-        if (!lib_contains(a.lower, a.upper, x)) {
-            return kLargeTimeStep;
+        T dx;
+        if (kMixed && !a.stored) {
+            dx = static_cast<T>(a.dx);
+        } else {
+            const double x = kMixed ? pos[dim] : lib_wrap(a, pos[dim]);
+            if (!lib_contains(a.lower, a.upper, x)) {
+                return large;
+            }
+            const double cell = static_cast<double>(lib_cell_index(a, x));
+            const double width =
+                __dsub_rn(lib_face(a, __dadd_rn(cell, 1.0)), lib_face(a, cell));
+            dx = static_cast<T>(fabs(__dmul_rn(1.0, width)));
         }
-        const double cell = static_cast<double>(lib_cell_index(a, x));
-        const double width = __dsub_rn(lib_face(a, __dadd_rn(cell, 1.0)), lib_face(a, cell));
-        const T dx = static_cast<T>(fabs(__dmul_rn(1.0, width)));
         if (!finite_positive(dx)) {
-            return -5.0;  // "local physical cell width must be positive"
+            return T(-5);  // "local physical cell width must be positive"
         }
-        T diffusion_dt = static_cast<T>(kLargeTimeStep);
+        T diffusion_dt = large;
         if (keff[dim] > T(0)) {
             const T limited = T(0.5) * dx;
             diffusion_dt = limited * limited / (T(2) * keff[dim]);
         }
         const T adv = M::abs(total[dim]);
-        T advection_dt = static_cast<T>(kLargeTimeStep);
+        T advection_dt = large;
         if (adv > T(0)) {
             advection_dt = T(1) * dx / adv;
         }
         dmin = diffusion_dt < dmin ? diffusion_dt : dmin;
         amin = advection_dt < amin ? advection_dt : amin;
     }
-    T mdt = static_cast<T>(kLargeTimeStep);
+    T mdt = large;
     const T dm = M::abs(divv);
     if (dm > T(0)) {
         mdt = T(3) * T(1) / dm;
     }
     const T da = dmin < amin ? dmin : amin;
-    return static_cast<double>(da < mdt ? da : mdt);
+    return da < mdt ? da : mdt;
+}
+
+// The block's minimum of the local dt bounds to the global minimum: one
+// atomic per block on the bit pattern of a positive double (exact and order
+// independent); an FP32 bound of +inf (no limiter) is the reference's large
+// step.
+template <typename T>
+__device__ __forceinline__ void block_min_to_global(T local, unsigned long long* min_bits) {
+    for (int off = 16; off > 0; off >>= 1) {
+        const T o = __shfl_down_sync(0xffffffffu, local, off);
+        local = o < local ? o : local;
+    }
+    __shared__ T warp_min[8];
+    if ((threadIdx.x & 31u) == 0u) warp_min[threadIdx.x >> 5] = local;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        T m = warp_min[0];
+        for (int k = 1; k < static_cast<int>(blockDim.x >> 5); ++k) m = warp_min[k] < m ? warp_min[k] : m;
+        const double md = isinf(m) ? kLargeTimeStep : static_cast<double>(m);
+        // positive doubles order like their bit patterns
+        atomicMin(min_bits, static_cast<unsigned long long>(__double_as_longlong(md)));
+    }
 }
 
 __device__ __forceinline__ void record_error(int* error, int code, uint32_t index,
@@ -443,7 +494,8 @@ __device__ __forceinline__ void record_error(int* error, int code, uint32_t inde
 // Pass 1: boundary conditions, terms, local dt -> global min (bit pattern).
 template <typename T>
 __global__ void __launch_bounds__(256) lib_parker_terms_kernel(const LibParkerLaunch L) {
-    double local = kLargeTimeStep;
+    T local = static_cast<T>(kLargeTimeStep);
+    T* terms = reinterpret_cast<T*>(L.terms);
     const bool stopped = *L.error != 0;  // an earlier step of a replayed sequence failed
     for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
          !stopped && i < L.count; i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
@@ -453,28 +505,15 @@ __global__ void __launch_bounds__(256) lib_parker_terms_kernel(const LibParkerLa
         if (L.apply_boundary && !lib_boundary(L.grid, L.sys, i)) {
             continue;
         }
-        const double dt = lib_parker_terms<T>(L, i, L.terms + i * kLibTermCount);
-        if (dt < 0.0) {
+        const T dt = lib_parker_terms<T>(L, i, terms + i * kLibTermCount);
+        if (dt < T(0)) {
             record_error(L.error, static_cast<int>(-dt), static_cast<uint32_t>(i),
                          L.error_index);
             continue;
         }
         local = dt < local ? dt : local;
     }
-    // warp then block minimum, one atomic per block
-    for (int off = 16; off > 0; off >>= 1) {
-        const double o = __shfl_down_sync(0xffffffffu, local, off);
-        local = o < local ? o : local;
-    }
-    __shared__ double warp_min[8];
-    if ((threadIdx.x & 31u) == 0u) warp_min[threadIdx.x >> 5] = local;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double m = warp_min[0];
-        for (int k = 1; k < static_cast<int>(blockDim.x >> 5); ++k) m = warp_min[k] < m ? warp_min[k] : m;
-        // positive doubles order like their bit patterns
-        atomicMin(L.min_bits, static_cast<unsigned long long>(__double_as_longlong(m)));
-    }
+    block_min_to_global(local, L.min_bits);
 }
 
 // Box-Muller pair from two stream draws (u1 = 1 - draw, u2 = draw): normals
@@ -525,43 +564,75 @@ __global__ void __launch_bounds__(256) lib_parker_advance_kernel(const LibParker
         if (i >= L.count || s.status[i] != 0) {
             continue;
         }
-        const double* t = L.terms + i * kLibTermCount;
-        double inc[2] = {0.0, 0.0};
-        if (L.stochastic) {
-            const uint32_t index = static_cast<uint32_t>(i);
-            double2 n01, n23;
-            if (L.noise != nullptr) {
-                n01 = make_double2(L.noise[i], L.noise[L.count + i]);
-                n23 = make_double2(L.noise[2 * L.count + i], L.noise[3 * L.count + i]);
-            } else {
-                n01 = lib_normal_pair<T>(L.key, 0u, index, L.frame);
-                n23 = lib_normal_pair<T>(L.key, 1u, index, L.frame);
+        const T* t = reinterpret_cast<const T*>(L.terms) + i * kLibTermCount;
+        if constexpr (sizeof(T) == 8) {
+            double inc[2] = {0.0, 0.0};
+            if (L.stochastic) {
+                const uint32_t index = static_cast<uint32_t>(i);
+                double2 n01, n23;
+                if (L.noise != nullptr) {
+                    n01 = make_double2(L.noise[i], L.noise[L.count + i]);
+                    n23 = make_double2(L.noise[2 * L.count + i], L.noise[3 * L.count + i]);
+                } else {
+                    n01 = lib_normal_pair<double>(L.key, 0u, index, L.frame);
+                    n23 = lib_normal_pair<double>(L.key, 1u, index, L.frame);
+                }
+                const double gv[3] = {n01.x, n01.y, n23.x};
+                double iso = 0.0;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) iso += gv[c] * t[kDirX + c];
+                const double pg = n23.y;
+                const double kperp = t[kKappaPerp];
+                const double kpar = t[kKappaPar];
+                const double perp_scale = kperp > 0.0 ? sqrt(2.0 * kperp * dt) : 0.0;
+                const double par_scale = kpar > 0.0 ? sqrt(2.0 * kpar * dt) : 0.0;
+                const double replacement = par_scale * pg - perp_scale * iso;
+#pragma unroll
+                for (int c = 0; c < 2; ++c) {
+                    inc[c] = perp_scale * gv[c] + replacement * t[kDirX + c];
+                }
             }
-            const T tdt = static_cast<T>(dt);
-            const T gv[3] = {static_cast<T>(n01.x), static_cast<T>(n01.y), static_cast<T>(n23.x)};
-            const T d[3] = {static_cast<T>(t[kDirX]), static_cast<T>(t[kDirY]),
-                            static_cast<T>(t[kDirZ])};
-            T iso = T(0);
-#pragma unroll
-            for (int c = 0; c < 3; ++c) iso += gv[c] * d[c];
-            const T pg = static_cast<T>(n23.y);
-            const T kperp = static_cast<T>(t[kKappaPerp]);
-            const T kpar = static_cast<T>(t[kKappaPar]);
-            const T perp_scale = kperp > T(0) ? LibMath<T>::sqrt(T(2) * kperp * tdt) : T(0);
-            const T par_scale = kpar > T(0) ? LibMath<T>::sqrt(T(2) * kpar * tdt) : T(0);
-            const T replacement = par_scale * pg - perp_scale * iso;
-#pragma unroll
-            for (int c = 0; c < 2; ++c) inc[c] = perp_scale * gv[c] + replacement * d[c];
-        }
-        if (L.stochastic) {
-            s.x[i] += dt * t[kRateX] + inc[0] * 1.0;
-            s.y[i] += dt * t[kRateY] + inc[1] * 1.0;
+            if (L.stochastic) {
+                s.x[i] += dt * t[kRateX] + inc[0] * 1.0;
+                s.y[i] += dt * t[kRateY] + inc[1] * 1.0;
+            } else {
+                s.x[i] += dt * t[kRateX];
+                s.y[i] += dt * t[kRateY];
+            }
+            const double updated = t[kMomentum] + dt * t[kMomentumRate];
+            s.p[i] = updated > 0.0 ? updated : 0.0;
         } else {
-            s.x[i] += dt * t[kRateX];
-            s.y[i] += dt * t[kRateY];
+            // the increments in FP32, added to the FP64 state
+            const float tdt = static_cast<float>(dt);
+            float inc[2] = {tdt * t[kRateX], tdt * t[kRateY]};
+            if (L.stochastic) {
+                const uint32_t index = static_cast<uint32_t>(i);
+                double2 n01, n23;
+                if (L.noise != nullptr) {
+                    n01 = make_double2(L.noise[i], L.noise[L.count + i]);
+                    n23 = make_double2(L.noise[2 * L.count + i], L.noise[3 * L.count + i]);
+                } else {
+                    n01 = lib_normal_pair<float>(L.key, 0u, index, L.frame);
+                    n23 = lib_normal_pair<float>(L.key, 1u, index, L.frame);
+                }
+                const float gv[3] = {static_cast<float>(n01.x), static_cast<float>(n01.y),
+                                     static_cast<float>(n23.x)};
+                const float iso = gv[0] * t[kDirX] + gv[1] * t[kDirY] + gv[2] * t[kDirZ];
+                const float kperp = t[kKappaPerp];
+                const float kpar = t[kKappaPar];
+                const float perp_scale = kperp > 0.0f ? sqrtf(2.0f * kperp * tdt) : 0.0f;
+                const float par_scale = kpar > 0.0f ? sqrtf(2.0f * kpar * tdt) : 0.0f;
+                const float replacement = par_scale * static_cast<float>(n23.y) - perp_scale * iso;
+                inc[0] += perp_scale * gv[0] + replacement * t[kDirX];
+                inc[1] += perp_scale * gv[1] + replacement * t[kDirY];
+            }
+            s.x[i] += static_cast<double>(inc[0]);
+            s.y[i] += static_cast<double>(inc[1]);
+            // the momentum base is the FP64 state, as the terms pass read it
+            const double base = s.p[i] >= 0.0 ? s.p[i] : -s.p[i];
+            const double updated = base + static_cast<double>(tdt * t[kMomentumRate]);
+            s.p[i] = updated > 0.0 ? updated : 0.0;
         }
-        const double updated = t[kMomentum] + dt * t[kMomentumRate];
-        s.p[i] = updated > 0.0 ? updated : 0.0;
         lib_boundary(L.grid, s, i);
     }
 }
@@ -640,7 +711,7 @@ struct PitchSetup {
 };
 
 template <typename T>
-__device__ PitchSetup<T> focus_pitch_setup(const LibFocusLaunch& L, const double* t) {
+__device__ PitchSetup<T> focus_pitch_setup(const LibFocusLaunch& L, const T* t) {
     PitchSetup<T> q{};
     q.speed = static_cast<T>(t[fSpeed]);
     if (q.speed <= T(0)) {
@@ -674,7 +745,7 @@ __device__ PitchSetup<T> focus_pitch_setup(const LibFocusLaunch& L, const double
 // evaluate_pitch_angle_at_mu with the slab-QLT evaluate_pitch_angle_scattering
 // (LegencyModel.hpp:539-693) at one trial cosine.
 template <typename T>
-__device__ PitchRates<T> focus_pitch(const LibFocusLaunch& L, const double* t,
+__device__ PitchRates<T> focus_pitch(const LibFocusLaunch& L, const T* t,
                                      const PitchSetup<T>& q, T trial, int* error) {
     PitchRates<T> r{T(0), T(0), T(0), T(0)};
     const T mu = focus_reflect(trial, static_cast<T>(L.max_mu), error);
@@ -718,8 +789,9 @@ __device__ PitchRates<T> focus_pitch(const LibFocusLaunch& L, const double* t,
 // arithmetic; T = float: the mixed step (FP32 basis, terms and closure; the
 // positions, boundary and cell-width decisions and the momentum stay FP64).
 template <typename T>
-__device__ double focus_terms(const LibFocusLaunch& L, size_t i, double* t, int* error) {
+__device__ T focus_terms(const LibFocusLaunch& L, size_t i, T* t, int* error) {
     using M = LibMath<T>;
+    constexpr bool kMixed = sizeof(T) == 4;
     const LibGrid& g = L.grid;
     const SystemArrays& s = L.sys;
     double pos[2] = {s.x[i], s.y[i]};
@@ -727,26 +799,26 @@ __device__ double focus_terms(const LibFocusLaunch& L, size_t i, double* t, int*
     for (int dim = 0; dim < 2; ++dim) {
         pos[dim] = lib_wrap(g.axis[dim], pos[dim]);
         if (!lib_contains(g.axis[dim].lower, g.axis[dim].upper, pos[dim])) {
-            for (int k = 0; k < kFocusTermCount; ++k) t[k] = 0.0;
-            return 0.0;
-        }
-    }
-    double q[2];
-#pragma unroll
-    for (int dim = 0; dim < 2; ++dim) {
-        q[dim] = lib_wrap(g.axis[dim], pos[dim]);
-        if (!lib_contains(g.axis[dim].ghost_lower, g.axis[dim].ghost_upper, q[dim])) {
-            set_error(error, 1);
-            return -1.0;
+            for (int k = 0; k < kFocusTermCount; ++k) t[k] = T(0);
+            return T(0);
         }
     }
     T v[kFocusBasis];
-    if constexpr (sizeof(T) == 8) {
-        lib_sample<kFocusBasis, kFocusBasisStride>(g, L.basis, q[0], q[1], v);
+    if constexpr (kMixed) {
+        // a wrapped physical position is its own wrap and inside the ghosts
+        lib_sample<kFocusBasis, kFocusBasisStrideF32>(g, L.basis_f32, pos[0], pos[1], v);
     } else {
-        lib_sample<kFocusBasis, kFocusBasisStrideF32>(g, L.basis_f32, q[0], q[1], v);
+        double q[2];
+#pragma unroll
+        for (int dim = 0; dim < 2; ++dim) {
+            q[dim] = lib_wrap(g.axis[dim], pos[dim]);
+            if (!lib_contains(g.axis[dim].ghost_lower, g.axis[dim].ghost_upper, q[dim])) {
+                set_error(error, 1);
+                return T(-1);
+            }
+        }
+        lib_sample<kFocusBasis, kFocusBasisStride>(g, L.basis, q[0], q[1], v);
     }
-    const double p_state = s.p[i] >= 0.0 ? s.p[i] : -s.p[i];
     const T p_in = static_cast<T>(s.p[i]);
     const T p = p_in >= T(0) ? p_in : -p_in;
     const T mu = focus_reflect(static_cast<T>(s.mu[i]), static_cast<T>(L.max_mu), error);
@@ -756,7 +828,7 @@ __device__ double focus_terms(const LibFocusLaunch& L, size_t i, double* t, int*
     const T bmag = v[18];
     if (!finite_positive(bmag)) {
         set_error(error, 9);  // "focused transport requires |B| > 0"
-        return -1.0;
+        return T(-1);
     }
     T s2 = T(0);
 #pragma unroll
@@ -764,7 +836,7 @@ __device__ double focus_terms(const LibFocusLaunch& L, size_t i, double* t, int*
     const T smag = M::sqrt(s2);
     if (!finite_positive(smag)) {
         set_error(error, 10);  // "interpolated magnetic direction is invalid"
-        return -1.0;
+        return T(-1);
     }
     const T inv = T(1) / smag;
     T dir[3];
@@ -776,7 +848,7 @@ __device__ double focus_terms(const LibFocusLaunch& L, size_t i, double* t, int*
     const T kperp = v[20] * perp_factor;
     if (!finite_nonnegative(kpar) || !finite_nonnegative(kperp)) {
         set_error(error, 11);  // "diffusion coefficients must be finite and non-negative"
-        return -1.0;
+        return T(-1);
     }
     const T mu2 = mu * mu;
     const T gdf = T(0.5) * (T(1) - mu2);
@@ -802,7 +874,7 @@ __device__ double focus_terms(const LibFocusLaunch& L, size_t i, double* t, int*
     t[fDirX] = dir[0];
     t[fDirY] = dir[1];
     t[fDirZ] = dir[2];
-    t[fMomentum] = sizeof(T) == 8 ? static_cast<double>(p) : p_state;
+    if constexpr (!kMixed) t[fMomentum] = p;
     t[fMu] = mu;
     t[fSpeed] = speed;
     t[fGamma] = gamma;
@@ -822,78 +894,75 @@ __device__ double focus_terms(const LibFocusLaunch& L, size_t i, double* t, int*
     t[fMomentumRate] = momentum_rate;
     const PitchRates<T> pitch = focus_pitch<T>(L, t, focus_pitch_setup<T>(L, t), mu, error);
 
-    T dmin = static_cast<T>(kLargeTimeStep);
-    T amin = static_cast<T>(kLargeTimeStep);
+    const T large = static_cast<T>(kLargeTimeStep);  // +inf in FP32
+    T dmin = large;
+    T amin = large;
 #pragma unroll
     for (int dim = 0; dim < 2; ++dim) {
         const LibAxis& a = g.axis[dim];
-        const double x = lib_wrap(a, pos[dim]);
-        if (!lib_contains(a.lower, a.upper, x)) {
-            return kLargeTimeStep;
+        T dx;
+        if (kMixed && !a.stored) {
+            dx = static_cast<T>(a.dx);
+        } else {
+            const double x = kMixed ? pos[dim] : lib_wrap(a, pos[dim]);
+            if (!lib_contains(a.lower, a.upper, x)) {
+                return large;
+            }
+            const double cell = static_cast<double>(lib_cell_index(a, x));
+            const double width =
+                __dsub_rn(lib_face(a, __dadd_rn(cell, 1.0)), lib_face(a, cell));
+            dx = static_cast<T>(fabs(__dmul_rn(1.0, width)));
         }
-        const double cell = static_cast<double>(lib_cell_index(a, x));
-        const double width = __dsub_rn(lib_face(a, __dadd_rn(cell, 1.0)), lib_face(a, cell));
-        const T dx = static_cast<T>(fabs(__dmul_rn(1.0, width)));
         if (!finite_positive(dx)) {
             set_error(error, 5);
-            return -1.0;
+            return T(-1);
         }
-        T diffusion_dt = static_cast<T>(kLargeTimeStep);
+        T diffusion_dt = large;
         if (keff[dim] > T(0)) {
             const T limited = T(0.5) * dx;
             diffusion_dt = limited * limited / (T(2) * keff[dim]);
         }
         const T adv = M::abs(total[dim]);
-        T advection_dt = static_cast<T>(kLargeTimeStep);
+        T advection_dt = large;
         if (adv > T(0)) advection_dt = T(1) * dx / adv;
         dmin = diffusion_dt < dmin ? diffusion_dt : dmin;
         amin = advection_dt < amin ? advection_dt : amin;
     }
-    T mdt = static_cast<T>(kLargeTimeStep);
+    T mdt = large;
     const T mrate = M::abs(momentum_rate);
     if (p > T(0) && mrate > T(0)) mdt = T(1) * p / mrate;
-    T padv = static_cast<T>(kLargeTimeStep);
+    T padv = large;
     const T murate = M::abs(pitch.rate);
     if (murate > T(0)) padv = T(10) * T(0.1) / murate;
-    T pdiff = static_cast<T>(kLargeTimeStep);
+    T pdiff = large;
     if (pitch.D > T(0)) pdiff = T(10) * T(0.1) * T(0.1) / (T(2) * pitch.D);
-    T pbal = static_cast<T>(kLargeTimeStep);
+    T pbal = large;
     if (pitch.D > T(0) && murate > T(0)) pbal = T(10) * T(2) * pitch.D / (murate * murate);
     const T a1 = dmin < amin ? dmin : amin;
     const T a2 = a1 < mdt ? a1 : mdt;
     const T b1 = pdiff < pbal ? pdiff : pbal;
     const T b2 = padv < b1 ? padv : b1;
-    return static_cast<double>(a2 < b2 ? a2 : b2);
+    return a2 < b2 ? a2 : b2;
 }
 
 template <typename T>
 __global__ void __launch_bounds__(256) focus_terms_kernel(const LibFocusLaunch L) {
-    double local = kLargeTimeStep;
+    T local = static_cast<T>(kLargeTimeStep);
+    T* terms = reinterpret_cast<T*>(L.terms);
     const bool stopped = *L.error != 0;
     for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
          !stopped && i < L.count; i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
         if (L.sys.status[i] != 0) continue;
         if (L.apply_boundary && !lib_boundary(L.grid, L.sys, i)) continue;
         int err = 0;
-        const double dt = focus_terms<T>(L, i, L.terms + i * kFocusTermCount, &err);
+        const T dt = focus_terms<T>(L, i, terms + i * kFocusTermCount, &err);
         if (err != 0) {
             record_error(L.error, err, static_cast<uint32_t>(i), L.error_index);
             continue;
         }
         local = dt < local ? dt : local;
     }
-    for (int off = 16; off > 0; off >>= 1) {
-        const double o = __shfl_down_sync(0xffffffffu, local, off);
-        local = o < local ? o : local;
-    }
-    __shared__ double warp_min[8];
-    if ((threadIdx.x & 31u) == 0u) warp_min[threadIdx.x >> 5] = local;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double m = warp_min[0];
-        for (int k = 1; k < static_cast<int>(blockDim.x >> 5); ++k) m = warp_min[k] < m ? warp_min[k] : m;
-        atomicMin(L.min_bits, static_cast<unsigned long long>(__double_as_longlong(m)));
-    }
+    block_min_to_global(local, L.min_bits);
 }
 
 // advance_*_with_packed_interpolator (FocusSolver.hpp:1580-1637) with the
@@ -916,8 +985,8 @@ __global__ void __launch_bounds__(256) focus_advance_kernel(const LibFocusLaunch
             s.prev_y[i] = s.y[i];
         }
         if (i >= L.count || s.status[i] != 0) continue;
-        const double* t = L.terms + i * kFocusTermCount;
-        double inc[2] = {0.0, 0.0};
+        const T* t = reinterpret_cast<const T*>(L.terms) + i * kFocusTermCount;
+        T inc[2] = {T(0), T(0)};
         T pitch_normal = T(0);
         const T tdt = static_cast<T>(dt);
         if (L.stochastic) {
@@ -942,10 +1011,20 @@ __global__ void __launch_bounds__(256) focus_advance_kernel(const LibFocusLaunch
             for (int c = 0; c < 2; ++c) inc[c] = scale * (gv[c] - parallel * d[c]);
             pitch_normal = static_cast<T>(n23.y);
         }
-        s.x[i] += dt * t[fRateX] + inc[0] * 1.0;
-        s.y[i] += dt * t[fRateY] + inc[1] * 1.0;
-        const double updated = t[fMomentum] + dt * t[fMomentumRate];
-        s.p[i] = updated > 0.0 ? updated : 0.0;
+        if constexpr (sizeof(T) == 8) {
+            s.x[i] += dt * t[fRateX] + inc[0] * 1.0;
+            s.y[i] += dt * t[fRateY] + inc[1] * 1.0;
+            const double updated = t[fMomentum] + dt * t[fMomentumRate];
+            s.p[i] = updated > 0.0 ? updated : 0.0;
+        } else {
+            // the increments in FP32, added to the FP64 state; the momentum
+            // base is the FP64 state, as the terms pass read it
+            s.x[i] += static_cast<double>(tdt * t[fRateX] + inc[0]);
+            s.y[i] += static_cast<double>(tdt * t[fRateY] + inc[1]);
+            const double base = s.p[i] >= 0.0 ? s.p[i] : -s.p[i];
+            const double updated = base + static_cast<double>(tdt * t[fMomentumRate]);
+            s.p[i] = updated > 0.0 ? updated : 0.0;
+        }
         int err = 0;
         const T max_mu = static_cast<T>(L.max_mu);
         const T initial = focus_reflect(static_cast<T>(t[fMu]), max_mu, &err);
