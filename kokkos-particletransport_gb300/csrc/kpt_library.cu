@@ -141,14 +141,42 @@ __device__ __forceinline__ void lib_stencil(const LibAxis& a, double x, int& lo,
     stencil_from_logical(a, logical, lo, hi, w);
 }
 
-// The mixed step's stencil: on a uniform axis the logical index comes from
-// one FP64 multiply-add by 1/dx instead of the reference's division (the
-// FP64 pipe is the scarce one here); stored axes keep their bisection.
+// The mixed step's stencil: on a uniform axis the logical index is the FP32
+// product of the FP64 offset x - x0 and 1/dx (its rounding, ~1e-7 of a
+// cell, moves the sample by less than the FP32 table's own precision; the
+// bilinear weights are continuous across cells, so a cell index that differs
+// from the FP64 one near a cell face gives the same value); stored axes keep
+// their FP64 bisection.
 __device__ __forceinline__ void lib_stencil_mixed(const LibAxis& a, double x, int& lo, int& hi,
-                                                  double& w) {
-    const double logical = a.stored ? stored_grid_index(a, x, false)
-                                    : fma(x - a.x0, a.inv_dx, -0.5);
-    stencil_from_logical(a, logical, lo, hi, w);
+                                                  float& w) {
+    if (a.stored) {
+        double wd;
+        stencil_from_logical(a, stored_grid_index(a, x, false), lo, hi, wd);
+        w = static_cast<float>(wd);
+        return;
+    }
+    const float logical =
+        fmaf(static_cast<float>(x - a.x0), static_cast<float>(a.inv_dx), -0.5f);
+    const int lower_bound = -2;
+    const int upper_bound = a.n + 1;
+    if (logical <= static_cast<float>(lower_bound)) {
+        lo = hi = lower_bound;
+        w = 0.0f;
+        return;
+    }
+    if (logical >= static_cast<float>(upper_bound)) {
+        lo = hi = upper_bound;
+        w = 0.0f;
+        return;
+    }
+    const float cell = floorf(logical);
+    lo = static_cast<int>(cell);
+    hi = lo + 1;
+    w = logical - cell;
+    if (hi > upper_bound) {
+        lo = hi = upper_bound;
+        w = 0.0f;
+    }
 }
 
 // FieldInterpolator's compute_axis_stencil on a logical index.
@@ -218,7 +246,7 @@ __device__ __forceinline__ void lib_sample(const LibGrid& g, const float* __rest
                                            double x, double y, float (&out)[C]) {
     static_assert(STRIDE % 4 == 0 && STRIDE >= C, "FP32 rows hold whole 16-byte chunks");
     int lo[2], hi[2];
-    double w[2];
+    float w[2];
     lib_stencil_mixed(g.axis[0], x, lo[0], hi[0], w[0]);
     lib_stencil_mixed(g.axis[1], y, lo[1], hi[1], w[1]);
 #pragma unroll
@@ -227,9 +255,7 @@ __device__ __forceinline__ void lib_sample(const LibGrid& g, const float* __rest
     for (int corner = 0; corner < 4; ++corner) {
         const bool ux = (corner & 1) != 0;
         const bool uy = (corner & 2) != 0;
-        const float wx = static_cast<float>(w[0]);
-        const float wy = static_cast<float>(w[1]);
-        const float weight = (ux ? wx : 1.0f - wx) * (uy ? wy : 1.0f - wy);
+        const float weight = (ux ? w[0] : 1.0f - w[0]) * (uy ? w[1] : 1.0f - w[1]);
         const int i = (ux ? hi[0] : lo[0]) + 2;
         const int j = (uy ? hi[1] : lo[1]) + 2;
         const float4* row =
@@ -313,6 +339,49 @@ __device__ __forceinline__ bool lib_boundary(const LibGrid& g, const SystemArray
     return !escaped;
 }
 
+// The mixed step's boundary pass: a coordinate already inside [lower, upper)
+// of a periodic axis is its own wrap, so only coordinates outside take the
+// reference's floor formula (two FP64 compares for most particles instead of
+// the full wrap; GB300's FP64 pipe is the scarce one).
+__device__ __forceinline__ bool lib_boundary_mixed(const LibGrid& g, const SystemArrays& s,
+                                                   size_t i) {
+    bool escaped = false;
+#pragma unroll
+    for (int dim = 0; dim < 2; ++dim) {
+        const LibAxis& a = g.axis[dim];
+        double* pos = dim == 0 ? s.x : s.y;
+        const double x = pos[i];
+        const bool inside = x >= a.lower && x < a.upper;
+        if (a.periodic) {
+            if (!inside) {
+                const double wrapped = lib_wrap(a, x);
+                const double shift = wrapped - x;
+                pos[i] = wrapped;
+                double* prev = dim == 0 ? s.prev_x : s.prev_y;
+                double* prevstep = dim == 0 ? s.prevstep_x : s.prevstep_y;
+                prev[i] = prev[i] + shift;
+                prevstep[i] = prevstep[i] + shift;
+            }
+        } else if (!inside && !lib_contains(a.lower, a.upper, x)) {
+            escaped = true;
+        }
+    }
+    if (escaped) {
+        s.status[i] = 1;
+    }
+    return !escaped;
+}
+
+template <typename T>
+__device__ __forceinline__ bool lib_boundary_t(const LibGrid& g, const SystemArrays& s,
+                                               size_t i) {
+    if constexpr (sizeof(T) == 4) {
+        return lib_boundary_mixed(g, s, i);
+    } else {
+        return lib_boundary(g, s, i);
+    }
+}
+
 // Kept per-particle terms (one row per particle, kLibTermCount doubles).
 enum TermSlot {
     kRateX = 0, kRateY, kMomentumRate, kKappaPar, kKappaPerp, kDirX, kDirY, kDirZ, kMomentum
@@ -335,8 +404,11 @@ __device__ T lib_parker_terms(const LibParkerLaunch& L, size_t i, T* terms) {
     // prepare_physical_position (:620-633)
 #pragma unroll
     for (int dim = 0; dim < 2; ++dim) {
-        pos[dim] = lib_wrap(g.axis[dim], pos[dim]);
-        if (!lib_contains(g.axis[dim].lower, g.axis[dim].upper, pos[dim])) {
+        const LibAxis& a = g.axis[dim];
+        if (!kMixed || !(pos[dim] >= a.lower && pos[dim] < a.upper)) {
+            pos[dim] = lib_wrap(a, pos[dim]);
+        }
+        if (!lib_contains(a.lower, a.upper, pos[dim])) {
             // the reference's empty terms: zero rates, zero time step
             for (int k = 0; k < kLibTermCount; ++k) terms[k] = T(0);
             return T(0);
@@ -502,7 +574,7 @@ __global__ void __launch_bounds__(256) lib_parker_terms_kernel(const LibParkerLa
         if (L.sys.status[i] != 0) {
             continue;
         }
-        if (L.apply_boundary && !lib_boundary(L.grid, L.sys, i)) {
+        if (L.apply_boundary && !lib_boundary_t<T>(L.grid, L.sys, i)) {
             continue;
         }
         const T dt = lib_parker_terms<T>(L, i, terms + i * kLibTermCount);
@@ -521,8 +593,13 @@ __global__ void __launch_bounds__(256) lib_parker_terms_kernel(const LibParkerLa
 // block m, as the shim pool's normal() hands them out.  The FP32 pair takes
 // the high word of each draw (24 bits), so it tracks the FP64 pair.
 template <typename T>
-__device__ __forceinline__ double2 lib_normal_pair(uint2 key, uint32_t block, uint32_t index,
-                                                   uint32_t frame) {
+struct NormalPair {
+    T x, y;
+};
+
+template <typename T>
+__device__ __forceinline__ NormalPair<T> lib_normal_pair(uint2 key, uint32_t block,
+                                                         uint32_t index, uint32_t frame) {
     const uint4 r = philox4x32_10(make_uint4(block, index, frame, kTagLibrary), key);
     if constexpr (sizeof(T) == 8) {
         const double u1 = 1.0 - u01_f64(r.x, r.y);
@@ -530,14 +607,30 @@ __device__ __forceinline__ double2 lib_normal_pair(uint2 key, uint32_t block, ui
         const double radius = sqrt(-2.0 * log(u1));
         double s, c;
         sincos(6.283185307179586 * u2, &s, &c);
-        return make_double2(radius * c, radius * s);
+        return NormalPair<T>{radius * c, radius * s};
     } else {
         const float u1 = 1.0f - u01_f32(r.y);
         const float u2 = u01_f32(r.w);
         const float radius = sqrtf(-2.0f * logf(u1));
         float s, c;
         sincosf(6.2831853071795865f * u2, &s, &c);
-        return make_double2(radius * c, radius * s);
+        return NormalPair<T>{radius * c, radius * s};
+    }
+}
+
+// The four normals of a particle's step: the keyed stream's two pairs, or
+// the caller's buffer [4][count].
+template <typename T>
+__device__ __forceinline__ void step_normals(uint2 key, uint32_t frame, const double* noise,
+                                             uint64_t count, uint64_t i, NormalPair<T>& n01,
+                                             NormalPair<T>& n23) {
+    if (noise != nullptr) {
+        n01 = NormalPair<T>{static_cast<T>(noise[i]), static_cast<T>(noise[count + i])};
+        n23 = NormalPair<T>{static_cast<T>(noise[2 * count + i]),
+                            static_cast<T>(noise[3 * count + i])};
+    } else {
+        n01 = lib_normal_pair<T>(key, 0u, static_cast<uint32_t>(i), frame);
+        n23 = lib_normal_pair<T>(key, 1u, static_cast<uint32_t>(i), frame);
     }
 }
 
@@ -568,15 +661,8 @@ __global__ void __launch_bounds__(256) lib_parker_advance_kernel(const LibParker
         if constexpr (sizeof(T) == 8) {
             double inc[2] = {0.0, 0.0};
             if (L.stochastic) {
-                const uint32_t index = static_cast<uint32_t>(i);
-                double2 n01, n23;
-                if (L.noise != nullptr) {
-                    n01 = make_double2(L.noise[i], L.noise[L.count + i]);
-                    n23 = make_double2(L.noise[2 * L.count + i], L.noise[3 * L.count + i]);
-                } else {
-                    n01 = lib_normal_pair<double>(L.key, 0u, index, L.frame);
-                    n23 = lib_normal_pair<double>(L.key, 1u, index, L.frame);
-                }
+                NormalPair<double> n01, n23;
+                step_normals<double>(L.key, L.frame, L.noise, L.count, i, n01, n23);
                 const double gv[3] = {n01.x, n01.y, n23.x};
                 double iso = 0.0;
 #pragma unroll
@@ -606,23 +692,15 @@ __global__ void __launch_bounds__(256) lib_parker_advance_kernel(const LibParker
             const float tdt = static_cast<float>(dt);
             float inc[2] = {tdt * t[kRateX], tdt * t[kRateY]};
             if (L.stochastic) {
-                const uint32_t index = static_cast<uint32_t>(i);
-                double2 n01, n23;
-                if (L.noise != nullptr) {
-                    n01 = make_double2(L.noise[i], L.noise[L.count + i]);
-                    n23 = make_double2(L.noise[2 * L.count + i], L.noise[3 * L.count + i]);
-                } else {
-                    n01 = lib_normal_pair<float>(L.key, 0u, index, L.frame);
-                    n23 = lib_normal_pair<float>(L.key, 1u, index, L.frame);
-                }
-                const float gv[3] = {static_cast<float>(n01.x), static_cast<float>(n01.y),
-                                     static_cast<float>(n23.x)};
+                NormalPair<float> n01, n23;
+                step_normals<float>(L.key, L.frame, L.noise, L.count, i, n01, n23);
+                const float gv[3] = {n01.x, n01.y, n23.x};
                 const float iso = gv[0] * t[kDirX] + gv[1] * t[kDirY] + gv[2] * t[kDirZ];
                 const float kperp = t[kKappaPerp];
                 const float kpar = t[kKappaPar];
                 const float perp_scale = kperp > 0.0f ? sqrtf(2.0f * kperp * tdt) : 0.0f;
                 const float par_scale = kpar > 0.0f ? sqrtf(2.0f * kpar * tdt) : 0.0f;
-                const float replacement = par_scale * static_cast<float>(n23.y) - perp_scale * iso;
+                const float replacement = par_scale * n23.y - perp_scale * iso;
                 inc[0] += perp_scale * gv[0] + replacement * t[kDirX];
                 inc[1] += perp_scale * gv[1] + replacement * t[kDirY];
             }
@@ -633,7 +711,7 @@ __global__ void __launch_bounds__(256) lib_parker_advance_kernel(const LibParker
             const double updated = base + static_cast<double>(tdt * t[kMomentumRate]);
             s.p[i] = updated > 0.0 ? updated : 0.0;
         }
-        lib_boundary(L.grid, s, i);
+        lib_boundary_t<T>(L.grid, s, i);
     }
 }
 
@@ -797,8 +875,11 @@ __device__ T focus_terms(const LibFocusLaunch& L, size_t i, T* t, int* error) {
     double pos[2] = {s.x[i], s.y[i]};
 #pragma unroll
     for (int dim = 0; dim < 2; ++dim) {
-        pos[dim] = lib_wrap(g.axis[dim], pos[dim]);
-        if (!lib_contains(g.axis[dim].lower, g.axis[dim].upper, pos[dim])) {
+        const LibAxis& a = g.axis[dim];
+        if (!kMixed || !(pos[dim] >= a.lower && pos[dim] < a.upper)) {
+            pos[dim] = lib_wrap(a, pos[dim]);
+        }
+        if (!lib_contains(a.lower, a.upper, pos[dim])) {
             for (int k = 0; k < kFocusTermCount; ++k) t[k] = T(0);
             return T(0);
         }
@@ -953,7 +1034,7 @@ __global__ void __launch_bounds__(256) focus_terms_kernel(const LibFocusLaunch L
     for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
          !stopped && i < L.count; i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
         if (L.sys.status[i] != 0) continue;
-        if (L.apply_boundary && !lib_boundary(L.grid, L.sys, i)) continue;
+        if (L.apply_boundary && !lib_boundary_t<T>(L.grid, L.sys, i)) continue;
         int err = 0;
         const T dt = focus_terms<T>(L, i, terms + i * kFocusTermCount, &err);
         if (err != 0) {
@@ -990,16 +1071,9 @@ __global__ void __launch_bounds__(256) focus_advance_kernel(const LibFocusLaunch
         T pitch_normal = T(0);
         const T tdt = static_cast<T>(dt);
         if (L.stochastic) {
-            const uint32_t index = static_cast<uint32_t>(i);
-            double2 n01, n23;
-            if (L.noise != nullptr) {
-                n01 = make_double2(L.noise[i], L.noise[L.count + i]);
-                n23 = make_double2(L.noise[2 * L.count + i], L.noise[3 * L.count + i]);
-            } else {
-                n01 = lib_normal_pair<T>(L.key, 0u, index, L.frame);
-                n23 = lib_normal_pair<T>(L.key, 1u, index, L.frame);
-            }
-            const T gv[3] = {static_cast<T>(n01.x), static_cast<T>(n01.y), static_cast<T>(n23.x)};
+            NormalPair<T> n01, n23;
+            step_normals<T>(L.key, L.frame, L.noise, L.count, i, n01, n23);
+            const T gv[3] = {n01.x, n01.y, n23.x};
             const T d[3] = {static_cast<T>(t[fDirX]), static_cast<T>(t[fDirY]),
                             static_cast<T>(t[fDirZ])};
             T parallel = T(0);
@@ -1009,7 +1083,7 @@ __global__ void __launch_bounds__(256) focus_advance_kernel(const LibFocusLaunch
             const T scale = kperp > T(0) ? LibMath<T>::sqrt(T(2) * kperp * tdt) : T(0);
 #pragma unroll
             for (int c = 0; c < 2; ++c) inc[c] = scale * (gv[c] - parallel * d[c]);
-            pitch_normal = static_cast<T>(n23.y);
+            pitch_normal = n23.y;
         }
         if constexpr (sizeof(T) == 8) {
             s.x[i] += dt * t[fRateX] + inc[0] * 1.0;
@@ -1041,7 +1115,7 @@ __global__ void __launch_bounds__(256) focus_advance_kernel(const LibFocusLaunch
             continue;
         }
         s.mu[i] = trial;
-        lib_boundary(L.grid, s, i);
+        lib_boundary_t<T>(L.grid, s, i);
     }
 }
 

@@ -7,7 +7,7 @@ restatement is the reference here.
 
 * FP64: particle count, ids (order included), statuses and split levels bit
   for bit; positions and momenta within the 1e-10 parity bar; every
-  histogram identical.
+  histogram identical -- in storage order and in the CLI's tile order.
 * Mixed precision: the final momentum spectrum within 1 % L1 of the
   oracle's, chi-square p > 0.01.
 * Focused transport with the slab-QLT closure through the same loop (the
@@ -52,7 +52,7 @@ def _oracle_loop(oracle, binding, params, frames):
     return {k: v[:count] for k, v in ref.items()}, hists, splits
 
 
-def _gpu_loop(ctx, kpt, params, frames, precision):
+def _gpu_loop(ctx, kpt, params, frames, precision, order=None):
     settings = kpt.settings_from_dict(params)
     kind = kpt.TABLE_FOCUSED21 if params["focused"] else kpt.TABLE_PARKER16
     fields = [ctx.field(f, kind, precision) for f in frames]
@@ -60,6 +60,8 @@ def _gpu_loop(ctx, kpt, params, frames, precision):
     hists, splits = [], []
     for f in range(len(frames) - 1):
         ctx.inject(parts, fields[f], settings, REQUESTED, f, SEED, band=(-0.2, 0.2))
+        if order == "tiles":
+            ctx.sort(parts, fields[f], 8, 8)
         ctx.push_interval(parts, fields[f], fields[f + 1], settings, f, SEED)
         splits.append(ctx.split(parts, settings))
         if (f + 1) % 4 == 0:
@@ -77,9 +79,11 @@ def loop_reference(oracle, binding, fields_mod):
     return params, frames, _oracle_loop(oracle, binding, params, frames)
 
 
-def test_frame_loop_f64_matches_oracle(ctx, kpt, loop_reference):
+@pytest.mark.parametrize("order", [None, "tiles"])
+def test_frame_loop_f64_matches_oracle(ctx, kpt, loop_reference, order):
+    """The work order (storage order, or the CLI's tile order) changes nothing."""
     params, frames, (ref, ref_hists, ref_splits) = loop_reference
-    got, hists, splits = _gpu_loop(ctx, kpt, params, frames, kpt.PRECISION_F64)
+    got, hists, splits = _gpu_loop(ctx, kpt, params, frames, kpt.PRECISION_F64, order)
     assert sum(s for s, _ in ref_splits) > 0  # the ladder is exercised
     assert splits == ref_splits
     assert got["x"].size == ref["x"].size
