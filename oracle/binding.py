@@ -16,7 +16,11 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libkpt_oracle.so")
+# the same restatement on the C library's pow: the build timed as the CPU baseline
+ORACLE_LIBM_SO = os.path.join(HERE, "_build", "libkpt_oracle_libm.so")
 REF_SO = os.path.join(HERE, "_ref", "libkpt_ref.so")
+# the reference on the shim with the C library's pow (timing only)
+REF_LIBM_SO = os.path.join(HERE, "_ref", "libkpt_ref_libm.so")
 
 PARTICLE_FIELDS = ("x", "y", "p", "t", "dt", "w", "mu", "status", "level")
 DOUBLE_PARAMS = ("mhd_dt", "p0", "pmin", "pmax", "gamma_turb", "kpara0", "kperp_over_kpara",
@@ -114,9 +118,13 @@ def build_oracle() -> str:
 
 
 class Oracle:
-    """The C restatement (oracle/kpt_oracle.c)."""
+    """The C restatement (oracle/kpt_oracle.c).  libm_pow: the build on the C
+    library's pow (the timed CPU baseline) instead of the project pow (the
+    parity checker)."""
 
-    def __init__(self, path: str = ORACLE_SO):
+    def __init__(self, path: str = ORACLE_SO, libm_pow: bool = False):
+        if libm_pow and path == ORACLE_SO:
+            path = ORACLE_LIBM_SO
         if not os.path.exists(path):
             build_oracle()
         lib = ctypes.CDLL(path)
@@ -253,7 +261,9 @@ class Oracle:
 class ReferenceHarness:
     """The reference's own driver functions on the Kokkos-API shim (oracle/_ref)."""
 
-    def __init__(self, path: str = REF_SO):
+    def __init__(self, path: str = REF_SO, libm_pow: bool = False):
+        if libm_pow and path == REF_SO:
+            path = REF_LIBM_SO
         if not os.path.exists(path):
             raise FileNotFoundError(path)
         lib = ctypes.CDLL(path)

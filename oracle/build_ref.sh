@@ -12,10 +12,19 @@ if [ ! -f "$ref/src/main.cpp" ]; then
     exit 0
 fi
 mkdir -p "$here/_ref"
-g++ -O2 -std=c++20 -fopenmp -ffp-contract=off -fPIC -shared \
-    -Dmain=kpt_ref_main \
-    -I "$here/kokkos_shim" -I "$here/../kokkos-particletransport_gb300/csrc" \
-    -I "$ref" -I "$ref/include" \
-    "$here/ref_harness.cpp" -o "$here/_ref/libkpt_ref.so.tmp"
-mv "$here/_ref/libkpt_ref.so.tmp" "$here/_ref/libkpt_ref.so"
-echo "build_ref: wrote $here/_ref/libkpt_ref.so"
+# libkpt_ref.so: Kokkos::pow is the project pow (bit-for-bit parity with the
+# GPU and the restatement); libkpt_ref_libm.so: the C library's pow, as a real
+# Kokkos host build calls (timed against the restatement's libm build)
+build() {
+    g++ -O2 -std=c++20 -fopenmp -ffp-contract=off -fPIC -shared \
+        -Dmain=kpt_ref_main "$@" \
+        -I "$here/kokkos_shim" -I "$here/../kokkos-particletransport_gb300/csrc" \
+        -I "$ref" -I "$ref/include" \
+        "$here/ref_harness.cpp" -o "$out.tmp"
+    mv "$out.tmp" "$out"
+    echo "build_ref: wrote $out"
+}
+out="$here/_ref/libkpt_ref.so" build & first=$!
+out="$here/_ref/libkpt_ref_libm.so" build -DKPT_SHIM_LIBM_POW & second=$!
+wait "$first"
+wait "$second"

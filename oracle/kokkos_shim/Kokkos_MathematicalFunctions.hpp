@@ -4,7 +4,9 @@
 // (kokkos-particletransport_gb300/csrc/kpt_pow.h), the one the GPU's FP64 push
 // and the C restatement call, so the reference's kernels round every power
 // exactly as the GPU does (CUDA's pow and glibc's pow each err by up to about
-// an ulp, and not alike).  Oracle-only shim.
+// an ulp, and not alike).  Built with -DKPT_SHIM_LIBM_POW, Kokkos::pow is the
+// C library's, as in a real Kokkos host build: that build is the one timed
+// against the C restatement.  Oracle-only shim.
 #pragma once
 
 #include <cmath>
@@ -22,11 +24,15 @@ using std::log;
 using std::sin;
 using std::sqrt;
 
+#ifdef KPT_SHIM_LIBM_POW
+inline double pow(double x, double y) { return std::pow(x, y); }
+#else
 inline double pow(double x, double y) { return kpt_pow(x, y); }
+#endif
 
 template <class X, class Y,
           class = std::enable_if_t<std::is_arithmetic_v<X> && std::is_arithmetic_v<Y>>>
 inline double pow(X x, Y y) {
-    return kpt_pow(static_cast<double>(x), static_cast<double>(y));
+    return Kokkos::pow(static_cast<double>(x), static_cast<double>(y));
 }
 }  // namespace Kokkos

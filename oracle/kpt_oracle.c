@@ -21,6 +21,18 @@
 /* the project pow, shared with the GPU push and the shim's Kokkos::pow */
 #include "kpt_pow.h"
 
+/* Powers: the project pow (kpt_pow.h, the one the GPU's strict FP64 push and
+ * the reference build on the shim call), so the restatement's trajectories
+ * equal theirs bit for bit.  Built with -DKPT_ORACLE_LIBM_POW the restatement
+ * calls the C library's pow instead, as the reference's own Kokkos build
+ * does: that build is the one timed as the CPU baseline (same algorithm,
+ * powers within an ulp, at the C library's speed). */
+#ifdef KPT_ORACLE_LIBM_POW
+#define ORACLE_POW pow
+#else
+#define ORACLE_POW kpt_pow
+#endif
+
 static _Thread_local char g_error[256];
 
 const char* kpt_oracle_last_error(void) { return g_error; }
@@ -552,11 +564,11 @@ double kpt_oracle_qlt_dmumu(double mu, double omega, double speed, double sigma2
     const double regularized_abs_mu = (mu >= 0.0 ? mu : -mu) + h0;
     const double gamma_k = spectral_index;
     const double xi = omega * lc / speed;
-    const double abs_mu_gamma = kpt_pow(regularized_abs_mu, gamma_k);
-    const double xi_gamma = kpt_pow(xi, gamma_k);
+    const double abs_mu_gamma = ORACLE_POW(regularized_abs_mu, gamma_k);
+    const double xi_gamma = ORACLE_POW(xi, gamma_k);
     const double denominator = abs_mu_gamma + xi_gamma;
     const double prefactor = 0.25 * kPi * omega * sigma2 * qlt_normalization(gamma_k);
-    return prefactor * one_minus_mu2 * xi * kpt_pow(regularized_abs_mu, gamma_k - 1.0) / denominator;
+    return prefactor * one_minus_mu2 * xi * ORACLE_POW(regularized_abs_mu, gamma_k - 1.0) / denominator;
 }
 
 double kpt_oracle_qlt_dmumu_dmu(double mu, double dmumu, double omega, double speed, double lc,
@@ -575,12 +587,12 @@ double kpt_oracle_qlt_dmumu_dmu(double mu, double dmumu, double omega, double sp
     const double regularized_abs_mu = (mu >= 0.0 ? mu : -mu) + h0;
     const double gamma_k = spectral_index;
     const double xi = omega * lc / speed;
-    const double abs_mu_gamma = kpt_pow(regularized_abs_mu, gamma_k);
-    const double xi_gamma = kpt_pow(xi, gamma_k);
+    const double abs_mu_gamma = ORACLE_POW(regularized_abs_mu, gamma_k);
+    const double xi_gamma = ORACLE_POW(xi, gamma_k);
     const double denominator = abs_mu_gamma + xi_gamma;
     const double shape_derivative =
         sign_mu * ((gamma_k - 1.0) / regularized_abs_mu -
-                   gamma_k * kpt_pow(regularized_abs_mu, gamma_k - 1.0) / denominator);
+                   gamma_k * ORACLE_POW(regularized_abs_mu, gamma_k - 1.0) / denominator);
     const double endpoint_derivative = -2.0 * mu / one_minus_mu2;
     return dmumu * (endpoint_derivative + shape_derivative);
 }
@@ -638,11 +650,11 @@ static void push_parker_one(const kpt_oracle_grid* g, const double* lower_table,
 
         double knorm_para = 1.0;
         if (s->magnetic_dependency == 1) {
-            knorm_para *= kpt_pow(b, s->gamma_turb - 2.0);
+            knorm_para *= ORACLE_POW(b, s->gamma_turb - 2.0);
         }
         double knorm = knorm_para;
         if (s->momentum_dependency == 1) {
-            knorm *= kpt_pow(p / s->p0, d->pindex);
+            knorm *= ORACLE_POW(p / s->p0, d->pindex);
         }
         const double kpara = s->kpara0 * knorm;
         const double kperp = kpara * s->kperp_over_kpara;
@@ -801,11 +813,11 @@ static void push_focused_one(const kpt_oracle_grid* g, const double* lower_table
 
         double knorm_para = 1.0;
         if (s->magnetic_dependency == 1) {
-            knorm_para *= kpt_pow(b, s->gamma_turb - 2.0);
+            knorm_para *= ORACLE_POW(b, s->gamma_turb - 2.0);
         }
         double knorm = knorm_para;
         if (s->momentum_dependency == 1) {
-            knorm *= kpt_pow(p / s->p0, d->pindex);
+            knorm *= ORACLE_POW(p / s->p0, d->pindex);
         }
         const double kpara = s->kpara0 * knorm;
         const double kperp = kpara * s->kperp_over_kpara;
@@ -892,21 +904,21 @@ static void push_focused_one(const kpt_oracle_grid* g, const double* lower_table
                                               s->qlt_spectral_index, s->qlt_h0);
         } else {
             const double abs_mu = fabs(pitch_mu);
-            const double dtmp = kpt_pow(abs_mu, s->gamma_turb - 1.0) + d->h0;
+            const double dtmp = ORACLE_POW(abs_mu, s->gamma_turb - 1.0) + d->h0;
             duu = s->duu0 * (1.0 - mu2) * dtmp;
             if (pitch_mu > 0.0) {
                 duu_du = s->duu0 * (-2.0 * pitch_mu * dtmp +
-                                    (1.0 - mu2) * kpt_pow(abs_mu, s->gamma_turb - 2.0));
+                                    (1.0 - mu2) * ORACLE_POW(abs_mu, s->gamma_turb - 2.0));
             } else if (pitch_mu < 0.0) {
                 duu_du = s->duu0 * (-2.0 * pitch_mu * dtmp -
-                                    (1.0 - mu2) * kpt_pow(abs_mu, s->gamma_turb - 2.0));
+                                    (1.0 - mu2) * ORACLE_POW(abs_mu, s->gamma_turb - 2.0));
             }
             double duu_norm = 1.0;
             if (s->magnetic_dependency == 1) {
-                duu_norm *= kpt_pow(b, 2.0 - s->gamma_turb);
+                duu_norm *= ORACLE_POW(b, 2.0 - s->gamma_turb);
             }
             if (s->momentum_dependency == 1) {
-                duu_norm *= kpt_pow(p / s->p0, s->gamma_turb - 1.0);
+                duu_norm *= ORACLE_POW(p / s->p0, s->gamma_turb - 1.0);
             }
             duu *= duu_norm;
             duu_du *= duu_norm;
@@ -1073,7 +1085,7 @@ uint64_t kpt_oracle_split(const kpt_oracle_params* s, uint64_t capacity, uint64_
             continue;
         }
         const int old_level = split_level[parent];
-        const double threshold = pmin_split * kpt_pow(s->split_ratio, (double)old_level);
+        const double threshold = pmin_split * ORACLE_POW(s->split_ratio, (double)old_level);
         const double pp = p[parent];
         if (!(pp > threshold && pp <= s->pmax)) {
             continue;
@@ -1084,7 +1096,7 @@ uint64_t kpt_oracle_split(const kpt_oracle_params* s, uint64_t capacity, uint64_
             continue;
         }
         const int new_level = old_level + 1;
-        const double new_weight = kpt_pow(0.5, (double)new_level);
+        const double new_weight = ORACLE_POW(0.5, (double)new_level);
         x[child] = x[parent];
         y[child] = y[parent];
         p[child] = p[parent];

@@ -43,8 +43,10 @@ def main():
     parser.add_argument("--particles", type=int, default=25600)
     args = parser.parse_args()
     threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    oracle = binding.Oracle()
-    ref = binding.ReferenceHarness()
+    # both on the C library's pow, as the bench's CPU baseline and a real
+    # Kokkos host build are
+    oracle = binding.Oracle(libm_pow=True)
+    ref = binding.ReferenceHarness(libm_pow=True)
     field = fields.harris_field(256, 512)
     frame, seed, n = 0, 114514, args.particles
     out = {"threads": threads, "cpu": platform_cpu(), "particles": n, "workloads": {}}
