@@ -188,6 +188,25 @@ void run_solver(const std::map<std::string, Record>& in, Writer& out, Coefficien
         out.put("graph_dts", 'd', replay.advance_stochastic_steps(rng2, steps));
         out.put_state("graph", again.copy_to_host(start.size()));
     }
+    // the mixed-precision step (an extension): the same steps from the same
+    // start, FP32 terms and noise with FP64 state
+    {
+        kpt::ParticleSystem mixed_particles(count, start.size(), kpt::ParticleProperties{});
+        mixed_particles.copy_from_host(start);
+        Solver mixed(mixed_particles, grid, B, V, coefficients);
+        mixed.set_dimensionless_courant_scale(scalar(in, "courant"));
+        if constexpr (FOCUSED) mixed.set_maximum_pitch_angle_cosine(scalar(in, "max_mu"));
+        mixed.set_precision(KPT_PRECISION_MIXED);
+        const kpt::RandomManager rng3(static_cast<std::uint64_t>(scalar(in, "seed")),
+                                      static_cast<std::uint32_t>(scalar(in, "first_step")));
+        std::vector<double> mixed_dts;
+        for (std::uint32_t k = 0; k < steps; ++k) {
+            mixed_dts.push_back(stochastic ? mixed.advance_stochastic(rng3)
+                                           : mixed.advance_deterministic());
+        }
+        out.put("mixed_dts", 'd', mixed_dts);
+        out.put_state("mixed", mixed_particles.copy_to_host(start.size()));
+    }
     // a Courant scale of zero is refused with the reference's message
     solver.set_dimensionless_courant_scale(0.0);
     out.put("error_courant", 'd',

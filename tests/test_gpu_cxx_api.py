@@ -131,6 +131,17 @@ def test_cxx_solver_steps_match_reference(tmp_path, kind, case):
         for key in FIELDS:
             assert np.array_equal(got[f"graph_{key}"], got[f"end_{key}"]), key
         assert "Courant" in _text(got["error_courant"])
+    # set_precision(KPT_PRECISION_MIXED): the bars of test_gpu_library_mixed.py
+    # against the FP64 steps of the same classes
+    np.testing.assert_allclose(got["mixed_dts"], got["dts"][1:],
+                               rtol=1e-3 if kind == "focus" else 1e-5, atol=0)
+    for key in ("status", "id", "w", "level", "key"):
+        assert np.array_equal(got[f"mixed_{key}"], got[f"end_{key}"]), key
+    wx = data["x_edges"][-1] - data["x_edges"][0]
+    wy = data["y_edges"][-1] - data["y_edges"][0]
+    for key, width in (("x", wx), ("y", wy)):
+        d = np.abs(got[f"mixed_{key}"] - got[f"end_{key}"])
+        assert (np.minimum(d, np.abs(width - d)) / width).max() <= 1e-6, key
 
 
 @pytest.mark.parametrize("name", ["lib_system.npz", "lib_system_stored.npz"])
