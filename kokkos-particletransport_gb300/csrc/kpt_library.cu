@@ -1868,10 +1868,32 @@ __device__ double coef_curl_derivative(const CoefLaunch& L, int i, int j, int di
                      width);
 }
 
-// One gamma-independent diffusion tensor basis component
-// (ParkerCoefficient.hpp:606-641); basis 0 parallel projection, 1
-// perpendicular projection, 2 constant parallel ratio.
-__device__ double coef_tensor(const CoefLaunch& L, int i, int j, int oc, int dc, int basis) {
+// The three-point weights of centered_three_point_derivative
+// (ParkerCoefficient.hpp:215-234) at one logical index: a derivative is
+// a lv + b cv + c uv, each product and sum rounded as coef_d3 rounds them.
+struct D3Weights {
+    double a, b, c;
+};
+__device__ __forceinline__ D3Weights coef_d3_weights(double lc, double cc, double uc) {
+    const double lw = __dsub_rn(cc, lc);
+    const double uw = __dsub_rn(uc, cc);
+    const double tw = __dsub_rn(uc, lc);
+    return D3Weights{__ddiv_rn(-uw, __dmul_rn(lw, tw)),
+                     __ddiv_rn(__dsub_rn(uw, lw), __dmul_rn(lw, uw)),
+                     __ddiv_rn(lw, __dmul_rn(uw, tw))};
+}
+__device__ __forceinline__ double coef_d3_apply(const D3Weights& w, double lv, double cv,
+                                                double uv) {
+    return __dadd_rn(__dadd_rn(__dmul_rn(w.a, lv), __dmul_rn(w.b, cv)), __dmul_rn(w.c, uv));
+}
+
+// The direction and kappas of one point of a diffusion tensor
+// (ParkerCoefficient.hpp:606-641): b = B / max(|B|, floor).
+struct TensorPoint {
+    double b[3];
+    double kpar, kperp;
+};
+__device__ TensorPoint coef_tensor_point(const CoefLaunch& L, int i, int j) {
     const size_t p = coef_point(L.grid, i, j);
     const double* row = L.b + 3 * p;
     const double magnitude = __dsqrt_rn(coef_norm2(row));
@@ -1879,53 +1901,84 @@ __device__ double coef_tensor(const CoefLaunch& L, int i, int j, int oc, int dc,
         coef_set_error(L.error, 26);  // diffusion tensor direction is undefined where |B| <= 0
     }
     const double den = magnitude > L.min_b ? magnitude : L.min_b;
-    const double bi = __ddiv_rn(row[oc], den);
-    const double bj = __ddiv_rn(row[dc], den);
-    const double projection = __dmul_rn(bi, bj);
-    const double identity = oc == dc ? 1.0 : 0.0;
-    const double kpar = L.packed[p * L.stride + L.kpar_slot];
-    if (basis == 0) return __dmul_rn(kpar, projection);
-    if (basis == 1) {
-        return __dmul_rn(L.packed[p * L.stride + L.kperp_slot], __dsub_rn(identity, projection));
-    }
-    return __dmul_rn(kpar, __dadd_rn(__dmul_rn(L.ratio, identity),
-                                     __dmul_rn(__dsub_rn(1.0, L.ratio), projection)));
+    TensorPoint t;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) t.b[c] = __ddiv_rn(row[c], den);
+    t.kpar = L.packed[p * L.stride + L.kpar_slot];
+    t.kperp = L.packed[p * L.stride + L.kperp_slot];
+    return t;
 }
 
-// centered_lame_derivative of h = 1 along dim (ParkerCoefficient.hpp:746-790).
-__device__ double coef_lame(const CoefLaunch& L, int i, int j, int dim) {
-    if (dim >= 2 || L.grid.axis[dim].n <= 1) return 0.0;
-    const LibAxis& a = L.grid.axis[dim];
-    const int k = dim == 0 ? i : j;
-    return coef_d3(gen_coordinate(a, k - 1, 0), gen_coordinate(a, k, 0),
-                   gen_coordinate(a, k + 1, 0), 1.0, 1.0, 1.0);
+// One gamma-independent diffusion tensor basis component
+// (ParkerCoefficient.hpp:606-641); basis 0 parallel projection, 1
+// perpendicular projection, 2 constant parallel ratio.
+__device__ __forceinline__ double coef_tensor(const CoefLaunch& L, const TensorPoint& t, int oc,
+                                              int dc, int basis) {
+    const double projection = __dmul_rn(t.b[oc], t.b[dc]);
+    const double identity = oc == dc ? 1.0 : 0.0;
+    if (basis == 0) return __dmul_rn(t.kpar, projection);
+    if (basis == 1) return __dmul_rn(t.kperp, __dsub_rn(identity, projection));
+    return __dmul_rn(t.kpar, __dadd_rn(__dmul_rn(L.ratio, identity),
+                                       __dmul_rn(__dsub_rn(1.0, L.ratio), projection)));
+}
+
+// Everything a point's divergence bases read, formed once per point: the
+// tensor points of the point and of its neighbours along each axis that has
+// more than one cell, the three-point weights of each such axis, and the
+// centred derivative of the Lame coefficient h = 1 along it
+// (centered_lame_derivative, ParkerCoefficient.hpp:746-790).  The values are
+// the ones the reference forms at every use, with the same rounding.
+struct TensorStencil {
+    TensorPoint centre, lower[2], upper[2];
+    D3Weights weights[2];
+    double lame[2];
+    bool active[2];
+};
+__device__ __forceinline__ TensorStencil coef_tensor_stencil(const CoefLaunch& L, int i, int j) {
+    TensorStencil s;
+#pragma unroll
+    for (int dim = 0; dim < 2; ++dim) {
+        const LibAxis& a = L.grid.axis[dim];
+        s.active[dim] = a.n > 1;
+        s.lame[dim] = 0.0;
+        if (!s.active[dim]) continue;
+        const int k = dim == 0 ? i : j;
+        s.weights[dim] = coef_d3_weights(gen_coordinate(a, k - 1, 0), gen_coordinate(a, k, 0),
+                                         gen_coordinate(a, k + 1, 0));
+        s.lame[dim] = coef_d3_apply(s.weights[dim], 1.0, 1.0, 1.0);
+        s.lower[dim] = coef_tensor_point(L, dim == 0 ? i - 1 : i, dim == 1 ? j - 1 : j);
+        s.upper[dim] = coef_tensor_point(L, dim == 0 ? i + 1 : i, dim == 1 ? j + 1 : j);
+    }
+    s.centre = coef_tensor_point(L, i, j);
+    return s;
 }
 
 // diffusion_tensor_divergence_basis_component (ParkerCoefficient.hpp:794-877).
-__device__ double coef_divergence_basis(const CoefLaunch& L, int i, int j, int oc, int basis) {
+__device__ __forceinline__ double coef_divergence_basis(const CoefLaunch& L,
+                                                        const TensorStencil& s, int oc,
+                                                        int basis) {
     double result = 0.0;
+#pragma unroll
     for (int dim = 0; dim < 2; ++dim) {
-        if (L.grid.axis[dim].n <= 1) {
+        if (!s.active[dim]) {
             result = __dadd_rn(result, 0.0);
             continue;
         }
-        const LibAxis& a = L.grid.axis[dim];
-        const int k = dim == 0 ? i : j;
-        const double lv = coef_tensor(L, dim == 0 ? i - 1 : i, dim == 1 ? j - 1 : j, oc, dim, basis);
-        const double cv = coef_tensor(L, i, j, oc, dim, basis);
-        const double uv = coef_tensor(L, dim == 0 ? i + 1 : i, dim == 1 ? j + 1 : j, oc, dim, basis);
-        result = __dadd_rn(result, coef_d3(gen_coordinate(a, k - 1, 0), gen_coordinate(a, k, 0),
-                                           gen_coordinate(a, k + 1, 0), lv, cv, uv));
+        const double lv = coef_tensor(L, s.lower[dim], oc, dim, basis);
+        const double cv = coef_tensor(L, s.centre, oc, dim, basis);
+        const double uv = coef_tensor(L, s.upper[dim], oc, dim, basis);
+        result = __dadd_rn(result, coef_d3_apply(s.weights[dim], lv, cv, uv));
     }
+#pragma unroll
     for (int c = 0; c < 3; ++c) {
         if (c == oc) continue;
         if (c < 2) {
-            const double t = coef_tensor(L, i, j, oc, c, basis);
-            result = __dadd_rn(result, __dmul_rn(t, coef_lame(L, i, j, c)));
+            const double t = coef_tensor(L, s.centre, oc, c, basis);
+            result = __dadd_rn(result, __dmul_rn(t, s.lame[c]));
         }
         if (oc < 2) {
-            const double t = coef_tensor(L, i, j, c, c, basis);
-            result = __dsub_rn(result, __dmul_rn(t, coef_lame(L, i, j, oc)));
+            const double t = coef_tensor(L, s.centre, c, c, basis);
+            result = __dsub_rn(result, __dmul_rn(t, s.lame[oc]));
         }
     }
     return result;
@@ -2078,15 +2131,16 @@ __global__ void coef_derivative_kernel(const CoefLaunch L) {
             out[6 + c] = __dsub_rn(a, b);
         }
         // diffusion tensor divergence bases (:960-1095)
-#pragma unroll 1
+        const TensorStencil ts = coef_tensor_stencil(L, i, j);
+#pragma unroll
         for (int c = 0; c < 3; ++c) {
             if (L.constant_ratio) {
-                const double value = coef_divergence_basis(L, i, j, c, 2);
+                const double value = coef_divergence_basis(L, ts, c, 2);
                 out[9 + c] = value;
                 out[12 + c] = value;
             } else {
-                out[9 + c] = coef_divergence_basis(L, i, j, c, 0);
-                out[12 + c] = coef_divergence_basis(L, i, j, c, 1);
+                out[9 + c] = coef_divergence_basis(L, ts, c, 0);
+                out[12 + c] = coef_divergence_basis(L, ts, c, 1);
             }
         }
         // FieldOperator::divergence_value of V (FieldOperator.hpp:262-277)
@@ -2263,8 +2317,9 @@ __global__ void focus_stage4_kernel(const CoefLaunch L) {
         if (!coef_physical(L, p, i, j)) continue;
         double* out = L.packed + p * L.stride;
         const double* scratch = L.scratch + p * kFocusScratch;
-#pragma unroll 1
-        for (int c = 0; c < 3; ++c) out[15 + c] = coef_divergence_basis(L, i, j, c, 1);
+        const TensorStencil ts = coef_tensor_stencil(L, i, j);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) out[15 + c] = coef_divergence_basis(L, ts, c, 1);
         double div = 0.0;
         for (int dim = 0; dim < 2; ++dim) {
             div = __dadd_rn(div, coef_component_derivative(L, L.v, 3, i, j, dim, dim));
