@@ -236,6 +236,18 @@ int kpt_context_set_push_schedule(kpt_context* ctx, int schedule, int blocks_per
  * strict ones (the reference's own optimised builds contract too). */
 enum kpt_fp64_arithmetic { KPT_FP64_STRICT = 0, KPT_FP64_CONTRACTED = 1 };
 int kpt_context_set_fp64_arithmetic(kpt_context* ctx, int mode);
+/* Cell records of the mixed pushes (no counterpart in the reference, whose
+ * push samples its point tables): for a pair of FP32 tables the context
+ * keeps one record per cell with each component's eight corner values of
+ * both frames in one 32-byte sector, so four lanes of a warp read a
+ * particle's cell one 128-byte line at a time.  KPT_RECORDS_AUTO (default)
+ * builds them (record_floats x 4 bytes per table point: 768 focused, 512
+ * Parker; rebuilt when the table pair changes) for a refill-scheduled
+ * mixed push of at least a quarter as many particles as the table has
+ * points; KPT_RECORDS_OFF never, KPT_RECORDS_ON for every refill-scheduled
+ * mixed push.  Results are bit-identical either way. */
+enum kpt_records_mode { KPT_RECORDS_AUTO = 0, KPT_RECORDS_OFF = 1, KPT_RECORDS_ON = 2 };
+int kpt_context_set_cell_records(kpt_context* ctx, int mode);
 
 /* ---- fields: one MHD frame as a device coefficient table ---------------- */
 /* Cells are 3 x ny x nx arrays (x fastest) of B and V, host memory.  Edges

@@ -34,6 +34,9 @@ SCHEDULE_REFILL = 0
 SCHEDULE_SIMPLE = 1
 FP64_STRICT = 0       # FP64 push rounds as the reference's code is written (oracle-exact)
 FP64_CONTRACTED = 1   # FP64 push with FMA contraction and CUDA's pow (faster)
+RECORDS_AUTO = 0      # mixed pushes sample cell records when the population is dense enough
+RECORDS_OFF = 1       # mixed pushes sample the point-major tables
+RECORDS_ON = 2        # every refill-scheduled mixed push samples cell records
 ENGINE_TCGEN05 = 0   # block-collective tcgen05.mma network, activations in tensor memory
 ENGINE_MMA_SYNC = 1  # warp-collective mma.sync network, activations in registers
 
@@ -231,6 +234,7 @@ def load_library() -> ctypes.CDLL:
         "kpt_context_fp64_fma_rate": (i32, [vp, ctypes.POINTER(ctypes.c_double)]),
         "kpt_math_pow": (i32, [vp, ctypes.c_uint64, vp, vp, vp]),
         "kpt_context_set_fp64_arithmetic": (i32, [vp, i32]),
+        "kpt_context_set_cell_records": (i32, [vp, i32]),
         "kpt_context_set_push_schedule": (i32, [vp, i32, i32]),
         "kpt_field_create": (i32, [vp, i32, i32, vp, vp, vp, vp, i32, i32, pvp]),
         "kpt_field_load": (i32, [vp, ctypes.c_char_p, i32, i32, pvp]),
@@ -411,6 +415,13 @@ class Context:
         """FP64_STRICT (oracle-exact rounding, the default) or FP64_CONTRACTED
         (FMA contraction and CUDA's pow, faster) for the FP64 push."""
         _check(self.lib.kpt_context_set_fp64_arithmetic(self.handle, int(mode)))
+
+    def set_cell_records(self, mode: int) -> None:
+        """RECORDS_AUTO (default), RECORDS_OFF or RECORDS_ON: whether the
+        mixed pushes sample per-cell records of the table pair (each
+        component's eight corner values in one 32-byte sector) or the
+        point-major tables.  The values are the same bit for bit."""
+        _check(self.lib.kpt_context_set_cell_records(self.handle, int(mode)))
 
     def pow(self, x, y) -> np.ndarray:
         """x^y elementwise by the FP64 push's power function, on the GPU."""

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -113,6 +114,10 @@ struct kpt_context {
     int push_schedule = kpt::kScheduleRefill;
     int fp64_arithmetic = KPT_FP64_STRICT;
     int push_blocks_per_sm = 0;  // 0: as many as fit (occupancy)
+    // cell records of the last table pair a mixed push used (by field serial)
+    DeviceBuffer records;
+    uint64_t records_lower = 0, records_upper = 0;
+    int records_mode = KPT_RECORDS_AUTO;
 };
 
 struct kpt_surrogate {
@@ -143,6 +148,7 @@ struct kpt_field {
     int* fixed_buckets[2] = {nullptr, nullptr};
     kpt::Grid grid{};
     kpt::FixedAxis fixed[2]{};
+    uint64_t serial = 0;  // unique per field of the process (record cache key)
 };
 
 struct kpt_field_data {
@@ -481,7 +487,7 @@ int kpt_context_destroy(kpt_context* ctx) {
                             &ctx->split_totals, &ctx->split_levels, &ctx->hist_bins,
                             &ctx->hist_edge_count, &ctx->hist_edge_index,
                             &ctx->summary_partials, &ctx->summary_result, &ctx->sample_io,
-                            &ctx->judge}) {
+                            &ctx->judge, &ctx->records}) {
         b->release();
     }
     if (ctx->own_stream != nullptr) {
@@ -516,6 +522,15 @@ int kpt_context_set_fp64_arithmetic(kpt_context* ctx, int mode) {
                 "kpt_context_set_fp64_arithmetic: mode must be KPT_FP64_STRICT or "
                 "KPT_FP64_CONTRACTED");
     ctx->fp64_arithmetic = mode;
+    return KPT_OK;
+}
+
+int kpt_context_set_cell_records(kpt_context* ctx, int mode) {
+    KPT_REQUIRE(ctx != nullptr, "kpt_context_set_cell_records: ctx is NULL");
+    KPT_REQUIRE(mode == KPT_RECORDS_AUTO || mode == KPT_RECORDS_OFF || mode == KPT_RECORDS_ON,
+                "kpt_context_set_cell_records: mode must be KPT_RECORDS_AUTO, KPT_RECORDS_OFF "
+                "or KPT_RECORDS_ON");
+    ctx->records_mode = mode;
     return KPT_OK;
 }
 
@@ -594,6 +609,8 @@ int field_create(kpt_context* ctx, int nx, int ny, const double* x_edges, const 
         void operator()(kpt_field* doomed) const { kpt_field_destroy(doomed); }
     };
     std::unique_ptr<kpt_field, FieldDeleter> f(new kpt_field());
+    static std::atomic<uint64_t> next_serial{1};
+    f->serial = next_serial.fetch_add(1);
     f->ctx = ctx;
     f->device = ctx->device;
     f->nx = nx;
@@ -1065,6 +1082,47 @@ void fill_push_launch(const kpt_context* ctx, const kpt_particles* parts, const 
     launch.surrogate = nullptr;
 }
 
+// The cell records a mixed push samples (*out = nullptr: the point-major
+// tables), built on the context's stream when the table pair differs from
+// the one they hold.  Should the records not fit in device memory the push
+// samples the point tables, which gives the same values.
+int push_records(kpt_context* ctx, const kpt_particles* parts, const kpt_field* lower,
+                 const kpt_field* upper, const float** out) {
+    *out = nullptr;
+    if (lower->precision != KPT_PRECISION_MIXED || ctx->push_schedule != kpt::kScheduleRefill ||
+        parts->count == 0 || ctx->records_mode == KPT_RECORDS_OFF ||
+        lower->points >= (1ull << 32)) {
+        return KPT_OK;
+    }
+    if (ctx->records_mode == KPT_RECORDS_AUTO && parts->count * 4 < lower->points) {
+        return KPT_OK;
+    }
+    if (ctx->records_lower != lower->serial || ctx->records_upper != upper->serial ||
+        ctx->records.ptr == nullptr) {
+        const bool focused = lower->kind == KPT_TABLE_FOCUSED21;
+        const size_t bytes = lower->points * kpt::record_floats(focused) * sizeof(float);
+        ctx->records_lower = ctx->records_upper = 0;
+        if (ctx->records.reserve(bytes) != cudaSuccess) {
+            cudaGetLastError();  // out of memory: sample the point tables
+            ctx->records.release();
+            return KPT_OK;
+        }
+        kpt::RecordLaunch rl{};
+        rl.lower = static_cast<const float*>(lower->table);
+        rl.upper = static_cast<const float*>(upper->table);
+        rl.records = ctx->records.as<float>();
+        rl.points = lower->points;
+        rl.ex = lower->nx + 4;
+        rl.ey = lower->ny + 4;
+        rl.focused = focused ? 1 : 0;
+        KPT_CUDA(kpt::launch_build_records(rl, ctx->stream));
+        ctx->records_lower = lower->serial;
+        ctx->records_upper = upper->serial;
+    }
+    *out = ctx->records.as<float>();
+    return KPT_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1115,6 +1173,7 @@ int kpt_push_interval(kpt_context* ctx, kpt_particles* parts, const kpt_field* l
         served.judge = ctx->judge.as<unsigned long long>();  // zeroed by set_surrogate
         launch.surrogate = &served;
     }
+    if (int rc = push_records(ctx, parts, lower, upper, &launch.records)) return rc;
     KPT_CUDA(cudaMemsetAsync(launch.counters, 0, sizeof(kpt::PushCounters), ctx->stream));
     if (parts->count > 0) {
         KPT_CUDA(kpt::launch_push_interval(launch, ctx->stream));

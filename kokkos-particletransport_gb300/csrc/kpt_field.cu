@@ -171,7 +171,57 @@ __global__ void build_table_kernel(const TableLaunch L) {
     }
 }
 
+// One thread per (cell, sector): sector s of line m holds frame m % 2 of
+// component pair 4 (m / 2) + s at the cell's four corners (zeros past the
+// last component).  Cells on the last ghosted column or row have no
+// upper-right corner and no record; no particle's stencil starts there.
+template <bool FOCUSED>
+__global__ void build_records_kernel(const RecordLaunch L) {
+    constexpr int C = FOCUSED ? 21 : 16;
+    constexpr int S = record_sectors(FOCUSED);
+    const uint64_t total = L.points * S;
+    const size_t ex = static_cast<size_t>(L.ex);
+    for (uint64_t q = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; q < total;
+         q += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        const size_t p = static_cast<size_t>(q / S);
+        const int sector = static_cast<int>(q % S);
+        const size_t i = p % ex, j = p / ex;
+        if (i + 1 >= ex || j + 2 > static_cast<size_t>(L.ey)) continue;
+        const int line = sector / 4;
+        const float* table = (line & 1) ? L.upper : L.lower;
+        const int first = 2 * (4 * (line / 2) + sector % 4);
+        const size_t corner[4] = {p, p + 1, p + ex, p + ex + 1};
+        float v[8];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            v[2 * k] = first < C ? __ldg(table + table_f32_offset(FOCUSED, L.points, corner[k],
+                                                                  first))
+                                 : 0.0f;
+            v[2 * k + 1] = first + 1 < C ? __ldg(table + table_f32_offset(FOCUSED, L.points,
+                                                                          corner[k], first + 1))
+                                         : 0.0f;
+        }
+        float4* out =
+            reinterpret_cast<float4*>(L.records + p * record_floats(FOCUSED) + 8 * sector);
+        out[0] = make_float4(v[0], v[1], v[2], v[3]);
+        out[1] = make_float4(v[4], v[5], v[6], v[7]);
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_build_records(const RecordLaunch& L, cudaStream_t stream) {
+    const uint64_t total = L.points * static_cast<uint64_t>(record_sectors(L.focused != 0));
+    const int threads = 256;
+    const uint64_t want = (total + threads - 1) / threads;
+    const int blocks = static_cast<int>(want < 1 ? 1 : (want > 152u * 64u ? 152u * 64u : want));
+    if (L.focused) {
+        build_records_kernel<true><<<blocks, threads, 0, stream>>>(L);
+    } else {
+        build_records_kernel<false><<<blocks, threads, 0, stream>>>(L);
+    }
+    return cudaGetLastError();
+}
 
 cudaError_t launch_build_table(const TableLaunch& L, cudaStream_t stream) {
     const size_t points = static_cast<size_t>(L.grid.axis[0].n + 4) *

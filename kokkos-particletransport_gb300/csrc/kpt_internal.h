@@ -38,6 +38,32 @@ __host__ __device__ inline size_t table_f32_offset(bool focused, size_t points, 
     return (static_cast<size_t>(c / w) * points + p) * w + c % w;
 }
 
+// Cell records of a pair of FP32 tables (the frames at the interval's two
+// ends), for the mixed pushes.  The record of a cell is indexed by its
+// lower-left ghosted point p and is made of 128-byte lines of four 32-byte
+// sectors.  Line m holds frame m % 2 (lower, upper) of the component pairs
+// 4 (m / 2) .. 4 (m / 2) + 3; the sector of pair k holds components 2k and
+// 2k + 1 at the cell's corners p, p + 1, p + ex, p + ex + 1, pair by pair --
+// the operands of the packed-pair interpolation, in the order the
+// point-major sampler accumulates them.  Four lanes then read one line of a
+// particle's record per request (four lines for the point-major rows), and
+// a lane interpolates a component pair from its own two sectors.
+// Components past the last are zero padding.
+__host__ __device__ constexpr int record_sectors(bool focused) { return focused ? 24 : 16; }
+__host__ __device__ constexpr int record_floats(bool focused) {
+    return 8 * record_sectors(focused);
+}
+
+struct RecordLaunch {
+    const float* lower;
+    const float* upper;
+    float* records;  // points x record_floats(focused)
+    uint64_t points;
+    int ex, ey;      // ghosted extents
+    int focused;
+};
+cudaError_t launch_build_records(const RecordLaunch& launch, cudaStream_t stream);
+
 struct PushLaunch {
     Grid grid;
     FixedGrid fixed;
@@ -60,6 +86,9 @@ struct PushLaunch {
     int fp64_contracted;  // FP64 push: 0 strict rounding (oracle-exact), 1 FMA contraction
     // learned closure (mixed focused push only); nullptr = plain closures
     const SurrogateDevice* surrogate;
+    // cell records of (lower, upper) for the mixed pushes; nullptr = sample
+    // the point-major tables (the same values, bit for bit)
+    const float* records;
 };
 
 cudaError_t launch_push_interval(const PushLaunch& launch, cudaStream_t stream);

@@ -704,6 +704,7 @@ struct PushParams {
     uint2 key;
     PushCounters* counters;
     SurrogateDevice sg;  // used by the surrogate instantiation only
+    const float* records;  // cell records of (lower, upper); nullptr: point-major sampling
 };
 
 // ------------------------------------------------------------- FP64 path
@@ -894,18 +895,14 @@ __device__ __forceinline__ void add_pair(float& hi, float& lo, float d) {
     lo = l - (hi - s);
 }
 
-// Table values at the particle (fixed-point stencil, time interpolation).
-template <bool FOCUSED>
-__device__ __forceinline__ void sample_mixed(const StateMixed& st, const PushParams& P,
-                                             float (&c)[FOCUSED ? 21 : 16]) {
-    constexpr int C = FOCUSED ? 21 : 16;
-    constexpr int STRIDE = FOCUSED ? 24 : 16;
-    const DeviceSettings& s = P.s;
+// The fixed-point stencil of a mixed particle: the cell's lower-left ghosted
+// point, the axis weights and the clamped time weight.
+__device__ __forceinline__ void mixed_stencil(const StateMixed& st, const PushParams& P,
+                                              size_t& cell, float& w0, float& w1, float& rt) {
     const FixedGrid& F = P.fixed;
     const uint64_t qx = st.px + F.axis[0].half_cell;
     const uint64_t qy = st.py + F.axis[1].half_cell;
     int lo0, lo1;
-    float w0, w1;
     if (F.axis[0].stored) {
         fixed_stencil_stored(F.axis[0], qx, lo0, w0);
     } else {
@@ -916,16 +913,132 @@ __device__ __forceinline__ void sample_mixed(const StateMixed& st, const PushPar
     } else {
         fixed_stencil_uniform(qy, F.axis[1].n, lo1, w1);
     }
+    cell = static_cast<size_t>(lo0 + 2) +
+           static_cast<size_t>(lo1 + 2) * static_cast<size_t>(P.grid.ex);
+    rt = st.tau <= 0 ? 0.0f : s64_to_float_scaled(st.tau, 1.0f / 1073741824.0f);
+    rt = rt > 1.0f ? 1.0f : rt;
+}
+
+// Table values at the particle (fixed-point stencil, time interpolation),
+// from the point-major tables.
+template <bool FOCUSED>
+__device__ __forceinline__ void sample_mixed(const StateMixed& st, const PushParams& P,
+                                             float (&c)[FOCUSED ? 21 : 16]) {
+    constexpr int C = FOCUSED ? 21 : 16;
+    constexpr int STRIDE = FOCUSED ? 24 : 16;
+    size_t cell;
+    float w0, w1, rt;
+    mixed_stencil(st, P, cell, w0, w1, rt);
     const float a0 = 1.0f - w0;
     const float a1 = 1.0f - w1;
     const float wc[4] = {a0 * a1, w0 * a1, a0 * w1, w0 * w1};
-    size_t pt[4];
-    corner_points(lo0, lo0 + 1, lo1, lo1 + 1, P.grid.ex, pt);
-    float rt = st.tau <= 0 ? 0.0f : s64_to_float_scaled(st.tau, 1.0f / 1073741824.0f);
-    rt = rt > 1.0f ? 1.0f : rt;
+    const size_t ex = static_cast<size_t>(P.grid.ex);
+    const size_t pt[4] = {cell, cell + 1, cell + ex, cell + ex + 1};
     sample_stencil_pairs<C, STRIDE>(static_cast<const float*>(P.lower),
                                     static_cast<const float*>(P.upper), P.table_points, pt, wc,
-                                    rt, s.time_interpolation, c);
+                                    rt, P.s.time_interpolation, c);
+}
+
+// Per-warp shared memory of the record sampler: 32 rows of the components
+// rounded up to whole pairs (row strides of 22 and 18 floats keep its 64-bit
+// stores and loads free of bank conflicts).
+__host__ __device__ constexpr int record_xpose_stride(bool focused) {
+    return focused ? 22 : 18;
+}
+__host__ __device__ constexpr size_t record_xpose_bytes(bool focused, int warps) {
+    return static_cast<size_t>(warps) * 32u * record_xpose_stride(focused) * sizeof(float);
+}
+
+// Warp-collective sampling from the cell records (every lane calls it,
+// converged; a lane without a particle passes cell 0).  Lanes 4g..4g+3 form
+// a group: for each of the group's four particles in turn, lane 4g+s reads
+// the sectors of component pairs s, s+4, s+8 of that particle's record --
+// one 128-byte line per request for the group -- and interpolates each pair
+// from its own sectors with the eight corner weights, in the operations and
+// the order of sample_stencil_pairs, so the values equal the point-major
+// sampler's bit for bit.  The pairs then reach their particle's lane
+// through the warp's rows of shared memory.
+template <bool FOCUSED, bool USE_TIME>
+__device__ __forceinline__ void sample_records(const PushParams& P, size_t cell, float w0,
+                                               float w1, float rt,
+                                               float (&c)[FOCUSED ? 21 : 16], float* xpose) {
+    constexpr int C = FOCUSED ? 21 : 16;
+    constexpr int RF = record_floats(FOCUSED);
+    constexpr int GROUPS = record_sectors(FOCUSED) / 8;  // line pairs (frames 0 and 1)
+    constexpr int XS = record_xpose_stride(FOCUSED);
+    const unsigned full = 0xffffffffu;
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned group = lane & ~3u;
+    const int s = static_cast<int>(lane & 3u);
+    const uint32_t my_cell = static_cast<uint32_t>(cell);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int src = static_cast<int>(group) + q;
+        const uint32_t qcell = __shfl_sync(full, my_cell, src);
+        const float qw0 = __shfl_sync(full, w0, src);
+        const float qw1 = __shfl_sync(full, w1, src);
+        const float qrt = USE_TIME ? __shfl_sync(full, rt, src) : 0.0f;
+        const float a0 = 1.0f - qw0;
+        const float a1 = 1.0f - qw1;
+        const float wc[4] = {a0 * a1, qw0 * a1, a0 * qw1, qw0 * qw1};
+        const float lw = USE_TIME ? 1.0f - qrt : 1.0f;
+        unsigned long long w_lo[4], w_hi[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            w_lo[k] = f2_splat(wc[k] * lw);
+            if (USE_TIME) w_hi[k] = f2_splat(wc[k] * qrt);
+        }
+        const float* rec = P.records + static_cast<size_t>(qcell) * RF + 8 * s;
+        float* row = xpose + (group + q) * XS;
+#pragma unroll
+        for (int m = 0; m < GROUPS; ++m) {
+            unsigned long long v[4];
+            load4_pairs(rec + 64 * m, v);
+            unsigned long long acc = f2_mul(w_lo[0], v[0]);
+#pragma unroll
+            for (int k = 1; k < 4; ++k) acc = f2_fma(w_lo[k], v[k], acc);
+            if (USE_TIME) {
+                load4_pairs(rec + 64 * m + 32, v);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) acc = f2_fma(w_hi[k], v[k], acc);
+            }
+            const int first = 2 * (4 * m + s);
+            if (8 * m + 7 < C || first < C) {
+                *reinterpret_cast<unsigned long long*>(row + first) = acc;
+            }
+        }
+    }
+    __syncwarp();
+    const unsigned long long* mine = reinterpret_cast<const unsigned long long*>(xpose + lane * XS);
+#pragma unroll
+    for (int k = 0; k < (C + 1) / 2; ++k) {
+        float lo, hi;
+        f2_split(mine[k], lo, hi);
+        c[2 * k] = lo;
+        if (2 * k + 1 < C) c[2 * k + 1] = hi;
+    }
+    __syncwarp();
+}
+
+// Warp-collective mixed sampling: the record sampler when the push has cell
+// records (xpose = the warp's shared rows), else the point-major sampler on
+// the lanes that hold a particle.
+template <bool FOCUSED>
+__device__ __forceinline__ void sample_mixed_warp(const StateMixed& st, const PushParams& P,
+                                                  bool have, float (&c)[FOCUSED ? 21 : 16],
+                                                  float* xpose) {
+    if (xpose != nullptr) {
+        size_t cell = 0;
+        float w0 = 0.0f, w1 = 0.0f, rt = 0.0f;
+        if (have) mixed_stencil(st, P, cell, w0, w1, rt);
+        if (P.s.time_interpolation != 0) {
+            sample_records<FOCUSED, true>(P, cell, w0, w1, rt, c, xpose);
+        } else {
+            sample_records<FOCUSED, false>(P, cell, w0, w1, rt, c, xpose);
+        }
+    } else if (have) {
+        sample_mixed<FOCUSED>(st, P, c);
+    }
 }
 
 // Physics, step size, noise and the state update of one substep.
@@ -982,6 +1095,17 @@ __device__ __forceinline__ bool substep(StateMixed& st, const PushParams& P) {
     float c[FOCUSED ? 21 : 16];
     sample_mixed<FOCUSED>(st, P, c);
     return advance_mixed<FOCUSED>(st, P, c);
+}
+
+// The same substep, warp-collective over the cell records (every lane calls
+// it; lanes without a particle only help sample).
+template <bool FOCUSED>
+__device__ __forceinline__ bool substep_records(StateMixed& st, const PushParams& P, bool have,
+                                                float* xpose) {
+    if (have) ++st.steps;
+    float c[FOCUSED ? 21 : 16];
+    sample_mixed_warp<FOCUSED>(st, P, have, c, xpose);
+    return have && advance_mixed<FOCUSED>(st, P, c);
 }
 
 // Per-lane tallies of the surrogate judge.
@@ -1074,17 +1198,17 @@ __device__ __forceinline__ Served serve_closure(const PushParams& P, bool use, f
 template <bool FP16, int H, bool TC = false>
 __device__ __forceinline__ bool substep_surrogate(StateMixed& st, const PushParams& P, bool have,
                                                   const uint2* smem, JudgeTally& tally,
-                                                  TcNet* net = nullptr, bool* fail = nullptr,
-                                                  bool* stop = nullptr) {
+                                                  float* xpose, TcNet* net = nullptr,
+                                                  bool* fail = nullptr, bool* stop = nullptr) {
     const SurrogateDevice& sg = P.sg;
     const SurrogateBox& box = sg.box;
     float c[21];
     float f[kMlpIn] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
     bool use = false;
     float mu = 0.0f;
+    if (have) ++st.steps;
+    sample_mixed_warp<true>(st, P, have, c, xpose);
     if (have) {
-        ++st.steps;
-        sample_mixed<true>(st, P, c);
         mu = clamp_mu(st.mu, P.kf.mu_max);
         const float b = c[6];
         const float p = st.p_hi;
@@ -1130,7 +1254,8 @@ __device__ __forceinline__ bool substep_surrogate(StateMixed& st, const PushPara
 // [mu_cut, 2 mu_cut] and judges one substep in judge_period, in FP64.
 template <bool FP16, int H>
 __device__ __forceinline__ bool substep_surrogate(StateF64& st, const PushParams& P, bool have,
-                                                  const uint2* smem, JudgeTally& tally) {
+                                                  const uint2* smem, JudgeTally& tally,
+                                                  float* /*xpose: FP64 tables have no records*/) {
     const SurrogateDevice& sg = P.sg;
     const SurrogateBox& box = sg.box;
     double c[21];
@@ -1331,6 +1456,13 @@ __global__ void __launch_bounds__(128, !std::is_same<State, StateMixed>::value
     if (SURR) {
         load_surrogate_block<surr_hidden(SURR)>(P.sg.block, surrogate_smem);
     }
+    // the warp's rows for the record sampler, after the network's block
+    float* xpose = nullptr;
+    if (std::is_same<State, StateMixed>::value && P.records != nullptr) {
+        xpose = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(surrogate_smem) +
+                                         (SURR ? mlp_smem_bytes(surr_hidden(SURR)) : 0)) +
+                (threadIdx.x >> 5) * 32 * record_xpose_stride(FOCUSED);
+    }
     State st;
     bool have = false;
     bool exhausted = false;
@@ -1375,8 +1507,11 @@ __global__ void __launch_bounds__(128, !std::is_same<State, StateMixed>::value
         }
         bool more;
         if constexpr (SURR) {
-            more = substep_surrogate<surr_fp16(SURR), surr_hidden(SURR)>(st, P, have,
-                                                                          surrogate_smem, tally);
+            more = substep_surrogate<surr_fp16(SURR), surr_hidden(SURR)>(
+                st, P, have, surrogate_smem, tally, xpose);
+        } else if constexpr (std::is_same<State, StateMixed>::value) {
+            more = xpose != nullptr ? substep_records<FOCUSED>(st, P, have, xpose)
+                                    : have && substep<FOCUSED>(st, P);
         } else {
             more = have && substep<FOCUSED>(st, P);
         }
@@ -1414,6 +1549,10 @@ __global__ void __launch_bounds__(128, KPT_SURROGATE_TC_MIN_BLOCKS)
     extern __shared__ __align__(128) unsigned char tc_smem[];
     TcNet net = tc_setup<H>(P.sg.tc_block, tc_smem);
     tc_constants<FP16, H>(net);
+    float* xpose = P.records == nullptr
+                       ? nullptr
+                       : reinterpret_cast<float*>(tc_smem + tc_xpose_offset<H>()) +
+                             (threadIdx.x >> 5) * 32 * record_xpose_stride(true);
     JudgeTally tally{0ull, 0ull, 0ull, 0.0f};
     StateMixed st;
     bool have = false;
@@ -1459,8 +1598,8 @@ __global__ void __launch_bounds__(128, KPT_SURROGATE_TC_MIN_BLOCKS)
             continue;
         }
         bool stop = false;
-        const bool more =
-            substep_surrogate<FP16, H, true>(st, P, have, nullptr, tally, &net, &fail, &stop);
+        const bool more = substep_surrogate<FP16, H, true>(st, P, have, nullptr, tally, xpose,
+                                                           &net, &fail, &stop);
         if (stop) {
             break;
         }
@@ -1533,6 +1672,7 @@ PushParams make_push_params(const PushLaunch& L) {
     if (L.surrogate != nullptr) {
         P.sg = *L.surrogate;
     }
+    P.records = L.precision == kPrecisionMixed ? L.records : nullptr;
     return P;
 }
 
@@ -1546,7 +1686,8 @@ template <bool FP16, int H>
 cudaError_t launch_push_tc(const PushParams& P, const PushLaunch& L, cudaStream_t stream) {
     const int threads = 128;
     constexpr int kTmemBlocks = 512 / static_cast<int>(TcMlp<H>::Cols);
-    size_t smem = tc_smem_bytes<H>();
+    size_t smem = P.records != nullptr ? tc_xpose_offset<H>() + record_xpose_bytes(true, 4)
+                                       : tc_smem_bytes<H>();
     cudaFuncAttributes attr{};
     cudaError_t err = cudaFuncGetAttributes(&attr, push_tc_kernel<FP16, H>);
     if (err != cudaSuccess) return err;
@@ -1582,7 +1723,8 @@ cudaError_t launch_push(const PushLaunch& L, cudaStream_t stream) {
             return launch_push_tc<surr_fp16(SURR), surr_hidden(SURR)>(P, L, stream);
         }
     }
-    const size_t smem = SURR ? mlp_smem_bytes(surr_hidden(SURR)) : 0;
+    const size_t smem = (SURR ? mlp_smem_bytes(surr_hidden(SURR)) : 0) +
+                        (P.records != nullptr ? record_xpose_bytes(FOCUSED, threads / 32) : 0);
     if (L.schedule == kScheduleSimple && !SURR) {
         const uint64_t want = (L.count + threads - 1) / threads;
         const int blocks =

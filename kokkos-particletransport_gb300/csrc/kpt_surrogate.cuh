@@ -457,6 +457,12 @@ __host__ __device__ constexpr size_t tc_smem_bytes() {
     return static_cast<size_t>(TcMlp<H>::Bytes) + 16;
 }
 
+// Start of the push's record-sampler rows behind the engine's footprint.
+template <int H>
+__host__ __device__ constexpr size_t tc_xpose_offset() {
+    return (tc_smem_bytes<H>() + 15) & ~static_cast<size_t>(15);
+}
+
 // Block prologue (all threads): weights to shared memory, barrier init,
 // TMEM allocation by warp 0.
 template <int H>
