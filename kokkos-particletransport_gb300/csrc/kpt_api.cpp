@@ -3805,12 +3805,63 @@ struct kpt_batch {
     int threads = 128;            // threads per block of the batched push
     int particles_per_lane = 1;   // particles a lane advances side by side
     DeviceBuffer params, offsets, cursor, counters, saved;
+    // cell records of every run's table pair (all runs or none), with the
+    // field serials they were built from
+    std::vector<DeviceBuffer> records;
+    std::vector<std::pair<uint64_t, uint64_t>> record_serials;
+    bool use_records = false;
     // cached graph of the last interval loop
     cudaGraphExec_t graph = nullptr;
-    uint32_t graph_key[7] = {0, 0, 0, 0, 0, 0, 0};
+    uint32_t graph_key[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 };
 
 namespace {
+
+// Cell records for the batched push: every run's table pair gets its
+// records (built on the context's stream, kept while the pair is the same)
+// when the context's mode asks for them -- KPT_RECORDS_AUTO: the runs
+// together hold at least a quarter as many particles as their tables have
+// points.  Out of device memory the batch samples the point tables.
+int batch_records(kpt_batch* b) {
+    kpt_context* ctx = b->ctx;
+    const size_t runs = b->runs.size();
+    uint64_t particles = 0, points = 0;
+    for (const kpt_batch::Run& run : b->runs) {
+        particles += run.parts->count;
+        points += run.lower->points;
+    }
+    b->use_records = ctx->records_mode == KPT_RECORDS_ON ||
+                     (ctx->records_mode == KPT_RECORDS_AUTO && particles * 4 >= points);
+    if (!b->use_records) return KPT_OK;
+    b->records.resize(runs);
+    b->record_serials.resize(runs, {0, 0});
+    for (size_t r = 0; r < runs; ++r) {
+        const kpt_batch::Run& run = b->runs[r];
+        const std::pair<uint64_t, uint64_t> key{run.lower->serial, run.upper->serial};
+        if (b->record_serials[r] == key && b->records[r].ptr != nullptr) continue;
+        const bool focused = run.lower->kind == KPT_TABLE_FOCUSED21;
+        b->record_serials[r] = {0, 0};
+        if (run.lower->points >= (1ull << 32) ||
+            b->records[r].reserve(run.lower->points * kpt::record_floats(focused) *
+                                  sizeof(float)) != cudaSuccess) {
+            cudaGetLastError();  // out of memory: the point tables for every run
+            for (DeviceBuffer& d : b->records) d.release();
+            b->use_records = false;
+            return KPT_OK;
+        }
+        kpt::RecordLaunch rl{};
+        rl.lower = static_cast<const float*>(run.lower->table);
+        rl.upper = static_cast<const float*>(run.upper->table);
+        rl.records = b->records[r].as<float>();
+        rl.points = run.lower->points;
+        rl.ex = run.lower->nx + 4;
+        rl.ey = run.lower->ny + 4;
+        rl.focused = focused ? 1 : 0;
+        KPT_CUDA(kpt::launch_build_records(rl, ctx->stream));
+        b->record_serials[r] = key;
+    }
+    return KPT_OK;
+}
 
 int batch_prepare(kpt_batch* b) {
     kpt_context* ctx = b->ctx;
@@ -3822,6 +3873,7 @@ int batch_prepare(kpt_batch* b) {
     KPT_CUDA(b->counters.reserve(runs * sizeof(kpt::PushCounters)));
     std::vector<char> host(runs * psize);
     std::vector<uint64_t> offsets(runs + 1, 0);
+    if (int rc = batch_records(b)) return rc;
     for (size_t r = 0; r < runs; ++r) {
         kpt_batch::Run& run = b->runs[r];
         kpt_particles* parts = run.parts;
@@ -3841,6 +3893,7 @@ int batch_prepare(kpt_batch* b) {
         kpt::PushLaunch launch;
         fill_push_launch(ctx, parts, run.lower, run.upper, &run.settings, run.frame, run.seed,
                          b->counters.as<kpt::PushCounters>() + r, launch);
+        launch.records = b->use_records ? b->records[r].as<float>() : nullptr;
         kpt::build_push_params(launch, host.data() + r * psize);
         offsets[r + 1] = offsets[r] + parts->count;
     }
@@ -3863,6 +3916,7 @@ kpt::BatchLaunch batch_launch(const kpt_batch* b) {
     B.blocks_per_sm = b->blocks_per_sm;
     B.threads = b->threads;
     B.particles_per_lane = b->particles_per_lane;
+    B.records = b->use_records ? 1 : 0;
     return B;
 }
 
@@ -3931,6 +3985,7 @@ int kpt_batch_destroy(kpt_batch* b) {
     for (DeviceBuffer* d : {&b->params, &b->offsets, &b->cursor, &b->counters, &b->saved}) {
         d->release();
     }
+    for (DeviceBuffer& d : b->records) d.release();
     delete b;
     return KPT_OK;
 }
@@ -4009,12 +4064,13 @@ int kpt_batch_run(kpt_batch* b, uint32_t intervals, int use_graph) {
     if (int rc = activate(ctx)) return rc;
     if (int rc = batch_prepare(b)) return rc;
     cudaStream_t st = ctx->stream;
-    const uint32_t key[7] = {intervals, static_cast<uint32_t>(b->sort_tile),
+    const uint32_t key[8] = {intervals, static_cast<uint32_t>(b->sort_tile),
                              static_cast<uint32_t>(b->blocks_per_sm),
                              static_cast<uint32_t>(b->sort_every),
                              static_cast<uint32_t>(b->runs.size()),
                              static_cast<uint32_t>(b->threads),
-                             static_cast<uint32_t>(b->particles_per_lane)};
+                             static_cast<uint32_t>(b->particles_per_lane),
+                             b->use_records ? 1u : 0u};
     if (use_graph && st != nullptr) {
         if (b->graph == nullptr || std::memcmp(key, b->graph_key, sizeof(key)) != 0) {
             batch_drop_graph(b);

@@ -114,6 +114,7 @@ struct BatchLaunch {
     int blocks_per_sm;       // resident blocks per SM, 0 = as many as fit
     int threads;             // threads per block: 64, 128 or 256
     int particles_per_lane;  // particles a lane advances side by side: 1 or 2
+    int records;             // every run's PushParams carries cell records
 };
 // The launch shapes the batched push is built for.
 bool batch_shape_supported(int threads, int particles_per_lane);

@@ -950,31 +950,30 @@ __host__ __device__ constexpr size_t record_xpose_bytes(bool focused, int warps)
 }
 
 // Warp-collective sampling from the cell records (every lane calls it,
-// converged; a lane without a particle passes cell 0).  Lanes 4g..4g+3 form
-// a group: for each of the group's four particles in turn, lane 4g+s reads
-// the sectors of component pairs s, s+4, s+8 of that particle's record --
-// one 128-byte line per request for the group -- and interpolates each pair
-// from its own sectors with the eight corner weights, in the operations and
-// the order of sample_stencil_pairs, so the values equal the point-major
-// sampler's bit for bit.  The pairs then reach their particle's lane
-// through the warp's rows of shared memory.
+// converged; rec = the lane's cell record, any valid record for a lane
+// without a particle).  Lanes 4g..4g+3 form a group: for each of the
+// group's four particles in turn, lane 4g+s reads the sectors of component
+// pairs s, s+4, s+8 of that particle's record -- one 128-byte line per
+// request for the group -- and interpolates each pair from its own sectors
+// with the eight corner weights, in the operations and the order of
+// sample_stencil_pairs, so the values equal the point-major sampler's bit
+// for bit.  The pairs then reach their particle's lane through the warp's
+// rows of shared memory.
 template <bool FOCUSED, bool USE_TIME>
-__device__ __forceinline__ void sample_records(const PushParams& P, size_t cell, float w0,
-                                               float w1, float rt,
+__device__ __forceinline__ void sample_records(const float* rec, float w0, float w1, float rt,
                                                float (&c)[FOCUSED ? 21 : 16], float* xpose) {
     constexpr int C = FOCUSED ? 21 : 16;
-    constexpr int RF = record_floats(FOCUSED);
     constexpr int GROUPS = record_sectors(FOCUSED) / 8;  // line pairs (frames 0 and 1)
     constexpr int XS = record_xpose_stride(FOCUSED);
     const unsigned full = 0xffffffffu;
     const unsigned lane = threadIdx.x & 31u;
     const unsigned group = lane & ~3u;
     const int s = static_cast<int>(lane & 3u);
-    const uint32_t my_cell = static_cast<uint32_t>(cell);
+    const unsigned long long my_rec = reinterpret_cast<unsigned long long>(rec);
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         const int src = static_cast<int>(group) + q;
-        const uint32_t qcell = __shfl_sync(full, my_cell, src);
+        const unsigned long long qrec = __shfl_sync(full, my_rec, src);
         const float qw0 = __shfl_sync(full, w0, src);
         const float qw1 = __shfl_sync(full, w1, src);
         const float qrt = USE_TIME ? __shfl_sync(full, rt, src) : 0.0f;
@@ -988,17 +987,17 @@ __device__ __forceinline__ void sample_records(const PushParams& P, size_t cell,
             w_lo[k] = f2_splat(wc[k] * lw);
             if (USE_TIME) w_hi[k] = f2_splat(wc[k] * qrt);
         }
-        const float* rec = P.records + static_cast<size_t>(qcell) * RF + 8 * s;
+        const float* sector = reinterpret_cast<const float*>(qrec) + 8 * s;
         float* row = xpose + (group + q) * XS;
 #pragma unroll
         for (int m = 0; m < GROUPS; ++m) {
             unsigned long long v[4];
-            load4_pairs(rec + 64 * m, v);
+            load4_pairs(sector + 64 * m, v);
             unsigned long long acc = f2_mul(w_lo[0], v[0]);
 #pragma unroll
             for (int k = 1; k < 4; ++k) acc = f2_fma(w_lo[k], v[k], acc);
             if (USE_TIME) {
-                load4_pairs(rec + 64 * m + 32, v);
+                load4_pairs(sector + 64 * m + 32, v);
 #pragma unroll
                 for (int k = 0; k < 4; ++k) acc = f2_fma(w_hi[k], v[k], acc);
             }
@@ -1031,10 +1030,11 @@ __device__ __forceinline__ void sample_mixed_warp(const StateMixed& st, const Pu
         size_t cell = 0;
         float w0 = 0.0f, w1 = 0.0f, rt = 0.0f;
         if (have) mixed_stencil(st, P, cell, w0, w1, rt);
+        const float* rec = P.records + cell * record_floats(FOCUSED);
         if (P.s.time_interpolation != 0) {
-            sample_records<FOCUSED, true>(P, cell, w0, w1, rt, c, xpose);
+            sample_records<FOCUSED, true>(rec, w0, w1, rt, c, xpose);
         } else {
-            sample_records<FOCUSED, false>(P, cell, w0, w1, rt, c, xpose);
+            sample_records<FOCUSED, false>(rec, w0, w1, rt, c, xpose);
         }
     } else if (have) {
         sample_mixed<FOCUSED>(st, P, c);
@@ -1777,6 +1777,36 @@ __device__ __forceinline__ void batch_finish(const PushParams& P, const StateMix
     atomicMax(&P.counters->max_steps, static_cast<unsigned int>(st.steps));
 }
 
+// A batched substep over the cell records, warp-collective: every lane
+// calls it; lanes of one warp may belong to different runs (each samples
+// its run's records) and lanes without a particle help sample.  A warp
+// whose particles' runs disagree on time interpolation samples the point
+// tables instead (the same values).
+template <bool FOCUSED>
+__device__ __forceinline__ bool substep_batch_records(StateMixed& st, const PushParams* runs,
+                                                      int run, bool have, float* xpose) {
+    const unsigned full = 0xffffffffu;
+    const PushParams& P = runs[run];
+    float c[FOCUSED ? 21 : 16];
+    size_t cell = 0;
+    float w0 = 0.0f, w1 = 0.0f, rt = 0.0f;
+    int time_on = 0;
+    if (have) {
+        ++st.steps;
+        mixed_stencil(st, P, cell, w0, w1, rt);
+        time_on = P.s.time_interpolation != 0 ? 1 : 0;
+    }
+    const float* rec = P.records + cell * record_floats(FOCUSED);
+    if (__all_sync(full, !have || time_on != 0)) {
+        sample_records<FOCUSED, true>(rec, w0, w1, rt, c, xpose);
+    } else if (__all_sync(full, !have || time_on == 0)) {
+        sample_records<FOCUSED, false>(rec, w0, w1, rt, c, xpose);
+    } else if (have) {
+        sample_mixed<FOCUSED>(st, P, c);
+    }
+    return have && advance_mixed<FOCUSED>(st, P, c);
+}
+
 // Register budget of the batched push per launch shape: the resident
 // threads per SM of the single-run mixed push (MinBlocks x 128), divided by
 // the particles a lane carries (each carries its own state).
@@ -1794,9 +1824,13 @@ template <bool FOCUSED, int THREADS, int PPL>
 __global__ void __launch_bounds__(THREADS, (BatchMinBlocks<FOCUSED, THREADS, PPL>::value))
     push_batch_kernel(const BatchLaunch B) {
     __shared__ uint64_t offsets[kBatchMaxRuns + 1];
+    extern __shared__ float batch_xpose[];
     for (int k = threadIdx.x; k <= B.runs; k += blockDim.x) offsets[k] = B.offsets[k];
     __syncthreads();
     const PushParams* runs = static_cast<const PushParams*>(B.params);
+    float* xpose = B.records != 0
+                       ? batch_xpose + (threadIdx.x >> 5) * 32 * record_xpose_stride(FOCUSED)
+                       : nullptr;
     const unsigned full = 0xffffffffu;
     const unsigned lane = threadIdx.x & 31u;
     const unsigned lanes_below = (1u << lane) - 1u;
@@ -1857,7 +1891,11 @@ __global__ void __launch_bounds__(THREADS, (BatchMinBlocks<FOCUSED, THREADS, PPL
         }
 #pragma unroll
         for (int s = 0; s < PPL; ++s) {
-            if (have[s] && !substep<FOCUSED>(st[s], runs[run[s]])) {
+            const bool more = xpose != nullptr
+                                  ? substep_batch_records<FOCUSED>(st[s], runs, run[s], have[s],
+                                                                   xpose)
+                                  : have[s] && substep<FOCUSED>(st[s], runs[run[s]]);
+            if (have[s] && !more) {
                 const PushParams& P = runs[run[s]];
                 store<FOCUSED>(st[s], P);
                 batch_finish(P, st[s]);
@@ -1964,14 +2002,15 @@ namespace {
 
 template <bool FOCUSED, int THREADS, int PPL>
 cudaError_t launch_batch_shape(const BatchLaunch& B, cudaStream_t stream) {
+    const size_t smem = B.records != 0 ? record_xpose_bytes(FOCUSED, THREADS / 32) : 0;
     int resident = 0;
     cudaError_t err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &resident, push_batch_kernel<FOCUSED, THREADS, PPL>, THREADS, 0);
+        &resident, push_batch_kernel<FOCUSED, THREADS, PPL>, THREADS, smem);
     if (err != cudaSuccess) return err;
     resident = resident < 1 ? 1 : resident;
     const int per_sm = B.blocks_per_sm > 0 && B.blocks_per_sm < resident ? B.blocks_per_sm
                                                                         : resident;
-    push_batch_kernel<FOCUSED, THREADS, PPL><<<B.sm_count * per_sm, THREADS, 0, stream>>>(B);
+    push_batch_kernel<FOCUSED, THREADS, PPL><<<B.sm_count * per_sm, THREADS, smem, stream>>>(B);
     return cudaGetLastError();
 }
 

@@ -105,6 +105,45 @@ def test_records_equal_point_tables_learned_closure(ctx, kpt, fields_mod, traine
             t.close()
 
 
+@pytest.mark.parametrize("focused", [False, True])
+@pytest.mark.parametrize("shape", [(128, 1), (256, 2)])
+def test_batched_records_equal_point_tables(ctx, kpt, fields_mod, binding, oracle, focused,
+                                            shape):
+    """Batched runs (lanes of one warp in different runs, each sampling its
+    run's records), one run without time interpolation among runs with it
+    (a warp that mixes them samples the point tables for that substep)."""
+    from test_gpu_batch import _runs, _tables
+    runs = _runs(kpt, fields_mod, binding, oracle, focused)
+    params = binding.default_params(kperp_over_kpara=0.05, focused=int(focused),
+                                    time_interpolation=0)
+    runs[1]["settings"] = kpt.settings_from_dict(params)
+    results = []
+    try:
+        for mode in (kpt.RECORDS_OFF, kpt.RECORDS_ON):
+            ctx.set_cell_records(mode)
+            batch = ctx.batch()
+            handles = []
+            for run in runs:
+                lower, upper = _tables(ctx, kpt, run, focused)
+                parts = ctx.particles(run["count"])
+                parts.upload(run["start"], run["count"])
+                batch.add_run(parts, lower, upper, run["settings"], run["seed"], run["frame"])
+                handles.append((parts, lower, upper))
+            batch.set_schedule(sort_tile=8, blocks_per_sm=0, sort_every=1)
+            batch.set_launch_shape(*shape)
+            batch.run(2, use_graph=True)
+            results.append([h[0].download() for h in handles])
+            batch.close()
+            for h in handles:
+                for x in h:
+                    x.close()
+    finally:
+        ctx.set_cell_records(kpt.RECORDS_AUTO)
+    for a, b in zip(*results):
+        for name in a:
+            assert np.array_equal(a[name], b[name]), name
+
+
 def test_records_mode_is_checked(ctx, kpt):
     with pytest.raises(kpt.KptError):
         ctx.set_cell_records(7)
