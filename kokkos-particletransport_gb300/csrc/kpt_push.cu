@@ -959,6 +959,12 @@ __host__ __device__ constexpr size_t record_xpose_bytes(bool focused, int warps)
 // sample_stencil_pairs, so the values equal the point-major sampler's bit
 // for bit.  The pairs then reach their particle's lane through the warp's
 // rows of shared memory.
+// Particles of a group whose requests the sampler unrolls together (4: all
+// of the group's loads may be in flight at once, register pressure allowing).
+#ifndef KPT_RECORD_Q_UNROLL
+#define KPT_RECORD_Q_UNROLL 4
+#endif
+constexpr int kRecordQUnroll = KPT_RECORD_Q_UNROLL;
 template <bool FOCUSED, bool USE_TIME>
 __device__ __forceinline__ void sample_records(const float* rec, float w0, float w1, float rt,
                                                float (&c)[FOCUSED ? 21 : 16], float* xpose) {
@@ -970,7 +976,7 @@ __device__ __forceinline__ void sample_records(const float* rec, float w0, float
     const unsigned group = lane & ~3u;
     const int s = static_cast<int>(lane & 3u);
     const unsigned long long my_rec = reinterpret_cast<unsigned long long>(rec);
-#pragma unroll
+#pragma unroll kRecordQUnroll
     for (int q = 0; q < 4; ++q) {
         const int src = static_cast<int>(group) + q;
         const unsigned long long qrec = __shfl_sync(full, my_rec, src);
@@ -1540,8 +1546,12 @@ __global__ void __launch_bounds__(128, !std::is_same<State, StateMixed>::value
 #ifndef KPT_SURROGATE_TC_MIN_BLOCKS
 #define KPT_SURROGATE_TC_MIN_BLOCKS 4
 #endif
+#ifndef KPT_SURROGATE_TC32_MIN_BLOCKS
+#define KPT_SURROGATE_TC32_MIN_BLOCKS 4
+#endif
 template <bool FP16, int H>
-__global__ void __launch_bounds__(128, KPT_SURROGATE_TC_MIN_BLOCKS)
+__global__ void __launch_bounds__(128, H == 32 ? KPT_SURROGATE_TC32_MIN_BLOCKS
+                                               : KPT_SURROGATE_TC_MIN_BLOCKS)
     push_tc_kernel(const PushParams P) {
     const unsigned full = 0xffffffffu;
     const unsigned lane = threadIdx.x & 31u;
@@ -1676,12 +1686,13 @@ PushParams make_push_params(const PushLaunch& L) {
     return P;
 }
 
-// Persistent grid of the tcgen05 push: 4 blocks per SM, the number whose
-// TMEM (TcMlp<H>::Cols each) fills the SM's 512 columns.  The occupancy
-// query reports 1 block per SM for this kernel, so the register bound is
-// computed from the kernel's attributes instead: should the registers ever
-// admit more than 4 blocks, the dynamic shared memory is padded until they
-// do not (a fifth block would only wait in tcgen05.alloc).
+// Persistent grid of the tcgen05 push: as many blocks per SM as both the
+// TMEM (TcMlp<H>::Cols of the SM's 512 columns each) and the registers
+// admit.  The occupancy query reports 1 block per SM for this kernel, so
+// the register bound is computed from the kernel's attributes (registers
+// per thread rounded to the allocation unit of 8); should the registers
+// admit more blocks than the TMEM, the dynamic shared memory is padded
+// until they do not (a further block would only wait in tcgen05.alloc).
 template <bool FP16, int H>
 cudaError_t launch_push_tc(const PushParams& P, const PushLaunch& L, cudaStream_t stream) {
     const int threads = 128;
@@ -1691,8 +1702,9 @@ cudaError_t launch_push_tc(const PushParams& P, const PushLaunch& L, cudaStream_
     cudaFuncAttributes attr{};
     cudaError_t err = cudaFuncGetAttributes(&attr, push_tc_kernel<FP16, H>);
     if (err != cudaSuccess) return err;
-    const int regs = attr.numRegs > 0 ? attr.numRegs : 1;
-    if (65536 / (regs * threads) > kTmemBlocks) {
+    const int regs = attr.numRegs > 0 ? (attr.numRegs + 7) / 8 * 8 : 8;
+    const int reg_blocks = 65536 / (regs * threads);
+    if (reg_blocks > kTmemBlocks) {
         int device = 0, per_sm_smem = 0;
         err = cudaGetDevice(&device);
         if (err != cudaSuccess) return err;
@@ -1708,8 +1720,10 @@ cudaError_t launch_push_tc(const PushParams& P, const PushLaunch& L, cudaStream_
             if (err != cudaSuccess) return err;
         }
     }
+    const int resident = reg_blocks < kTmemBlocks ? (reg_blocks > 0 ? reg_blocks : 1)
+                                                  : kTmemBlocks;
     const int per_sm =
-        L.blocks_per_sm > 0 && L.blocks_per_sm < kTmemBlocks ? L.blocks_per_sm : kTmemBlocks;
+        L.blocks_per_sm > 0 && L.blocks_per_sm < resident ? L.blocks_per_sm : resident;
     push_tc_kernel<FP16, H><<<L.sm_count * per_sm, threads, smem, stream>>>(P);
     return cudaGetLastError();
 }

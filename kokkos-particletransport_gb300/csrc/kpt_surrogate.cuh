@@ -79,8 +79,10 @@ constexpr size_t kSurrogateSmemMax = Mlp<64>::SmemBytes;
 // H, H+1), layer 3 N = 16 x K = H + 16 (outputs 3..15 zero).  Activations
 // live in tensor memory: the A operand of each layer (H/2 columns of 16-bit
 // pairs, row = TMEM lane) followed by the constant block (one column of
-// (1, 1), seven of zeros), the hidden accumulators (H FP32 columns) and the
-// output accumulators (16 columns).
+// (1, 1), seven of zeros) and the hidden accumulators (H FP32 columns); the
+// output accumulators (16 columns) reuse the first hidden columns, which the
+// layer-2 epilogue has read before the layer-3 MMA is issued.  H = 32 then
+// fits in 64 columns (eight blocks' worth per SM), H = 64 in 128.
 template <int H>
 struct TcMlp {
     static constexpr int K2 = H + 16;  // K of layers 2 and 3 (bias block included)
@@ -91,9 +93,11 @@ struct TcMlp {
     static constexpr uint32_t ColA = 0;
     static constexpr uint32_t ColOne = H / 2;  // constant block
     static constexpr uint32_t ColD = H / 2 + 8;
-    static constexpr uint32_t ColOut = ColD + H;
-    static constexpr uint32_t Cols = 128;  // TMEM allocation (power of two >= ColOut + 16)
-    static_assert(ColOut + 16 <= Cols, "tensor-memory layout exceeds the allocation");
+    static constexpr uint32_t ColOut = ColD;
+    // TMEM allocation: a power of two >= 32 covering the hidden accumulators
+    static constexpr uint32_t Cols = ColD + H <= 64 ? 64 : 128;
+    static_assert(ColD + H <= Cols && ColOut + 16 <= Cols,
+                  "tensor-memory layout exceeds the allocation");
 };
 __host__ __device__ constexpr size_t tc_block_bytes(int hidden) {
     return hidden == 64 ? TcMlp<64>::Bytes : TcMlp<32>::Bytes;
