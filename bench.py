@@ -9,9 +9,10 @@ consecutive MHD intervals of 1000 fixed steps each.  One step = one cell
 sort + one ``kpt_push_interval`` over the whole population.
 
 Headline: focused transport with the learned slab-QLT closure (sigma^2 =
-0.1, gamma_k = 5/3; a 5-64-64-3 network with BF16 weights and FP32
+0.1, gamma_k = 5/3; a 5-32-32-3 network with BF16 weights and FP32
 accumulation, trained on the GPU on 2 M closure samples before the timed
-region), mixed precision; beside it the plain FP64 push with the plain
+region, served on the engine the library picks for its width), mixed
+precision; beside it the other engine and the width-64 network, the plain FP64 push with the plain
 closure (the baseline the metric names), the mixed push with the plain
 closure (what the network gains or costs), momentum and pitch-cosine
 spectrum L1 of every leg against FP64 after one interval from the same
@@ -75,13 +76,27 @@ PORT_OVER_REFERENCE = {"parker_c1_100_steps": 1.070, "focused_reduced_closure_10
                               "x86 host, both on the C library's pow, results bit-identical"}
 
 
-def tensor_flop_per_step(hidden: int) -> int:
-    """Tensor flops of one network evaluation (one particle-step) on the
-    tcgen05 engine, as issued: layer 1 K = 16 (5 inputs, 2 bias inputs,
-    padding) x N = H, layer 2 K = H + 16 (the bias block) x N = H, layer 3
-    K = H + 16 x N = 16 (3 outputs, padding): 14 848 flop at H = 64."""
-    return 2 * (16 * hidden + (hidden + 16) * hidden + (hidden + 16) * 16)
-PROFILE = os.path.join(ROOT, "profiles", "push_tc_surrogate_focused_1024x2048.md")
+def tensor_flop_per_step(hidden: int, engine: str) -> int:
+    """Tensor flops of one network evaluation (one particle-step) as issued.
+    tcgen05: layer 1 K = 16 (5 inputs, 2 bias inputs, padding) x N = H,
+    layer 2 K = H + 16 (the bias block) x N = H, layer 3 K = H + 16 x N = 16
+    (3 outputs, padding): 14 848 flop at H = 64, 5 632 at H = 32.  mma.sync
+    (FP32 biases added outside the MMAs): layer 1 K = 16 x N = H, layer 2
+    K = H x N = H, layer 3 K = H x N = 8: 3 584 flop at H = 32."""
+    if engine == "tcgen05":
+        return 2 * (16 * hidden + (hidden + 16) * hidden + (hidden + 16) * 16)
+    return 2 * (16 * hidden + hidden * hidden + hidden * 8)
+
+
+def default_engine(hidden: int) -> str:
+    """The engine a trained network starts on (the library's choice by
+    width, measured faster on GB300): tcgen05 at 64, mma.sync at 32."""
+    return "tcgen05" if hidden == 64 else "mma.sync"
+
+
+PROFILES_HEAD = {
+    "tcgen05": os.path.join(ROOT, "profiles", "push_tc_surrogate_focused_1024x2048.md"),
+    "mma.sync": os.path.join(ROOT, "profiles", "push_refill_surrogate_focused_1024x2048.md")}
 PROFILE_F64_FOCUSED = os.path.join(ROOT, "profiles", "push_refill_f64_focused_1024x2048.md")
 PROFILE_F64_PARKER = os.path.join(ROOT, "profiles", "push_refill_f64_parker_1024x2048.md")
 
@@ -312,10 +327,17 @@ def run_focused(args, f0, f1):
     start["status"][:] = 0
     start["t"][:] = START_FRAME * plain.mhd_dt
     tc, warp = kpt.ENGINE_TCGEN05, kpt.ENGINE_MMA_SYNC
+    # every network serves the headline legs on the engine it starts on (the
+    # library's choice for its width); the other engine is timed beside it
+    defaults = {label: net.engine for label, net in nets.items()}
+    head = defaults["surrogate"]
+    assert (head == tc) == (default_engine(args.hidden_width) == "tcgen05")
+    side = warp if head == tc else tc
+    side_label = "surrogate_mma_sync" if side == warp else "surrogate_tcgen05"
     # the FP64 baseline is the faster of the two FP64 arithmetics (contracted:
     # FMA fusion and CUDA's pow); the strict one (the oracle's rounding, bit
     # for bit) is timed beside it
-    legs = [("surrogate", kpt.PRECISION_MIXED, learned, args.steps, "surrogate", tc),
+    legs = [("surrogate", kpt.PRECISION_MIXED, learned, args.steps, "surrogate", head),
             ("f64", kpt.PRECISION_F64, plain, 0, None, tc)]
     if WORLD == 1:
         # the FP64 push with the learned closure (mma.sync engine): where the
@@ -323,12 +345,11 @@ def run_focused(args, f0, f1):
         legs += [("f64_surrogate", kpt.PRECISION_F64, learned, 0, "surrogate", warp),
                  ("f64_strict", kpt.PRECISION_F64, plain, 0, None, tc),
                  ("mixed_qlt", kpt.PRECISION_MIXED, plain, args.steps, None, tc),
-                 ("surrogate_mma_sync", kpt.PRECISION_MIXED, learned, args.steps, "surrogate",
-                  warp),
+                 (side_label, kpt.PRECISION_MIXED, learned, args.steps, "surrogate", side),
                  ("surrogate_fp16", kpt.PRECISION_MIXED, learned, args.steps, "surrogate_fp16",
-                  tc),
+                  head),
                  (f"surrogate_h{other}", kpt.PRECISION_MIXED, learned, args.steps,
-                  f"surrogate_h{other}", tc)]
+                  f"surrogate_h{other}", defaults[f"surrogate_h{other}"])]
     finals = {}
     for label, precision, settings, steps, net_label, engine in legs:
         if net_label is not None:
@@ -431,7 +452,9 @@ def accuracy_report(args, kpt, ctx, nets, tables, start, plain, learned, stream)
     n = min(args.accuracy_particles, len(start["x"]))
     sub = {k: v[:n].copy() for k, v in start.items()}
     parts = ctx.particles(n)
-    tc = kpt.ENGINE_TCGEN05
+    # the headline's engine (the FP64 push serves the network on mma.sync)
+    head = (kpt.ENGINE_TCGEN05 if default_engine(args.hidden_width) == "tcgen05"
+            else kpt.ENGINE_MMA_SYNC)
     ctx.set_fp64_arithmetic(kpt.FP64_STRICT)  # the reference leg rounds as the oracle does
     legs = [("f64", kpt.PRECISION_F64, plain, None, SEED),
             ("mixed_qlt", kpt.PRECISION_MIXED, plain, None, SEED),
@@ -443,7 +466,7 @@ def accuracy_report(args, kpt, ctx, nets, tables, start, plain, learned, stream)
     finals, seconds = {}, {}
     for label, precision, settings, net_label, seed in legs:
         if net_label is not None:
-            nets[net_label].engine = tc
+            nets[net_label].engine = head
         ctx.set_surrogate(nets.get(net_label))
         lower, upper = tables[precision]
         parts.upload(sub, n)
@@ -1100,8 +1123,11 @@ def main():
               "nx": NX, "ny": NY, "particles": args.particles, "transport": "focused",
               "steps_per_interval": args.substeps,
               "closure": f"surrogate (5-{args.hidden_width}-{args.hidden_width}-3 MLP, BF16 "
-                         f"weights on the tcgen05 tensor cores, activations in tensor "
-                         f"memory, FP32 accumulation)",
+                         f"weights, FP32 accumulation, "
+                         + ("block-collective tcgen05 GEMMs, activations in tensor memory)"
+                            if default_engine(args.hidden_width) == "tcgen05" else
+                            "warp-level mma.sync GEMMs, activations in registers)"),
+              "engine": default_engine(args.hidden_width),
               "l2": "tables larger than L2 (no flush)", "sort_tile": args.sort_tile}
     if args.impl == "reference":
         if rank != 0:
@@ -1142,11 +1168,14 @@ def main():
     kernel_s = head["kernel_ms"] / 1e3
     steps_per_launch = head["particle_steps"] / head["steps"]
     achieved = steps_per_launch * BYTES_PER_STEP["focused_mixed"] / kernel_s / 1e9
-    per_step_traffic = profile_value(PROFILE, "dram_bytes_per_particle_step")
-    l1tex_frac = profile_value(PROFILE, "l1tex_data_pipe_frac")
-    issue_frac = profile_value(PROFILE, "issue_active_frac")
+    head_engine = default_engine(args.hidden_width)
+    profile = PROFILES_HEAD[head_engine]
+    per_step_traffic = profile_value(profile, "dram_bytes_per_particle_step")
+    l1tex_frac = profile_value(profile, "l1tex_data_pipe_frac")
+    issue_frac = profile_value(profile, "issue_active_frac")
     bf16_peak, bf16_kind = read_bf16_peak()
-    tensor_tflops = steps_per_launch * tensor_flop_per_step(args.hidden_width) / kernel_s / 1e12
+    tensor_tflops = (steps_per_launch * tensor_flop_per_step(args.hidden_width, head_engine)
+                     / kernel_s / 1e12)
     fp64 = fp64_roofline(
         {"contracted": f64["value"], "strict": focused.get("f64_strict", {}).get("value")},
         None if parker is None else {"contracted": parker["f64"]["value"],
@@ -1216,15 +1245,16 @@ def main():
         **{label: None if label not in focused else {
             k: focused[label][k] for k in
             ("value", "ms_per_step", "spectrum_l1_vs_f64", "mu_spectrum_l1_vs_f64", "judge")}
-           for label in ("surrogate_mma_sync", "surrogate_fp16",
+           for label in ("surrogate_mma_sync" if head_engine == "tcgen05"
+                         else "surrogate_tcgen05", "surrogate_fp16",
                          f"surrogate_h{96 - args.hidden_width}")},
         "train": focused["train"],
         # The gather model counts every table gather as HBM traffic; DRAM
         # moves a few percent of that (the gathers hit L2), and with the cell
         # records the L1TEX data pipe is no longer saturated either: the
         # kernel is bound by the latency of its dependent per-substep chain
-        # (record gathers, the block-collective network's MMA round trips,
-        # the physics) at 16 warps per SM -- "bound" names that.
+        # (record gathers, the network's layers, the physics) at 16 warps
+        # per SM -- "bound" names that.
         "roofline": {"bound": "latency", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                      "model": "672 B per particle-step (2 frames x 4 corners x 21 f32 "
@@ -1232,9 +1262,9 @@ def main():
                      "traffic": None if per_step_traffic is None
                      else per_step_traffic * steps_per_launch,
                      "traffic_source": "from_profile: ncu dram__bytes_read.sum + "
-                                       "dram__bytes_write.sum of push_tc_kernel per "
+                                       "dram__bytes_write.sum of the headline push per "
                                        "particle-step (capture of 100 steps per particle, "
-                                       f"{os.path.relpath(PROFILE, ROOT)}) x this launch's "
+                                       f"{os.path.relpath(profile, ROOT)}) x this launch's "
                                        "particle-steps",
                      "dram_frac": None if per_step_traffic is None
                      else per_step_traffic * steps_per_launch / kernel_s / 1e9 / peak,

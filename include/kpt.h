@@ -298,7 +298,10 @@ int kpt_surrogate_destroy(kpt_surrogate* surrogate);
 int kpt_surrogate_evaluate(kpt_surrogate* surrogate, uint64_t n, const double* inputs,
                            int tensor_cores, double* outputs, int32_t* served);
 /* Engine that serves the network in the push and in evaluate's
- * tensor-core path (default KPT_ENGINE_TCGEN05).  The engines compute the
+ * tensor-core path.  A trained network starts on the engine measured faster
+ * for its width on GB300: KPT_ENGINE_TCGEN05 at width 64, KPT_ENGINE_MMA_SYNC
+ * at width 32 (whose GEMMs are too small to repay the block-collective
+ * engine's barriers and tensor-memory round trips).  The engines compute the
  * same BF16/FP16 network with FP32 accumulation; their sums associate
  * differently, so results agree to FP32 rounding, not bit for bit. */
 int kpt_surrogate_set_engine(kpt_surrogate* surrogate, int engine);

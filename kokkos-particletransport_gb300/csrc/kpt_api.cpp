@@ -1582,6 +1582,11 @@ int kpt_surrogate_train(kpt_context* ctx, const kpt_settings* settings,
     box.mu_cut = static_cast<float>(c.mu_cut);
     box.fp16 = c.element_type == KPT_SURROGATE_FP16 ? 1 : 0;
     box.hidden = hidden;
+    // the engine measured faster on GB300 for the width: at width 32 the
+    // block-collective GEMMs' barriers and tensor-memory round trips cost
+    // more than the warp-level MMAs they replace (273 vs 314 ms per
+    // 1000-step interval of the 4 Mi-particle workload), at width 64 less
+    sg->engine = hidden == 32 ? kpt::kEngineMmaSync : kpt::kEngineTcgen05;
     box.magnetic_dependency = settings->magnetic_dependency;
     box.momentum_dependency = settings->momentum_dependency;
     box.p0 = settings->p0;

@@ -99,6 +99,7 @@ def test_spectra_match_fp64_oracle_over_ten_intervals(ctx, kpt, binding, workloa
                                                        closure):
     spectra = importlib.import_module("kokkos-particletransport_gb300.spectra")
     f0, f1, start, ref = workload
+    default_engine = network.engine
     if closure == "plain":
         ctx.set_surrogate(None)
         settings = kpt.settings_from_dict(_params(binding, 1))
@@ -119,7 +120,7 @@ def test_spectra_match_fp64_oracle_over_ten_intervals(ctx, kpt, binding, workloa
             assert judge["evaluations"] > 0 and judge["max_rel_error"] < 0.2, judge
     finally:
         ctx.set_surrogate(None)
-        network.engine = kpt.ENGINE_TCGEN05
+        network.engine = default_engine
     p0 = settings.p0
     same = spectra.compare_populations(paired, ref, p0)
     other = spectra.compare_populations(indep, ref, p0)

@@ -84,6 +84,7 @@ def test_records_equal_point_tables(ctx, kpt, binding, fields_mod, focused, stre
 @pytest.mark.parametrize("engine", ["tcgen05", "mma.sync"])
 def test_records_equal_point_tables_learned_closure(ctx, kpt, fields_mod, trained64, engine):
     _, settings, surrogate = trained64
+    default_engine = surrogate.engine
     surrogate.engine = kpt.ENGINE_TCGEN05 if engine == "tcgen05" else kpt.ENGINE_MMA_SYNC
     fields = _fields(fields_mod, 64, 128, True, (5, 6))
     tables = [ctx.field(f, kpt.TABLE_FOCUSED21, kpt.PRECISION_MIXED) for f in fields]
@@ -99,7 +100,7 @@ def test_records_equal_point_tables_learned_closure(ctx, kpt, fields_mod, traine
         _assert_same(_push_both_ways(ctx, kpt, tables, settings, start, n, (7,), 99,
                                      sort=False))
     finally:
-        surrogate.engine = kpt.ENGINE_TCGEN05
+        surrogate.engine = default_engine
         ctx.set_surrogate(None)
         for t in tables:
             t.close()

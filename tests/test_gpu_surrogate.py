@@ -169,12 +169,13 @@ def test_engines_agree(kpt, net, request):
     inputs = _box_inputs(rng, 20000, norm)  # 156 blocks of 128 and a ragged one
     inputs[:50, 0] *= 1e-3  # some below mu_cut: the plain closure
     outs = {}
+    default_engine = surrogate.engine
     try:
         for engine in (kpt.ENGINE_TCGEN05, kpt.ENGINE_MMA_SYNC):
             surrogate.engine = engine
             outs[engine] = surrogate.evaluate(inputs)
     finally:
-        surrogate.engine = kpt.ENGINE_TCGEN05
+        surrogate.engine = default_engine
     with pytest.raises(kpt.KptError, match="unknown engine"):
         surrogate.engine = 7
     (tc, served_tc), (warp, served_warp) = outs[kpt.ENGINE_TCGEN05], outs[kpt.ENGINE_MMA_SYNC]
@@ -214,6 +215,7 @@ def test_fallback_outside_the_box_is_the_plain_closure(trained):
 def test_surrogate_push_matches_fp64_spectrum(ctx, kpt, oracle, binding, fields_mod, net, engine,
                                               request):
     params, settings, surrogate = request.getfixturevalue(net)
+    default_engine = surrogate.engine
     surrogate.engine = kpt.ENGINE_TCGEN05 if engine == "tcgen05" else kpt.ENGINE_MMA_SYNC
     ye = fields_mod.stretched_edges(128, -2.0, 2.0)
     f0 = fields_mod.harris_field(64, 128, y_edges=ye, island_amplitude=0.1, noise=0.01, seed=5)
@@ -261,7 +263,7 @@ def test_surrogate_push_matches_fp64_spectrum(ctx, kpt, oracle, binding, fields_
     other = kpt.settings_from_dict(dict(params, kpara0=params["kpara0"] * 2))
     with pytest.raises(kpt.KptError, match="trained"):
         ctx.push_interval(parts, lower, upper, other, frame, seed)
-    surrogate.engine = kpt.ENGINE_TCGEN05
+    surrogate.engine = default_engine
     for f in (lower, upper):
         f.close()
     parts.close()
@@ -275,7 +277,9 @@ def test_tcgen05_push_does_not_depend_on_the_schedule(ctx, kpt, fields_mod, net,
     (other rows beside every particle, other lockstep partners) ends bit for
     bit the same."""
     _, settings, surrogate = request.getfixturevalue(net)
-    assert surrogate.engine == kpt.ENGINE_TCGEN05
+    default_engine = surrogate.engine
+    assert default_engine == (kpt.ENGINE_TCGEN05 if net == "trained64" else kpt.ENGINE_MMA_SYNC)
+    surrogate.engine = kpt.ENGINE_TCGEN05
     ye = fields_mod.stretched_edges(128, -2.0, 2.0)
     f0 = fields_mod.harris_field(64, 128, y_edges=ye, island_amplitude=0.1, noise=0.01, seed=5)
     f1 = fields_mod.harris_field(64, 128, y_edges=ye, island_amplitude=0.1, noise=0.01, seed=6)
@@ -297,6 +301,7 @@ def test_tcgen05_push_does_not_depend_on_the_schedule(ctx, kpt, fields_mod, net,
             results.append((parts.download(n), stats.particle_steps))
     finally:
         ctx.set_push_schedule(kpt.SCHEDULE_REFILL, 0)
+        surrogate.engine = default_engine
     base, steps = results[0]
     assert steps > 0
     for other, other_steps in results[1:]:
