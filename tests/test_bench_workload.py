@@ -50,3 +50,20 @@ def test_fixed_step_rule_gives_exactly_n_steps(oracle, binding, fields_mod):
         assert np.all(counts == n), (n, np.unique(counts))
     # the plain 1/N step can leave a remainder for one more step
     assert np.all(_steps(oracle, binding, fields_mod, 1.0 / 1000) == 1001)
+
+
+def test_tensor_flop_model_and_engine_choice():
+    """The bench's tensor-rate model (flops per network evaluation as each
+    engine issues them) and the engine a network of each width starts on."""
+    sys.path.insert(0, ROOT)
+    bench = importlib.import_module("bench")
+    assert bench.tensor_flop_per_step(64, "tcgen05") == 14848
+    assert bench.tensor_flop_per_step(32, "tcgen05") == 5632
+    assert bench.tensor_flop_per_step(32, "mma.sync") == 3584
+    assert bench.default_engine(64) == "tcgen05"
+    assert bench.default_engine(32) == "mma.sync"
+    assert set(bench.PROFILES_HEAD) == {"tcgen05", "mma.sync"}
+    for engine, path in bench.PROFILES_HEAD.items():
+        for key in ("dram_bytes_per_particle_step", "l1tex_data_pipe_frac",
+                    "issue_active_frac"):
+            assert bench.profile_value(path, key) is not None, (engine, key)
