@@ -114,10 +114,13 @@ struct kpt_context {
     int push_schedule = kpt::kScheduleRefill;
     int fp64_arithmetic = KPT_FP64_STRICT;
     int push_blocks_per_sm = 0;  // 0: as many as fit (occupancy)
-    // cell records of the last table pair a mixed push used (by field serial)
+    // cell records of the last table pair a mixed push used (by field serial),
+    // the stream they were built on and an event marking the build's end
     DeviceBuffer records;
     uint64_t records_lower = 0, records_upper = 0;
     int records_mode = KPT_RECORDS_AUTO;
+    cudaStream_t records_stream = nullptr;
+    cudaEvent_t records_ready = nullptr;
 };
 
 struct kpt_surrogate {
@@ -489,6 +492,9 @@ int kpt_context_destroy(kpt_context* ctx) {
                             &ctx->summary_partials, &ctx->summary_result, &ctx->sample_io,
                             &ctx->judge, &ctx->records}) {
         b->release();
+    }
+    if (ctx->records_ready != nullptr) {
+        cudaEventDestroy(ctx->records_ready);
     }
     if (ctx->own_stream != nullptr) {
         cudaStreamDestroy(ctx->own_stream);
@@ -1116,8 +1122,17 @@ int push_records(kpt_context* ctx, const kpt_particles* parts, const kpt_field* 
         rl.ey = lower->ny + 4;
         rl.focused = focused ? 1 : 0;
         KPT_CUDA(kpt::launch_build_records(rl, ctx->stream));
+        if (ctx->records_ready == nullptr) {
+            KPT_CUDA(cudaEventCreateWithFlags(&ctx->records_ready, cudaEventDisableTiming));
+        }
+        KPT_CUDA(cudaEventRecord(ctx->records_ready, ctx->stream));
+        ctx->records_stream = ctx->stream;
         ctx->records_lower = lower->serial;
         ctx->records_upper = upper->serial;
+    } else if (ctx->stream != ctx->records_stream) {
+        // built on another stream (the caller switched streams): order this
+        // push after the build
+        KPT_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->records_ready, 0));
     }
     *out = ctx->records.as<float>();
     return KPT_OK;

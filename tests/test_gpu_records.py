@@ -145,6 +145,40 @@ def test_batched_records_equal_point_tables(ctx, kpt, fields_mod, binding, oracl
             assert np.array_equal(a[name], b[name]), name
 
 
+def test_records_reused_on_another_stream(ctx, kpt, binding, fields_mod):
+    """Records built on one stream and reused by a push on another (the
+    caller switched the context's stream): the second push is ordered after
+    the build and ends where the point-table push does."""
+    import torch
+    params = binding.default_params(kperp_over_kpara=0.05, focused=1)
+    settings = kpt.settings_from_dict(params)
+    fields = _fields(fields_mod, 48, 96, True, (41, 42))
+    tables = [ctx.field(f, kpt.TABLE_FOCUSED21, kpt.PRECISION_MIXED) for f in fields]
+    n = 3000
+    parts = ctx.particles(n)
+    ctx.inject(parts, tables[0], settings, n, 4, 23)
+    start = parts.download(n)
+    first, second = torch.cuda.Stream(), torch.cuda.Stream()
+    results = []
+    try:
+        for mode in (kpt.RECORDS_OFF, kpt.RECORDS_ON):
+            ctx.set_cell_records(mode)
+            for stream in (first, second):
+                ctx.set_stream(stream.cuda_stream)
+                parts.upload(start, n)
+                ctx.push_interval(parts, tables[0], tables[1], settings, 4, 23)
+                results.append(parts.download(n))
+    finally:
+        ctx.set_stream(0)  # back to the context's own stream
+        ctx.set_cell_records(kpt.RECORDS_AUTO)
+        parts.close()
+        for t in tables:
+            t.close()
+    for other in results[1:]:
+        for name in results[0]:
+            assert np.array_equal(results[0][name], other[name]), name
+
+
 def test_records_mode_is_checked(ctx, kpt):
     with pytest.raises(kpt.KptError):
         ctx.set_cell_records(7)
