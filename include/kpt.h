@@ -245,7 +245,8 @@ int kpt_context_set_fp64_arithmetic(kpt_context* ctx, int mode);
  * Parker; rebuilt when the table pair changes) for a refill-scheduled
  * mixed push of at least a quarter as many particles as the table has
  * points; KPT_RECORDS_OFF never, KPT_RECORDS_ON for every refill-scheduled
- * mixed push.  Results are bit-identical either way. */
+ * mixed push.  Results are bit-identical either way.  The records are built
+ * on the context's stream; a later push on another stream waits for them. */
 enum kpt_records_mode { KPT_RECORDS_AUTO = 0, KPT_RECORDS_OFF = 1, KPT_RECORDS_ON = 2 };
 int kpt_context_set_cell_records(kpt_context* ctx, int mode);
 
