@@ -153,3 +153,53 @@ def test_f64_push_equals_the_oracle_bit_for_bit_over_ten_intervals(ctx, kpt, bin
         assert np.array_equal(got[name], ref[name]), name
     for obj in (lower, upper, parts):
         obj.close()
+
+
+def test_what_the_network_gains_in_the_fp64_push(ctx, kpt, binding, workload, network):
+    """What the trained network gains over the method without it.  In the
+    FP64 focused push the plain slab-QLT closure is five FP64 powers per
+    substep on a GPU whose FP64 pipe bounds the push; the network serves
+    D_mumu, dD_mumu/dmu and kappa_parallel instead.  On 262 144 particles of
+    the test field (one 500-step interval timed after a warm-up one, both
+    pushes with the contracted FP64 arithmetic, the bench's baseline) the
+    push with the network is faster by a clear margin (the bench measures
+    1.66x on its 4 Mi-particle workload) and its momentum spectrum stays
+    within the metric's 1 % L1 of the plain push's."""
+    import time
+    spectra = importlib.import_module("kokkos-particletransport_gb300.spectra")
+    f0, f1 = workload[0], workload[1]
+    n = 262144
+    plain = kpt.settings_from_dict(_params(binding, 1))
+    learned = kpt.settings_from_dict(_params(binding, 2))
+    lower = ctx.field(f0, kpt.TABLE_FOCUSED21, kpt.PRECISION_F64)
+    upper = ctx.field(f1, kpt.TABLE_FOCUSED21, kpt.PRECISION_F64)
+    parts = ctx.particles(n)
+    ctx.inject(parts, lower, plain, n, FRAME, SEED)
+    start = parts.download(n)
+    start["status"][:] = 0
+    start["t"][:] = FRAME * 0.1
+    seconds, finals = {}, {}
+    ctx.set_fp64_arithmetic(kpt.FP64_CONTRACTED)
+    try:
+        for label, settings, net in (("plain", plain, None), ("network", learned, network)):
+            ctx.set_surrogate(net)
+            parts.upload(start, n)
+            ctx.sort(parts, lower, 8, 8)
+            ctx.push_interval(parts, lower, upper, settings, FRAME, SEED)  # warm-up
+            parts.upload(start, n)
+            ctx.sort(parts, lower, 8, 8)
+            t0 = time.perf_counter()
+            stats = ctx.push_interval(parts, lower, upper, settings, FRAME, SEED)
+            seconds[label] = time.perf_counter() - t0
+            assert stats.failed == 0 and stats.particle_steps >= n * SUBSTEPS
+            finals[label] = parts.download(n)
+    finally:
+        ctx.set_surrogate(None)
+        ctx.set_fp64_arithmetic(kpt.FP64_STRICT)
+        for obj in (lower, upper, parts):
+            obj.close()
+    gain = seconds["plain"] / seconds["network"]
+    same = spectra.compare_populations(finals["network"], finals["plain"], plain.p0)
+    print("network gain in the FP64 push", gain, "momentum L1", same["p64"]["l1"])
+    assert gain > 1.3
+    assert same["p64"]["l1"] <= 0.01
